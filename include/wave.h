@@ -1,0 +1,194 @@
+/*
+ * wave.h — C ABI of the GB300-native forward solver for the WAVE-Simulation
+ * time-stepping hot path (ForwardSolver::run and everything it calls).
+ *
+ * Every entry point returns an int status (WAVE_OK on success). No C++
+ * exception and no pointer owned by the library ever crosses this boundary.
+ * A handle is bound to one CUDA device and one CUDA stream; handles are not
+ * thread-safe, use one handle per host thread (the reference calls
+ * ForwardSolver::run from one thread per MPI rank, Simulation.cpp:452).
+ *
+ * Axis convention (same as the reference, Coordinates.cpp:615-644):
+ *   x = horizontal inline (fastest), z = horizontal crossline, y = depth
+ *   (slowest); linear index idx = x + z*NX + y*NX*NZ. 2-D runs use NZ = 1.
+ */
+#ifndef WAVE_GB300_H
+#define WAVE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (replace COMMON_THROWEXCEPTION / SCAI_ASSERT_ERROR) ---- */
+#define WAVE_OK 0
+#define WAVE_ERR_ARG 1          /* invalid argument, size mismatch, null handle   */
+#define WAVE_ERR_CUDA 2         /* a CUDA runtime call failed                      */
+#define WAVE_ERR_NONFINITE 3    /* NaN/Inf found in the wavefield or seismogram    */
+#define WAVE_ERR_TIMEOUT 4      /* a bounded device-side wait ran out              */
+#define WAVE_ERR_UNSUPPORTED 5  /* dimension/equation combination not available   */
+#define WAVE_ERR_STATE 6        /* call out of order (e.g. step before set_model)  */
+#define WAVE_ERR_IO 7           /* file could not be read or parsed               */
+
+/* ---- equation types: the ForwardSolver factory keys
+ *      (ForwardSolver/ForwardSolverFactory.cpp:4-67) ---- */
+#define WAVE_EQ_ACOUSTIC 0
+#define WAVE_EQ_ELASTIC 1
+#define WAVE_EQ_VISCOELASTIC 2
+#define WAVE_EQ_SH 3
+#define WAVE_EQ_VISCOSH 4
+#define WAVE_EQ_TMEM 5
+#define WAVE_EQ_EMEM 6
+#define WAVE_EQ_VISCOTMEM 7
+#define WAVE_EQ_VISCOEMEM 8
+
+/* ---- seismogram / source component types (Acquisition/Acquisition.hpp:17-44)
+ *      seismic: 1=P 2=VX 3=VY 4=VZ ; EM: 1=EZ 2=EX 3=EY 4=HZ ---- */
+#define WAVE_TYPE_P 1
+#define WAVE_TYPE_VX 2
+#define WAVE_TYPE_VY 3
+#define WAVE_TYPE_VZ 4
+#define WAVE_TYPE_EZ 1
+#define WAVE_TYPE_EX 2
+#define WAVE_TYPE_EY 3
+#define WAVE_TYPE_HZ 4
+
+/* ---- memory flags for pointer arguments ---- */
+#define WAVE_MEM_HOST 0
+#define WAVE_MEM_DEVICE 1
+
+/*
+ * Solver configuration: the hot-path subset of the reference's
+ * Configuration keys (Configuration/Configuration.cpp:45-100, keys as read by
+ * Simulation.cpp, Derivatives.cpp:12-55 and ForwardSolver.cpp:34-54).
+ */
+typedef struct wave_config {
+    int dimension;              /* "dimension": 2 or 3                               */
+    int equation;               /* "equationType": WAVE_EQ_*                         */
+    int64_t NX, NY, NZ;         /* "NX","NY","NZ" (NY = depth; NZ = 1 in 2-D)       */
+    double DH;                  /* "DH"  grid spacing [m]                            */
+    double DT;                  /* "DT"  time step [s]                               */
+    double T;                   /* "T"   record length [s]; NT = int(T/DT + 0.5)    */
+    int spatialFDorder;         /* "spatialFDorder": 2,4,6,8,10,12                   */
+    int FreeSurface;            /* "FreeSurface": 0 none, 1 mirror/image method      */
+    int DampingBoundary;        /* "DampingBoundary": 0 none, 1 ABS, 2 CPML          */
+    int BoundaryWidth;          /* "BoundaryWidth" [grid points]                     */
+    double DampingCoeff;        /* "DampingCoeff" [%] (ABS)                          */
+    double NPower;              /* "NPower" (CPML)                                   */
+    double CenterFrequencyCPML; /* "CenterFrequencyCPML" [Hz] (CPML, visco ref. f)   */
+    double VMaxCPML;            /* "VMaxCPML" [m/s] (CPML)                           */
+    int numRelaxationMechanisms;       /* "numRelaxationMechanisms" (0..4)           */
+    double relaxationFrequency[4];     /* "relaxationFrequency", "...2", "...3", "...4" */
+    int useStencilMatrix;       /* "useStencilMatrix": 0 = sparse (CSR) operators,
+                                   1 = stencil operators (always zero-padded)      */
+    int edgeOrderReduction;     /* sparse operators only. 1 = reduce the FD order at
+                                   the grid edges until the stencil fits, as the
+                                   current Derivatives.cpp:166-179, 743-756 does;
+                                   0 = drop neighbours outside the grid (zero
+                                   padding), the rule the reference's CI golden
+                                   seismograms (par/ci, seismogram.<case>.ref.<c>.mtx)
+                                   were made with.
+                                   Config key "edgeOrderReduction" (default 1).   */
+} wave_config;
+
+typedef struct wave_handle wave_handle;
+
+/* Number of time samples the reference uses: int(T/DT + 0.5) evaluated in
+ * single precision (Common/Common.hpp:240-243, Sources.cpp:26). */
+int wave_config_nt(const wave_config* cfg, int* nt);
+
+/* Parse a reference parameter file (KEY=VALUE, '#' comments, keys
+ * case-insensitive) into *cfg. Replaces Configuration::Configuration(file)
+ * + the get<T>() calls of the hot path (Configuration/Configuration.cpp:45-100,
+ * Configuration.hpp:95-143). Missing mandatory keys -> WAVE_ERR_ARG. */
+int wave_config_from_file(const char* path, wave_config* cfg);
+
+/* ForwardSolver::Factory<float>::Create(dimension, type)
+ * (ForwardSolver/ForwardSolverFactory.cpp:4-67) followed by initForwardSolver
+ * (ForwardSolver.hpp:52, e.g. ForwardSolver3Delastic.cpp:20-48): validates the
+ * combination, allocates device state (wavefields, memory variables, CPML psi
+ * slabs) on the current CUDA device and builds the boundary tables. */
+int wave_solver_create(const wave_config* cfg, wave_handle** out);
+int wave_solver_destroy(wave_handle* h);
+
+/* Modelparameter init + Modelparameter::prepareForModelling (e.g.
+ * Elastic.cpp:28-45, Viscoelastic.cpp:650-715, ModelparameterSeismic.cpp:
+ * 131-136, 421-432, Modelparameter.cpp:336-651) + the solver's
+ * prepareForModelling (ForwardSolver.hpp:42, e.g. ForwardSolver3Dviscoelastic.cpp:103-118,
+ * FreeSurfaceElastic.cpp:11-47). Arrays have n = NX*NY*NZ entries in the
+ * reference index order; unused parameters may be NULL (vs for acoustic,
+ * vp for sh, taup/taus unless visco). mem = WAVE_MEM_HOST or WAVE_MEM_DEVICE. */
+int wave_set_model(wave_handle* h, const float* rho, const float* vp, const float* vs,
+                   const float* taup, const float* taus, size_t n, int mem);
+
+/* EM counterpart (ModelparameterEM/TMEM.cpp:145-170, 230-241; ForwardSolverEM.cpp:14-117):
+ * eps_r relative permittivity, sigma conductivity [S/m], mu_r relative
+ * permeability; tau_eps / tau_sigma for the visco-EM equations (else NULL). */
+int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, const float* mu_r,
+                      const float* tau_eps, const float* tau_sigma, size_t n, int mem);
+
+/* Source coupling (SourceReceiverImpl.cpp:29-37): n sources at 1-D grid
+ * indices idx, component types type[] (WAVE_TYPE_*), signals n x NT row-major
+ * (source i's trace is signals[i*NT .. i*NT+NT-1]); the raw sample of column t
+ * is added at step t. */
+int wave_set_sources(wave_handle* h, int n, const int64_t* idx, const int* type,
+                     const float* signals, int mem);
+
+/* Receiver gather (SourceReceiverImpl.cpp:12-19, FDTD*elastic.cpp pressure
+ * averages): n receivers at 1-D indices idx with component types type[]. */
+int wave_set_receivers(wave_handle* h, int n, const int64_t* idx, const int* type);
+
+/* ForwardSolver::run(receiver, sources, model, wavefield, derivatives, t) for
+ * every t in [t_begin, t_end) (ForwardSolver.hpp:38, caller Simulation.cpp:444-476).
+ * A multi-step call runs as one captured CUDA graph; a one-step call keeps the
+ * reference's run(t) granularity. Asynchronous on the handle's stream. */
+int wave_solver_step(wave_handle* h, int t_begin, int t_end);
+
+/* Wavefields::resetWavefields + ForwardSolver::resetCPML (ForwardSolver.hpp:40,
+ * Simulation.cpp:432, :514): zero all wavefields, memory variables, psi and
+ * the seismogram buffer. */
+int wave_solver_reset(wave_handle* h);
+
+/* Receiver seismograms, n_receivers x NT row-major, trace order = the order
+ * given to wave_set_receivers. Synchronises the handle's stream. */
+int wave_get_seismograms(wave_handle* h, float* out, size_t count, int mem);
+
+/* NaN/Inf check of the wavefields and seismograms (Simulation.cpp:519,
+ * WavefieldsSeismic.cpp:12-40) done on the device over every point:
+ * returns WAVE_OK or WAVE_ERR_NONFINITE. */
+int wave_check_finite(wave_handle* h);
+
+/* Full solver state (wavefields, memory variables, CPML psi slabs) as one
+ * blob, for checkpoint / resume. The reference has no counterpart (it only
+ * writes snapshots, Simulation.cpp:468-475). */
+int wave_get_state_size(wave_handle* h, size_t* bytes);
+int wave_get_state(wave_handle* h, void* out, size_t bytes, int mem);
+int wave_set_state(wave_handle* h, const void* in, size_t bytes, int mem);
+
+/* Query helpers. */
+int wave_get_nt(wave_handle* h, int* nt);
+int wave_get_num_receivers(wave_handle* h, int* n);
+/* Device pointer to the CUDA stream the handle launches on (cudaStream_t). */
+int wave_get_stream(wave_handle* h, void** stream);
+/* Number of kernels launched by this handle since creation. */
+int wave_get_launch_count(wave_handle* h, long long* count);
+/* Average duration [ms] of the most recent timed step kernels, measured with
+ * CUDA events on the handle's stream when timing is on (see wave_set_timing). */
+int wave_set_timing(wave_handle* h, int on);
+int wave_get_kernel_times(wave_handle* h, double* velocity_ms, double* stress_ms, long long* samples);
+
+/* Text of the last error on this handle (or of the last failed create when
+ * h == NULL). Never NULL. */
+const char* wave_last_error(const wave_handle* h);
+
+/* Source time functions of the reference (Sources.cpp:157-215 shapes 1..9:
+ * 1 Ricker, 2 SinW, 3 SinThree, 4 FGaussian, 5 Spike, 6 IntgSinThree,
+ * 7 Ricker_GprMax, 8 Berlage, 9 Sin) evaluated at t = k*DT, k < NT. */
+int wave_wavelet(int shape, int nt, double dt, double fc, double amp, double tshift, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WAVE_GB300_H */
