@@ -1,0 +1,211 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's golden
+seismograms and against the FP64 oracle.
+
+Tolerance: relative L2 over all traces and samples <= 1e-4 (FP32 kernels vs the
+FP64 oracle, and vs the reference's FP32 goldens); the reference's own gate
+(average misfit per sample <= 5e-7) is applied to the goldens as well.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import ci_cases
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+GATE = 5e-7
+
+
+def to_wave_cfg(wave, cfg):
+    c = wave.WaveConfig()
+    ctypes.memmove(ctypes.byref(c), ctypes.byref(cfg), ctypes.sizeof(c))
+    return c
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("name", list(ci_cases.CASES))
+def test_gpu_matches_reference_goldens(name, wave, refcpu):
+    case = ci_cases.load_case(name)
+    cfg = to_wave_cfg(wave, case["cfg"])
+    seis = wave.simulate(cfg, case["model"], case["src_idx"], case["src_type"], case["signals"],
+                         case["rec_idx"], case["rec_type"])
+    g = case["golden"]
+    assert refcpu.reference_misfit(seis.astype(np.float64), g) < GATE
+    assert rel(seis, g) < TOL
+
+
+# ----------------------------------------------------------------------------
+# every equation x boundary x operator mode against the FP64 oracle
+# ----------------------------------------------------------------------------
+def make_case(refcpu, eq, dim, order, fs=0, boundary=2, stencil=0, reduce=1, L=2, seed=0):
+    rng = np.random.default_rng(seed)
+    em = eq in ("tmem", "emem")
+    if dim == 2:
+        NX, NY, NZ = 90, 70, 1
+    else:
+        NX, NY, NZ = 44, 38, 36
+    n = NX * NY * NZ
+    if em:
+        DH = 0.02
+        eps_r = rng.uniform(4.0, 9.0, n)
+        model = dict(eps_r=eps_r, sigma=10 ** rng.uniform(-4, -2, n), mu_r=np.ones(n))
+        vmax, vmin = 3e8 / 2.0, 3e8 / 3.0
+        extra = dict(CenterFrequencyCPML=2e8, VMaxCPML=vmax)
+    else:
+        DH = 5.0
+        vp = rng.uniform(2500.0, 3200.0, n)
+        model = dict(vp=vp, vs=vp / 1.8, rho=310.0 * vp ** 0.25,
+                     taup=rng.uniform(0.02, 0.06, n), taus=rng.uniform(0.02, 0.06, n))
+        vmax, vmin = 3200.0, 2500.0 / 1.8 if eq not in ("acoustic",) else 2500.0
+        extra = dict(CenterFrequencyCPML=12.0, VMaxCPML=vmax)
+    DT = 0.35 * DH / (vmax * np.sqrt(dim) * (1.3 if order > 2 else 1.0))
+    nt = 600
+    cfg = refcpu.make_config(dimension=dim, equation=eq, NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=nt * DT,
+                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary,
+                             BoundaryWidth=10 if boundary else 0, DampingCoeff=8.0, NPower=4.0,
+                             numRelaxationMechanisms=L if eq.startswith("visco") else 0,
+                             relaxationFrequency=[8.0, 30.0, 0.0, 0.0], useStencilMatrix=stencil,
+                             edgeOrderReduction=reduce, **extra)
+    nt = refcpu.nt_of(cfg)
+    fc = vmin / (8 * DH)
+    sx, sy, sz = NX // 2, (2 if fs else NY // 3), NZ // 2
+    src_type = {"acoustic": 1, "elastic": 1, "viscoelastic": 1, "sh": 4, "viscosh": 4, "tmem": 1, "emem": 4}[eq]
+    sidx = np.array([refcpu.grid_index(cfg, sx, sy, sz)])
+    sig = refcpu.ricker(nt, DT, fc, 1.0, 0.0, np.float64)[None]
+    if eq in ("sh", "viscosh"):
+        rtypes = [4, 4, 4]
+    elif eq == "tmem":
+        rtypes = [1, 1, 1]
+    elif eq == "emem":
+        rtypes = [2, 3, 4]
+    else:
+        rtypes = [1, 2, 3] + ([4] if dim == 3 else [])
+    ridx = [refcpu.grid_index(cfg, 3 + (7 * k) % (NX - 6), (k * 5) % NY if not fs else 0, (3 * k) % NZ)
+            for k in range(len(rtypes))]
+    ridx += [refcpu.grid_index(cfg, NX - 4, NY - 3, NZ - 1), refcpu.grid_index(cfg, 1, NY // 2, 0)]
+    rtypes += [rtypes[0], rtypes[-1]]
+    model = {k: v for k, v in model.items()}
+    return cfg, model, sidx, np.array([src_type]), sig, np.array(ridx, dtype=np.int64), np.array(rtypes)
+
+
+def run_both(wave, refcpu, case):
+    cfg, model, sidx, stype, sig, ridx, rtype = case
+    o = refcpu.Oracle(cfg, model, sidx, stype, sig, ridx, rtype, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    gpu = wave.simulate(to_wave_cfg(wave, cfg), m32, sidx, stype, sig.astype(np.float32), ridx, rtype)
+    return gpu, ref
+
+
+SEISMIC = [
+    # (eq, dim, order, fs, boundary, stencil, reduce)
+    ("acoustic", 2, 4, 0, 2, 0, 1),
+    ("acoustic", 2, 8, 1, 1, 1, 0),
+    ("acoustic", 3, 6, 0, 2, 0, 1),
+    ("acoustic", 3, 4, 1, 2, 0, 0),
+    ("elastic", 2, 2, 0, 2, 0, 1),
+    ("elastic", 2, 12, 1, 2, 0, 1),
+    ("elastic", 2, 10, 1, 1, 0, 0),
+    ("elastic", 3, 8, 1, 2, 0, 1),
+    ("elastic", 3, 4, 0, 1, 1, 0),
+    ("elastic", 3, 2, 0, 0, 0, 1),
+    ("viscoelastic", 2, 6, 1, 2, 0, 1),
+    ("viscoelastic", 2, 4, 0, 1, 1, 0),
+    ("viscoelastic", 3, 4, 0, 2, 0, 1),
+    ("viscoelastic", 3, 2, 1, 1, 0, 1),
+    ("sh", 2, 4, 0, 2, 0, 1),
+    ("sh", 2, 8, 1, 1, 0, 0),
+    ("viscosh", 2, 6, 0, 2, 0, 1),
+    ("tmem", 2, 4, 0, 2, 0, 1),
+    ("tmem", 2, 6, 0, 1, 1, 0),
+    ("emem", 2, 4, 0, 2, 0, 1),
+    ("emem", 2, 2, 0, 1, 0, 0),
+]
+
+
+@pytest.mark.parametrize("eq,dim,order,fs,boundary,stencil,reduce", SEISMIC)
+def test_gpu_matches_fp64_oracle(eq, dim, order, fs, boundary, stencil, reduce, wave, refcpu):
+    case = make_case(refcpu, eq, dim, order, fs, boundary, stencil, reduce)
+    gpu, ref = run_both(wave, refcpu, case)
+    assert np.abs(ref).max() > 0
+    assert rel(gpu, ref) < TOL, f"relative L2 {rel(gpu, ref):.3e}"
+
+
+def test_multi_step_graph_equals_single_steps(wave, refcpu):
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "elastic", 2, 8, 1, 2)
+    wc = to_wave_cfg(wave, cfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    outs = []
+    for mode in ("graph", "single"):
+        s = wave.Factory.Create("2D", "elastic").initForwardSolver(wc)
+        s.prepareForModelling(m32)
+        s.setSources(sidx, stype, sig.astype(np.float32))
+        s.setReceivers(ridx, rtype)
+        if mode == "graph":
+            s.run(0, s.nt)
+        else:
+            for t in range(s.nt):
+                s.run(t)
+        outs.append(s.seismograms())
+        s.close()
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_checkpoint_resume_is_bit_identical(wave, refcpu):
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "viscoelastic", 3, 4, 0, 2)
+    wc = to_wave_cfg(wave, cfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    s = wave.Factory.Create("3D", "viscoelastic").initForwardSolver(wc)
+    s.prepareForModelling(m32)
+    s.setSources(sidx, stype, sig.astype(np.float32))
+    s.setReceivers(ridx, rtype)
+    s.run(0, 100)
+    blob = s.state()
+    s.run(100, 200)
+    a = s.seismograms()[:, 100:200].copy()
+    s.set_state(blob)
+    s.run(100, 200)
+    b = s.seismograms()[:, 100:200].copy()
+    s.close()
+    assert np.array_equal(a, b)
+
+
+def test_device_model_pointers_match_host(wave, refcpu):
+    torch = pytest.importorskip("torch")
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "acoustic", 2, 4, 0, 2)
+    wc = to_wave_cfg(wave, cfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    host = wave.simulate(wc, m32, sidx, stype, sig.astype(np.float32), ridx, rtype)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in m32.items()}
+    devout = wave.simulate(wc, dev, sidx, stype, torch.from_numpy(sig.astype(np.float32)).cuda(), ridx, rtype)
+    assert np.array_equal(host, devout)
+
+
+def test_nonfinite_wavefield_is_reported(wave, refcpu):
+    """A CFL violation blows the wavefield up; the device finite check reports
+    it as WAVE_ERR_NONFINITE (Simulation.cpp:519) and nothing traps."""
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "acoustic", 2, 4, 0, 0)
+    wc = to_wave_cfg(wave, cfg)
+    wc.DT = wc.DT * 20
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    with pytest.raises(wave.WaveError) as e:
+        wave.simulate(wc, m32, sidx, stype, sig.astype(np.float32), ridx, rtype)
+    assert e.value.code == wave.WAVE_ERR_NONFINITE
+
+
+def test_launch_count_is_native(wave, refcpu):
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "tmem", 2, 4, 0, 2)
+    s = wave.Factory.Create("2D", "tmem").initForwardSolver(to_wave_cfg(wave, cfg))
+    s.prepareForModelling({k: v.astype(np.float32) for k, v in model.items()})
+    s.setSources(sidx, stype, sig.astype(np.float32))
+    s.setReceivers(ridx, rtype)
+    before = s.launch_count()
+    s.run(0, 40)
+    s.seismograms()
+    assert s.launch_count() - before >= 40 * 3
+    s.close()

@@ -1,0 +1,331 @@
+"""Python host binding of the GB300 forward solver (libwavegpu.so, include/wave.h).
+
+It mirrors the reference's plugin interface for the time-stepping hot path so
+that tests read like the reference's own:
+
+* ``Factory.Create(dimension, equationType)`` ~ ForwardSolver::Factory<float>::Create
+  (src/ForwardSolver/ForwardSolverFactory.cpp:4-67), case-insensitive keys;
+* ``ForwardSolver.initForwardSolver(config)`` / ``prepareForModelling(model)`` /
+  ``run(t)`` / ``resetCPML()`` ~ the virtual methods of ForwardSolver
+  (src/ForwardSolver/ForwardSolver.hpp:25-70);
+* errors raise ``WaveError`` with the library's message (the reference throws
+  COMMON_THROWEXCEPTION / SCAI_ASSERT_ERROR).
+
+There is no CPU fallback: every call goes through the CUDA library, and loading
+fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libwavegpu.so")
+
+WAVE_OK, WAVE_ERR_ARG, WAVE_ERR_CUDA, WAVE_ERR_NONFINITE, WAVE_ERR_TIMEOUT, WAVE_ERR_UNSUPPORTED, WAVE_ERR_STATE, WAVE_ERR_IO = range(8)
+MEM_HOST, MEM_DEVICE = 0, 1
+EQUATIONS = {"acoustic": 0, "elastic": 1, "viscoelastic": 2, "sh": 3, "viscosh": 4,
+             "tmem": 5, "emem": 6, "viscotmem": 7, "viscoemem": 8}
+
+# every entry point declared in include/wave.h
+ABI_SYMBOLS = (
+    "wave_config_nt", "wave_config_from_file", "wave_solver_create", "wave_solver_destroy",
+    "wave_set_model", "wave_set_model_em", "wave_set_sources", "wave_set_receivers",
+    "wave_solver_step", "wave_solver_reset", "wave_get_seismograms", "wave_check_finite",
+    "wave_get_state_size", "wave_get_state", "wave_set_state", "wave_get_nt",
+    "wave_get_num_receivers", "wave_get_stream", "wave_get_launch_count", "wave_set_timing",
+    "wave_get_kernel_times", "wave_last_error", "wave_wavelet",
+)
+
+
+class WaveError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[wave error {code}] {msg}")
+        self.code = code
+
+
+class WaveConfig(ctypes.Structure):
+    """ctypes mirror of ``wave_config`` (include/wave.h)."""
+    _fields_ = [
+        ("dimension", ctypes.c_int),
+        ("equation", ctypes.c_int),
+        ("NX", ctypes.c_int64), ("NY", ctypes.c_int64), ("NZ", ctypes.c_int64),
+        ("DH", ctypes.c_double), ("DT", ctypes.c_double), ("T", ctypes.c_double),
+        ("spatialFDorder", ctypes.c_int),
+        ("FreeSurface", ctypes.c_int),
+        ("DampingBoundary", ctypes.c_int),
+        ("BoundaryWidth", ctypes.c_int),
+        ("DampingCoeff", ctypes.c_double),
+        ("NPower", ctypes.c_double),
+        ("CenterFrequencyCPML", ctypes.c_double),
+        ("VMaxCPML", ctypes.c_double),
+        ("numRelaxationMechanisms", ctypes.c_int),
+        ("relaxationFrequency", ctypes.c_double * 4),
+        ("useStencilMatrix", ctypes.c_int),
+        ("edgeOrderReduction", ctypes.c_int),
+    ]
+
+    @classmethod
+    def from_file(cls, path: str) -> "WaveConfig":
+        c = cls()
+        _check(None, lib().wave_config_from_file(path.encode(), ctypes.byref(c)))
+        return c
+
+    @classmethod
+    def make(cls, **kw) -> "WaveConfig":
+        c = cls()
+        c.dimension = kw.get("dimension", 2)
+        eq = kw.get("equation", "acoustic")
+        c.equation = EQUATIONS[eq.lower()] if isinstance(eq, str) else int(eq)
+        c.NX, c.NY, c.NZ = kw["NX"], kw["NY"], kw.get("NZ", 1)
+        c.DH, c.DT, c.T = kw["DH"], kw["DT"], kw["T"]
+        c.spatialFDorder = kw.get("spatialFDorder", 2)
+        c.FreeSurface = kw.get("FreeSurface", 0)
+        c.DampingBoundary = kw.get("DampingBoundary", 0)
+        c.BoundaryWidth = kw.get("BoundaryWidth", 0)
+        c.DampingCoeff = kw.get("DampingCoeff", 8.0)
+        c.NPower = kw.get("NPower", 4.0)
+        c.CenterFrequencyCPML = kw.get("CenterFrequencyCPML", 5.0)
+        c.VMaxCPML = kw.get("VMaxCPML", 3500.0)
+        c.numRelaxationMechanisms = kw.get("numRelaxationMechanisms", 0)
+        rf = list(kw.get("relaxationFrequency", [])) + [0.0] * 4
+        for i in range(4):
+            c.relaxationFrequency[i] = rf[i]
+        c.useStencilMatrix = kw.get("useStencilMatrix", 0)
+        c.edgeOrderReduction = kw.get("edgeOrderReduction", 1)
+        return c
+
+    def copy_from(self, other) -> "WaveConfig":
+        """Copies the fields of another ctypes config with the same layout."""
+        ctypes.memmove(ctypes.byref(self), ctypes.byref(other), ctypes.sizeof(WaveConfig))
+        return self
+
+    @property
+    def N(self) -> int:
+        return int(self.NX * self.NY * (self.NZ if self.dimension == 3 else 1))
+
+
+_lib = None
+
+
+def build(verbose: bool = False) -> str:
+    """Compiles libwavegpu.so for sm_103a with nvcc (Makefile next to this file)."""
+    jobs = str(min(8, os.cpu_count() or 1))
+    out = None if verbose else subprocess.DEVNULL
+    subprocess.run(["make", "-s", "-j", jobs, "-C", HERE], check=True, stdout=out)
+    return LIB_PATH
+
+
+def lib():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it first (__graft_entry__.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, CP = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER
+    L.wave_last_error.restype = ctypes.c_char_p
+    L.wave_last_error.argtypes = [P]
+    L.wave_config_from_file.argtypes = [ctypes.c_char_p, CP(WaveConfig)]
+    L.wave_config_nt.argtypes = [CP(WaveConfig), CP(I)]
+    L.wave_solver_create.argtypes = [CP(WaveConfig), CP(P)]
+    L.wave_solver_destroy.argtypes = [P]
+    L.wave_set_model.argtypes = [P, P, P, P, P, P, ctypes.c_size_t, I]
+    L.wave_set_model_em.argtypes = [P, P, P, P, P, P, ctypes.c_size_t, I]
+    L.wave_set_sources.argtypes = [P, I, P, P, P, I]
+    L.wave_set_receivers.argtypes = [P, I, P, P]
+    L.wave_solver_step.argtypes = [P, I, I]
+    L.wave_solver_reset.argtypes = [P]
+    L.wave_get_seismograms.argtypes = [P, P, ctypes.c_size_t, I]
+    L.wave_check_finite.argtypes = [P]
+    L.wave_get_state_size.argtypes = [P, CP(ctypes.c_size_t)]
+    L.wave_get_state.argtypes = [P, P, ctypes.c_size_t, I]
+    L.wave_set_state.argtypes = [P, P, ctypes.c_size_t, I]
+    L.wave_get_nt.argtypes = [P, CP(I)]
+    L.wave_get_num_receivers.argtypes = [P, CP(I)]
+    L.wave_get_stream.argtypes = [P, CP(P)]
+    L.wave_get_launch_count.argtypes = [P, CP(ctypes.c_longlong)]
+    L.wave_set_timing.argtypes = [P, I]
+    L.wave_get_kernel_times.argtypes = [P, CP(ctypes.c_double), CP(ctypes.c_double), CP(ctypes.c_longlong)]
+    L.wave_wavelet.argtypes = [I, I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
+    _lib = L
+    return L
+
+
+def _check(h, rc: int):
+    if rc != WAVE_OK:
+        raise WaveError(rc, lib().wave_last_error(h).decode())
+
+
+def _ptr(a):
+    """Pointer of a numpy array (host) or a torch tensor (host or device)."""
+    if a is None:
+        return None, MEM_HOST
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr()), (MEM_DEVICE if a.is_cuda else MEM_HOST)
+    return a.ctypes.data_as(ctypes.c_void_p), MEM_HOST
+
+
+def _f32(a):
+    if a is None or hasattr(a, "data_ptr"):
+        return a
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def wavelet(shape: int, nt: int, dt: float, fc: float, amp: float, tshift: float) -> np.ndarray:
+    """Source time function (Sources.cpp:157-215 shapes 1..9)."""
+    out = np.zeros(nt, dtype=np.float32)
+    _check(None, lib().wave_wavelet(shape, nt, dt, fc, amp, tshift, out.ctypes.data_as(ctypes.c_void_p)))
+    return out
+
+
+class ForwardSolver:
+    """One solver handle (ForwardSolver<float> + its boundary objects, on the GPU)."""
+
+    def __init__(self, dimension: str, equation_type: str):
+        self.dimension = dimension
+        self.equation_type = equation_type
+        self.h = None
+        self.cfg = None
+
+    # ForwardSolver::initForwardSolver (ForwardSolver.hpp:52)
+    def initForwardSolver(self, config: WaveConfig):
+        cfg = WaveConfig().copy_from(config)
+        d = 3 if self.dimension.lower() == "3d" else 2
+        if cfg.dimension != d or cfg.equation != EQUATIONS[self.equation_type.lower()]:
+            raise WaveError(WAVE_ERR_ARG, "configuration does not match the factory keys")
+        h = ctypes.c_void_p()
+        _check(None, lib().wave_solver_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h, self.cfg = h, cfg
+        nt = ctypes.c_int()
+        _check(self.h, lib().wave_get_nt(self.h, ctypes.byref(nt)))
+        self.nt = nt.value
+        return self
+
+    # Modelparameter::prepareForModelling + ForwardSolver::prepareForModelling (ForwardSolver.hpp:42)
+    def prepareForModelling(self, model: dict):
+        n = self.cfg.N
+        if self.cfg.equation >= EQUATIONS["tmem"]:
+            arrs = [_f32(model.get(k)) for k in ("eps_r", "sigma", "mu_r", "tau_eps", "tau_sigma")]
+            fn = lib().wave_set_model_em
+        else:
+            arrs = [_f32(model.get(k)) for k in ("rho", "vp", "vs", "taup", "taus")]
+            fn = lib().wave_set_model
+        ptrs = [_ptr(a) for a in arrs]
+        mems = {m for (p, m) in ptrs if p is not None}
+        if len(mems) > 1:
+            raise WaveError(WAVE_ERR_ARG, "model arrays must all be host or all be device")
+        self._model_keep = arrs
+        _check(self.h, fn(self.h, *[p for (p, _) in ptrs], n, mems.pop() if mems else MEM_HOST))
+
+    def setSources(self, idx, types, signals):
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        sig = _f32(signals)
+        p, mem = _ptr(sig)
+        _check(self.h, lib().wave_set_sources(self.h, len(idx), idx.ctypes.data_as(ctypes.c_void_p),
+                                              types.ctypes.data_as(ctypes.c_void_p), p, mem))
+
+    def setReceivers(self, idx, types):
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        self.nrec = len(idx)
+        _check(self.h, lib().wave_set_receivers(self.h, len(idx), idx.ctypes.data_as(ctypes.c_void_p),
+                                                types.ctypes.data_as(ctypes.c_void_p)))
+
+    # ForwardSolver::run(..., t) for one or many steps (ForwardSolver.hpp:38)
+    def run(self, t_begin: int, t_end: int | None = None):
+        _check(self.h, lib().wave_solver_step(self.h, t_begin, t_begin + 1 if t_end is None else t_end))
+
+    # Wavefields::resetWavefields + ForwardSolver::resetCPML (ForwardSolver.hpp:40)
+    def resetCPML(self):
+        _check(self.h, lib().wave_solver_reset(self.h))
+
+    def seismograms(self, out=None):
+        if out is None:
+            out = np.zeros((self.nrec, self.nt), dtype=np.float32)
+        p, mem = _ptr(out)
+        _check(self.h, lib().wave_get_seismograms(self.h, p, self.nrec * self.nt, mem))
+        return out
+
+    def check_finite(self) -> bool:
+        rc = lib().wave_check_finite(self.h)
+        if rc == WAVE_ERR_NONFINITE:
+            return False
+        _check(self.h, rc)
+        return True
+
+    def state(self) -> np.ndarray:
+        n = ctypes.c_size_t()
+        _check(self.h, lib().wave_get_state_size(self.h, ctypes.byref(n)))
+        buf = np.zeros(n.value, dtype=np.uint8)
+        _check(self.h, lib().wave_get_state(self.h, buf.ctypes.data_as(ctypes.c_void_p), n.value, MEM_HOST))
+        return buf
+
+    def set_state(self, buf: np.ndarray):
+        _check(self.h, lib().wave_set_state(self.h, buf.ctypes.data_as(ctypes.c_void_p), buf.nbytes, MEM_HOST))
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        _check(self.h, lib().wave_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def launch_count(self) -> int:
+        c = ctypes.c_longlong()
+        _check(self.h, lib().wave_get_launch_count(self.h, ctypes.byref(c)))
+        return c.value
+
+    def set_timing(self, on: bool):
+        _check(self.h, lib().wave_set_timing(self.h, int(on)))
+
+    def kernel_times(self):
+        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        _check(self.h, lib().wave_get_kernel_times(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)))
+        return a.value, b.value, n.value
+
+    def close(self):
+        if self.h:
+            lib().wave_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Factory:
+    """ForwardSolver::Factory<float>::Create (ForwardSolverFactory.cpp:4-67)."""
+
+    @staticmethod
+    def Create(dimension: str, equation_type: str) -> ForwardSolver:
+        d, t = dimension.lower(), equation_type.lower()
+        if d not in ("2d", "3d"):
+            raise WaveError(WAVE_ERR_ARG, "Unkown dimension")
+        if t not in EQUATIONS:
+            raise WaveError(WAVE_ERR_ARG, "Unkown type")
+        return ForwardSolver(d, t)
+
+
+def simulate(config: WaveConfig, model: dict, src_idx, src_type, signals, rec_idx, rec_type) -> np.ndarray:
+    """Runs one shot through the whole time loop (Simulation.cpp:432-533) and
+    returns the seismograms (n_receivers x NT)."""
+    dim = "3d" if config.dimension == 3 else "2d"
+    eq = [k for k, v in EQUATIONS.items() if v == config.equation][0]
+    s = Factory.Create(dim, eq).initForwardSolver(config)
+    try:
+        s.prepareForModelling(model)
+        s.setSources(src_idx, src_type, signals)
+        s.setReceivers(rec_idx, rec_type)
+        s.run(0, s.nt)
+        out = s.seismograms()
+        if not s.check_finite():
+            raise WaveError(WAVE_ERR_NONFINITE, "Infinite or NaN value in seismogram or/and velocity wavefield!")
+        return out
+    finally:
+        s.close()

@@ -1,0 +1,868 @@
+// kernels.cu — sm_103a kernels of the forward time step (one thread per grid
+// point, all arithmetic FP32). Each equation is two fused passes, matching the
+// two halves of the reference's ForwardSolver*::run:
+//   pass 1 (velocity / H field): every derivative, its CPML psi update and the
+//          field update in one kernel;
+//   pass 2 (stress / pressure / E field): derivatives, CPML, memory variables,
+//          free-surface exchange and ABS damping of the pass-2 fields.
+// The ABS damping of the pass-1 fields runs in abs_frame_kernel after pass 2
+// (pass 2 still needs their undamped values), then sources and receivers.
+//
+// Derivative operators are matrix-free: rows away from the grid edges use the
+// interior weights held in the kernel parameters; the few edge rows (and the
+// free-surface image rows) read a small per-axis table.
+#include <cuda_runtime.h>
+
+#include "wave_internal.h"
+
+namespace wave {
+
+// --------------------------------------------------------------------------
+// device helpers
+// --------------------------------------------------------------------------
+// 1-D derivative along an axis with stride `st`; c = coordinate along the axis.
+// FWD: taps at offsets -H+1..H, else -H..H-1 (Derivatives.cpp:149, 728).
+template <int H, bool FWD>
+__device__ __forceinline__ float deriv(const float* __restrict__ u, long long i, long long st, int c, const Op1D& op)
+{
+    float s = 0.0f;
+    if (!op.full && c >= op.E && c < op.n - op.E) {
+#pragma unroll
+        for (int k = (FWD ? -H + 1 : -H); k <= (FWD ? H : H - 1); ++k)
+            s += op.w[kMaxHalf + k] * __ldg(u + i + k * st);
+    } else {
+        const int slot = op.full ? c : (c < op.E ? c : op.E + c - (op.n - op.E));
+        const float* t = op.tab + slot * kTabW + kMaxHalf;
+#pragma unroll
+        for (int k = -H; k <= H; ++k) {
+            const int cc = c + k;
+            const float wk = __ldg(t + k);
+            if (cc >= 0 && cc < op.n && wk != 0.0f) s += wk * __ldg(u + i + k * st);
+        }
+    }
+    return s;
+}
+
+// index into a slab-compacted psi array along an axis (-1: outside the slabs)
+__device__ __forceinline__ int slab(int c, const Cpml1D& p)
+{
+    if (p.n <= 2 * p.w) return c;
+    if (c < p.w) return p.lo ? c : -1;
+    if (c >= p.n - p.w) return c - (p.n - p.ns);
+    return -1;
+}
+
+// CPML::applyCPML (CPML.cpp:84-95): psi = b*psi + a*d; d += psi
+__device__ __forceinline__ void cpml(float& d, float* __restrict__ psi, long long pidx, float a, float b)
+{
+    float ps = psi[pidx] * b;
+    ps += a * d;
+    psi[pidx] = ps;
+    d += ps;
+}
+
+struct Pt {
+    int x, y, z;
+    long long i;
+};
+
+__device__ __forceinline__ bool point(const StepParams& P, Pt& p)
+{
+    p.x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (p.x >= P.NX || r >= P.NY * P.NZ) return false;
+    p.y = r / P.NZ;
+    p.z = r - p.y * P.NZ;
+    p.i = p.x + (long long)P.NX * (p.z + (long long)P.NZ * p.y);
+    return true;
+}
+
+// psi indices along x / y / z for point p
+__device__ __forceinline__ long long pix(const StepParams& P, const Pt& p, int s) { return s + (long long)P.cx.ns * (p.z + (long long)P.NZ * p.y); }
+__device__ __forceinline__ long long piy(const StepParams& P, const Pt& p, int s) { return p.x + (long long)P.NX * (p.z + (long long)P.NZ * s); }
+__device__ __forceinline__ long long piz(const StepParams& P, const Pt& p, int s) { return p.x + (long long)P.NX * (s + (long long)P.cz.ns * p.y); }
+
+// derivative + CPML along x / y / z. half = forward-type derivative (uses the
+// half-grid profile, CPML3D.cpp:31-153).
+template <int H, bool FWD>
+__device__ __forceinline__ float dX(const StepParams& P, const Pt& p, const float* u, const Op1D& op, int psiSlot)
+{
+    float d = deriv<H, FWD>(u, p.i, 1, p.x, op);
+    if (P.useCpml) {
+        int s = slab(p.x, P.cx);
+        if (s >= 0) {
+            const float a = FWD ? P.cx.a_half[p.x] : P.cx.a_full[p.x];
+            const float b = FWD ? P.cx.b_half[p.x] : P.cx.b_full[p.x];
+            cpml(d, P.psi[psiSlot], pix(P, p, s), a, b);
+        }
+    }
+    return d;
+}
+template <int H, bool FWD>
+__device__ __forceinline__ float dY(const StepParams& P, const Pt& p, const float* u, const Op1D& op, int psiSlot)
+{
+    float d = deriv<H, FWD>(u, p.i, (long long)P.NX * P.NZ, p.y, op);
+    if (P.useCpml) {
+        int s = slab(p.y, P.cy);
+        if (s >= 0) {
+            const float a = FWD ? P.cy.a_half[p.y] : P.cy.a_full[p.y];
+            const float b = FWD ? P.cy.b_half[p.y] : P.cy.b_full[p.y];
+            cpml(d, P.psi[psiSlot], piy(P, p, s), a, b);
+        }
+    }
+    return d;
+}
+template <int H, bool FWD>
+__device__ __forceinline__ float dZ(const StepParams& P, const Pt& p, const float* u, const Op1D& op, int psiSlot)
+{
+    float d = deriv<H, FWD>(u, p.i, P.NX, p.z, op);
+    if (P.useCpml) {
+        int s = slab(p.z, P.cz);
+        if (s >= 0) {
+            const float a = FWD ? P.cz.a_half[p.z] : P.cz.a_full[p.z];
+            const float b = FWD ? P.cz.b_half[p.z] : P.cz.b_full[p.z];
+            cpml(d, P.psi[psiSlot], piz(P, p, s), a, b);
+        }
+    }
+    return d;
+}
+
+// ABS taper at a point (ABS2D.cpp:110-180, ABS3D.cpp:154-220); 1 outside the frame.
+__device__ __forceinline__ float absDamp(const StepParams& P, const Pt& p)
+{
+    const int w = P.absW;
+    auto edge = [](int c, int n) { return !((n - 1 - c) < c) ? c : (n - 1 - c); };
+    const int dx = edge(p.x, P.NX), dy = edge(p.y, P.NY), dz = edge(p.z, P.NZ);
+    int m;
+    if (!P.is3d) {
+        m = dx < dy ? dx : dy;
+        if (P.fs && p.y < w) return dx < w ? P.absCoeff[dx] : 1.0f;
+    } else {
+        m = dx < dy ? dx : dy;
+        m = m < dz ? m : dz;
+        if (P.fs && p.y < w) {
+            const int xz = !(dx < dz) ? dz : dx;
+            return (dz < w || dx < w) ? P.absCoeff[xz] : 1.0f;
+        }
+    }
+    return m < w ? P.absCoeff[m] : 1.0f;
+}
+
+#define LD(ptr) __ldg((ptr) + p.i)
+
+// --------------------------------------------------------------------------
+// acoustic: FD2Dacoustic::run (ForwardSolver2Dacoustic.cpp:121-190),
+//           FD3Dacoustic::run (ForwardSolver3Dacoustic.cpp:122-230)
+// --------------------------------------------------------------------------
+template <int H>
+__global__ void __launch_bounds__(256) acoustic_v(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    const float* pr = P.f[F_P];
+    float u = dX<H, true>(P, p, pr, P.Dxf, PS_P_X);
+    u *= LD(P.m[M_IRX]);
+    P.f[F_VX][p.i] += u;
+    u = P.fs ? dY<H, true>(P, p, pr, P.DyfS, PS_P_Y) : dY<H, true>(P, p, pr, P.Dyf, PS_P_Y);
+    u *= LD(P.m[M_IRY]);
+    P.f[F_VY][p.i] += u;
+    if (P.is3d) {
+        u = dZ<H, true>(P, p, pr, P.Dzf, PS_P_Z);
+        u *= LD(P.m[M_IRZ]);
+        P.f[F_VZ][p.i] += u;
+    }
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) acoustic_p(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    float u = dX<H, false>(P, p, P.f[F_VX], P.Dxb, PS_VXX);
+    float ut = dY<H, false>(P, p, P.f[F_VY], P.Dyb, PS_VYY);
+    u += ut;
+    if (P.is3d) {
+        ut = dZ<H, false>(P, p, P.f[F_VZ], P.Dzb, PS_VZZ);
+        u += ut;
+    }
+    u *= LD(P.m[M_M]);
+    float pv = P.f[F_P][p.i] + u;
+    if (P.abs) pv *= absDamp(P, p);
+    if (P.fs && p.y == 0) pv = 0.0f;   // FreeSurface::setSurfaceZero (FreeSurface.cpp:14-19)
+    P.f[F_P][p.i] = pv;
+}
+
+// --------------------------------------------------------------------------
+// elastic + visco-elastic velocity: ForwardSolver2Delastic.cpp:150-205,
+// ForwardSolver3Delastic.cpp:174-277, ForwardSolver3Dviscoelastic.cpp:186-268
+// --------------------------------------------------------------------------
+template <int H>
+__global__ void __launch_bounds__(256) elastic_v(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
+    const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
+    const float *Sxx = P.f[F_SXX], *Syy = P.f[F_SYY], *Sxy = P.f[F_SXY];
+    // vx
+    float u = dX<H, true>(P, p, Sxx, P.Dxf, PS_SXX_X);
+    float ut = dY<H, false>(P, p, Sxy, DybS, PS_SXY_Y);
+    u += ut;
+    if (P.is3d) {
+        ut = dZ<H, false>(P, p, P.f[F_SXZ], P.Dzb, PS_SXZ_Z);
+        u += ut;
+    }
+    u *= LD(P.m[M_IRX]);
+    P.f[F_VX][p.i] += u;
+    // vy
+    u = dX<H, false>(P, p, Sxy, P.Dxb, PS_SXY_X);
+    ut = dY<H, true>(P, p, Syy, DyfS, PS_SYY_Y);
+    u += ut;
+    if (P.is3d) {
+        ut = dZ<H, false>(P, p, P.f[F_SYZ], P.Dzb, PS_SYZ_Z);
+        u += ut;
+    }
+    u *= LD(P.m[M_IRY]);
+    P.f[F_VY][p.i] += u;
+    if (P.is3d) {
+        // vz
+        u = dX<H, false>(P, p, P.f[F_SXZ], P.Dxb, PS_SXZ_X);
+        ut = dY<H, false>(P, p, P.f[F_SYZ], DybS, PS_SYZ_Y);
+        u += ut;
+        ut = dZ<H, true>(P, p, P.f[F_SZZ], P.Dzf, PS_SZZ_Z);
+        u += ut;
+        u *= LD(P.m[M_IRZ]);
+        P.f[F_VZ][p.i] += u;
+    }
+}
+
+// elastic stress: ForwardSolver2Delastic.cpp:210-290, ForwardSolver3Delastic.cpp:283-409,
+// free surface FreeSurface2Delastic.cpp:14-45 / FreeSurface3Delastic.cpp:15-47
+template <int H>
+__global__ void __launch_bounds__(256) elastic_s(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    const float *vx = P.f[F_VX], *vy = P.f[F_VY];
+    const float M = LD(P.m[M_M]), mu = LD(P.m[M_MU]);
+    float vxx = dX<H, false>(P, p, vx, P.Dxb, PS_VXX);
+    float vyy = dY<H, false>(P, p, vy, P.Dyb, PS_VYY);
+    float vzz = 0.0f;
+    if (P.is3d) vzz = dZ<H, false>(P, p, P.f[F_VZ], P.Dzb, PS_VZZ);
+    float sxx = P.f[F_SXX][p.i], syy = P.f[F_SYY][p.i];
+    float szz = P.is3d ? P.f[F_SZZ][p.i] : 0.0f;
+    float u = vxx;
+    u += vyy;
+    if (P.is3d) u += vzz;
+    u *= M;
+    sxx += u; syy += u;
+    if (P.is3d) {
+        szz += u;
+        u = vyy + vzz; u *= mu; sxx -= 2.0f * u;
+        u = vxx + vzz; u *= mu; syy -= 2.0f * u;
+        u = vxx + vyy; u *= mu; szz -= 2.0f * u;
+    } else {
+        u = vyy; u *= mu; sxx -= 2.0f * u;
+        u = vxx; u *= mu; syy -= 2.0f * u;
+    }
+    // shear
+    u = dY<H, true>(P, p, vx, P.Dyf, PS_VXY);
+    float ut = dX<H, true>(P, p, vy, P.Dxf, PS_VYX);
+    u += ut;
+    u *= LD(P.m[M_MUXY]);
+    float sxy = P.f[F_SXY][p.i] + u;
+    float sxz = 0.0f, syz = 0.0f;
+    if (P.is3d) {
+        u = dZ<H, true>(P, p, vx, P.Dzf, PS_VXZ);
+        ut = dX<H, true>(P, p, P.f[F_VZ], P.Dxf, PS_VZX);
+        u += ut;
+        u *= LD(P.m[M_MUXZ]);
+        sxz = P.f[F_SXZ][p.i] + u;
+        u = dZ<H, true>(P, p, vy, P.Dzf, PS_VYZ);
+        ut = dY<H, true>(P, p, P.f[F_VZ], P.Dyf, PS_VZY);
+        u += ut;
+        u *= LD(P.m[M_MUYZ]);
+        syz = P.f[F_SYZ][p.i] + u;
+    }
+    if (P.fs && p.y == 0) {
+        // FreeSurfaceElastic::setModelparameter (FreeSurfaceElastic.cpp:11-47)
+        float sv = M - 2.0f * mu;
+        float sh = sv * sv;
+        sh /= M;
+        sh *= -1.0f;
+        syy = 0.0f;
+        const float hs = P.is3d ? vxx + vzz : vxx;
+        float t = sh * hs;
+        sxx += t;
+        if (P.is3d) szz += t;
+        t = sv * vyy;
+        sxx -= t;
+        if (P.is3d) szz -= t;
+    }
+    if (P.abs) {
+        const float d = absDamp(P, p);
+        sxx *= d; syy *= d; sxy *= d;
+        if (P.is3d) { szz *= d; sxz *= d; syz *= d; }
+    }
+    P.f[F_SXX][p.i] = sxx;
+    P.f[F_SYY][p.i] = syy;
+    P.f[F_SXY][p.i] = sxy;
+    if (P.is3d) {
+        P.f[F_SZZ][p.i] = szz;
+        P.f[F_SXZ][p.i] = sxz;
+        P.f[F_SYZ][p.i] = syz;
+    }
+}
+
+// visco-elastic stress: ForwardSolver2Dviscoelastic.cpp:223-303,
+// ForwardSolver3Dviscoelastic.cpp:270-446, free surface
+// FreeSurface2Dviscoelastic.cpp / FreeSurface3Dviscoelastic.cpp:17-75
+template <int H>
+__global__ void __launch_bounds__(256) visco_s(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    const int L = P.L;
+    const float DTh = P.DThalf;
+    const float *vx = P.f[F_VX], *vy = P.f[F_VY];
+    const float M = LD(P.m[M_M]), mu = LD(P.m[M_MU]);
+    const float tauP = LD(P.m[M_TAUP]), tauS = LD(P.m[M_TAUS]);
+    const float opP = LD(P.m[M_OPLTP]), opS = LD(P.m[M_OPLTS]);
+    float vxx = dX<H, false>(P, p, vx, P.Dxb, PS_VXX);
+    float vyy = dY<H, false>(P, p, vy, P.Dyb, PS_VYY);
+    float vzz = 0.0f;
+    if (P.is3d) vzz = dZ<H, false>(P, p, P.f[F_VZ], P.Dzb, PS_VZZ);
+    const int nN = P.is3d ? 3 : 2;
+    float S[3], R[3][kMaxL];
+    const int slotS[3] = {F_SXX, F_SYY, F_SZZ};
+    const int slotR[3] = {R_XX, R_YY, R_ZZ};
+    for (int k = 0; k < nN; ++k) {
+        S[k] = P.f[slotS[k]][p.i];
+        for (int l = 0; l < L; ++l) R[k][l] = P.r[slotR[k]][l][p.i];
+    }
+    float u = vxx;
+    u += vyy;
+    if (P.is3d) u += vzz;
+    u *= M;
+    for (int l = 0; l < L; ++l) {
+        float u2 = P.invRelax[l] * u;
+        u2 *= tauP;
+        for (int k = 0; k < nN; ++k) {
+            S[k] += DTh * R[k][l];
+            R[k][l] *= P.c1[l];
+            R[k][l] -= u2;
+        }
+    }
+    u *= opP;
+    for (int k = 0; k < nN; ++k) S[k] += u;
+    for (int k = 0; k < nN; ++k) {
+        float sum;
+        if (P.is3d) sum = k == 0 ? vyy + vzz : (k == 1 ? vxx + vzz : vxx + vyy);
+        else sum = k == 0 ? vyy : vxx;
+        u = sum;
+        u *= mu;
+        u *= 2.0f;
+        for (int l = 0; l < L; ++l) {
+            float u2 = P.invRelax[l] * u;
+            u2 *= tauS;
+            R[k][l] += u2;
+            R[k][l] *= P.c2[l];
+            S[k] += DTh * R[k][l];
+        }
+        u *= opS;
+        S[k] -= u;
+    }
+    // shear stresses
+    const int nS = P.is3d ? 3 : 1;
+    const int slotSh[3] = {F_SXY, F_SXZ, F_SYZ};
+    const int slotRh[3] = {R_XY, R_XZ, R_YZ};
+    const int matMu[3] = {M_MUXY, M_MUXZ, M_MUYZ};
+    const int matTau[3] = {M_TAUSXY, M_TAUSXZ, M_TAUSYZ};
+    float Sh[3];
+    for (int k = 0; k < nS; ++k) {
+        float ut;
+        if (k == 0) { u = dY<H, true>(P, p, vx, P.Dyf, PS_VXY); ut = dX<H, true>(P, p, vy, P.Dxf, PS_VYX); }
+        else if (k == 1) { u = dZ<H, true>(P, p, vx, P.Dzf, PS_VXZ); ut = dX<H, true>(P, p, P.f[F_VZ], P.Dxf, PS_VZX); }
+        else { u = dZ<H, true>(P, p, vy, P.Dzf, PS_VYZ); ut = dY<H, true>(P, p, P.f[F_VZ], P.Dyf, PS_VZY); }
+        u += ut;
+        u *= LD(P.m[matMu[k]]);
+        const float tauAv = LD(P.m[matTau[k]]);
+        float s = P.f[slotSh[k]][p.i];
+        for (int l = 0; l < L; ++l) {
+            float r = P.r[slotRh[k]][l][p.i];
+            s += DTh * r;
+            r *= P.c1[l];
+            float u2 = P.invRelax[l] * u;
+            u2 *= tauAv;
+            r -= u2;
+            r *= P.c2[l];
+            s += DTh * r;
+            P.r[slotRh[k]][l][p.i] = r;
+        }
+        u *= opS;
+        Sh[k] = s + u;
+    }
+    if (P.fs && p.y == 0) {
+        // FreeSurfaceViscoelastic::setModelparameter (FreeSurfaceViscoelastic.cpp:12-97)
+        float temp = -2.0f * mu * opS;
+        float temp2 = M * opP;
+        temp += temp2;
+        const float itemp2 = 1.0f / temp2;
+        const float sV = temp;
+        float sH = -1.0f * temp;
+        sH *= temp;
+        sH *= itemp2;
+        const float hsum = P.is3d ? vxx + vzz : vxx;
+        const int nx = P.is3d ? 2 : 1;
+        const int kk[2] = {0, 2};
+        for (int l = 0; l < L; ++l)
+            for (int q = 0; q < nx; ++q) S[kk[q]] -= DTh * R[kk[q]][l];
+        for (int q = 0; q < nx; ++q) S[kk[q]] += sH * hsum;
+        for (int q = 0; q < nx; ++q) S[kk[q]] -= sV * vyy;
+        float t3 = 2.0f * mu * tauS;
+        t3 -= M * tauP;
+        float ratio = 2.0f * mu * opS;
+        ratio /= M * opP;
+        ratio -= 1.0f;
+        for (int l = 0; l < L; ++l) {
+            float rv = t3; rv *= P.c2[l]; rv /= P.relaxTime[l];
+            float rh = t3; rh *= ratio; rh *= P.c2[l]; rh /= P.relaxTime[l];
+            for (int q = 0; q < nx; ++q) {
+                R[kk[q]][l] += rh * hsum;
+                R[kk[q]][l] -= rv * vyy;
+                S[kk[q]] += DTh * R[kk[q]][l];
+            }
+        }
+        S[1] = 0.0f;
+        for (int l = 0; l < L; ++l) R[1][l] = 0.0f;
+    }
+    if (P.abs) {
+        const float d = absDamp(P, p);
+        for (int k = 0; k < nN; ++k) S[k] *= d;
+        for (int k = 0; k < nS; ++k) Sh[k] *= d;
+    }
+    for (int k = 0; k < nN; ++k) {
+        P.f[slotS[k]][p.i] = S[k];
+        for (int l = 0; l < L; ++l) P.r[slotR[k]][l][p.i] = R[k][l];
+    }
+    for (int k = 0; k < nS; ++k) P.f[slotSh[k]][p.i] = Sh[k];
+}
+
+// --------------------------------------------------------------------------
+// SH / visco-SH: ForwardSolver2Dsh.cpp:137-190, ForwardSolver2Dviscosh.cpp:155-240
+// --------------------------------------------------------------------------
+template <int H>
+__global__ void __launch_bounds__(256) sh_v(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    float u = dX<H, false>(P, p, P.f[F_SXZ], P.Dxb, PS_SXZ_X);
+    float ut = P.fs ? dY<H, false>(P, p, P.f[F_SYZ], P.DybS, PS_SYZ_Y) : dY<H, false>(P, p, P.f[F_SYZ], P.Dyb, PS_SYZ_Y);
+    u += ut;
+    u *= LD(P.m[M_IR]);
+    P.f[F_VZ][p.i] += u;
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) sh_s(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    const float* vz = P.f[F_VZ];
+    const float d = P.abs ? absDamp(P, p) : 1.0f;
+    for (int k = 0; k < 2; ++k) {
+        float u = k == 0 ? dX<H, true>(P, p, vz, P.Dxf, PS_VZX) : dY<H, true>(P, p, vz, P.Dyf, PS_VZY);
+        u *= LD(P.m[k == 0 ? M_MUXZ : M_MUYZ]);
+        float s = P.f[k == 0 ? F_SXZ : F_SYZ][p.i];
+        if (P.L > 0) {
+            const float tauAv = LD(P.m[k == 0 ? M_TAUSXZ : M_TAUSYZ]);
+            const int rs = k == 0 ? R_XZ : R_YZ;
+            for (int l = 0; l < P.L; ++l) {
+                float r = P.r[rs][l][p.i];
+                s += P.DThalf * r;
+                r *= P.c1[l];
+                float u2 = P.invRelax[l] * u;
+                u2 *= tauAv;
+                r -= u2;
+                r *= P.c2[l];
+                s += P.DThalf * r;
+                P.r[rs][l][p.i] = r;
+            }
+            u *= LD(P.m[M_OPLTS]);
+        }
+        s += u;
+        P.f[k == 0 ? F_SXZ : F_SYZ][p.i] = s * d;
+    }
+}
+
+// --------------------------------------------------------------------------
+// EM TMz: FD2Dtmem::run (ForwardSolverEM/ForwardSolver2Dtmem.cpp:128-170)
+// --------------------------------------------------------------------------
+template <int H>
+__global__ void __launch_bounds__(256) tm_h(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    const float* ez = P.f[F_EZ];
+    float u = dY<H, true>(P, p, ez, P.Dyf, PS_EZY);
+    u *= LD(P.m[M_IMUYZ]);
+    P.f[F_HX][p.i] -= u;
+    float ut = dX<H, true>(P, p, ez, P.Dxf, PS_EZX);
+    u = -ut;
+    u *= LD(P.m[M_IMUXZ]);
+    P.f[F_HY][p.i] -= u;
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) tm_e(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    float u = dX<H, false>(P, p, P.f[F_HY], P.Dxb, PS_HYX);
+    float ut = dY<H, false>(P, p, P.f[F_HX], P.Dyb, PS_HXY);
+    u -= ut;
+    u *= LD(P.m[M_CBZ]);
+    float e = LD(P.m[M_CAZ]) * P.f[F_EZ][p.i];
+    e = e + u;
+    if (P.abs) e *= absDamp(P, p);
+    P.f[F_EZ][p.i] = e;
+}
+
+// EM TEz: FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:132-180)
+template <int H>
+__global__ void __launch_bounds__(256) te_h(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    float u = dX<H, true>(P, p, P.f[F_EY], P.Dxf, PS_EYX);
+    float ut = dY<H, true>(P, p, P.f[F_EX], P.Dyf, PS_EXY);
+    u -= ut;
+    u *= LD(P.m[M_IMUXY]);
+    P.f[F_HZ][p.i] -= u;
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) te_e(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    const float* hz = P.f[F_HZ];
+    const float d = P.abs ? absDamp(P, p) : 1.0f;
+    float u = dY<H, false>(P, p, hz, P.Dyb, PS_HZY);
+    u *= LD(P.m[M_CBX]);
+    float e = LD(P.m[M_CAX]) * P.f[F_EX][p.i];
+    P.f[F_EX][p.i] = (e + u) * d;
+    u = dX<H, false>(P, p, hz, P.Dxb, PS_HZX);
+    u *= LD(P.m[M_CBY]);
+    e = LD(P.m[M_CAY]) * P.f[F_EY][p.i];
+    P.f[F_EY][p.i] = (e - u) * d;
+}
+
+// --------------------------------------------------------------------------
+// ABS damping of the pass-1 fields (applied after pass 2 read them).
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) abs_frame_kernel(StepParams P, int f0, int f1, int f2)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    const float d = absDamp(P, p);
+    if (d == 1.0f) return;
+    if (f0 >= 0) P.f[f0][p.i] *= d;
+    if (f1 >= 0) P.f[f1][p.i] *= d;
+    if (f2 >= 0) P.f[f2][p.i] *= d;
+}
+
+// --------------------------------------------------------------------------
+// sources + receivers (SourceReceiverImpl.cpp:12-37 and the pressure variants
+// FDTDacoustic.cpp, FDTD2Delastic.cpp:12-49, FDTD3Delastic.cpp:12-53,
+// SourceReceiverImplEM.cpp): the raw sample of column t is added, then the
+// receivers copy column t. One block; t read from a device counter so the
+// same launch can be replayed from a CUDA graph.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ float* field_of(const SrcRecParams& Q, int type)
+{
+    if (Q.eq >= WAVE_EQ_TMEM) {
+        switch (type) {
+        case WAVE_TYPE_EZ: return Q.f[F_EZ];
+        case WAVE_TYPE_EX: return Q.f[F_EX];
+        case WAVE_TYPE_EY: return Q.f[F_EY];
+        default: return Q.f[F_HZ];
+        }
+    }
+    switch (type) {
+    case WAVE_TYPE_VX: return Q.f[F_VX];
+    case WAVE_TYPE_VY: return Q.f[F_VY];
+    case WAVE_TYPE_VZ: return Q.f[F_VZ];
+    default: return Q.f[F_P];
+    }
+}
+
+__global__ void __launch_bounds__(512) srcrec_kernel(SrcRecParams Q, int* tcounter)
+{
+    const int t = *tcounter;
+    const bool elasticP = (Q.eq == WAVE_EQ_ELASTIC || Q.eq == WAVE_EQ_VISCOELASTIC);
+    for (int type = 1; type <= 4; ++type) {
+        for (int s = threadIdx.x; s < Q.nsrc; s += blockDim.x) {
+            if (Q.stype[s] != type) continue;
+            const float v = Q.signals[(long long)s * Q.nt + t];
+            const long long i = Q.sidx[s];
+            if (Q.eq < WAVE_EQ_TMEM && type == WAVE_TYPE_P && elasticP) {
+                atomicAdd(Q.f[F_SXX] + i, v);
+                atomicAdd(Q.f[F_SYY] + i, v);
+                if (Q.is3d) atomicAdd(Q.f[F_SZZ] + i, v);
+            } else {
+                atomicAdd(field_of(Q, type) + i, v);
+            }
+        }
+        __syncthreads();
+    }
+    for (int r = threadIdx.x; r < Q.nrec; r += blockDim.x) {
+        const long long i = Q.ridx[r];
+        const int type = Q.rtype[r];
+        float v;
+        if (Q.eq < WAVE_EQ_TMEM && type == WAVE_TYPE_P && elasticP) {
+            v = Q.f[F_SXX][i];
+            v += Q.f[F_SYY][i];
+            if (Q.is3d) { v += Q.f[F_SZZ][i]; v /= 3.0f; }
+            else v *= 0.5f;
+        } else {
+            v = field_of(Q, type)[i];
+        }
+        Q.seis[(long long)r * Q.nt + t] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *tcounter = t + 1;
+}
+
+// --------------------------------------------------------------------------
+// NaN/Inf status (Simulation.cpp:519, WavefieldsSeismic.cpp:12-40) over every
+// point of a buffer; sets *flag when a non-finite value is found.
+// --------------------------------------------------------------------------
+__global__ void finite_kernel(const float* __restrict__ a, long long n, int* flag)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (!isfinite(a[i])) { *flag = 1; return; }
+    }
+}
+
+// --------------------------------------------------------------------------
+// model preparation (Modelparameter::prepareForModelling and the solvers'
+// prepareForModelling), all on the device.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ long long gidx(const PrepParams& G, int x, int y, int z) { return x + (long long)G.NX * (z + (long long)G.NZ * y); }
+
+__device__ __forceinline__ void gcoord(const PrepParams& G, long long i, int& x, int& y, int& z)
+{
+    y = (int)(i / ((long long)G.NX * G.NZ));
+    long long r = i - (long long)y * G.NX * G.NZ;
+    z = (int)(r / G.NX);
+    x = (int)(r - (long long)z * G.NX);
+}
+
+// 2-point average along an axis with the last point copied
+// (Modelparameter::calcAverageMatrixX/Y/Z, Modelparameter.cpp:336-420)
+__device__ __forceinline__ float avg2(const PrepParams& G, const float* a, long long i, int x, int y, int z, int axis)
+{
+    int nx = x, ny = y, nz = z;
+    bool ok;
+    if (axis == 0) { nx = x + 1; ok = nx < G.NX; }
+    else if (axis == 1) { ny = y + 1; ok = ny < G.NY; }
+    else { nz = z + 1; ok = nz < G.NZ; }
+    if (!ok) return 1.0f * a[i];
+    float s = 0.5f * a[i];
+    s += 0.5f * a[gidx(G, nx, ny, nz)];
+    return s;
+}
+
+// 4-point average in a plane with the edge fallbacks of
+// calc4PointAverageMatrixRow (Modelparameter.cpp:448-527). plane 0=XY,1=XZ,2=YZ.
+__device__ float avg4(const PrepParams& G, const float* a, long long i, int x, int y, int z, int plane)
+{
+    int p2x = x, p2y = y, p2z = z, p3x = x, p3y = y, p3z = z, p4x = x, p4y = y, p4z = z;
+    if (plane == 0) { p2x = x + 1; p3y = y + 1; p4x = x + 1; p4y = y + 1; }
+    else if (plane == 1) { p2x = x + 1; p3z = z + 1; p4x = x + 1; p4z = z + 1; }
+    else { p2y = y + 1; p3z = z + 1; p4y = y + 1; p4z = z + 1; }
+    const int maxX = max(x, max(p2x, max(p3x, p4x)));
+    const int maxY = max(y, max(p2y, max(p3y, p4y)));
+    const int maxZ = max(z, max(p2z, max(p3z, p4z)));
+    const bool inX = maxX < G.NX, inY = maxY < G.NY, inZ = maxZ < G.NZ;
+    if (inX && inY && inZ) {
+        float s = 0.25f * a[i];
+        s += 0.25f * a[gidx(G, p2x, p2y, p2z)];
+        s += 0.25f * a[gidx(G, p3x, p3y, p3z)];
+        s += 0.25f * a[gidx(G, p4x, p4y, p4z)];
+        return s;
+    }
+    if (inX && !inY && inZ) { float s = 0.5f * a[gidx(G, maxX, y, maxZ)]; s += 0.5f * a[i]; return s; }
+    if (!inX && inY && inZ) { float s = 0.5f * a[gidx(G, x, maxY, maxZ)]; s += 0.5f * a[i]; return s; }
+    if (inX && inY && !inZ) { float s = 0.5f * a[gidx(G, maxX, maxY, z)]; s += 0.5f * a[i]; return s; }
+    if ((!inX && !inY && inZ) || (inX && !inY && !inZ) || (!inX && inY && !inZ)) return 1.0f * a[i];
+    return 0.0f;
+}
+
+__device__ __forceinline__ float inv_valid(float v)
+{
+    // calcInverseAveragedParameter + Common::replaceInvalid (Modelparameter.cpp:633-639)
+    float r = 1.0f / v;
+    return isfinite(r) ? r : 0.0f;
+}
+
+#define PREP_LOOP for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < G.N; i += (long long)gridDim.x * blockDim.x)
+
+// modulus = rho * v * v, divided by (1 + sum*tau) for visco media
+// (ModelparameterSeismic.cpp:131-136, Viscoelastic.cpp:650-715); optional clamp
+// of values below 1 (ModelparameterSeismic.cpp:424).
+__global__ void prep_modulus(PrepParams G, const float* rho, const float* v, const float* tau, float sum, int clamp, float* out)
+{
+    PREP_LOOP {
+        float s = rho[i];
+        s *= v[i];
+        s *= v[i];
+        if (tau) s = s / (1.0f + sum * tau[i]);
+        if (clamp && s < 1.0f) s = 1.0f;
+        out[i] = s;
+    }
+}
+
+__global__ void prep_inverse(PrepParams G, const float* a, float* out)
+{
+    PREP_LOOP { out[i] = 1.0f / a[i]; }
+}
+
+__global__ void prep_inv_avg2(PrepParams G, const float* a, int axis, float* out)
+{
+    PREP_LOOP {
+        int x, y, z;
+        gcoord(G, i, x, y, z);
+        out[i] = inv_valid(avg2(G, a, i, x, y, z, axis));
+    }
+}
+
+__global__ void prep_inv_avg4(PrepParams G, const float* a, int plane, float* out)
+{
+    PREP_LOOP {
+        int x, y, z;
+        gcoord(G, i, x, y, z);
+        out[i] = inv_valid(avg4(G, a, i, x, y, z, plane));
+    }
+}
+
+__global__ void prep_avg2(PrepParams G, const float* a, int axis, float* out)
+{
+    PREP_LOOP {
+        int x, y, z;
+        gcoord(G, i, x, y, z);
+        out[i] = avg2(G, a, i, x, y, z, axis);
+    }
+}
+
+__global__ void prep_avg4(PrepParams G, const float* a, int plane, float* out)
+{
+    PREP_LOOP {
+        int x, y, z;
+        gcoord(G, i, x, y, z);
+        out[i] = avg4(G, a, i, x, y, z, plane);
+    }
+}
+
+// harmonic S-modulus average with the vacuum threshold
+// (ModelparameterSeismic::calcAveragedSWaveModulus, ModelparameterSeismic.cpp:421-432):
+// mu_av = 1 / A*(1/mu), values below 4 set to 0. mode: 0..2 = 4-point plane, 3+axis = 2-point
+__global__ void prep_harmonic(PrepParams G, const float* invmu, int mode, float* out)
+{
+    PREP_LOOP {
+        int x, y, z;
+        gcoord(G, i, x, y, z);
+        float av = mode < 3 ? avg4(G, invmu, i, x, y, z, mode) : avg2(G, invmu, i, x, y, z, mode - 3);
+        float r = 1.0f / av;
+        out[i] = r < 4.0f ? 0.0f : r;
+    }
+}
+
+__global__ void prep_one_plus(PrepParams G, const float* tau, float L, float* out)
+{
+    PREP_LOOP { out[i] = 1.0f + L * tau[i]; }
+}
+
+__global__ void prep_scale(PrepParams G, const float* a, float s, float* out)
+{
+    PREP_LOOP { out[i] = a[i] * s; }
+}
+
+// Ca, Cb (ForwardSolverEM.cpp:14-66)
+__global__ void prep_cacb(PrepParams G, const float* eps, const float* sig, float DT, float* ca, float* cb)
+{
+    PREP_LOOP {
+        float c = 0.5f / eps[i];
+        c *= sig[i];
+        c *= DT;
+        c += 1.0f;
+        const float cinv = 1.0f / c;
+        float a = 0.5f / eps[i];
+        a *= sig[i];
+        a *= DT;
+        a = 1.0f - a;
+        ca[i] = a * cinv;
+        float b = 1.0f / eps[i];
+        cb[i] = b * cinv;
+    }
+}
+
+// --------------------------------------------------------------------------
+// launch table
+// --------------------------------------------------------------------------
+#define WAVE_KTAB(name) { name<1>, name<2>, name<3>, name<4>, name<5>, name<6> }
+
+StepKernel kernel_for(int eq, int pass, int H)
+{
+    static const StepKernel ac_v[6] = WAVE_KTAB(acoustic_v), ac_p[6] = WAVE_KTAB(acoustic_p);
+    static const StepKernel el_v[6] = WAVE_KTAB(elastic_v), el_s[6] = WAVE_KTAB(elastic_s), vi_s[6] = WAVE_KTAB(visco_s);
+    static const StepKernel s_v[6] = WAVE_KTAB(sh_v), s_s[6] = WAVE_KTAB(sh_s);
+    static const StepKernel tmh[6] = WAVE_KTAB(tm_h), tme[6] = WAVE_KTAB(tm_e), teh[6] = WAVE_KTAB(te_h), tee[6] = WAVE_KTAB(te_e);
+    if (H < 1 || H > 6) return nullptr;
+    const int k = H - 1;
+    switch (eq) {
+    case WAVE_EQ_ACOUSTIC: return pass == 0 ? ac_v[k] : ac_p[k];
+    case WAVE_EQ_ELASTIC: return pass == 0 ? el_v[k] : el_s[k];
+    case WAVE_EQ_VISCOELASTIC: return pass == 0 ? el_v[k] : vi_s[k];
+    case WAVE_EQ_SH:
+    case WAVE_EQ_VISCOSH: return pass == 0 ? s_v[k] : s_s[k];
+    case WAVE_EQ_TMEM: return pass == 0 ? tmh[k] : tme[k];
+    case WAVE_EQ_EMEM: return pass == 0 ? teh[k] : tee[k];
+    default: return nullptr;
+    }
+}
+
+__global__ void set_counter_kernel(int* c, int v) { *c = v; }
+
+void launch_set_counter(int* c, int v, cudaStream_t s) { set_counter_kernel<<<1, 1, 0, s>>>(c, v); }
+
+void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s)
+{
+    srcrec_kernel<<<1, 512, 0, s>>>(Q, tcounter);
+}
+
+void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s)
+{
+    abs_frame_kernel<<<grid, block, 0, s>>>(P, f0, f1, f2);
+}
+
+void launch_finite(const float* a, long long n, int* flag, cudaStream_t s)
+{
+    finite_kernel<<<1216, 256, 0, s>>>(a, n, flag);
+}
+
+// model preparation launchers
+#define PREP_GRID 1216, 256, 0, s
+void k_modulus(PrepParams G, const float* rho, const float* v, const float* tau, float sum, int clamp, float* out, cudaStream_t s) { prep_modulus<<<PREP_GRID>>>(G, rho, v, tau, sum, clamp, out); }
+void k_inverse(PrepParams G, const float* a, float* out, cudaStream_t s) { prep_inverse<<<PREP_GRID>>>(G, a, out); }
+void k_inv_avg2(PrepParams G, const float* a, int axis, float* out, cudaStream_t s) { prep_inv_avg2<<<PREP_GRID>>>(G, a, axis, out); }
+void k_inv_avg4(PrepParams G, const float* a, int plane, float* out, cudaStream_t s) { prep_inv_avg4<<<PREP_GRID>>>(G, a, plane, out); }
+void k_avg2(PrepParams G, const float* a, int axis, float* out, cudaStream_t s) { prep_avg2<<<PREP_GRID>>>(G, a, axis, out); }
+void k_avg4(PrepParams G, const float* a, int plane, float* out, cudaStream_t s) { prep_avg4<<<PREP_GRID>>>(G, a, plane, out); }
+void k_harmonic(PrepParams G, const float* invmu, int mode, float* out, cudaStream_t s) { prep_harmonic<<<PREP_GRID>>>(G, invmu, mode, out); }
+void k_one_plus(PrepParams G, const float* tau, float L, float* out, cudaStream_t s) { prep_one_plus<<<PREP_GRID>>>(G, tau, L, out); }
+void k_scale(PrepParams G, const float* a, float sc, float* out, cudaStream_t s) { prep_scale<<<PREP_GRID>>>(G, a, sc, out); }
+void k_cacb(PrepParams G, const float* eps, const float* sig, float DT, float* ca, float* cb, cudaStream_t s) { prep_cacb<<<PREP_GRID>>>(G, eps, sig, DT, ca, cb); }
+
+} // namespace wave

@@ -1,0 +1,837 @@
+// solver.cu — the solver handle behind the C ABI of include/wave.h:
+// device-resident SoA state, model preparation on the device, the per-step
+// kernel sequence, CUDA-graph replay of multi-step calls, seismogram buffers,
+// checkpoint blobs and the finite check.
+//
+// Reference interface replaced: ForwardSolver<ValueType> (ForwardSolver/ForwardSolver.hpp:25-70)
+// created by ForwardSolver::Factory::Create (ForwardSolverFactory.cpp:4-67) and
+// driven once per time step by Simulation.cpp:444-476.
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <stdexcept>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "wave_internal.h"
+
+using namespace wave;
+
+namespace {
+
+thread_local std::string g_create_err;
+constexpr int kGraphSteps = 16;
+
+bool eq_visco(int eq) { return eq == WAVE_EQ_VISCOELASTIC || eq == WAVE_EQ_VISCOSH || eq == WAVE_EQ_VISCOTMEM || eq == WAVE_EQ_VISCOEMEM; }
+bool eq_em(int eq) { return eq >= WAVE_EQ_TMEM; }
+
+// psi slot -> axis (0 x, 1 y, 2 z)
+int psi_axis(int s)
+{
+    switch (s) {
+    case PS_P_X: case PS_VXX: case PS_SXX_X: case PS_SXY_X: case PS_SXZ_X: case PS_VYX: case PS_VZX:
+    case PS_EZX: case PS_HYX: case PS_EYX: case PS_HZX: return 0;
+    case PS_P_Z: case PS_VZZ: case PS_SXZ_Z: case PS_SYZ_Z: case PS_SZZ_Z: case PS_VXZ: case PS_VYZ: return 2;
+    default: return 1;
+    }
+}
+
+} // namespace
+
+struct wave_handle {
+    wave_config cfg{};
+    int NT = 0, NX = 1, NY = 1, NZ = 1, H = 1, L = 0;
+    long long N = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    std::vector<void*> allocs;
+    float* f[F_COUNT] = {};
+    float* r[R_COUNT][kMaxL] = {};
+    float* psi[PS_COUNT] = {};
+    long long psiLen[PS_COUNT] = {};
+    float* m[M_COUNT] = {};
+    float* opTab[8] = {};
+    float* cpmlProf[3][4] = {};
+    float* absCoeff = nullptr;
+    int* tcounter = nullptr;
+    int* flag = nullptr;
+
+    long long* sidx = nullptr; int* stype = nullptr; float* signals = nullptr; int nsrc = 0;
+    long long* ridx = nullptr; int* rtype = nullptr; float* seis = nullptr; int nrec = 0;
+
+    StepParams sp{};
+    SrcRecParams sq{};
+    dim3 grid, block;
+    bool modelSet = false;
+    std::vector<int> fields;          // allocated field slots
+    std::vector<int> pass1Fields;     // fields updated in pass 1 (ABS after pass 2)
+
+    cudaGraphExec_t graph = nullptr;
+    bool graphDirty = true;
+
+    bool timing = false;
+    double velMsSum = 0, strMsSum = 0;
+    long long timedSteps = 0;
+    long long launches = 0;
+
+    ~wave_handle()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (void* p : allocs) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    template <class T>
+    T* alloc(size_t count)
+    {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
+        if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    void check(cudaError_t e, const char* what)
+    {
+        if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+    }
+};
+
+namespace {
+
+
+int fail(wave_handle* h, int code, const std::string& msg)
+{
+    if (h) h->err = msg;
+    else g_create_err = msg;
+    return code;
+}
+
+#define WAVE_TRY(h, ...)                                                    \
+    try {                                                                   \
+        __VA_ARGS__                                                         \
+    } catch (std::exception & ex) {                                         \
+        return fail(h, WAVE_ERR_CUDA, ex.what());                           \
+    }
+
+int nt_from(const wave_config& c)
+{
+    float T = static_cast<float>(c.T), DT = static_cast<float>(c.DT);
+    return static_cast<int>(T / DT + 0.5f);
+}
+
+Op1D to_device(wave_handle* h, const OpHost& o, int slot)
+{
+    Op1D d;
+    d.n = o.n; d.E = o.E; d.full = o.full;
+    for (int k = 0; k < kTabW; ++k) d.w[k] = o.w[k];
+    float* t = h->alloc<float>(o.tab.size());
+    h->check(cudaMemcpy(t, o.tab.data(), o.tab.size() * sizeof(float), cudaMemcpyHostToDevice), "table upload");
+    h->opTab[slot] = t;
+    d.tab = t;
+    return d;
+}
+
+Cpml1D cpml_to_device(wave_handle* h, const CpmlHost& c, int axis, int n, int w)
+{
+    Cpml1D d;
+    d.n = n; d.w = w; d.ns = c.ns; d.lo = c.lo; d.on = 1;
+    const std::vector<float>* src[4] = {&c.a_full, &c.b_full, &c.a_half, &c.b_half};
+    for (int k = 0; k < 4; ++k) {
+        float* p = h->alloc<float>(n);
+        h->check(cudaMemcpy(p, src[k]->data(), n * sizeof(float), cudaMemcpyHostToDevice), "cpml upload");
+        h->cpmlProf[axis][k] = p;
+    }
+    d.a_full = h->cpmlProf[axis][0]; d.b_full = h->cpmlProf[axis][1];
+    d.a_half = h->cpmlProf[axis][2]; d.b_half = h->cpmlProf[axis][3];
+    return d;
+}
+
+std::vector<int> field_list(int eq, bool is3d)
+{
+    switch (eq) {
+    case WAVE_EQ_ACOUSTIC: return is3d ? std::vector<int>{F_VX, F_VY, F_VZ, F_P} : std::vector<int>{F_VX, F_VY, F_P};
+    case WAVE_EQ_ELASTIC:
+    case WAVE_EQ_VISCOELASTIC:
+        return is3d ? std::vector<int>{F_VX, F_VY, F_VZ, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ}
+                    : std::vector<int>{F_VX, F_VY, F_SXX, F_SYY, F_SXY};
+    case WAVE_EQ_SH:
+    case WAVE_EQ_VISCOSH: return {F_VZ, F_SXZ, F_SYZ};
+    case WAVE_EQ_TMEM: return {F_HX, F_HY, F_EZ};
+    case WAVE_EQ_EMEM: return {F_HZ, F_EX, F_EY};
+    default: return {};
+    }
+}
+
+std::vector<int> pass1_list(int eq, bool is3d)
+{
+    switch (eq) {
+    case WAVE_EQ_ACOUSTIC:
+    case WAVE_EQ_ELASTIC:
+    case WAVE_EQ_VISCOELASTIC: return is3d ? std::vector<int>{F_VX, F_VY, F_VZ} : std::vector<int>{F_VX, F_VY};
+    case WAVE_EQ_SH:
+    case WAVE_EQ_VISCOSH: return {F_VZ};
+    case WAVE_EQ_TMEM: return {F_HX, F_HY};
+    case WAVE_EQ_EMEM: return {F_HZ};
+    default: return {};
+    }
+}
+
+std::vector<int> mem_list(int eq, bool is3d)
+{
+    if (eq == WAVE_EQ_VISCOELASTIC) return is3d ? std::vector<int>{R_XX, R_YY, R_ZZ, R_XY, R_XZ, R_YZ} : std::vector<int>{R_XX, R_YY, R_XY};
+    if (eq == WAVE_EQ_VISCOSH) return {R_XZ, R_YZ};
+    return {};
+}
+
+std::vector<int> psi_list(int eq, bool is3d)
+{
+    switch (eq) {
+    case WAVE_EQ_ACOUSTIC:
+        return is3d ? std::vector<int>{PS_P_X, PS_P_Y, PS_P_Z, PS_VXX, PS_VYY, PS_VZZ} : std::vector<int>{PS_P_X, PS_P_Y, PS_VXX, PS_VYY};
+    case WAVE_EQ_ELASTIC:
+    case WAVE_EQ_VISCOELASTIC:
+        if (is3d)
+            return {PS_SXX_X, PS_SXY_Y, PS_SXZ_Z, PS_SXY_X, PS_SYY_Y, PS_SYZ_Z, PS_SXZ_X, PS_SYZ_Y, PS_SZZ_Z,
+                    PS_VXX, PS_VYY, PS_VZZ, PS_VXY, PS_VYX, PS_VXZ, PS_VZX, PS_VYZ, PS_VZY};
+        return {PS_SXX_X, PS_SXY_Y, PS_SXY_X, PS_SYY_Y, PS_VXX, PS_VYY, PS_VXY, PS_VYX};
+    case WAVE_EQ_SH:
+    case WAVE_EQ_VISCOSH: return {PS_SXZ_X, PS_SYZ_Y, PS_VZX, PS_VZY};
+    case WAVE_EQ_TMEM: return {PS_EZY, PS_EZX, PS_HYX, PS_HXY};
+    case WAVE_EQ_EMEM: return {PS_EYX, PS_EXY, PS_HZY, PS_HZX};
+    default: return {};
+    }
+}
+
+// component types the reference accepts per equation
+// (SourceReceiverImpl/FDTD2Dsh.hpp:29-34, ForwardSolverEM/SourceReceiverImpl/FDTD2Dtmem.hpp:29-34, ...)
+bool type_ok(int eq, bool is3d, int type, bool source)
+{
+    (void)source;
+    switch (eq) {
+    case WAVE_EQ_ACOUSTIC:
+    case WAVE_EQ_ELASTIC:
+    case WAVE_EQ_VISCOELASTIC: return type >= 1 && type <= (is3d ? 4 : 3);
+    case WAVE_EQ_SH:
+    case WAVE_EQ_VISCOSH: return type == WAVE_TYPE_VZ;
+    case WAVE_EQ_TMEM: return type == WAVE_TYPE_EZ;
+    case WAVE_EQ_EMEM: return type == WAVE_TYPE_EX || type == WAVE_TYPE_EY || type == WAVE_TYPE_HZ;
+    default: return false;
+    }
+}
+
+void launch_step(wave_handle* h)
+{
+    StepKernel k1 = kernel_for(h->cfg.equation, 0, h->H);
+    StepKernel k2 = kernel_for(h->cfg.equation, 1, h->H);
+    k1<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+    k2<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+    h->launches += 2;
+    if (h->sp.abs) {
+        const auto& p1 = h->pass1Fields;
+        launch_abs_frame(h->sp, h->grid, h->block, p1.size() > 0 ? p1[0] : -1, p1.size() > 1 ? p1[1] : -1,
+                         p1.size() > 2 ? p1[2] : -1, h->stream);
+        h->launches += 1;
+    }
+    launch_srcrec(h->sq, h->tcounter, h->stream);
+    h->launches += 1;
+}
+
+void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
+{
+    StepKernel k1 = kernel_for(h->cfg.equation, 0, h->H);
+    StepKernel k2 = kernel_for(h->cfg.equation, 1, h->H);
+    cudaEvent_t a, b, c;
+    cudaEventCreate(&a); cudaEventCreate(&b); cudaEventCreate(&c);
+    cudaEventRecord(a, h->stream);
+    k1<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+    cudaEventRecord(b, h->stream);
+    k2<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+    cudaEventRecord(c, h->stream);
+    ev.push_back(a); ev.push_back(b); ev.push_back(c);
+    h->launches += 2;
+    if (h->sp.abs) {
+        const auto& p1 = h->pass1Fields;
+        launch_abs_frame(h->sp, h->grid, h->block, p1.size() > 0 ? p1[0] : -1, p1.size() > 1 ? p1[1] : -1,
+                         p1.size() > 2 ? p1[2] : -1, h->stream);
+        h->launches += 1;
+    }
+    launch_srcrec(h->sq, h->tcounter, h->stream);
+    h->launches += 1;
+}
+
+void build_graph(wave_handle* h)
+{
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    cudaGraph_t g;
+    h->check(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    long long before = h->launches;
+    for (int s = 0; s < kGraphSteps; ++s) launch_step(h);
+    h->launches = before;
+    h->check(cudaStreamEndCapture(h->stream, &g), "end capture");
+    h->check(cudaGraphInstantiate(&h->graph, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    h->graphDirty = false;
+}
+
+// Copies n floats from a host or device pointer into a fresh device buffer.
+float* stage(wave_handle* h, const float* p, size_t n, int mem, std::vector<float*>& tmp)
+{
+    if (!p) return nullptr;
+    float* d = nullptr;
+    h->check(cudaMallocAsync(&d, n * sizeof(float), h->stream), "cudaMallocAsync");
+    tmp.push_back(d);
+    h->check(cudaMemcpyAsync(d, p, n * sizeof(float), mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream), "model upload");
+    return d;
+}
+
+// state blob layout: fields (solver order), memory variables, psi slabs, the step counter
+std::vector<std::pair<void*, size_t>> state_parts(wave_handle* h)
+{
+    std::vector<std::pair<void*, size_t>> parts;
+    for (int f : h->fields) parts.push_back({h->f[f], h->N * sizeof(float)});
+    for (int rr = 0; rr < R_COUNT; ++rr)
+        for (int l = 0; l < kMaxL; ++l)
+            if (h->r[rr][l]) parts.push_back({h->r[rr][l], h->N * sizeof(float)});
+    for (int s = 0; s < PS_COUNT; ++s)
+        if (h->psi[s]) parts.push_back({h->psi[s], h->psiLen[s] * sizeof(float)});
+    parts.push_back({h->tcounter, sizeof(int)});
+    return parts;
+}
+
+} // namespace
+
+extern "C" {
+
+const char* wave_last_error(const wave_handle* h)
+{
+    if (!h) return g_create_err.c_str();
+    return h->err.c_str();
+}
+
+int wave_config_nt(const wave_config* cfg, int* nt)
+{
+    if (!cfg || !nt || cfg->DT <= 0) return fail(nullptr, WAVE_ERR_ARG, "wave_config_nt: invalid argument");
+    *nt = nt_from(*cfg);
+    return WAVE_OK;
+}
+
+int wave_config_from_file(const char* path, wave_config* cfg)
+{
+    if (!path || !cfg) return fail(nullptr, WAVE_ERR_ARG, "wave_config_from_file: null argument");
+    std::string err;
+    int rc = parse_config_file(path, cfg, err);
+    if (rc != WAVE_OK) return fail(nullptr, rc, err);
+    return WAVE_OK;
+}
+
+int wave_wavelet(int shape, int nt, double dt, double fc, double amp, double tshift, float* out)
+{
+    int rc = make_wavelet(shape, nt, dt, fc, amp, tshift, out);
+    if (rc != WAVE_OK) return fail(nullptr, rc, "wave_wavelet: invalid shape or parameter");
+    return WAVE_OK;
+}
+
+int wave_solver_create(const wave_config* cfg, wave_handle** out)
+{
+    if (!cfg || !out) return fail(nullptr, WAVE_ERR_ARG, "wave_solver_create: null argument");
+    *out = nullptr;
+    const wave_config& c = *cfg;
+    if (c.dimension != 2 && c.dimension != 3) return fail(nullptr, WAVE_ERR_ARG, "Unkown dimension");
+    if (c.equation < WAVE_EQ_ACOUSTIC || c.equation > WAVE_EQ_VISCOEMEM) return fail(nullptr, WAVE_ERR_ARG, "Unkown type");
+    const bool is3d = c.dimension == 3;
+    // the reference factory's combinations (ForwardSolverFactory.cpp:13-66)
+    if (is3d && (c.equation == WAVE_EQ_SH || c.equation == WAVE_EQ_VISCOSH || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_VISCOTMEM))
+        return fail(nullptr, WAVE_ERR_UNSUPPORTED, "no 3-D solver for this equation type in the reference factory");
+    if (c.equation == WAVE_EQ_VISCOTMEM || c.equation == WAVE_EQ_VISCOEMEM || (is3d && c.equation == WAVE_EQ_EMEM))
+        return fail(nullptr, WAVE_ERR_UNSUPPORTED, "visco-EM and 3-D EM solvers are not available in this build");
+    std::vector<double> coef;
+    if (!fd_coefficients(c.spatialFDorder, coef)) return fail(nullptr, WAVE_ERR_ARG, "spatialFDorder = " + std::to_string(c.spatialFDorder) + " Unsupported spatialFDorder value.");
+    if (c.NX < 1 || c.NY < 1 || (is3d && c.NZ < 1) || c.DH <= 0 || c.DT <= 0 || c.T <= 0)
+        return fail(nullptr, WAVE_ERR_ARG, "grid dimensions, DH, DT and T must be positive");
+    const long long NZ = is3d ? c.NZ : 1;
+    if (c.NX > (1 << 30) || (c.NY * NZ + 7) / 8 > 65535 || c.NX * c.NY * NZ > (1LL << 40))
+        return fail(nullptr, WAVE_ERR_ARG, "grid too large");
+    if (c.DampingBoundary < 0 || c.DampingBoundary > 2) return fail(nullptr, WAVE_ERR_ARG, "DampingBoundary must be 0, 1 or 2");
+    if (c.DampingBoundary != 0 && c.BoundaryWidth <= 0) return fail(nullptr, WAVE_ERR_ARG, "BoundaryWidth must be positive");
+    if (c.DampingBoundary == 1 && (c.DampingCoeff <= 0 || c.DampingCoeff >= 100)) return fail(nullptr, WAVE_ERR_ARG, "DampingCoeff must be in (0, 100)");
+    if (c.FreeSurface != 0 && c.FreeSurface != 1 && c.FreeSurface != 2) return fail(nullptr, WAVE_ERR_ARG, "FreeSurface must be 0, 1 or 2");
+    if (eq_visco(c.equation) && (c.numRelaxationMechanisms < 1 || c.numRelaxationMechanisms > kMaxL))
+        return fail(nullptr, WAVE_ERR_ARG, "numRelaxationMechanisms must be 1..4 for visco equations");
+    if (eq_visco(c.equation))
+        for (int l = 0; l < c.numRelaxationMechanisms; ++l)
+            if (c.relaxationFrequency[l] <= 0) return fail(nullptr, WAVE_ERR_ARG, "relaxationFrequency must be positive");
+
+    auto h = std::make_unique<wave_handle>();
+    try {
+        h->cfg = c;
+        h->cfg.NZ = NZ;
+        h->NX = static_cast<int>(c.NX); h->NY = static_cast<int>(c.NY); h->NZ = static_cast<int>(NZ);
+        h->N = (long long)h->NX * h->NY * h->NZ;
+        h->NT = nt_from(c);
+        h->H = c.spatialFDorder / 2;
+        h->L = eq_visco(c.equation) ? c.numRelaxationMechanisms : 0;
+        h->check(cudaGetDevice(&h->device), "cudaGetDevice");
+        h->check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        const float DT = static_cast<float>(c.DT), DH = static_cast<float>(c.DH);
+        const int stencil = c.useStencilMatrix ? 1 : 0, reduce = c.edgeOrderReduction ? 1 : 0;
+        const int q = c.spatialFDorder;
+        StepParams& P = h->sp;
+        P = StepParams{};
+        P.NX = h->NX; P.NY = h->NY; P.NZ = h->NZ; P.is3d = is3d; P.N = h->N;
+        P.Dxf = to_device(h.get(), build_op(h->NX, q, OP_F, stencil, reduce, DH, DT), 0);
+        P.Dxb = to_device(h.get(), build_op(h->NX, q, OP_B, stencil, reduce, DH, DT), 1);
+        P.Dyf = to_device(h.get(), build_op(h->NY, q, OP_F, stencil, reduce, DH, DT), 2);
+        P.Dyb = to_device(h.get(), build_op(h->NY, q, OP_B, stencil, reduce, DH, DT), 3);
+        if (is3d) {
+            P.Dzf = to_device(h.get(), build_op(h->NZ, q, OP_F, stencil, reduce, DH, DT), 4);
+            P.Dzb = to_device(h.get(), build_op(h->NZ, q, OP_B, stencil, reduce, DH, DT), 5);
+        }
+        P.fs = c.FreeSurface == 1 ? 1 : 0;
+        if (P.fs) {
+            P.DyfS = to_device(h.get(), build_op(h->NY, q, OP_FS_F, stencil, reduce, DH, DT), 6);
+            P.DybS = to_device(h.get(), build_op(h->NY, q, OP_FS_B, stencil, reduce, DH, DT), 7);
+        }
+        // fields
+        h->fields = field_list(c.equation, is3d);
+        h->pass1Fields = pass1_list(c.equation, is3d);
+        for (int f : h->fields) P.f[f] = h->f[f] = h->alloc<float>(h->N);
+        for (int rr : mem_list(c.equation, is3d))
+            for (int l = 0; l < h->L; ++l) P.r[rr][l] = h->r[rr][l] = h->alloc<float>(h->N);
+        // boundaries
+        P.useCpml = c.DampingBoundary == 2;
+        if (P.useCpml) {
+            const float np = static_cast<float>(c.NPower), fc = static_cast<float>(c.CenterFrequencyCPML), vm = static_cast<float>(c.VMaxCPML);
+            const int w = c.BoundaryWidth;
+            P.cx = cpml_to_device(h.get(), build_cpml(h->NX, w, false, np, fc, vm, DT, DH), 0, h->NX, w);
+            P.cy = cpml_to_device(h.get(), build_cpml(h->NY, w, c.FreeSurface != 0, np, fc, vm, DT, DH), 1, h->NY, w);
+            if (is3d) P.cz = cpml_to_device(h.get(), build_cpml(h->NZ, w, false, np, fc, vm, DT, DH), 2, h->NZ, w);
+            for (int s : psi_list(c.equation, is3d)) {
+                const int ax = psi_axis(s);
+                long long len = ax == 0 ? (long long)P.cx.ns * h->NZ * h->NY
+                               : ax == 1 ? (long long)h->NX * h->NZ * P.cy.ns
+                                         : (long long)h->NX * P.cz.ns * h->NY;
+                P.psi[s] = h->psi[s] = h->alloc<float>(len);
+                h->psiLen[s] = len;
+            }
+        }
+        P.abs = c.DampingBoundary == 1;
+        if (P.abs) {
+            auto coeff = build_abs_coeff(c.BoundaryWidth, static_cast<float>(c.DampingCoeff));
+            h->absCoeff = h->alloc<float>(coeff.size());
+            h->check(cudaMemcpy(h->absCoeff, coeff.data(), coeff.size() * sizeof(float), cudaMemcpyHostToDevice), "abs upload");
+            P.absW = c.BoundaryWidth;
+            P.absCoeff = h->absCoeff;
+        }
+        // visco coefficients (ForwardSolver3Dviscoelastic.cpp:56-66)
+        P.L = h->L;
+        P.DThalf = static_cast<float>(DT / 2.0);
+        for (int l = 0; l < h->L; ++l) {
+            const float rt = static_cast<float>(1.0 / (2.0 * M_PI * static_cast<float>(c.relaxationFrequency[l])));
+            P.relaxTime[l] = rt;
+            P.invRelax[l] = static_cast<float>(1.0 / rt);
+            P.c1[l] = static_cast<float>(1.0 - DT / (2.0 * rt));
+            P.c2[l] = static_cast<float>(1.0 / (1.0 + DT / (2.0 * rt)));
+        }
+        h->tcounter = h->alloc<int>(1);
+        h->flag = h->alloc<int>(1);
+        // launch shape: 32 x 8 threads over (x, z + NZ*y)
+        h->block = dim3(32, 8, 1);
+        h->grid = dim3((h->NX + 31) / 32, static_cast<unsigned>((static_cast<long long>(h->NY) * h->NZ + 7) / 8), 1);
+        // source/receiver parameters
+        SrcRecParams& Q = h->sq;
+        Q = SrcRecParams{};
+        Q.eq = c.equation; Q.is3d = is3d; Q.nt = h->NT;
+        for (int f = 0; f < F_COUNT; ++f) Q.f[f] = h->f[f];
+        int rc = wave_solver_reset(h.get());
+        if (rc != WAVE_OK) return fail(nullptr, rc, h->err);
+    } catch (std::exception& ex) {
+        return fail(nullptr, WAVE_ERR_CUDA, ex.what());
+    }
+    *out = h.release();
+    return WAVE_OK;
+}
+
+int wave_solver_destroy(wave_handle* h)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_solver_destroy: null handle");
+    cudaStreamSynchronize(h->stream);
+    delete h;
+    return WAVE_OK;
+}
+
+int wave_set_model(wave_handle* h, const float* rho, const float* vp, const float* vs, const float* taup,
+                   const float* taus, size_t n, int mem)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_model: null handle");
+    const int eq = h->cfg.equation;
+    if (eq_em(eq)) return fail(h, WAVE_ERR_ARG, "wave_set_model: EM equation, use wave_set_model_em");
+    if (n != static_cast<size_t>(h->N)) return fail(h, WAVE_ERR_ARG, "wave_set_model: n != NX*NY*NZ");
+    const bool needVp = eq != WAVE_EQ_SH && eq != WAVE_EQ_VISCOSH;
+    const bool needVs = eq != WAVE_EQ_ACOUSTIC;
+    const bool visco = eq_visco(eq);
+    if (!rho || (needVp && !vp) || (needVs && !vs) || (visco && !taus) || (eq == WAVE_EQ_VISCOELASTIC && !taup))
+        return fail(h, WAVE_ERR_ARG, "wave_set_model: a parameter the equation needs is NULL");
+    WAVE_TRY(h, {
+        const bool is3d = h->sp.is3d;
+        PrepParams G{h->NX, h->NY, h->NZ, h->N};
+        cudaStream_t s = h->stream;
+        std::vector<float*> tmp;
+        float* dRho = stage(h, rho, n, mem, tmp);
+        float* dVp = needVp ? stage(h, vp, n, mem, tmp) : nullptr;
+        float* dVs = needVs ? stage(h, vs, n, mem, tmp) : nullptr;
+        float* dTp = eq == WAVE_EQ_VISCOELASTIC ? stage(h, taup, n, mem, tmp) : nullptr;
+        float* dTs = visco ? stage(h, taus, n, mem, tmp) : nullptr;
+        auto mat = [&](int slot) {
+            if (!h->m[slot]) h->m[slot] = h->alloc<float>(h->N);
+            h->sp.m[slot] = h->m[slot];
+            return h->m[slot];
+        };
+        float sum = 0.0f; // visco modulus relaxation (Viscoelastic.cpp:650-715)
+        if (visco) {
+            const float w_ref = static_cast<float>(2.0 * M_PI * h->cfg.CenterFrequencyCPML);
+            for (int l = 0; l < h->L; ++l) {
+                const float ts = static_cast<float>(1.0 / (2.0 * M_PI * static_cast<float>(h->cfg.relaxationFrequency[l])));
+                sum += w_ref * w_ref * ts * ts / (1.0 + w_ref * w_ref * ts * ts);
+            }
+        }
+        if (needVp) k_modulus(G, dRho, dVp, dTp, sum, 0, mat(M_M), s);
+        if (needVs) k_modulus(G, dRho, dVs, visco ? dTs : nullptr, sum, 1, mat(M_MU), s);
+        if (eq == WAVE_EQ_SH || eq == WAVE_EQ_VISCOSH) {
+            k_inverse(G, dRho, mat(M_IR), s);
+            float* inv = nullptr;
+            h->check(cudaMallocAsync(&inv, n * sizeof(float), s), "cudaMallocAsync");
+            tmp.push_back(inv);
+            k_inverse(G, h->m[M_MU], inv, s);
+            k_harmonic(G, inv, 3, mat(M_MUXZ), s);   // 2-point along x (SH.cpp:429)
+            k_harmonic(G, inv, 4, mat(M_MUYZ), s);   // 2-point along y (SH.cpp:430)
+            if (visco) {
+                k_avg2(G, dTs, 0, mat(M_TAUSXZ), s);
+                k_avg2(G, dTs, 1, mat(M_TAUSYZ), s);
+                k_one_plus(G, dTs, static_cast<float>(h->L), mat(M_OPLTS), s);
+            }
+        } else {
+            k_inv_avg2(G, dRho, 0, mat(M_IRX), s);
+            k_inv_avg2(G, dRho, 1, mat(M_IRY), s);
+            if (is3d) k_inv_avg2(G, dRho, 2, mat(M_IRZ), s);
+            if (needVs) {
+                float* inv = nullptr;
+                h->check(cudaMallocAsync(&inv, n * sizeof(float), s), "cudaMallocAsync");
+                tmp.push_back(inv);
+                k_inverse(G, h->m[M_MU], inv, s);
+                k_harmonic(G, inv, 0, mat(M_MUXY), s);
+                if (is3d) {
+                    k_harmonic(G, inv, 1, mat(M_MUXZ), s);
+                    k_harmonic(G, inv, 2, mat(M_MUYZ), s);
+                }
+            }
+            if (eq == WAVE_EQ_VISCOELASTIC) {
+                h->check(cudaMemcpyAsync(mat(M_TAUP), dTp, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+                h->check(cudaMemcpyAsync(mat(M_TAUS), dTs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+                k_avg4(G, dTs, 0, mat(M_TAUSXY), s);
+                if (is3d) {
+                    k_avg4(G, dTs, 1, mat(M_TAUSXZ), s);
+                    k_avg4(G, dTs, 2, mat(M_TAUSYZ), s);
+                }
+                k_one_plus(G, dTp, static_cast<float>(h->L), mat(M_OPLTP), s);
+                k_one_plus(G, dTs, static_cast<float>(h->L), mat(M_OPLTS), s);
+            }
+        }
+        h->check(cudaGetLastError(), "model preparation");
+        for (float* p : tmp) cudaFreeAsync(p, s);
+        h->check(cudaStreamSynchronize(s), "model preparation");
+        h->modelSet = true;
+        h->graphDirty = true;
+    })
+    return WAVE_OK;
+}
+
+int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, const float* mu_r,
+                      const float* tau_eps, const float* tau_sigma, size_t n, int mem)
+{
+    (void)tau_eps; (void)tau_sigma;
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_model_em: null handle");
+    const int eq = h->cfg.equation;
+    if (!eq_em(eq)) return fail(h, WAVE_ERR_ARG, "wave_set_model_em: seismic equation, use wave_set_model");
+    if (n != static_cast<size_t>(h->N)) return fail(h, WAVE_ERR_ARG, "wave_set_model_em: n != NX*NY*NZ");
+    if (!eps_r || !sigma || !mu_r) return fail(h, WAVE_ERR_ARG, "wave_set_model_em: eps_r, sigma and mu_r are required");
+    WAVE_TRY(h, {
+        PrepParams G{h->NX, h->NY, h->NZ, h->N};
+        cudaStream_t s = h->stream;
+        std::vector<float*> tmp;
+        float* dEr = stage(h, eps_r, n, mem, tmp);
+        float* dSig = stage(h, sigma, n, mem, tmp);
+        float* dMr = stage(h, mu_r, n, mem, tmp);
+        auto mat = [&](int slot) {
+            if (!h->m[slot]) h->m[slot] = h->alloc<float>(h->N);
+            h->sp.m[slot] = h->m[slot];
+            return h->m[slot];
+        };
+        auto scratch = [&]() {
+            float* p = nullptr;
+            h->check(cudaMallocAsync(&p, n * sizeof(float), s), "cudaMallocAsync");
+            tmp.push_back(p);
+            return p;
+        };
+        // absolute permittivity / permeability (TMEM.cpp:230-241, Modelparameter.hpp:359-360)
+        float* eps = scratch();
+        float* mu = scratch();
+        k_scale(G, dEr, 8.8541878176e-12f, eps, s);
+        k_scale(G, dMr, 1.2566370614e-6f, mu, s);
+        if (eq == WAVE_EQ_TMEM) {
+            // TMEM::calculateAveraging (TMEM.cpp:366-374), FD2Dtmem::prepareForModelling (ForwardSolver2Dtmem.cpp:77-106)
+            k_inv_avg2(G, mu, 0, mat(M_IMUXZ), s);
+            k_inv_avg2(G, mu, 1, mat(M_IMUYZ), s);
+            k_cacb(G, eps, dSig, static_cast<float>(h->cfg.DT), mat(M_CAZ), mat(M_CBZ), s);
+        } else {
+            // EMEM::calculateAveraging (EMEM.cpp:378-392), FD2Demem::prepareForModelling (ForwardSolver2Demem.cpp:72-85)
+            k_inv_avg4(G, mu, 0, mat(M_IMUXY), s);
+            float* ex = scratch(); float* sx = scratch(); float* ey = scratch(); float* sy = scratch();
+            k_avg2(G, eps, 0, ex, s); k_avg2(G, dSig, 0, sx, s);
+            k_avg2(G, eps, 1, ey, s); k_avg2(G, dSig, 1, sy, s);
+            k_cacb(G, ex, sx, static_cast<float>(h->cfg.DT), mat(M_CAX), mat(M_CBX), s);
+            k_cacb(G, ey, sy, static_cast<float>(h->cfg.DT), mat(M_CAY), mat(M_CBY), s);
+        }
+        h->check(cudaGetLastError(), "model preparation");
+        for (float* p : tmp) cudaFreeAsync(p, s);
+        h->check(cudaStreamSynchronize(s), "model preparation");
+        h->modelSet = true;
+        h->graphDirty = true;
+    })
+    return WAVE_OK;
+}
+
+int wave_set_sources(wave_handle* h, int n, const int64_t* idx, const int* type, const float* signals, int mem)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_sources: null handle");
+    if (n < 0 || (n > 0 && (!idx || !type || !signals))) return fail(h, WAVE_ERR_ARG, "wave_set_sources: invalid arguments");
+    for (int i = 0; i < n; ++i) {
+        if (idx[i] < 0 || idx[i] >= h->N) return fail(h, WAVE_ERR_ARG, "wave_set_sources: source index outside the grid");
+        if (!type_ok(h->cfg.equation, h->sp.is3d, type[i], true))
+            return fail(h, WAVE_ERR_UNSUPPORTED, "wave_set_sources: source type " + std::to_string(type[i]) + " can not be implemented for this equation");
+    }
+    WAVE_TRY(h, {
+        h->check(cudaStreamSynchronize(h->stream), "sync");
+        h->nsrc = n;
+        if (n > 0) {
+            h->sidx = h->alloc<long long>(n);
+            h->stype = h->alloc<int>(n);
+            h->signals = h->alloc<float>(static_cast<size_t>(n) * h->NT);
+            h->check(cudaMemcpy(h->sidx, idx, n * sizeof(long long), cudaMemcpyHostToDevice), "upload");
+            h->check(cudaMemcpy(h->stype, type, n * sizeof(int), cudaMemcpyHostToDevice), "upload");
+            h->check(cudaMemcpy(h->signals, signals, static_cast<size_t>(n) * h->NT * sizeof(float),
+                                mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice), "upload");
+        }
+        h->sq.nsrc = n; h->sq.sidx = h->sidx; h->sq.stype = h->stype; h->sq.signals = h->signals;
+        h->graphDirty = true;
+    })
+    return WAVE_OK;
+}
+
+int wave_set_receivers(wave_handle* h, int n, const int64_t* idx, const int* type)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_receivers: null handle");
+    if (n < 0 || (n > 0 && (!idx || !type))) return fail(h, WAVE_ERR_ARG, "wave_set_receivers: invalid arguments");
+    for (int i = 0; i < n; ++i) {
+        if (idx[i] < 0 || idx[i] >= h->N) return fail(h, WAVE_ERR_ARG, "wave_set_receivers: receiver index outside the grid");
+        if (!type_ok(h->cfg.equation, h->sp.is3d, type[i], false))
+            return fail(h, WAVE_ERR_UNSUPPORTED, "wave_set_receivers: receiver type " + std::to_string(type[i]) + " can not be implemented for this equation");
+    }
+    WAVE_TRY(h, {
+        h->check(cudaStreamSynchronize(h->stream), "sync");
+        h->nrec = n;
+        if (n > 0) {
+            h->ridx = h->alloc<long long>(n);
+            h->rtype = h->alloc<int>(n);
+            h->check(cudaMemcpy(h->ridx, idx, n * sizeof(long long), cudaMemcpyHostToDevice), "upload");
+            h->check(cudaMemcpy(h->rtype, type, n * sizeof(int), cudaMemcpyHostToDevice), "upload");
+        }
+        h->seis = h->alloc<float>(static_cast<size_t>(n > 0 ? n : 1) * h->NT);
+        h->check(cudaMemset(h->seis, 0, static_cast<size_t>(n > 0 ? n : 1) * h->NT * sizeof(float)), "memset");
+        h->sq.nrec = n; h->sq.ridx = h->ridx; h->sq.rtype = h->rtype; h->sq.seis = h->seis;
+        h->graphDirty = true;
+    })
+    return WAVE_OK;
+}
+
+int wave_solver_step(wave_handle* h, int t_begin, int t_end)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_solver_step: null handle");
+    if (t_begin < 0 || t_end < t_begin || t_end > h->NT) return fail(h, WAVE_ERR_ARG, "wave_solver_step: time range outside [0, NT]");
+    if (!h->modelSet) return fail(h, WAVE_ERR_STATE, "wave_solver_step: call wave_set_model first");
+    if (!h->seis) return fail(h, WAVE_ERR_STATE, "wave_solver_step: call wave_set_receivers first");
+    WAVE_TRY(h, {
+        launch_set_counter(h->tcounter, t_begin, h->stream);
+        h->launches += 1;
+        int t = t_begin;
+        if (h->timing) {
+            std::vector<cudaEvent_t> ev;
+            for (; t < t_end; ++t) launch_step_timed(h, ev);
+            h->check(cudaGetLastError(), "step launch");
+            h->check(cudaStreamSynchronize(h->stream), "step");
+            for (size_t k = 0; k + 2 < ev.size(); k += 3) {
+                float a = 0, b = 0;
+                cudaEventElapsedTime(&a, ev[k], ev[k + 1]);
+                cudaEventElapsedTime(&b, ev[k + 1], ev[k + 2]);
+                h->velMsSum += a;
+                h->strMsSum += b;
+                h->timedSteps += 1;
+            }
+            for (auto e : ev) cudaEventDestroy(e);
+        } else {
+            if (t_end - t >= kGraphSteps) {
+                if (h->graphDirty || !h->graph) build_graph(h);
+                const long long per = h->sp.abs ? 4 : 3;
+                for (; t + kGraphSteps <= t_end; t += kGraphSteps) {
+                    h->check(cudaGraphLaunch(h->graph, h->stream), "graph launch");
+                    h->launches += per * kGraphSteps;
+                }
+            }
+            for (; t < t_end; ++t) launch_step(h);
+            h->check(cudaGetLastError(), "step launch");
+        }
+    })
+    return WAVE_OK;
+}
+
+int wave_solver_reset(wave_handle* h)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_solver_reset: null handle");
+    WAVE_TRY(h, {
+        for (int f : h->fields) h->check(cudaMemsetAsync(h->f[f], 0, h->N * sizeof(float), h->stream), "memset");
+        for (int rr = 0; rr < R_COUNT; ++rr)
+            for (int l = 0; l < kMaxL; ++l)
+                if (h->r[rr][l]) h->check(cudaMemsetAsync(h->r[rr][l], 0, h->N * sizeof(float), h->stream), "memset");
+        for (int s = 0; s < PS_COUNT; ++s)
+            if (h->psi[s]) h->check(cudaMemsetAsync(h->psi[s], 0, h->psiLen[s] * sizeof(float), h->stream), "memset");
+        if (h->seis) h->check(cudaMemsetAsync(h->seis, 0, static_cast<size_t>(h->nrec > 0 ? h->nrec : 1) * h->NT * sizeof(float), h->stream), "memset");
+        h->check(cudaStreamSynchronize(h->stream), "reset");
+    })
+    return WAVE_OK;
+}
+
+int wave_get_seismograms(wave_handle* h, float* out, size_t count, int mem)
+{
+    if (!h || !out) return fail(h, WAVE_ERR_ARG, "wave_get_seismograms: null argument");
+    if (count != static_cast<size_t>(h->nrec) * h->NT) return fail(h, WAVE_ERR_ARG, "wave_get_seismograms: count != n_receivers*NT");
+    if (count == 0) return WAVE_OK;
+    WAVE_TRY(h, {
+        h->check(cudaMemcpyAsync(out, h->seis, count * sizeof(float), mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream), "seismogram copy");
+        h->check(cudaStreamSynchronize(h->stream), "seismogram copy");
+    })
+    return WAVE_OK;
+}
+
+int wave_check_finite(wave_handle* h)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_check_finite: null handle");
+    int flag = 0;
+    WAVE_TRY(h, {
+        h->check(cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream), "memset");
+        for (int f : h->fields) launch_finite(h->f[f], h->N, h->flag, h->stream);
+        if (h->seis && h->nrec > 0) launch_finite(h->seis, static_cast<long long>(h->nrec) * h->NT, h->flag, h->stream);
+        h->check(cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "flag copy");
+        h->check(cudaStreamSynchronize(h->stream), "finite check");
+    })
+    if (flag) return fail(h, WAVE_ERR_NONFINITE, "Infinite or NaN value in seismogram or/and velocity wavefield!");
+    return WAVE_OK;
+}
+
+int wave_get_state_size(wave_handle* h, size_t* bytes)
+{
+    if (!h || !bytes) return fail(h, WAVE_ERR_ARG, "wave_get_state_size: null argument");
+    size_t b = 0;
+    for (auto& p : state_parts(h)) b += p.second;
+    *bytes = b;
+    return WAVE_OK;
+}
+
+int wave_get_state(wave_handle* h, void* out, size_t bytes, int mem)
+{
+    size_t need = 0;
+    if (!h || !out) return fail(h, WAVE_ERR_ARG, "wave_get_state: null argument");
+    wave_get_state_size(h, &need);
+    if (bytes != need) return fail(h, WAVE_ERR_ARG, "wave_get_state: wrong blob size");
+    WAVE_TRY(h, {
+        char* o = static_cast<char*>(out);
+        for (auto& p : state_parts(h)) {
+            h->check(cudaMemcpyAsync(o, p.first, p.second, mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream), "state copy");
+            o += p.second;
+        }
+        h->check(cudaStreamSynchronize(h->stream), "state copy");
+    })
+    return WAVE_OK;
+}
+
+int wave_set_state(wave_handle* h, const void* in, size_t bytes, int mem)
+{
+    size_t need = 0;
+    if (!h || !in) return fail(h, WAVE_ERR_ARG, "wave_set_state: null argument");
+    wave_get_state_size(h, &need);
+    if (bytes != need) return fail(h, WAVE_ERR_ARG, "wave_set_state: wrong blob size");
+    WAVE_TRY(h, {
+        const char* o = static_cast<const char*>(in);
+        for (auto& p : state_parts(h)) {
+            h->check(cudaMemcpyAsync(p.first, o, p.second, mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream), "state copy");
+            o += p.second;
+        }
+        h->check(cudaStreamSynchronize(h->stream), "state copy");
+    })
+    return WAVE_OK;
+}
+
+int wave_get_nt(wave_handle* h, int* nt)
+{
+    if (!h || !nt) return fail(h, WAVE_ERR_ARG, "wave_get_nt: null argument");
+    *nt = h->NT;
+    return WAVE_OK;
+}
+
+int wave_get_num_receivers(wave_handle* h, int* n)
+{
+    if (!h || !n) return fail(h, WAVE_ERR_ARG, "wave_get_num_receivers: null argument");
+    *n = h->nrec;
+    return WAVE_OK;
+}
+
+int wave_get_stream(wave_handle* h, void** stream)
+{
+    if (!h || !stream) return fail(h, WAVE_ERR_ARG, "wave_get_stream: null argument");
+    *stream = h->stream;
+    return WAVE_OK;
+}
+
+int wave_get_launch_count(wave_handle* h, long long* count)
+{
+    if (!h || !count) return fail(h, WAVE_ERR_ARG, "wave_get_launch_count: null argument");
+    *count = h->launches;
+    return WAVE_OK;
+}
+
+int wave_set_timing(wave_handle* h, int on)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_timing: null handle");
+    h->timing = on != 0;
+    h->velMsSum = h->strMsSum = 0;
+    h->timedSteps = 0;
+    return WAVE_OK;
+}
+
+int wave_get_kernel_times(wave_handle* h, double* velocity_ms, double* stress_ms, long long* samples)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_get_kernel_times: null handle");
+    const double n = h->timedSteps > 0 ? static_cast<double>(h->timedSteps) : 1.0;
+    if (velocity_ms) *velocity_ms = h->velMsSum / n;
+    if (stress_ms) *stress_ms = h->strMsSum / n;
+    if (samples) *samples = h->timedSteps;
+    return WAVE_OK;
+}
+
+} // extern "C"
