@@ -179,6 +179,13 @@ int wave_get_launch_count(wave_handle* h, long long* count);
 int wave_set_timing(wave_handle* h, int on);
 int wave_get_kernel_times(wave_handle* h, double* velocity_ms, double* stress_ms, long long* samples);
 
+/* Kernel path: 0 = automatic (the streaming TMA kernels for 3-D elastic grids
+ * with NX % 4 == 0, the generic kernels otherwise), 1 = generic kernels only.
+ * wave_get_kernel_path reports whether the streaming kernels are active. The
+ * reference has no counterpart (LAMA picks its own SpMV kernels). */
+int wave_set_kernel_path(wave_handle* h, int path);
+int wave_get_kernel_path(wave_handle* h, int* streaming_active);
+
 /* Text of the last error on this handle (or of the last failed create when
  * h == NULL). Never NULL. */
 const char* wave_last_error(const wave_handle* h);

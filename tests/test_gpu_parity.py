@@ -41,10 +41,12 @@ def test_gpu_matches_reference_goldens(name, wave, refcpu):
 # ----------------------------------------------------------------------------
 # every equation x boundary x operator mode against the FP64 oracle
 # ----------------------------------------------------------------------------
-def make_case(refcpu, eq, dim, order, fs=0, boundary=2, stencil=0, reduce=1, L=2, seed=0):
+def make_case(refcpu, eq, dim, order, fs=0, boundary=2, stencil=0, reduce=1, L=2, seed=0, dims=None):
     rng = np.random.default_rng(seed)
     em = eq in ("tmem", "emem")
-    if dim == 2:
+    if dims is not None:
+        NX, NY, NZ = dims
+    elif dim == 2:
         NX, NY, NZ = 90, 70, 1
     else:
         NX, NY, NZ = 44, 38, 36
@@ -134,6 +136,34 @@ def test_gpu_matches_fp64_oracle(eq, dim, order, fs, boundary, stencil, reduce, 
     gpu, ref = run_both(wave, refcpu, case)
     assert np.abs(ref).max() > 0
     assert rel(gpu, ref) < TOL, f"relative L2 {rel(gpu, ref):.3e}"
+
+
+STREAMING = [
+    # (order, fs, boundary, stencil, reduce, (NX, NY, NZ)): NX % 4 == 0 selects the TMA kernels
+    (8, 1, 2, 0, 1, (64, 50, 48)),
+    (2, 0, 1, 1, 0, (40, 33, 37)),
+    (4, 1, 1, 0, 0, (44, 38, 36)),
+    (12, 0, 2, 0, 1, (48, 45, 35)),
+    (6, 1, 0, 0, 1, (36, 40, 33)),
+    (10, 1, 2, 1, 0, (52, 41, 30)),
+]
+
+
+@pytest.mark.parametrize("order,fs,boundary,stencil,reduce,dims", STREAMING)
+def test_streaming_elastic_kernels_match_oracle_and_generic(order, fs, boundary, stencil, reduce, dims, wave, refcpu):
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "elastic", 3, order, fs, boundary, stencil, reduce,
+                                                          dims=dims)
+    o = refcpu.Oracle(cfg, model, sidx, stype, sig, ridx, rtype, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    wc = to_wave_cfg(wave, cfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    s32 = sig.astype(np.float32)
+    fast = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=0, expect_streaming=True)
+    generic = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=1, expect_streaming=False)
+    assert rel(fast, ref) < TOL, f"streaming vs FP64 oracle {rel(fast, ref):.3e}"
+    assert rel(generic, ref) < TOL
+    assert rel(fast, generic) < 1e-5
 
 
 def test_multi_step_graph_equals_single_steps(wave, refcpu):

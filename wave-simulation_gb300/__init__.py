@@ -37,7 +37,8 @@ ABI_SYMBOLS = (
     "wave_solver_step", "wave_solver_reset", "wave_get_seismograms", "wave_check_finite",
     "wave_get_state_size", "wave_get_state", "wave_set_state", "wave_get_nt",
     "wave_get_num_receivers", "wave_get_stream", "wave_get_launch_count", "wave_set_timing",
-    "wave_get_kernel_times", "wave_last_error", "wave_wavelet",
+    "wave_get_kernel_times", "wave_last_error", "wave_wavelet", "wave_set_kernel_path",
+    "wave_get_kernel_path",
 )
 
 
@@ -152,6 +153,8 @@ def lib():
     L.wave_set_timing.argtypes = [P, I]
     L.wave_get_kernel_times.argtypes = [P, CP(ctypes.c_double), CP(ctypes.c_double), CP(ctypes.c_longlong)]
     L.wave_wavelet.argtypes = [I, I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
+    L.wave_set_kernel_path.argtypes = [P, I]
+    L.wave_get_kernel_path.argtypes = [P, CP(I)]
     _lib = L
     return L
 
@@ -279,6 +282,15 @@ class ForwardSolver:
         _check(self.h, lib().wave_get_launch_count(self.h, ctypes.byref(c)))
         return c.value
 
+    def set_kernel_path(self, path: int):
+        """0 = automatic (streaming kernels where they apply), 1 = generic kernels."""
+        _check(self.h, lib().wave_set_kernel_path(self.h, path))
+
+    def streaming_active(self) -> bool:
+        v = ctypes.c_int()
+        _check(self.h, lib().wave_get_kernel_path(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
     def set_timing(self, on: bool):
         _check(self.h, lib().wave_set_timing(self.h, int(on)))
 
@@ -312,7 +324,8 @@ class Factory:
         return ForwardSolver(d, t)
 
 
-def simulate(config: WaveConfig, model: dict, src_idx, src_type, signals, rec_idx, rec_type) -> np.ndarray:
+def simulate(config: WaveConfig, model: dict, src_idx, src_type, signals, rec_idx, rec_type,
+             kernel_path: int = 0, expect_streaming: bool | None = None) -> np.ndarray:
     """Runs one shot through the whole time loop (Simulation.cpp:432-533) and
     returns the seismograms (n_receivers x NT)."""
     dim = "3d" if config.dimension == 3 else "2d"
@@ -320,6 +333,9 @@ def simulate(config: WaveConfig, model: dict, src_idx, src_type, signals, rec_id
     s = Factory.Create(dim, eq).initForwardSolver(config)
     try:
         s.prepareForModelling(model)
+        s.set_kernel_path(kernel_path)
+        if expect_streaming is not None and s.streaming_active() != expect_streaming:
+            raise WaveError(WAVE_ERR_STATE, f"streaming kernels active={s.streaming_active()}, expected {expect_streaming}")
         s.setSources(src_idx, src_type, signals)
         s.setReceivers(rec_idx, rec_type)
         s.run(0, s.nt)

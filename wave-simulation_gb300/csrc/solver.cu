@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include "el3d.h"
 #include "wave_internal.h"
 
 using namespace wave;
@@ -73,6 +74,11 @@ struct wave_handle {
 
     cudaGraphExec_t graph = nullptr;
     bool graphDirty = true;
+
+    // streaming 3-D elastic path (kernels_el3d.cu)
+    El3dPlan el3d;
+    int kernelPath = 0;          // 0 = automatic, 1 = generic kernels only
+    int* errWord = nullptr;      // device error word of the bounded waits
 
     bool timing = false;
     double velMsSum = 0, strMsSum = 0;
@@ -224,12 +230,22 @@ bool type_ok(int eq, bool is3d, int type, bool source)
     }
 }
 
+bool streaming(const wave_handle* h) { return h->kernelPath == 0 && h->el3d.ready; }
+
+void launch_pass(wave_handle* h, int pass)
+{
+    if (streaming(h)) {
+        h->check(el3d_launch(h->el3d, h->sp, pass, h->stream), "streaming kernel launch");
+    } else {
+        StepKernel k = kernel_for(h->cfg.equation, pass, h->H);
+        k<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+    }
+}
+
 void launch_step(wave_handle* h)
 {
-    StepKernel k1 = kernel_for(h->cfg.equation, 0, h->H);
-    StepKernel k2 = kernel_for(h->cfg.equation, 1, h->H);
-    k1<<<h->grid, h->block, 0, h->stream>>>(h->sp);
-    k2<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+    launch_pass(h, 0);
+    launch_pass(h, 1);
     h->launches += 2;
     if (h->sp.abs) {
         const auto& p1 = h->pass1Fields;
@@ -243,14 +259,12 @@ void launch_step(wave_handle* h)
 
 void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
 {
-    StepKernel k1 = kernel_for(h->cfg.equation, 0, h->H);
-    StepKernel k2 = kernel_for(h->cfg.equation, 1, h->H);
     cudaEvent_t a, b, c;
     cudaEventCreate(&a); cudaEventCreate(&b); cudaEventCreate(&c);
     cudaEventRecord(a, h->stream);
-    k1<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+    launch_pass(h, 0);
     cudaEventRecord(b, h->stream);
-    k2<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+    launch_pass(h, 1);
     cudaEventRecord(c, h->stream);
     ev.push_back(a); ev.push_back(b); ev.push_back(c);
     h->launches += 2;
@@ -442,6 +456,8 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
         }
         h->tcounter = h->alloc<int>(1);
         h->flag = h->alloc<int>(1);
+        h->errWord = h->alloc<int>(1);
+        h->check(cudaMemset(h->errWord, 0, sizeof(int)), "memset");
         // launch shape: 32 x 8 threads over (x, z + NZ*y)
         h->block = dim3(32, 8, 1);
         h->grid = dim3((h->NX + 31) / 32, static_cast<unsigned>((static_cast<long long>(h->NY) * h->NZ + 7) / 8), 1);
@@ -502,6 +518,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
                 sum += w_ref * w_ref * ts * ts / (1.0 + w_ref * w_ref * ts * ts);
             }
         }
+        h->check(cudaMemcpyAsync(mat(M_RHO), dRho, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         if (needVp) k_modulus(G, dRho, dVp, dTp, sum, 0, mat(M_M), s);
         if (needVs) k_modulus(G, dRho, dVs, visco ? dTs : nullptr, sum, 1, mat(M_MU), s);
         if (eq == WAVE_EQ_SH || eq == WAVE_EQ_VISCOSH) {
@@ -547,6 +564,8 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         h->check(cudaGetLastError(), "model preparation");
         for (float* p : tmp) cudaFreeAsync(p, s);
         h->check(cudaStreamSynchronize(s), "model preparation");
+        if (eq == WAVE_EQ_ELASTIC && is3d)
+            el3d_prepare(h->el3d, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord);
         h->modelSet = true;
         h->graphDirty = true;
     })
@@ -717,6 +736,16 @@ int wave_solver_reset(wave_handle* h)
     return WAVE_OK;
 }
 
+// Reads and clears the device error word of the bounded waits.
+static int device_error(wave_handle* h)
+{
+    int e = 0;
+    if (!h->errWord) return 0;
+    if (cudaMemcpy(&e, h->errWord, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return WAVE_ERR_CUDA;
+    if (e) cudaMemset(h->errWord, 0, sizeof(int));
+    return e;
+}
+
 int wave_get_seismograms(wave_handle* h, float* out, size_t count, int mem)
 {
     if (!h || !out) return fail(h, WAVE_ERR_ARG, "wave_get_seismograms: null argument");
@@ -726,6 +755,7 @@ int wave_get_seismograms(wave_handle* h, float* out, size_t count, int mem)
         h->check(cudaMemcpyAsync(out, h->seis, count * sizeof(float), mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream), "seismogram copy");
         h->check(cudaStreamSynchronize(h->stream), "seismogram copy");
     })
+    if (int e = device_error(h)) return fail(h, e, "a bounded device wait ran out during the time steps");
     return WAVE_OK;
 }
 
@@ -740,6 +770,7 @@ int wave_check_finite(wave_handle* h)
         h->check(cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "flag copy");
         h->check(cudaStreamSynchronize(h->stream), "finite check");
     })
+    if (int e = device_error(h)) return fail(h, e, "a bounded device wait ran out during the time steps");
     if (flag) return fail(h, WAVE_ERR_NONFINITE, "Infinite or NaN value in seismogram or/and velocity wavefield!");
     return WAVE_OK;
 }
@@ -812,6 +843,22 @@ int wave_get_launch_count(wave_handle* h, long long* count)
 {
     if (!h || !count) return fail(h, WAVE_ERR_ARG, "wave_get_launch_count: null argument");
     *count = h->launches;
+    return WAVE_OK;
+}
+
+int wave_set_kernel_path(wave_handle* h, int path)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_kernel_path: null handle");
+    if (path != 0 && path != 1) return fail(h, WAVE_ERR_ARG, "wave_set_kernel_path: path must be 0 or 1");
+    h->kernelPath = path;
+    h->graphDirty = true;
+    return WAVE_OK;
+}
+
+int wave_get_kernel_path(wave_handle* h, int* streamingActive)
+{
+    if (!h || !streamingActive) return fail(h, WAVE_ERR_ARG, "wave_get_kernel_path: null argument");
+    *streamingActive = streaming(h) ? 1 : 0;
     return WAVE_OK;
 }
 

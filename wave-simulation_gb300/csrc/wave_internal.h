@@ -64,6 +64,7 @@ enum Mat {
     M_TAUP, M_TAUS, M_TAUSXY, M_TAUSXZ, M_TAUSYZ, M_OPLTP, M_OPLTS,
     M_CAX, M_CBX, M_CAY, M_CBY, M_CAZ, M_CBZ, M_IMUXY, M_IMUXZ, M_IMUYZ,
     M_CD0, M_CD1, M_CD2, M_CD3,   // visco-EM Cd per mechanism (x/y/z share for 2-D TM)
+    M_RHO,                        // density, kept for kernels that average it in-kernel
     M_COUNT
 };
 

@@ -1,0 +1,197 @@
+// wave_simulation.cpp — command-line driver that runs a reference parameter
+// file end to end on the GPU solver, the way Simulation.cpp:36-570 does for the
+// reference: read the configuration, build the model (homogeneous from the
+// velocityP/velocityS/rho keys, or MatrixMarket files <ModelFilename>.<p>.mtx
+// for ModelRead=1), loop over the shots of <SourceFilename>.txt, generate the
+// wavelets, run the time loop and write <SeismogramFilename>.shot_<n>.<c>.mtx.
+//
+//   wave_simulation <parameter file>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <set>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "forward_solver.hpp"
+
+namespace {
+
+std::map<std::string, std::string> read_keys(const std::string& path)
+{
+    std::map<std::string, std::string> m;
+    std::ifstream f(path);
+    std::string line;
+    while (std::getline(f, line)) {
+        size_t end = line.size(), c = line.find('#');
+        if (c != std::string::npos) {
+            if (c == 0) continue;
+            end = c;
+        }
+        size_t e = line.find('=');
+        if (e == std::string::npos) continue;
+        std::string k = line.substr(0, e);
+        for (auto& ch : k) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+        m[k] = line.substr(e + 1, end > e ? end - e - 1 : 0);
+    }
+    return m;
+}
+
+template <class T>
+T key(const std::map<std::string, std::string>& m, const char* k, T def)
+{
+    std::string kk(k);
+    for (auto& ch : kk) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+    auto it = m.find(kk);
+    if (it == m.end()) return def;
+    std::istringstream in(it->second);
+    T v = def;
+    in >> v;
+    return in.fail() ? def : v;
+}
+
+std::vector<float> read_mtx_vector(const std::string& path, size_t n)
+{
+    std::ifstream f(path);
+    if (!f.good()) throw wave::gpu::Error(WAVE_ERR_IO, "cannot open " + path);
+    std::string line;
+    while (std::getline(f, line))
+        if (!line.empty() && line[0] != '%') break;
+    std::vector<float> v;
+    v.reserve(n);
+    double x;
+    while (f >> x) v.push_back(static_cast<float>(x));
+    if (v.size() != n) throw wave::gpu::Error(WAVE_ERR_IO, path + ": wrong number of values");
+    return v;
+}
+
+void write_mtx(const std::string& path, const std::vector<float>& data, int ntr, int nt)
+{
+    std::ofstream f(path);
+    f << "%%MatrixMarket matrix array real general\n" << ntr << " " << nt << "\n";
+    char buf[64];
+    for (int t = 0; t < nt; ++t)          // column-major: trace index fastest (Seismogram.cpp mtx layout)
+        for (int r = 0; r < ntr; ++r) {
+            std::snprintf(buf, sizeof(buf), "%.9g\n", data[static_cast<size_t>(r) * nt + t]);
+            f << buf;
+        }
+}
+
+} // namespace
+
+int main(int argc, char** argv)
+{
+    if (argc != 2) {
+        std::cerr << "usage: wave_simulation <parameter file>\n";
+        return 2;
+    }
+    try {
+        wave_config cfg;
+        wave::gpu::check(nullptr, wave_config_from_file(argv[1], &cfg));
+        auto keys = read_keys(argv[1]);
+        const std::string dir = [&] {
+            std::string p(argv[1]);
+            size_t s = p.find_last_of('/');
+            return s == std::string::npos ? std::string(".") : p.substr(0, s);
+        }();
+        const size_t n = static_cast<size_t>(cfg.NX * cfg.NY * (cfg.dimension == 3 ? cfg.NZ : 1));
+        wave::gpu::Model model;
+        const bool em = cfg.equation >= WAVE_EQ_TMEM;
+        const std::string mf = key<std::string>(keys, "ModelFilename", "model/model");
+        if (key<int>(keys, "ModelRead", 0) == 1) {
+            auto rd = [&](const char* p) { return read_mtx_vector(dir + "/../" + mf + "." + p + ".mtx", n); };
+            if (em) { model.eps_r = rd("epsilonr"); model.sigma = rd("sigma"); model.mu_r = rd("mur"); }
+            else {
+                model.rho = rd("density");
+                if (cfg.equation != WAVE_EQ_SH && cfg.equation != WAVE_EQ_VISCOSH) model.vp = rd("vp");
+                if (cfg.equation != WAVE_EQ_ACOUSTIC) model.vs = rd("vs");
+                if (cfg.equation == WAVE_EQ_VISCOELASTIC) { model.taup = rd("tauP"); model.taus = rd("tauS"); }
+                if (cfg.equation == WAVE_EQ_VISCOELASTIC || cfg.equation == WAVE_EQ_VISCOSH) model.taus = rd("tauS");
+            }
+        } else if (em) {
+            model.eps_r.assign(n, key<float>(keys, "epsilonr", 1.0f));
+            model.sigma.assign(n, key<float>(keys, "sigma", 0.0f));
+            model.mu_r.assign(n, key<float>(keys, "mur", 1.0f));
+        } else {
+            model.rho.assign(n, key<float>(keys, "rho", 1000.0f));
+            model.vp.assign(n, key<float>(keys, "velocityP", 0.0f));
+            model.vs.assign(n, key<float>(keys, "velocityS", 0.0f));
+            model.taup.assign(n, key<float>(keys, "tauP", 0.0f));
+            model.taus.assign(n, key<float>(keys, "tauS", 0.0f));
+        }
+        // acquisition (AcquisitionSettings.hpp:55-109; receivers: x y z type)
+        struct Src { int no, x, y, z, type, wtype, shape; double fc, amp, ts; };
+        std::vector<Src> srcs;
+        {
+            std::ifstream f(dir + "/../" + key<std::string>(keys, "SourceFilename", "") + ".txt");
+            std::string line;
+            while (std::getline(f, line)) {
+                if (line.empty() || line[0] == '#') continue;
+                std::istringstream in(line);
+                Src s;
+                if (in >> s.no >> s.x >> s.y >> s.z >> s.type >> s.wtype >> s.shape >> s.fc >> s.amp >> s.ts) srcs.push_back(s);
+            }
+        }
+        wave::gpu::Acquisition rec;
+        {
+            std::ifstream f(dir + "/../" + key<std::string>(keys, "ReceiverFilename", "") + ".txt");
+            std::string line;
+            while (std::getline(f, line)) {
+                if (line.empty() || line[0] == '#') continue;
+                std::istringstream in(line);
+                long long x, y, z;
+                int t;
+                if (in >> x >> y >> z >> t) {
+                    rec.index.push_back(x + z * cfg.NX + y * cfg.NX * (cfg.dimension == 3 ? cfg.NZ : 1));
+                    rec.type.push_back(t);
+                }
+            }
+        }
+        if (srcs.empty() || rec.index.empty()) throw wave::gpu::Error(WAVE_ERR_IO, "no sources or receivers read");
+        const std::string eqname[] = {"acoustic", "elastic", "viscoelastic", "sh", "viscosh", "tmem", "emem", "viscotmem", "viscoemem"};
+        auto solver = wave::gpu::Factory::Create(cfg.dimension == 3 ? "3D" : "2D", eqname[cfg.equation]);
+        solver->initForwardSolver(cfg);
+        solver->prepareForModelling(model);
+        solver->setReceivers(rec);
+        const int nt = solver->NT();
+        std::set<int> shots;
+        for (auto& s : srcs) shots.insert(s.no);
+        const char* names[2][4] = {{"p", "vx", "vy", "vz"}, {"ez", "ex", "ey", "hz"}};
+        for (int shot : shots) {
+            wave::gpu::Acquisition src;
+            for (auto& s : srcs) {
+                if (s.no != shot) continue;
+                src.index.push_back(s.x + static_cast<long long>(s.z) * cfg.NX + static_cast<long long>(s.y) * cfg.NX * (cfg.dimension == 3 ? cfg.NZ : 1));
+                src.type.push_back(s.type);
+                std::vector<float> w(nt);
+                wave::gpu::check(nullptr, wave_wavelet(s.shape, nt, cfg.DT, s.fc, s.amp, s.ts, w.data()));
+                src.signals.insert(src.signals.end(), w.begin(), w.end());
+            }
+            solver->resetCPML();
+            solver->setSources(src);
+            solver->run(0, nt);
+            auto seis = solver->seismograms();
+            if (!solver->isFinite()) throw wave::gpu::Error(WAVE_ERR_NONFINITE, "Infinite or NaN value in seismogram or/and velocity wavefield!");
+            for (int type = 1; type <= 4; ++type) {
+                std::vector<float> part;
+                int ntr = 0;
+                for (size_t r = 0; r < rec.type.size(); ++r)
+                    if (rec.type[r] == type) {
+                        part.insert(part.end(), seis.begin() + r * nt, seis.begin() + (r + 1) * nt);
+                        ++ntr;
+                    }
+                if (!ntr) continue;
+                write_mtx(dir + "/../" + key<std::string>(keys, "SeismogramFilename", "seismogram") + ".shot_" + std::to_string(shot) +
+                              "." + names[em ? 1 : 0][type - 1] + ".mtx",
+                          part, ntr, nt);
+            }
+            std::cout << "shot " << shot << ": " << nt << " time steps done\n";
+        }
+    } catch (wave::gpu::Error& e) {
+        std::cerr << "wave_simulation: " << e.what() << "\n";
+        return 1;
+    }
+    return 0;
+}
