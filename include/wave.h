@@ -179,12 +179,42 @@ int wave_get_launch_count(wave_handle* h, long long* count);
 int wave_set_timing(wave_handle* h, int on);
 int wave_get_kernel_times(wave_handle* h, double* velocity_ms, double* stress_ms, long long* samples);
 
+/* Harmonic S-wave-modulus average with the reference's vacuum rules
+ * (ModelparameterSeismic::calcAveragedSWaveModulus, ModelparameterSeismic.cpp:421-432):
+ * moduli below 1 are raised to 1, their inverses are averaged over the 4 points
+ * of a grid plane with the edge fallbacks of Modelparameter.cpp:448-527
+ * (mode 0 = XY, 1 = XZ, 2 = YZ) or over 2 points along an axis (mode 3 = x,
+ * 4 = y; the SH models, SH.cpp:429-430), and averages below 4 become 0.
+ * mu and out hold NX*NY*NZ values in the reference index order, both on the
+ * host or both on the current CUDA device (mem). Synchronous; no handle. */
+int wave_average_shear_modulus(const float* mu, float* out, int64_t NX, int64_t NY, int64_t NZ, int mode, int mem);
+
 /* Kernel path: 0 = automatic (the streaming TMA kernels for 3-D elastic grids
  * with NX % 4 == 0, the generic kernels otherwise), 1 = generic kernels only.
  * wave_get_kernel_path reports whether the streaming kernels are active. The
  * reference has no counterpart (LAMA picks its own SpMV kernels). */
 int wave_set_kernel_path(wave_handle* h, int path);
 int wave_get_kernel_path(wave_handle* h, int* streaming_active);
+
+/* ---- batches of shots (the shot parallelism of Simulation.cpp:116-121, 339-369
+ *      as one device-wide launch per pass) ---- */
+typedef struct wave_batch wave_batch;
+
+/* nshots configurations that share dimension, equation, order, DT, T, boundary
+ * type, free surface and relaxation mechanisms; grid sizes may differ. */
+int wave_batch_create(const wave_config* cfgs, int nshots, wave_batch** out);
+int wave_batch_destroy(wave_batch* b);
+/* The per-shot handle, for wave_set_model*, wave_set_sources,
+ * wave_set_receivers, wave_get_seismograms and wave_check_finite. Owned by
+ * the batch; do not destroy it or step it on its own. */
+int wave_batch_shot(wave_batch* b, int shot, wave_handle** h);
+/* Steps t in [t_begin, t_end) of every shot: per step one launch per pass
+ * over all shots' tiles and one source/receiver launch; multi-step calls
+ * replay a captured CUDA graph. Returns after the steps completed. */
+int wave_batch_step(wave_batch* b, int t_begin, int t_end);
+int wave_batch_get_stream(wave_batch* b, void** stream);
+int wave_batch_get_launch_count(wave_batch* b, long long* count);
+const char* wave_batch_last_error(const wave_batch* b);
 
 /* Text of the last error on this handle (or of the last failed create when
  * h == NULL). Never NULL. */

@@ -38,7 +38,9 @@ ABI_SYMBOLS = (
     "wave_get_state_size", "wave_get_state", "wave_set_state", "wave_get_nt",
     "wave_get_num_receivers", "wave_get_stream", "wave_get_launch_count", "wave_set_timing",
     "wave_get_kernel_times", "wave_last_error", "wave_wavelet", "wave_set_kernel_path",
-    "wave_get_kernel_path",
+    "wave_get_kernel_path", "wave_average_shear_modulus", "wave_batch_create", "wave_batch_destroy",
+    "wave_batch_shot", "wave_batch_step", "wave_batch_get_stream", "wave_batch_get_launch_count",
+    "wave_batch_last_error",
 )
 
 
@@ -155,6 +157,15 @@ def lib():
     L.wave_wavelet.argtypes = [I, I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
     L.wave_set_kernel_path.argtypes = [P, I]
     L.wave_get_kernel_path.argtypes = [P, CP(I)]
+    L.wave_average_shear_modulus.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, I]
+    L.wave_batch_create.argtypes = [P, I, CP(P)]
+    L.wave_batch_destroy.argtypes = [P]
+    L.wave_batch_shot.argtypes = [P, I, CP(P)]
+    L.wave_batch_step.argtypes = [P, I, I]
+    L.wave_batch_get_stream.argtypes = [P, CP(P)]
+    L.wave_batch_get_launch_count.argtypes = [P, CP(ctypes.c_longlong)]
+    L.wave_batch_last_error.restype = ctypes.c_char_p
+    L.wave_batch_last_error.argtypes = [P]
     _lib = L
     return L
 
@@ -183,6 +194,18 @@ def wavelet(shape: int, nt: int, dt: float, fc: float, amp: float, tshift: float
     """Source time function (Sources.cpp:157-215 shapes 1..9)."""
     out = np.zeros(nt, dtype=np.float32)
     _check(None, lib().wave_wavelet(shape, nt, dt, fc, amp, tshift, out.ctypes.data_as(ctypes.c_void_p)))
+    return out
+
+
+def average_shear_modulus(mu, dims, mode: int, out=None):
+    """Harmonic S-modulus average with the reference's vacuum rules
+    (ModelparameterSeismic.cpp:421-432); dims = (NX, NY, NZ); mode 0..2 = XY/XZ/YZ
+    4-point, 3/4 = 2-point along x/y. numpy (host) or torch cuda arrays."""
+    mu = _f32(mu)
+    if out is None:
+        out = np.zeros(int(np.prod(dims)), dtype=np.float32) if not hasattr(mu, "data_ptr") else mu.new_zeros(mu.shape)
+    (pm, mem), (po, _) = _ptr(mu), _ptr(out)
+    _check(None, lib().wave_average_shear_modulus(pm, po, dims[0], dims[1], dims[2], mode, mem))
     return out
 
 
@@ -303,6 +326,74 @@ class ForwardSolver:
         if self.h:
             lib().wave_solver_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _ShotView(ForwardSolver):
+    """A shot of a batch: the per-shot handle, owned by the batch."""
+
+    def __init__(self, h, cfg):
+        super().__init__("3d" if cfg.dimension == 3 else "2d", [k for k, v in EQUATIONS.items() if v == cfg.equation][0])
+        self.h, self.cfg = h, cfg
+        nt = ctypes.c_int()
+        _check(self.h, lib().wave_get_nt(self.h, ctypes.byref(nt)))
+        self.nt = nt.value
+
+    def run(self, *a):
+        raise WaveError(WAVE_ERR_STATE, "step the batch, not a single shot")
+
+    def close(self):
+        self.h = None   # owned by the batch
+
+
+class Batch:
+    """Many shots with uneven grids stepped together (wave_batch_*)."""
+
+    def __init__(self, configs):
+        arr = (WaveConfig * len(configs))()
+        for i, c in enumerate(configs):
+            arr[i].copy_from(c)
+        self._cfgs = arr
+        b = ctypes.c_void_p()
+        rc = lib().wave_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(configs), ctypes.byref(b))
+        if rc != WAVE_OK:
+            raise WaveError(rc, lib().wave_batch_last_error(None).decode())
+        self.b = b
+        self.shots = []
+        for i in range(len(configs)):
+            h = ctypes.c_void_p()
+            self._check(lib().wave_batch_shot(self.b, i, ctypes.byref(h)))
+            self.shots.append(_ShotView(h, arr[i]))
+        self.nt = self.shots[0].nt
+
+    def _check(self, rc):
+        if rc != WAVE_OK:
+            raise WaveError(rc, lib().wave_batch_last_error(self.b).decode())
+
+    def run(self, t0: int, t1: int):
+        self._check(lib().wave_batch_step(self.b, t0, t1))
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._check(lib().wave_batch_get_stream(self.b, ctypes.byref(s)))
+        return s.value or 0
+
+    def launch_count(self) -> int:
+        c = ctypes.c_longlong()
+        self._check(lib().wave_batch_get_launch_count(self.b, ctypes.byref(c)))
+        return c.value
+
+    def close(self):
+        if getattr(self, "b", None):
+            for s in self.shots:
+                s.h = None
+            lib().wave_batch_destroy(self.b)
+            self.b = None
 
     def __del__(self):
         try:

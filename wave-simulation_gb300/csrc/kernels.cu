@@ -77,6 +77,28 @@ __device__ __forceinline__ bool point(const StepParams& P, Pt& p)
     return true;
 }
 
+// batched launches: one block per (shot, 32 x 8 tile); the shot's parameters
+// are staged in shared memory once per block
+__device__ __forceinline__ void load_params(StepParams& dst, const StepParams* src)
+{
+    const int n = sizeof(StepParams) / sizeof(int);
+    int* d = reinterpret_cast<int*>(&dst);
+    const int* sp = reinterpret_cast<const int*>(src);
+    for (int k = threadIdx.y * blockDim.x + threadIdx.x; k < n; k += blockDim.x * blockDim.y) d[k] = sp[k];
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool point_tile(const StepParams& P, const BatchTile& w, Pt& p)
+{
+    p.x = w.x0 + threadIdx.x;
+    const int r = w.r0 + threadIdx.y;
+    if (p.x >= P.NX || r >= P.NY * P.NZ) return false;
+    p.y = r / P.NZ;
+    p.z = r - p.y * P.NZ;
+    p.i = p.x + (long long)P.NX * (p.z + (long long)P.NZ * p.y);
+    return true;
+}
+
 // psi indices along x / y / z for point p
 __device__ __forceinline__ long long pix(const StepParams& P, const Pt& p, int s) { return s + (long long)P.cx.ns * (p.z + (long long)P.NZ * p.y); }
 __device__ __forceinline__ long long piy(const StepParams& P, const Pt& p, int s) { return p.x + (long long)P.NX * (p.z + (long long)P.NZ * s); }
@@ -155,10 +177,8 @@ __device__ __forceinline__ float absDamp(const StepParams& P, const Pt& p)
 //           FD3Dacoustic::run (ForwardSolver3Dacoustic.cpp:122-230)
 // --------------------------------------------------------------------------
 template <int H>
-__global__ void __launch_bounds__(256) acoustic_v(StepParams P)
+__device__ __forceinline__ void acoustic_v_body(const StepParams& P, const Pt& p)
 {
-    Pt p;
-    if (!point(P, p)) return;
     const float* pr = P.f[F_P];
     float u = dX<H, true>(P, p, pr, P.Dxf, PS_P_X);
     u *= LD(P.m[M_IRX]);
@@ -174,10 +194,27 @@ __global__ void __launch_bounds__(256) acoustic_v(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) acoustic_p(StepParams P)
+__global__ void __launch_bounds__(256) acoustic_v(StepParams P)
 {
     Pt p;
     if (!point(P, p)) return;
+    acoustic_v_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) acoustic_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    acoustic_v_body<H>(sP, p);
+}
+
+template <int H>
+__device__ __forceinline__ void acoustic_p_body(const StepParams& P, const Pt& p)
+{
     float u = dX<H, false>(P, p, P.f[F_VX], P.Dxb, PS_VXX);
     float ut = dY<H, false>(P, p, P.f[F_VY], P.Dyb, PS_VYY);
     u += ut;
@@ -192,15 +229,32 @@ __global__ void __launch_bounds__(256) acoustic_p(StepParams P)
     P.f[F_P][p.i] = pv;
 }
 
+template <int H>
+__global__ void __launch_bounds__(256) acoustic_p(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    acoustic_p_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) acoustic_p_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    acoustic_p_body<H>(sP, p);
+}
+
 // --------------------------------------------------------------------------
 // elastic + visco-elastic velocity: ForwardSolver2Delastic.cpp:150-205,
 // ForwardSolver3Delastic.cpp:174-277, ForwardSolver3Dviscoelastic.cpp:186-268
 // --------------------------------------------------------------------------
 template <int H>
-__global__ void __launch_bounds__(256) elastic_v(StepParams P)
+__device__ __forceinline__ void elastic_v_body(const StepParams& P, const Pt& p)
 {
-    Pt p;
-    if (!point(P, p)) return;
     const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
     const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
     const float *Sxx = P.f[F_SXX], *Syy = P.f[F_SYY], *Sxy = P.f[F_SXY];
@@ -236,13 +290,30 @@ __global__ void __launch_bounds__(256) elastic_v(StepParams P)
     }
 }
 
-// elastic stress: ForwardSolver2Delastic.cpp:210-290, ForwardSolver3Delastic.cpp:283-409,
-// free surface FreeSurface2Delastic.cpp:14-45 / FreeSurface3Delastic.cpp:15-47
 template <int H>
-__global__ void __launch_bounds__(256) elastic_s(StepParams P)
+__global__ void __launch_bounds__(256) elastic_v(StepParams P)
 {
     Pt p;
     if (!point(P, p)) return;
+    elastic_v_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) elastic_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    elastic_v_body<H>(sP, p);
+}
+
+// elastic stress: ForwardSolver2Delastic.cpp:210-290, ForwardSolver3Delastic.cpp:283-409,
+// free surface FreeSurface2Delastic.cpp:14-45 / FreeSurface3Delastic.cpp:15-47
+template <int H>
+__device__ __forceinline__ void elastic_s_body(const StepParams& P, const Pt& p)
+{
     const float *vx = P.f[F_VX], *vy = P.f[F_VY];
     const float M = LD(P.m[M_M]), mu = LD(P.m[M_MU]);
     float vxx = dX<H, false>(P, p, vx, P.Dxb, PS_VXX);
@@ -314,14 +385,31 @@ __global__ void __launch_bounds__(256) elastic_s(StepParams P)
     }
 }
 
+template <int H>
+__global__ void __launch_bounds__(256) elastic_s(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    elastic_s_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) elastic_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    elastic_s_body<H>(sP, p);
+}
+
 // visco-elastic stress: ForwardSolver2Dviscoelastic.cpp:223-303,
 // ForwardSolver3Dviscoelastic.cpp:270-446, free surface
 // FreeSurface2Dviscoelastic.cpp / FreeSurface3Dviscoelastic.cpp:17-75
 template <int H>
-__global__ void __launch_bounds__(256) visco_s(StepParams P)
+__device__ __forceinline__ void visco_s_body(const StepParams& P, const Pt& p)
 {
-    Pt p;
-    if (!point(P, p)) return;
     const int L = P.L;
     const float DTh = P.DThalf;
     const float *vx = P.f[F_VX], *vy = P.f[F_VY];
@@ -448,14 +536,31 @@ __global__ void __launch_bounds__(256) visco_s(StepParams P)
     for (int k = 0; k < nS; ++k) P.f[slotSh[k]][p.i] = Sh[k];
 }
 
+template <int H>
+__global__ void __launch_bounds__(256) visco_s(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    visco_s_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) visco_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    visco_s_body<H>(sP, p);
+}
+
 // --------------------------------------------------------------------------
 // SH / visco-SH: ForwardSolver2Dsh.cpp:137-190, ForwardSolver2Dviscosh.cpp:155-240
 // --------------------------------------------------------------------------
 template <int H>
-__global__ void __launch_bounds__(256) sh_v(StepParams P)
+__device__ __forceinline__ void sh_v_body(const StepParams& P, const Pt& p)
 {
-    Pt p;
-    if (!point(P, p)) return;
     float u = dX<H, false>(P, p, P.f[F_SXZ], P.Dxb, PS_SXZ_X);
     float ut = P.fs ? dY<H, false>(P, p, P.f[F_SYZ], P.DybS, PS_SYZ_Y) : dY<H, false>(P, p, P.f[F_SYZ], P.Dyb, PS_SYZ_Y);
     u += ut;
@@ -464,10 +569,27 @@ __global__ void __launch_bounds__(256) sh_v(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) sh_s(StepParams P)
+__global__ void __launch_bounds__(256) sh_v(StepParams P)
 {
     Pt p;
     if (!point(P, p)) return;
+    sh_v_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) sh_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    sh_v_body<H>(sP, p);
+}
+
+template <int H>
+__device__ __forceinline__ void sh_s_body(const StepParams& P, const Pt& p)
+{
     const float* vz = P.f[F_VZ];
     const float d = P.abs ? absDamp(P, p) : 1.0f;
     for (int k = 0; k < 2; ++k) {
@@ -495,14 +617,31 @@ __global__ void __launch_bounds__(256) sh_s(StepParams P)
     }
 }
 
+template <int H>
+__global__ void __launch_bounds__(256) sh_s(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    sh_s_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) sh_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    sh_s_body<H>(sP, p);
+}
+
 // --------------------------------------------------------------------------
 // EM TMz: FD2Dtmem::run (ForwardSolverEM/ForwardSolver2Dtmem.cpp:128-170)
 // --------------------------------------------------------------------------
 template <int H>
-__global__ void __launch_bounds__(256) tm_h(StepParams P)
+__device__ __forceinline__ void tm_h_body(const StepParams& P, const Pt& p)
 {
-    Pt p;
-    if (!point(P, p)) return;
     const float* ez = P.f[F_EZ];
     float u = dY<H, true>(P, p, ez, P.Dyf, PS_EZY);
     u *= LD(P.m[M_IMUYZ]);
@@ -514,10 +653,27 @@ __global__ void __launch_bounds__(256) tm_h(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) tm_e(StepParams P)
+__global__ void __launch_bounds__(256) tm_h(StepParams P)
 {
     Pt p;
     if (!point(P, p)) return;
+    tm_h_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) tm_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    tm_h_body<H>(sP, p);
+}
+
+template <int H>
+__device__ __forceinline__ void tm_e_body(const StepParams& P, const Pt& p)
+{
     float u = dX<H, false>(P, p, P.f[F_HY], P.Dxb, PS_HYX);
     float ut = dY<H, false>(P, p, P.f[F_HX], P.Dyb, PS_HXY);
     u -= ut;
@@ -528,12 +684,29 @@ __global__ void __launch_bounds__(256) tm_e(StepParams P)
     P.f[F_EZ][p.i] = e;
 }
 
-// EM TEz: FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:132-180)
 template <int H>
-__global__ void __launch_bounds__(256) te_h(StepParams P)
+__global__ void __launch_bounds__(256) tm_e(StepParams P)
 {
     Pt p;
     if (!point(P, p)) return;
+    tm_e_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) tm_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    tm_e_body<H>(sP, p);
+}
+
+// EM TEz: FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:132-180)
+template <int H>
+__device__ __forceinline__ void te_h_body(const StepParams& P, const Pt& p)
+{
     float u = dX<H, true>(P, p, P.f[F_EY], P.Dxf, PS_EYX);
     float ut = dY<H, true>(P, p, P.f[F_EX], P.Dyf, PS_EXY);
     u -= ut;
@@ -542,10 +715,27 @@ __global__ void __launch_bounds__(256) te_h(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) te_e(StepParams P)
+__global__ void __launch_bounds__(256) te_h(StepParams P)
 {
     Pt p;
     if (!point(P, p)) return;
+    te_h_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) te_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    te_h_body<H>(sP, p);
+}
+
+template <int H>
+__device__ __forceinline__ void te_e_body(const StepParams& P, const Pt& p)
+{
     const float* hz = P.f[F_HZ];
     const float d = P.abs ? absDamp(P, p) : 1.0f;
     float u = dY<H, false>(P, p, hz, P.Dyb, PS_HZY);
@@ -558,18 +748,52 @@ __global__ void __launch_bounds__(256) te_e(StepParams P)
     P.f[F_EY][p.i] = (e - u) * d;
 }
 
-// --------------------------------------------------------------------------
-// ABS damping of the pass-1 fields (applied after pass 2 read them).
-// --------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) abs_frame_kernel(StepParams P, int f0, int f1, int f2)
+template <int H>
+__global__ void __launch_bounds__(256) te_e(StepParams P)
 {
     Pt p;
     if (!point(P, p)) return;
+    te_e_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) te_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    te_e_body<H>(sP, p);
+}
+
+// --------------------------------------------------------------------------
+// ABS damping of the pass-1 fields (applied after pass 2 read them).
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void abs_frame_body(const StepParams& P, const Pt& p, int f0, int f1, int f2)
+{
     const float d = absDamp(P, p);
     if (d == 1.0f) return;
     if (f0 >= 0) P.f[f0][p.i] *= d;
     if (f1 >= 0) P.f[f1][p.i] *= d;
     if (f2 >= 0) P.f[f2][p.i] *= d;
+}
+
+__global__ void __launch_bounds__(256) abs_frame_kernel(StepParams P, int f0, int f1, int f2)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    abs_frame_body(P, p, f0, f1, f2);
+}
+
+__global__ void __launch_bounds__(256) abs_frame_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, int f0, int f1, int f2)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    abs_frame_body(sP, p, f0, f1, f2);
 }
 
 // --------------------------------------------------------------------------
@@ -597,7 +821,7 @@ __device__ __forceinline__ float* field_of(const SrcRecParams& Q, int type)
     }
 }
 
-__global__ void __launch_bounds__(512) srcrec_kernel(SrcRecParams Q, int* tcounter)
+__device__ __forceinline__ void srcrec_body(const SrcRecParams& Q, int* tcounter)
 {
     const int t = *tcounter;
     const bool elasticP = (Q.eq == WAVE_EQ_ELASTIC || Q.eq == WAVE_EQ_VISCOELASTIC);
@@ -632,6 +856,14 @@ __global__ void __launch_bounds__(512) srcrec_kernel(SrcRecParams Q, int* tcount
     }
     __syncthreads();
     if (threadIdx.x == 0) *tcounter = t + 1;
+}
+
+__global__ void __launch_bounds__(512) srcrec_kernel(SrcRecParams Q, int* tcounter) { srcrec_body(Q, tcounter); }
+
+// one block per shot, each with its own step counter
+__global__ void __launch_bounds__(512) srcrec_batch(const SrcRecParams* __restrict__ Qs, int* tcounters)
+{
+    srcrec_body(Qs[blockIdx.x], tcounters + blockIdx.x);
 }
 
 // --------------------------------------------------------------------------
@@ -779,6 +1011,15 @@ __global__ void prep_harmonic(PrepParams G, const float* invmu, int mode, float*
     }
 }
 
+// 1/mu with moduli below 1 raised to 1 (ModelparameterSeismic.cpp:424-426)
+__global__ void prep_inv_clamped(PrepParams G, const float* mu, float* out)
+{
+    PREP_LOOP {
+        const float m = mu[i] < 1.0f ? 1.0f : mu[i];
+        out[i] = 1.0f / m;
+    }
+}
+
 __global__ void prep_one_plus(PrepParams G, const float* tau, float L, float* out)
 {
     PREP_LOOP { out[i] = 1.0f + L * tau[i]; }
@@ -837,6 +1078,48 @@ __global__ void set_counter_kernel(int* c, int v) { *c = v; }
 
 void launch_set_counter(int* c, int v, cudaStream_t s) { set_counter_kernel<<<1, 1, 0, s>>>(c, v); }
 
+using BatchKernel = void (*)(const StepParams*, const BatchTile*);
+
+BatchKernel batch_kernel_for(int eq, int pass, int H)
+{
+    static const BatchKernel ac_v[6] = WAVE_KTAB(acoustic_v_batch), ac_p[6] = WAVE_KTAB(acoustic_p_batch);
+    static const BatchKernel el_v[6] = WAVE_KTAB(elastic_v_batch), el_s[6] = WAVE_KTAB(elastic_s_batch), vi_s[6] = WAVE_KTAB(visco_s_batch);
+    static const BatchKernel s_v[6] = WAVE_KTAB(sh_v_batch), s_s[6] = WAVE_KTAB(sh_s_batch);
+    static const BatchKernel tmh[6] = WAVE_KTAB(tm_h_batch), tme[6] = WAVE_KTAB(tm_e_batch), teh[6] = WAVE_KTAB(te_h_batch), tee[6] = WAVE_KTAB(te_e_batch);
+    if (H < 1 || H > 6) return nullptr;
+    const int k = H - 1;
+    switch (eq) {
+    case WAVE_EQ_ACOUSTIC: return pass == 0 ? ac_v[k] : ac_p[k];
+    case WAVE_EQ_ELASTIC: return pass == 0 ? el_v[k] : el_s[k];
+    case WAVE_EQ_VISCOELASTIC: return pass == 0 ? el_v[k] : vi_s[k];
+    case WAVE_EQ_SH:
+    case WAVE_EQ_VISCOSH: return pass == 0 ? s_v[k] : s_s[k];
+    case WAVE_EQ_TMEM: return pass == 0 ? tmh[k] : tme[k];
+    case WAVE_EQ_EMEM: return pass == 0 ? teh[k] : tee[k];
+    default: return nullptr;
+    }
+}
+
+void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const BatchTile* tiles, int ntiles, cudaStream_t s)
+{
+    BatchKernel k = batch_kernel_for(eq, pass, H);
+    if (k && ntiles > 0) k<<<ntiles, dim3(32, 8, 1), 0, s>>>(Ps, tiles);
+}
+
+void launch_batch_aux(const StepParams* Ps, const BatchTile* tiles, int ntiles, int f0, int f1, int f2,
+                      const SrcRecParams* Qs, int* counters, int nshots, bool abs, cudaStream_t s)
+{
+    if (abs && ntiles > 0) abs_frame_batch<<<ntiles, dim3(32, 8, 1), 0, s>>>(Ps, tiles, f0, f1, f2);
+    if (nshots > 0) srcrec_batch<<<nshots, 512, 0, s>>>(Qs, counters);
+}
+
+__global__ void set_counters_kernel(int* c, int n, int v)
+{
+    for (int i = threadIdx.x; i < n; i += blockDim.x) c[i] = v;
+}
+
+void launch_set_counters(int* c, int n, int v, cudaStream_t s) { set_counters_kernel<<<1, 256, 0, s>>>(c, n, v); }
+
 void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s)
 {
     srcrec_kernel<<<1, 512, 0, s>>>(Q, tcounter);
@@ -861,6 +1144,7 @@ void k_inv_avg4(PrepParams G, const float* a, int plane, float* out, cudaStream_
 void k_avg2(PrepParams G, const float* a, int axis, float* out, cudaStream_t s) { prep_avg2<<<PREP_GRID>>>(G, a, axis, out); }
 void k_avg4(PrepParams G, const float* a, int plane, float* out, cudaStream_t s) { prep_avg4<<<PREP_GRID>>>(G, a, plane, out); }
 void k_harmonic(PrepParams G, const float* invmu, int mode, float* out, cudaStream_t s) { prep_harmonic<<<PREP_GRID>>>(G, invmu, mode, out); }
+void k_inv_clamped(PrepParams G, const float* mu, float* out, cudaStream_t s) { prep_inv_clamped<<<PREP_GRID>>>(G, mu, out); }
 void k_one_plus(PrepParams G, const float* tau, float L, float* out, cudaStream_t s) { prep_one_plus<<<PREP_GRID>>>(G, tau, L, out); }
 void k_scale(PrepParams G, const float* a, float sc, float* out, cudaStream_t s) { prep_scale<<<PREP_GRID>>>(G, a, sc, out); }
 void k_cacb(PrepParams G, const float* eps, const float* sig, float DT, float* ca, float* cb, cudaStream_t s) { prep_cacb<<<PREP_GRID>>>(G, eps, sig, DT, ca, cb); }

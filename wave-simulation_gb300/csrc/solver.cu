@@ -42,73 +42,16 @@ int psi_axis(int s)
 
 } // namespace
 
-struct wave_handle {
-    wave_config cfg{};
-    int NT = 0, NX = 1, NY = 1, NZ = 1, H = 1, L = 0;
-    long long N = 0;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-
-    std::vector<void*> allocs;
-    float* f[F_COUNT] = {};
-    float* r[R_COUNT][kMaxL] = {};
-    float* psi[PS_COUNT] = {};
-    long long psiLen[PS_COUNT] = {};
-    float* m[M_COUNT] = {};
-    float* opTab[8] = {};
-    float* cpmlProf[3][4] = {};
-    float* absCoeff = nullptr;
-    int* tcounter = nullptr;
-    int* flag = nullptr;
-
-    long long* sidx = nullptr; int* stype = nullptr; float* signals = nullptr; int nsrc = 0;
-    long long* ridx = nullptr; int* rtype = nullptr; float* seis = nullptr; int nrec = 0;
-
-    StepParams sp{};
-    SrcRecParams sq{};
-    dim3 grid, block;
-    bool modelSet = false;
-    std::vector<int> fields;          // allocated field slots
-    std::vector<int> pass1Fields;     // fields updated in pass 1 (ABS after pass 2)
-
-    cudaGraphExec_t graph = nullptr;
-    bool graphDirty = true;
-
-    // streaming 3-D elastic path (kernels_el3d.cu)
-    El3dPlan el3d;
-    int kernelPath = 0;          // 0 = automatic, 1 = generic kernels only
-    int* errWord = nullptr;      // device error word of the bounded waits
-
-    bool timing = false;
-    double velMsSum = 0, strMsSum = 0;
-    long long timedSteps = 0;
-    long long launches = 0;
-
-    ~wave_handle()
-    {
-        if (graph) cudaGraphExecDestroy(graph);
-        for (void* p : allocs) cudaFree(p);
-        if (stream) cudaStreamDestroy(stream);
-    }
-
-    template <class T>
-    T* alloc(size_t count)
-    {
-        void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
-        if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        allocs.push_back(p);
-        return static_cast<T*>(p);
-    }
-    void check(cudaError_t e, const char* what)
-    {
-        if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
-    }
-};
+#include "handle.h"
 
 namespace {
 
+
+} // namespace
+
+void wave::set_global_error(const std::string& msg) { g_create_err = msg; }
+
+namespace {
 
 int fail(wave_handle* h, int code, const std::string& msg)
 {

@@ -102,6 +102,11 @@ struct SrcRecParams {
     float* f[F_COUNT];
 };
 
+// one block of a batched launch: shot index and tile origin (x0, row r0 = z + NZ*y)
+struct BatchTile {
+    int shot, x0, r0, pad;
+};
+
 struct PrepParams {
     int NX, NY, NZ;
     long long N;
@@ -112,6 +117,10 @@ using StepKernel = void (*)(StepParams);
 StepKernel kernel_for(int eq, int pass, int H);
 void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s);
 void launch_set_counter(int* c, int v, cudaStream_t s);
+void launch_set_counters(int* c, int n, int v, cudaStream_t s);
+void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const BatchTile* tiles, int ntiles, cudaStream_t s);
+void launch_batch_aux(const StepParams* Ps, const BatchTile* tiles, int ntiles, int f0, int f1, int f2,
+                      const SrcRecParams* Qs, int* counters, int nshots, bool abs, cudaStream_t s);
 void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s);
 void launch_finite(const float* a, long long n, int* flag, cudaStream_t s);
 void k_modulus(PrepParams G, const float* rho, const float* v, const float* tau, float sum, int clamp, float* out, cudaStream_t s);
@@ -121,6 +130,7 @@ void k_inv_avg4(PrepParams G, const float* a, int plane, float* out, cudaStream_
 void k_avg2(PrepParams G, const float* a, int axis, float* out, cudaStream_t s);
 void k_avg4(PrepParams G, const float* a, int plane, float* out, cudaStream_t s);
 void k_harmonic(PrepParams G, const float* invmu, int mode, float* out, cudaStream_t s);
+void k_inv_clamped(PrepParams G, const float* mu, float* out, cudaStream_t s);
 void k_one_plus(PrepParams G, const float* tau, float L, float* out, cudaStream_t s);
 void k_scale(PrepParams G, const float* a, float sc, float* out, cudaStream_t s);
 void k_cacb(PrepParams G, const float* eps, const float* sig, float DT, float* ca, float* cb, cudaStream_t s);
@@ -140,6 +150,9 @@ struct CpmlHost {
 CpmlHost build_cpml(int n, int width, bool dropTop, float NPower, float fc, float vmax, float DT, float DH);
 std::vector<float> build_abs_coeff(int width, float dampingCoeff);
 bool fd_coefficients(int order, std::vector<double>& c);
+
+// error text for calls without a handle (wave_last_error(NULL))
+void set_global_error(const std::string& msg);
 
 // config parser (config.cpp)
 int parse_config_file(const char* path, wave_config* cfg, std::string& err);
