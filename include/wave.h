@@ -189,9 +189,12 @@ int wave_get_kernel_times(wave_handle* h, double* velocity_ms, double* stress_ms
  * host or both on the current CUDA device (mem). Synchronous; no handle. */
 int wave_average_shear_modulus(const float* mu, float* out, int64_t NX, int64_t NY, int64_t NZ, int mode, int mem);
 
-/* Kernel path: 0 = automatic (the streaming TMA kernels for 3-D elastic grids
- * with NX % 4 == 0, the generic kernels otherwise), 1 = generic kernels only.
- * wave_get_kernel_path reports whether the streaming kernels are active. The
+/* Kernel path: 0 = automatic, 1 = generic kernels only, 2 = the streaming
+ * TMA kernels wherever they apply (3-D elastic grids with NX % 4 == 0 whose
+ * 32x16 column tiles meet at most one CPML slab per axis). The automatic path
+ * times both kernels of each pass when the model is set on an unstepped state
+ * and keeps the faster one per pass. wave_get_kernel_path reports which passes
+ * run the streaming kernels (bit 0 velocity pass, bit 1 stress pass). The
  * reference has no counterpart (LAMA picks its own SpMV kernels). */
 int wave_set_kernel_path(wave_handle* h, int path);
 int wave_get_kernel_path(wave_handle* h, int* streaming_active);

@@ -159,11 +159,14 @@ def test_streaming_elastic_kernels_match_oracle_and_generic(order, fs, boundary,
     wc = to_wave_cfg(wave, cfg)
     m32 = {k: v.astype(np.float32) for k, v in model.items()}
     s32 = sig.astype(np.float32)
-    fast = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=0, expect_streaming=True)
+    fast = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=2, expect_streaming=True)
     generic = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=1, expect_streaming=False)
+    auto = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=0)
     assert rel(fast, ref) < TOL, f"streaming vs FP64 oracle {rel(fast, ref):.3e}"
     assert rel(generic, ref) < TOL
     assert rel(fast, generic) < 1e-5
+    # the automatic path times both kernels per pass on the unstepped state and must leave it untouched
+    assert rel(auto, generic) < 1e-5
 
 
 def test_multi_step_graph_equals_single_steps(wave, refcpu):

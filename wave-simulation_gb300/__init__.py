@@ -306,13 +306,18 @@ class ForwardSolver:
         return c.value
 
     def set_kernel_path(self, path: int):
-        """0 = automatic (streaming kernels where they apply), 1 = generic kernels."""
+        """0 = automatic (faster kernel per pass, timed when the model is set),
+        1 = generic kernels, 2 = streaming TMA kernels wherever they apply."""
         _check(self.h, lib().wave_set_kernel_path(self.h, path))
 
-    def streaming_active(self) -> bool:
+    def streaming_passes(self) -> int:
+        """Bit 0: the velocity pass runs the streaming kernel; bit 1: the stress pass."""
         v = ctypes.c_int()
         _check(self.h, lib().wave_get_kernel_path(self.h, ctypes.byref(v)))
-        return bool(v.value)
+        return v.value
+
+    def streaming_active(self) -> bool:
+        return self.streaming_passes() != 0
 
     def set_timing(self, on: bool):
         _check(self.h, lib().wave_set_timing(self.h, int(on)))

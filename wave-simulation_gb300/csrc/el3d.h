@@ -12,6 +12,7 @@ struct El3dMaps {
     CUtensorMap hSxx, hSxy, hSxz, hSyz, hSzz, hVx, hVy, hVz;           // halo boxes
     CUtensorMap cSxx, cSyy, cSzz, cSxy, cSxz, cSyz, cVx, cVy, cVz, cM;  // centre boxes
     CUtensorMap pRho, pMu;                                              // (x,z)+1 boxes
+    CUtensorMap psV[9], psS[9];   // CPML memory variables of the velocity / stress pass (x-, y-, z-type, three each)
 };
 
 struct El3dSched {

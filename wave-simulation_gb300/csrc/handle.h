@@ -54,7 +54,9 @@ struct wave_handle {
 
     // streaming 3-D elastic path (kernels_el3d.cu)
     El3dPlan el3d;
-    int kernelPath = 0;          // 0 = automatic, 1 = generic kernels only
+    int kernelPath = 0;          // 0 = automatic, 1 = generic kernels only, 2 = streaming where available
+    int passStreaming[2] = {1, 1};   // automatic path: timed choice per pass (1 = streaming)
+    long long stepsSinceReset = 0;   // steps run since creation or the last reset
     int* errWord = nullptr;      // device error word of the bounded waits
 
     bool timing = false;

@@ -3,19 +3,27 @@
 //
 // Each CTA owns a 32 (x) x 16 (z) column tile and marches it down the depth
 // axis y (the slowest axis, reference layout idx = x + z*NX + y*NX*NZ). The
-// CTAs are persistent: the grid is one CTA per SM and each CTA takes a
-// contiguous run of (tile, plane) work, so every field plane is fetched from
-// HBM once. Planes arrive through TMA bulk-tensor copies
-// (cp.async.bulk.tensor.3d) into a 4-stage shared-memory ring tracked by
-// mbarriers; one thread issues the copies four planes ahead of the compute.
-// Depth derivatives come from per-thread register queues (2H+1 planes),
-// x- and z-derivatives from the halo tiles in shared memory. The averaged
-// material terms (1/rho averages, harmonic mu averages with the vacuum rules)
-// are formed in-kernel from rho and mu, so the kernels read only the base
-// material arrays. All waits are bounded: a wait that runs out sets the
-// handle's error word and the CTA returns.
+// CTAs are persistent (one per SM); each takes a contiguous run of the
+// (tile, plane) work, so every field plane is fetched from HBM once. Planes
+// arrive through TMA bulk-tensor copies (cp.async.bulk.tensor.3d) into a
+// 3-stage shared-memory ring ("full" mbarriers carry the transaction
+// bytes). Each of the 16 warps computes one z row of the tile and releases a
+// stage through an "empty" mbarrier; thread 0 refills a stage once all warps
+// have released it, one iteration behind its own warp. Warps never meet at a
+// block barrier, so they run up to a ring's length apart and hide each
+// other's latency. Depth derivatives come from
+// per-thread register queues (2H+1 planes), x- and z-derivatives from the
+// halo tiles in shared memory. Interior rows multiply compile-time FD
+// coefficients and scale once by DT/DH; edge rows (order reduction, zero
+// padding, free-surface image rows) use the operator's edge table. The
+// averaged material terms (1/rho averages, harmonic mu averages with the
+// vacuum rules and edge fallbacks) are formed in-kernel from rho and mu, so
+// the kernels read only base material arrays. Every wait is bounded: a wait
+// that runs out sets the handle's error word and the CTA returns.
 #include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "el3d.h"
 
@@ -23,8 +31,9 @@ namespace wave {
 
 namespace el3d {
 
-constexpr int TX = 32, TZ = 16, NTHR = TX * TZ, NSTAGE = 4;
-constexpr int CB = TX * TZ * 4;                 // centre box bytes
+constexpr int TX = 32, TZ = 16, NTHR = TX * TZ, MAXSEG = 64;
+constexpr int NCWARP = NTHR / 32;                // warps of a CTA, one per z row of the tile
+constexpr int CB = TX * TZ * 4;                  // centre box bytes
 constexpr int PW = TX + 4, PH = TZ + 1;          // "+1" box (x0..x0+35, z0..z0+16)
 constexpr int PBYTES = PW * PH * 4;              // bytes one "+1" box copy delivers
 constexpr int PB = ((PBYTES + 127) / 128) * 128; // its slot in the stage layout
@@ -34,8 +43,33 @@ __host__ __device__ constexpr int bw_of(int H) { return TX + 2 * hx_of(H); }
 __host__ __device__ constexpr int bh_of(int H) { return TZ + 2 * H; }
 __host__ __device__ constexpr int hbytes_of(int H) { return bw_of(H) * bh_of(H) * 4; }          // delivered
 __host__ __device__ constexpr int hb_of(int H) { return ((hbytes_of(H) + 127) / 128) * 128; }  // layout slot
-__host__ __device__ constexpr int vel_stage(int H) { return 5 * hb_of(H) + 6 * CB + PB; }
-__host__ __device__ constexpr int str_stage(int H) { return 3 * hb_of(H) + 10 * CB + PB; }
+
+// Staggered FD coefficients (Derivatives::setFDCoef, Derivatives.cpp:2000-2042)
+// as compile-time constants, so that the interior taps are FFMAs with
+// immediates.
+__host__ __device__ constexpr float fdc(int q, int j)
+{
+    switch (q) {
+    case 2: return j == 0 ? -1.0f : 1.0f;
+    case 4: { constexpr double c[2] = {1.0 / 24.0, -9.0 / 8.0}; return static_cast<float>(j < 2 ? c[j] : -c[3 - j]); }
+    case 6: { constexpr double c[3] = {-3.0 / 640.0, 25.0 / 384.0, -75.0 / 64.0}; return static_cast<float>(j < 3 ? c[j] : -c[5 - j]); }
+    case 8: {
+        constexpr double c[4] = {5.0 / 7168.0, -49.0 / 5120.0, 245.0 / 3072.0, -1225.0 / 1024.0};
+        return static_cast<float>(j < 4 ? c[j] : -c[7 - j]);
+    }
+    case 10: {
+        constexpr double c[5] = {-8756999275442633.0 / 73786976294838206464.0, 8142668969129685.0 / 4611686018427387904.0,
+                                 -567.0 / 40960.0, 735.0 / 8192.0, -19845.0 / 16384.0};
+        return static_cast<float>(j < 5 ? c[j] : -c[9 - j]);
+    }
+    default: {
+        constexpr double c[6] = {6448335830095439.0 / 295147905179352825856.0, -1655620175512543.0 / 4611686018427387904.0,
+                                 6842103786556949.0 / 2305843009213693952.0, -628618285389933.0 / 36028797018963968.0,
+                                 436540475965291.0 / 4503599627370496.0, -2750204998582123.0 / 2251799813685248.0};
+        return static_cast<float>(j < 6 ? c[j] : -c[11 - j]);
+    }
+    }
+}
 
 // ---------------------------------------------------------------- PTX helpers
 __device__ __forceinline__ uint32_t saddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
@@ -82,127 +116,116 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 // length L takes L + 2H iterations: 2H to fill the depth queues, then one
 // compute plane per iteration. Iteration k of a segment starting at plane ya
 // fetches queue plane q = ya - H + k and computes plane c = ya - 2H + k.
-struct Iter {
-    int tile, q, c, ya;
-    bool compute;
+struct Segs {
+    int n;
+    int tile[MAXSEG], ya[MAXSEG], len[MAXSEG];
 };
 
-__device__ __forceinline__ bool iter_at(int it, long long g0, long long g1, int NY, int H, Iter& out)
+__device__ __forceinline__ int build_segments(Segs& S, long long g0, long long g1, int NY, int H)
 {
+    int n = 0, total = 0;
     long long g = g0;
-    while (g < g1) {
-        const int t = static_cast<int>(g / NY);
-        const int ya = static_cast<int>(g - (long long)t * NY);
-        const long long gend = g1 < (long long)(t + 1) * NY ? g1 : (long long)(t + 1) * NY;
-        const int len = static_cast<int>(gend - g) + 2 * H;
-        if (it < len) {
-            out.tile = t;
-            out.ya = ya;
-            out.q = ya - H + it;
-            out.c = ya - 2 * H + it;
-            out.compute = out.c >= ya;
-            return true;
-        }
-        it -= len;
-        g = gend;
-    }
-    return false;
-}
-
-__device__ __forceinline__ int total_iters(long long g0, long long g1, int NY, int H)
-{
-    int n = 0;
-    long long g = g0;
-    while (g < g1) {
+    while (g < g1 && n < MAXSEG) {
         const long long t = g / NY;
         const long long gend = g1 < (t + 1) * NY ? g1 : (t + 1) * NY;
-        n += static_cast<int>(gend - g) + 2 * H;
+        S.tile[n] = static_cast<int>(t);
+        S.ya[n] = static_cast<int>(g - t * NY);
+        S.len[n] = static_cast<int>(gend - g) + 2 * H;
+        total += S.len[n];
+        ++n;
         g = gend;
     }
-    return n;
+    S.n = n;
+    return total;
 }
 
-// ------------------------------------------------------------ derivatives
-// x from a halo tile (centre index ci), z from a halo tile (row stride BW),
-// y from a register queue q[0..2H] holding planes c-H..c+H. Interior rows use
-// the operator's interior weights; edge rows use the edge table (zero-filled
-// neighbours outside the grid carry zero weight there).
-template <int H, bool FWD>
-__device__ __forceinline__ float d_line(const float* __restrict__ s, int ci, int stride, int c, const Op1D& op)
-{
-    float acc = 0.0f;
-    if (!op.full && c >= op.E && c < op.n - op.E) {
-#pragma unroll
-        for (int k = (FWD ? -H + 1 : -H); k <= (FWD ? H : H - 1); ++k) acc += op.w[kMaxHalf + k] * s[ci + k * stride];
-    } else {
-        const int slot = op.full ? c : (c < op.E ? c : op.E + c - (op.n - op.E));
-        const float* t = op.tab + slot * kTabW + kMaxHalf;
-#pragma unroll
-        for (int k = -H; k <= H; ++k) {
-            const float wk = __ldg(t + k);
-            if (wk != 0.0f) acc += wk * s[ci + k * stride];
-        }
+// cursor over the iterations of the CTA's segments
+struct Cursor {
+    int seg, k;
+    __device__ __forceinline__ void advance(const Segs& S)
+    {
+        if (++k == S.len[seg]) { ++seg; k = 0; }
     }
+};
+
+// ------------------------------------------------------------ derivatives
+// Interior rows: compile-time coefficients, two interleaved partial sums (even
+// and odd taps) to halve the dependent FMA chain; DT/DH is applied once after.
+template <int H, bool FWD>
+__device__ __forceinline__ float dsum(const float* __restrict__ s, int ci, int stride)
+{
+    float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 2 * H; j += 2) {
+        a0 += fdc(2 * H, j) * s[ci + (FWD ? j - H + 1 : j - H) * stride];
+        a1 += fdc(2 * H, j + 1) * s[ci + (FWD ? j - H + 2 : j - H + 1) * stride];
+    }
+    return a0 + a1;
+}
+
+// Edge rows (order reduction, zero padding, free-surface images): weights
+// from the operator's edge table, offsets -H..H, branch-free (every offset is
+// inside the staged halo, dropped columns carry weight zero).
+template <int H>
+__device__ __forceinline__ float dtab(const float* __restrict__ s, int ci, int stride, const float* __restrict__ t)
+{
+    float w[2 * H + 1];
+#pragma unroll
+    for (int k = -H; k <= H; ++k) w[k + H] = __ldg(t + k);
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = -H; k <= H; ++k) acc += w[k + H] * s[ci + k * stride];
     return acc;
 }
 
-template <int H, bool FWD>
-__device__ __forceinline__ float d_queue(const float (&q)[2 * H + 1], int c, const Op1D& op)
+// derivative along a line of a smem tile; INT: the whole warp is on interior rows
+template <int H, bool FWD, bool INT>
+__device__ __forceinline__ float dline(const float* __restrict__ s, int ci, int stride, bool interior, const float* row, float scale)
 {
-    float acc = 0.0f;
-    if (!op.full && c >= op.E && c < op.n - op.E) {
-#pragma unroll
-        for (int k = (FWD ? -H + 1 : -H); k <= (FWD ? H : H - 1); ++k) acc += op.w[kMaxHalf + k] * q[H + k];
+    if constexpr (INT) {
+        return dsum<H, FWD>(s, ci, stride) * scale;
     } else {
-        const int slot = op.full ? c : (c < op.E ? c : op.E + c - (op.n - op.E));
-        const float* t = op.tab + slot * kTabW + kMaxHalf;
-#pragma unroll
-        for (int k = -H; k <= H; ++k) {
-            const float wk = __ldg(t + k);
-            if (wk != 0.0f) acc += wk * q[H + k];
-        }
+        if (interior) return dsum<H, FWD>(s, ci, stride) * scale;
+        return dtab<H>(s, ci, stride, row);
     }
+}
+
+template <int H, bool FWD, bool INT>
+__device__ __forceinline__ float dqueue(const float (&q)[2 * H + 1], bool interior, const float* row, float scale)
+{
+    float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 2 * H; j += 2) {
+        a0 += fdc(2 * H, j) * q[H + (FWD ? j - H + 1 : j - H)];
+        a1 += fdc(2 * H, j + 1) * q[H + (FWD ? j - H + 2 : j - H + 1)];
+    }
+    if constexpr (INT) return (a0 + a1) * scale;
+    if (interior) return (a0 + a1) * scale;
+    float w[2 * H + 1];
+#pragma unroll
+    for (int k = -H; k <= H; ++k) w[k + H] = __ldg(row + k);
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = -H; k <= H; ++k) acc += w[k + H] * q[H + k];
     return acc;
 }
 
 __device__ __forceinline__ int slab_of(int c, const Cpml1D& p)
 {
+    if (!p.on) return -1;
     if (p.n <= 2 * p.w) return c;
     if (c < p.w) return p.lo ? c : -1;
     if (c >= p.n - p.w) return c - (p.n - p.ns);
     return -1;
 }
 
-__device__ __forceinline__ void cpml_x(const StepParams& P, float& d, int x, int y, int z, bool half, int slot)
+// table row for coordinate c of an operator (edge rows only)
+__device__ __forceinline__ const float* row_of(const Op1D& op, int c)
 {
-    const int s = slab_of(x, P.cx);
-    if (s < 0) return;
-    float* psi = P.psi[slot] + s + (long long)P.cx.ns * (z + (long long)P.NZ * y);
-    float ps = *psi * (half ? P.cx.b_half[x] : P.cx.b_full[x]);
-    ps += (half ? P.cx.a_half[x] : P.cx.a_full[x]) * d;
-    *psi = ps;
-    d += ps;
+    const int slot = op.full ? c : (c < op.E ? c : op.E + c - (op.n - op.E));
+    return op.tab + slot * kTabW + kMaxHalf;
 }
-__device__ __forceinline__ void cpml_y(const StepParams& P, float& d, int x, int y, int z, bool half, int slot)
-{
-    const int s = slab_of(y, P.cy);
-    if (s < 0) return;
-    float* psi = P.psi[slot] + x + (long long)P.NX * (z + (long long)P.NZ * s);
-    float ps = *psi * (half ? P.cy.b_half[y] : P.cy.b_full[y]);
-    ps += (half ? P.cy.a_half[y] : P.cy.a_full[y]) * d;
-    *psi = ps;
-    d += ps;
-}
-__device__ __forceinline__ void cpml_z(const StepParams& P, float& d, int x, int y, int z, bool half, int slot)
-{
-    const int s = slab_of(z, P.cz);
-    if (s < 0) return;
-    float* psi = P.psi[slot] + x + (long long)P.NX * (s + (long long)P.cz.ns * y);
-    float ps = *psi * (half ? P.cz.b_half[z] : P.cz.b_full[z]);
-    ps += (half ? P.cz.a_half[z] : P.cz.a_full[z]) * d;
-    *psi = ps;
-    d += ps;
-}
+__device__ __forceinline__ bool interior_of(const Op1D& op, int c) { return !op.full && c >= op.E && c < op.n - op.E; }
 
 __device__ __forceinline__ float abs_damp(const StepParams& P, int x, int y, int z)
 {
@@ -218,38 +241,70 @@ __device__ __forceinline__ float abs_damp(const StepParams& P, int x, int y, int
     return m < w ? P.absCoeff[m] : 1.0f;
 }
 
-// calcInverseAveragedParameter on a 2-point average (Modelparameter.cpp:336-420, 633-639)
-__device__ __forceinline__ float inv_avg2(float a, float b, bool in)
+// per-thread state of the current column: coordinates, edge flags, CPML
+// coefficients and psi offsets along x and z (fixed while the CTA marches
+// down one tile)
+struct Column {
+    int x, z;
+    bool ok;                 // inside the grid
+    bool xi, zi;             // interior rows along x / z
+    int sx, sz;              // CPML slab indices (-1 outside)
+    float axf, bxf, axh, bxh, azf, bzf, azh, bzh;
+    long long px, pz;        // psi offsets without the y term
+    const float *rxf, *rxb, *rzf, *rzb;   // edge-table rows (edge columns only)
+    bool wint;               // every lane of the warp is on interior x and z rows
+};
+
+__device__ __forceinline__ void column_setup(Column& C, const StepParams& P, int x0, int z0)
 {
-    float s;
-    if (in) { s = 0.5f * a; s += 0.5f * b; }
-    else s = 1.0f * a;
-    const float r = 1.0f / s;
-    return isfinite(r) ? r : 0.0f;
+    C.x = x0 + (threadIdx.x & 31);
+    C.z = z0 + (threadIdx.x >> 5);
+    C.ok = C.x < P.NX && C.z < P.NZ;
+    C.xi = interior_of(P.Dxf, C.x);
+    C.zi = interior_of(P.Dzf, C.z);
+    C.sx = P.useCpml && C.ok ? slab_of(C.x, P.cx) : -1;
+    C.sz = P.useCpml && C.ok ? slab_of(C.z, P.cz) : -1;
+    C.axf = C.bxf = C.axh = C.bxh = C.azf = C.bzf = C.azh = C.bzh = 0.0f;
+    if (C.sx >= 0) { C.axf = P.cx.a_full[C.x]; C.bxf = P.cx.b_full[C.x]; C.axh = P.cx.a_half[C.x]; C.bxh = P.cx.b_half[C.x]; }
+    if (C.sz >= 0) { C.azf = P.cz.a_full[C.z]; C.bzf = P.cz.b_full[C.z]; C.azh = P.cz.a_half[C.z]; C.bzh = P.cz.b_half[C.z]; }
+    C.px = C.sx + (long long)P.cx.ns * C.z;            // + ns*NZ*y
+    C.pz = C.x + (long long)P.NX * C.sz;               // + NX*nsz*y
+    C.rxf = C.xi || !C.ok ? nullptr : row_of(P.Dxf, C.x);
+    C.rxb = C.xi || !C.ok ? nullptr : row_of(P.Dxb, C.x);
+    C.rzf = C.zi || !C.ok ? nullptr : row_of(P.Dzf, C.z);
+    C.rzb = C.zi || !C.ok ? nullptr : row_of(P.Dzb, C.z);
+    C.wint = __all_sync(0xffffffffu, (C.xi && C.zi) || !C.ok);
 }
 
-// harmonic 4-point modulus average with the edge fallbacks of
-// calc4PointAverageMatrixRow (Modelparameter.cpp:448-527) and the vacuum rule
-// of calcAveragedSWaveModulus (ModelparameterSeismic.cpp:421-432). i1..i4 are
-// the inverse moduli at the row point and its 2nd/3rd/4th neighbours; in2 /
-// in3 say whether the two axes of the plane stay inside the grid.
-__device__ __forceinline__ float harm4(float i1, float i2, float i3, float i4, bool inA, bool inB)
+// per-plane (CTA-uniform) state along y
+struct Plane {
+    int y;
+    bool yi;
+    int sy;
+    float ayf, byf, ayh, byh;
+};
+
+__device__ __forceinline__ void plane_setup(Plane& L, const StepParams& P, int y)
 {
-    float s;
-    if (inA && inB) {
-        s = 0.25f * i1; s += 0.25f * i2; s += 0.25f * i3; s += 0.25f * i4;
-    } else if (inA) {       // second axis out: 2-point along the first axis
-        s = 0.5f * i2; s += 0.5f * i1;
-    } else if (inB) {       // first axis out: 2-point along the second axis
-        s = 0.5f * i3; s += 0.5f * i1;
-    } else {
-        s = 1.0f * i1;
-    }
-    const float r = 1.0f / s;
-    return r < 4.0f ? 0.0f : r;
+    L.y = y;
+    L.yi = interior_of(P.Dyf, y);
+    L.sy = P.useCpml ? slab_of(y, P.cy) : -1;
+    L.ayf = L.byf = L.ayh = L.byh = 0.0f;
+    if (L.sy >= 0) { L.ayf = P.cy.a_full[y]; L.byf = P.cy.b_full[y]; L.ayh = P.cy.a_half[y]; L.byh = P.cy.b_half[y]; }
 }
 
-__device__ __forceinline__ float inv_clamped(float mu) { return 1.0f / (mu < 1.0f ? 1.0f : mu); }
+__device__ __forceinline__ float* psi_x(const StepParams& P, int slot, const Column& C, int y)
+{
+    return P.psi[slot] + C.px + (long long)P.cx.ns * P.NZ * y;
+}
+__device__ __forceinline__ float* psi_z(const StepParams& P, int slot, const Column& C, int y)
+{
+    return P.psi[slot] + C.pz + (long long)P.NX * P.cz.ns * y;
+}
+__device__ __forceinline__ float* psi_y(const StepParams& P, int slot, const Column& C, const Plane& L)
+{
+    return P.psi[slot] + C.x + (long long)P.NX * (C.z + (long long)P.NZ * L.sy);
+}
 
 __device__ __forceinline__ void report(int* err, int code)
 {
@@ -261,138 +316,350 @@ __device__ __forceinline__ void report(int* err, int code)
 using namespace el3d;
 
 // ------------------------------------------------------------------------
-// velocity pass (ForwardSolver3Delastic.cpp:174-277)
+// pipeline skeleton shared by the two passes
 // ------------------------------------------------------------------------
-template <int H>
-__device__ __forceinline__ void vel_issue(const El3dMaps& T, const StepParams& P, const El3dSched& S, unsigned char* smem,
-                                          uint64_t* bars, int it, long long g0, long long g1)
+// Box coordinate (along x or z) of a tile's CPML memory-variable box in the
+// compact slab layout, or kNoBox when the tile lies outside both slabs. The
+// host checks that no tile meets both slabs of an axis.
+constexpr int kNoBox = -(1 << 30);
+
+__device__ __forceinline__ int slab_box(const Cpml1D& p, int c0, int T)
 {
-    Iter I;
-    if (!iter_at(it, g0, g1, P.NY, H, I)) return;
-    constexpr int HB = hb_of(H), HX = hx_of(H);
-    const int s = it % NSTAGE;
-    unsigned char* st = smem + s * vel_stage(H);
-    uint64_t* bar = bars + s;
-    const int x0 = (I.tile % S.ntx) * TX, z0 = (I.tile / S.ntx) * TZ;
-    uint32_t bytes = 3 * CB + PBYTES;
-    if (I.compute) bytes += 5 * hbytes_of(H) + 3 * CB;
-    mbar_expect_tx(bar, bytes);
-    unsigned char* c = st + 5 * HB;
-    tma_load(c + 0 * CB, &T.cSxy, bar, x0, z0, I.q);
-    tma_load(c + 1 * CB, &T.cSyy, bar, x0, z0, I.q);
-    tma_load(c + 2 * CB, &T.cSyz, bar, x0, z0, I.q);
-    tma_load(st + 5 * HB + 6 * CB, &T.pRho, bar, x0, z0, I.c + 1);
-    if (I.compute) {
-        tma_load(st + 0 * HB, &T.hSxx, bar, x0 - HX, z0 - H, I.c);
-        tma_load(st + 1 * HB, &T.hSxy, bar, x0 - HX, z0 - H, I.c);
-        tma_load(st + 2 * HB, &T.hSxz, bar, x0 - HX, z0 - H, I.c);
-        tma_load(st + 3 * HB, &T.hSyz, bar, x0 - HX, z0 - H, I.c);
-        tma_load(st + 4 * HB, &T.hSzz, bar, x0 - HX, z0 - H, I.c);
-        tma_load(c + 3 * CB, &T.cVx, bar, x0, z0, I.c);
-        tma_load(c + 4 * CB, &T.cVy, bar, x0, z0, I.c);
-        tma_load(c + 5 * CB, &T.cVz, bar, x0, z0, I.c);
+    if (!p.on) return kNoBox;
+    if (p.n <= 2 * p.w) return c0;
+    if (p.lo && c0 < p.w) return c0;
+    if (c0 + T > p.n - p.w) return c0 - (p.n - p.ns);
+    return kNoBox;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
+}
+
+// reciprocal by the hardware approximation (rcp.approx, 1 ulp)
+__device__ __forceinline__ float rcp_fast(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// calcInverseAveragedParameter on a 2-point average (Modelparameter.cpp:336-420, 633-639)
+__device__ __forceinline__ float inv_avg2f(float a, float b, bool in)
+{
+    float s;
+    if (in) { s = 0.5f * a; s += 0.5f * b; }
+    else s = a;
+    const float r = rcp_fast(s);
+    return isfinite(r) ? r : 0.0f;
+}
+
+// harmonic 4-point modulus average with the edge fallbacks of
+// calc4PointAverageMatrixRow (Modelparameter.cpp:448-527) and the vacuum rule
+// of calcAveragedSWaveModulus (ModelparameterSeismic.cpp:421-432). i1..i4 are
+// the inverse moduli at the row point and its 2nd/3rd/4th neighbours; inA /
+// inB say whether the two axes of the plane stay inside the grid.
+__device__ __forceinline__ float harm4f(float i1, float i2, float i3, float i4, bool inA, bool inB)
+{
+    float s;
+    if (inA && inB) {
+        s = 0.25f * i1; s += 0.25f * i2; s += 0.25f * i3; s += 0.25f * i4;
+    } else if (inA) {
+        s = 0.5f * i2; s += 0.5f * i1;
+    } else if (inB) {
+        s = 0.5f * i3; s += 0.5f * i1;
+    } else {
+        s = i1;
+    }
+    const float r = rcp_fast(s);
+    return r < 4.0f ? 0.0f : r;
+}
+
+__device__ __forceinline__ float inv_clampedf(float mu) { return rcp_fast(mu < 1.0f ? 1.0f : mu); }
+
+// CPML::applyCPML (CPML.cpp:84-95): psi = b*psi + a*d; d += psi, with the old
+// psi staged in shared memory by the producer and the new one written to HBM
+__device__ __forceinline__ void cpml_s(float& d, float ps, float* gpsi, float a, float b)
+{
+    ps *= b;
+    ps += a * d;
+    *gpsi = ps;
+    d += ps;
+}
+
+// Layout of one pipeline stage; psi boxes are x-type [0,3), y-type [3,6), z-type [6,9).
+template <int H, int NHALO, int NCEN>
+struct Stage {
+    static constexpr int HB = hb_of(H);
+    static constexpr int HALO = 0;
+    static constexpr int CEN = NHALO * HB;
+    static constexpr int PLUS = CEN + NCEN * CB;
+    static constexpr int PSI = PLUS + PB;
+    static constexpr int BYTES = PSI + 9 * CB;
+    static constexpr int NST = 3;   // measured faster than 4 (more L1 left beside the ring)
+};
+
+template <int H> using VelStage = Stage<H, 5, 6>;
+template <int H> using StrStage = Stage<H, 3, 10>;
+
+// The CPML memory-variable boxes a (tile, plane c) iteration needs.
+struct PsiBoxes {
+    int bx, bz, sy;   // x-type / z-type box coordinates (kNoBox: none), y slab plane (-1: none)
+    __device__ __forceinline__ uint32_t bytes() const
+    {
+        return ((bx != kNoBox) + (sy >= 0) + (bz != kNoBox)) * 3u * CB;
+    }
+};
+
+__device__ __forceinline__ PsiBoxes psi_boxes(const StepParams& P, int x0, int z0, int c)
+{
+    if (!P.useCpml) return {kNoBox, kNoBox, -1};
+    return {slab_box(P.cx, x0, TX), slab_box(P.cz, z0, TZ), slab_of(c, P.cy)};
+}
+
+// issues the psi boxes of one iteration into the stage's psi slots
+__device__ __forceinline__ void issue_psi(const PsiBoxes& B, const CUtensorMap* m, unsigned char* ps, uint64_t* bar,
+                                          int x0, int z0, int c)
+{
+    if (B.bx != kNoBox)
+        for (int j = 0; j < 3; ++j) tma_load(ps + j * CB, m + j, bar, B.bx, z0, c);
+    if (B.sy >= 0)
+        for (int j = 3; j < 6; ++j) tma_load(ps + j * CB, m + j, bar, x0, z0, B.sy);
+    if (B.bz != kNoBox)
+        for (int j = 6; j < 9; ++j) tma_load(ps + j * CB, m + j, bar, x0, B.bz, c);
+}
+
+// The copy feeder, run by thread 0: issues iterations in order into the ring.
+struct Feeder {
+    Cursor cur{0, 0};
+    int issued = 0;
+};
+
+// fills the ring with iterations [0, NST)
+template <int NST, class IssueFn>
+__device__ __forceinline__ void start_feed(Feeder& F, const Segs& G, int total, IssueFn issue)
+{
+    for (int i = 0; i < NST && i < total; ++i) {
+        issue(i, F.cur);
+        F.cur.advance(G);
+        ++F.issued;
     }
 }
 
+// waits (bounded) for the feeder's copies that may still be in flight
+template <int NST>
+__device__ __forceinline__ void drain(const Feeder& F, uint64_t* full)
+{
+    const int from = F.issued > NST ? F.issued - NST : 0;
+    for (int k = from; k < F.issued; ++k) mbar_wait(full + k % NST, (k / NST) & 1);
+}
+
+// Refills the stage of iteration j (all warps have released it) with
+// iteration j + NST. On a timed-out wait it sets the failure flag, waits for
+// its own copies in flight and returns false.
+template <int NST, class IssueFn>
+__device__ __forceinline__ bool refill(Feeder& F, const Segs& G, int j, int total, uint64_t* full, uint64_t* empty,
+                                       volatile int* failed, int* err, IssueFn issue)
+{
+    if (j < 0 || j + NST >= total) return true;
+    const int s = j % NST;
+    if (!mbar_wait(empty + s, (j / NST) & 1)) {
+        *failed = 1;
+        report(err, WAVE_ERR_TIMEOUT);
+        drain<NST>(F, full);
+        return false;
+    }
+    issue(s, F.cur);
+    F.cur.advance(G);
+    ++F.issued;
+    return true;
+}
+
+// common prologue: barrier init, schedule, abort check, tensor-map prefetch.
+// Returns the CTA's iteration count.
+template <int NST>
+__device__ __forceinline__ int prologue(Segs& G, uint64_t* full, uint64_t* empty, int* abortRun, volatile int* failed,
+                                        const StepParams& P, const El3dSched& S, int H, const El3dMaps& T)
+{
+    if (threadIdx.x < sizeof(El3dMaps) / sizeof(CUtensorMap)) {
+        const CUtensorMap* m = reinterpret_cast<const CUtensorMap*>(&T) + threadIdx.x;
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
+    }
+    const long long GT = (long long)S.ntx * S.ntz * P.NY;
+    const long long g0 = GT * blockIdx.x / gridDim.x, g1 = GT * (blockIdx.x + 1) / gridDim.x;
+    if (threadIdx.x == 0) {
+        // a failed wait in an earlier launch leaves the error word set: skip the work
+        *abortRun = (S.err && *reinterpret_cast<volatile int*>(S.err) != 0) ? 1 : 0;
+        *failed = 0;
+        for (int s = 0; s < NST; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, NCWARP);
+        }
+        fence_barrier_init();
+        build_segments(G, g0, g1, P.NY, H);
+    }
+    __syncthreads();
+    int total = 0;
+    for (int k = 0; k < G.n; ++k) total += G.len[k];
+    return *abortRun ? 0 : total;
+}
+
+// consumer side of one iteration's end: the warp releases the stage
+__device__ __forceinline__ void release(uint64_t* empty)
+{
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(empty);
+}
+
+// ------------------------------------------------------------------------
+// velocity pass (ForwardSolver3Delastic.cpp:174-277)
+// ------------------------------------------------------------------------
 template <int H>
 __global__ void __launch_bounds__(NTHR, 1) el3d_vel(const __grid_constant__ El3dMaps T, const StepParams P, const El3dSched S)
 {
+    using L = VelStage<H>;
+    constexpr int NST = L::NST, HX = hx_of(H), BW = bw_of(H), TT = TX * TZ;
     extern __shared__ __align__(128) unsigned char smem[];
-    constexpr int HB = hb_of(H), HX = hx_of(H), BW = bw_of(H), ST = vel_stage(H);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NSTAGE * ST);
-    const int tx = threadIdx.x, tz = threadIdx.y, tid = tz * TX + tx;
-    const long long G = (long long)S.ntx * S.ntz * P.NY;
-    const long long g0 = G * blockIdx.x / gridDim.x, g1 = G * (blockIdx.x + 1) / gridDim.x;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * L::BYTES);
+    uint64_t* empty = full + NST;
+    __shared__ Segs G;
     __shared__ int abortRun;
-    if (tid == 0) {
-        // a failed wait in an earlier launch leaves the error word set: skip the work
-        abortRun = (S.err && *reinterpret_cast<volatile int*>(S.err) != 0) ? 1 : 0;
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(bars + s, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    const int total = abortRun ? 0 : total_iters(g0, g1, P.NY, H);
-    if (tid == 0)
-        for (int i = 0; i < NSTAGE && i < total; ++i) vel_issue<H>(T, P, S, smem, bars, i, g0, g1);
+    __shared__ volatile int failed;
+    const int total = prologue<NST>(G, full, empty, &abortRun, &failed, P, S, H, T);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+    auto issue = [&](int s, const Cursor& cur) {
+        unsigned char* st = smem + s * L::BYTES;
+        uint64_t* bar = full + s;
+        const int tile = G.tile[cur.seg], ya = G.ya[cur.seg];
+        const int q = ya - H + cur.k, c = ya - 2 * H + cur.k;
+        const bool compute = c >= ya;
+        const int x0 = (tile % S.ntx) * TX, z0 = (tile / S.ntx) * TZ;
+        const PsiBoxes B = compute ? psi_boxes(P, x0, z0, c) : PsiBoxes{kNoBox, kNoBox, -1};
+        uint32_t bytes = 3 * CB + PBYTES + B.bytes();
+        if (compute) bytes += 5 * hbytes_of(H) + 3 * CB;
+        mbar_expect_tx(bar, bytes);
+        issue_psi(B, T.psV, st + L::PSI, bar, x0, z0, c);
+        unsigned char* cen = st + L::CEN;
+        tma_load(cen + 0 * CB, &T.cSxy, bar, x0, z0, q);
+        tma_load(cen + 1 * CB, &T.cSyy, bar, x0, z0, q);
+        tma_load(cen + 2 * CB, &T.cSyz, bar, x0, z0, q);
+        tma_load(st + L::PLUS, &T.pRho, bar, x0, z0, c + 1);
+        if (compute) {
+            tma_load(st + 0 * L::HB, &T.hSxx, bar, x0 - HX, z0 - H, c);
+            tma_load(st + 1 * L::HB, &T.hSxy, bar, x0 - HX, z0 - H, c);
+            tma_load(st + 2 * L::HB, &T.hSxz, bar, x0 - HX, z0 - H, c);
+            tma_load(st + 3 * L::HB, &T.hSyz, bar, x0 - HX, z0 - H, c);
+            tma_load(st + 4 * L::HB, &T.hSzz, bar, x0 - HX, z0 - H, c);
+            tma_load(cen + 3 * CB, &T.cVx, bar, x0, z0, c);
+            tma_load(cen + 4 * CB, &T.cVy, bar, x0, z0, c);
+            tma_load(cen + 5 * CB, &T.cVz, bar, x0, z0, c);
+        }
+    };
+    Feeder F;
+    if (threadIdx.x == 0) start_feed<NST>(F, G, total, issue);
+
+    const int tid = threadIdx.x;    // x = x0 + lane, z = z0 + warp
     float qxy[2 * H + 1], qyy[2 * H + 1], qyz[2 * H + 1];
 #pragma unroll
     for (int k = 0; k <= 2 * H; ++k) qxy[k] = qyy[k] = qyz[k] = 0.0f;
     float r0 = 0.0f, rx = 0.0f, rz = 0.0f;   // rho at the compute plane: (x,z), (x+1,z), (x,z+1)
     const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
     const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
-    const int ci = (tz + H) * BW + (tx + HX);
-    bool failed = false;
+    const float scale = P.scale;
+    const int ci = (warp + H) * BW + (lane + HX);
+    Cursor cur{0, 0};
+    Column C;
 
     for (int it = 0; it < total; ++it) {
-        const int s = it % NSTAGE;
-        Iter I;
-        iter_at(it, g0, g1, P.NY, H, I);
-        if (!mbar_wait(bars + s, (it / NSTAGE) & 1)) failed = true;
-        if (__syncthreads_or(failed)) {
-            if (tid == 0) report(S.err, WAVE_ERR_TIMEOUT);
+        const int s = it % NST;
+        const int tile = G.tile[cur.seg], ya = G.ya[cur.seg];
+        if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ);
+        const int y = ya - 2 * H + cur.k;
+        const bool compute = y >= ya;
+        if (!mbar_wait(full + s, (it / NST) & 1)) {
+            failed = 1;
+            report(S.err, WAVE_ERR_TIMEOUT);
+            if (threadIdx.x == 0) drain<NST>(F, full);
             return;
         }
-        const unsigned char* st = smem + s * ST;
-        const float* cen = reinterpret_cast<const float*>(st + 5 * HB);
+        const unsigned char* st = smem + s * L::BYTES;
+        const float* cen = reinterpret_cast<const float*>(st + L::CEN);
 #pragma unroll
         for (int k = 0; k < 2 * H; ++k) { qxy[k] = qxy[k + 1]; qyy[k] = qyy[k + 1]; qyz[k] = qyz[k + 1]; }
-        qxy[2 * H] = cen[0 * TX * TZ + tid];
-        qyy[2 * H] = cen[1 * TX * TZ + tid];
-        qyz[2 * H] = cen[2 * TX * TZ + tid];
-        const float* rb = reinterpret_cast<const float*>(st + 5 * HB + 6 * CB);
-        const float rn = rb[tz * PW + tx];      // rho at (x, z, c+1)
-        const int x = (I.tile % S.ntx) * TX + tx, z = (I.tile / S.ntx) * TZ + tz, y = I.c;
-        if (I.compute && x < P.NX && z < P.NZ) {
-            const float* hSxx = reinterpret_cast<const float*>(st + 0 * HB);
-            const float* hSxy = reinterpret_cast<const float*>(st + 1 * HB);
-            const float* hSxz = reinterpret_cast<const float*>(st + 2 * HB);
-            const float* hSyz = reinterpret_cast<const float*>(st + 3 * HB);
-            const float* hSzz = reinterpret_cast<const float*>(st + 4 * HB);
-            const long long i = x + (long long)P.NX * (z + (long long)P.NZ * y);
-            // vx
-            float u = d_line<H, true>(hSxx, ci, 1, x, P.Dxf);
-            if (P.useCpml) cpml_x(P, u, x, y, z, true, PS_SXX_X);
-            float ut = d_queue<H, false>(qxy, y, DybS);
-            if (P.useCpml) cpml_y(P, ut, x, y, z, false, PS_SXY_Y);
-            u += ut;
-            ut = d_line<H, false>(hSxz, ci, BW, z, P.Dzb);
-            if (P.useCpml) cpml_z(P, ut, x, y, z, false, PS_SXZ_Z);
-            u += ut;
-            u *= inv_avg2(r0, rx, x + 1 < P.NX);
-            P.f[F_VX][i] = cen[3 * TX * TZ + tid] + u;
-            // vy
-            u = d_line<H, false>(hSxy, ci, 1, x, P.Dxb);
-            if (P.useCpml) cpml_x(P, u, x, y, z, false, PS_SXY_X);
-            ut = d_queue<H, true>(qyy, y, DyfS);
-            if (P.useCpml) cpml_y(P, ut, x, y, z, true, PS_SYY_Y);
-            u += ut;
-            ut = d_line<H, false>(hSyz, ci, BW, z, P.Dzb);
-            if (P.useCpml) cpml_z(P, ut, x, y, z, false, PS_SYZ_Z);
-            u += ut;
-            u *= inv_avg2(r0, rn, y + 1 < P.NY);
-            P.f[F_VY][i] = cen[4 * TX * TZ + tid] + u;
-            // vz
-            u = d_line<H, false>(hSxz, ci, 1, x, P.Dxb);
-            if (P.useCpml) cpml_x(P, u, x, y, z, false, PS_SXZ_X);
-            ut = d_queue<H, false>(qyz, y, DybS);
-            if (P.useCpml) cpml_y(P, ut, x, y, z, false, PS_SYZ_Y);
-            u += ut;
-            ut = d_line<H, true>(hSzz, ci, BW, z, P.Dzf);
-            if (P.useCpml) cpml_z(P, ut, x, y, z, true, PS_SZZ_Z);
-            u += ut;
-            u *= inv_avg2(r0, rz, z + 1 < P.NZ);
-            P.f[F_VZ][i] = cen[5 * TX * TZ + tid] + u;
+        qxy[2 * H] = cen[0 * TT + tid];
+        qyy[2 * H] = cen[1 * TT + tid];
+        qyz[2 * H] = cen[2 * TT + tid];
+        const float* rb = reinterpret_cast<const float*>(st + L::PLUS);
+        const float rn = rb[warp * PW + lane];      // rho at (x, z, y+1)
+        if (compute && C.ok) {
+            Plane Y;
+            plane_setup(Y, P, y);
+            const float* hSxx = reinterpret_cast<const float*>(st + 0 * L::HB);
+            const float* hSxy = reinterpret_cast<const float*>(st + 1 * L::HB);
+            const float* hSxz = reinterpret_cast<const float*>(st + 2 * L::HB);
+            const float* hSyz = reinterpret_cast<const float*>(st + 3 * L::HB);
+            const float* hSzz = reinterpret_cast<const float*>(st + 4 * L::HB);
+            const float* ps = reinterpret_cast<const float*>(st + L::PSI) + tid;
+            const float* ryb = Y.yi ? nullptr : row_of(DybS, y);
+            const float* ryf = Y.yi ? nullptr : row_of(DyfS, y);
+            const long long i = C.x + (long long)P.NX * (C.z + (long long)P.NZ * y);
+            auto body = [&](auto interior) {
+                constexpr bool INT = decltype(interior)::value;
+                // the nine stress derivatives first (independent FMA chains), then CPML
+                float dSxx_x = dline<H, true, INT>(hSxx, ci, 1, C.xi, C.rxf, scale);
+                float dSxy_x = dline<H, false, INT>(hSxy, ci, 1, C.xi, C.rxb, scale);
+                float dSxz_x = dline<H, false, INT>(hSxz, ci, 1, C.xi, C.rxb, scale);
+                float dSxy_y = dqueue<H, false, INT>(qxy, Y.yi, ryb, scale);
+                float dSyy_y = dqueue<H, true, INT>(qyy, Y.yi, ryf, scale);
+                float dSyz_y = dqueue<H, false, INT>(qyz, Y.yi, ryb, scale);
+                float dSxz_z = dline<H, false, INT>(hSxz, ci, BW, C.zi, C.rzb, scale);
+                float dSyz_z = dline<H, false, INT>(hSyz, ci, BW, C.zi, C.rzb, scale);
+                float dSzz_z = dline<H, true, INT>(hSzz, ci, BW, C.zi, C.rzf, scale);
+                if (C.sx >= 0) {
+                    cpml_s(dSxx_x, ps[0 * TT], psi_x(P, PS_SXX_X, C, y), C.axh, C.bxh);
+                    cpml_s(dSxy_x, ps[1 * TT], psi_x(P, PS_SXY_X, C, y), C.axf, C.bxf);
+                    cpml_s(dSxz_x, ps[2 * TT], psi_x(P, PS_SXZ_X, C, y), C.axf, C.bxf);
+                }
+                if (Y.sy >= 0) {
+                    cpml_s(dSxy_y, ps[3 * TT], psi_y(P, PS_SXY_Y, C, Y), Y.ayf, Y.byf);
+                    cpml_s(dSyy_y, ps[4 * TT], psi_y(P, PS_SYY_Y, C, Y), Y.ayh, Y.byh);
+                    cpml_s(dSyz_y, ps[5 * TT], psi_y(P, PS_SYZ_Y, C, Y), Y.ayf, Y.byf);
+                }
+                if (C.sz >= 0) {
+                    cpml_s(dSxz_z, ps[6 * TT], psi_z(P, PS_SXZ_Z, C, y), C.azf, C.bzf);
+                    cpml_s(dSyz_z, ps[7 * TT], psi_z(P, PS_SYZ_Z, C, y), C.azf, C.bzf);
+                    cpml_s(dSzz_z, ps[8 * TT], psi_z(P, PS_SZZ_Z, C, y), C.azh, C.bzh);
+                }
+                float u = dSxx_x;
+                u += dSxy_y;
+                u += dSxz_z;
+                u *= inv_avg2f(r0, rx, C.x + 1 < P.NX);
+                P.f[F_VX][i] = cen[3 * TT + tid] + u;
+                u = dSxy_x;
+                u += dSyy_y;
+                u += dSyz_z;
+                u *= inv_avg2f(r0, rn, y + 1 < P.NY);
+                P.f[F_VY][i] = cen[4 * TT + tid] + u;
+                u = dSxz_x;
+                u += dSyz_y;
+                u += dSzz_z;
+                u *= inv_avg2f(r0, rz, C.z + 1 < P.NZ);
+                P.f[F_VZ][i] = cen[5 * TT + tid] + u;
+            };
+            if (C.wint && Y.yi) body(std::true_type{});
+            else body(std::false_type{});
         }
-        // carry rho of plane c+1 into the next iteration
+        // carry rho of plane y+1 into the next iteration
         r0 = rn;
-        rx = rb[tz * PW + tx + 1];
-        rz = rb[(tz + 1) * PW + tx];
-        __syncthreads();
-        if (tid == 0 && it + NSTAGE < total) {
-            fence_proxy_async();
-            vel_issue<H>(T, P, S, smem, bars, it + NSTAGE, g0, g1);
-        }
+        rx = rb[warp * PW + lane + 1];
+        rz = rb[(warp + 1) * PW + lane];
+        release(empty + s);
+        // thread 0 refills the stage released one iteration earlier
+        if (threadIdx.x == 0) refill<NST>(F, G, it - 1, total, full, empty, &failed, S.err, issue);
+        if (failed) return;
+        cur.advance(G);
     }
 }
 
@@ -400,170 +667,188 @@ __global__ void __launch_bounds__(NTHR, 1) el3d_vel(const __grid_constant__ El3d
 // stress pass (ForwardSolver3Delastic.cpp:283-409, FreeSurface3Delastic.cpp:15-47)
 // ------------------------------------------------------------------------
 template <int H>
-__device__ __forceinline__ void str_issue(const El3dMaps& T, const StepParams& P, const El3dSched& S, unsigned char* smem,
-                                          uint64_t* bars, int it, long long g0, long long g1)
-{
-    Iter I;
-    if (!iter_at(it, g0, g1, P.NY, H, I)) return;
-    constexpr int HB = hb_of(H), HX = hx_of(H);
-    const int s = it % NSTAGE;
-    unsigned char* st = smem + s * str_stage(H);
-    uint64_t* bar = bars + s;
-    const int x0 = (I.tile % S.ntx) * TX, z0 = (I.tile / S.ntx) * TZ;
-    uint32_t bytes = 3 * CB + PBYTES;
-    if (I.compute) bytes += 3 * hbytes_of(H) + 7 * CB;
-    mbar_expect_tx(bar, bytes);
-    unsigned char* c = st + 3 * HB;
-    tma_load(c + 0 * CB, &T.cVx, bar, x0, z0, I.q);
-    tma_load(c + 1 * CB, &T.cVy, bar, x0, z0, I.q);
-    tma_load(c + 2 * CB, &T.cVz, bar, x0, z0, I.q);
-    tma_load(st + 3 * HB + 10 * CB, &T.pMu, bar, x0, z0, I.c + 1);
-    if (I.compute) {
-        tma_load(st + 0 * HB, &T.hVx, bar, x0 - HX, z0 - H, I.c);
-        tma_load(st + 1 * HB, &T.hVy, bar, x0 - HX, z0 - H, I.c);
-        tma_load(st + 2 * HB, &T.hVz, bar, x0 - HX, z0 - H, I.c);
-        tma_load(c + 3 * CB, &T.cSxx, bar, x0, z0, I.c);
-        tma_load(c + 4 * CB, &T.cSyy, bar, x0, z0, I.c);
-        tma_load(c + 5 * CB, &T.cSzz, bar, x0, z0, I.c);
-        tma_load(c + 6 * CB, &T.cSxy, bar, x0, z0, I.c);
-        tma_load(c + 7 * CB, &T.cSxz, bar, x0, z0, I.c);
-        tma_load(c + 8 * CB, &T.cSyz, bar, x0, z0, I.c);
-        tma_load(c + 9 * CB, &T.cM, bar, x0, z0, I.c);
-    }
-}
-
-template <int H>
 __global__ void __launch_bounds__(NTHR, 1) el3d_str(const __grid_constant__ El3dMaps T, const StepParams P, const El3dSched S)
 {
+    using L = StrStage<H>;
+    constexpr int NST = L::NST, HX = hx_of(H), BW = bw_of(H), TT = TX * TZ;
     extern __shared__ __align__(128) unsigned char smem[];
-    constexpr int HB = hb_of(H), HX = hx_of(H), BW = bw_of(H), ST = str_stage(H);
-    constexpr int TT = TX * TZ;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NSTAGE * ST);
-    const int tx = threadIdx.x, tz = threadIdx.y, tid = tz * TX + tx;
-    const long long G = (long long)S.ntx * S.ntz * P.NY;
-    const long long g0 = G * blockIdx.x / gridDim.x, g1 = G * (blockIdx.x + 1) / gridDim.x;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * L::BYTES);
+    uint64_t* empty = full + NST;
+    __shared__ Segs G;
     __shared__ int abortRun;
-    if (tid == 0) {
-        // a failed wait in an earlier launch leaves the error word set: skip the work
-        abortRun = (S.err && *reinterpret_cast<volatile int*>(S.err) != 0) ? 1 : 0;
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(bars + s, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    const int total = abortRun ? 0 : total_iters(g0, g1, P.NY, H);
-    if (tid == 0)
-        for (int i = 0; i < NSTAGE && i < total; ++i) str_issue<H>(T, P, S, smem, bars, i, g0, g1);
+    __shared__ volatile int failed;
+    const int total = prologue<NST>(G, full, empty, &abortRun, &failed, P, S, H, T);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+    auto issue = [&](int s, const Cursor& cur) {
+        unsigned char* st = smem + s * L::BYTES;
+        uint64_t* bar = full + s;
+        const int tile = G.tile[cur.seg], ya = G.ya[cur.seg];
+        const int q = ya - H + cur.k, c = ya - 2 * H + cur.k;
+        const bool compute = c >= ya;
+        const int x0 = (tile % S.ntx) * TX, z0 = (tile / S.ntx) * TZ;
+        const PsiBoxes B = compute ? psi_boxes(P, x0, z0, c) : PsiBoxes{kNoBox, kNoBox, -1};
+        uint32_t bytes = 3 * CB + PBYTES + B.bytes();
+        if (compute) bytes += 3 * hbytes_of(H) + 7 * CB;
+        mbar_expect_tx(bar, bytes);
+        issue_psi(B, T.psS, st + L::PSI, bar, x0, z0, c);
+        unsigned char* cen = st + L::CEN;
+        tma_load(cen + 0 * CB, &T.cVx, bar, x0, z0, q);
+        tma_load(cen + 1 * CB, &T.cVy, bar, x0, z0, q);
+        tma_load(cen + 2 * CB, &T.cVz, bar, x0, z0, q);
+        tma_load(st + L::PLUS, &T.pMu, bar, x0, z0, c + 1);
+        if (compute) {
+            tma_load(st + 0 * L::HB, &T.hVx, bar, x0 - HX, z0 - H, c);
+            tma_load(st + 1 * L::HB, &T.hVy, bar, x0 - HX, z0 - H, c);
+            tma_load(st + 2 * L::HB, &T.hVz, bar, x0 - HX, z0 - H, c);
+            tma_load(cen + 3 * CB, &T.cSxx, bar, x0, z0, c);
+            tma_load(cen + 4 * CB, &T.cSyy, bar, x0, z0, c);
+            tma_load(cen + 5 * CB, &T.cSzz, bar, x0, z0, c);
+            tma_load(cen + 6 * CB, &T.cSxy, bar, x0, z0, c);
+            tma_load(cen + 7 * CB, &T.cSxz, bar, x0, z0, c);
+            tma_load(cen + 8 * CB, &T.cSyz, bar, x0, z0, c);
+            tma_load(cen + 9 * CB, &T.cM, bar, x0, z0, c);
+        }
+    };
+    Feeder F;
+    if (threadIdx.x == 0) start_feed<NST>(F, G, total, issue);
+
+    const int tid = threadIdx.x;
     float qx[2 * H + 1], qy[2 * H + 1], qz[2 * H + 1];
 #pragma unroll
     for (int k = 0; k <= 2 * H; ++k) qx[k] = qy[k] = qz[k] = 0.0f;
-    // mu at the compute plane: (x,z), (x+1,z), (x,z+1), (x+1,z+1)
-    float m00 = 1.0f, m10 = 1.0f, m01 = 1.0f, m11 = 1.0f;
-    const int ci = (tz + H) * BW + (tx + HX);
-    bool failed = false;
+    // inverse clamped mu at the compute plane: (x,z), (x+1,z), (x,z+1), (x+1,z+1), and mu itself
+    float i00 = 1.0f, i10 = 1.0f, i01 = 1.0f, i11 = 1.0f, m00 = 1.0f;
+    const float scale = P.scale;
+    const int ci = (warp + H) * BW + (lane + HX);
+    Cursor cur{0, 0};
+    Column C;
 
     for (int it = 0; it < total; ++it) {
-        const int s = it % NSTAGE;
-        Iter I;
-        iter_at(it, g0, g1, P.NY, H, I);
-        if (!mbar_wait(bars + s, (it / NSTAGE) & 1)) failed = true;
-        if (__syncthreads_or(failed)) {
-            if (tid == 0) report(S.err, WAVE_ERR_TIMEOUT);
+        const int s = it % NST;
+        const int tile = G.tile[cur.seg], ya = G.ya[cur.seg];
+        if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ);
+        const int y = ya - 2 * H + cur.k;
+        const bool compute = y >= ya;
+        if (!mbar_wait(full + s, (it / NST) & 1)) {
+            failed = 1;
+            report(S.err, WAVE_ERR_TIMEOUT);
+            if (threadIdx.x == 0) drain<NST>(F, full);
             return;
         }
-        const unsigned char* st = smem + s * ST;
-        const float* cen = reinterpret_cast<const float*>(st + 3 * HB);
+        const unsigned char* st = smem + s * L::BYTES;
+        const float* cen = reinterpret_cast<const float*>(st + L::CEN);
 #pragma unroll
         for (int k = 0; k < 2 * H; ++k) { qx[k] = qx[k + 1]; qy[k] = qy[k + 1]; qz[k] = qz[k + 1]; }
         qx[2 * H] = cen[0 * TT + tid];
         qy[2 * H] = cen[1 * TT + tid];
         qz[2 * H] = cen[2 * TT + tid];
-        const float* mb = reinterpret_cast<const float*>(st + 3 * HB + 10 * CB);
-        const float n00 = mb[tz * PW + tx], n10 = mb[tz * PW + tx + 1], n01 = mb[(tz + 1) * PW + tx];
-        const int x = (I.tile % S.ntx) * TX + tx, z = (I.tile / S.ntx) * TZ + tz, y = I.c;
-        if (I.compute && x < P.NX && z < P.NZ) {
-            const float* hVx = reinterpret_cast<const float*>(st + 0 * HB);
-            const float* hVy = reinterpret_cast<const float*>(st + 1 * HB);
-            const float* hVz = reinterpret_cast<const float*>(st + 2 * HB);
-            const long long i = x + (long long)P.NX * (z + (long long)P.NZ * y);
-            const bool inX = x + 1 < P.NX, inY = y + 1 < P.NY, inZ = z + 1 < P.NZ;
+        const float* mb = reinterpret_cast<const float*>(st + L::PLUS);
+        const float n00 = mb[warp * PW + lane];
+        const float j00 = inv_clampedf(n00), j10 = inv_clampedf(mb[warp * PW + lane + 1]);
+        const float j01 = inv_clampedf(mb[(warp + 1) * PW + lane]), j11 = inv_clampedf(mb[(warp + 1) * PW + lane + 1]);
+        if (compute && C.ok) {
+            Plane Y;
+            plane_setup(Y, P, y);
+            const float* hVx = reinterpret_cast<const float*>(st + 0 * L::HB);
+            const float* hVy = reinterpret_cast<const float*>(st + 1 * L::HB);
+            const float* hVz = reinterpret_cast<const float*>(st + 2 * L::HB);
+            const float* ps = reinterpret_cast<const float*>(st + L::PSI) + tid;
+            const float* ryf = Y.yi ? nullptr : row_of(P.Dyf, y);
+            const float* ryb = Y.yi ? nullptr : row_of(P.Dyb, y);
+            const long long i = C.x + (long long)P.NX * (C.z + (long long)P.NZ * y);
+            const bool inX = C.x + 1 < P.NX, inY = y + 1 < P.NY, inZ = C.z + 1 < P.NZ;
             const float M = cen[9 * TT + tid];
             const float mu = m00 < 1.0f ? 1.0f : m00;
-            const float i00 = inv_clamped(m00), i10 = inv_clamped(m10), i01 = inv_clamped(m01), i11 = inv_clamped(m11);
-            const float j00 = inv_clamped(n00), j10 = inv_clamped(n10), j01 = inv_clamped(n01);
             // XY: (x,y) (x+1,y) (x,y+1) (x+1,y+1); XZ: (x,z) (x+1,z) (x,z+1) (x+1,z+1);
             // YZ: (y,z) (y+1,z) (y,z+1) (y+1,z+1)  (calcAverageMatrixXY/XZ/YZ, Modelparameter.cpp:533-624)
-            const float muXY = harm4(i00, i10, j00, j10, inX, inY);
-            const float muXZ = harm4(i00, i10, i01, i11, inX, inZ);
-            const float muYZ = harm4(i00, j00, i01, j01, inY, inZ);
+            const float muXY = harm4f(i00, i10, j00, j10, inX, inY);
+            const float muXZ = harm4f(i00, i10, i01, i11, inX, inZ);
+            const float muYZ = harm4f(i00, j00, i01, j01, inY, inZ);
 
-            float vxx = d_line<H, false>(hVx, ci, 1, x, P.Dxb);
-            if (P.useCpml) cpml_x(P, vxx, x, y, z, false, PS_VXX);
-            float vyy = d_queue<H, false>(qy, y, P.Dyb);
-            if (P.useCpml) cpml_y(P, vyy, x, y, z, false, PS_VYY);
-            float vzz = d_line<H, false>(hVz, ci, BW, z, P.Dzb);
-            if (P.useCpml) cpml_z(P, vzz, x, y, z, false, PS_VZZ);
-            float sxx = cen[3 * TT + tid], syy = cen[4 * TT + tid], szz = cen[5 * TT + tid];
-            float u = vxx;
-            u += vyy;
-            u += vzz;
-            u *= M;
-            sxx += u; syy += u; szz += u;
-            u = vyy + vzz; u *= mu; sxx -= 2.0f * u;
-            u = vxx + vzz; u *= mu; syy -= 2.0f * u;
-            u = vxx + vyy; u *= mu; szz -= 2.0f * u;
-            // shear
-            u = d_queue<H, true>(qx, y, P.Dyf);
-            if (P.useCpml) cpml_y(P, u, x, y, z, true, PS_VXY);
-            float ut = d_line<H, true>(hVy, ci, 1, x, P.Dxf);
-            if (P.useCpml) cpml_x(P, ut, x, y, z, true, PS_VYX);
-            u += ut;
-            u *= muXY;
-            float sxy = cen[6 * TT + tid] + u;
-            u = d_line<H, true>(hVx, ci, BW, z, P.Dzf);
-            if (P.useCpml) cpml_z(P, u, x, y, z, true, PS_VXZ);
-            ut = d_line<H, true>(hVz, ci, 1, x, P.Dxf);
-            if (P.useCpml) cpml_x(P, ut, x, y, z, true, PS_VZX);
-            u += ut;
-            u *= muXZ;
-            float sxz = cen[7 * TT + tid] + u;
-            u = d_line<H, true>(hVy, ci, BW, z, P.Dzf);
-            if (P.useCpml) cpml_z(P, u, x, y, z, true, PS_VYZ);
-            ut = d_queue<H, true>(qz, y, P.Dyf);
-            if (P.useCpml) cpml_y(P, ut, x, y, z, true, PS_VZY);
-            u += ut;
-            u *= muYZ;
-            float syz = cen[8 * TT + tid] + u;
-            if (P.fs && y == 0) {
-                float sv = M - 2.0f * mu;
-                float sh = sv * sv;
-                sh /= M;
-                sh *= -1.0f;
-                syy = 0.0f;
-                float t = sh * (vxx + vzz);
-                sxx += t; szz += t;
-                t = sv * vyy;
-                sxx -= t; szz -= t;
-            }
-            if (P.abs) {
-                const float d = abs_damp(P, x, y, z);
-                sxx *= d; syy *= d; szz *= d; sxy *= d; sxz *= d; syz *= d;
-            }
-            P.f[F_SXX][i] = sxx;
-            P.f[F_SYY][i] = syy;
-            P.f[F_SZZ][i] = szz;
-            P.f[F_SXY][i] = sxy;
-            P.f[F_SXZ][i] = sxz;
-            P.f[F_SYZ][i] = syz;
+            auto finish = [&](float sxx, float syy, float szz, float sxy, float sxz, float syz, float vxx, float vyy, float vzz) {
+                if (P.fs && y == 0) {
+                    float sv = M - 2.0f * mu;
+                    float sh = sv * sv;
+                    sh /= M;
+                    sh *= -1.0f;
+                    syy = 0.0f;
+                    float t = sh * (vxx + vzz);
+                    sxx += t; szz += t;
+                    t = sv * vyy;
+                    sxx -= t; szz -= t;
+                }
+                float d = 1.0f;
+                if (P.abs) d = abs_damp(P, C.x, y, C.z);
+                P.f[F_SXX][i] = sxx * d;
+                P.f[F_SYY][i] = syy * d;
+                P.f[F_SZZ][i] = szz * d;
+                P.f[F_SXY][i] = sxy * d;
+                P.f[F_SXZ][i] = sxz * d;
+                P.f[F_SYZ][i] = syz * d;
+            };
+            auto body = [&](auto interior) {
+                constexpr bool INT = decltype(interior)::value;
+                // the nine velocity derivatives first (independent FMA chains), then CPML
+                float vxx = dline<H, false, INT>(hVx, ci, 1, C.xi, C.rxb, scale);
+                float vyx = dline<H, true, INT>(hVy, ci, 1, C.xi, C.rxf, scale);
+                float vzx = dline<H, true, INT>(hVz, ci, 1, C.xi, C.rxf, scale);
+                float vyy = dqueue<H, false, INT>(qy, Y.yi, ryb, scale);
+                float vxy = dqueue<H, true, INT>(qx, Y.yi, ryf, scale);
+                float vzy = dqueue<H, true, INT>(qz, Y.yi, ryf, scale);
+                float vzz = dline<H, false, INT>(hVz, ci, BW, C.zi, C.rzb, scale);
+                float vxz = dline<H, true, INT>(hVx, ci, BW, C.zi, C.rzf, scale);
+                float vyz = dline<H, true, INT>(hVy, ci, BW, C.zi, C.rzf, scale);
+                if (C.sx >= 0) {
+                    cpml_s(vxx, ps[0 * TT], psi_x(P, PS_VXX, C, y), C.axf, C.bxf);
+                    cpml_s(vyx, ps[1 * TT], psi_x(P, PS_VYX, C, y), C.axh, C.bxh);
+                    cpml_s(vzx, ps[2 * TT], psi_x(P, PS_VZX, C, y), C.axh, C.bxh);
+                }
+                if (Y.sy >= 0) {
+                    cpml_s(vyy, ps[3 * TT], psi_y(P, PS_VYY, C, Y), Y.ayf, Y.byf);
+                    cpml_s(vxy, ps[4 * TT], psi_y(P, PS_VXY, C, Y), Y.ayh, Y.byh);
+                    cpml_s(vzy, ps[5 * TT], psi_y(P, PS_VZY, C, Y), Y.ayh, Y.byh);
+                }
+                if (C.sz >= 0) {
+                    cpml_s(vzz, ps[6 * TT], psi_z(P, PS_VZZ, C, y), C.azf, C.bzf);
+                    cpml_s(vxz, ps[7 * TT], psi_z(P, PS_VXZ, C, y), C.azh, C.bzh);
+                    cpml_s(vyz, ps[8 * TT], psi_z(P, PS_VYZ, C, y), C.azh, C.bzh);
+                }
+                float sxx = cen[3 * TT + tid], syy = cen[4 * TT + tid], szz = cen[5 * TT + tid];
+                float u = vxx;
+                u += vyy;
+                u += vzz;
+                u *= M;
+                sxx += u; syy += u; szz += u;
+                u = vyy + vzz; u *= mu; sxx -= 2.0f * u;
+                u = vxx + vzz; u *= mu; syy -= 2.0f * u;
+                u = vxx + vyy; u *= mu; szz -= 2.0f * u;
+                // shear
+                u = vxy;
+                u += vyx;
+                u *= muXY;
+                const float sxy = cen[6 * TT + tid] + u;
+                u = vxz;
+                u += vzx;
+                u *= muXZ;
+                const float sxz = cen[7 * TT + tid] + u;
+                u = vyz;
+                u += vzy;
+                u *= muYZ;
+                const float syz = cen[8 * TT + tid] + u;
+                finish(sxx, syy, szz, sxy, sxz, syz, vxx, vyy, vzz);
+            };
+            if (C.wint && Y.yi) body(std::true_type{});
+            else body(std::false_type{});
         }
-        // carry mu of plane c+1 into the next iteration
-        m00 = n00; m10 = n10; m01 = n01;
-        m11 = mb[(tz + 1) * PW + tx + 1];
-        __syncthreads();
-        if (tid == 0 && it + NSTAGE < total) {
-            fence_proxy_async();
-            str_issue<H>(T, P, S, smem, bars, it + NSTAGE, g0, g1);
-        }
+        // carry mu of plane y+1 into the next iteration
+        m00 = n00;
+        i00 = j00; i10 = j10; i01 = j01; i11 = j11;
+        release(empty + s);
+        // thread 0 refills the stage released one iteration earlier
+        if (threadIdx.x == 0) refill<NST>(F, G, it - 1, total, full, empty, &failed, S.err, issue);
+        if (failed) return;
+        cur.advance(G);
     }
 }
 
@@ -589,6 +874,20 @@ EncodeFn encoder()
     return fn;
 }
 
+// 3-D fp32 map over a (d0 fastest, d1, d2) array with box (bx, bz, 1)
+bool make_map_dims(CUtensorMap* m, const float* base, int d0, int d1, int d2, int bx, int bz)
+{
+    EncodeFn enc = encoder();
+    if (!enc || d0 < 1 || d1 < 1 || d2 < 1) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+    cuuint64_t strides[2] = {(cuuint64_t)d0 * 4, (cuuint64_t)d0 * d1 * 4};
+    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)bz, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 bool make_map(CUtensorMap* m, const float* base, int NX, int NZ, int NY, int bx, int bz)
 {
     EncodeFn enc = encoder();
@@ -603,30 +902,36 @@ bool make_map(CUtensorMap* m, const float* base, int NX, int NZ, int NY, int bx,
 }
 
 template <int H>
-size_t vel_smem() { return NSTAGE * vel_stage(H) + NSTAGE * sizeof(uint64_t); }
+size_t vel_smem() { return VelStage<H>::NST * (VelStage<H>::BYTES + 2 * sizeof(uint64_t)); }
 template <int H>
-size_t str_smem() { return NSTAGE * str_stage(H) + NSTAGE * sizeof(uint64_t); }
-
-} // namespace
+size_t str_smem() { return StrStage<H>::NST * (StrStage<H>::BYTES + 2 * sizeof(uint64_t)); }
 
 template <int H>
-static cudaError_t configure_h()
+cudaError_t configure_h()
 {
     cudaError_t e = cudaFuncSetAttribute(el3d_vel<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vel_smem<H>());
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(el3d_str<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)str_smem<H>());
+    e = cudaFuncSetAttribute(el3d_str<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)str_smem<H>());
+    if (e != cudaSuccess) return e;
+    // one CTA (NTHR threads at up to 120 registers, the stage ring) must fit an SM
+    int nv = 0, ns = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nv, el3d_vel<H>, NTHR, vel_smem<H>());
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ns, el3d_str<H>, NTHR, str_smem<H>());
+    if (e != cudaSuccess) return e;
+    return nv >= 1 && ns >= 1 ? cudaSuccess : cudaErrorInvalidConfiguration;
 }
 
 template <int H>
-static cudaError_t launch_h(const El3dPlan& plan, const StepParams& P, int pass, cudaStream_t s)
+cudaError_t launch_h(const El3dPlan& plan, const StepParams& P, int pass, cudaStream_t s)
 {
-    const dim3 block(TX, TZ, 1);
+    const dim3 block(NTHR, 1, 1);
     if (pass == 0) el3d_vel<H><<<plan.grid, block, vel_smem<H>(), s>>>(plan.maps, P, plan.sched);
     else el3d_str<H><<<plan.grid, block, str_smem<H>(), s>>>(plan.maps, P, plan.sched);
     return cudaGetLastError();
 }
 
-static cudaError_t configure(int H)
+cudaError_t configure(int H)
 {
     switch (H) {
     case 1: return configure_h<1>();
@@ -639,6 +944,30 @@ static cudaError_t configure(int H)
     }
 }
 
+} // namespace
+
+// A tile's x (or z) range may meet at most one CPML slab of that axis, and
+// the compact slab layout must keep TMA's 16-byte rules (slab length and
+// slab offset multiples of 4 floats along x).
+static bool slab_tiles_ok(const Cpml1D& p, int T, bool xAxis)
+{
+    if (!p.on || p.n <= 2 * p.w) return true;
+    if (xAxis && ((p.ns % 4) != 0 || ((p.n - p.ns) % 4) != 0)) return false;
+    for (int c0 = 0; c0 < p.n; c0 += T)
+        if (p.lo && c0 < p.w && c0 + T > p.n - p.w) return false;
+    return true;
+}
+
+static bool make_psi_map(CUtensorMap* m, const float* base, int axis, const StepParams& P)
+{
+    if (!base) return false;
+    switch (axis) {
+    case 0: return make_map_dims(m, base, P.cx.ns, P.NZ, P.NY, TX, TZ);
+    case 1: return make_map_dims(m, base, P.NX, P.NZ, P.cy.ns, TX, TZ);
+    default: return make_map_dims(m, base, P.NX, P.cz.ns, P.NY, TX, TZ);
+    }
+}
+
 // Builds the tensor maps for the current field/material pointers. Returns
 // false when the streaming path does not apply (then the generic kernels run).
 bool el3d_prepare(El3dPlan& plan, const StepParams& P, const float* rho, const float* M, const float* mu, int H, int* errWord)
@@ -646,6 +975,7 @@ bool el3d_prepare(El3dPlan& plan, const StepParams& P, const float* rho, const f
     plan.ready = false;
     if (!P.is3d || H < 1 || H > 6 || (P.NX % 4) != 0 || P.NX < 8 || P.NZ < 2) return false;
     if (!rho || !M || !mu) return false;
+    if (P.useCpml && (!slab_tiles_ok(P.cx, TX, true) || !slab_tiles_ok(P.cz, TZ, false))) return false;
     const int bx = bw_of(H), bz = bh_of(H);
     El3dMaps& T = plan.maps;
     bool ok = true;
@@ -669,6 +999,18 @@ bool el3d_prepare(El3dPlan& plan, const StepParams& P, const float* rho, const f
     ok &= make_map(&T.cM, M, P.NX, P.NZ, P.NY, TX, TZ);
     ok &= make_map(&T.pRho, rho, P.NX, P.NZ, P.NY, PW, PH);
     ok &= make_map(&T.pMu, mu, P.NX, P.NZ, P.NY, PW, PH);
+    if (P.useCpml) {
+        // order of the boxes in a stage: x-type, y-type, z-type (three each)
+        const int vel[9] = {PS_SXX_X, PS_SXY_X, PS_SXZ_X, PS_SXY_Y, PS_SYY_Y, PS_SYZ_Y, PS_SXZ_Z, PS_SYZ_Z, PS_SZZ_Z};
+        const int str[9] = {PS_VXX, PS_VYX, PS_VZX, PS_VYY, PS_VXY, PS_VZY, PS_VZZ, PS_VXZ, PS_VYZ};
+        for (int j = 0; j < 9; ++j) {
+            const int axis = j / 3 == 0 ? 0 : (j / 3 == 1 ? 1 : 2);
+            const Cpml1D& ax = axis == 0 ? P.cx : (axis == 1 ? P.cy : P.cz);
+            if (!ax.on) continue;
+            ok &= make_psi_map(&T.psV[j], P.psi[vel[j]], axis, P);
+            ok &= make_psi_map(&T.psS[j], P.psi[str[j]], axis, P);
+        }
+    }
     if (!ok) return false;
     plan.sched.ntx = (P.NX + TX - 1) / TX;
     plan.sched.ntz = (P.NZ + TZ - 1) / TZ;
@@ -677,8 +1019,13 @@ bool el3d_prepare(El3dPlan& plan, const StepParams& P, const float* rho, const f
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long work = (long long)plan.sched.ntx * plan.sched.ntz * P.NY;
-    plan.grid = static_cast<int>(work < sms ? work : sms);
+    const long long tiles = (long long)plan.sched.ntx * plan.sched.ntz;
+    const long long work = tiles * P.NY;
+    long long grid = sms;                 // one persistent CTA per SM
+    if (grid > work) grid = work;
+    // each CTA's plane range must fit the segment table
+    if (tiles / grid + 2 > MAXSEG) return false;
+    plan.grid = static_cast<int>(grid);
     if (configure(H) != cudaSuccess) return false;
     plan.ready = plan.grid > 0;
     return plan.ready;

@@ -173,11 +173,16 @@ bool type_ok(int eq, bool is3d, int type, bool source)
     }
 }
 
-bool streaming(const wave_handle* h) { return h->kernelPath == 0 && h->el3d.ready; }
+// whether a pass runs the streaming TMA kernels
+bool streaming_pass(const wave_handle* h, int pass)
+{
+    if (!h->el3d.ready || h->kernelPath == 1) return false;
+    return h->kernelPath == 2 || h->passStreaming[pass] != 0;
+}
 
 void launch_pass(wave_handle* h, int pass)
 {
-    if (streaming(h)) {
+    if (streaming_pass(h, pass)) {
         h->check(el3d_launch(h->el3d, h->sp, pass, h->stream), "streaming kernel launch");
     } else {
         StepKernel k = kernel_for(h->cfg.equation, pass, h->H);
@@ -219,6 +224,45 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
     }
     launch_srcrec(h->sq, h->tcounter, h->stream);
     h->launches += 1;
+}
+
+// Automatic kernel choice: times each pass with the generic and the streaming
+// kernels on the current state and keeps the faster one per pass. Runs only
+// on a state that has not been stepped, which every pass leaves at zero (all
+// updates are linear in the wavefields and there is no source term in them).
+void tune_passes(wave_handle* h)
+{
+    h->passStreaming[0] = h->passStreaming[1] = 1;
+    if (!h->el3d.ready || h->stepsSinceReset != 0) return;
+    cudaEvent_t e0, e1;
+    h->check(cudaEventCreate(&e0), "event");
+    h->check(cudaEventCreate(&e1), "event");
+    float best[2][2] = {{0, 0}, {0, 0}};
+    for (int pass = 0; pass < 2; ++pass)
+        for (int path = 0; path < 2; ++path) {
+            auto launch = [&] {
+                if (path) h->check(el3d_launch(h->el3d, h->sp, pass, h->stream), "streaming kernel launch");
+                else kernel_for(h->cfg.equation, pass, h->H)<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+            };
+            for (int k = 0; k < 2; ++k) launch();
+            h->check(cudaEventRecord(e0, h->stream), "event");
+            for (int k = 0; k < 5; ++k) launch();
+            h->check(cudaEventRecord(e1, h->stream), "event");
+            h->check(cudaEventSynchronize(e1), "tuning");
+            h->check(cudaEventElapsedTime(&best[pass][path], e0, e1), "event");
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->check(cudaGetLastError(), "tuning launch");
+    for (int pass = 0; pass < 2; ++pass) h->passStreaming[pass] = best[pass][1] <= best[pass][0] ? 1 : 0;
+    // the state was zero and stays zero; clear it anyway so tuning leaves no trace
+    for (int f : h->fields) h->check(cudaMemsetAsync(h->f[f], 0, h->N * sizeof(float), h->stream), "memset");
+    for (int rr = 0; rr < R_COUNT; ++rr)
+        for (int l = 0; l < kMaxL; ++l)
+            if (h->r[rr][l]) h->check(cudaMemsetAsync(h->r[rr][l], 0, h->N * sizeof(float), h->stream), "memset");
+    for (int s2 = 0; s2 < PS_COUNT; ++s2)
+        if (h->psi[s2]) h->check(cudaMemsetAsync(h->psi[s2], 0, h->psiLen[s2] * sizeof(float), h->stream), "memset");
+    h->check(cudaStreamSynchronize(h->stream), "tuning");
 }
 
 void build_graph(wave_handle* h)
@@ -343,6 +387,7 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
         StepParams& P = h->sp;
         P = StepParams{};
         P.NX = h->NX; P.NY = h->NY; P.NZ = h->NZ; P.is3d = is3d; P.N = h->N;
+        P.scale = DT / DH;
         P.Dxf = to_device(h.get(), build_op(h->NX, q, OP_F, stencil, reduce, DH, DT), 0);
         P.Dxb = to_device(h.get(), build_op(h->NX, q, OP_B, stencil, reduce, DH, DT), 1);
         P.Dyf = to_device(h.get(), build_op(h->NY, q, OP_F, stencil, reduce, DH, DT), 2);
@@ -507,8 +552,10 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         h->check(cudaGetLastError(), "model preparation");
         for (float* p : tmp) cudaFreeAsync(p, s);
         h->check(cudaStreamSynchronize(s), "model preparation");
-        if (eq == WAVE_EQ_ELASTIC && is3d)
+        if (eq == WAVE_EQ_ELASTIC && is3d) {
             el3d_prepare(h->el3d, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord);
+            tune_passes(h);
+        }
         h->modelSet = true;
         h->graphDirty = true;
     })
@@ -659,6 +706,7 @@ int wave_solver_step(wave_handle* h, int t_begin, int t_end)
             for (; t < t_end; ++t) launch_step(h);
             h->check(cudaGetLastError(), "step launch");
         }
+        h->stepsSinceReset += t_end - t_begin;
     })
     return WAVE_OK;
 }
@@ -675,6 +723,7 @@ int wave_solver_reset(wave_handle* h)
             if (h->psi[s]) h->check(cudaMemsetAsync(h->psi[s], 0, h->psiLen[s] * sizeof(float), h->stream), "memset");
         if (h->seis) h->check(cudaMemsetAsync(h->seis, 0, static_cast<size_t>(h->nrec > 0 ? h->nrec : 1) * h->NT * sizeof(float), h->stream), "memset");
         h->check(cudaStreamSynchronize(h->stream), "reset");
+        h->stepsSinceReset = 0;
     })
     return WAVE_OK;
 }
@@ -740,6 +789,7 @@ int wave_get_state(wave_handle* h, void* out, size_t bytes, int mem)
             o += p.second;
         }
         h->check(cudaStreamSynchronize(h->stream), "state copy");
+        h->stepsSinceReset = 1;   // a restored state is not the zero state
     })
     return WAVE_OK;
 }
@@ -757,6 +807,7 @@ int wave_set_state(wave_handle* h, const void* in, size_t bytes, int mem)
             o += p.second;
         }
         h->check(cudaStreamSynchronize(h->stream), "state copy");
+        h->stepsSinceReset = 1;   // a restored state is not the zero state
     })
     return WAVE_OK;
 }
@@ -792,7 +843,7 @@ int wave_get_launch_count(wave_handle* h, long long* count)
 int wave_set_kernel_path(wave_handle* h, int path)
 {
     if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_kernel_path: null handle");
-    if (path != 0 && path != 1) return fail(h, WAVE_ERR_ARG, "wave_set_kernel_path: path must be 0 or 1");
+    if (path < 0 || path > 2) return fail(h, WAVE_ERR_ARG, "wave_set_kernel_path: path must be 0, 1 or 2");
     h->kernelPath = path;
     h->graphDirty = true;
     return WAVE_OK;
@@ -801,7 +852,7 @@ int wave_set_kernel_path(wave_handle* h, int path)
 int wave_get_kernel_path(wave_handle* h, int* streamingActive)
 {
     if (!h || !streamingActive) return fail(h, WAVE_ERR_ARG, "wave_get_kernel_path: null argument");
-    *streamingActive = streaming(h) ? 1 : 0;
+    *streamingActive = (streaming_pass(h, 0) ? 1 : 0) | (streaming_pass(h, 1) ? 2 : 0);
     return WAVE_OK;
 }
 

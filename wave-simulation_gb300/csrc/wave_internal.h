@@ -86,6 +86,7 @@ struct StepParams {
     int absW;
     const float* absCoeff;  // BoundaryWidth entries
     int L;
+    float scale;            // DT/DH: interior FD taps use compile-time coefficients times this
     float DThalf;
     float invRelax[kMaxL], c1[kMaxL], c2[kMaxL], Cc[kMaxL], relaxTime[kMaxL];
 };
