@@ -189,6 +189,27 @@ int wave_get_kernel_times(wave_handle* h, double* velocity_ms, double* stress_ms
  * host or both on the current CUDA device (mem). Synchronous; no handle. */
 int wave_average_shear_modulus(const float* mu, float* out, int64_t NX, int64_t NY, int64_t NZ, int mode, int mem);
 
+/* The same average without any device allocation. No counterpart in the
+ * reference (its LAMA matrices own their storage).
+ * For callers that must not allocate device memory: an FWI loop that updates
+ * the model between iterations while the wavefields, checkpoints and
+ * gradients fill the device (a cudaMalloc there can fail), and code that
+ * cannot accept the device-wide synchronisation cudaMalloc/cudaFree imply.
+ * mu and out are device pointers on the current device (out may equal mu);
+ * the work is queued on `stream` (a cudaStream_t, NULL = legacy default
+ * stream) and the call returns without waiting.
+ * Limit: NX*NY*NZ <= 4194304 (2^22) points; the inverse moduli go to a fixed
+ * 16 MiB scratch array in device global memory. Larger models return
+ * WAVE_ERR_ARG: use wave_average_shear_modulus.
+ * The first call on each device does a one-time set-up (it looks up the
+ * scratch array's address with that device current); make that first call
+ * before any stream capture. Nothing has to start at zero: every scratch
+ * value that is read was written earlier in the same call. The scratch is
+ * shared by all calls on a device, so calls that overlap in time (other
+ * streams, other host threads) race on it and must be serialised by the
+ * caller. */
+int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, int64_t NY, int64_t NZ, int mode, void* stream);
+
 /* Kernel path: 0 = automatic, 1 = generic kernels only, 2 = the streaming
  * TMA kernels wherever they apply (3-D elastic grids with NX % 4 == 0 whose
  * 32x16 column tiles meet at most one CPML slab per axis). The automatic path

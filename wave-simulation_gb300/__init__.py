@@ -40,7 +40,7 @@ ABI_SYMBOLS = (
     "wave_get_kernel_times", "wave_last_error", "wave_wavelet", "wave_set_kernel_path",
     "wave_get_kernel_path", "wave_average_shear_modulus", "wave_batch_create", "wave_batch_destroy",
     "wave_batch_shot", "wave_batch_step", "wave_batch_get_stream", "wave_batch_get_launch_count",
-    "wave_batch_last_error",
+    "wave_batch_last_error", "wave_average_shear_modulus_noalloc",
 )
 
 
@@ -158,6 +158,7 @@ def lib():
     L.wave_set_kernel_path.argtypes = [P, I]
     L.wave_get_kernel_path.argtypes = [P, CP(I)]
     L.wave_average_shear_modulus.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, I]
+    L.wave_average_shear_modulus_noalloc.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, P]
     L.wave_batch_create.argtypes = [P, I, CP(P)]
     L.wave_batch_destroy.argtypes = [P]
     L.wave_batch_shot.argtypes = [P, I, CP(P)]
@@ -206,6 +207,17 @@ def average_shear_modulus(mu, dims, mode: int, out=None):
         out = np.zeros(int(np.prod(dims)), dtype=np.float32) if not hasattr(mu, "data_ptr") else mu.new_zeros(mu.shape)
     (pm, mem), (po, _) = _ptr(mu), _ptr(out)
     _check(None, lib().wave_average_shear_modulus(pm, po, dims[0], dims[1], dims[2], mode, mem))
+    return out
+
+
+def average_shear_modulus_noalloc(mu, out, dims, mode: int, stream: int = 0):
+    """wave_average_shear_modulus_noalloc: the same average with no device
+    allocation (fixed 2^22-point scratch). mu and out are torch cuda float32
+    tensors; the work is queued on `stream` (a raw cudaStream_t, 0 = default)."""
+    if not (hasattr(mu, "data_ptr") and hasattr(out, "data_ptr")):
+        raise WaveError(WAVE_ERR_ARG, "mu and out must be device tensors")
+    _check(None, lib().wave_average_shear_modulus_noalloc(ctypes.c_void_p(mu.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                                          dims[0], dims[1], dims[2], mode, ctypes.c_void_p(stream or None)))
     return out
 
 

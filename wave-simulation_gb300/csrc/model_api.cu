@@ -1,6 +1,8 @@
 // model_api.cu — model-preparation helpers exposed without a solver handle
 // (the device side of Modelparameter::prepareForModelling, usable by FWI
 // model updates between iterations).
+#include <climits>
+#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -45,6 +47,86 @@ extern "C" int wave_average_shear_modulus(const float* mu, float* out, int64_t N
     cleanup();
     if (e != cudaSuccess) {
         set_global_error(std::string("wave_average_shear_modulus: ") + cudaGetErrorString(e));
+        return WAVE_ERR_CUDA;
+    }
+    return WAVE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of wave_average_shear_modulus.
+//
+// The inverse moduli that the harmonic average reads go to a fixed scratch
+// array in device global memory instead of a cudaMalloc'd buffer, so the call
+// allocates nothing. The scratch holds kNoAllocMaxPoints floats (16 MiB), which
+// bounds the model size this entry point accepts.
+constexpr long long kNoAllocMaxPoints = 1LL << 22;
+static __device__ __align__(256) float g_invmu_scratch[kNoAllocMaxPoints];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+float* g_scratch_ptr[kMaxDevices] = {};
+
+// One-time set-up per device (with that device current): the scratch array's
+// device address.
+cudaError_t scratch_for_current_device(float** ptr)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_invmu_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[dev] = static_cast<float*>(p);
+    }
+    *ptr = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+
+bool on_device(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();   // the query's error for an unknown pointer is not sticky: clear it
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+} // namespace
+
+extern "C" int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, int64_t NY, int64_t NZ, int mode,
+                                                  void* stream)
+{
+    if (!mu || !out || NX < 1 || NY < 1 || NZ < 1 || mode < 0 || mode > 4 || NX > INT_MAX || NY > INT_MAX || NZ > INT_MAX) {
+        set_global_error("wave_average_shear_modulus_noalloc: invalid argument");
+        return WAVE_ERR_ARG;
+    }
+    const long long n = NX * NY * NZ;
+    if (n > kNoAllocMaxPoints) {
+        set_global_error("wave_average_shear_modulus_noalloc: NX*NY*NZ = " + std::to_string(n) + " exceeds the fixed scratch of " +
+                         std::to_string(kNoAllocMaxPoints) + " points; use wave_average_shear_modulus");
+        return WAVE_ERR_ARG;
+    }
+    if (!on_device(mu) || !on_device(out)) {
+        set_global_error("wave_average_shear_modulus_noalloc: mu and out must be device memory of the current device");
+        return WAVE_ERR_ARG;
+    }
+    float* inv = nullptr;
+    cudaError_t e = scratch_for_current_device(&inv);
+    if (e == cudaSuccess) {
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        PrepParams G{static_cast<int>(NX), static_cast<int>(NY), static_cast<int>(NZ), n};
+        k_inv_clamped(G, mu, inv, s);     // writes all n scratch values ...
+        k_harmonic(G, inv, mode, out, s); // ... before any is read
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        set_global_error(std::string("wave_average_shear_modulus_noalloc: ") + cudaGetErrorString(e));
         return WAVE_ERR_CUDA;
     }
     return WAVE_OK;
