@@ -337,6 +337,371 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# The other measured workloads (--workload): 2-D acoustic whole job, 3-D
+# visco-elastic, 128-shot batched 2-D TMz EM. Each prints one JSON line of the
+# same shape as the default 3-D elastic line.
+# ---------------------------------------------------------------------------
+EPS0, MU0 = 8.8541878176e-12, 1.2566370614e-6      # the reference's vacuum constants
+
+
+def _clocked(fn, stream):
+    """Runs fn() between two CUDA events on `stream` with nvidia-smi sampling; returns (ms, clocks)."""
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1), clk.summary()
+
+
+def _timed(fn, stream):
+    """fn() between two CUDA events on `stream`; returns ms."""
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    fn()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def _line(metric, value, steps, warmup, ms_step, config, roof, e2e, launches, clocks, cpu, extra=None):
+    line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded, shapes of the workload)", "config": config, "roofline": roof, "e2e": e2e,
+            "gpu_launches": launches}
+    if clocks:
+        line["clocks"] = clocks
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if extra:
+        line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def _roof(alg_bytes_step, ms_step, kernel, note=None):
+    peak, kind = load_peaks()
+    ach = alg_bytes_step / (ms_step * 1e-3) / 1e9
+    r = {"bound": "hbm", "kernel": kernel, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+         "peak_kind": f"{kind} copy bandwidth (burst)", "traffic": None, "alg_bytes_per_step": alg_bytes_step}
+    if note:
+        r["note"] = note
+    return r
+
+
+def _oracle_rate(cfg_kw, model, acq, steps, budget_s=20.0):
+    """Gpt/s of the CPU oracle (fp32, all host threads) over at most `steps` steps / `budget_s` s."""
+    from oracle import refcpu
+    cores = os.cpu_count() or 1
+    refcpu.set_threads(cores)
+    cfg = refcpu.make_config(**cfg_kw)
+    n = cfg.NX * cfg.NY * (cfg.NZ if cfg.dimension == 3 else 1)
+    sidx, stype, sig, ridx, rtype = acq
+    o = refcpu.Oracle(cfg, model, sidx, stype, sig, ridx, rtype, dtype=np.float32)
+    o.step(0, 1, copy_state=True)
+    sec, done = 0.0, 0
+    while done < steps and sec < budget_s:
+        sec += o.step(1 + done, 2 + done, copy_state=True)
+        done += 1
+    o.close()
+    return n * done / sec / 1e9, cores, done, sec
+
+
+# ---- config 1: 2-D acoustic 400 x 200 -------------------------------------
+AC2_KW = dict(dimension=2, equation="acoustic", NX=400, NY=200, NZ=1, DH=1.0, DT=2e-4, T=0.4, spatialFDorder=4,
+              FreeSurface=0, DampingBoundary=2, BoundaryWidth=20, NPower=4.0, CenterFrequencyCPML=15.0,
+              VMaxCPML=2500.0, useStencilMatrix=0, edgeOrderReduction=1)
+
+
+def ac2_model():
+    y = np.arange(200)[:, None] * np.ones((1, 400))
+    vp = np.where(y < 100, 1500.0, 2500.0).astype(np.float32).reshape(-1)
+    rho = np.where(y < 100, 1000.0, 2000.0).astype(np.float32).reshape(-1)
+    return dict(rho=rho, vp=vp)
+
+
+def ac2_acq(nt, dt):
+    from oracle.refcpu import ricker
+    sidx = np.array([200 + 400 * 20], np.int64)
+    sig = ricker(nt, dt, 15.0, 1.0, 0.0, np.float32)[None, :]
+    ridx = (2 + 4 * np.arange(100) + 400 * 10).astype(np.int64)
+    return sidx, np.array([1], np.int32), sig, ridx, np.ones(100, np.int32)
+
+
+def run_acoustic2d(args, wave):
+    import torch
+    n = 400 * 200
+    psi_pts = 2 * 20 * 200 + 2 * 20 * 400
+    alg = 4 * (2 * 3 + 2) * n + 2 * 8 * psi_pts            # 32 B/pt + psi
+    vals = {}
+    for stencil in (0, 1):
+        cfg = wave.WaveConfig.make(**dict(AC2_KW, useStencilMatrix=stencil))
+        s = wave.Factory.Create("2D", "acoustic").initForwardSolver(cfg)
+        acq = ac2_acq(s.nt, cfg.DT)
+        s.prepareForModelling({k: torch.from_numpy(v).cuda() for k, v in ac2_model().items()})
+        s.setSources(*acq[:3])
+        s.setReceivers(*acq[3:])
+        s.run(0, s.nt)                                        # warm-up job (graph capture)
+        s.resetCPML()
+        l0 = s.launch_count()
+        ms, clocks = _clocked(lambda: s.run(0, s.nt), torch.cuda.ExternalStream(s.stream()))
+        launches = s.launch_count() - l0
+        nt = s.nt
+        s.close()
+        vals[stencil] = (n * nt / (ms * 1e-3) / 1e9, ms / nt, launches, clocks)
+    value, ms_step, launches, clocks = vals[0]
+    # end to end with host buffers: create, model, acquisition, whole job, seismograms
+    t0 = time.perf_counter()
+    cfg = wave.WaveConfig.make(**AC2_KW)
+    s = wave.Factory.Create("2D", "acoustic").initForwardSolver(cfg)
+    acq = ac2_acq(s.nt, cfg.DT)
+    m = ac2_model()
+    s.prepareForModelling(m)
+    s.setSources(*acq[:3])
+    s.setReceivers(*acq[3:])
+    s.run(0, s.nt)
+    seis = s.seismograms()
+    nt = s.nt
+    s.close()
+    e2e_s = time.perf_counter() - t0
+    h2d = sum(v.nbytes for v in m.values()) + sum(a.nbytes for a in acq)
+    e2e = {"value": n * nt / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d / nt, "d2h_bytes_per_step": seis.nbytes / nt}
+    cpu = None
+    if not args.no_cpu:
+        g, cores, done, sec = _oracle_rate(AC2_KW, {k: v.astype(np.float64) for k, v in ac2_model().items()}, acq, nt, 20.0)
+        cpu = {"value": g, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{done} steps of the 400x200 job with the CPU oracle (FP32), {sec:.1f} s"}
+    cfgd = {"workload": "2-D acoustic 400x200, order 4, 20-pt CPML, NT=2000, whole job graph-captured",
+            "grid": [400, 200], "order": 4, "l2": "L2-resident (state 0.96 MB): launch/latency bound",
+            "stencil_mode_value": vals[1][0], "parallelism": "1 GPU"}
+    _line(UNIT, value, nt, nt, ms_step, cfgd, _roof(alg, ms_step, "acoustic_v<2> + acoustic_p<2>",
+          "whole state in L2: the HBM roofline is not the bound here"), e2e, launches, clocks, cpu)
+
+
+# ---- config 3: 3-D visco-elastic 512 x 256 (depth) x 512 -------------------
+def _tau_method(q, f0, freqs):
+    w0 = 2 * np.pi * f0
+    ts = [1.0 / (2 * np.pi * f) for f in freqs]
+    return (1.0 / q) / sum(w0 * t / (1 + w0 * w0 * t * t) for t in ts)
+
+
+VI3_FREQ = [10.0 / 3.0, 30.0]
+VI3_KW = dict(dimension=3, equation="viscoelastic", NX=512, NY=256, NZ=512, DH=5.0, DT=5e-4, T=2.0, spatialFDorder=4,
+              FreeSurface=0, DampingBoundary=2, BoundaryWidth=20, NPower=4.0, CenterFrequencyCPML=10.0, VMaxCPML=3600.0,
+              numRelaxationMechanisms=2, relaxationFrequency=VI3_FREQ, useStencilMatrix=0, edgeOrderReduction=1)
+
+
+def vi3_model(NX, NY, NZ, device):
+    """vp 3000, vs 1700, rho 2200 times (1 + 0.05 n); n = white noise (seed 20260003)
+    smoothed by a Gaussian of sigma = 10 cells (reflecting edges, separable, on
+    the GPU), rescaled to unit std and clipped to +-3; tau from the tau-method
+    at 10 Hz with Qp = 80, Qs = 50."""
+    import torch
+    g = np.random.default_rng(20260003).standard_normal((NY, NZ, NX), dtype=np.float32)
+    t = torch.from_numpy(g).to(device)
+    for dim in range(3):
+        x = t.movedim(dim, -1)
+        shp = x.shape
+        r = min(40, shp[-1] - 1)                     # 4 sigma, or less on short axes
+        k = torch.arange(-r, r + 1, device=device, dtype=torch.float32)
+        w = torch.exp(-0.5 * (k / 10.0) ** 2)
+        w = (w / w.sum()).view(1, 1, -1)
+        x = x.reshape(-1, 1, shp[-1])
+        x = torch.cat([x[..., 1:r + 1].flip(-1), x, x[..., -r - 1:-1].flip(-1)], dim=-1)   # reflecting edges
+        out = torch.empty((x.shape[0], 1, shp[-1]), device=device, dtype=torch.float32)
+        for c0 in range(0, x.shape[0], 16384):
+            out[c0:c0 + 16384] = torch.nn.functional.conv1d(x[c0:c0 + 16384], w)
+        t = out.reshape(shp).movedim(-1, dim)
+    t = ((t - t.mean()) / t.std()).clamp_(-3, 3)
+    f = (1 + 0.05 * t).reshape(-1).contiguous()
+    tp, ts = _tau_method(80.0, 10.0, VI3_FREQ), _tau_method(50.0, 10.0, VI3_FREQ)
+    return dict(vp=3000.0 * f, vs=1700.0 * f, rho=2200.0 * f, taup=torch.full_like(f, tp), taus=torch.full_like(f, ts))
+
+
+def vi3_acq(NX, NY, NZ, nt, dt):
+    from oracle.refcpu import ricker
+    sidx = np.array([NX // 2 + NX * (NZ // 2 + NZ * min(40, NY - 1))], np.int64)
+    sig = ricker(nt, dt, 10.0, 1.0, 0.0, np.float32)[None, :]
+    xs = (40 + 7 * np.arange(64)) % NX
+    zs = (40 + 7 * np.arange(64)) % NZ
+    X, Z = np.meshgrid(xs, zs, indexing="ij")
+    ridx = (X + NX * (Z + NZ * min(20, NY - 1))).reshape(-1).astype(np.int64)
+    return sidx, np.array([1], np.int32), sig, ridx, np.full(ridx.size, 3, np.int32)
+
+
+def run_visco3d(args, wave):
+    import torch
+    kw = dict(VI3_KW)
+    if args.grid != 256:
+        kw.update(NX=2 * args.grid, NY=args.grid, NZ=2 * args.grid)
+    NXv, NYv, NZv = kw["NX"], kw["NY"], kw["NZ"]
+    n = NXv * NYv * NZv
+    cfg = wave.WaveConfig.make(**kw)
+    s = wave.Factory.Create("3D", "viscoelastic").initForwardSolver(cfg)
+    model = vi3_model(NXv, NYv, NZv, "cuda")
+    acq = vi3_acq(NXv, NYv, NZv, s.nt, cfg.DT)
+    s.prepareForModelling(model)
+    s.setSources(*acq[:3])
+    s.setReceivers(*acq[3:])
+    s.run(0, args.warmup)
+    l0 = s.launch_count()
+    ms, clocks = _clocked(lambda: s.run(args.warmup, args.warmup + args.steps), torch.cuda.ExternalStream(s.stream()))
+    launches = s.launch_count() - l0
+    finite = s.check_finite()
+    s.close()
+    ms_step = ms / args.steps
+    value = n * args.steps / (ms * 1e-3) / 1e9
+    w = 20
+    psi_pts = 2 * w * NYv * NZv + 2 * w * NXv * NYv + 2 * w * NXv * NZv
+    alg = 4 * (2 * (9 + 6 * 2) + 5) * n + 6 * 8 * psi_pts       # 188 B/pt + psi
+    e2e = None
+    if not args.no_e2e:
+        host_model = {k: v.cpu().numpy() for k, v in model.items()}
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = wave.Factory.Create("3D", "viscoelastic").initForwardSolver(cfg)
+        s2.prepareForModelling(host_model)
+        s2.setSources(*acq[:3])
+        s2.setReceivers(*acq[3:])
+        s2.run(0, args.steps)
+        seis = s2.seismograms()
+        s2.close()
+        sec = time.perf_counter() - t0
+        h2d = sum(v.nbytes for v in host_model.values()) + sum(a.nbytes for a in acq)
+        e2e = {"value": n * args.steps / sec / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+               "d2h_bytes_per_step": seis.nbytes / args.steps}
+    del model
+    cpu = None
+    if not args.no_cpu:
+        sk = dict(kw, NX=128, NY=64, NZ=128)
+        smodel = {k: v.cpu().numpy().astype(np.float64) for k, v in vi3_model(128, 64, 128, "cuda").items()}
+        g, cores, done, sec = _oracle_rate(sk, smodel, vi3_acq(128, 64, 128, 4000, kw["DT"]), 10, 20.0)
+        cpu = {"value": g, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{done} steps of the same physics on a 128x64x128 sub-grid with the CPU oracle (FP32), {sec:.1f} s"}
+    cfgd = {"workload": f"3-D visco-elastic {NXv}x{NYv}(depth)x{NZv}, order 4, L=2, 20-pt CPML, DT=5e-4, NT=4000, 4096 receivers",
+            "grid": [NXv, NYv, NZv], "order": 4, "L": 2, "l2": "inputs larger than L2 (state 21 x N x 4 B)",
+            "parallelism": "1 GPU"}
+    _line(UNIT, value, args.steps, args.warmup, ms_step, cfgd, _roof(alg, ms_step, "elastic_v<2> + visco_s<2>"),
+          e2e, launches, clocks, cpu, {"finite": finite})
+
+
+# ---- config 4: 128-shot batched 2-D TMz EM --------------------------------
+C0 = 1.0 / np.sqrt(MU0 * EPS0)
+TM_DT = 0.9 * 0.02 / ((7.0 / 6.0) * np.sqrt(2.0) * C0 / 2.0)
+
+
+def tm_shots(nshots):
+    rng = np.random.default_rng(20260004)
+    shots = []
+    for _ in range(nshots):
+        nx, ny = int(rng.integers(300, 1201)), int(rng.integers(150, 501))
+        K = int(rng.integers(3, 9))
+        depths = np.sort(rng.integers(1, ny, K - 1))
+        er_l = rng.uniform(4.0, 25.0, K)
+        sg_l = 10 ** rng.uniform(-4.0, -2.0, K)
+        layer = np.searchsorted(depths, np.arange(ny), side="right")
+        er = np.repeat(er_l[layer][:, None], nx, axis=1)
+        sg = np.repeat(sg_l[layer][:, None], nx, axis=1)
+        for _r in range(int(rng.integers(0, 4))):
+            x0, y0 = int(rng.integers(0, nx - 10)), int(rng.integers(0, ny - 10))
+            w, h = int(rng.integers(10, max(11, nx // 4))), int(rng.integers(5, max(6, ny // 4)))
+            er[y0:y0 + h, x0:x0 + w] = rng.uniform(4.0, 25.0)
+            sg[y0:y0 + h, x0:x0 + w] = 10 ** rng.uniform(-4.0, -2.0)
+        shots.append((nx, ny, dict(eps_r=er.astype(np.float32).reshape(-1), sigma=sg.astype(np.float32).reshape(-1),
+                                   mu_r=np.ones(nx * ny, np.float32))))
+    return shots
+
+
+def tm_cfg_kw(nx, ny):
+    return dict(dimension=2, equation="tmem", NX=nx, NY=ny, NZ=1, DH=0.02, DT=TM_DT, T=3000 * TM_DT, spatialFDorder=4,
+                FreeSurface=0, DampingBoundary=2, BoundaryWidth=20, NPower=4.0, CenterFrequencyCPML=2e8, VMaxCPML=C0 / 2,
+                useStencilMatrix=0, edgeOrderReduction=1)
+
+
+def tm_acq(nx, nt):
+    from oracle.refcpu import ricker
+    sidx = np.array([30 + nx * 25], np.int64)
+    sig = ricker(nt, TM_DT, 2e8, 1.0, 0.0, np.float32)[None, :]
+    ridx = (40 + 4 * np.arange(60) + nx * 25).astype(np.int64)
+    return sidx, np.array([1], np.int32), sig, ridx, np.ones(60, np.int32)
+
+
+def run_tmem_batch(args, wave):
+    import torch
+    nshots = args.shots
+    shots = tm_shots(nshots)
+    npts = sum(nx * ny for nx, ny, _ in shots)
+    cfgs = [wave.WaveConfig.make(**tm_cfg_kw(nx, ny)) for nx, ny, _ in shots]
+    # batched: all shots in each launch
+    b = wave.Batch(cfgs)
+    for shot, (nx, ny, m) in zip(b.shots, shots):
+        shot.prepareForModelling({k: torch.from_numpy(v).cuda() for k, v in m.items()})
+        acq = tm_acq(nx, shot.nt)
+        shot.setSources(*acq[:3])
+        shot.setReceivers(*acq[3:])
+    b.run(0, args.warmup)
+    l0 = b.launch_count()
+    ms, clocks = _clocked(lambda: b.run(args.warmup, args.warmup + args.steps), torch.cuda.ExternalStream(b.stream()))
+    launches = b.launch_count() - l0
+    b.close()
+    value = npts * args.steps / (ms * 1e-3) / 1e9
+    # plain: the same shots one at a time through single-shot handles
+    plain_ms = 0.0
+    for (nx, ny, m), cfg in zip(shots, cfgs):
+        s = wave.Factory.Create("2D", "tmem").initForwardSolver(cfg)
+        s.prepareForModelling({k: torch.from_numpy(v).cuda() for k, v in m.items()})
+        acq = tm_acq(nx, s.nt)
+        s.setSources(*acq[:3])
+        s.setReceivers(*acq[3:])
+        s.run(0, args.warmup)
+        plain_ms += _timed(lambda: s.run(args.warmup, args.warmup + args.steps), torch.cuda.ExternalStream(s.stream()))
+        s.close()
+    plain = npts * args.steps / (plain_ms * 1e-3) / 1e9
+    psi_b = sum(2 * 8 * 2 * 20 * (nx + ny) for nx, ny, _ in shots)
+    alg = 36 * npts + psi_b
+    e2e = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        b2 = wave.Batch(cfgs)
+        h2d = d2h = 0
+        for shot, (nx, ny, m) in zip(b2.shots, shots):
+            shot.prepareForModelling(m)
+            acq = tm_acq(nx, shot.nt)
+            shot.setSources(*acq[:3])
+            shot.setReceivers(*acq[3:])
+            h2d += sum(v.nbytes for v in m.values()) + sum(a.nbytes for a in acq)
+        b2.run(0, args.steps)
+        for shot in b2.shots:
+            d2h += shot.seismograms().nbytes
+        b2.close()
+        sec = time.perf_counter() - t0
+        e2e = {"value": npts * args.steps / sec / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+               "d2h_bytes_per_step": d2h / args.steps}
+    cpu = None
+    if not args.no_cpu:
+        rates = []
+        done_tot, sec_tot, cores = 0, 0.0, 1
+        for nx, ny, m in shots[:4]:
+            g, cores, done, sec = _oracle_rate(tm_cfg_kw(nx, ny), {k: v.astype(np.float64) for k, v in m.items()},
+                                               tm_acq(nx, 3000), 50, 5.0)
+            rates.append(g)
+            done_tot += done
+            sec_tot += sec
+        cpu = {"value": float(np.mean(rates)), "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"4 of the shots, {done_tot} shot-steps in {sec_tot:.1f} s with the CPU oracle (FP32)"}
+    cfgd = {"workload": f"batched 2-D TMz EM, {nshots} shots, nx U[300,1200], ny U[150,500], order 4, 20-pt CPML, "
+                        f"DT={TM_DT:.3e}, NT=3000, 60 Ez receivers per shot",
+            "shots": nshots, "points_per_step": npts, "l2": "inputs larger than L2 (3 x 31 M x 4 B)", "parallelism": "1 GPU"}
+    _line(UNIT, value, args.steps, args.warmup, ms / args.steps, cfgd,
+          _roof(alg, ms / args.steps, "tm_h_batch<2> + tm_e_batch<2>"), e2e, launches, clocks, cpu,
+          {"plain_value": plain, "batched_over_plain": value / plain})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -347,11 +712,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube edge (profiling captures use a smaller cube)")
+    ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch"])
+    ap.add_argument("--shots", type=int, default=128, help="shots of the batched EM workload")
     args = ap.parse_args()
-    if args.grid != 256:
-        set_grid(args.grid)
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload != "elastic3d":
+        import __graft_entry__ as g
+        wave = g.load_package()
+        {"acoustic2d": run_acoustic2d, "visco3d": run_visco3d, "tmem_batch": run_tmem_batch}[args.workload](args, wave)
+        return
+    if args.grid != 256:
+        set_grid(args.grid)
     if args.impl == "reference":
         run_reference(args)
     else:
