@@ -26,6 +26,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../include/wave.h"
@@ -425,6 +426,8 @@ class Sim {
     T DThalf = 0;
     // EM
     std::vector<T> CaZ, CbZ, CaX, CbX, CaY, CbY, invMuXZ, invMuYZ, invMuXY;
+    std::vector<T> emCc;                              // visco EM: C_c per mechanism
+    std::vector<std::vector<T>> CdX, CdY, CdZ;        // visco EM: C_d per mechanism (DT folded in)
     // boundaries
     std::vector<T> damping;                   // ABS (1 outside the frame)
     std::vector<T> fsZero, fsSelect, scaleH, scaleV;  // free surface
@@ -463,6 +466,7 @@ class Sim {
     void stepSH(int t);
     void stepTM(int t);
     void stepTE(int t);
+    void stepEM3D(int t);
 };
 
 } // namespace refcpu

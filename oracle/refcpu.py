@@ -258,7 +258,7 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
 
 
-MODEL_KEYS = ("rho", "vp", "vs", "taup", "taus", "eps_r", "sigma", "mu_r")
+MODEL_KEYS = ("rho", "vp", "vs", "taup", "taus", "eps_r", "sigma", "mu_r", "tau_eps", "tau_sigma")
 
 
 @dataclass

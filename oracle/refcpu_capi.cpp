@@ -24,12 +24,12 @@ struct Handle {
 template <class T>
 refcpu::Model<T> make_model(const wave_config* c, const T* const* arr)
 {
-    // arr: rho, vp, vs, taup, taus, eps_r, sigma, mu_r (any may be NULL)
+    // arr: rho, vp, vs, taup, taus, eps_r, sigma, mu_r, tau_eps, tau_sigma (any may be NULL)
     const refcpu::idx_t N = c->NX * c->NY * (c->dimension == 2 ? 1 : c->NZ);
     refcpu::Model<T> m;
     auto cp = [&](const T* p, std::vector<T>& v) { if (p) v.assign(p, p + N); };
     cp(arr[0], m.rho); cp(arr[1], m.vp); cp(arr[2], m.vs); cp(arr[3], m.taup); cp(arr[4], m.taus);
-    cp(arr[5], m.eps_r); cp(arr[6], m.sigma); cp(arr[7], m.mu_r);
+    cp(arr[5], m.eps_r); cp(arr[6], m.sigma); cp(arr[7], m.mu_r); cp(arr[8], m.tau_eps); cp(arr[9], m.tau_sigma);
     return m;
 }
 

@@ -167,33 +167,85 @@ void Sim<T>::prepareModel(const Model<T>& m)
             }
         }
     } else {
-        // EM: TMEM::init (TMEM.cpp:230-241), calculateAveraging (TMEM.cpp:366-374, EMEM.cpp:378-392)
+        // EM: TMEM::init (TMEM.cpp:230-241), ViscoTMEM::init (ViscoTMEM.cpp:274-292) with
+        // eps = eps_r*eps0, mu = mu_r*mu0 and tau_sigma times tau_ref = 1/(2 pi f_c);
+        // calculateAveraging (TMEM.cpp:366-374, EMEM.cpp:378-392, ViscoTMEM.cpp:442-450,
+        // ViscoEMEM.cpp:409-432); coefficients ForwardSolverEM.cpp:14-152.
         const T eps0 = static_cast<T>(8.8541878176e-12), mu0 = static_cast<T>(1.2566370614e-6);
-        std::vector<T> eps(N), sig(m.sigma), muv(N);
+        const bool visco = eq == WAVE_EQ_VISCOTMEM || eq == WAVE_EQ_VISCOEMEM;
+        std::vector<T> eps(N), sig(m.sigma), muv(N), tauE, tauSg;
         for_n(N, [&](idx_t i) { eps[i] = m.eps_r[i] * eps0; muv[i] = m.mu_r[i] * mu0; });
+        std::vector<T> relax;   // 1 / (2 pi f_l)
+        if (visco) {
+            if (m.tau_eps.size() != static_cast<size_t>(N) || m.tau_sigma.size() != static_cast<size_t>(N))
+                throw std::invalid_argument("visco-EM needs tau_eps and tau_sigma");
+            tauE = m.tau_eps;
+            tauSg = m.tau_sigma;
+            const T tauRef = static_cast<T>(1.0 / (2.0 * M_PI * static_cast<T>(cfg.CenterFrequencyCPML)));
+            for_n(N, [&](idx_t i) { tauSg[i] *= tauRef; });
+            for (int l = 0; l < L; ++l) relax.push_back(static_cast<T>(1.0 / (2.0 * M_PI * static_cast<T>(cfg.relaxationFrequency[l]))));
+        }
         auto Cinv = [&](T e, T s) { T c = T(0.5) / e; c *= s; c *= DT; c += T(1); return T(1) / c; };
         auto Ca = [&](T e, T s) { T c = T(0.5) / e; c *= s; c *= DT; c = T(1) - c; return c * Cinv(e, s); };
         auto Cb = [&](T e, T s) { T c = T(1) / e; return c * Cinv(e, s); };
-        if (eq == WAVE_EQ_TMEM) {
+        // getDielectricPermittivityEffectiveOptical (ForwardSolverEM.cpp:140-152), clamped below at eps0
+        auto epsOpt = [&](T es, T ss, T te, T ts) {
+            T e = T(1) - te; e *= es; T tmp = ss * ts; e += tmp;
+            return e < eps0 ? eps0 : e;
+        };
+        // getElectricConductivityEffectiveOptical (ForwardSolverEM.cpp:118-133)
+        T sumInv = 0;
+        for (int l = 0; l < L && visco; ++l) sumInv = static_cast<T>(static_cast<double>(sumInv) + 1.0 / static_cast<double>(relax[l]));
+        if (visco) sumInv /= static_cast<T>(L);
+        auto sigOpt = [&](T es, T ss, T te) { T s = te * sumInv; s *= es; s += ss; return s; };
+        // getCc / getAveragedCd (ForwardSolverEM.cpp:68-109)
+        emCc.clear();
+        std::vector<T> cdScale;
+        for (int l = 0; l < L && visco; ++l) {
+            const double r = static_cast<double>(relax[l]);
+            emCc.push_back(static_cast<T>((1 - 0.5 * static_cast<double>(DT) / r) / (1 + 0.5 * static_cast<double>(DT) / r)));
+            T tv = static_cast<T>(1 / (1 + 0.5 * static_cast<double>(DT) / r));
+            tv /= (static_cast<T>(L) * relax[l] * relax[l]);
+            cdScale.push_back(tv);
+        }
+        // coefficients of one E component from its (averaged) material values
+        auto coeffs = [&](const std::vector<T>& e, const std::vector<T>& s, const std::vector<T>* te, const std::vector<T>* ts,
+                          std::vector<T>& ca, std::vector<T>& cb, std::vector<std::vector<T>>& cd) {
+            ca.assign(N, 0); cb.assign(N, 0);
+            for_n(N, [&](idx_t i) {
+                T ee = e[i], ss = s[i];
+                if (visco) { T eo = epsOpt(e[i], s[i], (*te)[i], (*ts)[i]); ss = sigOpt(e[i], s[i], (*te)[i]); ee = eo; }
+                ca[i] = Ca(ee, ss); cb[i] = Cb(ee, ss);
+            });
+            cd.assign(visco ? L : 0, std::vector<T>(N, 0));
+            for (int l = 0; l < L && visco; ++l)
+                for_n(N, [&](idx_t i) { T c = (*te)[i] * cdScale[l]; c *= e[i]; c *= -DT; cd[l][i] = c; });
+        };
+        auto inv4 = [&](int plane, std::vector<T>& out) {
+            out.assign(N, 0);
+            average4<T>(g, plane, muv.data(), out.data());
+            for_n(N, [&](idx_t i) { T v = T(1) / out[i]; out[i] = is_invalid(v) ? T(0) : v; });
+        };
+        auto avg = [&](const std::vector<T>& in, Axis a) { std::vector<T> o(N); average2<T>(g, a, in.data(), o.data()); return o; };
+        if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_VISCOTMEM) {
+            if (is3d) throw std::invalid_argument("TM modelling is 2-D only");
             inv_avg(muv, Axis::X, invMuXZ);
             inv_avg(muv, Axis::Y, invMuYZ);
-            CaZ.assign(N, 0); CbZ.assign(N, 0);
-            for_n(N, [&](idx_t i) { CaZ[i] = Ca(eps[i], sig[i]); CbZ[i] = Cb(eps[i], sig[i]); });
-        } else if (eq == WAVE_EQ_EMEM) {
-            // 4-point average then inverse (calcInverseAveragedParameter with averageMatrixXY)
-            invMuXY.assign(N, 0);
-            average4<T>(g, 0, muv.data(), invMuXY.data());
-            for_n(N, [&](idx_t i) { T v = T(1) / invMuXY[i]; invMuXY[i] = is_invalid(v) ? T(0) : v; });
-            std::vector<T> sX(N), sY(N), eX(N), eY(N);
-            average2<T>(g, Axis::X, sig.data(), sX.data());
-            average2<T>(g, Axis::Y, sig.data(), sY.data());
-            average2<T>(g, Axis::X, eps.data(), eX.data());
-            average2<T>(g, Axis::Y, eps.data(), eY.data());
-            CaX.assign(N, 0); CbX.assign(N, 0); CaY.assign(N, 0); CbY.assign(N, 0);
-            for_n(N, [&](idx_t i) {
-                CaX[i] = Ca(eX[i], sX[i]); CbX[i] = Cb(eX[i], sX[i]);
-                CaY[i] = Ca(eY[i], sY[i]); CbY[i] = Cb(eY[i], sY[i]);
-            });
+            coeffs(eps, sig, visco ? &tauE : nullptr, visco ? &tauSg : nullptr, CaZ, CbZ, CdZ);
+        } else if (eq == WAVE_EQ_EMEM || eq == WAVE_EQ_VISCOEMEM) {
+            inv4(0, invMuXY);
+            if (is3d) { inv4(1, invMuXZ); inv4(2, invMuYZ); }
+            std::vector<Axis> axes = {Axis::X, Axis::Y};
+            if (is3d) axes.push_back(Axis::Z);
+            for (Axis a : axes) {
+                auto e = avg(eps, a), s = avg(sig, a);
+                std::vector<T> te, ts;
+                if (visco) { te = avg(tauE, a); ts = avg(tauSg, a); }
+                auto& ca = a == Axis::X ? CaX : (a == Axis::Y ? CaY : CaZ);
+                auto& cb = a == Axis::X ? CbX : (a == Axis::Y ? CbY : CbZ);
+                auto& cd = a == Axis::X ? CdX : (a == Axis::Y ? CdY : CdZ);
+                coeffs(e, s, visco ? &te : nullptr, visco ? &ts : nullptr, ca, cb, cd);
+            }
         } else {
             throw std::invalid_argument("equation not available in the oracle");
         }
@@ -323,8 +375,12 @@ void Sim<T>::reset()
         break;
     case WAVE_EQ_SH:
     case WAVE_EQ_VISCOSH: names = {"vz", "sxz", "syz"}; break;
-    case WAVE_EQ_TMEM: names = {"hx", "hy", "ez"}; break;
-    case WAVE_EQ_EMEM: names = {"hz", "ex", "ey"}; break;
+    case WAVE_EQ_TMEM:
+    case WAVE_EQ_VISCOTMEM: names = {"hx", "hy", "ez"}; break;
+    case WAVE_EQ_EMEM:
+    case WAVE_EQ_VISCOEMEM:
+        names = is3d ? std::vector<const char*>{"hx", "hy", "hz", "ex", "ey", "ez"} : std::vector<const char*>{"hz", "ex", "ey"};
+        break;
     }
     for (auto n : names) F[n].assign(N, 0);
     if (eq == WAVE_EQ_VISCOELASTIC) {
@@ -334,6 +390,12 @@ void Sim<T>::reset()
     if (eq == WAVE_EQ_VISCOSH) {
         R["rxz"].assign(L, std::vector<T>(N, 0));
         R["ryz"].assign(L, std::vector<T>(N, 0));
+    }
+    if (eq == WAVE_EQ_VISCOTMEM) R["rz"].assign(L, std::vector<T>(N, 0));
+    if (eq == WAVE_EQ_VISCOEMEM) {
+        R["rx"].assign(L, std::vector<T>(N, 0));
+        R["ry"].assign(L, std::vector<T>(N, 0));
+        if (is3d) R["rz"].assign(L, std::vector<T>(N, 0));
     }
     upd.assign(N, 0); updt.assign(N, 0); upd2.assign(N, 0); vxx.assign(N, 0); vyy.assign(N, 0); vzz.assign(N, 0); tmp.assign(N, 0);
     seis.assign(rec.idx.size() * static_cast<size_t>(NT), 0);
@@ -419,8 +481,13 @@ void Sim<T>::step(int t)
     case WAVE_EQ_VISCOELASTIC: stepVisco(t); break;
     case WAVE_EQ_SH:
     case WAVE_EQ_VISCOSH: stepSH(t); break;
-    case WAVE_EQ_TMEM: stepTM(t); break;
-    case WAVE_EQ_EMEM: stepTE(t); break;
+    case WAVE_EQ_TMEM:
+    case WAVE_EQ_VISCOTMEM: stepTM(t); break;
+    case WAVE_EQ_EMEM:
+    case WAVE_EQ_VISCOEMEM:
+        if (is3d) stepEM3D(t);
+        else stepTE(t);
+        break;
     default: throw std::invalid_argument("equation not available in the oracle");
     }
 }
@@ -851,10 +918,18 @@ void Sim<T>::stepTM(int t)
     VEC_OP(upd[i] = -updt[i]);
     VEC_OP(upd[i] *= invMuXZ[i]);
     VEC_OP(hY[i] -= upd[i]);
+    // visco-TM memory variables (ForwardSolver2Dviscotmem.cpp:175-182)
+    for (int l = 0; l < L; ++l) {
+        auto& r = R["rz"][l];
+        const T cc = emCc[l];
+        const auto& cd = CdZ[l];
+        VEC_OP(T u = cc * r[i]; T ut = cd[i] * eZ[i]; r[i] = ut + u);
+    }
     Dxb.spmv(hY.data(), upd.data());
     Dyb.spmv(hX.data(), updt.data());
     if (useCpml) { cpml(upd, "hyx", ax, bx); cpml(updt, "hxy", ay, by); }
     VEC_OP(upd[i] -= updt[i]);
+    for (int l = 0; l < L; ++l) { const auto& r = R["rz"][l]; VEC_OP(upd[i] -= DT * r[i]); }
     VEC_OP(upd[i] *= CbZ[i]);
     VEC_OP(updt[i] = CaZ[i] * eZ[i]);
     VEC_OP(eZ[i] = updt[i] + upd[i]);
@@ -865,7 +940,8 @@ void Sim<T>::stepTM(int t)
     gather(t);
 }
 
-// FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:112-185)
+// FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:112-185),
+// FD2Dviscoemem::run (ForwardSolverEM/ForwardSolver2Dviscoemem.cpp:154-228)
 template <class T>
 void Sim<T>::stepTE(int t)
 {
@@ -877,18 +953,101 @@ void Sim<T>::stepTE(int t)
     VEC_OP(upd[i] -= updt[i]);
     VEC_OP(upd[i] *= invMuXY[i]);
     VEC_OP(hZ[i] -= upd[i]);
+    for (int l = 0; l < L; ++l) {
+        const T cc = emCc[l];
+        auto& rx = R["rx"][l];
+        auto& ry = R["ry"][l];
+        const auto& cdx = CdX[l];
+        const auto& cdy = CdY[l];
+        VEC_OP(T u = cc * rx[i]; T ut = cdx[i] * eX[i]; rx[i] = ut + u);
+        VEC_OP(T u = cc * ry[i]; T ut = cdy[i] * eY[i]; ry[i] = ut + u);
+    }
     Dyb.spmv(hZ.data(), upd.data());
     if (useCpml) cpml(upd, "hzy", ay, by);
+    for (int l = 0; l < L; ++l) { const auto& r = R["rx"][l]; VEC_OP(upd[i] -= DT * r[i]); }
     VEC_OP(upd[i] *= CbX[i]);
     VEC_OP(updt[i] = CaX[i] * eX[i]);
     VEC_OP(eX[i] = updt[i] + upd[i]);
-    Dxb.spmv(hZ.data(), upd.data());
-    if (useCpml) cpml(upd, "hzx", ax, bx);
+    Dxb.spmv(hZ.data(), updt.data());
+    if (useCpml) cpml(updt, "hzx", ax, bx);
+    VEC_OP(upd[i] = -updt[i]);
+    for (int l = 0; l < L; ++l) { const auto& r = R["ry"][l]; VEC_OP(upd[i] -= DT * r[i]); }
     VEC_OP(upd[i] *= CbY[i]);
     VEC_OP(updt[i] = CaY[i] * eY[i]);
-    VEC_OP(eY[i] = updt[i] - upd[i]);
+    VEC_OP(eY[i] = updt[i] + upd[i]);
     if (useAbs) {
         for (auto* v : {&eY, &eX, &hZ}) { auto& w = *v; VEC_OP(w[i] *= damping[i]); }
+    }
+    applySources(t);
+    gather(t);
+}
+
+// FD3Demem::run (ForwardSolverEM/ForwardSolver3Demem.cpp:140-237) and
+// FD3Dviscoemem::run (ForwardSolverEM/ForwardSolver3Dviscoemem.cpp:186-309).
+// CPML as CPMLEM3D.cpp:25-108: E derivatives use the half profile, H
+// derivatives the full one, except hyx, which uses the half profile there.
+template <class T>
+void Sim<T>::stepEM3D(int t)
+{
+    const idx_t N = g.N();
+    auto& hX = F["hx"]; auto& hY = F["hy"]; auto& hZ = F["hz"];
+    auto& eX = F["ex"]; auto& eY = F["ey"]; auto& eZ = F["ez"];
+    Dyf.spmv(eZ.data(), upd.data());
+    Dzf.spmv(eY.data(), updt.data());
+    if (useCpml) { cpml(upd, "ezy", ayh, byh); cpml(updt, "eyz", azh, bzh); }
+    VEC_OP(upd[i] -= updt[i]);
+    VEC_OP(upd[i] *= invMuYZ[i]);
+    VEC_OP(hX[i] -= upd[i]);
+    Dzf.spmv(eX.data(), upd.data());
+    Dxf.spmv(eZ.data(), updt.data());
+    if (useCpml) { cpml(upd, "exz", azh, bzh); cpml(updt, "ezx", axh, bxh); }
+    VEC_OP(upd[i] -= updt[i]);
+    VEC_OP(upd[i] *= invMuXZ[i]);
+    VEC_OP(hY[i] -= upd[i]);
+    Dxf.spmv(eY.data(), upd.data());
+    Dyf.spmv(eX.data(), updt.data());
+    if (useCpml) { cpml(upd, "eyx", axh, bxh); cpml(updt, "exy", ayh, byh); }
+    VEC_OP(upd[i] -= updt[i]);
+    VEC_OP(upd[i] *= invMuXY[i]);
+    VEC_OP(hZ[i] -= upd[i]);
+    for (int l = 0; l < L; ++l) {
+        const T cc = emCc[l];
+        for (auto [rn, cdv, e] : {std::make_tuple("rx", &CdX, &eX), std::make_tuple("ry", &CdY, &eY), std::make_tuple("rz", &CdZ, &eZ)}) {
+            auto& r = R[rn][l];
+            const auto& cd = (*cdv)[l];
+            const auto& ef = *e;
+            VEC_OP(T u = cc * r[i]; T ut = cd[i] * ef[i]; r[i] = ut + u);
+        }
+    }
+    // ex
+    Dyb.spmv(hZ.data(), upd.data());
+    Dzb.spmv(hY.data(), updt.data());
+    if (useCpml) { cpml(upd, "hzy", ay, by); cpml(updt, "hyz", az, bz); }
+    VEC_OP(upd[i] -= updt[i]);
+    for (int l = 0; l < L; ++l) { const auto& r = R["rx"][l]; VEC_OP(upd[i] -= DT * r[i]); }
+    VEC_OP(upd[i] *= CbX[i]);
+    VEC_OP(updt[i] = CaX[i] * eX[i]);
+    VEC_OP(eX[i] = updt[i] + upd[i]);
+    // ey
+    Dzb.spmv(hX.data(), upd.data());
+    Dxb.spmv(hZ.data(), updt.data());
+    if (useCpml) { cpml(upd, "hxz", az, bz); cpml(updt, "hzx", ax, bx); }
+    VEC_OP(upd[i] -= updt[i]);
+    for (int l = 0; l < L; ++l) { const auto& r = R["ry"][l]; VEC_OP(upd[i] -= DT * r[i]); }
+    VEC_OP(upd[i] *= CbY[i]);
+    VEC_OP(updt[i] = CaY[i] * eY[i]);
+    VEC_OP(eY[i] = updt[i] + upd[i]);
+    // ez
+    Dxb.spmv(hY.data(), upd.data());
+    Dyb.spmv(hX.data(), updt.data());
+    if (useCpml) { cpml(upd, "hyx", axh, bxh); cpml(updt, "hxy", ay, by); }
+    VEC_OP(upd[i] -= updt[i]);
+    for (int l = 0; l < L; ++l) { const auto& r = R["rz"][l]; VEC_OP(upd[i] -= DT * r[i]); }
+    VEC_OP(upd[i] *= CbZ[i]);
+    VEC_OP(updt[i] = CaZ[i] * eZ[i]);
+    VEC_OP(eZ[i] = updt[i] + upd[i]);
+    if (useAbs) {
+        for (auto* v : {&eZ, &eY, &eX, &hX, &hY, &hZ}) { auto& w = *v; VEC_OP(w[i] *= damping[i]); }
     }
     applySources(t);
     gather(t);

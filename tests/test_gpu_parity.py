@@ -43,7 +43,7 @@ def test_gpu_matches_reference_goldens(name, wave, refcpu):
 # ----------------------------------------------------------------------------
 def make_case(refcpu, eq, dim, order, fs=0, boundary=2, stencil=0, reduce=1, L=2, seed=0, dims=None):
     rng = np.random.default_rng(seed)
-    em = eq in ("tmem", "emem")
+    em = eq in ("tmem", "emem", "viscotmem", "viscoemem")
     if dims is not None:
         NX, NY, NZ = dims
     elif dim == 2:
@@ -55,6 +55,8 @@ def make_case(refcpu, eq, dim, order, fs=0, boundary=2, stencil=0, reduce=1, L=2
         DH = 0.02
         eps_r = rng.uniform(4.0, 9.0, n)
         model = dict(eps_r=eps_r, sigma=10 ** rng.uniform(-4, -2, n), mu_r=np.ones(n))
+        if eq.startswith("visco"):
+            model.update(tau_eps=rng.uniform(0.05, 0.3, n), tau_sigma=rng.uniform(0.05, 0.3, n))
         vmax, vmin = 3e8 / 2.0, 3e8 / 3.0
         extra = dict(CenterFrequencyCPML=2e8, VMaxCPML=vmax)
     else:
@@ -70,20 +72,22 @@ def make_case(refcpu, eq, dim, order, fs=0, boundary=2, stencil=0, reduce=1, L=2
                              spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary,
                              BoundaryWidth=10 if boundary else 0, DampingCoeff=8.0, NPower=4.0,
                              numRelaxationMechanisms=L if eq.startswith("visco") else 0,
-                             relaxationFrequency=[8.0, 30.0, 0.0, 0.0], useStencilMatrix=stencil,
+                             relaxationFrequency=[1e8, 6e8, 0.0, 0.0] if em else [8.0, 30.0, 0.0, 0.0],
+                             useStencilMatrix=stencil,
                              edgeOrderReduction=reduce, **extra)
     nt = refcpu.nt_of(cfg)
     fc = vmin / (8 * DH)
     sx, sy, sz = NX // 2, (2 if fs else NY // 3), NZ // 2
-    src_type = {"acoustic": 1, "elastic": 1, "viscoelastic": 1, "sh": 4, "viscosh": 4, "tmem": 1, "emem": 4}[eq]
+    src_type = {"acoustic": 1, "elastic": 1, "viscoelastic": 1, "sh": 4, "viscosh": 4, "tmem": 1, "viscotmem": 1,
+                "emem": 1 if dim == 3 else 4, "viscoemem": 1 if dim == 3 else 4}[eq]
     sidx = np.array([refcpu.grid_index(cfg, sx, sy, sz)])
     sig = refcpu.ricker(nt, DT, fc, 1.0, 0.0, np.float64)[None]
     if eq in ("sh", "viscosh"):
         rtypes = [4, 4, 4]
-    elif eq == "tmem":
+    elif eq in ("tmem", "viscotmem"):
         rtypes = [1, 1, 1]
-    elif eq == "emem":
-        rtypes = [2, 3, 4]
+    elif eq in ("emem", "viscoemem"):
+        rtypes = [1, 2, 3, 4] if dim == 3 else [2, 3, 4]
     else:
         rtypes = [1, 2, 3] + ([4] if dim == 3 else [])
     ridx = [refcpu.grid_index(cfg, 3 + (7 * k) % (NX - 6), (k * 5) % NY if not fs else 0, (3 * k) % NZ)
@@ -127,6 +131,14 @@ SEISMIC = [
     ("tmem", 2, 6, 0, 1, 1, 0),
     ("emem", 2, 4, 0, 2, 0, 1),
     ("emem", 2, 2, 0, 1, 0, 0),
+    ("viscotmem", 2, 4, 0, 2, 0, 1),
+    ("viscotmem", 2, 8, 0, 1, 1, 0),
+    ("viscoemem", 2, 6, 0, 2, 0, 1),
+    ("viscoemem", 2, 2, 0, 0, 0, 1),
+    ("emem", 3, 4, 0, 2, 0, 1),
+    ("emem", 3, 2, 0, 1, 0, 0),
+    ("viscoemem", 3, 6, 0, 2, 0, 1),
+    ("viscoemem", 3, 4, 0, 1, 1, 0),
 ]
 
 

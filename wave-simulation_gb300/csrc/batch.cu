@@ -130,7 +130,7 @@ int wave_batch_create(const wave_config* cfgs, int nshots, wave_batch** out)
         ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         ck(cudaMalloc(&b->counters, nshots * sizeof(int)), "cudaMalloc");
         wave_handle* h0 = b->shots[0];
-        b->eq = h0->cfg.equation;
+        b->eq = kernel_eq(h0->cfg.equation, h0->cfg.dimension == 3);
         b->H = h0->H;
         b->NT = h0->NT;
         b->abs = h0->sp.abs != 0;

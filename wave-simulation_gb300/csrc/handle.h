@@ -23,6 +23,7 @@ struct wave_handle {
     wave_config cfg{};
     int NT = 0, NX = 1, NY = 1, NZ = 1, H = 1, L = 0;
     long long N = 0;
+    bool is3d() const { return cfg.dimension == 3; }
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;

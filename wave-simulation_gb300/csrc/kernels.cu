@@ -104,45 +104,45 @@ __device__ __forceinline__ long long pix(const StepParams& P, const Pt& p, int s
 __device__ __forceinline__ long long piy(const StepParams& P, const Pt& p, int s) { return p.x + (long long)P.NX * (p.z + (long long)P.NZ * s); }
 __device__ __forceinline__ long long piz(const StepParams& P, const Pt& p, int s) { return p.x + (long long)P.NX * (s + (long long)P.cz.ns * p.y); }
 
-// derivative + CPML along x / y / z. half = forward-type derivative (uses the
-// half-grid profile, CPML3D.cpp:31-153).
-template <int H, bool FWD>
+// derivative + CPML along x / y / z. HALF: the half-grid profile, by default
+// for forward-type derivatives (CPML3D.cpp:31-153).
+template <int H, bool FWD, bool HALF = FWD>
 __device__ __forceinline__ float dX(const StepParams& P, const Pt& p, const float* u, const Op1D& op, int psiSlot)
 {
     float d = deriv<H, FWD>(u, p.i, 1, p.x, op);
     if (P.useCpml) {
         int s = slab(p.x, P.cx);
         if (s >= 0) {
-            const float a = FWD ? P.cx.a_half[p.x] : P.cx.a_full[p.x];
-            const float b = FWD ? P.cx.b_half[p.x] : P.cx.b_full[p.x];
+            const float a = HALF ? P.cx.a_half[p.x] : P.cx.a_full[p.x];
+            const float b = HALF ? P.cx.b_half[p.x] : P.cx.b_full[p.x];
             cpml(d, P.psi[psiSlot], pix(P, p, s), a, b);
         }
     }
     return d;
 }
-template <int H, bool FWD>
+template <int H, bool FWD, bool HALF = FWD>
 __device__ __forceinline__ float dY(const StepParams& P, const Pt& p, const float* u, const Op1D& op, int psiSlot)
 {
     float d = deriv<H, FWD>(u, p.i, (long long)P.NX * P.NZ, p.y, op);
     if (P.useCpml) {
         int s = slab(p.y, P.cy);
         if (s >= 0) {
-            const float a = FWD ? P.cy.a_half[p.y] : P.cy.a_full[p.y];
-            const float b = FWD ? P.cy.b_half[p.y] : P.cy.b_full[p.y];
+            const float a = HALF ? P.cy.a_half[p.y] : P.cy.a_full[p.y];
+            const float b = HALF ? P.cy.b_half[p.y] : P.cy.b_full[p.y];
             cpml(d, P.psi[psiSlot], piy(P, p, s), a, b);
         }
     }
     return d;
 }
-template <int H, bool FWD>
+template <int H, bool FWD, bool HALF = FWD>
 __device__ __forceinline__ float dZ(const StepParams& P, const Pt& p, const float* u, const Op1D& op, int psiSlot)
 {
     float d = deriv<H, FWD>(u, p.i, P.NX, p.z, op);
     if (P.useCpml) {
         int s = slab(p.z, P.cz);
         if (s >= 0) {
-            const float a = FWD ? P.cz.a_half[p.z] : P.cz.a_full[p.z];
-            const float b = FWD ? P.cz.b_half[p.z] : P.cz.b_full[p.z];
+            const float a = HALF ? P.cz.a_half[p.z] : P.cz.a_full[p.z];
+            const float b = HALF ? P.cz.b_half[p.z] : P.cz.b_full[p.z];
             cpml(d, P.psi[psiSlot], piz(P, p, s), a, b);
         }
     }
@@ -637,7 +637,8 @@ __global__ void __launch_bounds__(256) sh_s_batch(const StepParams* __restrict__
 }
 
 // --------------------------------------------------------------------------
-// EM TMz: FD2Dtmem::run (ForwardSolverEM/ForwardSolver2Dtmem.cpp:128-170)
+// EM TMz: FD2Dtmem::run (ForwardSolverEM/ForwardSolver2Dtmem.cpp:128-170),
+// FD2Dviscotmem::run (ForwardSolverEM/ForwardSolver2Dviscotmem.cpp:150-205)
 // --------------------------------------------------------------------------
 template <int H>
 __device__ __forceinline__ void tm_h_body(const StepParams& P, const Pt& p)
@@ -671,14 +672,31 @@ __global__ void __launch_bounds__(256) tm_h_batch(const StepParams* __restrict__
     tm_h_body<H>(sP, p);
 }
 
+// memory variables of one E component (ForwardSolver2Dviscotmem.cpp:175-182,
+// ForwardSolverEM/ForwardSolver2Dviscoemem.cpp:176-184): r_l = Cd_l e + Cc_l r_l,
+// then the E update subtracts DT r_l for every mechanism
+__device__ __forceinline__ void em_memory(const StepParams& P, const Pt& p, int rslot, int cd0, float e, float& u)
+{
+    for (int l = 0; l < P.L; ++l) {
+        float* r = P.r[rslot][l] + p.i;
+        const float ru = P.Cc[l] * *r;
+        const float rt = __ldg(P.m[cd0 + l] + p.i) * e;
+        const float rn = rt + ru;
+        *r = rn;
+        u -= P.DT * rn;
+    }
+}
+
 template <int H>
 __device__ __forceinline__ void tm_e_body(const StepParams& P, const Pt& p)
 {
+    const float e0 = P.f[F_EZ][p.i];
     float u = dX<H, false>(P, p, P.f[F_HY], P.Dxb, PS_HYX);
     float ut = dY<H, false>(P, p, P.f[F_HX], P.Dyb, PS_HXY);
     u -= ut;
+    em_memory(P, p, R_EZ, M_CDZ0, e0, u);
     u *= LD(P.m[M_CBZ]);
-    float e = LD(P.m[M_CAZ]) * P.f[F_EZ][p.i];
+    float e = LD(P.m[M_CAZ]) * e0;
     e = e + u;
     if (P.abs) e *= absDamp(P, p);
     P.f[F_EZ][p.i] = e;
@@ -703,7 +721,8 @@ __global__ void __launch_bounds__(256) tm_e_batch(const StepParams* __restrict__
     tm_e_body<H>(sP, p);
 }
 
-// EM TEz: FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:132-180)
+// EM TEz: FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:132-180),
+// FD2Dviscoemem::run (ForwardSolverEM/ForwardSolver2Dviscoemem.cpp:154-228)
 template <int H>
 __device__ __forceinline__ void te_h_body(const StepParams& P, const Pt& p)
 {
@@ -738,14 +757,18 @@ __device__ __forceinline__ void te_e_body(const StepParams& P, const Pt& p)
 {
     const float* hz = P.f[F_HZ];
     const float d = P.abs ? absDamp(P, p) : 1.0f;
+    const float ex0 = P.f[F_EX][p.i], ey0 = P.f[F_EY][p.i];
     float u = dY<H, false>(P, p, hz, P.Dyb, PS_HZY);
+    em_memory(P, p, R_EX, M_CDX0, ex0, u);
     u *= LD(P.m[M_CBX]);
-    float e = LD(P.m[M_CAX]) * P.f[F_EX][p.i];
+    float e = LD(P.m[M_CAX]) * ex0;
     P.f[F_EX][p.i] = (e + u) * d;
-    u = dX<H, false>(P, p, hz, P.Dxb, PS_HZX);
+    const float ut = dX<H, false>(P, p, hz, P.Dxb, PS_HZX);
+    u = -ut;
+    em_memory(P, p, R_EY, M_CDY0, ey0, u);
     u *= LD(P.m[M_CBY]);
-    e = LD(P.m[M_CAY]) * P.f[F_EY][p.i];
-    P.f[F_EY][p.i] = (e - u) * d;
+    e = LD(P.m[M_CAY]) * ey0;
+    P.f[F_EY][p.i] = (e + u) * d;
 }
 
 template <int H>
@@ -765,6 +788,103 @@ __global__ void __launch_bounds__(256) te_e_batch(const StepParams* __restrict__
     Pt p;
     if (!point_tile(sP, w, p)) return;
     te_e_body<H>(sP, p);
+}
+
+// --------------------------------------------------------------------------
+// 3-D EM: FD3Demem::run (ForwardSolverEM/ForwardSolver3Demem.cpp:140-237),
+// FD3Dviscoemem::run (ForwardSolverEM/ForwardSolver3Dviscoemem.cpp:186-309).
+// CPML as CPMLEM3D.cpp:25-108: E derivatives on the half profile, H
+// derivatives on the full one except hyx, which uses the half profile there.
+// --------------------------------------------------------------------------
+template <int H>
+__device__ __forceinline__ void em3_h_body(const StepParams& P, const Pt& p)
+{
+    const float *ex = P.f[F_EX], *ey = P.f[F_EY], *ez = P.f[F_EZ];
+    float u = dY<H, true>(P, p, ez, P.Dyf, PS_EZY);
+    float ut = dZ<H, true>(P, p, ey, P.Dzf, PS_EYZ);
+    u -= ut;
+    u *= LD(P.m[M_IMUYZ]);
+    P.f[F_HX][p.i] -= u;
+    u = dZ<H, true>(P, p, ex, P.Dzf, PS_EXZ);
+    ut = dX<H, true>(P, p, ez, P.Dxf, PS_EZX);
+    u -= ut;
+    u *= LD(P.m[M_IMUXZ]);
+    P.f[F_HY][p.i] -= u;
+    u = dX<H, true>(P, p, ey, P.Dxf, PS_EYX);
+    ut = dY<H, true>(P, p, ex, P.Dyf, PS_EXY);
+    u -= ut;
+    u *= LD(P.m[M_IMUXY]);
+    P.f[F_HZ][p.i] -= u;
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) em3_h(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    em3_h_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) em3_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    em3_h_body<H>(sP, p);
+}
+
+template <int H>
+__device__ __forceinline__ void em3_e_body(const StepParams& P, const Pt& p)
+{
+    const float *hx = P.f[F_HX], *hy = P.f[F_HY], *hz = P.f[F_HZ];
+    const float d = P.abs ? absDamp(P, p) : 1.0f;
+    const float ex0 = P.f[F_EX][p.i], ey0 = P.f[F_EY][p.i], ez0 = P.f[F_EZ][p.i];
+    // ex
+    float u = dY<H, false>(P, p, hz, P.Dyb, PS_HZY);
+    float ut = dZ<H, false>(P, p, hy, P.Dzb, PS_HYZ);
+    u -= ut;
+    em_memory(P, p, R_EX, M_CDX0, ex0, u);
+    u *= LD(P.m[M_CBX]);
+    float e = LD(P.m[M_CAX]) * ex0;
+    P.f[F_EX][p.i] = (e + u) * d;
+    // ey
+    u = dZ<H, false>(P, p, hx, P.Dzb, PS_HXZ);
+    ut = dX<H, false>(P, p, hz, P.Dxb, PS_HZX);
+    u -= ut;
+    em_memory(P, p, R_EY, M_CDY0, ey0, u);
+    u *= LD(P.m[M_CBY]);
+    e = LD(P.m[M_CAY]) * ey0;
+    P.f[F_EY][p.i] = (e + u) * d;
+    // ez
+    u = dX<H, false, true>(P, p, hy, P.Dxb, PS_HYX);
+    ut = dY<H, false>(P, p, hx, P.Dyb, PS_HXY);
+    u -= ut;
+    em_memory(P, p, R_EZ, M_CDZ0, ez0, u);
+    u *= LD(P.m[M_CBZ]);
+    e = LD(P.m[M_CAZ]) * ez0;
+    P.f[F_EZ][p.i] = (e + u) * d;
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) em3_e(StepParams P)
+{
+    Pt p;
+    if (!point(P, p)) return;
+    em3_e_body<H>(P, p);
+}
+
+template <int H>
+__global__ void __launch_bounds__(256) em3_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    em3_e_body<H>(sP, p);
 }
 
 // --------------------------------------------------------------------------
@@ -1060,16 +1180,21 @@ StepKernel kernel_for(int eq, int pass, int H)
     static const StepKernel el_v[6] = WAVE_KTAB(elastic_v), el_s[6] = WAVE_KTAB(elastic_s), vi_s[6] = WAVE_KTAB(visco_s);
     static const StepKernel s_v[6] = WAVE_KTAB(sh_v), s_s[6] = WAVE_KTAB(sh_s);
     static const StepKernel tmh[6] = WAVE_KTAB(tm_h), tme[6] = WAVE_KTAB(tm_e), teh[6] = WAVE_KTAB(te_h), tee[6] = WAVE_KTAB(te_e);
+    static const StepKernel e3h[6] = WAVE_KTAB(em3_h), e3e[6] = WAVE_KTAB(em3_e);
     if (H < 1 || H > 6) return nullptr;
     const int k = H - 1;
     switch (eq) {
+    case WAVE_EQ_EMEM + kEm3d:
+    case WAVE_EQ_VISCOEMEM + kEm3d: return pass == 0 ? e3h[k] : e3e[k];
     case WAVE_EQ_ACOUSTIC: return pass == 0 ? ac_v[k] : ac_p[k];
     case WAVE_EQ_ELASTIC: return pass == 0 ? el_v[k] : el_s[k];
     case WAVE_EQ_VISCOELASTIC: return pass == 0 ? el_v[k] : vi_s[k];
     case WAVE_EQ_SH:
     case WAVE_EQ_VISCOSH: return pass == 0 ? s_v[k] : s_s[k];
-    case WAVE_EQ_TMEM: return pass == 0 ? tmh[k] : tme[k];
-    case WAVE_EQ_EMEM: return pass == 0 ? teh[k] : tee[k];
+    case WAVE_EQ_TMEM:
+    case WAVE_EQ_VISCOTMEM: return pass == 0 ? tmh[k] : tme[k];
+    case WAVE_EQ_EMEM:
+    case WAVE_EQ_VISCOEMEM: return pass == 0 ? teh[k] : tee[k];
     default: return nullptr;
     }
 }
@@ -1086,16 +1211,21 @@ BatchKernel batch_kernel_for(int eq, int pass, int H)
     static const BatchKernel el_v[6] = WAVE_KTAB(elastic_v_batch), el_s[6] = WAVE_KTAB(elastic_s_batch), vi_s[6] = WAVE_KTAB(visco_s_batch);
     static const BatchKernel s_v[6] = WAVE_KTAB(sh_v_batch), s_s[6] = WAVE_KTAB(sh_s_batch);
     static const BatchKernel tmh[6] = WAVE_KTAB(tm_h_batch), tme[6] = WAVE_KTAB(tm_e_batch), teh[6] = WAVE_KTAB(te_h_batch), tee[6] = WAVE_KTAB(te_e_batch);
+    static const BatchKernel e3h[6] = WAVE_KTAB(em3_h_batch), e3e[6] = WAVE_KTAB(em3_e_batch);
     if (H < 1 || H > 6) return nullptr;
     const int k = H - 1;
     switch (eq) {
+    case WAVE_EQ_EMEM + kEm3d:
+    case WAVE_EQ_VISCOEMEM + kEm3d: return pass == 0 ? e3h[k] : e3e[k];
     case WAVE_EQ_ACOUSTIC: return pass == 0 ? ac_v[k] : ac_p[k];
     case WAVE_EQ_ELASTIC: return pass == 0 ? el_v[k] : el_s[k];
     case WAVE_EQ_VISCOELASTIC: return pass == 0 ? el_v[k] : vi_s[k];
     case WAVE_EQ_SH:
     case WAVE_EQ_VISCOSH: return pass == 0 ? s_v[k] : s_s[k];
-    case WAVE_EQ_TMEM: return pass == 0 ? tmh[k] : tme[k];
-    case WAVE_EQ_EMEM: return pass == 0 ? teh[k] : tee[k];
+    case WAVE_EQ_TMEM:
+    case WAVE_EQ_VISCOTMEM: return pass == 0 ? tmh[k] : tme[k];
+    case WAVE_EQ_EMEM:
+    case WAVE_EQ_VISCOEMEM: return pass == 0 ? teh[k] : tee[k];
     default: return nullptr;
     }
 }
@@ -1148,5 +1278,54 @@ void k_inv_clamped(PrepParams G, const float* mu, float* out, cudaStream_t s) { 
 void k_one_plus(PrepParams G, const float* tau, float L, float* out, cudaStream_t s) { prep_one_plus<<<PREP_GRID>>>(G, tau, L, out); }
 void k_scale(PrepParams G, const float* a, float sc, float* out, cudaStream_t s) { prep_scale<<<PREP_GRID>>>(G, a, sc, out); }
 void k_cacb(PrepParams G, const float* eps, const float* sig, float DT, float* ca, float* cb, cudaStream_t s) { prep_cacb<<<PREP_GRID>>>(G, eps, sig, DT, ca, cb); }
+
+struct CdOut {
+    float* p[kMaxL];
+};
+
+// Visco-EM coefficients of one E component from its (averaged) static
+// permittivity, conductivity and relaxation parameters: effective optical
+// permittivity (clamped below at eps0) and conductivity, Ca/Cb, and C_d per
+// mechanism (ForwardSolverEM.cpp:14-152).
+__global__ void prep_visco_em(PrepParams G, const float* eps, const float* sig, const float* te, const float* ts, ViscoEmCoef c,
+                              float* ca, float* cb, CdOut cd)
+{
+    PREP_LOOP {
+        float eo = 1.0f - te[i];
+        eo *= eps[i];
+        const float tmp = sig[i] * ts[i];
+        eo += tmp;
+        if (eo < c.eps0) eo = c.eps0;
+        float so = te[i] * c.sumInv;
+        so *= eps[i];
+        so += sig[i];
+        float q = 0.5f / eo;
+        q *= so;
+        q *= c.DT;
+        q += 1.0f;
+        const float cinv = 1.0f / q;
+        float a = 0.5f / eo;
+        a *= so;
+        a *= c.DT;
+        a = 1.0f - a;
+        ca[i] = a * cinv;
+        const float b = 1.0f / eo;
+        cb[i] = b * cinv;
+        for (int l = 0; l < c.L; ++l) {
+            float v = te[i] * c.cdScale[l];
+            v *= eps[i];
+            v *= -c.DT;
+            cd.p[l][i] = v;
+        }
+    }
+}
+
+void k_visco_em(PrepParams G, const float* eps, const float* sig, const float* te, const float* ts, const ViscoEmCoef& c,
+                float* ca, float* cb, float* const* cd, cudaStream_t s)
+{
+    CdOut o{};
+    for (int l = 0; l < c.L && l < kMaxL; ++l) o.p[l] = cd[l];
+    prep_visco_em<<<PREP_GRID>>>(G, eps, sig, te, ts, c, ca, cb, o);
+}
 
 } // namespace wave

@@ -35,7 +35,8 @@ int psi_axis(int s)
     switch (s) {
     case PS_P_X: case PS_VXX: case PS_SXX_X: case PS_SXY_X: case PS_SXZ_X: case PS_VYX: case PS_VZX:
     case PS_EZX: case PS_HYX: case PS_EYX: case PS_HZX: return 0;
-    case PS_P_Z: case PS_VZZ: case PS_SXZ_Z: case PS_SYZ_Z: case PS_SZZ_Z: case PS_VXZ: case PS_VYZ: return 2;
+    case PS_P_Z: case PS_VZZ: case PS_SXZ_Z: case PS_SYZ_Z: case PS_SZZ_Z: case PS_VXZ: case PS_VYZ:
+    case PS_EYZ: case PS_EXZ: case PS_HYZ: case PS_HXZ: return 2;
     default: return 1;
     }
 }
@@ -110,8 +111,10 @@ std::vector<int> field_list(int eq, bool is3d)
                     : std::vector<int>{F_VX, F_VY, F_SXX, F_SYY, F_SXY};
     case WAVE_EQ_SH:
     case WAVE_EQ_VISCOSH: return {F_VZ, F_SXZ, F_SYZ};
-    case WAVE_EQ_TMEM: return {F_HX, F_HY, F_EZ};
-    case WAVE_EQ_EMEM: return {F_HZ, F_EX, F_EY};
+    case WAVE_EQ_TMEM:
+    case WAVE_EQ_VISCOTMEM: return {F_HX, F_HY, F_EZ};
+    case WAVE_EQ_EMEM:
+    case WAVE_EQ_VISCOEMEM: return is3d ? std::vector<int>{F_HX, F_HY, F_HZ, F_EX, F_EY, F_EZ} : std::vector<int>{F_HZ, F_EX, F_EY};
     default: return {};
     }
 }
@@ -124,8 +127,10 @@ std::vector<int> pass1_list(int eq, bool is3d)
     case WAVE_EQ_VISCOELASTIC: return is3d ? std::vector<int>{F_VX, F_VY, F_VZ} : std::vector<int>{F_VX, F_VY};
     case WAVE_EQ_SH:
     case WAVE_EQ_VISCOSH: return {F_VZ};
-    case WAVE_EQ_TMEM: return {F_HX, F_HY};
-    case WAVE_EQ_EMEM: return {F_HZ};
+    case WAVE_EQ_TMEM:
+    case WAVE_EQ_VISCOTMEM: return {F_HX, F_HY};
+    case WAVE_EQ_EMEM:
+    case WAVE_EQ_VISCOEMEM: return is3d ? std::vector<int>{F_HX, F_HY, F_HZ} : std::vector<int>{F_HZ};
     default: return {};
     }
 }
@@ -134,6 +139,8 @@ std::vector<int> mem_list(int eq, bool is3d)
 {
     if (eq == WAVE_EQ_VISCOELASTIC) return is3d ? std::vector<int>{R_XX, R_YY, R_ZZ, R_XY, R_XZ, R_YZ} : std::vector<int>{R_XX, R_YY, R_XY};
     if (eq == WAVE_EQ_VISCOSH) return {R_XZ, R_YZ};
+    if (eq == WAVE_EQ_VISCOTMEM) return {R_EZ};
+    if (eq == WAVE_EQ_VISCOEMEM) return is3d ? std::vector<int>{R_EX, R_EY, R_EZ} : std::vector<int>{R_EX, R_EY};
     return {};
 }
 
@@ -150,8 +157,13 @@ std::vector<int> psi_list(int eq, bool is3d)
         return {PS_SXX_X, PS_SXY_Y, PS_SXY_X, PS_SYY_Y, PS_VXX, PS_VYY, PS_VXY, PS_VYX};
     case WAVE_EQ_SH:
     case WAVE_EQ_VISCOSH: return {PS_SXZ_X, PS_SYZ_Y, PS_VZX, PS_VZY};
-    case WAVE_EQ_TMEM: return {PS_EZY, PS_EZX, PS_HYX, PS_HXY};
-    case WAVE_EQ_EMEM: return {PS_EYX, PS_EXY, PS_HZY, PS_HZX};
+    case WAVE_EQ_TMEM:
+    case WAVE_EQ_VISCOTMEM: return {PS_EZY, PS_EZX, PS_HYX, PS_HXY};
+    case WAVE_EQ_EMEM:
+    case WAVE_EQ_VISCOEMEM:
+        if (is3d)
+            return {PS_EZY, PS_EYZ, PS_EXZ, PS_EZX, PS_EYX, PS_EXY, PS_HZY, PS_HYZ, PS_HXZ, PS_HZX, PS_HYX, PS_HXY};
+        return {PS_EYX, PS_EXY, PS_HZY, PS_HZX};
     default: return {};
     }
 }
@@ -167,8 +179,12 @@ bool type_ok(int eq, bool is3d, int type, bool source)
     case WAVE_EQ_VISCOELASTIC: return type >= 1 && type <= (is3d ? 4 : 3);
     case WAVE_EQ_SH:
     case WAVE_EQ_VISCOSH: return type == WAVE_TYPE_VZ;
-    case WAVE_EQ_TMEM: return type == WAVE_TYPE_EZ;
-    case WAVE_EQ_EMEM: return type == WAVE_TYPE_EX || type == WAVE_TYPE_EY || type == WAVE_TYPE_HZ;
+    case WAVE_EQ_TMEM:
+    case WAVE_EQ_VISCOTMEM: return type == WAVE_TYPE_EZ;
+    case WAVE_EQ_EMEM:
+    case WAVE_EQ_VISCOEMEM:
+        // SourceReceiverImplEM.cpp:95-110: EZ, EX, EY and HZ; the 2-D TE fields have no EZ
+        return is3d ? (type >= WAVE_TYPE_EZ && type <= WAVE_TYPE_HZ) : (type == WAVE_TYPE_EX || type == WAVE_TYPE_EY || type == WAVE_TYPE_HZ);
     default: return false;
     }
 }
@@ -185,7 +201,7 @@ void launch_pass(wave_handle* h, int pass)
     if (streaming_pass(h, pass)) {
         h->check(el3d_launch(h->el3d, h->sp, pass, h->stream), "streaming kernel launch");
     } else {
-        StepKernel k = kernel_for(h->cfg.equation, pass, h->H);
+        StepKernel k = kernel_for(kernel_eq(h->cfg.equation, h->is3d()), pass, h->H);
         k<<<h->grid, h->block, 0, h->stream>>>(h->sp);
     }
 }
@@ -242,7 +258,7 @@ void tune_passes(wave_handle* h)
         for (int path = 0; path < 2; ++path) {
             auto launch = [&] {
                 if (path) h->check(el3d_launch(h->el3d, h->sp, pass, h->stream), "streaming kernel launch");
-                else kernel_for(h->cfg.equation, pass, h->H)<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+                else kernel_for(kernel_eq(h->cfg.equation, h->is3d()), pass, h->H)<<<h->grid, h->block, 0, h->stream>>>(h->sp);
             };
             for (int k = 0; k < 2; ++k) launch();
             h->check(cudaEventRecord(e0, h->stream), "event");
@@ -351,8 +367,6 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
     // the reference factory's combinations (ForwardSolverFactory.cpp:13-66)
     if (is3d && (c.equation == WAVE_EQ_SH || c.equation == WAVE_EQ_VISCOSH || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_VISCOTMEM))
         return fail(nullptr, WAVE_ERR_UNSUPPORTED, "no 3-D solver for this equation type in the reference factory");
-    if (c.equation == WAVE_EQ_VISCOTMEM || c.equation == WAVE_EQ_VISCOEMEM || (is3d && c.equation == WAVE_EQ_EMEM))
-        return fail(nullptr, WAVE_ERR_UNSUPPORTED, "visco-EM and 3-D EM solvers are not available in this build");
     std::vector<double> coef;
     if (!fd_coefficients(c.spatialFDorder, coef)) return fail(nullptr, WAVE_ERR_ARG, "spatialFDorder = " + std::to_string(c.spatialFDorder) + " Unsupported spatialFDorder value.");
     if (c.NX < 1 || c.NY < 1 || (is3d && c.NZ < 1) || c.DH <= 0 || c.DT <= 0 || c.T <= 0)
@@ -435,6 +449,7 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
         // visco coefficients (ForwardSolver3Dviscoelastic.cpp:56-66)
         P.L = h->L;
         P.DThalf = static_cast<float>(DT / 2.0);
+        P.DT = static_cast<float>(DT);
         for (int l = 0; l < h->L; ++l) {
             const float rt = static_cast<float>(1.0 / (2.0 * M_PI * static_cast<float>(c.relaxationFrequency[l])));
             P.relaxTime[l] = rt;
@@ -565,12 +580,13 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
 int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, const float* mu_r,
                       const float* tau_eps, const float* tau_sigma, size_t n, int mem)
 {
-    (void)tau_eps; (void)tau_sigma;
     if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_model_em: null handle");
     const int eq = h->cfg.equation;
     if (!eq_em(eq)) return fail(h, WAVE_ERR_ARG, "wave_set_model_em: seismic equation, use wave_set_model");
     if (n != static_cast<size_t>(h->N)) return fail(h, WAVE_ERR_ARG, "wave_set_model_em: n != NX*NY*NZ");
     if (!eps_r || !sigma || !mu_r) return fail(h, WAVE_ERR_ARG, "wave_set_model_em: eps_r, sigma and mu_r are required");
+    if ((eq == WAVE_EQ_VISCOTMEM || eq == WAVE_EQ_VISCOEMEM) && (!tau_eps || !tau_sigma))
+        return fail(h, WAVE_ERR_ARG, "wave_set_model_em: visco-EM needs tau_eps and tau_sigma");
     WAVE_TRY(h, {
         PrepParams G{h->NX, h->NY, h->NZ, h->N};
         cudaStream_t s = h->stream;
@@ -589,24 +605,82 @@ int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, co
             tmp.push_back(p);
             return p;
         };
-        // absolute permittivity / permeability (TMEM.cpp:230-241, Modelparameter.hpp:359-360)
+        // absolute permittivity / permeability (TMEM.cpp:230-241, ViscoTMEM.cpp:274-292,
+        // Modelparameter.hpp:359-360)
+        const float eps0 = 8.8541878176e-12f;
         float* eps = scratch();
         float* mu = scratch();
-        k_scale(G, dEr, 8.8541878176e-12f, eps, s);
+        k_scale(G, dEr, eps0, eps, s);
         k_scale(G, dMr, 1.2566370614e-6f, mu, s);
-        if (eq == WAVE_EQ_TMEM) {
-            // TMEM::calculateAveraging (TMEM.cpp:366-374), FD2Dtmem::prepareForModelling (ForwardSolver2Dtmem.cpp:77-106)
+        const bool visco = eq == WAVE_EQ_VISCOTMEM || eq == WAVE_EQ_VISCOEMEM;
+        const bool is3d = h->is3d();
+        const float DTf = static_cast<float>(h->cfg.DT);
+        float *dTe = nullptr, *dTs = nullptr;
+        ViscoEmCoef vc{};
+        if (visco) {
+            // tau_sigma relative to tau_ref = 1/(2 pi f_c) (ViscoTMEM.cpp:285-286); the
+            // solver coefficients of ForwardSolverEM.cpp:68-133
+            dTe = stage(h, tau_eps, n, mem, tmp);
+            float* ts = stage(h, tau_sigma, n, mem, tmp);
+            dTs = scratch();
+            const float tauRef = static_cast<float>(1.0 / (2.0 * M_PI * static_cast<float>(h->cfg.CenterFrequencyCPML)));
+            k_scale(G, ts, tauRef, dTs, s);
+            vc.DT = DTf;
+            vc.eps0 = eps0;
+            vc.L = h->L;
+            float sumInv = 0.0f;
+            for (int l = 0; l < h->L; ++l) {
+                const float rt = h->sp.relaxTime[l];
+                sumInv = static_cast<float>(static_cast<double>(sumInv) + 1.0 / static_cast<double>(rt));
+                const double r = rt;
+                h->sp.Cc[l] = static_cast<float>((1 - 0.5 * static_cast<double>(DTf) / r) / (1 + 0.5 * static_cast<double>(DTf) / r));
+                float tv = static_cast<float>(1 / (1 + 0.5 * static_cast<double>(DTf) / r));
+                tv /= (static_cast<float>(h->L) * rt * rt);
+                vc.cdScale[l] = tv;
+            }
+            vc.sumInv = sumInv / static_cast<float>(h->L);
+        }
+        // Ca/Cb (and C_d) of one E component from its material values
+        auto coeffs = [&](const float* e, const float* sg, const float* te, const float* ts, int ca, int cb, int cd0) {
+            if (!visco) {
+                k_cacb(G, e, sg, DTf, mat(ca), mat(cb), s);
+                return;
+            }
+            float* cd[kMaxL] = {};
+            for (int l = 0; l < h->L; ++l) cd[l] = mat(cd0 + l);
+            k_visco_em(G, e, sg, te, ts, vc, mat(ca), mat(cb), cd, s);
+        };
+        if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_VISCOTMEM) {
+            // TMEM/ViscoTMEM::calculateAveraging (TMEM.cpp:366-374, ViscoTMEM.cpp:442-450),
+            // FD2Dtmem/FD2Dviscotmem::prepareForModelling (ForwardSolver2Dtmem.cpp:77-106,
+            // ForwardSolver2Dviscotmem.cpp:95-124)
             k_inv_avg2(G, mu, 0, mat(M_IMUXZ), s);
             k_inv_avg2(G, mu, 1, mat(M_IMUYZ), s);
-            k_cacb(G, eps, dSig, static_cast<float>(h->cfg.DT), mat(M_CAZ), mat(M_CBZ), s);
+            coeffs(eps, dSig, dTe, dTs, M_CAZ, M_CBZ, M_CDZ0);
         } else {
-            // EMEM::calculateAveraging (EMEM.cpp:378-392), FD2Demem::prepareForModelling (ForwardSolver2Demem.cpp:72-85)
+            // EMEM/ViscoEMEM::calculateAveraging (EMEM.cpp:378-392, ViscoEMEM.cpp:409-432),
+            // prepareForModelling of FD2Demem/FD2Dviscoemem/FD3Demem/FD3Dviscoemem
             k_inv_avg4(G, mu, 0, mat(M_IMUXY), s);
-            float* ex = scratch(); float* sx = scratch(); float* ey = scratch(); float* sy = scratch();
-            k_avg2(G, eps, 0, ex, s); k_avg2(G, dSig, 0, sx, s);
-            k_avg2(G, eps, 1, ey, s); k_avg2(G, dSig, 1, sy, s);
-            k_cacb(G, ex, sx, static_cast<float>(h->cfg.DT), mat(M_CAX), mat(M_CBX), s);
-            k_cacb(G, ey, sy, static_cast<float>(h->cfg.DT), mat(M_CAY), mat(M_CBY), s);
+            if (is3d) {
+                k_inv_avg4(G, mu, 1, mat(M_IMUXZ), s);
+                k_inv_avg4(G, mu, 2, mat(M_IMUYZ), s);
+            }
+            const int naxes = is3d ? 3 : 2;
+            const int caS[3] = {M_CAX, M_CAY, M_CAZ}, cbS[3] = {M_CBX, M_CBY, M_CBZ}, cdS[3] = {M_CDX0, M_CDY0, M_CDZ0};
+            for (int a = 0; a < naxes; ++a) {
+                float* ea = scratch();
+                float* sa = scratch();
+                k_avg2(G, eps, a, ea, s);
+                k_avg2(G, dSig, a, sa, s);
+                float *ta = nullptr, *tsa = nullptr;
+                if (visco) {
+                    ta = scratch();
+                    tsa = scratch();
+                    k_avg2(G, dTe, a, ta, s);
+                    k_avg2(G, dTs, a, tsa, s);
+                }
+                coeffs(ea, sa, ta, tsa, caS[a], cbS[a], cdS[a]);
+            }
         }
         h->check(cudaGetLastError(), "model preparation");
         for (float* p : tmp) cudaFreeAsync(p, s);

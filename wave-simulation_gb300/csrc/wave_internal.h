@@ -63,8 +63,8 @@ enum Mat {
     M_M, M_MU, M_IRX, M_IRY, M_IRZ, M_IR, M_MUXY, M_MUXZ, M_MUYZ,
     M_TAUP, M_TAUS, M_TAUSXY, M_TAUSXZ, M_TAUSYZ, M_OPLTP, M_OPLTS,
     M_CAX, M_CBX, M_CAY, M_CBY, M_CAZ, M_CBZ, M_IMUXY, M_IMUXZ, M_IMUYZ,
-    M_CD0, M_CD1, M_CD2, M_CD3,   // visco-EM Cd per mechanism (x/y/z share for 2-D TM)
-    M_RHO,                        // density, kept for kernels that average it in-kernel
+    M_CDX0, M_CDY0 = M_CDX0 + kMaxL, M_CDZ0 = M_CDY0 + kMaxL,   // visco-EM C_d per E component and mechanism
+    M_RHO = M_CDZ0 + kMaxL,       // density, kept for kernels that average it in-kernel
     M_COUNT
 };
 
@@ -87,6 +87,7 @@ struct StepParams {
     const float* absCoeff;  // BoundaryWidth entries
     int L;
     float scale;            // DT/DH: interior FD taps use compile-time coefficients times this
+    float DT;
     float DThalf;
     float invRelax[kMaxL], c1[kMaxL], c2[kMaxL], Cc[kMaxL], relaxTime[kMaxL];
 };
@@ -113,7 +114,10 @@ struct PrepParams {
     long long N;
 };
 
-// kernel launchers (kernels.cu)
+// kernel launchers (kernels.cu). The kernel tables take the equation code,
+// with kEm3d added for the 3-D EM solvers (FD3Demem, FD3Dviscoemem).
+constexpr int kEm3d = 100;
+inline int kernel_eq(int eq, bool is3d) { return (is3d && eq >= WAVE_EQ_TMEM) ? eq + kEm3d : eq; }
 using StepKernel = void (*)(StepParams);
 StepKernel kernel_for(int eq, int pass, int H);
 void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s);
@@ -134,6 +138,13 @@ void k_harmonic(PrepParams G, const float* invmu, int mode, float* out, cudaStre
 void k_inv_clamped(PrepParams G, const float* mu, float* out, cudaStream_t s);
 void k_one_plus(PrepParams G, const float* tau, float L, float* out, cudaStream_t s);
 void k_scale(PrepParams G, const float* a, float sc, float* out, cudaStream_t s);
+struct ViscoEmCoef {
+    float DT, eps0, sumInv;   // sumInv = (sum_l 1/tau_l) / L
+    int L;
+    float cdScale[kMaxL];     // 1/(1 + DT/(2 tau_l)) / (L tau_l^2)
+};
+void k_visco_em(PrepParams G, const float* eps, const float* sig, const float* te, const float* ts, const ViscoEmCoef& c,
+                float* ca, float* cb, float* const* cd, cudaStream_t s);
 void k_cacb(PrepParams G, const float* eps, const float* sig, float DT, float* ca, float* cb, cudaStream_t s);
 
 // host-side builders (tables.cpp)
