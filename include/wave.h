@@ -220,6 +220,19 @@ int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, 
 int wave_set_kernel_path(wave_handle* h, int path);
 int wave_get_kernel_path(wave_handle* h, int* streaming_active);
 
+/* ---- adjoint gradient (new; the reference's inversion is a separate project) ----
+ * Gradient of J = 1/2 sum over receivers and steps of (d - d_obs)^2 with
+ * respect to vp, vs and rho, by the discrete adjoint of the 2-D elastic time
+ * step (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297) with CPML or no
+ * damping boundary (free surface and ABS: WAVE_ERR_UNSUPPORTED). Runs the
+ * forward over all NT steps from a zero state (the handle's sources and
+ * receivers; seismograms are left as computed), saving the state every
+ * `checkpoint_every` steps, then the backward sweep, recomputing each
+ * checkpoint segment. d_obs: n_receivers x NT (dobs_mem host or device);
+ * grad_*: NX*NY floats each (grad_mem). *misfit receives J. */
+int wave_adjoint_gradient(wave_handle* h, const float* dobs, int dobs_mem, int checkpoint_every, double* misfit,
+                          float* grad_vp, float* grad_vs, float* grad_rho, int grad_mem);
+
 /* ---- batches of shots (the shot parallelism of Simulation.cpp:116-121, 339-369
  *      as one device-wide launch per pass) ---- */
 typedef struct wave_batch wave_batch;

@@ -1,0 +1,137 @@
+"""Adjoint gradient of the 2-D elastic seismogram misfit (wave_adjoint_gradient)
+against central finite differences of the misfit computed with the forward
+solver itself, for vp, vs and rho along smooth perturbation directions; the
+checkpoint interval must not change the result; unsupported set-ups are
+rejected. The reference has no adjoint; the forward it differentiates is
+FD2Delastic::run (ForwardSolver2Delastic.cpp:117-297).
+
+Tolerance: |<g, dm> - (J(m + h dm) - J(m - h dm)) / 2h| <= 2e-2 |FD| (FP32
+forward and adjoint, relative step 1e-3 of the parameter).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+NX, NY, DH = 72, 60, 5.0
+FD_TOL = 2e-2
+
+
+def _blob(cx, cy, s):
+    y, x = np.mgrid[0:NY, 0:NX]
+    return np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2.0 * s * s)).reshape(-1)
+
+
+def _models():
+    y = np.arange(NY)[:, None] * np.ones((1, NX))
+    vp = np.where(y < 25, 2200.0, 2900.0) + 150.0 * (y / NY)
+    vs = vp / 1.75
+    rho = 310.0 * vp ** 0.25
+    true = dict(vp=vp.reshape(-1) * (1 + 0.06 * _blob(36, 32, 5)), vs=vs.reshape(-1) * (1 - 0.05 * _blob(30, 36, 5)),
+                rho=rho.reshape(-1))
+    start = dict(vp=vp.reshape(-1), vs=vs.reshape(-1), rho=rho.reshape(-1))
+    return ({k: v.astype(np.float32) for k, v in true.items()}, {k: v.astype(np.float32) for k, v in start.items()})
+
+
+def _config(wave, order=4, boundary=2, fs=0, stencil=0, dim=2):
+    vmax = 3300.0
+    DT = 0.3 * DH / (vmax * np.sqrt(2) * 1.3)
+    return wave.WaveConfig.make(dimension=dim, equation="elastic", NX=NX, NY=NY, NZ=1 if dim == 2 else 20, DH=DH, DT=DT,
+                                T=420 * DT, spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary,
+                                BoundaryWidth=10, DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=15.0,
+                                VMaxCPML=vmax, useStencilMatrix=stencil)
+
+
+def _acq(wave, cfg, nt):
+    sig = wave.wavelet(1, nt, cfg.DT, 3300.0 / (10 * DH), 1.0, 0.0)
+    sidx = np.array([NX // 2 + NX * 8, 14 + NX * 10], np.int64)
+    stype = np.array([1, 3], np.int32)
+    xs = np.arange(6, NX - 6, 4)
+    ridx = np.concatenate([xs + NX * 6, xs + NX * 6, xs[::3] + NX * 50]).astype(np.int64)
+    rtype = np.concatenate([np.full(xs.size, 2), np.full(xs.size, 3), np.full(xs[::3].size, 1)]).astype(np.int32)
+    return sidx, stype, np.stack([sig, 0.5 * sig]), ridx, rtype
+
+
+def _solver(wave, cfg, model, acq):
+    s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
+    s.prepareForModelling(model)
+    s.setSources(*acq[:3])
+    s.setReceivers(*acq[3:])
+    return s
+
+
+def _misfit(wave, cfg, model, acq, dobs):
+    s = _solver(wave, cfg, model, acq)
+    s.run(0, s.nt)
+    r = s.seismograms().astype(np.float64) - dobs
+    s.close()
+    return 0.5 * float(np.sum(r * r))
+
+
+@pytest.mark.parametrize("order,boundary,stencil", [(4, 2, 0), (8, 2, 0), (2, 0, 1), (6, 2, 1)])
+def test_adjoint_gradient_matches_finite_differences(wave, order, boundary, stencil):
+    cfg = _config(wave, order=order, boundary=boundary, stencil=stencil)
+    true, start = _models()
+    s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
+    nt = s.nt
+    s.close()
+    acq = _acq(wave, cfg, nt)
+    st = _solver(wave, cfg, true, acq)
+    st.run(0, nt)
+    dobs = st.seismograms().astype(np.float64)
+    st.close()
+    sa = _solver(wave, cfg, start, acq)
+    J, gvp, gvs, grho = sa.adjoint_gradient(dobs.astype(np.float32), checkpoint_every=50)
+    sa.close()
+    J0 = _misfit(wave, cfg, start, acq, dobs)
+    assert J > 0 and abs(J - J0) <= 1e-5 * J0
+    dirs = {"vp": _blob(40, 28, 6), "vs": _blob(28, 34, 6), "rho": _blob(34, 40, 6)}
+    grads = {"vp": gvp, "vs": gvs, "rho": grho}
+    for name, d in dirs.items():
+        h = 1e-3 * float(np.mean(start[name]))
+        mp = dict(start); mp[name] = (start[name] + h * d).astype(np.float32)
+        mm = dict(start); mm[name] = (start[name] - h * d).astype(np.float32)
+        # the step actually applied after rounding to FP32
+        dp = (mp[name].astype(np.float64) - mm[name].astype(np.float64)) / 2.0
+        fd = (_misfit(wave, cfg, mp, acq, dobs) - _misfit(wave, cfg, mm, acq, dobs)) / 2.0
+        ad = float(np.dot(grads[name].astype(np.float64), dp))
+        assert abs(fd) > 0
+        assert abs(ad - fd) <= FD_TOL * abs(fd), f"{name}: adjoint {ad:.6e} vs finite difference {fd:.6e}"
+
+
+def test_checkpoint_interval_does_not_change_the_gradient(wave):
+    cfg = _config(wave)
+    true, start = _models()
+    s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
+    nt = s.nt
+    s.close()
+    acq = _acq(wave, cfg, nt)
+    st = _solver(wave, cfg, true, acq)
+    st.run(0, nt)
+    dobs = st.seismograms()
+    st.close()
+    out = []
+    for K in (7, 50, nt + 3):
+        sa = _solver(wave, cfg, start, acq)
+        out.append(sa.adjoint_gradient(dobs, checkpoint_every=K))
+        sa.close()
+    for o in out[1:]:
+        assert o[0] == out[0][0]
+        for a, b in zip(o[1:], out[0][1:]):
+            assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("kw", [dict(fs=1), dict(boundary=1), dict(dim=3)])
+def test_adjoint_rejects_unsupported_setups(wave, kw):
+    cfg = _config(wave, **kw)
+    true, start = _models()
+    dim = kw.get("dim", 2)
+    n = cfg.N
+    model = {k: np.resize(v, n).astype(np.float32) for k, v in start.items()}
+    s = wave.Factory.Create("3D" if dim == 3 else "2D", "elastic").initForwardSolver(cfg)
+    s.prepareForModelling(model)
+    s.setSources(np.array([5], np.int64), np.array([1], np.int32), np.zeros((1, s.nt), np.float32))
+    s.setReceivers(np.array([7], np.int64), np.array([2], np.int32))
+    with pytest.raises(wave.WaveError) as e:
+        s.adjoint_gradient(np.zeros((1, s.nt), np.float32))
+    assert e.value.code == wave.WAVE_ERR_UNSUPPORTED
+    s.close()

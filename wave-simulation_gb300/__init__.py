@@ -40,7 +40,7 @@ ABI_SYMBOLS = (
     "wave_get_kernel_times", "wave_last_error", "wave_wavelet", "wave_set_kernel_path",
     "wave_get_kernel_path", "wave_average_shear_modulus", "wave_batch_create", "wave_batch_destroy",
     "wave_batch_shot", "wave_batch_step", "wave_batch_get_stream", "wave_batch_get_launch_count",
-    "wave_batch_last_error", "wave_average_shear_modulus_noalloc",
+    "wave_batch_last_error", "wave_average_shear_modulus_noalloc", "wave_adjoint_gradient",
 )
 
 
@@ -159,6 +159,7 @@ def lib():
     L.wave_get_kernel_path.argtypes = [P, CP(I)]
     L.wave_average_shear_modulus.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, I]
     L.wave_average_shear_modulus_noalloc.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, P]
+    L.wave_adjoint_gradient.argtypes = [P, P, I, I, ctypes.POINTER(ctypes.c_double), P, P, P, I]
     L.wave_batch_create.argtypes = [P, I, CP(P)]
     L.wave_batch_destroy.argtypes = [P]
     L.wave_batch_shot.argtypes = [P, I, CP(P)]
@@ -321,6 +322,20 @@ class ForwardSolver:
         """0 = automatic (faster kernel per pass, timed when the model is set),
         1 = generic kernels, 2 = streaming TMA kernels wherever they apply."""
         _check(self.h, lib().wave_set_kernel_path(self.h, path))
+
+    def adjoint_gradient(self, dobs, checkpoint_every: int = 50):
+        """Misfit J = 1/2 ||d - d_obs||^2 and its gradient w.r.t. (vp, vs, rho)
+        by the discrete adjoint (2-D elastic). d_obs: n_receivers x NT (numpy
+        or torch cuda). Returns (J, g_vp, g_vs, g_rho) as float64 / numpy arrays."""
+        d = _f32(dobs)
+        pd, mem = _ptr(d)
+        n = self.cfg.N
+        g = [np.zeros(n, dtype=np.float32) for _ in range(3)]
+        J = ctypes.c_double(0.0)
+        _check(self.h, lib().wave_adjoint_gradient(self.h, pd, mem, int(checkpoint_every), ctypes.byref(J),
+                                                    g[0].ctypes.data_as(ctypes.c_void_p), g[1].ctypes.data_as(ctypes.c_void_p),
+                                                    g[2].ctypes.data_as(ctypes.c_void_p), MEM_HOST))
+        return J.value, g[0], g[1], g[2]
 
     def streaming_passes(self) -> int:
         """Bit 0: the velocity pass runs the streaming kernel; bit 1: the stress pass."""

@@ -1,0 +1,567 @@
+// adjoint.cu — gradient of the seismogram misfit J = 1/2 sum (d - d_obs)^2 with
+// respect to vp, vs and rho for the 2-D elastic time step, by the discrete
+// adjoint of the forward step (FD2Delastic::run, ForwardSolver2Delastic.cpp:
+// 117-297) with CPML (CPML.cpp:84-95) and checkpointing.
+//
+// The forward step is linear in the state X = (vx, vy, sxx, syy, sxy, psi):
+//   velocity pass   a_k = D_k sigma,  P_k' = b P_k + a a_k,  a_k' = a_k + P_k',
+//                   vx' = vx + irx (a1' + a2'),  vy' = vy + iry (a3' + a4')
+//   stress pass     c_k = D_k v',     Q_k' = b Q_k + a c_k,  c_k' = c_k + Q_k',
+//                   sxx' = sxx + M (c1' + c2') - 2 mu c2', syy' = syy + M (c1' + c2') - 2 mu c1',
+//                   sxy' = sxy + mu_xy (c3' + c4')
+// plus source terms, and receivers read X after each step. The adjoint runs
+// the transposed pieces backwards (three kernels per step: stress transpose,
+// velocity transpose, stress-derivative transpose) and accumulates
+// dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry, which a last kernel maps to
+// vp, vs, rho through the model preparation (moduli, 2-point inverse density
+// averages, harmonic 4-point shear average with its edge fallbacks and vacuum
+// rules; Modelparameter.cpp:336-639, ModelparameterSeismic.cpp:131-136, 421-432).
+//
+// Checkpointing: the forward run saves the state every K steps; the backward
+// sweep recomputes each K-step segment into a buffer of K+1 states and walks
+// it backwards. The reference has no adjoint (its inversion lives in a
+// separate project); this file has no counterpart there.
+#include <cmath>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "handle.h"
+#include "stencil.cuh"
+
+namespace wave {
+
+// parts of one saved state, in view order
+enum AdjPart { AV_VX, AV_VY, AV_SXX, AV_SYY, AV_SXY, AV_P1, AV_P2, AV_P3, AV_P4, AV_Q1, AV_Q2, AV_Q3, AV_Q4, AV_COUNT };
+
+// psi slot of each psi part: velocity pass P1..P4, stress pass Q1..Q4
+static const int kAdjPsiSlot[8] = {PS_SXX_X, PS_SXY_Y, PS_SXY_X, PS_SYY_Y, PS_VXX, PS_VYY, PS_VXY, PS_VYX};
+
+struct AdjShot {
+    float* view;                 // recompute buffer: K+1 states
+    long long stride;            // floats per state
+    long long off[AV_COUNT];     // part offsets within a state (0 = absent psi)
+    float* lf[5];                // adjoint fields: vx, vy, sxx, syy, sxy
+    float* lpsi[8];              // adjoint psi (slab layout of the forward psi)
+    float* T[8];                 // adjoints of the raw derivatives c1..c4, a1..a4
+    float* g[5];                 // dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry
+    const long long* ridx;
+    const int* rtype;
+    const float* res;            // residual d - d_obs, nrec x nt
+    int nrec, nt;
+};
+
+struct CopyPart {
+    const float* src;
+    float* dst;
+    long long n;
+    long long srcStride, dstStride;   // per state index
+};
+
+namespace {
+
+// (D^T lam)[c] = sum_k w_{c-k}(k) lam[c-k] over the rows c-k inside the axis,
+// with the row weights of deriv(): interior weights or the edge-table row
+template <int H>
+__device__ __forceinline__ float derivT(const float* __restrict__ lam, long long i, long long st, int c, const Op1D& op)
+{
+    float s = 0.0f;
+#pragma unroll
+    for (int k = -H; k <= H; ++k) {
+        const int r = c - k;
+        if (r < 0 || r >= op.n) continue;
+        float w;
+        if (!op.full && r >= op.E && r < op.n - op.E) {
+            w = op.w[kMaxHalf + k];
+        } else {
+            const int slot = op.full ? r : (r < op.E ? r : op.E + r - (op.n - op.E));
+            w = __ldg(op.tab + slot * kTabW + kMaxHalf + k);
+        }
+        if (w != 0.0f) s += w * __ldg(lam + i - k * st);
+    }
+    return s;
+}
+
+// adjoint of (c, Q) -> (c' = (1 + a) c + b Q, Q' = a c + b Q)
+__device__ __forceinline__ void cpml_adj(float& l, float* lpsi, float a, float b)
+{
+    const float lq = *lpsi;
+    const float lc = (1.0f + a) * l + a * lq;
+    *lpsi = b * (l + lq);
+    l = lc;
+}
+
+struct Slabs {
+    int sx, sy;
+    long long px, py;
+};
+
+__device__ __forceinline__ Slabs slabs_of(const StepParams& P, const Pt& p)
+{
+    Slabs S;
+    S.sx = P.useCpml ? slab(p.x, P.cx) : -1;
+    S.sy = P.useCpml ? slab(p.y, P.cy) : -1;
+    S.px = S.sx >= 0 ? pix(P, p, S.sx) : 0;
+    S.py = S.sy >= 0 ? piy(P, p, S.sy) : 0;
+    return S;
+}
+
+// stress-pass transpose at step n (state n = view vn, state n+1 = view vn+1)
+template <int H>
+__device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float *vx1 = X1 + A.off[AV_VX], *vy1 = X1 + A.off[AV_VY];
+    const float M = __ldg(P.m[M_M] + i), mu = __ldg(P.m[M_MU] + i), mxy = __ldg(P.m[M_MUXY] + i);
+    const Slabs S = slabs_of(P, p);
+    // forward derivatives with their CPML correction, c' = c + Q_{n+1}
+    float c1 = deriv<H, false>(vx1, i, 1, p.x, P.Dxb);
+    float c2 = deriv<H, false>(vy1, i, sy, p.y, P.Dyb);
+    float c3 = deriv<H, true>(vx1, i, sy, p.y, P.Dyf);
+    float c4 = deriv<H, true>(vy1, i, 1, p.x, P.Dxf);
+    if (S.sx >= 0) { c1 += X1[A.off[AV_Q1] + S.px]; c4 += X1[A.off[AV_Q4] + S.px]; }
+    if (S.sy >= 0) { c2 += X1[A.off[AV_Q2] + S.py]; c3 += X1[A.off[AV_Q3] + S.py]; }
+    const float lxx = A.lf[2][i], lyy = A.lf[3][i], lxy = A.lf[4][i];
+    const float lam = M - 2.0f * mu;
+    float l1 = M * lxx + lam * lyy;
+    float l2 = lam * lxx + M * lyy;
+    float l3 = mxy * lxy, l4 = l3;
+    if (S.sx >= 0) {
+        cpml_adj(l1, A.lpsi[4] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // Q1 (vxx): x, full profile
+        cpml_adj(l4, A.lpsi[7] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // Q4 (vyx): x, half profile
+    }
+    if (S.sy >= 0) {
+        cpml_adj(l2, A.lpsi[5] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // Q2 (vyy): y, full profile
+        cpml_adj(l3, A.lpsi[6] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // Q3 (vxy): y, half profile
+    }
+    A.T[0][i] = l1;
+    A.T[1][i] = l2;
+    A.T[2][i] = l3;
+    A.T[3][i] = l4;
+    A.g[0][i] += (lxx + lyy) * (c1 + c2);
+    A.g[1][i] += -2.0f * (lxx * c2 + lyy * c1);
+    A.g[2][i] += lxy * (c3 + c4);
+}
+
+// velocity-pass transpose (and the transposed stress-pass derivatives of v)
+template <int H>
+__device__ __forceinline__ void adj_vel_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    float lvx = A.lf[0][i];
+    lvx += derivT<H>(A.T[0], i, 1, p.x, P.Dxb);
+    lvx += derivT<H>(A.T[2], i, sy, p.y, P.Dyf);
+    float lvy = A.lf[1][i];
+    lvy += derivT<H>(A.T[1], i, sy, p.y, P.Dyb);
+    lvy += derivT<H>(A.T[3], i, 1, p.x, P.Dxf);
+    const Slabs S = slabs_of(P, p);
+    const float *sxx = X0 + A.off[AV_SXX], *syy = X0 + A.off[AV_SYY], *sxy = X0 + A.off[AV_SXY];
+    float a1 = deriv<H, true>(sxx, i, 1, p.x, P.Dxf);
+    float a2 = deriv<H, false>(sxy, i, sy, p.y, P.Dyb);
+    float a3 = deriv<H, false>(sxy, i, 1, p.x, P.Dxb);
+    float a4 = deriv<H, true>(syy, i, sy, p.y, P.Dyf);
+    if (S.sx >= 0) { a1 += X1[A.off[AV_P1] + S.px]; a3 += X1[A.off[AV_P3] + S.px]; }
+    if (S.sy >= 0) { a2 += X1[A.off[AV_P2] + S.py]; a4 += X1[A.off[AV_P4] + S.py]; }
+    const float irx = __ldg(P.m[M_IRX] + i), iry = __ldg(P.m[M_IRY] + i);
+    float l1 = irx * lvx, l2 = l1, l3 = iry * lvy, l4 = l3;
+    if (S.sx >= 0) {
+        cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // P1 (sxx_x): x, half profile
+        cpml_adj(l3, A.lpsi[2] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // P3 (sxy_x): x, full profile
+    }
+    if (S.sy >= 0) {
+        cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // P2 (sxy_y): y, full profile
+        cpml_adj(l4, A.lpsi[3] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // P4 (syy_y): y, half profile
+    }
+    A.T[4][i] = l1;
+    A.T[5][i] = l2;
+    A.T[6][i] = l3;
+    A.T[7][i] = l4;
+    A.lf[0][i] = lvx;
+    A.lf[1][i] = lvy;
+    A.g[3][i] += lvx * (a1 + a2);
+    A.g[4][i] += lvy * (a3 + a4);
+}
+
+// transposed velocity-pass derivatives of sigma
+template <int H>
+__device__ __forceinline__ void adj_sigma_body(const StepParams& P, const AdjShot& A, const Pt& p)
+{
+    const long long i = p.i, sy = P.NX;
+    A.lf[2][i] += derivT<H>(A.T[4], i, 1, p.x, P.Dxf);
+    float u = derivT<H>(A.T[5], i, sy, p.y, P.Dyb);
+    u += derivT<H>(A.T[6], i, 1, p.x, P.Dxb);
+    A.lf[4][i] += u;
+    A.lf[3][i] += derivT<H>(A.T[7], i, sy, p.y, P.Dyf);
+}
+
+template <int H, int PASS>
+__global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
+                                                const BatchTile* __restrict__ W, int vn)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    Pt p;
+    if (!point_tile(sP, w, p)) return;
+    const AdjShot& A = As[w.shot];
+    if (PASS == 0) adj_stress_body<H>(sP, A, p, vn);
+    else if (PASS == 1) adj_vel_body<H>(sP, A, p, vn);
+    else adj_sigma_body<H>(sP, A, p);
+}
+
+// residual of step n at the receivers into the adjoint state (transposed gather;
+// a pressure trace is (sxx + syy) / 2, FDTD2Delastic.cpp:12-49)
+__global__ void adj_inject(const AdjShot* __restrict__ As, int n)
+{
+    const AdjShot& A = As[blockIdx.x];
+    for (int r = threadIdx.x; r < A.nrec; r += blockDim.x) {
+        const float v = A.res[(long long)r * A.nt + n];
+        const long long i = A.ridx[r];
+        switch (A.rtype[r]) {
+        case WAVE_TYPE_P:
+            atomicAdd(A.lf[2] + i, 0.5f * v);
+            atomicAdd(A.lf[3] + i, 0.5f * v);
+            break;
+        case WAVE_TYPE_VX: atomicAdd(A.lf[0] + i, v); break;
+        default: atomicAdd(A.lf[1] + i, v); break;
+        }
+    }
+}
+
+__global__ void copy_parts(const CopyPart* __restrict__ parts, long long srcIdx, long long dstIdx)
+{
+    const CopyPart c = parts[blockIdx.y];
+    const float* s = c.src + srcIdx * c.srcStride;
+    float* d = c.dst + dstIdx * c.dstStride;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < c.n; k += (long long)gridDim.x * blockDim.x) d[k] = s[k];
+}
+
+__global__ void residual_kernel(const float* __restrict__ seis, const float* __restrict__ dobs, float* res, long long n, double* misfit)
+{
+    double acc = 0.0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const float r = seis[k] - dobs[k];
+        res[k] = r;
+        acc += 0.5 * static_cast<double>(r) * static_cast<double>(r);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(misfit, acc);
+}
+
+// weight of point (kx, ky) in the 4-point XY average row at (x, y), with the
+// edge fallbacks of calc4PointAverageMatrixRow (Modelparameter.cpp:448-527)
+__device__ __forceinline__ float w4(int x, int y, int kx, int ky, int NX, int NY)
+{
+    const bool inX = x + 1 < NX, inY = y + 1 < NY;
+    const bool mx = kx == x || kx == x + 1, my = ky == y || ky == y + 1;
+    if (inX && inY) return (mx && my) ? 0.25f : 0.0f;
+    if (inX) return (ky == y && mx) ? 0.5f : 0.0f;
+    if (inY) return (kx == x && my) ? 0.5f : 0.0f;
+    return (kx == x && ky == y) ? 1.0f : 0.0f;
+}
+
+// chain rule from the prepared materials to vp, vs, rho (2-D elastic):
+// M = rho vp^2; mu = max(rho vs^2, 1); mu_xy = 1 / sum_k w_k / mu_k (0 below 4);
+// irx = 1 / (2-point average of rho along x), iry along y (0 where invalid)
+__global__ void adj_grad_final(PrepParams G, const StepParams P, const AdjShot A, float* gvp, float* gvs, float* grho, int accumulate)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
+        const int kx = static_cast<int>(k % G.NX), ky = static_cast<int>(k / G.NX);
+        const float rho = P.m[M_RHO][k], vp = P.m[M_VP][k], vs = P.m[M_VS][k];
+        const float muk = P.m[M_MU][k];
+        float gmu = A.g[1][k];
+        for (int dy = 0; dy <= 1; ++dy)
+            for (int dx = 0; dx <= 1; ++dx) {
+                const int x = kx - dx, y = ky - dy;
+                if (x < 0 || y < 0) continue;
+                const long long r = x + (long long)G.NX * y;
+                const float mxy = P.m[M_MUXY][r];
+                if (mxy == 0.0f) continue;
+                const float w = w4(x, y, kx, ky, G.NX, G.NY);
+                if (w != 0.0f) gmu += A.g[2][r] * w * (mxy / muk) * (mxy / muk);
+            }
+        const bool unclamped = rho * vs * vs >= 1.0f;
+        float gr = A.g[0][k] * vp * vp;
+        if (unclamped) gr += gmu * vs * vs;
+        // inverse density averages: rows (kx, ky) and (kx-1, ky) along x, (kx, ky-1) along y
+        for (int d = 0; d <= 1; ++d) {
+            if (kx - d >= 0) {
+                const long long r = k - d;
+                const float ir = P.m[M_IRX][r];
+                const float w = (kx - d + 1 < G.NX) ? 0.5f : 1.0f;
+                if (ir != 0.0f && (d == 0 || w == 0.5f)) gr -= A.g[3][r] * ir * ir * w;
+            }
+            if (ky - d >= 0) {
+                const long long r = k - d * (long long)G.NX;
+                const float ir = P.m[M_IRY][r];
+                const float w = (ky - d + 1 < G.NY) ? 0.5f : 1.0f;
+                if (ir != 0.0f && (d == 0 || w == 0.5f)) gr -= A.g[4][r] * ir * ir * w;
+            }
+        }
+        const float gp = A.g[0][k] * 2.0f * rho * vp;
+        const float gs = unclamped ? gmu * 2.0f * rho * vs : 0.0f;
+        if (accumulate) { gvp[k] += gp; gvs[k] += gs; grho[k] += gr; }
+        else { gvp[k] = gp; gvs[k] = gs; grho[k] = gr; }
+    }
+}
+
+template <int H>
+void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, int ntiles, int vn, cudaStream_t s)
+{
+    const dim3 block(32, 8, 1);
+    if (pass == 0) adj_pass<H, 0><<<ntiles, block, 0, s>>>(Ps, As, W, vn);
+    else if (pass == 1) adj_pass<H, 1><<<ntiles, block, 0, s>>>(Ps, As, W, vn);
+    else adj_pass<H, 2><<<ntiles, block, 0, s>>>(Ps, As, W, vn);
+}
+
+void launch_adj(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, int ntiles, int vn, cudaStream_t s)
+{
+    switch (H) {
+    case 1: launch_adj_h<1>(pass, Ps, As, W, ntiles, vn, s); break;
+    case 2: launch_adj_h<2>(pass, Ps, As, W, ntiles, vn, s); break;
+    case 3: launch_adj_h<3>(pass, Ps, As, W, ntiles, vn, s); break;
+    case 4: launch_adj_h<4>(pass, Ps, As, W, ntiles, vn, s); break;
+    case 5: launch_adj_h<5>(pass, Ps, As, W, ntiles, vn, s); break;
+    default: launch_adj_h<6>(pass, Ps, As, W, ntiles, vn, s); break;
+    }
+}
+
+void ck(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// device allocations of one adjoint run, freed on scope exit
+struct DevPool {
+    std::vector<void*> ptrs;
+    cudaStream_t s = nullptr;
+    template <class T>
+    T* get(size_t n)
+    {
+        void* p = nullptr;
+        ck(cudaMallocAsync(&p, (n > 0 ? n : 1) * sizeof(T), s), "cudaMallocAsync");
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    ~DevPool()
+    {
+        for (void* p : ptrs) cudaFreeAsync(p, s);
+        if (s) cudaStreamSynchronize(s);
+    }
+};
+
+} // namespace
+
+// Checks that a handle can run the adjoint; returns an error message or "".
+std::string adjoint_supported(const wave_handle* h)
+{
+    const wave_config& c = h->cfg;
+    if (c.dimension != 2 || c.equation != WAVE_EQ_ELASTIC) return "the adjoint gradient is implemented for 2-D elastic modelling";
+    if (c.FreeSurface != 0) return "the adjoint gradient does not support the free surface";
+    if (c.DampingBoundary == 1) return "the adjoint gradient supports CPML or no damping boundary, not ABS";
+    if (!h->modelSet) return "set the model first";
+    if (!h->seis || h->nrec < 1) return "set receivers first";
+    return "";
+}
+
+struct AdjStepper {
+    cudaStream_t stream;
+    std::function<void(int)> set_counter;   // every shot's step counter to n
+    std::function<void()> step;             // one forward step of every shot
+};
+
+// Runs forward + checkpoints, residuals, and the backward sweep for the shots.
+// dobs[s] and the gradient outputs are device pointers; with `sum` the
+// gradients of all shots are added into output 0.
+void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, const float* const* dobs, int K, double* misfit,
+                 float* const* gvp, float* const* gvs, float* const* grho, bool sum)
+{
+    const int ns = static_cast<int>(shots.size());
+    const int NT = shots[0]->NT;
+    const int H = shots[0]->H;
+    cudaStream_t st = S.stream;
+    DevPool pool;
+    pool.s = st;
+    std::vector<AdjShot> A(ns);
+    std::vector<StepParams> Ps(ns);
+    std::vector<CopyPart> toView, toCkpt, fromCkpt;
+    std::vector<BatchTile> tiles;
+    std::vector<float*> ckpt(ns);
+    std::vector<long long> stride(ns);
+    const int nck = (NT + K - 1) / K;
+    double* dMisfit = pool.get<double>(ns);
+    ck(cudaMemsetAsync(dMisfit, 0, ns * sizeof(double), st), "memset");
+    for (int s = 0; s < ns; ++s) {
+        wave_handle* h = shots[s];
+        const long long N = h->N;
+        // state layout: 5 fields then the 8 psi arrays (absent psi: length 0)
+        long long off[AV_COUNT], len[AV_COUNT], o = 0;
+        const int fields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
+        for (int k = 0; k < 5; ++k) { off[k] = o; len[k] = N; o += N; }
+        for (int k = 0; k < 8; ++k) {
+            const int slot = kAdjPsiSlot[k];
+            off[5 + k] = o;
+            len[5 + k] = h->psi[slot] ? h->psiLen[slot] : 0;
+            o += len[5 + k];
+        }
+        stride[s] = o;
+        AdjShot& a = A[s];
+        a.view = pool.get<float>(static_cast<size_t>(o) * (K + 1));
+        a.stride = o;
+        for (int k = 0; k < AV_COUNT; ++k) a.off[k] = off[k];
+        float* lstate = pool.get<float>(o);
+        ck(cudaMemsetAsync(lstate, 0, o * sizeof(float), st), "memset");
+        for (int k = 0; k < 5; ++k) a.lf[k] = lstate + off[k];
+        for (int k = 0; k < 8; ++k) a.lpsi[k] = lstate + off[5 + k];
+        float* temps = pool.get<float>(8 * N);
+        for (int k = 0; k < 8; ++k) a.T[k] = temps + k * N;
+        float* grads = pool.get<float>(5 * N);
+        ck(cudaMemsetAsync(grads, 0, 5 * N * sizeof(float), st), "memset");
+        for (int k = 0; k < 5; ++k) a.g[k] = grads + k * N;
+        a.ridx = h->ridx;
+        a.rtype = h->rtype;
+        a.nrec = h->nrec;
+        a.nt = NT;
+        float* res = pool.get<float>(static_cast<size_t>(h->nrec) * NT);
+        a.res = res;
+        ckpt[s] = pool.get<float>(static_cast<size_t>(o) * nck);
+        for (int k = 0; k < AV_COUNT; ++k) {
+            if (len[k] == 0) continue;
+            float* live = k < 5 ? h->f[fields[k]] : h->psi[kAdjPsiSlot[k - 5]];
+            toView.push_back({live, a.view + off[k], len[k], 0, o});
+            toCkpt.push_back({live, ckpt[s] + off[k], len[k], 0, o});
+            fromCkpt.push_back({ckpt[s] + off[k], live, len[k], o, 0});
+        }
+        Ps[s] = h->sp;
+        const int rows = h->NY * h->NZ;
+        for (int r0 = 0; r0 < rows; r0 += 8)
+            for (int x0 = 0; x0 < h->NX; x0 += 32) tiles.push_back({s, x0, r0, 0});
+    }
+    auto upload = [&](auto& v) {
+        using T = typename std::decay_t<decltype(v)>::value_type;
+        T* d = pool.get<T>(v.size());
+        ck(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+        return d;
+    };
+    const StepParams* dP = upload(Ps);
+    const AdjShot* dA = upload(A);
+    const BatchTile* dT = upload(tiles);
+    const CopyPart* dToView = upload(toView);
+    const CopyPart* dToCkpt = upload(toCkpt);
+    const CopyPart* dFromCkpt = upload(fromCkpt);
+    const int ntiles = static_cast<int>(tiles.size());
+    const dim3 cgrid(64, 1, 1);
+    auto copy = [&](const CopyPart* parts, size_t nparts, long long si, long long di) {
+        copy_parts<<<dim3(cgrid.x, static_cast<unsigned>(nparts), 1), 256, 0, st>>>(parts, si, di);
+    };
+    // the shots' own streams may still hold work: order them before this run
+    for (auto* h : shots) ck(cudaStreamSynchronize(h->stream), "shot sync");
+
+    // 1. forward with checkpoints (state zeroed first)
+    for (auto* h : shots) {
+        for (int f : h->fields) ck(cudaMemsetAsync(h->f[f], 0, h->N * sizeof(float), st), "memset");
+        for (int k = 0; k < PS_COUNT; ++k)
+            if (h->psi[k]) ck(cudaMemsetAsync(h->psi[k], 0, h->psiLen[k] * sizeof(float), st), "memset");
+        ck(cudaMemsetAsync(h->seis, 0, static_cast<size_t>(h->nrec) * NT * sizeof(float), st), "memset");
+    }
+    S.set_counter(0);
+    for (int n = 0; n < NT; ++n) {
+        if (n % K == 0) copy(dToCkpt, toCkpt.size(), 0, n / K);
+        S.step();
+    }
+    // 2. residuals and misfits
+    for (int s = 0; s < ns; ++s) {
+        const long long n = static_cast<long long>(shots[s]->nrec) * NT;
+        residual_kernel<<<256, 256, 0, st>>>(shots[s]->seis, dobs[s], const_cast<float*>(A[s].res), n, dMisfit + s);
+    }
+    // 3. backward sweep over the checkpoint segments
+    for (int seg = nck - 1; seg >= 0; --seg) {
+        const int n0 = seg * K, n1 = n0 + K < NT ? n0 + K : NT;
+        copy(dFromCkpt, fromCkpt.size(), seg, 0);
+        copy(dToView, toView.size(), 0, 0);
+        S.set_counter(n0);
+        for (int n = n0; n < n1; ++n) {
+            S.step();
+            copy(dToView, toView.size(), 0, n - n0 + 1);
+        }
+        for (int n = n1 - 1; n >= n0; --n) {
+            adj_inject<<<ns, 256, 0, st>>>(dA, n);
+            launch_adj(H, 0, dP, dA, dT, ntiles, n - n0, st);
+            launch_adj(H, 1, dP, dA, dT, ntiles, n - n0, st);
+            launch_adj(H, 2, dP, dA, dT, ntiles, n - n0, st);
+        }
+        ck(cudaGetLastError(), "adjoint launch");
+    }
+    // 4. chain rule to vp, vs, rho
+    for (int s = 0; s < ns; ++s) {
+        wave_handle* h = shots[s];
+        PrepParams G{h->NX, h->NY, h->NZ, h->N};
+        const int o = sum ? 0 : s;
+        adj_grad_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
+    }
+    ck(cudaGetLastError(), "gradient launch");
+    ck(cudaMemcpyAsync(misfit, dMisfit, ns * sizeof(double), cudaMemcpyDeviceToHost, st), "misfit copy");
+    ck(cudaStreamSynchronize(st), "adjoint");
+    for (auto* h : shots) h->stepsSinceReset = NT;
+}
+
+} // namespace wave
+
+using namespace wave;
+
+extern "C" int wave_adjoint_gradient(wave_handle* h, const float* dobs, int dobs_mem, int checkpoint_every, double* misfit,
+                                     float* grad_vp, float* grad_vs, float* grad_rho, int grad_mem)
+{
+    if (!h) return WAVE_ERR_ARG;
+    if (!dobs || !misfit || !grad_vp || !grad_vs || !grad_rho || checkpoint_every < 1) {
+        h->err = "wave_adjoint_gradient: invalid argument";
+        return WAVE_ERR_ARG;
+    }
+    const std::string why = adjoint_supported(h);
+    if (!why.empty()) {
+        h->err = "wave_adjoint_gradient: " + why;
+        return WAVE_ERR_UNSUPPORTED;
+    }
+    try {
+        const size_t nd = static_cast<size_t>(h->nrec) * h->NT;
+        const size_t N = static_cast<size_t>(h->N);
+        std::vector<void*> tmp;
+        auto dev = [&](size_t n) {
+            void* p = nullptr;
+            ck(cudaMalloc(&p, n * sizeof(float)), "cudaMalloc");
+            tmp.push_back(p);
+            return static_cast<float*>(p);
+        };
+        struct Free {
+            std::vector<void*>& v;
+            ~Free() { for (void* p : v) cudaFree(p); }
+        } freeTmp{tmp};
+        const float* dDobs = dobs;
+        if (dobs_mem != WAVE_MEM_DEVICE) {
+            float* d = dev(nd);
+            ck(cudaMemcpy(d, dobs, nd * sizeof(float), cudaMemcpyHostToDevice), "dobs upload");
+            dDobs = d;
+        }
+        float* out[3] = {grad_vp, grad_vs, grad_rho};
+        float* dOut[3];
+        for (int k = 0; k < 3; ++k) dOut[k] = grad_mem == WAVE_MEM_DEVICE ? out[k] : dev(N);
+        AdjStepper S;
+        S.stream = h->stream;
+        S.set_counter = [h](int n) { launch_set_counter(h->tcounter, n, h->stream); };
+        S.step = [h]() { step_once(h); };
+        adjoint_run({h}, S, &dDobs, checkpoint_every, misfit, &dOut[0], &dOut[1], &dOut[2], false);
+        if (grad_mem != WAVE_MEM_DEVICE)
+            for (int k = 0; k < 3; ++k) ck(cudaMemcpy(out[k], dOut[k], N * sizeof(float), cudaMemcpyDeviceToHost), "gradient copy");
+    } catch (std::exception& e) {
+        h->err = std::string("wave_adjoint_gradient: ") + e.what();
+        return WAVE_ERR_CUDA;
+    }
+    return WAVE_OK;
+}

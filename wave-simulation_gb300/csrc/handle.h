@@ -87,3 +87,8 @@ struct wave_handle {
     }
 };
 
+
+namespace wave {
+// one forward time step of a handle on its stream (solver.cu)
+void step_once(wave_handle* h);
+} // namespace wave

@@ -325,6 +325,9 @@ std::vector<std::pair<void*, size_t>> state_parts(wave_handle* h)
 
 } // namespace
 
+void wave::step_once(wave_handle* h) { launch_step(h); }
+
+
 extern "C" {
 
 const char* wave_last_error(const wave_handle* h)
@@ -522,6 +525,10 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
             }
         }
         h->check(cudaMemcpyAsync(mat(M_RHO), dRho, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+        if (eq == WAVE_EQ_ELASTIC && !is3d) {
+            h->check(cudaMemcpyAsync(mat(M_VP), dVp, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+            h->check(cudaMemcpyAsync(mat(M_VS), dVs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+        }
         if (needVp) k_modulus(G, dRho, dVp, dTp, sum, 0, mat(M_M), s);
         if (needVs) k_modulus(G, dRho, dVs, visco ? dTs : nullptr, sum, 1, mat(M_MU), s);
         if (eq == WAVE_EQ_SH || eq == WAVE_EQ_VISCOSH) {
