@@ -702,6 +702,114 @@ def run_tmem_batch(args, wave):
           {"plain_value": plain, "batched_over_plain": value / plain})
 
 
+# ---- config 5: 2-D elastic FWI gradient, 32 shots ---------------------------
+FWI_KW = dict(dimension=2, equation="elastic", NX=600, NY=300, NZ=1, DH=5.0, DT=5e-4, T=2.0, spatialFDorder=4,
+              FreeSurface=0, DampingBoundary=2, BoundaryWidth=20, NPower=4.0, CenterFrequencyCPML=10.0, VMaxCPML=4400.0,
+              useStencilMatrix=0, edgeOrderReduction=1)
+
+
+def fwi_models(NX, NY):
+    """True model: 6 layers, vp 1800 -> 4000 with depth, vs = vp/1.73, rho = 310 vp^0.25,
+    Gaussian anomalies +-10 % on vp and vs (sigma 15 cells) at (200, 120) and
+    (400, 180); start model = true smoothed by a Gaussian of 10 cells."""
+    from scipy.ndimage import gaussian_filter
+    y, x = np.mgrid[0:NY, 0:NX]
+    layer = np.minimum(y * 6 // NY, 5)
+    vp = 1800.0 + (4000.0 - 1800.0) * layer / 5.0
+    blob = lambda cx, cy: np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * 15.0 ** 2))
+    pert = 0.10 * blob(200, 120) - 0.10 * blob(400, 180)
+    vpt = vp * (1 + pert)
+    vst = vp / 1.73 * (1 + pert)
+    true = dict(vp=vpt, vs=vst, rho=310.0 * vpt ** 0.25)
+    start = {k: gaussian_filter(v, 10.0, mode="nearest") for k, v in true.items()}
+    f = lambda d: {k: v.astype(np.float32).reshape(-1) for k, v in d.items()}
+    return f(true), f(start)
+
+
+def fwi_acq(NX, k, nt, dt):
+    from oracle.refcpu import ricker
+    sidx = np.array([30 + 17 * k + NX * 10], np.int64)
+    sig = ricker(nt, dt, 10.0, 1.0, 0.0, np.float32)[None, :]
+    xs = 30 + 4 * np.arange(136)
+    ridx = np.concatenate([xs + NX * 10, xs + NX * 10]).astype(np.int64)
+    rtype = np.concatenate([np.full(136, 2), np.full(136, 3)]).astype(np.int32)
+    return sidx, np.array([1], np.int32), sig, ridx, rtype
+
+
+def run_fwi2d(args, wave):
+    import torch
+    nshots = min(args.shots, 32)
+    cfg = wave.WaveConfig.make(**FWI_KW)
+    NX, NY = 600, 300
+    true, start = fwi_models(NX, NY)
+    K = 50
+    # observed data: the FP32 forward on the true model, one shot at a time
+    dobs, acqs = [], []
+    for k in range(nshots):
+        s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
+        acq = fwi_acq(NX, k, s.nt, cfg.DT)
+        s.prepareForModelling(true)
+        s.setSources(*acq[:3])
+        s.setReceivers(*acq[3:])
+        s.run(0, s.nt)
+        dobs.append(s.seismograms())
+        acqs.append(acq)
+        nt = s.nt
+        s.close()
+    # plain: one shot-gradient at a time through the single-handle entry point
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_grad = None
+    misfit_plain = 0.0
+    for k in range(nshots):
+        s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
+        s.prepareForModelling(start)
+        s.setSources(*acqs[k][:3])
+        s.setReceivers(*acqs[k][3:])
+        J, gvp, gvs, grho = s.adjoint_gradient(dobs[k], checkpoint_every=K)
+        misfit_plain += J
+        plain_grad = gvp.astype(np.float64) if plain_grad is None else plain_grad + gvp
+        s.close()
+    plain_s = time.perf_counter() - t0
+    # batched: all shots in every launch, gradients summed on the device
+    b = wave.Batch([cfg] * nshots)
+    for shot, acq in zip(b.shots, acqs):
+        shot.prepareForModelling(start)
+        shot.setSources(*acq[:3])
+        shot.setReceivers(*acq[3:])
+    b.run(0, 3)                                            # warm-up launches
+    l0 = b.launch_count()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mis, bvp, bvs, brho = b.adjoint_gradient(dobs, checkpoint_every=K, sum_shots=True)
+        torch.cuda.synchronize()
+        batch_s = time.perf_counter() - t0
+    # forward steps counted by the batch plus the adjoint driver's own launches (per step: view copy,
+    # residual injection, three adjoint passes; per segment: two state copies; per shot: residual, chain rule)
+    launches = (b.launch_count() - l0) + 5 * nt + 2 * ((nt + K - 1) // K) + 2 * nshots
+    b.close()
+    rel = float(np.linalg.norm(bvp - plain_grad) / np.linalg.norm(plain_grad))
+    value = nshots / batch_s
+    plain = nshots / plain_s
+    n = NX * NY
+    # algorithmic bytes per shot-step: forward 52 + recompute 72 + adjoint/imaging 96 B/pt
+    alg = 220 * n * nt * nshots
+    h2d = sum(d.nbytes for d in dobs) + sum(a.nbytes for acq in acqs for a in acq)
+    line_cfg = {"workload": f"2-D elastic FWI gradient 600x300 order 4, 20-pt CPML, DT=5e-4, NT={nt}, {nshots} shots, "
+                            f"136 two-component receivers, checkpoints every {K} steps",
+                "shots": nshots, "grid": [NX, NY], "order": 4, "checkpoint_every": K, "parallelism": "1 GPU",
+                "l2": "inputs larger than L2 over a shot-gradient (recompute buffers 51 states x 32 shots)"}
+    ms_grad = batch_s * 1e3 / nshots
+    roof = _roof(alg / nshots, ms_grad, "elastic_v/s_batch<2> + adj_pass<2> (batched)",
+                 "220 B/pt per shot-step (forward 52, recompute 72, adjoint+imaging 96)")
+    _line("shot-gradients/s", value, nshots, 1, ms_grad, line_cfg, roof,
+          {"value": value, "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d / nshots, "d2h_bytes_per_step": 3 * n * 4},
+          launches, clk.summary(), None,
+          {"unit": "shot-gradients/s", "plain_value": plain, "batched_over_plain": value / plain,
+           "misfit": float(sum(mis)), "misfit_plain": misfit_plain, "batched_vs_plain_grad_rel_l2": rel})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -712,7 +820,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube edge (profiling captures use a smaller cube)")
-    ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch"])
+    ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch", "fwi2d"])
     ap.add_argument("--shots", type=int, default=128, help="shots of the batched EM workload")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -720,7 +828,8 @@ def main():
     if args.workload != "elastic3d":
         import __graft_entry__ as g
         wave = g.load_package()
-        {"acoustic2d": run_acoustic2d, "visco3d": run_visco3d, "tmem_batch": run_tmem_batch}[args.workload](args, wave)
+        {"acoustic2d": run_acoustic2d, "visco3d": run_visco3d, "tmem_batch": run_tmem_batch,
+         "fwi2d": run_fwi2d}[args.workload](args, wave)
         return
     if args.grid != 256:
         set_grid(args.grid)

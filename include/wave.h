@@ -249,6 +249,12 @@ int wave_batch_shot(wave_batch* b, int shot, wave_handle** h);
  * over all shots' tiles and one source/receiver launch; multi-step calls
  * replay a captured CUDA graph. Returns after the steps completed. */
 int wave_batch_step(wave_batch* b, int t_begin, int t_end);
+/* Adjoint gradients of all shots of a batch (wave_adjoint_gradient per shot,
+ * every launch covering all shots). dobs[s]: n_receivers(s) x NT; misfits[s]
+ * receives shot s's J; with sum_shots = 1 (shots on one grid) the gradients of
+ * all shots are summed into grad_*[0], else grad_*[s] receive shot s's. */
+int wave_batch_adjoint_gradient(wave_batch* b, const float* const* dobs, int dobs_mem, int checkpoint_every, double* misfits,
+                                float* const* grad_vp, float* const* grad_vs, float* const* grad_rho, int grad_mem, int sum_shots);
 int wave_batch_get_stream(wave_batch* b, void** stream);
 int wave_batch_get_launch_count(wave_batch* b, long long* count);
 const char* wave_batch_last_error(const wave_batch* b);

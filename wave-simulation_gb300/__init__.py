@@ -41,6 +41,7 @@ ABI_SYMBOLS = (
     "wave_get_kernel_path", "wave_average_shear_modulus", "wave_batch_create", "wave_batch_destroy",
     "wave_batch_shot", "wave_batch_step", "wave_batch_get_stream", "wave_batch_get_launch_count",
     "wave_batch_last_error", "wave_average_shear_modulus_noalloc", "wave_adjoint_gradient",
+    "wave_batch_adjoint_gradient",
 )
 
 
@@ -160,6 +161,7 @@ def lib():
     L.wave_average_shear_modulus.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, I]
     L.wave_average_shear_modulus_noalloc.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, P]
     L.wave_adjoint_gradient.argtypes = [P, P, I, I, ctypes.POINTER(ctypes.c_double), P, P, P, I]
+    L.wave_batch_adjoint_gradient.argtypes = [P, P, I, I, ctypes.POINTER(ctypes.c_double), P, P, P, I, I]
     L.wave_batch_create.argtypes = [P, I, CP(P)]
     L.wave_batch_destroy.argtypes = [P]
     L.wave_batch_shot.argtypes = [P, I, CP(P)]
@@ -409,6 +411,26 @@ class Batch:
 
     def run(self, t0: int, t1: int):
         self._check(lib().wave_batch_step(self.b, t0, t1))
+
+    def adjoint_gradient(self, dobs, checkpoint_every: int = 50, sum_shots: bool = True):
+        """Misfits and (vp, vs, rho) gradients of every shot (wave_batch_adjoint_gradient).
+        dobs: one n_receivers x NT array per shot. With sum_shots the shots' gradients
+        are summed (shots on one grid). Returns (misfits, g_vp, g_vs, g_rho); the
+        gradients are arrays (summed) or lists of arrays (per shot)."""
+        ns = len(self.shots)
+        d = [np.ascontiguousarray(x, dtype=np.float32) for x in dobs]
+        dptr = (ctypes.c_void_p * ns)(*[x.ctypes.data for x in d])
+        nout = 1 if sum_shots else ns
+        sizes = [self.shots[k].cfg.N for k in range(nout)]
+        g = [[np.zeros(n, dtype=np.float32) for n in sizes] for _ in range(3)]
+        ptrs = [(ctypes.c_void_p * nout)(*[a.ctypes.data for a in gk]) for gk in g]
+        mis = (ctypes.c_double * ns)()
+        self._check(lib().wave_batch_adjoint_gradient(self.b, ctypes.cast(dptr, ctypes.c_void_p), MEM_HOST, int(checkpoint_every),
+                                                      mis, ctypes.cast(ptrs[0], ctypes.c_void_p), ctypes.cast(ptrs[1], ctypes.c_void_p),
+                                                      ctypes.cast(ptrs[2], ctypes.c_void_p), MEM_HOST, int(sum_shots)))
+        if sum_shots:
+            return list(mis), g[0][0], g[1][0], g[2][0]
+        return list(mis), g[0], g[1], g[2]
 
     def stream(self) -> int:
         s = ctypes.c_void_p()

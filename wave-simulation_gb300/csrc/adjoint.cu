@@ -371,12 +371,6 @@ std::string adjoint_supported(const wave_handle* h)
     return "";
 }
 
-struct AdjStepper {
-    cudaStream_t stream;
-    std::function<void(int)> set_counter;   // every shot's step counter to n
-    std::function<void()> step;             // one forward step of every shot
-};
-
 // Runs forward + checkpoints, residuals, and the backward sweep for the shots.
 // dobs[s] and the gradient outputs are device pointers; with `sum` the
 // gradients of all shots are added into output 0.

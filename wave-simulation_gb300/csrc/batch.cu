@@ -202,6 +202,66 @@ int wave_batch_step(wave_batch* b, int t_begin, int t_end)
     return WAVE_OK;
 }
 
+int wave_batch_adjoint_gradient(wave_batch* b, const float* const* dobs, int dobs_mem, int checkpoint_every, double* misfits,
+                                float* const* grad_vp, float* const* grad_vs, float* const* grad_rho, int grad_mem, int sum_shots)
+{
+    if (!b) return bfail(nullptr, WAVE_ERR_ARG, "wave_batch_adjoint_gradient: null batch");
+    const int ns = static_cast<int>(b->shots.size());
+    if (!dobs || !misfits || !grad_vp || !grad_vs || !grad_rho || checkpoint_every < 1)
+        return bfail(b, WAVE_ERR_ARG, "wave_batch_adjoint_gradient: invalid argument");
+    for (int s = 0; s < ns; ++s) {
+        const std::string why = adjoint_supported(b->shots[s]);
+        if (!why.empty()) return bfail(b, WAVE_ERR_UNSUPPORTED, "wave_batch_adjoint_gradient: shot " + std::to_string(s) + ": " + why);
+        if (!dobs[s]) return bfail(b, WAVE_ERR_ARG, "wave_batch_adjoint_gradient: missing observed data");
+        if (sum_shots && b->shots[s]->N != b->shots[0]->N)
+            return bfail(b, WAVE_ERR_ARG, "wave_batch_adjoint_gradient: summed gradients need shots of one grid");
+    }
+    std::vector<void*> tmp;
+    auto dev = [&](size_t n) {
+        void* p = nullptr;
+        ck(cudaMalloc(&p, n * sizeof(float)), "cudaMalloc");
+        tmp.push_back(p);
+        return static_cast<float*>(p);
+    };
+    int rc = WAVE_OK;
+    try {
+        for (auto* h : b->shots) ck(cudaStreamSynchronize(h->stream), "shot sync");
+        if (b->dirty) {
+            refresh(b);
+            if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+            b->dirty = false;
+        }
+        std::vector<const float*> dD(ns);
+        for (int s = 0; s < ns; ++s) {
+            const size_t nd = static_cast<size_t>(b->shots[s]->nrec) * b->NT;
+            if (dobs_mem == WAVE_MEM_DEVICE) dD[s] = dobs[s];
+            else {
+                float* d = dev(nd);
+                ck(cudaMemcpy(d, dobs[s], nd * sizeof(float), cudaMemcpyHostToDevice), "dobs upload");
+                dD[s] = d;
+            }
+        }
+        const int nout = sum_shots ? 1 : ns;
+        std::vector<float*> g[3];
+        float* const* outs[3] = {grad_vp, grad_vs, grad_rho};
+        for (int k = 0; k < 3; ++k)
+            for (int s = 0; s < nout; ++s) g[k].push_back(grad_mem == WAVE_MEM_DEVICE ? outs[k][s] : dev(b->shots[s]->N));
+        AdjStepper S;
+        S.stream = b->stream;
+        S.set_counter = [b, ns](int n) { launch_set_counters(b->counters, ns, n, b->stream); };
+        S.step = [b]() { launch_batch_step(b); };
+        adjoint_run(b->shots, S, dD.data(), checkpoint_every, misfits, g[0].data(), g[1].data(), g[2].data(), sum_shots != 0);
+        if (grad_mem != WAVE_MEM_DEVICE)
+            for (int k = 0; k < 3; ++k)
+                for (int s = 0; s < nout; ++s)
+                    ck(cudaMemcpy(outs[k][s], g[k][s], b->shots[s]->N * sizeof(float), cudaMemcpyDeviceToHost), "gradient copy");
+    } catch (std::exception& e) {
+        rc = bfail(b, WAVE_ERR_CUDA, e.what());
+    }
+    for (void* p : tmp) cudaFree(p);
+    return rc;
+}
+
 int wave_batch_get_stream(wave_batch* b, void** stream)
 {
     if (!b || !stream) return bfail(b, WAVE_ERR_ARG, "wave_batch_get_stream: null argument");

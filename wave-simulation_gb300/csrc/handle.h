@@ -1,6 +1,7 @@
 // handle.h — the solver handle behind wave_handle* (solver.cu, batch.cu).
 #pragma once
 
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -91,4 +92,15 @@ struct wave_handle {
 namespace wave {
 // one forward time step of a handle on its stream (solver.cu)
 void step_once(wave_handle* h);
+
+// the adjoint gradient driver (adjoint.cu), shared by the single-handle and
+// the batched entry points
+struct AdjStepper {
+    cudaStream_t stream;
+    std::function<void(int)> set_counter;   // every shot's step counter to n
+    std::function<void()> step;             // one forward step of every shot
+};
+std::string adjoint_supported(const wave_handle* h);
+void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, const float* const* dobs, int K, double* misfit,
+                 float* const* gvp, float* const* gvs, float* const* grho, bool sum);
 } // namespace wave
