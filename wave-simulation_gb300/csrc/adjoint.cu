@@ -66,10 +66,16 @@ namespace {
 
 // (D^T lam)[c] = sum_k w_{c-k}(k) lam[c-k] over the rows c-k inside the axis,
 // with the row weights of deriv(): interior weights or the edge-table row
-template <int H>
+template <int H, bool FWD>
 __device__ __forceinline__ float derivT(const float* __restrict__ lam, long long i, long long st, int c, const Op1D& op)
 {
     float s = 0.0f;
+    if (!op.full && c - H >= op.E && c + H < op.n - op.E) {
+        // every row c-k is an interior row: its weight at offset k is the interior weight
+#pragma unroll
+        for (int k = (FWD ? -H + 1 : -H); k <= (FWD ? H : H - 1); ++k) s += op.w[kMaxHalf + k] * __ldg(lam + i - k * st);
+        return s;
+    }
 #pragma unroll
     for (int k = -H; k <= H; ++k) {
         const int r = c - k;
@@ -156,11 +162,11 @@ __device__ __forceinline__ void adj_vel_body(const StepParams& P, const AdjShot&
     const float* X1 = X0 + A.stride;
     const long long i = p.i, sy = P.NX;
     float lvx = A.lf[0][i];
-    lvx += derivT<H>(A.T[0], i, 1, p.x, P.Dxb);
-    lvx += derivT<H>(A.T[2], i, sy, p.y, P.Dyf);
+    lvx += derivT<H, false>(A.T[0], i, 1, p.x, P.Dxb);
+    lvx += derivT<H, true>(A.T[2], i, sy, p.y, P.Dyf);
     float lvy = A.lf[1][i];
-    lvy += derivT<H>(A.T[1], i, sy, p.y, P.Dyb);
-    lvy += derivT<H>(A.T[3], i, 1, p.x, P.Dxf);
+    lvy += derivT<H, false>(A.T[1], i, sy, p.y, P.Dyb);
+    lvy += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
     const Slabs S = slabs_of(P, p);
     const float *sxx = X0 + A.off[AV_SXX], *syy = X0 + A.off[AV_SYY], *sxy = X0 + A.off[AV_SXY];
     float a1 = deriv<H, true>(sxx, i, 1, p.x, P.Dxf);
@@ -194,11 +200,11 @@ template <int H>
 __device__ __forceinline__ void adj_sigma_body(const StepParams& P, const AdjShot& A, const Pt& p)
 {
     const long long i = p.i, sy = P.NX;
-    A.lf[2][i] += derivT<H>(A.T[4], i, 1, p.x, P.Dxf);
-    float u = derivT<H>(A.T[5], i, sy, p.y, P.Dyb);
-    u += derivT<H>(A.T[6], i, 1, p.x, P.Dxb);
+    A.lf[2][i] += derivT<H, true>(A.T[4], i, 1, p.x, P.Dxf);
+    float u = derivT<H, false>(A.T[5], i, sy, p.y, P.Dyb);
+    u += derivT<H, false>(A.T[6], i, 1, p.x, P.Dxb);
     A.lf[4][i] += u;
-    A.lf[3][i] += derivT<H>(A.T[7], i, sy, p.y, P.Dyf);
+    A.lf[3][i] += derivT<H, true>(A.T[7], i, sy, p.y, P.Dyf);
 }
 
 template <int H, int PASS>
@@ -208,12 +214,14 @@ __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ P
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
     const AdjShot& A = As[w.shot];
-    if (PASS == 0) adj_stress_body<H>(sP, A, p, vn);
-    else if (PASS == 1) adj_vel_body<H>(sP, A, p, vn);
-    else adj_sigma_body<H>(sP, A, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (!point_tile(sP, w, p, rr)) continue;
+        if (PASS == 0) adj_stress_body<H>(sP, A, p, vn);
+        else if (PASS == 1) adj_vel_body<H>(sP, A, p, vn);
+        else adj_sigma_body<H>(sP, A, p);
+    }
 }
 
 // residual of step n at the receivers into the adjoint state (transposed gather;
@@ -435,7 +443,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         }
         Ps[s] = h->sp;
         const int rows = h->NY * h->NZ;
-        for (int r0 = 0; r0 < rows; r0 += 8)
+        for (int r0 = 0; r0 < rows; r0 += kTileRows)
             for (int x0 = 0; x0 < h->NX; x0 += 32) tiles.push_back({s, x0, r0, 0});
     }
     auto upload = [&](auto& v) {

@@ -75,7 +75,7 @@ void refresh(wave_batch* b)
         P[s] = h->sp;
         Q[s] = h->sq;
         const int rows = h->NY * h->NZ;
-        for (int r0 = 0; r0 < rows; r0 += 8)
+        for (int r0 = 0; r0 < rows; r0 += kTileRows)
             for (int x0 = 0; x0 < h->NX; x0 += 32) tiles.push_back({s, x0, r0, 0});
     }
     cudaFree(b->dP);

@@ -54,9 +54,10 @@ __global__ void __launch_bounds__(256) acoustic_v_batch(const StepParams* __rest
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    acoustic_v_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) acoustic_v_body<H>(sP, p);
+    }
 }
 
 template <int H>
@@ -90,9 +91,10 @@ __global__ void __launch_bounds__(256) acoustic_p_batch(const StepParams* __rest
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    acoustic_p_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) acoustic_p_body<H>(sP, p);
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -151,9 +153,10 @@ __global__ void __launch_bounds__(256) elastic_v_batch(const StepParams* __restr
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    elastic_v_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) elastic_v_body<H>(sP, p);
+    }
 }
 
 // elastic stress: ForwardSolver2Delastic.cpp:210-290, ForwardSolver3Delastic.cpp:283-409,
@@ -246,9 +249,10 @@ __global__ void __launch_bounds__(256) elastic_s_batch(const StepParams* __restr
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    elastic_s_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) elastic_s_body<H>(sP, p);
+    }
 }
 
 // visco-elastic stress: ForwardSolver2Dviscoelastic.cpp:223-303,
@@ -397,9 +401,10 @@ __global__ void __launch_bounds__(256) visco_s_batch(const StepParams* __restric
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    visco_s_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) visco_s_body<H>(sP, p);
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -429,9 +434,10 @@ __global__ void __launch_bounds__(256) sh_v_batch(const StepParams* __restrict__
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    sh_v_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) sh_v_body<H>(sP, p);
+    }
 }
 
 template <int H>
@@ -478,9 +484,10 @@ __global__ void __launch_bounds__(256) sh_s_batch(const StepParams* __restrict__
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    sh_s_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) sh_s_body<H>(sP, p);
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -514,9 +521,10 @@ __global__ void __launch_bounds__(256) tm_h_batch(const StepParams* __restrict__
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    tm_h_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) tm_h_body<H>(sP, p);
+    }
 }
 
 // memory variables of one E component (ForwardSolver2Dviscotmem.cpp:175-182,
@@ -563,9 +571,10 @@ __global__ void __launch_bounds__(256) tm_e_batch(const StepParams* __restrict__
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    tm_e_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) tm_e_body<H>(sP, p);
+    }
 }
 
 // EM TEz: FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:132-180),
@@ -594,9 +603,10 @@ __global__ void __launch_bounds__(256) te_h_batch(const StepParams* __restrict__
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    te_h_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) te_h_body<H>(sP, p);
+    }
 }
 
 template <int H>
@@ -632,9 +642,10 @@ __global__ void __launch_bounds__(256) te_e_batch(const StepParams* __restrict__
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    te_e_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) te_e_body<H>(sP, p);
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -678,9 +689,10 @@ __global__ void __launch_bounds__(256) em3_h_batch(const StepParams* __restrict_
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    em3_h_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) em3_h_body<H>(sP, p);
+    }
 }
 
 template <int H>
@@ -729,9 +741,10 @@ __global__ void __launch_bounds__(256) em3_e_batch(const StepParams* __restrict_
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    em3_e_body<H>(sP, p);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) em3_e_body<H>(sP, p);
+    }
 }
 
 // --------------------------------------------------------------------------
@@ -758,9 +771,10 @@ __global__ void __launch_bounds__(256) abs_frame_batch(const StepParams* __restr
     __shared__ StepParams sP;
     const BatchTile w = W[blockIdx.x];
     load_params(sP, Ps + w.shot);
-    Pt p;
-    if (!point_tile(sP, w, p)) return;
-    abs_frame_body(sP, p, f0, f1, f2);
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (point_tile(sP, w, p, rr)) abs_frame_body(sP, p, f0, f1, f2);
+    }
 }
 
 // --------------------------------------------------------------------------

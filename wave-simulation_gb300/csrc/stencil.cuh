@@ -70,8 +70,8 @@ __device__ __forceinline__ bool point(const StepParams& P, Pt& p)
     return true;
 }
 
-// batched launches: one block per (shot, 32 x 8 tile); the shot's parameters
-// are staged in shared memory once per block
+// batched launches: one block per (shot, 32 x kTileRows tile); the shot's
+// parameters are staged in shared memory once per block
 __device__ __forceinline__ void load_params(StepParams& dst, const StepParams* src)
 {
     const int n = sizeof(StepParams) / sizeof(int);
@@ -81,10 +81,11 @@ __device__ __forceinline__ void load_params(StepParams& dst, const StepParams* s
     __syncthreads();
 }
 
-__device__ __forceinline__ bool point_tile(const StepParams& P, const BatchTile& w, Pt& p)
+// rows rr..rr+7 of a 32 x kTileRows tile
+__device__ __forceinline__ bool point_tile(const StepParams& P, const BatchTile& w, Pt& p, int rr)
 {
     p.x = w.x0 + threadIdx.x;
-    const int r = w.r0 + threadIdx.y;
+    const int r = w.r0 + rr + threadIdx.y;
     if (p.x >= P.NX || r >= P.NY * P.NZ) return false;
     p.y = r / P.NZ;
     p.z = r - p.y * P.NZ;

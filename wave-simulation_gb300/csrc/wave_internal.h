@@ -105,7 +105,9 @@ struct SrcRecParams {
     float* f[F_COUNT];
 };
 
-// one block of a batched launch: shot index and tile origin (x0, row r0 = z + NZ*y)
+// one block of a batched launch: shot index and tile origin (x0, row r0 = z + NZ*y);
+// a tile is 32 points along x by kTileRows rows, a 32 x 8 block covering it in 4 passes
+constexpr int kTileRows = 32;
 struct BatchTile {
     int shot, x0, r0, pad;
 };
