@@ -236,6 +236,8 @@ def run_gpu(args):
     sidx, stype, sig, ridx, rtype = make_acquisition(s.nt, cfg.DT)
     dev_model = {k: torch.from_numpy(v).cuda() for k, v in model.items()}
     s.prepareForModelling(dev_model)
+    if args.kernel_path:
+        s.set_kernel_path(args.kernel_path)
     s.setSources(sidx, stype, sig)
     s.setReceivers(ridx, rtype)
     assert args.warmup + args.steps <= s.nt
@@ -308,7 +310,8 @@ def run_gpu(args):
              "stress": "el3d_str<4> (TMA streaming)" if passes & 2 else "elastic_s<4> (generic)"}
     roof = {"bound": "hbm", "kernel": names[dominant], "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth (burst)",
-            "traffic": (traffic or {}).get(dominant),
+            "traffic": (traffic or {}).get(names[dominant].split("<")[0]),
+            "traffic_note": "DRAM bytes per launch: ncu ratio to algorithmic bytes at 160^3 times the 256^3 algorithmic bytes",
             "alg_bytes_per_launch": dom_bytes,
             "step_pair": {"alg_bytes_per_step": step_alg, "ms": vel_ms + str_ms,
                           "achieved": step_alg / ((vel_ms + str_ms) * 1e-3) / 1e9,
@@ -822,6 +825,8 @@ def main():
     ap.add_argument("--grid", type=int, default=256, help="cube edge (profiling captures use a smaller cube)")
     ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch", "fwi2d"])
     ap.add_argument("--shots", type=int, default=128, help="shots of the batched EM workload")
+    ap.add_argument("--kernel-path", type=int, default=0, choices=[0, 1, 2],
+                    help="3-D elastic kernels: 0 automatic, 1 generic, 2 streaming (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
