@@ -220,6 +220,28 @@ int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, 
 int wave_set_kernel_path(wave_handle* h, int path);
 int wave_get_kernel_path(wave_handle* h, int* streaming_active);
 
+/* ---- seismogram output path and file formats ---- */
+/* Resampling of ntr traces (row-major ntr x nt, sample interval dt) to
+ * seismo_dt by linear interpolation (Common::calcResampleMat,
+ * Common.hpp:202-230, applied as data * resampleMat in Seismogram::write,
+ * Seismogram.cpp:109); seismo_dt = 0 keeps dt. *nt_out receives
+ * floor((nt-1) / (seismo_dt/dt)) + 1; with out == NULL only *nt_out is set.
+ * in/out on the host or the current device (mem). */
+int wave_resample_traces(const float* in, int64_t ntr, int64_t nt, double dt, double seismo_dt, float* out, int64_t* nt_out, int mem);
+/* Seismogram::normalizeTrace (Seismogram.cpp:215-240) in place: mode 0 none,
+ * 1 each trace divided by its max |value|, 2 by its l2 norm (a zero norm
+ * divides by 1). AGC and envelope normalisation (modes 3, 4) are not built. */
+int wave_normalize_traces(float* data, int64_t ntr, int64_t nt, int mode, int mem);
+/* MatrixMarket files (IO::readVector/writeMatrix with fileFormat 1, IO.hpp:21-145):
+ * read "array" or "coordinate" real files into a row-major rows x cols buffer
+ * (out == NULL: dimensions only); write a row-major matrix in array format. */
+int wave_read_mtx(const char* path, float* out, int64_t capacity, int64_t* rows, int64_t* cols);
+int wave_write_mtx(const char* path, const float* data, int64_t rows, int64_t cols);
+/* SeismicUnix traces with the trace headers of SUIO::writeSU (SUIO.hpp:156-262):
+ * ntr x ns row-major samples, receiver and source grid indices, grid and DH. */
+int wave_write_su(const char* path, const float* data, int64_t ntr, int64_t ns, double dt, const int64_t* rec_idx, int64_t src_idx,
+                  int64_t NX, int64_t NY, int64_t NZ, double DH);
+
 /* ---- adjoint gradient (new; the reference's inversion is a separate project) ----
  * Gradient of J = 1/2 sum over receivers and steps of (d - d_obs)^2 with
  * respect to vp, vs and rho, by the discrete adjoint of the 2-D elastic time

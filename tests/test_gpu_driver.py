@@ -1,0 +1,62 @@
+"""The C++ driver (wave_simulation, the Simulation.cpp-style loop over shots)
+end to end on the reference's 2-D acoustic CI case: parameter file, source and
+receiver files, the time loop on the GPU, and the seismogram output path
+(SeismogramFormat 4 = SU as the CI file asks, and MatrixMarket with trace
+normalisation and resampling), compared with the reference's golden seismogram
+(par/ci/seismogram.2D.acoustic.ref.p.mtx) under the reference's gate."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import refcpu
+from test_gpu_seismo import resample_reference
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ci")
+GATE = 5e-7
+
+
+def _setup(tmp_path, edits):
+    ci = tmp_path / "ci"
+    ci.mkdir()
+    for f in ("sources_ci.2D.txt", "receiver_ci.2D.txt"):
+        shutil.copy(os.path.join(GOLDEN, f), ci / f)
+    text = open(os.path.join(GOLDEN, "configuration_ci.2D.acoustic.txt")).read().splitlines()
+    out = []
+    for line in text:
+        key = line.split("=")[0].strip() if "=" in line else None
+        out.append(f"{key}={edits[key]}" if key in edits else line)
+    cfg = ci / "configuration.txt"
+    cfg.write_text("\n".join(out) + "\n")
+    return cfg, ci
+
+
+def _run(wave, cfg):
+    exe = os.path.join(os.path.dirname(wave.LIB_PATH), "wave_simulation")
+    r = subprocess.run([exe, str(cfg)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+
+
+def test_driver_su_output_matches_reference_golden(wave, tmp_path):
+    cfg, ci = _setup(tmp_path, {})
+    _run(wave, cfg)
+    raw = open(ci / "seismogram.2D.acoustic.ci.shot_1.p.su", "rb").read()
+    ns = int(np.frombuffer(raw, dtype="<u2", count=1, offset=114)[0])
+    trace = np.frombuffer(raw, dtype="<f4", count=ns, offset=240)[None, :].astype(np.float64)
+    golden = refcpu.read_mtx_array(os.path.join(GOLDEN, "seismogram.2D.acoustic.ref.p.mtx"))
+    assert trace.shape == golden.shape
+    assert refcpu.reference_misfit(trace, golden) < GATE
+    assert np.linalg.norm(trace - golden) / np.linalg.norm(golden) < 1e-4
+
+
+def test_driver_mtx_output_with_normalisation_and_resampling(wave, tmp_path):
+    cfg, ci = _setup(tmp_path, {"SeismogramFormat": "1", "normalizeTraces": "1", "seismoDT": "6.0e-03"})
+    _run(wave, cfg)
+    got = refcpu.read_mtx_array(str(ci / "seismogram.2D.acoustic.ci.shot_1.p.mtx"))
+    golden = refcpu.read_mtx_array(os.path.join(GOLDEN, "seismogram.2D.acoustic.ref.p.mtx")).astype(np.float32)
+    ref = resample_reference(golden / np.abs(golden).max(axis=1, keepdims=True), 2e-3, 6e-3)
+    assert got.shape == ref.shape
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-4

@@ -41,7 +41,8 @@ ABI_SYMBOLS = (
     "wave_get_kernel_path", "wave_average_shear_modulus", "wave_batch_create", "wave_batch_destroy",
     "wave_batch_shot", "wave_batch_step", "wave_batch_get_stream", "wave_batch_get_launch_count",
     "wave_batch_last_error", "wave_average_shear_modulus_noalloc", "wave_adjoint_gradient",
-    "wave_batch_adjoint_gradient",
+    "wave_batch_adjoint_gradient", "wave_resample_traces", "wave_normalize_traces", "wave_read_mtx",
+    "wave_write_mtx", "wave_write_su",
 )
 
 
@@ -161,6 +162,12 @@ def lib():
     L.wave_average_shear_modulus.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, I]
     L.wave_average_shear_modulus_noalloc.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, P]
     L.wave_adjoint_gradient.argtypes = [P, P, I, I, ctypes.POINTER(ctypes.c_double), P, P, P, I]
+    i64 = ctypes.c_int64
+    L.wave_resample_traces.argtypes = [P, i64, i64, ctypes.c_double, ctypes.c_double, P, ctypes.POINTER(i64), I]
+    L.wave_normalize_traces.argtypes = [P, i64, i64, I, I]
+    L.wave_read_mtx.argtypes = [ctypes.c_char_p, P, i64, ctypes.POINTER(i64), ctypes.POINTER(i64)]
+    L.wave_write_mtx.argtypes = [ctypes.c_char_p, P, i64, i64]
+    L.wave_write_su.argtypes = [ctypes.c_char_p, P, i64, i64, ctypes.c_double, P, i64, i64, i64, i64, ctypes.c_double]
     L.wave_batch_adjoint_gradient.argtypes = [P, P, I, I, ctypes.POINTER(ctypes.c_double), P, P, P, I, I]
     L.wave_batch_create.argtypes = [P, I, CP(P)]
     L.wave_batch_destroy.argtypes = [P]
@@ -211,6 +218,48 @@ def average_shear_modulus(mu, dims, mode: int, out=None):
     (pm, mem), (po, _) = _ptr(mu), _ptr(out)
     _check(None, lib().wave_average_shear_modulus(pm, po, dims[0], dims[1], dims[2], mode, mem))
     return out
+
+
+def resample_traces(data, dt: float, seismo_dt: float):
+    """Seismogram resampling to seismo_dt (wave_resample_traces); data: ntr x nt."""
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    ntr, nt = d.shape
+    nout = ctypes.c_int64()
+    _check(None, lib().wave_resample_traces(None, ntr, nt, dt, seismo_dt, None, ctypes.byref(nout), MEM_HOST))
+    out = np.zeros((ntr, nout.value), dtype=np.float32)
+    _check(None, lib().wave_resample_traces(d.ctypes.data_as(ctypes.c_void_p), ntr, nt, dt, seismo_dt,
+                                            out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nout), MEM_HOST))
+    return out
+
+
+def normalize_traces(data, mode: int):
+    """Seismogram::normalizeTrace modes 0..2 (wave_normalize_traces); returns a new array."""
+    d = np.array(data, dtype=np.float32, order="C", copy=True)
+    _check(None, lib().wave_normalize_traces(d.ctypes.data_as(ctypes.c_void_p), d.shape[0], d.shape[1], mode, MEM_HOST))
+    return d
+
+
+def read_mtx(path: str) -> np.ndarray:
+    """A MatrixMarket file as a rows x cols float32 array (wave_read_mtx)."""
+    r, c = ctypes.c_int64(), ctypes.c_int64()
+    _check(None, lib().wave_read_mtx(path.encode(), None, 0, ctypes.byref(r), ctypes.byref(c)))
+    out = np.zeros((r.value, c.value), dtype=np.float32)
+    _check(None, lib().wave_read_mtx(path.encode(), out.ctypes.data_as(ctypes.c_void_p), out.size, ctypes.byref(r), ctypes.byref(c)))
+    return out
+
+
+def write_mtx(path: str, data) -> None:
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    if d.ndim == 1:
+        d = d[:, None]
+    _check(None, lib().wave_write_mtx(path.encode(), d.ctypes.data_as(ctypes.c_void_p), d.shape[0], d.shape[1]))
+
+
+def write_su(path: str, data, dt: float, rec_idx, src_idx: int, dims, DH: float) -> None:
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    r = np.ascontiguousarray(rec_idx, dtype=np.int64)
+    _check(None, lib().wave_write_su(path.encode(), d.ctypes.data_as(ctypes.c_void_p), d.shape[0], d.shape[1], dt,
+                                     r.ctypes.data_as(ctypes.c_void_p), int(src_idx), dims[0], dims[1], dims[2], DH))
 
 
 def average_shear_modulus_noalloc(mu, out, dims, mode: int, stream: int = 0):

@@ -1,0 +1,132 @@
+// seismo.cu — the seismogram output path on the device: per-trace
+// normalisation (Seismogram::normalizeTrace, Seismogram.cpp:215-240) and
+// resampling to seismoDT (Seismogram::setSeismoDT + Common::calcResampleMat,
+// Seismogram.cpp:610-618, Common.hpp:202-230; applied as data * resampleMat
+// when a seismogram is written, Seismogram.cpp:109).
+#include <cmath>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "wave_internal.h"
+
+namespace wave {
+void set_global_error(const std::string& msg);
+}
+
+using namespace wave;
+
+namespace {
+
+// linear interpolation at k * coeff (coeff = seismoDT / DT in FP32): weight
+// 1 - frac on sample floor(k coeff), frac on the next one, each only inside
+// the trace
+__global__ void resample_kernel(const float* __restrict__ in, long long ntr, long long nt, float coeff, long long ntOut,
+                                float* __restrict__ out)
+{
+    const long long total = ntr * ntOut;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const long long tr = q / ntOut, k = q - tr * ntOut;
+        const float rel = static_cast<float>(k) * coeff;
+        const float fl = floorf(rel);
+        const long long c0 = static_cast<long long>(fl);
+        const float w1 = fmodf(rel, 1.0f);
+        const float w0 = 1.0f - w1;
+        const float* t = in + tr * nt;
+        float s = 0.0f;
+        if (c0 < nt) s += w0 * t[c0];
+        if (c0 + 1 < nt) s += w1 * t[c0 + 1];
+        out[q] = s;
+    }
+}
+
+// one block per trace: max norm (mode 1) or l2 norm (mode >= 2); a zero norm divides by 1
+__global__ void normalize_kernel(float* data, long long nt, int mode)
+{
+    __shared__ double part[32];
+    float* t = data + blockIdx.x * nt;
+    double acc = 0.0;
+    for (long long k = threadIdx.x; k < nt; k += blockDim.x) {
+        const double v = t[k];
+        acc = mode == 1 ? fmax(acc, fabs(v)) : acc + v * v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_down_sync(0xffffffffu, acc, o);
+        acc = mode == 1 ? fmax(acc, w) : acc + w;
+    }
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = mode == 1 ? fmax(r, part[w]) : r + part[w];
+        part[0] = mode == 1 ? r : sqrt(r);
+    }
+    __syncthreads();
+    float norm = static_cast<float>(part[0]);
+    if (norm == 0.0f) norm = 1.0f;
+    for (long long k = threadIdx.x; k < nt; k += blockDim.x) t[k] /= norm;
+}
+
+int err(int code, const std::string& m)
+{
+    set_global_error(m);
+    return code;
+}
+
+} // namespace
+
+extern "C" int wave_resample_traces(const float* in, int64_t ntr, int64_t nt, double dt, double seismo_dt, float* out,
+                                    int64_t* nt_out, int mem)
+{
+    if (!nt_out || ntr < 0 || nt < 1 || dt <= 0 || seismo_dt < 0) return err(WAVE_ERR_ARG, "wave_resample_traces: invalid argument");
+    const float coeff = seismo_dt > 0 ? static_cast<float>(seismo_dt) / static_cast<float>(dt) : 1.0f;
+    if (!(coeff > 0.0f)) return err(WAVE_ERR_ARG, "wave_resample_traces: invalid seismoDT");
+    const long long ntNew = static_cast<long long>(std::floor(static_cast<float>(nt - 1) / coeff)) + 1;
+    *nt_out = ntNew;
+    if (!out || ntr == 0) return WAVE_OK;
+    if (!in) return err(WAVE_ERR_ARG, "wave_resample_traces: null input");
+    const float* dIn = in;
+    float* dOut = out;
+    float *tIn = nullptr, *tOut = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (mem != WAVE_MEM_DEVICE) {
+        e = cudaMalloc(&tIn, ntr * nt * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&tOut, ntr * ntNew * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemcpy(tIn, in, ntr * nt * sizeof(float), cudaMemcpyHostToDevice);
+        dIn = tIn;
+        dOut = tOut;
+    }
+    if (e == cudaSuccess) {
+        resample_kernel<<<1216, 256>>>(dIn, ntr, nt, coeff, ntNew, dOut);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && mem != WAVE_MEM_DEVICE) e = cudaMemcpy(out, tOut, ntr * ntNew * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(tIn);
+    cudaFree(tOut);
+    if (e != cudaSuccess) return err(WAVE_ERR_CUDA, std::string("wave_resample_traces: ") + cudaGetErrorString(e));
+    return WAVE_OK;
+}
+
+extern "C" int wave_normalize_traces(float* data, int64_t ntr, int64_t nt, int mode, int mem)
+{
+    if (!data || ntr < 0 || nt < 1 || mode < 0 || mode > 2) return err(WAVE_ERR_ARG, "wave_normalize_traces: invalid argument (mode 0, 1 or 2)");
+    if (mode == 0 || ntr == 0) return WAVE_OK;
+    float* d = data;
+    float* t = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (mem != WAVE_MEM_DEVICE) {
+        e = cudaMalloc(&t, ntr * nt * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemcpy(t, data, ntr * nt * sizeof(float), cudaMemcpyHostToDevice);
+        d = t;
+    }
+    if (e == cudaSuccess) {
+        normalize_kernel<<<static_cast<unsigned>(ntr), 256>>>(d, nt, mode);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && mem != WAVE_MEM_DEVICE) e = cudaMemcpy(data, t, ntr * nt * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(t);
+    if (e != cudaSuccess) return err(WAVE_ERR_CUDA, std::string("wave_normalize_traces: ") + cudaGetErrorString(e));
+    return WAVE_OK;
+}

@@ -2,8 +2,11 @@
 // file end to end on the GPU solver, the way Simulation.cpp:36-570 does for the
 // reference: read the configuration, build the model (homogeneous from the
 // velocityP/velocityS/rho keys, or MatrixMarket files <ModelFilename>.<p>.mtx
-// for ModelRead=1), loop over the shots of <SourceFilename>.txt, generate the
-// wavelets, run the time loop and write <SeismogramFilename>.shot_<n>.<c>.mtx.
+// for ModelRead=1, FileFormat=1), loop over the shots of <SourceFilename>.txt,
+// generate the wavelets, run the time loop, normalise the traces
+// (normalizeTraces 0-2), resample them to seismoDT and write
+// <SeismogramFilename>.shot_<n>.<c>.mtx (SeismogramFormat 1) or .su (4), as
+// Simulation.cpp:521-531 does.
 //
 //   wave_simulation <parameter file>
 #include <cstdio>
@@ -54,29 +57,12 @@ T key(const std::map<std::string, std::string>& m, const char* k, T def)
 
 std::vector<float> read_mtx_vector(const std::string& path, size_t n)
 {
-    std::ifstream f(path);
-    if (!f.good()) throw wave::gpu::Error(WAVE_ERR_IO, "cannot open " + path);
-    std::string line;
-    while (std::getline(f, line))
-        if (!line.empty() && line[0] != '%') break;
-    std::vector<float> v;
-    v.reserve(n);
-    double x;
-    while (f >> x) v.push_back(static_cast<float>(x));
-    if (v.size() != n) throw wave::gpu::Error(WAVE_ERR_IO, path + ": wrong number of values");
+    int64_t rows = 0, cols = 0;
+    wave::gpu::check(nullptr, wave_read_mtx(path.c_str(), nullptr, 0, &rows, &cols));
+    if (static_cast<size_t>(rows * cols) != n) throw wave::gpu::Error(WAVE_ERR_IO, path + ": wrong number of values");
+    std::vector<float> v(n);
+    wave::gpu::check(nullptr, wave_read_mtx(path.c_str(), v.data(), static_cast<int64_t>(n), &rows, &cols));
     return v;
-}
-
-void write_mtx(const std::string& path, const std::vector<float>& data, int ntr, int nt)
-{
-    std::ofstream f(path);
-    f << "%%MatrixMarket matrix array real general\n" << ntr << " " << nt << "\n";
-    char buf[64];
-    for (int t = 0; t < nt; ++t)          // column-major: trace index fastest (Seismogram.cpp mtx layout)
-        for (int r = 0; r < ntr; ++r) {
-            std::snprintf(buf, sizeof(buf), "%.9g\n", data[static_cast<size_t>(r) * nt + t]);
-            f << buf;
-        }
 }
 
 } // namespace
@@ -101,6 +87,8 @@ int main(int argc, char** argv)
         const bool em = cfg.equation >= WAVE_EQ_TMEM;
         const std::string mf = key<std::string>(keys, "ModelFilename", "model/model");
         if (key<int>(keys, "ModelRead", 0) == 1) {
+            if (key<int>(keys, "FileFormat", 1) != 1)
+                throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "model files: only FileFormat=1 (MatrixMarket) is readable here; lmf/frv are LAMA formats");
             auto rd = [&](const char* p) { return read_mtx_vector(dir + "/../" + mf + "." + p + ".mtx", n); };
             if (em) { model.eps_r = rd("epsilonr"); model.sigma = rd("sigma"); model.mu_r = rd("mur"); }
             else {
@@ -159,6 +147,11 @@ int main(int argc, char** argv)
         std::set<int> shots;
         for (auto& s : srcs) shots.insert(s.no);
         const char* names[2][4] = {{"p", "vx", "vy", "vz"}, {"ez", "ex", "ey", "hz"}};
+        const int normalize = key<int>(keys, "normalizeTraces", 0);
+        const double seismoDT = key<double>(keys, "seismoDT", cfg.DT);
+        const int format = key<int>(keys, "SeismogramFormat", 1);
+        if (normalize < 0 || normalize > 2) throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "normalizeTraces 3 (AGC) and 4 (envelope) are not built");
+        if (format != 1 && format != 4) throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "SeismogramFormat: 1 (mtx) and 4 (su) are written here");
         for (int shot : shots) {
             wave::gpu::Acquisition src;
             for (auto& s : srcs) {
@@ -183,9 +176,24 @@ int main(int argc, char** argv)
                         ++ntr;
                     }
                 if (!ntr) continue;
-                write_mtx(dir + "/../" + key<std::string>(keys, "SeismogramFilename", "seismogram") + ".shot_" + std::to_string(shot) +
-                              "." + names[em ? 1 : 0][type - 1] + ".mtx",
-                          part, ntr, nt);
+                // Seismogram::normalizeTrace, then the resampling of Seismogram::write
+                wave::gpu::check(nullptr, wave_normalize_traces(part.data(), ntr, nt, normalize, WAVE_MEM_HOST));
+                int64_t ntOut = 0;
+                wave::gpu::check(nullptr, wave_resample_traces(nullptr, ntr, nt, cfg.DT, seismoDT, nullptr, &ntOut, WAVE_MEM_HOST));
+                std::vector<float> out(static_cast<size_t>(ntr) * ntOut);
+                wave::gpu::check(nullptr, wave_resample_traces(part.data(), ntr, nt, cfg.DT, seismoDT, out.data(), &ntOut, WAVE_MEM_HOST));
+                const std::string base = dir + "/../" + key<std::string>(keys, "SeismogramFilename", "seismogram") + ".shot_" +
+                                         std::to_string(shot) + "." + names[em ? 1 : 0][type - 1];
+                if (format == 4) {
+                    std::vector<int64_t> ridx;
+                    for (size_t r = 0; r < rec.type.size(); ++r)
+                        if (rec.type[r] == type) ridx.push_back(rec.index[r]);
+                    wave::gpu::check(nullptr, wave_write_su((base + ".su").c_str(), out.data(), ntr, ntOut, seismoDT > 0 ? seismoDT : cfg.DT,
+                                                           ridx.data(), src.index.empty() ? 0 : src.index[0], cfg.NX, cfg.NY,
+                                                           cfg.dimension == 3 ? cfg.NZ : 1, cfg.DH));
+                } else {
+                    wave::gpu::check(nullptr, wave_write_mtx((base + ".mtx").c_str(), out.data(), ntr, ntOut));
+                }
             }
             std::cout << "shot " << shot << ": " << nt << " time steps done\n";
         }
