@@ -1,13 +1,13 @@
 // kernels_el3d.cu — streaming sm_103a kernels for the 3-D elastic time step
 // (FD3Delastic::run, ForwardSolver3Delastic.cpp:120-414) on large grids.
 //
-// Each CTA owns a 32 (x) x 16 (z) column tile and marches it down the depth
+// Each CTA owns a 32 (x) x 8 (z) column tile and marches it down the depth
 // axis y (the slowest axis, reference layout idx = x + z*NX + y*NX*NZ). The
-// CTAs are persistent (one per SM); each takes a contiguous run of the
+// CTAs are persistent (two per SM); each takes a contiguous run of the
 // (tile, plane) work, so every field plane is fetched from HBM once. Planes
 // arrive through TMA bulk-tensor copies (cp.async.bulk.tensor.3d) into a
 // 3-stage shared-memory ring ("full" mbarriers carry the transaction
-// bytes). Each of the 16 warps computes one z row of the tile and releases a
+// bytes). Each of the 8 warps computes one z row of the tile and releases a
 // stage through an "empty" mbarrier; thread 0 refills a stage once all warps
 // have released it, one iteration behind its own warp. Warps never meet at a
 // block barrier, so they run up to a ring's length apart and hide each
@@ -31,10 +31,10 @@ namespace wave {
 
 namespace el3d {
 
-constexpr int TX = 32, TZ = 16, NTHR = TX * TZ, MAXSEG = 64;
+constexpr int TX = 32, TZ = 8, NTHR = TX * TZ, MAXSEG = 64;
 constexpr int NCWARP = NTHR / 32;                // warps of a CTA, one per z row of the tile
 constexpr int CB = TX * TZ * 4;                  // centre box bytes
-constexpr int PW = TX + 4, PH = TZ + 1;          // "+1" box (x0..x0+35, z0..z0+16)
+constexpr int PW = TX + 4, PH = TZ + 1;          // "+1" box (x0..x0+35, z0..z0+8)
 constexpr int PBYTES = PW * PH * 4;              // bytes one "+1" box copy delivers
 constexpr int PB = ((PBYTES + 127) / 128) * 128; // its slot in the stage layout
 
@@ -516,7 +516,7 @@ __device__ __forceinline__ void release(uint64_t* empty)
 // velocity pass (ForwardSolver3Delastic.cpp:174-277)
 // ------------------------------------------------------------------------
 template <int H>
-__global__ void __launch_bounds__(NTHR, 1) el3d_vel(const __grid_constant__ El3dMaps T, const StepParams P, const El3dSched S)
+__global__ void __launch_bounds__(NTHR, 2) el3d_vel(const __grid_constant__ El3dMaps T, const StepParams P, const El3dSched S)
 {
     using L = VelStage<H>;
     constexpr int NST = L::NST, HX = hx_of(H), BW = bw_of(H), TT = TX * TZ;
@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(NTHR, 1) el3d_vel(const __grid_constant__ El3d
 // stress pass (ForwardSolver3Delastic.cpp:283-409, FreeSurface3Delastic.cpp:15-47)
 // ------------------------------------------------------------------------
 template <int H>
-__global__ void __launch_bounds__(NTHR, 1) el3d_str(const __grid_constant__ El3dMaps T, const StepParams P, const El3dSched S)
+__global__ void __launch_bounds__(NTHR, 2) el3d_str(const __grid_constant__ El3dMaps T, const StepParams P, const El3dSched S)
 {
     using L = StrStage<H>;
     constexpr int NST = L::NST, HX = hx_of(H), BW = bw_of(H), TT = TX * TZ;
@@ -913,7 +913,7 @@ cudaError_t configure_h()
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(el3d_str<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)str_smem<H>());
     if (e != cudaSuccess) return e;
-    // one CTA (NTHR threads at up to 120 registers, the stage ring) must fit an SM
+    // a CTA (NTHR threads, the stage ring) must fit an SM; two are resident per SM
     int nv = 0, ns = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nv, el3d_vel<H>, NTHR, vel_smem<H>());
     if (e != cudaSuccess) return e;
@@ -1021,7 +1021,7 @@ bool el3d_prepare(El3dPlan& plan, const StepParams& P, const float* rho, const f
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long tiles = (long long)plan.sched.ntx * plan.sched.ntz;
     const long long work = tiles * P.NY;
-    long long grid = sms;                 // one persistent CTA per SM
+    long long grid = 2LL * sms;           // two persistent CTAs per SM
     if (grid > work) grid = work;
     // each CTA's plane range must fit the segment table
     if (tiles / grid + 2 > MAXSEG) return false;
