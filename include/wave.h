@@ -228,9 +228,10 @@ int wave_get_kernel_path(wave_handle* h, int* streaming_active);
  * floor((nt-1) / (seismo_dt/dt)) + 1; with out == NULL only *nt_out is set.
  * in/out on the host or the current device (mem). */
 int wave_resample_traces(const float* in, int64_t ntr, int64_t nt, double dt, double seismo_dt, float* out, int64_t* nt_out, int mem);
-/* Seismogram::normalizeTrace (Seismogram.cpp:215-240) in place: mode 0 none,
+/* Seismogram::normalizeTrace (Seismogram.cpp:215-275) in place: mode 0 none,
  * 1 each trace divided by its max |value|, 2 by its l2 norm (a zero norm
- * divides by 1). AGC and envelope normalisation (modes 3, 4) are not built. */
+ * divides by 1), 4 l2 norm then division by the envelope plus 1e-3 of its
+ * maximum. AGC normalisation (mode 3) is not built. */
 int wave_normalize_traces(float* data, int64_t ntr, int64_t nt, int mode, int mem);
 /* MatrixMarket files (IO::readVector/writeMatrix with fileFormat 1, IO.hpp:21-145):
  * read "array" or "coordinate" real files into a row-major rows x cols buffer
@@ -241,6 +242,25 @@ int wave_write_mtx(const char* path, const float* data, int64_t rows, int64_t co
  * ntr x ns row-major samples, receiver and source grid indices, grid and DH. */
 int wave_write_su(const char* path, const float* data, int64_t ntr, int64_t ns, double dt, const int64_t* rec_idx, int64_t src_idx,
                   int64_t NX, int64_t NY, int64_t NZ, double DH);
+
+/* ---- snapshots and trace attributes ---- */
+/* One wavefield of the handle ("VX", "VY", "VZ", "P", "Sxx", ..., "Syz", "HX",
+ * "HY", "HZ", "EX", "EY", "EZ"; case-insensitive) into out (N floats), the
+ * data Wavefields::write stores for snapType 1/2 (Wavefields3Delastic.cpp:62-96). */
+int wave_get_field(wave_handle* h, const char* name, float* out, int mem);
+/* snapType 3 energies of (visco-)elastic wavefields with the solver's
+ * operators: 2-D curl = (Dyf vx - Dxf vy) sqrt(mu), div = (Dxb vx + Dyb vy)
+ * sqrt(M) (Wavefields2Delastic.cpp:218-250); 3-D curl = sqrt(mu |curl v|^2),
+ * div = sqrt(M (div v)^2) (Wavefields3Delastic.cpp:197-240). */
+int wave_get_curl_div(wave_handle* h, float* curl, float* div, int mem);
+/* Envelope sqrt(x^2 + H(x)^2) of ntr traces in place, H the FFT Hilbert
+ * transform on the next power of two of nt-1 samples (Common::calcEnvelope,
+ * Common.hpp:272-290, HilbertFFT.cpp). */
+int wave_envelope(float* data, int64_t ntr, int64_t nt, int mem);
+/* Common::calcInstantaneousPhase (Common.hpp:297-345) in place, phase type 1
+ * (atan), 2 (atan2) or 3 (unwrapped); as there, the imaginary part is -data
+ * (the Hilbert call of that function is commented out in the reference). */
+int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_type, int mem);
 
 /* ---- adjoint gradient (new; the reference's inversion is a separate project) ----
  * Gradient of J = 1/2 sum over receivers and steps of (d - d_obs)^2 with

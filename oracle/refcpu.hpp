@@ -451,6 +451,7 @@ class Sim {
     void setup(const wave_config& c, const Model<T>& m);
     void step(int t);
     void reset();
+    void curlDiv(std::vector<T>& curl, std::vector<T>& div);
 
   private:
     void buildOperators();

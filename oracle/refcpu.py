@@ -246,6 +246,7 @@ def lib():
         L.refcpu_step.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         L.refcpu_seismograms.argtypes = [P, P]
         L.refcpu_field.argtypes = [P, ctypes.c_char_p, P]
+        L.refcpu_curl_div.argtypes = [P, P, P]
         L.refcpu_nt.argtypes = [P]
         L.refcpu_destroy.argtypes = [P]
         L.refcpu_last_error.restype = ctypes.c_char_p
@@ -317,6 +318,15 @@ class Oracle:
         if lib().refcpu_field(self.h, name.encode(), _ptr(out)) != 0:
             raise KeyError(name)
         return out
+
+    def curl_div(self):
+        """snapType 3 energies (curl, div) of the current wavefields."""
+        n = self.cfg.NX * self.cfg.NY * (1 if self.cfg.dimension == 2 else self.cfg.NZ)
+        c = np.zeros(n, dtype=np.float64)
+        d = np.zeros(n, dtype=np.float64)
+        if lib().refcpu_curl_div(self.h, _ptr(c), _ptr(d)) != 0:
+            raise RuntimeError(lib().refcpu_last_error().decode())
+        return c, d
 
     def close(self):
         if getattr(self, "h", None):

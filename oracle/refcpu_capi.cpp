@@ -5,6 +5,7 @@
 #include <cstring>
 #include <exception>
 #include <string>
+#include <type_traits>
 
 #include "refcpu.hpp"
 
@@ -131,6 +132,27 @@ int refcpu_seismograms(void* hv, double* out)
         std::copy(s->seis.begin(), s->seis.end(), out);
     }
     return 0;
+}
+
+// snapType 3 curl and div energies as double (elastic equations)
+int refcpu_curl_div(void* hv, double* curl, double* div)
+{
+    auto* h = static_cast<Handle*>(hv);
+    auto run = [&](auto* s) -> int {
+        using T = typename std::decay_t<decltype(s->M)>::value_type;
+        std::vector<T> c, d;
+        s->curlDiv(c, d);
+        std::copy(c.begin(), c.end(), curl);
+        std::copy(d.begin(), d.end(), div);
+        return 0;
+    };
+    try {
+        if (h->is_double) return run(static_cast<refcpu::Sim<double>*>(h->sim));
+        return run(static_cast<refcpu::Sim<float>*>(h->sim));
+    } catch (std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
 }
 
 // Copies a named wavefield ("vx", "sxx", "p", "ez", ... or "rxx0" for memory

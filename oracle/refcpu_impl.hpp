@@ -1053,6 +1053,43 @@ void Sim<T>::stepEM3D(int t)
     gather(t);
 }
 
+// snapType 3 energies: FD2Delastic::getCurl/getDiv (Wavefields2Delastic.cpp:218-250),
+// FD3Delastic::getCurl/getDiv (Wavefields3Delastic.cpp:197-240)
+template <class T>
+void Sim<T>::curlDiv(std::vector<T>& curl, std::vector<T>& div)
+{
+    const idx_t N = g.N();
+    curl.assign(N, 0);
+    div.assign(N, 0);
+    auto& vX = F["vx"];
+    auto& vY = F["vy"];
+    std::vector<T> a(N), b(N);
+    if (!is3d) {
+        Dyf.spmv(vX.data(), a.data());
+        Dxf.spmv(vY.data(), b.data());
+        VEC_OP(T c = a[i]; c -= b[i]; c *= std::sqrt(mu[i]); curl[i] = c);
+        Dxb.spmv(vX.data(), a.data());
+        Dyb.spmv(vY.data(), b.data());
+        VEC_OP(T d = a[i]; d += b[i]; d *= std::sqrt(M[i]); div[i] = d);
+        return;
+    }
+    auto& vZ = F["vz"];
+    Dyf.spmv(vZ.data(), a.data());
+    Dzf.spmv(vY.data(), b.data());
+    VEC_OP(T u = a[i] - b[i]; curl[i] = u * u);
+    Dzf.spmv(vX.data(), a.data());
+    Dxf.spmv(vZ.data(), b.data());
+    VEC_OP(T u = a[i] - b[i]; curl[i] += u * u);
+    Dxf.spmv(vY.data(), a.data());
+    Dyf.spmv(vX.data(), b.data());
+    VEC_OP(T u = a[i] - b[i]; curl[i] += u * u; curl[i] *= mu[i]; curl[i] = std::sqrt(curl[i]));
+    Dxb.spmv(vX.data(), a.data());
+    Dyb.spmv(vY.data(), b.data());
+    VEC_OP(div[i] = a[i] + b[i]);
+    Dzb.spmv(vZ.data(), a.data());
+    VEC_OP(T d = div[i] + a[i]; d *= d; d *= M[i]; div[i] = std::sqrt(d));
+}
+
 #undef VEC_OP
 
 } // namespace refcpu

@@ -25,10 +25,13 @@ def _setup(tmp_path, edits):
     for f in ("sources_ci.2D.txt", "receiver_ci.2D.txt"):
         shutil.copy(os.path.join(GOLDEN, f), ci / f)
     text = open(os.path.join(GOLDEN, "configuration_ci.2D.acoustic.txt")).read().splitlines()
-    out = []
+    out, seen = [], set()
     for line in text:
         key = line.split("=")[0].strip() if "=" in line else None
+        if key in edits:
+            seen.add(key)
         out.append(f"{key}={edits[key]}" if key in edits else line)
+    out += [f"{k}={v}" for k, v in edits.items() if k not in seen]
     cfg = ci / "configuration.txt"
     cfg.write_text("\n".join(out) + "\n")
     return cfg, ci
@@ -60,3 +63,27 @@ def test_driver_mtx_output_with_normalisation_and_resampling(wave, tmp_path):
     ref = resample_reference(golden / np.abs(golden).max(axis=1, keepdims=True), 2e-3, 6e-3)
     assert got.shape == ref.shape
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-4
+
+
+def test_driver_snapshots_equal_the_solver_fields(wave, tmp_path):
+    cfg, ci = _setup(tmp_path, {"snapType": "1", "tFirstSnapshot": "0.2", "tlastSnapshot": "0.6", "tincSnapshot": "0.2",
+                                "WavefieldFileName": "ci/wavefield"})
+    _run(wave, cfg)
+    wc = wave.WaveConfig.from_file(str(cfg))
+    s = wave.Factory.Create("2D", "acoustic").initForwardSolver(wc)
+    s.prepareForModelling(dict(rho=np.full(wc.N, 2000.0, np.float32), vp=np.full(wc.N, 3500.0, np.float32)))
+    src = [l.split() for l in open(ci / "sources_ci.2D.txt") if l.strip() and not l.startswith("#")][0]
+    x, y, z, typ, shape, fc, amp, ts = (int(src[1]), int(src[2]), int(src[3]), int(src[4]), int(src[6]), float(src[7]),
+                                        float(src[8]), float(src[9]))
+    s.setSources(np.array([x + wc.NX * y], np.int64), np.array([typ], np.int32),
+                 wave.wavelet(shape, s.nt, wc.DT, fc, amp, ts)[None])
+    rec = [l.split() for l in open(ci / "receiver_ci.2D.txt") if l.strip() and not l.startswith("#")]
+    s.setReceivers(np.array([int(r[0]) + wc.NX * int(r[1]) for r in rec], np.int64), np.array([int(r[3]) for r in rec], np.int32))
+    t = 0
+    for step in (100, 200, 300):
+        s.run(t, step + 1)
+        t = step + 1
+        for name in ("VX", "VY"):
+            snap = refcpu.read_mtx_array(str(ci / f"wavefield.shot_1.{name}.{step}.mtx"))[:, 0]
+            assert np.array_equal(snap.astype(np.float32), s.field(name)), (name, step)
+    s.close()

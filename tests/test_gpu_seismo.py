@@ -52,3 +52,58 @@ def test_normalize_matches_reference(wave, mode):
         ref = d / n[:, None]
     np.testing.assert_allclose(got, ref, rtol=2e-6, atol=0)
     assert np.array_equal(got[4], d[4])
+
+
+def _next_pow2(n):
+    t = np.float32(np.log(np.float32(n)))
+    t = np.float32(t / np.log(2.0))
+    return int(np.float32(2.0) ** np.ceil(t))
+
+
+def hilbert_reference(d):
+    """HilbertFFT (HilbertFFT.cpp): zero padding to the next power of two of
+    nt-1, weights 1 / 2 / 0 over the spectrum, 1/N, inverse FFT, imaginary part."""
+    nt = d.shape[1]
+    N = max(_next_pow2(nt - 1), nt)
+    f = np.fft.fft(d.astype(np.float64), n=N, axis=1)
+    w = np.zeros(N)
+    if N % 2 == 0:
+        w[0] = w[N // 2] = 1.0
+        w[1:N // 2] = 2.0
+    else:
+        w[0] = 1.0
+        w[1:(N + 1) // 2] = 2.0
+    return np.fft.ifft(f * w, axis=1).imag[:, :nt]
+
+
+@pytest.mark.parametrize("nt", [1000, 513, 64, 37])
+def test_envelope_matches_fft_hilbert(wave, nt):
+    rng = np.random.default_rng(nt)
+    t = np.arange(nt)
+    d = (np.sin(0.07 * t)[None, :] * rng.uniform(0.5, 2, (5, 1)) + 0.1 * rng.standard_normal((5, nt))).astype(np.float32)
+    got = wave.envelope(d)
+    ref = np.sqrt(d.astype(np.float64) ** 2 + hilbert_reference(d) ** 2)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+
+
+@pytest.mark.parametrize("ptype", [1, 2, 3])
+def test_instantaneous_phase_as_reference(wave, ptype):
+    d = np.random.default_rng(ptype).standard_normal((4, 200)).astype(np.float32)
+    got = wave.instantaneous_phase(d, ptype)
+    imag = -d.astype(np.float64)              # Common.hpp:301-302: the imaginary part is -data there
+    if ptype == 1:
+        ref = np.arctan(imag / d)
+    else:
+        ref = np.arctan2(imag, d)
+        if ptype == 3:
+            ref = np.unwrap(ref, axis=1)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-5)
+
+
+def test_normalize_mode4_envelope(wave):
+    d = np.random.default_rng(9).standard_normal((6, 300)).astype(np.float32)
+    got = wave.normalize_traces(d, 4)
+    l2 = d / np.sqrt((d.astype(np.float64) ** 2).sum(axis=1, keepdims=True))
+    env = np.sqrt(l2 ** 2 + hilbert_reference(l2) ** 2)
+    ref = l2 / (env + 1e-3 * env.max(axis=1, keepdims=True))
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5

@@ -42,7 +42,8 @@ ABI_SYMBOLS = (
     "wave_batch_shot", "wave_batch_step", "wave_batch_get_stream", "wave_batch_get_launch_count",
     "wave_batch_last_error", "wave_average_shear_modulus_noalloc", "wave_adjoint_gradient",
     "wave_batch_adjoint_gradient", "wave_resample_traces", "wave_normalize_traces", "wave_read_mtx",
-    "wave_write_mtx", "wave_write_su",
+    "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
+    "wave_instantaneous_phase",
 )
 
 
@@ -168,6 +169,10 @@ def lib():
     L.wave_read_mtx.argtypes = [ctypes.c_char_p, P, i64, ctypes.POINTER(i64), ctypes.POINTER(i64)]
     L.wave_write_mtx.argtypes = [ctypes.c_char_p, P, i64, i64]
     L.wave_write_su.argtypes = [ctypes.c_char_p, P, i64, i64, ctypes.c_double, P, i64, i64, i64, i64, ctypes.c_double]
+    L.wave_get_field.argtypes = [P, ctypes.c_char_p, P, I]
+    L.wave_get_curl_div.argtypes = [P, P, P, I]
+    L.wave_envelope.argtypes = [P, i64, i64, I]
+    L.wave_instantaneous_phase.argtypes = [P, i64, i64, I, I]
     L.wave_batch_adjoint_gradient.argtypes = [P, P, I, I, ctypes.POINTER(ctypes.c_double), P, P, P, I, I]
     L.wave_batch_create.argtypes = [P, I, CP(P)]
     L.wave_batch_destroy.argtypes = [P]
@@ -233,9 +238,22 @@ def resample_traces(data, dt: float, seismo_dt: float):
 
 
 def normalize_traces(data, mode: int):
-    """Seismogram::normalizeTrace modes 0..2 (wave_normalize_traces); returns a new array."""
+    """Seismogram::normalizeTrace modes 0, 1, 2, 4 (wave_normalize_traces); returns a new array."""
     d = np.array(data, dtype=np.float32, order="C", copy=True)
     _check(None, lib().wave_normalize_traces(d.ctypes.data_as(ctypes.c_void_p), d.shape[0], d.shape[1], mode, MEM_HOST))
+    return d
+
+
+def envelope(data):
+    """Trace envelopes (wave_envelope); data: ntr x nt."""
+    d = np.array(data, dtype=np.float32, order="C", copy=True)
+    _check(None, lib().wave_envelope(d.ctypes.data_as(ctypes.c_void_p), d.shape[0], d.shape[1], MEM_HOST))
+    return d
+
+
+def instantaneous_phase(data, phase_type: int):
+    d = np.array(data, dtype=np.float32, order="C", copy=True)
+    _check(None, lib().wave_instantaneous_phase(d.ctypes.data_as(ctypes.c_void_p), d.shape[0], d.shape[1], phase_type, MEM_HOST))
     return d
 
 
@@ -387,6 +405,19 @@ class ForwardSolver:
                                                     g[0].ctypes.data_as(ctypes.c_void_p), g[1].ctypes.data_as(ctypes.c_void_p),
                                                     g[2].ctypes.data_as(ctypes.c_void_p), MEM_HOST))
         return J.value, g[0], g[1], g[2]
+
+    def field(self, name: str) -> np.ndarray:
+        """One wavefield (wave_get_field), e.g. "VX", "Sxx", "EZ"."""
+        out = np.zeros(self.cfg.N, dtype=np.float32)
+        _check(self.h, lib().wave_get_field(self.h, name.encode(), out.ctypes.data_as(ctypes.c_void_p), MEM_HOST))
+        return out
+
+    def curl_div(self):
+        """snapType 3 energies (wave_get_curl_div): (curl, div)."""
+        c = np.zeros(self.cfg.N, dtype=np.float32)
+        d = np.zeros(self.cfg.N, dtype=np.float32)
+        _check(self.h, lib().wave_get_curl_div(self.h, c.ctypes.data_as(ctypes.c_void_p), d.ctypes.data_as(ctypes.c_void_p), MEM_HOST))
+        return c, d
 
     def streaming_passes(self) -> int:
         """Bit 0: the velocity pass runs the streaming kernel; bit 1: the stress pass."""

@@ -12,6 +12,7 @@
 
 namespace wave {
 void set_global_error(const std::string& msg);
+cudaError_t envelope_device(float* d, long long ntr, long long nt, int mode);   // snapshot.cu
 }
 
 using namespace wave;
@@ -110,7 +111,8 @@ extern "C" int wave_resample_traces(const float* in, int64_t ntr, int64_t nt, do
 
 extern "C" int wave_normalize_traces(float* data, int64_t ntr, int64_t nt, int mode, int mem)
 {
-    if (!data || ntr < 0 || nt < 1 || mode < 0 || mode > 2) return err(WAVE_ERR_ARG, "wave_normalize_traces: invalid argument (mode 0, 1 or 2)");
+    if (!data || ntr < 0 || nt < 1 || mode < 0 || mode > 4 || mode == 3 || (mode == 4 && nt < 2))
+        return err(WAVE_ERR_ARG, "wave_normalize_traces: invalid argument (mode 0, 1, 2 or 4)");
     if (mode == 0 || ntr == 0) return WAVE_OK;
     float* d = data;
     float* t = nullptr;
@@ -121,10 +123,12 @@ extern "C" int wave_normalize_traces(float* data, int64_t ntr, int64_t nt, int m
         d = t;
     }
     if (e == cudaSuccess) {
-        normalize_kernel<<<static_cast<unsigned>(ntr), 256>>>(d, nt, mode);
+        normalize_kernel<<<static_cast<unsigned>(ntr), 256>>>(d, nt, mode == 1 ? 1 : 2);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    // mode 4: after the l2 normalisation, divide by the water-levelled envelope
+    if (e == cudaSuccess && mode == 4) e = envelope_device(d, ntr, nt, 1);
     if (e == cudaSuccess && mem != WAVE_MEM_DEVICE) e = cudaMemcpy(data, t, ntr * nt * sizeof(float), cudaMemcpyDeviceToHost);
     cudaFree(t);
     if (e != cudaSuccess) return err(WAVE_ERR_CUDA, std::string("wave_normalize_traces: ") + cudaGetErrorString(e));

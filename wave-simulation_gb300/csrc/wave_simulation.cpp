@@ -65,6 +65,29 @@ std::vector<float> read_mtx_vector(const std::string& path, size_t n)
     return v;
 }
 
+// wavefields written for snapType 1 / 2 (/ 4 for 2-D acoustic), as the
+// Wavefields*::write functions name them (Wavefields2Delastic.cpp:62-72, ...)
+std::vector<std::string> snapshot_fields(int eq, bool is3d, int snapType)
+{
+    const bool em = eq >= WAVE_EQ_TMEM;
+    if (em) {
+        if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_VISCOTMEM) return snapType == 1 ? std::vector<std::string>{"HX", "HY"} : std::vector<std::string>{"EZ"};
+        if (!is3d) return snapType == 1 ? std::vector<std::string>{"HZ"} : std::vector<std::string>{"EX", "EY"};
+        return snapType == 1 ? std::vector<std::string>{"HX", "HY", "HZ"} : std::vector<std::string>{"EX", "EY", "EZ"};
+    }
+    if (eq == WAVE_EQ_SH || eq == WAVE_EQ_VISCOSH) return snapType == 1 ? std::vector<std::string>{"VZ"} : std::vector<std::string>{"Sxz", "Syz"};
+    std::vector<std::string> v = is3d ? std::vector<std::string>{"VX", "VY", "VZ"} : std::vector<std::string>{"VX", "VY"};
+    if (eq == WAVE_EQ_ACOUSTIC) {
+        if (snapType == 1) return v;
+        if (snapType == 2) return {"P"};
+        if (snapType == 4 && !is3d) return {"P", "VX", "VY"};
+        return {};
+    }
+    if (snapType == 1) return v;
+    if (snapType == 2) return is3d ? std::vector<std::string>{"Sxx", "Syy", "Szz", "Sxy", "Sxz", "Syz"} : std::vector<std::string>{"Sxx", "Syy", "Sxy"};
+    return {};
+}
+
 } // namespace
 
 int main(int argc, char** argv)
@@ -150,7 +173,10 @@ int main(int argc, char** argv)
         const int normalize = key<int>(keys, "normalizeTraces", 0);
         const double seismoDT = key<double>(keys, "seismoDT", cfg.DT);
         const int format = key<int>(keys, "SeismogramFormat", 1);
-        if (normalize < 0 || normalize > 2) throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "normalizeTraces 3 (AGC) and 4 (envelope) are not built");
+        if (normalize < 0 || normalize > 4 || normalize == 3) throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "normalizeTraces 3 (AGC) is not built");
+        const int snapType = key<int>(keys, "snapType", 0);
+        if (snapType < 0 || snapType > 4) throw wave::gpu::Error(WAVE_ERR_ARG, "Invalid snapType.");
+        const int instantaneous = key<int>(keys, "outputInstantaneous", 0);
         if (format != 1 && format != 4) throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "SeismogramFormat: 1 (mtx) and 4 (su) are written here");
         for (int shot : shots) {
             wave::gpu::Acquisition src;
@@ -164,7 +190,35 @@ int main(int argc, char** argv)
             }
             solver->resetCPML();
             solver->setSources(src);
-            solver->run(0, nt);
+            // time loop with snapshots after the steps tFirst, tFirst + tinc, ... <= tLast (Simulation.cpp:468-475)
+            int t = 0;
+            if (snapType > 0) {
+                const int t1 = static_cast<int>(key<double>(keys, "tFirstSnapshot", 0.0) / cfg.DT + 0.5);
+                const int t2 = static_cast<int>(key<double>(keys, "tlastSnapshot", 0.0) / cfg.DT + 0.5);
+                int inc = static_cast<int>(key<double>(keys, "tincSnapshot", cfg.DT) / cfg.DT + 0.5);
+                if (inc < 1) inc = 1;
+                const std::string wbase = dir + "/../" + key<std::string>(keys, "WavefieldFileName", "wavefields/wavefield") + ".shot_" + std::to_string(shot);
+                const size_t npts = n;
+                for (int ts = t1; ts <= t2 && ts < nt; ts += inc) {
+                    solver->run(t, ts + 1);
+                    t = ts + 1;
+                    const std::string step = std::to_string(ts);
+                    if (snapType == 3) {
+                        std::vector<float> curl(npts), div(npts);
+                        wave::gpu::check(solver->handle(), wave_get_curl_div(solver->handle(), curl.data(), div.data(), WAVE_MEM_HOST));
+                        const bool big = cfg.dimension == 3;
+                        wave::gpu::check(nullptr, wave_write_mtx((wbase + (big ? ".CURL." : ".curl.") + step + ".mtx").c_str(), curl.data(), static_cast<int64_t>(npts), 1));
+                        wave::gpu::check(nullptr, wave_write_mtx((wbase + (big ? ".DIV." : ".div.") + step + ".mtx").c_str(), div.data(), static_cast<int64_t>(npts), 1));
+                    } else {
+                        std::vector<float> f(npts);
+                        for (const auto& name : snapshot_fields(cfg.equation, cfg.dimension == 3, snapType)) {
+                            wave::gpu::check(solver->handle(), wave_get_field(solver->handle(), name.c_str(), f.data(), WAVE_MEM_HOST));
+                            wave::gpu::check(nullptr, wave_write_mtx((wbase + "." + name + "." + step + ".mtx").c_str(), f.data(), static_cast<int64_t>(npts), 1));
+                        }
+                    }
+                }
+            }
+            solver->run(t, nt);
             auto seis = solver->seismograms();
             if (!solver->isFinite()) throw wave::gpu::Error(WAVE_ERR_NONFINITE, "Infinite or NaN value in seismogram or/and velocity wavefield!");
             for (int type = 1; type <= 4; ++type) {
@@ -193,6 +247,25 @@ int main(int argc, char** argv)
                                                            cfg.dimension == 3 ? cfg.NZ : 1, cfg.DH));
                 } else {
                     wave::gpu::check(nullptr, wave_write_mtx((base + ".mtx").c_str(), out.data(), ntr, ntOut));
+                }
+                // Seismogram::write: envelope or instantaneous phase of the written traces (Seismogram.cpp:127-145)
+                if ((instantaneous == 1 || instantaneous == 2) && ntOut >= 2) {
+                    std::string suffix = ".envelope";
+                    if (instantaneous == 1) wave::gpu::check(nullptr, wave_envelope(out.data(), ntr, ntOut, WAVE_MEM_HOST));
+                    else {
+                        wave::gpu::check(nullptr, wave_instantaneous_phase(out.data(), ntr, ntOut, 2, WAVE_MEM_HOST));
+                        suffix = ".instantaneousPhase";
+                    }
+                    if (format == 4) {
+                        std::vector<int64_t> ridx;
+                        for (size_t r = 0; r < rec.type.size(); ++r)
+                            if (rec.type[r] == type) ridx.push_back(rec.index[r]);
+                        wave::gpu::check(nullptr, wave_write_su((base + suffix + ".su").c_str(), out.data(), ntr, ntOut, seismoDT > 0 ? seismoDT : cfg.DT,
+                                                               ridx.data(), src.index.empty() ? 0 : src.index[0], cfg.NX, cfg.NY,
+                                                               cfg.dimension == 3 ? cfg.NZ : 1, cfg.DH));
+                    } else {
+                        wave::gpu::check(nullptr, wave_write_mtx((base + suffix + ".mtx").c_str(), out.data(), ntr, ntOut));
+                    }
                 }
             }
             std::cout << "shot " << shot << ": " << nt << " time steps done\n";
