@@ -243,6 +243,12 @@ int wave_write_mtx(const char* path, const float* data, int64_t rows, int64_t co
 int wave_write_su(const char* path, const float* data, int64_t ntr, int64_t ns, double dt, const int64_t* rec_idx, int64_t src_idx,
                   int64_t NX, int64_t NY, int64_t NZ, double DH);
 
+/* Diagnostic of the device-side failure path: runs the streaming kernels'
+ * bounded mbarrier wait on a barrier that never completes; *status receives
+ * WAVE_ERR_TIMEOUT when the wait gave up as designed (the context stays
+ * usable). No counterpart in the reference. */
+int wave_selftest_bounded_wait(int* status);
+
 /* ---- snapshots and trace attributes ---- */
 /* One wavefield of the handle ("VX", "VY", "VZ", "P", "Sxx", ..., "Syz", "HX",
  * "HY", "HZ", "EX", "EY", "EZ"; case-insensitive) into out (N floats), the

@@ -43,7 +43,7 @@ ABI_SYMBOLS = (
     "wave_batch_last_error", "wave_average_shear_modulus_noalloc", "wave_adjoint_gradient",
     "wave_batch_adjoint_gradient", "wave_resample_traces", "wave_normalize_traces", "wave_read_mtx",
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
-    "wave_instantaneous_phase",
+    "wave_instantaneous_phase", "wave_selftest_bounded_wait",
 )
 
 
@@ -169,6 +169,7 @@ def lib():
     L.wave_read_mtx.argtypes = [ctypes.c_char_p, P, i64, ctypes.POINTER(i64), ctypes.POINTER(i64)]
     L.wave_write_mtx.argtypes = [ctypes.c_char_p, P, i64, i64]
     L.wave_write_su.argtypes = [ctypes.c_char_p, P, i64, i64, ctypes.c_double, P, i64, i64, i64, i64, ctypes.c_double]
+    L.wave_selftest_bounded_wait.argtypes = [ctypes.POINTER(ctypes.c_int)]
     L.wave_get_field.argtypes = [P, ctypes.c_char_p, P, I]
     L.wave_get_curl_div.argtypes = [P, P, P, I]
     L.wave_envelope.argtypes = [P, i64, i64, I]

@@ -94,9 +94,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 }
 // bounded wait: gives up after 2^20 polls (well under a second of waiting for
 // copies that take microseconds); the caller reports it
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1u << 20)
 {
-    for (uint32_t i = 0; i < (1u << 20); ++i)
+    for (uint32_t i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -853,6 +853,20 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_str(const __grid_constant__ El3d
 }
 
 // ------------------------------------------------------------------------
+// self-test of the bounded wait: an mbarrier that nothing completes
+// ------------------------------------------------------------------------
+__global__ void wait_selftest_kernel(int* err, uint32_t limit)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait(&bar, 0, limit)) report(err, WAVE_ERR_TIMEOUT);
+}
+
+// ------------------------------------------------------------------------
 // host side: tensor maps and launches
 // ------------------------------------------------------------------------
 namespace {
@@ -1045,3 +1059,23 @@ cudaError_t el3d_launch(const El3dPlan& plan, const StepParams& P, int pass, cud
 }
 
 } // namespace wave
+
+// Runs the streaming kernels' bounded mbarrier wait on a barrier that no
+// thread and no copy ever completes: the wait gives up after 2^14 polls and
+// reports WAVE_ERR_TIMEOUT in *status, the kernel returns normally and the
+// context stays usable. Diagnostic of the device-side failure path.
+extern "C" int wave_selftest_bounded_wait(int* status)
+{
+    if (!status) return WAVE_ERR_ARG;
+    int* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        wave::wait_selftest_kernel<<<1, 32>>>(d, 1u << 14);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(status, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? WAVE_OK : WAVE_ERR_CUDA;
+}
