@@ -220,6 +220,14 @@ int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, 
 int wave_set_kernel_path(wave_handle* h, int path);
 int wave_get_kernel_path(wave_handle* h, int* streaming_active);
 
+/* Programmatic dependent launch of the one-thread-per-point kernels, the ABS
+ * frame and the source/receiver kernel (on = 1, the default): each such
+ * launch may be scheduled before its predecessor in the stream has finished
+ * and waits for it inside the kernel, so the launch latency between the
+ * 3-4 kernels of a step is hidden on small grids. Results do not depend on
+ * this switch. The reference has no counterpart. */
+int wave_set_dependent_launch(wave_handle* h, int on);
+
 /* ---- seismogram output path and file formats ---- */
 /* Resampling of ntr traces (row-major ntr x nt, sample interval dt) to
  * seismo_dt by linear interpolation (Common::calcResampleMat,

@@ -43,7 +43,7 @@ ABI_SYMBOLS = (
     "wave_batch_last_error", "wave_average_shear_modulus_noalloc", "wave_adjoint_gradient",
     "wave_batch_adjoint_gradient", "wave_resample_traces", "wave_normalize_traces", "wave_read_mtx",
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
-    "wave_instantaneous_phase", "wave_selftest_bounded_wait",
+    "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
 )
 
 
@@ -159,6 +159,7 @@ def lib():
     L.wave_get_kernel_times.argtypes = [P, CP(ctypes.c_double), CP(ctypes.c_double), CP(ctypes.c_longlong)]
     L.wave_wavelet.argtypes = [I, I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
     L.wave_set_kernel_path.argtypes = [P, I]
+    L.wave_set_dependent_launch.argtypes = [P, I]
     L.wave_get_kernel_path.argtypes = [P, CP(I)]
     L.wave_average_shear_modulus.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, I]
     L.wave_average_shear_modulus_noalloc.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, P]
@@ -392,6 +393,11 @@ class ForwardSolver:
         """0 = automatic (faster kernel per pass, timed when the model is set),
         1 = generic kernels, 2 = streaming TMA kernels wherever they apply."""
         _check(self.h, lib().wave_set_kernel_path(self.h, path))
+
+    def set_dependent_launch(self, on: bool):
+        """Programmatic dependent launch of the per-point kernels (default on);
+        the results do not depend on it."""
+        _check(self.h, lib().wave_set_dependent_launch(self.h, 1 if on else 0))
 
     def adjoint_gradient(self, dobs, checkpoint_every: int = 50):
         """Misfit J = 1/2 ||d - d_obs||^2 and its gradient w.r.t. (vp, vs, rho)

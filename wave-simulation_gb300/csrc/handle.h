@@ -58,6 +58,7 @@ struct wave_handle {
     El3dPlan el3d;
     int kernelPath = 0;          // 0 = automatic, 1 = generic kernels only, 2 = streaming where available
     int passStreaming[2] = {1, 1};   // automatic path: timed choice per pass (1 = streaming)
+    bool dependentLaunch = true;     // generic kernels launched with programmatic stream serialization
     long long stepsSinceReset = 0;   // steps run since creation or the last reset
     int* errWord = nullptr;      // device error word of the bounded waits
 

@@ -43,6 +43,7 @@ __device__ __forceinline__ void acoustic_v_body(const StepParams& P, const Pt& p
 template <int H>
 __global__ void __launch_bounds__(256) acoustic_v(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     acoustic_v_body<H>(P, p);
@@ -80,6 +81,7 @@ __device__ __forceinline__ void acoustic_p_body(const StepParams& P, const Pt& p
 template <int H>
 __global__ void __launch_bounds__(256) acoustic_p(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     acoustic_p_body<H>(P, p);
@@ -142,6 +144,7 @@ __device__ __forceinline__ void elastic_v_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) elastic_v(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     elastic_v_body<H>(P, p);
@@ -238,6 +241,7 @@ __device__ __forceinline__ void elastic_s_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) elastic_s(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     elastic_s_body<H>(P, p);
@@ -390,6 +394,7 @@ __device__ __forceinline__ void visco_s_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) visco_s(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     visco_s_body<H>(P, p);
@@ -423,6 +428,7 @@ __device__ __forceinline__ void sh_v_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) sh_v(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     sh_v_body<H>(P, p);
@@ -473,6 +479,7 @@ __device__ __forceinline__ void sh_s_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) sh_s(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     sh_s_body<H>(P, p);
@@ -510,6 +517,7 @@ __device__ __forceinline__ void tm_h_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) tm_h(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     tm_h_body<H>(P, p);
@@ -560,6 +568,7 @@ __device__ __forceinline__ void tm_e_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) tm_e(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     tm_e_body<H>(P, p);
@@ -592,6 +601,7 @@ __device__ __forceinline__ void te_h_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) te_h(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     te_h_body<H>(P, p);
@@ -631,6 +641,7 @@ __device__ __forceinline__ void te_e_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) te_e(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     te_e_body<H>(P, p);
@@ -678,6 +689,7 @@ __device__ __forceinline__ void em3_h_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) em3_h(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     em3_h_body<H>(P, p);
@@ -730,6 +742,7 @@ __device__ __forceinline__ void em3_e_body(const StepParams& P, const Pt& p)
 template <int H>
 __global__ void __launch_bounds__(256) em3_e(StepParams P)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     em3_e_body<H>(P, p);
@@ -761,6 +774,7 @@ __device__ __forceinline__ void abs_frame_body(const StepParams& P, const Pt& p,
 
 __global__ void __launch_bounds__(256) abs_frame_kernel(StepParams P, int f0, int f1, int f2)
 {
+    dependent_launch_prologue();
     Pt p;
     if (!point(P, p)) return;
     abs_frame_body(P, p, f0, f1, f2);
@@ -839,7 +853,11 @@ __device__ __forceinline__ void srcrec_body(const SrcRecParams& Q, int* tcounter
     if (threadIdx.x == 0) *tcounter = t + 1;
 }
 
-__global__ void __launch_bounds__(512) srcrec_kernel(SrcRecParams Q, int* tcounter) { srcrec_body(Q, tcounter); }
+__global__ void __launch_bounds__(512) srcrec_kernel(SrcRecParams Q, int* tcounter)
+{
+    dependent_launch_prologue();
+    srcrec_body(Q, tcounter);
+}
 
 // one block per shot, each with its own step counter
 __global__ void __launch_bounds__(512) srcrec_batch(const SrcRecParams* __restrict__ Qs, int* tcounters)
@@ -1111,14 +1129,37 @@ __global__ void set_counters_kernel(int* c, int n, int v)
 
 void launch_set_counters(int* c, int n, int v, cudaStream_t s) { set_counters_kernel<<<1, 256, 0, s>>>(c, n, v); }
 
-void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s)
+// Launch with programmatic stream serialization when dep is set: the kernel's
+// blocks may be scheduled before its predecessor in the stream completes and
+// wait in dependent_launch_prologue (kernel launch latency hidden on small grids).
+template <typename... Args>
+cudaError_t launch_maybe_dependent(void (*k)(Args...), dim3 grid, dim3 block, bool dep, cudaStream_t s, Args... args)
 {
-    srcrec_kernel<<<1, 512, 0, s>>>(Q, tcounter);
+    cudaLaunchConfig_t c{};
+    c.gridDim = grid;
+    c.blockDim = block;
+    c.stream = s;
+    cudaLaunchAttribute a[1];
+    a[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    a[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = a;
+    c.numAttrs = dep ? 1 : 0;
+    return cudaLaunchKernelEx(&c, k, args...);
 }
 
-void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s)
+cudaError_t launch_step_kernel(StepKernel k, dim3 grid, dim3 block, const StepParams& P, bool dep, cudaStream_t s)
 {
-    abs_frame_kernel<<<grid, block, 0, s>>>(P, f0, f1, f2);
+    return launch_maybe_dependent(k, grid, block, dep, s, P);
+}
+
+void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s, bool dep)
+{
+    launch_maybe_dependent(srcrec_kernel, dim3(1), dim3(512), dep, s, Q, tcounter);
+}
+
+void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s, bool dep)
+{
+    launch_maybe_dependent(abs_frame_kernel, grid, block, dep, s, P, f0, f1, f2);
 }
 
 void launch_finite(const float* a, long long n, int* flag, cudaStream_t s)

@@ -196,13 +196,13 @@ bool streaming_pass(const wave_handle* h, int pass)
     return h->kernelPath == 2 || h->passStreaming[pass] != 0;
 }
 
-void launch_pass(wave_handle* h, int pass)
+void launch_pass(wave_handle* h, int pass, bool dep = true)
 {
     if (streaming_pass(h, pass)) {
         h->check(el3d_launch(h->el3d, h->sp, pass, h->stream), "streaming kernel launch");
     } else {
         StepKernel k = kernel_for(kernel_eq(h->cfg.equation, h->is3d()), pass, h->H);
-        k<<<h->grid, h->block, 0, h->stream>>>(h->sp);
+        launch_step_kernel(k, h->grid, h->block, h->sp, dep && h->dependentLaunch, h->stream);
     }
 }
 
@@ -214,10 +214,10 @@ void launch_step(wave_handle* h)
     if (h->sp.abs) {
         const auto& p1 = h->pass1Fields;
         launch_abs_frame(h->sp, h->grid, h->block, p1.size() > 0 ? p1[0] : -1, p1.size() > 1 ? p1[1] : -1,
-                         p1.size() > 2 ? p1[2] : -1, h->stream);
+                         p1.size() > 2 ? p1[2] : -1, h->stream, h->dependentLaunch);
         h->launches += 1;
     }
-    launch_srcrec(h->sq, h->tcounter, h->stream);
+    launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
     h->launches += 1;
 }
 
@@ -226,9 +226,9 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
     cudaEvent_t a, b, c;
     cudaEventCreate(&a); cudaEventCreate(&b); cudaEventCreate(&c);
     cudaEventRecord(a, h->stream);
-    launch_pass(h, 0);
+    launch_pass(h, 0, false);
     cudaEventRecord(b, h->stream);
-    launch_pass(h, 1);
+    launch_pass(h, 1, false);
     cudaEventRecord(c, h->stream);
     ev.push_back(a); ev.push_back(b); ev.push_back(c);
     h->launches += 2;
@@ -926,6 +926,14 @@ int wave_set_kernel_path(wave_handle* h, int path)
     if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_kernel_path: null handle");
     if (path < 0 || path > 2) return fail(h, WAVE_ERR_ARG, "wave_set_kernel_path: path must be 0, 1 or 2");
     h->kernelPath = path;
+    h->graphDirty = true;
+    return WAVE_OK;
+}
+
+int wave_set_dependent_launch(wave_handle* h, int on)
+{
+    if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_dependent_launch: null handle");
+    h->dependentLaunch = on != 0;
     h->graphDirty = true;
     return WAVE_OK;
 }

@@ -13,6 +13,17 @@ namespace wave {
 // --------------------------------------------------------------------------
 // device helpers
 // --------------------------------------------------------------------------
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may be scheduled while its predecessor in the stream still
+// runs. It first lets its own dependent launch be scheduled, then waits until
+// the predecessor has completed and its writes are visible; no global memory
+// is touched before the wait. Both instructions are no-ops in a normal launch.
+__device__ __forceinline__ void dependent_launch_prologue()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // 1-D derivative along an axis with stride `st`; c = coordinate along the axis.
 // FWD: taps at offsets -H+1..H, else -H..H-1 (Derivatives.cpp:149, 728).
 template <int H, bool FWD>

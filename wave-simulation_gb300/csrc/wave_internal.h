@@ -123,13 +123,15 @@ constexpr int kEm3d = 100;
 inline int kernel_eq(int eq, bool is3d) { return (is3d && eq >= WAVE_EQ_TMEM) ? eq + kEm3d : eq; }
 using StepKernel = void (*)(StepParams);
 StepKernel kernel_for(int eq, int pass, int H);
-void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s);
+// dep: programmatic dependent launch (the kernel waits for its predecessor in-kernel)
+cudaError_t launch_step_kernel(StepKernel k, dim3 grid, dim3 block, const StepParams& P, bool dep, cudaStream_t s);
+void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s, bool dep = false);
 void launch_set_counter(int* c, int v, cudaStream_t s);
 void launch_set_counters(int* c, int n, int v, cudaStream_t s);
 void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const BatchTile* tiles, int ntiles, cudaStream_t s);
 void launch_batch_aux(const StepParams* Ps, const BatchTile* tiles, int ntiles, int f0, int f1, int f2,
                       const SrcRecParams* Qs, int* counters, int nshots, bool abs, cudaStream_t s);
-void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s);
+void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s, bool dep = false);
 void launch_finite(const float* a, long long n, int* flag, cudaStream_t s);
 void k_modulus(PrepParams G, const float* rho, const float* v, const float* tau, float sum, int clamp, float* out, cudaStream_t s);
 void k_inverse(PrepParams G, const float* a, float* out, cudaStream_t s);
