@@ -825,8 +825,8 @@ def main():
     ap.add_argument("--grid", type=int, default=256, help="cube edge (profiling captures use a smaller cube)")
     ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch", "fwi2d"])
     ap.add_argument("--shots", type=int, default=128, help="shots of the batched EM workload")
-    ap.add_argument("--kernel-path", type=int, default=0, choices=[0, 1, 2],
-                    help="3-D elastic kernels: 0 automatic, 1 generic, 2 streaming (profiling)")
+    ap.add_argument("--kernel-path", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="3-D elastic kernels: 0 automatic, 1 generic, 2 one-point streaming, 3 two-point streaming (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

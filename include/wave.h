@@ -210,13 +210,16 @@ int wave_average_shear_modulus(const float* mu, float* out, int64_t NX, int64_t 
  * caller. */
 int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, int64_t NY, int64_t NZ, int mode, void* stream);
 
-/* Kernel path: 0 = automatic, 1 = generic kernels only, 2 = the streaming
- * TMA kernels wherever they apply (3-D elastic grids with NX % 4 == 0 whose
- * 32x16 column tiles meet at most one CPML slab per axis). The automatic path
- * times both kernels of each pass when the model is set on an unstepped state
- * and keeps the faster one per pass. wave_get_kernel_path reports which passes
- * run the streaming kernels (bit 0 velocity pass, bit 1 stress pass). The
- * reference has no counterpart (LAMA picks its own SpMV kernels). */
+/* Kernel path: 0 = automatic, 1 = generic kernels only, 2 = the one-point
+ * streaming TMA kernels wherever they apply (3-D elastic grids with
+ * NX % 4 == 0 whose 32x8 column tiles meet at most one CPML slab per axis),
+ * 3 = the two-points-per-thread streaming kernels wherever they apply (64x8
+ * tiles, even x CPML slab width). The automatic path times the applicable
+ * kernels of each pass when the model is set on an unstepped state and keeps
+ * the fastest per pass. wave_get_kernel_path reports which passes run a
+ * streaming kernel (bit 0 velocity pass, bit 1 stress pass) and which of those
+ * run the two-point kernels (bit 2 velocity, bit 3 stress). The reference has
+ * no counterpart (LAMA picks its own SpMV kernels). */
 int wave_set_kernel_path(wave_handle* h, int path);
 int wave_get_kernel_path(wave_handle* h, int* streaming_active);
 

@@ -181,6 +181,35 @@ def test_streaming_elastic_kernels_match_oracle_and_generic(order, fs, boundary,
     assert rel(auto, generic) < 1e-5
 
 
+PAIRS = [
+    # (order, fs, boundary, stencil, reduce, (NX, NY, NZ)): 64-wide tiles meeting at most one x CPML slab
+    (8, 1, 2, 0, 1, (128, 50, 48)),
+    (2, 0, 1, 1, 0, (128, 33, 37)),
+    (4, 1, 1, 0, 0, (132, 38, 36)),
+    (12, 0, 2, 0, 1, (136, 45, 35)),
+    (6, 1, 0, 0, 1, (128, 40, 33)),
+    (10, 1, 2, 1, 0, (132, 41, 30)),
+]
+
+
+@pytest.mark.parametrize("order,fs,boundary,stencil,reduce,dims", PAIRS)
+def test_two_point_streaming_kernels_match_oracle_and_generic(order, fs, boundary, stencil, reduce, dims, wave, refcpu):
+    """The two-points-per-thread streaming kernels (path 3) against the FP64
+    oracle and the generic kernels."""
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "elastic", 3, order, fs, boundary, stencil, reduce,
+                                                          dims=dims)
+    o = refcpu.Oracle(cfg, model, sidx, stype, sig, ridx, rtype, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    wc = to_wave_cfg(wave, cfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    s32 = sig.astype(np.float32)
+    pairs = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=3, expect_streaming=True)
+    generic = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=1, expect_streaming=False)
+    assert rel(pairs, ref) < TOL, f"two-point streaming vs FP64 oracle {rel(pairs, ref):.3e}"
+    assert rel(pairs, generic) < 1e-5
+
+
 def test_multi_step_graph_equals_single_steps(wave, refcpu):
     cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "elastic", 2, 8, 1, 2)
     wc = to_wave_cfg(wave, cfg)

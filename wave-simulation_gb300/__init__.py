@@ -390,8 +390,9 @@ class ForwardSolver:
         return c.value
 
     def set_kernel_path(self, path: int):
-        """0 = automatic (faster kernel per pass, timed when the model is set),
-        1 = generic kernels, 2 = streaming TMA kernels wherever they apply."""
+        """0 = automatic (fastest kernel per pass, timed when the model is set),
+        1 = generic kernels, 2 = one-point streaming TMA kernels, 3 = two-point
+        streaming TMA kernels (2 and 3 wherever they apply)."""
         _check(self.h, lib().wave_set_kernel_path(self.h, path))
 
     def set_dependent_launch(self, on: bool):
@@ -427,7 +428,8 @@ class ForwardSolver:
         return c, d
 
     def streaming_passes(self) -> int:
-        """Bit 0: the velocity pass runs the streaming kernel; bit 1: the stress pass."""
+        """Bit 0: the velocity pass runs a streaming kernel; bit 1: the stress pass;
+        bits 2 / 3: that kernel is the two-points-per-thread one."""
         v = ctypes.c_int()
         _check(self.h, lib().wave_get_kernel_path(self.h, ctypes.byref(v)))
         return v.value

@@ -33,5 +33,8 @@ struct El3dPlan {
 bool el3d_prepare(El3dPlan& plan, const StepParams& P, const float* rho, const float* M, const float* mu, int H, int* errWord);
 // pass 0 = velocity, 1 = stress
 cudaError_t el3d_launch(const El3dPlan& plan, const StepParams& P, int pass, cudaStream_t s);
+// the same for the two-points-per-thread kernels (kernels_el3d_pairs.cu)
+bool el3d_prepare_pairs(El3dPlan& plan, const StepParams& P, const float* rho, const float* M, const float* mu, int H, int* errWord);
+cudaError_t el3d_launch_pairs(const El3dPlan& plan, const StepParams& P, int pass, cudaStream_t s);
 
 } // namespace wave

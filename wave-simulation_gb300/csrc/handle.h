@@ -54,10 +54,11 @@ struct wave_handle {
     cudaGraphExec_t graph = nullptr;
     bool graphDirty = true;
 
-    // streaming 3-D elastic path (kernels_el3d.cu)
-    El3dPlan el3d;
-    int kernelPath = 0;          // 0 = automatic, 1 = generic kernels only, 2 = streaming where available
-    int passStreaming[2] = {1, 1};   // automatic path: timed choice per pass (1 = streaming)
+    // streaming 3-D elastic paths (kernels_el3d.cu: one point per thread;
+    // kernels_el3d_pairs.cu: two x-adjacent points per thread)
+    El3dPlan el3d, el3dp;
+    int kernelPath = 0;          // 0 automatic, 1 generic only, 2 one-point streaming, 3 pair streaming (where available)
+    int passStreaming[2] = {0, 0};   // automatic path: timed choice per pass (0 generic, 1 one-point, 2 pair streaming)
     bool dependentLaunch = true;     // generic kernels launched with programmatic stream serialization
     long long stepsSinceReset = 0;   // steps run since creation or the last reset
     int* errWord = nullptr;      // device error word of the bounded waits

@@ -8,10 +8,10 @@
 // arrive through TMA bulk-tensor copies (cp.async.bulk.tensor.3d) into a
 // 3-stage shared-memory ring ("full" mbarriers carry the transaction
 // bytes). Each of the 8 warps computes one z row of the tile and releases a
-// stage through an "empty" mbarrier; thread 0 refills a stage once all warps
-// have released it, one iteration behind its own warp. Warps never meet at a
-// block barrier, so they run up to a ring's length apart and hide each
-// other's latency. Depth derivatives come from
+// stage by a shared-memory counter; the warp that releases a stage last
+// refills it at once, so copies lead the compute by two iterations. Warps
+// never meet at a block barrier, so they run up to a ring's length apart and
+// hide each other's latency. Depth derivatives come from
 // per-thread register queues (2H+1 planes), x- and z-derivatives from the
 // halo tiles in shared memory. Interior rows multiply compile-time FD
 // coefficients and scale once by DT/DH; edge rows (order reduction, zero
@@ -26,13 +26,14 @@
 #include <type_traits>
 
 #include "el3d.h"
+#include "el3d_common.cuh"
 
 namespace wave {
 
 namespace el3d {
 
-constexpr int TX = 32, TZ = 8, NTHR = TX * TZ, MAXSEG = 64;
-constexpr int NCWARP = NTHR / 32;                // warps of a CTA, one per z row of the tile
+constexpr int TX = 32, TZ = 8, NTHR = TX * TZ;
+static_assert(NTHR / 32 == NCWARP, "one warp per z row of the tile");
 constexpr int CB = TX * TZ * 4;                  // centre box bytes
 constexpr int PW = TX + 4, PH = TZ + 1;          // "+1" box (x0..x0+35, z0..z0+8)
 constexpr int PBYTES = PW * PH * 4;              // bytes one "+1" box copy delivers
@@ -43,110 +44,6 @@ __host__ __device__ constexpr int bw_of(int H) { return TX + 2 * hx_of(H); }
 __host__ __device__ constexpr int bh_of(int H) { return TZ + 2 * H; }
 __host__ __device__ constexpr int hbytes_of(int H) { return bw_of(H) * bh_of(H) * 4; }          // delivered
 __host__ __device__ constexpr int hb_of(int H) { return ((hbytes_of(H) + 127) / 128) * 128; }  // layout slot
-
-// Staggered FD coefficients (Derivatives::setFDCoef, Derivatives.cpp:2000-2042)
-// as compile-time constants, so that the interior taps are FFMAs with
-// immediates.
-__host__ __device__ constexpr float fdc(int q, int j)
-{
-    switch (q) {
-    case 2: return j == 0 ? -1.0f : 1.0f;
-    case 4: { constexpr double c[2] = {1.0 / 24.0, -9.0 / 8.0}; return static_cast<float>(j < 2 ? c[j] : -c[3 - j]); }
-    case 6: { constexpr double c[3] = {-3.0 / 640.0, 25.0 / 384.0, -75.0 / 64.0}; return static_cast<float>(j < 3 ? c[j] : -c[5 - j]); }
-    case 8: {
-        constexpr double c[4] = {5.0 / 7168.0, -49.0 / 5120.0, 245.0 / 3072.0, -1225.0 / 1024.0};
-        return static_cast<float>(j < 4 ? c[j] : -c[7 - j]);
-    }
-    case 10: {
-        constexpr double c[5] = {-8756999275442633.0 / 73786976294838206464.0, 8142668969129685.0 / 4611686018427387904.0,
-                                 -567.0 / 40960.0, 735.0 / 8192.0, -19845.0 / 16384.0};
-        return static_cast<float>(j < 5 ? c[j] : -c[9 - j]);
-    }
-    default: {
-        constexpr double c[6] = {6448335830095439.0 / 295147905179352825856.0, -1655620175512543.0 / 4611686018427387904.0,
-                                 6842103786556949.0 / 2305843009213693952.0, -628618285389933.0 / 36028797018963968.0,
-                                 436540475965291.0 / 4503599627370496.0, -2750204998582123.0 / 2251799813685248.0};
-        return static_cast<float>(j < 6 ? c[j] : -c[11 - j]);
-    }
-    }
-}
-
-// ---------------------------------------------------------------- PTX helpers
-__device__ __forceinline__ uint32_t saddr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(saddr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait: gives up after 2^20 polls (well under a second of waiting for
-// copies that take microseconds); the caller reports it
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1u << 20)
-{
-    for (uint32_t i = 0; i < limit; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int z, int y)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(saddr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(z), "r"(y), "r"(saddr(bar))
-        : "memory");
-}
-__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// ------------------------------------------------------------- work schedule
-// The CTA's work is the contiguous range [g0, g1) of the (tile, plane) space
-// (plane fastest). A run of planes of one tile is a segment; a segment of
-// length L takes L + 2H iterations: 2H to fill the depth queues, then one
-// compute plane per iteration. Iteration k of a segment starting at plane ya
-// fetches queue plane q = ya - H + k and computes plane c = ya - 2H + k.
-struct Segs {
-    int n;
-    int tile[MAXSEG], ya[MAXSEG], len[MAXSEG];
-};
-
-__device__ __forceinline__ int build_segments(Segs& S, long long g0, long long g1, int NY, int H)
-{
-    int n = 0, total = 0;
-    long long g = g0;
-    while (g < g1 && n < MAXSEG) {
-        const long long t = g / NY;
-        const long long gend = g1 < (t + 1) * NY ? g1 : (t + 1) * NY;
-        S.tile[n] = static_cast<int>(t);
-        S.ya[n] = static_cast<int>(g - t * NY);
-        S.len[n] = static_cast<int>(gend - g) + 2 * H;
-        total += S.len[n];
-        ++n;
-        g = gend;
-    }
-    S.n = n;
-    return total;
-}
-
-// cursor over the iterations of the CTA's segments
-struct Cursor {
-    int seg, k;
-    __device__ __forceinline__ void advance(const Segs& S)
-    {
-        if (++k == S.len[seg]) { ++seg; k = 0; }
-    }
-};
 
 // ------------------------------------------------------------ derivatives
 // Interior rows: compile-time coefficients, two interleaved partial sums (even
@@ -210,37 +107,6 @@ __device__ __forceinline__ float dqueue(const float (&q)[2 * H + 1], bool interi
     return acc;
 }
 
-__device__ __forceinline__ int slab_of(int c, const Cpml1D& p)
-{
-    if (!p.on) return -1;
-    if (p.n <= 2 * p.w) return c;
-    if (c < p.w) return p.lo ? c : -1;
-    if (c >= p.n - p.w) return c - (p.n - p.ns);
-    return -1;
-}
-
-// table row for coordinate c of an operator (edge rows only)
-__device__ __forceinline__ const float* row_of(const Op1D& op, int c)
-{
-    const int slot = op.full ? c : (c < op.E ? c : op.E + c - (op.n - op.E));
-    return op.tab + slot * kTabW + kMaxHalf;
-}
-__device__ __forceinline__ bool interior_of(const Op1D& op, int c) { return !op.full && c >= op.E && c < op.n - op.E; }
-
-__device__ __forceinline__ float abs_damp(const StepParams& P, int x, int y, int z)
-{
-    const int w = P.absW;
-    auto edge = [](int c, int n) { return !((n - 1 - c) < c) ? c : (n - 1 - c); };
-    const int dx = edge(x, P.NX), dy = edge(y, P.NY), dz = edge(z, P.NZ);
-    int m = dx < dy ? dx : dy;
-    m = m < dz ? m : dz;
-    if (P.fs && y < w) {
-        const int xz = !(dx < dz) ? dz : dx;
-        return (dz < w || dx < w) ? P.absCoeff[xz] : 1.0f;
-    }
-    return m < w ? P.absCoeff[m] : 1.0f;
-}
-
 // per-thread state of the current column: coordinates, edge flags, CPML
 // coefficients and psi offsets along x and z (fixed while the CTA marches
 // down one tile)
@@ -276,23 +142,6 @@ __device__ __forceinline__ void column_setup(Column& C, const StepParams& P, int
     C.wint = __all_sync(0xffffffffu, (C.xi && C.zi) || !C.ok);
 }
 
-// per-plane (CTA-uniform) state along y
-struct Plane {
-    int y;
-    bool yi;
-    int sy;
-    float ayf, byf, ayh, byh;
-};
-
-__device__ __forceinline__ void plane_setup(Plane& L, const StepParams& P, int y)
-{
-    L.y = y;
-    L.yi = interior_of(P.Dyf, y);
-    L.sy = P.useCpml ? slab_of(y, P.cy) : -1;
-    L.ayf = L.byf = L.ayh = L.byh = 0.0f;
-    if (L.sy >= 0) { L.ayf = P.cy.a_full[y]; L.byf = P.cy.b_full[y]; L.ayh = P.cy.a_half[y]; L.byh = P.cy.b_half[y]; }
-}
-
 __device__ __forceinline__ float* psi_x(const StepParams& P, int slot, const Column& C, int y)
 {
     return P.psi[slot] + C.px + (long long)P.cx.ns * P.NZ * y;
@@ -306,11 +155,6 @@ __device__ __forceinline__ float* psi_y(const StepParams& P, int slot, const Col
     return P.psi[slot] + C.x + (long long)P.NX * (C.z + (long long)P.NZ * L.sy);
 }
 
-__device__ __forceinline__ void report(int* err, int code)
-{
-    if (err) atomicExch(err, code);
-}
-
 } // namespace el3d
 
 using namespace el3d;
@@ -318,66 +162,6 @@ using namespace el3d;
 // ------------------------------------------------------------------------
 // pipeline skeleton shared by the two passes
 // ------------------------------------------------------------------------
-// Box coordinate (along x or z) of a tile's CPML memory-variable box in the
-// compact slab layout, or kNoBox when the tile lies outside both slabs. The
-// host checks that no tile meets both slabs of an axis.
-constexpr int kNoBox = -(1 << 30);
-
-__device__ __forceinline__ int slab_box(const Cpml1D& p, int c0, int T)
-{
-    if (!p.on) return kNoBox;
-    if (p.n <= 2 * p.w) return c0;
-    if (p.lo && c0 < p.w) return c0;
-    if (c0 + T > p.n - p.w) return c0 - (p.n - p.ns);
-    return kNoBox;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
-}
-
-// reciprocal by the hardware approximation (rcp.approx, 1 ulp)
-__device__ __forceinline__ float rcp_fast(float x)
-{
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
-// calcInverseAveragedParameter on a 2-point average (Modelparameter.cpp:336-420, 633-639)
-__device__ __forceinline__ float inv_avg2f(float a, float b, bool in)
-{
-    float s;
-    if (in) { s = 0.5f * a; s += 0.5f * b; }
-    else s = a;
-    const float r = rcp_fast(s);
-    return isfinite(r) ? r : 0.0f;
-}
-
-// harmonic 4-point modulus average with the edge fallbacks of
-// calc4PointAverageMatrixRow (Modelparameter.cpp:448-527) and the vacuum rule
-// of calcAveragedSWaveModulus (ModelparameterSeismic.cpp:421-432). i1..i4 are
-// the inverse moduli at the row point and its 2nd/3rd/4th neighbours; inA /
-// inB say whether the two axes of the plane stay inside the grid.
-__device__ __forceinline__ float harm4f(float i1, float i2, float i3, float i4, bool inA, bool inB)
-{
-    float s;
-    if (inA && inB) {
-        s = 0.25f * i1; s += 0.25f * i2; s += 0.25f * i3; s += 0.25f * i4;
-    } else if (inA) {
-        s = 0.5f * i2; s += 0.5f * i1;
-    } else if (inB) {
-        s = 0.5f * i3; s += 0.5f * i1;
-    } else {
-        s = i1;
-    }
-    const float r = rcp_fast(s);
-    return r < 4.0f ? 0.0f : r;
-}
-
-__device__ __forceinline__ float inv_clampedf(float mu) { return rcp_fast(mu < 1.0f ? 1.0f : mu); }
-
 // CPML::applyCPML (CPML.cpp:84-95): psi = b*psi + a*d; d += psi, with the old
 // psi staged in shared memory by the producer and the new one written to HBM
 __device__ __forceinline__ void cpml_s(float& d, float ps, float* gpsi, float a, float b)
@@ -430,88 +214,6 @@ __device__ __forceinline__ void issue_psi(const PsiBoxes& B, const CUtensorMap* 
         for (int j = 6; j < 9; ++j) tma_load(ps + j * CB, m + j, bar, x0, B.bz, c);
 }
 
-// The copy feeder, run by thread 0: issues iterations in order into the ring.
-struct Feeder {
-    Cursor cur{0, 0};
-    int issued = 0;
-};
-
-// fills the ring with iterations [0, NST)
-template <int NST, class IssueFn>
-__device__ __forceinline__ void start_feed(Feeder& F, const Segs& G, int total, IssueFn issue)
-{
-    for (int i = 0; i < NST && i < total; ++i) {
-        issue(i, F.cur);
-        F.cur.advance(G);
-        ++F.issued;
-    }
-}
-
-// waits (bounded) for the feeder's copies that may still be in flight
-template <int NST>
-__device__ __forceinline__ void drain(const Feeder& F, uint64_t* full)
-{
-    const int from = F.issued > NST ? F.issued - NST : 0;
-    for (int k = from; k < F.issued; ++k) mbar_wait(full + k % NST, (k / NST) & 1);
-}
-
-// Refills the stage of iteration j (all warps have released it) with
-// iteration j + NST. On a timed-out wait it sets the failure flag, waits for
-// its own copies in flight and returns false.
-template <int NST, class IssueFn>
-__device__ __forceinline__ bool refill(Feeder& F, const Segs& G, int j, int total, uint64_t* full, uint64_t* empty,
-                                       volatile int* failed, int* err, IssueFn issue)
-{
-    if (j < 0 || j + NST >= total) return true;
-    const int s = j % NST;
-    if (!mbar_wait(empty + s, (j / NST) & 1)) {
-        *failed = 1;
-        report(err, WAVE_ERR_TIMEOUT);
-        drain<NST>(F, full);
-        return false;
-    }
-    issue(s, F.cur);
-    F.cur.advance(G);
-    ++F.issued;
-    return true;
-}
-
-// common prologue: barrier init, schedule, abort check, tensor-map prefetch.
-// Returns the CTA's iteration count.
-template <int NST>
-__device__ __forceinline__ int prologue(Segs& G, uint64_t* full, uint64_t* empty, int* abortRun, volatile int* failed,
-                                        const StepParams& P, const El3dSched& S, int H, const El3dMaps& T)
-{
-    if (threadIdx.x < sizeof(El3dMaps) / sizeof(CUtensorMap)) {
-        const CUtensorMap* m = reinterpret_cast<const CUtensorMap*>(&T) + threadIdx.x;
-        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
-    }
-    const long long GT = (long long)S.ntx * S.ntz * P.NY;
-    const long long g0 = GT * blockIdx.x / gridDim.x, g1 = GT * (blockIdx.x + 1) / gridDim.x;
-    if (threadIdx.x == 0) {
-        // a failed wait in an earlier launch leaves the error word set: skip the work
-        *abortRun = (S.err && *reinterpret_cast<volatile int*>(S.err) != 0) ? 1 : 0;
-        *failed = 0;
-        for (int s = 0; s < NST; ++s) {
-            mbar_init(full + s, 1);
-            mbar_init(empty + s, NCWARP);
-        }
-        fence_barrier_init();
-        build_segments(G, g0, g1, P.NY, H);
-    }
-    __syncthreads();
-    int total = 0;
-    for (int k = 0; k < G.n; ++k) total += G.len[k];
-    return *abortRun ? 0 : total;
-}
-
-// consumer side of one iteration's end: the warp releases the stage
-__device__ __forceinline__ void release(uint64_t* empty)
-{
-    __syncwarp();
-    if ((threadIdx.x & 31) == 0) mbar_arrive(empty);
-}
-
 // ------------------------------------------------------------------------
 // velocity pass (ForwardSolver3Delastic.cpp:174-277)
 // ------------------------------------------------------------------------
@@ -522,11 +224,12 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_vel(const __grid_constant__ El3d
     constexpr int NST = L::NST, HX = hx_of(H), BW = bw_of(H), TT = TX * TZ;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * L::BYTES);
-    uint64_t* empty = full + NST;
+    unsigned* rel = reinterpret_cast<unsigned*>(full + NST);   // per-stage release counters
     __shared__ Segs G;
     __shared__ int abortRun;
     __shared__ volatile int failed;
-    const int total = prologue<NST>(G, full, empty, &abortRun, &failed, P, S, H, T);
+    __shared__ int issued;
+    const int total = prologue<NST>(G, full, rel, &abortRun, &failed, P, S, H, T);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     auto issue = [&](int s, const Cursor& cur) {
@@ -557,8 +260,7 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_vel(const __grid_constant__ El3d
             tma_load(cen + 5 * CB, &T.cVz, bar, x0, z0, c);
         }
     };
-    Feeder F;
-    if (threadIdx.x == 0) start_feed<NST>(F, G, total, issue);
+    if (threadIdx.x == 0) start_feed<NST>(G, total, &issued, issue);
 
     const int tid = threadIdx.x;    // x = x0 + lane, z = z0 + warp
     float qxy[2 * H + 1], qyy[2 * H + 1], qyz[2 * H + 1];
@@ -578,11 +280,10 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_vel(const __grid_constant__ El3d
         if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ);
         const int y = ya - 2 * H + cur.k;
         const bool compute = y >= ya;
-        if (!mbar_wait(full + s, (it / NST) & 1)) {
+        if (!__all_sync(0xffffffffu, mbar_wait(full + s, (it / NST) & 1))) {
             failed = 1;
             report(S.err, WAVE_ERR_TIMEOUT);
-            if (threadIdx.x == 0) drain<NST>(F, full);
-            return;
+            break;
         }
         const unsigned char* st = smem + s * L::BYTES;
         const float* cen = reinterpret_cast<const float*>(st + L::CEN);
@@ -655,12 +356,11 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_vel(const __grid_constant__ El3d
         r0 = rn;
         rx = rb[warp * PW + lane + 1];
         rz = rb[(warp + 1) * PW + lane];
-        release(empty + s);
-        // thread 0 refills the stage released one iteration earlier
-        if (threadIdx.x == 0) refill<NST>(F, G, it - 1, total, full, empty, &failed, S.err, issue);
-        if (failed) return;
+        release_and_refill<NST>(it, total, cur, G, rel, &issued, &failed, issue);
+        if (__any_sync(0xffffffffu, failed != 0)) break;
         cur.advance(G);
     }
+    finish_ring<NST>(full, &issued, &failed);
 }
 
 // ------------------------------------------------------------------------
@@ -673,11 +373,12 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_str(const __grid_constant__ El3d
     constexpr int NST = L::NST, HX = hx_of(H), BW = bw_of(H), TT = TX * TZ;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * L::BYTES);
-    uint64_t* empty = full + NST;
+    unsigned* rel = reinterpret_cast<unsigned*>(full + NST);   // per-stage release counters
     __shared__ Segs G;
     __shared__ int abortRun;
     __shared__ volatile int failed;
-    const int total = prologue<NST>(G, full, empty, &abortRun, &failed, P, S, H, T);
+    __shared__ int issued;
+    const int total = prologue<NST>(G, full, rel, &abortRun, &failed, P, S, H, T);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     auto issue = [&](int s, const Cursor& cur) {
@@ -710,8 +411,7 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_str(const __grid_constant__ El3d
             tma_load(cen + 9 * CB, &T.cM, bar, x0, z0, c);
         }
     };
-    Feeder F;
-    if (threadIdx.x == 0) start_feed<NST>(F, G, total, issue);
+    if (threadIdx.x == 0) start_feed<NST>(G, total, &issued, issue);
 
     const int tid = threadIdx.x;
     float qx[2 * H + 1], qy[2 * H + 1], qz[2 * H + 1];
@@ -730,11 +430,10 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_str(const __grid_constant__ El3d
         if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ);
         const int y = ya - 2 * H + cur.k;
         const bool compute = y >= ya;
-        if (!mbar_wait(full + s, (it / NST) & 1)) {
+        if (!__all_sync(0xffffffffu, mbar_wait(full + s, (it / NST) & 1))) {
             failed = 1;
             report(S.err, WAVE_ERR_TIMEOUT);
-            if (threadIdx.x == 0) drain<NST>(F, full);
-            return;
+            break;
         }
         const unsigned char* st = smem + s * L::BYTES;
         const float* cen = reinterpret_cast<const float*>(st + L::CEN);
@@ -844,12 +543,11 @@ __global__ void __launch_bounds__(NTHR, 2) el3d_str(const __grid_constant__ El3d
         // carry mu of plane y+1 into the next iteration
         m00 = n00;
         i00 = j00; i10 = j10; i01 = j01; i11 = j11;
-        release(empty + s);
-        // thread 0 refills the stage released one iteration earlier
-        if (threadIdx.x == 0) refill<NST>(F, G, it - 1, total, full, empty, &failed, S.err, issue);
-        if (failed) return;
+        release_and_refill<NST>(it, total, cur, G, rel, &issued, &failed, issue);
+        if (__any_sync(0xffffffffu, failed != 0)) break;
         cur.advance(G);
     }
+    finish_ring<NST>(full, &issued, &failed);
 }
 
 // ------------------------------------------------------------------------
@@ -871,49 +569,7 @@ __global__ void wait_selftest_kernel(int* err, uint32_t limit)
 // ------------------------------------------------------------------------
 namespace {
 
-using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
-                              const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeFn encoder()
-{
-    static EncodeFn fn = nullptr;
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeFn>(p);
-    }
-    return fn;
-}
-
-// 3-D fp32 map over a (d0 fastest, d1, d2) array with box (bx, bz, 1)
-bool make_map_dims(CUtensorMap* m, const float* base, int d0, int d1, int d2, int bx, int bz)
-{
-    EncodeFn enc = encoder();
-    if (!enc || d0 < 1 || d1 < 1 || d2 < 1) return false;
-    cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
-    cuuint64_t strides[2] = {(cuuint64_t)d0 * 4, (cuuint64_t)d0 * d1 * 4};
-    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)bz, 1};
-    cuuint32_t es[3] = {1, 1, 1};
-    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-bool make_map(CUtensorMap* m, const float* base, int NX, int NZ, int NY, int bx, int bz)
-{
-    EncodeFn enc = encoder();
-    if (!enc) return false;
-    cuuint64_t dims[3] = {(cuuint64_t)NX, (cuuint64_t)NZ, (cuuint64_t)NY};
-    cuuint64_t strides[2] = {(cuuint64_t)NX * 4, (cuuint64_t)NX * NZ * 4};
-    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)bz, 1};
-    cuuint32_t es[3] = {1, 1, 1};
-    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
+using namespace el3d_host;
 
 template <int H>
 size_t vel_smem() { return VelStage<H>::NST * (VelStage<H>::BYTES + 2 * sizeof(uint64_t)); }

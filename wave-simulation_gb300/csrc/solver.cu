@@ -189,22 +189,33 @@ bool type_ok(int eq, bool is3d, int type, bool source)
     }
 }
 
-// whether a pass runs the streaming TMA kernels
-bool streaming_pass(const wave_handle* h, int pass)
+// the kernel a pass runs: 0 generic, 1 one-point streaming, 2 pair streaming
+int pass_kernel(const wave_handle* h, int pass)
 {
-    if (!h->el3d.ready || h->kernelPath == 1) return false;
-    return h->kernelPath == 2 || h->passStreaming[pass] != 0;
+    switch (h->kernelPath) {
+    case 1: return 0;
+    case 2: return h->el3d.ready ? 1 : 0;
+    case 3: return h->el3dp.ready ? 2 : 0;
+    default: {
+        const int k = h->passStreaming[pass];
+        return (k == 1 && h->el3d.ready) || (k == 2 && h->el3dp.ready) ? k : 0;
+    }
+    }
 }
 
-void launch_pass(wave_handle* h, int pass, bool dep = true)
+void launch_kernel_of(wave_handle* h, int kind, int pass, bool dep)
 {
-    if (streaming_pass(h, pass)) {
+    if (kind == 1) {
         h->check(el3d_launch(h->el3d, h->sp, pass, h->stream), "streaming kernel launch");
+    } else if (kind == 2) {
+        h->check(el3d_launch_pairs(h->el3dp, h->sp, pass, h->stream), "streaming kernel launch");
     } else {
         StepKernel k = kernel_for(kernel_eq(h->cfg.equation, h->is3d()), pass, h->H);
         launch_step_kernel(k, h->grid, h->block, h->sp, dep && h->dependentLaunch, h->stream);
     }
 }
+
+void launch_pass(wave_handle* h, int pass, bool dep = true) { launch_kernel_of(h, pass_kernel(h, pass), pass, dep); }
 
 void launch_step(wave_handle* h)
 {
@@ -248,29 +259,32 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
 // updates are linear in the wavefields and there is no source term in them).
 void tune_passes(wave_handle* h)
 {
-    h->passStreaming[0] = h->passStreaming[1] = 1;
-    if (!h->el3d.ready || h->stepsSinceReset != 0) return;
+    h->passStreaming[0] = h->passStreaming[1] = h->el3dp.ready ? 2 : (h->el3d.ready ? 1 : 0);
+    if ((!h->el3d.ready && !h->el3dp.ready) || h->stepsSinceReset != 0) return;
     cudaEvent_t e0, e1;
     h->check(cudaEventCreate(&e0), "event");
     h->check(cudaEventCreate(&e1), "event");
-    float best[2][2] = {{0, 0}, {0, 0}};
-    for (int pass = 0; pass < 2; ++pass)
-        for (int path = 0; path < 2; ++path) {
-            auto launch = [&] {
-                if (path) h->check(el3d_launch(h->el3d, h->sp, pass, h->stream), "streaming kernel launch");
-                else kernel_for(kernel_eq(h->cfg.equation, h->is3d()), pass, h->H)<<<h->grid, h->block, 0, h->stream>>>(h->sp);
-            };
-            for (int k = 0; k < 2; ++k) launch();
+    const bool ready[3] = {true, h->el3d.ready, h->el3dp.ready};
+    for (int pass = 0; pass < 2; ++pass) {
+        float best = 0.0f;
+        for (int kind = 0; kind < 3; ++kind) {
+            if (!ready[kind]) continue;
+            for (int k = 0; k < 2; ++k) launch_kernel_of(h, kind, pass, false);
             h->check(cudaEventRecord(e0, h->stream), "event");
-            for (int k = 0; k < 5; ++k) launch();
+            for (int k = 0; k < 5; ++k) launch_kernel_of(h, kind, pass, false);
             h->check(cudaEventRecord(e1, h->stream), "event");
             h->check(cudaEventSynchronize(e1), "tuning");
-            h->check(cudaEventElapsedTime(&best[pass][path], e0, e1), "event");
+            float ms = 0.0f;
+            h->check(cudaEventElapsedTime(&ms, e0, e1), "event");
+            if (kind == 0 || ms <= best) {
+                best = ms;
+                h->passStreaming[pass] = kind;
+            }
         }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     h->check(cudaGetLastError(), "tuning launch");
-    for (int pass = 0; pass < 2; ++pass) h->passStreaming[pass] = best[pass][1] <= best[pass][0] ? 1 : 0;
     // the state was zero and stays zero; clear it anyway so tuning leaves no trace
     for (int f : h->fields) h->check(cudaMemsetAsync(h->f[f], 0, h->N * sizeof(float), h->stream), "memset");
     for (int rr = 0; rr < R_COUNT; ++rr)
@@ -576,6 +590,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         h->check(cudaStreamSynchronize(s), "model preparation");
         if (eq == WAVE_EQ_ELASTIC && is3d) {
             el3d_prepare(h->el3d, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord);
+            el3d_prepare_pairs(h->el3dp, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord);
             tune_passes(h);
         }
         h->modelSet = true;
@@ -924,7 +939,7 @@ int wave_get_launch_count(wave_handle* h, long long* count)
 int wave_set_kernel_path(wave_handle* h, int path)
 {
     if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_kernel_path: null handle");
-    if (path < 0 || path > 2) return fail(h, WAVE_ERR_ARG, "wave_set_kernel_path: path must be 0, 1 or 2");
+    if (path < 0 || path > 3) return fail(h, WAVE_ERR_ARG, "wave_set_kernel_path: path must be 0, 1, 2 or 3");
     h->kernelPath = path;
     h->graphDirty = true;
     return WAVE_OK;
@@ -941,7 +956,8 @@ int wave_set_dependent_launch(wave_handle* h, int on)
 int wave_get_kernel_path(wave_handle* h, int* streamingActive)
 {
     if (!h || !streamingActive) return fail(h, WAVE_ERR_ARG, "wave_get_kernel_path: null argument");
-    *streamingActive = (streaming_pass(h, 0) ? 1 : 0) | (streaming_pass(h, 1) ? 2 : 0);
+    const int k0 = pass_kernel(h, 0), k1 = pass_kernel(h, 1);
+    *streamingActive = (k0 ? 1 : 0) | (k1 ? 2 : 0) | (k0 == 2 ? 4 : 0) | (k1 == 2 ? 8 : 0);
     return WAVE_OK;
 }
 
