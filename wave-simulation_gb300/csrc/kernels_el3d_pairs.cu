@@ -146,18 +146,64 @@ __device__ __forceinline__ float2 dx_int(const float* r, const Coef<H>& k)
     return acc;
 }
 
-// edge-table rows of the pair's points that lie on edge rows
-__device__ __forceinline__ float dx_row(const float* r, const float* row, int H)
-{
-    float a = 0.0f;
-    for (int t = -H; t <= H; ++t) a += __ldg(row + t) * r[t];
-    return a;
-}
+// Weighted x derivative used by the warps of the first and last x tile, whose
+// outer pairs hold edge rows: d = sum_t W[t] * (u[t], u[t+1]) over the
+// offsets t = -H..H of the pair's first point, with W the pair's row of the
+// x-weight table in shared memory (each point's edge-table row, or the
+// interior weights for an interior point). Uniform over the warp: no lane
+// diverges.
 template <int H>
-__device__ __forceinline__ void dx_fix(float2& d, const float* r, bool xi0, bool xi1, int x, const Op1D& op)
+__device__ __forceinline__ float2 dx_w(const float* r, const float2* W)
 {
-    if (!xi0) d.x = dx_row(r, row_of(op, x), H);
-    if (!xi1) d.y = dx_row(r + 1, row_of(op, x + 1), H);
+    constexpr int A0 = -H - ((H & 1) ? 1 : 0);
+    constexpr int NA = (H + 1 - A0) / 2 + 1;
+    float v[2 * NA];
+#pragma unroll
+    for (int m = 0; m < NA; ++m) {
+        const float2 t = ld2(r + A0 + 2 * m);
+        v[2 * m] = t.x;
+        v[2 * m + 1] = t.y;
+    }
+    float2 a0 = make_float2(0.0f, 0.0f), a1 = a0;
+#pragma unroll
+    for (int t = -H; t <= H; ++t) {
+        const float2 u = make_float2(v[t - A0], v[t + 1 - A0]);
+        if ((t + H) & 1) a1 = fma2(W[t + H], u, a1);
+        else a0 = fma2(W[t + H], u, a0);
+    }
+    return add2(a0, a1);
+}
+
+// rows of the x-weight table: 0 = interior pair, 1..NL = pairs starting at
+// x = 0, 2, .., 2NL-2, NL+1..2NL = pairs starting at NX-2NL, .., NX-2, where
+// NL pairs cover the edge band of H+1 columns on each side
+template <int H>
+struct XRows {
+    static constexpr int NL = (H + 2) / 2;
+    static constexpr int N = 1 + 2 * NL;
+};
+__device__ __forceinline__ int xrow_of(int xs, int NX, int NL)
+{
+    if (xs < 2 * NL) return 1 + xs / 2;
+    if (xs >= NX - 2 * NL) return 1 + NL + (xs - (NX - 2 * NL)) / 2;
+    return 0;
+}
+// weight of the point at column c for offset t (edge-table row or interior weights)
+__device__ __forceinline__ float xweight(const Op1D& op, int c, int t)
+{
+    return interior_of(op, c) ? op.w[kMaxHalf + t] : __ldg(row_of(op, c) + t);
+}
+// fills the table for two x operators (called by all threads before the first barrier)
+template <int H>
+__device__ __forceinline__ void fill_xw(float2 (*xw)[XRows<H>::N][2 * H + 1], const Op1D& op0, const Op1D& op1, int NX)
+{
+    constexpr int NL = XRows<H>::NL, NR = XRows<H>::N, NT = 2 * H + 1;
+    for (int e = threadIdx.x; e < 2 * NR * NT; e += blockDim.x) {
+        const int o = e / (NR * NT), r = (e / NT) % NR, t = e % NT - H;
+        const Op1D& op = o ? op1 : op0;
+        const int xs = r == 0 ? NX / 2 - (NX / 2) % 2 : (r <= NL ? 2 * (r - 1) : NX - 2 * NL + 2 * (r - NL - 1));
+        xw[o][r][t + H] = make_float2(xweight(op, xs, t), xweight(op, xs + 1, t));
+    }
 }
 
 // along z (row stride BW): every row of the pair is aligned
@@ -206,20 +252,22 @@ __device__ __forceinline__ float2 dy_tab(const float2 (&q)[2 * H + 1], const flo
 struct ColumnP {
     int x, z;                 // x: first point of the pair (even)
     bool ok;                  // the pair lies inside the grid (NX is even)
-    bool xi0, xi1, zi;        // interior rows along x (each point) and z
+    bool zi;                  // interior row along z
+    int xr;                   // row of the x-weight table (0: interior pair)
+    bool xedge;               // some pair of the warp uses an edge row of the x-weight table
     int sx, sz;               // CPML slab indices (-1 outside); x + 1 is slab index sx + 1
     float2 axf, bxf, axh, bxh;
     float azf, bzf, azh, bzh;
     long long px, pz;         // psi offsets without the y term
 };
 
-__device__ __forceinline__ void column_setup(ColumnP& C, const StepParams& P, int x0, int z0)
+__device__ __forceinline__ void column_setup(ColumnP& C, const StepParams& P, int x0, int z0, int NL)
 {
     C.x = x0 + 2 * (threadIdx.x & 31);
     C.z = z0 + (threadIdx.x >> 5);
     C.ok = C.x < P.NX && C.z < P.NZ;
-    C.xi0 = interior_of(P.Dxf, C.x);
-    C.xi1 = interior_of(P.Dxf, C.x + 1);
+    C.xr = C.ok ? xrow_of(C.x, P.NX, NL) : 0;
+    C.xedge = __any_sync(0xffffffffu, C.xr != 0);
     C.zi = interior_of(P.Dzf, C.z);
     C.sx = P.useCpml && C.ok ? slab_of(C.x, P.cx) : -1;
     C.sz = P.useCpml && C.ok ? slab_of(C.z, P.cz) : -1;
@@ -311,6 +359,8 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_vel(const __grid_c
     __shared__ int abortRun;
     __shared__ volatile int failed;
     __shared__ int issued;
+    __shared__ float2 xw[2][XRows<H>::N][2 * H + 1];   // x weights: Dxf, Dxb
+    fill_xw<H>(xw, P.Dxf, P.Dxb, P.NX);
     const int total = prologue<NST>(G, full, rel, &abortRun, &failed, P, S, H, T);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -362,7 +412,7 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_vel(const __grid_c
     for (; it < total; ++it) {
         const int s = it % NST;
         const int tile = G.tile[cur.seg], ya = G.ya[cur.seg];
-        if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ);
+        if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ, XRows<H>::NL);
         const int y = ya - 2 * H + cur.k;
         const bool compute = y >= ya;
         if (!__all_sync(0xffffffffu, mbar_wait(full + s, (it / NST) & 1))) {
@@ -392,13 +442,15 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_vel(const __grid_c
             const float* ryf = Y.yi ? nullptr : row_of(DyfS, y);
             const long long i = C.x + (long long)P.NX * (C.z + (long long)P.NZ * y);
             {
-                float2 dSxx_x = dx_int<H, true>(hSxx, K);
-                float2 dSxy_x = dx_int<H, false>(hSxy, K);
-                float2 dSxz_x = dx_int<H, false>(hSxz, K);
-                if (!(C.xi0 && C.xi1)) {
-                    dx_fix<H>(dSxx_x, hSxx, C.xi0, C.xi1, C.x, P.Dxf);
-                    dx_fix<H>(dSxy_x, hSxy, C.xi0, C.xi1, C.x, P.Dxb);
-                    dx_fix<H>(dSxz_x, hSxz, C.xi0, C.xi1, C.x, P.Dxb);
+                float2 dSxx_x, dSxy_x, dSxz_x;
+                if (C.xedge) {
+                    dSxx_x = dx_w<H>(hSxx, xw[0][C.xr]);
+                    dSxy_x = dx_w<H>(hSxy, xw[1][C.xr]);
+                    dSxz_x = dx_w<H>(hSxz, xw[1][C.xr]);
+                } else {
+                    dSxx_x = dx_int<H, true>(hSxx, K);
+                    dSxy_x = dx_int<H, false>(hSxy, K);
+                    dSxz_x = dx_int<H, false>(hSxz, K);
                 }
                 float2 dSxy_y, dSyy_y, dSyz_y;
                 if (Y.yi) {
@@ -473,6 +525,8 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_str(const __grid_c
     __shared__ int abortRun;
     __shared__ volatile int failed;
     __shared__ int issued;
+    __shared__ float2 xw[2][XRows<H>::N][2 * H + 1];   // x weights: Dxb, Dxf
+    fill_xw<H>(xw, P.Dxb, P.Dxf, P.NX);
     const int total = prologue<NST>(G, full, rel, &abortRun, &failed, P, S, H, T);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -525,7 +579,7 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_str(const __grid_c
     for (; it < total; ++it) {
         const int s = it % NST;
         const int tile = G.tile[cur.seg], ya = G.ya[cur.seg];
-        if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ);
+        if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ, XRows<H>::NL);
         const int y = ya - 2 * H + cur.k;
         const bool compute = y >= ya;
         if (!__all_sync(0xffffffffu, mbar_wait(full + s, (it / NST) & 1))) {
@@ -553,13 +607,15 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_str(const __grid_c
             const long long i = C.x + (long long)P.NX * (C.z + (long long)P.NZ * y);
             const bool x2in = C.x + 2 < P.NX, inY = y + 1 < P.NY, inZ = C.z + 1 < P.NZ;
             {
-                float2 vxx = dx_int<H, false>(hVx, K);
-                float2 vyx = dx_int<H, true>(hVy, K);
-                float2 vzx = dx_int<H, true>(hVz, K);
-                if (!(C.xi0 && C.xi1)) {
-                    dx_fix<H>(vxx, hVx, C.xi0, C.xi1, C.x, P.Dxb);
-                    dx_fix<H>(vyx, hVy, C.xi0, C.xi1, C.x, P.Dxf);
-                    dx_fix<H>(vzx, hVz, C.xi0, C.xi1, C.x, P.Dxf);
+                float2 vxx, vyx, vzx;
+                if (C.xedge) {
+                    vxx = dx_w<H>(hVx, xw[0][C.xr]);
+                    vyx = dx_w<H>(hVy, xw[1][C.xr]);
+                    vzx = dx_w<H>(hVz, xw[1][C.xr]);
+                } else {
+                    vxx = dx_int<H, false>(hVx, K);
+                    vyx = dx_int<H, true>(hVy, K);
+                    vzx = dx_int<H, true>(hVz, K);
                 }
                 float2 vyy, vxy, vzy;
                 if (Y.yi) {
@@ -748,6 +804,8 @@ bool el3d_prepare_pairs(El3dPlan& plan, const StepParams& P, const float* rho, c
     if (!P.is3d || H < 1 || H > 6 || (P.NX % 4) != 0 || P.NX < 8 || P.NZ < 2) return false;
     if (!rho || !M || !mu) return false;
     if (P.useCpml && (!slab_tiles_ok(P.cx, TX, true) || !slab_tiles_ok(P.cz, TZ, false))) return false;
+    // the x-weight table holds the edge bands of both sides and one interior pair
+    if (P.Dxf.full || P.Dxb.full || P.Dxf.E > H + 1 || P.Dxb.E > H + 1 || P.NX < 4 * ((H + 2) / 2) + 4) return false;
     const int bx = bw_of(H), bz = bh_of(H);
     El3dMaps& T = plan.maps;
     bool ok = true;
