@@ -306,12 +306,15 @@ def run_gpu(args):
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = load_traffic()
     step_alg = ALG_BYTES_PER_PT * N + 2 * psi_b
-    names = {"velocity": "el3d_vel<4> (TMA streaming)" if passes & 1 else "elastic_v<4> (generic)",
-             "stress": "el3d_str<4> (TMA streaming)" if passes & 2 else "elastic_s<4> (generic)"}
+    def kname(pass_bit, pair_bit, base):
+        if passes & pair_bit:
+            return f"el3dp_{base}<4> (TMA streaming, two points per thread)"
+        return f"el3d_{base}<4> (TMA streaming)" if passes & pass_bit else f"elastic_{base[0]}<4> (generic)"
+    names = {"velocity": kname(1, 4, "vel"), "stress": kname(2, 8, "str")}
     roof = {"bound": "hbm", "kernel": names[dominant], "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth (burst)",
             "traffic": (traffic or {}).get(names[dominant].split("<")[0]),
-            "traffic_note": "DRAM bytes per launch: ncu ratio to algorithmic bytes at 160^3 times the 256^3 algorithmic bytes",
+            "traffic_note": (traffic or {}).get("notes", {}).get(names[dominant].split("<")[0]),
             "alg_bytes_per_launch": dom_bytes,
             "step_pair": {"alg_bytes_per_step": step_alg, "ms": vel_ms + str_ms,
                           "achieved": step_alg / ((vel_ms + str_ms) * 1e-3) / 1e9,
@@ -819,7 +822,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=40, help="full-grid CPU oracle steps for cpu_baseline (at most 30 s)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube edge (profiling captures use a smaller cube)")

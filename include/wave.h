@@ -214,9 +214,10 @@ int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, 
  * streaming TMA kernels wherever they apply (3-D elastic grids with
  * NX % 4 == 0 whose 32x8 column tiles meet at most one CPML slab per axis),
  * 3 = the two-points-per-thread streaming kernels wherever they apply (64x8
- * tiles, even x CPML slab width). The automatic path times the applicable
- * kernels of each pass when the model is set on an unstepped state and keeps
- * the fastest per pass. wave_get_kernel_path reports which passes run a
+ * tiles, even x CPML slab width). The automatic path times the generic
+ * kernel and the streaming kernel that applies (the two-point one where it
+ * applies) of each pass when the model is set on an unstepped state and keeps
+ * the faster per pass. wave_get_kernel_path reports which passes run a
  * streaming kernel (bit 0 velocity pass, bit 1 stress pass) and which of those
  * run the two-point kernels (bit 2 velocity, bit 3 stress). The reference has
  * no counterpart (LAMA picks its own SpMV kernels). */

@@ -264,14 +264,17 @@ void tune_passes(wave_handle* h)
     cudaEvent_t e0, e1;
     h->check(cudaEventCreate(&e0), "event");
     h->check(cudaEventCreate(&e1), "event");
-    const bool ready[3] = {true, h->el3d.ready, h->el3dp.ready};
+    // candidates: the generic kernels and the streaming kernels that apply
+    // (the two-point ones where they apply: on GB300 they beat the one-point
+    // ones on every measured grid)
+    const bool ready[3] = {true, h->el3d.ready && !h->el3dp.ready, h->el3dp.ready};
     for (int pass = 0; pass < 2; ++pass) {
         float best = 0.0f;
         for (int kind = 0; kind < 3; ++kind) {
             if (!ready[kind]) continue;
-            for (int k = 0; k < 2; ++k) launch_kernel_of(h, kind, pass, false);
+            launch_kernel_of(h, kind, pass, false);
             h->check(cudaEventRecord(e0, h->stream), "event");
-            for (int k = 0; k < 5; ++k) launch_kernel_of(h, kind, pass, false);
+            for (int k = 0; k < 3; ++k) launch_kernel_of(h, kind, pass, false);
             h->check(cudaEventRecord(e1, h->stream), "event");
             h->check(cudaEventSynchronize(e1), "tuning");
             float ms = 0.0f;
