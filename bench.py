@@ -559,9 +559,12 @@ def run_visco3d(args, wave):
     ms, clocks = _clocked(lambda: s.run(args.warmup, args.warmup + args.steps), torch.cuda.ExternalStream(s.stream()))
     launches = s.launch_count() - l0
     finite = s.check_finite()
+    passes = s.streaming_passes()
     s.close()
     ms_step = ms / args.steps
     value = n * args.steps / (ms * 1e-3) / 1e9
+    vel_kernel = ("el3dp_vel<2> (TMA streaming, two points per thread)" if passes & 4 else
+                  "el3d_vel<2> (TMA streaming)" if passes & 1 else "elastic_v<2> (generic)")
     w = 20
     psi_pts = 2 * w * NYv * NZv + 2 * w * NXv * NYv + 2 * w * NXv * NZv
     alg = 4 * (2 * (9 + 6 * 2) + 5) * n + 6 * 8 * psi_pts       # 188 B/pt + psi
@@ -592,7 +595,7 @@ def run_visco3d(args, wave):
     cfgd = {"workload": f"3-D visco-elastic {NXv}x{NYv}(depth)x{NZv}, order 4, L=2, 20-pt CPML, DT=5e-4, NT=4000, 4096 receivers",
             "grid": [NXv, NYv, NZv], "order": 4, "L": 2, "l2": "inputs larger than L2 (state 21 x N x 4 B)",
             "parallelism": "1 GPU"}
-    _line(UNIT, value, args.steps, args.warmup, ms_step, cfgd, _roof(alg, ms_step, "elastic_v<2> + visco_s<2>"),
+    _line(UNIT, value, args.steps, args.warmup, ms_step, cfgd, _roof(alg, ms_step, vel_kernel + " + visco_s<2> (generic)"),
           e2e, launches, clocks, cpu, {"finite": finite})
 
 

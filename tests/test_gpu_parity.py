@@ -210,6 +210,34 @@ def test_two_point_streaming_kernels_match_oracle_and_generic(order, fs, boundar
     assert rel(pairs, generic) < 1e-5
 
 
+@pytest.mark.parametrize("order,fs,boundary,dims", [(8, 1, 2, (128, 44, 40)), (4, 0, 1, (132, 40, 36))])
+def test_visco_elastic_streaming_velocity_pass(order, fs, boundary, dims, wave, refcpu):
+    """3-D visco-elastic: the streaming velocity kernels (paths 2 and 3) with
+    the generic memory-variable stress kernel, against the FP64 oracle and the
+    generic kernels."""
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "viscoelastic", 3, order, fs, boundary, dims=dims)
+    o = refcpu.Oracle(cfg, model, sidx, stype, sig, ridx, rtype, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    wc = to_wave_cfg(wave, cfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    s32 = sig.astype(np.float32)
+    generic = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=1, expect_streaming=False)
+    assert rel(generic, ref) < TOL
+    for path, bits in ((2, 0b0001), (3, 0b0101)):
+        s = wave.Factory.Create("3D", "viscoelastic").initForwardSolver(wc)
+        s.prepareForModelling(m32)
+        s.set_kernel_path(path)
+        assert s.streaming_passes() == bits
+        s.setSources(sidx, stype, s32)
+        s.setReceivers(ridx, rtype)
+        s.run(0, s.nt)
+        out = s.seismograms()
+        s.close()
+        assert rel(out, ref) < TOL, f"path {path} vs FP64 oracle {rel(out, ref):.3e}"
+        assert rel(out, generic) < 1e-5
+
+
 def test_multi_step_graph_equals_single_steps(wave, refcpu):
     cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "elastic", 2, 8, 1, 2)
     wc = to_wave_cfg(wave, cfg)

@@ -189,9 +189,12 @@ bool type_ok(int eq, bool is3d, int type, bool source)
     }
 }
 
-// the kernel a pass runs: 0 generic, 1 one-point streaming, 2 pair streaming
+// the kernel a pass runs: 0 generic, 1 one-point streaming, 2 pair streaming.
+// The streaming kernels cover both elastic passes and the velocity pass of the
+// visco-elastic step (the same update; its stress pass has memory variables).
 int pass_kernel(const wave_handle* h, int pass)
 {
+    if (pass == 1 && h->cfg.equation != WAVE_EQ_ELASTIC) return 0;
     switch (h->kernelPath) {
     case 1: return 0;
     case 2: return h->el3d.ready ? 1 : 0;
@@ -270,8 +273,9 @@ void tune_passes(wave_handle* h)
     const bool ready[3] = {true, h->el3d.ready && !h->el3dp.ready, h->el3dp.ready};
     for (int pass = 0; pass < 2; ++pass) {
         float best = 0.0f;
+        h->passStreaming[pass] = 0;
         for (int kind = 0; kind < 3; ++kind) {
-            if (!ready[kind]) continue;
+            if (!ready[kind] || (kind > 0 && pass == 1 && h->cfg.equation != WAVE_EQ_ELASTIC)) continue;
             launch_kernel_of(h, kind, pass, false);
             h->check(cudaEventRecord(e0, h->stream), "event");
             for (int k = 0; k < 3; ++k) launch_kernel_of(h, kind, pass, false);
@@ -591,7 +595,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         h->check(cudaGetLastError(), "model preparation");
         for (float* p : tmp) cudaFreeAsync(p, s);
         h->check(cudaStreamSynchronize(s), "model preparation");
-        if (eq == WAVE_EQ_ELASTIC && is3d) {
+        if ((eq == WAVE_EQ_ELASTIC || eq == WAVE_EQ_VISCOELASTIC) && is3d) {
             el3d_prepare(h->el3d, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord);
             el3d_prepare_pairs(h->el3dp, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord);
             tune_passes(h);
