@@ -75,8 +75,13 @@ __device__ __forceinline__ bool point(const StepParams& P, Pt& p)
     p.x = blockIdx.x * blockDim.x + threadIdx.x;
     const int r = blockIdx.y * blockDim.y + threadIdx.y;
     if (p.x >= P.NX || r >= P.NY * P.NZ) return false;
-    p.y = r / P.NZ;
-    p.z = r - p.y * P.NZ;
+    if (P.NZ == 1) {   // 2-D: no division
+        p.y = r;
+        p.z = 0;
+    } else {
+        p.y = r / P.NZ;
+        p.z = r - p.y * P.NZ;
+    }
     p.i = p.x + (long long)P.NX * (p.z + (long long)P.NZ * p.y);
     return true;
 }
@@ -98,8 +103,13 @@ __device__ __forceinline__ bool point_tile(const StepParams& P, const BatchTile&
     p.x = w.x0 + threadIdx.x;
     const int r = w.r0 + rr + threadIdx.y;
     if (p.x >= P.NX || r >= P.NY * P.NZ) return false;
-    p.y = r / P.NZ;
-    p.z = r - p.y * P.NZ;
+    if (P.NZ == 1) {   // 2-D: no division
+        p.y = r;
+        p.z = 0;
+    } else {
+        p.y = r / P.NZ;
+        p.z = r - p.y * P.NZ;
+    }
     p.i = p.x + (long long)P.NX * (p.z + (long long)P.NZ * p.y);
     return true;
 }
