@@ -317,7 +317,22 @@ struct Stage {
     static constexpr int BYTES = PSI + 9 * CB;
     static constexpr int NST = 2;
 };
-template <int H> using VelStage = Stage<H, 5, 6>;
+// The velocity stage carries each stress field only with the halo its
+// derivatives need: Sxx and Sxy along x (x-halo box), Syz and Szz along z
+// (z-halo box), Sxz along both.
+template <int H>
+struct VelStage {
+    static constexpr int XB = ((bw_of(H) * TZ * 4 + 127) / 128) * 128;   // x-halo box: BW x TZ
+    static constexpr int HB = hb_of(H);                                  // x- and z-halo box: BW x BH
+    static constexpr int ZB = ((TX * bh_of(H) * 4 + 127) / 128) * 128;   // z-halo box: TX x BH
+    static constexpr int OXX = 0, OXY = XB, OXZ = 2 * XB, OYZ = 2 * XB + HB, OZZ = OYZ + ZB;
+    static constexpr int CEN = OZZ + ZB;
+    static constexpr int PLUS = CEN + 6 * CB;
+    static constexpr int PSI = PLUS + PB;
+    static constexpr int BYTES = PSI + 9 * CB;
+    static constexpr int NST = 2;
+    static constexpr uint32_t HALO_TX = 2 * bw_of(H) * TZ * 4 + hbytes_of(H) + 2 * TX * bh_of(H) * 4;   // delivered halo bytes
+};
 template <int H> using StrStage = Stage<H, 3, 10>;
 
 struct PsiBoxes {
@@ -373,7 +388,7 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_vel(const __grid_c
         const int x0 = (tile % S.ntx) * TX, z0 = (tile / S.ntx) * TZ;
         const PsiBoxes B = compute ? psi_boxes(P, x0, z0, c) : PsiBoxes{kNoBox, kNoBox, -1};
         uint32_t bytes = 3 * CB + PBYTES + B.bytes();
-        if (compute) bytes += 5 * hbytes_of(H) + 3 * CB;
+        if (compute) bytes += L::HALO_TX + 3 * CB;
         mbar_expect_tx(bar, bytes);
         issue_psi(B, T.psV, st + L::PSI, bar, x0, z0, c);
         unsigned char* cen = st + L::CEN;
@@ -382,11 +397,11 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_vel(const __grid_c
         tma_load(cen + 2 * CB, &T.cSyz, bar, x0, z0, q);
         tma_load(st + L::PLUS, &T.pRho, bar, x0, z0, c + 1);
         if (compute) {
-            tma_load(st + 0 * L::HB, &T.hSxx, bar, x0 - HX, z0 - H, c);
-            tma_load(st + 1 * L::HB, &T.hSxy, bar, x0 - HX, z0 - H, c);
-            tma_load(st + 2 * L::HB, &T.hSxz, bar, x0 - HX, z0 - H, c);
-            tma_load(st + 3 * L::HB, &T.hSyz, bar, x0 - HX, z0 - H, c);
-            tma_load(st + 4 * L::HB, &T.hSzz, bar, x0 - HX, z0 - H, c);
+            tma_load(st + L::OXX, &T.hSxx, bar, x0 - HX, z0, c);
+            tma_load(st + L::OXY, &T.hSxy, bar, x0 - HX, z0, c);
+            tma_load(st + L::OXZ, &T.hSxz, bar, x0 - HX, z0 - H, c);
+            tma_load(st + L::OYZ, &T.hSyz, bar, x0, z0 - H, c);
+            tma_load(st + L::OZZ, &T.hSzz, bar, x0, z0 - H, c);
             tma_load(cen + 3 * CB, &T.cVx, bar, x0, z0, c);
             tma_load(cen + 4 * CB, &T.cVy, bar, x0, z0, c);
             tma_load(cen + 5 * CB, &T.cVz, bar, x0, z0, c);
@@ -395,7 +410,9 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_vel(const __grid_c
     if (threadIdx.x == 0) start_feed<NST>(G, total, &issued, issue);
 
     const int pi = warp * TX + 2 * lane;            // the pair in a centre / psi box
-    const int ci = (warp + H) * BW + (HX + 2 * lane);   // the pair in a halo box
+    const int ci = (warp + H) * BW + (HX + 2 * lane);   // the pair in the x- and z-halo box
+    const int xi = warp * BW + (HX + 2 * lane);         // the pair in an x-halo box
+    const int zi = (warp + H) * TX + 2 * lane;          // the pair in a z-halo box
     const int ri = warp * PW + 2 * lane;            // the pair in the "+1" box
     float2 qxy[2 * H + 1], qyy[2 * H + 1], qyz[2 * H + 1];
 #pragma unroll
@@ -432,11 +449,11 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_vel(const __grid_c
         if (compute && C.ok) {
             Plane Y;
             plane_setup(Y, P, y);
-            const float* hSxx = reinterpret_cast<const float*>(st + 0 * L::HB) + ci;
-            const float* hSxy = reinterpret_cast<const float*>(st + 1 * L::HB) + ci;
-            const float* hSxz = reinterpret_cast<const float*>(st + 2 * L::HB) + ci;
-            const float* hSyz = reinterpret_cast<const float*>(st + 3 * L::HB) + ci;
-            const float* hSzz = reinterpret_cast<const float*>(st + 4 * L::HB) + ci;
+            const float* hSxx = reinterpret_cast<const float*>(st + L::OXX) + xi;
+            const float* hSxy = reinterpret_cast<const float*>(st + L::OXY) + xi;
+            const float* hSxz = reinterpret_cast<const float*>(st + L::OXZ) + ci;
+            const float* hSyz = reinterpret_cast<const float*>(st + L::OYZ) + zi;
+            const float* hSzz = reinterpret_cast<const float*>(st + L::OZZ) + zi;
             const float* ps = reinterpret_cast<const float*>(st + L::PSI) + pi;
             const float* ryb = Y.yi ? nullptr : row_of(DybS, y);
             const float* ryf = Y.yi ? nullptr : row_of(DyfS, y);
@@ -465,12 +482,12 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_vel(const __grid_c
                 float2 dSxz_z, dSyz_z, dSzz_z;
                 if (C.zi) {
                     dSxz_z = dz_int<H, false>(hSxz, BW, K);
-                    dSyz_z = dz_int<H, false>(hSyz, BW, K);
-                    dSzz_z = dz_int<H, true>(hSzz, BW, K);
+                    dSyz_z = dz_int<H, false>(hSyz, TX, K);
+                    dSzz_z = dz_int<H, true>(hSzz, TX, K);
                 } else {
                     dSxz_z = dz_tab<H>(hSxz, BW, row_of(P.Dzb, C.z));
-                    dSyz_z = dz_tab<H>(hSyz, BW, row_of(P.Dzb, C.z));
-                    dSzz_z = dz_tab<H>(hSzz, BW, row_of(P.Dzf, C.z));
+                    dSyz_z = dz_tab<H>(hSyz, TX, row_of(P.Dzb, C.z));
+                    dSzz_z = dz_tab<H>(hSzz, TX, row_of(P.Dzf, C.z));
                 }
                 if (C.sx >= 0) {
                     cpml2(dSxx_x, ld2(ps + 0 * TT), psi_x(P, PS_SXX_X, C, y), C.axh, C.bxh);
@@ -809,11 +826,11 @@ bool el3d_prepare_pairs(El3dPlan& plan, const StepParams& P, const float* rho, c
     const int bx = bw_of(H), bz = bh_of(H);
     El3dMaps& T = plan.maps;
     bool ok = true;
-    ok &= make_map(&T.hSxx, P.f[F_SXX], P.NX, P.NZ, P.NY, bx, bz);
-    ok &= make_map(&T.hSxy, P.f[F_SXY], P.NX, P.NZ, P.NY, bx, bz);
-    ok &= make_map(&T.hSxz, P.f[F_SXZ], P.NX, P.NZ, P.NY, bx, bz);
-    ok &= make_map(&T.hSyz, P.f[F_SYZ], P.NX, P.NZ, P.NY, bx, bz);
-    ok &= make_map(&T.hSzz, P.f[F_SZZ], P.NX, P.NZ, P.NY, bx, bz);
+    ok &= make_map(&T.hSxx, P.f[F_SXX], P.NX, P.NZ, P.NY, bx, TZ);   // x halo only
+    ok &= make_map(&T.hSxy, P.f[F_SXY], P.NX, P.NZ, P.NY, bx, TZ);
+    ok &= make_map(&T.hSxz, P.f[F_SXZ], P.NX, P.NZ, P.NY, bx, bz);   // x and z halo
+    ok &= make_map(&T.hSyz, P.f[F_SYZ], P.NX, P.NZ, P.NY, TX, bz);   // z halo only
+    ok &= make_map(&T.hSzz, P.f[F_SZZ], P.NX, P.NZ, P.NY, TX, bz);
     ok &= make_map(&T.hVx, P.f[F_VX], P.NX, P.NZ, P.NY, bx, bz);
     ok &= make_map(&T.hVy, P.f[F_VY], P.NX, P.NZ, P.NY, bx, bz);
     ok &= make_map(&T.hVz, P.f[F_VZ], P.NX, P.NZ, P.NY, bx, bz);
