@@ -278,7 +278,7 @@ void tune_passes(wave_handle* h)
             if (!ready[kind] || (kind > 0 && pass == 1 && h->cfg.equation != WAVE_EQ_ELASTIC)) continue;
             launch_kernel_of(h, kind, pass, false);
             h->check(cudaEventRecord(e0, h->stream), "event");
-            for (int k = 0; k < 3; ++k) launch_kernel_of(h, kind, pass, false);
+            for (int k = 0; k < 2; ++k) launch_kernel_of(h, kind, pass, false);
             h->check(cudaEventRecord(e1, h->stream), "event");
             h->check(cudaEventSynchronize(e1), "tuning");
             float ms = 0.0f;
