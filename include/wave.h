@@ -243,8 +243,16 @@ int wave_resample_traces(const float* in, int64_t ntr, int64_t nt, double dt, do
 /* Seismogram::normalizeTrace (Seismogram.cpp:215-275) in place: mode 0 none,
  * 1 each trace divided by its max |value|, 2 by its l2 norm (a zero norm
  * divides by 1), 4 l2 norm then division by the envelope plus 1e-3 of its
- * maximum. AGC normalisation (mode 3) is not built. */
+ * maximum. Mode 3 (AGC) needs dt and the AGC frequency: wave_agc_normalize_traces. */
 int wave_normalize_traces(float* data, int64_t ntr, int64_t nt, int mode, int mem);
+/* AGC normalisation, normalizeTraces = 3 (Seismogram::calcInverseAGC,
+ * Seismogram.cpp:323-387, then normalizeTrace(3), :235-237), in place: the
+ * inverse AGC of the l2-normalised traces over a window of round(1/(f_agc dt))
+ * samples on each side (at most nt/2; the reference passes
+ * CenterFrequencyCPML as f_agc), then data = l2-normalised data x inverse AGC.
+ * inverse_agc (ntr x nt, may be NULL) receives the inverse AGC, which the
+ * reference writes as <seismogram>.<component>.inverseAGC.mtx. */
+int wave_agc_normalize_traces(float* data, int64_t ntr, int64_t nt, double dt, double f_agc, float* inverse_agc, int mem);
 /* MatrixMarket files (IO::readVector/writeMatrix with fileFormat 1, IO.hpp:21-145):
  * read "array" or "coordinate" real files into a row-major rows x cols buffer
  * (out == NULL: dimensions only); write a row-major matrix in array format. */

@@ -65,6 +65,26 @@ def test_driver_mtx_output_with_normalisation_and_resampling(wave, tmp_path):
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-4
 
 
+def test_driver_agc_normalisation_writes_the_inverse_agc(wave, tmp_path):
+    """normalizeTraces=3 (Simulation.cpp:521-525): the inverse AGC is written as
+    <seismogram>.shot_1.p.inverseAGC.mtx and the seismogram is the l2-normalised
+    trace times it; the AGC window comes from CenterFrequencyCPML."""
+    from test_gpu_seismo import agc_reference
+    cfg, ci = _setup(tmp_path, {"SeismogramFormat": "1", "normalizeTraces": "3", "CenterFrequencyCPML": "5.0"})
+    _run(wave, cfg)
+    got = refcpu.read_mtx_array(str(ci / "seismogram.2D.acoustic.ci.shot_1.p.mtx"))
+    inv = refcpu.read_mtx_array(str(ci / "seismogram.2D.acoustic.ci.shot_1.p.inverseAGC.mtx"))
+    keys = dict(line.split("#")[0].split("=", 1) for line in open(cfg).read().splitlines() if "=" in line.split("#")[0])
+    keys = {k.strip(): v.strip() for k, v in keys.items()}
+    dt, fc = float(keys["DT"]), float(keys.get("CenterFrequencyCPML", "5"))
+    golden = refcpu.read_mtx_array(os.path.join(GOLDEN, "seismogram.2D.acoustic.ref.p.mtx")).astype(np.float32)
+    ref, ref_inv = agc_reference(golden, dt, fc)
+    assert got.shape == ref.shape and inv.shape == ref_inv.shape
+    # the GPU seismogram differs from the reference golden at the 1e-5 level; the AGC output follows
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-3
+    assert np.linalg.norm(inv - ref_inv) / np.linalg.norm(ref_inv) < 1e-3
+
+
 def test_driver_snapshots_equal_the_solver_fields(wave, tmp_path):
     cfg, ci = _setup(tmp_path, {"snapType": "1", "tFirstSnapshot": "0.2", "tlastSnapshot": "0.6", "tincSnapshot": "0.2",
                                 "WavefieldFileName": "ci/wavefield"})

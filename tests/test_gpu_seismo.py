@@ -1,7 +1,8 @@
 """Seismogram output path on the GPU against numpy restatements of the
 reference: resampling to seismoDT (Common::calcResampleMat, Common.hpp:202-230,
-applied in Seismogram::write, Seismogram.cpp:109) and per-trace normalisation
-(Seismogram::normalizeTrace, Seismogram.cpp:215-240)."""
+applied in Seismogram::write, Seismogram.cpp:109), per-trace normalisation
+(Seismogram::normalizeTrace, Seismogram.cpp:215-240) and AGC normalisation
+(Seismogram::calcInverseAGC, Seismogram.cpp:323-387)."""
 import numpy as np
 import pytest
 
@@ -52,6 +53,63 @@ def test_normalize_matches_reference(wave, mode):
         ref = d / n[:, None]
     np.testing.assert_allclose(got, ref, rtol=2e-6, atol=0)
     assert np.array_equal(got[4], d[4])
+
+
+def agc_reference(d, dt, f):
+    """normalizeTraces 3 restated in FP32 (Seismogram::calcInverseAGC,
+    Seismogram.cpp:323-387, then normalizeTrace(3), :235-237): l2-normalised
+    traces, inverse AGC from a backward running window sum of squares, product."""
+    d = np.asarray(d, np.float32)
+    ntr, nt = d.shape
+    norm = np.sqrt((d.astype(np.float64) ** 2).sum(axis=1)).astype(np.float32)
+    norm = np.where(norm == 0, np.float32(1), norm)
+    nd = (d / norm[:, None]).astype(np.float32)
+    x = 1.0 / float(np.float32(f) * np.float32(dt))
+    nagc = min(int(np.floor(x + 0.5)), nt // 2)
+    total = np.float32(np.sqrt((nd.astype(np.float64) ** 2).sum()))
+    wl0 = np.float32(1e-3 * float(total) / nt / ntr)
+    inv = np.zeros_like(nd)
+    f32 = np.float32
+    for tr in range(ntr):
+        row = nd[tr]
+        ss = f32(0)
+        for t in range(nt):
+            ss = f32(ss + f32(row[t] * row[t]))
+        l2 = f32(np.sqrt(ss))
+        wl = f32(f32(l2 * l2) / f32(nt))
+        wl = f32(float(wl) * 1e-3) if wl != 0 else wl0
+        acc, win = f32(0), f32(nagc)
+        for t in range(nt - nagc, nt):
+            acc = f32(acc + f32(row[t] * row[t]))
+            acc = f32(acc + wl)
+        for t in range(nt - 1, -1, -1):
+            if t >= nt - nagc:
+                v = row[t - nagc]
+                acc = f32(f32(acc + f32(v * v)) + wl)
+                win = f32(win + f32(1))
+            elif t >= nagc:
+                a, b = row[t - nagc], row[t + nagc]
+                acc = f32(f32(acc + f32(a * a)) - f32(b * b))
+            else:
+                b = row[t + nagc]
+                acc = f32(f32(acc - f32(b * b)) - wl)
+                win = f32(win - f32(1))
+            with np.errstate(divide="ignore", invalid="ignore"):
+                r = f32(acc / win)
+            inv[tr, t] = f32(f32(1) / f32(np.sqrt(r))) if r > 0 else f32(0)
+    return (nd * inv).astype(np.float32), inv
+
+
+@pytest.mark.parametrize("ntr,nt,dt,f", [(7, 400, 1e-3, 15.0), (5, 301, 2e-3, 1.0), (4, 256, 5e-4, 500.0)])
+def test_agc_normalisation_matches_reference_formula(wave, ntr, nt, dt, f):
+    rng = np.random.default_rng(nt)
+    d = (rng.standard_normal((ntr, nt)) * np.exp(-np.linspace(0, 4, nt))[None, :]).astype(np.float32)
+    d[1] = 0.0                                   # a zero trace takes the global water level
+    got, inv = wave.agc_normalize_traces(d, dt, f)
+    ref, ref_inv = agc_reference(d, dt, f)
+    np.testing.assert_allclose(inv, ref_inv, rtol=1e-5, atol=0)
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-12)
+    assert np.all(np.isfinite(got))
 
 
 def _next_pow2(n):

@@ -44,6 +44,7 @@ ABI_SYMBOLS = (
     "wave_batch_adjoint_gradient", "wave_resample_traces", "wave_normalize_traces", "wave_read_mtx",
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
     "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
+    "wave_agc_normalize_traces",
 )
 
 
@@ -167,6 +168,7 @@ def lib():
     i64 = ctypes.c_int64
     L.wave_resample_traces.argtypes = [P, i64, i64, ctypes.c_double, ctypes.c_double, P, ctypes.POINTER(i64), I]
     L.wave_normalize_traces.argtypes = [P, i64, i64, I, I]
+    L.wave_agc_normalize_traces.argtypes = [P, i64, i64, ctypes.c_double, ctypes.c_double, P, I]
     L.wave_read_mtx.argtypes = [ctypes.c_char_p, P, i64, ctypes.POINTER(i64), ctypes.POINTER(i64)]
     L.wave_write_mtx.argtypes = [ctypes.c_char_p, P, i64, i64]
     L.wave_write_su.argtypes = [ctypes.c_char_p, P, i64, i64, ctypes.c_double, P, i64, i64, i64, i64, ctypes.c_double]
@@ -237,6 +239,16 @@ def resample_traces(data, dt: float, seismo_dt: float):
     _check(None, lib().wave_resample_traces(d.ctypes.data_as(ctypes.c_void_p), ntr, nt, dt, seismo_dt,
                                             out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(nout), MEM_HOST))
     return out
+
+
+def agc_normalize_traces(data, dt: float, f_agc: float):
+    """normalizeTraces 3 (wave_agc_normalize_traces): returns (AGC-normalised
+    traces, inverse AGC), both new arrays."""
+    d = np.ascontiguousarray(np.array(data, dtype=np.float32, copy=True))
+    inv = np.zeros_like(d)
+    _check(None, lib().wave_agc_normalize_traces(d.ctypes.data_as(ctypes.c_void_p), d.shape[0], d.shape[1], dt, f_agc,
+                                                 inv.ctypes.data_as(ctypes.c_void_p), MEM_HOST))
+    return d, inv
 
 
 def normalize_traces(data, mode: int):

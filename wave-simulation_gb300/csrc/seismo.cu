@@ -1,5 +1,6 @@
 // seismo.cu — the seismogram output path on the device: per-trace
-// normalisation (Seismogram::normalizeTrace, Seismogram.cpp:215-240) and
+// normalisation (Seismogram::normalizeTrace, Seismogram.cpp:215-240; AGC,
+// Seismogram::calcInverseAGC, :323-387) and
 // resampling to seismoDT (Seismogram::setSeismoDT + Common::calcResampleMat,
 // Seismogram.cpp:610-618, Common.hpp:202-230; applied as data * resampleMat
 // when a seismogram is written, Seismogram.cpp:109).
@@ -68,6 +69,68 @@ __global__ void normalize_kernel(float* data, long long nt, int mode)
     for (long long k = threadIdx.x; k < nt; k += blockDim.x) t[k] /= norm;
 }
 
+// Inverse AGC of one trace per thread (Seismogram::calcInverseAGC,
+// Seismogram.cpp:323-387) over the l2-normalised traces nd: a water level of
+// 1e-3 x (the trace's squared l2 norm / nt) (wl0 for a zero trace), then a
+// running sum of squares over the window [t - nagc, t + nagc] taken from the
+// last sample backwards (the window ramps in over the last nagc samples and
+// out over the first nagc, each sample adding its water level), inv[t] =
+// 1 / sqrt(sum / window) or 0. FP32 throughout, no contraction, in the
+// reference's order.
+__global__ void agc_kernel(const float* __restrict__ nd, long long ntr, long long nt, long long nagc, float wl0,
+                           float* __restrict__ inv)
+{
+    const long long tr = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (tr >= ntr) return;
+    const float* row = nd + tr * nt;
+    float* out = inv + tr * nt;
+    float ss = 0.0f;
+    for (long long t = 0; t < nt; ++t) ss = __fadd_rn(ss, __fmul_rn(row[t], row[t]));
+    const float l2 = sqrtf(ss);
+    float wl = __fdiv_rn(__fmul_rn(l2, l2), static_cast<float>(nt));
+    wl = wl != 0.0f ? static_cast<float>(static_cast<double>(wl) * 1e-3) : wl0;
+    float sum = 0.0f, win = static_cast<float>(nagc);
+    for (long long t = nt - nagc; t < nt; ++t) {
+        sum = __fadd_rn(sum, __fmul_rn(row[t], row[t]));
+        sum = __fadd_rn(sum, wl);
+    }
+    for (long long t = nt - 1; t >= 0; --t) {
+        if (t >= nt - nagc) {
+            const float v = row[t - nagc];
+            sum = __fadd_rn(sum, __fmul_rn(v, v));
+            sum = __fadd_rn(sum, wl);
+            win = __fadd_rn(win, 1.0f);
+        } else if (t >= nagc) {
+            const float a = row[t - nagc], b = row[t + nagc];
+            sum = __fadd_rn(sum, __fmul_rn(a, a));
+            sum = __fsub_rn(sum, __fmul_rn(b, b));
+        } else {
+            const float b = row[t + nagc];
+            sum = __fsub_rn(sum, __fmul_rn(b, b));
+            sum = __fsub_rn(sum, wl);
+            win = __fsub_rn(win, 1.0f);
+        }
+        float r = __fdiv_rn(sum, win);
+        r = r > 0.0f ? __fdiv_rn(1.0f, sqrtf(r)) : 0.0f;
+        out[t] = r;
+    }
+}
+
+__global__ void mul_kernel(float* __restrict__ a, const float* __restrict__ b, long long n)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        a[q] = __fmul_rn(a[q], b[q]);
+}
+
+__global__ void sumsq_kernel(const float* __restrict__ a, long long n, double* out)
+{
+    double acc = 0.0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        acc += static_cast<double>(a[q]) * a[q];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
 int err(int code, const std::string& m)
 {
     set_global_error(m);
@@ -132,5 +195,57 @@ extern "C" int wave_normalize_traces(float* data, int64_t ntr, int64_t nt, int m
     if (e == cudaSuccess && mem != WAVE_MEM_DEVICE) e = cudaMemcpy(data, t, ntr * nt * sizeof(float), cudaMemcpyDeviceToHost);
     cudaFree(t);
     if (e != cudaSuccess) return err(WAVE_ERR_CUDA, std::string("wave_normalize_traces: ") + cudaGetErrorString(e));
+    return WAVE_OK;
+}
+
+extern "C" int wave_agc_normalize_traces(float* data, int64_t ntr, int64_t nt, double dt, double f_agc, float* inverse_agc, int mem)
+{
+    if (!data || ntr < 0 || nt < 1 || !(dt > 0) || !(f_agc > 0)) return err(WAVE_ERR_ARG, "wave_agc_normalize_traces: invalid argument");
+    if (ntr == 0) return WAVE_OK;
+    // NAGC = round(1 / (f DT)) with f DT formed in FP32, at most nt / 2 (Seismogram.cpp:333-335)
+    const float prod = static_cast<float>(f_agc) * static_cast<float>(dt);
+    long long nagc = std::llround(1.0 / static_cast<double>(prod));
+    if (nagc > nt / 2) nagc = nt / 2;
+    if (nagc < 0) nagc = 0;
+    const size_t bytes = static_cast<size_t>(ntr) * nt * sizeof(float);
+    float *d = data, *nd = nullptr, *inv = nullptr, *tmp = nullptr;
+    double* acc = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (mem != WAVE_MEM_DEVICE) {
+        e = cudaMalloc(&tmp, bytes);
+        if (e == cudaSuccess) e = cudaMemcpy(tmp, data, bytes, cudaMemcpyHostToDevice);
+        d = tmp;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&nd, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&inv, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&acc, sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(acc, 0, sizeof(double));
+    // the l2-normalised copy (normalizeTrace(2) before the AGC)
+    if (e == cudaSuccess) e = cudaMemcpy(nd, d, bytes, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess) {
+        normalize_kernel<<<static_cast<unsigned>(ntr), 256>>>(nd, nt, 2);
+        sumsq_kernel<<<1216, 256>>>(nd, static_cast<long long>(ntr) * nt, acc);
+        e = cudaGetLastError();
+    }
+    double total = 0.0;
+    if (e == cudaSuccess) e = cudaMemcpy(&total, acc, sizeof(double), cudaMemcpyDeviceToHost);
+    // water level of a zero trace: 1e-3 x the l2 norm of all normalised traces / nt / ntr
+    const float wl0 = static_cast<float>(1e-3 * static_cast<double>(static_cast<float>(std::sqrt(total))) / nt / ntr);
+    if (e == cudaSuccess) {
+        agc_kernel<<<static_cast<unsigned>((ntr + 127) / 128), 128>>>(nd, ntr, nt, nagc, wl0, inv);
+        // normalizeTrace(3): the l2-normalised traces times the inverse AGC (Seismogram.cpp:235-237)
+        mul_kernel<<<1216, 256>>>(nd, inv, static_cast<long long>(ntr) * nt);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(d, nd, bytes, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess && mem != WAVE_MEM_DEVICE) e = cudaMemcpy(data, d, bytes, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && inverse_agc)
+        e = cudaMemcpy(inverse_agc, inv, bytes, mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(tmp);
+    cudaFree(nd);
+    cudaFree(inv);
+    cudaFree(acc);
+    if (e != cudaSuccess) return err(WAVE_ERR_CUDA, std::string("wave_agc_normalize_traces: ") + cudaGetErrorString(e));
     return WAVE_OK;
 }

@@ -4,7 +4,7 @@
 // velocityP/velocityS/rho keys, or MatrixMarket files <ModelFilename>.<p>.mtx
 // for ModelRead=1, FileFormat=1), loop over the shots of <SourceFilename>.txt,
 // generate the wavelets, run the time loop, normalise the traces
-// (normalizeTraces 0-2), resample them to seismoDT and write
+// (normalizeTraces 0-4), resample them to seismoDT and write
 // <SeismogramFilename>.shot_<n>.<c>.mtx (SeismogramFormat 1) or .su (4), as
 // Simulation.cpp:521-531 does.
 //
@@ -173,7 +173,7 @@ int main(int argc, char** argv)
         const int normalize = key<int>(keys, "normalizeTraces", 0);
         const double seismoDT = key<double>(keys, "seismoDT", cfg.DT);
         const int format = key<int>(keys, "SeismogramFormat", 1);
-        if (normalize < 0 || normalize > 4 || normalize == 3) throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "normalizeTraces 3 (AGC) is not built");
+        if (normalize < 0 || normalize > 4) throw wave::gpu::Error(WAVE_ERR_ARG, "normalizeTraces must be 0-4");
         const int snapType = key<int>(keys, "snapType", 0);
         if (snapType < 0 || snapType > 4) throw wave::gpu::Error(WAVE_ERR_ARG, "Invalid snapType.");
         const int instantaneous = key<int>(keys, "outputInstantaneous", 0);
@@ -231,13 +231,23 @@ int main(int argc, char** argv)
                     }
                 if (!ntr) continue;
                 // Seismogram::normalizeTrace, then the resampling of Seismogram::write
-                wave::gpu::check(nullptr, wave_normalize_traces(part.data(), ntr, nt, normalize, WAVE_MEM_HOST));
                 int64_t ntOut = 0;
                 wave::gpu::check(nullptr, wave_resample_traces(nullptr, ntr, nt, cfg.DT, seismoDT, nullptr, &ntOut, WAVE_MEM_HOST));
-                std::vector<float> out(static_cast<size_t>(ntr) * ntOut);
-                wave::gpu::check(nullptr, wave_resample_traces(part.data(), ntr, nt, cfg.DT, seismoDT, out.data(), &ntOut, WAVE_MEM_HOST));
                 const std::string base = dir + "/../" + key<std::string>(keys, "SeismogramFilename", "seismogram") + ".shot_" +
                                          std::to_string(shot) + "." + names[em ? 1 : 0][type - 1];
+                if (normalize == 3) {
+                    // Simulation.cpp:521-524: the inverse AGC (window from CenterFrequencyCPML) is written
+                    // resampled as <seismogram>.<component>.inverseAGC.mtx, then normalizeTrace(3)
+                    std::vector<float> inv(part.size()), invOut(static_cast<size_t>(ntr) * ntOut);
+                    wave::gpu::check(nullptr, wave_agc_normalize_traces(part.data(), ntr, nt, cfg.DT, cfg.CenterFrequencyCPML, inv.data(),
+                                                                        WAVE_MEM_HOST));
+                    wave::gpu::check(nullptr, wave_resample_traces(inv.data(), ntr, nt, cfg.DT, seismoDT, invOut.data(), &ntOut, WAVE_MEM_HOST));
+                    wave::gpu::check(nullptr, wave_write_mtx((base + ".inverseAGC.mtx").c_str(), invOut.data(), ntr, ntOut));
+                } else {
+                    wave::gpu::check(nullptr, wave_normalize_traces(part.data(), ntr, nt, normalize, WAVE_MEM_HOST));
+                }
+                std::vector<float> out(static_cast<size_t>(ntr) * ntOut);
+                wave::gpu::check(nullptr, wave_resample_traces(part.data(), ntr, nt, cfg.DT, seismoDT, out.data(), &ntOut, WAVE_MEM_HOST));
                 if (format == 4) {
                     std::vector<int64_t> ridx;
                     for (size_t r = 0; r < rec.type.size(); ++r)
