@@ -263,6 +263,8 @@ __global__ void __launch_bounds__(256) elastic_s_batch(const StepParams* __restr
 // ForwardSolver3Dviscoelastic.cpp:270-446, free surface
 // FreeSurface2Dviscoelastic.cpp / FreeSurface3Dviscoelastic.cpp:17-75
 template <int H>
+// The loops over stress components and relaxation mechanisms run to their
+// compile-time bounds with run-time guards, so that S and R stay in registers.
 __device__ __forceinline__ void visco_s_body(const StepParams& P, const Pt& p)
 {
     const int L = P.L;
@@ -279,33 +281,40 @@ __device__ __forceinline__ void visco_s_body(const StepParams& P, const Pt& p)
     float S[3], R[3][kMaxL];
     const int slotS[3] = {F_SXX, F_SYY, F_SZZ};
     const int slotR[3] = {R_XX, R_YY, R_ZZ};
-    for (int k = 0; k < nN; ++k) {
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) if (k < nN) {
         S[k] = P.f[slotS[k]][p.i];
-        for (int l = 0; l < L; ++l) R[k][l] = P.r[slotR[k]][l][p.i];
+        #pragma unroll
+        for (int l = 0; l < kMaxL; ++l) if (l < L) R[k][l] = P.r[slotR[k]][l][p.i];
     }
     float u = vxx;
     u += vyy;
     if (P.is3d) u += vzz;
     u *= M;
-    for (int l = 0; l < L; ++l) {
+    #pragma unroll
+    for (int l = 0; l < kMaxL; ++l) if (l < L) {
         float u2 = P.invRelax[l] * u;
         u2 *= tauP;
-        for (int k = 0; k < nN; ++k) {
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) if (k < nN) {
             S[k] += DTh * R[k][l];
             R[k][l] *= P.c1[l];
             R[k][l] -= u2;
         }
     }
     u *= opP;
-    for (int k = 0; k < nN; ++k) S[k] += u;
-    for (int k = 0; k < nN; ++k) {
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) if (k < nN) S[k] += u;
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) if (k < nN) {
         float sum;
         if (P.is3d) sum = k == 0 ? vyy + vzz : (k == 1 ? vxx + vzz : vxx + vyy);
         else sum = k == 0 ? vyy : vxx;
         u = sum;
         u *= mu;
         u *= 2.0f;
-        for (int l = 0; l < L; ++l) {
+        #pragma unroll
+        for (int l = 0; l < kMaxL; ++l) if (l < L) {
             float u2 = P.invRelax[l] * u;
             u2 *= tauS;
             R[k][l] += u2;
@@ -322,7 +331,8 @@ __device__ __forceinline__ void visco_s_body(const StepParams& P, const Pt& p)
     const int matMu[3] = {M_MUXY, M_MUXZ, M_MUYZ};
     const int matTau[3] = {M_TAUSXY, M_TAUSXZ, M_TAUSYZ};
     float Sh[3];
-    for (int k = 0; k < nS; ++k) {
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) if (k < nS) {
         float ut;
         if (k == 0) { u = dY<H, true>(P, p, vx, P.Dyf, PS_VXY); ut = dX<H, true>(P, p, vy, P.Dxf, PS_VYX); }
         else if (k == 1) { u = dZ<H, true>(P, p, vx, P.Dzf, PS_VXZ); ut = dX<H, true>(P, p, P.f[F_VZ], P.Dxf, PS_VZX); }
@@ -331,7 +341,8 @@ __device__ __forceinline__ void visco_s_body(const StepParams& P, const Pt& p)
         u *= LD(P.m[matMu[k]]);
         const float tauAv = LD(P.m[matTau[k]]);
         float s = P.f[slotSh[k]][p.i];
-        for (int l = 0; l < L; ++l) {
+        #pragma unroll
+        for (int l = 0; l < kMaxL; ++l) if (l < L) {
             float r = P.r[slotRh[k]][l][p.i];
             s += DTh * r;
             r *= P.c1[l];
@@ -358,37 +369,49 @@ __device__ __forceinline__ void visco_s_body(const StepParams& P, const Pt& p)
         const float hsum = P.is3d ? vxx + vzz : vxx;
         const int nx = P.is3d ? 2 : 1;
         const int kk[2] = {0, 2};
-        for (int l = 0; l < L; ++l)
-            for (int q = 0; q < nx; ++q) S[kk[q]] -= DTh * R[kk[q]][l];
-        for (int q = 0; q < nx; ++q) S[kk[q]] += sH * hsum;
-        for (int q = 0; q < nx; ++q) S[kk[q]] -= sV * vyy;
+        #pragma unroll
+        for (int l = 0; l < kMaxL; ++l) if (l < L)
+            #pragma unroll
+            for (int q = 0; q < 2; ++q) if (q < nx) S[kk[q]] -= DTh * R[kk[q]][l];
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) if (q < nx) S[kk[q]] += sH * hsum;
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) if (q < nx) S[kk[q]] -= sV * vyy;
         float t3 = 2.0f * mu * tauS;
         t3 -= M * tauP;
         float ratio = 2.0f * mu * opS;
         ratio /= M * opP;
         ratio -= 1.0f;
-        for (int l = 0; l < L; ++l) {
+        #pragma unroll
+        for (int l = 0; l < kMaxL; ++l) if (l < L) {
             float rv = t3; rv *= P.c2[l]; rv /= P.relaxTime[l];
             float rh = t3; rh *= ratio; rh *= P.c2[l]; rh /= P.relaxTime[l];
-            for (int q = 0; q < nx; ++q) {
+            #pragma unroll
+            for (int q = 0; q < 2; ++q) if (q < nx) {
                 R[kk[q]][l] += rh * hsum;
                 R[kk[q]][l] -= rv * vyy;
                 S[kk[q]] += DTh * R[kk[q]][l];
             }
         }
         S[1] = 0.0f;
-        for (int l = 0; l < L; ++l) R[1][l] = 0.0f;
+        #pragma unroll
+        for (int l = 0; l < kMaxL; ++l) if (l < L) R[1][l] = 0.0f;
     }
     if (P.abs) {
         const float d = absDamp(P, p);
-        for (int k = 0; k < nN; ++k) S[k] *= d;
-        for (int k = 0; k < nS; ++k) Sh[k] *= d;
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) if (k < nN) S[k] *= d;
+        #pragma unroll
+        for (int k = 0; k < 3; ++k) if (k < nS) Sh[k] *= d;
     }
-    for (int k = 0; k < nN; ++k) {
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) if (k < nN) {
         P.f[slotS[k]][p.i] = S[k];
-        for (int l = 0; l < L; ++l) P.r[slotR[k]][l][p.i] = R[k][l];
+        #pragma unroll
+        for (int l = 0; l < kMaxL; ++l) if (l < L) P.r[slotR[k]][l][p.i] = R[k][l];
     }
-    for (int k = 0; k < nS; ++k) P.f[slotSh[k]][p.i] = Sh[k];
+    #pragma unroll
+    for (int k = 0; k < 3; ++k) if (k < nS) P.f[slotSh[k]][p.i] = Sh[k];
 }
 
 template <int H>
