@@ -64,6 +64,8 @@ extern "C" {
  * Configuration keys (Configuration/Configuration.cpp:45-100, keys as read by
  * Simulation.cpp, Derivatives.cpp:12-55 and ForwardSolver.cpp:34-54).
  */
+#define WAVE_MAX_GRID_LAYERS 16
+
 typedef struct wave_config {
     int dimension;              /* "dimension": 2 or 3                               */
     int equation;               /* "equationType": WAVE_EQ_*                         */
@@ -91,6 +93,17 @@ typedef struct wave_config {
                                    seismograms (par/ci, seismogram.<case>.ref.<c>.mtx)
                                    were made with.
                                    Config key "edgeOrderReduction" (default 1).   */
+    /* Variable (discontinuous) grid, Acquisition/Coordinates.cpp:35-245 and
+     * Derivatives.cpp:852-1656. Acoustic equations only; CPML or no damping
+     * boundary. The grid's index space replaces NX*NY*NZ everywhere (model
+     * arrays, source/receiver indices, wavefields): see wave_grid_*. */
+    int useVariableGrid;        /* "useVariableGrid": layers of spacing DH*dhFactor   */
+    int useVariableFDoperators; /* "useVariableFDoperators": FD order per layer      */
+    int gridLayers;             /* rows of "gridConfigurationFilename" (1..16)       */
+    int gridInterface[WAVE_MAX_GRID_LAYERS]; /* column 0: first depth index of each
+                                   layer (the first is 0)                          */
+    int gridDHFactor[WAVE_MAX_GRID_LAYERS];  /* column 1: spacing factor, 3^n        */
+    int gridFDOrder[WAVE_MAX_GRID_LAYERS];   /* column 2: FD order of the layer      */
 } wave_config;
 
 typedef struct wave_handle wave_handle;
@@ -105,6 +118,19 @@ int wave_config_nt(const wave_config* cfg, int* nt);
  * Configuration.hpp:95-143). Missing mandatory keys -> WAVE_ERR_ARG. */
 int wave_config_from_file(const char* path, wave_config* cfg);
 
+/* Grid index space of a configuration: NX*NY*NZ points in the reference
+ * order x + z*NX + y*NX*NZ, or the variable grid's layered points
+ * (Coordinates::getNGridpoints, Coordinates.cpp:340-346). */
+int wave_grid_num_points(const wave_config* cfg, int64_t* n);
+/* Coordinates::coordinate2index (Coordinates.cpp:668-698): 1-D index of the
+ * fine-grid coordinate (x, y, z); on a coarse layer the coordinate is rounded
+ * down to the layer's points. WAVE_ERR_ARG outside the grid. */
+int wave_grid_index(const wave_config* cfg, int64_t x, int64_t y, int64_t z, int64_t* idx);
+/* Coordinates::index2coordinate (Coordinates.cpp:603-650) for every index:
+ * x, y, z receive n = wave_grid_num_points values each. Also returns the
+ * extents the variable grid reduced NX, NY, NZ to (NULL to skip). */
+int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_t* z, int64_t n, int64_t* extents3);
+
 /* ForwardSolver::Factory<float>::Create(dimension, type)
  * (ForwardSolver/ForwardSolverFactory.cpp:4-67) followed by initForwardSolver
  * (ForwardSolver.hpp:52, e.g. ForwardSolver3Delastic.cpp:20-48): validates the
@@ -117,8 +143,8 @@ int wave_solver_destroy(wave_handle* h);
  * Elastic.cpp:28-45, Viscoelastic.cpp:650-715, ModelparameterSeismic.cpp:
  * 131-136, 421-432, Modelparameter.cpp:336-651) + the solver's
  * prepareForModelling (ForwardSolver.hpp:42, e.g. ForwardSolver3Dviscoelastic.cpp:103-118,
- * FreeSurfaceElastic.cpp:11-47). Arrays have n = NX*NY*NZ entries in the
- * reference index order; unused parameters may be NULL (vs for acoustic,
+ * FreeSurfaceElastic.cpp:11-47). Arrays have n = wave_grid_num_points entries
+ * (NX*NY*NZ on a regular grid) in the reference index order; unused parameters may be NULL (vs for acoustic,
  * vp for sh, taup/taus unless visco). mem = WAVE_MEM_HOST or WAVE_MEM_DEVICE. */
 int wave_set_model(wave_handle* h, const float* rho, const float* vp, const float* vs,
                    const float* taup, const float* taus, size_t n, int mem);

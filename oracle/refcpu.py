@@ -47,6 +47,12 @@ class WaveConfig(ctypes.Structure):
         ("relaxationFrequency", ctypes.c_double * 4),
         ("useStencilMatrix", ctypes.c_int),
         ("edgeOrderReduction", ctypes.c_int),
+        ("useVariableGrid", ctypes.c_int),
+        ("useVariableFDoperators", ctypes.c_int),
+        ("gridLayers", ctypes.c_int),
+        ("gridInterface", ctypes.c_int * 16),
+        ("gridDHFactor", ctypes.c_int * 16),
+        ("gridFDOrder", ctypes.c_int * 16),
     ]
 
 
@@ -72,6 +78,13 @@ def make_config(**kw) -> WaveConfig:
         c.relaxationFrequency[i] = rf[i]
     c.useStencilMatrix = kw.get("useStencilMatrix", 0)
     c.edgeOrderReduction = kw.get("edgeOrderReduction", 1)
+    c.useVariableGrid = kw.get("useVariableGrid", 0)
+    c.useVariableFDoperators = kw.get("useVariableFDoperators", 0)
+    grid = kw.get("grid", [])
+    c.gridLayers = len(grid)
+    for i, row in enumerate(grid):
+        c.gridInterface[i], c.gridDHFactor[i] = int(row[0]), int(row[1])
+        c.gridFDOrder[i] = int(row[2]) if len(row) > 2 else c.spatialFDorder
     return c
 
 
@@ -119,7 +132,9 @@ def _num(v: str, cast):
     raise ValueError(v)
 
 
-def config_from_parameters(p: dict) -> WaveConfig:
+def config_from_parameters(p: dict, base_dir: str | None = None) -> WaveConfig:
+    """base_dir: folder against which gridConfigurationFilename is resolved
+    (tried as given, then base_dir/name, then base_dir/../name)."""
     g = lambda k, cast=float, default=None: (_num(p[k.lower()], cast) if k.lower() in p else default)
     dim = 3 if _tok(p["dimension"]).lower() == "3d" else 2
     kw = dict(
@@ -139,9 +154,19 @@ def config_from_parameters(p: dict) -> WaveConfig:
                              g("relaxationFrequency3", float, 0.0), g("relaxationFrequency4", float, 0.0)],
         useStencilMatrix=g("useStencilMatrix", int, 0),
         edgeOrderReduction=g("edgeOrderReduction", int, 1),
+        useVariableGrid=g("useVariableGrid", int, 0),
+        useVariableFDoperators=g("useVariableFDoperators", int, 0),
     )
     if kw["equation"] == "visco":
         kw["equation"] = "viscoelastic"
+    if kw["useVariableGrid"] or kw["useVariableFDoperators"]:
+        from oracle import vargrid
+        name = _tok(p["gridconfigurationfilename"])
+        tries = [name] + ([os.path.join(base_dir, name), os.path.join(base_dir, "..", name)] if base_dir else [])
+        path = next(t for t in tries if os.path.exists(t))
+        iface, dhf, order = vargrid.read_grid_config(path)
+        kw["grid"] = [(a, b, c if order else kw["spatialFDorder"]) for a, b, c in
+                      zip(iface, dhf, order or [0] * len(iface))]
     return make_config(**kw)
 
 

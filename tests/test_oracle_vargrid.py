@@ -1,0 +1,116 @@
+"""The variable-grid oracle against the reference's variable-grid goldens
+(par/ci/seismogram.{2D,3D}.acoustic.varGrid.ref.p.mtx, gate of
+Test_CompareSeismogram.cpp:57-88), and the library's grid index space
+(wave_grid_*, no GPU needed) against the oracle's restatement of
+Acquisition/Coordinates.cpp."""
+import numpy as np
+import pytest
+
+import ci_cases
+
+GATE = 5e-7
+
+
+def test_vargrid_oracle_matches_2d_golden(refcpu):
+    case = ci_cases.load_vargrid_case("2D.acoustic.varGrid")
+    seis = ci_cases.run_vargrid_oracle(case, np.float32)
+    g = case["golden"]
+    assert seis.shape == g.shape
+    assert refcpu.reference_misfit(seis, g) < GATE
+
+
+def test_vargrid_oracle_matches_3d_golden(refcpu):
+    case = ci_cases.load_vargrid_case("3D.acoustic.varGrid")
+    seis = ci_cases.run_vargrid_oracle(case, np.float32)
+    g = case["golden"]
+    assert seis.shape == g.shape
+    assert refcpu.reference_misfit(seis, g) < GATE
+
+
+def test_vargrid_goldens_predate_edge_order_reduction(refcpu):
+    """As for the regular-grid goldens: with the current edge rule
+    (Derivatives.cpp:166-179) the 2-D variable-grid golden fails the gate."""
+    case = ci_cases.load_vargrid_case("2D.acoustic.varGrid", edge_order_reduction=1)
+    case["cfg"].edgeOrderReduction = 1
+    seis = ci_cases.run_vargrid_oracle(case, np.float32)
+    assert refcpu.reference_misfit(seis, case["golden"]) > 10 * GATE
+
+
+GRIDS = [
+    # (dimension, NX, NY, NZ, [(interface, dhFactor, order), ...])
+    (2, 305, 303, 1, [(0, 1, 2), (30, 3, 6), (150, 1, 2), (200, 3, 6)]),     # the CI grid
+    (3, 104, 303, 104, [(0, 1, 2), (30, 3, 6), (150, 1, 2), (200, 3, 6)]),
+    (2, 120, 100, 1, [(0, 1, 4), (31, 3, 4), (70, 9, 2)]),                    # interfaces moved to whole cells
+    (3, 40, 61, 47, [(0, 1, 4), (20, 3, 6)]),
+    (2, 50, 60, 1, [(0, 1, 2), (25, 1, 8)]),                                  # variable FD orders only
+]
+
+
+def _cfg(wave, refcpu, dim, NX, NY, NZ, grid, var_grid=True):
+    kw = dict(dimension=dim, equation="acoustic", NX=NX, NY=NY, NZ=NZ, DH=10.0, DT=1e-3, T=0.1,
+              spatialFDorder=2, useVariableGrid=int(var_grid), useVariableFDoperators=1, grid=grid)
+    return wave.WaveConfig.make(**kw), refcpu.make_config(**kw)
+
+
+@pytest.mark.parametrize("k", range(len(GRIDS)))
+def test_library_grid_index_space_matches_oracle(k, wave, refcpu):
+    from oracle import vargrid
+    dim, NX, NY, NZ, grid = GRIDS[k]
+    var_grid = any(r[1] != 1 for r in grid)
+    c, _ = _cfg(wave, refcpu, dim, NX, NY, NZ, grid, var_grid)
+    g = vargrid.VarGrid(NX, NY, NZ, 10.0, [r[0] for r in grid], [r[1] for r in grid] if var_grid else [1] * len(grid))
+    assert wave.grid_num_points(c) == g.N
+    x, y, z, ext = wave.grid_coordinates(c)
+    assert ext == (g.NX, g.NY, g.NZ)
+    np.testing.assert_array_equal(x, g.x)
+    np.testing.assert_array_equal(y, g.y)
+    np.testing.assert_array_equal(z, g.z)
+    rng = np.random.default_rng(k)
+    for _ in range(200):
+        X, Y, Z = rng.integers(0, g.NX), rng.integers(0, g.NY), rng.integers(0, g.NZ)
+        try:
+            want = int(g.coordinate2index(X, Y, Z))
+        except IndexError:
+            with pytest.raises(wave.WaveError):
+                wave.grid_index(c, X, Y, Z)
+            continue
+        assert wave.grid_index(c, X, Y, Z) == want
+    # index -> coordinate -> index is the identity
+    sel = rng.integers(0, g.N, 500)
+    np.testing.assert_array_equal(g.coordinate2index(g.x[sel], g.y[sel], g.z[sel]), sel)
+
+
+def test_regular_grid_index_space(wave):
+    c = wave.WaveConfig.make(dimension=3, NX=7, NY=5, NZ=3, DH=1.0, DT=1e-3, T=0.01)
+    assert wave.grid_num_points(c) == 105
+    assert wave.grid_index(c, 2, 3, 1) == 2 + 1 * 7 + 3 * 21
+    x, y, z, ext = wave.grid_coordinates(c)
+    assert ext == (7, 5, 3)
+    assert (x[2 + 7 + 63], y[2 + 7 + 63], z[2 + 7 + 63]) == (2, 3, 1)
+
+
+@pytest.mark.parametrize("name", sorted(ci_cases.VARGRID_CASES))
+def test_parameter_reader_reads_the_grid_configuration(name, wave, refcpu):
+    import ctypes
+    import os
+    path = os.path.join(ci_cases.CI, ci_cases.VARGRID_CASES[name][0])
+    mine = wave.WaveConfig.from_file(path)
+    ref = refcpu.config_from_parameters(refcpu.read_parameter_file(path), base_dir=ci_cases.CI)
+    for f, _ in wave.WaveConfig._fields_:
+        a, b = getattr(mine, f), getattr(ref, f)
+        assert (list(a) == list(b)) if isinstance(a, ctypes.Array) else (a == b), f
+    assert mine.useVariableGrid == 1 and mine.gridLayers == 4
+    assert list(mine.gridDHFactor)[:4] == [1, 3, 1, 3] and list(mine.gridFDOrder)[:4] == [2, 6, 2, 6]
+
+
+def test_invalid_grid_configurations_are_rejected(wave, refcpu):
+    bad = [
+        [(1, 1, 2), (30, 3, 2)],          # first interface not at y = 0
+        [(0, 1, 2), (30, 2, 2)],          # factor 2
+        [(0, 1, 2), (30, 9, 2)],          # jump 1 -> 9
+        [(0, 1, 2), (30, 3, 5)],          # odd order
+    ]
+    for grid in bad:
+        c, _ = _cfg(wave, refcpu, 2, 100, 100, 1, grid)
+        with pytest.raises(wave.WaveError):
+            wave.grid_num_points(c)

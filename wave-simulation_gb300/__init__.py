@@ -44,7 +44,7 @@ ABI_SYMBOLS = (
     "wave_batch_adjoint_gradient", "wave_resample_traces", "wave_normalize_traces", "wave_read_mtx",
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
     "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
-    "wave_agc_normalize_traces",
+    "wave_agc_normalize_traces", "wave_grid_num_points", "wave_grid_index", "wave_grid_coordinates",
 )
 
 
@@ -73,6 +73,12 @@ class WaveConfig(ctypes.Structure):
         ("relaxationFrequency", ctypes.c_double * 4),
         ("useStencilMatrix", ctypes.c_int),
         ("edgeOrderReduction", ctypes.c_int),
+        ("useVariableGrid", ctypes.c_int),
+        ("useVariableFDoperators", ctypes.c_int),
+        ("gridLayers", ctypes.c_int),
+        ("gridInterface", ctypes.c_int * 16),
+        ("gridDHFactor", ctypes.c_int * 16),
+        ("gridFDOrder", ctypes.c_int * 16),
     ]
 
     @classmethod
@@ -103,6 +109,17 @@ class WaveConfig(ctypes.Structure):
             c.relaxationFrequency[i] = rf[i]
         c.useStencilMatrix = kw.get("useStencilMatrix", 0)
         c.edgeOrderReduction = kw.get("edgeOrderReduction", 1)
+        # variable grid: grid = [(first depth index, dhFactor, FD order), ...]
+        # (the rows of the reference's gridConfigurationFilename)
+        c.useVariableGrid = kw.get("useVariableGrid", 0)
+        c.useVariableFDoperators = kw.get("useVariableFDoperators", 0)
+        grid = kw.get("grid", [])
+        if len(grid) > 16:
+            raise ValueError("at most 16 grid layers")
+        c.gridLayers = len(grid)
+        for i, row in enumerate(grid):
+            c.gridInterface[i], c.gridDHFactor[i] = int(row[0]), int(row[1])
+            c.gridFDOrder[i] = int(row[2]) if len(row) > 2 else c.spatialFDorder
         return c
 
     def copy_from(self, other) -> "WaveConfig":
@@ -112,7 +129,8 @@ class WaveConfig(ctypes.Structure):
 
     @property
     def N(self) -> int:
-        return int(self.NX * self.NY * (self.NZ if self.dimension == 3 else 1))
+        """Number of grid points (the variable grid's layered points, or NX*NY*NZ)."""
+        return grid_num_points(self)
 
 
 _lib = None
@@ -184,6 +202,9 @@ def lib():
     L.wave_batch_step.argtypes = [P, I, I]
     L.wave_batch_get_stream.argtypes = [P, CP(P)]
     L.wave_batch_get_launch_count.argtypes = [P, CP(ctypes.c_longlong)]
+    L.wave_grid_num_points.argtypes = [CP(WaveConfig), ctypes.POINTER(i64)]
+    L.wave_grid_index.argtypes = [CP(WaveConfig), i64, i64, i64, ctypes.POINTER(i64)]
+    L.wave_grid_coordinates.argtypes = [CP(WaveConfig), P, P, P, i64, P]
     L.wave_batch_last_error.restype = ctypes.c_char_p
     L.wave_batch_last_error.argtypes = [P]
     _lib = L
@@ -208,6 +229,32 @@ def _f32(a):
     if a is None or hasattr(a, "data_ptr"):
         return a
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def grid_num_points(cfg: WaveConfig) -> int:
+    """Points of the configuration's grid: NX*NY*NZ, or the variable grid's
+    layered points (Coordinates::getNGridpoints)."""
+    n = ctypes.c_int64()
+    _check(None, lib().wave_grid_num_points(ctypes.byref(cfg), ctypes.byref(n)))
+    return int(n.value)
+
+
+def grid_index(cfg: WaveConfig, x: int, y: int, z: int) -> int:
+    """Coordinates::coordinate2index of a fine-grid coordinate (x, y = depth, z)."""
+    i = ctypes.c_int64()
+    _check(None, lib().wave_grid_index(ctypes.byref(cfg), int(x), int(y), int(z), ctypes.byref(i)))
+    return int(i.value)
+
+
+def grid_coordinates(cfg: WaveConfig):
+    """Coordinates::index2coordinate of every index: (x, y, z) int64 arrays and
+    the (NX, NY, NZ) the variable grid reduced the extents to."""
+    n = grid_num_points(cfg)
+    xyz = [np.zeros(n, dtype=np.int64) for _ in range(3)]
+    ext = np.zeros(3, dtype=np.int64)
+    _check(None, lib().wave_grid_coordinates(ctypes.byref(cfg), *(a.ctypes.data_as(ctypes.c_void_p) for a in xyz), n,
+                                             ext.ctypes.data_as(ctypes.c_void_p)))
+    return xyz[0], xyz[1], xyz[2], tuple(int(v) for v in ext)
 
 
 def wavelet(shape: int, nt: int, dt: float, fc: float, amp: float, tshift: float) -> np.ndarray:

@@ -113,6 +113,8 @@ int wave_batch_create(const wave_config* cfgs, int nshots, wave_batch** out)
     *out = nullptr;
     for (int s = 1; s < nshots; ++s) {
         const wave_config &a = cfgs[0], &c = cfgs[s];
+        if (c.useVariableGrid || c.useVariableFDoperators)
+            return bfail(nullptr, WAVE_ERR_UNSUPPORTED, "wave_batch_create: the batched launches run on regular grids only");
         if (c.dimension != a.dimension || c.equation != a.equation || c.spatialFDorder != a.spatialFDorder ||
             c.DT != a.DT || c.T != a.T || c.DampingBoundary != a.DampingBoundary || c.FreeSurface != a.FreeSurface ||
             c.numRelaxationMechanisms != a.numRelaxationMechanisms)

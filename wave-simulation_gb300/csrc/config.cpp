@@ -11,6 +11,7 @@
 #include <map>
 #include <sstream>
 #include <string>
+#include <vector>
 
 #include "wave_internal.h"
 
@@ -35,6 +36,53 @@ bool get(const std::map<std::string, std::string>& m, const char* key, T& out)
     if (in.fail()) return false;
     out = v;
     return true;
+}
+
+// gridConfigurationFilename: rows "interface dhFactor FDorder", '#' lines and
+// blank lines skipped (Common::readColumnFromFile, Common/Common.hpp:27-60).
+// The name is taken as given (relative to the working directory, as the
+// reference does), else relative to the parameter file's folder or its parent.
+int read_grid_config(const std::string& name, const char* paramPath, wave_config& c, std::string& err)
+{
+    std::string dir(paramPath);
+    size_t sl = dir.find_last_of('/');
+    dir = sl == std::string::npos ? std::string(".") : dir.substr(0, sl);
+    const std::string tries[3] = {name, dir + "/" + name, dir + "/../" + name};
+    std::ifstream f;
+    for (const std::string& t : tries) {
+        f.open(t);
+        if (f.is_open()) break;
+        f.clear();
+    }
+    if (!f.is_open()) {
+        err = "Could not open grid configuration " + name;
+        return WAVE_ERR_IO;
+    }
+    std::string line;
+    int rows = 0, lineNo = 0;
+    while (std::getline(f, line)) {
+        ++lineNo;
+        if (line.empty() || line[0] == '#' || std::all_of(line.begin(), line.end(), [](unsigned char ch) { return std::isspace(ch); }))
+            continue;
+        std::istringstream in(line);
+        std::vector<int> v;
+        int x;
+        while (in >> x) v.push_back(x);
+        if (v.size() < 2 || (c.useVariableFDoperators && v.size() < 3)) {
+            err = "line " + std::to_string(lineNo) + " in file " + name + " has too few columns";
+            return WAVE_ERR_ARG;
+        }
+        if (rows == WAVE_MAX_GRID_LAYERS) {
+            err = "more than " + std::to_string(WAVE_MAX_GRID_LAYERS) + " layers in " + name;
+            return WAVE_ERR_ARG;
+        }
+        c.gridInterface[rows] = v[0];
+        c.gridDHFactor[rows] = v[1];
+        c.gridFDOrder[rows] = v.size() > 2 ? v[2] : c.spatialFDorder;
+        ++rows;
+    }
+    c.gridLayers = rows;
+    return WAVE_OK;
 }
 
 } // namespace
@@ -95,6 +143,17 @@ int parse_config_file(const char* path, wave_config* cfg, std::string& err)
     for (int l = 0; l < 4; ++l) { c.relaxationFrequency[l] = 0.0; get(m, rk[l], c.relaxationFrequency[l]); }
     c.useStencilMatrix = 0; get(m, "useStencilMatrix", c.useStencilMatrix);
     c.edgeOrderReduction = 1; get(m, "edgeOrderReduction", c.edgeOrderReduction);
+    c.useVariableGrid = 0; get(m, "useVariableGrid", c.useVariableGrid);
+    c.useVariableFDoperators = 0; get(m, "useVariableFDoperators", c.useVariableFDoperators);
+    if (c.useVariableGrid || c.useVariableFDoperators) {
+        std::string grid;
+        if (!get(m, "gridConfigurationFilename", grid)) {
+            err = "Parameter gridConfigurationFilename: Not found in Configuration file!";
+            return WAVE_ERR_ARG;
+        }
+        int rc = read_grid_config(grid, path, c, err);
+        if (rc != WAVE_OK) return rc;
+    }
     *cfg = c;
     return WAVE_OK;
 }

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <functional>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -9,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "el3d.h"
+#include "vargrid.h"
 #include "wave_internal.h"
 
 using wave::StepParams;
@@ -57,6 +59,8 @@ struct wave_handle {
     // streaming 3-D elastic paths (kernels_el3d.cu: one point per thread;
     // kernels_el3d_pairs.cu: two x-adjacent points per thread)
     El3dPlan el3d, el3dp;
+    // variable-grid operators (vargrid.cu); null on a regular grid
+    std::shared_ptr<wave::VarGridDev> vg;
     int kernelPath = 0;          // 0 automatic, 1 generic only, 2 one-point streaming, 3 pair streaming (where available)
     int passStreaming[2] = {0, 0};   // automatic path: timed choice per pass (0 generic, 1 one-point, 2 pair streaming)
     bool dependentLaunch = true;     // generic kernels launched with programmatic stream serialization
@@ -94,6 +98,13 @@ struct wave_handle {
 namespace wave {
 // one forward time step of a handle on its stream (solver.cu)
 void step_once(wave_handle* h);
+
+// variable grid (vargrid.cu): upload of the host-built operators, model
+// preparation, and the launches of one step (returns the kernel count;
+// mid, if given, is recorded between the velocity and pressure halves)
+void vargrid_setup(wave_handle* h, const VarGridHost& G);
+void vargrid_set_model(wave_handle* h, const float* rho, const float* vp);
+int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid);
 
 // the adjoint gradient driver (adjoint.cu), shared by the single-handle and
 // the batched entry points

@@ -222,6 +222,12 @@ void launch_pass(wave_handle* h, int pass, bool dep = true) { launch_kernel_of(h
 
 void launch_step(wave_handle* h)
 {
+    if (h->vg) {
+        h->launches += wave::vargrid_launch_step(h, h->dependentLaunch, nullptr);
+        launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
+        h->launches += 1;
+        return;
+    }
     launch_pass(h, 0);
     launch_pass(h, 1);
     h->launches += 2;
@@ -240,6 +246,14 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
     cudaEvent_t a, b, c;
     cudaEventCreate(&a); cudaEventCreate(&b); cudaEventCreate(&c);
     cudaEventRecord(a, h->stream);
+    if (h->vg) {
+        h->launches += wave::vargrid_launch_step(h, false, &b);
+        cudaEventRecord(c, h->stream);
+        ev.push_back(a); ev.push_back(b); ev.push_back(c);
+        launch_srcrec(h->sq, h->tcounter, h->stream);
+        h->launches += 1;
+        return;
+    }
     launch_pass(h, 0, false);
     cudaEventRecord(b, h->stream);
     launch_pass(h, 1, false);
@@ -380,6 +394,74 @@ int wave_wavelet(int shape, int nt, double dt, double fc, double amp, double tsh
     return WAVE_OK;
 }
 
+int wave_grid_num_points(const wave_config* cfg, int64_t* n)
+{
+    if (!cfg || !n) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_num_points: null argument");
+    if (cfg->useVariableGrid || cfg->useVariableFDoperators) {
+        wave::VarGridLayout L;
+        std::string err;
+        int rc = wave::vargrid_layout(*cfg, L, err);
+        if (rc != WAVE_OK) return fail(nullptr, rc, err);
+        *n = L.N;
+    } else {
+        *n = cfg->NX * cfg->NY * (cfg->dimension == 3 ? cfg->NZ : 1);
+    }
+    return WAVE_OK;
+}
+
+int wave_grid_index(const wave_config* cfg, int64_t x, int64_t y, int64_t z, int64_t* idx)
+{
+    if (!cfg || !idx) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_index: null argument");
+    const int64_t NZ = cfg->dimension == 3 ? cfg->NZ : 1;
+    if (cfg->useVariableGrid || cfg->useVariableFDoperators) {
+        wave::VarGridLayout L;
+        std::string err;
+        int rc = wave::vargrid_layout(*cfg, L, err);
+        if (rc != WAVE_OK) return fail(nullptr, rc, err);
+        const long long i = L.index(x, y, z);
+        if (i < 0) return fail(nullptr, WAVE_ERR_ARG, "Could not map from coordinate to index!");
+        *idx = i;
+        return WAVE_OK;
+    }
+    if (x < 0 || x >= cfg->NX || y < 0 || y >= cfg->NY || z < 0 || z >= NZ)
+        return fail(nullptr, WAVE_ERR_ARG, "Could not map from coordinate to index!");
+    *idx = x + z * cfg->NX + y * cfg->NX * NZ;
+    return WAVE_OK;
+}
+
+int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_t* z, int64_t n, int64_t* extents3)
+{
+    if (!cfg) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_coordinates: null argument");
+    const int64_t NZ = cfg->dimension == 3 ? cfg->NZ : 1;
+    wave::VarGridLayout L;
+    const bool vg = cfg->useVariableGrid || cfg->useVariableFDoperators;
+    if (vg) {
+        std::string err;
+        int rc = wave::vargrid_layout(*cfg, L, err);
+        if (rc != WAVE_OK) return fail(nullptr, rc, err);
+    }
+    const int64_t N = vg ? L.N : cfg->NX * cfg->NY * NZ;
+    if (extents3) {
+        extents3[0] = vg ? L.NX : cfg->NX;
+        extents3[1] = vg ? L.NY : cfg->NY;
+        extents3[2] = vg ? L.NZ : NZ;
+    }
+    if (!x && !y && !z) return WAVE_OK;
+    if (!x || !y || !z || n != N) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_coordinates: n != the number of grid points");
+    for (int64_t i = 0; i < N; ++i) {
+        if (vg) {
+            int a, b, c;
+            L.coord(i, a, b, c);
+            x[i] = a; y[i] = b; z[i] = c;
+        } else {
+            x[i] = i % cfg->NX;
+            z[i] = (i / cfg->NX) % NZ;
+            y[i] = i / (cfg->NX * NZ);
+        }
+    }
+    return WAVE_OK;
+}
+
 int wave_solver_create(const wave_config* cfg, wave_handle** out)
 {
     if (!cfg || !out) return fail(nullptr, WAVE_ERR_ARG, "wave_solver_create: null argument");
@@ -407,6 +489,20 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
     if (eq_visco(c.equation))
         for (int l = 0; l < c.numRelaxationMechanisms; ++l)
             if (c.relaxationFrequency[l] <= 0) return fail(nullptr, WAVE_ERR_ARG, "relaxationFrequency must be positive");
+    // variable grid / variable FD orders (Coordinates.cpp:35-95, Derivatives.cpp:12-55)
+    const bool vgrid = c.useVariableGrid != 0 || c.useVariableFDoperators != 0;
+    wave::VarGridHost vgHost;
+    if (vgrid) {
+        if (c.equation != WAVE_EQ_ACOUSTIC)
+            return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built for the acoustic equations only");
+        if (c.DampingBoundary == 1)
+            return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built with CPML or without a damping boundary (not ABS)");
+        if (c.useStencilMatrix)
+            return fail(nullptr, WAVE_ERR_ARG, "Variable FD operators are not available for stencil matrices");
+        std::string err;
+        int rc = wave::vargrid_build(c, vgHost, err);
+        if (rc != WAVE_OK) return fail(nullptr, rc, err);
+    }
 
     auto h = std::make_unique<wave_handle>();
     try {
@@ -414,6 +510,10 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
         h->cfg.NZ = NZ;
         h->NX = static_cast<int>(c.NX); h->NY = static_cast<int>(c.NY); h->NZ = static_cast<int>(NZ);
         h->N = (long long)h->NX * h->NY * h->NZ;
+        if (vgrid) {
+            h->NX = vgHost.L.NX; h->NY = vgHost.L.NY; h->NZ = vgHost.L.NZ;
+            h->N = vgHost.L.N;
+        }
         h->NT = nt_from(c);
         h->H = c.spatialFDorder / 2;
         h->L = eq_visco(c.equation) ? c.numRelaxationMechanisms : 0;
@@ -426,6 +526,7 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
         P = StepParams{};
         P.NX = h->NX; P.NY = h->NY; P.NZ = h->NZ; P.is3d = is3d; P.N = h->N;
         P.scale = DT / DH;
+        if (!vgrid) {
         P.Dxf = to_device(h.get(), build_op(h->NX, q, OP_F, stencil, reduce, DH, DT), 0);
         P.Dxb = to_device(h.get(), build_op(h->NX, q, OP_B, stencil, reduce, DH, DT), 1);
         P.Dyf = to_device(h.get(), build_op(h->NY, q, OP_F, stencil, reduce, DH, DT), 2);
@@ -439,14 +540,16 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
             P.DyfS = to_device(h.get(), build_op(h->NY, q, OP_FS_F, stencil, reduce, DH, DT), 6);
             P.DybS = to_device(h.get(), build_op(h->NY, q, OP_FS_B, stencil, reduce, DH, DT), 7);
         }
+        }
         // fields
         h->fields = field_list(c.equation, is3d);
         h->pass1Fields = pass1_list(c.equation, is3d);
         for (int f : h->fields) P.f[f] = h->f[f] = h->alloc<float>(h->N);
         for (int rr : mem_list(c.equation, is3d))
             for (int l = 0; l < h->L; ++l) P.r[rr][l] = h->r[rr][l] = h->alloc<float>(h->N);
-        // boundaries
-        P.useCpml = c.DampingBoundary == 2;
+        // boundaries (the variable grid keeps per-point CPML coefficients, vargrid.cu)
+        if (vgrid) wave::vargrid_setup(h.get(), vgHost);
+        P.useCpml = c.DampingBoundary == 2 && !vgrid;
         if (P.useCpml) {
             const float np = static_cast<float>(c.NPower), fc = static_cast<float>(c.CenterFrequencyCPML), vm = static_cast<float>(c.VMaxCPML);
             const int w = c.BoundaryWidth;
@@ -516,7 +619,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
     if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_model: null handle");
     const int eq = h->cfg.equation;
     if (eq_em(eq)) return fail(h, WAVE_ERR_ARG, "wave_set_model: EM equation, use wave_set_model_em");
-    if (n != static_cast<size_t>(h->N)) return fail(h, WAVE_ERR_ARG, "wave_set_model: n != NX*NY*NZ");
+    if (n != static_cast<size_t>(h->N)) return fail(h, WAVE_ERR_ARG, "wave_set_model: n != the number of grid points");
     const bool needVp = eq != WAVE_EQ_SH && eq != WAVE_EQ_VISCOSH;
     const bool needVs = eq != WAVE_EQ_ACOUSTIC;
     const bool visco = eq_visco(eq);
@@ -532,6 +635,14 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         float* dVs = needVs ? stage(h, vs, n, mem, tmp) : nullptr;
         float* dTp = eq == WAVE_EQ_VISCOELASTIC ? stage(h, taup, n, mem, tmp) : nullptr;
         float* dTs = visco ? stage(h, taus, n, mem, tmp) : nullptr;
+        if (h->vg) {
+            wave::vargrid_set_model(h, dRho, dVp);
+            for (float* p : tmp) cudaFreeAsync(p, s);
+            h->check(cudaStreamSynchronize(s), "model preparation");
+            h->modelSet = true;
+            h->graphDirty = true;
+            return WAVE_OK;
+        }
         auto mat = [&](int slot) {
             if (!h->m[slot]) h->m[slot] = h->alloc<float>(h->N);
             h->sp.m[slot] = h->m[slot];

@@ -1,0 +1,351 @@
+// vargrid.cu — the acoustic time step on the variable (discontinuous) grid:
+// FD2Dacoustic / FD3Dacoustic::run (ForwardSolver2Dacoustic.cpp:91-190,
+// ForwardSolver3Dacoustic.cpp:91-230) with the grid's sparse operators.
+//
+// Layout in HBM: every field, psi and material array is one vector over the
+// variable-grid index space (layer after layer). Each operator is an ELL
+// block (W entries per row, entry-major: entry k of row i at k*N + i), so a
+// warp's 32 rows read 32 consecutive column indices and weights per entry.
+// One step is four launches plus the source/receiver kernel:
+//   vg_vel    Dxf p, Dyf p (or DyfFreeSurface p), Dzf p, CPML, velocity update
+//   vg_interp velocity rows on the interfaces (InterpolationStaggeredX/Full/StaggeredZ)
+//   vg_pres   Dxb vx + Dyb vy + Dzb vz, CPML, pressure update, surface zero
+//   vg_interp pressure rows on the interfaces (InterpolationFull)
+// The interpolations run in place where the rows they rewrite read only the
+// coarse-aligned rows of the same interface (which they leave unchanged);
+// otherwise (a 3:9 step) the new values go through a scratch array first.
+#include <cuda_runtime.h>
+
+#include "handle.h"
+#include "stencil.cuh"
+#include "vargrid.h"
+
+namespace wave {
+
+namespace {
+
+struct VgParams {
+    long long N, nSurface;
+    int fs, cpml;
+    float* vx;
+    float* vy;
+    float* vz;
+    float* p;
+    float* psi[6];              // p_x, p_y, p_z, vxx, vyy, vzz
+    const float* M;
+    const float* ir[3];
+    const int* col[6];          // Dxf, Dyf, Dzf, Dxb, Dyb, Dzb
+    const float* val[6];
+    int W[6];
+    const float* cp[3][4];      // per axis a_full, b_full, a_half, b_half
+};
+
+// phase 0: in place; 1: new values into tmp; 2: tmp into the field
+struct VgInterp {
+    int n[3];
+    int phase[3];
+    float* f[3];
+    float* tmp[3];
+    const int* row[3];
+    const int* col[3];
+    const float* w[3];
+};
+
+__device__ __forceinline__ float ell_row(const VgParams& P, int op, long long i, const float* __restrict__ u)
+{
+    const int* __restrict__ c = P.col[op] + i;
+    const float* __restrict__ v = P.val[op] + i;
+    float s = 0.0f;
+    for (int k = 0; k < P.W[op]; ++k) s += v[k * P.N] * u[c[k * P.N]];
+    return s;
+}
+
+// CPML::applyCPML (CPML.cpp:84-95); zero coefficients outside the frame
+__device__ __forceinline__ void vg_cpml(const VgParams& P, float& d, int slot, int axis, bool half, long long i)
+{
+    const float a = P.cp[axis][half ? 2 : 0][i];
+    const float b = P.cp[axis][half ? 3 : 1][i];
+    if (a == 0.0f && b == 0.0f) return;
+    float ps = P.psi[slot][i] * b;
+    ps += a * d;
+    P.psi[slot][i] = ps;
+    d += ps;
+}
+
+template <bool IS3D, bool CPML>
+__global__ void __launch_bounds__(256) vg_vel(VgParams P)
+{
+    dependent_launch_prologue();
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const float* p = P.p;
+    float d = ell_row(P, 0, i, p);
+    if (CPML) vg_cpml(P, d, 0, 0, true, i);
+    P.vx[i] += d * P.ir[0][i];
+    d = ell_row(P, 1, i, p);
+    if (CPML) vg_cpml(P, d, 1, 1, true, i);
+    P.vy[i] += d * P.ir[1][i];
+    if (IS3D) {
+        d = ell_row(P, 2, i, p);
+        if (CPML) vg_cpml(P, d, 2, 2, true, i);
+        P.vz[i] += d * P.ir[2][i];
+    }
+}
+
+template <bool IS3D, bool CPML>
+__global__ void __launch_bounds__(256) vg_pres(VgParams P)
+{
+    dependent_launch_prologue();
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    float d = ell_row(P, 3, i, P.vx);
+    if (CPML) vg_cpml(P, d, 3, 0, false, i);
+    float d2 = ell_row(P, 4, i, P.vy);
+    if (CPML) vg_cpml(P, d2, 4, 1, false, i);
+    d += d2;
+    if (IS3D) {
+        d2 = ell_row(P, 5, i, P.vz);
+        if (CPML) vg_cpml(P, d2, 5, 2, false, i);
+        d += d2;
+    }
+    d *= P.M[i];
+    float pv = P.p[i] + d;
+    // FreeSurface::setSurfaceZero (FreeSurface.cpp:14-19): the rows at y = 0
+    // come first in the index order and never lie on an interface
+    if (P.fs && i < P.nSurface) pv = 0.0f;
+    P.p[i] = pv;
+}
+
+// blockIdx.y selects one of up to three (field, row list) pairs
+__global__ void __launch_bounds__(256) vg_interp(VgInterp I)
+{
+    dependent_launch_prologue();
+    const int s = blockIdx.y;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= I.n[s]) return;
+    float* f = I.f[s];
+    if (I.phase[s] == 2) {
+        f[I.row[s][k]] = I.tmp[s][k];
+        return;
+    }
+    const int* c = I.col[s] + 4 * k;
+    const float* w = I.w[s] + 4 * k;
+    float v = w[0] * f[c[0]];
+    v += w[1] * f[c[1]];
+    v += w[2] * f[c[2]];
+    v += w[3] * f[c[3]];
+    if (I.phase[s] == 1) I.tmp[s][k] = v;
+    else f[I.row[s][k]] = v;
+}
+
+// Acoustic::prepareForModelling on the variable grid: pWaveModulus = rho vp^2,
+// inverse densities averaged with the grid's partners (Modelparameter.cpp:
+// 336-446, 633-640; invalid values become 0)
+__global__ void __launch_bounds__(256) vg_model(long long N, int naxes, const float* __restrict__ rho, const float* __restrict__ vp,
+                                                const int* __restrict__ px, const int* __restrict__ py, const int* __restrict__ pz,
+                                                float* M, float* irx, float* iry, float* irz)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float r = rho[i];
+    float m = r;
+    m *= vp[i];
+    m *= vp[i];
+    M[i] = m;
+    const int* part[3] = {px, py, pz};
+    float* out[3] = {irx, iry, irz};
+    for (int a = 0; a < naxes; ++a) {
+        const int j = part[a][i];
+        const float avg = j >= 0 ? 0.5f * r + 0.5f * rho[j] : r;
+        const float inv = 1.0f / avg;
+        out[a][i] = isfinite(inv) ? inv : 0.0f;
+    }
+}
+
+template <class K>
+void launch(K kernel, dim3 grid, dim3 block, bool dep, cudaStream_t s, const VgParams& P)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = dep ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, P);
+}
+
+VgParams params_of(wave_handle* h)
+{
+    const VarGridDev& G = *h->vg;
+    VgParams P{};
+    P.N = G.N;
+    P.nSurface = G.nSurface;
+    P.fs = G.fs;
+    P.cpml = G.cp[0][0] != nullptr;
+    P.vx = h->f[F_VX];
+    P.vy = h->f[F_VY];
+    P.vz = G.is3d ? h->f[F_VZ] : nullptr;
+    P.p = h->f[F_P];
+    const int slots[6] = {PS_P_X, PS_P_Y, PS_P_Z, PS_VXX, PS_VYY, PS_VZZ};
+    for (int k = 0; k < 6; ++k) P.psi[k] = h->psi[slots[k]];
+    P.M = h->m[M_M];
+    P.ir[0] = h->m[M_IRX];
+    P.ir[1] = h->m[M_IRY];
+    P.ir[2] = G.is3d ? h->m[M_IRZ] : nullptr;
+    for (int k = 0; k < 6; ++k) {
+        P.col[k] = G.col[k];
+        P.val[k] = G.val[k];
+        P.W[k] = G.W[k];
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int k = 0; k < 4; ++k) P.cp[a][k] = G.cp[a][k];
+    return P;
+}
+
+template <class T>
+const T* upload(wave_handle* h, const std::vector<T>& v)
+{
+    T* d = h->alloc<T>(v.size());
+    if (!v.empty()) h->check(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "variable grid upload");
+    return d;
+}
+
+} // namespace
+
+void vargrid_setup(wave_handle* h, const VarGridHost& G)
+{
+    auto D = std::make_shared<VarGridDev>();
+    const bool is3d = h->is3d();
+    D->N = G.L.N;
+    D->is3d = is3d;
+    const EllHost* ops[6] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb};
+    for (int k = 0; k < 6; ++k) {
+        if (!is3d && (k == 2 || k == 5)) continue;
+        D->W[k] = ops[k]->W;
+        D->col[k] = upload(h, ops[k]->col);
+        D->val[k] = upload(h, ops[k]->val);
+    }
+    const InterpHost* in[3] = {&G.full, &G.stagX, &G.stagZ};
+    long long total = 0;
+    for (int k = 0; k < 3; ++k) {
+        D->nInterp[k] = static_cast<int>(in[k]->row.size());
+        D->inplace[k] = in[k]->inplace ? 1 : 0;
+        total += D->nInterp[k];
+        if (D->nInterp[k] == 0) continue;
+        D->irow[k] = upload(h, in[k]->row);
+        D->icol[k] = upload(h, in[k]->col);
+        D->iw[k] = upload(h, in[k]->w);
+    }
+    if (total > 0) D->itmp = h->alloc<float>(total);
+    if (h->cfg.DampingBoundary == 2) {
+        for (int a = 0; a < (is3d ? 3 : 2); ++a)
+            for (int k = 0; k < 4; ++k) D->cp[a][k] = upload(h, G.cpml[a][k]);
+        const int slots[6] = {PS_P_X, PS_P_Y, PS_P_Z, PS_VXX, PS_VYY, PS_VZZ};
+        for (int k = 0; k < 6; ++k) {
+            if (!is3d && (k == 2 || k == 5)) continue;
+            h->psi[slots[k]] = h->alloc<float>(D->N);
+            h->psiLen[slots[k]] = D->N;
+        }
+    }
+    for (int a = 0; a < (is3d ? 3 : 2); ++a) D->partner[a] = upload(h, G.avgPartner[a]);
+    D->nSurface = G.nSurface;
+    D->fs = h->cfg.FreeSurface == 1 ? 1 : 0;
+    h->vg = D;
+}
+
+void vargrid_set_model(wave_handle* h, const float* rho, const float* vp)
+{
+    const VarGridDev& G = *h->vg;
+    auto mat = [&](int slot) {
+        if (!h->m[slot]) h->m[slot] = h->alloc<float>(h->N);
+        h->sp.m[slot] = h->m[slot];
+        return h->m[slot];
+    };
+    float* M = mat(M_M);
+    float* irx = mat(M_IRX);
+    float* iry = mat(M_IRY);
+    float* irz = G.is3d ? mat(M_IRZ) : nullptr;
+    const unsigned blocks = static_cast<unsigned>((G.N + 255) / 256);
+    vg_model<<<blocks, 256, 0, h->stream>>>(G.N, G.is3d ? 3 : 2, rho, vp, G.partner[0], G.partner[1], G.partner[2], M, irx, iry, irz);
+    h->check(cudaGetLastError(), "variable grid model preparation");
+}
+
+int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid)
+{
+    const VarGridDev& G = *h->vg;
+    const VgParams P = params_of(h);
+    const dim3 block(256);
+    const dim3 grid(static_cast<unsigned>((G.N + 255) / 256));
+    const bool cp = P.cpml != 0;
+    auto vel = G.is3d ? (cp ? vg_vel<true, true> : vg_vel<true, false>) : (cp ? vg_vel<false, true> : vg_vel<false, false>);
+    auto pres = G.is3d ? (cp ? vg_pres<true, true> : vg_pres<true, false>) : (cp ? vg_pres<false, true> : vg_pres<false, false>);
+    int launches = 0;
+    launch(vel, grid, block, dep, h->stream, P);
+    ++launches;
+    const bool interp = G.nInterp[0] + G.nInterp[1] + G.nInterp[2] > 0;
+    auto run_interp = [&](VgInterp I, int lists) {
+        int mx = 0;
+        for (int s = 0; s < lists; ++s) mx = I.n[s] > mx ? I.n[s] : mx;
+        if (mx == 0) return;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(static_cast<unsigned>((mx + 255) / 256), static_cast<unsigned>(lists));
+        cfg.blockDim = dim3(256);
+        cfg.stream = h->stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = dep ? 1 : 0;
+        cudaLaunchKernelEx(&cfg, vg_interp, I);
+        ++launches;
+    };
+    // the lists of one launch: in place where allowed, else gather into the
+    // scratch in one launch and scatter back in a second
+    auto interp_fields = [&](const int* kinds, float* const* fields, int m) {
+        VgInterp I{};
+        int n = 0;
+        bool twoPhase = false;
+        long long off = 0;
+        for (int q = 0; q < m; ++q) {
+            const int kind = kinds[q];
+            if (!fields[q] || G.nInterp[kind] == 0) continue;
+            I.n[n] = G.nInterp[kind];
+            I.f[n] = fields[q];
+            I.row[n] = G.irow[kind];
+            I.col[n] = G.icol[kind];
+            I.w[n] = G.iw[kind];
+            I.tmp[n] = G.itmp + off;
+            off += G.nInterp[kind];
+            I.phase[n] = G.inplace[kind] ? 0 : 1;
+            twoPhase = twoPhase || !G.inplace[kind];
+            ++n;
+        }
+        run_interp(I, n);
+        if (twoPhase) {
+            for (int q = 0; q < n; ++q) I.n[q] = I.phase[q] == 1 ? I.n[q] : 0;
+            for (int q = 0; q < n; ++q) I.phase[q] = 2;
+            run_interp(I, n);
+        }
+    };
+    if (interp) {
+        // vx: StaggeredX, vy: Full, vz: StaggeredZ (ForwardSolver3Dacoustic.cpp:139-197)
+        const int kinds[3] = {1, 0, 2};
+        float* const fields[3] = {P.vx, P.vy, G.is3d ? P.vz : nullptr};
+        interp_fields(kinds, fields, 3);
+    }
+    if (mid) cudaEventRecord(*mid, h->stream);
+    launch(pres, grid, block, dep, h->stream, P);
+    ++launches;
+    if (interp && G.nInterp[0] > 0) {
+        const int kinds[1] = {0};
+        float* const fields[1] = {P.p};
+        interp_fields(kinds, fields, 1);
+    }
+    h->check(cudaGetLastError(), "variable grid step launch");
+    return launches;
+}
+
+} // namespace wave

@@ -1,0 +1,95 @@
+// vargrid.h — the variable (discontinuous) grid: layered index space, its
+// sparse operators in ELL form, and the device-side state of a handle that
+// runs on it (vargrid_host.cpp builds, vargrid.cu launches).
+//
+// The grid is the reference's Coordinates with dhFactor layers
+// (Acquisition/Coordinates.cpp:119-245): depth is cut into layers at the
+// interfaces of gridConfigurationFilename, layer l has spacing DH*dhFactor[l]
+// (dhFactor a power of 3) and its own box of varNX x varNY x varNZ points,
+// stored layer after layer in the reference index order. The rows on an
+// interface are stored at the fine spacing and filled from the coarse-aligned
+// points by bilinear interpolation after each update.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/wave.h"
+
+namespace wave {
+
+struct VarGridLayout {
+    int NX = 1, NY = 1, NZ = 1;        // fine-grid extents (NX, NZ, NY reduced to fit the coarse layers)
+    float DH = 0.0f;
+    int nl = 1;
+    bool varGrid = false;              // layers of different spacing (interface order reduction + interpolation)
+    bool varOrder = false;             // FD order per layer
+    std::vector<int> dhf, order;       // per layer
+    std::vector<int> iface;            // nl + 1 entries: -1, the interfaces, NY - 1
+    std::vector<int> start, end, trans, vnx, vny, vnz;
+    std::vector<long long> offset;     // nl + 1 entries: first index of each layer, N
+    long long N = 0;
+    // functions of the depth row y only
+    std::vector<int> layerY, transY, distY;
+    std::vector<char> onIfaceY;
+
+    float dh(int layer) const { return DH * static_cast<float>(dhf[layer]); }
+    // Coordinates::mapIndex2coordinate (Coordinates.cpp:603-634)
+    void coord(long long idx, int& x, int& y, int& z) const;
+    // Coordinates::map3Dcoordinate2index (Coordinates.cpp:668-698); -1 outside the grid
+    long long index(long long X, long long Y, long long Z) const;
+};
+
+// ELL operator: W entries per row, stored entry-major (col[k*N + row]) so a
+// warp reads consecutive rows; unused entries have col = row, val = 0.
+struct EllHost {
+    int W = 0;
+    std::vector<int> col;
+    std::vector<float> val;
+};
+
+// Interface rows that the interpolation rewrites: 4 (col, weight) pairs per row.
+struct InterpHost {
+    std::vector<int> row;
+    std::vector<int> col;      // 4 per row
+    std::vector<float> w;      // 4 per row
+    bool inplace = true;       // no rewritten row reads another rewritten row
+};
+
+struct VarGridHost {
+    VarGridLayout L;
+    EllHost Dxf, Dxb, Dyf, Dyb, Dzf, Dzb;
+    InterpHost full, stagX, stagZ;
+    std::vector<float> cpml[3][4];     // per axis: a_full, b_full, a_half, b_half (N each; CPML only)
+    std::vector<int> avgPartner[3];    // averaging partner per axis (-1: the point alone)
+    long long nSurface = 0;            // rows with y == 0 (the first rows of layer 0)
+};
+
+// Coordinates set-up from the configuration (Coordinates.cpp:35-95, 119-245).
+int vargrid_layout(const wave_config& c, VarGridLayout& L, std::string& err);
+// Every operator, interpolation, CPML coefficient and averaging partner of
+// the acoustic equations on the grid.
+int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err);
+
+// device side of a variable-grid handle (vargrid.cu)
+struct VarGridDev {
+    long long N = 0;
+    int is3d = 0;
+    int nOps = 0;
+    int W[6] = {};                          // Dxf, Dyf, Dzf, Dxb, Dyb, Dzb
+    const int* col[6] = {};
+    const float* val[6] = {};
+    int nInterp[3] = {};                    // full, staggered x, staggered z
+    const int* irow[3] = {};
+    const int* icol[3] = {};
+    const float* iw[3] = {};
+    int inplace[3] = {1, 1, 1};
+    float* itmp = nullptr;                  // scratch of the two-phase interpolation (sum of the row counts)
+    const float* cp[3][4] = {};             // CPML coefficients per axis (null: no CPML)
+    const int* partner[3] = {};
+    long long nSurface = 0;
+    int fs = 0;
+};
+
+} // namespace wave
