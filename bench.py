@@ -489,6 +489,116 @@ def run_acoustic2d(args, wave):
           "whole state in L2: the HBM roofline is not the bound here"), e2e, launches, clocks, cpu)
 
 
+# ---- variable grid: the reference's 3-D acoustic variable-grid CI case ------
+def vg_case(wave):
+    """Configuration, homogeneous model and acquisition of the 3-D variable-grid
+    CI case (104 x 303 x 104 fine grid, layers of spacing 17 m / 51 m with FD
+    orders 2 / 6, CPML 30, free surface, NT = 1000), from the committed fixtures."""
+    ci = os.path.join(ROOT, "tests", "golden", "ci")
+    cfg = wave.WaveConfig.from_file(os.path.join(ci, "configuration_ci.3D.acoustic.varGrid.txt"))
+    cfg.edgeOrderReduction = 0
+    n = wave.grid_num_points(cfg)
+    model = dict(rho=np.full(n, 2000.0, np.float32), vp=np.full(n, 3500.0, np.float32))
+
+    def rows(name):
+        with open(os.path.join(ci, name)) as f:
+            return [l.split() for l in f if l.strip() and not l.startswith("#")]
+    nt = int(np.float32(np.float32(cfg.T) / np.float32(cfg.DT)) + np.float32(0.5))
+    srcs = [r for r in rows("sources_ci.3D.varGrid.txt")]
+    srcs = [r for r in srcs if r[0] == srcs[0][0]]
+    sidx = np.array([wave.grid_index(cfg, int(r[1]), int(r[2]), int(r[3])) for r in srcs], np.int64)
+    stype = np.array([int(r[4]) for r in srcs], np.int32)
+    sig = np.stack([wave.wavelet(int(r[6]), nt, cfg.DT, float(r[7]), float(r[8]), float(r[9])) for r in srcs])
+    recs = rows("receiver_ci.3D.varGrid.txt")
+    ridx = np.array([wave.grid_index(cfg, int(r[0]), int(r[1]), int(r[2])) for r in recs], np.int64)
+    rtype = np.array([int(r[3]) for r in recs], np.int32)
+    return cfg, model, (sidx, stype, sig, ridx, rtype)
+
+
+def vg_alg_bytes(wave, cfg):
+    """Algorithmic bytes of one step of the ELL formulation: per point, the 6
+    operators' column indices and weights (W entries, 8 B each), the fields,
+    materials and CPML coefficients each read or written once, and psi read and
+    written where the per-layer CPML frame has coefficients."""
+    x, y, z, (NX, NY, NZ) = wave.grid_coordinates(cfg)
+    n = len(x)
+    iface = [cfg.gridInterface[i] for i in range(cfg.gridLayers)] + [NY]
+    dhf = np.ones(n, np.int64)
+    for l in range(cfg.gridLayers):
+        dhf[(y >= iface[l]) & (y < iface[l + 1])] = cfg.gridDHFactor[l]
+    w = np.ceil(cfg.BoundaryWidth / dhf)
+    frame = 0
+    for c, ext, top in ((x, NX, True), (y, NY, cfg.FreeSurface == 0), (z, NZ, True)):
+        d = np.minimum(c, ext - 1 - c) // dhf
+        inside = d < w
+        if not top:
+            inside &= ~(c // dhf < w)
+        frame += int(inside.sum())
+    W = 6                                               # the widest row (order 6)
+    per_point = 6 * W * 8 + (4 + 24 + 12 + 24) + (12 + 4 + 8 + 24)
+    return n * per_point + 2 * 8 * frame, n, per_point, frame
+
+
+def run_vargrid3d(args, wave):
+    import torch
+    cfg, model, acq = vg_case(wave)
+    alg, n, per_point, frame = vg_alg_bytes(wave, cfg)
+    s = wave.Factory.Create("3D", "acoustic").initForwardSolver(cfg)
+    s.prepareForModelling({k: torch.from_numpy(v).cuda() for k, v in model.items()})
+    s.setSources(*acq[:3])
+    s.setReceivers(*acq[3:])
+    nt = s.nt
+    for _ in range(max(1, args.warmup // 20)):          # warm-up jobs (graph capture)
+        s.run(0, nt)
+        s.resetCPML()
+    l0 = s.launch_count()
+    ms, clocks = _clocked(lambda: s.run(0, nt), torch.cuda.ExternalStream(s.stream()))
+    launches = s.launch_count() - l0
+    s.close()
+    value, ms_step = n * nt / (ms * 1e-3) / 1e9, ms / nt
+    e2e = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        s = wave.Factory.Create("3D", "acoustic").initForwardSolver(cfg)
+        s.prepareForModelling(model)
+        s.setSources(*acq[:3])
+        s.setReceivers(*acq[3:])
+        s.run(0, nt)
+        seis = s.seismograms()
+        s.close()
+        e2e_s = time.perf_counter() - t0
+        h2d = sum(v.nbytes for v in model.values()) + sum(a.nbytes for a in acq)
+        e2e = {"value": n * nt / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d / nt,
+               "d2h_bytes_per_step": seis.nbytes / nt,
+               "note": "includes the host assembly of the grid's operators and their upload"}
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import ci_cases
+        from oracle import vargrid
+        case = ci_cases.load_vargrid_case("3D.acoustic.varGrid")
+        c = case["cfg"]
+        cp = vargrid.cpml_coefficients(case["grid"], c.BoundaryWidth, c.NPower, c.CenterFrequencyCPML, c.VMaxCPML,
+                                       c.DT, c.FreeSurface != 0)
+        sim = vargrid.AcousticVarGrid(case["grid"], case["orders"], c.DT, case["model"]["rho"], case["model"]["vp"],
+                                      c.FreeSurface, cp, case["src_idx"], case["src_type"], case["signals"],
+                                      case["rec_idx"], case["rec_type"], edge=False)
+        sim.step(0)
+        t0, done = time.perf_counter(), 0
+        while done < nt - 1 and time.perf_counter() - t0 < 20.0:
+            sim.step(1 + done)
+            done += 1
+        sec = time.perf_counter() - t0
+        cpu = {"value": n * done / sec / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{done} steps of the job with the variable-grid oracle (scipy.sparse CSR, FP32), {sec:.1f} s"}
+    cfgd = {"workload": "3-D acoustic variable grid (the reference's CI case): 104x303x104 fine grid, "
+                        f"{n} points in 4 layers (17 m / 51 m), orders 2/6, CPML 30, free surface, NT={nt}",
+            "points": n, "parallelism": "1 GPU", "l2": "state ~0.4 GB > L2"}
+    roof = _roof(alg, ms_step, "vg_vel + vg_interp + vg_pres (ELL)",
+                 f"ELL formulation: {per_point} B/pt of which {6 * 6 * 8} B/pt are operator columns and weights")
+    _line(UNIT, value, nt, nt, ms_step, cfgd, roof, e2e, launches, clocks, cpu)
+
+
 # ---- config 3: 3-D visco-elastic 512 x 256 (depth) x 512 -------------------
 def _tau_method(q, f0, freqs):
     w0 = 2 * np.pi * f0
@@ -829,7 +939,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="cube edge (profiling captures use a smaller cube)")
-    ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch", "fwi2d"])
+    ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch", "fwi2d", "vargrid3d"])
     ap.add_argument("--shots", type=int, default=128, help="shots of the batched EM workload")
     ap.add_argument("--kernel-path", type=int, default=0, choices=[0, 1, 2, 3],
                     help="3-D elastic kernels: 0 automatic, 1 generic, 2 one-point streaming, 3 two-point streaming (profiling)")
@@ -840,7 +950,7 @@ def main():
         import __graft_entry__ as g
         wave = g.load_package()
         {"acoustic2d": run_acoustic2d, "visco3d": run_visco3d, "tmem_batch": run_tmem_batch,
-         "fwi2d": run_fwi2d}[args.workload](args, wave)
+         "fwi2d": run_fwi2d, "vargrid3d": run_vargrid3d}[args.workload](args, wave)
         return
     if args.grid != 256:
         set_grid(args.grid)

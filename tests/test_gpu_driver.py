@@ -107,3 +107,21 @@ def test_driver_snapshots_equal_the_solver_fields(wave, tmp_path):
             snap = refcpu.read_mtx_array(str(ci / f"wavefield.shot_1.{name}.{step}.mtx"))[:, 0]
             assert np.array_equal(snap.astype(np.float32), s.field(name)), (name, step)
     s.close()
+
+
+def test_driver_runs_the_variable_grid_ci_case(wave, tmp_path):
+    """The 2-D variable-grid CI case through the driver: gridConfigurationFilename
+    read relative to the parameter file, sources and receivers mapped with
+    Coordinates::coordinate2index, the seismogram under the reference's gate."""
+    ci = tmp_path / "ci"
+    ci.mkdir()
+    for f in ("sources_ci.2D.varGrid.txt", "receiver_ci.2D.varGrid.txt", "gridConfig.txt"):
+        shutil.copy(os.path.join(GOLDEN, f), ci / f)
+    text = open(os.path.join(GOLDEN, "configuration_ci.2D.acoustic.varGrid.txt")).read()
+    cfg = ci / "configuration.txt"
+    cfg.write_text(text + "\nedgeOrderReduction=0\n")
+    _run(wave, cfg)
+    got = refcpu.read_mtx_array(str(ci / "seismogram.2D.acoustic.varGrid.ci.shot_0.p.mtx"))
+    golden = refcpu.read_mtx_array(os.path.join(GOLDEN, "seismogram.2D.acoustic.varGrid.ref.p.mtx"))
+    assert got.shape == golden.shape
+    assert refcpu.reference_misfit(got, golden) < GATE

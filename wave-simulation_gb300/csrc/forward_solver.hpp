@@ -69,7 +69,9 @@ class ForwardSolver {
 
     void prepareForModelling(const Model& m)
     {
-        const size_t n = static_cast<size_t>(cfg_.NX * cfg_.NY * (cfg_.dimension == 3 ? cfg_.NZ : 1));
+        int64_t npts = 0;
+        check(nullptr, wave_grid_num_points(&cfg_, &npts));
+        const size_t n = static_cast<size_t>(npts);
         auto p = [](const std::vector<float>& v) { return v.empty() ? nullptr : v.data(); };
         if (cfg_.equation >= WAVE_EQ_TMEM)
             check(h_, wave_set_model_em(h_, p(m.eps_r), p(m.sigma), p(m.mu_r), nullptr, nullptr, n, WAVE_MEM_HOST));

@@ -105,14 +105,38 @@ int main(int argc, char** argv)
             size_t s = p.find_last_of('/');
             return s == std::string::npos ? std::string(".") : p.substr(0, s);
         }();
-        const size_t n = static_cast<size_t>(cfg.NX * cfg.NY * (cfg.dimension == 3 ? cfg.NZ : 1));
+        // grid points: NX*NY*NZ, or the variable grid's (Coordinates.cpp:119-245)
+        int64_t npts = 0;
+        wave::gpu::check(nullptr, wave_grid_num_points(&cfg, &npts));
+        const size_t n = static_cast<size_t>(npts);
+        const bool layered = cfg.useVariableGrid || cfg.useVariableFDoperators;
+        const size_t nRegular = static_cast<size_t>(cfg.NX * cfg.NY * (cfg.dimension == 3 ? cfg.NZ : 1));
+        // a regular-grid model onto the grid's points (Acoustic.cpp:180-200:
+        // each point takes the value at its fine-grid coordinate)
+        std::vector<int64_t> gx, gy, gz;
+        if (layered) {
+            gx.resize(n); gy.resize(n); gz.resize(n);
+            wave::gpu::check(nullptr, wave_grid_coordinates(&cfg, gx.data(), gy.data(), gz.data(), npts, nullptr));
+        }
+        auto onto_grid = [&](std::vector<float> v) {
+            if (!layered) return v;
+            std::vector<float> out(n);
+            const int64_t NZr = cfg.dimension == 3 ? cfg.NZ : 1;
+            for (size_t i = 0; i < n; ++i) out[i] = v[static_cast<size_t>(gx[i] + gz[i] * cfg.NX + gy[i] * cfg.NX * NZr)];
+            return out;
+        };
+        auto grid_index = [&](long long x, long long y, long long z) {
+            int64_t idx = 0;
+            wave::gpu::check(nullptr, wave_grid_index(&cfg, x, y, z, &idx));
+            return static_cast<long long>(idx);
+        };
         wave::gpu::Model model;
         const bool em = cfg.equation >= WAVE_EQ_TMEM;
         const std::string mf = key<std::string>(keys, "ModelFilename", "model/model");
         if (key<int>(keys, "ModelRead", 0) == 1) {
             if (key<int>(keys, "FileFormat", 1) != 1)
                 throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "model files: only FileFormat=1 (MatrixMarket) is readable here; lmf/frv are LAMA formats");
-            auto rd = [&](const char* p) { return read_mtx_vector(dir + "/../" + mf + "." + p + ".mtx", n); };
+            auto rd = [&](const char* p) { return onto_grid(read_mtx_vector(dir + "/../" + mf + "." + p + ".mtx", nRegular)); };
             if (em) { model.eps_r = rd("epsilonr"); model.sigma = rd("sigma"); model.mu_r = rd("mur"); }
             else {
                 model.rho = rd("density");
@@ -155,7 +179,7 @@ int main(int argc, char** argv)
                 long long x, y, z;
                 int t;
                 if (in >> x >> y >> z >> t) {
-                    rec.index.push_back(x + z * cfg.NX + y * cfg.NX * (cfg.dimension == 3 ? cfg.NZ : 1));
+                    rec.index.push_back(grid_index(x, y, z));
                     rec.type.push_back(t);
                 }
             }
@@ -182,7 +206,7 @@ int main(int argc, char** argv)
             wave::gpu::Acquisition src;
             for (auto& s : srcs) {
                 if (s.no != shot) continue;
-                src.index.push_back(s.x + static_cast<long long>(s.z) * cfg.NX + static_cast<long long>(s.y) * cfg.NX * (cfg.dimension == 3 ? cfg.NZ : 1));
+                src.index.push_back(grid_index(s.x, s.y, s.z));
                 src.type.push_back(s.type);
                 std::vector<float> w(nt);
                 wave::gpu::check(nullptr, wave_wavelet(s.shape, nt, cfg.DT, s.fc, s.amp, s.ts, w.data()));
