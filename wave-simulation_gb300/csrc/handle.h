@@ -55,6 +55,7 @@ struct wave_handle {
 
     cudaGraphExec_t graph = nullptr;
     bool graphDirty = true;
+    long long graphLaunchesPerStep = 0;   // kernels in one captured step
 
     // streaming 3-D elastic paths (kernels_el3d.cu: one point per thread;
     // kernels_el3d_pairs.cu: two x-adjacent points per thread)

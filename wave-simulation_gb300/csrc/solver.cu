@@ -326,6 +326,7 @@ void build_graph(wave_handle* h)
     h->check(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     long long before = h->launches;
     for (int s = 0; s < kGraphSteps; ++s) launch_step(h);
+    h->graphLaunchesPerStep = (h->launches - before) / kGraphSteps;   // kernels per captured step
     h->launches = before;
     h->check(cudaStreamEndCapture(h->stream, &g), "end capture");
     h->check(cudaGraphInstantiate(&h->graph, g, 0), "graph instantiate");
@@ -911,10 +912,9 @@ int wave_solver_step(wave_handle* h, int t_begin, int t_end)
         } else {
             if (t_end - t >= kGraphSteps) {
                 if (h->graphDirty || !h->graph) build_graph(h);
-                const long long per = h->sp.abs ? 4 : 3;
                 for (; t + kGraphSteps <= t_end; t += kGraphSteps) {
                     h->check(cudaGraphLaunch(h->graph, h->stream), "graph launch");
-                    h->launches += per * kGraphSteps;
+                    h->launches += h->graphLaunchesPerStep * kGraphSteps;
                 }
             }
             for (; t < t_end; ++t) launch_step(h);
