@@ -133,3 +133,17 @@ def test_gpu_vargrid_rejects_what_it_does_not_build(wave, refcpu):
         cfg = wave.WaveConfig.make(equation=eq, **base, **extra)
         with pytest.raises(wave.WaveError):
             wave.Factory.Create("2d", eq).initForwardSolver(cfg)
+
+
+@pytest.mark.parametrize("k", [0, 1, 4])
+def test_gpu_vargrid_stencil_classes_equal_the_ell_operators(k, wave, refcpu):
+    """The default kernels read each row's entries from its stencil class;
+    kernel path 1 streams the ELL blocks. Same entries in the same order:
+    bit-identical seismograms."""
+    case = synth_case(refcpu, k)
+    cfg = to_wave_cfg(wave, case["cfg"])
+    m = {kk: v.astype(np.float32) for kk, v in case["model"].items()}
+    args = (case["src_idx"], case["src_type"], case["signals"].astype(np.float32), case["rec_idx"], case["rec_type"])
+    a = wave.simulate(cfg, m, *args, kernel_path=0)
+    b = wave.simulate(cfg, m, *args, kernel_path=1)
+    np.testing.assert_array_equal(a, b)

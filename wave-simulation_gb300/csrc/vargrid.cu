@@ -6,6 +6,10 @@
 // variable-grid index space (layer after layer). Each operator is an ELL
 // block (W entries per row, entry-major: entry k of row i at k*N + i), so a
 // warp's 32 rows read 32 consecutive column indices and weights per entry.
+// The default kernels read instead one 32-bit stencil class per row and pass
+// and take the (offset, weight) entries from the class table: the rows of a
+// layer's interior share a handful of classes, so the operators cost 4 B per
+// point and pass instead of 8 B per entry.
 // One step is four launches plus the source/receiver kernel:
 //   vg_vel    Dxf p, Dyf p (or DyfFreeSurface p), Dzf p, CPML, velocity update
 //   vg_interp velocity rows on the interfaces (InterpolationStaggeredX/Full/StaggeredZ)
@@ -37,7 +41,14 @@ struct VgParams {
     const int* col[6];          // Dxf, Dyf, Dzf, Dxb, Dyb, Dzb
     const float* val[6];
     int W[6];
-    const float* cp[3][4];      // per axis a_full, b_full, a_half, b_half
+    const unsigned short* cpc[3];   // per axis: coefficient code of each point (0: none)
+    const float* cpt[3];            // per axis: (a_full, b_full, a_half, b_half) per code
+    // stencil classes of the launched pass (CLS kernels)
+    const unsigned* cid;
+    const int* coff;
+    const float* cw;
+    int KW;
+    int base[3];
 };
 
 // phase 0: in place; 1: new values into tmp; 2: tmp into the field
@@ -56,60 +67,98 @@ __device__ __forceinline__ float ell_row(const VgParams& P, int op, long long i,
     const int* __restrict__ c = P.col[op] + i;
     const float* __restrict__ v = P.val[op] + i;
     float s = 0.0f;
-    for (int k = 0; k < P.W[op]; ++k) s += v[k * P.N] * u[c[k * P.N]];
+    for (int k = 0; k < P.W[op]; ++k) s = __fmaf_rn(v[k * P.N], u[c[k * P.N]], s);
+    return s;
+}
+
+// the same row through the row's stencil class: identical entries in the
+// same order and explicit fused multiply-adds, so identical results; rows of
+// one class in a warp share the table reads. (All arithmetic in these kernels
+// is written with rounding intrinsics so that no kernel variant depends on
+// the compiler's contraction choices.)
+// WU: compile-time bound of the entry loop (every W <= WU), so the table
+// reads and the gathers of a row are all issued before the sums
+template <bool CLS, int WU>
+__device__ __forceinline__ float op_row(const VgParams& P, int op, int q, long long i, unsigned cls, const float* __restrict__ u)
+{
+    if (!CLS) return ell_row(P, op, i, u);
+    const size_t b = static_cast<size_t>(cls) * P.KW + P.base[q];
+    const int* __restrict__ o = P.coff + b;
+    const float* __restrict__ w = P.cw + b;
+    const int W = P.W[op];
+    float wk[WU], uk[WU];
+#pragma unroll
+    for (int k = 0; k < WU; ++k) {
+        wk[k] = 0.0f;
+        uk[k] = 0.0f;
+        if (k < W) {
+            wk[k] = __ldg(w + k);
+            uk[k] = u[i + __ldg(o + k)];
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < WU; ++k)
+        if (k < W) s = __fmaf_rn(wk[k], uk[k], s);
     return s;
 }
 
 // CPML::applyCPML (CPML.cpp:84-95); zero coefficients outside the frame
 __device__ __forceinline__ void vg_cpml(const VgParams& P, float& d, int slot, int axis, bool half, long long i)
 {
-    const float a = P.cp[axis][half ? 2 : 0][i];
-    const float b = P.cp[axis][half ? 3 : 1][i];
+    const unsigned code = P.cpc[axis][i];
+    if (code == 0) return;
+    const float a = __ldg(P.cpt[axis] + 4 * code + (half ? 2 : 0));
+    const float b = __ldg(P.cpt[axis] + 4 * code + (half ? 3 : 1));
     if (a == 0.0f && b == 0.0f) return;
-    float ps = P.psi[slot][i] * b;
-    ps += a * d;
+    // the reference's three vector operations, each rounded (Psi *= b;
+    // temp = a * Vec; Psi += temp; Vec += Psi), not contracted: the result
+    // does not depend on which kernel variant the compiler fused
+    const float ps = __fadd_rn(__fmul_rn(P.psi[slot][i], b), __fmul_rn(a, d));
     P.psi[slot][i] = ps;
-    d += ps;
+    d = __fadd_rn(d, ps);
 }
 
-template <bool IS3D, bool CPML>
+template <bool IS3D, bool CPML, bool CLS, int WU = 12>
 __global__ void __launch_bounds__(256) vg_vel(VgParams P)
 {
     dependent_launch_prologue();
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const float* p = P.p;
-    float d = ell_row(P, 0, i, p);
+    const unsigned cls = CLS ? P.cid[i] : 0u;
+    float d = op_row<CLS, WU>(P, 0, 0, i, cls, p);
     if (CPML) vg_cpml(P, d, 0, 0, true, i);
-    P.vx[i] += d * P.ir[0][i];
-    d = ell_row(P, 1, i, p);
+    P.vx[i] = __fadd_rn(P.vx[i], __fmul_rn(d, P.ir[0][i]));
+    d = op_row<CLS, WU>(P, 1, 1, i, cls, p);
     if (CPML) vg_cpml(P, d, 1, 1, true, i);
-    P.vy[i] += d * P.ir[1][i];
+    P.vy[i] = __fadd_rn(P.vy[i], __fmul_rn(d, P.ir[1][i]));
     if (IS3D) {
-        d = ell_row(P, 2, i, p);
+        d = op_row<CLS, WU>(P, 2, 2, i, cls, p);
         if (CPML) vg_cpml(P, d, 2, 2, true, i);
-        P.vz[i] += d * P.ir[2][i];
+        P.vz[i] = __fadd_rn(P.vz[i], __fmul_rn(d, P.ir[2][i]));
     }
 }
 
-template <bool IS3D, bool CPML>
+template <bool IS3D, bool CPML, bool CLS, int WU = 12>
 __global__ void __launch_bounds__(256) vg_pres(VgParams P)
 {
     dependent_launch_prologue();
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
-    float d = ell_row(P, 3, i, P.vx);
+    const unsigned cls = CLS ? P.cid[i] : 0u;
+    float d = op_row<CLS, WU>(P, 3, 0, i, cls, P.vx);
     if (CPML) vg_cpml(P, d, 3, 0, false, i);
-    float d2 = ell_row(P, 4, i, P.vy);
+    float d2 = op_row<CLS, WU>(P, 4, 1, i, cls, P.vy);
     if (CPML) vg_cpml(P, d2, 4, 1, false, i);
-    d += d2;
+    d = __fadd_rn(d, d2);
     if (IS3D) {
-        d2 = ell_row(P, 5, i, P.vz);
+        d2 = op_row<CLS, WU>(P, 5, 2, i, cls, P.vz);
         if (CPML) vg_cpml(P, d2, 5, 2, false, i);
-        d += d2;
+        d = __fadd_rn(d, d2);
     }
-    d *= P.M[i];
-    float pv = P.p[i] + d;
+    d = __fmul_rn(d, P.M[i]);
+    float pv = __fadd_rn(P.p[i], d);
     // FreeSurface::setSurfaceZero (FreeSurface.cpp:14-19): the rows at y = 0
     // come first in the index order and never lie on an interface
     if (P.fs && i < P.nSurface) pv = 0.0f;
@@ -130,10 +179,10 @@ __global__ void __launch_bounds__(256) vg_interp(VgInterp I)
     }
     const int* c = I.col[s] + 4 * k;
     const float* w = I.w[s] + 4 * k;
-    float v = w[0] * f[c[0]];
-    v += w[1] * f[c[1]];
-    v += w[2] * f[c[2]];
-    v += w[3] * f[c[3]];
+    float v = __fmul_rn(w[0], f[c[0]]);
+    v = __fmaf_rn(w[1], f[c[1]], v);
+    v = __fmaf_rn(w[2], f[c[2]], v);
+    v = __fmaf_rn(w[3], f[c[3]], v);
     if (I.phase[s] == 1) I.tmp[s][k] = v;
     else f[I.row[s][k]] = v;
 }
@@ -184,7 +233,7 @@ VgParams params_of(wave_handle* h)
     P.N = G.N;
     P.nSurface = G.nSurface;
     P.fs = G.fs;
-    P.cpml = G.cp[0][0] != nullptr;
+    P.cpml = G.cpCode[0] != nullptr;
     P.vx = h->f[F_VX];
     P.vy = h->f[F_VY];
     P.vz = G.is3d ? h->f[F_VZ] : nullptr;
@@ -200,8 +249,10 @@ VgParams params_of(wave_handle* h)
         P.val[k] = G.val[k];
         P.W[k] = G.W[k];
     }
-    for (int a = 0; a < 3; ++a)
-        for (int k = 0; k < 4; ++k) P.cp[a][k] = G.cp[a][k];
+    for (int a = 0; a < 3; ++a) {
+        P.cpc[a] = G.cpCode[a];
+        P.cpt[a] = G.cpTab[a];
+    }
     return P;
 }
 
@@ -241,8 +292,10 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
     }
     if (total > 0) D->itmp = h->alloc<float>(total);
     if (h->cfg.DampingBoundary == 2) {
-        for (int a = 0; a < (is3d ? 3 : 2); ++a)
-            for (int k = 0; k < 4; ++k) D->cp[a][k] = upload(h, G.cpml[a][k]);
+        for (int a = 0; a < (is3d ? 3 : 2); ++a) {
+            D->cpCode[a] = upload(h, G.cpCode[a]);
+            D->cpTab[a] = upload(h, G.cpTab[a]);
+        }
         const int slots[6] = {PS_P_X, PS_P_Y, PS_P_Z, PS_VXX, PS_VYY, PS_VZZ};
         for (int k = 0; k < 6; ++k) {
             if (!is3d && (k == 2 || k == 5)) continue;
@@ -251,6 +304,15 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
         }
     }
     for (int a = 0; a < (is3d ? 3 : 2); ++a) D->partner[a] = upload(h, G.avgPartner[a]);
+    for (int pass = 0; pass < 2; ++pass) {
+        const ClassHost& C = G.cls[pass];
+        if (!C.ok) continue;
+        D->clsId[pass] = upload(h, C.id);
+        D->clsOff[pass] = upload(h, C.off);
+        D->clsW[pass] = upload(h, C.w);
+        D->clsKW[pass] = C.KW;
+        for (int q = 0; q < 3; ++q) D->clsBase[pass][q] = C.opBase[q];
+    }
     D->nSurface = G.nSurface;
     D->fs = h->cfg.FreeSurface == 1 ? 1 : 0;
     h->vg = D;
@@ -280,10 +342,37 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid)
     const dim3 block(256);
     const dim3 grid(static_cast<unsigned>((G.N + 255) / 256));
     const bool cp = P.cpml != 0;
-    auto vel = G.is3d ? (cp ? vg_vel<true, true> : vg_vel<true, false>) : (cp ? vg_vel<false, true> : vg_vel<false, false>);
-    auto pres = G.is3d ? (cp ? vg_pres<true, true> : vg_pres<true, false>) : (cp ? vg_pres<false, true> : vg_pres<false, false>);
+    // kernel path 1 (generic only) keeps the ELL blocks; otherwise the
+    // stencil classes wherever they were built
+    const bool cls[2] = {h->kernelPath != 1 && G.clsId[0] != nullptr, h->kernelPath != 1 && G.clsId[1] != nullptr};
+    using K = void (*)(VgParams);
+    // class kernels with an entry loop of 6 (orders up to 6) or 12
+    int wmax = 0;
+    for (int k = 0; k < 6; ++k) wmax = G.W[k] > wmax ? G.W[k] : wmax;
+    const bool w6 = wmax <= 6;
+    const K velK[2][2][2] = {{{vg_vel<false, false, false>, w6 ? vg_vel<false, false, true, 6> : vg_vel<false, false, true>},
+                              {vg_vel<false, true, false>, w6 ? vg_vel<false, true, true, 6> : vg_vel<false, true, true>}},
+                             {{vg_vel<true, false, false>, w6 ? vg_vel<true, false, true, 6> : vg_vel<true, false, true>},
+                              {vg_vel<true, true, false>, w6 ? vg_vel<true, true, true, 6> : vg_vel<true, true, true>}}};
+    const K presK[2][2][2] = {{{vg_pres<false, false, false>, w6 ? vg_pres<false, false, true, 6> : vg_pres<false, false, true>},
+                               {vg_pres<false, true, false>, w6 ? vg_pres<false, true, true, 6> : vg_pres<false, true, true>}},
+                              {{vg_pres<true, false, false>, w6 ? vg_pres<true, false, true, 6> : vg_pres<true, false, true>},
+                               {vg_pres<true, true, false>, w6 ? vg_pres<true, true, true, 6> : vg_pres<true, true, true>}}};
+    auto with_classes = [&](int pass) {
+        VgParams Q = P;
+        if (cls[pass]) {
+            Q.cid = G.clsId[pass];
+            Q.coff = G.clsOff[pass];
+            Q.cw = G.clsW[pass];
+            Q.KW = G.clsKW[pass];
+            for (int q = 0; q < 3; ++q) Q.base[q] = G.clsBase[pass][q];
+        }
+        return Q;
+    };
+    K vel = velK[G.is3d ? 1 : 0][cp ? 1 : 0][cls[0] ? 1 : 0];
+    K pres = presK[G.is3d ? 1 : 0][cp ? 1 : 0][cls[1] ? 1 : 0];
     int launches = 0;
-    launch(vel, grid, block, dep, h->stream, P);
+    launch(vel, grid, block, dep, h->stream, with_classes(0));
     ++launches;
     const bool interp = G.nInterp[0] + G.nInterp[1] + G.nInterp[2] > 0;
     auto run_interp = [&](VgInterp I, int lists) {
@@ -337,7 +426,7 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid)
         interp_fields(kinds, fields, 3);
     }
     if (mid) cudaEventRecord(*mid, h->stream);
-    launch(pres, grid, block, dep, h->stream, P);
+    launch(pres, grid, block, dep, h->stream, with_classes(1));
     ++launches;
     if (interp && G.nInterp[0] > 0) {
         const int kinds[1] = {0};

@@ -57,11 +57,30 @@ struct InterpHost {
     bool inplace = true;       // no rewritten row reads another rewritten row
 };
 
+// Stencil classes of one pass (its three operators): rows whose entries have
+// the same column offsets (col - row) and weights share a class. Per row a
+// 32-bit class id; per class KW = sum of the operators' ELL widths (offset,
+// weight) pairs, operator after operator, in ELL entry order.
+struct ClassHost {
+    bool ok = false;                   // false: too many classes, use the ELL blocks
+    int KW = 0;
+    int nClass = 0;
+    int opBase[3] = {};                // first entry of each operator in a class row
+    std::vector<unsigned> id;          // N
+    std::vector<int> off;              // nClass x KW
+    std::vector<float> w;              // nClass x KW
+};
+
 struct VarGridHost {
     VarGridLayout L;
     EllHost Dxf, Dxb, Dyf, Dyb, Dzf, Dzb;
+    ClassHost cls[2];                  // velocity pass (Dxf, Dyf, Dzf), pressure pass (Dxb, Dyb, Dzb)
     InterpHost full, stagX, stagZ;
     std::vector<float> cpml[3][4];     // per axis: a_full, b_full, a_half, b_half (N each; CPML only)
+    // the same as a per-point code per axis into a table of (a_full, b_full,
+    // a_half, b_half) quadruples; code 0 = no coefficients
+    std::vector<unsigned short> cpCode[3];
+    std::vector<float> cpTab[3];
     std::vector<int> avgPartner[3];    // averaging partner per axis (-1: the point alone)
     long long nSurface = 0;            // rows with y == 0 (the first rows of layer 0)
 };
@@ -86,10 +105,17 @@ struct VarGridDev {
     const float* iw[3] = {};
     int inplace[3] = {1, 1, 1};
     float* itmp = nullptr;                  // scratch of the two-phase interpolation (sum of the row counts)
-    const float* cp[3][4] = {};             // CPML coefficients per axis (null: no CPML)
+    const unsigned short* cpCode[3] = {};   // CPML coefficient code per axis and point (null: no CPML)
+    const float* cpTab[3] = {};             // 4 floats per code
     const int* partner[3] = {};
     long long nSurface = 0;
     int fs = 0;
+    // stencil classes per pass (null: not available)
+    const unsigned* clsId[2] = {};
+    const int* clsOff[2] = {};
+    const float* clsW[2] = {};
+    int clsKW[2] = {};
+    int clsBase[2][3] = {};
 };
 
 } // namespace wave

@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
+#include <unordered_map>
 
 #include "wave_internal.h"
 
@@ -472,6 +474,60 @@ int build_interp(const VarGridLayout& L, const std::vector<long long>& rows, int
     return WAVE_OK;
 }
 
+// Groups the rows of one pass by their (offset, weight) entries. Gives up
+// (ok = false) when the classes would not be much smaller than the ELL blocks.
+void build_classes(long long N, const EllHost* const* ops, int nops, ClassHost& C)
+{
+    C = ClassHost{};
+    int KW = 0;
+    for (int q = 0; q < nops; ++q) {
+        C.opBase[q] = KW;
+        KW += ops[q]->W;
+    }
+    C.KW = KW;
+    if (KW == 0) return;
+    const long long cap = std::max<long long>(1024, N / 8);
+    std::unordered_map<std::string, unsigned> index;
+    index.reserve(4096);
+    C.id.resize(N);
+    std::string key(static_cast<size_t>(KW) * 8, '\0');
+    for (long long i = 0; i < N; ++i) {
+        char* k = &key[0];
+        for (int q = 0; q < nops; ++q) {
+            const EllHost& E = *ops[q];
+            for (int e = 0; e < E.W; ++e) {
+                const int off = static_cast<int>(E.col[static_cast<size_t>(e) * N + i] - i);
+                const float w = E.val[static_cast<size_t>(e) * N + i];
+                std::memcpy(k, &off, 4);
+                std::memcpy(k + 4, &w, 4);
+                k += 8;
+            }
+        }
+        auto it = index.find(key);
+        if (it == index.end()) {
+            if (static_cast<long long>(index.size()) >= cap) {
+                C = ClassHost{};
+                return;
+            }
+            const unsigned cls = static_cast<unsigned>(index.size());
+            index.emplace(key, cls);
+            for (int e = 0; e < KW; ++e) {
+                int off;
+                float w;
+                std::memcpy(&off, key.data() + 8 * e, 4);
+                std::memcpy(&w, key.data() + 8 * e + 4, 4);
+                C.off.push_back(off);
+                C.w.push_back(w);
+            }
+            C.id[i] = cls;
+        } else {
+            C.id[i] = it->second;
+        }
+    }
+    C.nClass = static_cast<int>(index.size());
+    C.ok = true;
+}
+
 } // namespace
 
 int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err)
@@ -543,6 +599,33 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err)
             }
         }
     }
+    // coefficient codes: the distinct quadruples of each axis (a layer's
+    // profile on the near and the far side), code 0 for none
+    if (c.DampingBoundary == 2) {
+        for (int ax = 0; ax < (is3d ? 3 : 2); ++ax) {
+            std::unordered_map<std::string, unsigned short> codes;
+            G.cpTab[ax].assign(4, 0.0f);
+            G.cpCode[ax].assign(N, 0);
+            std::string key(16, '\0');
+            for (long long i = 0; i < N; ++i) {
+                float q[4];
+                for (int k = 0; k < 4; ++k) q[k] = G.cpml[ax][k][i];
+                if (q[0] == 0.0f && q[1] == 0.0f && q[2] == 0.0f && q[3] == 0.0f) continue;
+                std::memcpy(&key[0], q, 16);
+                auto it = codes.find(key);
+                if (it == codes.end()) {
+                    if (codes.size() >= 65535) {
+                        err = "too many distinct CPML coefficients";
+                        return WAVE_ERR_ARG;
+                    }
+                    const unsigned short code = static_cast<unsigned short>(codes.size() + 1);
+                    it = codes.emplace(key, code).first;
+                    G.cpTab[ax].insert(G.cpTab[ax].end(), q, q + 4);
+                }
+                G.cpCode[ax][i] = it->second;
+            }
+        }
+    }
     // density averaging partners (Modelparameter.cpp:336-446)
     for (int ax = 0; ax < (is3d ? 3 : 2); ++ax) {
         G.avgPartner[ax].assign(N, -1);
@@ -564,6 +647,10 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err)
         }
     }
     G.nSurface = static_cast<long long>(L.vnx[0]) * L.vnz[0];   // layer 0 starts at y = 0
+    const EllHost* vel[3] = {&G.Dxf, &G.Dyf, &G.Dzf};
+    const EllHost* pres[3] = {&G.Dxb, &G.Dyb, &G.Dzb};
+    build_classes(N, vel, is3d ? 3 : 2, G.cls[0]);
+    build_classes(N, pres, is3d ? 3 : 2, G.cls[1]);
     return WAVE_OK;
 }
 
