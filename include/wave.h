@@ -198,7 +198,8 @@ int wave_get_nt(wave_handle* h, int* nt);
 int wave_get_num_receivers(wave_handle* h, int* n);
 /* Device pointer to the CUDA stream the handle launches on (cudaStream_t). */
 int wave_get_stream(wave_handle* h, void** stream);
-/* Number of kernels launched by this handle since creation. */
+/* Number of kernels launched by this handle since creation (memory copies
+ * and memsets are not counted). */
 int wave_get_launch_count(wave_handle* h, long long* count);
 /* Average duration [ms] of the most recent timed step kernels, measured with
  * CUDA events on the handle's stream when timing is on (see wave_set_timing). */
@@ -257,6 +258,18 @@ int wave_get_kernel_path(wave_handle* h, int* streaming_active);
  * 3-4 kernels of a step is hidden on small grids. Results do not depend on
  * this switch. The reference has no counterpart. */
 int wave_set_dependent_launch(wave_handle* h, int on);
+
+/* Wavefield decomposition after every step (config key decomposeWavefieldType,
+ * Simulation.cpp:316, 450-461; FD2Dacoustic::decompose, Wavefields2Dacoustic.cpp:
+ * 119-300): type 1 splits P, VX, VY into up- and down-going parts, type 2
+ * into left- and right-going parts, by the sign of S2 * max|S1|/max|S2| + S1
+ * with S1 = -P*VY (resp. -P*VX) and S2 = -(Dyf F)(dF/dt) (resp. Dxf); 0 turns
+ * it off. 2-D acoustic on a regular grid only. The parts are read with
+ * wave_get_field under the reference's file-name tokens "P.up", "P.down",
+ * "VX.up", ... or "P.left", "P.right", .... The reference's Dyf is empty for
+ * acoustic modelling with a free surface (FDTD2D.cpp:258-262), which makes
+ * its type-1 parts undefined there; this build uses Dyf regardless. */
+int wave_set_decomposition(wave_handle* h, int type);
 
 /* ---- seismogram output path and file formats ---- */
 /* Resampling of ntr traces (row-major ntr x nt, sample interval dt) to

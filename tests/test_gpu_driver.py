@@ -125,3 +125,21 @@ def test_driver_runs_the_variable_grid_ci_case(wave, tmp_path):
     golden = refcpu.read_mtx_array(os.path.join(GOLDEN, "seismogram.2D.acoustic.varGrid.ref.p.mtx"))
     assert got.shape == golden.shape
     assert refcpu.reference_misfit(got, golden) < GATE
+
+
+def test_driver_writes_the_decomposition_snapshots(wave, tmp_path):
+    """decomposeWavefieldType=1 with snapType=4: the driver writes P, VX, VY
+    and their up/down parts (Wavefields2Dacoustic.cpp:86-95); each part is the
+    field or zero and the two parts cover the field."""
+    cfg, ci = _setup(tmp_path, {"snapType": "4", "decomposeWavefieldType": "1", "tFirstSnapshot": "0.3",
+                                "tlastSnapshot": "0.3", "tincSnapshot": "0.1", "WavefieldFileName": "ci/wavefield"})
+    _run(wave, cfg)
+    step = 150
+    for f in ("P", "VX", "VY"):
+        F = refcpu.read_mtx_array(str(ci / f"wavefield.shot_1.{f}.{step}.mtx"))[:, 0]
+        up = refcpu.read_mtx_array(str(ci / f"wavefield.shot_1.{f}.up.{step}.mtx"))[:, 0]
+        down = refcpu.read_mtx_array(str(ci / f"wavefield.shot_1.{f}.down.{step}.mtx"))[:, 0]
+        assert np.abs(F).max() > 0
+        assert np.all((up == F) | (up == 0)) and np.all((down == F) | (down == 0))
+        assert np.all((up == F) | (down == F))
+        assert np.any(up != F) and np.any(down != F)

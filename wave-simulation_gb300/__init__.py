@@ -45,6 +45,7 @@ ABI_SYMBOLS = (
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
     "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
     "wave_agc_normalize_traces", "wave_grid_num_points", "wave_grid_index", "wave_grid_coordinates",
+    "wave_set_decomposition",
 )
 
 
@@ -179,6 +180,7 @@ def lib():
     L.wave_wavelet.argtypes = [I, I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
     L.wave_set_kernel_path.argtypes = [P, I]
     L.wave_set_dependent_launch.argtypes = [P, I]
+    L.wave_set_decomposition.argtypes = [P, I]
     L.wave_get_kernel_path.argtypes = [P, CP(I)]
     L.wave_average_shear_modulus.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, I]
     L.wave_average_shear_modulus_noalloc.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, I, P]
@@ -458,6 +460,11 @@ class ForwardSolver:
         """Programmatic dependent launch of the per-point kernels (default on);
         the results do not depend on it."""
         _check(self.h, lib().wave_set_dependent_launch(self.h, 1 if on else 0))
+
+    def set_decomposition(self, kind: int):
+        """decomposeWavefieldType: 1 up/down, 2 left/right parts of P, VX, VY
+        after every step (2-D acoustic); read them with field("P.up") etc."""
+        _check(self.h, lib().wave_set_decomposition(self.h, int(kind)))
 
     def adjoint_gradient(self, dobs, checkpoint_every: int = 50):
         """Misfit J = 1/2 ||d - d_obs||^2 and its gradient w.r.t. (vp, vs, rho)

@@ -62,6 +62,12 @@ struct wave_handle {
     El3dPlan el3d, el3dp;
     // variable-grid operators (vargrid.cu); null on a regular grid
     std::shared_ptr<wave::VarGridDev> vg;
+    // wavefield decomposition after every step (decompose.cu): 0 off, 1 up/down, 2 left/right
+    int decompType = 0;
+    float* decOld[3] = {};     // P, VX, VY before the step
+    float* decS2[3] = {};      // Poynting estimates per field
+    float* decOut[6] = {};     // P.up/left, P.down/right, VX.., VY..
+    unsigned* decMax = nullptr;
     int kernelPath = 0;          // 0 automatic, 1 generic only, 2 one-point streaming, 3 pair streaming (where available)
     int passStreaming[2] = {0, 0};   // automatic path: timed choice per pass (0 generic, 1 one-point, 2 pair streaming)
     bool dependentLaunch = true;     // generic kernels launched with programmatic stream serialization
@@ -106,6 +112,11 @@ void step_once(wave_handle* h);
 void vargrid_setup(wave_handle* h, const VarGridHost& G);
 void vargrid_set_model(wave_handle* h, const float* rho, const float* vp);
 int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid);
+
+// wavefield decomposition (decompose.cu): the copy of the fields before a
+// step, and the two kernels after it (returns the kernel count)
+void decompose_before_step(wave_handle* h);
+int decompose_after_step(wave_handle* h);
 
 // the adjoint gradient driver (adjoint.cu), shared by the single-handle and
 // the batched entry points

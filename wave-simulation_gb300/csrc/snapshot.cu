@@ -229,8 +229,18 @@ int wave_get_field(wave_handle* h, const char* name, float* out, int mem)
     int f = -1;
     for (auto& e : names)
         if (s == e.n) f = e.f;
-    if (f < 0 || !h->f[f]) return herr(h, WAVE_ERR_ARG, std::string("wave_get_field: no wavefield ") + name + " for this equation");
-    cudaError_t e = cudaMemcpyAsync(out, h->f[f], h->N * sizeof(float), mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream);
+    // decomposition parts (Wavefields2Dacoustic.cpp:86-107 file names): "p.up", "vx.down", "vy.left", ...
+    const float* src = f >= 0 ? h->f[f] : nullptr;
+    static const char* parts[2][6] = {{"p.up", "p.down", "vx.up", "vx.down", "vy.up", "vy.down"},
+                                      {"p.left", "p.right", "vx.left", "vx.right", "vy.left", "vy.right"}};
+    for (int t = 0; t < 2; ++t)
+        for (int k = 0; k < 6; ++k)
+            if (s == parts[t][k]) {
+                if (h->decompType != t + 1) return herr(h, WAVE_ERR_STATE, std::string("wave_get_field: ") + name + " needs wave_set_decomposition(h, " + std::to_string(t + 1) + ")");
+                src = h->decOut[k];
+            }
+    if (!src) return herr(h, WAVE_ERR_ARG, std::string("wave_get_field: no wavefield ") + name + " for this equation");
+    cudaError_t e = cudaMemcpyAsync(out, src, h->N * sizeof(float), mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return herr(h, WAVE_ERR_CUDA, std::string("wave_get_field: ") + cudaGetErrorString(e));
     return WAVE_OK;

@@ -228,6 +228,7 @@ void launch_step(wave_handle* h)
         h->launches += 1;
         return;
     }
+    if (h->decompType) wave::decompose_before_step(h);
     launch_pass(h, 0);
     launch_pass(h, 1);
     h->launches += 2;
@@ -239,12 +240,14 @@ void launch_step(wave_handle* h)
     }
     launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
     h->launches += 1;
+    if (h->decompType) h->launches += wave::decompose_after_step(h);
 }
 
 void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
 {
     cudaEvent_t a, b, c;
     cudaEventCreate(&a); cudaEventCreate(&b); cudaEventCreate(&c);
+    if (h->decompType) wave::decompose_before_step(h);
     cudaEventRecord(a, h->stream);
     if (h->vg) {
         h->launches += wave::vargrid_launch_step(h, false, &b);
@@ -268,6 +271,7 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
     }
     launch_srcrec(h->sq, h->tcounter, h->stream);
     h->launches += 1;
+    if (h->decompType) h->launches += wave::decompose_after_step(h);
 }
 
 // Automatic kernel choice: times each pass with the generic and the streaming

@@ -80,7 +80,9 @@ std::vector<std::string> snapshot_fields(int eq, bool is3d, int snapType)
     if (eq == WAVE_EQ_ACOUSTIC) {
         if (snapType == 1) return v;
         if (snapType == 2) return {"P"};
-        if (snapType == 4 && !is3d) return {"P", "VX", "VY"};
+        // snapType 4 / 5 add the decomposition parts (Wavefields2Dacoustic.cpp:86-107)
+        if (snapType == 4 && !is3d) return {"P", "VX", "VY", "P.up", "P.down", "VX.up", "VX.down", "VY.up", "VY.down"};
+        if (snapType == 5 && !is3d) return {"P", "VX", "VY", "P.left", "P.right", "VX.left", "VX.right", "VY.left", "VY.right"};
         return {};
     }
     if (snapType == 1) return v;
@@ -188,6 +190,9 @@ int main(int argc, char** argv)
         const std::string eqname[] = {"acoustic", "elastic", "viscoelastic", "sh", "viscosh", "tmem", "emem", "viscotmem", "viscoemem"};
         auto solver = wave::gpu::Factory::Create(cfg.dimension == 3 ? "3D" : "2D", eqname[cfg.equation]);
         solver->initForwardSolver(cfg);
+        // wavefield decomposition (Simulation.cpp:316, 457-461)
+        const int decomposition = key<int>(keys, "decomposeWavefieldType", 0);
+        if (decomposition != 0) wave::gpu::check(solver->handle(), wave_set_decomposition(solver->handle(), decomposition));
         solver->prepareForModelling(model);
         solver->setReceivers(rec);
         const int nt = solver->NT();
@@ -199,7 +204,7 @@ int main(int argc, char** argv)
         const int format = key<int>(keys, "SeismogramFormat", 1);
         if (normalize < 0 || normalize > 4) throw wave::gpu::Error(WAVE_ERR_ARG, "normalizeTraces must be 0-4");
         const int snapType = key<int>(keys, "snapType", 0);
-        if (snapType < 0 || snapType > 4) throw wave::gpu::Error(WAVE_ERR_ARG, "Invalid snapType.");
+        if (snapType < 0 || snapType > 5) throw wave::gpu::Error(WAVE_ERR_ARG, "Invalid snapType.");
         const int instantaneous = key<int>(keys, "outputInstantaneous", 0);
         if (format != 1 && format != 4) throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "SeismogramFormat: 1 (mtx) and 4 (su) are written here");
         for (int shot : shots) {
@@ -236,7 +241,11 @@ int main(int argc, char** argv)
                     } else {
                         std::vector<float> f(npts);
                         for (const auto& name : snapshot_fields(cfg.equation, cfg.dimension == 3, snapType)) {
-                            wave::gpu::check(solver->handle(), wave_get_field(solver->handle(), name.c_str(), f.data(), WAVE_MEM_HOST));
+                            // decomposition parts of another (or no) decomposition type are zero, as in the reference
+                            const bool part = name.find('.') != std::string::npos;
+                            const bool have = !part || (snapType == 4 && decomposition == 1) || (snapType == 5 && decomposition == 2);
+                            if (have) wave::gpu::check(solver->handle(), wave_get_field(solver->handle(), name.c_str(), f.data(), WAVE_MEM_HOST));
+                            else std::fill(f.begin(), f.end(), 0.0f);
                             wave::gpu::check(nullptr, wave_write_mtx((wbase + "." + name + "." + step + ".mtx").c_str(), f.data(), static_cast<int64_t>(npts), 1));
                         }
                     }
