@@ -415,7 +415,7 @@ __device__ __forceinline__ void visco_s_body(const StepParams& P, const Pt& p)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) visco_s(StepParams P)
+__global__ void __launch_bounds__(256, 5) visco_s(StepParams P)   // 48 registers: 5 blocks per SM (4.4 % faster than 64 at 4)
 {
     dependent_launch_prologue();
     Pt p;
