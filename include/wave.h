@@ -237,7 +237,10 @@ int wave_average_shear_modulus(const float* mu, float* out, int64_t NX, int64_t 
  * caller. */
 int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, int64_t NY, int64_t NZ, int mode, void* stream);
 
-/* Kernel path: 0 = automatic, 1 = generic kernels only, 2 = the one-point
+/* Kernel path: 0 = automatic, 1 = generic kernels only (and the separate
+ * source/receiver kernel: by default, acoustic grids of at most 2^20 points
+ * with pressure sources and no ABS add the sources and record the receivers
+ * inside the pressure kernel, one launch less per step), 2 = the one-point
  * streaming TMA kernels wherever they apply (3-D elastic grids with
  * NX % 4 == 0 whose 32x8 column tiles meet at most one CPML slab per axis),
  * 3 = the two-points-per-thread streaming kernels wherever they apply (64x8

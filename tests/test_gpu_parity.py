@@ -348,3 +348,26 @@ def test_launch_count_is_native(wave, refcpu):
     s.seismograms()
     assert s.launch_count() - before >= 40 * 3
     s.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_acoustic_fused_source_receiver_step_is_bit_identical(dim, wave, refcpu):
+    """On small acoustic grids the pressure kernel adds the sources and records
+    the receivers itself (one launch less per step); kernel path 1 keeps the
+    separate source/receiver kernel. Same operations: same bits. Two sources,
+    receivers of every component, two of them at one point."""
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "acoustic", dim, 4, 1, 2)
+    sidx = np.concatenate([sidx, sidx + 7])
+    stype = np.concatenate([stype, stype])
+    sig = np.concatenate([sig, 0.5 * sig])
+    ridx = np.concatenate([ridx, ridx[:1]])
+    rtype = np.concatenate([rtype, [2]])
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    wc = to_wave_cfg(wave, cfg)
+    a = wave.simulate(wc, m32, sidx, stype, sig.astype(np.float32), ridx, rtype, kernel_path=0)
+    b = wave.simulate(wc, m32, sidx, stype, sig.astype(np.float32), ridx, rtype, kernel_path=1)
+    np.testing.assert_array_equal(a, b)
+    o = refcpu.Oracle(cfg, model, sidx, stype, sig, ridx, rtype, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    assert rel(a, ref) < TOL

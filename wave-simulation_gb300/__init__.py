@@ -452,8 +452,9 @@ class ForwardSolver:
 
     def set_kernel_path(self, path: int):
         """0 = automatic (fastest kernel per pass, timed when the model is set),
-        1 = generic kernels, 2 = one-point streaming TMA kernels, 3 = two-point
-        streaming TMA kernels (2 and 3 wherever they apply)."""
+        1 = generic kernels (and the separate source/receiver kernel), 2 =
+        one-point streaming TMA kernels, 3 = two-point streaming TMA kernels
+        (2 and 3 wherever they apply)."""
         _check(self.h, lib().wave_set_kernel_path(self.h, path))
 
     def set_dependent_launch(self, on: bool):

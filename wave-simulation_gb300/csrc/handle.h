@@ -45,6 +45,11 @@ struct wave_handle {
 
     long long* sidx = nullptr; int* stype = nullptr; float* signals = nullptr; int nsrc = 0;
     long long* ridx = nullptr; int* rtype = nullptr; float* seis = nullptr; int nrec = 0;
+    // host copies of the acquisition and the point map of the fused acoustic
+    // source/receiver step (solver.cu update_fusion)
+    std::vector<long long> hSrcIdx, hRecIdx;
+    std::vector<int> hSrcType, hRecType;
+    int* srMap = nullptr;
 
     StepParams sp{};
     SrcRecParams sq{};

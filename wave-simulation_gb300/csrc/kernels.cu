@@ -44,6 +44,8 @@ template <int H>
 __global__ void __launch_bounds__(256) acoustic_v(StepParams P)
 {
     dependent_launch_prologue();
+    // the pressure kernel of this step reads t = counter - 1
+    if (P.sr.on && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *P.sr.tcounter += 1;
     Pt p;
     if (!point(P, p)) return;
     acoustic_v_body<H>(P, p);
@@ -78,6 +80,24 @@ __device__ __forceinline__ void acoustic_p_body(const StepParams& P, const Pt& p
     P.f[F_P][p.i] = pv;
 }
 
+// SourceReceiverImpl::applySource + gatherSeismogram (SourceReceiverImpl.cpp:
+// 12-37, FDTDacoustic.cpp) at one marked point, after its pressure update:
+// pressure sources in index order, then the receivers at the point
+__device__ __forceinline__ void fused_srcrec(const StepParams& P, long long i)
+{
+    const int k = P.sr.map[i];
+    if (k < 0) return;
+    const int t = *P.sr.tcounter - 1;
+    float pv = P.f[F_P][i];
+    for (int s = P.sr.ptSrc[k]; s >= 0; s = P.sr.srcNext[s]) pv += P.sr.signals[(long long)s * P.sr.nt + t];
+    P.f[F_P][i] = pv;
+    for (int r = P.sr.ptRec[k]; r >= 0; r = P.sr.recNext[r]) {
+        const int ty = P.sr.rtype[r];
+        const float v = ty == WAVE_TYPE_P ? pv : ty == WAVE_TYPE_VX ? P.f[F_VX][i] : ty == WAVE_TYPE_VY ? P.f[F_VY][i] : P.f[F_VZ][i];
+        P.sr.seis[(long long)r * P.sr.nt + t] = v;
+    }
+}
+
 template <int H>
 __global__ void __launch_bounds__(256) acoustic_p(StepParams P)
 {
@@ -85,6 +105,7 @@ __global__ void __launch_bounds__(256) acoustic_p(StepParams P)
     Pt p;
     if (!point(P, p)) return;
     acoustic_p_body<H>(P, p);
+    if (P.sr.on) fused_srcrec(P, p.i);
 }
 
 template <int H>

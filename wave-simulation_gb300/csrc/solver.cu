@@ -12,6 +12,7 @@
 #include <stdexcept>
 #include <memory>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -220,6 +221,65 @@ void launch_kernel_of(wave_handle* h, int kind, int pass, bool dep)
 
 void launch_pass(wave_handle* h, int pass, bool dep = true) { launch_kernel_of(h, pass_kernel(h, pass), pass, dep); }
 
+// Sources and receivers inside the acoustic pressure kernel (SrFuse): on
+// grids of at most 2^20 points (the point map, 4 B per point, stays in L2)
+// with pressure sources only and no ABS (whose damping of the velocities
+// runs after the pressure kernel), unless kernel path 1 asks for the separate
+// source/receiver kernel. Saves one launch per step on small grids.
+void update_fusion(wave_handle* h)
+{
+    wave::SrFuse& F = h->sp.sr;
+    F = wave::SrFuse{};
+    h->graphDirty = true;
+    bool ok = h->cfg.equation == WAVE_EQ_ACOUSTIC && !h->vg && !h->sp.abs && h->kernelPath != 1 &&
+              h->N <= (1LL << 20) && h->seis != nullptr && h->nrec > 0 && h->nsrc == static_cast<int>(h->hSrcIdx.size()) &&
+              h->nrec == static_cast<int>(h->hRecIdx.size());
+    for (int t : h->hSrcType) ok = ok && t == WAVE_TYPE_P;
+    if (!ok) return;
+    // one record per marked point; sources and receivers chained in index order
+    std::unordered_map<long long, int> rec;
+    std::vector<int> ptSrc, ptRec, lastS, lastR;
+    std::vector<int> srcNext(h->nsrc, -1), recNext(h->nrec, -1);
+    auto record = [&](long long i) {
+        auto it = rec.find(i);
+        if (it != rec.end()) return it->second;
+        const int k = static_cast<int>(ptSrc.size());
+        rec.emplace(i, k);
+        ptSrc.push_back(-1); ptRec.push_back(-1); lastS.push_back(-1); lastR.push_back(-1);
+        return k;
+    };
+    for (int s = 0; s < h->nsrc; ++s) {
+        const int k = record(h->hSrcIdx[s]);
+        if (lastS[k] < 0) ptSrc[k] = s; else srcNext[lastS[k]] = s;
+        lastS[k] = s;
+    }
+    for (int r = 0; r < h->nrec; ++r) {
+        const int k = record(h->hRecIdx[r]);
+        if (lastR[k] < 0) ptRec[k] = r; else recNext[lastR[k]] = r;
+        lastR[k] = r;
+    }
+    std::vector<int> map(h->N, -1);
+    for (const auto& e : rec) map[e.first] = e.second;
+    if (!h->srMap) h->srMap = h->alloc<int>(h->N);
+    h->check(cudaMemcpy(h->srMap, map.data(), h->N * sizeof(int), cudaMemcpyHostToDevice), "upload");
+    auto up = [&](const std::vector<int>& v) {
+        int* d = h->alloc<int>(v.size());
+        if (!v.empty()) h->check(cudaMemcpy(d, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice), "upload");
+        return d;
+    };
+    F.ptSrc = up(ptSrc);
+    F.ptRec = up(ptRec);
+    F.srcNext = up(srcNext);
+    F.recNext = up(recNext);
+    F.map = h->srMap;
+    F.nt = h->NT;
+    F.tcounter = h->tcounter;
+    F.signals = h->signals;
+    F.rtype = h->rtype;
+    F.seis = h->seis;
+    F.on = 1;
+}
+
 void launch_step(wave_handle* h)
 {
     if (h->vg) {
@@ -238,8 +298,10 @@ void launch_step(wave_handle* h)
                          p1.size() > 2 ? p1[2] : -1, h->stream, h->dependentLaunch);
         h->launches += 1;
     }
-    launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
-    h->launches += 1;
+    if (!h->sp.sr.on) {
+        launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
+        h->launches += 1;
+    }
     if (h->decompType) h->launches += wave::decompose_after_step(h);
 }
 
@@ -269,8 +331,10 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
                          p1.size() > 2 ? p1[2] : -1, h->stream);
         h->launches += 1;
     }
-    launch_srcrec(h->sq, h->tcounter, h->stream);
-    h->launches += 1;
+    if (!h->sp.sr.on) {
+        launch_srcrec(h->sq, h->tcounter, h->stream);
+        h->launches += 1;
+    }
     if (h->decompType) h->launches += wave::decompose_after_step(h);
 }
 
@@ -858,6 +922,9 @@ int wave_set_sources(wave_handle* h, int n, const int64_t* idx, const int* type,
                                 mem == WAVE_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice), "upload");
         }
         h->sq.nsrc = n; h->sq.sidx = h->sidx; h->sq.stype = h->stype; h->sq.signals = h->signals;
+        h->hSrcIdx.assign(idx, idx + n);
+        h->hSrcType.assign(type, type + n);
+        update_fusion(h);
         h->graphDirty = true;
     })
     return WAVE_OK;
@@ -884,6 +951,9 @@ int wave_set_receivers(wave_handle* h, int n, const int64_t* idx, const int* typ
         h->seis = h->alloc<float>(static_cast<size_t>(n > 0 ? n : 1) * h->NT);
         h->check(cudaMemset(h->seis, 0, static_cast<size_t>(n > 0 ? n : 1) * h->NT * sizeof(float)), "memset");
         h->sq.nrec = n; h->sq.ridx = h->ridx; h->sq.rtype = h->rtype; h->sq.seis = h->seis;
+        h->hRecIdx.assign(idx, idx + n);
+        h->hRecType.assign(type, type + n);
+        update_fusion(h);
         h->graphDirty = true;
     })
     return WAVE_OK;
@@ -1064,6 +1134,7 @@ int wave_set_kernel_path(wave_handle* h, int path)
     if (path < 0 || path > 3) return fail(h, WAVE_ERR_ARG, "wave_set_kernel_path: path must be 0, 1, 2 or 3");
     h->kernelPath = path;
     h->graphDirty = true;
+    WAVE_TRY(h, { update_fusion(h); })
     return WAVE_OK;
 }
 

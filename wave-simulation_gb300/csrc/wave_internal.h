@@ -69,6 +69,23 @@ enum Mat {
     M_COUNT
 };
 
+// Sources and receivers handled inside the acoustic pressure kernel (small
+// grids, pressure sources, no ABS): the thread that updates a marked point
+// adds its sources and records its receivers; the velocity kernel advances
+// the step counter.
+struct SrFuse {
+    int on, nt;
+    int* tcounter;
+    const int* map;        // N entries: -1, or the point's record
+    const int* ptSrc;      // per record: first source at the point (-1: none)
+    const int* ptRec;      // per record: first receiver at the point
+    const int* srcNext;    // next source at the same point, in index order
+    const int* recNext;
+    const float* signals;  // nsrc x nt
+    const int* rtype;
+    float* seis;           // nrec x nt
+};
+
 // Everything a step kernel needs, passed by value.
 struct StepParams {
     int NX, NY, NZ;
@@ -91,6 +108,7 @@ struct StepParams {
     float DT;
     float DThalf;
     float invRelax[kMaxL], c1[kMaxL], c2[kMaxL], Cc[kMaxL], relaxTime[kMaxL];
+    SrFuse sr;
 };
 
 struct SrcRecParams {
