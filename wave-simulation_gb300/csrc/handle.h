@@ -116,7 +116,7 @@ void step_once(wave_handle* h);
 // mid, if given, is recorded between the velocity and pressure halves)
 void vargrid_setup(wave_handle* h, const VarGridHost& G);
 void vargrid_set_model(wave_handle* h, const float* rho, const float* vp);
-int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid);
+int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrecDone);
 
 // wavefield decomposition (decompose.cu): the copy of the fields before a
 // step, and the two kernels after it (returns the kernel count)

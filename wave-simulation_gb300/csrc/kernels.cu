@@ -842,60 +842,7 @@ __global__ void __launch_bounds__(256) abs_frame_batch(const StepParams* __restr
 // receivers copy column t. One block; t read from a device counter so the
 // same launch can be replayed from a CUDA graph.
 // --------------------------------------------------------------------------
-__device__ __forceinline__ float* field_of(const SrcRecParams& Q, int type)
-{
-    if (Q.eq >= WAVE_EQ_TMEM) {
-        switch (type) {
-        case WAVE_TYPE_EZ: return Q.f[F_EZ];
-        case WAVE_TYPE_EX: return Q.f[F_EX];
-        case WAVE_TYPE_EY: return Q.f[F_EY];
-        default: return Q.f[F_HZ];
-        }
-    }
-    switch (type) {
-    case WAVE_TYPE_VX: return Q.f[F_VX];
-    case WAVE_TYPE_VY: return Q.f[F_VY];
-    case WAVE_TYPE_VZ: return Q.f[F_VZ];
-    default: return Q.f[F_P];
-    }
-}
-
-__device__ __forceinline__ void srcrec_body(const SrcRecParams& Q, int* tcounter)
-{
-    const int t = *tcounter;
-    const bool elasticP = (Q.eq == WAVE_EQ_ELASTIC || Q.eq == WAVE_EQ_VISCOELASTIC);
-    for (int type = 1; type <= 4; ++type) {
-        for (int s = threadIdx.x; s < Q.nsrc; s += blockDim.x) {
-            if (Q.stype[s] != type) continue;
-            const float v = Q.signals[(long long)s * Q.nt + t];
-            const long long i = Q.sidx[s];
-            if (Q.eq < WAVE_EQ_TMEM && type == WAVE_TYPE_P && elasticP) {
-                atomicAdd(Q.f[F_SXX] + i, v);
-                atomicAdd(Q.f[F_SYY] + i, v);
-                if (Q.is3d) atomicAdd(Q.f[F_SZZ] + i, v);
-            } else {
-                atomicAdd(field_of(Q, type) + i, v);
-            }
-        }
-        __syncthreads();
-    }
-    for (int r = threadIdx.x; r < Q.nrec; r += blockDim.x) {
-        const long long i = Q.ridx[r];
-        const int type = Q.rtype[r];
-        float v;
-        if (Q.eq < WAVE_EQ_TMEM && type == WAVE_TYPE_P && elasticP) {
-            v = Q.f[F_SXX][i];
-            v += Q.f[F_SYY][i];
-            if (Q.is3d) { v += Q.f[F_SZZ][i]; v /= 3.0f; }
-            else v *= 0.5f;
-        } else {
-            v = field_of(Q, type)[i];
-        }
-        Q.seis[(long long)r * Q.nt + t] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) *tcounter = t + 1;
-}
+// field_of and srcrec_body: stencil.cuh (shared with the variable-grid step)
 
 __global__ void __launch_bounds__(512) srcrec_kernel(SrcRecParams Q, int* tcounter)
 {

@@ -283,9 +283,12 @@ void update_fusion(wave_handle* h)
 void launch_step(wave_handle* h)
 {
     if (h->vg) {
-        h->launches += wave::vargrid_launch_step(h, h->dependentLaunch, nullptr);
-        launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
-        h->launches += 1;
+        bool done = false;
+        h->launches += wave::vargrid_launch_step(h, h->dependentLaunch, nullptr, &done);
+        if (!done) {
+            launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
+            h->launches += 1;
+        }
         return;
     }
     if (h->decompType) wave::decompose_before_step(h);
@@ -312,11 +315,14 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
     if (h->decompType) wave::decompose_before_step(h);
     cudaEventRecord(a, h->stream);
     if (h->vg) {
-        h->launches += wave::vargrid_launch_step(h, false, &b);
+        bool done = false;
+        h->launches += wave::vargrid_launch_step(h, false, &b, &done);
         cudaEventRecord(c, h->stream);
         ev.push_back(a); ev.push_back(b); ev.push_back(c);
-        launch_srcrec(h->sq, h->tcounter, h->stream);
-        h->launches += 1;
+        if (!done) {
+            launch_srcrec(h->sq, h->tcounter, h->stream);
+            h->launches += 1;
+        }
         return;
     }
     launch_pass(h, 0, false);

@@ -51,7 +51,10 @@ struct VgParams {
     int base[3];
 };
 
-// phase 0: in place; 1: new values into tmp; 2: tmp into the field
+// phase 0: in place; 1: new values into tmp; 2: tmp into the field.
+// srSlot >= 0: the blocks with blockIdx.y == srSlot run the step's sources
+// and receivers instead (block 0 only), when none of them is on an interface
+// row, so they touch no row the interpolation reads or writes.
 struct VgInterp {
     int n[3];
     int phase[3];
@@ -60,6 +63,9 @@ struct VgInterp {
     const int* row[3];
     const int* col[3];
     const float* w[3];
+    int srSlot;
+    SrcRecParams Q;
+    int* tcounter;
 };
 
 __device__ __forceinline__ float ell_row(const VgParams& P, int op, long long i, const float* __restrict__ u)
@@ -170,6 +176,10 @@ __global__ void __launch_bounds__(256) vg_interp(VgInterp I)
 {
     dependent_launch_prologue();
     const int s = blockIdx.y;
+    if (s == I.srSlot) {
+        if (blockIdx.x == 0) srcrec_body(I.Q, I.tcounter);
+        return;
+    }
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= I.n[s]) return;
     float* f = I.f[s];
@@ -269,6 +279,7 @@ const T* upload(wave_handle* h, const std::vector<T>& v)
 void vargrid_setup(wave_handle* h, const VarGridHost& G)
 {
     auto D = std::make_shared<VarGridDev>();
+    D->L = G.L;
     const bool is3d = h->is3d();
     D->N = G.L.N;
     D->is3d = is3d;
@@ -335,8 +346,9 @@ void vargrid_set_model(wave_handle* h, const float* rho, const float* vp)
     h->check(cudaGetLastError(), "variable grid model preparation");
 }
 
-int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid)
+int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrecDone)
 {
+    *srcrecDone = false;
     const VarGridDev& G = *h->vg;
     const VgParams P = params_of(h);
     const dim3 block(256);
@@ -379,8 +391,9 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid)
         int mx = 0;
         for (int s = 0; s < lists; ++s) mx = I.n[s] > mx ? I.n[s] : mx;
         if (mx == 0) return;
+        const int slots = I.srSlot >= 0 ? lists + 1 : lists;
         cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3(static_cast<unsigned>((mx + 255) / 256), static_cast<unsigned>(lists));
+        cfg.gridDim = dim3(static_cast<unsigned>((mx + 255) / 256), static_cast<unsigned>(slots));
         cfg.blockDim = dim3(256);
         cfg.stream = h->stream;
         cudaLaunchAttribute attr[1];
@@ -393,8 +406,9 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid)
     };
     // the lists of one launch: in place where allowed, else gather into the
     // scratch in one launch and scatter back in a second
-    auto interp_fields = [&](const int* kinds, float* const* fields, int m) {
+    auto interp_fields = [&](const int* kinds, float* const* fields, int m, bool withSrcrec) {
         VgInterp I{};
+        I.srSlot = -1;
         int n = 0;
         bool twoPhase = false;
         long long off = 0;
@@ -412,10 +426,22 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid)
             twoPhase = twoPhase || !G.inplace[kind];
             ++n;
         }
+        if (withSrcrec && !twoPhase && n > 0) {
+            I.srSlot = n;
+            I.Q = h->sq;
+            I.tcounter = h->tcounter;
+            *srcrecDone = true;
+        }
         run_interp(I, n);
         if (twoPhase) {
             for (int q = 0; q < n; ++q) I.n[q] = I.phase[q] == 1 ? I.n[q] : 0;
             for (int q = 0; q < n; ++q) I.phase[q] = 2;
+            if (withSrcrec && n > 0) {   // after the scatter
+                I.srSlot = n;
+                I.Q = h->sq;
+                I.tcounter = h->tcounter;
+                *srcrecDone = true;
+            }
             run_interp(I, n);
         }
     };
@@ -423,15 +449,26 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid)
         // vx: StaggeredX, vy: Full, vz: StaggeredZ (ForwardSolver3Dacoustic.cpp:139-197)
         const int kinds[3] = {1, 0, 2};
         float* const fields[3] = {P.vx, P.vy, G.is3d ? P.vz : nullptr};
-        interp_fields(kinds, fields, 3);
+        interp_fields(kinds, fields, 3, false);
     }
     if (mid) cudaEventRecord(*mid, h->stream);
     launch(pres, grid, block, dep, h->stream, with_classes(1));
     ++launches;
     if (interp && G.nInterp[0] > 0) {
+        // sources and receivers in the same launch when none is on an interface row
+        bool apart = true;
+        auto off_interface = [&](const std::vector<long long>& idx) {
+            for (long long i : idx) {
+                int x, y, z;
+                G.L.coord(i, x, y, z);
+                if (G.L.onIfaceY[y]) apart = false;
+            }
+        };
+        off_interface(h->hSrcIdx);
+        off_interface(h->hRecIdx);
         const int kinds[1] = {0};
         float* const fields[1] = {P.p};
-        interp_fields(kinds, fields, 1);
+        interp_fields(kinds, fields, 1, apart && h->kernelPath != 1);
     }
     h->check(cudaGetLastError(), "variable grid step launch");
     return launches;

@@ -93,6 +93,7 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err);
 
 // device side of a variable-grid handle (vargrid.cu)
 struct VarGridDev {
+    VarGridLayout L;                        // host copy of the index space
     long long N = 0;
     int is3d = 0;
     int nOps = 0;
