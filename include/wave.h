@@ -264,12 +264,14 @@ int wave_set_dependent_launch(wave_handle* h, int on);
 
 /* Wavefield decomposition after every step (config key decomposeWavefieldType,
  * Simulation.cpp:316, 450-461; FD2Dacoustic::decompose, Wavefields2Dacoustic.cpp:
- * 119-300): type 1 splits P, VX, VY into up- and down-going parts, type 2
- * into left- and right-going parts, by the sign of S2 * max|S1|/max|S2| + S1
- * with S1 = -P*VY (resp. -P*VX) and S2 = -(Dyf F)(dF/dt) (resp. Dxf); 0 turns
- * it off. 2-D acoustic on a regular grid only. The parts are read with
- * wave_get_field under the reference's file-name tokens "P.up", "P.down",
- * "VX.up", ... or "P.left", "P.right", .... The reference's Dyf is empty for
+ * 119-300; FD2Dtmem::decompose, Wavefields2Dtmem.cpp:109-160): type 1 splits
+ * P, VX, VY (TMz: EZ) into up- and down-going parts, type 2 into left- and
+ * right-going parts, by the sign of S2 * max|S1|/max|S2| + S1 with
+ * S1 = -P*VY (resp. -P*VX; TMz: EZ*HX, resp. -EZ*HY) and
+ * S2 = -(Dyf F)(dF/dt) (resp. Dxf); 0 turns it off. 2-D acoustic and 2-D TMz
+ * on a regular grid (the reference's other decompositions are empty). The
+ * parts are read with wave_get_field under the reference's file-name tokens
+ * "P.up", "P.down", "VX.up", ..., "P.left", ..., "EZ.up", "EZ.left", .... The reference's Dyf is empty for
  * acoustic modelling with a free surface (FDTD2D.cpp:258-262), which makes
  * its type-1 parts undefined there; this build uses Dyf regardless. */
 int wave_set_decomposition(wave_handle* h, int type);

@@ -1,11 +1,12 @@
-// decompose.cu — wavefield decomposition of the 2-D acoustic wavefields into
-// up/down-going (decomposeWavefieldType 1) or left/right-going (2) parts by
-// the sign of a Poynting-vector estimate, after every time step:
-// Simulation.cpp:450-461 (time derivative of the step: (new - old) / DT) and
-// FD2Dacoustic::decompose (Wavefields2Dacoustic.cpp:119-300).
+// decompose.cu — wavefield decomposition of the 2-D acoustic and 2-D TMz
+// wavefields into up/down-going (decomposeWavefieldType 1) or
+// left/right-going (2) parts by the sign of a Poynting-vector estimate, after
+// every time step: Simulation.cpp:450-461 (time derivative of the step:
+// (new - old) / DT), FD2Dacoustic::decompose (Wavefields2Dacoustic.cpp:
+// 119-300) and FD2Dtmem::decompose (Wavefields2Dtmem.cpp:109-160).
 //
-// Per field F in (P, VX, VY) and point:
-//   S1  = -P * VY (type 1) or -P * VX (type 2)
+// Per field F (P, VX, VY; or EZ) and point:
+//   S1  = -P * VY (type 1) or -P * VX (type 2); EZ * HX or -(EZ * HY)
 //   S2F = -(D F) * dF/dt, D = Dyf (type 1) or Dxf (type 2), DT folded in
 //   QF  = S2F * (max|S1| / max|S2F|) + S1
 //   F.up / F.left  = F where QF <= 0, else 0
@@ -26,18 +27,22 @@ namespace {
 struct DecompParams {
     StepParams P;
     int type;
+    int nf;                    // decomposed fields: 3 (P, VX, VY) or 1 (EZ)
     float negDTinv;            // -(1/DT) in single precision
-    const float* cur[3];       // P, VX, VY after the step
+    const float* s1a;          // S1 = s1sign * (s1a * s1b)
+    const float* s1b;
+    float s1sign;
+    const float* cur[3];       // fields after the step
     const float* old[3];       // before the step
     float* s2[3];
     float* out[6];             // F.up/left, F.down/right for P, VX, VY
     unsigned* mx;              // max|S1|, max|S2P|, max|S2VX|, max|S2VY| as float bits
 };
 
+// the sign is applied exactly, so (-P)*VY = -(P*VY) and (EZ*HY)*(-1) are the same
 __device__ __forceinline__ float s1_of(const DecompParams& D, long long i)
 {
-    const float p = D.cur[0][i];
-    return __fmul_rn(-p, D.type == 1 ? D.cur[2][i] : D.cur[1][i]);
+    return D.s1sign * __fmul_rn(D.s1a[i], D.s1b[i]);
 }
 
 template <int H>
@@ -47,7 +52,7 @@ __global__ void __launch_bounds__(256) decomp_a(DecompParams D)
     if (!point(D.P, p)) return;
     const float s1 = s1_of(D, p.i);
     atomicMax(D.mx, __float_as_uint(fabsf(s1)));
-    for (int q = 0; q < 3; ++q) {
+    for (int q = 0; q < D.nf; ++q) {
         const float* f = D.cur[q];
         // wavefieldsTemp -= wavefields; wavefieldsTemp *= -DTinv
         const float dfdt = __fmul_rn(__fsub_rn(D.old[q][p.i], f[p.i]), D.negDTinv);
@@ -65,7 +70,7 @@ __global__ void __launch_bounds__(256) decomp_b(DecompParams D)
     if (!point(D.P, p)) return;
     const float s1 = s1_of(D, p.i);
     const float m1 = __uint_as_float(D.mx[0]);
-    for (int q = 0; q < 3; ++q) {
+    for (int q = 0; q < D.nf; ++q) {
         const float ratio = __fdiv_rn(m1, __uint_as_float(D.mx[1 + q]));
         const float Q = __fadd_rn(__fmul_rn(D.s2[q][p.i], ratio), s1);
         const int sg = (Q > 0.0f) - (Q < 0.0f);
@@ -82,11 +87,22 @@ DecompParams params_of(wave_handle* h)
     D.type = h->decompType;
     const float DT = static_cast<float>(h->cfg.DT);
     D.negDTinv = -(1.0f / DT);
-    const int f[3] = {F_P, F_VX, F_VY};
-    for (int q = 0; q < 3; ++q) {
-        D.cur[q] = h->f[f[q]];
+    const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
+    const int acoustic[3] = {F_P, F_VX, F_VY};
+    D.nf = tm ? 1 : 3;
+    for (int q = 0; q < D.nf; ++q) {
+        D.cur[q] = h->f[tm ? F_EZ : acoustic[q]];
         D.old[q] = h->decOld[q];
         D.s2[q] = h->decS2[q];
+    }
+    if (tm) {   // EZ * HX, or -(EZ * HY)
+        D.s1a = h->f[F_EZ];
+        D.s1b = h->f[D.type == 1 ? F_HX : F_HY];
+        D.s1sign = D.type == 1 ? 1.0f : -1.0f;
+    } else {    // -P * VY, or -P * VX
+        D.s1a = h->f[F_P];
+        D.s1b = h->f[D.type == 1 ? F_VY : F_VX];
+        D.s1sign = -1.0f;
     }
     for (int k = 0; k < 6; ++k) D.out[k] = h->decOut[k];
     D.mx = h->decMax;
@@ -97,9 +113,11 @@ DecompParams params_of(wave_handle* h)
 
 void decompose_before_step(wave_handle* h)
 {
+    const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
     const int f[3] = {F_P, F_VX, F_VY};
-    for (int q = 0; q < 3; ++q)
-        h->check(cudaMemcpyAsync(h->decOld[q], h->f[f[q]], h->N * sizeof(float), cudaMemcpyDeviceToDevice, h->stream), "decomposition copy");
+    for (int q = 0; q < (tm ? 1 : 3); ++q)
+        h->check(cudaMemcpyAsync(h->decOld[q], h->f[tm ? F_EZ : f[q]], h->N * sizeof(float), cudaMemcpyDeviceToDevice, h->stream),
+                 "decomposition copy");
 }
 
 int decompose_after_step(wave_handle* h)
@@ -128,8 +146,8 @@ extern "C" int wave_set_decomposition(wave_handle* h, int type)
         h->err = "wave_set_decomposition: decomposeWavefieldType must be 0, 1 or 2";
         return WAVE_ERR_ARG;
     }
-    if (type != 0 && (h->cfg.equation != WAVE_EQ_ACOUSTIC || h->is3d() || h->vg)) {
-        h->err = "wave_set_decomposition: the decomposition exists for 2-D acoustic modelling on a regular grid";
+    if (type != 0 && ((h->cfg.equation != WAVE_EQ_ACOUSTIC && h->cfg.equation != WAVE_EQ_TMEM) || h->is3d() || h->vg)) {
+        h->err = "wave_set_decomposition: the decomposition exists for 2-D acoustic and 2-D TMz modelling on a regular grid";
         return WAVE_ERR_UNSUPPORTED;
     }
     try {

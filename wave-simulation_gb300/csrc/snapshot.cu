@@ -233,9 +233,11 @@ int wave_get_field(wave_handle* h, const char* name, float* out, int mem)
     const float* src = f >= 0 ? h->f[f] : nullptr;
     static const char* parts[2][6] = {{"p.up", "p.down", "vx.up", "vx.down", "vy.up", "vy.down"},
                                       {"p.left", "p.right", "vx.left", "vx.right", "vy.left", "vy.right"}};
+    static const char* partsEz[2][6] = {{"ez.up", "ez.down", "", "", "", ""}, {"ez.left", "ez.right", "", "", "", ""}};
+    const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
     for (int t = 0; t < 2; ++t)
         for (int k = 0; k < 6; ++k)
-            if (s == parts[t][k]) {
+            if (s == (tm ? partsEz : parts)[t][k]) {
                 if (h->decompType != t + 1) return herr(h, WAVE_ERR_STATE, std::string("wave_get_field: ") + name + " needs wave_set_decomposition(h, " + std::to_string(t + 1) + ")");
                 src = h->decOut[k];
             }

@@ -71,6 +71,9 @@ std::vector<std::string> snapshot_fields(int eq, bool is3d, int snapType)
 {
     const bool em = eq >= WAVE_EQ_TMEM;
     if (em) {
+        // snapType 4 / 5 of TMz add the decomposition parts (Wavefields2Dtmem.cpp:88-96)
+        if (eq == WAVE_EQ_TMEM && snapType == 4) return {"EZ", "EZ.up", "EZ.down"};
+        if (eq == WAVE_EQ_TMEM && snapType == 5) return {"EZ", "EZ.left", "EZ.right"};
         if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_VISCOTMEM) return snapType == 1 ? std::vector<std::string>{"HX", "HY"} : std::vector<std::string>{"EZ"};
         if (!is3d) return snapType == 1 ? std::vector<std::string>{"HZ"} : std::vector<std::string>{"EX", "EY"};
         return snapType == 1 ? std::vector<std::string>{"HX", "HY", "HZ"} : std::vector<std::string>{"EX", "EY", "EZ"};
