@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <unordered_map>
 
 #include "wave_internal.h"
@@ -360,47 +361,81 @@ struct Assembler {
     }
 };
 
+// Rows are independent: contiguous row ranges are assembled on host threads
+// (up to 16), each into its own tap lists, then packed into the ELL block.
 template <class RowFn>
 int build_ell(long long N, RowFn fn, EllHost& E, std::string& err, const char* name)
 {
-    std::vector<Tap> taps;
-    std::vector<int> cnt(N);
-    std::vector<long long> cols;
-    std::vector<float> vals;
-    std::vector<long long> first(N + 1, 0);
-    cols.reserve(N * 6);
-    vals.reserve(N * 6);
-    for (long long i = 0; i < N; ++i) {
-        taps.clear();
-        fn(i, taps);
-        first[i] = static_cast<long long>(cols.size());
-        for (const Tap& t : taps) {
-            if (t.col < 0) {
-                err = std::string(name) + ": a stencil tap falls between the stored rows of the variable grid";
-                return WAVE_ERR_ARG;
+    unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (N < (1LL << 16)) nt = 1;
+    struct Part {
+        std::vector<int> cnt;
+        std::vector<long long> cols;
+        std::vector<float> vals;
+        bool bad = false;
+    };
+    std::vector<Part> parts(nt);
+    auto range = [&](unsigned t, long long& lo, long long& hi) {
+        lo = N * t / nt;
+        hi = N * (t + 1) / nt;
+    };
+    auto gather = [&](unsigned t) {
+        long long lo, hi;
+        range(t, lo, hi);
+        Part& P = parts[t];
+        P.cnt.resize(hi - lo);
+        P.cols.reserve((hi - lo) * 6);
+        P.vals.reserve((hi - lo) * 6);
+        std::vector<Tap> taps;
+        for (long long i = lo; i < hi; ++i) {
+            taps.clear();
+            fn(i, taps);
+            P.cnt[i - lo] = static_cast<int>(taps.size());
+            for (const Tap& tp : taps) {
+                if (tp.col < 0) P.bad = true;
+                P.cols.push_back(tp.col);
+                P.vals.push_back(tp.val);
             }
-            cols.push_back(t.col);
-            vals.push_back(t.val);
         }
-    }
-    first[N] = static_cast<long long>(cols.size());
+    };
+    auto run = [&](auto&& f) {
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nt; ++t) th.emplace_back(f, t);
+        f(0u);
+        for (auto& x : th) x.join();
+    };
+    run(gather);
     int W = 0;
-    for (long long i = 0; i < N; ++i) W = std::max(W, static_cast<int>(first[i + 1] - first[i]));
+    for (const Part& P : parts) {
+        if (P.bad) {
+            err = std::string(name) + ": a stencil tap falls between the stored rows of the variable grid";
+            return WAVE_ERR_ARG;
+        }
+        for (int c : P.cnt) W = std::max(W, c);
+    }
     E.W = W;
     E.col.assign(static_cast<size_t>(W) * N, 0);
     E.val.assign(static_cast<size_t>(W) * N, 0.0f);
-    for (long long i = 0; i < N; ++i) {
-        const int n = static_cast<int>(first[i + 1] - first[i]);
-        for (int k = 0; k < W; ++k) {
-            const size_t o = static_cast<size_t>(k) * N + i;
-            if (k < n) {
-                E.col[o] = static_cast<int>(cols[first[i] + k]);
-                E.val[o] = vals[first[i] + k];
-            } else {
-                E.col[o] = static_cast<int>(i);
+    auto pack = [&](unsigned t) {
+        long long lo, hi;
+        range(t, lo, hi);
+        const Part& P = parts[t];
+        size_t at = 0;
+        for (long long i = lo; i < hi; ++i) {
+            const int n = P.cnt[i - lo];
+            for (int k = 0; k < W; ++k) {
+                const size_t o = static_cast<size_t>(k) * N + i;
+                if (k < n) {
+                    E.col[o] = static_cast<int>(P.cols[at + k]);
+                    E.val[o] = P.vals[at + k];
+                } else {
+                    E.col[o] = static_cast<int>(i);   // padding: weight 0 on the row itself
+                }
             }
+            at += n;
         }
-    }
+    };
+    run(pack);
     return WAVE_OK;
 }
 
