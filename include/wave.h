@@ -273,7 +273,7 @@ int wave_set_dependent_launch(wave_handle* h, int on);
  * parts are read with wave_get_field under the reference's file-name tokens
  * "P.up", "P.down", "VX.up", ..., "P.left", ..., "EZ.up", "EZ.left", .... The reference's Dyf is empty for
  * acoustic modelling with a free surface (FDTD2D.cpp:258-262), which makes
- * its type-1 parts undefined there; this build uses Dyf regardless. */
+ * its type-1 parts undefined there; this library applies Dyf regardless. */
 int wave_set_decomposition(wave_handle* h, int type);
 
 /* ---- seismogram output path and file formats ---- */

@@ -17,8 +17,8 @@ from oracle import refcpu  # noqa: E402
 
 CI = os.path.join(ROOT, "tests", "golden", "ci")
 
-# name -> (config file, golden file). The variable-grid cases need the
-# discontinuous-grid operators, which are not part of this build.
+# name -> (config file, golden file). The variable-grid cases are in
+# VARGRID_CASES below.
 CASES = {
     "2D.acoustic": ("configuration_ci.2D.acoustic.txt", "seismogram.2D.acoustic.ref.p.mtx"),
     "2D.sh": ("configuration_ci.2D.sh.txt", "seismogram.2D.sh.ref.vz.mtx"),
