@@ -130,6 +130,15 @@ int wave_grid_index(const wave_config* cfg, int64_t x, int64_t y, int64_t z, int
  * x, y, z receive n = wave_grid_num_points values each. Also returns the
  * extents the variable grid reduced NX, NY, NZ to (NULL to skip). */
 int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_t* z, int64_t n, int64_t* extents3);
+/* The assembled sparse operator `op` of a variable-grid configuration
+ * (host only, no GPU): 0 Dxf, 1 Dyf (DyfFreeSurface with FreeSurface=1),
+ * 2 Dzf, 3 Dxb, 4 Dyb, 5 Dzb, DT folded in (Derivatives.cpp:129-1245,
+ * FDTD2D.cpp:193-229), or the interface interpolation 6 Full, 7 StaggeredX,
+ * 8 StaggeredZ (Derivatives.cpp:1252-1546; rows off the interfaces are the
+ * identity). Returned as an ELL block: *width entries per row, entry k of
+ * row i at k*N + i, unused entries with weight 0. With cols == NULL only
+ * *width is set; otherwise capacity must be at least width * N. */
+int wave_grid_operator(const wave_config* cfg, int op, int* width, int32_t* cols, float* vals, int64_t capacity);
 
 /* ForwardSolver::Factory<float>::Create(dimension, type)
  * (ForwardSolver/ForwardSolverFactory.cpp:4-67) followed by initForwardSolver

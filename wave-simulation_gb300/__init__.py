@@ -45,7 +45,7 @@ ABI_SYMBOLS = (
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
     "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
     "wave_agc_normalize_traces", "wave_grid_num_points", "wave_grid_index", "wave_grid_coordinates",
-    "wave_set_decomposition",
+    "wave_set_decomposition", "wave_grid_operator",
 )
 
 
@@ -207,6 +207,7 @@ def lib():
     L.wave_grid_num_points.argtypes = [CP(WaveConfig), ctypes.POINTER(i64)]
     L.wave_grid_index.argtypes = [CP(WaveConfig), i64, i64, i64, ctypes.POINTER(i64)]
     L.wave_grid_coordinates.argtypes = [CP(WaveConfig), P, P, P, i64, P]
+    L.wave_grid_operator.argtypes = [CP(WaveConfig), I, CP(I), P, P, i64]
     L.wave_batch_last_error.restype = ctypes.c_char_p
     L.wave_batch_last_error.argtypes = [P]
     _lib = L
@@ -257,6 +258,20 @@ def grid_coordinates(cfg: WaveConfig):
     _check(None, lib().wave_grid_coordinates(ctypes.byref(cfg), *(a.ctypes.data_as(ctypes.c_void_p) for a in xyz), n,
                                              ext.ctypes.data_as(ctypes.c_void_p)))
     return xyz[0], xyz[1], xyz[2], tuple(int(v) for v in ext)
+
+
+def grid_operator(cfg: WaveConfig, op: int):
+    """The host-assembled operator `op` of a variable-grid configuration
+    (wave_grid_operator: 0 Dxf, 1 Dyf, 2 Dzf, 3 Dxb, 4 Dyb, 5 Dzb, 6-8 the
+    interface interpolations) as (cols, vals), each W x N."""
+    n = grid_num_points(cfg)
+    w = ctypes.c_int()
+    _check(None, lib().wave_grid_operator(ctypes.byref(cfg), int(op), ctypes.byref(w), None, None, 0))
+    cols = np.zeros((w.value, n), dtype=np.int32)
+    vals = np.zeros((w.value, n), dtype=np.float32)
+    _check(None, lib().wave_grid_operator(ctypes.byref(cfg), int(op), ctypes.byref(w), cols.ctypes.data_as(ctypes.c_void_p),
+                                          vals.ctypes.data_as(ctypes.c_void_p), cols.size))
+    return cols, vals
 
 
 def wavelet(shape: int, nt: int, dt: float, fc: float, amp: float, tshift: float) -> np.ndarray:

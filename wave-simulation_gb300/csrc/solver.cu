@@ -537,6 +537,44 @@ int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_
     return WAVE_OK;
 }
 
+int wave_grid_operator(const wave_config* cfg, int op, int* width, int32_t* cols, float* vals, int64_t capacity)
+{
+    if (!cfg || !width || op < 0 || op > 8) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: invalid arguments");
+    if (!(cfg->useVariableGrid || cfg->useVariableFDoperators))
+        return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: not a variable-grid configuration");
+    wave::VarGridHost G;
+    std::string err;
+    int rc = wave::vargrid_build(*cfg, G, err);
+    if (rc != WAVE_OK) return fail(nullptr, rc, err);
+    const long long N = G.L.N;
+    if (op < 6) {
+        const wave::EllHost* ops[6] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb};
+        const wave::EllHost& E = *ops[op];
+        *width = E.W;
+        if (!cols) return WAVE_OK;
+        if (!vals || capacity < static_cast<int64_t>(E.W) * N) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: capacity too small");
+        std::memcpy(cols, E.col.data(), E.col.size() * sizeof(int32_t));
+        std::memcpy(vals, E.val.data(), E.val.size() * sizeof(float));
+        return WAVE_OK;
+    }
+    const wave::InterpHost* in[3] = {&G.full, &G.stagX, &G.stagZ};
+    const wave::InterpHost& I = *in[op - 6];
+    *width = 4;
+    if (!cols) return WAVE_OK;
+    if (!vals || capacity < 4 * N) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: capacity too small");
+    for (long long i = 0; i < N; ++i)
+        for (int k = 0; k < 4; ++k) {
+            cols[k * N + i] = static_cast<int32_t>(i);
+            vals[k * N + i] = k == 0 ? 1.0f : 0.0f;
+        }
+    for (size_t r = 0; r < I.row.size(); ++r)
+        for (int k = 0; k < 4; ++k) {
+            cols[k * N + I.row[r]] = I.col[4 * r + k];
+            vals[k * N + I.row[r]] = I.w[4 * r + k];
+        }
+    return WAVE_OK;
+}
+
 int wave_solver_create(const wave_config* cfg, wave_handle** out)
 {
     if (!cfg || !out) return fail(nullptr, WAVE_ERR_ARG, "wave_solver_create: null argument");
