@@ -179,6 +179,24 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The largest x over all ranks (all_reduce MAX on the initialised process
+    group, NCCL with device "cuda" or gloo with "cpu"); x itself on one rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, seconds_max: float, world: int) -> float:
+    """Whole-job throughput of N shot replicas: the units all ranks processed
+    over the slowest rank's time (weak scaling: per-rank work is fixed)."""
+    return world * units_per_rank / seconds_max
+
+
 def cpu_sample(steps: int, warm: int, budget_s: float = 60.0):
     """The reference formulation (oracle refcpu<float>, CSR operators and one
     pass per vector operation) on the full grid, all host threads, for at most
@@ -266,12 +284,9 @@ def run_gpu(args):
     vel_ms, str_ms, nsamp = s.kernel_times()
     passes = s.streaming_passes()
     s.set_timing(False)
-    t_max = torch.tensor([ms_total], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t_max, op=torch.distributed.ReduceOp.MAX)
-    ms_total = float(t_max.item())
+    ms_total = max_over_ranks(ms_total, world)
     ms_step = ms_total / args.steps
-    value = world * N * args.steps / (ms_total * 1e-3) / 1e9
+    value = whole_job_rate(N * args.steps, ms_total * 1e-3, world) / 1e9
     finite = s.check_finite()
     s.close()
 
@@ -294,7 +309,8 @@ def run_gpu(args):
         s2.close()
         h2d = sum(v.nbytes for v in model.values()) + sig.nbytes + sidx.nbytes + stype.nbytes + ridx.nbytes + rtype.nbytes
         d2h = seis.nbytes
-        e2e = {"value": world * N * args.steps / (t1 - t0) / 1e9, "unit": UNIT,
+        e2e_s = max_over_ranks(t1 - t0, world)
+        e2e = {"value": whole_job_rate(N * args.steps, e2e_s, world) / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps}
 
     peak, peak_kind = load_peaks()
