@@ -50,6 +50,9 @@ struct wave_handle {
     std::vector<long long> hSrcIdx, hRecIdx;
     std::vector<int> hSrcType, hRecType;
     int* srMap = nullptr;
+    int* srList[4] = {};               // point records: first source, first receiver; source and receiver chains
+    size_t srListCap[4] = {};
+    size_t capSidx = 0, capStype = 0, capSignals = 0, capRidx = 0, capRtype = 0, capSeis = 0;
 
     StepParams sp{};
     SrcRecParams sq{};
@@ -99,6 +102,25 @@ struct wave_handle {
         if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
         allocs.push_back(p);
         return static_cast<T*>(p);
+    }
+    // A device buffer of at least `need` elements in slot p (capacity cap):
+    // kept when it is large enough, else freed and replaced, so repeated
+    // calls (one per shot) do not accumulate allocations.
+    template <class T>
+    T* reuse(T*& p, size_t& cap, size_t need)
+    {
+        if (p && cap >= need) return p;
+        if (p) {
+            for (auto it = allocs.begin(); it != allocs.end(); ++it)
+                if (*it == static_cast<void*>(p)) {
+                    allocs.erase(it);
+                    break;
+                }
+            cudaFree(p);
+        }
+        p = alloc<T>(need > 0 ? need : 1);
+        cap = need > 0 ? need : 1;
+        return p;
     }
     void check(cudaError_t e, const char* what)
     {

@@ -262,15 +262,15 @@ void update_fusion(wave_handle* h)
     for (const auto& e : rec) map[e.first] = e.second;
     if (!h->srMap) h->srMap = h->alloc<int>(h->N);
     h->check(cudaMemcpy(h->srMap, map.data(), h->N * sizeof(int), cudaMemcpyHostToDevice), "upload");
-    auto up = [&](const std::vector<int>& v) {
-        int* d = h->alloc<int>(v.size());
+    auto up = [&](int slot, const std::vector<int>& v) {
+        int* d = h->reuse(h->srList[slot], h->srListCap[slot], v.size());
         if (!v.empty()) h->check(cudaMemcpy(d, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice), "upload");
-        return d;
+        return static_cast<const int*>(d);
     };
-    F.ptSrc = up(ptSrc);
-    F.ptRec = up(ptRec);
-    F.srcNext = up(srcNext);
-    F.recNext = up(recNext);
+    F.ptSrc = up(0, ptSrc);
+    F.ptRec = up(1, ptRec);
+    F.srcNext = up(2, srcNext);
+    F.recNext = up(3, recNext);
     F.map = h->srMap;
     F.nt = h->NT;
     F.tcounter = h->tcounter;
@@ -957,9 +957,9 @@ int wave_set_sources(wave_handle* h, int n, const int64_t* idx, const int* type,
         h->check(cudaStreamSynchronize(h->stream), "sync");
         h->nsrc = n;
         if (n > 0) {
-            h->sidx = h->alloc<long long>(n);
-            h->stype = h->alloc<int>(n);
-            h->signals = h->alloc<float>(static_cast<size_t>(n) * h->NT);
+            h->reuse(h->sidx, h->capSidx, n);
+            h->reuse(h->stype, h->capStype, n);
+            h->reuse(h->signals, h->capSignals, static_cast<size_t>(n) * h->NT);
             h->check(cudaMemcpy(h->sidx, idx, n * sizeof(long long), cudaMemcpyHostToDevice), "upload");
             h->check(cudaMemcpy(h->stype, type, n * sizeof(int), cudaMemcpyHostToDevice), "upload");
             h->check(cudaMemcpy(h->signals, signals, static_cast<size_t>(n) * h->NT * sizeof(float),
@@ -987,12 +987,12 @@ int wave_set_receivers(wave_handle* h, int n, const int64_t* idx, const int* typ
         h->check(cudaStreamSynchronize(h->stream), "sync");
         h->nrec = n;
         if (n > 0) {
-            h->ridx = h->alloc<long long>(n);
-            h->rtype = h->alloc<int>(n);
+            h->reuse(h->ridx, h->capRidx, n);
+            h->reuse(h->rtype, h->capRtype, n);
             h->check(cudaMemcpy(h->ridx, idx, n * sizeof(long long), cudaMemcpyHostToDevice), "upload");
             h->check(cudaMemcpy(h->rtype, type, n * sizeof(int), cudaMemcpyHostToDevice), "upload");
         }
-        h->seis = h->alloc<float>(static_cast<size_t>(n > 0 ? n : 1) * h->NT);
+        h->reuse(h->seis, h->capSeis, static_cast<size_t>(n > 0 ? n : 1) * h->NT);
         h->check(cudaMemset(h->seis, 0, static_cast<size_t>(n > 0 ? n : 1) * h->NT * sizeof(float)), "memset");
         h->sq.nrec = n; h->sq.ridx = h->ridx; h->sq.rtype = h->rtype; h->sq.seis = h->seis;
         h->hRecIdx.assign(idx, idx + n);
