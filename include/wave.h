@@ -285,6 +285,22 @@ int wave_set_dependent_launch(wave_handle* h, int on);
  * its type-1 parts undefined there; this library applies Dyf regardless. */
 int wave_set_decomposition(wave_handle* h, int type);
 
+/* Source encoding (config keys useSourceEncode, NumShotDomains;
+ * Sources::calcSourceSettingsEncode, Acquisition/Sources.cpp:569-660, for
+ * time-domain modelling): the n shots (one source row each; shot_no and amp
+ * as read from the source file) are regrouped into num_domains super-shots.
+ * mode 1: the first num_domains shots go to super-shots 0.. in order, the
+ * others to random super-shots that are not yet full (at most
+ * ceil(n / num_domains) shots each), then each amplitude's sign is flipped at
+ * random; mode 2: shot i to super-shot i % num_domains; mode 3: contiguous
+ * runs of ceil(n / num_domains) shots. shot_no_out[i] = num_domains*10^4 + 1 +
+ * super-shot; amp_out the (signed) amplitudes. Random numbers are the C
+ * library's rand() after srand(seed) (the reference seeds with time(0)).
+ * Host only. The reference's receiver-side encode/decode of per-shot
+ * receiver sets (Receivers.cpp:569-573) is not part of this call. */
+int wave_encode_sources(int mode, int num_domains, unsigned int seed, int n, const int* shot_no, const float* amp,
+                        int* shot_no_out, float* amp_out);
+
 /* ---- seismogram output path and file formats ---- */
 /* Resampling of ntr traces (row-major ntr x nt, sample interval dt) to
  * seismo_dt by linear interpolation (Common::calcResampleMat,

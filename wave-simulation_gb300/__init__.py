@@ -45,7 +45,7 @@ ABI_SYMBOLS = (
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
     "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
     "wave_agc_normalize_traces", "wave_grid_num_points", "wave_grid_index", "wave_grid_coordinates",
-    "wave_set_decomposition", "wave_grid_operator",
+    "wave_set_decomposition", "wave_grid_operator", "wave_encode_sources",
 )
 
 
@@ -208,6 +208,7 @@ def lib():
     L.wave_grid_index.argtypes = [CP(WaveConfig), i64, i64, i64, ctypes.POINTER(i64)]
     L.wave_grid_coordinates.argtypes = [CP(WaveConfig), P, P, P, i64, P]
     L.wave_grid_operator.argtypes = [CP(WaveConfig), I, CP(I), P, P, i64]
+    L.wave_encode_sources.argtypes = [I, I, ctypes.c_uint, I, P, P, P, P]
     L.wave_batch_last_error.restype = ctypes.c_char_p
     L.wave_batch_last_error.argtypes = [P]
     _lib = L
@@ -272,6 +273,19 @@ def grid_operator(cfg: WaveConfig, op: int):
     _check(None, lib().wave_grid_operator(ctypes.byref(cfg), int(op), ctypes.byref(w), cols.ctypes.data_as(ctypes.c_void_p),
                                           vals.ctypes.data_as(ctypes.c_void_p), cols.size))
     return cols, vals
+
+
+def encode_sources(mode: int, num_domains: int, seed: int, shot_no, amp):
+    """Source encoding (wave_encode_sources): (super-shot numbers, signed
+    amplitudes) for one source row per shot."""
+    no = np.ascontiguousarray(shot_no, dtype=np.int32)
+    a = np.ascontiguousarray(amp, dtype=np.float32)
+    no_out = np.zeros_like(no)
+    a_out = np.zeros_like(a)
+    _check(None, lib().wave_encode_sources(int(mode), int(num_domains), int(seed) & 0xFFFFFFFF, len(no),
+                                           no.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p),
+                                           no_out.ctypes.data_as(ctypes.c_void_p), a_out.ctypes.data_as(ctypes.c_void_p)))
+    return no_out, a_out
 
 
 def wavelet(shape: int, nt: int, dt: float, fc: float, amp: float, tshift: float) -> np.ndarray:

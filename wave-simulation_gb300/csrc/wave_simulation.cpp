@@ -10,6 +10,7 @@
 //
 //   wave_simulation <parameter file>
 #include <cstdio>
+#include <ctime>
 #include <fstream>
 #include <iostream>
 #include <map>
@@ -199,6 +200,20 @@ int main(int argc, char** argv)
         solver->prepareForModelling(model);
         solver->setReceivers(rec);
         const int nt = solver->NT();
+        // source encoding into NumShotDomains super-shots (Simulation.cpp:255-266,
+        // Sources.cpp:569-660); seeded with time(0) as in the reference unless
+        // the key seedtime is given
+        const int encodeMode = key<int>(keys, "useSourceEncode", 0);
+        if (encodeMode != 0) {
+            const int domains = key<int>(keys, "NumShotDomains", 1);
+            const unsigned seed = static_cast<unsigned>(key<long long>(keys, "seedtime", static_cast<long long>(std::time(nullptr))));
+            std::vector<int> no(srcs.size()), noOut(srcs.size());
+            std::vector<float> amp(srcs.size()), ampOut(srcs.size());
+            for (size_t i = 0; i < srcs.size(); ++i) { no[i] = srcs[i].no; amp[i] = static_cast<float>(srcs[i].amp); }
+            wave::gpu::check(nullptr, wave_encode_sources(encodeMode, domains, seed, static_cast<int>(srcs.size()), no.data(), amp.data(),
+                                                          noOut.data(), ampOut.data()));
+            for (size_t i = 0; i < srcs.size(); ++i) { srcs[i].no = noOut[i]; srcs[i].amp = ampOut[i]; }
+        }
         std::set<int> shots;
         for (auto& s : srcs) shots.insert(s.no);
         const char* names[2][4] = {{"p", "vx", "vy", "vz"}, {"ez", "ex", "ey", "hz"}};
