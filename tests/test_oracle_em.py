@@ -63,3 +63,35 @@ def test_3d_em_is_finite_and_absorbed():
     assert np.isfinite(s).all()
     # the CPML absorbs: the late part of the traces is much weaker than the peak
     assert np.abs(s[:, -40:]).max() < 0.2 * np.abs(s).max()
+
+
+@pytest.mark.parametrize("boundary", [0, 2])
+def test_lossless_tmz_oracle_equals_the_pinned_acoustic_oracle(boundary, refcpu):
+    """The reference has no EM golden. Lossless 2-D TMz is the 2-D acoustic
+    system under Ez <-> p, Hy <-> vx, -Hx <-> vy, 1/eps <-> M, mu <-> rho
+    (ForwardSolver2Dtmem.cpp:108-174 against ForwardSolver2Dacoustic.cpp:
+    91-190), and the CPML profiles are the same functions of VMaxCPML, DH and
+    DT; so on a homogeneous model the EM oracle must reproduce the acoustic
+    oracle, which the reference's goldens pin. FP64, CPML or no boundary."""
+    eps0, mu0 = 8.854187817e-12, 4e-7 * np.pi
+    NX, NY, DH, eps_r, mu_r = 120, 100, 0.02, 4.0, 1.0
+    c = 1.0 / np.sqrt(eps_r * eps0 * mu_r * mu0)
+    DT = 0.3 * DH / (c * np.sqrt(2.0))
+    kw = dict(dimension=2, NX=NX, NY=NY, DH=DH, DT=DT, T=400 * DT, spatialFDorder=4, DampingBoundary=boundary,
+              BoundaryWidth=10, NPower=4.0, CenterFrequencyCPML=2e8, VMaxCPML=float(c))
+    cfg_a = refcpu.make_config(equation="acoustic", **kw)
+    cfg_e = refcpu.make_config(equation="tmem", **kw)
+    nt, n = refcpu.nt_of(cfg_a), NX * NY
+    sidx = np.array([NX // 2 + NX * (NY // 2)])
+    sig = refcpu.ricker(nt, DT, 6e8, 1.0, 0.0, np.float64)[None]
+    ridx = np.array([10 + NX * 10, NX - 20 + NX * 30, 40 + NX * (NY - 15), NX // 2 + NX * 3])
+    o = refcpu.Oracle(cfg_a, dict(rho=np.full(n, mu_r * mu0), vp=np.full(n, c)), sidx, np.array([1]), sig, ridx,
+                      np.ones(4, int), dtype=np.float64)
+    p = o.run()
+    o.close()
+    o = refcpu.Oracle(cfg_e, dict(eps_r=np.full(n, eps_r), sigma=np.zeros(n), mu_r=np.full(n, mu_r)), sidx,
+                      np.array([1]), sig, ridx, np.ones(4, int), dtype=np.float64)
+    ez = o.run()
+    o.close()
+    assert np.abs(p).max() > 0
+    assert np.linalg.norm(ez - p) / np.linalg.norm(p) < 1e-8
