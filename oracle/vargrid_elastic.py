@@ -1,0 +1,234 @@
+"""TEST INFRASTRUCTURE ONLY — CPU restatement of the reference's 2-D elastic
+time step on the variable grid (no GPU counterpart yet): the checker for a
+future variable-grid elastic path.
+
+Restates, on top of oracle/vargrid.py (layout, Dxf/Dxb/Dyf/Dyb, the
+interface interpolations, CPML coefficients, density averages):
+
+* the staggered-x y-derivatives DyfStaggeredX / DybStaggeredX
+  (src/ForwardSolver/Derivatives/Derivatives.cpp:852-1011), whose taps shift
+  in x by dhFactor/3 where the staggered point of the coarse layer sits at a
+  different x (always zero-padded at the grid edges);
+* the 4-point S-modulus average XY (src/Modelparameter/Modelparameter.cpp:
+  449-533) with the vacuum rules of ModelparameterSeismic::
+  calcAveragedSWaveModulus (ModelparameterSeismic.cpp:421-432);
+* FD2Delastic::run with the variable-grid interpolations
+  (src/ForwardSolver/ForwardSolver2Delastic.cpp:117-297) for CPML or no
+  damping boundary, without a free surface.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle import vargrid as vg
+
+
+def _stag_rows(g: vg.VarGrid, y: int, x: int, orders, var_order: bool, forward: bool):
+    """Taps [(X, Y, order, j, dh layer)] of one row of DyfStaggeredX (forward)
+    or DybStaggeredX (Derivatives.cpp:852-1011)."""
+    layer = int(g.layer_y[y])
+    order = orders[layer] if var_order else orders[0]
+    dist = int(g.dist_y[y]) // g.dhf[layer]
+    if dist == 0:
+        order = 2
+    elif order > dist * 2:
+        order = dist * 2
+    on = bool(g.on_iface_y[y])
+    tr = int(g.trans_y[y])
+
+    def iface(yy):
+        return 0 <= yy < g.NY and bool(g.on_iface_y[yy])
+
+    def trans(yy):
+        return int(g.trans_y[yy])
+
+    X = [x] * order
+    out = []
+    if forward:
+        if on and tr == -1:
+            f, dl = g.dhf[layer + 1], layer + 1
+        else:
+            f, dl = g.dhf[layer], layer
+        if on and tr == 1 and X[0] >= f // 3:
+            X[1] -= f // 3
+        yq = y + (order // 2) * f
+        if iface(yq) and trans(yq) == -1 and X[0] < g.NX - f // 3:
+            X[order - 1] += f // 3
+        for j in range(order):
+            Y = y + f * (j - order // 2 + 1)
+            if 0 <= Y < g.NY:
+                out.append((X[j], Y, order, j, dl))
+        return out
+    f = g.dhf[layer]
+    yq = y - (order // 2) * f
+    if iface(yq) and trans(yq) == 1 and X[1] < g.NX - f // 3:
+        X[0] += f // 3
+    if on and tr == -1 and X[1] >= f // 3:
+        X[0] -= f // 3
+    for j in range(order):
+        Y = y + f * (j - order // 2)
+        if on:
+            if j == 0 and tr == 1:
+                Y += g.dhf[layer - 1]
+            if j == 1 and tr == -1:
+                Y += g.dhf[layer + 1]
+        if 0 <= Y < g.NY:
+            out.append((X[j], Y, order, j, layer))
+    return out
+
+
+def staggered_x_operator(op: vg.Operators, orders, var_order: bool, forward: bool):
+    """DyfStaggeredX / DybStaggeredX times DT, as a CSR matrix. The rows of
+    one depth y differ only at the x edges (the shifted taps are guarded by
+    x >= f/3 and x < NX - f/3), so each (y, x class) stencil is built once."""
+    g = op.g
+    rows, cols, vals = [], [], []
+    order_rows = np.argsort(g.y, kind="stable")
+    bounds = np.searchsorted(g.y[order_rows], np.arange(g.NY + 1))
+    for y in range(g.NY):
+        r = order_rows[bounds[y]:bounds[y + 1]]
+        if not len(r):
+            continue
+        layer = int(g.layer_y[y])
+        f = g.dhf[layer] if not (g.on_iface_y[y] and g.trans_y[y] == -1 and forward) else g.dhf[layer + 1]
+        xs = g.x[r]
+        cls = (xs >= f // 3).astype(int) * 2 + (xs < g.NX - f // 3).astype(int)
+        for c in np.unique(cls):
+            rr = r[cls == c]
+            x_rep = int(g.x[rr[0]])
+            for X, Y, o, j, dl in _stag_rows(g, y, x_rep, orders, var_order, forward):
+                dx = X - x_rep
+                cols.append(g.coordinate2index(g.x[rr] + dx, Y, g.z[rr]))
+                rows.append(rr)
+                vals.append(np.full(len(rr), op._val(o, j, dl), dtype=op.dtype))
+    return op._finish(rows, cols, vals)
+
+
+def shear_average_xy(g: vg.VarGrid, mu, dtype=np.float32):
+    """calcAveragedSWaveModulus with the XY 4-point matrix
+    (Modelparameter.cpp:449-533, ModelparameterSeismic.cpp:421-432): moduli
+    below 1 raised to 1, their inverses averaged over the 4 points (2 at the
+    bottom / right edge, 1 in the corner), the average inverted, results
+    below 4 set to 0."""
+    d = np.dtype(dtype).type
+    mu = np.asarray(mu, dtype=dtype).copy()
+    mu[mu < 1] = 1
+    inv = (d(1) / mu).astype(dtype)
+    f = np.array(g.dhf, dtype=np.int64)[g.layer]
+    x2, y2 = g.x + f, g.y + f
+    okx, oky = x2 < g.NX, y2 < g.NY
+    out = np.zeros(g.N, dtype=dtype)
+    q = d(0.25)
+    h = d(0.5)
+    full = okx & oky
+    i = np.nonzero(full)[0]
+    c2 = g.coordinate2index(x2[i], g.y[i], g.z[i])
+    c3 = g.coordinate2index(g.x[i], y2[i], g.z[i])
+    c4 = g.coordinate2index(x2[i], y2[i], g.z[i])
+    s = (q * inv[i]).astype(dtype)
+    s = (s + q * inv[c2]).astype(dtype)
+    s = (s + q * inv[c3]).astype(dtype)
+    out[i] = (s + q * inv[c4]).astype(dtype)
+    b = np.nonzero(okx & ~oky)[0]          # bottom side: the point to the right
+    cb = g.coordinate2index(x2[b], g.y[b], g.z[b])
+    out[b] = (h * inv[cb] + h * inv[b]).astype(dtype)
+    rgt = np.nonzero(~okx & oky)[0]        # right side: the point below
+    cr = g.coordinate2index(g.x[rgt], y2[rgt], g.z[rgt])
+    out[rgt] = (h * inv[cr] + h * inv[rgt]).astype(dtype)
+    corner = np.nonzero(~okx & ~oky)[0]
+    out[corner] = inv[corner]
+    with np.errstate(divide="ignore"):
+        av = (d(1) / out).astype(dtype)
+    av[av < 4] = 0
+    return av
+
+
+class ElasticVarGrid2D:
+    """FD2Delastic::run on a 2-D variable grid (ForwardSolver2Delastic.cpp:
+    117-297), CPML or no damping boundary, no free surface."""
+
+    def __init__(self, g: vg.VarGrid, orders, DT: float, rho, vp, vs, cpml: dict | None,
+                 src_idx, src_type, signals, rec_idx, rec_type, dtype=np.float32, var_order: bool = True,
+                 edge: bool = True, var_grid: bool = True):
+        if g.NZ != 1:
+            raise ValueError("2-D only")
+        self.g, self.dtype = g, dtype
+        self.op = vg.Operators(g, orders, DT, False, dtype, var_order, edge, var_grid)
+        self.DyfSX = staggered_x_operator(self.op, orders, var_order, True)
+        self.DybSX = staggered_x_operator(self.op, orders, var_order, False)
+        rho = np.asarray(rho, dtype=dtype)
+        vp = np.asarray(vp, dtype=dtype)
+        vs = np.asarray(vs, dtype=dtype)
+        self.M = (rho * vp * vp).astype(dtype)
+        self.mu = (rho * vs * vs).astype(dtype)
+        self.muXY = shear_average_xy(g, self.mu, dtype)
+        self.irx, self.iry = vg.inverse_density_averages(g, rho, dtype)
+        self.cpml = cpml
+        z = lambda: np.zeros(g.N, dtype=dtype)
+        self.vx, self.vy, self.sxx, self.syy, self.sxy = z(), z(), z(), z(), z()
+        self.psi = {k: z() for k in ("sxx_x", "sxy_y", "sxy_x", "syy_y", "vxx", "vyy", "vxy", "vyx")}
+        self.src_idx = np.asarray(src_idx, np.int64)
+        self.src_type = np.asarray(src_type)
+        self.signals = np.asarray(signals, dtype=dtype)
+        self.rec_idx = np.asarray(rec_idx, np.int64)
+        self.rec_type = np.asarray(rec_type)
+
+    def _cpml(self, upd, key, ax, half):
+        if self.cpml is None:
+            return upd
+        af, bf, ah, bh = self.cpml[ax]
+        a, b = (ah, bh) if half else (af, bf)
+        ps = (self.psi[key] * b).astype(self.dtype)
+        ps = (ps + (a * upd).astype(self.dtype)).astype(self.dtype)
+        self.psi[key] = ps
+        return (upd + ps).astype(self.dtype)
+
+    def step(self, t: int):
+        op, dt, d = self.op, self.dtype, np.dtype(self.dtype).type
+        # velocities (CPML2D.cpp: sxx_x half-x, sxy_y full-y, sxy_x full-x, syy_y half-y)
+        u = self._cpml(op.Dxf @ self.sxx, "sxx_x", "x", True)
+        u2 = self._cpml(self.DybSX @ self.sxy, "sxy_y", "y", False)
+        u = ((u + u2).astype(dt) * self.irx).astype(dt)
+        self.vx = op.IStagX @ (self.vx + u).astype(dt)
+        u = self._cpml(op.Dxb @ self.sxy, "sxy_x", "x", False)
+        u2 = self._cpml(op.Dyf @ self.syy, "syy_y", "y", True)
+        u = ((u + u2).astype(dt) * self.iry).astype(dt)
+        self.vy = op.IFull @ (self.vy + u).astype(dt)
+        # normal stresses
+        vxx = self._cpml(op.Dxb @ self.vx, "vxx", "x", False)
+        vyy = self._cpml(op.Dyb @ self.vy, "vyy", "y", False)
+        u = ((vxx + vyy).astype(dt) * self.M).astype(dt)
+        sxx = (self.sxx + u).astype(dt)
+        syy = (self.syy + u).astype(dt)
+        sxx = (sxx - (d(2.0) * (vyy * self.mu).astype(dt)).astype(dt)).astype(dt)
+        syy = (syy - (d(2.0) * (vxx * self.mu).astype(dt)).astype(dt)).astype(dt)
+        self.sxx = op.IFull @ sxx
+        self.syy = op.IFull @ syy
+        # shear stress (vxy half-y, vyx half-x)
+        u = self._cpml(self.DyfSX @ self.vx, "vxy", "y", True)
+        u2 = self._cpml(op.Dxf @ self.vy, "vyx", "x", True)
+        u = ((u + u2).astype(dt) * self.muXY).astype(dt)
+        self.sxy = op.IStagX @ (self.sxy + u).astype(dt)
+        # sources and receivers (FDTD2Delastic.cpp:12-49)
+        for s in range(len(self.src_idx)):
+            i, v = self.src_idx[s], self.signals[s, t]
+            if self.src_type[s] == 1:
+                self.sxx[i] += v
+                self.syy[i] += v
+            elif self.src_type[s] == 2:
+                self.vx[i] += v
+            elif self.src_type[s] == 3:
+                self.vy[i] += v
+        out = np.zeros(len(self.rec_idx), dtype=dt)
+        for r, (i, k) in enumerate(zip(self.rec_idx, self.rec_type)):
+            if k == 1:
+                out[r] = d((self.sxx[i] + self.syy[i]) * d(0.5))
+            else:
+                out[r] = (self.vx if k == 2 else self.vy)[i]
+        return out
+
+    def run(self, nt: int) -> np.ndarray:
+        out = np.zeros((len(self.rec_idx), nt), dtype=self.dtype)
+        for t in range(nt):
+            out[:, t] = self.step(t)
+        return out

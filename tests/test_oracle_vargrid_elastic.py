@@ -1,0 +1,70 @@
+"""The 2-D elastic variable-grid oracle (oracle/vargrid_elastic.py), checker
+of a future variable-grid elastic path. The reference has no elastic
+variable-grid golden, so it is tied to the pinned regular-grid oracle: with
+one layer the two must agree to rounding, and on a 1:3:1 grid the receivers
+in the fine layers must track an all-fine regular run."""
+import numpy as np
+import pytest
+
+
+def _model(n, rng):
+    vp = rng.uniform(2400.0, 3000.0, n)
+    return 310.0 * vp ** 0.25, vp, vp / 1.8
+
+
+@pytest.mark.parametrize("boundary", [2, 0])
+def test_single_layer_elastic_vargrid_equals_regular_oracle(boundary, refcpu):
+    from oracle import vargrid as vg, vargrid_elastic as ve
+    NX, NY, DH, order, vmax = 70, 60, 5.0, 4, 3000.0
+    DT = 0.3 * DH / (vmax * np.sqrt(2.0))
+    cfg = refcpu.make_config(dimension=2, equation="elastic", NX=NX, NY=NY, DH=DH, DT=DT, T=300 * DT,
+                             spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=8, NPower=4.0,
+                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0)
+    nt = refcpu.nt_of(cfg)
+    rho, vp, vs = _model(NX * NY, np.random.default_rng(1))
+    sidx = np.array([NX // 2 + NX * (NY // 3)])
+    sig = refcpu.ricker(nt, DT, 30.0, 1.0, 0.0, np.float64)[None]
+    ridx = np.array([5 + NX * 10, NX - 6 + NX * (NY - 4), 7 + NX * 20])
+    rtype = np.array([1, 2, 3])
+    o = refcpu.Oracle(cfg, dict(rho=rho, vp=vp, vs=vs), sidx, np.array([1]), sig, ridx, rtype, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    g = vg.VarGrid(NX, NY, 1, DH, [0], [1])
+    cp = vg.cpml_coefficients(g, 8, 4.0, 20.0, vmax, DT, False, np.float64) if boundary == 2 else None
+    sim = ve.ElasticVarGrid2D(g, [order], DT, rho, vp, vs, cp, sidx, [1], sig, ridx, rtype, dtype=np.float64,
+                              var_order=False, edge=False, var_grid=False)
+    got = sim.run(nt)
+    assert np.abs(ref).max() > 0
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
+
+
+def test_elastic_vargrid_tracks_the_all_fine_grid(refcpu):
+    from oracle import vargrid as vg, vargrid_elastic as ve
+    NX, NY, DH = 122, 100, 5.0
+    vp0, vs0, rho0, fc = 3000.0, 1700.0, 2200.0, 8.0
+    DT = 0.3 * DH / (vp0 * np.sqrt(2.0) * 1.2)
+    nt = 1400
+    grid = [(0, 1, 4), (40, 3, 4), (70, 1, 4)]
+    g = vg.VarGrid(NX, NY, 1, DH, [r[0] for r in grid], [r[1] for r in grid])
+    sig = refcpu.ricker(nt, DT, fc, 1.0, 0.0, np.float64)[None]
+    sx, sy = 60, 20
+    recs = [(30, 10), (90, 25), (60, 85)]          # fine layers above and below the coarse one
+    cp = vg.cpml_coefficients(g, 12, 4.0, fc, vp0, DT, False, np.float64)
+    sidx = g.coordinate2index([sx], [sy], [0])
+    ridx = g.coordinate2index([r[0] for r in recs], [r[1] for r in recs], [0] * len(recs))
+    sim = ve.ElasticVarGrid2D(g, [r[2] for r in grid], DT, np.full(g.N, rho0), np.full(g.N, vp0), np.full(g.N, vs0),
+                              cp, sidx, [1], sig, ridx, [1] * len(recs), dtype=np.float64, edge=False)
+    a = sim.run(nt)
+    cfg = refcpu.make_config(dimension=2, equation="elastic", NX=g.NX, NY=g.NY, DH=DH, DT=DT, T=nt * DT,
+                             spatialFDorder=4, DampingBoundary=2, BoundaryWidth=12, NPower=4.0,
+                             CenterFrequencyCPML=fc, VMaxCPML=vp0, edgeOrderReduction=0)
+    n = g.NX * g.NY
+    o = refcpu.Oracle(cfg, dict(rho=np.full(n, rho0), vp=np.full(n, vp0), vs=np.full(n, vs0)),
+                      np.array([sx + g.NX * sy]), np.array([1]), sig[:, :refcpu.nt_of(cfg)],
+                      np.array([r[0] + g.NX * r[1] for r in recs]), np.ones(len(recs), int), dtype=np.float64)
+    b = o.run()
+    o.close()
+    m = min(a.shape[1], b.shape[1])
+    assert np.isfinite(a).all()
+    for k in range(len(recs)):
+        assert np.linalg.norm(a[k, :m] - b[k, :m]) / np.linalg.norm(b[k, :m]) < 0.02
