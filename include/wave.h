@@ -133,9 +133,10 @@ int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_
 /* The assembled sparse operator `op` of a variable-grid configuration
  * (host only, no GPU): 0 Dxf, 1 Dyf (DyfFreeSurface with FreeSurface=1),
  * 2 Dzf, 3 Dxb, 4 Dyb, 5 Dzb, DT folded in (Derivatives.cpp:129-1245,
- * FDTD2D.cpp:193-229), or the interface interpolation 6 Full, 7 StaggeredX,
+ * FDTD2D.cpp:193-229), the interface interpolation 6 Full, 7 StaggeredX,
  * 8 StaggeredZ (Derivatives.cpp:1252-1546; rows off the interfaces are the
- * identity). Returned as an ELL block: *width entries per row, entry k of
+ * identity), or the elastic staggered-x y-derivatives 9 DyfStaggeredX,
+ * 10 DybStaggeredX (Derivatives.cpp:852-1011, 2-D). Returned as an ELL block: *width entries per row, entry k of
  * row i at k*N + i, unused entries with weight 0. With cols == NULL only
  * *width is set; otherwise capacity must be at least width * N. */
 int wave_grid_operator(const wave_config* cfg, int op, int* width, int32_t* cols, float* vals, int64_t capacity);

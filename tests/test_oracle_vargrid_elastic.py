@@ -68,3 +68,30 @@ def test_elastic_vargrid_tracks_the_all_fine_grid(refcpu):
     assert np.isfinite(a).all()
     for k in range(len(recs)):
         assert np.linalg.norm(a[k, :m] - b[k, :m]) / np.linalg.norm(b[k, :m]) < 0.02
+
+
+@pytest.mark.parametrize("grid,NX,NY", [
+    ([(0, 1, 2), (30, 3, 6), (150, 1, 2), (200, 3, 6)], 305, 303),    # the CI grid
+    ([(0, 1, 4), (31, 3, 6), (70, 1, 4)], 122, 100),
+    ([(0, 1, 2), (30, 3, 2), (57, 9, 2)], 113, 96),
+])
+def test_library_staggered_operators_equal_the_oracle(grid, NX, NY, wave, refcpu):
+    """DyfStaggeredX / DybStaggeredX as the library assembles them on the host
+    (wave_grid_operator 9, 10) against the oracle, entry for entry."""
+    import scipy.sparse as sp
+    from oracle import vargrid as vg, vargrid_elastic as ve
+    DT = 4e-4
+    kw = dict(dimension=2, equation="elastic", NX=NX, NY=NY, NZ=1, DH=10.0, DT=DT, T=0.01, spatialFDorder=grid[0][2],
+              useVariableGrid=1, useVariableFDoperators=1, grid=grid)
+    c = wave.WaveConfig.make(**kw)
+    g = vg.VarGrid(NX, NY, 1, 10.0, [r[0] for r in grid], [r[1] for r in grid])
+    op = vg.Operators(g, [r[2] for r in grid], DT, False, np.float32, True, True, True)
+    for k, fwd in ((9, True), (10, False)):
+        cols, vals = wave.grid_operator(c, k)
+        w = cols.shape[0]
+        got = sp.csr_matrix((vals.ravel().astype(np.float64), (np.tile(np.arange(g.N), w), cols.ravel())), shape=(g.N, g.N))
+        got.eliminate_zeros()
+        want = ve.staggered_x_operator(op, [r[2] for r in grid], True, fwd).astype(np.float64).tocsr()
+        want.eliminate_zeros()
+        diff = abs(got - want)
+        assert diff.nnz == 0 or diff.max() == 0, (k, diff.max())

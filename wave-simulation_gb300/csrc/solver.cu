@@ -539,16 +539,17 @@ int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_
 
 int wave_grid_operator(const wave_config* cfg, int op, int* width, int32_t* cols, float* vals, int64_t capacity)
 {
-    if (!cfg || !width || op < 0 || op > 8) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: invalid arguments");
+    if (!cfg || !width || op < 0 || op > 10) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: invalid arguments");
+    if (op > 8 && cfg->dimension != 2) return fail(nullptr, WAVE_ERR_UNSUPPORTED, "wave_grid_operator: the staggered-x operators are built for 2-D");
     if (!(cfg->useVariableGrid || cfg->useVariableFDoperators))
         return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: not a variable-grid configuration");
     wave::VarGridHost G;
     std::string err;
-    int rc = wave::vargrid_build(*cfg, G, err);
+    int rc = wave::vargrid_build(*cfg, G, err, op > 8);
     if (rc != WAVE_OK) return fail(nullptr, rc, err);
     const long long N = G.L.N;
-    if (op < 6) {
-        const wave::EllHost* ops[6] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb};
+    if (op < 6 || op > 8) {
+        const wave::EllHost* ops[11] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb, nullptr, nullptr, nullptr, &G.DyfSX, &G.DybSX};
         const wave::EllHost& E = *ops[op];
         *width = E.W;
         if (!cols) return WAVE_OK;

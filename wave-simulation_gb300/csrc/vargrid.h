@@ -74,6 +74,7 @@ struct ClassHost {
 struct VarGridHost {
     VarGridLayout L;
     EllHost Dxf, Dxb, Dyf, Dyb, Dzf, Dzb;
+    EllHost DyfSX, DybSX;              // staggered-x y-derivatives (elastic only, 2-D)
     ClassHost cls[2];                  // velocity pass (Dxf, Dyf, Dzf), pressure pass (Dxb, Dyb, Dzb)
     InterpHost full, stagX, stagZ;
     std::vector<float> cpml[3][4];     // per axis: a_full, b_full, a_half, b_half (N each; CPML only)
@@ -89,7 +90,8 @@ struct VarGridHost {
 int vargrid_layout(const wave_config& c, VarGridLayout& L, std::string& err);
 // Every operator, interpolation, CPML coefficient and averaging partner of
 // the acoustic equations on the grid.
-int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err);
+// elastic: also the staggered-x y-derivatives of the elastic step
+int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool elastic = false);
 
 // device side of a variable-grid handle (vargrid.cu)
 struct VarGridDev {

@@ -323,6 +323,48 @@ struct Assembler {
         }
     }
 
+    // DyfStaggeredX / DybStaggeredX (:852-1011): the y-derivatives of the
+    // elastic step at x-staggered points. Near an interface the staggered
+    // point of the coarse layer sits at another x, so single taps shift by
+    // dhFactor/3; taps outside the grid are dropped (no edge rule).
+    void stag_row(int x, int y, int z, bool forward, std::vector<Tap>& out) const
+    {
+        const int layer = L.layerY[y];
+        int order = order_of(layer);
+        const int dist = L.distY[y] / L.dhf[layer];
+        if (dist == 0) order = 2;
+        else if (order > 2 * dist) order = 2 * dist;
+        const bool on = L.onIfaceY[y] != 0;
+        const int tr = L.transY[y];
+        auto iface = [&](long long yy) { return yy >= 0 && yy < L.NY && L.onIfaceY[yy]; };
+        std::vector<int> X(order, x);
+        if (forward) {
+            const bool c2f = on && tr == -1;
+            const int f = c2f ? L.dhf[layer + 1] : L.dhf[layer];
+            const int dl = c2f ? layer + 1 : layer;
+            if (on && tr == 1 && X[0] >= f / 3) X[1] -= f / 3;
+            const long long yq = y + static_cast<long long>(order / 2) * f;
+            if (iface(yq) && L.transY[yq] == -1 && X[0] < L.NX - f / 3) X[order - 1] += f / 3;
+            for (int j = 0; j < order; ++j) {
+                const int Y = y + f * (j - order / 2 + 1);
+                if (Y >= 0 && Y < L.NY) out.push_back({L.index(X[j], Y, z), value(order, j, dl)});
+            }
+            return;
+        }
+        const int f = L.dhf[layer];
+        const long long yq = y - static_cast<long long>(order / 2) * f;
+        if (iface(yq) && L.transY[yq] == 1 && X[1] < L.NX - f / 3) X[0] += f / 3;
+        if (on && tr == -1 && X[1] >= f / 3) X[0] -= f / 3;
+        for (int j = 0; j < order; ++j) {
+            int Y = y + f * (j - order / 2);
+            if (on) {
+                if (j == 0 && tr == 1) Y += L.dhf[layer - 1];
+                if (j == 1 && tr == -1) Y += L.dhf[layer + 1];
+            }
+            if (Y >= 0 && Y < L.NY) out.push_back({L.index(X[j], Y, z), value(order, j, layer)});
+        }
+    }
+
     // Dyb (:790-840)
     void dyb_row(int x, int y, int z, std::vector<Tap>& out) const
     {
@@ -565,7 +607,7 @@ void build_classes(long long N, const EllHost* const* ops, int nops, ClassHost& 
 
 } // namespace
 
-int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err)
+int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool elastic)
 {
     int rc = vargrid_layout(c, G.L, err);
     if (rc != WAVE_OK) return rc;
@@ -590,6 +632,14 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err)
     if (is3d) {
         if ((rc = build_ell(N, axis(2, false), G.Dzf, err, "Dzf")) != WAVE_OK) return rc;
         if ((rc = build_ell(N, axis(2, true), G.Dzb, err, "Dzb")) != WAVE_OK) return rc;
+    }
+    if (elastic && !is3d) {
+        if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], true, t); }, G.DyfSX, err,
+                            "DyfStaggeredX")) != WAVE_OK)
+            return rc;
+        if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], false, t); }, G.DybSX, err,
+                            "DybStaggeredX")) != WAVE_OK)
+            return rc;
     }
     if (L.varGrid) {
         std::vector<long long> rows;
