@@ -205,6 +205,12 @@ int wave_set_state(wave_handle* h, const void* in, size_t bytes, int mem);
 
 /* Query helpers. */
 int wave_get_nt(wave_handle* h, int* nt);
+/* Device memory the handle holds (wavefields, memory variables, materials,
+ * CPML slabs, operator tables, acquisition and seismogram buffers), in bytes.
+ * Replaces ForwardSolver::estimateMemory plus the wavefield/model estimates
+ * Simulation.cpp:169-174 prints (ForwardSolver.hpp:46), measured instead of
+ * estimated. */
+int wave_device_bytes(wave_handle* h, int64_t* bytes);
 int wave_get_num_receivers(wave_handle* h, int* n);
 /* Device pointer to the CUDA stream the handle launches on (cudaStream_t). */
 int wave_get_stream(wave_handle* h, void** stream);
@@ -244,7 +250,11 @@ int wave_average_shear_modulus(const float* mu, float* out, int64_t NX, int64_t 
  * value that is read was written earlier in the same call. The scratch is
  * shared by all calls on a device, so calls that overlap in time (other
  * streams, other host threads) race on it and must be serialised by the
- * caller. */
+ * caller. The scratch address is looked up once per device and kept for the
+ * life of the process: do not call this entry point on a device after a
+ * cudaDeviceReset. The C ABI cannot check the length of mu and out: both
+ * must hold NX*NY*NZ floats. A CUDA error left pending by earlier work is
+ * reported as WAVE_ERR_CUDA before anything is launched (and not cleared). */
 int wave_average_shear_modulus_noalloc(const float* mu, float* out, int64_t NX, int64_t NY, int64_t NZ, int mode, void* stream);
 
 /* Kernel path: 0 = automatic, 1 = generic kernels only (and the separate

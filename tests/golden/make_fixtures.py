@@ -7,20 +7,21 @@ by src/Tests/IntegrationTest/Test_CompareSeismogram.cpp. The reference tree is
 not available where the GPU tests run, so the files are committed here as
 fixtures. Run from the repository root:
 
-    python tests/golden/make_fixtures.py [/path/to/reference]
+    python tests/golden/make_fixtures.py /path/to/reference
 """
 import os
 import shutil
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-SRC = os.path.join(REF, "par", "ci")
 DST = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ci")
 
 KEEP_PREFIX = ("configuration_ci.", "sources_ci.", "receiver_ci.", "seismogram.")
 
 
 def main():
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py <path of the reference checkout>")
+    SRC = os.path.join(sys.argv[1], "par", "ci")
     os.makedirs(DST, exist_ok=True)
     n = 0
     for name in sorted(os.listdir(SRC)):

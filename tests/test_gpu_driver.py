@@ -143,3 +143,44 @@ def test_driver_writes_the_decomposition_snapshots(wave, tmp_path):
         assert np.all((up == F) | (up == 0)) and np.all((down == F) | (down == 0))
         assert np.all((up == F) | (down == F))
         assert np.any(up != F) and np.any(down != F)
+
+
+def test_driver_runs_a_visco_tm_parameter_file(wave, tmp_path):
+    """equationType=viscotmem through the C++ plugin mirror and the driver:
+    the relaxation times come from the tauEpsilon / tauSigmar keys
+    (ViscoTMEM.cpp:206), are passed by prepareForModelling, and the
+    seismogram equals the same run through the Python binding and the FP64
+    oracle within 1e-4."""
+    DT, nt = 4.0e-11, 500
+    edits = {"equationType": "viscotmem", "DH": "0.02", "DT": f"{DT:.3e}", "T": f"{(nt - 0.4) * DT:.6e}",
+             "spatialFDorder": "4", "DampingBoundary": "2", "BoundaryWidth": "10", "centerfrequencycpml": "1.0e8",
+             "vmaxcpml": "1.0e8", "numRelaxationMechanisms": "1", "relaxationFrequency": "1.0e8", "epsilonr": "9.0",
+             "sigma": "0.005", "mur": "1.0", "tauEpsilon": "0.1", "tauSigmar": "0.1", "SeismogramFormat": "1",
+             "useStencilMatrix": "0", "SourceFilename": "ci/sources_em", "ReceiverFilename": "ci/receiver_em",
+             "SeismogramFilename": "ci/seismogram.em"}
+    cfg, ci = _setup(tmp_path, edits)
+    (ci / "sources_em.txt").write_text("1 49 49 0 1 1 1 4.0e8 1.0 0.0\n")
+    (ci / "receiver_em.txt").write_text("69 69 0 1\n30 40 0 1\n")
+    _run(wave, cfg)
+    got = refcpu.read_mtx_array(str(ci / "seismogram.em.shot_1.ez.mtx"))
+    wc = wave.WaveConfig.from_file(str(cfg))
+    assert wc.equation == wave.EQUATIONS["viscotmem"] and wc.numRelaxationMechanisms == 1
+    n = wc.N
+    model = dict(eps_r=np.full(n, 9.0), sigma=np.full(n, 0.005), mu_r=np.ones(n), tau_eps=np.full(n, 0.1),
+                 tau_sigma=np.full(n, 0.1))
+    nt = refcpu.nt_of(wc)
+    sidx = np.array([49 + 100 * 49], np.int64)
+    sig = wave.wavelet(1, nt, wc.DT, 4.0e8, 1.0, 0.0)[None].astype(np.float64)
+    ridx = np.array([69 + 100 * 69, 30 + 100 * 40], np.int64)
+    stype, rtype = np.array([1], np.int32), np.array([1, 1], np.int32)
+    py = wave.simulate(wc, {k: v.astype(np.float32) for k, v in model.items()}, sidx, stype, sig.astype(np.float32),
+                       ridx, rtype)
+    ocfg = refcpu.WaveConfig()
+    wave.WaveConfig.copy_from(ocfg, wc)
+    o = refcpu.Oracle(ocfg, model, sidx, stype, sig, ridx, rtype, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    assert got.shape == ref.shape
+    assert np.abs(ref).max() > 0
+    assert np.linalg.norm(got - py) / np.linalg.norm(py) < 1e-6
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-4

@@ -59,3 +59,22 @@ def test_average_shear_modulus_device_pointers(wave):
     host = wave.average_shear_modulus(mu, dims, 1)
     dev = wave.average_shear_modulus(torch.from_numpy(mu).cuda(), dims, 1).cpu().numpy()
     assert np.array_equal(host, dev)
+
+
+def test_device_bytes_cover_the_state_and_grow_with_the_acquisition(wave):
+    """wave_device_bytes (ForwardSolver::estimateMemory): at least the nine
+    wavefields, the three base materials and the CPML slabs of a 3-D elastic
+    handle; receivers add their seismogram buffer."""
+    NX = NY = NZ = 48
+    cfg = wave.WaveConfig.make(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=5.0, DT=4e-4, T=0.04,
+                               spatialFDorder=4, DampingBoundary=2, BoundaryWidth=8, NPower=4.0,
+                               CenterFrequencyCPML=10.0, VMaxCPML=3500.0)
+    s = wave.Factory.Create("3D", "elastic").initForwardSolver(cfg)
+    n = NX * NY * NZ
+    b0 = s.estimateMemory()
+    assert b0 >= (9 + 3) * n * 4
+    s.prepareForModelling(dict(rho=np.full(n, 2000.0, np.float32), vp=np.full(n, 3000.0, np.float32),
+                               vs=np.full(n, 1700.0, np.float32)))
+    s.setReceivers(np.arange(1000, dtype=np.int64), np.full(1000, 2, np.int32))
+    assert s.estimateMemory() >= b0 + 1000 * s.nt * 4
+    s.close()

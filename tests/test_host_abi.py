@@ -108,3 +108,11 @@ def test_null_handle_errors(wave):
     assert L.wave_solver_step(None, 0, 1) == wave.WAVE_ERR_ARG
     assert L.wave_solver_destroy(None) == wave.WAVE_ERR_ARG
     assert L.wave_check_finite(None) == wave.WAVE_ERR_ARG
+
+
+def test_noalloc_wrapper_rejects_host_tensors_without_touching_the_gpu(wave):
+    torch = pytest.importorskip("torch")
+    t = torch.ones(64)
+    with pytest.raises(wave.WaveError) as e:
+        wave.average_shear_modulus_noalloc(t, t, (4, 4, 4), 0)
+    assert "CUDA tensor" in str(e.value)

@@ -53,11 +53,32 @@ def test_noalloc_on_a_side_stream_and_in_place(wave):
 def test_noalloc_rejects_models_above_its_scratch_and_host_memory(wave):
     torch = pytest.importorskip("torch")
     small = torch.ones(16, device="cuda")
-    with pytest.raises(wave.WaveError) as e:
-        wave.average_shear_modulus_noalloc(small, small, (256, 128, 129), 0)   # 4,227,072 > 2^22 points
-    assert "exceeds the fixed scratch" in str(e.value)
+    ptr = ctypes.c_void_p(small.data_ptr())
+    # 4,227,072 > 2^22 points: the C ABI refuses before it touches the pointers
+    rc = wave.lib().wave_average_shear_modulus_noalloc(ptr, ptr, 256, 128, 129, 0, None)
+    assert rc == wave.WAVE_ERR_ARG
+    assert b"exceeds the fixed scratch" in wave.lib().wave_last_error(None)
     host = np.ones(16, dtype=np.float32)
     rc = wave.lib().wave_average_shear_modulus_noalloc(host.ctypes.data_as(ctypes.c_void_p), host.ctypes.data_as(ctypes.c_void_p),
                                                        4, 2, 2, 0, None)
     assert rc == wave.WAVE_ERR_ARG
     assert b"device memory" in wave.lib().wave_last_error(None)
+
+
+def test_noalloc_wrapper_rejects_short_or_mistyped_tensors_before_any_launch(wave):
+    """A tensor shorter than NX*NY*NZ would be read or written past its end by
+    the kernels (the C ABI cannot see its length): the wrapper refuses it, and
+    the output tensor stays untouched."""
+    torch = pytest.importorskip("torch")
+    small = torch.ones(16, device="cuda")
+    big = torch.full((100 * 100 * 100,), 7.0, device="cuda")
+    for mu, out in ((small, big), (big, small)):
+        with pytest.raises(wave.WaveError) as e:
+            wave.average_shear_modulus_noalloc(mu, out, (100, 100, 100), 0)
+        assert "fewer than NX*NY*NZ" in str(e.value)
+    with pytest.raises(wave.WaveError):
+        wave.average_shear_modulus_noalloc(big.double(), big, (100, 100, 100), 0)
+    with pytest.raises(wave.WaveError):
+        wave.average_shear_modulus_noalloc(big.view(100, 10000)[:, :100], big, (10, 10, 100), 0)
+    torch.cuda.synchronize()
+    assert bool((big == 7.0).all())

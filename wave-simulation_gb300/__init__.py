@@ -173,6 +173,7 @@ def lib():
     L.wave_set_state.argtypes = [P, P, ctypes.c_size_t, I]
     L.wave_get_nt.argtypes = [P, CP(I)]
     L.wave_get_num_receivers.argtypes = [P, CP(I)]
+    L.wave_device_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.wave_get_stream.argtypes = [P, CP(P)]
     L.wave_get_launch_count.argtypes = [P, CP(ctypes.c_longlong)]
     L.wave_set_timing.argtypes = [P, I]
@@ -376,8 +377,15 @@ def average_shear_modulus_noalloc(mu, out, dims, mode: int, stream: int = 0):
     """wave_average_shear_modulus_noalloc: the same average with no device
     allocation (fixed 2^22-point scratch). mu and out are torch cuda float32
     tensors; the work is queued on `stream` (a raw cudaStream_t, 0 = default)."""
-    if not (hasattr(mu, "data_ptr") and hasattr(out, "data_ptr")):
-        raise WaveError(WAVE_ERR_ARG, "mu and out must be device tensors")
+    n = int(dims[0]) * int(dims[1]) * int(dims[2])
+    for name, t in (("mu", mu), ("out", out)):
+        # the C ABI cannot see a tensor's length: a short one would be read or written past its end
+        if not (hasattr(t, "data_ptr") and getattr(t, "is_cuda", False)):
+            raise WaveError(WAVE_ERR_ARG, f"{name} must be a CUDA tensor")
+        if str(t.dtype) != "torch.float32" or not t.is_contiguous():
+            raise WaveError(WAVE_ERR_ARG, f"{name} must be a contiguous float32 tensor")
+        if t.numel() < n:
+            raise WaveError(WAVE_ERR_ARG, f"{name} holds {t.numel()} values, fewer than NX*NY*NZ = {n}")
     _check(None, lib().wave_average_shear_modulus_noalloc(ctypes.c_void_p(mu.data_ptr()), ctypes.c_void_p(out.data_ptr()),
                                                           dims[0], dims[1], dims[2], mode, ctypes.c_void_p(stream or None)))
     return out
@@ -478,6 +486,12 @@ class ForwardSolver:
         c = ctypes.c_longlong()
         _check(self.h, lib().wave_get_launch_count(self.h, ctypes.byref(c)))
         return c.value
+
+    # ForwardSolver::estimateMemory (ForwardSolver.hpp:46), measured: the handle's device bytes
+    def estimateMemory(self) -> int:
+        b = ctypes.c_int64()
+        _check(self.h, lib().wave_device_bytes(self.h, ctypes.byref(b)))
+        return int(b.value)
 
     def set_kernel_path(self, path: int):
         """0 = automatic (fastest kernel per pass, timed when the model is set),

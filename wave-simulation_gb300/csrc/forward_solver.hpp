@@ -36,8 +36,9 @@ inline void check(const wave_handle* h, int rc)
 
 // Material arrays in the reference's index order (x fastest, then z, then y).
 struct Model {
-    std::vector<float> rho, vp, vs, taup, taus;   // seismic
-    std::vector<float> eps_r, sigma, mu_r;        // EM
+    std::vector<float> rho, vp, vs, taup, taus;         // seismic
+    std::vector<float> eps_r, sigma, mu_r;              // EM
+    std::vector<float> tau_eps, tau_sigma;              // visco-EM relaxation (tauEpsilon, tauSigmar)
 };
 
 // Acquisition in the reference's terms: 1-D grid indices, component types
@@ -58,8 +59,15 @@ class ForwardSolver {
     ForwardSolver(const ForwardSolver&) = delete;
     ForwardSolver& operator=(const ForwardSolver&) = delete;
 
+    // The configuration must describe the equation this solver was created
+    // for (ForwardSolverFactory.cpp:4-67 picks the class from the same keys).
     void initForwardSolver(const wave_config& cfg)
     {
+        const int dim = dim_ == "3d" ? 3 : 2;
+        if (cfg.dimension != dim || cfg.equation != equation_of(type_))
+            throw Error(WAVE_ERR_ARG, "configuration (dimension " + std::to_string(cfg.dimension) + ", equation " +
+                                          std::to_string(cfg.equation) + ") does not match the solver created as " + dim_ +
+                                          " " + type_);
         if (h_) wave_solver_destroy(h_);
         h_ = nullptr;
         check(nullptr, wave_solver_create(&cfg, &h_));
@@ -74,7 +82,7 @@ class ForwardSolver {
         const size_t n = static_cast<size_t>(npts);
         auto p = [](const std::vector<float>& v) { return v.empty() ? nullptr : v.data(); };
         if (cfg_.equation >= WAVE_EQ_TMEM)
-            check(h_, wave_set_model_em(h_, p(m.eps_r), p(m.sigma), p(m.mu_r), nullptr, nullptr, n, WAVE_MEM_HOST));
+            check(h_, wave_set_model_em(h_, p(m.eps_r), p(m.sigma), p(m.mu_r), p(m.tau_eps), p(m.tau_sigma), n, WAVE_MEM_HOST));
         else
             check(h_, wave_set_model(h_, p(m.rho), p(m.vp), p(m.vs), p(m.taup), p(m.taus), n, WAVE_MEM_HOST));
     }
@@ -112,8 +120,26 @@ class ForwardSolver {
         return true;
     }
 
+    // ForwardSolver::estimateMemory (ForwardSolver.hpp:46): the handle's device memory in MB, measured
+    double estimateMemory()
+    {
+        int64_t b = 0;
+        check(h_, wave_device_bytes(h_, &b));
+        return static_cast<double>(b) / (1024.0 * 1024.0);
+    }
+
     int NT() const { return nt_; }
     wave_handle* handle() { return h_; }
+
+    // factory key -> WAVE_EQ_* (the order of wave.h's equation enumeration)
+    static int equation_of(const std::string& type)
+    {
+        static const char* keys[] = {"acoustic", "elastic", "viscoelastic", "sh", "viscosh",
+                                     "tmem", "emem", "viscotmem", "viscoemem"};
+        for (int k = 0; k < 9; ++k)
+            if (type == keys[k]) return k;
+        return -1;
+    }
 
   private:
     std::string dim_, type_;

@@ -32,6 +32,7 @@ struct wave_handle {
     std::string err;
 
     std::vector<void*> allocs;
+    std::vector<size_t> allocBytes;   // the size of each entry of allocs
     float* f[F_COUNT] = {};
     float* r[R_COUNT][kMaxL] = {};
     float* psi[PS_COUNT] = {};
@@ -98,9 +99,11 @@ struct wave_handle {
     T* alloc(size_t count)
     {
         void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
+        const size_t bytes = count * sizeof(T) > 0 ? count * sizeof(T) : 16;
+        cudaError_t e = cudaMalloc(&p, bytes);
         if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
         allocs.push_back(p);
+        allocBytes.push_back(bytes);
         return static_cast<T*>(p);
     }
     // A device buffer of at least `need` elements in slot p (capacity cap):
@@ -111,9 +114,10 @@ struct wave_handle {
     {
         if (p && cap >= need) return p;
         if (p) {
-            for (auto it = allocs.begin(); it != allocs.end(); ++it)
-                if (*it == static_cast<void*>(p)) {
-                    allocs.erase(it);
+            for (size_t k = 0; k < allocs.size(); ++k)
+                if (allocs[k] == static_cast<void*>(p)) {
+                    allocs.erase(allocs.begin() + k);
+                    allocBytes.erase(allocBytes.begin() + k);
                     break;
                 }
             cudaFree(p);

@@ -69,7 +69,9 @@ std::mutex g_scratch_mutex;
 float* g_scratch_ptr[kMaxDevices] = {};
 
 // One-time set-up per device (with that device current): the scratch array's
-// device address.
+// device address. The address is cached for the life of the process, so this
+// entry point must not be used on a device after cudaDeviceReset (the module
+// is reloaded there and the array may move).
 cudaError_t scratch_for_current_device(float** ptr)
 {
     int dev = 0;
@@ -87,14 +89,18 @@ cudaError_t scratch_for_current_device(float** ptr)
     return cudaSuccess;
 }
 
-bool on_device(const void* p)
+// Device memory of device `dev`, or managed memory. Called only when no CUDA
+// error is pending (checked at entry), so clearing the query's own error for
+// an unknown pointer drops nothing of the caller's.
+bool on_device(const void* p, int dev)
 {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();   // the query's error for an unknown pointer is not sticky: clear it
+        cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 } // namespace
@@ -112,7 +118,15 @@ extern "C" int wave_average_shear_modulus_noalloc(const float* mu, float* out, i
                          std::to_string(kNoAllocMaxPoints) + " points; use wave_average_shear_modulus");
         return WAVE_ERR_ARG;
     }
-    if (!on_device(mu) || !on_device(out)) {
+    // an error left pending by an earlier call would otherwise be reported (and cleared) as this call's
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        set_global_error(std::string("wave_average_shear_modulus_noalloc: a CUDA error is pending from earlier work (") +
+                         cudaGetErrorString(pending) + "); nothing was launched");
+        return WAVE_ERR_CUDA;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || !on_device(mu, dev) || !on_device(out, dev)) {
         set_global_error("wave_average_shear_modulus_noalloc: mu and out must be device memory of the current device");
         return WAVE_ERR_ARG;
     }

@@ -1152,6 +1152,15 @@ int wave_get_nt(wave_handle* h, int* nt)
     return WAVE_OK;
 }
 
+int wave_device_bytes(wave_handle* h, int64_t* bytes)
+{
+    if (!h || !bytes) return fail(h, WAVE_ERR_ARG, "wave_device_bytes: null argument");
+    size_t b = 0;
+    for (size_t x : h->allocBytes) b += x;
+    *bytes = static_cast<int64_t>(b);
+    return WAVE_OK;
+}
+
 int wave_get_num_receivers(wave_handle* h, int* n)
 {
     if (!h || !n) return fail(h, WAVE_ERR_ARG, "wave_get_num_receivers: null argument");

@@ -143,18 +143,30 @@ int main(int argc, char** argv)
             if (key<int>(keys, "FileFormat", 1) != 1)
                 throw wave::gpu::Error(WAVE_ERR_UNSUPPORTED, "model files: only FileFormat=1 (MatrixMarket) is readable here; lmf/frv are LAMA formats");
             auto rd = [&](const char* p) { return onto_grid(read_mtx_vector(dir + "/../" + mf + "." + p + ".mtx", nRegular)); };
-            if (em) { model.eps_r = rd("epsilonr"); model.sigma = rd("sigma"); model.mu_r = rd("mur"); }
+            if (em) {
+                model.eps_r = rd("epsilonr"); model.sigma = rd("sigma"); model.mu_r = rd("mur");
+                // ViscoTMEM.cpp:320-329 / ViscoEMEM: the relaxation times' files
+                if (cfg.equation == WAVE_EQ_VISCOTMEM || cfg.equation == WAVE_EQ_VISCOEMEM) {
+                    model.tau_sigma = rd("tauSigmar");
+                    model.tau_eps = rd("tauEpsilon");
+                }
+            }
             else {
                 model.rho = rd("density");
                 if (cfg.equation != WAVE_EQ_SH && cfg.equation != WAVE_EQ_VISCOSH) model.vp = rd("vp");
                 if (cfg.equation != WAVE_EQ_ACOUSTIC) model.vs = rd("vs");
-                if (cfg.equation == WAVE_EQ_VISCOELASTIC) { model.taup = rd("tauP"); model.taus = rd("tauS"); }
+                if (cfg.equation == WAVE_EQ_VISCOELASTIC) model.taup = rd("tauP");
                 if (cfg.equation == WAVE_EQ_VISCOELASTIC || cfg.equation == WAVE_EQ_VISCOSH) model.taus = rd("tauS");
             }
         } else if (em) {
             model.eps_r.assign(n, key<float>(keys, "epsilonr", 1.0f));
             model.sigma.assign(n, key<float>(keys, "sigma", 0.0f));
             model.mu_r.assign(n, key<float>(keys, "mur", 1.0f));
+            // ViscoTMEM.cpp:206 / ViscoEMEM.cpp:192: homogeneous relaxation times from the keys
+            if (cfg.equation == WAVE_EQ_VISCOTMEM || cfg.equation == WAVE_EQ_VISCOEMEM) {
+                model.tau_sigma.assign(n, key<float>(keys, "tauSigmar", 0.0f));
+                model.tau_eps.assign(n, key<float>(keys, "tauEpsilon", 0.0f));
+            }
         } else {
             model.rho.assign(n, key<float>(keys, "rho", 1000.0f));
             model.vp.assign(n, key<float>(keys, "velocityP", 0.0f));
