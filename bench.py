@@ -82,11 +82,18 @@ def make_model():
     return dict(rho=rho, vp=vp, vs=vs)
 
 
-def make_acquisition(nt, dt):
-    from oracle.refcpu import ricker  # plain host formula for the synthetic source signal
-    sidx = np.array([NX // 2 + NX * (NZ // 2 + NZ * 20)], dtype=np.int64)
+def make_acquisition(nt, dt, wavelet=None, shot=0):
+    """Explosive source of shot `shot` (shots step 16 cells along x) and the
+    2,000 three-component surface receivers. `wavelet(shape, nt, dt, fc, amp,
+    tshift)` makes the source signal: the library's wave_wavelet on the GPU
+    arm, the oracle's restatement on the CPU reference arm."""
+    if wavelet is None:
+        from oracle.refcpu import ricker
+        wavelet = lambda shape, n, d, fc, amp, ts: ricker(n, d, fc, amp, ts, np.float32)
+    sx = (NX // 2 + 16 * shot) % NX
+    sidx = np.array([sx + NX * (NZ // 2 + NZ * 20)], dtype=np.int64)
     stype = np.array([1], dtype=np.int32)
-    sig = ricker(nt, dt, 10.0, 1.0, 0.0, np.float32)[None, :]
+    sig = np.asarray(wavelet(1, nt, dt, 10.0, 1.0, 0.0), dtype=np.float32)[None, :]
     xs = (30 + 5 * np.arange(40)) % NX
     zs = (30 + 4 * np.arange(50)) % NZ
     X, Z = np.meshgrid(xs, zs, indexing="ij")
@@ -197,11 +204,15 @@ def whole_job_rate(units_per_rank: float, seconds_max: float, world: int) -> flo
     return world * units_per_rank / seconds_max
 
 
-def cpu_sample(steps: int, warm: int, budget_s: float = 60.0):
+FIELDS_3D = ("vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz")
+
+
+def cpu_sample(steps: int, warm: int, budget_s: float = 60.0, fields_out: dict | None = None):
     """The reference formulation (oracle refcpu<float>, CSR operators and one
     pass per vector operation) on the full grid, all host threads, for at most
     `steps` steps or `budget_s` seconds of stepping; returns
-    (Gpt/s, cores, seconds, steps timed)."""
+    (Gpt/s, cores, seconds, steps timed). With `fields_out`, the nine
+    wavefields after the last step are stored there (float32)."""
     from oracle import refcpu
     cores = os.cpu_count() or 1
     refcpu.set_threads(cores)
@@ -215,6 +226,9 @@ def cpu_sample(steps: int, warm: int, budget_s: float = 60.0):
     while done < steps and sec < budget_s:
         sec += o.step(warm + done, warm + done + 1, copy_state=True)
         done += 1
+    if fields_out is not None:
+        for f in FIELDS_3D:
+            fields_out[f] = o.field(f).astype(np.float32)
     o.close()
     return N * done / sec / 1e9, cores, sec, done
 
@@ -238,6 +252,44 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def step_roofline(vel_ms, str_ms, passes):
+    """The 3-D elastic step against the HBM roofline. `achieved` is the step's
+    algorithmic bytes (84 B per grid point + 8 B per CPML psi array and slab
+    point: 1.724 GB at 256^3) over the CUDA-event time of the step kernels, so
+    a kernel pair that moves more than the single-sweep figure reads lower;
+    `traffic` is the step kernels' measured DRAM bytes (ncu) per step."""
+    peak, peak_kind = load_peaks()
+    psi_b = psi_bytes_per_kernel()
+    step_alg = ALG_BYTES_PER_PT * N + 2 * psi_b
+    step_ms = vel_ms + str_ms
+    achieved = step_alg / (step_ms * 1e-3) / 1e9
+
+    def kname(pass_bit, pair_bit, base):
+        if passes & pair_bit:
+            return f"el3dp_{base}<4> (TMA streaming, two points per thread)"
+        return f"el3d_{base}<4> (TMA streaming)" if passes & pass_bit else f"elastic_{base[0]}<4> (generic)"
+    names = {"velocity": kname(1, 4, "vel"), "stress": kname(2, 8, "str")}
+    traffic = load_traffic() or {}
+    t_v, t_s = (traffic.get(names[k].split("<")[0]) for k in ("velocity", "stress"))
+    step_traffic = (t_v + t_s) if (t_v and t_s and NX == 256) else None
+    vel_b = VEL_BYTES_PER_PT * N + psi_b
+    str_b = STR_BYTES_PER_PT * N + psi_b
+    return {"bound": "hbm", "kernel": f"{names['velocity'].split(' ')[0]} + {names['stress'].split(' ')[0]} (one time step)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": f"{peak_kind} copy bandwidth (burst)", "traffic": step_traffic,
+            "traffic_note": "DRAM bytes per step: ncu dram__bytes_read.sum + dram__bytes_write.sum of the step kernels "
+                            "at 256^3 (profiles/el3dp_*_streaming_256.md)",
+            "alg_bytes_per_step": step_alg, "alg_bytes_note": "84 B/pt (9 state arrays read+written, 3 base materials "
+                                                              "read) + 8 B per psi array per slab point",
+            "step_ms": step_ms,
+            "per_pass": {"velocity": {"kernel": names["velocity"], "ms": vel_ms, "alg_bytes": vel_b,
+                                      "frac_of_own_bytes": vel_b / (vel_ms * 1e-3) / 1e9 / peak,
+                                      "traffic": t_v if NX == 256 else None},
+                         "stress": {"kernel": names["stress"], "ms": str_ms, "alg_bytes": str_b,
+                                    "frac_of_own_bytes": str_b / (str_ms * 1e-3) / 1e9 / peak,
+                                    "traffic": t_s if NX == 256 else None}}}
+
+
 def run_gpu(args):
     import torch
 
@@ -251,7 +303,8 @@ def run_gpu(args):
     cfg = wave.WaveConfig.make(**CONFIG_KW)
     model = make_model()
     s = wave.Factory.Create("3D", "elastic").initForwardSolver(cfg)
-    sidx, stype, sig, ridx, rtype = make_acquisition(s.nt, cfg.DT)
+    # one shot per rank (disjoint shot lists, no data-path collective)
+    sidx, stype, sig, ridx, rtype = make_acquisition(s.nt, cfg.DT, wave.wavelet, shot=rank)
     dev_model = {k: torch.from_numpy(v).cuda() for k, v in model.items()}
     s.prepareForModelling(dev_model)
     if args.kernel_path:
@@ -290,69 +343,65 @@ def run_gpu(args):
     finite = s.check_finite()
     s.close()
 
-    # end-to-end through the public API with host buffers: model upload and
-    # preparation, sources/receivers, K steps, seismogram read-back
+    # end to end through the public API with host buffers, one whole shot:
+    # handle creation, model upload and preparation, acquisition, every time
+    # step of the shot, seismogram read-back
     e2e = None
-    if args.no_e2e:
-        s2 = None
-    else:
-        s2 = wave.Factory.Create("3D", "elastic").initForwardSolver(cfg)
-    if s2 is not None:
+    if not args.no_e2e:
+        e2e_steps = args.e2e_steps or s.nt
         barrier()
         t0 = time.perf_counter()
+        s2 = wave.Factory.Create("3D", "elastic").initForwardSolver(cfg)
         s2.prepareForModelling(model)
         s2.setSources(sidx, stype, sig)
         s2.setReceivers(ridx, rtype)
-        s2.run(0, args.steps)
+        s2.run(0, e2e_steps)
         seis = s2.seismograms()
         t1 = time.perf_counter()
         s2.close()
         h2d = sum(v.nbytes for v in model.values()) + sig.nbytes + sidx.nbytes + stype.nbytes + ridx.nbytes + rtype.nbytes
         d2h = seis.nbytes
         e2e_s = max_over_ranks(t1 - t0, world)
-        e2e = {"value": whole_job_rate(N * args.steps, e2e_s, world) / 1e9, "unit": UNIT,
-               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps}
+        e2e = {"value": whole_job_rate(N * e2e_steps, e2e_s, world) / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps, "steps": e2e_steps,
+               "what": "create + model upload/preparation + acquisition + all steps of one shot + seismogram read-back"}
 
-    peak, peak_kind = load_peaks()
-    psi_b = psi_bytes_per_kernel()
-    str_bytes = STR_BYTES_PER_PT * N + psi_b
-    vel_bytes = VEL_BYTES_PER_PT * N + psi_b
-    dominant = "stress" if str_ms >= vel_ms else "velocity"
-    dom_bytes, dom_ms = (str_bytes, str_ms) if dominant == "stress" else (vel_bytes, vel_ms)
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = load_traffic()
-    step_alg = ALG_BYTES_PER_PT * N + 2 * psi_b
-    def kname(pass_bit, pair_bit, base):
-        if passes & pair_bit:
-            return f"el3dp_{base}<4> (TMA streaming, two points per thread)"
-        return f"el3d_{base}<4> (TMA streaming)" if passes & pass_bit else f"elastic_{base[0]}<4> (generic)"
-    names = {"velocity": kname(1, 4, "vel"), "stress": kname(2, 8, "str")}
-    roof = {"bound": "hbm", "kernel": names[dominant], "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} copy bandwidth (burst)",
-            "traffic": (traffic or {}).get(names[dominant].split("<")[0]),
-            "traffic_note": (traffic or {}).get("notes", {}).get(names[dominant].split("<")[0]),
-            "alg_bytes_per_launch": dom_bytes,
-            "step_pair": {"alg_bytes_per_step": step_alg, "ms": vel_ms + str_ms,
-                          "achieved": step_alg / ((vel_ms + str_ms) * 1e-3) / 1e9,
-                          "frac": step_alg / ((vel_ms + str_ms) * 1e-3) / 1e9 / peak},
-            "kernel_ms": {"velocity": vel_ms, "stress": str_ms, "samples": nsamp}, "kernels": names}
+    roof = step_roofline(vel_ms, str_ms, passes)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered model, Ricker source)",
         "config": {"workload": WORKLOAD if NX == 256 else f"3-D elastic {NX}^3 (profiling size)", "grid": [NX, NY, NZ],
                    "order": 8, "l2": "inputs larger than L2 (state 9 x N x 4 B)",
-                   "parallelism": f"shot replicas x{world}" if world > 1 else "1 GPU"},
+                   "parallelism": f"one shot per rank x{world}" if world > 1 else "1 GPU"},
         "roofline": roof, "e2e": e2e, "gpu_launches": launches, "finite": finite,
     }
     clocks = clk.summary()
     if clocks:
         line["clocks"] = clocks
     if rank == 0 and world == 1 and not args.no_cpu:
-        gpts, cores, sec, done = cpu_sample(args.cpu_steps, 1, budget_s=30.0)
+        ref_fields = {}
+        gpts, cores, sec, done = cpu_sample(args.cpu_steps, 1, budget_s=30.0, fields_out=ref_fields)
         line["cpu_baseline"] = {"value": gpts, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"1 warm-up + {done} timed steps of the full 256^3 grid "
                                           f"with the CPU oracle (reference formulation, FP32), {sec:.1f} s"}
+        # parity on this workload: the same steps from rest on the GPU (same inputs), all nine wavefields
+        s3 = wave.Factory.Create("3D", "elastic").initForwardSolver(cfg)
+        s3.prepareForModelling(dev_model)
+        acq = make_acquisition(s3.nt, cfg.DT)
+        s3.setSources(*acq[:3])
+        s3.setReceivers(*acq[3:])
+        s3.run(0, 1 + done)
+        num = den = 0.0
+        for f in FIELDS_3D:
+            a, b = s3.field(f).astype(np.float64), ref_fields[f].astype(np.float64)
+            num += float(np.sum((a - b) ** 2))
+            den += float(np.sum(b ** 2))
+        s3.close()
+        line["parity"] = {"rel_l2": (num / den) ** 0.5 if den > 0 else None, "steps": 1 + done,
+                          "vs": "CPU oracle refcpu<float> (the reference formulation in FP32)",
+                          "what": "all nine wavefields of the full 256^3 grid after the same steps from rest; "
+                                  "the tests check the FP64 oracle on this configuration"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -434,6 +483,12 @@ def _oracle_rate(cfg_kw, model, acq, steps, budget_s=20.0):
     return n * done / sec / 1e9, cores, done, sec
 
 
+def _ricker(nt, dt, fc):
+    """Ricker source signal from the library's own wave_wavelet (shape 1)."""
+    import __graft_entry__ as g
+    return g.load_package().wavelet(1, nt, dt, fc, 1.0, 0.0)
+
+
 # ---- config 1: 2-D acoustic 400 x 200 -------------------------------------
 AC2_KW = dict(dimension=2, equation="acoustic", NX=400, NY=200, NZ=1, DH=1.0, DT=2e-4, T=0.4, spatialFDorder=4,
               FreeSurface=0, DampingBoundary=2, BoundaryWidth=20, NPower=4.0, CenterFrequencyCPML=15.0,
@@ -448,9 +503,8 @@ def ac2_model():
 
 
 def ac2_acq(nt, dt):
-    from oracle.refcpu import ricker
     sidx = np.array([200 + 400 * 20], np.int64)
-    sig = ricker(nt, dt, 15.0, 1.0, 0.0, np.float32)[None, :]
+    sig = _ricker(nt, dt, 15.0)[None, :]
     ridx = (2 + 4 * np.arange(100) + 400 * 10).astype(np.int64)
     return sidx, np.array([1], np.int32), sig, ridx, np.ones(100, np.int32)
 
@@ -656,9 +710,8 @@ def vi3_model(NX, NY, NZ, device):
 
 
 def vi3_acq(NX, NY, NZ, nt, dt):
-    from oracle.refcpu import ricker
     sidx = np.array([NX // 2 + NX * (NZ // 2 + NZ * min(40, NY - 1))], np.int64)
-    sig = ricker(nt, dt, 10.0, 1.0, 0.0, np.float32)[None, :]
+    sig = _ricker(nt, dt, 10.0)[None, :]
     xs = (40 + 7 * np.arange(64)) % NX
     zs = (40 + 7 * np.arange(64)) % NZ
     X, Z = np.meshgrid(xs, zs, indexing="ij")
@@ -759,9 +812,8 @@ def tm_cfg_kw(nx, ny):
 
 
 def tm_acq(nx, nt):
-    from oracle.refcpu import ricker
     sidx = np.array([30 + nx * 25], np.int64)
-    sig = ricker(nt, TM_DT, 2e8, 1.0, 0.0, np.float32)[None, :]
+    sig = _ricker(nt, TM_DT, 2e8)[None, :]
     ridx = (40 + 4 * np.arange(60) + nx * 25).astype(np.int64)
     return sidx, np.array([1], np.int32), sig, ridx, np.ones(60, np.int32)
 
@@ -862,9 +914,8 @@ def fwi_models(NX, NY):
 
 
 def fwi_acq(NX, k, nt, dt):
-    from oracle.refcpu import ricker
     sidx = np.array([30 + 17 * k + NX * 10], np.int64)
-    sig = ricker(nt, dt, 10.0, 1.0, 0.0, np.float32)[None, :]
+    sig = _ricker(nt, dt, 10.0)[None, :]
     xs = 30 + 4 * np.arange(136)
     ridx = np.concatenate([xs + NX * 10, xs + NX * 10]).astype(np.int64)
     rtype = np.concatenate([np.full(136, 2), np.full(136, 3)]).astype(np.int32)
@@ -891,39 +942,50 @@ def run_fwi2d(args, wave):
         acqs.append(acq)
         nt = s.nt
         s.close()
-    # plain: one shot-gradient at a time through the single-handle entry point
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    plain_grad = None
-    misfit_plain = 0.0
-    for k in range(nshots):
-        s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
-        s.prepareForModelling(start)
-        s.setSources(*acqs[k][:3])
-        s.setReceivers(*acqs[k][3:])
-        J, gvp, gvs, grho = s.adjoint_gradient(dobs[k], checkpoint_every=K)
-        misfit_plain += J
-        plain_grad = gvp.astype(np.float64) if plain_grad is None else plain_grad + gvp
-        s.close()
-    plain_s = time.perf_counter() - t0
-    # batched: all shots in every launch, gradients summed on the device
-    b = wave.Batch([cfg] * nshots)
-    for shot, acq in zip(b.shots, acqs):
-        shot.prepareForModelling(start)
-        shot.setSources(*acq[:3])
-        shot.setReceivers(*acq[3:])
-    b.run(0, 3)                                            # warm-up launches
-    l0 = b.launch_count()
-    with ClockSampler(torch.cuda.current_device()) as clk:
+    # Both arms time the same work from the same starting point: handle
+    # creation, model upload and preparation, acquisition, forward +
+    # checkpointed adjoint of every shot, gradients back on the host.
+    def plain_once():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        grad, J = None, 0.0
+        for k in range(nshots):
+            s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
+            s.prepareForModelling(start)
+            s.setSources(*acqs[k][:3])
+            s.setReceivers(*acqs[k][3:])
+            Jk, gvp, gvs, grho = s.adjoint_gradient(dobs[k], checkpoint_every=K)
+            J += Jk
+            grad = gvp.astype(np.float64) if grad is None else grad + gvp
+            s.close()
+        return time.perf_counter() - t0, J, grad
+
+    def batched_once(count=False):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b = wave.Batch([cfg] * nshots)
+        for shot, acq in zip(b.shots, acqs):
+            shot.prepareForModelling(start)
+            shot.setSources(*acq[:3])
+            shot.setReceivers(*acq[3:])
+        l0 = b.launch_count()
         mis, bvp, bvs, brho = b.adjoint_gradient(dobs, checkpoint_every=K, sum_shots=True)
         torch.cuda.synchronize()
-        batch_s = time.perf_counter() - t0
+        sec = time.perf_counter() - t0
+        nl = b.launch_count() - l0
+        b.close()
+        return sec, mis, bvp, nl
+
+    plain_runs = [plain_once() for _ in range(args.repeats)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        batch_runs = [batched_once() for _ in range(args.repeats)]
+    plain_s = statistics.median(r[0] for r in plain_runs)
+    batch_s = statistics.median(r[0] for r in batch_runs)
+    misfit_plain, plain_grad = plain_runs[-1][1], plain_runs[-1][2]
+    mis, bvp = batch_runs[-1][1], batch_runs[-1][2]
     # forward steps counted by the batch plus the adjoint driver's own launches (per step: view copy,
     # residual injection, three adjoint passes; per segment: two state copies; per shot: residual, chain rule)
-    launches = (b.launch_count() - l0) + 5 * nt + 2 * ((nt + K - 1) // K) + 2 * nshots
-    b.close()
+    launches = batch_runs[-1][3] + 5 * nt + 2 * ((nt + K - 1) // K) + 2 * nshots
     rel = float(np.linalg.norm(bvp - plain_grad) / np.linalg.norm(plain_grad))
     value = nshots / batch_s
     plain = nshots / plain_s
@@ -942,6 +1004,9 @@ def run_fwi2d(args, wave):
           {"value": value, "unit": "shot-gradients/s", "h2d_bytes_per_step": h2d / nshots, "d2h_bytes_per_step": 3 * n * 4},
           launches, clk.summary(), None,
           {"unit": "shot-gradients/s", "plain_value": plain, "batched_over_plain": value / plain,
+           "repeats": args.repeats, "timing": "median of the repeats; both arms time handle creation, model, "
+                                             "acquisition, forward + adjoint and the gradient read-back",
+           "batched_s_all": [r[0] for r in batch_runs], "plain_s_all": [r[0] for r in plain_runs],
            "misfit": float(sum(mis)), "misfit_plain": misfit_plain, "batched_vs_plain_grad_rel_l2": rel})
 
 
@@ -954,9 +1019,11 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=40, help="full-grid CPU oracle steps for cpu_baseline (at most 30 s)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="time steps of the end-to-end shot (0 = the whole shot, NT)")
     ap.add_argument("--grid", type=int, default=256, help="cube edge (profiling captures use a smaller cube)")
     ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch", "fwi2d", "vargrid3d"])
     ap.add_argument("--shots", type=int, default=128, help="shots of the batched EM workload")
+    ap.add_argument("--repeats", type=int, default=3, help="repeats of the FWI-gradient arms (median reported)")
     ap.add_argument("--kernel-path", type=int, default=0, choices=[0, 1, 2, 3],
                     help="3-D elastic kernels: 0 automatic, 1 generic, 2 one-point streaming, 3 two-point streaming (profiling)")
     args = ap.parse_args()

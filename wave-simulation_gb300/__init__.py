@@ -36,7 +36,7 @@ ABI_SYMBOLS = (
     "wave_set_model", "wave_set_model_em", "wave_set_sources", "wave_set_receivers",
     "wave_solver_step", "wave_solver_reset", "wave_get_seismograms", "wave_check_finite",
     "wave_get_state_size", "wave_get_state", "wave_set_state", "wave_get_nt",
-    "wave_get_num_receivers", "wave_get_stream", "wave_get_launch_count", "wave_set_timing",
+    "wave_get_num_receivers", "wave_device_bytes", "wave_get_stream", "wave_get_launch_count", "wave_set_timing",
     "wave_get_kernel_times", "wave_last_error", "wave_wavelet", "wave_set_kernel_path",
     "wave_get_kernel_path", "wave_average_shear_modulus", "wave_batch_create", "wave_batch_destroy",
     "wave_batch_shot", "wave_batch_step", "wave_batch_get_stream", "wave_batch_get_launch_count",
