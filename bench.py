@@ -924,11 +924,18 @@ def fwi_acq(NX, k, nt, dt):
 
 def run_fwi2d(args, wave):
     import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     nshots = min(args.shots, 32)
     cfg = wave.WaveConfig.make(**FWI_KW)
     NX, NY = 600, 300
     true, start = fwi_models(NX, NY)
     K = 50
+    if world > 1:
+        return run_fwi2d_shot_domains(args, wave, cfg, nshots, true, start, K, world, rank)
     # observed data: the FP32 forward on the true model, one shot at a time
     dobs, acqs = [], []
     for k in range(nshots):
@@ -1008,6 +1015,43 @@ def run_fwi2d(args, wave):
                                              "acquisition, forward + adjoint and the gradient read-back",
            "batched_s_all": [r[0] for r in batch_runs], "plain_s_all": [r[0] for r in plain_runs],
            "misfit": float(sum(mis)), "misfit_plain": misfit_plain, "batched_vs_plain_grad_rel_l2": rel})
+
+
+def run_fwi2d_shot_domains(args, wave, cfg, nshots, true, start, K, world, rank):
+    """--gpus N: the 32 shots split into contiguous blocks over the ranks (one
+    GPU each), each block one batch, the gradients summed over the ranks
+    (the only collective); rate = all shots over the slowest rank's time."""
+    import torch
+    import torch.distributed as dist
+    lb, ub = wave.shot_range(nshots, rank, world)
+    dobs, acqs = [None] * nshots, [None] * nshots
+    for k in range(lb, ub):
+        s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
+        acqs[k] = fwi_acq(600, k, s.nt, cfg.DT)
+        s.prepareForModelling(true)
+        s.setSources(*acqs[k][:3])
+        s.setReceivers(*acqs[k][3:])
+        s.run(0, s.nt)
+        dobs[k] = s.seismograms()
+        s.close()
+    times = []
+    for _ in range(args.repeats):
+        torch.cuda.synchronize()
+        dist.barrier()
+        t0 = time.perf_counter()
+        mis, gvp, gvs, grho = wave.fwi_gradient_shot_domains(cfg, start, acqs, dobs, checkpoint_every=K)
+        torch.cuda.synchronize()
+        times.append(max_over_ranks(time.perf_counter() - t0, world))
+    sec = statistics.median(times)
+    if rank == 0:
+        n = 600 * 300
+        cfgd = {"workload": f"2-D elastic FWI gradient 600x300 order 4, {nshots} shots over {world} ranks",
+                "shots": nshots, "parallelism": f"shot domains x{world} (gradient sum over ranks)"}
+        _line("shot-gradients/s", nshots / sec, nshots, 0, sec * 1e3 / nshots, cfgd, None,
+              {"value": nshots / sec, "unit": "shot-gradients/s", "h2d_bytes_per_step": None,
+               "d2h_bytes_per_step": 3 * n * 4}, None, None, None,
+              {"unit": "shot-gradients/s", "n_gpus": world, "misfit": mis, "repeats": args.repeats})
+    dist.destroy_process_group()
 
 
 def main():

@@ -689,3 +689,86 @@ def simulate(config: WaveConfig, model: dict, src_idx, src_type, signals, rec_id
         return out
     finally:
         s.close()
+
+
+# ---------------------------------------------------------------------------
+# Shot domains across processes (one process per GPU)
+# ---------------------------------------------------------------------------
+def shot_range(num_shots: int, domain: int, num_domains: int) -> tuple:
+    """Shots [lb, ub) of shot domain `domain` out of `num_domains`: contiguous
+    blocks of ceil(num_shots / num_domains) shots, the block distribution
+    the reference builds over its inter-shot communicator
+    (Simulation.cpp:339-345, blockDistribution(numshots, commInterShot)); the
+    last domains may get fewer shots or none."""
+    if num_shots < 0 or num_domains < 1 or not 0 <= domain < num_domains:
+        raise WaveError(WAVE_ERR_ARG, "shot_range: invalid shot or domain count")
+    block = (num_shots + num_domains - 1) // num_domains
+    lb = min(domain * block, num_shots)
+    return lb, min(lb + block, num_shots)
+
+
+def sum_over_shot_domains(local, group=None):
+    """Sum of a per-process partial result (seismograms, gradients, misfits)
+    over all processes of the torch.distributed group, as the reference sums
+    its seismograms over the inter-shot communicator (SeismogramHandler.cpp:
+    479). `local` is a numpy array (reduced through a CPU tensor: gloo) or a
+    torch tensor (reduced in place on its device: NCCL for CUDA tensors).
+    Without an initialised process group the input comes back unchanged."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size(group) == 1:
+        return local
+    if isinstance(local, torch.Tensor):
+        dist.all_reduce(local, op=dist.ReduceOp.SUM, group=group)
+        return local
+    t = torch.from_numpy(np.ascontiguousarray(local)).clone()
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return t.numpy()
+
+
+def run_shot_domains(num_shots: int, compute, group=None):
+    """Runs this process's block of shots and sums the result over all
+    processes: compute(lb, ub) returns the partial result of shots [lb, ub)
+    (a numpy array or a tuple of them, zeros for an empty block), and every
+    process receives the sums. One process per GPU; no collective runs inside
+    `compute`, only the final sum."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        rank, world = dist.get_rank(group), dist.get_world_size(group)
+    else:
+        rank, world = 0, 1
+    lb, ub = shot_range(num_shots, rank, world)
+    part = compute(lb, ub)
+    if isinstance(part, tuple):
+        return tuple(sum_over_shot_domains(p, group) for p in part)
+    return sum_over_shot_domains(part, group)
+
+
+def fwi_gradient_shot_domains(config: WaveConfig, model: dict, acquisitions, dobs, checkpoint_every: int = 50,
+                              group=None):
+    """Summed misfit and vp / vs / rho gradients over all shots, the shots
+    split into contiguous blocks over the processes of the torch.distributed
+    group: each process runs its block as one batch on its own GPU
+    (wave_batch_adjoint_gradient, gradients summed on the device), then one
+    sum over the processes. acquisitions[k] = (src_idx, src_type, signals,
+    rec_idx, rec_type) and dobs[k] are shot k's."""
+    n = config.N
+
+    def compute(lb, ub):
+        if ub <= lb:
+            z = np.zeros(n, np.float64)
+            return np.zeros(1, np.float64), z, z.copy(), z.copy()
+        b = Batch([config] * (ub - lb))
+        try:
+            for shot, k in zip(b.shots, range(lb, ub)):
+                shot.prepareForModelling(model)
+                shot.setSources(*acquisitions[k][:3])
+                shot.setReceivers(*acquisitions[k][3:])
+            mis, gvp, gvs, grho = b.adjoint_gradient(list(dobs[lb:ub]), checkpoint_every=checkpoint_every, sum_shots=True)
+        finally:
+            b.close()
+        f = lambda a: np.asarray(a, np.float64)
+        return np.array([float(np.sum(mis))]), f(gvp), f(gvs), f(grho)
+
+    mis, gvp, gvs, grho = run_shot_domains(len(acquisitions), compute, group)
+    return float(mis[0]), gvp, gvs, grho
