@@ -1,0 +1,327 @@
+// adjoint_impl.hpp — TEST INFRASTRUCTURE ONLY (the oracle).
+//
+// Discrete adjoint of the oracle's 2-D elastic step (Sim<T>::stepElastic,
+// restating FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297, with CPML
+// CPML.cpp:84-95, the free surface FreeSurface2Delastic.cpp:14-45 and the ABS
+// taper ABS2D.cpp:14-50): the gradient of J = 1/2 sum (d - d_obs)^2 over all
+// receivers and samples with respect to vp, vs and rho, in the oracle's value
+// type (double: the FP64 gradient the CUDA adjoint is checked against).
+//
+// The reference has no adjoint; this is an independent restatement on the
+// oracle's CSR operators (transposed explicitly), written from the forward
+// operation list, not from the CUDA adjoint.
+//
+// Per step t the forward maps state X_t = (vx, vy, sxx, syy, sxy, psi) to
+// X_{t+1}; the receivers read X_{t+1}. Intermediates of step t are formed
+// from X_t and X_{t+1}:
+//   a1' = Dxf sxx + P1   a2' = DybS sxy + P2   a3' = Dxb sxy + P3   a4' = DyfS syy + P4
+//   vx' = vx + irx (a1' + a2')                  vy' = vy + iry (a3' + a4')
+//   c1' = Dxb vx' + Q1   c2' = Dyb vy' + Q2   c3' = Dyf vx' + Q3   c4' = Dxf vy' + Q4
+// (P, Q: the psi arrays of X_{t+1}; vx', vy' are the velocities before the
+// ABS taper and the sources). Checkpoints every K steps; each segment is
+// recomputed with the oracle's own step and walked backwards.
+#pragma once
+
+#include <cmath>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "refcpu.hpp"
+
+namespace refcpu {
+
+template <class T>
+CSR<T> transpose(const CSR<T>& A)
+{
+    CSR<T> B;
+    B.n = A.n;
+    B.ptr.assign(A.n + 1, 0);
+    for (idx_t k = 0; k < A.ptr[A.n]; ++k) ++B.ptr[A.col[k] + 1];
+    for (idx_t r = 0; r < A.n; ++r) B.ptr[r + 1] += B.ptr[r];
+    B.col.resize(A.ptr[A.n]);
+    B.val.resize(A.ptr[A.n]);
+    std::vector<idx_t> fill(B.ptr.begin(), B.ptr.end() - 1);
+    for (idx_t r = 0; r < A.n; ++r)
+        for (idx_t k = A.ptr[r]; k < A.ptr[r + 1]; ++k) {
+            const idx_t d = fill[A.col[k]]++;
+            B.col[d] = r;
+            B.val[d] = A.val[k];
+        }
+    return B;
+}
+
+// y += A x
+template <class T>
+void spmv_add(const CSR<T>& A, const std::vector<T>& x, std::vector<T>& y)
+{
+#pragma omp parallel for schedule(static)
+    for (idx_t r = 0; r < A.n; ++r) {
+        T s = 0;
+        for (idx_t k = A.ptr[r]; k < A.ptr[r + 1]; ++k) s += A.val[k] * x[A.col[k]];
+        y[r] += s;
+    }
+}
+
+template <class T>
+struct ElasticAdjoint2D {
+    Sim<T>& s;
+    const idx_t N;
+    CSR<T> DxfT, DxbT, DyfT, DybT, DyfST, DybST;
+    // psi names and (a, b) profiles, in the forward's order (stepElastic 2-D)
+    static constexpr const char* kP[4] = {"sxx_x", "sxy_y", "sxy_x", "syy_y"};
+    static constexpr const char* kQ[4] = {"vxx", "vyy", "vxy", "vyx"};
+
+    explicit ElasticAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    {
+        if (s.is3d || s.eq != WAVE_EQ_ELASTIC) throw std::invalid_argument("oracle adjoint: 2-D elastic only");
+        DxfT = transpose(s.Dxf);
+        DxbT = transpose(s.Dxb);
+        DyfT = transpose(s.Dyf);
+        DybT = transpose(s.Dyb);
+        DyfST = transpose(s.fs ? s.DyfFS : s.Dyf);
+        DybST = transpose(s.fs ? s.DybFS : s.Dyb);
+    }
+
+    struct State {
+        std::map<std::string, std::vector<T>> F, psi;
+    };
+    State save() const { return {s.F, s.psi}; }
+    void load(const State& x)
+    {
+        s.F = x.F;
+        s.psi = x.psi;
+    }
+    const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
+    {
+        auto it = x.psi.find(n);
+        return it == x.psi.end() ? zero : it->second;
+    }
+    std::pair<const std::vector<T>*, const std::vector<T>*> prof(const char* n) const
+    {
+        const std::string k(n);
+        if (k == "sxx_x" || k == "vyx") return {&s.axh, &s.bxh};
+        if (k == "sxy_y" || k == "vyy") return {&s.ay, &s.by};
+        if (k == "sxy_x" || k == "vxx") return {&s.ax, &s.bx};
+        return {&s.ayh, &s.byh};   // syy_y, vxy
+    }
+
+    // adjoint of (c, psi) -> (c' = (1 + a) c + b psi, psi' = a c + b psi) at every point:
+    // in: lc = adjoint of c', lp = adjoint of psi'; out: lc = adjoint of c, lp = adjoint of psi
+    void cpmlT(std::vector<T>& lc, std::vector<T>& lp, const char* n) const
+    {
+        if (!s.useCpml) return;
+        auto ab = prof(n);
+        const std::vector<T>& a = *ab.first;
+        const std::vector<T>& b = *ab.second;
+        for_n(N, [&](idx_t i) {
+            const T c = (T(1) + a[i]) * lc[i] + a[i] * lp[i];
+            lp[i] = b[i] * (lc[i] + lp[i]);
+            lc[i] = c;
+        });
+    }
+
+    // Returns the misfit; writes the gradients with respect to vp, vs, rho.
+    double run(const std::vector<T>& vp, const std::vector<T>& vs, const std::vector<T>& rho, const T* dobs, int K,
+               T* gvp, T* gvs, T* grho)
+    {
+        const int NT = s.NT;
+        const size_t nrec = s.rec.idx.size();
+        const std::vector<T> zero(N, T(0));
+        // 1. forward with checkpoints
+        s.reset();
+        std::vector<State> ck;
+        for (int t = 0; t < NT; ++t) {
+            if (t % K == 0) ck.push_back(save());
+            s.step(t);
+        }
+        std::vector<T> res(nrec * static_cast<size_t>(NT));
+        double J = 0;
+        for (size_t k = 0; k < res.size(); ++k) {
+            res[k] = s.seis[k] - dobs[k];
+            J += 0.5 * static_cast<double>(res[k]) * static_cast<double>(res[k]);
+        }
+        // adjoint state and material gradients
+        std::map<std::string, std::vector<T>> lF, lpsi;
+        for (const char* n : {"vx", "vy", "sxx", "syy", "sxy"}) lF[n].assign(N, 0);
+        for (int k = 0; k < 4; ++k) { lpsi[kP[k]].assign(N, 0); lpsi[kQ[k]].assign(N, 0); }
+        std::vector<T> gM(N, 0), gMu(N, 0), gMuXY(N, 0), gIrx(N, 0), gIry(N, 0);
+        std::vector<T> a[4], c[4], vxp(N), vyp(N), la[4], lc[4];
+        for (int k = 0; k < 4; ++k) { a[k].assign(N, 0); c[k].assign(N, 0); la[k].assign(N, 0); lc[k].assign(N, 0); }
+        // 2. backward over the segments
+        const int nseg = static_cast<int>(ck.size());
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int t0 = seg * K, t1 = std::min(NT, t0 + K);
+            std::vector<State> X;
+            load(ck[seg]);
+            X.push_back(save());
+            for (int t = t0; t < t1; ++t) {
+                s.step(t);
+                X.push_back(save());
+            }
+            for (int t = t1 - 1; t >= t0; --t) {
+                const State& X0 = X[t - t0];
+                const State& X1 = X[t - t0 + 1];
+                // intermediates of step t
+                const CSR<T>& DybS = s.fs ? s.DybFS : s.Dyb;
+                const CSR<T>& DyfS = s.fs ? s.DyfFS : s.Dyf;
+                s.Dxf.spmv(X0.F.at("sxx").data(), a[0].data());
+                DybS.spmv(X0.F.at("sxy").data(), a[1].data());
+                s.Dxb.spmv(X0.F.at("sxy").data(), a[2].data());
+                DyfS.spmv(X0.F.at("syy").data(), a[3].data());
+                for (int k = 0; k < 4; ++k) {
+                    const std::vector<T>& p = psiOf(X1, kP[k], zero);
+                    for_n(N, [&](idx_t i) { a[k][i] += p[i]; });
+                }
+                const std::vector<T>& vx0 = X0.F.at("vx");
+                const std::vector<T>& vy0 = X0.F.at("vy");
+                for_n(N, [&](idx_t i) {
+                    vxp[i] = vx0[i] + s.invRhoX[i] * (a[0][i] + a[1][i]);
+                    vyp[i] = vy0[i] + s.invRhoY[i] * (a[2][i] + a[3][i]);
+                });
+                s.Dxb.spmv(vxp.data(), c[0].data());
+                s.Dyb.spmv(vyp.data(), c[1].data());
+                s.Dyf.spmv(vxp.data(), c[2].data());
+                s.Dxf.spmv(vyp.data(), c[3].data());
+                for (int k = 0; k < 4; ++k) {
+                    const std::vector<T>& q = psiOf(X1, kQ[k], zero);
+                    for_n(N, [&](idx_t i) { c[k][i] += q[i]; });
+                }
+                // receivers read X_{t+1}: gather^T of the residual
+                for (size_t r = 0; r < nrec; ++r) {
+                    const idx_t i = s.rec.idx[r];
+                    const T v = res[r * NT + t];
+                    switch (s.rec.type[r]) {
+                    case WAVE_TYPE_P: lF["sxx"][i] += T(0.5) * v; lF["syy"][i] += T(0.5) * v; break;
+                    case WAVE_TYPE_VX: lF["vx"][i] += v; break;
+                    default: lF["vy"][i] += v; break;
+                    }
+                }
+                auto& lvx = lF["vx"];
+                auto& lvy = lF["vy"];
+                auto& lxx = lF["sxx"];
+                auto& lyy = lF["syy"];
+                auto& lxy = lF["sxy"];
+                // ABS taper on all five fields (after the free surface)
+                if (s.useAbs)
+                    for (auto* v : {&lxx, &lyy, &lxy, &lvx, &lvy}) {
+                        auto& w = *v;
+                        for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
+                    }
+                for (int k = 0; k < 4; ++k) std::fill(lc[k].begin(), lc[k].end(), T(0));
+                if (s.fs) {
+                    // sxx += scaleH c1' - scaleV c2'; syy *= fsZero
+                    for_n(N, [&](idx_t i) {
+                        lyy[i] *= s.fsZero[i];
+                        lc[0][i] += s.scaleH[i] * lxx[i];
+                        lc[1][i] -= s.scaleV[i] * lxx[i];
+                        // scaleV = sel (M - 2 mu), scaleH = -sel (M - 2 mu)^2 / M
+                        const T sel = s.fsSelect[i];
+                        if (sel != T(0)) {
+                            const T gH = lxx[i] * c[0][i], gV = -lxx[i] * c[1][i];
+                            const T sv = s.M[i] - T(2) * s.mu[i];
+                            gM[i] += gV * sel - gH * sel * (T(2) * sv / s.M[i] - sv * sv / (s.M[i] * s.M[i]));
+                            gMu[i] += -T(2) * gV * sel + gH * sel * T(4) * sv / s.M[i];
+                        }
+                    });
+                }
+                // sxy += muXY (c3' + c4')
+                for_n(N, [&](idx_t i) {
+                    lc[2][i] += s.muXY[i] * lxy[i];
+                    lc[3][i] += s.muXY[i] * lxy[i];
+                    gMuXY[i] += lxy[i] * (c[2][i] + c[3][i]);
+                });
+                // sxx += M (c1' + c2') - 2 mu c2', syy += M (c1' + c2') - 2 mu c1'
+                for_n(N, [&](idx_t i) {
+                    lc[0][i] += s.M[i] * (lxx[i] + lyy[i]) - T(2) * s.mu[i] * lyy[i];
+                    lc[1][i] += s.M[i] * (lxx[i] + lyy[i]) - T(2) * s.mu[i] * lxx[i];
+                    gM[i] += (lxx[i] + lyy[i]) * (c[0][i] + c[1][i]);
+                    gMu[i] += -T(2) * (lxx[i] * c[1][i] + lyy[i] * c[0][i]);
+                });
+                for (int k = 0; k < 4; ++k) cpmlT(lc[k], lpsi[kQ[k]], kQ[k]);
+                // the undamped velocities vx', vy' feed c1..c4
+                spmv_add(DxbT, lc[0], lvx);
+                spmv_add(DyfT, lc[2], lvx);
+                spmv_add(DybT, lc[1], lvy);
+                spmv_add(DxfT, lc[3], lvy);
+                // vx' = vx + irx (a1' + a2'), vy' = vy + iry (a3' + a4')
+                for_n(N, [&](idx_t i) {
+                    la[0][i] = la[1][i] = s.invRhoX[i] * lvx[i];
+                    la[2][i] = la[3][i] = s.invRhoY[i] * lvy[i];
+                    gIrx[i] += lvx[i] * (a[0][i] + a[1][i]);
+                    gIry[i] += lvy[i] * (a[2][i] + a[3][i]);
+                });
+                for (int k = 0; k < 4; ++k) cpmlT(la[k], lpsi[kP[k]], kP[k]);
+                spmv_add(DxfT, la[0], lxx);
+                spmv_add(DybST, la[1], lxy);
+                spmv_add(DxbT, la[2], lxy);
+                spmv_add(DyfST, la[3], lyy);
+            }
+        }
+        chain(vp, vs, rho, gM, gMu, gMuXY, gIrx, gIry, gvp, gvs, grho);
+        return J;
+    }
+
+    // A^T y for the averaging operator `avg` (out = avg(in)), whose row r reads
+    // at most the 2 x 2 block at r (x, x+1) x (y, y+1): probed with one unit
+    // pattern per (x mod 2, y mod 2) colour, so the edge fallbacks come from
+    // the oracle's own averaging code.
+    template <class Avg>
+    void avgT(Avg avg, const std::vector<T>& y, std::vector<T>& out) const
+    {
+        std::vector<T> e(N), col(N);
+        for (int cx = 0; cx < 2; ++cx)
+            for (int cy = 0; cy < 2; ++cy) {
+                for (idx_t k = 0; k < N; ++k) {
+                    idx_t x, yy, z;
+                    s.g.coord(k, x, yy, z);
+                    e[k] = (x % 2 == cx && yy % 2 == cy) ? T(1) : T(0);
+                }
+                avg(e.data(), col.data());   // col[r] = A[r, k_c(r)]
+                for (idx_t r = 0; r < N; ++r) {
+                    if (col[r] == T(0)) continue;
+                    idx_t x, yy, z;
+                    s.g.coord(r, x, yy, z);
+                    const idx_t kx = (x % 2 == cx) ? x : x + 1, ky = (yy % 2 == cy) ? yy : yy + 1;
+                    out[s.g.index(kx, ky, 0)] += col[r] * y[r];
+                }
+            }
+    }
+
+    // the model preparation's transpose: (M, mu, muXY, irx, iry) -> (vp, vs, rho)
+    void chain(const std::vector<T>& vp, const std::vector<T>& vs, const std::vector<T>& rho, const std::vector<T>& gM,
+               const std::vector<T>& gMu, const std::vector<T>& gMuXY, const std::vector<T>& gIrx, const std::vector<T>& gIry,
+               T* gvp, T* gvs, T* grho) const
+    {
+        // muXY = 1 / A4 (1 / mu_c) (0 below 4): d muXY_r / d mu_c,k = muXY_r^2 A4[r, k] / mu_c,k^2
+        std::vector<T> y(N), gmuc(gMu);
+        for_n(N, [&](idx_t r) { y[r] = gMuXY[r] * s.muXY[r] * s.muXY[r]; });
+        std::vector<T> t(N, 0);
+        avgT([&](const T* in, T* out) { average4<T>(s.g, 0, in, out); }, y, t);
+        for_n(N, [&](idx_t k) { gmuc[k] += t[k] / (s.mu[k] * s.mu[k]); });
+        // irx = 1 / A2x(rho) (0 where invalid): d irx_r / d rho_k = -irx_r^2 A2x[r, k]; the same along y
+        std::vector<T> grhoAvg(N, 0);
+        for_n(N, [&](idx_t r) { y[r] = -gIrx[r] * s.invRhoX[r] * s.invRhoX[r]; });
+        avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::X, in, out); }, y, grhoAvg);
+        for_n(N, [&](idx_t r) { y[r] = -gIry[r] * s.invRhoY[r] * s.invRhoY[r]; });
+        avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::Y, in, out); }, y, grhoAvg);
+        for (idx_t k = 0; k < N; ++k) {
+            // M = rho vp^2; mu_c = max(rho vs^2, 1) (clamped values do not move)
+            T raw = rho[k];
+            raw *= vs[k];
+            raw *= vs[k];
+            const bool unclamped = raw >= T(1);
+            gvp[k] = gM[k] * T(2) * rho[k] * vp[k];
+            gvs[k] = unclamped ? gmuc[k] * T(2) * rho[k] * vs[k] : T(0);
+            grho[k] = gM[k] * vp[k] * vp[k] + (unclamped ? gmuc[k] * vs[k] * vs[k] : T(0)) + grhoAvg[k];
+        }
+    }
+};
+
+template <class T>
+constexpr const char* ElasticAdjoint2D<T>::kP[4];
+template <class T>
+constexpr const char* ElasticAdjoint2D<T>::kQ[4];
+
+} // namespace refcpu

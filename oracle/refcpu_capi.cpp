@@ -8,6 +8,7 @@
 #include <type_traits>
 
 #include "refcpu.hpp"
+#include "adjoint_impl.hpp"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -178,6 +179,36 @@ int refcpu_field(void* hv, const char* name, double* out)
     };
     if (h->is_double) return grab(static_cast<refcpu::Sim<double>*>(h->sim));
     return grab(static_cast<refcpu::Sim<float>*>(h->sim));
+}
+
+// Gradient of J = 1/2 sum (d - dobs)^2 with respect to vp, vs, rho for a 2-D
+// elastic simulation (adjoint_impl.hpp), in the handle's value type; dobs is
+// nrec x NT. The model arrays are the ones the handle was created with. The
+// handle's state is left at the end of the forward run. Returns the misfit
+// through *misfit; 0 on success.
+int refcpu_adjoint_elastic2d(void* hv, const double* vp, const double* vs, const double* rho, const double* dobs, int K,
+                             double* misfit, double* gvp, double* gvs, double* grho)
+{
+    auto* h = static_cast<Handle*>(hv);
+    auto run = [&](auto* s) -> int {
+        using T = typename std::decay_t<decltype(s->M)>::value_type;
+        const size_t N = s->g.N(), nd = s->rec.idx.size() * static_cast<size_t>(s->NT);
+        std::vector<T> P(vp, vp + N), S(vs, vs + N), R(rho, rho + N), D(dobs, dobs + nd), a(N), b(N), c(N);
+        refcpu::ElasticAdjoint2D<T> adj(*s);
+        *misfit = adj.run(P, S, R, D.data(), K, a.data(), b.data(), c.data());
+        std::copy(a.begin(), a.end(), gvp);
+        std::copy(b.begin(), b.end(), gvs);
+        std::copy(c.begin(), c.end(), grho);
+        return 0;
+    };
+    try {
+        if (K < 1) throw std::invalid_argument("checkpoint interval must be >= 1");
+        if (h->is_double) return run(static_cast<refcpu::Sim<double>*>(h->sim));
+        return run(static_cast<refcpu::Sim<float>*>(h->sim));
+    } catch (std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
 }
 
 void refcpu_destroy(void* hv)

@@ -1,0 +1,98 @@
+"""The oracle's FP64 discrete adjoint of the 2-D elastic step
+(oracle/adjoint_impl.hpp), checked without a GPU against central finite
+differences of the FP64 oracle's own misfit: along seeded smooth directions
+and at single grid points, for vp, vs and rho, with CPML, no boundary, ABS and
+the free surface, both edge rules and stencil operators. This pins the FP64
+gradient the CUDA adjoint is compared with (tests/test_gpu_adjoint.py).
+
+Gate: relative error of the directional derivative <= 1e-6 (FP64 forward
+with a relative step of 1e-4: truncation ~1e-8, rounding ~1e-11)."""
+import numpy as np
+import pytest
+
+
+def case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, seed=3, NX=44, NY=36, nt=160):
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:NY, 0:NX]
+    vp = 2000.0 + 600.0 * (y / NY) + 80.0 * np.sin(x / 5.0) + 30 * rng.standard_normal((NY, NX))
+    vs = vp / 1.75
+    rho = 310.0 * vp ** 0.25
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(vp=vp, vs=vs, rho=rho).items()}
+    DH, DT = 5.0, 4e-4
+    cfg = refcpu.make_config(dimension=2, equation="elastic", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT, T=(nt - 0.4) * DT,
+                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary, BoundaryWidth=8,
+                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=20.0, VMaxCPML=2700.0,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    sidx = np.array([refcpu.grid_index(cfg, NX // 2, 2 if fs else 6, 0)], np.int64)
+    sig = refcpu.ricker(nt, DT, 25.0, 1.0, -0.02, np.float64)[None]
+    rx = np.arange(4, NX - 4, 3)
+    ry = 0 if fs else 5
+    ridx = np.concatenate([rx + NX * ry, rx + NX * ry, rx + NX * (NY - 6)]).astype(np.int64)
+    rtype = np.concatenate([np.full(rx.size, 2), np.full(rx.size, 3), np.full(rx.size, 1)]).astype(np.int32)
+    return cfg, model, (sidx, np.array([1], np.int32), sig, ridx, rtype)
+
+
+def misfit(refcpu, cfg, model, acq, dobs):
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    d = o.run()
+    o.close()
+    return 0.5 * float(np.sum((d - dobs) ** 2))
+
+
+def smooth_direction(rng, NY, NX):
+    from scipy.ndimage import gaussian_filter
+    return gaussian_filter(rng.standard_normal((NY, NX)), 3.0, mode="nearest").reshape(-1)
+
+
+@pytest.mark.parametrize("fs,boundary,stencil,reduce", [(0, 2, 0, 1), (0, 0, 0, 0), (1, 2, 0, 1), (0, 1, 0, 1),
+                                                        (1, 1, 1, 0)])
+def test_oracle_adjoint_matches_fp64_finite_differences(refcpu, fs, boundary, stencil, reduce):
+    cfg, model, acq = case(refcpu, fs, boundary, stencil, reduce)
+    # observed data: the same survey on a perturbed model
+    true = dict(model)
+    yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
+    blob = np.exp(-((xx - cfg.NX * 0.4) ** 2 + (yy - cfg.NY * 0.6) ** 2) / 40.0).reshape(-1)
+    true["vp"] = model["vp"] * (1 + 0.05 * blob)
+    true["vs"] = model["vs"] * (1 - 0.04 * blob)
+    o = refcpu.Oracle(cfg, true, *acq, dtype=np.float64)
+    dobs = o.run()
+    o.close()
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    J, gvp, gvs, grho = o.adjoint_gradient(dobs, checkpoint_every=37)
+    o.close()
+    assert J == pytest.approx(misfit(refcpu, cfg, model, acq, dobs), rel=1e-12)
+    rng = np.random.default_rng(11)
+    grads = dict(vp=gvp, vs=gvs, rho=grho)
+    for name in ("vp", "vs", "rho"):
+        d = smooth_direction(rng, cfg.NY, cfg.NX) * model[name]
+        h = 1e-4
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name] + h * d
+        mm[name] = model[name] - h * d
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        ad = float(np.dot(grads[name], d))
+        assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
+    # one single-point probe per parameter, at the point of the largest gradient
+    for name in ("vp", "vs", "rho"):
+        k = int(np.argmax(np.abs(grads[name])))
+        h = 1e-4 * model[name][k]
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name].copy()
+        mm[name] = model[name].copy()
+        mp[name][k] += h
+        mm[name][k] -= h
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        assert abs(grads[name][k] - fd) <= 1e-6 * abs(fd), (name, k, grads[name][k], fd)
+
+
+def test_oracle_adjoint_is_independent_of_the_checkpoint_interval(refcpu):
+    cfg, model, acq = case(refcpu, fs=1, boundary=2)
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    d = o.run()
+    dobs = 0.9 * d
+    g1 = o.adjoint_gradient(dobs, checkpoint_every=1)
+    g2 = o.adjoint_gradient(dobs, checkpoint_every=1000)
+    o.close()
+    assert g1[0] == g2[0]
+    for a, b in zip(g1[1:], g2[1:]):
+        assert np.array_equal(a, b)
