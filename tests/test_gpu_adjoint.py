@@ -6,7 +6,12 @@ rejected. The reference has no adjoint; the forward it differentiates is
 FD2Delastic::run (ForwardSolver2Delastic.cpp:117-297).
 
 Tolerance: |<g, dm> - (J(m + h dm) - J(m - h dm)) / 2h| <= 2e-2 |FD| (FP32
-forward and adjoint, relative step 1e-3 of the parameter).
+forward and adjoint, relative step 1e-3 of the parameter: the FP32 forward's
+rounding bounds this check). The tight checks are against the FP64 oracle
+gradient (oracle/adjoint_impl.hpp, itself pinned to FP64 finite differences
+at 1e-6): relative L2 <= 1e-4 per parameter, with the free surface and ABS,
+through a test-only torch.autograd.Function, and on a sub-grid of the
+32-shot FWI workload.
 """
 import numpy as np
 import pytest
@@ -120,7 +125,7 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("kw", [dict(fs=1), dict(boundary=1), dict(dim=3)])
+@pytest.mark.parametrize("kw", [dict(dim=3)])
 def test_adjoint_rejects_unsupported_setups(wave, kw):
     cfg = _config(wave, **kw)
     true, start = _models()
@@ -177,3 +182,171 @@ def test_batched_adjoint_equals_single_shot_adjoints(wave):
     for summed, parts in ((svp, gvp), (svs, gvs), (srho, grho)):
         ref = np.sum([p.astype(np.float64) for p in parts], axis=0)
         assert np.linalg.norm(summed - ref) <= 1e-6 * np.linalg.norm(ref)
+
+
+# ----------------------------------------------------------------------------
+# against the FP64 oracle gradient
+# ----------------------------------------------------------------------------
+GRAD_TOL = 1e-4
+
+
+def _oracle_gradient(refcpu, cfg, model, acq, dobs, K=50):
+    ocfg = refcpu.WaveConfig()
+    import ctypes
+    ctypes.memmove(ctypes.byref(ocfg), ctypes.byref(cfg), ctypes.sizeof(ocfg))
+    o = refcpu.Oracle(ocfg, {k: np.asarray(v, np.float64) for k, v in model.items()}, acq[0], acq[1],
+                      np.asarray(acq[2], np.float64), acq[3], acq[4], dtype=np.float64)
+    out = o.adjoint_gradient(np.asarray(dobs, np.float64), checkpoint_every=K)
+    o.close()
+    return out
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+def _survey(wave, **kw):
+    cfg = _config(wave, **kw)
+    true, start = _models()
+    s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
+    nt = s.nt
+    s.close()
+    acq = _acq(wave, cfg, nt)
+    if kw.get("fs"):
+        # sources below the surface row, receivers on it
+        acq = (acq[0] + NX * 2, acq[1], acq[2], np.where(acq[3] < NX * 10, acq[3] % NX, acq[3]), acq[4])
+    st = _solver(wave, cfg, true, acq)
+    st.run(0, nt)
+    dobs = st.seismograms()
+    st.close()
+    return cfg, start, acq, dobs
+
+
+@pytest.mark.parametrize("kw", [dict(order=4, boundary=2), dict(order=2, boundary=0, stencil=1),
+                                dict(order=4, boundary=2, fs=1), dict(order=4, boundary=1),
+                                dict(order=6, boundary=1, fs=1), dict(order=8, boundary=2, fs=1, stencil=1)])
+def test_adjoint_gradient_matches_the_fp64_oracle_gradient(wave, refcpu, kw):
+    """P and VY sources (the VY source exercises the re-formed pre-taper
+    velocities), P / VX / VY receivers; every free-surface / ABS / CPML
+    combination the adjoint supports."""
+    cfg, start, acq, dobs = _survey(wave, **kw)
+    sa = _solver(wave, cfg, start, acq)
+    J, gvp, gvs, grho = sa.adjoint_gradient(dobs, checkpoint_every=50)
+    sa.close()
+    J64, g64vp, g64vs, g64rho = _oracle_gradient(refcpu, cfg, start, acq, dobs)
+    errs = [_rel(g, r) for g, r in ((gvp, g64vp), (gvs, g64vs), (grho, g64rho))]
+    print(f"adjoint {kw}: misfit {J:.6e} vs FP64 {J64:.6e}; gradient rel L2 vp {errs[0]:.2e} vs {errs[1]:.2e} "
+          f"rho {errs[2]:.2e}")
+    assert abs(J - J64) <= 1e-4 * J64
+    assert max(errs) <= GRAD_TOL
+
+
+def _smooth(rng):
+    from scipy.ndimage import gaussian_filter
+    return gaussian_filter(rng.standard_normal((NY, NX)), 4.0, mode="nearest").reshape(-1)
+
+
+def _oracle_misfit(refcpu, cfg, model, acq, dobs):
+    import ctypes
+    ocfg = refcpu.WaveConfig()
+    ctypes.memmove(ctypes.byref(ocfg), ctypes.byref(cfg), ctypes.sizeof(ocfg))
+    o = refcpu.Oracle(ocfg, model, acq[0], acq[1], np.asarray(acq[2], np.float64), acq[3], acq[4], dtype=np.float64)
+    d = o.run()
+    o.close()
+    return 0.5 * float(np.sum((d - np.asarray(dobs, np.float64)) ** 2))
+
+
+def test_autograd_gradient_against_fp64_finite_differences(wave, refcpu):
+    """Through the test-only torch.autograd.Function: the gradients equal the
+    C ABI's, and their projections on 8 seeded smooth directions (per
+    parameter) and 16 single points (the largest gradient entries) match
+    central finite differences of the FP64 oracle's misfit (relative step
+    1e-4) within 1e-4 (directions) / 1e-3 of the largest entry (points)."""
+    torch = pytest.importorskip("torch")
+    import adjoint_autograd
+    cfg, start, acq, dobs = _survey(wave, order=4, boundary=2, fs=1)
+    t = {k: torch.tensor(v, dtype=torch.float32, requires_grad=True) for k, v in start.items()}
+    sa = _solver(wave, cfg, start, acq)
+    J = adjoint_autograd.misfit(t["vp"], t["vs"], t["rho"], sa, dobs, 50)
+    J.backward()
+    _, gvp, gvs, grho = sa.adjoint_gradient(dobs, checkpoint_every=50)
+    sa.close()
+    grads = {"vp": t["vp"].grad.numpy(), "vs": t["vs"].grad.numpy(), "rho": t["rho"].grad.numpy()}
+    for k, g in (("vp", gvp), ("vs", gvs), ("rho", grho)):
+        assert np.array_equal(grads[k], g)
+    m64 = {k: v.astype(np.float64) for k, v in start.items()}
+    rng = np.random.default_rng(20260005)
+    worst = 0.0
+    for name in ("vp", "vs", "rho"):
+        for _ in range(8):
+            d = _smooth(rng) * m64[name]
+            h = 1e-4
+            mp, mm = dict(m64), dict(m64)
+            mp[name] = m64[name] + h * d
+            mm[name] = m64[name] - h * d
+            fd = (_oracle_misfit(refcpu, cfg, mp, acq, dobs) - _oracle_misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+            ad = float(np.dot(grads[name].astype(np.float64), d))
+            worst = max(worst, abs(ad - fd) / abs(fd))
+            assert abs(ad - fd) <= 1e-4 * abs(fd), (name, ad, fd)
+    g_all = np.concatenate([grads["vp"], grads["vs"], grads["rho"]]).astype(np.float64)
+    top = np.argsort(-np.abs(g_all))[:16]
+    for k in top:
+        name, i = ("vp", "vs", "rho")[k // cfg.N], int(k % cfg.N)
+        h = 1e-4 * m64[name][i]
+        mp, mm = dict(m64), dict(m64)
+        mp[name] = m64[name].copy()
+        mm[name] = m64[name].copy()
+        mp[name][i] += h
+        mm[name][i] -= h
+        fd = (_oracle_misfit(refcpu, cfg, mp, acq, dobs) - _oracle_misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        assert abs(grads[name][i] - fd) <= 1e-3 * abs(fd), (name, i, grads[name][i], fd)
+    print(f"autograd directional derivatives: worst relative error {worst:.2e}")
+
+
+def test_fwi_workload_subgrid_batched_against_fp64(wave, refcpu):
+    """The 32-shot FWI-gradient workload's physics (order 4, DH 5 m, DT 5e-4,
+    20-pt CPML, layered model with two +-10 % anomalies, smoothed start
+    model, P sources at depth 10, 136 two-component receivers rows) on a
+    200 x 100 sub-grid, 1000 steps, 3 shots in one batch with the gradients
+    summed, checkpoints every 50 steps: against the sum of the FP64 oracle's
+    per-shot gradients."""
+    import bench
+    NXs, NYs, nt = 200, 100, 1000
+    kw = dict(bench.FWI_KW, NX=NXs, NY=NYs, T=(nt - 0.4) * bench.FWI_KW["DT"], VMaxCPML=4400.0)
+    cfg = wave.WaveConfig.make(**kw)
+    true, start = bench.fwi_models(NXs, NYs)
+    acqs = []
+    for k in range(3):
+        sidx = np.array([30 + 60 * k + NXs * 10], np.int64)
+        sig = wave.wavelet(1, nt, cfg.DT, 10.0, 1.0, 0.0)[None]
+        xs = 10 + 4 * np.arange(45)
+        ridx = np.concatenate([xs + NXs * 10, xs + NXs * 10]).astype(np.int64)
+        rtype = np.concatenate([np.full(45, 2), np.full(45, 3)]).astype(np.int32)
+        acqs.append((sidx, np.array([1], np.int32), sig, ridx, rtype))
+    dobs = []
+    for acq in acqs:
+        st = _solver(wave, cfg, true, acq)
+        st.run(0, nt)
+        dobs.append(st.seismograms())
+        st.close()
+    b = wave.Batch([cfg] * 3)
+    try:
+        for shot, acq in zip(b.shots, acqs):
+            shot.prepareForModelling(start)
+            shot.setSources(*acq[:3])
+            shot.setReceivers(*acq[3:])
+        mis, gvp, gvs, grho = b.adjoint_gradient(dobs, checkpoint_every=50, sum_shots=True)
+    finally:
+        b.close()
+    ref = [np.zeros(cfg.N) for _ in range(3)]
+    J64 = 0.0
+    for acq, d in zip(acqs, dobs):
+        J, a, bb, c = _oracle_gradient(refcpu, cfg, start, acq, d)
+        J64 += J
+        for r, g in zip(ref, (a, bb, c)):
+            r += g
+    errs = [_rel(g, r) for g, r in zip((gvp, gvs, grho), ref)]
+    print(f"FWI sub-grid 200x100, 3 shots, NT={nt}: misfit {sum(mis):.6e} vs FP64 {J64:.6e}; "
+          f"gradient rel L2 vp {errs[0]:.2e} vs {errs[1]:.2e} rho {errs[2]:.2e}")
+    assert abs(sum(mis) - J64) <= 1e-4 * J64
+    assert max(errs) <= GRAD_TOL

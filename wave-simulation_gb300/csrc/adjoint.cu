@@ -1,7 +1,9 @@
 // adjoint.cu — gradient of the seismogram misfit J = 1/2 sum (d - d_obs)^2 with
 // respect to vp, vs and rho for the 2-D elastic time step, by the discrete
 // adjoint of the forward step (FD2Delastic::run, ForwardSolver2Delastic.cpp:
-// 117-297) with CPML (CPML.cpp:84-95) and checkpointing.
+// 117-297) with CPML (CPML.cpp:84-95), the free surface (image operators and
+// FreeSurface2Delastic.cpp:14-45), the ABS taper (ABS2D.cpp:14-50) and
+// checkpointing.
 //
 // The forward step is linear in the state X = (vx, vy, sxx, syy, sxy, psi):
 //   velocity pass   a_k = D_k sigma,  P_k' = b P_k + a a_k,  a_k' = a_k + P_k',
@@ -9,7 +11,11 @@
 //   stress pass     c_k = D_k v',     Q_k' = b Q_k + a c_k,  c_k' = c_k + Q_k',
 //                   sxx' = sxx + M (c1' + c2') - 2 mu c2', syy' = syy + M (c1' + c2') - 2 mu c1',
 //                   sxy' = sxy + mu_xy (c3' + c4')
-// plus source terms, and receivers read X after each step. The adjoint runs
+// then at y = 0 with the free surface sxx' += sh c1' - sv c2', syy' = 0
+// (sv = M - 2 mu, sh = -sv^2 / M), then the ABS taper d on all five fields,
+// plus source terms, and receivers read X after each step. The stress pass
+// reads the velocities before the taper and the sources, v' = (v_{n+1} - s) / d,
+// re-formed from the saved state when ABS or velocity sources are on. The adjoint runs
 // the transposed pieces backwards (three kernels per step: stress transpose,
 // velocity transpose, stress-derivative transpose) and accumulates
 // dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry, which a last kernel maps to
@@ -53,6 +59,11 @@ struct AdjShot {
     const int* rtype;
     const float* res;            // residual d - d_obs, nrec x nt
     int nrec, nt;
+    float* vprime[2];            // vx', vy' of the current step (null: the saved state's vx, vy are they)
+    const long long* sidx;       // sources (velocity sources are taken out of v')
+    const int* stype;
+    const float* signals;        // nsrc x nt
+    int nsrc;
 };
 
 struct CopyPart {
@@ -122,7 +133,8 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
 {
     const float* X1 = A.view + (long long)(vn + 1) * A.stride;
     const long long i = p.i, sy = P.NX;
-    const float *vx1 = X1 + A.off[AV_VX], *vy1 = X1 + A.off[AV_VY];
+    const float* vx1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
+    const float* vy1 = A.vprime[1] ? A.vprime[1] : X1 + A.off[AV_VY];
     const float M = __ldg(P.m[M_M] + i), mu = __ldg(P.m[M_MU] + i), mxy = __ldg(P.m[M_MUXY] + i);
     const Slabs S = slabs_of(P, p);
     // forward derivatives with their CPML correction, c' = c + Q_{n+1}
@@ -132,11 +144,34 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
     float c4 = deriv<H, true>(vy1, i, 1, p.x, P.Dxf);
     if (S.sx >= 0) { c1 += X1[A.off[AV_Q1] + S.px]; c4 += X1[A.off[AV_Q4] + S.px]; }
     if (S.sy >= 0) { c2 += X1[A.off[AV_Q2] + S.py]; c3 += X1[A.off[AV_Q3] + S.py]; }
-    const float lxx = A.lf[2][i], lyy = A.lf[3][i], lxy = A.lf[4][i];
+    float lxx = A.lf[2][i], lyy = A.lf[3][i], lxy = A.lf[4][i];
+    if (P.abs) {
+        // the taper multiplied all five fields last: their adjoints first
+        const float d = absDamp(P, p);
+        lxx *= d; lyy *= d; lxy *= d;
+        A.lf[0][i] *= d;
+        A.lf[1][i] *= d;
+    }
+    const bool fsRow = P.fs && p.y == 0;
+    if (fsRow) lyy = 0.0f;                 // syy' = 0 on the surface
+    A.lf[2][i] = lxx;
+    A.lf[3][i] = lyy;
+    A.lf[4][i] = lxy;
     const float lam = M - 2.0f * mu;
     float l1 = M * lxx + lam * lyy;
     float l2 = lam * lxx + M * lyy;
     float l3 = mxy * lxy, l4 = l3;
+    if (fsRow) {
+        // sxx' += sh c1' - sv c2' with sv = M - 2 mu, sh = -sv^2 / M
+        const float sv = lam, sh = -(sv * sv) / M;
+        l1 += sh * lxx;
+        l2 -= sv * lxx;
+        // dJ/dsh = lxx c1', dJ/dsv = -lxx c2' (c1, c2 carry their CPML correction here);
+        // d sv / dM = 1, d sv / dmu = -2; d sh / dM = -(2 sv / M - sv^2 / M^2), d sh / dmu = 4 sv / M
+        const float gh = lxx * c1, gv = -lxx * c2;
+        A.g[0][i] += gv - gh * (2.0f * sv / M - (sv * sv) / (M * M));
+        A.g[1][i] += -2.0f * gv + gh * 4.0f * sv / M;
+    }
     if (S.sx >= 0) {
         cpml_adj(l1, A.lpsi[4] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // Q1 (vxx): x, full profile
         cpml_adj(l4, A.lpsi[7] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // Q4 (vyx): x, half profile
@@ -169,10 +204,12 @@ __device__ __forceinline__ void adj_vel_body(const StepParams& P, const AdjShot&
     lvy += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
     const Slabs S = slabs_of(P, p);
     const float *sxx = X0 + A.off[AV_SXX], *syy = X0 + A.off[AV_SYY], *sxy = X0 + A.off[AV_SXY];
+    const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
+    const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
     float a1 = deriv<H, true>(sxx, i, 1, p.x, P.Dxf);
-    float a2 = deriv<H, false>(sxy, i, sy, p.y, P.Dyb);
+    float a2 = deriv<H, false>(sxy, i, sy, p.y, DybS);
     float a3 = deriv<H, false>(sxy, i, 1, p.x, P.Dxb);
-    float a4 = deriv<H, true>(syy, i, sy, p.y, P.Dyf);
+    float a4 = deriv<H, true>(syy, i, sy, p.y, DyfS);
     if (S.sx >= 0) { a1 += X1[A.off[AV_P1] + S.px]; a3 += X1[A.off[AV_P3] + S.px]; }
     if (S.sy >= 0) { a2 += X1[A.off[AV_P2] + S.py]; a4 += X1[A.off[AV_P4] + S.py]; }
     const float irx = __ldg(P.m[M_IRX] + i), iry = __ldg(P.m[M_IRY] + i);
@@ -200,11 +237,13 @@ template <int H>
 __device__ __forceinline__ void adj_sigma_body(const StepParams& P, const AdjShot& A, const Pt& p)
 {
     const long long i = p.i, sy = P.NX;
+    const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
+    const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
     A.lf[2][i] += derivT<H, true>(A.T[4], i, 1, p.x, P.Dxf);
-    float u = derivT<H, false>(A.T[5], i, sy, p.y, P.Dyb);
+    float u = derivT<H, false>(A.T[5], i, sy, p.y, DybS);
     u += derivT<H, false>(A.T[6], i, 1, p.x, P.Dxb);
     A.lf[4][i] += u;
-    A.lf[3][i] += derivT<H, true>(A.T[7], i, sy, p.y, P.Dyf);
+    A.lf[3][i] += derivT<H, true>(A.T[7], i, sy, p.y, DyfS);
 }
 
 template <int H, int PASS>
@@ -221,6 +260,44 @@ __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ P
         if (PASS == 0) adj_stress_body<H>(sP, A, p, vn);
         else if (PASS == 1) adj_vel_body<H>(sP, A, p, vn);
         else adj_sigma_body<H>(sP, A, p);
+    }
+}
+
+// v' = (v_{n+1} - sources of step n) / d: the velocities the stress pass of
+// step n read (before the ABS taper and the source injection)
+__global__ void adj_vprime(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As, const BatchTile* __restrict__ W, int vn)
+{
+    __shared__ StepParams sP;
+    const BatchTile w = W[blockIdx.x];
+    load_params(sP, Ps + w.shot);
+    const AdjShot& A = As[w.shot];
+    if (!A.vprime[0]) return;
+    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
+    for (int rr = 0; rr < kTileRows; rr += 8) {
+        Pt p;
+        if (!point_tile(sP, w, p, rr)) continue;
+        const float d = sP.abs ? absDamp(sP, p) : 1.0f;
+        A.vprime[0][p.i] = X1[A.off[AV_VX] + p.i] / d;
+        A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
+    }
+}
+
+__global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As, int n)
+{
+    const StepParams& P = Ps[blockIdx.x];
+    const AdjShot& A = As[blockIdx.x];
+    if (!A.vprime[0]) return;
+    for (int k = threadIdx.x; k < A.nsrc; k += blockDim.x) {
+        const int t = A.stype[k];
+        if (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY) continue;
+        const long long i = A.sidx[k];
+        Pt p;
+        p.i = i;
+        p.x = static_cast<int>(i % P.NX);
+        p.y = static_cast<int>(i / P.NX);
+        p.z = 0;
+        const float d = P.abs ? absDamp(P, p) : 1.0f;
+        atomicAdd(A.vprime[t == WAVE_TYPE_VX ? 0 : 1] + i, -A.signals[(long long)k * A.nt + n] / d);
     }
 }
 
@@ -372,8 +449,6 @@ std::string adjoint_supported(const wave_handle* h)
 {
     const wave_config& c = h->cfg;
     if (c.dimension != 2 || c.equation != WAVE_EQ_ELASTIC) return "the adjoint gradient is implemented for 2-D elastic modelling";
-    if (c.FreeSurface != 0) return "the adjoint gradient does not support the free surface";
-    if (c.DampingBoundary == 1) return "the adjoint gradient supports CPML or no damping boundary, not ABS";
     if (!h->modelSet) return "set the model first";
     if (!h->seis || h->nrec < 1) return "set receivers first";
     return "";
@@ -433,6 +508,17 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         a.nt = NT;
         float* res = pool.get<float>(static_cast<size_t>(h->nrec) * NT);
         a.res = res;
+        bool velocitySources = false;
+        for (int t : h->hSrcType) velocitySources |= (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
+        a.vprime[0] = a.vprime[1] = nullptr;
+        if (h->cfg.DampingBoundary == 1 || velocitySources) {
+            a.vprime[0] = pool.get<float>(2 * N);
+            a.vprime[1] = a.vprime[0] + N;
+        }
+        a.sidx = h->sidx;
+        a.stype = h->stype;
+        a.signals = h->signals;
+        a.nsrc = h->nsrc;
         ckpt[s] = pool.get<float>(static_cast<size_t>(o) * nck);
         for (int k = 0; k < AV_COUNT; ++k) {
             if (len[k] == 0) continue;
@@ -459,6 +545,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
     const CopyPart* dToCkpt = upload(toCkpt);
     const CopyPart* dFromCkpt = upload(fromCkpt);
     const int ntiles = static_cast<int>(tiles.size());
+    bool anyVprime = false;
+    for (const AdjShot& a : A) anyVprime |= a.vprime[0] != nullptr;
     const dim3 cgrid(64, 1, 1);
     auto copy = [&](const CopyPart* parts, size_t nparts, long long si, long long di) {
         copy_parts<<<dim3(cgrid.x, static_cast<unsigned>(nparts), 1), 256, 0, st>>>(parts, si, di);
@@ -494,6 +582,10 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             copy(dToView, toView.size(), 0, n - n0 + 1);
         }
         for (int n = n1 - 1; n >= n0; --n) {
+            if (anyVprime) {
+                adj_vprime<<<ntiles, dim3(32, 8, 1), 0, st>>>(dP, dA, dT, n - n0);
+                adj_vprime_sources<<<ns, 128, 0, st>>>(dP, dA, n);
+            }
             adj_inject<<<ns, 256, 0, st>>>(dA, n);
             launch_adj(H, 0, dP, dA, dT, ntiles, n - n0, st);
             launch_adj(H, 1, dP, dA, dT, ntiles, n - n0, st);
