@@ -832,6 +832,7 @@ def run_tmem_batch(args, wave):
         shot.setSources(*acq[:3])
         shot.setReceivers(*acq[3:])
     b.run(0, args.warmup)
+    sched = b.schedule()
     l0 = b.launch_count()
     ms, clocks = _clocked(lambda: b.run(args.warmup, args.warmup + args.steps), torch.cuda.ExternalStream(b.stream()))
     launches = b.launch_count() - l0
@@ -886,7 +887,7 @@ def run_tmem_batch(args, wave):
             "shots": nshots, "points_per_step": npts, "l2": "inputs larger than L2 (3 x 31 M x 4 B)", "parallelism": "1 GPU"}
     _line(UNIT, value, args.steps, args.warmup, ms / args.steps, cfgd,
           _roof(alg, ms / args.steps, "tm_h_batch<2> + tm_e_batch<2>"), e2e, launches, clocks, cpu,
-          {"plain_value": plain, "batched_over_plain": value / plain})
+          {"plain_value": plain, "batched_over_plain": value / plain, "schedule": sched})
 
 
 # ---- config 5: 2-D elastic FWI gradient, 32 shots ---------------------------

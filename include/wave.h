@@ -403,6 +403,23 @@ int wave_batch_step(wave_batch* b, int t_begin, int t_end);
  * all shots are summed into grad_*[0], else grad_*[s] receive shot s's. */
 int wave_batch_adjoint_gradient(wave_batch* b, const float* const* dobs, int dobs_mem, int checkpoint_every, double* misfits,
                                 float* const* grad_vp, float* const* grad_vs, float* const* grad_rho, int grad_mem, int sum_shots);
+/* Schedule of the batched launches (no counterpart in the reference, whose
+ * shots run one after another, Simulation.cpp:339-369): each launch's blocks
+ * walk the (shot, tile) work list with a grid stride. tile_cols (a multiple of
+ * 32) x tile_rows (a multiple of 8) points per work-list entry; blocks_per_sm
+ * persistent 256-thread blocks per SM (at most the resident count), or 0 for
+ * one block per entry. wave_batch_set_schedule fixes it (0, 0 returns to the
+ * autotuner); otherwise the first step call of an unstepped batch times every
+ * candidate (tile 32 or 64 wide, 8/16/32/64 rows; 0/1/2/4/8 blocks per SM;
+ * one untimed and two timed steps each, state reset afterwards) and keeps the
+ * fastest, cached for the process per (equation, FD order, log2 of the mean
+ * points per shot, log2 of the shot count). wave_batch_get_schedule reports
+ * the schedule and where it came from (source: 0 default, 1 timed by this
+ * batch, 2 from the cache, 3 set by the caller). Every schedule gives the same
+ * results bit for bit: each grid point's update does not depend on the
+ * tiling. */
+int wave_batch_set_schedule(wave_batch* b, int tile_cols, int tile_rows, int blocks_per_sm);
+int wave_batch_get_schedule(wave_batch* b, int* tile_cols, int* tile_rows, int* blocks_per_sm, int* source);
 int wave_batch_get_stream(wave_batch* b, void** stream);
 int wave_batch_get_launch_count(wave_batch* b, long long* count);
 const char* wave_batch_last_error(const wave_batch* b);

@@ -17,7 +17,11 @@ FP32-vs-FP64 drift per workload is in the test log.
   the nine wavefields after them.
 * The same 3-D elastic physics on a 96^3 grid (layers of 12 cells) for all
   NT = 3000 steps: FP32 drift over the full record, with the CPML and the
-  free surface reached by the wave.
+  free surface reached by the wave. This run uses the zero-padded edge rows
+  (edgeOrderReduction = 0): with the current edge-order reduction the
+  reference formulation itself grows without bound on this heterogeneous
+  model after ~1500 steps, in FP64 as in FP32 (tests/test_oracle_stability.py),
+  so no precision comparison is meaningful there.
 * 3-D visco-elastic, order 4, L = 2 (Qp 80, Qs 50 by the tau-method), 20-pt
   CPML on a 128 x 64 x 128 sub-grid of the 512 x 256 x 512 workload, 800 steps.
 * Batched 2-D TMz: 4 of the 128 shots of the batched workload at full
@@ -114,10 +118,11 @@ def _elastic_cube_model(n, seed_layers=2, seed_pert=20260002):
 
 def test_elastic_cube_full_record_drift(wave, refcpu):
     """The 256^3 workload's physics (order 8, free surface, 20-pt CPML, DT,
-    NT = 3000, Ricker 10 Hz, surface receivers) on a 96^3 grid, every step:
-    the FP32 drift over the whole record with the wave through the CPML."""
+    NT = 3000, Ricker 10 Hz, surface receivers) on a 96^3 grid, every step,
+    zero-padded edge rows: the FP32 drift over the whole record with the wave
+    through the CPML."""
     n = 96
-    kw = dict(bench.CONFIG_KW, NX=n, NY=n, NZ=n)
+    kw = dict(bench.CONFIG_KW, NX=n, NY=n, NZ=n, edgeOrderReduction=0)
     cfg = wave.WaveConfig.make(**kw)
     model = _elastic_cube_model(n)
     nt = int(np.float32(np.float32(cfg.T) / np.float32(cfg.DT)) + np.float32(0.5))

@@ -85,3 +85,51 @@ def test_batch_rejects_mixed_equations(wave, refcpu):
     e = make_case(refcpu, "elastic", 2, 4)[0]
     with pytest.raises(wave.WaveError):
         wave.Batch([to_wave_cfg(wave, a), to_wave_cfg(wave, e)])
+
+
+def _tm_batch(wave, refcpu, seeds=(0, 1, 2), grids=((80, 60, 1), (72, 72, 1), (100, 40, 1))):
+    cases = [make_case(refcpu, "tmem", 2, 4, 0, 2, dims=g, seed=k) for k, g in zip(seeds, grids)]
+    return cases, [to_wave_cfg(wave, c[0]) for c in cases]
+
+
+def _run_batch(wave, cases, cfgs, schedule=None, steps=None):
+    b = wave.Batch(cfgs)
+    try:
+        if schedule is not None:
+            b.set_schedule(*schedule)
+        for shot, (cfg, model, sidx, stype, sig, ridx, rtype) in zip(b.shots, cases):
+            shot.prepareForModelling({k: v.astype(np.float32) for k, v in model.items()})
+            shot.setSources(sidx, stype, sig.astype(np.float32))
+            shot.setReceivers(ridx, rtype)
+        b.run(0, steps or b.nt)
+        return [s.seismograms() for s in b.shots], b.schedule()
+    finally:
+        b.close()
+
+
+@pytest.mark.parametrize("schedule", [(64, 8, 0), (32, 16, 2), (64, 64, 1), (32, 8, 8), (96, 24, 4)])
+def test_every_batch_schedule_gives_the_same_bits(wave, refcpu, schedule):
+    """Tile shape and persistent blocks per SM change only which block updates
+    a point, not the arithmetic: bit-identical seismograms."""
+    cases, cfgs = _tm_batch(wave, refcpu)
+    ref, s0 = _run_batch(wave, cases, cfgs, (32, 32, 0))
+    got, s1 = _run_batch(wave, cases, cfgs, schedule)
+    assert s0["source"] == "set" and (s1["tile_cols"], s1["tile_rows"]) == schedule[:2]
+    for a, c in zip(ref, got):
+        assert np.abs(a).max() > 0 and np.array_equal(a, c)
+
+
+def test_autotuner_times_once_then_uses_its_cache(wave, refcpu):
+    """The first unstepped batch of a kind is timed over the candidate
+    schedules and reset; the result equals a run with the schedule fixed; a
+    second batch of the same kind takes the schedule from the cache."""
+    cases, cfgs = _tm_batch(wave, refcpu, seeds=(5, 6), grids=((150, 90, 1), (130, 110, 1)))
+    tuned, s1 = _run_batch(wave, cases, cfgs)
+    assert s1["source"] in ("autotuned", "cache")
+    assert s1["tile_cols"] in (32, 64) and s1["tile_rows"] in (8, 16, 32, 64) and s1["blocks_per_sm"] in (0, 1, 2, 4, 8)
+    again, s2 = _run_batch(wave, cases, cfgs)
+    assert s2["source"] == "cache" and {k: s2[k] for k in ("tile_cols", "tile_rows")} == \
+        {k: s1[k] for k in ("tile_cols", "tile_rows")}
+    fixed, _ = _run_batch(wave, cases, cfgs, (32, 32, 0))
+    for a, b_, c in zip(tuned, again, fixed):
+        assert np.array_equal(a, c) and np.array_equal(b_, c)

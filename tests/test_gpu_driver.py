@@ -156,6 +156,7 @@ def test_driver_runs_a_visco_tm_parameter_file(wave, tmp_path):
              "spatialFDorder": "4", "DampingBoundary": "2", "BoundaryWidth": "10", "centerfrequencycpml": "1.0e8",
              "vmaxcpml": "1.0e8", "numRelaxationMechanisms": "1", "relaxationFrequency": "1.0e8", "epsilonr": "9.0",
              "sigma": "0.005", "mur": "1.0", "tauEpsilon": "0.1", "tauSigmar": "0.1", "SeismogramFormat": "1",
+             "seismoDT": f"{DT:.3e}",
              "useStencilMatrix": "0", "SourceFilename": "ci/sources_em", "ReceiverFilename": "ci/receiver_em",
              "SeismogramFilename": "ci/seismogram.em"}
     cfg, ci = _setup(tmp_path, edits)

@@ -40,7 +40,7 @@ ABI_SYMBOLS = (
     "wave_get_kernel_times", "wave_last_error", "wave_wavelet", "wave_set_kernel_path",
     "wave_get_kernel_path", "wave_average_shear_modulus", "wave_batch_create", "wave_batch_destroy",
     "wave_batch_shot", "wave_batch_step", "wave_batch_get_stream", "wave_batch_get_launch_count",
-    "wave_batch_last_error", "wave_average_shear_modulus_noalloc", "wave_adjoint_gradient",
+    "wave_batch_last_error", "wave_batch_set_schedule", "wave_batch_get_schedule", "wave_average_shear_modulus_noalloc", "wave_adjoint_gradient",
     "wave_batch_adjoint_gradient", "wave_resample_traces", "wave_normalize_traces", "wave_read_mtx",
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
     "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
@@ -205,6 +205,8 @@ def lib():
     L.wave_batch_step.argtypes = [P, I, I]
     L.wave_batch_get_stream.argtypes = [P, CP(P)]
     L.wave_batch_get_launch_count.argtypes = [P, CP(ctypes.c_longlong)]
+    L.wave_batch_set_schedule.argtypes = [P, I, I, I]
+    L.wave_batch_get_schedule.argtypes = [P, CP(I), CP(I), CP(I), CP(I)]
     L.wave_grid_num_points.argtypes = [CP(WaveConfig), ctypes.POINTER(i64)]
     L.wave_grid_index.argtypes = [CP(WaveConfig), i64, i64, i64, ctypes.POINTER(i64)]
     L.wave_grid_coordinates.argtypes = [CP(WaveConfig), P, P, P, i64, P]
@@ -630,6 +632,17 @@ class Batch:
         if sum_shots:
             return list(mis), g[0][0], g[1][0], g[2][0]
         return list(mis), g[0], g[1], g[2]
+
+    def set_schedule(self, tile_cols: int, tile_rows: int, blocks_per_sm: int):
+        """Fixes the batched launches' schedule (wave_batch_set_schedule); (0, 0, 0) returns to the autotuner."""
+        self._check(lib().wave_batch_set_schedule(self.b, int(tile_cols), int(tile_rows), int(blocks_per_sm)))
+
+    def schedule(self) -> dict:
+        """The schedule in use and its source (wave_batch_get_schedule)."""
+        c, r, p, src = (ctypes.c_int() for _ in range(4))
+        self._check(lib().wave_batch_get_schedule(self.b, ctypes.byref(c), ctypes.byref(r), ctypes.byref(p), ctypes.byref(src)))
+        return {"tile_cols": c.value, "tile_rows": r.value, "blocks_per_sm": p.value,
+                "source": ("default", "autotuned", "cache", "set")[src.value]}
 
     def stream(self) -> int:
         s = ctypes.c_void_p()

@@ -2,14 +2,28 @@
 //
 // Each shot is an ordinary solver handle (its own device state, model,
 // sources, receivers, seismograms); the batch fuses the time step of all
-// shots into one launch per pass over a work list of (shot, 32x8 tile)
-// blocks, followed by one source/receiver block per shot. Multi-step calls
-// replay a captured CUDA graph of kGraphSteps steps. The shot-level parallelism
-// of the reference (MPI shot domains, Simulation.cpp:116-121, 339-369) becomes
-// one device-wide launch.
+// shots into one launch per pass over a work list of (shot, tile) entries,
+// followed by one source/receiver block per shot. The launches are
+// persistent: their blocks walk the work list with a grid stride. Multi-step
+// calls replay a captured CUDA graph of kBatchGraphSteps steps. The
+// shot-level parallelism of the reference (MPI shot domains,
+// Simulation.cpp:116-121, 339-369) becomes one device-wide launch.
+//
+// Schedule autotuner: the tile shape (32 or 64 points along x, 8 to 64 rows)
+// and the resident blocks per SM (1, 2, 4 or 8 persistent blocks per SM, or
+// one block per tile) are chosen by timing every candidate on the batch
+// itself (one untimed and two timed steps each) the first time an unstepped
+// batch is stepped; the state is reset afterwards. The choice is cached per
+// (equation, FD order, size bucket: log2 of the mean points per shot and of
+// the shot count) for the life of the process, so later batches of the same
+// kind start with it.
 #include <algorithm>
+#include <cmath>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -33,6 +47,13 @@ struct wave_batch {
     cudaGraphExec_t graph = nullptr;
     bool dirty = true;
     long long launches = 0;
+    // schedule: tile cols x rows, persistent blocks per SM (0 = one block per tile)
+    int cols = 32, rows = kTileRows, perSM = 0;
+    int grid = 0;
+    BatchSched sched{};
+    bool forced = false;      // set by wave_batch_set_schedule
+    bool tuned = false;       // autotuned (or taken from the cache) once
+    int tuneSource = 0;       // 0 default, 1 timed here, 2 from the cache, 3 forced
 
     ~wave_batch()
     {
@@ -63,42 +84,138 @@ void ck(cudaError_t e, const char* what)
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Uploads the shots' step and source/receiver parameters and the tile list.
+// (equation, order, log2 mean points per shot, log2 shot count) -> (cols, rows, blocks per SM)
+using TuneKey = std::tuple<int, int, int, int>;
+std::mutex g_tune_mutex;
+std::map<TuneKey, std::tuple<int, int, int>> g_tune_cache;
+
+TuneKey tune_key(const wave_batch* b)
+{
+    double pts = 0;
+    for (auto* h : b->shots) pts += static_cast<double>(h->N);
+    const int n = static_cast<int>(b->shots.size());
+    return TuneKey{b->eq, b->H, static_cast<int>(std::lround(std::log2(std::max(1.0, pts / n)))),
+                   static_cast<int>(std::lround(std::log2(static_cast<double>(n))))};
+}
+
+// Builds and uploads the work list for the batch's current tile shape and sets the grid.
+void build_tiles(wave_batch* b)
+{
+    const int n = static_cast<int>(b->shots.size());
+    std::vector<BatchTile> tiles;
+    for (int s = 0; s < n; ++s) {
+        wave_handle* h = b->shots[s];
+        const int rows = h->NY * h->NZ;
+        for (int r0 = 0; r0 < rows; r0 += b->rows)
+            for (int x0 = 0; x0 < h->NX; x0 += b->cols) tiles.push_back({s, x0, r0, 0});
+    }
+    cudaFree(b->dTiles);
+    b->dTiles = nullptr;
+    ck(cudaMalloc(&b->dTiles, tiles.size() * sizeof(BatchTile)), "cudaMalloc");
+    ck(cudaMemcpy(b->dTiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice), "upload");
+    b->ntiles = static_cast<int>(tiles.size());
+    b->sched = BatchSched{b->ntiles, b->cols, b->rows, 0};
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int resident = std::max(1, batch_blocks_per_sm(b->eq, b->H));
+    const int per = b->perSM > 0 ? std::min(b->perSM, resident) : 0;
+    b->grid = per > 0 ? std::min(b->ntiles, per * sms) : b->ntiles;
+    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+}
+
+// Uploads the shots' step and source/receiver parameters and the work list.
 void refresh(wave_batch* b)
 {
     const int n = static_cast<int>(b->shots.size());
     std::vector<StepParams> P(n);
     std::vector<SrcRecParams> Q(n);
-    std::vector<BatchTile> tiles;
     for (int s = 0; s < n; ++s) {
-        wave_handle* h = b->shots[s];
-        P[s] = h->sp;
-        Q[s] = h->sq;
-        const int rows = h->NY * h->NZ;
-        for (int r0 = 0; r0 < rows; r0 += kTileRows)
-            for (int x0 = 0; x0 < h->NX; x0 += 32) tiles.push_back({s, x0, r0, 0});
+        P[s] = b->shots[s]->sp;
+        Q[s] = b->shots[s]->sq;
     }
     cudaFree(b->dP);
     cudaFree(b->dQ);
-    cudaFree(b->dTiles);
-    b->dP = nullptr; b->dQ = nullptr; b->dTiles = nullptr;
+    b->dP = nullptr; b->dQ = nullptr;
     ck(cudaMalloc(&b->dP, n * sizeof(StepParams)), "cudaMalloc");
     ck(cudaMalloc(&b->dQ, n * sizeof(SrcRecParams)), "cudaMalloc");
-    ck(cudaMalloc(&b->dTiles, tiles.size() * sizeof(BatchTile)), "cudaMalloc");
     ck(cudaMemcpy(b->dP, P.data(), n * sizeof(StepParams), cudaMemcpyHostToDevice), "upload");
     ck(cudaMemcpy(b->dQ, Q.data(), n * sizeof(SrcRecParams), cudaMemcpyHostToDevice), "upload");
-    ck(cudaMemcpy(b->dTiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice), "upload");
-    b->ntiles = static_cast<int>(tiles.size());
+    build_tiles(b);
 }
 
 void launch_batch_step(wave_batch* b)
 {
-    launch_batch_pass(b->eq, 0, b->H, b->dP, b->dTiles, b->ntiles, b->stream);
-    launch_batch_pass(b->eq, 1, b->H, b->dP, b->dTiles, b->ntiles, b->stream);
+    launch_batch_pass(b->eq, 0, b->H, b->dP, b->dTiles, b->sched, b->grid, b->stream);
+    launch_batch_pass(b->eq, 1, b->H, b->dP, b->dTiles, b->sched, b->grid, b->stream);
     const auto& p1 = b->pass1;
-    launch_batch_aux(b->dP, b->dTiles, b->ntiles, p1.size() > 0 ? p1[0] : -1, p1.size() > 1 ? p1[1] : -1,
+    launch_batch_aux(b->dP, b->dTiles, b->sched, b->grid, p1.size() > 0 ? p1[0] : -1, p1.size() > 1 ? p1[1] : -1,
                      p1.size() > 2 ? p1[2] : -1, b->dQ, b->counters, static_cast<int>(b->shots.size()), b->abs, b->stream);
     b->launches += b->abs ? 4 : 3;
+}
+
+// Zeroes every shot's wavefields, memory variables and CPML state.
+void reset_shots(wave_batch* b)
+{
+    for (auto* h : b->shots) {
+        const int rc = wave_solver_reset(h);
+        if (rc != WAVE_OK) throw std::runtime_error(std::string("reset after tuning: ") + wave_last_error(h));
+        ck(cudaStreamSynchronize(h->stream), "reset");
+    }
+}
+
+// The schedule autotuner (see the file comment). Runs on an unstepped batch
+// at its first step call; leaves the state reset and the schedule set.
+void autotune(wave_batch* b)
+{
+    const TuneKey key = tune_key(b);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            std::tie(b->cols, b->rows, b->perSM) = it->second;
+            build_tiles(b);
+            b->tuned = true;
+            b->tuneSource = 2;
+            return;
+        }
+    }
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    float best = 1e30f;
+    std::tuple<int, int, int> pick{b->cols, b->rows, b->perSM};
+    const long long launches0 = b->launches;
+    for (int cols : {32, 64})
+        for (int rows : {8, 16, 32, 64})
+            for (int per : {0, 1, 2, 4, 8}) {
+                b->cols = cols;
+                b->rows = rows;
+                b->perSM = per;
+                build_tiles(b);
+                launch_set_counters(b->counters, static_cast<int>(b->shots.size()), 0, b->stream);
+                launch_batch_step(b);
+                ck(cudaEventRecord(e0, b->stream), "event");
+                launch_batch_step(b);
+                launch_batch_step(b);
+                ck(cudaEventRecord(e1, b->stream), "event");
+                ck(cudaEventSynchronize(e1), "tuning step");
+                float ms = 0;
+                ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+                if (ms < best) { best = ms; pick = std::make_tuple(cols, rows, per); }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->launches = launches0;
+    std::tie(b->cols, b->rows, b->perSM) = pick;
+    build_tiles(b);
+    reset_shots(b);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = pick;
+    }
+    b->tuned = true;
+    b->tuneSource = 1;
 }
 
 } // namespace
@@ -175,6 +292,11 @@ int wave_batch_step(wave_batch* b, int t_begin, int t_end)
             refresh(b);
             if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
             b->dirty = false;
+        }
+        if (!b->tuned && !b->forced && t_begin == 0) {
+            bool fresh = true;
+            for (auto* h : b->shots) fresh = fresh && h->stepsSinceReset == 0;
+            if (fresh) autotune(b);
         }
         launch_set_counters(b->counters, static_cast<int>(b->shots.size()), t_begin, b->stream);
         int t = t_begin;
@@ -262,6 +384,42 @@ int wave_batch_adjoint_gradient(wave_batch* b, const float* const* dobs, int dob
     }
     for (void* p : tmp) cudaFree(p);
     return rc;
+}
+
+int wave_batch_set_schedule(wave_batch* b, int tile_cols, int tile_rows, int blocks_per_sm)
+{
+    if (!b) return bfail(nullptr, WAVE_ERR_ARG, "wave_batch_set_schedule: null batch");
+    if (tile_cols == 0 && tile_rows == 0) {   // back to the autotuner
+        b->forced = false;
+        b->tuned = false;
+        return WAVE_OK;
+    }
+    if (tile_cols < 32 || tile_cols % 32 != 0 || tile_cols > 1024 || tile_rows < 8 || tile_rows % 8 != 0 || tile_rows > 1024 ||
+        blocks_per_sm < 0 || blocks_per_sm > 64)
+        return bfail(b, WAVE_ERR_ARG, "wave_batch_set_schedule: tile columns a multiple of 32, rows a multiple of 8 (up to 1024), "
+                                      "0..64 blocks per SM");
+    try {
+        b->cols = tile_cols;
+        b->rows = tile_rows;
+        b->perSM = blocks_per_sm;
+        b->forced = true;
+        b->tuned = true;
+        b->tuneSource = 3;
+        if (!b->dirty) build_tiles(b);
+    } catch (std::exception& e) {
+        return bfail(b, WAVE_ERR_CUDA, e.what());
+    }
+    return WAVE_OK;
+}
+
+int wave_batch_get_schedule(wave_batch* b, int* tile_cols, int* tile_rows, int* blocks_per_sm, int* source)
+{
+    if (!b || !tile_cols || !tile_rows || !blocks_per_sm) return bfail(b, WAVE_ERR_ARG, "wave_batch_get_schedule: null argument");
+    *tile_cols = b->cols;
+    *tile_rows = b->rows;
+    *blocks_per_sm = b->perSM;
+    if (source) *source = b->tuneSource;
+    return WAVE_OK;
 }
 
 int wave_batch_get_stream(wave_batch* b, void** stream)

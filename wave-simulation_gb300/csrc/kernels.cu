@@ -52,15 +52,10 @@ __global__ void __launch_bounds__(256) acoustic_v(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) acoustic_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) acoustic_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) acoustic_v_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { acoustic_v_body<H>(P, p); });
 }
 
 template <int H>
@@ -109,15 +104,10 @@ __global__ void __launch_bounds__(256) acoustic_p(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) acoustic_p_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) acoustic_p_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) acoustic_p_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { acoustic_p_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -172,15 +162,10 @@ __global__ void __launch_bounds__(256) elastic_v(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) elastic_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) elastic_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) elastic_v_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { elastic_v_body<H>(P, p); });
 }
 
 // elastic stress: ForwardSolver2Delastic.cpp:210-290, ForwardSolver3Delastic.cpp:283-409,
@@ -269,15 +254,10 @@ __global__ void __launch_bounds__(256) elastic_s(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) elastic_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) elastic_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) elastic_s_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { elastic_s_body<H>(P, p); });
 }
 
 // visco-elastic stress: ForwardSolver2Dviscoelastic.cpp:223-303,
@@ -445,15 +425,10 @@ __global__ void __launch_bounds__(256, 5) visco_s(StepParams P)   // 48 register
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) visco_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) visco_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) visco_s_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { visco_s_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -479,15 +454,10 @@ __global__ void __launch_bounds__(256) sh_v(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) sh_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) sh_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) sh_v_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { sh_v_body<H>(P, p); });
 }
 
 template <int H>
@@ -530,15 +500,10 @@ __global__ void __launch_bounds__(256) sh_s(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) sh_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) sh_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) sh_s_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { sh_s_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -568,15 +533,10 @@ __global__ void __launch_bounds__(256) tm_h(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) tm_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) tm_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) tm_h_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { tm_h_body<H>(P, p); });
 }
 
 // memory variables of one E component (ForwardSolver2Dviscotmem.cpp:175-182,
@@ -619,15 +579,10 @@ __global__ void __launch_bounds__(256) tm_e(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) tm_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) tm_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) tm_e_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { tm_e_body<H>(P, p); });
 }
 
 // EM TEz: FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:132-180),
@@ -652,15 +607,10 @@ __global__ void __launch_bounds__(256) te_h(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) te_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) te_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) te_h_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { te_h_body<H>(P, p); });
 }
 
 template <int H>
@@ -692,15 +642,10 @@ __global__ void __launch_bounds__(256) te_e(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) te_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) te_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) te_e_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { te_e_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -740,15 +685,10 @@ __global__ void __launch_bounds__(256) em3_h(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) em3_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) em3_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) em3_h_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { em3_h_body<H>(P, p); });
 }
 
 template <int H>
@@ -793,15 +733,10 @@ __global__ void __launch_bounds__(256) em3_e(StepParams P)
 }
 
 template <int H>
-__global__ void __launch_bounds__(256) em3_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W)
+__global__ void __launch_bounds__(256) em3_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) em3_e_body<H>(sP, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { em3_e_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -824,15 +759,11 @@ __global__ void __launch_bounds__(256) abs_frame_kernel(StepParams P, int f0, in
     abs_frame_body(P, p, f0, f1, f2);
 }
 
-__global__ void __launch_bounds__(256) abs_frame_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, int f0, int f1, int f2)
+__global__ void __launch_bounds__(256) abs_frame_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S,
+                                                       int f0, int f1, int f2)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (point_tile(sP, w, p, rr)) abs_frame_body(sP, p, f0, f1, f2);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [=](const StepParams& P, const Pt& p) { abs_frame_body(P, p, f0, f1, f2); });
 }
 
 // --------------------------------------------------------------------------
@@ -1073,7 +1004,7 @@ __global__ void set_counter_kernel(int* c, int v) { *c = v; }
 
 void launch_set_counter(int* c, int v, cudaStream_t s) { set_counter_kernel<<<1, 1, 0, s>>>(c, v); }
 
-using BatchKernel = void (*)(const StepParams*, const BatchTile*);
+using BatchKernel = void (*)(const StepParams*, const BatchTile*, BatchSched);
 
 BatchKernel batch_kernel_for(int eq, int pass, int H)
 {
@@ -1100,17 +1031,28 @@ BatchKernel batch_kernel_for(int eq, int pass, int H)
     }
 }
 
-void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const BatchTile* tiles, int ntiles, cudaStream_t s)
+void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const BatchTile* tiles, const BatchSched& S, int grid,
+                       cudaStream_t s)
 {
     BatchKernel k = batch_kernel_for(eq, pass, H);
-    if (k && ntiles > 0) k<<<ntiles, dim3(32, 8, 1), 0, s>>>(Ps, tiles);
+    if (k && S.ntiles > 0) k<<<grid, dim3(32, 8, 1), 0, s>>>(Ps, tiles, S);
 }
 
-void launch_batch_aux(const StepParams* Ps, const BatchTile* tiles, int ntiles, int f0, int f1, int f2,
+void launch_batch_aux(const StepParams* Ps, const BatchTile* tiles, const BatchSched& S, int grid, int f0, int f1, int f2,
                       const SrcRecParams* Qs, int* counters, int nshots, bool abs, cudaStream_t s)
 {
-    if (abs && ntiles > 0) abs_frame_batch<<<ntiles, dim3(32, 8, 1), 0, s>>>(Ps, tiles, f0, f1, f2);
+    if (abs && S.ntiles > 0) abs_frame_batch<<<grid, dim3(32, 8, 1), 0, s>>>(Ps, tiles, S, f0, f1, f2);
     if (nshots > 0) srcrec_batch<<<nshots, 512, 0, s>>>(Qs, counters);
+}
+
+int batch_blocks_per_sm(int eq, int H)
+{
+    BatchKernel k = batch_kernel_for(eq, 0, H), k2 = batch_kernel_for(eq, 1, H);
+    int a = 0, b = 0;
+    if (!k || !k2) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, 256, 0) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k2, 256, 0) != cudaSuccess) return 0;
+    return a < b ? a : b;
 }
 
 __global__ void set_counters_kernel(int* c, int n, int v)

@@ -114,6 +114,51 @@ __device__ __forceinline__ bool point_tile(const StepParams& P, const BatchTile&
     return true;
 }
 
+// Shared-memory copy of a shot's StepParams in a batched kernel (raw storage:
+// StepParams has default member initialisers, which a __shared__ object
+// cannot run; load_params fills every byte).
+#define BATCH_SHARED_PARAMS(name)                                                  \
+    __shared__ __align__(16) unsigned char name##_mem[sizeof(StepParams)];          \
+    StepParams& name = *reinterpret_cast<StepParams*>(name##_mem)
+
+// Persistent batched launches: the block walks the work list with a grid
+// stride; the parameters of a tile's shot are staged in shared memory when
+// the shot changes (every thread first leaves the previous shot's). A tile of
+// S.cols x S.rows points is covered by the 32 x 8 block in column groups of
+// 32 and row groups of 8.
+template <class Body>
+__device__ __forceinline__ void batch_loop(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, const BatchSched& S,
+                                           StepParams& sP, Body body)
+{
+    int shot = -1;
+    for (int t = blockIdx.x; t < S.ntiles; t += gridDim.x) {
+        const BatchTile w = W[t];
+        if (w.shot != shot) {
+            __syncthreads();
+            load_params(sP, Ps + w.shot);
+            shot = w.shot;
+        }
+        for (int xg = 0; xg < S.cols; xg += 32) {
+            const int x = w.x0 + xg + static_cast<int>(threadIdx.x);
+            for (int rr = 0; rr < S.rows; rr += 8) {
+                const int r = w.r0 + rr + static_cast<int>(threadIdx.y);
+                if (x >= sP.NX || r >= sP.NY * sP.NZ) continue;
+                Pt p;
+                p.x = x;
+                if (sP.NZ == 1) {   // 2-D: no division
+                    p.y = r;
+                    p.z = 0;
+                } else {
+                    p.y = r / sP.NZ;
+                    p.z = r - p.y * sP.NZ;
+                }
+                p.i = p.x + (long long)sP.NX * (p.z + (long long)sP.NZ * p.y);
+                body(sP, p);
+            }
+        }
+    }
+}
+
 // psi indices along x / y / z for point p
 __device__ __forceinline__ long long pix(const StepParams& P, const Pt& p, int s) { return s + (long long)P.cx.ns * (p.z + (long long)P.NZ * p.y); }
 __device__ __forceinline__ long long piy(const StepParams& P, const Pt& p, int s) { return p.x + (long long)P.NX * (p.z + (long long)P.NZ * s); }

@@ -129,6 +129,13 @@ constexpr int kTileRows = 32;
 struct BatchTile {
     int shot, x0, r0, pad;
 };
+// Schedule of a batched launch: the work list holds `ntiles` tiles of
+// `cols` (a multiple of 32) x `rows` (a multiple of 8) points; the launch's
+// blocks walk the list with a grid stride (one block per tile when the grid
+// equals ntiles, persistent blocks when it is smaller).
+struct BatchSched {
+    int ntiles, cols, rows, pad;
+};
 
 struct PrepParams {
     int NX, NY, NZ;
@@ -146,9 +153,12 @@ cudaError_t launch_step_kernel(StepKernel k, dim3 grid, dim3 block, const StepPa
 void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s, bool dep = false);
 void launch_set_counter(int* c, int v, cudaStream_t s);
 void launch_set_counters(int* c, int n, int v, cudaStream_t s);
-void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const BatchTile* tiles, int ntiles, cudaStream_t s);
-void launch_batch_aux(const StepParams* Ps, const BatchTile* tiles, int ntiles, int f0, int f1, int f2,
+void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const BatchTile* tiles, const BatchSched& S, int grid,
+                       cudaStream_t s);
+void launch_batch_aux(const StepParams* Ps, const BatchTile* tiles, const BatchSched& S, int grid, int f0, int f1, int f2,
                       const SrcRecParams* Qs, int* counters, int nshots, bool abs, cudaStream_t s);
+// resident blocks per SM of the batched kernels of an equation (the smaller of the two passes)
+int batch_blocks_per_sm(int eq, int H);
 void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s, bool dep = false);
 void launch_finite(const float* a, long long n, int* flag, cudaStream_t s);
 void k_modulus(PrepParams G, const float* rho, const float* v, const float* tau, float sum, int clamp, float* out, cudaStream_t s);
