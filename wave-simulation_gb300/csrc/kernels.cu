@@ -781,6 +781,22 @@ __global__ void __launch_bounds__(512) srcrec_kernel(SrcRecParams Q, int* tcount
     srcrec_body(Q, tcounter);
 }
 
+// Many receivers: the sources (and the step counter) in one block, then the
+// receivers over a grid, so the gather is not one block's serial loop of
+// dependent loads. The receiver launch reads the step the source launch
+// advanced the counter past.
+__global__ void __launch_bounds__(512) sources_kernel(SrcRecParams Q, int* tcounter)
+{
+    dependent_launch_prologue();
+    srcrec_body(Q, tcounter, false);
+}
+
+__global__ void __launch_bounds__(256) receivers_kernel(SrcRecParams Q, const int* tcounter)
+{
+    dependent_launch_prologue();
+    receivers_body(Q, *tcounter - 1, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
 // one block per shot, each with its own step counter
 __global__ void __launch_bounds__(512) srcrec_batch(const SrcRecParams* __restrict__ Qs, int* tcounters)
 {
@@ -1085,9 +1101,16 @@ cudaError_t launch_step_kernel(StepKernel k, dim3 grid, dim3 block, const StepPa
     return launch_maybe_dependent(k, grid, block, dep, s, P);
 }
 
-void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s, bool dep)
+int launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s, bool dep)
 {
+    if (Q.nrec > kSplitReceivers) {
+        launch_maybe_dependent(sources_kernel, dim3(1), dim3(512), dep, s, Q, tcounter);
+        const int blocks = (Q.nrec + 255) / 256;
+        launch_maybe_dependent(receivers_kernel, dim3(blocks), dim3(256), dep, s, Q, static_cast<const int*>(tcounter));
+        return 2;
+    }
     launch_maybe_dependent(srcrec_kernel, dim3(1), dim3(512), dep, s, Q, tcounter);
+    return 1;
 }
 
 void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s, bool dep)

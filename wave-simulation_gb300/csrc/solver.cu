@@ -286,8 +286,7 @@ void launch_step(wave_handle* h)
         bool done = false;
         h->launches += wave::vargrid_launch_step(h, h->dependentLaunch, nullptr, &done);
         if (!done) {
-            launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
-            h->launches += 1;
+            h->launches += launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
         }
         return;
     }
@@ -302,8 +301,7 @@ void launch_step(wave_handle* h)
         h->launches += 1;
     }
     if (!h->sp.sr.on) {
-        launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
-        h->launches += 1;
+        h->launches += launch_srcrec(h->sq, h->tcounter, h->stream, h->dependentLaunch);
     }
     if (h->decompType) h->launches += wave::decompose_after_step(h);
 }
@@ -320,8 +318,7 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
         cudaEventRecord(c, h->stream);
         ev.push_back(a); ev.push_back(b); ev.push_back(c);
         if (!done) {
-            launch_srcrec(h->sq, h->tcounter, h->stream);
-            h->launches += 1;
+            h->launches += launch_srcrec(h->sq, h->tcounter, h->stream);
         }
         return;
     }
@@ -338,8 +335,7 @@ void launch_step_timed(wave_handle* h, std::vector<cudaEvent_t>& ev)
         h->launches += 1;
     }
     if (!h->sp.sr.on) {
-        launch_srcrec(h->sq, h->tcounter, h->stream);
-        h->launches += 1;
+        h->launches += launch_srcrec(h->sq, h->tcounter, h->stream);
     }
     if (h->decompType) h->launches += wave::decompose_after_step(h);
 }

@@ -252,7 +252,27 @@ __device__ __forceinline__ float* field_of(const SrcRecParams& Q, int type)
     }
 }
 
-__device__ __forceinline__ void srcrec_body(const SrcRecParams& Q, int* tcounter)
+// receivers of step t, threads [first, first + stride) ... (SourceReceiverImpl.cpp:12-19)
+__device__ __forceinline__ void receivers_body(const SrcRecParams& Q, int t, int first, int stride)
+{
+    const bool elasticP = (Q.eq == WAVE_EQ_ELASTIC || Q.eq == WAVE_EQ_VISCOELASTIC);
+    for (int r = first; r < Q.nrec; r += stride) {
+        const long long i = Q.ridx[r];
+        const int type = Q.rtype[r];
+        float v;
+        if (Q.eq < WAVE_EQ_TMEM && type == WAVE_TYPE_P && elasticP) {
+            v = Q.f[F_SXX][i];
+            v += Q.f[F_SYY][i];
+            if (Q.is3d) { v += Q.f[F_SZZ][i]; v /= 3.0f; }
+            else v *= 0.5f;
+        } else {
+            v = field_of(Q, type)[i];
+        }
+        Q.seis[(long long)r * Q.nt + t] = v;
+    }
+}
+
+__device__ __forceinline__ void srcrec_body(const SrcRecParams& Q, int* tcounter, bool withReceivers = true)
 {
     const int t = *tcounter;
     const bool elasticP = (Q.eq == WAVE_EQ_ELASTIC || Q.eq == WAVE_EQ_VISCOELASTIC);
@@ -271,20 +291,7 @@ __device__ __forceinline__ void srcrec_body(const SrcRecParams& Q, int* tcounter
         }
         __syncthreads();
     }
-    for (int r = threadIdx.x; r < Q.nrec; r += blockDim.x) {
-        const long long i = Q.ridx[r];
-        const int type = Q.rtype[r];
-        float v;
-        if (Q.eq < WAVE_EQ_TMEM && type == WAVE_TYPE_P && elasticP) {
-            v = Q.f[F_SXX][i];
-            v += Q.f[F_SYY][i];
-            if (Q.is3d) { v += Q.f[F_SZZ][i]; v /= 3.0f; }
-            else v *= 0.5f;
-        } else {
-            v = field_of(Q, type)[i];
-        }
-        Q.seis[(long long)r * Q.nt + t] = v;
-    }
+    if (withReceivers) receivers_body(Q, t, threadIdx.x, blockDim.x);
     __syncthreads();
     if (threadIdx.x == 0) *tcounter = t + 1;
 }

@@ -150,7 +150,10 @@ using StepKernel = void (*)(StepParams);
 StepKernel kernel_for(int eq, int pass, int H);
 // dep: programmatic dependent launch (the kernel waits for its predecessor in-kernel)
 cudaError_t launch_step_kernel(StepKernel k, dim3 grid, dim3 block, const StepParams& P, bool dep, cudaStream_t s);
-void launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s, bool dep = false);
+// sources and receivers of one step; returns the launches made (2 when the
+// receivers, more than kSplitReceivers, get a grid of their own)
+constexpr int kSplitReceivers = 1024;
+int launch_srcrec(const SrcRecParams& Q, int* tcounter, cudaStream_t s, bool dep = false);
 void launch_set_counter(int* c, int v, cudaStream_t s);
 void launch_set_counters(int* c, int n, int v, cudaStream_t s);
 void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const BatchTile* tiles, const BatchSched& S, int grid,
