@@ -67,12 +67,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
         : "memory");
     return ok != 0;
 }
-// bounded wait: gives up after 2^20 polls (well under a second of waiting for
-// copies that take microseconds); the caller reports it
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1u << 20)
+// try_wait with a suspend-time hint: a thread whose phase is not complete
+// sleeps until it completes or `ns` nanoseconds pass, instead of returning at
+// once, so waiting warps do not spin through the issue slots of the warps
+// that compute.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t ns)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: gives up after `limit` sleeps of at most 1 us (2^17: about
+// 0.13 s of waiting for copies that take microseconds); the caller reports it
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = 1u << 17)
 {
     for (uint32_t i = 0; i < limit; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait_sleep(bar, parity, 1000u)) return true;
     return false;
 }
 __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int z, int y)
