@@ -65,6 +65,39 @@ void spmv_add(const CSR<T>& A, const std::vector<T>& x, std::vector<T>& y)
 }
 
 template <class T>
+struct AverageTranspose {
+    const Sim<T>& s;
+    const idx_t N;
+    explicit AverageTranspose(const Sim<T>& sim) : s(sim), N(sim.g.N()) {}
+    // A^T y for the averaging operator `avg` (out = avg(in)), whose row r reads
+    // at most the 2 x 2 block at r (x, x+1) x (y, y+1): probed with one unit
+    // pattern per (x mod 2, y mod 2) colour, so the edge fallbacks come from
+    // the oracle's own averaging code.
+    template <class Avg>
+    void avgT(Avg avg, const std::vector<T>& y, std::vector<T>& out) const
+    {
+        std::vector<T> e(N), col(N);
+        for (int cx = 0; cx < 2; ++cx)
+            for (int cy = 0; cy < 2; ++cy) {
+                for (idx_t k = 0; k < N; ++k) {
+                    idx_t x, yy, z;
+                    s.g.coord(k, x, yy, z);
+                    e[k] = (x % 2 == cx && yy % 2 == cy) ? T(1) : T(0);
+                }
+                avg(e.data(), col.data());   // col[r] = A[r, k_c(r)]
+                for (idx_t r = 0; r < N; ++r) {
+                    if (col[r] == T(0)) continue;
+                    idx_t x, yy, z;
+                    s.g.coord(r, x, yy, z);
+                    const idx_t kx = (x % 2 == cx) ? x : x + 1, ky = (yy % 2 == cy) ? yy : yy + 1;
+                    out[s.g.index(kx, ky, 0)] += col[r] * y[r];
+                }
+            }
+    }
+
+};
+
+template <class T>
 struct ElasticAdjoint2D {
     Sim<T>& s;
     const idx_t N;
@@ -263,31 +296,8 @@ struct ElasticAdjoint2D {
         return J;
     }
 
-    // A^T y for the averaging operator `avg` (out = avg(in)), whose row r reads
-    // at most the 2 x 2 block at r (x, x+1) x (y, y+1): probed with one unit
-    // pattern per (x mod 2, y mod 2) colour, so the edge fallbacks come from
-    // the oracle's own averaging code.
     template <class Avg>
-    void avgT(Avg avg, const std::vector<T>& y, std::vector<T>& out) const
-    {
-        std::vector<T> e(N), col(N);
-        for (int cx = 0; cx < 2; ++cx)
-            for (int cy = 0; cy < 2; ++cy) {
-                for (idx_t k = 0; k < N; ++k) {
-                    idx_t x, yy, z;
-                    s.g.coord(k, x, yy, z);
-                    e[k] = (x % 2 == cx && yy % 2 == cy) ? T(1) : T(0);
-                }
-                avg(e.data(), col.data());   // col[r] = A[r, k_c(r)]
-                for (idx_t r = 0; r < N; ++r) {
-                    if (col[r] == T(0)) continue;
-                    idx_t x, yy, z;
-                    s.g.coord(r, x, yy, z);
-                    const idx_t kx = (x % 2 == cx) ? x : x + 1, ky = (yy % 2 == cy) ? yy : yy + 1;
-                    out[s.g.index(kx, ky, 0)] += col[r] * y[r];
-                }
-            }
-    }
+    void avgT(Avg avg, const std::vector<T>& y, std::vector<T>& out) const { AverageTranspose<T>(s).avgT(avg, y, out); }
 
     // the model preparation's transpose: (M, mu, muXY, irx, iry) -> (vp, vs, rho)
     void chain(const std::vector<T>& vp, const std::vector<T>& vs, const std::vector<T>& rho, const std::vector<T>& gM,
@@ -316,6 +326,161 @@ struct ElasticAdjoint2D {
             gvs[k] = unclamped ? gmuc[k] * T(2) * rho[k] * vs[k] : T(0);
             grho[k] = gM[k] * vp[k] * vp[k] + (unclamped ? gmuc[k] * vs[k] * vs[k] : T(0)) + grhoAvg[k];
         }
+    }
+};
+
+
+// Discrete adjoint of the oracle's lossless 2-D TMz step (Sim<T>::stepTM,
+// restating FD2Dtmem::run, ForwardSolver2Dtmem.cpp:108-174, with CPML and the
+// ABS taper): the gradient of J = 1/2 sum (d - d_obs)^2 (Ez receivers) with
+// respect to eps_r, sigma and mu_r. Per step, from X_t and X_{t+1}:
+//   a1' = Dyf ez + P(ezy)   a2' = Dxf ez + P(ezx)
+//   hx' = hx - iMyz a1'     hy' = hy + iMxz a2'          (before the taper)
+//   c1' = Dxb hy' + P(hyx)  c2' = Dyb hx' + P(hxy)
+//   ez  <- Ca ez + Cb (c1' - c2'), then the taper on ez, hx, hy
+// with Ca = (1 - k) / (1 + k), Cb = (1 / eps) / (1 + k), k = sigma DT / (2 eps),
+// eps = eps_r eps0 (TMEM.cpp:230-241, ForwardSolverEM.cpp:14-67) and
+// iMxz, iMyz the inverse 2-point averages of mu = mu_r mu0 (TMEM.cpp:366-374).
+template <class T>
+struct TMAdjoint2D {
+    Sim<T>& s;
+    const idx_t N;
+    CSR<T> DxfT, DxbT, DyfT, DybT;
+    explicit TMAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    {
+        if (s.is3d || s.eq != WAVE_EQ_TMEM) throw std::invalid_argument("oracle adjoint: lossless 2-D TMz only");
+        DxfT = transpose(s.Dxf);
+        DxbT = transpose(s.Dxb);
+        DyfT = transpose(s.Dyf);
+        DybT = transpose(s.Dyb);
+    }
+    struct State {
+        std::map<std::string, std::vector<T>> F, psi;
+    };
+    const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
+    {
+        auto it = x.psi.find(n);
+        return it == x.psi.end() ? zero : it->second;
+    }
+    void cpmlT(std::vector<T>& lc, std::vector<T>& lp, const std::vector<T>& a, const std::vector<T>& b) const
+    {
+        if (!s.useCpml) return;
+        for_n(N, [&](idx_t i) {
+            const T c = (T(1) + a[i]) * lc[i] + a[i] * lp[i];
+            lp[i] = b[i] * (lc[i] + lp[i]);
+            lc[i] = c;
+        });
+    }
+
+    double run(const std::vector<T>& epsr, const std::vector<T>& sigma, const std::vector<T>& mur, const T* dobs, int K,
+               T* geps, T* gsig, T* gmu)
+    {
+        const int NT = s.NT;
+        const size_t nrec = s.rec.idx.size();
+        for (size_t r = 0; r < nrec; ++r)
+            if (s.rec.type[r] != WAVE_TYPE_EZ) throw std::invalid_argument("oracle TMz adjoint: Ez receivers only");
+        const std::vector<T> zero(N, T(0));
+        s.reset();
+        std::vector<State> ck;
+        for (int t = 0; t < NT; ++t) {
+            if (t % K == 0) ck.push_back({s.F, s.psi});
+            s.step(t);
+        }
+        std::vector<T> res(nrec * static_cast<size_t>(NT));
+        double J = 0;
+        for (size_t k = 0; k < res.size(); ++k) {
+            res[k] = s.seis[k] - dobs[k];
+            J += 0.5 * static_cast<double>(res[k]) * static_cast<double>(res[k]);
+        }
+        std::vector<T> lhx(N, 0), lhy(N, 0), lez(N, 0);
+        std::map<std::string, std::vector<T>> lp;
+        for (const char* n : {"ezy", "ezx", "hyx", "hxy"}) lp[n].assign(N, 0);
+        std::vector<T> gCa(N, 0), gCb(N, 0), gMxz(N, 0), gMyz(N, 0);
+        std::vector<T> a1(N), a2(N), c1(N), c2(N), hxp(N), hyp(N), la1(N), la2(N), lc1(N), lc2(N);
+        const int nseg = static_cast<int>(ck.size());
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int t0 = seg * K, t1 = std::min(NT, t0 + K);
+            std::vector<State> X;
+            s.F = ck[seg].F;
+            s.psi = ck[seg].psi;
+            X.push_back({s.F, s.psi});
+            for (int t = t0; t < t1; ++t) {
+                s.step(t);
+                X.push_back({s.F, s.psi});
+            }
+            for (int t = t1 - 1; t >= t0; --t) {
+                const State& X0 = X[t - t0];
+                const State& X1 = X[t - t0 + 1];
+                s.Dyf.spmv(X0.F.at("ez").data(), a1.data());
+                s.Dxf.spmv(X0.F.at("ez").data(), a2.data());
+                const auto& pezy = psiOf(X1, "ezy", zero);
+                const auto& pezx = psiOf(X1, "ezx", zero);
+                const auto& hx1 = X1.F.at("hx");
+                const auto& hy1 = X1.F.at("hy");
+                for_n(N, [&](idx_t i) {
+                    a1[i] += pezy[i];
+                    a2[i] += pezx[i];
+                    const T d = s.useAbs ? s.damping[i] : T(1);
+                    hxp[i] = hx1[i] / d;
+                    hyp[i] = hy1[i] / d;
+                });
+                s.Dxb.spmv(hyp.data(), c1.data());
+                s.Dyb.spmv(hxp.data(), c2.data());
+                const auto& phyx = psiOf(X1, "hyx", zero);
+                const auto& phxy = psiOf(X1, "hxy", zero);
+                for_n(N, [&](idx_t i) { c1[i] += phyx[i]; c2[i] += phxy[i]; });
+                for (size_t r = 0; r < nrec; ++r) lez[s.rec.idx[r]] += res[r * NT + t];
+                if (s.useAbs)
+                    for (auto* v : {&lez, &lhx, &lhy}) {
+                        auto& w = *v;
+                        for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
+                    }
+                // ez <- Ca ez + Cb (c1' - c2')
+                const auto& ez0 = X0.F.at("ez");
+                for_n(N, [&](idx_t i) {
+                    lc1[i] = s.CbZ[i] * lez[i];
+                    lc2[i] = -s.CbZ[i] * lez[i];
+                    gCa[i] += lez[i] * ez0[i];
+                    gCb[i] += lez[i] * (c1[i] - c2[i]);
+                    lez[i] *= s.CaZ[i];
+                });
+                cpmlT(lc1, lp["hyx"], s.ax, s.bx);
+                cpmlT(lc2, lp["hxy"], s.ay, s.by);
+                spmv_add(DxbT, lc1, lhy);
+                spmv_add(DybT, lc2, lhx);
+                // hx' = hx - iMyz a1', hy' = hy + iMxz a2'
+                for_n(N, [&](idx_t i) {
+                    la1[i] = -s.invMuYZ[i] * lhx[i];
+                    la2[i] = s.invMuXZ[i] * lhy[i];
+                    gMyz[i] -= lhx[i] * a1[i];
+                    gMxz[i] += lhy[i] * a2[i];
+                });
+                cpmlT(la1, lp["ezy"], s.ayh, s.byh);
+                cpmlT(la2, lp["ezx"], s.axh, s.bxh);
+                spmv_add(DyfT, la1, lez);
+                spmv_add(DxfT, la2, lez);
+            }
+        }
+        // Ca, Cb -> eps, sigma; iMxz, iMyz -> mu
+        const T eps0 = static_cast<T>(8.8541878176e-12), mu0 = static_cast<T>(1.2566370614e-6);
+        const T DT = s.DT;
+        for (idx_t i = 0; i < N; ++i) {
+            const T e = epsr[i] * eps0, sg = sigma[i];
+            const T k = sg * DT / (T(2) * e), q = T(1) + k;
+            const T dCa_de = T(2) * k / (e * q * q), dCa_ds = -T(2) / (q * q) * DT / (T(2) * e);
+            const T dCb_de = -T(1) / (e * e * q) + k / (e * e * q * q), dCb_ds = -(T(1) / e) / (q * q) * DT / (T(2) * e);
+            geps[i] = eps0 * (gCa[i] * dCa_de + gCb[i] * dCb_de);
+            gsig[i] = gCa[i] * dCa_ds + gCb[i] * dCb_ds;
+        }
+        std::vector<T> y(N), gm(N, 0);
+        AverageTranspose<T> probe(s);
+        for_n(N, [&](idx_t r) { y[r] = -gMxz[r] * s.invMuXZ[r] * s.invMuXZ[r]; });
+        probe.avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::X, in, out); }, y, gm);
+        for_n(N, [&](idx_t r) { y[r] = -gMyz[r] * s.invMuYZ[r] * s.invMuYZ[r]; });
+        probe.avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::Y, in, out); }, y, gm);
+        for (idx_t i = 0; i < N; ++i) gmu[i] = gm[i] * mu0;
+        (void)mur;
+        return J;
     }
 };
 

@@ -277,6 +277,7 @@ def lib():
         L.refcpu_last_error.restype = ctypes.c_char_p
         L.refcpu_set_threads.argtypes = [ctypes.c_int]
         L.refcpu_adjoint_elastic2d.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P, P, P]
+        L.refcpu_adjoint_tmz.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P, P, P]
         _lib = L
     return _lib
 
@@ -356,17 +357,20 @@ class Oracle:
 
     def adjoint_gradient(self, dobs: np.ndarray, checkpoint_every: int = 50):
         """Misfit 1/2 sum (d - dobs)^2 and its gradients with respect to vp, vs
-        and rho (2-D elastic), by the oracle's own discrete adjoint
-        (adjoint_impl.hpp) in this oracle's value type."""
+        and rho (2-D elastic) or eps_r, sigma and mu_r (lossless 2-D TMz), by
+        the oracle's own discrete adjoint (adjoint_impl.hpp) in this oracle's
+        value type."""
         n = self.cfg.NX * self.cfg.NY
-        m = [np.ascontiguousarray(self.model[k], dtype=np.float64) for k in ("vp", "vs", "rho")]
+        em = self.cfg.equation >= 5
+        keys = ("eps_r", "sigma", "mu_r") if em else ("vp", "vs", "rho")
+        m = [np.ascontiguousarray(self.model[k], dtype=np.float64) for k in keys]
         d = np.ascontiguousarray(dobs, dtype=np.float64)
         if d.size != len(self._ridx) * self.nt:
             raise ValueError("dobs must hold n_receivers x NT samples")
         g = [np.zeros(n, dtype=np.float64) for _ in range(3)]
         J = ctypes.c_double(0)
-        if lib().refcpu_adjoint_elastic2d(self.h, *(_ptr(a) for a in m), _ptr(d), int(checkpoint_every), ctypes.byref(J),
-                                          *(_ptr(a) for a in g)) != 0:
+        fn = lib().refcpu_adjoint_tmz if em else lib().refcpu_adjoint_elastic2d
+        if fn(self.h, *(_ptr(a) for a in m), _ptr(d), int(checkpoint_every), ctypes.byref(J), *(_ptr(a) for a in g)) != 0:
             raise RuntimeError(lib().refcpu_last_error().decode())
         return J.value, g[0], g[1], g[2]
 

@@ -211,6 +211,33 @@ int refcpu_adjoint_elastic2d(void* hv, const double* vp, const double* vs, const
     }
 }
 
+// The same for a lossless 2-D TMz simulation (Ez receivers): gradients with
+// respect to eps_r, sigma and mu_r (adjoint_impl.hpp, TMAdjoint2D).
+int refcpu_adjoint_tmz(void* hv, const double* epsr, const double* sigma, const double* mur, const double* dobs, int K,
+                       double* misfit, double* geps, double* gsig, double* gmu)
+{
+    auto* h = static_cast<Handle*>(hv);
+    auto run = [&](auto* s) -> int {
+        using T = typename std::decay_t<decltype(s->M)>::value_type;
+        const size_t N = s->g.N(), nd = s->rec.idx.size() * static_cast<size_t>(s->NT);
+        std::vector<T> E(epsr, epsr + N), S(sigma, sigma + N), U(mur, mur + N), D(dobs, dobs + nd), a(N), b(N), c(N);
+        refcpu::TMAdjoint2D<T> adj(*s);
+        *misfit = adj.run(E, S, U, D.data(), K, a.data(), b.data(), c.data());
+        std::copy(a.begin(), a.end(), geps);
+        std::copy(b.begin(), b.end(), gsig);
+        std::copy(c.begin(), c.end(), gmu);
+        return 0;
+    };
+    try {
+        if (K < 1) throw std::invalid_argument("checkpoint interval must be >= 1");
+        if (h->is_double) return run(static_cast<refcpu::Sim<double>*>(h->sim));
+        return run(static_cast<refcpu::Sim<float>*>(h->sim));
+    } catch (std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
+}
+
 void refcpu_destroy(void* hv)
 {
     auto* h = static_cast<Handle*>(hv);
