@@ -369,10 +369,16 @@ int wave_envelope(float* data, int64_t ntr, int64_t nt, int mem);
 int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_type, int mem);
 
 /* ---- adjoint gradient (new; the reference's inversion is a separate project) ----
- * Gradient of J = 1/2 sum over receivers and steps of (d - d_obs)^2 with
- * respect to vp, vs and rho, by the discrete adjoint of the 2-D elastic time
- * step (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297) with CPML or no
- * damping boundary (free surface and ABS: WAVE_ERR_UNSUPPORTED). Runs the
+ * Gradient of J = 1/2 sum over receivers and steps of (d - d_obs)^2 by the
+ * discrete adjoint of the time step:
+ *  - 2-D elastic (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297) with
+ *    CPML, ABS or no damping boundary and with or without the free surface:
+ *    grad_vp, grad_vs, grad_rho receive dJ/dvp, dJ/dvs, dJ/drho;
+ *  - lossless 2-D TMz (FD2Dtmem::run, ForwardSolver2Dtmem.cpp:108-174) with
+ *    Ez sources and receivers, CPML, ABS or no damping boundary: the three
+ *    outputs receive dJ/deps_r, dJ/dsigma, dJ/dmu_r (the model's relative
+ *    permittivity, conductivity and relative permeability);
+ * other equations return WAVE_ERR_UNSUPPORTED. Runs the
  * forward over all NT steps from a zero state (the handle's sources and
  * receivers; seismograms are left as computed), saving the state every
  * `checkpoint_every` steps, then the backward sweep, recomputing each

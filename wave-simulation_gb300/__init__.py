@@ -513,9 +513,10 @@ class ForwardSolver:
         _check(self.h, lib().wave_set_decomposition(self.h, int(kind)))
 
     def adjoint_gradient(self, dobs, checkpoint_every: int = 50):
-        """Misfit J = 1/2 ||d - d_obs||^2 and its gradient w.r.t. (vp, vs, rho)
-        by the discrete adjoint (2-D elastic). d_obs: n_receivers x NT (numpy
-        or torch cuda). Returns (J, g_vp, g_vs, g_rho) as float64 / numpy arrays."""
+        """Misfit J = 1/2 ||d - d_obs||^2 and its gradient by the discrete
+        adjoint: w.r.t. (vp, vs, rho) for 2-D elastic, (eps_r, sigma, mu_r) for
+        lossless 2-D TMz. d_obs: n_receivers x NT (numpy or torch cuda).
+        Returns (J, g1, g2, g3) as float64 / numpy arrays."""
         d = _f32(dobs)
         pd, mem = _ptr(d)
         n = self.cfg.N

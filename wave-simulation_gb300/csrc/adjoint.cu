@@ -23,6 +23,14 @@
 // averages, harmonic 4-point shear average with its edge fallbacks and vacuum
 // rules; Modelparameter.cpp:336-639, ModelparameterSeismic.cpp:131-136, 421-432).
 //
+// The lossless 2-D TMz step (FD2Dtmem::run, ForwardSolver2Dtmem.cpp:108-174)
+// has its own three kernels per step on the same driver:
+//   hx' = hx - iMyz (Dyf ez + P_ezy)'   hy' = hy + iMxz (Dxf ez + P_ezx)'
+//   ez' = Ca ez + Cb ((Dxb hy' + P_hyx)' - (Dyb hx' + P_hxy)'), then the ABS taper,
+// and a last kernel maps dJ/dCa, dJ/dCb, dJ/diMxz, dJ/diMyz to eps_r, sigma
+// and mu_r (Ca, Cb of ForwardSolverEM.cpp:14-67 with eps = eps_r eps0; the
+// inverse 2-point mu averages of TMEM.cpp:366-374).
+//
 // Checkpointing: the forward run saves the state every K steps; the backward
 // sweep recomputes each K-step segment into a buffer of K+1 states and walks
 // it backwards. The reference has no adjoint (its inversion lives in a
@@ -59,7 +67,8 @@ struct AdjShot {
     const int* rtype;
     const float* res;            // residual d - d_obs, nrec x nt
     int nrec, nt;
-    float* vprime[2];            // vx', vy' of the current step (null: the saved state's vx, vy are they)
+    int tm;                      // 1: lossless 2-D TMz (parts: hx, hy, ez; psi ezy, ezx, hyx, hxy)
+    float* vprime[2];            // vx', vy' (TMz: hx', hy') of the current step (null: the saved state's are they)
     const long long* sidx;       // sources (velocity sources are taken out of v')
     const int* stype;
     const float* signals;        // nsrc x nt
@@ -246,6 +255,81 @@ __device__ __forceinline__ void adj_sigma_body(const StepParams& P, const AdjSho
     A.lf[3][i] += derivT<H, true>(A.T[7], i, sy, p.y, DyfS);
 }
 
+// ---- lossless 2-D TMz --------------------------------------------------------
+// parts of a TMz state in the view: AV_VX = hx, AV_VY = hy, AV_SXX = ez,
+// AV_P1..AV_P4 = psi of ezy, ezx, hyx, hxy; lf[0..2] = adjoints of hx, hy, ez;
+// T[0..3] = adjoints of c1, c2, a1, a2; g[0..3] = dJ/dCa, dJ/dCb, dJ/diMyz, dJ/diMxz
+
+// E-update transpose at step n
+template <int H>
+__device__ __forceinline__ void adj_tm_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float* hx1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
+    const float* hy1 = A.vprime[1] ? A.vprime[1] : X1 + A.off[AV_VY];
+    const Slabs S = slabs_of(P, p);
+    float c1 = deriv<H, false>(hy1, i, 1, p.x, P.Dxb);
+    float c2 = deriv<H, false>(hx1, i, sy, p.y, P.Dyb);
+    if (S.sx >= 0) c1 += X1[A.off[AV_P3] + S.px];
+    if (S.sy >= 0) c2 += X1[A.off[AV_P4] + S.py];
+    float lez = A.lf[2][i];
+    if (P.abs) {
+        // the taper multiplied ez, hx and hy last: their adjoints first
+        const float d = absDamp(P, p);
+        lez *= d;
+        A.lf[0][i] *= d;
+        A.lf[1][i] *= d;
+    }
+    const float ca = __ldg(P.m[M_CAZ] + i), cb = __ldg(P.m[M_CBZ] + i);
+    float l1 = cb * lez, l2 = -l1;
+    A.g[0][i] += lez * X0[A.off[AV_SXX] + i];
+    A.g[1][i] += lez * (c1 - c2);
+    A.lf[2][i] = ca * lez;
+    if (S.sx >= 0) cpml_adj(l1, A.lpsi[2] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // hyx: x, full profile
+    if (S.sy >= 0) cpml_adj(l2, A.lpsi[3] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // hxy: y, full profile
+    A.T[0][i] = l1;
+    A.T[1][i] = l2;
+}
+
+// H-update transpose at step n (after the E transpose of every point)
+template <int H>
+__device__ __forceinline__ void adj_tm_h_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float lhy = A.lf[1][i] + derivT<H, false>(A.T[0], i, 1, p.x, P.Dxb);
+    const float lhx = A.lf[0][i] + derivT<H, false>(A.T[1], i, sy, p.y, P.Dyb);
+    const float* ez0 = X0 + A.off[AV_SXX];
+    const Slabs S = slabs_of(P, p);
+    float a1 = deriv<H, true>(ez0, i, sy, p.y, P.Dyf);
+    float a2 = deriv<H, true>(ez0, i, 1, p.x, P.Dxf);
+    if (S.sy >= 0) a1 += X1[A.off[AV_P1] + S.py];
+    if (S.sx >= 0) a2 += X1[A.off[AV_P2] + S.px];
+    const float imyz = __ldg(P.m[M_IMUYZ] + i), imxz = __ldg(P.m[M_IMUXZ] + i);
+    float l1 = -imyz * lhx, l2 = imxz * lhy;
+    A.g[2][i] += -lhx * a1;
+    A.g[3][i] += lhy * a2;
+    if (S.sy >= 0) cpml_adj(l1, A.lpsi[0] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // ezy: y, half profile
+    if (S.sx >= 0) cpml_adj(l2, A.lpsi[1] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // ezx: x, half profile
+    A.T[2][i] = l1;
+    A.T[3][i] = l2;
+    A.lf[0][i] = lhx;
+    A.lf[1][i] = lhy;
+}
+
+// transposed H-update derivatives of ez
+template <int H>
+__device__ __forceinline__ void adj_tm_ez_body(const StepParams& P, const AdjShot& A, const Pt& p)
+{
+    const long long i = p.i, sy = P.NX;
+    float u = derivT<H, true>(A.T[2], i, sy, p.y, P.Dyf);
+    u += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
+    A.lf[2][i] += u;
+}
+
 template <int H, int PASS>
 __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
                                                 const BatchTile* __restrict__ W, int vn)
@@ -259,7 +343,10 @@ __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ P
         if (!point_tile(sP, w, p, rr)) continue;
         if (PASS == 0) adj_stress_body<H>(sP, A, p, vn);
         else if (PASS == 1) adj_vel_body<H>(sP, A, p, vn);
-        else adj_sigma_body<H>(sP, A, p);
+        else if (PASS == 2) adj_sigma_body<H>(sP, A, p);
+        else if (PASS == 3) adj_tm_e_body<H>(sP, A, p, vn);
+        else if (PASS == 4) adj_tm_h_body<H>(sP, A, p, vn);
+        else adj_tm_ez_body<H>(sP, A, p);
     }
 }
 
@@ -309,6 +396,10 @@ __global__ void adj_inject(const AdjShot* __restrict__ As, int n)
     for (int r = threadIdx.x; r < A.nrec; r += blockDim.x) {
         const float v = A.res[(long long)r * A.nt + n];
         const long long i = A.ridx[r];
+        if (A.tm) {   // Ez receivers
+            atomicAdd(A.lf[2] + i, v);
+            continue;
+        }
         switch (A.rtype[r]) {
         case WAVE_TYPE_P:
             atomicAdd(A.lf[2] + i, 0.5f * v);
@@ -397,13 +488,56 @@ __global__ void adj_grad_final(PrepParams G, const StepParams P, const AdjShot A
     }
 }
 
+// chain rule for TMz: Ca = (1 - k) / (1 + k), Cb = (1 / eps) / (1 + k) with
+// k = sigma DT / (2 eps), eps = eps_r eps0; iMxz, iMyz = 1 / (2-point average of
+// mu = mu_r mu0) along x, y (0 where invalid)
+__global__ void adj_tm_final(PrepParams G, const StepParams P, const AdjShot A, float DT, float* geps, float* gsig, float* gmu,
+                             int accumulate)
+{
+    const float eps0 = 8.8541878176e-12f, mu0 = 1.2566370614e-6f;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
+        const int kx = static_cast<int>(k % G.NX), ky = static_cast<int>(k / G.NX);
+        const float e = P.m[M_EPSR][k] * eps0, sg = P.m[M_SIG][k];
+        const float kk = sg * DT / (2.0f * e), q = 1.0f + kk;
+        const float gca = A.g[0][k], gcb = A.g[1][k];
+        const float dca_de = 2.0f * kk / (e * q * q), dca_ds = -2.0f / (q * q) * (DT / (2.0f * e));
+        const float dcb_de = (-1.0f / (e * q) + kk / (e * q * q)) / e, dcb_ds = -(1.0f / e) / (q * q) * (DT / (2.0f * e));
+        const float ge = eps0 * (gca * dca_de + gcb * dcb_de);
+        const float gs = gca * dca_ds + gcb * dcb_ds;
+        // rows (kx, ky) and (kx-1, ky) of the x average, (kx, ky) and (kx, ky-1) of the y average
+        float gm = 0.0f;
+        for (int d = 0; d <= 1; ++d) {
+            if (kx - d >= 0) {
+                const long long r = k - d;
+                const float im = P.m[M_IMUXZ][r];
+                const float w = (kx - d + 1 < G.NX) ? 0.5f : 1.0f;
+                if (im != 0.0f && (d == 0 || w == 0.5f)) gm -= A.g[3][r] * im * im * w;
+            }
+            if (ky - d >= 0) {
+                const long long r = k - d * (long long)G.NX;
+                const float im = P.m[M_IMUYZ][r];
+                const float w = (ky - d + 1 < G.NY) ? 0.5f : 1.0f;
+                if (im != 0.0f && (d == 0 || w == 0.5f)) gm -= A.g[2][r] * im * im * w;
+            }
+        }
+        gm *= mu0;
+        if (accumulate) { geps[k] += ge; gsig[k] += gs; gmu[k] += gm; }
+        else { geps[k] = ge; gsig[k] = gs; gmu[k] = gm; }
+    }
+}
+
 template <int H>
 void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, int ntiles, int vn, cudaStream_t s)
 {
     const dim3 block(32, 8, 1);
-    if (pass == 0) adj_pass<H, 0><<<ntiles, block, 0, s>>>(Ps, As, W, vn);
-    else if (pass == 1) adj_pass<H, 1><<<ntiles, block, 0, s>>>(Ps, As, W, vn);
-    else adj_pass<H, 2><<<ntiles, block, 0, s>>>(Ps, As, W, vn);
+    switch (pass) {
+    case 0: adj_pass<H, 0><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
+    case 1: adj_pass<H, 1><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
+    case 2: adj_pass<H, 2><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
+    case 3: adj_pass<H, 3><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
+    case 4: adj_pass<H, 4><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
+    default: adj_pass<H, 5><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
+    }
 }
 
 void launch_adj(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, int ntiles, int vn, cudaStream_t s)
@@ -448,7 +582,14 @@ struct DevPool {
 std::string adjoint_supported(const wave_handle* h)
 {
     const wave_config& c = h->cfg;
-    if (c.dimension != 2 || c.equation != WAVE_EQ_ELASTIC) return "the adjoint gradient is implemented for 2-D elastic modelling";
+    if (c.dimension != 2 || (c.equation != WAVE_EQ_ELASTIC && c.equation != WAVE_EQ_TMEM))
+        return "the adjoint gradient is implemented for 2-D elastic and lossless 2-D TMz modelling";
+    if (c.equation == WAVE_EQ_TMEM) {
+        for (int t : h->hRecType)
+            if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez receivers only";
+        for (int t : h->hSrcType)
+            if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez sources only";
+    }
     if (!h->modelSet) return "set the model first";
     if (!h->seis || h->nrec < 1) return "set receivers first";
     return "";
@@ -478,18 +619,25 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
     for (int s = 0; s < ns; ++s) {
         wave_handle* h = shots[s];
         const long long N = h->N;
-        // state layout: 5 fields then the 8 psi arrays (absent psi: length 0)
+        // state layout: 5 field parts then 8 psi parts (absent parts: length 0);
+        // TMz: hx, hy, ez and the psi of ezy, ezx, hyx, hxy
+        const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
         long long off[AV_COUNT], len[AV_COUNT], o = 0;
-        const int fields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
-        for (int k = 0; k < 5; ++k) { off[k] = o; len[k] = N; o += N; }
+        const int elasticFields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
+        const int tmFields[5] = {F_HX, F_HY, F_EZ, -1, -1};
+        const int tmPsi[8] = {PS_EZY, PS_EZX, PS_HYX, PS_HXY, -1, -1, -1, -1};
+        const int* fields = tm ? tmFields : elasticFields;
+        const int* psiSlot = tm ? tmPsi : kAdjPsiSlot;
+        for (int k = 0; k < 5; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
         for (int k = 0; k < 8; ++k) {
-            const int slot = kAdjPsiSlot[k];
+            const int slot = psiSlot[k];
             off[5 + k] = o;
-            len[5 + k] = h->psi[slot] ? h->psiLen[slot] : 0;
+            len[5 + k] = (slot >= 0 && h->psi[slot]) ? h->psiLen[slot] : 0;
             o += len[5 + k];
         }
         stride[s] = o;
         AdjShot& a = A[s];
+        a.tm = tm ? 1 : 0;
         a.view = pool.get<float>(static_cast<size_t>(o) * (K + 1));
         a.stride = o;
         for (int k = 0; k < AV_COUNT; ++k) a.off[k] = off[k];
@@ -522,7 +670,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         ckpt[s] = pool.get<float>(static_cast<size_t>(o) * nck);
         for (int k = 0; k < AV_COUNT; ++k) {
             if (len[k] == 0) continue;
-            float* live = k < 5 ? h->f[fields[k]] : h->psi[kAdjPsiSlot[k - 5]];
+            float* live = k < 5 ? h->f[fields[k]] : h->psi[psiSlot[k - 5]];
             toView.push_back({live, a.view + off[k], len[k], 0, o});
             toCkpt.push_back({live, ckpt[s] + off[k], len[k], 0, o});
             fromCkpt.push_back({ckpt[s] + off[k], live, len[k], o, 0});
@@ -587,9 +735,10 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
                 adj_vprime_sources<<<ns, 128, 0, st>>>(dP, dA, n);
             }
             adj_inject<<<ns, 256, 0, st>>>(dA, n);
-            launch_adj(H, 0, dP, dA, dT, ntiles, n - n0, st);
-            launch_adj(H, 1, dP, dA, dT, ntiles, n - n0, st);
-            launch_adj(H, 2, dP, dA, dT, ntiles, n - n0, st);
+            const int first = A[0].tm ? 3 : 0;
+            launch_adj(H, first, dP, dA, dT, ntiles, n - n0, st);
+            launch_adj(H, first + 1, dP, dA, dT, ntiles, n - n0, st);
+            launch_adj(H, first + 2, dP, dA, dT, ntiles, n - n0, st);
         }
         ck(cudaGetLastError(), "adjoint launch");
     }
@@ -598,7 +747,11 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         wave_handle* h = shots[s];
         PrepParams G{h->NX, h->NY, h->NZ, h->N};
         const int o = sum ? 0 : s;
-        adj_grad_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
+        if (A[s].tm)
+            adj_tm_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
+                                               sum && s > 0 ? 1 : 0);
+        else
+            adj_grad_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
     }
     ck(cudaGetLastError(), "gradient launch");
     ck(cudaMemcpyAsync(misfit, dMisfit, ns * sizeof(double), cudaMemcpyDeviceToHost, st), "misfit copy");
