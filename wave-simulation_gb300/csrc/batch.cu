@@ -355,6 +355,9 @@ int wave_batch_adjoint_gradient(wave_batch* b, const float* const* dobs, int dob
             if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
             b->dirty = false;
         }
+        // the forward steps of the gradient run on the tuned schedule too (the
+        // adjoint starts from a zero state, so tuning on it changes nothing)
+        if (!b->tuned && !b->forced) autotune(b);
         std::vector<const float*> dD(ns);
         for (int s = 0; s < ns; ++s) {
             const size_t nd = static_cast<size_t>(b->shots[s]->nrec) * b->NT;

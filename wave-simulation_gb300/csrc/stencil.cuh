@@ -140,20 +140,26 @@ __device__ __forceinline__ void batch_loop(const StepParams* __restrict__ Ps, co
         }
         for (int xg = 0; xg < S.cols; xg += 32) {
             const int x = w.x0 + xg + static_cast<int>(threadIdx.x);
-            for (int rr = 0; rr < S.rows; rr += 8) {
-                const int r = w.r0 + rr + static_cast<int>(threadIdx.y);
-                if (x >= sP.NX || r >= sP.NY * sP.NZ) continue;
-                Pt p;
-                p.x = x;
-                if (sP.NZ == 1) {   // 2-D: no division
-                    p.y = r;
-                    p.z = 0;
-                } else {
-                    p.y = r / sP.NZ;
-                    p.z = r - p.y * sP.NZ;
+            // four row groups per pass, unrolled, so that their (read-only
+            // path) loads overlap: these kernels are bound by load latency
+            for (int r0 = 0; r0 < S.rows; r0 += 32) {
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    const int rr = r0 + 8 * g;
+                    const int r = w.r0 + rr + static_cast<int>(threadIdx.y);
+                    if (rr >= S.rows || x >= sP.NX || r >= sP.NY * sP.NZ) continue;
+                    Pt p;
+                    p.x = x;
+                    if (sP.NZ == 1) {   // 2-D: no division
+                        p.y = r;
+                        p.z = 0;
+                    } else {
+                        p.y = r / sP.NZ;
+                        p.z = r - p.y * sP.NZ;
+                    }
+                    p.i = p.x + (long long)sP.NX * (p.z + (long long)sP.NZ * p.y);
+                    body(sP, p);
                 }
-                p.i = p.x + (long long)sP.NX * (p.z + (long long)sP.NZ * p.y);
-                body(sP, p);
             }
         }
     }
