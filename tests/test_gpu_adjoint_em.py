@@ -39,7 +39,10 @@ def _survey(wave, refcpu, boundary, stencil, reduce):
     s.setSources(*acq32[:3])
     s.setReceivers(*acq32[3:])
     s.run(0, s.nt)
-    dobs = s.seismograms()
+    # observed data scaled so that the residual is a large part of the signal:
+    # the TMz forward's FP32 rounding (this survey runs at a small Courant
+    # number) then stays far below the residual the adjoint propagates
+    dobs = (0.6 * s.seismograms()).astype(np.float32)
     s.close()
     return ocfg, cfg, m32, acq32, dobs
 

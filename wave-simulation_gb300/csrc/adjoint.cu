@@ -332,41 +332,34 @@ __device__ __forceinline__ void adj_tm_ez_body(const StepParams& P, const AdjSho
 
 template <int H, int PASS>
 __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
-                                                const BatchTile* __restrict__ W, int vn)
+                                                const BatchTile* __restrict__ W, BatchSched S, int vn)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    const AdjShot& A = As[w.shot];
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (!point_tile(sP, w, p, rr)) continue;
-        if (PASS == 0) adj_stress_body<H>(sP, A, p, vn);
-        else if (PASS == 1) adj_vel_body<H>(sP, A, p, vn);
-        else if (PASS == 2) adj_sigma_body<H>(sP, A, p);
-        else if (PASS == 3) adj_tm_e_body<H>(sP, A, p, vn);
-        else if (PASS == 4) adj_tm_h_body<H>(sP, A, p, vn);
-        else adj_tm_ez_body<H>(sP, A, p);
-    }
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [&](const StepParams& P, const Pt& p, int shot) {
+        const AdjShot& A = As[shot];
+        if (PASS == 0) adj_stress_body<H>(P, A, p, vn);
+        else if (PASS == 1) adj_vel_body<H>(P, A, p, vn);
+        else if (PASS == 2) adj_sigma_body<H>(P, A, p);
+        else if (PASS == 3) adj_tm_e_body<H>(P, A, p, vn);
+        else if (PASS == 4) adj_tm_h_body<H>(P, A, p, vn);
+        else adj_tm_ez_body<H>(P, A, p);
+    });
 }
 
 // v' = (v_{n+1} - sources of step n) / d: the velocities the stress pass of
 // step n read (before the ABS taper and the source injection)
-__global__ void adj_vprime(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As, const BatchTile* __restrict__ W, int vn)
+__global__ void adj_vprime(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As, const BatchTile* __restrict__ W,
+                           BatchSched S, int vn)
 {
-    __shared__ StepParams sP;
-    const BatchTile w = W[blockIdx.x];
-    load_params(sP, Ps + w.shot);
-    const AdjShot& A = As[w.shot];
-    if (!A.vprime[0]) return;
-    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
-    for (int rr = 0; rr < kTileRows; rr += 8) {
-        Pt p;
-        if (!point_tile(sP, w, p, rr)) continue;
-        const float d = sP.abs ? absDamp(sP, p) : 1.0f;
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [&](const StepParams& P, const Pt& p, int shot) {
+        const AdjShot& A = As[shot];
+        if (!A.vprime[0]) return;
+        const float* X1 = A.view + (long long)(vn + 1) * A.stride;
+        const float d = P.abs ? absDamp(P, p) : 1.0f;
         A.vprime[0][p.i] = X1[A.off[AV_VX] + p.i] / d;
         A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
-    }
+    });
 }
 
 __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As, int n)
@@ -527,28 +520,30 @@ __global__ void adj_tm_final(PrepParams G, const StepParams P, const AdjShot A, 
 }
 
 template <int H>
-void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, int ntiles, int vn, cudaStream_t s)
+void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
+                  cudaStream_t s)
 {
     const dim3 block(32, 8, 1);
     switch (pass) {
-    case 0: adj_pass<H, 0><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
-    case 1: adj_pass<H, 1><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
-    case 2: adj_pass<H, 2><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
-    case 3: adj_pass<H, 3><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
-    case 4: adj_pass<H, 4><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
-    default: adj_pass<H, 5><<<ntiles, block, 0, s>>>(Ps, As, W, vn); break;
+    case 0: adj_pass<H, 0><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
+    case 1: adj_pass<H, 1><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
+    case 2: adj_pass<H, 2><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
+    case 3: adj_pass<H, 3><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
+    case 4: adj_pass<H, 4><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
+    default: adj_pass<H, 5><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
     }
 }
 
-void launch_adj(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, int ntiles, int vn, cudaStream_t s)
+void launch_adj(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
+                cudaStream_t s)
 {
     switch (H) {
-    case 1: launch_adj_h<1>(pass, Ps, As, W, ntiles, vn, s); break;
-    case 2: launch_adj_h<2>(pass, Ps, As, W, ntiles, vn, s); break;
-    case 3: launch_adj_h<3>(pass, Ps, As, W, ntiles, vn, s); break;
-    case 4: launch_adj_h<4>(pass, Ps, As, W, ntiles, vn, s); break;
-    case 5: launch_adj_h<5>(pass, Ps, As, W, ntiles, vn, s); break;
-    default: launch_adj_h<6>(pass, Ps, As, W, ntiles, vn, s); break;
+    case 1: launch_adj_h<1>(pass, Ps, As, W, S, grid, vn, s); break;
+    case 2: launch_adj_h<2>(pass, Ps, As, W, S, grid, vn, s); break;
+    case 3: launch_adj_h<3>(pass, Ps, As, W, S, grid, vn, s); break;
+    case 4: launch_adj_h<4>(pass, Ps, As, W, S, grid, vn, s); break;
+    case 5: launch_adj_h<5>(pass, Ps, As, W, S, grid, vn, s); break;
+    default: launch_adj_h<6>(pass, Ps, As, W, S, grid, vn, s); break;
     }
 }
 
@@ -677,8 +672,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         }
         Ps[s] = h->sp;
         const int rows = h->NY * h->NZ;
-        for (int r0 = 0; r0 < rows; r0 += kTileRows)
-            for (int x0 = 0; x0 < h->NX; x0 += 32) tiles.push_back({s, x0, r0, 0});
+        for (int r0 = 0; r0 < rows; r0 += S.rows)
+            for (int x0 = 0; x0 < h->NX; x0 += S.cols) tiles.push_back({s, x0, r0, 0});
     }
     auto upload = [&](auto& v) {
         using T = typename std::decay_t<decltype(v)>::value_type;
@@ -693,6 +688,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
     const CopyPart* dToCkpt = upload(toCkpt);
     const CopyPart* dFromCkpt = upload(fromCkpt);
     const int ntiles = static_cast<int>(tiles.size());
+    const BatchSched sched{ntiles, S.cols, S.rows, 0};
+    const int grid = S.blocks > 0 ? std::min(ntiles, S.blocks) : ntiles;
     bool anyVprime = false;
     for (const AdjShot& a : A) anyVprime |= a.vprime[0] != nullptr;
     const dim3 cgrid(64, 1, 1);
@@ -731,14 +728,14 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         }
         for (int n = n1 - 1; n >= n0; --n) {
             if (anyVprime) {
-                adj_vprime<<<ntiles, dim3(32, 8, 1), 0, st>>>(dP, dA, dT, n - n0);
+                adj_vprime<<<grid, dim3(32, 8, 1), 0, st>>>(dP, dA, dT, sched, n - n0);
                 adj_vprime_sources<<<ns, 128, 0, st>>>(dP, dA, n);
             }
             adj_inject<<<ns, 256, 0, st>>>(dA, n);
             const int first = A[0].tm ? 3 : 0;
-            launch_adj(H, first, dP, dA, dT, ntiles, n - n0, st);
-            launch_adj(H, first + 1, dP, dA, dT, ntiles, n - n0, st);
-            launch_adj(H, first + 2, dP, dA, dT, ntiles, n - n0, st);
+            launch_adj(H, first, dP, dA, dT, sched, grid, n - n0, st);
+            launch_adj(H, first + 1, dP, dA, dT, sched, grid, n - n0, st);
+            launch_adj(H, first + 2, dP, dA, dT, sched, grid, n - n0, st);
         }
         ck(cudaGetLastError(), "adjoint launch");
     }

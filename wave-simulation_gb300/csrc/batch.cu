@@ -377,6 +377,9 @@ int wave_batch_adjoint_gradient(wave_batch* b, const float* const* dobs, int dob
         S.stream = b->stream;
         S.set_counter = [b, ns](int n) { launch_set_counters(b->counters, ns, n, b->stream); };
         S.step = [b]() { launch_batch_step(b); };
+        S.cols = b->cols;   // the tuned schedule
+        S.rows = b->rows;
+        S.blocks = b->grid < b->ntiles ? b->grid : 0;
         adjoint_run(b->shots, S, dD.data(), checkpoint_every, misfits, g[0].data(), g[1].data(), g[2].data(), sum_shots != 0);
         if (grad_mem != WAVE_MEM_DEVICE)
             for (int k = 0; k < 3; ++k)

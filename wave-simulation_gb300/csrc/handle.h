@@ -155,6 +155,8 @@ struct AdjStepper {
     cudaStream_t stream;
     std::function<void(int)> set_counter;   // every shot's step counter to n
     std::function<void()> step;             // one forward step of every shot
+    int cols = 32, rows = kTileRows;        // tile shape of the adjoint launches (points)
+    int blocks = 0;                         // persistent blocks per launch (0: one per tile)
 };
 std::string adjoint_supported(const wave_handle* h);
 void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, const float* const* dobs, int K, double* misfit,

@@ -55,7 +55,7 @@ template <int H>
 __global__ void __launch_bounds__(256) acoustic_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { acoustic_v_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { acoustic_v_body<H>(P, p); });
 }
 
 template <int H>
@@ -107,7 +107,7 @@ template <int H>
 __global__ void __launch_bounds__(256) acoustic_p_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { acoustic_p_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { acoustic_p_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -165,7 +165,7 @@ template <int H>
 __global__ void __launch_bounds__(256) elastic_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { elastic_v_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { elastic_v_body<H>(P, p); });
 }
 
 // elastic stress: ForwardSolver2Delastic.cpp:210-290, ForwardSolver3Delastic.cpp:283-409,
@@ -257,7 +257,7 @@ template <int H>
 __global__ void __launch_bounds__(256) elastic_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { elastic_s_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { elastic_s_body<H>(P, p); });
 }
 
 // visco-elastic stress: ForwardSolver2Dviscoelastic.cpp:223-303,
@@ -428,7 +428,7 @@ template <int H>
 __global__ void __launch_bounds__(256) visco_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { visco_s_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { visco_s_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -457,7 +457,7 @@ template <int H>
 __global__ void __launch_bounds__(256) sh_v_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { sh_v_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { sh_v_body<H>(P, p); });
 }
 
 template <int H>
@@ -503,7 +503,7 @@ template <int H>
 __global__ void __launch_bounds__(256) sh_s_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { sh_s_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { sh_s_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -536,7 +536,7 @@ template <int H>
 __global__ void __launch_bounds__(256) tm_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { tm_h_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { tm_h_body<H>(P, p); });
 }
 
 // memory variables of one E component (ForwardSolver2Dviscotmem.cpp:175-182,
@@ -582,7 +582,7 @@ template <int H>
 __global__ void __launch_bounds__(256) tm_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { tm_e_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { tm_e_body<H>(P, p); });
 }
 
 // EM TEz: FD2Demem::run (ForwardSolverEM/ForwardSolver2Demem.cpp:132-180),
@@ -610,7 +610,7 @@ template <int H>
 __global__ void __launch_bounds__(256) te_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { te_h_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { te_h_body<H>(P, p); });
 }
 
 template <int H>
@@ -645,7 +645,7 @@ template <int H>
 __global__ void __launch_bounds__(256) te_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { te_e_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { te_e_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -688,7 +688,7 @@ template <int H>
 __global__ void __launch_bounds__(256) em3_h_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { em3_h_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { em3_h_body<H>(P, p); });
 }
 
 template <int H>
@@ -736,7 +736,7 @@ template <int H>
 __global__ void __launch_bounds__(256) em3_e_batch(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, BatchSched S)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p) { em3_e_body<H>(P, p); });
+    batch_loop(Ps, W, S, sP, [](const StepParams& P, const Pt& p, int) { em3_e_body<H>(P, p); });
 }
 
 // --------------------------------------------------------------------------
@@ -763,7 +763,7 @@ __global__ void __launch_bounds__(256) abs_frame_batch(const StepParams* __restr
                                                        int f0, int f1, int f2)
 {
     BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [=](const StepParams& P, const Pt& p) { abs_frame_body(P, p, f0, f1, f2); });
+    batch_loop(Ps, W, S, sP, [=](const StepParams& P, const Pt& p, int) { abs_frame_body(P, p, f0, f1, f2); });
 }
 
 // --------------------------------------------------------------------------

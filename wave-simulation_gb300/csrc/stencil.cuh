@@ -125,7 +125,7 @@ __device__ __forceinline__ bool point_tile(const StepParams& P, const BatchTile&
 // stride; the parameters of a tile's shot are staged in shared memory when
 // the shot changes (every thread first leaves the previous shot's). A tile of
 // S.cols x S.rows points is covered by the 32 x 8 block in column groups of
-// 32 and row groups of 8.
+// 32 and row groups of 8. body(params, point, shot index).
 template <class Body>
 __device__ __forceinline__ void batch_loop(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, const BatchSched& S,
                                            StepParams& sP, Body body)
@@ -158,7 +158,7 @@ __device__ __forceinline__ void batch_loop(const StepParams* __restrict__ Ps, co
                         p.z = r - p.y * sP.NZ;
                     }
                     p.i = p.x + (long long)sP.NX * (p.z + (long long)sP.NZ * p.y);
-                    body(sP, p);
+                    body(sP, p, w.shot);
                 }
             }
         }
