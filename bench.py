@@ -997,8 +997,8 @@ def run_fwi2d(args, wave):
     misfit_plain, plain_grad = plain_runs[-1][1], plain_runs[-1][2]
     mis, bvp = batch_runs[-1][1], batch_runs[-1][2]
     # forward steps counted by the batch plus the adjoint driver's own launches (per step: view copy,
-    # residual injection, three adjoint passes; per segment: two state copies; per shot: residual, chain rule)
-    launches = batch_runs[-1][3] + 5 * nt + 2 * ((nt + K - 1) // K) + 2 * nshots
+    # residual injection, two adjoint kernels; per segment: two state copies; per shot: residual, chain rule)
+    launches = batch_runs[-1][3] + 4 * nt + 2 * ((nt + K - 1) // K) + 2 * nshots
     rel = float(np.linalg.norm(bvp - plain_grad) / np.linalg.norm(plain_grad))
     value = nshots / batch_s
     plain = nshots / plain_s

@@ -16,15 +16,17 @@
 // plus source terms, and receivers read X after each step. The stress pass
 // reads the velocities before the taper and the sources, v' = (v_{n+1} - s) / d,
 // re-formed from the saved state when ABS or velocity sources are on. The adjoint runs
-// the transposed pieces backwards (three kernels per step: stress transpose,
-// velocity transpose, stress-derivative transpose) and accumulates
+// the transposed pieces backwards (three stages per step: stress transpose,
+// velocity transpose, stress-derivative transpose; the third stage of a step
+// runs inside the first kernel of the next one back, so two kernels per
+// step) and accumulates
 // dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry, which a last kernel maps to
 // vp, vs, rho through the model preparation (moduli, 2-point inverse density
 // averages, harmonic 4-point shear average with its edge fallbacks and vacuum
 // rules; Modelparameter.cpp:336-639, ModelparameterSeismic.cpp:131-136, 421-432).
 //
 // The lossless 2-D TMz step (FD2Dtmem::run, ForwardSolver2Dtmem.cpp:108-174)
-// has its own three kernels per step on the same driver:
+// has its own stages on the same driver (again two kernels per step):
 //   hx' = hx - iMyz (Dyf ez + P_ezy)'   hy' = hy + iMxz (Dxf ez + P_ezx)'
 //   ez' = Ca ez + Cb ((Dxb hy' + P_hyx)' - (Dyb hx' + P_hxy)'), then the ABS taper,
 // and a last kernel maps dJ/dCa, dJ/dCb, dJ/diMxz, dJ/diMyz to eps_r, sigma
@@ -138,7 +140,7 @@ __device__ __forceinline__ Slabs slabs_of(const StepParams& P, const Pt& p)
 
 // stress-pass transpose at step n (state n = view vn, state n+1 = view vn+1)
 template <int H>
-__device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+__device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
 {
     const float* X1 = A.view + (long long)(vn + 1) * A.stride;
     const long long i = p.i, sy = P.NX;
@@ -154,6 +156,17 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
     if (S.sx >= 0) { c1 += X1[A.off[AV_Q1] + S.px]; c4 += X1[A.off[AV_Q4] + S.px]; }
     if (S.sy >= 0) { c2 += X1[A.off[AV_Q2] + S.py]; c3 += X1[A.off[AV_Q3] + S.py]; }
     float lxx = A.lf[2][i], lyy = A.lf[3][i], lxy = A.lf[4][i];
+    if (pending) {
+        // the transposed velocity-pass derivatives of sigma from the step after
+        // this one (its third stage, folded in here to save a launch)
+        const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
+        const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
+        lxx += derivT<H, true>(A.T[4], i, 1, p.x, P.Dxf);
+        float u = derivT<H, false>(A.T[5], i, sy, p.y, DybS);
+        u += derivT<H, false>(A.T[6], i, 1, p.x, P.Dxb);
+        lxy += u;
+        lyy += derivT<H, true>(A.T[7], i, sy, p.y, DyfS);
+    }
     if (P.abs) {
         // the taper multiplied all five fields last: their adjoints first
         const float d = absDamp(P, p);
@@ -241,19 +254,6 @@ __device__ __forceinline__ void adj_vel_body(const StepParams& P, const AdjShot&
     A.g[4][i] += lvy * (a3 + a4);
 }
 
-// transposed velocity-pass derivatives of sigma
-template <int H>
-__device__ __forceinline__ void adj_sigma_body(const StepParams& P, const AdjShot& A, const Pt& p)
-{
-    const long long i = p.i, sy = P.NX;
-    const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
-    const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
-    A.lf[2][i] += derivT<H, true>(A.T[4], i, 1, p.x, P.Dxf);
-    float u = derivT<H, false>(A.T[5], i, sy, p.y, DybS);
-    u += derivT<H, false>(A.T[6], i, 1, p.x, P.Dxb);
-    A.lf[4][i] += u;
-    A.lf[3][i] += derivT<H, true>(A.T[7], i, sy, p.y, DyfS);
-}
 
 // ---- lossless 2-D TMz --------------------------------------------------------
 // parts of a TMz state in the view: AV_VX = hx, AV_VY = hy, AV_SXX = ez,
@@ -262,7 +262,7 @@ __device__ __forceinline__ void adj_sigma_body(const StepParams& P, const AdjSho
 
 // E-update transpose at step n
 template <int H>
-__device__ __forceinline__ void adj_tm_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+__device__ __forceinline__ void adj_tm_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
 {
     const float* X0 = A.view + (long long)vn * A.stride;
     const float* X1 = X0 + A.stride;
@@ -275,6 +275,12 @@ __device__ __forceinline__ void adj_tm_e_body(const StepParams& P, const AdjShot
     if (S.sx >= 0) c1 += X1[A.off[AV_P3] + S.px];
     if (S.sy >= 0) c2 += X1[A.off[AV_P4] + S.py];
     float lez = A.lf[2][i];
+    if (pending) {
+        // the transposed H-update derivatives of ez from the step after this one
+        float u = derivT<H, true>(A.T[2], i, sy, p.y, P.Dyf);
+        u += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
+        lez += u;
+    }
     if (P.abs) {
         // the taper multiplied ez, hx and hy last: their adjoints first
         const float d = absDamp(P, p);
@@ -320,29 +326,18 @@ __device__ __forceinline__ void adj_tm_h_body(const StepParams& P, const AdjShot
     A.lf[1][i] = lhy;
 }
 
-// transposed H-update derivatives of ez
-template <int H>
-__device__ __forceinline__ void adj_tm_ez_body(const StepParams& P, const AdjShot& A, const Pt& p)
-{
-    const long long i = p.i, sy = P.NX;
-    float u = derivT<H, true>(A.T[2], i, sy, p.y, P.Dyf);
-    u += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
-    A.lf[2][i] += u;
-}
 
 template <int H, int PASS>
 __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
-                                                const BatchTile* __restrict__ W, BatchSched S, int vn)
+                                                const BatchTile* __restrict__ W, BatchSched S, int vn, int pending)
 {
     BATCH_SHARED_PARAMS(sP);
     batch_loop(Ps, W, S, sP, [&](const StepParams& P, const Pt& p, int shot) {
         const AdjShot& A = As[shot];
-        if (PASS == 0) adj_stress_body<H>(P, A, p, vn);
+        if (PASS == 0) adj_stress_body<H>(P, A, p, vn, pending != 0);
         else if (PASS == 1) adj_vel_body<H>(P, A, p, vn);
-        else if (PASS == 2) adj_sigma_body<H>(P, A, p);
-        else if (PASS == 3) adj_tm_e_body<H>(P, A, p, vn);
-        else if (PASS == 4) adj_tm_h_body<H>(P, A, p, vn);
-        else adj_tm_ez_body<H>(P, A, p);
+        else if (PASS == 3) adj_tm_e_body<H>(P, A, p, vn, pending != 0);
+        else adj_tm_h_body<H>(P, A, p, vn);
     });
 }
 
@@ -521,29 +516,27 @@ __global__ void adj_tm_final(PrepParams G, const StepParams P, const AdjShot A, 
 
 template <int H>
 void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
-                  cudaStream_t s)
+                  int pending, cudaStream_t s)
 {
     const dim3 block(32, 8, 1);
     switch (pass) {
-    case 0: adj_pass<H, 0><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
-    case 1: adj_pass<H, 1><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
-    case 2: adj_pass<H, 2><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
-    case 3: adj_pass<H, 3><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
-    case 4: adj_pass<H, 4><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
-    default: adj_pass<H, 5><<<grid, block, 0, s>>>(Ps, As, W, S, vn); break;
+    case 0: adj_pass<H, 0><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 1: adj_pass<H, 1><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 3: adj_pass<H, 3><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    default: adj_pass<H, 4><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
     }
 }
 
 void launch_adj(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
-                cudaStream_t s)
+                int pending, cudaStream_t s)
 {
     switch (H) {
-    case 1: launch_adj_h<1>(pass, Ps, As, W, S, grid, vn, s); break;
-    case 2: launch_adj_h<2>(pass, Ps, As, W, S, grid, vn, s); break;
-    case 3: launch_adj_h<3>(pass, Ps, As, W, S, grid, vn, s); break;
-    case 4: launch_adj_h<4>(pass, Ps, As, W, S, grid, vn, s); break;
-    case 5: launch_adj_h<5>(pass, Ps, As, W, S, grid, vn, s); break;
-    default: launch_adj_h<6>(pass, Ps, As, W, S, grid, vn, s); break;
+    case 1: launch_adj_h<1>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    case 2: launch_adj_h<2>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    case 3: launch_adj_h<3>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    case 4: launch_adj_h<4>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    case 5: launch_adj_h<5>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    default: launch_adj_h<6>(pass, Ps, As, W, S, grid, vn, pending, s); break;
     }
 }
 
@@ -732,10 +725,13 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
                 adj_vprime_sources<<<ns, 128, 0, st>>>(dP, dA, n);
             }
             adj_inject<<<ns, 256, 0, st>>>(dA, n);
+            // two kernels per step: the third stage of step n (the transposed
+            // derivatives of the first-pass inputs) runs inside the first kernel
+            // of step n - 1; after step 0 it is not needed
             const int first = A[0].tm ? 3 : 0;
-            launch_adj(H, first, dP, dA, dT, sched, grid, n - n0, st);
-            launch_adj(H, first + 1, dP, dA, dT, sched, grid, n - n0, st);
-            launch_adj(H, first + 2, dP, dA, dT, sched, grid, n - n0, st);
+            const int pending = n < NT - 1 ? 1 : 0;
+            launch_adj(H, first, dP, dA, dT, sched, grid, n - n0, pending, st);
+            launch_adj(H, first + 1, dP, dA, dT, sched, grid, n - n0, pending, st);
         }
         ck(cudaGetLastError(), "adjoint launch");
     }
