@@ -736,6 +736,8 @@ def run_visco3d(args, wave):
     model = vi3_model(NXv, NYv, NZv, "cuda")
     acq = vi3_acq(NXv, NYv, NZv, s.nt, cfg.DT)
     s.prepareForModelling(model)
+    if args.kernel_path:
+        s.set_kernel_path(args.kernel_path)
     s.setSources(*acq[:3])
     s.setReceivers(*acq[3:])
     s.run(0, args.warmup)
@@ -749,6 +751,7 @@ def run_visco3d(args, wave):
     value = n * args.steps / (ms * 1e-3) / 1e9
     vel_kernel = ("el3dp_vel<2> (TMA streaming, two points per thread)" if passes & 4 else
                   "el3d_vel<2> (TMA streaming)" if passes & 1 else "elastic_v<2> (generic)")
+    str_kernel = ("el3dp_vstr<2,2> (TMA streaming, two points per thread)" if passes & 8 else "visco_s<2> (generic)")
     w = 20
     psi_pts = 2 * w * NYv * NZv + 2 * w * NXv * NYv + 2 * w * NXv * NZv
     alg = 4 * (2 * (9 + 6 * 2) + 5) * n + 6 * 8 * psi_pts       # 188 B/pt + psi
@@ -779,7 +782,7 @@ def run_visco3d(args, wave):
     cfgd = {"workload": f"3-D visco-elastic {NXv}x{NYv}(depth)x{NZv}, order 4, L=2, 20-pt CPML, DT=5e-4, NT=4000, 4096 receivers",
             "grid": [NXv, NYv, NZv], "order": 4, "L": 2, "l2": "inputs larger than L2 (state 21 x N x 4 B)",
             "parallelism": "1 GPU"}
-    _line(UNIT, value, args.steps, args.warmup, ms_step, cfgd, _roof(alg, ms_step, vel_kernel + " + visco_s<2> (generic)"),
+    _line(UNIT, value, args.steps, args.warmup, ms_step, cfgd, _roof(alg, ms_step, vel_kernel + " + " + str_kernel),
           e2e, launches, clocks, cpu, {"finite": finite})
 
 
@@ -829,8 +832,10 @@ def run_tmem_batch(args, wave):
     shots = tm_shots(nshots)
     npts = sum(nx * ny for nx, ny, _ in shots)
     cfgs = [wave.WaveConfig.make(**tm_cfg_kw(nx, ny)) for nx, ny, _ in shots]
-    # batched: all shots in each launch
+    # batched: all shots in each launch (schedule autotuned unless --schedule fixes it)
     b = wave.Batch(cfgs)
+    if args.schedule:
+        b.set_schedule(*(int(v) for v in args.schedule.split(",")))
     for shot, (nx, ny, m) in zip(b.shots, shots):
         shot.prepareForModelling({k: torch.from_numpy(v).cuda() for k, v in m.items()})
         acq = tm_acq(nx, shot.nt)
@@ -1074,8 +1079,10 @@ def main():
     ap.add_argument("--workload", default="elastic3d", choices=["elastic3d", "acoustic2d", "visco3d", "tmem_batch", "fwi2d", "vargrid3d"])
     ap.add_argument("--shots", type=int, default=128, help="shots of the batched EM workload")
     ap.add_argument("--repeats", type=int, default=3, help="repeats of the FWI-gradient arms (median reported)")
+    ap.add_argument("--schedule", default="", help="tmem_batch: fix the batch schedule as 'cols,rows,blocks_per_sm' "
+                                                  "(profiling; default: the autotuner)")
     ap.add_argument("--kernel-path", type=int, default=0, choices=[0, 1, 2, 3],
-                    help="3-D elastic kernels: 0 automatic, 1 generic, 2 one-point streaming, 3 two-point streaming (profiling)")
+                    help="3-D elastic and visco-elastic kernels: 0 automatic, 1 generic, 2 one-point streaming, 3 two-point streaming (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

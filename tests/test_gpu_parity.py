@@ -210,12 +210,16 @@ def test_two_point_streaming_kernels_match_oracle_and_generic(order, fs, boundar
     assert rel(pairs, generic) < 1e-5
 
 
-@pytest.mark.parametrize("order,fs,boundary,dims", [(8, 1, 2, (128, 44, 40)), (4, 0, 1, (132, 40, 36))])
-def test_visco_elastic_streaming_velocity_pass(order, fs, boundary, dims, wave, refcpu):
-    """3-D visco-elastic: the streaming velocity kernels (paths 2 and 3) with
-    the generic memory-variable stress kernel, against the FP64 oracle and the
-    generic kernels."""
-    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "viscoelastic", 3, order, fs, boundary, dims=dims)
+@pytest.mark.parametrize("order,fs,boundary,dims,L", [(8, 1, 2, (128, 44, 40), 2), (4, 0, 1, (132, 40, 36), 2),
+                                                    (4, 1, 2, (128, 40, 36), 2), (2, 0, 2, (96, 36, 32), 1),
+                                                    (6, 0, 2, (100, 38, 34), 1)])
+def test_visco_elastic_streaming_kernels(order, fs, boundary, dims, L, wave, refcpu):
+    """3-D visco-elastic: path 2 runs the one-point streaming velocity kernel
+    with the generic memory-variable stress kernel; path 3 runs the two-point
+    streaming kernels for both passes (the memory-variable stress kernel
+    el3dp_vstr: orders 2-8, one or two mechanisms). Against the FP64 oracle
+    and the generic kernels."""
+    cfg, model, sidx, stype, sig, ridx, rtype = make_case(refcpu, "viscoelastic", 3, order, fs, boundary, dims=dims, L=L)
     o = refcpu.Oracle(cfg, model, sidx, stype, sig, ridx, rtype, dtype=np.float64)
     ref = o.run()
     o.close()
@@ -224,7 +228,7 @@ def test_visco_elastic_streaming_velocity_pass(order, fs, boundary, dims, wave, 
     s32 = sig.astype(np.float32)
     generic = wave.simulate(wc, m32, sidx, stype, s32, ridx, rtype, kernel_path=1, expect_streaming=False)
     assert rel(generic, ref) < TOL
-    for path, bits in ((2, 0b0001), (3, 0b0101)):
+    for path, bits in ((2, 0b0001), (3, 0b1111)):
         s = wave.Factory.Create("3D", "viscoelastic").initForwardSolver(wc)
         s.prepareForModelling(m32)
         s.set_kernel_path(path)
@@ -235,7 +239,7 @@ def test_visco_elastic_streaming_velocity_pass(order, fs, boundary, dims, wave, 
         out = s.seismograms()
         s.close()
         assert rel(out, ref) < TOL, f"path {path} vs FP64 oracle {rel(out, ref):.3e}"
-        assert rel(out, generic) < 1e-5
+        assert rel(out, generic) < 1e-5, f"path {path} vs generic {rel(out, generic):.3e}"
 
 
 def test_multi_step_graph_equals_single_steps(wave, refcpu):

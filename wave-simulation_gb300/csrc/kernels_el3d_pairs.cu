@@ -744,6 +744,375 @@ __global__ void __launch_bounds__(NTHR, H <= 4 ? 2 : 1) el3dp_str(const __grid_c
 }
 
 // ------------------------------------------------------------------------
+// visco-elastic stress pass (ForwardSolver3Dviscoelastic.cpp:270-446, free
+// surface FreeSurface3Dviscoelastic.cpp:17-75): the stress kernel's pipeline
+// and derivatives; the stage also carries a tau_S "+1" box, from which the
+// shear tau averages (4-point arithmetic, calc4PointAverageMatrixRow edge
+// rules) and 1 + L tau_S are formed in-kernel. tau_P and the memory
+// variables are read and written at the pair itself with 8-byte accesses
+// (no halo). The update of each point follows visco_s_body (kernels.cu) op
+// for op.
+// ------------------------------------------------------------------------
+template <int H>
+struct VStrStage {
+    static constexpr int HB = hb_of(H);
+    static constexpr int CEN = 3 * HB;
+    static constexpr int PLUS = CEN + 10 * CB;   // mu "+1" box
+    static constexpr int PLUS2 = PLUS + PB;      // tau_S "+1" box
+    static constexpr int PSI = PLUS2 + PB;
+    static constexpr int BYTES = PSI + 9 * CB;
+    static constexpr int NST = 2;
+};
+
+// 4-point arithmetic average with the edge fallbacks (the avg4 of the model
+// preparation, kernels.cu), same operation order
+__device__ __forceinline__ float avg4f(float a1, float a2, float a3, float a4, bool inA, bool inB)
+{
+    float s;
+    if (inA && inB) {
+        s = 0.25f * a1; s += 0.25f * a2; s += 0.25f * a3; s += 0.25f * a4;
+    } else if (inA) {
+        s = 0.5f * a2; s += 0.5f * a1;
+    } else if (inB) {
+        s = 0.5f * a3; s += 0.5f * a1;
+    } else {
+        s = 1.0f * a1;
+    }
+    return s;
+}
+
+// one point's visco-elastic stress update; d*: CPML-corrected derivatives
+// (vxx = dx vx, vxy = dy vx, ...); S: sxx syy szz, Sh: sxy sxz syz, R[k][l]:
+// the memory variables of rxx ryy rzz rxy rxz ryz (in/out)
+template <int LL>
+__device__ __forceinline__ void visco_point(const StepParams& P, float vxx, float vyy, float vzz, float vxy, float vyx, float vxz,
+                                            float vzx, float vyz, float vzy, float M, float mu, float tauP, float tauS,
+                                            float opP, float opS, const float muAv[3], const float tauAv[3], float S[3],
+                                            float Sh[3], float (&R)[6][LL], bool fsRow)
+{
+    const float DTh = P.DThalf;
+    float u = vxx;
+    u += vyy;
+    u += vzz;
+    u *= M;
+#pragma unroll
+    for (int l = 0; l < LL; ++l) {
+        float u2 = P.invRelax[l] * u;
+        u2 *= tauP;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            S[k] += DTh * R[k][l];
+            R[k][l] *= P.c1[l];
+            R[k][l] -= u2;
+        }
+    }
+    u *= opP;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) S[k] += u;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float sum = k == 0 ? vyy + vzz : (k == 1 ? vxx + vzz : vxx + vyy);
+        u = sum;
+        u *= mu;
+        u *= 2.0f;
+#pragma unroll
+        for (int l = 0; l < LL; ++l) {
+            float u2 = P.invRelax[l] * u;
+            u2 *= tauS;
+            R[k][l] += u2;
+            R[k][l] *= P.c2[l];
+            S[k] += DTh * R[k][l];
+        }
+        u *= opS;
+        S[k] -= u;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        u = k == 0 ? vxy : (k == 1 ? vxz : vyz);
+        const float ut = k == 0 ? vyx : (k == 1 ? vzx : vzy);
+        u += ut;
+        u *= muAv[k];
+        float sh = Sh[k];
+#pragma unroll
+        for (int l = 0; l < LL; ++l) {
+            float r = R[3 + k][l];
+            sh += DTh * r;
+            r *= P.c1[l];
+            float u2 = P.invRelax[l] * u;
+            u2 *= tauAv[k];
+            r -= u2;
+            r *= P.c2[l];
+            sh += DTh * r;
+            R[3 + k][l] = r;
+        }
+        u *= opS;
+        Sh[k] = sh + u;
+    }
+    if (fsRow) {
+        // FreeSurfaceViscoelastic::setModelparameter (FreeSurfaceViscoelastic.cpp:12-97), as in visco_s_body
+        float temp = -2.0f * mu * opS;
+        float temp2 = M * opP;
+        temp += temp2;
+        const float itemp2 = 1.0f / temp2;
+        const float sV = temp;
+        float sH = -1.0f * temp;
+        sH *= temp;
+        sH *= itemp2;
+        const float hsum = vxx + vzz;
+        const int kk[2] = {0, 2};
+#pragma unroll
+        for (int l = 0; l < LL; ++l)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) S[kk[q]] -= DTh * R[kk[q]][l];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) S[kk[q]] += sH * hsum;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) S[kk[q]] -= sV * vyy;
+        float t3 = 2.0f * mu * tauS;
+        t3 -= M * tauP;
+        float ratio = 2.0f * mu * opS;
+        ratio /= M * opP;
+        ratio -= 1.0f;
+#pragma unroll
+        for (int l = 0; l < LL; ++l) {
+            float rv = t3; rv *= P.c2[l]; rv /= P.relaxTime[l];
+            float rh = t3; rh *= ratio; rh *= P.c2[l]; rh /= P.relaxTime[l];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                R[kk[q]][l] += rh * hsum;
+                R[kk[q]][l] -= rv * vyy;
+                S[kk[q]] += DTh * R[kk[q]][l];
+            }
+        }
+        S[1] = 0.0f;
+#pragma unroll
+        for (int l = 0; l < LL; ++l) R[1][l] = 0.0f;
+    }
+}
+
+template <int H, int LL>
+__global__ void __launch_bounds__(NTHR, 2) el3dp_vstr(const __grid_constant__ El3dMaps T, const StepParams P, const El3dSched S)
+{
+    using L = VStrStage<H>;
+    constexpr int NST = L::NST, HX = hx_of(H), BW = bw_of(H), TT = TX * TZ;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * L::BYTES);
+    unsigned* rel = reinterpret_cast<unsigned*>(full + NST);
+    __shared__ Segs G;
+    __shared__ int abortRun;
+    __shared__ volatile int failed;
+    __shared__ int issued;
+    __shared__ float2 xw[2][XRows<H>::N][2 * H + 1];   // x weights: Dxb, Dxf
+    fill_xw<H>(xw, P.Dxb, P.Dxf, P.NX);
+    const int total = prologue<NST>(G, full, rel, &abortRun, &failed, P, S, H, T);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    auto issue = [&](int s, const Cursor& cur) {
+        unsigned char* st = smem + s * L::BYTES;
+        uint64_t* bar = full + s;
+        const int tile = G.tile[cur.seg], ya = G.ya[cur.seg];
+        const int q = ya - H + cur.k, c = ya - 2 * H + cur.k;
+        const bool compute = c >= ya;
+        const int x0 = (tile % S.ntx) * TX, z0 = (tile / S.ntx) * TZ;
+        const PsiBoxes B = compute ? psi_boxes(P, x0, z0, c) : PsiBoxes{kNoBox, kNoBox, -1};
+        uint32_t bytes = 3 * CB + 2 * PBYTES + B.bytes();
+        if (compute) bytes += 3 * hbytes_of(H) + 7 * CB;
+        mbar_expect_tx(bar, bytes);
+        issue_psi(B, T.psS, st + L::PSI, bar, x0, z0, c);
+        unsigned char* cen = st + L::CEN;
+        tma_load(cen + 0 * CB, &T.cVx, bar, x0, z0, q);
+        tma_load(cen + 1 * CB, &T.cVy, bar, x0, z0, q);
+        tma_load(cen + 2 * CB, &T.cVz, bar, x0, z0, q);
+        tma_load(st + L::PLUS, &T.pMu, bar, x0, z0, c + 1);
+        tma_load(st + L::PLUS2, &T.pTauS, bar, x0, z0, c + 1);
+        if (compute) {
+            tma_load(st + 0 * L::HB, &T.hVx, bar, x0 - HX, z0 - H, c);
+            tma_load(st + 1 * L::HB, &T.hVy, bar, x0 - HX, z0 - H, c);
+            tma_load(st + 2 * L::HB, &T.hVz, bar, x0 - HX, z0 - H, c);
+            tma_load(cen + 3 * CB, &T.cSxx, bar, x0, z0, c);
+            tma_load(cen + 4 * CB, &T.cSyy, bar, x0, z0, c);
+            tma_load(cen + 5 * CB, &T.cSzz, bar, x0, z0, c);
+            tma_load(cen + 6 * CB, &T.cSxy, bar, x0, z0, c);
+            tma_load(cen + 7 * CB, &T.cSxz, bar, x0, z0, c);
+            tma_load(cen + 8 * CB, &T.cSyz, bar, x0, z0, c);
+            tma_load(cen + 9 * CB, &T.cM, bar, x0, z0, c);
+        }
+    };
+    if (threadIdx.x == 0) start_feed<NST>(G, total, &issued, issue);
+
+    const int pi = warp * TX + 2 * lane;
+    const int ci = (warp + H) * BW + (HX + 2 * lane);
+    const int ri = warp * PW + 2 * lane;
+    float2 qx[2 * H + 1], qy[2 * H + 1], qz[2 * H + 1];
+#pragma unroll
+    for (int k = 0; k <= 2 * H; ++k) qx[k] = qy[k] = qz[k] = make_float2(0.0f, 0.0f);
+    // plane-y values carried from the previous iteration's "+1" boxes:
+    // inverse clamped mu and mu at (x, x+1), x+2 of rows z and z+1; tau_S likewise
+    float2 i0 = make_float2(1.0f, 1.0f), i1 = i0, m00 = i0;
+    float i0r = 1.0f, i1r = 1.0f;
+    float2 t0 = make_float2(0.0f, 0.0f), t1 = t0;
+    float t0r = 0.0f, t1r = 0.0f;
+    const float Lf = static_cast<float>(LL);
+    const Coef<H> K = make_coef<H>(P.scale);
+    Cursor cur{0, 0};
+    ColumnP C;
+
+    int it = 0;
+    for (; it < total; ++it) {
+        const int s = it % NST;
+        const int tile = G.tile[cur.seg], ya = G.ya[cur.seg];
+        if (cur.k == 0) column_setup(C, P, (tile % S.ntx) * TX, (tile / S.ntx) * TZ, XRows<H>::NL);
+        const int y = ya - 2 * H + cur.k;
+        const bool compute = y >= ya;
+        if (!__all_sync(0xffffffffu, mbar_wait(full + s, (it / NST) & 1))) {
+            failed = 1;
+            report(S.err, WAVE_ERR_TIMEOUT);
+            break;
+        }
+        const unsigned char* st = smem + s * L::BYTES;
+        const float* cen = reinterpret_cast<const float*>(st + L::CEN);
+#pragma unroll
+        for (int k = 0; k < 2 * H; ++k) { qx[k] = qx[k + 1]; qy[k] = qy[k + 1]; qz[k] = qz[k + 1]; }
+        qx[2 * H] = ld2(cen + 0 * TT + pi);
+        qy[2 * H] = ld2(cen + 1 * TT + pi);
+        qz[2 * H] = ld2(cen + 2 * TT + pi);
+        const float* mb = reinterpret_cast<const float*>(st + L::PLUS);
+        const float* tb = reinterpret_cast<const float*>(st + L::PLUS2);
+        if (compute && C.ok) {
+            Plane Y;
+            plane_setup(Y, P, y);
+            const float* hVx = reinterpret_cast<const float*>(st + 0 * L::HB) + ci;
+            const float* hVy = reinterpret_cast<const float*>(st + 1 * L::HB) + ci;
+            const float* hVz = reinterpret_cast<const float*>(st + 2 * L::HB) + ci;
+            const float* ps = reinterpret_cast<const float*>(st + L::PSI) + pi;
+            const float* ryf = Y.yi ? nullptr : row_of(P.Dyf, y);
+            const float* ryb = Y.yi ? nullptr : row_of(P.Dyb, y);
+            const long long i = C.x + (long long)P.NX * (C.z + (long long)P.NZ * y);
+            const bool x2in = C.x + 2 < P.NX, inY = y + 1 < P.NY, inZ = C.z + 1 < P.NZ;
+            float2 vxx, vyx, vzx;
+            if (C.xedge) {
+                vxx = dx_w<H>(hVx, xw[0][C.xr]);
+                vyx = dx_w<H>(hVy, xw[1][C.xr]);
+                vzx = dx_w<H>(hVz, xw[1][C.xr]);
+            } else {
+                vxx = dx_int<H, false>(hVx, K);
+                vyx = dx_int<H, true>(hVy, K);
+                vzx = dx_int<H, true>(hVz, K);
+            }
+            float2 vyy, vxy, vzy;
+            if (Y.yi) {
+                vyy = dy_int<H, false>(qy, K);
+                vxy = dy_int<H, true>(qx, K);
+                vzy = dy_int<H, true>(qz, K);
+            } else {
+                vyy = dy_tab<H>(qy, ryb);
+                vxy = dy_tab<H>(qx, ryf);
+                vzy = dy_tab<H>(qz, ryf);
+            }
+            float2 vzz, vxz, vyz;
+            if (C.zi) {
+                vzz = dz_int<H, false>(hVz, BW, K);
+                vxz = dz_int<H, true>(hVx, BW, K);
+                vyz = dz_int<H, true>(hVy, BW, K);
+            } else {
+                vzz = dz_tab<H>(hVz, BW, row_of(P.Dzb, C.z));
+                vxz = dz_tab<H>(hVx, BW, row_of(P.Dzf, C.z));
+                vyz = dz_tab<H>(hVy, BW, row_of(P.Dzf, C.z));
+            }
+            if (C.sx >= 0) {
+                cpml2(vxx, ld2(ps + 0 * TT), psi_x(P, PS_VXX, C, y), C.axf, C.bxf);
+                cpml2(vyx, ld2(ps + 1 * TT), psi_x(P, PS_VYX, C, y), C.axh, C.bxh);
+                cpml2(vzx, ld2(ps + 2 * TT), psi_x(P, PS_VZX, C, y), C.axh, C.bxh);
+            }
+            if (Y.sy >= 0) {
+                cpml2(vyy, ld2(ps + 3 * TT), psi_y(P, PS_VYY, C, Y), dup(Y.ayf), dup(Y.byf));
+                cpml2(vxy, ld2(ps + 4 * TT), psi_y(P, PS_VXY, C, Y), dup(Y.ayh), dup(Y.byh));
+                cpml2(vzy, ld2(ps + 5 * TT), psi_y(P, PS_VZY, C, Y), dup(Y.ayh), dup(Y.byh));
+            }
+            if (C.sz >= 0) {
+                cpml2(vzz, ld2(ps + 6 * TT), psi_z(P, PS_VZZ, C, y), dup(C.azf), dup(C.bzf));
+                cpml2(vxz, ld2(ps + 7 * TT), psi_z(P, PS_VXZ, C, y), dup(C.azh), dup(C.bzh));
+                cpml2(vyz, ld2(ps + 8 * TT), psi_z(P, PS_VYZ, C, y), dup(C.azh), dup(C.bzh));
+            }
+            // mu and tau_S of plane y+1 (the "+1" boxes) and the averages
+            const float2 n0 = ld2(mb + ri), n1 = ld2(mb + ri + PW);
+            const float j0x = inv_clampedf(n0.x), j0y = inv_clampedf(n0.y), j0r = inv_clampedf(mb[ri + 2]);
+            const float j1x = inv_clampedf(n1.x), j1y = inv_clampedf(n1.y);
+            const float muXY[2] = {harm4f(i0.x, i0.y, j0x, j0y, true, inY), harm4f(i0.y, i0r, j0y, j0r, x2in, inY)};
+            const float muXZ[2] = {harm4f(i0.x, i0.y, i1.x, i1.y, true, inZ), harm4f(i0.y, i0r, i1.y, i1r, x2in, inZ)};
+            const float muYZ[2] = {harm4f(i0.x, j0x, i1.x, j1x, inY, inZ), harm4f(i0.y, j0y, i1.y, j1y, inY, inZ)};
+            const float2 u0 = ld2(tb + ri), u1 = ld2(tb + ri + PW);
+            const float u0r = tb[ri + 2];
+            const float tXY[2] = {avg4f(t0.x, t0.y, u0.x, u0.y, true, inY), avg4f(t0.y, t0r, u0.y, u0r, x2in, inY)};
+            const float tXZ[2] = {avg4f(t0.x, t0.y, t1.x, t1.y, true, inZ), avg4f(t0.y, t0r, t1.y, t1r, x2in, inZ)};
+            const float tYZ[2] = {avg4f(t0.x, u0.x, t1.x, u1.x, inY, inZ), avg4f(t0.y, u0.y, t1.y, u1.y, inY, inZ)};
+            const float2 M = ld2(cen + 9 * TT + pi);
+            const float2 tauP = ld2(P.m[M_TAUP] + i);
+            float2 sxx = ld2(cen + 3 * TT + pi), syy = ld2(cen + 4 * TT + pi), szz = ld2(cen + 5 * TT + pi);
+            float2 sxy = ld2(cen + 6 * TT + pi), sxz = ld2(cen + 7 * TT + pi), syz = ld2(cen + 8 * TT + pi);
+            const int slotR[6] = {R_XX, R_YY, R_ZZ, R_XY, R_XZ, R_YZ};
+            float Ra[6][LL], Rb[6][LL];
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+#pragma unroll
+                for (int l = 0; l < LL; ++l) {
+                    const float2 r = ld2(P.r[slotR[k]][l] + i);
+                    Ra[k][l] = r.x;
+                    Rb[k][l] = r.y;
+                }
+            const bool fsRow = P.fs && y == 0;
+            {
+                float Sn[3] = {sxx.x, syy.x, szz.x}, Sh[3] = {sxy.x, sxz.x, syz.x};
+                const float mav[3] = {muXY[0], muXZ[0], muYZ[0]}, tav[3] = {tXY[0], tXZ[0], tYZ[0]};
+                const float mu = m00.x;   // the prepared modulus (already clamped)
+                const float opP = 1.0f + Lf * tauP.x, opS = 1.0f + Lf * t0.x;
+                visco_point<LL>(P, vxx.x, vyy.x, vzz.x, vxy.x, vyx.x, vxz.x, vzx.x, vyz.x, vzy.x, M.x, mu, tauP.x, t0.x, opP, opS,
+                            mav, tav, Sn, Sh, Ra, fsRow);
+                sxx.x = Sn[0]; syy.x = Sn[1]; szz.x = Sn[2]; sxy.x = Sh[0]; sxz.x = Sh[1]; syz.x = Sh[2];
+            }
+            {
+                float Sn[3] = {sxx.y, syy.y, szz.y}, Sh[3] = {sxy.y, sxz.y, syz.y};
+                const float mav[3] = {muXY[1], muXZ[1], muYZ[1]}, tav[3] = {tXY[1], tXZ[1], tYZ[1]};
+                const float mu = m00.y;
+                const float opP = 1.0f + Lf * tauP.y, opS = 1.0f + Lf * t0.y;
+                visco_point<LL>(P, vxx.y, vyy.y, vzz.y, vxy.y, vyx.y, vxz.y, vzx.y, vyz.y, vzy.y, M.y, mu, tauP.y, t0.y, opP, opS,
+                            mav, tav, Sn, Sh, Rb, fsRow);
+                sxx.y = Sn[0]; syy.y = Sn[1]; szz.y = Sn[2]; sxy.y = Sh[0]; sxz.y = Sh[1]; syz.y = Sh[2];
+            }
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+#pragma unroll
+                for (int l = 0; l < LL; ++l) st2(P.r[slotR[k]][l] + i, make_float2(Ra[k][l], Rb[k][l]));
+            float2 d = make_float2(1.0f, 1.0f);
+            if (P.abs) d = make_float2(abs_damp(P, C.x, y, C.z), abs_damp(P, C.x + 1, y, C.z));
+            st2(P.f[F_SXX] + i, mul2(sxx, d));
+            st2(P.f[F_SYY] + i, mul2(syy, d));
+            st2(P.f[F_SZZ] + i, mul2(szz, d));
+            st2(P.f[F_SXY] + i, mul2(sxy, d));
+            st2(P.f[F_SXZ] + i, mul2(sxz, d));
+            st2(P.f[F_SYZ] + i, mul2(syz, d));
+        }
+        // carry mu and tau_S of plane y+1 into the next iteration
+        {
+            const float2 n0 = ld2(mb + ri), n1 = ld2(mb + ri + PW);
+            m00 = n0;
+            i0 = make_float2(inv_clampedf(n0.x), inv_clampedf(n0.y));
+            i0r = inv_clampedf(mb[ri + 2]);
+            i1 = make_float2(inv_clampedf(n1.x), inv_clampedf(n1.y));
+            i1r = inv_clampedf(mb[ri + PW + 2]);
+            t0 = ld2(tb + ri);
+            t0r = tb[ri + 2];
+            t1 = ld2(tb + ri + PW);
+            t1r = tb[ri + PW + 2];
+        }
+        release_and_refill<NST>(it, total, cur, G, rel, &issued, &failed, issue);
+        if (__any_sync(0xffffffffu, failed != 0)) break;
+        cur.advance(G);
+    }
+    finish_ring<NST>(full, &issued, &failed);
+}
+
+// ------------------------------------------------------------------------
 // host side: tensor maps and launches
 // ------------------------------------------------------------------------
 namespace {
@@ -754,6 +1123,51 @@ template <int H>
 size_t vel_smem() { return VelStage<H>::NST * (VelStage<H>::BYTES + 2 * sizeof(uint64_t)); }
 template <int H>
 size_t str_smem() { return StrStage<H>::NST * (StrStage<H>::BYTES + 2 * sizeof(uint64_t)); }
+template <int H>
+size_t vstr_smem() { return VStrStage<H>::NST * (VStrStage<H>::BYTES + 2 * sizeof(uint64_t)); }
+
+// The visco-elastic stress kernel is built for orders 2-8 and one or two
+// relaxation mechanisms (other set-ups run the generic kernel).
+constexpr int kViscoMaxH = 4, kViscoMaxL = 2;
+
+// resident CTAs per SM of the visco-elastic stress kernel (0: does not fit)
+template <int H, int LL>
+int configure_visco_hl()
+{
+    if (cudaFuncSetAttribute(el3dp_vstr<H, LL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vstr_smem<H>()) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, el3dp_vstr<H, LL>, NTHR, vstr_smem<H>()) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+template <int H>
+int configure_visco_h(int L) { return L == 1 ? configure_visco_hl<H, 1>() : configure_visco_hl<H, 2>(); }
+
+int configure_visco(int H, int L)
+{
+    if (L < 1 || L > kViscoMaxL) return 0;
+    switch (H) {
+    case 1: return configure_visco_h<1>(L);
+    case 2: return configure_visco_h<2>(L);
+    case 3: return configure_visco_h<3>(L);
+    case 4: return configure_visco_h<4>(L);
+    default: return 0;
+    }
+}
+
+template <int H>
+void launch_visco(const El3dPlan& plan, const StepParams& P, cudaStream_t s)
+{
+    const dim3 block(NTHR, 1, 1);
+    if (P.L == 1) el3dp_vstr<H, 1><<<plan.gridVisco, block, vstr_smem<H>(), s>>>(plan.maps, P, plan.sched);
+    else el3dp_vstr<H, 2><<<plan.gridVisco, block, vstr_smem<H>(), s>>>(plan.maps, P, plan.sched);
+}
 
 // CTAs of each kernel resident per SM (0: does not fit)
 template <int H>
@@ -785,7 +1199,10 @@ cudaError_t launch_h(const El3dPlan& plan, const StepParams& P, int pass, cudaSt
 {
     const dim3 block(NTHR, 1, 1);
     if (pass == 0) el3dp_vel<H><<<plan.grid, block, vel_smem<H>(), s>>>(plan.maps, P, plan.sched);
-    else el3dp_str<H><<<plan.grid, block, str_smem<H>(), s>>>(plan.maps, P, plan.sched);
+    else if (P.L > 0) {
+        if (plan.gridVisco < 1 || H > kViscoMaxH) return cudaErrorInvalidValue;
+        launch_visco<(H <= kViscoMaxH ? H : 1)>(plan, P, s);
+    } else el3dp_str<H><<<plan.grid, block, str_smem<H>(), s>>>(plan.maps, P, plan.sched);
     return cudaGetLastError();
 }
 
@@ -815,9 +1232,11 @@ bool make_psi_map(CUtensorMap* m, const float* base, int axis, const StepParams&
 
 // Builds the tensor maps of the pair kernels for the current field/material
 // pointers. Returns false when they do not apply.
-bool el3d_prepare_pairs(El3dPlan& plan, const StepParams& P, const float* rho, const float* M, const float* mu, int H, int* errWord)
+bool el3d_prepare_pairs(El3dPlan& plan, const StepParams& P, const float* rho, const float* M, const float* mu, int H, int* errWord,
+                        const float* tauS)
 {
     plan.ready = false;
+    plan.gridVisco = 0;
     if (!P.is3d || H < 1 || H > 6 || (P.NX % 4) != 0 || P.NX < 8 || P.NZ < 2) return false;
     if (!rho || !M || !mu) return false;
     if (P.useCpml && (!slab_tiles_ok(P.cx, TX, true) || !slab_tiles_ok(P.cz, TZ, false))) return false;
@@ -846,6 +1265,7 @@ bool el3d_prepare_pairs(El3dPlan& plan, const StepParams& P, const float* rho, c
     ok &= make_map(&T.cM, M, P.NX, P.NZ, P.NY, TX, TZ);
     ok &= make_map(&T.pRho, rho, P.NX, P.NZ, P.NY, PW, PH);
     ok &= make_map(&T.pMu, mu, P.NX, P.NZ, P.NY, PW, PH);
+    if (tauS) ok &= make_map(&T.pTauS, tauS, P.NX, P.NZ, P.NY, PW, PH);
     if (P.useCpml) {
         const int vel[9] = {PS_SXX_X, PS_SXY_X, PS_SXZ_X, PS_SXY_Y, PS_SYY_Y, PS_SYZ_Y, PS_SXZ_Z, PS_SYZ_Z, PS_SZZ_Z};
         const int str[9] = {PS_VXX, PS_VYX, PS_VZX, PS_VYY, PS_VXY, PS_VZY, PS_VZZ, PS_VXZ, PS_VYZ};
@@ -873,6 +1293,13 @@ bool el3d_prepare_pairs(El3dPlan& plan, const StepParams& P, const float* rho, c
     if (tiles / grid + 2 > MAXSEG) return false;
     plan.grid = static_cast<int>(grid);
     plan.ready = plan.grid > 0;
+    if (plan.ready && tauS && P.L > 0 && P.L <= kViscoMaxL && H <= kViscoMaxH) {
+        // the visco-elastic stress kernel: its larger stage may fit fewer CTAs per SM
+        const int perV = configure_visco(H, P.L);
+        long long gv = (long long)perV * sms;
+        if (gv > tiles * P.NY) gv = tiles * P.NY;
+        if (perV > 0 && tiles / gv + 2 <= MAXSEG) plan.gridVisco = static_cast<int>(gv);
+    }
     return plan.ready;
 }
 

@@ -195,10 +195,13 @@ bool type_ok(int eq, bool is3d, int type, bool source)
 // visco-elastic step (the same update; its stress pass has memory variables).
 int pass_kernel(const wave_handle* h, int pass)
 {
-    if (pass == 1 && h->cfg.equation != WAVE_EQ_ELASTIC) return 0;
+    // the visco-elastic stress pass has a two-point streaming kernel only
+    const bool viscoStress = pass == 1 && h->cfg.equation == WAVE_EQ_VISCOELASTIC;
+    if (pass == 1 && h->cfg.equation != WAVE_EQ_ELASTIC && !viscoStress) return 0;
+    if (viscoStress && h->el3dp.gridVisco < 1) return 0;
     switch (h->kernelPath) {
     case 1: return 0;
-    case 2: return h->el3d.ready ? 1 : 0;
+    case 2: return h->el3d.ready && !viscoStress ? 1 : 0;
     case 3: return h->el3dp.ready ? 2 : 0;
     default: {
         const int k = h->passStreaming[pass];
@@ -359,7 +362,10 @@ void tune_passes(wave_handle* h)
         float best = 0.0f;
         h->passStreaming[pass] = 0;
         for (int kind = 0; kind < 3; ++kind) {
-            if (!ready[kind] || (kind > 0 && pass == 1 && h->cfg.equation != WAVE_EQ_ELASTIC)) continue;
+            if (!ready[kind]) continue;
+            if (kind > 0 && pass == 1 && h->cfg.equation != WAVE_EQ_ELASTIC &&
+                !(kind == 2 && h->cfg.equation == WAVE_EQ_VISCOELASTIC && h->el3dp.gridVisco > 0))
+                continue;
             launch_kernel_of(h, kind, pass, false);
             h->check(cudaEventRecord(e0, h->stream), "event");
             for (int k = 0; k < 2; ++k) launch_kernel_of(h, kind, pass, false);
@@ -818,7 +824,8 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         h->check(cudaStreamSynchronize(s), "model preparation");
         if ((eq == WAVE_EQ_ELASTIC || eq == WAVE_EQ_VISCOELASTIC) && is3d) {
             el3d_prepare(h->el3d, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord);
-            el3d_prepare_pairs(h->el3dp, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord);
+            el3d_prepare_pairs(h->el3dp, h->sp, h->m[M_RHO], h->m[M_M], h->m[M_MU], h->H, h->errWord,
+                               eq == WAVE_EQ_VISCOELASTIC ? h->m[M_TAUS] : nullptr);
             tune_passes(h);
         }
         h->modelSet = true;
