@@ -133,3 +133,20 @@ def test_autotuner_times_once_then_uses_its_cache(wave, refcpu):
     fixed, _ = _run_batch(wave, cases, cfgs, (32, 32, 0))
     for a, b_, c in zip(tuned, again, fixed):
         assert np.array_equal(a, c) and np.array_equal(b_, c)
+
+
+@pytest.mark.parametrize("schedule", [(32, 8, 0), (64, 16, 0), (64, 32, 2)])
+def test_tmz_interior_tiles_equal_single_shots(wave, refcpu, schedule):
+    """Lossless TMz: tiles wholly inside a shot's interior (away from the
+    operators' edge bands and the CPML slabs) take the batched kernels' lean
+    path; the batch still gives the single-shot generic kernels' bits."""
+    grids = ((220, 130, 1), (180, 150, 1), (260, 90, 1))
+    cases, cfgs = _tm_batch(wave, refcpu, seeds=(7, 8, 9), grids=grids)
+    singles = []
+    for wc, (cfg, model, sidx, stype, sig, ridx, rtype) in zip(cfgs, cases):
+        m32 = {k: v.astype(np.float32) for k, v in model.items()}
+        singles.append(wave.simulate(wc, m32, sidx, stype, sig.astype(np.float32), ridx, rtype, kernel_path=1))
+    got, s = _run_batch(wave, cases, cfgs, schedule)
+    assert (s["tile_cols"], s["tile_rows"]) == schedule[:2]
+    for one, many in zip(singles, got):
+        assert np.abs(one).max() > 0 and np.array_equal(one, many)

@@ -99,26 +99,54 @@ TuneKey tune_key(const wave_batch* b)
 }
 
 // Builds and uploads the work list for the batch's current tile shape and sets the grid.
+} // namespace
+
+bool wave::batch_tile_interior(const StepParams& P, int x0, int r0, int cols, int rows)
+{
+    if (P.is3d || P.NZ != 1 || P.L != 0) return false;
+    const int x1 = x0 + cols, y1 = r0 + rows;   // exclusive ends
+    if (x1 > P.NX || y1 > P.NY) return false;
+    // interior rows of an operator: c in [E, n - E) (the edge band E > H keeps every tap inside the axis)
+    auto interior = [](const Op1D& o, int c0, int c1) { return !o.full && c0 >= o.E && c1 <= o.n - o.E; };
+    if (!interior(P.Dxf, x0, x1) || !interior(P.Dxb, x0, x1) || !interior(P.Dyf, r0, y1) || !interior(P.Dyb, r0, y1))
+        return false;
+    // outside both CPML slabs of each axis (slab() of the kernels returns -1)
+    auto noSlab = [](const Cpml1D& c, int c0, int c1) { return c.w <= 0 || (c.n > 2 * c.w && c0 >= c.w && c1 <= c.n - c.w); };
+    if (P.useCpml && (!noSlab(P.cx, x0, x1) || !noSlab(P.cy, r0, y1))) return false;
+    // outside the ABS frame (damping factor 1)
+    if (P.abs && (x0 < P.absW || x1 > P.NX - P.absW || r0 < P.absW || y1 > P.NY - P.absW)) return false;
+    return true;
+}
+
+namespace {
+
 void build_tiles(wave_batch* b)
 {
     const int n = static_cast<int>(b->shots.size());
     std::vector<BatchTile> tiles;
+    // interior tiles of the lossless 2-D TMz passes are staged in shared memory
+    const int smem = batch_tile_smem(b->eq, b->H, b->cols, b->rows);
+    int interior = 0;
     for (int s = 0; s < n; ++s) {
         wave_handle* h = b->shots[s];
         const int rows = h->NY * h->NZ;
         for (int r0 = 0; r0 < rows; r0 += b->rows)
-            for (int x0 = 0; x0 < h->NX; x0 += b->cols) tiles.push_back({s, x0, r0, 0});
+            for (int x0 = 0; x0 < h->NX; x0 += b->cols) {
+                const bool in = smem > 0 && batch_tile_interior(h->sp, x0, r0, b->cols, b->rows);
+                interior += in ? 1 : 0;
+                tiles.push_back({s, x0, r0, in ? kTileInterior : 0});
+            }
     }
     cudaFree(b->dTiles);
     b->dTiles = nullptr;
     ck(cudaMalloc(&b->dTiles, tiles.size() * sizeof(BatchTile)), "cudaMalloc");
     ck(cudaMemcpy(b->dTiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice), "upload");
     b->ntiles = static_cast<int>(tiles.size());
-    b->sched = BatchSched{b->ntiles, b->cols, b->rows, 0};
+    b->sched = BatchSched{b->ntiles, b->cols, b->rows, interior > 0 ? smem : 0};
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int resident = std::max(1, batch_blocks_per_sm(b->eq, b->H));
+    const int resident = std::max(1, batch_blocks_per_sm(b->eq, b->H, b->sched.smem));
     const int per = b->perSM > 0 ? std::min(b->perSM, resident) : 0;
     b->grid = per > 0 ? std::min(b->ntiles, per * sms) : b->ntiles;
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }

@@ -97,23 +97,6 @@ __device__ __forceinline__ void load_params(StepParams& dst, const StepParams* s
     __syncthreads();
 }
 
-// rows rr..rr+7 of a 32 x kTileRows tile
-__device__ __forceinline__ bool point_tile(const StepParams& P, const BatchTile& w, Pt& p, int rr)
-{
-    p.x = w.x0 + threadIdx.x;
-    const int r = w.r0 + rr + threadIdx.y;
-    if (p.x >= P.NX || r >= P.NY * P.NZ) return false;
-    if (P.NZ == 1) {   // 2-D: no division
-        p.y = r;
-        p.z = 0;
-    } else {
-        p.y = r / P.NZ;
-        p.z = r - p.y * P.NZ;
-    }
-    p.i = p.x + (long long)P.NX * (p.z + (long long)P.NZ * p.y);
-    return true;
-}
-
 // Shared-memory copy of a shot's StepParams in a batched kernel (raw storage:
 // StepParams has default member initialisers, which a __shared__ object
 // cannot run; load_params fills every byte).
@@ -121,11 +104,42 @@ __device__ __forceinline__ bool point_tile(const StepParams& P, const BatchTile&
     __shared__ __align__(16) unsigned char name##_mem[sizeof(StepParams)];          \
     StepParams& name = *reinterpret_cast<StepParams*>(name##_mem)
 
+// The points of one tile of a batched launch: the 32 x 8 block covers
+// S.cols x S.rows points in column groups of 32 and row groups of 8.
+// body(params, point).
+template <class Body>
+__device__ __forceinline__ void tile_points(const StepParams& sP, const BatchTile& w, const BatchSched& S, Body body)
+{
+    for (int xg = 0; xg < S.cols; xg += 32) {
+        const int x = w.x0 + xg + static_cast<int>(threadIdx.x);
+        // four row groups per pass, unrolled, so that their (read-only
+        // path) loads overlap: these kernels are bound by load latency
+        for (int r0 = 0; r0 < S.rows; r0 += 32) {
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                const int rr = r0 + 8 * g;
+                const int r = w.r0 + rr + static_cast<int>(threadIdx.y);
+                if (rr >= S.rows || x >= sP.NX || r >= sP.NY * sP.NZ) continue;
+                Pt p;
+                p.x = x;
+                if (sP.NZ == 1) {   // 2-D: no division
+                    p.y = r;
+                    p.z = 0;
+                } else {
+                    p.y = r / sP.NZ;
+                    p.z = r - p.y * sP.NZ;
+                }
+                p.i = p.x + (long long)sP.NX * (p.z + (long long)sP.NZ * p.y);
+                body(sP, p);
+            }
+        }
+    }
+}
+
 // Persistent batched launches: the block walks the work list with a grid
 // stride; the parameters of a tile's shot are staged in shared memory when
-// the shot changes (every thread first leaves the previous shot's). A tile of
-// S.cols x S.rows points is covered by the 32 x 8 block in column groups of
-// 32 and row groups of 8. body(params, point, shot index).
+// the shot changes (every thread first leaves the previous shot's).
+// body(params, point, shot index).
 template <class Body>
 __device__ __forceinline__ void batch_loop(const StepParams* __restrict__ Ps, const BatchTile* __restrict__ W, const BatchSched& S,
                                            StepParams& sP, Body body)
@@ -138,30 +152,7 @@ __device__ __forceinline__ void batch_loop(const StepParams* __restrict__ Ps, co
             load_params(sP, Ps + w.shot);
             shot = w.shot;
         }
-        for (int xg = 0; xg < S.cols; xg += 32) {
-            const int x = w.x0 + xg + static_cast<int>(threadIdx.x);
-            // four row groups per pass, unrolled, so that their (read-only
-            // path) loads overlap: these kernels are bound by load latency
-            for (int r0 = 0; r0 < S.rows; r0 += 32) {
-#pragma unroll
-                for (int g = 0; g < 4; ++g) {
-                    const int rr = r0 + 8 * g;
-                    const int r = w.r0 + rr + static_cast<int>(threadIdx.y);
-                    if (rr >= S.rows || x >= sP.NX || r >= sP.NY * sP.NZ) continue;
-                    Pt p;
-                    p.x = x;
-                    if (sP.NZ == 1) {   // 2-D: no division
-                        p.y = r;
-                        p.z = 0;
-                    } else {
-                        p.y = r / sP.NZ;
-                        p.z = r - p.y * sP.NZ;
-                    }
-                    p.i = p.x + (long long)sP.NX * (p.z + (long long)sP.NZ * p.y);
-                    body(sP, p, w.shot);
-                }
-            }
-        }
+        tile_points(sP, w, S, [&](const StepParams& P, const Pt& p) { body(P, p, w.shot); });
     }
 }
 

@@ -127,15 +127,24 @@ struct SrcRecParams {
 // one block of a batched launch: shot index and tile origin (x0, row r0 = z + NZ*y);
 // a tile is 32 points along x by kTileRows rows, a 32 x 8 block covering it in 4 passes
 constexpr int kTileRows = 32;
+// BatchTile::flags: the tile lies wholly inside its shot's grid, away from
+// the operators' edge bands, the CPML slabs and the ABS frame (set by the
+// host for the lossless 2-D TMz batch, whose kernels then skip every
+// per-point boundary test on it)
+constexpr int kTileInterior = 1;
 struct BatchTile {
-    int shot, x0, r0, pad;
+    int shot, x0, r0, flags;
 };
+// kTileInterior for the tile [x0, x0+cols) x [r0, r0+rows) of a shot
+bool batch_tile_interior(const StepParams& P, int x0, int r0, int cols, int rows);
 // Schedule of a batched launch: the work list holds `ntiles` tiles of
 // `cols` (a multiple of 32) x `rows` (a multiple of 8) points; the launch's
 // blocks walk the list with a grid stride (one block per tile when the grid
 // equals ntiles, persistent blocks when it is smaller).
+// `smem`: dynamic shared memory of the launch, the staging area of an
+// interior tile (lossless 2-D TMz passes; 0 otherwise).
 struct BatchSched {
-    int ntiles, cols, rows, pad;
+    int ntiles, cols, rows, smem;
 };
 
 struct PrepParams {
@@ -162,7 +171,11 @@ void launch_batch_pass(int eq, int pass, int H, const StepParams* Ps, const Batc
 void launch_batch_aux(const StepParams* Ps, const BatchTile* tiles, const BatchSched& S, int grid, int f0, int f1, int f2,
                       const SrcRecParams* Qs, int* counters, int nshots, bool abs, cudaStream_t s);
 // resident blocks per SM of the batched kernels of an equation (the smaller of the two passes)
-int batch_blocks_per_sm(int eq, int H);
+int batch_blocks_per_sm(int eq, int H, int smem = 0);
+// Staging bytes of an interior tile of the batched passes of `eq` for a
+// cols x rows tile (0: no staged path for it), with the passes' dynamic
+// shared-memory limit raised to them.
+int batch_tile_smem(int eq, int H, int cols, int rows);
 void launch_abs_frame(const StepParams& P, dim3 grid, dim3 block, int f0, int f1, int f2, cudaStream_t s, bool dep = false);
 void launch_finite(const float* a, long long n, int* flag, cudaStream_t s);
 void k_modulus(PrepParams G, const float* rho, const float* v, const float* tau, float sum, int clamp, float* out, cudaStream_t s);
