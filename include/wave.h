@@ -94,9 +94,12 @@ typedef struct wave_config {
                                    were made with.
                                    Config key "edgeOrderReduction" (default 1).   */
     /* Variable (discontinuous) grid, Acquisition/Coordinates.cpp:35-245 and
-     * Derivatives.cpp:852-1656. Acoustic equations only; CPML or no damping
-     * boundary. The grid's index space replaces NX*NY*NZ everywhere (model
-     * arrays, source/receiver indices, wavefields): see wave_grid_*. */
+     * Derivatives.cpp:852-1656. Acoustic equations (2-D and 3-D, free
+     * surface allowed) and 2-D elastic (FD2Delastic::run with
+     * DyfStaggeredX / DybStaggeredX, no free surface); CPML or no damping
+     * boundary; no adjoint. The grid's index space replaces NX*NY*NZ
+     * everywhere (model arrays, source/receiver indices, wavefields): see
+     * wave_grid_*. */
     int useVariableGrid;        /* "useVariableGrid": layers of spacing DH*dhFactor   */
     int useVariableFDoperators; /* "useVariableFDoperators": FD order per layer      */
     int gridLayers;             /* rows of "gridConfigurationFilename" (1..16)       */

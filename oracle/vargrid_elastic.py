@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE ONLY — CPU restatement of the reference's 2-D elastic
-time step on the variable grid (no GPU counterpart yet): the checker for a
-future variable-grid elastic path.
+time step on the variable grid: the checker of the variable-grid elastic
+GPU path (tests/test_gpu_vargrid_elastic.py).
 
 Restates, on top of oracle/vargrid.py (layout, Dxf/Dxb/Dyf/Dyb, the
 interface interpolations, CPML coefficients, density averages):

@@ -129,10 +129,11 @@ def test_gpu_vargrid_chunked_stepping_is_bit_identical(wave, refcpu):
 def test_gpu_vargrid_rejects_what_it_does_not_build(wave, refcpu):
     base = dict(dimension=2, NX=122, NY=100, NZ=1, DH=5.0, DT=5e-4, T=0.01, spatialFDorder=4,
                 useVariableGrid=1, useVariableFDoperators=1, grid=[(0, 1, 4), (31, 3, 4)])
-    for eq, extra in (("elastic", {}), ("acoustic", dict(DampingBoundary=1, BoundaryWidth=10))):
-        cfg = wave.WaveConfig.make(equation=eq, **base, **extra)
+    for eq, extra in (("sh", {}), ("elastic", dict(FreeSurface=1)), ("elastic", dict(dimension=3, NZ=40)),
+                      ("acoustic", dict(DampingBoundary=1, BoundaryWidth=10))):
+        cfg = wave.WaveConfig.make(equation=eq, **dict(base, **extra))
         with pytest.raises(wave.WaveError):
-            wave.Factory.Create("2d", eq).initForwardSolver(cfg)
+            wave.Factory.Create("3d" if extra.get("dimension") == 3 else "2d", eq).initForwardSolver(cfg)
 
 
 @pytest.mark.parametrize("k", [0, 1, 4])

@@ -1,5 +1,5 @@
 """The 2-D elastic variable-grid oracle (oracle/vargrid_elastic.py), checker
-of a future variable-grid elastic path. The reference has no elastic
+of the variable-grid elastic GPU path (tests/test_gpu_vargrid_elastic.py). The reference has no elastic
 variable-grid golden, so it is tied to the pinned regular-grid oracle: with
 one layer the two must agree to rounding, and on a 1:3:1 grid the receivers
 in the fine layers must track an all-fine regular run."""

@@ -578,6 +578,7 @@ std::string adjoint_supported(const wave_handle* h)
         for (int t : h->hSrcType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez sources only";
     }
+    if (h->vg) return "the adjoint gradient is implemented on regular grids";
     if (!h->modelSet) return "set the model first";
     if (!h->seis || h->nrec < 1) return "set receivers first";
     return "";

@@ -141,7 +141,8 @@ void step_once(wave_handle* h);
 // preparation, and the launches of one step (returns the kernel count;
 // mid, if given, is recorded between the velocity and pressure halves)
 void vargrid_setup(wave_handle* h, const VarGridHost& G);
-void vargrid_set_model(wave_handle* h, const float* rho, const float* vp);
+// vs: the S-wave velocity of the 2-D elastic step (null for the acoustic step)
+void vargrid_set_model(wave_handle* h, const float* rho, const float* vp, const float* vs);
 int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrecDone);
 
 // wavefield decomposition (decompose.cu): the copy of the fields before a

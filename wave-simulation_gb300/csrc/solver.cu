@@ -609,14 +609,17 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
     const bool vgrid = c.useVariableGrid != 0 || c.useVariableFDoperators != 0;
     wave::VarGridHost vgHost;
     if (vgrid) {
-        if (c.equation != WAVE_EQ_ACOUSTIC)
-            return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built for the acoustic equations only");
+        const bool el2d = c.equation == WAVE_EQ_ELASTIC && !is3d;
+        if (c.equation != WAVE_EQ_ACOUSTIC && !el2d)
+            return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built for the acoustic equations and 2-D elastic");
+        if (el2d && c.FreeSurface != 0)
+            return fail(nullptr, WAVE_ERR_UNSUPPORTED, "the elastic variable grid is built without a free surface");
         if (c.DampingBoundary == 1)
             return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built with CPML or without a damping boundary (not ABS)");
         if (c.useStencilMatrix)
             return fail(nullptr, WAVE_ERR_ARG, "Variable FD operators are not available for stencil matrices");
         std::string err;
-        int rc = wave::vargrid_build(c, vgHost, err);
+        int rc = wave::vargrid_build(c, vgHost, err, el2d);
         if (rc != WAVE_OK) return fail(nullptr, rc, err);
     }
 
@@ -752,7 +755,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         float* dTp = eq == WAVE_EQ_VISCOELASTIC ? stage(h, taup, n, mem, tmp) : nullptr;
         float* dTs = visco ? stage(h, taus, n, mem, tmp) : nullptr;
         if (h->vg) {
-            wave::vargrid_set_model(h, dRho, dVp);
+            wave::vargrid_set_model(h, dRho, dVp, dVs);
             for (float* p : tmp) cudaFreeAsync(p, s);
             h->check(cudaStreamSynchronize(s), "model preparation");
             h->modelSet = true;

@@ -18,6 +18,13 @@
 // The interpolations run in place where the rows they rewrite read only the
 // coarse-aligned rows of the same interface (which they leave unchanged);
 // otherwise (a 3:9 step) the new values go through a scratch array first.
+//
+// The 2-D elastic step (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297)
+// has the same shape with the ELL operators:
+//   vge_vel   vx += (Dxf sxx + DybStaggeredX sxy) / rho_x, vy += (Dxb sxy + Dyf syy) / rho_y
+//   vg_interp vx (StaggeredX), vy (Full)
+//   vge_str   sxx, syy from Dxb vx, Dyb vy; sxy from DyfStaggeredX vx + Dxf vy
+//   vg_interp sxx, syy (Full), sxy (StaggeredX)
 #include <cuda_runtime.h>
 
 #include "handle.h"
@@ -221,8 +228,147 @@ __global__ void __launch_bounds__(256) vg_model(long long N, int naxes, const fl
     }
 }
 
-template <class K>
-void launch(K kernel, dim3 grid, dim3 block, bool dep, cudaStream_t s, const VgParams& P)
+// ---------------------------------------------------------------- elastic
+struct VgeParams {
+    long long N;
+    float* vx;
+    float* vy;
+    float* sxx;
+    float* syy;
+    float* sxy;
+    float* psi[8];              // sxx_x, sxy_y, sxy_x, syy_y, vxx, vyy, vxy, vyx
+    const float* M;
+    const float* mu;
+    const float* muXY;
+    const float* irx;
+    const float* iry;
+    const int* col[8];          // as VarGridDev: 0 Dxf, 1 Dyf, 3 Dxb, 4 Dyb, 6 DyfStaggeredX, 7 DybStaggeredX
+    const float* val[8];
+    int W[8];
+    const unsigned short* cpc[2];
+    const float* cpt[2];
+};
+
+__device__ __forceinline__ float vge_row(const VgeParams& P, int op, long long i, const float* __restrict__ u)
+{
+    const int* __restrict__ c = P.col[op] + i;
+    const float* __restrict__ v = P.val[op] + i;
+    float s = 0.0f;
+    for (int k = 0; k < P.W[op]; ++k) s = __fmaf_rn(v[k * P.N], u[c[k * P.N]], s);
+    return s;
+}
+
+// CPML::applyCPML (CPML.cpp:84-95), as vg_cpml
+__device__ __forceinline__ void vge_cpml(const VgeParams& P, float& d, int slot, int axis, bool half, long long i)
+{
+    const unsigned code = P.cpc[axis][i];
+    if (code == 0) return;
+    const float a = __ldg(P.cpt[axis] + 4 * code + (half ? 2 : 0));
+    const float b = __ldg(P.cpt[axis] + 4 * code + (half ? 3 : 1));
+    if (a == 0.0f && b == 0.0f) return;
+    const float ps = __fadd_rn(__fmul_rn(P.psi[slot][i], b), __fmul_rn(a, d));
+    P.psi[slot][i] = ps;
+    d = __fadd_rn(d, ps);
+}
+
+// velocities (ForwardSolver2Delastic.cpp:150-190): the CPML profiles of
+// CPML2D: sxx_x half-x, sxy_y full-y, sxy_x full-x, syy_y half-y
+template <bool CPML>
+__global__ void __launch_bounds__(256) vge_vel(VgeParams P)
+{
+    dependent_launch_prologue();
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    float d = vge_row(P, 0, i, P.sxx);
+    if (CPML) vge_cpml(P, d, 0, 0, true, i);
+    float d2 = vge_row(P, 7, i, P.sxy);
+    if (CPML) vge_cpml(P, d2, 1, 1, false, i);
+    P.vx[i] = __fadd_rn(P.vx[i], __fmul_rn(__fadd_rn(d, d2), P.irx[i]));
+    d = vge_row(P, 3, i, P.sxy);
+    if (CPML) vge_cpml(P, d, 2, 0, false, i);
+    d2 = vge_row(P, 1, i, P.syy);
+    if (CPML) vge_cpml(P, d2, 3, 1, true, i);
+    P.vy[i] = __fadd_rn(P.vy[i], __fmul_rn(__fadd_rn(d, d2), P.iry[i]));
+}
+
+// stresses (ForwardSolver2Delastic.cpp:200-260): vxx full-x, vyy full-y,
+// vxy half-y, vyx half-x
+template <bool CPML>
+__global__ void __launch_bounds__(256) vge_str(VgeParams P)
+{
+    dependent_launch_prologue();
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    float vxx = vge_row(P, 3, i, P.vx);
+    if (CPML) vge_cpml(P, vxx, 4, 0, false, i);
+    float vyy = vge_row(P, 4, i, P.vy);
+    if (CPML) vge_cpml(P, vyy, 5, 1, false, i);
+    const float u = __fmul_rn(__fadd_rn(vxx, vyy), P.M[i]);
+    const float mu = P.mu[i];
+    P.sxx[i] = __fsub_rn(__fadd_rn(P.sxx[i], u), __fmul_rn(2.0f, __fmul_rn(vyy, mu)));
+    P.syy[i] = __fsub_rn(__fadd_rn(P.syy[i], u), __fmul_rn(2.0f, __fmul_rn(vxx, mu)));
+    float vxy = vge_row(P, 6, i, P.vx);
+    if (CPML) vge_cpml(P, vxy, 6, 1, true, i);
+    float vyx = vge_row(P, 0, i, P.vy);
+    if (CPML) vge_cpml(P, vyx, 7, 0, true, i);
+    P.sxy[i] = __fadd_rn(P.sxy[i], __fmul_rn(__fadd_rn(vxy, vyx), P.muXY[i]));
+}
+
+// Elastic::prepareForModelling on the 2-D variable grid: M = rho vp^2,
+// mu = rho vs^2; inverse densities averaged with the grid's partners
+// (Modelparameter.cpp:336-446, 633-640); the shear modulus at the
+// staggered xy point: calcAverageMatrixXY's 4-point average of 1/max(mu, 1)
+// (2 points on the bottom / right edge, 1 in the corner), inverted, results
+// below 4 set to 0 (Modelparameter.cpp:449-533, ModelparameterSeismic.cpp:
+// 421-432). A partner the index map does not find counts as the point itself.
+__device__ __forceinline__ float inv_mu(const float* mu, int j) { return __fdiv_rn(1.0f, fmaxf(mu[j], 1.0f)); }
+
+__global__ void __launch_bounds__(256) vge_model(long long N, const float* __restrict__ rho, const float* __restrict__ vp,
+                                                 const float* __restrict__ vs, const int* __restrict__ px,
+                                                 const int* __restrict__ py, float* M, float* mu, float* irx, float* iry)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float r = rho[i];
+    M[i] = __fmul_rn(__fmul_rn(r, vp[i]), vp[i]);
+    mu[i] = __fmul_rn(__fmul_rn(r, vs[i]), vs[i]);
+    const int* part[2] = {px, py};
+    float* out[2] = {irx, iry};
+    for (int a = 0; a < 2; ++a) {
+        const int j = part[a][i];
+        const float avg = j >= 0 ? __fadd_rn(__fmul_rn(0.5f, r), __fmul_rn(0.5f, rho[j])) : r;
+        const float inv = __fdiv_rn(1.0f, avg);
+        out[a][i] = isfinite(inv) ? inv : 0.0f;
+    }
+}
+
+// after vge_model (it reads mu of the partners)
+__global__ void __launch_bounds__(256) vge_shear(long long N, const float* __restrict__ mu, const int* __restrict__ s1,
+                                                 const int* __restrict__ s2, const int* __restrict__ s3, float* muXY)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int a = s1[i], b = s2[i], c = s3[i];
+    const float ii = inv_mu(mu, static_cast<int>(i));
+    float s;
+    if (a >= 0 && b >= 0) {
+        s = __fmul_rn(0.25f, ii);
+        s = __fadd_rn(s, __fmul_rn(0.25f, inv_mu(mu, a)));
+        s = __fadd_rn(s, __fmul_rn(0.25f, inv_mu(mu, b)));
+        s = __fadd_rn(s, __fmul_rn(0.25f, c >= 0 ? inv_mu(mu, c) : ii));
+    } else if (a >= 0) {
+        s = __fadd_rn(__fmul_rn(0.5f, inv_mu(mu, a)), __fmul_rn(0.5f, ii));
+    } else if (b >= 0) {
+        s = __fadd_rn(__fmul_rn(0.5f, inv_mu(mu, b)), __fmul_rn(0.5f, ii));
+    } else {
+        s = ii;
+    }
+    const float av = __fdiv_rn(1.0f, s);
+    muXY[i] = av < 4.0f ? 0.0f : av;
+}
+
+template <class K, class Prm>
+void launch(K kernel, dim3 grid, dim3 block, bool dep, cudaStream_t s, const Prm& P)
 {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = grid;
@@ -234,6 +380,37 @@ void launch(K kernel, dim3 grid, dim3 block, bool dep, cudaStream_t s, const VgP
     cfg.attrs = attr;
     cfg.numAttrs = dep ? 1 : 0;
     cudaLaunchKernelEx(&cfg, kernel, P);
+}
+
+// the elastic step's CPML memory variables, in VgeParams::psi order
+constexpr int kElasticPsi[8] = {PS_SXX_X, PS_SXY_Y, PS_SXY_X, PS_SYY_Y, PS_VXX, PS_VYY, PS_VXY, PS_VYX};
+
+VgeParams elastic_params_of(wave_handle* h)
+{
+    const VarGridDev& G = *h->vg;
+    VgeParams P{};
+    P.N = G.N;
+    P.vx = h->f[F_VX];
+    P.vy = h->f[F_VY];
+    P.sxx = h->f[F_SXX];
+    P.syy = h->f[F_SYY];
+    P.sxy = h->f[F_SXY];
+    for (int k = 0; k < 8; ++k) P.psi[k] = h->psi[kElasticPsi[k]];
+    P.M = h->m[M_M];
+    P.mu = h->m[M_MU];
+    P.muXY = h->m[M_MUXY];
+    P.irx = h->m[M_IRX];
+    P.iry = h->m[M_IRY];
+    for (int k = 0; k < 8; ++k) {
+        P.col[k] = G.col[k];
+        P.val[k] = G.val[k];
+        P.W[k] = G.W[k];
+    }
+    for (int a = 0; a < 2; ++a) {
+        P.cpc[a] = G.cpCode[a];
+        P.cpt[a] = G.cpTab[a];
+    }
+    return P;
 }
 
 VgParams params_of(wave_handle* h)
@@ -283,8 +460,10 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
     const bool is3d = h->is3d();
     D->N = G.L.N;
     D->is3d = is3d;
-    const EllHost* ops[6] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb};
-    for (int k = 0; k < 6; ++k) {
+    const bool elastic = h->cfg.equation == WAVE_EQ_ELASTIC;
+    D->elastic = elastic ? 1 : 0;
+    const EllHost* ops[8] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb, &G.DyfSX, &G.DybSX};
+    for (int k = 0; k < (elastic ? 8 : 6); ++k) {
         if (!is3d && (k == 2 || k == 5)) continue;
         D->W[k] = ops[k]->W;
         D->col[k] = upload(h, ops[k]->col);
@@ -301,20 +480,30 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
         D->icol[k] = upload(h, in[k]->col);
         D->iw[k] = upload(h, in[k]->w);
     }
-    if (total > 0) D->itmp = h->alloc<float>(total);
+    // the elastic stress interpolation rewrites two fields with the Full rows
+    if (total > 0) D->itmp = h->alloc<float>(elastic ? 2 * total : total);
     if (h->cfg.DampingBoundary == 2) {
         for (int a = 0; a < (is3d ? 3 : 2); ++a) {
             D->cpCode[a] = upload(h, G.cpCode[a]);
             D->cpTab[a] = upload(h, G.cpTab[a]);
         }
-        const int slots[6] = {PS_P_X, PS_P_Y, PS_P_Z, PS_VXX, PS_VYY, PS_VZZ};
-        for (int k = 0; k < 6; ++k) {
-            if (!is3d && (k == 2 || k == 5)) continue;
-            h->psi[slots[k]] = h->alloc<float>(D->N);
-            h->psiLen[slots[k]] = D->N;
+        if (elastic) {
+            for (int slot : kElasticPsi) {
+                h->psi[slot] = h->alloc<float>(D->N);
+                h->psiLen[slot] = D->N;
+            }
+        } else {
+            const int slots[6] = {PS_P_X, PS_P_Y, PS_P_Z, PS_VXX, PS_VYY, PS_VZZ};
+            for (int k = 0; k < 6; ++k) {
+                if (!is3d && (k == 2 || k == 5)) continue;
+                h->psi[slots[k]] = h->alloc<float>(D->N);
+                h->psiLen[slots[k]] = D->N;
+            }
         }
     }
     for (int a = 0; a < (is3d ? 3 : 2); ++a) D->partner[a] = upload(h, G.avgPartner[a]);
+    if (elastic)
+        for (int a = 0; a < 3; ++a) D->shear[a] = upload(h, G.shearPartner[a]);
     for (int pass = 0; pass < 2; ++pass) {
         const ClassHost& C = G.cls[pass];
         if (!C.ok) continue;
@@ -329,7 +518,7 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
     h->vg = D;
 }
 
-void vargrid_set_model(wave_handle* h, const float* rho, const float* vp)
+void vargrid_set_model(wave_handle* h, const float* rho, const float* vp, const float* vs)
 {
     const VarGridDev& G = *h->vg;
     auto mat = [&](int slot) {
@@ -337,6 +526,15 @@ void vargrid_set_model(wave_handle* h, const float* rho, const float* vp)
         h->sp.m[slot] = h->m[slot];
         return h->m[slot];
     };
+    if (G.elastic) {
+        const unsigned blocks = static_cast<unsigned>((G.N + 255) / 256);
+        float* mu = mat(M_MU);
+        vge_model<<<blocks, 256, 0, h->stream>>>(G.N, rho, vp, vs, G.partner[0], G.partner[1], mat(M_M), mu, mat(M_IRX),
+                                                 mat(M_IRY));
+        vge_shear<<<blocks, 256, 0, h->stream>>>(G.N, mu, G.shear[0], G.shear[1], G.shear[2], mat(M_MUXY));
+        h->check(cudaGetLastError(), "variable grid model preparation");
+        return;
+    }
     float* M = mat(M_M);
     float* irx = mat(M_IRX);
     float* iry = mat(M_IRY);
@@ -353,7 +551,7 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
     const VgParams P = params_of(h);
     const dim3 block(256);
     const dim3 grid(static_cast<unsigned>((G.N + 255) / 256));
-    const bool cp = P.cpml != 0;
+    const bool cp = G.cpCode[0] != nullptr;
     // kernel path 1 (generic only) keeps the ELL blocks; otherwise the
     // stencil classes wherever they were built
     const bool cls[2] = {h->kernelPath != 1 && G.clsId[0] != nullptr, h->kernelPath != 1 && G.clsId[1] != nullptr};
@@ -384,7 +582,12 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
     K vel = velK[G.is3d ? 1 : 0][cp ? 1 : 0][cls[0] ? 1 : 0];
     K pres = presK[G.is3d ? 1 : 0][cp ? 1 : 0][cls[1] ? 1 : 0];
     int launches = 0;
-    launch(vel, grid, block, dep, h->stream, with_classes(0));
+    const VgeParams E = G.elastic ? elastic_params_of(h) : VgeParams{};
+    if (G.elastic) {
+        launch(cp ? vge_vel<true> : vge_vel<false>, grid, block, dep, h->stream, E);
+    } else {
+        launch(vel, grid, block, dep, h->stream, with_classes(0));
+    }
     ++launches;
     const bool interp = G.nInterp[0] + G.nInterp[1] + G.nInterp[2] > 0;
     auto run_interp = [&](VgInterp I, int lists) {
@@ -446,15 +649,36 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
         }
     };
     if (interp) {
-        // vx: StaggeredX, vy: Full, vz: StaggeredZ (ForwardSolver3Dacoustic.cpp:139-197)
+        // vx: StaggeredX, vy: Full, vz: StaggeredZ (ForwardSolver3Dacoustic.cpp:139-197,
+        // ForwardSolver2Delastic.cpp:190-197)
         const int kinds[3] = {1, 0, 2};
         float* const fields[3] = {P.vx, P.vy, G.is3d ? P.vz : nullptr};
         interp_fields(kinds, fields, 3, false);
     }
     if (mid) cudaEventRecord(*mid, h->stream);
-    launch(pres, grid, block, dep, h->stream, with_classes(1));
+    if (G.elastic) {
+        launch(cp ? vge_str<true> : vge_str<false>, grid, block, dep, h->stream, E);
+    } else {
+        launch(pres, grid, block, dep, h->stream, with_classes(1));
+    }
     ++launches;
-    if (interp && G.nInterp[0] > 0) {
+    if (interp && G.elastic) {
+        // sxx, syy: Full, sxy: StaggeredX (ForwardSolver2Delastic.cpp:262-270); sources
+        // and receivers in the same launch when none is on an interface row
+        bool apart = true;
+        auto off_interface = [&](const std::vector<long long>& idx) {
+            for (long long i : idx) {
+                int x, y, z;
+                G.L.coord(i, x, y, z);
+                if (G.L.onIfaceY[y]) apart = false;
+            }
+        };
+        off_interface(h->hSrcIdx);
+        off_interface(h->hRecIdx);
+        const int kinds[3] = {0, 0, 1};
+        float* const fields[3] = {E.sxx, E.syy, E.sxy};
+        interp_fields(kinds, fields, 3, apart && h->kernelPath != 1);
+    } else if (interp && G.nInterp[0] > 0) {
         // sources and receivers in the same launch when none is on an interface row
         bool apart = true;
         auto off_interface = [&](const std::vector<long long>& idx) {

@@ -83,6 +83,9 @@ struct VarGridHost {
     std::vector<unsigned short> cpCode[3];
     std::vector<float> cpTab[3];
     std::vector<int> avgPartner[3];    // averaging partner per axis (-1: the point alone)
+    // elastic (2-D): the 4-point shear-modulus average's partners (x+f, y),
+    // (x, y+f), (x+f, y+f), f the layer's dhFactor (-1: outside the grid)
+    std::vector<int> shearPartner[3];
     long long nSurface = 0;            // rows with y == 0 (the first rows of layer 0)
 };
 
@@ -90,7 +93,8 @@ struct VarGridHost {
 int vargrid_layout(const wave_config& c, VarGridLayout& L, std::string& err);
 // Every operator, interpolation, CPML coefficient and averaging partner of
 // the acoustic equations on the grid.
-// elastic: also the staggered-x y-derivatives of the elastic step
+// elastic: also the staggered-x y-derivatives and the shear-average
+// partners of the 2-D elastic step
 int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool elastic = false);
 
 // device side of a variable-grid handle (vargrid.cu)
@@ -98,10 +102,11 @@ struct VarGridDev {
     VarGridLayout L;                        // host copy of the index space
     long long N = 0;
     int is3d = 0;
+    int elastic = 0;                        // 2-D elastic step (else acoustic)
     int nOps = 0;
-    int W[6] = {};                          // Dxf, Dyf, Dzf, Dxb, Dyb, Dzb
-    const int* col[6] = {};
-    const float* val[6] = {};
+    int W[8] = {};                          // Dxf, Dyf, Dzf, Dxb, Dyb, Dzb, DyfStaggeredX, DybStaggeredX
+    const int* col[8] = {};
+    const float* val[8] = {};
     int nInterp[3] = {};                    // full, staggered x, staggered z
     const int* irow[3] = {};
     const int* icol[3] = {};
@@ -111,6 +116,7 @@ struct VarGridDev {
     const unsigned short* cpCode[3] = {};   // CPML coefficient code per axis and point (null: no CPML)
     const float* cpTab[3] = {};             // 4 floats per code
     const int* partner[3] = {};
+    const int* shear[3] = {};               // elastic: shear-average partners
     long long nSurface = 0;
     int fs = 0;
     // stencil classes per pass (null: not available)

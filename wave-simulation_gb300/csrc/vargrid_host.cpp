@@ -731,6 +731,17 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool e
             G.avgPartner[ax][i] = static_cast<int>(j);
         }
     }
+    if (elastic && !is3d) {
+        // calcAverageMatrixXY's 4-point partners (Modelparameter.cpp:449-533)
+        for (auto& v : G.shearPartner) v.assign(N, -1);
+        for (long long i = 0; i < N; ++i) {
+            const long long f = L.dhf[L.layerY[Y[i]]];
+            const bool okx = X[i] + f < L.NX, oky = Y[i] + f < L.NY;
+            if (okx) G.shearPartner[0][i] = static_cast<int>(L.index(X[i] + f, Y[i], Z[i]));
+            if (oky) G.shearPartner[1][i] = static_cast<int>(L.index(X[i], Y[i] + f, Z[i]));
+            if (okx && oky) G.shearPartner[2][i] = static_cast<int>(L.index(X[i] + f, Y[i] + f, Z[i]));
+        }
+    }
     G.nSurface = static_cast<long long>(L.vnx[0]) * L.vnz[0];   // layer 0 starts at y = 0
     const EllHost* vel[3] = {&G.Dxf, &G.Dyf, &G.Dzf};
     const EllHost* pres[3] = {&G.Dxb, &G.Dyb, &G.Dzb};
