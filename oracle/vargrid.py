@@ -392,8 +392,9 @@ class Operators:
             self.IStagX = self._interp("x")
             if is3d:
                 self.IStagZ = self._interp("z")
+                self.IStagXZ = self._interp("xz")
         else:   # variable FD orders on a regular grid: no interpolation
-            self.IFull = self.IStagX = self.IStagZ = sp.identity(g.N, dtype=dtype, format="csr")
+            self.IFull = self.IStagX = self.IStagZ = self.IStagXZ = sp.identity(g.N, dtype=dtype, format="csr")
 
     def _val(self, order: int, j: int, dl: int, img: int = -1):
         """coefficient / DH (ValueType), then * DT (FDTD2D.cpp:212-215)."""
@@ -463,7 +464,8 @@ class Operators:
         return self._finish(rows, cols, vals)
 
     def _interp(self, kind):
-        """Derivatives.cpp:1252-1335 / 1356-1440 / 1462-1546: identity off the
+        """Derivatives.cpp:1252-1335 / 1356-1440 / 1462-1546 / 1568-1661
+        (full, staggered x, staggered z, staggered xz): identity off the
         interfaces, bilinear from the coarse-aligned points on them."""
         g = self.g
         d = np.dtype(self.dtype).type
@@ -494,12 +496,18 @@ class Operators:
                    (x + ff < g.NX, x + f - mx, z - mz, mx * (f - mz)),
                    ((x >= mx) & (z + 2 * ff < g.NZ), x - mx, z + f - mz, (f - mx) * mz),
                    ((x + ff < g.NX) & (z + 2 * ff < g.NZ), x + f - mx, z + f - mz, mx * mz)]
-        else:
+        elif kind == "z":
             mx, mz = cm(x, f), cm(z - f // 2, f)
             pts = [(z >= mz, x - mx, z - mz, (f - mx) * (f - mz)),
                    (x + 2 * ff < g.NX, x + f - mx, z - mz, mx * (f - mz)),
                    ((x >= mx) & (z + ff < g.NZ), x - mx, z + f - mz, (f - mx) * mz),
                    ((x + 2 * ff < g.NX) & (z + ff < g.NZ), x + f - mx, z + f - mz, mx * mz)]
+        else:
+            mx, mz = cm(x - f // 2, f), cm(z - f // 2, f)
+            pts = [((x >= mx) & (z >= mz), x - mx, z - mz, (f - mx) * (f - mz)),
+                   (x + ff < g.NX, x + f - mx, z - mz, mx * (f - mz)),
+                   ((x >= mx) & (z + ff < g.NZ), x - mx, z + f - mz, (f - mx) * mz),
+                   ((x + ff < g.NX) & (z + ff < g.NZ), x + f - mx, z + f - mz, mx * mz)]
         for ok, X, Z, w in pts:
             rows.append(on[ok]); cols.append(g.coordinate2index(X[ok], y[ok], Z[ok]))
             vals.append((w[ok].astype(self.dtype) * den[ok]).astype(self.dtype))

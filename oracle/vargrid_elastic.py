@@ -23,9 +23,11 @@ import numpy as np
 from oracle import vargrid as vg
 
 
-def _stag_rows(g: vg.VarGrid, y: int, x: int, orders, var_order: bool, forward: bool):
-    """Taps [(X, Y, order, j, dh layer)] of one row of DyfStaggeredX (forward)
-    or DybStaggeredX (Derivatives.cpp:852-1011)."""
+def _stag_rows(g: vg.VarGrid, y: int, c: int, n: int, orders, var_order: bool, forward: bool):
+    """Taps [(C, Y, order, j, dh layer)] of one row of DyfStaggeredX / Z
+    (forward) or DybStaggeredX / Z (Derivatives.cpp:852-1168): c is the row's
+    coordinate along the staggered axis (x or z), n that axis' length, C the
+    tap's coordinate along it."""
     layer = int(g.layer_y[y])
     order = orders[layer] if var_order else orders[0]
     dist = int(g.dist_y[y]) // g.dhf[layer]
@@ -42,7 +44,7 @@ def _stag_rows(g: vg.VarGrid, y: int, x: int, orders, var_order: bool, forward: 
     def trans(yy):
         return int(g.trans_y[yy])
 
-    X = [x] * order
+    X = [c] * order
     out = []
     if forward:
         if on and tr == -1:
@@ -52,7 +54,7 @@ def _stag_rows(g: vg.VarGrid, y: int, x: int, orders, var_order: bool, forward: 
         if on and tr == 1 and X[0] >= f // 3:
             X[1] -= f // 3
         yq = y + (order // 2) * f
-        if iface(yq) and trans(yq) == -1 and X[0] < g.NX - f // 3:
+        if iface(yq) and trans(yq) == -1 and X[0] < n - f // 3:
             X[order - 1] += f // 3
         for j in range(order):
             Y = y + f * (j - order // 2 + 1)
@@ -61,7 +63,7 @@ def _stag_rows(g: vg.VarGrid, y: int, x: int, orders, var_order: bool, forward: 
         return out
     f = g.dhf[layer]
     yq = y - (order // 2) * f
-    if iface(yq) and trans(yq) == 1 and X[1] < g.NX - f // 3:
+    if iface(yq) and trans(yq) == 1 and X[1] < n - f // 3:
         X[0] += f // 3
     if on and tr == -1 and X[1] >= f // 3:
         X[0] -= f // 3
@@ -77,11 +79,14 @@ def _stag_rows(g: vg.VarGrid, y: int, x: int, orders, var_order: bool, forward: 
     return out
 
 
-def staggered_x_operator(op: vg.Operators, orders, var_order: bool, forward: bool):
-    """DyfStaggeredX / DybStaggeredX times DT, as a CSR matrix. The rows of
-    one depth y differ only at the x edges (the shifted taps are guarded by
-    x >= f/3 and x < NX - f/3), so each (y, x class) stencil is built once."""
+def staggered_operator(op: vg.Operators, orders, var_order: bool, forward: bool, axis: str = "x"):
+    """DyfStaggeredX / DybStaggeredX (axis "x") or DyfStaggeredZ /
+    DybStaggeredZ (axis "z") times DT, as a CSR matrix. The rows of one depth
+    y differ only at the edges of the staggered axis (the shifted taps are
+    guarded by c >= f/3 and c < n - f/3), so each (y, edge class) stencil is
+    built once."""
     g = op.g
+    n = g.NX if axis == "x" else g.NZ
     rows, cols, vals = [], [], []
     order_rows = np.argsort(g.y, kind="stable")
     bounds = np.searchsorted(g.y[order_rows], np.arange(g.NY + 1))
@@ -91,17 +96,24 @@ def staggered_x_operator(op: vg.Operators, orders, var_order: bool, forward: boo
             continue
         layer = int(g.layer_y[y])
         f = g.dhf[layer] if not (g.on_iface_y[y] and g.trans_y[y] == -1 and forward) else g.dhf[layer + 1]
-        xs = g.x[r]
-        cls = (xs >= f // 3).astype(int) * 2 + (xs < g.NX - f // 3).astype(int)
-        for c in np.unique(cls):
-            rr = r[cls == c]
-            x_rep = int(g.x[rr[0]])
-            for X, Y, o, j, dl in _stag_rows(g, y, x_rep, orders, var_order, forward):
-                dx = X - x_rep
-                cols.append(g.coordinate2index(g.x[rr] + dx, Y, g.z[rr]))
+        cs = g.x[r] if axis == "x" else g.z[r]
+        cls = (cs >= f // 3).astype(int) * 2 + (cs < n - f // 3).astype(int)
+        for k in np.unique(cls):
+            rr = r[cls == k]
+            c_rep = int((g.x if axis == "x" else g.z)[rr[0]])
+            for C, Y, o, j, dl in _stag_rows(g, y, c_rep, n, orders, var_order, forward):
+                dc = C - c_rep
+                if axis == "x":
+                    cols.append(g.coordinate2index(g.x[rr] + dc, Y, g.z[rr]))
+                else:
+                    cols.append(g.coordinate2index(g.x[rr], Y, g.z[rr] + dc))
                 rows.append(rr)
                 vals.append(np.full(len(rr), op._val(o, j, dl), dtype=op.dtype))
     return op._finish(rows, cols, vals)
+
+
+def staggered_x_operator(op: vg.Operators, orders, var_order: bool, forward: bool):
+    return staggered_operator(op, orders, var_order, forward, "x")
 
 
 def shear_average_xy(g: vg.VarGrid, mu, dtype=np.float32):
@@ -137,6 +149,49 @@ def shear_average_xy(g: vg.VarGrid, mu, dtype=np.float32):
     out[rgt] = (h * inv[cr] + h * inv[rgt]).astype(dtype)
     corner = np.nonzero(~okx & ~oky)[0]
     out[corner] = inv[corner]
+    with np.errstate(divide="ignore"):
+        av = (d(1) / out).astype(dtype)
+    av[av < 4] = 0
+    return av
+
+
+def shear_average(g: vg.VarGrid, mu, pair: str, dtype=np.float32):
+    """calcAveragedSWaveModulus with the 4-point matrix of the axis pair
+    "xy", "xz" or "yz" (calc4PointAverageMatrixRow and calcAverageMatrixXY /
+    XZ / YZ, Modelparameter.cpp:449-624; ModelparameterSeismic.cpp:421-432):
+    the point and its neighbours f along each axis of the pair and along
+    both (f the layer's dhFactor); with one axis past the grid the point and
+    its neighbour along the other axis, with both past it the point alone;
+    1/max(mu, 1) averaged, inverted, results below 4 set to 0."""
+    d = np.dtype(dtype).type
+    mu = np.asarray(mu, dtype=dtype).copy()
+    mu[mu < 1] = 1
+    inv = (d(1) / mu).astype(dtype)
+    f = np.array(g.dhf, dtype=np.int64)[g.layer]
+    c = {"x": g.x, "y": g.y, "z": g.z}
+    n = {"x": g.NX, "y": g.NY, "z": g.NZ}
+    a, b = pair[0], pair[1]
+
+    def idx(sel, da, db):
+        p = {k: c[k][sel].copy() for k in "xyz"}
+        p[a] = p[a] + da * f[sel]
+        p[b] = p[b] + db * f[sel]
+        return g.coordinate2index(p["x"], p["y"], p["z"])
+
+    oka, okb = c[a] + f < n[a], c[b] + f < n[b]
+    out = np.zeros(g.N, dtype=dtype)
+    q, h = d(0.25), d(0.5)
+    i = np.nonzero(oka & okb)[0]
+    s = (q * inv[i]).astype(dtype)
+    s = (s + q * inv[idx(i, 1, 0)]).astype(dtype)
+    s = (s + q * inv[idx(i, 0, 1)]).astype(dtype)
+    out[i] = (s + q * inv[idx(i, 1, 1)]).astype(dtype)
+    i = np.nonzero(oka & ~okb)[0]
+    out[i] = (h * inv[idx(i, 1, 0)] + h * inv[i]).astype(dtype)
+    i = np.nonzero(~oka & okb)[0]
+    out[i] = (h * inv[idx(i, 0, 1)] + h * inv[i]).astype(dtype)
+    i = np.nonzero(~oka & ~okb)[0]
+    out[i] = inv[i]
     with np.errstate(divide="ignore"):
         av = (d(1) / out).astype(dtype)
     av[av < 4] = 0
@@ -225,6 +280,119 @@ class ElasticVarGrid2D:
                 out[r] = d((self.sxx[i] + self.syy[i]) * d(0.5))
             else:
                 out[r] = (self.vx if k == 2 else self.vy)[i]
+        return out
+
+    def run(self, nt: int) -> np.ndarray:
+        out = np.zeros((len(self.rec_idx), nt), dtype=self.dtype)
+        for t in range(nt):
+            out[:, t] = self.step(t)
+        return out
+
+
+class ElasticVarGrid3D:
+    """FD3Delastic::run on a 3-D variable grid (ForwardSolver3Delastic.cpp:
+    120-414), CPML or no damping boundary, no free surface: DybStaggeredX /
+    DybStaggeredZ for the y-derivatives of sxy / syz in the velocity update,
+    DyfStaggeredX / DyfStaggeredZ for those of vx / vz in the shear update,
+    and the interface interpolations vx StaggeredX, vy Full, vz StaggeredZ,
+    sxx / syy / szz Full, sxy StaggeredX, sxz StaggeredXZ, syz StaggeredZ
+    (applied twice, as the reference does)."""
+
+    def __init__(self, g: vg.VarGrid, orders, DT: float, rho, vp, vs, cpml: dict | None,
+                 src_idx, src_type, signals, rec_idx, rec_type, dtype=np.float32, var_order: bool = True,
+                 edge: bool = True, var_grid: bool = True):
+        if g.NZ < 2:
+            raise ValueError("3-D only")
+        self.g, self.dtype = g, dtype
+        self.op = vg.Operators(g, orders, DT, False, dtype, var_order, edge, var_grid)
+        self.DyfSX = staggered_operator(self.op, orders, var_order, True, "x")
+        self.DybSX = staggered_operator(self.op, orders, var_order, False, "x")
+        self.DyfSZ = staggered_operator(self.op, orders, var_order, True, "z")
+        self.DybSZ = staggered_operator(self.op, orders, var_order, False, "z")
+        rho = np.asarray(rho, dtype=dtype)
+        vp = np.asarray(vp, dtype=dtype)
+        vs = np.asarray(vs, dtype=dtype)
+        self.M = (rho * vp * vp).astype(dtype)
+        self.mu = (rho * vs * vs).astype(dtype)
+        self.muXY = shear_average(g, self.mu, "xy", dtype)
+        self.muXZ = shear_average(g, self.mu, "xz", dtype)
+        self.muYZ = shear_average(g, self.mu, "yz", dtype)
+        self.irx, self.iry, self.irz = vg.inverse_density_averages(g, rho, dtype)
+        self.cpml = cpml
+        z = lambda: np.zeros(g.N, dtype=dtype)
+        self.f = {k: z() for k in ("vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz")}
+        self.psi = {k: z() for k in ("sxx_x", "sxy_y", "sxz_z", "sxy_x", "syy_y", "syz_z", "sxz_x", "syz_y", "szz_z",
+                                     "vxx", "vyy", "vzz", "vxy", "vyx", "vxz", "vzx", "vyz", "vzy")}
+        self.src_idx = np.asarray(src_idx, np.int64)
+        self.src_type = np.asarray(src_type)
+        self.signals = np.asarray(signals, dtype=dtype)
+        self.rec_idx = np.asarray(rec_idx, np.int64)
+        self.rec_type = np.asarray(rec_type)
+
+    def _cpml(self, upd, key, ax, half):
+        if self.cpml is None:
+            return upd
+        af, bf, ah, bh = self.cpml[ax]
+        a, b = (ah, bh) if half else (af, bf)
+        ps = (self.psi[key] * b).astype(self.dtype)
+        ps = (ps + (a * upd).astype(self.dtype)).astype(self.dtype)
+        self.psi[key] = ps
+        return (upd + ps).astype(self.dtype)
+
+    def _vel(self, terms, ir):
+        dt = self.dtype
+        u = None
+        for mat, field, key, ax, half in terms:
+            t = self._cpml(mat @ self.f[field], key, ax, half)
+            u = t if u is None else (u + t).astype(dt)
+        return (u * ir).astype(dt)
+
+    def step(self, t: int):
+        op, dt, d, F = self.op, self.dtype, np.dtype(self.dtype).type, self.f
+        # velocities (CPML3D: forward derivatives take the half profiles)
+        u = self._vel([(op.Dxf, "sxx", "sxx_x", "x", True), (self.DybSX, "sxy", "sxy_y", "y", False),
+                       (op.Dzb, "sxz", "sxz_z", "z", False)], self.irx)
+        F["vx"] = op.IStagX @ (F["vx"] + u).astype(dt)
+        u = self._vel([(op.Dxb, "sxy", "sxy_x", "x", False), (op.Dyf, "syy", "syy_y", "y", True),
+                       (op.Dzb, "syz", "syz_z", "z", False)], self.iry)
+        F["vy"] = op.IFull @ (F["vy"] + u).astype(dt)
+        u = self._vel([(op.Dxb, "sxz", "sxz_x", "x", False), (self.DybSZ, "syz", "syz_y", "y", False),
+                       (op.Dzf, "szz", "szz_z", "z", True)], self.irz)
+        F["vz"] = op.IStagZ @ (F["vz"] + u).astype(dt)
+        # normal stresses
+        vxx = self._cpml(op.Dxb @ F["vx"], "vxx", "x", False)
+        vyy = self._cpml(op.Dyb @ F["vy"], "vyy", "y", False)
+        vzz = self._cpml(op.Dzb @ F["vz"], "vzz", "z", False)
+        u = ((((vxx + vyy).astype(dt) + vzz).astype(dt)) * self.M).astype(dt)
+        sxx = (F["sxx"] + u).astype(dt)
+        syy = (F["syy"] + u).astype(dt)
+        szz = (F["szz"] + u).astype(dt)
+        two = d(2.0)
+        sxx = (sxx - (two * (((vyy + vzz).astype(dt)) * self.mu).astype(dt)).astype(dt)).astype(dt)
+        syy = (syy - (two * (((vxx + vzz).astype(dt)) * self.mu).astype(dt)).astype(dt)).astype(dt)
+        szz = (szz - (two * (((vxx + vyy).astype(dt)) * self.mu).astype(dt)).astype(dt)).astype(dt)
+        F["sxx"], F["syy"], F["szz"] = op.IFull @ sxx, op.IFull @ syy, op.IFull @ szz
+        # shear stresses
+        u = self._vel([(self.DyfSX, "vx", "vxy", "y", True), (op.Dxf, "vy", "vyx", "x", True)], self.muXY)
+        F["sxy"] = op.IStagX @ (F["sxy"] + u).astype(dt)
+        u = self._vel([(op.Dzf, "vx", "vxz", "z", True), (op.Dxf, "vz", "vzx", "x", True)], self.muXZ)
+        F["sxz"] = op.IStagXZ @ (F["sxz"] + u).astype(dt)
+        u = self._vel([(op.Dzf, "vy", "vyz", "z", True), (self.DyfSZ, "vz", "vzy", "y", True)], self.muYZ)
+        F["syz"] = op.IStagZ @ (op.IStagZ @ (F["syz"] + u).astype(dt))
+        # sources and receivers (FDTD3Delastic.cpp:12-53)
+        for k in range(len(self.src_idx)):
+            i, v = self.src_idx[k], self.signals[k, t]
+            if self.src_type[k] == 1:
+                for c in ("sxx", "syy", "szz"):
+                    F[c][i] += v
+            elif self.src_type[k] in (2, 3, 4):
+                F[("vx", "vy", "vz")[self.src_type[k] - 2]][i] += v
+        out = np.zeros(len(self.rec_idx), dtype=dt)
+        for r, (i, k) in enumerate(zip(self.rec_idx, self.rec_type)):
+            if k == 1:
+                out[r] = d((F["sxx"][i] + F["syy"][i] + F["szz"][i]) / d(3.0))
+            else:
+                out[r] = F[("vx", "vy", "vz")[k - 2]][i]
         return out
 
     def run(self, nt: int) -> np.ndarray:

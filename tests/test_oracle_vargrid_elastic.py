@@ -95,3 +95,72 @@ def test_library_staggered_operators_equal_the_oracle(grid, NX, NY, wave, refcpu
         want.eliminate_zeros()
         diff = abs(got - want)
         assert diff.nnz == 0 or diff.max() == 0, (k, diff.max())
+
+
+@pytest.mark.parametrize("boundary", [2, 0])
+def test_single_layer_3d_elastic_vargrid_equals_regular_oracle(boundary, refcpu):
+    """The 3-D elastic variable-grid oracle (staggered-Z operators, the XZ /
+    YZ shear averages, the 3-D interpolation set) on one layer against the
+    pinned regular 3-D elastic oracle, FP64."""
+    from oracle import vargrid as vg, vargrid_elastic as ve
+    NX, NY, NZ, DH, order, vmax = 30, 28, 26, 5.0, 4, 3000.0
+    DT = 0.3 * DH / (vmax * np.sqrt(3.0))
+    cfg = refcpu.make_config(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=160 * DT,
+                             spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=6, NPower=4.0,
+                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0)
+    nt = refcpu.nt_of(cfg)
+    rho, vp, vs = _model(NX * NY * NZ, np.random.default_rng(2))
+    g = vg.VarGrid(NX, NY, NZ, DH, [0], [1])
+    sidx = g.coordinate2index([NX // 2], [NY // 3], [NZ // 2])
+    sig = refcpu.ricker(nt, DT, 40.0, 1.0, 0.0, np.float64)[None]
+    ridx = g.coordinate2index([5, NX - 6, 7, 12], [10, NY - 4, 20, 5], [4, 9, NZ - 5, 13])
+    rtype = np.array([1, 2, 3, 4])
+    o = refcpu.Oracle(cfg, dict(rho=rho, vp=vp, vs=vs), sidx, np.array([1]), sig, ridx, rtype, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    cp = vg.cpml_coefficients(g, 6, 4.0, 20.0, vmax, DT, False, np.float64) if boundary == 2 else None
+    sim = ve.ElasticVarGrid3D(g, [order], DT, rho, vp, vs, cp, sidx, [1], sig, ridx, rtype, dtype=np.float64,
+                              var_order=False, edge=False, var_grid=False)
+    got = sim.run(nt)
+    assert np.abs(ref).max() > 0
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
+
+
+def test_3d_elastic_vargrid_tracks_the_all_fine_grid(refcpu):
+    """A 1:3:1 3-D grid (every staggered-X / Z operator shift and the
+    StaggeredX / Z / XZ and Full interpolations in play): receivers in the fine
+    layers stay within 2 % of an all-fine regular run (the misfit is the
+    coarse layer's dispersion: 4 % at a 10 Hz peak, 0.6 % at 6 Hz), and two
+    receivers that mirror each other under x <-> z record the same trace (the
+    x- and z-staggered operators and interpolations agree)."""
+    from oracle import vargrid as vg, vargrid_elastic as ve
+    NX, NY, NZ, DH = 49, 60, 49, 5.0
+    vp0, vs0, rho0, fc = 3000.0, 1700.0, 2200.0, 6.0
+    DT = 0.3 * DH / (vp0 * np.sqrt(3.0) * 1.2)
+    nt = 700
+    grid = [(0, 1, 4), (21, 3, 4), (42, 1, 4)]
+    g = vg.VarGrid(NX, NY, NZ, DH, [r[0] for r in grid], [r[1] for r in grid])
+    sig = refcpu.ricker(nt, DT, fc, 1.0, 0.0, np.float64)[None]
+    src = (g.NX // 2, 12, g.NZ // 2)
+    recs = [(12, 8, 20), (36, 15, 30), (24, 50, 24), (24, 50, 10), (10, 50, 24)]
+    cp = vg.cpml_coefficients(g, 9, 4.0, fc, vp0, DT, False, np.float64)
+    sidx = g.coordinate2index([src[0]], [src[1]], [src[2]])
+    ridx = g.coordinate2index([r[0] for r in recs], [r[1] for r in recs], [r[2] for r in recs])
+    sim = ve.ElasticVarGrid3D(g, [r[2] for r in grid], DT, np.full(g.N, rho0), np.full(g.N, vp0), np.full(g.N, vs0),
+                              cp, sidx, [1], sig, ridx, [1] * len(recs), dtype=np.float64, edge=False)
+    a = sim.run(nt)
+    cfg = refcpu.make_config(dimension=3, equation="elastic", NX=g.NX, NY=g.NY, NZ=g.NZ, DH=DH, DT=DT, T=nt * DT,
+                             spatialFDorder=4, DampingBoundary=2, BoundaryWidth=9, NPower=4.0,
+                             CenterFrequencyCPML=fc, VMaxCPML=vp0, edgeOrderReduction=0)
+    n = g.NX * g.NY * g.NZ
+    o = refcpu.Oracle(cfg, dict(rho=np.full(n, rho0), vp=np.full(n, vp0), vs=np.full(n, vs0)),
+                      np.array([src[0] + g.NX * (src[2] + g.NZ * src[1])]), np.array([1]), sig[:, :refcpu.nt_of(cfg)],
+                      np.array([r[0] + g.NX * (r[2] + g.NZ * r[1]) for r in recs]), np.ones(len(recs), int),
+                      dtype=np.float64)
+    b = o.run()
+    o.close()
+    m = min(a.shape[1], b.shape[1])
+    assert np.isfinite(a).all()
+    for k in range(len(recs)):
+        assert np.linalg.norm(a[k, :m] - b[k, :m]) / np.linalg.norm(b[k, :m]) < 0.02, k
+    assert np.linalg.norm(a[3] - a[4]) <= 1e-10 * np.linalg.norm(a[3])
