@@ -95,9 +95,9 @@ typedef struct wave_config {
                                    Config key "edgeOrderReduction" (default 1).   */
     /* Variable (discontinuous) grid, Acquisition/Coordinates.cpp:35-245 and
      * Derivatives.cpp:852-1656. Acoustic equations (2-D and 3-D, free
-     * surface allowed) and 2-D elastic (FD2Delastic::run with
-     * DyfStaggeredX / DybStaggeredX, no free surface); CPML or no damping
-     * boundary; no adjoint. The grid's index space replaces NX*NY*NZ
+     * surface allowed) and elastic (2-D and 3-D, FD2Delastic / FD3Delastic
+     * ::run with the staggered-x / -z y-derivatives, no free surface); CPML
+     * or no damping boundary; no adjoint. The grid's index space replaces NX*NY*NZ
      * everywhere (model arrays, source/receiver indices, wavefields): see
      * wave_grid_*. */
     int useVariableGrid;        /* "useVariableGrid": layers of spacing DH*dhFactor   */
@@ -138,10 +138,13 @@ int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_
  * 2 Dzf, 3 Dxb, 4 Dyb, 5 Dzb, DT folded in (Derivatives.cpp:129-1245,
  * FDTD2D.cpp:193-229), the interface interpolation 6 Full, 7 StaggeredX,
  * 8 StaggeredZ (Derivatives.cpp:1252-1546; rows off the interfaces are the
- * identity), or the elastic staggered-x y-derivatives 9 DyfStaggeredX,
- * 10 DybStaggeredX (Derivatives.cpp:852-1011, 2-D). Returned as an ELL block: *width entries per row, entry k of
- * row i at k*N + i, unused entries with weight 0. With cols == NULL only
- * *width is set; otherwise capacity must be at least width * N. */
+ * identity), the elastic staggered y-derivatives 9 DyfStaggeredX,
+ * 10 DybStaggeredX (Derivatives.cpp:852-1011), 11 DyfStaggeredZ,
+ * 12 DybStaggeredZ (Derivatives.cpp:1012-1168, 3-D), or 13 the interface
+ * interpolation StaggeredXZ (Derivatives.cpp:1568-1661, 3-D). Returned as an
+ * ELL block: *width entries per row, entry k of row i at k*N + i, unused
+ * entries with weight 0. With cols == NULL only *width is set; otherwise
+ * capacity must be at least width * N. */
 int wave_grid_operator(const wave_config* cfg, int op, int* width, int32_t* cols, float* vals, int64_t capacity);
 
 /* ForwardSolver::Factory<float>::Create(dimension, type)

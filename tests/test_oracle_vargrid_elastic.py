@@ -164,3 +164,36 @@ def test_3d_elastic_vargrid_tracks_the_all_fine_grid(refcpu):
     for k in range(len(recs)):
         assert np.linalg.norm(a[k, :m] - b[k, :m]) / np.linalg.norm(b[k, :m]) < 0.02, k
     assert np.linalg.norm(a[3] - a[4]) <= 1e-10 * np.linalg.norm(a[3])
+
+
+@pytest.mark.parametrize("grid,dims", [
+    ([(0, 1, 4), (21, 3, 4), (42, 1, 4)], (49, 60, 49)),
+    ([(0, 1, 2), (12, 3, 6), (30, 9, 2)], (55, 48, 37)),
+])
+def test_library_3d_staggered_operators_equal_the_oracle(grid, dims, wave, refcpu):
+    """DyfStaggeredX / DybStaggeredX / DyfStaggeredZ / DybStaggeredZ and the
+    StaggeredXZ interpolation as the library assembles them on the host
+    (wave_grid_operator 9-13) against the oracle, entry for entry, on 3-D
+    variable grids."""
+    import scipy.sparse as sp
+    from oracle import vargrid as vg, vargrid_elastic as ve
+    NX, NY, NZ = dims
+    DT = 4e-4
+    kw = dict(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=10.0, DT=DT, T=0.01, spatialFDorder=grid[0][2],
+              useVariableGrid=1, useVariableFDoperators=1, grid=grid)
+    c = wave.WaveConfig.make(**kw)
+    g = vg.VarGrid(NX, NY, NZ, 10.0, [r[0] for r in grid], [r[1] for r in grid])
+    orders = [r[2] for r in grid]
+    op = vg.Operators(g, orders, DT, False, np.float32, True, True, True)
+    want = {9: ve.staggered_operator(op, orders, True, True, "x"), 10: ve.staggered_operator(op, orders, True, False, "x"),
+            11: ve.staggered_operator(op, orders, True, True, "z"), 12: ve.staggered_operator(op, orders, True, False, "z"),
+            13: op.IStagXZ}
+    for k, w_ in want.items():
+        cols, vals = wave.grid_operator(c, k)
+        w = cols.shape[0]
+        got = sp.csr_matrix((vals.ravel().astype(np.float64), (np.tile(np.arange(g.N), w), cols.ravel())), shape=(g.N, g.N))
+        got.eliminate_zeros()
+        ref = w_.astype(np.float64).tocsr()
+        ref.eliminate_zeros()
+        diff = abs(got - ref)
+        assert diff.nnz == 0 or diff.max() == 0, (k, diff.max())

@@ -541,8 +541,9 @@ int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_
 
 int wave_grid_operator(const wave_config* cfg, int op, int* width, int32_t* cols, float* vals, int64_t capacity)
 {
-    if (!cfg || !width || op < 0 || op > 10) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: invalid arguments");
-    if (op > 8 && cfg->dimension != 2) return fail(nullptr, WAVE_ERR_UNSUPPORTED, "wave_grid_operator: the staggered-x operators are built for 2-D");
+    if (!cfg || !width || op < 0 || op > 13) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: invalid arguments");
+    if (op > 10 && cfg->dimension != 3)
+        return fail(nullptr, WAVE_ERR_UNSUPPORTED, "wave_grid_operator: the staggered-z operators and StaggeredXZ are 3-D");
     if (!(cfg->useVariableGrid || cfg->useVariableFDoperators))
         return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: not a variable-grid configuration");
     wave::VarGridHost G;
@@ -550,8 +551,9 @@ int wave_grid_operator(const wave_config* cfg, int op, int* width, int32_t* cols
     int rc = wave::vargrid_build(*cfg, G, err, op > 8);
     if (rc != WAVE_OK) return fail(nullptr, rc, err);
     const long long N = G.L.N;
-    if (op < 6 || op > 8) {
-        const wave::EllHost* ops[11] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb, nullptr, nullptr, nullptr, &G.DyfSX, &G.DybSX};
+    if (op < 6 || (op > 8 && op < 13)) {
+        const wave::EllHost* ops[13] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb, nullptr, nullptr, nullptr,
+                                        &G.DyfSX, &G.DybSX, &G.DyfSZ, &G.DybSZ};
         const wave::EllHost& E = *ops[op];
         *width = E.W;
         if (!cols) return WAVE_OK;
@@ -560,8 +562,8 @@ int wave_grid_operator(const wave_config* cfg, int op, int* width, int32_t* cols
         std::memcpy(vals, E.val.data(), E.val.size() * sizeof(float));
         return WAVE_OK;
     }
-    const wave::InterpHost* in[3] = {&G.full, &G.stagX, &G.stagZ};
-    const wave::InterpHost& I = *in[op - 6];
+    const wave::InterpHost* in[4] = {&G.full, &G.stagX, &G.stagZ, &G.stagXZ};
+    const wave::InterpHost& I = *in[op == 13 ? 3 : op - 6];
     *width = 4;
     if (!cols) return WAVE_OK;
     if (!vals || capacity < 4 * N) return fail(nullptr, WAVE_ERR_ARG, "wave_grid_operator: capacity too small");
@@ -609,17 +611,17 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
     const bool vgrid = c.useVariableGrid != 0 || c.useVariableFDoperators != 0;
     wave::VarGridHost vgHost;
     if (vgrid) {
-        const bool el2d = c.equation == WAVE_EQ_ELASTIC && !is3d;
-        if (c.equation != WAVE_EQ_ACOUSTIC && !el2d)
-            return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built for the acoustic equations and 2-D elastic");
-        if (el2d && c.FreeSurface != 0)
+        const bool elastic = c.equation == WAVE_EQ_ELASTIC;
+        if (c.equation != WAVE_EQ_ACOUSTIC && !elastic)
+            return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built for the acoustic and elastic equations");
+        if (elastic && c.FreeSurface != 0)
             return fail(nullptr, WAVE_ERR_UNSUPPORTED, "the elastic variable grid is built without a free surface");
         if (c.DampingBoundary == 1)
             return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built with CPML or without a damping boundary (not ABS)");
         if (c.useStencilMatrix)
             return fail(nullptr, WAVE_ERR_ARG, "Variable FD operators are not available for stencil matrices");
         std::string err;
-        int rc = wave::vargrid_build(c, vgHost, err, el2d);
+        int rc = wave::vargrid_build(c, vgHost, err, elastic);
         if (rc != WAVE_OK) return fail(nullptr, rc, err);
     }
 

@@ -19,12 +19,18 @@
 // coarse-aligned rows of the same interface (which they leave unchanged);
 // otherwise (a 3:9 step) the new values go through a scratch array first.
 //
-// The 2-D elastic step (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297)
-// has the same shape with the ELL operators:
-//   vge_vel   vx += (Dxf sxx + DybStaggeredX sxy) / rho_x, vy += (Dxb sxy + Dyf syy) / rho_y
-//   vg_interp vx (StaggeredX), vy (Full)
-//   vge_str   sxx, syy from Dxb vx, Dyb vy; sxy from DyfStaggeredX vx + Dxf vy
-//   vg_interp sxx, syy (Full), sxy (StaggeredX)
+// The elastic step (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297;
+// FD3Delastic::run, ForwardSolver3Delastic.cpp:120-414) has the same shape
+// with the ELL operators:
+//   vge_vel   vx += (Dxf sxx + DybStaggeredX sxy [+ Dzb sxz]) / rho_x,
+//             vy += (Dxb sxy + Dyf syy [+ Dzb syz]) / rho_y,
+//             [vz += (Dxb sxz + DybStaggeredZ syz + Dzf szz) / rho_z]
+//   vg_interp vx (StaggeredX), vy (Full) [, vz (StaggeredZ)]
+//   vge_str   normal stresses from Dxb vx, Dyb vy [, Dzb vz]; sxy from
+//             DyfStaggeredX vx + Dxf vy [; sxz from Dzf vx + Dxf vz; syz from
+//             Dzf vy + DyfStaggeredZ vz]
+//   vg_interp sxx, syy [, szz] (Full), sxy (StaggeredX) [, sxz (StaggeredXZ),
+//             syz (StaggeredZ)]
 #include <cuda_runtime.h>
 
 #include "handle.h"
@@ -62,14 +68,15 @@ struct VgParams {
 // srSlot >= 0: the blocks with blockIdx.y == srSlot run the step's sources
 // and receivers instead (block 0 only), when none of them is on an interface
 // row, so they touch no row the interpolation reads or writes.
+constexpr int kMaxInterpLists = 6;
 struct VgInterp {
-    int n[3];
-    int phase[3];
-    float* f[3];
-    float* tmp[3];
-    const int* row[3];
-    const int* col[3];
-    const float* w[3];
+    int n[kMaxInterpLists];
+    int phase[kMaxInterpLists];
+    float* f[kMaxInterpLists];
+    float* tmp[kMaxInterpLists];
+    const int* row[kMaxInterpLists];
+    const int* col[kMaxInterpLists];
+    const float* w[kMaxInterpLists];
     int srSlot;
     SrcRecParams Q;
     int* tcounter;
@@ -178,7 +185,7 @@ __global__ void __launch_bounds__(256) vg_pres(VgParams P)
     P.p[i] = pv;
 }
 
-// blockIdx.y selects one of up to three (field, row list) pairs
+// blockIdx.y selects one of up to six (field, row list) pairs
 __global__ void __launch_bounds__(256) vg_interp(VgInterp I)
 {
     dependent_launch_prologue();
@@ -229,24 +236,28 @@ __global__ void __launch_bounds__(256) vg_model(long long N, int naxes, const fl
 }
 
 // ---------------------------------------------------------------- elastic
+// CPML memory variables of the elastic step, in VgeParams::psi order
+enum ElasticPsi {
+    Q_SXX_X, Q_SXY_Y, Q_SXZ_Z, Q_SXY_X, Q_SYY_Y, Q_SYZ_Z, Q_SXZ_X, Q_SYZ_Y, Q_SZZ_Z,
+    Q_VXX, Q_VYY, Q_VZZ, Q_VXY, Q_VYX, Q_VXZ, Q_VZX, Q_VYZ, Q_VZY, Q_COUNT
+};
+// operator slots of VarGridDev
+enum ElasticOp { O_DXF, O_DYF, O_DZF, O_DXB, O_DYB, O_DZB, O_DYF_SX, O_DYB_SX, O_DYF_SZ, O_DYB_SZ };
+
 struct VgeParams {
     long long N;
-    float* vx;
-    float* vy;
-    float* sxx;
-    float* syy;
-    float* sxy;
-    float* psi[8];              // sxx_x, sxy_y, sxy_x, syy_y, vxx, vyy, vxy, vyx
+    float* v[3];                // vx vy vz
+    float* s[6];                // sxx syy szz sxy sxz syz
+    float* psi[Q_COUNT];
     const float* M;
     const float* mu;
-    const float* muXY;
-    const float* irx;
-    const float* iry;
-    const int* col[8];          // as VarGridDev: 0 Dxf, 1 Dyf, 3 Dxb, 4 Dyb, 6 DyfStaggeredX, 7 DybStaggeredX
-    const float* val[8];
-    int W[8];
-    const unsigned short* cpc[2];
-    const float* cpt[2];
+    const float* muS[3];        // shear averages xy, xz, yz
+    const float* ir[3];         // inverse density averages x, y, z
+    const int* col[10];
+    const float* val[10];
+    int W[10];
+    const unsigned short* cpc[3];
+    const float* cpt[3];
 };
 
 __device__ __forceinline__ float vge_row(const VgeParams& P, int op, long long i, const float* __restrict__ u)
@@ -271,70 +282,96 @@ __device__ __forceinline__ void vge_cpml(const VgeParams& P, float& d, int slot,
     d = __fadd_rn(d, ps);
 }
 
-// velocities (ForwardSolver2Delastic.cpp:150-190): the CPML profiles of
-// CPML2D: sxx_x half-x, sxy_y full-y, sxy_x full-x, syy_y half-y
+// one derivative term of an update: operator row, then its CPML correction
 template <bool CPML>
+__device__ __forceinline__ float vge_term(const VgeParams& P, int op, const float* u, int slot, int axis, bool half, long long i)
+{
+    float d = vge_row(P, op, i, u);
+    if (CPML) vge_cpml(P, d, slot, axis, half, i);
+    return d;
+}
+
+// velocities (ForwardSolver2Delastic.cpp:150-197, ForwardSolver3Delastic.cpp:
+// 176-275); the CPML profiles of CPML2D / CPML3D: the forward derivatives
+// (sxx_x, syy_y, szz_z) take the half-grid profiles, the others the full ones
+template <bool IS3D, bool CPML>
 __global__ void __launch_bounds__(256) vge_vel(VgeParams P)
 {
     dependent_launch_prologue();
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
-    float d = vge_row(P, 0, i, P.sxx);
-    if (CPML) vge_cpml(P, d, 0, 0, true, i);
-    float d2 = vge_row(P, 7, i, P.sxy);
-    if (CPML) vge_cpml(P, d2, 1, 1, false, i);
-    P.vx[i] = __fadd_rn(P.vx[i], __fmul_rn(__fadd_rn(d, d2), P.irx[i]));
-    d = vge_row(P, 3, i, P.sxy);
-    if (CPML) vge_cpml(P, d, 2, 0, false, i);
-    d2 = vge_row(P, 1, i, P.syy);
-    if (CPML) vge_cpml(P, d2, 3, 1, true, i);
-    P.vy[i] = __fadd_rn(P.vy[i], __fmul_rn(__fadd_rn(d, d2), P.iry[i]));
+    float* const* S = P.s;
+    float d = vge_term<CPML>(P, O_DXF, S[0], Q_SXX_X, 0, true, i);
+    d = __fadd_rn(d, vge_term<CPML>(P, O_DYB_SX, S[3], Q_SXY_Y, 1, false, i));
+    if (IS3D) d = __fadd_rn(d, vge_term<CPML>(P, O_DZB, S[4], Q_SXZ_Z, 2, false, i));
+    P.v[0][i] = __fadd_rn(P.v[0][i], __fmul_rn(d, P.ir[0][i]));
+    d = vge_term<CPML>(P, O_DXB, S[3], Q_SXY_X, 0, false, i);
+    d = __fadd_rn(d, vge_term<CPML>(P, O_DYF, S[1], Q_SYY_Y, 1, true, i));
+    if (IS3D) d = __fadd_rn(d, vge_term<CPML>(P, O_DZB, S[5], Q_SYZ_Z, 2, false, i));
+    P.v[1][i] = __fadd_rn(P.v[1][i], __fmul_rn(d, P.ir[1][i]));
+    if (IS3D) {
+        d = vge_term<CPML>(P, O_DXB, S[4], Q_SXZ_X, 0, false, i);
+        d = __fadd_rn(d, vge_term<CPML>(P, O_DYB_SZ, S[5], Q_SYZ_Y, 1, false, i));
+        d = __fadd_rn(d, vge_term<CPML>(P, O_DZF, S[2], Q_SZZ_Z, 2, true, i));
+        P.v[2][i] = __fadd_rn(P.v[2][i], __fmul_rn(d, P.ir[2][i]));
+    }
 }
 
-// stresses (ForwardSolver2Delastic.cpp:200-260): vxx full-x, vyy full-y,
-// vxy half-y, vyx half-x
-template <bool CPML>
+// stresses (ForwardSolver2Delastic.cpp:200-260, ForwardSolver3Delastic.cpp:
+// 280-384): vxx, vyy, vzz with the full profiles, the shear derivatives
+// (vxy, vyx, vxz, vzx, vyz, vzy) with the half ones
+template <bool IS3D, bool CPML>
 __global__ void __launch_bounds__(256) vge_str(VgeParams P)
 {
     dependent_launch_prologue();
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
-    float vxx = vge_row(P, 3, i, P.vx);
-    if (CPML) vge_cpml(P, vxx, 4, 0, false, i);
-    float vyy = vge_row(P, 4, i, P.vy);
-    if (CPML) vge_cpml(P, vyy, 5, 1, false, i);
-    const float u = __fmul_rn(__fadd_rn(vxx, vyy), P.M[i]);
+    float* const* V = P.v;
+    const float vxx = vge_term<CPML>(P, O_DXB, V[0], Q_VXX, 0, false, i);
+    const float vyy = vge_term<CPML>(P, O_DYB, V[1], Q_VYY, 1, false, i);
+    const float vzz = IS3D ? vge_term<CPML>(P, O_DZB, V[2], Q_VZZ, 2, false, i) : 0.0f;
+    float sum = __fadd_rn(vxx, vyy);
+    if (IS3D) sum = __fadd_rn(sum, vzz);
+    const float u = __fmul_rn(sum, P.M[i]);
     const float mu = P.mu[i];
-    P.sxx[i] = __fsub_rn(__fadd_rn(P.sxx[i], u), __fmul_rn(2.0f, __fmul_rn(vyy, mu)));
-    P.syy[i] = __fsub_rn(__fadd_rn(P.syy[i], u), __fmul_rn(2.0f, __fmul_rn(vxx, mu)));
-    float vxy = vge_row(P, 6, i, P.vx);
-    if (CPML) vge_cpml(P, vxy, 6, 1, true, i);
-    float vyx = vge_row(P, 0, i, P.vy);
-    if (CPML) vge_cpml(P, vyx, 7, 0, true, i);
-    P.sxy[i] = __fadd_rn(P.sxy[i], __fmul_rn(__fadd_rn(vxy, vyx), P.muXY[i]));
+    if (IS3D) {
+        P.s[0][i] = __fsub_rn(__fadd_rn(P.s[0][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vyy, vzz), mu)));
+        P.s[1][i] = __fsub_rn(__fadd_rn(P.s[1][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vxx, vzz), mu)));
+        P.s[2][i] = __fsub_rn(__fadd_rn(P.s[2][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vxx, vyy), mu)));
+    } else {
+        P.s[0][i] = __fsub_rn(__fadd_rn(P.s[0][i], u), __fmul_rn(2.0f, __fmul_rn(vyy, mu)));
+        P.s[1][i] = __fsub_rn(__fadd_rn(P.s[1][i], u), __fmul_rn(2.0f, __fmul_rn(vxx, mu)));
+    }
+    float a = vge_term<CPML>(P, O_DYF_SX, V[0], Q_VXY, 1, true, i);
+    float b = vge_term<CPML>(P, O_DXF, V[1], Q_VYX, 0, true, i);
+    P.s[3][i] = __fadd_rn(P.s[3][i], __fmul_rn(__fadd_rn(a, b), P.muS[0][i]));
+    if (IS3D) {
+        a = vge_term<CPML>(P, O_DZF, V[0], Q_VXZ, 2, true, i);
+        b = vge_term<CPML>(P, O_DXF, V[2], Q_VZX, 0, true, i);
+        P.s[4][i] = __fadd_rn(P.s[4][i], __fmul_rn(__fadd_rn(a, b), P.muS[1][i]));
+        a = vge_term<CPML>(P, O_DZF, V[1], Q_VYZ, 2, true, i);
+        b = vge_term<CPML>(P, O_DYF_SZ, V[2], Q_VZY, 1, true, i);
+        P.s[5][i] = __fadd_rn(P.s[5][i], __fmul_rn(__fadd_rn(a, b), P.muS[2][i]));
+    }
 }
 
-// Elastic::prepareForModelling on the 2-D variable grid: M = rho vp^2,
+// Elastic::prepareForModelling on the variable grid: M = rho vp^2,
 // mu = rho vs^2; inverse densities averaged with the grid's partners
-// (Modelparameter.cpp:336-446, 633-640); the shear modulus at the
-// staggered xy point: calcAverageMatrixXY's 4-point average of 1/max(mu, 1)
-// (2 points on the bottom / right edge, 1 in the corner), inverted, results
-// below 4 set to 0 (Modelparameter.cpp:449-533, ModelparameterSeismic.cpp:
-// 421-432). A partner the index map does not find counts as the point itself.
-__device__ __forceinline__ float inv_mu(const float* mu, int j) { return __fdiv_rn(1.0f, fmaxf(mu[j], 1.0f)); }
-
-__global__ void __launch_bounds__(256) vge_model(long long N, const float* __restrict__ rho, const float* __restrict__ vp,
-                                                 const float* __restrict__ vs, const int* __restrict__ px,
-                                                 const int* __restrict__ py, float* M, float* mu, float* irx, float* iry)
+// (Modelparameter.cpp:336-446, 633-640)
+__global__ void __launch_bounds__(256) vge_model(long long N, int naxes, const float* __restrict__ rho,
+                                                 const float* __restrict__ vp, const float* __restrict__ vs,
+                                                 const int* __restrict__ px, const int* __restrict__ py,
+                                                 const int* __restrict__ pz, float* M, float* mu, float* irx, float* iry,
+                                                 float* irz)
 {
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const float r = rho[i];
     M[i] = __fmul_rn(__fmul_rn(r, vp[i]), vp[i]);
     mu[i] = __fmul_rn(__fmul_rn(r, vs[i]), vs[i]);
-    const int* part[2] = {px, py};
-    float* out[2] = {irx, iry};
-    for (int a = 0; a < 2; ++a) {
+    const int* part[3] = {px, py, pz};
+    float* out[3] = {irx, iry, irz};
+    for (int a = 0; a < naxes; ++a) {
         const int j = part[a][i];
         const float avg = j >= 0 ? __fadd_rn(__fmul_rn(0.5f, r), __fmul_rn(0.5f, rho[j])) : r;
         const float inv = __fdiv_rn(1.0f, avg);
@@ -342,9 +379,17 @@ __global__ void __launch_bounds__(256) vge_model(long long N, const float* __res
     }
 }
 
-// after vge_model (it reads mu of the partners)
+// the shear modulus at a staggered point of one axis pair: calc4PointAverage
+// MatrixRow's average of 1/max(mu, 1) over the point and its neighbours along
+// the pair's first axis (s1), second axis (s2) and both (s3); with one axis
+// past the grid the point and its neighbour along the other, with both the
+// point alone; inverted, results below 4 set to 0 (Modelparameter.cpp:
+// 449-624, ModelparameterSeismic.cpp:421-432). A partner the index map does
+// not find counts as the point itself. Runs after vge_model (reads mu).
+__device__ __forceinline__ float inv_mu(const float* mu, int j) { return __fdiv_rn(1.0f, fmaxf(mu[j], 1.0f)); }
+
 __global__ void __launch_bounds__(256) vge_shear(long long N, const float* __restrict__ mu, const int* __restrict__ s1,
-                                                 const int* __restrict__ s2, const int* __restrict__ s3, float* muXY)
+                                                 const int* __restrict__ s2, const int* __restrict__ s3, float* muS)
 {
     const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= N) return;
@@ -364,7 +409,7 @@ __global__ void __launch_bounds__(256) vge_shear(long long N, const float* __res
         s = ii;
     }
     const float av = __fdiv_rn(1.0f, s);
-    muXY[i] = av < 4.0f ? 0.0f : av;
+    muS[i] = av < 4.0f ? 0.0f : av;
 }
 
 template <class K, class Prm>
@@ -383,30 +428,34 @@ void launch(K kernel, dim3 grid, dim3 block, bool dep, cudaStream_t s, const Prm
 }
 
 // the elastic step's CPML memory variables, in VgeParams::psi order
-constexpr int kElasticPsi[8] = {PS_SXX_X, PS_SXY_Y, PS_SXY_X, PS_SYY_Y, PS_VXX, PS_VYY, PS_VXY, PS_VYX};
+constexpr int kElasticPsi[Q_COUNT] = {PS_SXX_X, PS_SXY_Y, PS_SXZ_Z, PS_SXY_X, PS_SYY_Y, PS_SYZ_Z, PS_SXZ_X, PS_SYZ_Y, PS_SZZ_Z,
+                                      PS_VXX, PS_VYY, PS_VZZ, PS_VXY, PS_VYX, PS_VXZ, PS_VZX, PS_VYZ, PS_VZY};
+// the ones the 2-D step uses
+constexpr int kElasticPsi2D[8] = {Q_SXX_X, Q_SXY_Y, Q_SXY_X, Q_SYY_Y, Q_VXX, Q_VYY, Q_VXY, Q_VYX};
 
 VgeParams elastic_params_of(wave_handle* h)
 {
     const VarGridDev& G = *h->vg;
     VgeParams P{};
     P.N = G.N;
-    P.vx = h->f[F_VX];
-    P.vy = h->f[F_VY];
-    P.sxx = h->f[F_SXX];
-    P.syy = h->f[F_SYY];
-    P.sxy = h->f[F_SXY];
-    for (int k = 0; k < 8; ++k) P.psi[k] = h->psi[kElasticPsi[k]];
+    const int vf[3] = {F_VX, F_VY, F_VZ}, sf[6] = {F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ};
+    for (int k = 0; k < 3; ++k) P.v[k] = h->f[vf[k]];
+    for (int k = 0; k < 6; ++k) P.s[k] = h->f[sf[k]];
+    for (int k = 0; k < Q_COUNT; ++k) P.psi[k] = h->psi[kElasticPsi[k]];
     P.M = h->m[M_M];
     P.mu = h->m[M_MU];
-    P.muXY = h->m[M_MUXY];
-    P.irx = h->m[M_IRX];
-    P.iry = h->m[M_IRY];
-    for (int k = 0; k < 8; ++k) {
+    P.muS[0] = h->m[M_MUXY];
+    P.muS[1] = h->m[M_MUXZ];
+    P.muS[2] = h->m[M_MUYZ];
+    P.ir[0] = h->m[M_IRX];
+    P.ir[1] = h->m[M_IRY];
+    P.ir[2] = h->m[M_IRZ];
+    for (int k = 0; k < 10; ++k) {
         P.col[k] = G.col[k];
         P.val[k] = G.val[k];
         P.W[k] = G.W[k];
     }
-    for (int a = 0; a < 2; ++a) {
+    for (int a = 0; a < 3; ++a) {
         P.cpc[a] = G.cpCode[a];
         P.cpt[a] = G.cpTab[a];
     }
@@ -462,16 +511,16 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
     D->is3d = is3d;
     const bool elastic = h->cfg.equation == WAVE_EQ_ELASTIC;
     D->elastic = elastic ? 1 : 0;
-    const EllHost* ops[8] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb, &G.DyfSX, &G.DybSX};
-    for (int k = 0; k < (elastic ? 8 : 6); ++k) {
+    const EllHost* ops[10] = {&G.Dxf, &G.Dyf, &G.Dzf, &G.Dxb, &G.Dyb, &G.Dzb, &G.DyfSX, &G.DybSX, &G.DyfSZ, &G.DybSZ};
+    for (int k = 0; k < (elastic ? (is3d ? 10 : 8) : 6); ++k) {
         if (!is3d && (k == 2 || k == 5)) continue;
         D->W[k] = ops[k]->W;
         D->col[k] = upload(h, ops[k]->col);
         D->val[k] = upload(h, ops[k]->val);
     }
-    const InterpHost* in[3] = {&G.full, &G.stagX, &G.stagZ};
+    const InterpHost* in[4] = {&G.full, &G.stagX, &G.stagZ, &G.stagXZ};
     long long total = 0;
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
         D->nInterp[k] = static_cast<int>(in[k]->row.size());
         D->inplace[k] = in[k]->inplace ? 1 : 0;
         total += D->nInterp[k];
@@ -480,15 +529,17 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
         D->icol[k] = upload(h, in[k]->col);
         D->iw[k] = upload(h, in[k]->w);
     }
-    // the elastic stress interpolation rewrites two fields with the Full rows
-    if (total > 0) D->itmp = h->alloc<float>(elastic ? 2 * total : total);
+    // scratch of the two-phase interpolation: the elastic stress launch
+    // rewrites up to three fields with the Full rows
+    if (total > 0) D->itmp = h->alloc<float>(elastic ? 3 * total : total);
     if (h->cfg.DampingBoundary == 2) {
         for (int a = 0; a < (is3d ? 3 : 2); ++a) {
             D->cpCode[a] = upload(h, G.cpCode[a]);
             D->cpTab[a] = upload(h, G.cpTab[a]);
         }
         if (elastic) {
-            for (int slot : kElasticPsi) {
+            for (int q = 0; q < (is3d ? static_cast<int>(Q_COUNT) : 8); ++q) {
+                const int slot = kElasticPsi[is3d ? q : kElasticPsi2D[q]];
                 h->psi[slot] = h->alloc<float>(D->N);
                 h->psiLen[slot] = D->N;
             }
@@ -503,7 +554,8 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
     }
     for (int a = 0; a < (is3d ? 3 : 2); ++a) D->partner[a] = upload(h, G.avgPartner[a]);
     if (elastic)
-        for (int a = 0; a < 3; ++a) D->shear[a] = upload(h, G.shearPartner[a]);
+        for (int q = 0; q < (is3d ? 3 : 1); ++q)
+            for (int a = 0; a < 3; ++a) D->shear[q][a] = upload(h, G.shearPartner[q][a]);
     for (int pass = 0; pass < 2; ++pass) {
         const ClassHost& C = G.cls[pass];
         if (!C.ok) continue;
@@ -529,9 +581,11 @@ void vargrid_set_model(wave_handle* h, const float* rho, const float* vp, const 
     if (G.elastic) {
         const unsigned blocks = static_cast<unsigned>((G.N + 255) / 256);
         float* mu = mat(M_MU);
-        vge_model<<<blocks, 256, 0, h->stream>>>(G.N, rho, vp, vs, G.partner[0], G.partner[1], mat(M_M), mu, mat(M_IRX),
-                                                 mat(M_IRY));
-        vge_shear<<<blocks, 256, 0, h->stream>>>(G.N, mu, G.shear[0], G.shear[1], G.shear[2], mat(M_MUXY));
+        vge_model<<<blocks, 256, 0, h->stream>>>(G.N, G.is3d ? 3 : 2, rho, vp, vs, G.partner[0], G.partner[1], G.partner[2],
+                                                 mat(M_M), mu, mat(M_IRX), mat(M_IRY), G.is3d ? mat(M_IRZ) : nullptr);
+        const int slots[3] = {M_MUXY, M_MUXZ, M_MUYZ};
+        for (int q = 0; q < (G.is3d ? 3 : 1); ++q)
+            vge_shear<<<blocks, 256, 0, h->stream>>>(G.N, mu, G.shear[q][0], G.shear[q][1], G.shear[q][2], mat(slots[q]));
         h->check(cudaGetLastError(), "variable grid model preparation");
         return;
     }
@@ -584,12 +638,13 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
     int launches = 0;
     const VgeParams E = G.elastic ? elastic_params_of(h) : VgeParams{};
     if (G.elastic) {
-        launch(cp ? vge_vel<true> : vge_vel<false>, grid, block, dep, h->stream, E);
+        launch(G.is3d ? (cp ? vge_vel<true, true> : vge_vel<true, false>) : (cp ? vge_vel<false, true> : vge_vel<false, false>), grid,
+               block, dep, h->stream, E);
     } else {
         launch(vel, grid, block, dep, h->stream, with_classes(0));
     }
     ++launches;
-    const bool interp = G.nInterp[0] + G.nInterp[1] + G.nInterp[2] > 0;
+    const bool interp = G.nInterp[0] + G.nInterp[1] + G.nInterp[2] + G.nInterp[3] > 0;
     auto run_interp = [&](VgInterp I, int lists) {
         int mx = 0;
         for (int s = 0; s < lists; ++s) mx = I.n[s] > mx ? I.n[s] : mx;
@@ -657,7 +712,8 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
     }
     if (mid) cudaEventRecord(*mid, h->stream);
     if (G.elastic) {
-        launch(cp ? vge_str<true> : vge_str<false>, grid, block, dep, h->stream, E);
+        launch(G.is3d ? (cp ? vge_str<true, true> : vge_str<true, false>) : (cp ? vge_str<false, true> : vge_str<false, false>), grid,
+               block, dep, h->stream, E);
     } else {
         launch(pres, grid, block, dep, h->stream, with_classes(1));
     }
@@ -675,9 +731,21 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
         };
         off_interface(h->hSrcIdx);
         off_interface(h->hRecIdx);
-        const int kinds[3] = {0, 0, 1};
-        float* const fields[3] = {E.sxx, E.syy, E.sxy};
-        interp_fields(kinds, fields, 3, apart && h->kernelPath != 1);
+        // 3-D (ForwardSolver3Delastic.cpp:315-392): szz Full, sxz StaggeredXZ,
+        // syz StaggeredZ, which the reference applies twice: the second pass
+        // changes nothing where the interpolation runs in place (its rows
+        // read only rows it leaves unchanged), so only a two-phase StaggeredZ
+        // list is applied again
+        const bool again = G.is3d && G.nInterp[2] > 0 && !G.inplace[2];
+        const int kinds[6] = {0, 0, 1, 0, 3, 2};
+        float* const fields[6] = {E.s[0], E.s[1], E.s[3], G.is3d ? E.s[2] : nullptr, G.is3d ? E.s[4] : nullptr,
+                                  G.is3d ? E.s[5] : nullptr};
+        interp_fields(kinds, fields, 6, !again && apart && h->kernelPath != 1);
+        if (again) {
+            const int k2[1] = {2};
+            float* const f2[1] = {E.s[5]};
+            interp_fields(k2, f2, 1, apart && h->kernelPath != 1);
+        }
     } else if (interp && G.nInterp[0] > 0) {
         // sources and receivers in the same launch when none is on an interface row
         bool apart = true;

@@ -74,18 +74,20 @@ struct ClassHost {
 struct VarGridHost {
     VarGridLayout L;
     EllHost Dxf, Dxb, Dyf, Dyb, Dzf, Dzb;
-    EllHost DyfSX, DybSX;              // staggered-x y-derivatives (elastic only, 2-D)
+    EllHost DyfSX, DybSX;              // staggered-x y-derivatives (elastic only)
+    EllHost DyfSZ, DybSZ;              // staggered-z y-derivatives (3-D elastic only)
     ClassHost cls[2];                  // velocity pass (Dxf, Dyf, Dzf), pressure pass (Dxb, Dyb, Dzb)
-    InterpHost full, stagX, stagZ;
+    InterpHost full, stagX, stagZ, stagXZ;   // stagXZ: 3-D elastic only
     std::vector<float> cpml[3][4];     // per axis: a_full, b_full, a_half, b_half (N each; CPML only)
     // the same as a per-point code per axis into a table of (a_full, b_full,
     // a_half, b_half) quadruples; code 0 = no coefficients
     std::vector<unsigned short> cpCode[3];
     std::vector<float> cpTab[3];
     std::vector<int> avgPartner[3];    // averaging partner per axis (-1: the point alone)
-    // elastic (2-D): the 4-point shear-modulus average's partners (x+f, y),
-    // (x, y+f), (x+f, y+f), f the layer's dhFactor (-1: outside the grid)
-    std::vector<int> shearPartner[3];
+    // elastic: the 4-point shear-modulus averages' partners per axis pair
+    // (xy; 3-D also xz, yz): the neighbours f along the pair's first axis,
+    // its second axis and both, f the layer's dhFactor (-1: outside the grid)
+    std::vector<int> shearPartner[3][3];
     long long nSurface = 0;            // rows with y == 0 (the first rows of layer 0)
 };
 
@@ -104,19 +106,20 @@ struct VarGridDev {
     int is3d = 0;
     int elastic = 0;                        // 2-D elastic step (else acoustic)
     int nOps = 0;
-    int W[8] = {};                          // Dxf, Dyf, Dzf, Dxb, Dyb, Dzb, DyfStaggeredX, DybStaggeredX
-    const int* col[8] = {};
-    const float* val[8] = {};
-    int nInterp[3] = {};                    // full, staggered x, staggered z
-    const int* irow[3] = {};
-    const int* icol[3] = {};
-    const float* iw[3] = {};
-    int inplace[3] = {1, 1, 1};
+    // Dxf, Dyf, Dzf, Dxb, Dyb, Dzb, DyfStaggeredX, DybStaggeredX, DyfStaggeredZ, DybStaggeredZ
+    int W[10] = {};
+    const int* col[10] = {};
+    const float* val[10] = {};
+    int nInterp[4] = {};                    // full, staggered x, staggered z, staggered xz
+    const int* irow[4] = {};
+    const int* icol[4] = {};
+    const float* iw[4] = {};
+    int inplace[4] = {1, 1, 1, 1};
     float* itmp = nullptr;                  // scratch of the two-phase interpolation (sum of the row counts)
     const unsigned short* cpCode[3] = {};   // CPML coefficient code per axis and point (null: no CPML)
     const float* cpTab[3] = {};             // 4 floats per code
     const int* partner[3] = {};
-    const int* shear[3] = {};               // elastic: shear-average partners
+    const int* shear[3][3] = {};            // elastic: shear-average partners per axis pair
     long long nSurface = 0;
     int fs = 0;
     // stencil classes per pass (null: not available)

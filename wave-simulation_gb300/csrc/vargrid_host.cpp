@@ -327,7 +327,9 @@ struct Assembler {
     // elastic step at x-staggered points. Near an interface the staggered
     // point of the coarse layer sits at another x, so single taps shift by
     // dhFactor/3; taps outside the grid are dropped (no edge rule).
-    void stag_row(int x, int y, int z, bool forward, std::vector<Tap>& out) const
+    // zAxis: DyfStaggeredZ / DybStaggeredZ (:1012-1168), the same rule with
+    // the taps shifting along z
+    void stag_row(int x, int y, int z, bool forward, std::vector<Tap>& out, bool zAxis = false) const
     {
         const int layer = L.layerY[y];
         int order = order_of(layer);
@@ -336,32 +338,34 @@ struct Assembler {
         else if (order > 2 * dist) order = 2 * dist;
         const bool on = L.onIfaceY[y] != 0;
         const int tr = L.transY[y];
+        const int n = zAxis ? L.NZ : L.NX;
         auto iface = [&](long long yy) { return yy >= 0 && yy < L.NY && L.onIfaceY[yy]; };
-        std::vector<int> X(order, x);
+        auto at = [&](int c, int Y) { return zAxis ? L.index(x, Y, c) : L.index(c, Y, z); };
+        std::vector<int> C(order, zAxis ? z : x);
         if (forward) {
             const bool c2f = on && tr == -1;
             const int f = c2f ? L.dhf[layer + 1] : L.dhf[layer];
             const int dl = c2f ? layer + 1 : layer;
-            if (on && tr == 1 && X[0] >= f / 3) X[1] -= f / 3;
+            if (on && tr == 1 && C[0] >= f / 3) C[1] -= f / 3;
             const long long yq = y + static_cast<long long>(order / 2) * f;
-            if (iface(yq) && L.transY[yq] == -1 && X[0] < L.NX - f / 3) X[order - 1] += f / 3;
+            if (iface(yq) && L.transY[yq] == -1 && C[0] < n - f / 3) C[order - 1] += f / 3;
             for (int j = 0; j < order; ++j) {
                 const int Y = y + f * (j - order / 2 + 1);
-                if (Y >= 0 && Y < L.NY) out.push_back({L.index(X[j], Y, z), value(order, j, dl)});
+                if (Y >= 0 && Y < L.NY) out.push_back({at(C[j], Y), value(order, j, dl)});
             }
             return;
         }
         const int f = L.dhf[layer];
         const long long yq = y - static_cast<long long>(order / 2) * f;
-        if (iface(yq) && L.transY[yq] == 1 && X[1] < L.NX - f / 3) X[0] += f / 3;
-        if (on && tr == -1 && X[1] >= f / 3) X[0] -= f / 3;
+        if (iface(yq) && L.transY[yq] == 1 && C[1] < n - f / 3) C[0] += f / 3;
+        if (on && tr == -1 && C[1] >= f / 3) C[0] -= f / 3;
         for (int j = 0; j < order; ++j) {
             int Y = y + f * (j - order / 2);
             if (on) {
                 if (j == 0 && tr == 1) Y += L.dhf[layer - 1];
                 if (j == 1 && tr == -1) Y += L.dhf[layer + 1];
             }
-            if (Y >= 0 && Y < L.NY) out.push_back({L.index(X[j], Y, z), value(order, j, layer)});
+            if (Y >= 0 && Y < L.NY) out.push_back({at(C[j], Y), value(order, j, layer)});
         }
     }
 
@@ -508,12 +512,18 @@ int build_interp(const VarGridLayout& L, const std::vector<long long>& rows, int
             ok[1] = x + ff < L.NX;
             ok[2] = x >= mx && z + 2 * ff < L.NZ;
             ok[3] = x + ff < L.NX && z + 2 * ff < L.NZ;
-        } else {
+        } else if (kind == 2) {
             mx = x % f; mz = (z - f / 2) % f;
             ok[0] = z >= mz;
             ok[1] = x + 2 * ff < L.NX;
             ok[2] = x >= mx && z + ff < L.NZ;
             ok[3] = x + 2 * ff < L.NX && z + ff < L.NZ;
+        } else {   // staggered xz (:1568-1661)
+            mx = (x - f / 2) % f; mz = (z - f / 2) % f;
+            ok[0] = x >= mx && z >= mz;
+            ok[1] = x + ff < L.NX;
+            ok[2] = x >= mx && z + ff < L.NZ;
+            ok[3] = x + ff < L.NX && z + ff < L.NZ;
         }
         const int X[4] = {x - mx, x + f - mx, x - mx, x + f - mx};
         const int Z[4] = {z - mz, z - mz, z + f - mz, z + f - mz};
@@ -633,12 +643,20 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool e
         if ((rc = build_ell(N, axis(2, false), G.Dzf, err, "Dzf")) != WAVE_OK) return rc;
         if ((rc = build_ell(N, axis(2, true), G.Dzb, err, "Dzb")) != WAVE_OK) return rc;
     }
-    if (elastic && !is3d) {
+    if (elastic) {
         if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], true, t); }, G.DyfSX, err,
                             "DyfStaggeredX")) != WAVE_OK)
             return rc;
         if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], false, t); }, G.DybSX, err,
                             "DybStaggeredX")) != WAVE_OK)
+            return rc;
+    }
+    if (elastic && is3d) {
+        if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], true, t, true); }, G.DyfSZ,
+                            err, "DyfStaggeredZ")) != WAVE_OK)
+            return rc;
+        if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], false, t, true); },
+                            G.DybSZ, err, "DybStaggeredZ")) != WAVE_OK)
             return rc;
     }
     if (L.varGrid) {
@@ -648,6 +666,7 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool e
         if ((rc = build_interp(L, rows, 0, G.full, err)) != WAVE_OK) return rc;
         if ((rc = build_interp(L, rows, 1, G.stagX, err)) != WAVE_OK) return rc;
         if (is3d && (rc = build_interp(L, rows, 2, G.stagZ, err)) != WAVE_OK) return rc;
+        if (is3d && elastic && (rc = build_interp(L, rows, 3, G.stagXZ, err)) != WAVE_OK) return rc;
     }
     // CPML coefficients per point (CPML2DAcoustic.cpp:140-205): the layer's
     // profile over ceil(BoundaryWidth / dhFactor) points at its own spacing
@@ -731,15 +750,28 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool e
             G.avgPartner[ax][i] = static_cast<int>(j);
         }
     }
-    if (elastic && !is3d) {
-        // calcAverageMatrixXY's 4-point partners (Modelparameter.cpp:449-533)
-        for (auto& v : G.shearPartner) v.assign(N, -1);
-        for (long long i = 0; i < N; ++i) {
-            const long long f = L.dhf[L.layerY[Y[i]]];
-            const bool okx = X[i] + f < L.NX, oky = Y[i] + f < L.NY;
-            if (okx) G.shearPartner[0][i] = static_cast<int>(L.index(X[i] + f, Y[i], Z[i]));
-            if (oky) G.shearPartner[1][i] = static_cast<int>(L.index(X[i], Y[i] + f, Z[i]));
-            if (okx && oky) G.shearPartner[2][i] = static_cast<int>(L.index(X[i] + f, Y[i] + f, Z[i]));
+    if (elastic) {
+        // calcAverageMatrixXY / XZ / YZ's 4-point partners (Modelparameter.cpp:
+        // 449-624): per pair of axes (a, b) the neighbours f along a, along b
+        // and along both, -1 where a coordinate passes the grid
+        const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        for (int q = 0; q < (is3d ? 3 : 1); ++q) {
+            for (auto& v : G.shearPartner[q]) v.assign(N, -1);
+            for (long long i = 0; i < N; ++i) {
+                const int f = L.dhf[L.layerY[Y[i]]];
+                const int c[3] = {X[i], Y[i], Z[i]}, n[3] = {L.NX, L.NY, L.NZ};
+                const int a = pairs[q][0], b = pairs[q][1];
+                const bool oka = c[a] + f < n[a], okb = c[b] + f < n[b];
+                auto at = [&](int da, int db) {
+                    int p[3] = {c[0], c[1], c[2]};
+                    p[a] += da * f;
+                    p[b] += db * f;
+                    return static_cast<int>(L.index(p[0], p[1], p[2]));
+                };
+                if (oka) G.shearPartner[q][0][i] = at(1, 0);
+                if (okb) G.shearPartner[q][1][i] = at(0, 1);
+                if (oka && okb) G.shearPartner[q][2][i] = at(1, 1);
+            }
         }
     }
     G.nSurface = static_cast<long long>(L.vnx[0]) * L.vnz[0];   // layer 0 starts at y = 0
