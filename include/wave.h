@@ -96,8 +96,8 @@ typedef struct wave_config {
     /* Variable (discontinuous) grid, Acquisition/Coordinates.cpp:35-245 and
      * Derivatives.cpp:852-1656. Acoustic equations (2-D and 3-D, free
      * surface allowed) and elastic (2-D and 3-D, FD2Delastic / FD3Delastic
-     * ::run with the staggered-x / -z y-derivatives, no free surface); CPML
-     * or no damping boundary; no adjoint. The grid's index space replaces NX*NY*NZ
+     * ::run with the staggered-x / -z y-derivatives, FreeSurface 0 or 1);
+     * CPML or no damping boundary; no adjoint. The grid's index space replaces NX*NY*NZ
      * everywhere (model arrays, source/receiver indices, wavefields): see
      * wave_grid_*. */
     int useVariableGrid;        /* "useVariableGrid": layers of spacing DH*dhFactor   */
@@ -140,7 +140,8 @@ int wave_grid_coordinates(const wave_config* cfg, int64_t* x, int64_t* y, int64_
  * 8 StaggeredZ (Derivatives.cpp:1252-1546; rows off the interfaces are the
  * identity), the elastic staggered y-derivatives 9 DyfStaggeredX,
  * 10 DybStaggeredX (Derivatives.cpp:852-1011), 11 DyfStaggeredZ,
- * 12 DybStaggeredZ (Derivatives.cpp:1012-1168, 3-D), or 13 the interface
+ * 12 DybStaggeredZ (Derivatives.cpp:1012-1168, 3-D; with FreeSurface=1,
+ * 10 and 12 are DybStaggeredX / ZFreeSurface, :533-704), or 13 the interface
  * interpolation StaggeredXZ (Derivatives.cpp:1568-1661, 3-D). Returned as an
  * ELL block: *width entries per row, entry k of row i at k*N + i, unused
  * entries with weight 0. With cols == NULL only *width is set; otherwise

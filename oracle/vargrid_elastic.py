@@ -23,11 +23,14 @@ import numpy as np
 from oracle import vargrid as vg
 
 
-def _stag_rows(g: vg.VarGrid, y: int, c: int, n: int, orders, var_order: bool, forward: bool):
-    """Taps [(C, Y, order, j, dh layer)] of one row of DyfStaggeredX / Z
+def _stag_rows(g: vg.VarGrid, y: int, c: int, n: int, orders, var_order: bool, forward: bool, fs: bool = False):
+    """Taps [(C, Y, order, j, dh layer, image)] of one row of DyfStaggeredX / Z
     (forward) or DybStaggeredX / Z (Derivatives.cpp:852-1168): c is the row's
     coordinate along the staggered axis (x or z), n that axis' length, C the
-    tap's coordinate along it."""
+    tap's coordinate along it. fs (backward only): DybStaggeredX /
+    ZFreeSurface (Derivatives.cpp:533-704), the image coefficient
+    c[order - 1 - (2 y)/f - j] subtracted where it exists (image -1: none;
+    integer division as the reference's C++ evaluates it)."""
     layer = int(g.layer_y[y])
     order = orders[layer] if var_order else orders[0]
     dist = int(g.dist_y[y]) // g.dhf[layer]
@@ -59,7 +62,7 @@ def _stag_rows(g: vg.VarGrid, y: int, c: int, n: int, orders, var_order: bool, f
         for j in range(order):
             Y = y + f * (j - order // 2 + 1)
             if 0 <= Y < g.NY:
-                out.append((X[j], Y, order, j, dl))
+                out.append((X[j], Y, order, j, dl, -1))
         return out
     f = g.dhf[layer]
     yq = y - (order // 2) * f
@@ -74,17 +77,18 @@ def _stag_rows(g: vg.VarGrid, y: int, c: int, n: int, orders, var_order: bool, f
                 Y += g.dhf[layer - 1]
             if j == 1 and tr == -1:
                 Y += g.dhf[layer + 1]
+        img = order - 1 - (2 * y) // f - j if fs and order >= 1 + (2 * y) // f + j else -1
         if 0 <= Y < g.NY:
-            out.append((X[j], Y, order, j, layer))
+            out.append((X[j], Y, order, j, layer, img))
     return out
 
 
-def staggered_operator(op: vg.Operators, orders, var_order: bool, forward: bool, axis: str = "x"):
+def staggered_operator(op: vg.Operators, orders, var_order: bool, forward: bool, axis: str = "x", fs: bool = False):
     """DyfStaggeredX / DybStaggeredX (axis "x") or DyfStaggeredZ /
-    DybStaggeredZ (axis "z") times DT, as a CSR matrix. The rows of one depth
-    y differ only at the edges of the staggered axis (the shifted taps are
-    guarded by c >= f/3 and c < n - f/3), so each (y, edge class) stencil is
-    built once."""
+    DybStaggeredZ (axis "z") times DT, as a CSR matrix (fs: the backward
+    operators' free-surface variants). The rows of one depth y differ only at
+    the edges of the staggered axis (the shifted taps are guarded by c >= f/3
+    and c < n - f/3), so each (y, edge class) stencil is built once."""
     g = op.g
     n = g.NX if axis == "x" else g.NZ
     rows, cols, vals = [], [], []
@@ -101,14 +105,14 @@ def staggered_operator(op: vg.Operators, orders, var_order: bool, forward: bool,
         for k in np.unique(cls):
             rr = r[cls == k]
             c_rep = int((g.x if axis == "x" else g.z)[rr[0]])
-            for C, Y, o, j, dl in _stag_rows(g, y, c_rep, n, orders, var_order, forward):
+            for C, Y, o, j, dl, img in _stag_rows(g, y, c_rep, n, orders, var_order, forward, fs):
                 dc = C - c_rep
                 if axis == "x":
                     cols.append(g.coordinate2index(g.x[rr] + dc, Y, g.z[rr]))
                 else:
                     cols.append(g.coordinate2index(g.x[rr], Y, g.z[rr] + dc))
                 rows.append(rr)
-                vals.append(np.full(len(rr), op._val(o, j, dl), dtype=op.dtype))
+                vals.append(np.full(len(rr), op._val(o, j, dl, img), dtype=op.dtype))
     return op._finish(rows, cols, vals)
 
 
@@ -198,19 +202,35 @@ def shear_average(g: vg.VarGrid, mu, pair: str, dtype=np.float32):
     return av
 
 
+def free_surface_scales(g: vg.VarGrid, M, mu, dtype=np.float32):
+    """FreeSurfaceElastic::setModelparameter / init (FreeSurfaceElastic.cpp:
+    11-88) on the grid's surface points (y = 0): scaleV = M - 2 mu,
+    scaleH = -(M - 2 mu)^2 / M there, 0 elsewhere; fsZero 0 there, 1
+    elsewhere."""
+    d = np.dtype(dtype).type
+    sel = (g.y == 0).astype(dtype)
+    t = (M - (d(2) * mu).astype(dtype)).astype(dtype)
+    scaleV = (sel * t).astype(dtype)
+    t2 = ((t * t).astype(dtype) / M).astype(dtype)
+    scaleH = (sel * (t2 * d(-1)).astype(dtype)).astype(dtype)
+    return scaleH, scaleV, (d(1) - sel).astype(dtype)
+
+
 class ElasticVarGrid2D:
     """FD2Delastic::run on a 2-D variable grid (ForwardSolver2Delastic.cpp:
-    117-297), CPML or no damping boundary, no free surface."""
+    117-297), CPML or no damping boundary; with free_surface the image
+    operators DybStaggeredXFreeSurface / DyfFreeSurface and the surface
+    exchange (FreeSurface2Delastic.cpp:14-40)."""
 
     def __init__(self, g: vg.VarGrid, orders, DT: float, rho, vp, vs, cpml: dict | None,
                  src_idx, src_type, signals, rec_idx, rec_type, dtype=np.float32, var_order: bool = True,
-                 edge: bool = True, var_grid: bool = True):
+                 edge: bool = True, var_grid: bool = True, free_surface: bool = False):
         if g.NZ != 1:
             raise ValueError("2-D only")
-        self.g, self.dtype = g, dtype
-        self.op = vg.Operators(g, orders, DT, False, dtype, var_order, edge, var_grid)
-        self.DyfSX = staggered_x_operator(self.op, orders, var_order, True)
-        self.DybSX = staggered_x_operator(self.op, orders, var_order, False)
+        self.g, self.dtype, self.fs = g, dtype, free_surface
+        self.op = vg.Operators(g, orders, DT, free_surface, dtype, var_order, edge, var_grid)
+        self.DyfSX = staggered_operator(self.op, orders, var_order, True, "x")
+        self.DybSX = staggered_operator(self.op, orders, var_order, False, "x", free_surface)
         rho = np.asarray(rho, dtype=dtype)
         vp = np.asarray(vp, dtype=dtype)
         vs = np.asarray(vs, dtype=dtype)
@@ -218,6 +238,8 @@ class ElasticVarGrid2D:
         self.mu = (rho * vs * vs).astype(dtype)
         self.muXY = shear_average_xy(g, self.mu, dtype)
         self.irx, self.iry = vg.inverse_density_averages(g, rho, dtype)
+        if free_surface:
+            self.scaleH, self.scaleV, self.fsZero = free_surface_scales(g, self.M, self.mu, dtype)
         self.cpml = cpml
         z = lambda: np.zeros(g.N, dtype=dtype)
         self.vx, self.vy, self.sxx, self.syy, self.sxy = z(), z(), z(), z(), z()
@@ -264,6 +286,11 @@ class ElasticVarGrid2D:
         u2 = self._cpml(op.Dxf @ self.vy, "vyx", "x", True)
         u = ((u + u2).astype(dt) * self.muXY).astype(dt)
         self.sxy = op.IStagX @ (self.sxy + u).astype(dt)
+        if self.fs:
+            # exchangeHorizontalUpdate(vxx, vyy, Sxx), setSurfaceZero(Syy)
+            self.sxx = (self.sxx + (self.scaleH * vxx).astype(dt)).astype(dt)
+            self.sxx = (self.sxx - (self.scaleV * vyy).astype(dt)).astype(dt)
+            self.syy = (self.syy * self.fsZero).astype(dt)
         # sources and receivers (FDTD2Delastic.cpp:12-49)
         for s in range(len(self.src_idx)):
             i, v = self.src_idx[s], self.signals[s, t]
@@ -296,19 +323,22 @@ class ElasticVarGrid3D:
     DyfStaggeredX / DyfStaggeredZ for those of vx / vz in the shear update,
     and the interface interpolations vx StaggeredX, vy Full, vz StaggeredZ,
     sxx / syy / szz Full, sxy StaggeredX, sxz StaggeredXZ, syz StaggeredZ
-    (applied twice, as the reference does)."""
+    (applied twice, as the reference does). With free_surface the image
+    operators DybStaggeredX / ZFreeSurface and DyfFreeSurface and the surface
+    exchange (FreeSurface3Delastic.cpp:15-47, ForwardSolver3Delastic.cpp:
+    400-404)."""
 
     def __init__(self, g: vg.VarGrid, orders, DT: float, rho, vp, vs, cpml: dict | None,
                  src_idx, src_type, signals, rec_idx, rec_type, dtype=np.float32, var_order: bool = True,
-                 edge: bool = True, var_grid: bool = True):
+                 edge: bool = True, var_grid: bool = True, free_surface: bool = False):
         if g.NZ < 2:
             raise ValueError("3-D only")
-        self.g, self.dtype = g, dtype
-        self.op = vg.Operators(g, orders, DT, False, dtype, var_order, edge, var_grid)
+        self.g, self.dtype, self.fs = g, dtype, free_surface
+        self.op = vg.Operators(g, orders, DT, free_surface, dtype, var_order, edge, var_grid)
         self.DyfSX = staggered_operator(self.op, orders, var_order, True, "x")
-        self.DybSX = staggered_operator(self.op, orders, var_order, False, "x")
+        self.DybSX = staggered_operator(self.op, orders, var_order, False, "x", free_surface)
         self.DyfSZ = staggered_operator(self.op, orders, var_order, True, "z")
-        self.DybSZ = staggered_operator(self.op, orders, var_order, False, "z")
+        self.DybSZ = staggered_operator(self.op, orders, var_order, False, "z", free_surface)
         rho = np.asarray(rho, dtype=dtype)
         vp = np.asarray(vp, dtype=dtype)
         vs = np.asarray(vs, dtype=dtype)
@@ -318,6 +348,8 @@ class ElasticVarGrid3D:
         self.muXZ = shear_average(g, self.mu, "xz", dtype)
         self.muYZ = shear_average(g, self.mu, "yz", dtype)
         self.irx, self.iry, self.irz = vg.inverse_density_averages(g, rho, dtype)
+        if free_surface:
+            self.scaleH, self.scaleV, self.fsZero = free_surface_scales(g, self.M, self.mu, dtype)
         self.cpml = cpml
         z = lambda: np.zeros(g.N, dtype=dtype)
         self.f = {k: z() for k in ("vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz")}
@@ -379,6 +411,16 @@ class ElasticVarGrid3D:
         F["sxz"] = op.IStagXZ @ (F["sxz"] + u).astype(dt)
         u = self._vel([(op.Dzf, "vy", "vyz", "z", True), (self.DyfSZ, "vz", "vzy", "y", True)], self.muYZ)
         F["syz"] = op.IStagZ @ (op.IStagZ @ (F["syz"] + u).astype(dt))
+        if self.fs:
+            # setSurfaceZero(Syy), exchangeHorizontalUpdate(vxx + vzz, vyy, Sxx, Szz)
+            upd = (vxx + vzz).astype(dt)
+            F["syy"] = (F["syy"] * self.fsZero).astype(dt)
+            tmp = (self.scaleH * upd).astype(dt)
+            F["sxx"] = (F["sxx"] + tmp).astype(dt)
+            F["szz"] = (F["szz"] + tmp).astype(dt)
+            tmp = (self.scaleV * vyy).astype(dt)
+            F["sxx"] = (F["sxx"] - tmp).astype(dt)
+            F["szz"] = (F["szz"] - tmp).astype(dt)
         # sources and receivers (FDTD3Delastic.cpp:12-53)
         for k in range(len(self.src_idx)):
             i, v = self.src_idx[k], self.signals[k, t]

@@ -129,7 +129,7 @@ def test_gpu_vargrid_chunked_stepping_is_bit_identical(wave, refcpu):
 def test_gpu_vargrid_rejects_what_it_does_not_build(wave, refcpu):
     base = dict(dimension=2, NX=122, NY=100, NZ=1, DH=5.0, DT=5e-4, T=0.01, spatialFDorder=4,
                 useVariableGrid=1, useVariableFDoperators=1, grid=[(0, 1, 4), (31, 3, 4)])
-    for eq, extra in (("sh", {}), ("elastic", dict(FreeSurface=1)), ("elastic", dict(dimension=3, NZ=40, FreeSurface=1)),
+    for eq, extra in (("sh", {}), ("elastic", dict(FreeSurface=2)), ("elastic", dict(DampingBoundary=1, BoundaryWidth=10)),
                       ("viscoelastic", dict(numRelaxationMechanisms=1, relaxationFrequency=[5.0, 0, 0, 0])),
                       ("acoustic", dict(DampingBoundary=1, BoundaryWidth=10))):
         cfg = wave.WaveConfig.make(equation=eq, **dict(base, **extra))

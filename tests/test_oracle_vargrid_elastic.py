@@ -12,14 +12,14 @@ def _model(n, rng):
     return 310.0 * vp ** 0.25, vp, vp / 1.8
 
 
-@pytest.mark.parametrize("boundary", [2, 0])
-def test_single_layer_elastic_vargrid_equals_regular_oracle(boundary, refcpu):
+@pytest.mark.parametrize("boundary,fs", [(2, 0), (0, 0), (2, 1), (0, 1)])
+def test_single_layer_elastic_vargrid_equals_regular_oracle(boundary, fs, refcpu):
     from oracle import vargrid as vg, vargrid_elastic as ve
     NX, NY, DH, order, vmax = 70, 60, 5.0, 4, 3000.0
     DT = 0.3 * DH / (vmax * np.sqrt(2.0))
     cfg = refcpu.make_config(dimension=2, equation="elastic", NX=NX, NY=NY, DH=DH, DT=DT, T=300 * DT,
                              spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=8, NPower=4.0,
-                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0)
+                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0, FreeSurface=fs)
     nt = refcpu.nt_of(cfg)
     rho, vp, vs = _model(NX * NY, np.random.default_rng(1))
     sidx = np.array([NX // 2 + NX * (NY // 3)])
@@ -30,9 +30,9 @@ def test_single_layer_elastic_vargrid_equals_regular_oracle(boundary, refcpu):
     ref = o.run()
     o.close()
     g = vg.VarGrid(NX, NY, 1, DH, [0], [1])
-    cp = vg.cpml_coefficients(g, 8, 4.0, 20.0, vmax, DT, False, np.float64) if boundary == 2 else None
+    cp = vg.cpml_coefficients(g, 8, 4.0, 20.0, vmax, DT, fs != 0, np.float64) if boundary == 2 else None
     sim = ve.ElasticVarGrid2D(g, [order], DT, rho, vp, vs, cp, sidx, [1], sig, ridx, rtype, dtype=np.float64,
-                              var_order=False, edge=False, var_grid=False)
+                              var_order=False, edge=False, var_grid=False, free_surface=fs != 0)
     got = sim.run(nt)
     assert np.abs(ref).max() > 0
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
@@ -97,8 +97,8 @@ def test_library_staggered_operators_equal_the_oracle(grid, NX, NY, wave, refcpu
         assert diff.nnz == 0 or diff.max() == 0, (k, diff.max())
 
 
-@pytest.mark.parametrize("boundary", [2, 0])
-def test_single_layer_3d_elastic_vargrid_equals_regular_oracle(boundary, refcpu):
+@pytest.mark.parametrize("boundary,fs", [(2, 0), (0, 0), (2, 1)])
+def test_single_layer_3d_elastic_vargrid_equals_regular_oracle(boundary, fs, refcpu):
     """The 3-D elastic variable-grid oracle (staggered-Z operators, the XZ /
     YZ shear averages, the 3-D interpolation set) on one layer against the
     pinned regular 3-D elastic oracle, FP64."""
@@ -107,7 +107,7 @@ def test_single_layer_3d_elastic_vargrid_equals_regular_oracle(boundary, refcpu)
     DT = 0.3 * DH / (vmax * np.sqrt(3.0))
     cfg = refcpu.make_config(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=160 * DT,
                              spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=6, NPower=4.0,
-                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0)
+                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0, FreeSurface=fs)
     nt = refcpu.nt_of(cfg)
     rho, vp, vs = _model(NX * NY * NZ, np.random.default_rng(2))
     g = vg.VarGrid(NX, NY, NZ, DH, [0], [1])
@@ -118,9 +118,9 @@ def test_single_layer_3d_elastic_vargrid_equals_regular_oracle(boundary, refcpu)
     o = refcpu.Oracle(cfg, dict(rho=rho, vp=vp, vs=vs), sidx, np.array([1]), sig, ridx, rtype, dtype=np.float64)
     ref = o.run()
     o.close()
-    cp = vg.cpml_coefficients(g, 6, 4.0, 20.0, vmax, DT, False, np.float64) if boundary == 2 else None
+    cp = vg.cpml_coefficients(g, 6, 4.0, 20.0, vmax, DT, fs != 0, np.float64) if boundary == 2 else None
     sim = ve.ElasticVarGrid3D(g, [order], DT, rho, vp, vs, cp, sidx, [1], sig, ridx, rtype, dtype=np.float64,
-                              var_order=False, edge=False, var_grid=False)
+                              var_order=False, edge=False, var_grid=False, free_surface=fs != 0)
     got = sim.run(nt)
     assert np.abs(ref).max() > 0
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
@@ -166,12 +166,15 @@ def test_3d_elastic_vargrid_tracks_the_all_fine_grid(refcpu):
     assert np.linalg.norm(a[3] - a[4]) <= 1e-10 * np.linalg.norm(a[3])
 
 
-@pytest.mark.parametrize("grid,dims", [
-    ([(0, 1, 4), (21, 3, 4), (42, 1, 4)], (49, 60, 49)),
-    ([(0, 1, 2), (12, 3, 6), (30, 9, 2)], (55, 48, 37)),
+@pytest.mark.parametrize("grid,dims,fs", [
+    ([(0, 1, 4), (21, 3, 4), (42, 1, 4)], (49, 60, 49), 0),
+    ([(0, 1, 2), (12, 3, 6), (30, 9, 2)], (55, 48, 37), 0),
+    ([(0, 1, 6), (12, 3, 6), (30, 9, 2)], (55, 48, 37), 1),
+    ([(0, 3, 4), (12, 1, 4)], (49, 40, 49), 1),
 ])
-def test_library_3d_staggered_operators_equal_the_oracle(grid, dims, wave, refcpu):
-    """DyfStaggeredX / DybStaggeredX / DyfStaggeredZ / DybStaggeredZ and the
+def test_library_3d_staggered_operators_equal_the_oracle(grid, dims, fs, wave, refcpu):
+    """DyfStaggeredX / DybStaggeredX / DyfStaggeredZ / DybStaggeredZ (with
+    FreeSurface=1 the backward ones are their image variants) and the
     StaggeredXZ interpolation as the library assembles them on the host
     (wave_grid_operator 9-13) against the oracle, entry for entry, on 3-D
     variable grids."""
@@ -180,14 +183,15 @@ def test_library_3d_staggered_operators_equal_the_oracle(grid, dims, wave, refcp
     NX, NY, NZ = dims
     DT = 4e-4
     kw = dict(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=10.0, DT=DT, T=0.01, spatialFDorder=grid[0][2],
-              useVariableGrid=1, useVariableFDoperators=1, grid=grid)
+              useVariableGrid=1, useVariableFDoperators=1, grid=grid, FreeSurface=fs)
     c = wave.WaveConfig.make(**kw)
     g = vg.VarGrid(NX, NY, NZ, 10.0, [r[0] for r in grid], [r[1] for r in grid])
     orders = [r[2] for r in grid]
-    op = vg.Operators(g, orders, DT, False, np.float32, True, True, True)
-    want = {9: ve.staggered_operator(op, orders, True, True, "x"), 10: ve.staggered_operator(op, orders, True, False, "x"),
-            11: ve.staggered_operator(op, orders, True, True, "z"), 12: ve.staggered_operator(op, orders, True, False, "z"),
-            13: op.IStagXZ}
+    op = vg.Operators(g, orders, DT, fs != 0, np.float32, True, True, True)
+    want = {9: ve.staggered_operator(op, orders, True, True, "x"),
+            10: ve.staggered_operator(op, orders, True, False, "x", fs != 0),
+            11: ve.staggered_operator(op, orders, True, True, "z"),
+            12: ve.staggered_operator(op, orders, True, False, "z", fs != 0), 13: op.IStagXZ}
     for k, w_ in want.items():
         cols, vals = wave.grid_operator(c, k)
         w = cols.shape[0]

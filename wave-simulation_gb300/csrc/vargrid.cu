@@ -246,6 +246,8 @@ enum ElasticOp { O_DXF, O_DYF, O_DZF, O_DXB, O_DYB, O_DZB, O_DYF_SX, O_DYB_SX, O
 
 struct VgeParams {
     long long N;
+    long long nSurface;         // the y = 0 rows (first in the index order); free surface when fs
+    int fs;
     float* v[3];                // vx vy vz
     float* s[6];                // sxx syy szz sxy sxz syz
     float* psi[Q_COUNT];
@@ -332,16 +334,38 @@ __global__ void __launch_bounds__(256) vge_str(VgeParams P)
     const float vzz = IS3D ? vge_term<CPML>(P, O_DZB, V[2], Q_VZZ, 2, false, i) : 0.0f;
     float sum = __fadd_rn(vxx, vyy);
     if (IS3D) sum = __fadd_rn(sum, vzz);
-    const float u = __fmul_rn(sum, P.M[i]);
+    const float M = P.M[i];
+    const float u = __fmul_rn(sum, M);
     const float mu = P.mu[i];
+    float sxx, syy, szz = 0.0f;
     if (IS3D) {
-        P.s[0][i] = __fsub_rn(__fadd_rn(P.s[0][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vyy, vzz), mu)));
-        P.s[1][i] = __fsub_rn(__fadd_rn(P.s[1][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vxx, vzz), mu)));
-        P.s[2][i] = __fsub_rn(__fadd_rn(P.s[2][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vxx, vyy), mu)));
+        sxx = __fsub_rn(__fadd_rn(P.s[0][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vyy, vzz), mu)));
+        syy = __fsub_rn(__fadd_rn(P.s[1][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vxx, vzz), mu)));
+        szz = __fsub_rn(__fadd_rn(P.s[2][i], u), __fmul_rn(2.0f, __fmul_rn(__fadd_rn(vxx, vyy), mu)));
     } else {
-        P.s[0][i] = __fsub_rn(__fadd_rn(P.s[0][i], u), __fmul_rn(2.0f, __fmul_rn(vyy, mu)));
-        P.s[1][i] = __fsub_rn(__fadd_rn(P.s[1][i], u), __fmul_rn(2.0f, __fmul_rn(vxx, mu)));
+        sxx = __fsub_rn(__fadd_rn(P.s[0][i], u), __fmul_rn(2.0f, __fmul_rn(vyy, mu)));
+        syy = __fsub_rn(__fadd_rn(P.s[1][i], u), __fmul_rn(2.0f, __fmul_rn(vxx, mu)));
     }
+    if (P.fs && i < P.nSurface) {
+        // FreeSurfaceElastic::setModelparameter (FreeSurfaceElastic.cpp:11-47):
+        // scaleV = M - 2 mu, scaleH = -(M - 2 mu)^2 / M; exchangeHorizontalUpdate
+        // and setSurfaceZero (FreeSurface2Delastic.cpp:14-40,
+        // FreeSurface3Delastic.cpp:15-47). The surface rows are never
+        // interface rows, so doing it before the interpolations changes nothing.
+        const float t = __fsub_rn(M, __fmul_rn(2.0f, mu));
+        const float scaleH = -__fdiv_rn(__fmul_rn(t, t), M);
+        if (IS3D) {
+            const float h = __fmul_rn(scaleH, __fadd_rn(vxx, vzz)), v = __fmul_rn(t, vyy);
+            sxx = __fsub_rn(__fadd_rn(sxx, h), v);
+            szz = __fsub_rn(__fadd_rn(szz, h), v);
+        } else {
+            sxx = __fsub_rn(__fadd_rn(sxx, __fmul_rn(scaleH, vxx)), __fmul_rn(t, vyy));
+        }
+        syy = 0.0f;
+    }
+    P.s[0][i] = sxx;
+    P.s[1][i] = syy;
+    if (IS3D) P.s[2][i] = szz;
     float a = vge_term<CPML>(P, O_DYF_SX, V[0], Q_VXY, 1, true, i);
     float b = vge_term<CPML>(P, O_DXF, V[1], Q_VYX, 0, true, i);
     P.s[3][i] = __fadd_rn(P.s[3][i], __fmul_rn(__fadd_rn(a, b), P.muS[0][i]));
@@ -438,6 +462,8 @@ VgeParams elastic_params_of(wave_handle* h)
     const VarGridDev& G = *h->vg;
     VgeParams P{};
     P.N = G.N;
+    P.nSurface = G.nSurface;
+    P.fs = G.fs;
     const int vf[3] = {F_VX, F_VY, F_VZ}, sf[6] = {F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ};
     for (int k = 0; k < 3; ++k) P.v[k] = h->f[vf[k]];
     for (int k = 0; k < 6; ++k) P.s[k] = h->f[sf[k]];

@@ -328,8 +328,10 @@ struct Assembler {
     // point of the coarse layer sits at another x, so single taps shift by
     // dhFactor/3; taps outside the grid are dropped (no edge rule).
     // zAxis: DyfStaggeredZ / DybStaggeredZ (:1012-1168), the same rule with
-    // the taps shifting along z
-    void stag_row(int x, int y, int z, bool forward, std::vector<Tap>& out, bool zAxis = false) const
+    // the taps shifting along z. fsImage (backward only): the free-surface
+    // variants DybStaggeredX / ZFreeSurface (:533-704), the image coefficient
+    // c[order - 1 - 2y/f - j] subtracted where it exists.
+    void stag_row(int x, int y, int z, bool forward, std::vector<Tap>& out, bool zAxis = false, bool fsImage = false) const
     {
         const int layer = L.layerY[y];
         int order = order_of(layer);
@@ -365,7 +367,8 @@ struct Assembler {
                 if (j == 0 && tr == 1) Y += L.dhf[layer - 1];
                 if (j == 1 && tr == -1) Y += L.dhf[layer + 1];
             }
-            if (Y >= 0 && Y < L.NY) out.push_back({at(C[j], Y), value(order, j, layer)});
+            const int img = fsImage && order >= 1 + 2 * y / f + j ? order - 1 - 2 * y / f - j : -1;
+            if (Y >= 0 && Y < L.NY) out.push_back({at(C[j], Y), value(order, j, layer, img)});
         }
     }
 
@@ -643,19 +646,21 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool e
         if ((rc = build_ell(N, axis(2, false), G.Dzf, err, "Dzf")) != WAVE_OK) return rc;
         if ((rc = build_ell(N, axis(2, true), G.Dzb, err, "Dzb")) != WAVE_OK) return rc;
     }
+    // with the free surface the backward staggered operators are their image
+    // variants (the only ones the elastic step then uses)
     if (elastic) {
         if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], true, t); }, G.DyfSX, err,
                             "DyfStaggeredX")) != WAVE_OK)
             return rc;
-        if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], false, t); }, G.DybSX, err,
-                            "DybStaggeredX")) != WAVE_OK)
+        if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], false, t, false, fs); },
+                            G.DybSX, err, "DybStaggeredX")) != WAVE_OK)
             return rc;
     }
     if (elastic && is3d) {
         if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], true, t, true); }, G.DyfSZ,
                             err, "DyfStaggeredZ")) != WAVE_OK)
             return rc;
-        if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], false, t, true); },
+        if ((rc = build_ell(N, [&](long long i, std::vector<Tap>& t) { A.stag_row(X[i], Y[i], Z[i], false, t, true, fs); },
                             G.DybSZ, err, "DybStaggeredZ")) != WAVE_OK)
             return rc;
     }
