@@ -97,7 +97,7 @@ typedef struct wave_config {
      * Derivatives.cpp:852-1656. Acoustic equations (2-D and 3-D, free
      * surface allowed) and elastic (2-D and 3-D, FD2Delastic / FD3Delastic
      * ::run with the staggered-x / -z y-derivatives, FreeSurface 0 or 1);
-     * CPML or no damping boundary; no adjoint. The grid's index space replaces NX*NY*NZ
+     * CPML, ABS or no damping boundary; no adjoint. The grid's index space replaces NX*NY*NZ
      * everywhere (model arrays, source/receiver indices, wavefields): see
      * wave_grid_*. */
     int useVariableGrid;        /* "useVariableGrid": layers of spacing DH*dhFactor   */

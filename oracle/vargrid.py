@@ -612,16 +612,55 @@ def cpml_coefficients(g: VarGrid, BW: int, npower: float, fc: float, vmax: float
 
 
 # --------------------------------------------------------------------------
+# ABS on the variable grid
+# --------------------------------------------------------------------------
+def abs_damping(g: VarGrid, BW: int, damping_coeff: float, free_surface: bool, dtype=np.float32):
+    """ABS2D::init / ABS3D::init (ABS2D.cpp:110-180, ABS3D.cpp:154-220) per
+    point of the grid at its fine-grid coordinates (Coordinates::edgeDistance,
+    Coordinates.cpp:734-760): coeff[j] = exp(-a^2 (w - j)^2),
+    a = sqrt(-ln(1 - DampingCoeff/100) / w^2), at the smallest edge distance
+    below w (with a free surface the top rows take the x (and z) distance
+    only); 1 elsewhere."""
+    d = np.dtype(dtype).type
+    w = int(BW)
+    amp = d(1) - d(damping_coeff) / d(100)
+    a = np.sqrt(d(-np.log(amp)) / d(w * w)).astype(dtype)
+    j = np.arange(w)
+    coeff = np.exp(-(a * a * ((w - j) * (w - j)).astype(dtype)).astype(dtype)).astype(dtype)
+    dx = np.minimum(g.x, g.NX - 1 - g.x)
+    dy = np.minimum(g.y, g.NY - 1 - g.y)
+    dz = np.minimum(g.z, g.NZ - 1 - g.z)
+    is3d = g.NZ > 1
+    m = np.minimum(dx, dy)
+    if is3d:
+        m = np.minimum(m, dz)
+    out = np.ones(g.N, dtype=dtype)
+    if not free_surface:
+        sel = m < w
+        out[sel] = coeff[m[sel]]
+        return out
+    top = g.y < w
+    xz = np.where(dx < dz, dx, dz) if is3d else dx
+    sel_top = top & ((dx < w) | (dz < w)) if is3d else top & (dx < w)
+    out[sel_top] = coeff[xz[sel_top]]
+    sel = ~top & (m < w)
+    out[sel] = coeff[m[sel]]
+    return out
+
+
+# --------------------------------------------------------------------------
 # the acoustic time loop
 # --------------------------------------------------------------------------
 class AcousticVarGrid:
-    """FD2Dacoustic / FD3Dacoustic::run on a variable grid, CPML or no
-    damping boundary, mirror free surface (FreeSurface=1) or none."""
+    """FD2Dacoustic / FD3Dacoustic::run on a variable grid, CPML, ABS
+    (`damping`: abs_damping's per-point factors) or no damping boundary,
+    mirror free surface (FreeSurface=1) or none."""
 
     def __init__(self, g: VarGrid, orders, DT: float, rho, vp, free_surface: int, cpml: dict | None,
                  src_idx, src_type, signals, rec_idx, rec_type, dtype=np.float32, var_order: bool = True,
-                 edge: bool = True, var_grid: bool = True):
+                 edge: bool = True, var_grid: bool = True, damping=None):
         self.g, self.dtype = g, dtype
+        self.damping = None if damping is None else np.asarray(damping, dtype=dtype)
         d = np.dtype(dtype).type
         self.op = Operators(g, orders, DT, free_surface == 1, dtype, var_order, edge, var_grid)
         self.is3d = g.NZ > 1
@@ -673,6 +712,13 @@ class AcousticVarGrid:
             upd = (upd + u2).astype(dt)
         upd = (upd * self.M).astype(dt)
         self.p = (self.p + upd).astype(dt)
+        if self.damping is not None:
+            # DampingBoundary.apply(p, vX, vY[, vZ]) before the interpolation
+            self.p = (self.p * self.damping).astype(dt)
+            self.vx = (self.vx * self.damping).astype(dt)
+            self.vy = (self.vy * self.damping).astype(dt)
+            if self.is3d:
+                self.vz = (self.vz * self.damping).astype(dt)
         self.p = op.IFull @ self.p
         if self.fs:
             self.p = (self.p * self.surface).astype(dt)

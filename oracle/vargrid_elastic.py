@@ -224,10 +224,11 @@ class ElasticVarGrid2D:
 
     def __init__(self, g: vg.VarGrid, orders, DT: float, rho, vp, vs, cpml: dict | None,
                  src_idx, src_type, signals, rec_idx, rec_type, dtype=np.float32, var_order: bool = True,
-                 edge: bool = True, var_grid: bool = True, free_surface: bool = False):
+                 edge: bool = True, var_grid: bool = True, free_surface: bool = False, damping=None):
         if g.NZ != 1:
             raise ValueError("2-D only")
         self.g, self.dtype, self.fs = g, dtype, free_surface
+        self.damping = None if damping is None else np.asarray(damping, dtype=dtype)
         self.op = vg.Operators(g, orders, DT, free_surface, dtype, var_order, edge, var_grid)
         self.DyfSX = staggered_operator(self.op, orders, var_order, True, "x")
         self.DybSX = staggered_operator(self.op, orders, var_order, False, "x", free_surface)
@@ -291,6 +292,10 @@ class ElasticVarGrid2D:
             self.sxx = (self.sxx + (self.scaleH * vxx).astype(dt)).astype(dt)
             self.sxx = (self.sxx - (self.scaleV * vyy).astype(dt)).astype(dt)
             self.syy = (self.syy * self.fsZero).astype(dt)
+        if self.damping is not None:
+            # DampingBoundary.apply(Sxx, Syy, Sxy, vX, vY)
+            for k in ("sxx", "syy", "sxy", "vx", "vy"):
+                setattr(self, k, (getattr(self, k) * self.damping).astype(dt))
         # sources and receivers (FDTD2Delastic.cpp:12-49)
         for s in range(len(self.src_idx)):
             i, v = self.src_idx[s], self.signals[s, t]
@@ -330,10 +335,11 @@ class ElasticVarGrid3D:
 
     def __init__(self, g: vg.VarGrid, orders, DT: float, rho, vp, vs, cpml: dict | None,
                  src_idx, src_type, signals, rec_idx, rec_type, dtype=np.float32, var_order: bool = True,
-                 edge: bool = True, var_grid: bool = True, free_surface: bool = False):
+                 edge: bool = True, var_grid: bool = True, free_surface: bool = False, damping=None):
         if g.NZ < 2:
             raise ValueError("3-D only")
         self.g, self.dtype, self.fs = g, dtype, free_surface
+        self.damping = None if damping is None else np.asarray(damping, dtype=dtype)
         self.op = vg.Operators(g, orders, DT, free_surface, dtype, var_order, edge, var_grid)
         self.DyfSX = staggered_operator(self.op, orders, var_order, True, "x")
         self.DybSX = staggered_operator(self.op, orders, var_order, False, "x", free_surface)
@@ -421,6 +427,10 @@ class ElasticVarGrid3D:
             tmp = (self.scaleV * vyy).astype(dt)
             F["sxx"] = (F["sxx"] - tmp).astype(dt)
             F["szz"] = (F["szz"] - tmp).astype(dt)
+        if self.damping is not None:
+            # DampingBoundary.apply(Sxx, Syy, Szz, Sxy, Sxz, Syz, vX, vY, vZ)
+            for k in ("sxx", "syy", "szz", "sxy", "sxz", "syz", "vx", "vy", "vz"):
+                F[k] = (F[k] * self.damping).astype(dt)
         # sources and receivers (FDTD3Delastic.cpp:12-53)
         for k in range(len(self.src_idx)):
             i, v = self.src_idx[k], self.signals[k, t]

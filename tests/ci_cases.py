@@ -115,13 +115,15 @@ def load_vargrid_case(name: str, dtype=np.float32, edge_order_reduction: int = 0
 def run_vargrid_oracle(case: dict, dtype=np.float32) -> np.ndarray:
     from oracle import vargrid
     cfg, g = case["cfg"], case["grid"]
-    cp = None
+    cp = damp = None
     if cfg.DampingBoundary == 2:
         cp = vargrid.cpml_coefficients(g, cfg.BoundaryWidth, cfg.NPower, cfg.CenterFrequencyCPML, cfg.VMaxCPML,
                                        cfg.DT, cfg.FreeSurface != 0, dtype)
+    elif cfg.DampingBoundary == 1:
+        damp = vargrid.abs_damping(g, cfg.BoundaryWidth, cfg.DampingCoeff, cfg.FreeSurface != 0, dtype)
     sim = vargrid.AcousticVarGrid(g, case["orders"], cfg.DT, case["model"]["rho"], case["model"]["vp"], cfg.FreeSurface,
                                   cp, case["src_idx"], case["src_type"], case["signals"].astype(dtype),
                                   case["rec_idx"], case["rec_type"], dtype=dtype,
                                   var_order=bool(cfg.useVariableFDoperators), edge=bool(cfg.edgeOrderReduction),
-                                  var_grid=bool(cfg.useVariableGrid))
+                                  var_grid=bool(cfg.useVariableGrid), damping=damp)
     return sim.run(case["nt"])

@@ -59,6 +59,8 @@ SYNTH = [
     (2, 90, 80, 1, [(0, 1, 2), (40, 1, 8)], 0, 0, 2, 1),
     (3, 41, 60, 41, [(0, 1, 4), (20, 3, 4)], 1, 0, 2, 0),
     (3, 44, 54, 38, [(0, 1, 6), (18, 3, 2), (36, 1, 4)], 1, 1, 2, 1),
+    (2, 122, 100, 1, [(0, 1, 4), (31, 3, 6), (70, 1, 4)], 1, 1, 1, 1),
+    (3, 41, 60, 41, [(0, 1, 4), (20, 3, 4)], 1, 0, 1, 0),
 ]
 
 
@@ -71,7 +73,7 @@ def synth_case(refcpu, k):
     nt = 500
     cfg = refcpu.make_config(dimension=dim, equation="acoustic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=nt * DT,
                              spatialFDorder=grid[0][2], FreeSurface=fs, DampingBoundary=boundary,
-                             BoundaryWidth=12 if boundary else 0, NPower=4.0, CenterFrequencyCPML=12.0,
+                             BoundaryWidth=12 if boundary else 0, DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=12.0,
                              VMaxCPML=vmax, edgeOrderReduction=edge, useVariableGrid=vgrid,
                              useVariableFDoperators=1, grid=grid)
     g = vargrid.VarGrid(NX, NY, NZ, DH, [r[0] for r in grid], [r[1] for r in grid] if vgrid else [1] * len(grid))
@@ -129,9 +131,9 @@ def test_gpu_vargrid_chunked_stepping_is_bit_identical(wave, refcpu):
 def test_gpu_vargrid_rejects_what_it_does_not_build(wave, refcpu):
     base = dict(dimension=2, NX=122, NY=100, NZ=1, DH=5.0, DT=5e-4, T=0.01, spatialFDorder=4,
                 useVariableGrid=1, useVariableFDoperators=1, grid=[(0, 1, 4), (31, 3, 4)])
-    for eq, extra in (("sh", {}), ("elastic", dict(FreeSurface=2)), ("elastic", dict(DampingBoundary=1, BoundaryWidth=10)),
+    for eq, extra in (("sh", {}), ("elastic", dict(FreeSurface=2)),
                       ("viscoelastic", dict(numRelaxationMechanisms=1, relaxationFrequency=[5.0, 0, 0, 0])),
-                      ("acoustic", dict(DampingBoundary=1, BoundaryWidth=10))):
+                      ("tmem", {})):
         cfg = wave.WaveConfig.make(equation=eq, **dict(base, **extra))
         with pytest.raises(wave.WaveError):
             wave.Factory.Create("3d" if extra.get("dimension") == 3 else "2d", eq).initForwardSolver(cfg)

@@ -8,8 +8,8 @@ The step is FD2Delastic::run (ForwardSolver2Delastic.cpp:117-297) and
 FD3Delastic::run (ForwardSolver3Delastic.cpp:120-414) on the layered grid of
 Coordinates (Coordinates.cpp:119-245), with DyfStaggeredX / DybStaggeredX
 (Derivatives.cpp:852-1011), DyfStaggeredZ / DybStaggeredZ (:1012-1168) and
-the StaggeredXZ interpolation (:1568-1661), CPML or no damping boundary,
-with or without the mirror free surface (DybStaggeredX / ZFreeSurface,
+the StaggeredXZ interpolation (:1568-1661), CPML, ABS or no damping
+boundary, with or without the mirror free surface (DybStaggeredX / ZFreeSurface,
 DyfFreeSurface and the surface exchange).
 
 Tolerance: relative L2 over all traces and samples <= 1e-4 against FP64."""
@@ -29,6 +29,8 @@ CASES = [
     (90, 80, [(0, 1, 2), (40, 1, 8)], 0, 2, 1, 0),
     (122, 100, [(0, 1, 4), (31, 3, 6), (70, 1, 4)], 1, 2, 1, 1),
     (113, 96, [(0, 1, 6), (30, 3, 2), (57, 9, 2)], 1, 0, 0, 1),
+    (122, 100, [(0, 1, 4), (31, 3, 4), (70, 1, 4)], 1, 1, 0, 0),
+    (113, 96, [(0, 1, 4), (30, 3, 2), (57, 9, 2)], 1, 1, 1, 1),
 ]
 
 
@@ -40,7 +42,7 @@ def _case(refcpu, k):
     nt = 500
     cfg = refcpu.make_config(dimension=2, equation="elastic", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT, T=nt * DT,
                              spatialFDorder=grid[0][2], FreeSurface=fs, DampingBoundary=boundary,
-                             BoundaryWidth=12 if boundary else 0, NPower=4.0, CenterFrequencyCPML=12.0,
+                             BoundaryWidth=12 if boundary else 0, DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=12.0,
                              VMaxCPML=vmax, edgeOrderReduction=edge, useVariableGrid=vgrid,
                              useVariableFDoperators=1, grid=grid)
     g = vargrid.VarGrid(NX, NY, 1, DH, [r[0] for r in grid], [r[1] for r in grid] if vgrid else [1] * len(grid))
@@ -68,12 +70,14 @@ def _oracle(case, dtype=np.float64):
     if cfg.DampingBoundary == 2:
         cp = vargrid.cpml_coefficients(g, cfg.BoundaryWidth, cfg.NPower, cfg.CenterFrequencyCPML, cfg.VMaxCPML, cfg.DT,
                                        cfg.FreeSurface != 0, dtype)
+    damp = vargrid.abs_damping(g, cfg.BoundaryWidth, cfg.DampingCoeff, cfg.FreeSurface != 0, dtype) \
+        if cfg.DampingBoundary == 1 else None
     m = {k: v.astype(dtype) for k, v in case["model"].items()}
     sim = vargrid_elastic.ElasticVarGrid2D(g, case["orders"], cfg.DT, m["rho"], m["vp"], m["vs"], cp, case["src"],
                                            case["stype"], case["sig"].astype(dtype), case["ridx"], case["rtype"],
                                            dtype=dtype, var_order=bool(cfg.useVariableFDoperators),
                                            edge=bool(cfg.edgeOrderReduction), var_grid=bool(cfg.useVariableGrid),
-                                           free_surface=cfg.FreeSurface != 0)
+                                           free_surface=cfg.FreeSurface != 0, damping=damp)
     return sim.run(case["nt"])
 
 
@@ -120,6 +124,7 @@ CASES_3D = [
     (55, 48, 37, [(0, 1, 2), (12, 3, 6), (30, 9, 2)], 1, 0, 1, 0),
     (40, 38, 36, [(0, 1, 4), (20, 1, 6)], 0, 2, 1, 0),
     (49, 60, 49, [(0, 1, 4), (21, 3, 4), (42, 1, 4)], 1, 2, 0, 1),
+    (49, 60, 49, [(0, 1, 4), (21, 3, 4), (42, 1, 4)], 1, 1, 0, 1),
 ]
 
 
@@ -131,7 +136,7 @@ def _case3d(refcpu, k):
     nt = 300
     cfg = refcpu.make_config(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=nt * DT,
                              spatialFDorder=grid[0][2], FreeSurface=fs, DampingBoundary=boundary,
-                             BoundaryWidth=8 if boundary else 0, NPower=4.0, CenterFrequencyCPML=15.0,
+                             BoundaryWidth=8 if boundary else 0, DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=15.0,
                              VMaxCPML=vmax, edgeOrderReduction=edge, useVariableGrid=vgrid,
                              useVariableFDoperators=1, grid=grid)
     g = vargrid.VarGrid(NX, NY, NZ, DH, [r[0] for r in grid], [r[1] for r in grid] if vgrid else [1] * len(grid))
@@ -164,12 +169,14 @@ def _oracle3d(case, dtype=np.float64):
     if cfg.DampingBoundary == 2:
         cp = vargrid.cpml_coefficients(g, cfg.BoundaryWidth, cfg.NPower, cfg.CenterFrequencyCPML, cfg.VMaxCPML, cfg.DT,
                                        cfg.FreeSurface != 0, dtype)
+    damp = vargrid.abs_damping(g, cfg.BoundaryWidth, cfg.DampingCoeff, cfg.FreeSurface != 0, dtype) \
+        if cfg.DampingBoundary == 1 else None
     m = {k: v.astype(dtype) for k, v in case["model"].items()}
     sim = vargrid_elastic.ElasticVarGrid3D(g, case["orders"], cfg.DT, m["rho"], m["vp"], m["vs"], cp, case["src"],
                                            case["stype"], case["sig"].astype(dtype), case["ridx"], case["rtype"],
                                            dtype=dtype, var_order=bool(cfg.useVariableFDoperators),
                                            edge=bool(cfg.edgeOrderReduction), var_grid=bool(cfg.useVariableGrid),
-                                           free_surface=cfg.FreeSurface != 0)
+                                           free_surface=cfg.FreeSurface != 0, damping=damp)
     return sim.run(case["nt"])
 
 

@@ -162,18 +162,20 @@ def test_library_operators_equal_the_oracle_entry_for_entry(name, edge, fs, wave
         assert diff.nnz == 0 or diff.max() == 0, (k, diff.max())
 
 
-@pytest.mark.parametrize("dim,edge,fs", [(2, 1, 1), (2, 0, 0), (3, 1, 0)])
-def test_single_layer_vargrid_oracle_equals_the_regular_grid_oracle(dim, edge, fs, refcpu):
+@pytest.mark.parametrize("dim,edge,fs,boundary", [(2, 1, 1, 2), (2, 0, 0, 2), (3, 1, 0, 2), (2, 1, 1, 1), (2, 0, 0, 1),
+                                                   (3, 1, 1, 1)])
+def test_single_layer_vargrid_oracle_equals_the_regular_grid_oracle(dim, edge, fs, boundary, refcpu):
     """With one layer the variable-grid restatement must reduce to the regular
-    grid: the two oracles (scipy CSR and the C++ refcpu) agree in FP64."""
+    grid: the two oracles (scipy CSR and the C++ refcpu) agree in FP64, with
+    CPML or ABS."""
     from oracle import vargrid
     NX, NY, NZ = (60, 50, 1) if dim == 2 else (24, 22, 20)
     DH, order = 5.0, 4
     DT = 0.3 * DH / (3000.0 * np.sqrt(dim))
     nt = 150
     cfg = refcpu.make_config(dimension=dim, equation="acoustic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=nt * DT,
-                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=2, BoundaryWidth=8, NPower=4.0,
-                             CenterFrequencyCPML=20.0, VMaxCPML=3000.0, edgeOrderReduction=edge)
+                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary, BoundaryWidth=8, NPower=4.0,
+                             CenterFrequencyCPML=20.0, VMaxCPML=3000.0, edgeOrderReduction=edge, DampingCoeff=8.0)
     nt = refcpu.nt_of(cfg)
     rng = np.random.default_rng(dim)
     n = NX * NY * NZ
@@ -187,9 +189,10 @@ def test_single_layer_vargrid_oracle_equals_the_regular_grid_oracle(dim, edge, f
     ref = o.run()
     o.close()
     g = vargrid.VarGrid(NX, NY, NZ, DH, [0], [1])
-    cp = vargrid.cpml_coefficients(g, 8, 4.0, 20.0, 3000.0, DT, fs != 0, np.float64)
+    cp = vargrid.cpml_coefficients(g, 8, 4.0, 20.0, 3000.0, DT, fs != 0, np.float64) if boundary == 2 else None
+    damp = vargrid.abs_damping(g, 8, 8.0, fs != 0, np.float64) if boundary == 1 else None
     sim = vargrid.AcousticVarGrid(g, [order], DT, rho, vp, fs, cp, sidx, [1], sig, ridx, rtype, dtype=np.float64,
-                                  var_order=False, edge=bool(edge), var_grid=False)
+                                  var_order=False, edge=bool(edge), var_grid=False, damping=damp)
     got = sim.run(nt)
     assert np.abs(ref).max() > 0
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-9

@@ -12,14 +12,15 @@ def _model(n, rng):
     return 310.0 * vp ** 0.25, vp, vp / 1.8
 
 
-@pytest.mark.parametrize("boundary,fs", [(2, 0), (0, 0), (2, 1), (0, 1)])
+@pytest.mark.parametrize("boundary,fs", [(2, 0), (0, 0), (2, 1), (0, 1), (1, 0), (1, 1)])
 def test_single_layer_elastic_vargrid_equals_regular_oracle(boundary, fs, refcpu):
     from oracle import vargrid as vg, vargrid_elastic as ve
     NX, NY, DH, order, vmax = 70, 60, 5.0, 4, 3000.0
     DT = 0.3 * DH / (vmax * np.sqrt(2.0))
     cfg = refcpu.make_config(dimension=2, equation="elastic", NX=NX, NY=NY, DH=DH, DT=DT, T=300 * DT,
                              spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=8, NPower=4.0,
-                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0, FreeSurface=fs)
+                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0, FreeSurface=fs,
+                             DampingCoeff=8.0)
     nt = refcpu.nt_of(cfg)
     rho, vp, vs = _model(NX * NY, np.random.default_rng(1))
     sidx = np.array([NX // 2 + NX * (NY // 3)])
@@ -31,8 +32,9 @@ def test_single_layer_elastic_vargrid_equals_regular_oracle(boundary, fs, refcpu
     o.close()
     g = vg.VarGrid(NX, NY, 1, DH, [0], [1])
     cp = vg.cpml_coefficients(g, 8, 4.0, 20.0, vmax, DT, fs != 0, np.float64) if boundary == 2 else None
+    damp = vg.abs_damping(g, 8, 8.0, fs != 0, np.float64) if boundary == 1 else None
     sim = ve.ElasticVarGrid2D(g, [order], DT, rho, vp, vs, cp, sidx, [1], sig, ridx, rtype, dtype=np.float64,
-                              var_order=False, edge=False, var_grid=False, free_surface=fs != 0)
+                              var_order=False, edge=False, var_grid=False, free_surface=fs != 0, damping=damp)
     got = sim.run(nt)
     assert np.abs(ref).max() > 0
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12
@@ -97,7 +99,7 @@ def test_library_staggered_operators_equal_the_oracle(grid, NX, NY, wave, refcpu
         assert diff.nnz == 0 or diff.max() == 0, (k, diff.max())
 
 
-@pytest.mark.parametrize("boundary,fs", [(2, 0), (0, 0), (2, 1)])
+@pytest.mark.parametrize("boundary,fs", [(2, 0), (0, 0), (2, 1), (1, 0), (1, 1)])
 def test_single_layer_3d_elastic_vargrid_equals_regular_oracle(boundary, fs, refcpu):
     """The 3-D elastic variable-grid oracle (staggered-Z operators, the XZ /
     YZ shear averages, the 3-D interpolation set) on one layer against the
@@ -107,7 +109,8 @@ def test_single_layer_3d_elastic_vargrid_equals_regular_oracle(boundary, fs, ref
     DT = 0.3 * DH / (vmax * np.sqrt(3.0))
     cfg = refcpu.make_config(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=160 * DT,
                              spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=6, NPower=4.0,
-                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0, FreeSurface=fs)
+                             CenterFrequencyCPML=20.0, VMaxCPML=vmax, edgeOrderReduction=0, FreeSurface=fs,
+                             DampingCoeff=8.0)
     nt = refcpu.nt_of(cfg)
     rho, vp, vs = _model(NX * NY * NZ, np.random.default_rng(2))
     g = vg.VarGrid(NX, NY, NZ, DH, [0], [1])
@@ -119,8 +122,9 @@ def test_single_layer_3d_elastic_vargrid_equals_regular_oracle(boundary, fs, ref
     ref = o.run()
     o.close()
     cp = vg.cpml_coefficients(g, 6, 4.0, 20.0, vmax, DT, fs != 0, np.float64) if boundary == 2 else None
+    damp = vg.abs_damping(g, 6, 8.0, fs != 0, np.float64) if boundary == 1 else None
     sim = ve.ElasticVarGrid3D(g, [order], DT, rho, vp, vs, cp, sidx, [1], sig, ridx, rtype, dtype=np.float64,
-                              var_order=False, edge=False, var_grid=False, free_surface=fs != 0)
+                              var_order=False, edge=False, var_grid=False, free_surface=fs != 0, damping=damp)
     got = sim.run(nt)
     assert np.abs(ref).max() > 0
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-12

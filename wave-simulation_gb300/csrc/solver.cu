@@ -616,8 +616,6 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
             return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built for the acoustic and elastic equations");
         if (elastic && c.FreeSurface == 2)
             return fail(nullptr, WAVE_ERR_UNSUPPORTED, "the elastic variable grid is built with the mirror free surface (FreeSurface=1)");
-        if (c.DampingBoundary == 1)
-            return fail(nullptr, WAVE_ERR_UNSUPPORTED, "variable grids are built with CPML or without a damping boundary (not ABS)");
         if (c.useStencilMatrix)
             return fail(nullptr, WAVE_ERR_ARG, "Variable FD operators are not available for stencil matrices");
         std::string err;

@@ -10,7 +10,8 @@
 // and take the (offset, weight) entries from the class table: the rows of a
 // layer's interior share a handful of classes, so the operators cost 4 B per
 // point and pass instead of 8 B per entry.
-// One step is four launches plus the source/receiver kernel:
+// One step is four launches plus the source/receiver kernel (and vg_abs
+// with ABS):
 //   vg_vel    Dxf p, Dyf p (or DyfFreeSurface p), Dzf p, CPML, velocity update
 //   vg_interp velocity rows on the interfaces (InterpolationStaggeredX/Full/StaggeredZ)
 //   vg_pres   Dxb vx + Dyb vy + Dzb vz, CPML, pressure update, surface zero
@@ -209,6 +210,24 @@ __global__ void __launch_bounds__(256) vg_interp(VgInterp I)
     v = __fmaf_rn(w[3], f[c[3]], v);
     if (I.phase[s] == 1) I.tmp[s][k] = v;
     else f[I.row[s][k]] = v;
+}
+
+// DampingBoundary.apply (ABS2D.cpp:14-50, ABS3D.cpp:15-100): every listed
+// field times the point's taper factor
+struct VgAbs {
+    long long N;
+    const float* damp;
+    float* f[9];
+    int n;
+};
+__global__ void __launch_bounds__(256) vg_abs(VgAbs A)
+{
+    dependent_launch_prologue();
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    const float d = A.damp[i];
+    if (d == 1.0f) return;
+    for (int k = 0; k < A.n; ++k) A.f[k][i] = __fmul_rn(A.f[k][i], d);
 }
 
 // Acoustic::prepareForModelling on the variable grid: pWaveModulus = rho vp^2,
@@ -593,6 +612,7 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G)
     }
     D->nSurface = G.nSurface;
     D->fs = h->cfg.FreeSurface == 1 ? 1 : 0;
+    if (!G.absDamp.empty()) D->absDamp = upload(h, G.absDamp);
     h->vg = D;
 }
 
@@ -744,6 +764,21 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
         launch(pres, grid, block, dep, h->stream, with_classes(1));
     }
     ++launches;
+    // ABS: every field of the step times the taper, after the pressure update
+    // and before its interpolation (ForwardSolver2Dacoustic.cpp:176-184,
+    // ForwardSolver3Dacoustic.cpp:212-221), after the stress interpolations
+    // and the free surface (ForwardSolver2Delastic.cpp:283-285,
+    // ForwardSolver3Delastic.cpp:407-409)
+    auto run_abs = [&](std::initializer_list<float*> fields) {
+        VgAbs A{};
+        A.N = G.N;
+        A.damp = G.absDamp;
+        for (float* f : fields)
+            if (f) A.f[A.n++] = f;
+        launch(vg_abs, grid, block, dep, h->stream, A);
+        ++launches;
+    };
+    if (G.absDamp && !G.elastic) run_abs({P.p, P.vx, P.vy, G.is3d ? P.vz : nullptr});
     if (interp && G.elastic) {
         // sxx, syy: Full, sxy: StaggeredX (ForwardSolver2Delastic.cpp:262-270); sources
         // and receivers in the same launch when none is on an interface row
@@ -763,14 +798,15 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
         // read only rows it leaves unchanged), so only a two-phase StaggeredZ
         // list is applied again
         const bool again = G.is3d && G.nInterp[2] > 0 && !G.inplace[2];
+        const bool fuse = apart && h->kernelPath != 1 && !G.absDamp;   // the taper comes before the sources
         const int kinds[6] = {0, 0, 1, 0, 3, 2};
         float* const fields[6] = {E.s[0], E.s[1], E.s[3], G.is3d ? E.s[2] : nullptr, G.is3d ? E.s[4] : nullptr,
                                   G.is3d ? E.s[5] : nullptr};
-        interp_fields(kinds, fields, 6, !again && apart && h->kernelPath != 1);
+        interp_fields(kinds, fields, 6, !again && fuse);
         if (again) {
             const int k2[1] = {2};
             float* const f2[1] = {E.s[5]};
-            interp_fields(k2, f2, 1, apart && h->kernelPath != 1);
+            interp_fields(k2, f2, 1, fuse);
         }
     } else if (interp && G.nInterp[0] > 0) {
         // sources and receivers in the same launch when none is on an interface row
@@ -788,6 +824,9 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
         float* const fields[1] = {P.p};
         interp_fields(kinds, fields, 1, apart && h->kernelPath != 1);
     }
+    if (G.absDamp && G.elastic)
+        run_abs({E.s[0], E.s[1], G.is3d ? E.s[2] : nullptr, E.s[3], G.is3d ? E.s[4] : nullptr, G.is3d ? E.s[5] : nullptr,
+                 E.v[0], E.v[1], G.is3d ? E.v[2] : nullptr});
     h->check(cudaGetLastError(), "variable grid step launch");
     return launches;
 }

@@ -89,6 +89,7 @@ struct VarGridHost {
     // its second axis and both, f the layer's dhFactor (-1: outside the grid)
     std::vector<int> shearPartner[3][3];
     long long nSurface = 0;            // rows with y == 0 (the first rows of layer 0)
+    std::vector<float> absDamp;        // ABS (DampingBoundary=1): the taper factor per point, else empty
 };
 
 // Coordinates set-up from the configuration (Coordinates.cpp:35-95, 119-245).
@@ -122,6 +123,7 @@ struct VarGridDev {
     const int* shear[3][3] = {};            // elastic: shear-average partners per axis pair
     long long nSurface = 0;
     int fs = 0;
+    const float* absDamp = nullptr;         // ABS taper per point (null: no ABS)
     // stencil classes per pass (null: not available)
     const unsigned* clsId[2] = {};
     const int* clsOff[2] = {};

@@ -779,6 +779,30 @@ int vargrid_build(const wave_config& c, VarGridHost& G, std::string& err, bool e
             }
         }
     }
+    if (c.DampingBoundary == 1) {
+        // ABS2D / ABS3D::init (ABS2D.cpp:110-180, ABS3D.cpp:154-220) at each
+        // point's fine-grid coordinates (Coordinates::edgeDistance,
+        // Coordinates.cpp:734-760); the top rows of a free surface take the
+        // x (and z) distance only
+        const int w = c.BoundaryWidth;
+        const std::vector<float> coeff = build_abs_coeff(w, static_cast<float>(c.DampingCoeff));
+        const bool fsTop = c.FreeSurface != 0;
+        auto edge = [](int v, int n) { return !((n - 1 - v) < v) ? v : n - 1 - v; };
+        G.absDamp.assign(N, 1.0f);
+        for (long long i = 0; i < N; ++i) {
+            const int dx = edge(X[i], L.NX), dy = edge(Y[i], L.NY), dz = edge(Z[i], L.NZ);
+            int m = dx < dy ? dx : dy;
+            if (is3d) m = m < dz ? m : dz;
+            float f = 1.0f;
+            if (fsTop && Y[i] < w) {
+                const int xz = is3d ? (!(dx < dz) ? dz : dx) : dx;
+                if (dx < w || (is3d && dz < w)) f = coeff[xz];
+            } else if (m < w) {
+                f = coeff[m];
+            }
+            G.absDamp[i] = f;
+        }
+    }
     G.nSurface = static_cast<long long>(L.vnx[0]) * L.vnz[0];   // layer 0 starts at y = 0
     const EllHost* vel[3] = {&G.Dxf, &G.Dyf, &G.Dzf};
     const EllHost* pres[3] = {&G.Dxb, &G.Dyb, &G.Dzb};
