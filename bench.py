@@ -316,18 +316,19 @@ def run_gpu(args):
         s.set_kernel_path(args.kernel_path)
     s.setSources(sidx, stype, sig)
     s.setReceivers(ridx, rtype)
-    assert args.warmup + args.steps <= s.nt
+    assert args.warmup + args.steps + 8 <= s.nt, "warmup + steps must leave at least 8 steps for the kernel timing"
 
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
 
-    # warm-up, then the timed region: K steps with per-kernel CUDA events on
-    # the solver's stream (inputs resident in HBM, state 9 x 64 MiB >> L2)
+    # warm-up (it also captures the step graph), then the timed region: K
+    # steps of the product path (graph replay of 16-step chunks with
+    # programmatic dependent launch) between two CUDA events on the solver's
+    # stream (inputs resident in HBM, state 9 x 64 MiB >> L2)
     s.run(0, args.warmup)
     barrier()
-    s.set_timing(True)
     launches0 = s.launch_count()
     stream = torch.cuda.ExternalStream(s.stream())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -339,6 +340,12 @@ def run_gpu(args):
         barrier()
     launches = s.launch_count() - launches0
     ms_total = ev0.elapsed_time(ev1)
+    # the step kernels' own durations (roofline): a few more steps with an
+    # event pair around every kernel (no graph)
+    t_k = args.warmup + args.steps
+    n_k = min(32, s.nt - t_k)
+    s.set_timing(True)
+    s.run(t_k, t_k + n_k)
     vel_ms, str_ms, nsamp = s.kernel_times()
     passes = s.streaming_passes()
     s.set_timing(False)
@@ -380,6 +387,8 @@ def run_gpu(args):
                    "order": 8, "l2": "inputs larger than L2 (state 9 x N x 4 B)",
                    "parallelism": f"one shot per rank x{world}" if world > 1 else "1 GPU"},
         "roofline": roof, "e2e": e2e, "gpu_launches": launches, "finite": finite,
+        "timed_path": "CUDA graph replay of 16-step chunks (the library's multi-step path); roofline kernel times "
+                      "from further steps with per-kernel events",
     }
     clocks = clk.summary()
     if clocks:

@@ -1041,8 +1041,11 @@ int wave_solver_step(wave_handle* h, int t_begin, int t_end)
             }
             for (auto e : ev) cudaEventDestroy(e);
         } else {
+            // the step graph is captured at the first call after any change
+            // (capture only: the host records the launches), so that a later
+            // multi-step call replays it without a capture in its way
+            if (h->graphDirty || !h->graph) build_graph(h);
             if (t_end - t >= kGraphSteps) {
-                if (h->graphDirty || !h->graph) build_graph(h);
                 for (; t + kGraphSteps <= t_end; t += kGraphSteps) {
                     h->check(cudaGraphLaunch(h->graph, h->stream), "graph launch");
                     h->launches += h->graphLaunchesPerStep * kGraphSteps;
