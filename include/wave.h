@@ -381,6 +381,9 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *  - 2-D elastic (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297) with
  *    CPML, ABS or no damping boundary and with or without the free surface:
  *    grad_vp, grad_vs, grad_rho receive dJ/dvp, dJ/dvs, dJ/drho;
+ *  - 2-D SH (FD2Dsh::run, ForwardSolver2Dsh.cpp:108-196) with CPML, ABS or
+ *    no damping boundary and with or without the free surface: grad_vs and
+ *    grad_rho receive dJ/dvs, dJ/drho, grad_vp is set to zero;
  *  - lossless 2-D TMz (FD2Dtmem::run, ForwardSolver2Dtmem.cpp:108-174) with
  *    Ez sources and receivers, CPML, ABS or no damping boundary: the three
  *    outputs receive dJ/deps_r, dJ/dsigma, dJ/dmu_r (the model's relative

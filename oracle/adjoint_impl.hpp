@@ -484,6 +484,152 @@ struct TMAdjoint2D {
     }
 };
 
+// Discrete adjoint of the oracle's 2-D SH step (Sim<T>::stepSH, restating
+// FD2Dsh::run, ForwardSolver2Dsh.cpp:108-196, with CPML, the ABS taper and the
+// free surface's image operator on syz): the gradient of J = 1/2 sum
+// (d - d_obs)^2 (vz receivers) with respect to vs and rho. Per step, from X_t
+// and X_{t+1}:
+//   a1' = Dxb sxz + P(sxz_x)   a2' = DybS syz + P(syz_y)
+//   vz' = vz + irho (a1' + a2')                        (before the taper)
+//   c1' = Dxf vz' + P(vzx)     c2' = Dyf vz' + P(vzy)
+//   sxz <- sxz + muXZ c1',  syz <- syz + muYZ c2', then the taper on sxz, syz, vz
+// with irho = 1 / rho and muXZ, muYZ the harmonic 2-point averages of
+// mu = max(rho vs^2, 1) along x and y (0 below 4; SH.cpp:424-431,
+// ModelparameterSeismic.cpp:421-432).
+template <class T>
+struct SHAdjoint2D {
+    Sim<T>& s;
+    const idx_t N;
+    CSR<T> DxfT, DxbT, DyfT, DybST;
+    explicit SHAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    {
+        if (s.is3d || s.eq != WAVE_EQ_SH) throw std::invalid_argument("oracle adjoint: 2-D SH only");
+        DxfT = transpose(s.Dxf);
+        DxbT = transpose(s.Dxb);
+        DyfT = transpose(s.Dyf);
+        DybST = transpose(s.fs ? s.DybFS : s.Dyb);
+    }
+    struct State {
+        std::map<std::string, std::vector<T>> F, psi;
+    };
+    const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
+    {
+        auto it = x.psi.find(n);
+        return it == x.psi.end() ? zero : it->second;
+    }
+    void cpmlT(std::vector<T>& lc, std::vector<T>& lp, const std::vector<T>& a, const std::vector<T>& b) const
+    {
+        if (!s.useCpml) return;
+        for_n(N, [&](idx_t i) {
+            const T c = (T(1) + a[i]) * lc[i] + a[i] * lp[i];
+            lp[i] = b[i] * (lc[i] + lp[i]);
+            lc[i] = c;
+        });
+    }
+
+    double run(const std::vector<T>& vs, const std::vector<T>& rho, const T* dobs, int K, T* gvs, T* grho)
+    {
+        const int NT = s.NT;
+        const size_t nrec = s.rec.idx.size();
+        for (size_t r = 0; r < nrec; ++r)
+            if (s.rec.type[r] != WAVE_TYPE_VZ) throw std::invalid_argument("oracle SH adjoint: vz receivers only");
+        const std::vector<T> zero(N, T(0));
+        s.reset();
+        std::vector<State> ck;
+        for (int t = 0; t < NT; ++t) {
+            if (t % K == 0) ck.push_back({s.F, s.psi});
+            s.step(t);
+        }
+        std::vector<T> res(nrec * static_cast<size_t>(NT));
+        double J = 0;
+        for (size_t k = 0; k < res.size(); ++k) {
+            res[k] = s.seis[k] - dobs[k];
+            J += 0.5 * static_cast<double>(res[k]) * static_cast<double>(res[k]);
+        }
+        std::vector<T> lvz(N, 0), lxz(N, 0), lyz(N, 0);
+        std::map<std::string, std::vector<T>> lp;
+        for (const char* n : {"sxz_x", "syz_y", "vzx", "vzy"}) lp[n].assign(N, 0);
+        std::vector<T> gMuXZ(N, 0), gMuYZ(N, 0), gIr(N, 0);
+        std::vector<T> a1(N), a2(N), c1(N), c2(N), vzp(N), la1(N), la2(N), lc1(N), lc2(N);
+        const int nseg = static_cast<int>(ck.size());
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int t0 = seg * K, t1 = std::min(NT, t0 + K);
+            std::vector<State> X;
+            s.F = ck[seg].F;
+            s.psi = ck[seg].psi;
+            X.push_back({s.F, s.psi});
+            for (int t = t0; t < t1; ++t) {
+                s.step(t);
+                X.push_back({s.F, s.psi});
+            }
+            for (int t = t1 - 1; t >= t0; --t) {
+                const State& X0 = X[t - t0];
+                const State& X1 = X[t - t0 + 1];
+                s.Dxb.spmv(X0.F.at("sxz").data(), a1.data());
+                (s.fs ? s.DybFS : s.Dyb).spmv(X0.F.at("syz").data(), a2.data());
+                const auto& p1 = psiOf(X1, "sxz_x", zero);
+                const auto& p2 = psiOf(X1, "syz_y", zero);
+                const auto& vz0 = X0.F.at("vz");
+                for_n(N, [&](idx_t i) {
+                    a1[i] += p1[i];
+                    a2[i] += p2[i];
+                    vzp[i] = vz0[i] + s.invRho[i] * (a1[i] + a2[i]);
+                });
+                s.Dxf.spmv(vzp.data(), c1.data());
+                s.Dyf.spmv(vzp.data(), c2.data());
+                const auto& q1 = psiOf(X1, "vzx", zero);
+                const auto& q2 = psiOf(X1, "vzy", zero);
+                for_n(N, [&](idx_t i) { c1[i] += q1[i]; c2[i] += q2[i]; });
+                // receivers read X_{t+1}
+                for (size_t r = 0; r < nrec; ++r) lvz[s.rec.idx[r]] += res[r * NT + t];
+                if (s.useAbs)
+                    for (auto* v : {&lxz, &lyz, &lvz}) {
+                        auto& w = *v;
+                        for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
+                    }
+                // sxz += muXZ c1', syz += muYZ c2'
+                for_n(N, [&](idx_t i) {
+                    lc1[i] = s.muXZ[i] * lxz[i];
+                    lc2[i] = s.muYZ[i] * lyz[i];
+                    gMuXZ[i] += lxz[i] * c1[i];
+                    gMuYZ[i] += lyz[i] * c2[i];
+                });
+                cpmlT(lc1, lp["vzx"], s.axh, s.bxh);
+                cpmlT(lc2, lp["vzy"], s.ayh, s.byh);
+                spmv_add(DxfT, lc1, lvz);
+                spmv_add(DyfT, lc2, lvz);
+                // vz' = vz + irho (a1' + a2')
+                for_n(N, [&](idx_t i) {
+                    la1[i] = la2[i] = s.invRho[i] * lvz[i];
+                    gIr[i] += lvz[i] * (a1[i] + a2[i]);
+                });
+                cpmlT(la1, lp["sxz_x"], s.ax, s.bx);
+                cpmlT(la2, lp["syz_y"], s.ay, s.by);
+                spmv_add(DxbT, la1, lxz);
+                spmv_add(DybST, la2, lyz);
+            }
+        }
+        // muXZ = 1 / A2x(1 / mu) (0 below 4): d muXZ_r / d mu_k = muXZ_r^2 A2x[r, k] / mu_k^2; the same along y
+        std::vector<T> y(N), gmu(N, 0);
+        AverageTranspose<T> probe(s);
+        for_n(N, [&](idx_t r) { y[r] = gMuXZ[r] * s.muXZ[r] * s.muXZ[r]; });
+        probe.avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::X, in, out); }, y, gmu);
+        for_n(N, [&](idx_t r) { y[r] = gMuYZ[r] * s.muYZ[r] * s.muYZ[r]; });
+        probe.avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::Y, in, out); }, y, gmu);
+        for (idx_t k = 0; k < N; ++k) {
+            // mu = max(rho vs^2, 1) (clamped values do not move); irho = 1 / rho
+            T raw = rho[k];
+            raw *= vs[k];
+            raw *= vs[k];
+            const bool unclamped = raw >= T(1);
+            const T gm = gmu[k] / (s.mu[k] * s.mu[k]);
+            gvs[k] = unclamped ? gm * T(2) * rho[k] * vs[k] : T(0);
+            grho[k] = (unclamped ? gm * vs[k] * vs[k] : T(0)) - gIr[k] * s.invRho[k] * s.invRho[k];
+        }
+        return J;
+    }
+};
+
 template <class T>
 constexpr const char* ElasticAdjoint2D<T>::kP[4];
 template <class T>

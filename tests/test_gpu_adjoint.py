@@ -187,14 +187,14 @@ def test_batched_adjoint_equals_single_shot_adjoints(wave):
 # ----------------------------------------------------------------------------
 # against the FP64 oracle gradient
 # ----------------------------------------------------------------------------
-# Gate on surveys shaped like the FWI workload (smooth layered model, P
-# sources): 1e-4 relative L2. The blocky two-layer test survey below has a
-# strong velocity source next to a sharp contrast: its FP32 forward already
-# differs from FP64 by 6e-7 (zero-padded edge rows) to 3e-6 (edge-order
-# reduction), and the gradient, a time integral with cancellation, amplifies
-# that to ~1e-4 .. 6e-4; these boundary/operator variants are gated at 1e-3.
+# Gate: 1e-4 relative L2 per parameter. The observed data of the two-layer
+# survey below are 0.8 x the true model's seismograms, so that the residual
+# holds part of the direct wave: with the unscaled data the residual at the
+# receivers next to the sources is a small difference of large direct
+# arrivals, and FP32 rounding alone moves the gradient by 2e-4 .. 6e-4 (the
+# oracle's own FP32 adjoint shows the same); scaled, the oracle's FP32 and
+# FP64 gradients agree to ~2e-5.
 GRAD_TOL = 1e-4
-GRAD_TOL_BLOCKY = 1e-3
 
 
 def _oracle_gradient(refcpu, cfg, model, acq, dobs, K=50):
@@ -224,7 +224,7 @@ def _survey(wave, **kw):
         acq = (acq[0] + NX * 2, acq[1], acq[2], np.where(acq[3] < NX * 10, acq[3] % NX, acq[3]), acq[4])
     st = _solver(wave, cfg, true, acq)
     st.run(0, nt)
-    dobs = st.seismograms()
+    dobs = (0.8 * st.seismograms()).astype(np.float32)
     st.close()
     return cfg, start, acq, dobs
 
@@ -246,7 +246,7 @@ def test_adjoint_gradient_matches_the_fp64_oracle_gradient(wave, refcpu, kw):
     print(f"adjoint {kw}: misfit {J:.6e} vs FP64 {J64:.6e}; gradient rel L2 vp {errs[0]:.2e} vs {errs[1]:.2e} "
           f"rho {errs[2]:.2e}")
     assert abs(J - J64) <= 1e-4 * J64
-    assert max(errs) <= GRAD_TOL_BLOCKY
+    assert max(errs) <= GRAD_TOL
 
 
 def _smooth(rng, ny=NY, nx=NX):

@@ -148,3 +148,66 @@ def test_oracle_tmz_adjoint_matches_fp64_finite_differences(refcpu, boundary, st
         ad = float(np.dot(grads[name], d))
         assert abs(fd) > 0
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
+
+
+def sh_case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=44, NY=36, nt=180):
+    rng = np.random.default_rng(7)
+    y, x = np.mgrid[0:NY, 0:NX]
+    vs = 1200.0 + 500.0 * (y / NY) + 60.0 * np.sin(x / 5.0) + 20 * rng.standard_normal((NY, NX))
+    rho = 1800.0 + 300.0 * (y > NY // 2) + 40.0 * np.cos(x / 7.0)
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(vs=vs, rho=rho).items()}
+    DH, DT = 5.0, 6e-4
+    cfg = refcpu.make_config(dimension=2, equation="sh", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT, T=(nt - 0.4) * DT,
+                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary, BoundaryWidth=8,
+                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=20.0, VMaxCPML=1800.0,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    sidx = np.array([refcpu.grid_index(cfg, NX // 2, 2 if fs else 6, 0)], np.int64)
+    sig = refcpu.ricker(nt, DT, 20.0, 1.0, -0.02, np.float64)[None]
+    rx = np.arange(4, NX - 4, 3)
+    ridx = np.concatenate([rx + NX * (0 if fs else 5), rx + NX * (NY - 6)]).astype(np.int64)
+    return cfg, model, (sidx, np.array([4], np.int32), sig, ridx, np.full(ridx.size, 4, np.int32))
+
+
+@pytest.mark.parametrize("fs,boundary,stencil,reduce", [(0, 2, 0, 1), (0, 0, 1, 0), (1, 2, 0, 1), (0, 1, 0, 1),
+                                                        (1, 1, 1, 0)])
+def test_oracle_sh_adjoint_matches_fp64_finite_differences(refcpu, fs, boundary, stencil, reduce):
+    """The oracle's FP64 adjoint of the 2-D SH step (gradients with respect
+    to vs and rho; the vp gradient is zero) against central finite
+    differences of its own misfit (relative step 1e-5) along smooth
+    directions and at the point of the largest gradient, with CPML, no
+    boundary, ABS and the free surface."""
+    cfg, model, acq = sh_case(refcpu, fs, boundary, stencil, reduce)
+    true = dict(model)
+    yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
+    blob = np.exp(-((xx - cfg.NX * 0.45) ** 2 + (yy - cfg.NY * 0.55) ** 2) / 40.0).reshape(-1)
+    true["vs"] = model["vs"] * (1 + 0.06 * blob)
+    true["rho"] = model["rho"] * (1 - 0.04 * blob)
+    o = refcpu.Oracle(cfg, true, *acq, dtype=np.float64)
+    dobs = o.run()
+    o.close()
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    J, gvp, gvs, grho = o.adjoint_gradient(dobs, checkpoint_every=43)
+    o.close()
+    assert J > 0 and J == pytest.approx(misfit(refcpu, cfg, model, acq, dobs), rel=1e-12)
+    assert not np.any(gvp)
+    rng = np.random.default_rng(13)
+    grads = dict(vs=gvs, rho=grho)
+    for name in ("vs", "rho"):
+        d = smooth_direction(rng, cfg.NY, cfg.NX) * model[name]
+        h = 1e-5   # the SH misfit's curvature puts the truncation at ~1e-6 for 1e-4
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name] + h * d
+        mm[name] = model[name] - h * d
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        ad = float(np.dot(grads[name], d))
+        assert abs(fd) > 0
+        assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
+        k = int(np.argmax(np.abs(grads[name])))
+        hk = 1e-5 * model[name][k]
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name].copy()
+        mm[name] = model[name].copy()
+        mp[name][k] += hk
+        mm[name][k] -= hk
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * hk)
+        assert abs(grads[name][k] - fd) <= 1e-6 * abs(fd), (name, k, grads[name][k], fd)

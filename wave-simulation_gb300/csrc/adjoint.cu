@@ -33,6 +33,13 @@
 // and mu_r (Ca, Cb of ForwardSolverEM.cpp:14-67 with eps = eps_r eps0; the
 // inverse 2-point mu averages of TMEM.cpp:366-374).
 //
+// The 2-D SH step (FD2Dsh::run, ForwardSolver2Dsh.cpp:108-196) likewise:
+//   vz' = vz + irho ((Dxb sxz + P_sxz_x)' + (DybS syz + P_syz_y)')
+//   sxz' = sxz + muXZ (Dxf vz' + P_vzx)',  syz' = syz + muYZ (Dyf vz' + P_vzy)',
+// then the ABS taper on all three, and a last kernel maps dJ/dmuXZ, dJ/dmuYZ,
+// dJ/dirho to vs and rho (mu = max(rho vs^2, 1), its harmonic 2-point averages
+// along x and y, SH.cpp:424-431; irho = 1 / rho).
+//
 // Checkpointing: the forward run saves the state every K steps; the backward
 // sweep recomputes each K-step segment into a buffer of K+1 states and walks
 // it backwards. The reference has no adjoint (its inversion lives in a
@@ -70,6 +77,7 @@ struct AdjShot {
     const float* res;            // residual d - d_obs, nrec x nt
     int nrec, nt;
     int tm;                      // 1: lossless 2-D TMz (parts: hx, hy, ez; psi ezy, ezx, hyx, hxy)
+    int sh;                      // 1: 2-D SH (parts: vz, sxz, syz; psi sxz_x, syz_y, vzx, vzy)
     float* vprime[2];            // vx', vy' (TMz: hx', hy') of the current step (null: the saved state's are they)
     const long long* sidx;       // sources (velocity sources are taken out of v')
     const int* stype;
@@ -327,6 +335,75 @@ __device__ __forceinline__ void adj_tm_h_body(const StepParams& P, const AdjShot
 }
 
 
+// ---- 2-D SH ---------------------------------------------------------------
+// parts of an SH state in the view: AV_VX = vz, AV_SXX = sxz, AV_SYY = syz,
+// AV_P1, AV_P2 = psi of sxz_x, syz_y, AV_Q1, AV_Q2 = psi of vzx, vzy;
+// lf[0], lf[2], lf[3] = adjoints of vz, sxz, syz; T[0..1] = adjoints of the
+// stress-pass derivatives c1, c2, T[2..3] of the velocity-pass ones a1, a2;
+// g[0..2] = dJ/dmuXZ, dJ/dmuYZ, dJ/dirho
+
+// stress-update transpose at step n
+template <int H>
+__device__ __forceinline__ void adj_sh_s_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float* vz1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
+    const Slabs S = slabs_of(P, p);
+    float c1 = deriv<H, true>(vz1, i, 1, p.x, P.Dxf);
+    float c2 = deriv<H, true>(vz1, i, sy, p.y, P.Dyf);
+    if (S.sx >= 0) c1 += X1[A.off[AV_Q1] + S.px];
+    if (S.sy >= 0) c2 += X1[A.off[AV_Q2] + S.py];
+    float lxz = A.lf[2][i], lyz = A.lf[3][i];
+    if (pending) {
+        // the transposed velocity-update derivatives of the stresses from the step after this one
+        lxz += derivT<H, false>(A.T[2], i, 1, p.x, P.Dxb);
+        lyz += derivT<H, false>(A.T[3], i, sy, p.y, P.fs ? P.DybS : P.Dyb);
+    }
+    if (P.abs) {
+        // the taper multiplied sxz, syz and vz last: their adjoints first
+        const float d = absDamp(P, p);
+        lxz *= d;
+        lyz *= d;
+        A.lf[0][i] *= d;
+    }
+    A.lf[2][i] = lxz;
+    A.lf[3][i] = lyz;
+    float l1 = __ldg(P.m[M_MUXZ] + i) * lxz, l2 = __ldg(P.m[M_MUYZ] + i) * lyz;
+    A.g[0][i] += lxz * c1;
+    A.g[1][i] += lyz * c2;
+    if (S.sx >= 0) cpml_adj(l1, A.lpsi[4] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // vzx: x, half profile
+    if (S.sy >= 0) cpml_adj(l2, A.lpsi[5] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // vzy: y, half profile
+    A.T[0][i] = l1;
+    A.T[1][i] = l2;
+}
+
+// velocity-update transpose at step n (after the stress transpose of every point)
+template <int H>
+__device__ __forceinline__ void adj_sh_v_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    float lvz = A.lf[0][i];
+    lvz += derivT<H, true>(A.T[0], i, 1, p.x, P.Dxf);
+    lvz += derivT<H, true>(A.T[1], i, sy, p.y, P.Dyf);
+    const Slabs S = slabs_of(P, p);
+    float a1 = deriv<H, false>(X0 + A.off[AV_SXX], i, 1, p.x, P.Dxb);
+    float a2 = deriv<H, false>(X0 + A.off[AV_SYY], i, sy, p.y, P.fs ? P.DybS : P.Dyb);
+    if (S.sx >= 0) a1 += X1[A.off[AV_P1] + S.px];
+    if (S.sy >= 0) a2 += X1[A.off[AV_P2] + S.py];
+    const float ir = __ldg(P.m[M_IR] + i);
+    float l1 = ir * lvz, l2 = l1;
+    A.g[2][i] += lvz * (a1 + a2);
+    if (S.sx >= 0) cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // sxz_x: x, full profile
+    if (S.sy >= 0) cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // syz_y: y, full profile
+    A.T[2][i] = l1;
+    A.T[3][i] = l2;
+    A.lf[0][i] = lvz;
+}
+
+
 template <int H, int PASS>
 __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
                                                 const BatchTile* __restrict__ W, BatchSched S, int vn, int pending)
@@ -337,7 +414,9 @@ __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ P
         if (PASS == 0) adj_stress_body<H>(P, A, p, vn, pending != 0);
         else if (PASS == 1) adj_vel_body<H>(P, A, p, vn);
         else if (PASS == 3) adj_tm_e_body<H>(P, A, p, vn, pending != 0);
-        else adj_tm_h_body<H>(P, A, p, vn);
+        else if (PASS == 4) adj_tm_h_body<H>(P, A, p, vn);
+        else if (PASS == 5) adj_sh_s_body<H>(P, A, p, vn, pending != 0);
+        else adj_sh_v_body<H>(P, A, p, vn);
     });
 }
 
@@ -353,7 +432,7 @@ __global__ void adj_vprime(const StepParams* __restrict__ Ps, const AdjShot* __r
         const float* X1 = A.view + (long long)(vn + 1) * A.stride;
         const float d = P.abs ? absDamp(P, p) : 1.0f;
         A.vprime[0][p.i] = X1[A.off[AV_VX] + p.i] / d;
-        A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
+        if (!A.sh) A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
     });
 }
 
@@ -364,7 +443,7 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
     if (!A.vprime[0]) return;
     for (int k = threadIdx.x; k < A.nsrc; k += blockDim.x) {
         const int t = A.stype[k];
-        if (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY) continue;
+        if (A.sh ? t != WAVE_TYPE_VZ : (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY)) continue;
         const long long i = A.sidx[k];
         Pt p;
         p.i = i;
@@ -372,7 +451,7 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
         p.y = static_cast<int>(i / P.NX);
         p.z = 0;
         const float d = P.abs ? absDamp(P, p) : 1.0f;
-        atomicAdd(A.vprime[t == WAVE_TYPE_VX ? 0 : 1] + i, -A.signals[(long long)k * A.nt + n] / d);
+        atomicAdd(A.vprime[(A.sh || t == WAVE_TYPE_VX) ? 0 : 1] + i, -A.signals[(long long)k * A.nt + n] / d);
     }
 }
 
@@ -386,6 +465,10 @@ __global__ void adj_inject(const AdjShot* __restrict__ As, int n)
         const long long i = A.ridx[r];
         if (A.tm) {   // Ez receivers
             atomicAdd(A.lf[2] + i, v);
+            continue;
+        }
+        if (A.sh) {   // vz receivers
+            atomicAdd(A.lf[0] + i, v);
             continue;
         }
         switch (A.rtype[r]) {
@@ -514,6 +597,41 @@ __global__ void adj_tm_final(PrepParams G, const StepParams P, const AdjShot A, 
     }
 }
 
+// chain rule for SH: mu = max(rho vs^2, 1); muXZ, muYZ = 1 / (2-point average
+// of 1 / mu) along x, y (0 below 4); irho = 1 / rho. grad_vp is zero.
+__global__ void adj_sh_final(PrepParams G, const StepParams P, const AdjShot A, float* gvp, float* gvs, float* grho, int accumulate)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
+        const int kx = static_cast<int>(k % G.NX), ky = static_cast<int>(k / G.NX);
+        const float rho = P.m[M_RHO][k], vs = P.m[M_VS][k], muk = P.m[M_MU][k];
+        // rows (kx, ky) and (kx-1, ky) of the x average, (kx, ky) and (kx, ky-1) of the y average
+        float gmu = 0.0f;
+        for (int d = 0; d <= 1; ++d) {
+            if (kx - d >= 0) {
+                const long long r = k - d;
+                const float m = P.m[M_MUXZ][r];
+                const float w = (kx - d + 1 < G.NX) ? 0.5f : 1.0f;
+                if (m != 0.0f && (d == 0 || w == 0.5f)) gmu += A.g[0][r] * w * (m / muk) * (m / muk);
+            }
+            if (ky - d >= 0) {
+                const long long r = k - d * (long long)G.NX;
+                const float m = P.m[M_MUYZ][r];
+                const float w = (ky - d + 1 < G.NY) ? 0.5f : 1.0f;
+                if (m != 0.0f && (d == 0 || w == 0.5f)) gmu += A.g[1][r] * w * (m / muk) * (m / muk);
+            }
+        }
+        float raw = rho;
+        raw *= vs;
+        raw *= vs;
+        const bool unclamped = raw >= 1.0f;
+        const float ir = P.m[M_IR][k];
+        const float gs = unclamped ? gmu * 2.0f * rho * vs : 0.0f;
+        const float gr = (unclamped ? gmu * vs * vs : 0.0f) - A.g[2][k] * ir * ir;
+        if (accumulate) { gvs[k] += gs; grho[k] += gr; }
+        else { gvp[k] = 0.0f; gvs[k] = gs; grho[k] = gr; }
+    }
+}
+
 template <int H>
 void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
                   int pending, cudaStream_t s)
@@ -523,7 +641,9 @@ void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const Batch
     case 0: adj_pass<H, 0><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
     case 1: adj_pass<H, 1><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
     case 3: adj_pass<H, 3><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    default: adj_pass<H, 4><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 4: adj_pass<H, 4><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 5: adj_pass<H, 5><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    default: adj_pass<H, 6><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
     }
 }
 
@@ -570,8 +690,8 @@ struct DevPool {
 std::string adjoint_supported(const wave_handle* h)
 {
     const wave_config& c = h->cfg;
-    if (c.dimension != 2 || (c.equation != WAVE_EQ_ELASTIC && c.equation != WAVE_EQ_TMEM))
-        return "the adjoint gradient is implemented for 2-D elastic and lossless 2-D TMz modelling";
+    if (c.dimension != 2 || (c.equation != WAVE_EQ_ELASTIC && c.equation != WAVE_EQ_TMEM && c.equation != WAVE_EQ_SH))
+        return "the adjoint gradient is implemented for 2-D elastic, 2-D SH and lossless 2-D TMz modelling";
     if (c.equation == WAVE_EQ_TMEM) {
         for (int t : h->hRecType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez receivers only";
@@ -610,13 +730,17 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const long long N = h->N;
         // state layout: 5 field parts then 8 psi parts (absent parts: length 0);
         // TMz: hx, hy, ez and the psi of ezy, ezx, hyx, hxy
+        // SH: vz, -, sxz, syz and the psi of sxz_x, syz_y, -, -, vzx, vzy
         const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
+        const bool sh = h->cfg.equation == WAVE_EQ_SH;
         long long off[AV_COUNT], len[AV_COUNT], o = 0;
         const int elasticFields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
         const int tmFields[5] = {F_HX, F_HY, F_EZ, -1, -1};
         const int tmPsi[8] = {PS_EZY, PS_EZX, PS_HYX, PS_HXY, -1, -1, -1, -1};
-        const int* fields = tm ? tmFields : elasticFields;
-        const int* psiSlot = tm ? tmPsi : kAdjPsiSlot;
+        const int shFields[5] = {F_VZ, -1, F_SXZ, F_SYZ, -1};
+        const int shPsi[8] = {PS_SXZ_X, PS_SYZ_Y, -1, -1, PS_VZX, PS_VZY, -1, -1};
+        const int* fields = tm ? tmFields : sh ? shFields : elasticFields;
+        const int* psiSlot = tm ? tmPsi : sh ? shPsi : kAdjPsiSlot;
         for (int k = 0; k < 5; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
         for (int k = 0; k < 8; ++k) {
             const int slot = psiSlot[k];
@@ -627,6 +751,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         stride[s] = o;
         AdjShot& a = A[s];
         a.tm = tm ? 1 : 0;
+        a.sh = sh ? 1 : 0;
         a.view = pool.get<float>(static_cast<size_t>(o) * (K + 1));
         a.stride = o;
         for (int k = 0; k < AV_COUNT; ++k) a.off[k] = off[k];
@@ -646,7 +771,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         float* res = pool.get<float>(static_cast<size_t>(h->nrec) * NT);
         a.res = res;
         bool velocitySources = false;
-        for (int t : h->hSrcType) velocitySources |= (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
+        for (int t : h->hSrcType) velocitySources |= sh ? t == WAVE_TYPE_VZ : (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
         a.vprime[0] = a.vprime[1] = nullptr;
         if (h->cfg.DampingBoundary == 1 || velocitySources) {
             a.vprime[0] = pool.get<float>(2 * N);
@@ -729,7 +854,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             // two kernels per step: the third stage of step n (the transposed
             // derivatives of the first-pass inputs) runs inside the first kernel
             // of step n - 1; after step 0 it is not needed
-            const int first = A[0].tm ? 3 : 0;
+            const int first = A[0].tm ? 3 : A[0].sh ? 5 : 0;
             const int pending = n < NT - 1 ? 1 : 0;
             launch_adj(H, first, dP, dA, dT, sched, grid, n - n0, pending, st);
             launch_adj(H, first + 1, dP, dA, dT, sched, grid, n - n0, pending, st);
@@ -744,6 +869,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         if (A[s].tm)
             adj_tm_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
                                                sum && s > 0 ? 1 : 0);
+        else if (A[s].sh)
+            adj_sh_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
         else
             adj_grad_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
     }
