@@ -630,6 +630,180 @@ struct SHAdjoint2D {
     }
 };
 
+// Discrete adjoint of the oracle's lossless 2-D TEz step (Sim<T>::stepTE,
+// restating FD2Demem::run, ForwardSolver2Demem.cpp:112-185, with CPML and the
+// ABS taper): the gradient of J = 1/2 sum (d - d_obs)^2 (Ex, Ey and Hz
+// receivers) with respect to eps_r, sigma and mu_r. Per step, from X_t and
+// X_{t+1}:
+//   a1' = Dxf ey + P(eyx)   a2' = Dyf ex + P(exy)
+//   hz' = hz - iMxy (a1' - a2')                          (before the taper)
+//   c1' = Dyb hz' + P(hzy)  c2' = Dxb hz' + P(hzx)
+//   ex <- CaX ex + CbX c1',  ey <- CaY ey - CbY c2', then the taper on ey, ex, hz
+// with CaX, CbX of the 2-point x averages of eps = eps_r eps0 and sigma (CaY,
+// CbY along y; ForwardSolverEM.cpp:14-67, EMEM.cpp:378-392) and iMxy the
+// inverse 4-point average of mu = mu_r mu0.
+template <class T>
+struct TEAdjoint2D {
+    Sim<T>& s;
+    const idx_t N;
+    CSR<T> DxfT, DxbT, DyfT, DybT;
+    explicit TEAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    {
+        if (s.is3d || s.eq != WAVE_EQ_EMEM) throw std::invalid_argument("oracle adjoint: lossless 2-D TEz only");
+        DxfT = transpose(s.Dxf);
+        DxbT = transpose(s.Dxb);
+        DyfT = transpose(s.Dyf);
+        DybT = transpose(s.Dyb);
+    }
+    struct State {
+        std::map<std::string, std::vector<T>> F, psi;
+    };
+    const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
+    {
+        auto it = x.psi.find(n);
+        return it == x.psi.end() ? zero : it->second;
+    }
+    void cpmlT(std::vector<T>& lc, std::vector<T>& lp, const std::vector<T>& a, const std::vector<T>& b) const
+    {
+        if (!s.useCpml) return;
+        for_n(N, [&](idx_t i) {
+            const T c = (T(1) + a[i]) * lc[i] + a[i] * lp[i];
+            lp[i] = b[i] * (lc[i] + lp[i]);
+            lc[i] = c;
+        });
+    }
+
+    double run(const std::vector<T>& epsr, const std::vector<T>& sigma, const std::vector<T>& mur, const T* dobs, int K,
+               T* geps, T* gsig, T* gmu)
+    {
+        const int NT = s.NT;
+        const size_t nrec = s.rec.idx.size();
+        const std::vector<T> zero(N, T(0));
+        s.reset();
+        std::vector<State> ck;
+        for (int t = 0; t < NT; ++t) {
+            if (t % K == 0) ck.push_back({s.F, s.psi});
+            s.step(t);
+        }
+        std::vector<T> res(nrec * static_cast<size_t>(NT));
+        double J = 0;
+        for (size_t k = 0; k < res.size(); ++k) {
+            res[k] = s.seis[k] - dobs[k];
+            J += 0.5 * static_cast<double>(res[k]) * static_cast<double>(res[k]);
+        }
+        std::vector<T> lhz(N, 0), lex(N, 0), ley(N, 0);
+        std::map<std::string, std::vector<T>> lp;
+        for (const char* n : {"eyx", "exy", "hzy", "hzx"}) lp[n].assign(N, 0);
+        std::vector<T> gCaX(N, 0), gCbX(N, 0), gCaY(N, 0), gCbY(N, 0), gMxy(N, 0);
+        std::vector<T> a1(N), a2(N), c1(N), c2(N), hzp(N), la1(N), la2(N), lc1(N), lc2(N);
+        const int nseg = static_cast<int>(ck.size());
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int t0 = seg * K, t1 = std::min(NT, t0 + K);
+            std::vector<State> X;
+            s.F = ck[seg].F;
+            s.psi = ck[seg].psi;
+            X.push_back({s.F, s.psi});
+            for (int t = t0; t < t1; ++t) {
+                s.step(t);
+                X.push_back({s.F, s.psi});
+            }
+            for (int t = t1 - 1; t >= t0; --t) {
+                const State& X0 = X[t - t0];
+                const State& X1 = X[t - t0 + 1];
+                const auto& ex0 = X0.F.at("ex");
+                const auto& ey0 = X0.F.at("ey");
+                const auto& hz0 = X0.F.at("hz");
+                s.Dxf.spmv(ey0.data(), a1.data());
+                s.Dyf.spmv(ex0.data(), a2.data());
+                const auto& peyx = psiOf(X1, "eyx", zero);
+                const auto& pexy = psiOf(X1, "exy", zero);
+                for_n(N, [&](idx_t i) {
+                    a1[i] += peyx[i];
+                    a2[i] += pexy[i];
+                    hzp[i] = hz0[i] - s.invMuXY[i] * (a1[i] - a2[i]);
+                });
+                s.Dyb.spmv(hzp.data(), c1.data());
+                s.Dxb.spmv(hzp.data(), c2.data());
+                const auto& phzy = psiOf(X1, "hzy", zero);
+                const auto& phzx = psiOf(X1, "hzx", zero);
+                for_n(N, [&](idx_t i) { c1[i] += phzy[i]; c2[i] += phzx[i]; });
+                for (size_t r = 0; r < nrec; ++r) {
+                    const idx_t i = s.rec.idx[r];
+                    const T v = res[r * NT + t];
+                    switch (s.rec.type[r]) {
+                    case WAVE_TYPE_EX: lex[i] += v; break;
+                    case WAVE_TYPE_EY: ley[i] += v; break;
+                    case WAVE_TYPE_HZ: lhz[i] += v; break;
+                    default: throw std::invalid_argument("oracle TEz adjoint: Ex, Ey and Hz receivers only");
+                    }
+                }
+                if (s.useAbs)
+                    for (auto* v : {&ley, &lex, &lhz}) {
+                        auto& w = *v;
+                        for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
+                    }
+                // ex <- CaX ex + CbX c1', ey <- CaY ey - CbY c2'
+                for_n(N, [&](idx_t i) {
+                    lc1[i] = s.CbX[i] * lex[i];
+                    lc2[i] = -s.CbY[i] * ley[i];
+                    gCaX[i] += lex[i] * ex0[i];
+                    gCbX[i] += lex[i] * c1[i];
+                    gCaY[i] += ley[i] * ey0[i];
+                    gCbY[i] -= ley[i] * c2[i];
+                    lex[i] *= s.CaX[i];
+                    ley[i] *= s.CaY[i];
+                });
+                cpmlT(lc1, lp["hzy"], s.ay, s.by);
+                cpmlT(lc2, lp["hzx"], s.ax, s.bx);
+                spmv_add(DybT, lc1, lhz);
+                spmv_add(DxbT, lc2, lhz);
+                // hz' = hz - iMxy (a1' - a2')
+                for_n(N, [&](idx_t i) {
+                    la1[i] = -s.invMuXY[i] * lhz[i];
+                    la2[i] = s.invMuXY[i] * lhz[i];
+                    gMxy[i] -= lhz[i] * (a1[i] - a2[i]);
+                });
+                cpmlT(la1, lp["eyx"], s.axh, s.bxh);
+                cpmlT(la2, lp["exy"], s.ayh, s.byh);
+                spmv_add(DxfT, la1, ley);
+                spmv_add(DyfT, la2, lex);
+            }
+        }
+        // CaX, CbX -> the x averages of eps and sigma -> eps_r, sigma (the same along y)
+        const T eps0 = static_cast<T>(8.8541878176e-12), mu0 = static_cast<T>(1.2566370614e-6);
+        const T DT = s.DT;
+        std::vector<T> eps(N), ge(N, 0), gs(N, 0), ye(N), ys(N), avE(N), avS(N);
+        for (idx_t i = 0; i < N; ++i) eps[i] = epsr[i] * eps0;
+        AverageTranspose<T> probe(s);
+        for (Axis a : {Axis::X, Axis::Y}) {
+            average2<T>(s.g, a, eps.data(), avE.data());
+            average2<T>(s.g, a, sigma.data(), avS.data());
+            const std::vector<T>& gCa = a == Axis::X ? gCaX : gCaY;
+            const std::vector<T>& gCb = a == Axis::X ? gCbX : gCbY;
+            for (idx_t i = 0; i < N; ++i) {
+                const T e = avE[i], sg = avS[i];
+                const T k = sg * DT / (T(2) * e), q = T(1) + k;
+                const T dCa_de = T(2) * k / (e * q * q), dCa_ds = -T(2) / (q * q) * DT / (T(2) * e);
+                const T dCb_de = -T(1) / (e * e * q) + k / (e * e * q * q), dCb_ds = -(T(1) / e) / (q * q) * DT / (T(2) * e);
+                ye[i] = gCa[i] * dCa_de + gCb[i] * dCb_de;
+                ys[i] = gCa[i] * dCa_ds + gCb[i] * dCb_ds;
+            }
+            probe.avgT([&](const T* in, T* out) { average2<T>(s.g, a, in, out); }, ye, ge);
+            probe.avgT([&](const T* in, T* out) { average2<T>(s.g, a, in, out); }, ys, gs);
+        }
+        std::vector<T> y(N), gm(N, 0);
+        for_n(N, [&](idx_t r) { y[r] = -gMxy[r] * s.invMuXY[r] * s.invMuXY[r]; });
+        probe.avgT([&](const T* in, T* out) { average4<T>(s.g, 0, in, out); }, y, gm);
+        for (idx_t i = 0; i < N; ++i) {
+            geps[i] = eps0 * ge[i];
+            gsig[i] = gs[i];
+            gmu[i] = mu0 * gm[i];
+        }
+        (void)mur;
+        return J;
+    }
+};
+
 template <class T>
 constexpr const char* ElasticAdjoint2D<T>::kP[4];
 template <class T>

@@ -237,8 +237,9 @@ int refcpu_adjoint_sh(void* hv, const double* vs, const double* rho, const doubl
     }
 }
 
-// The same for a lossless 2-D TMz simulation (Ez receivers): gradients with
-// respect to eps_r, sigma and mu_r (adjoint_impl.hpp, TMAdjoint2D).
+// The same for a lossless 2-D TMz simulation (Ez receivers) or a lossless 2-D
+// TEz one (Ex, Ey, Hz receivers): gradients with respect to eps_r, sigma and
+// mu_r (adjoint_impl.hpp, TMAdjoint2D / TEAdjoint2D).
 int refcpu_adjoint_tmz(void* hv, const double* epsr, const double* sigma, const double* mur, const double* dobs, int K,
                        double* misfit, double* geps, double* gsig, double* gmu)
 {
@@ -247,8 +248,13 @@ int refcpu_adjoint_tmz(void* hv, const double* epsr, const double* sigma, const 
         using T = typename std::decay_t<decltype(s->M)>::value_type;
         const size_t N = s->g.N(), nd = s->rec.idx.size() * static_cast<size_t>(s->NT);
         std::vector<T> E(epsr, epsr + N), S(sigma, sigma + N), U(mur, mur + N), D(dobs, dobs + nd), a(N), b(N), c(N);
-        refcpu::TMAdjoint2D<T> adj(*s);
-        *misfit = adj.run(E, S, U, D.data(), K, a.data(), b.data(), c.data());
+        if (s->eq == WAVE_EQ_EMEM) {
+            refcpu::TEAdjoint2D<T> adj(*s);
+            *misfit = adj.run(E, S, U, D.data(), K, a.data(), b.data(), c.data());
+        } else {
+            refcpu::TMAdjoint2D<T> adj(*s);
+            *misfit = adj.run(E, S, U, D.data(), K, a.data(), b.data(), c.data());
+        }
         std::copy(a.begin(), a.end(), geps);
         std::copy(b.begin(), b.end(), gsig);
         std::copy(c.begin(), c.end(), gmu);

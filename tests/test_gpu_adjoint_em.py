@@ -1,10 +1,12 @@
-"""Adjoint gradient of the lossless 2-D TMz misfit (wave_adjoint_gradient on a
-TMz handle: dJ/deps_r, dJ/dsigma, dJ/dmu_r) against the FP64 oracle's own
-discrete adjoint (oracle/adjoint_impl.hpp, TMAdjoint2D, pinned to FP64 finite
-differences at 1e-6 in tests/test_oracle_adjoint.py), with CPML, ABS and no
-boundary, sparse and stencil operators; the batched entry equals the
-single-shot one bit for bit. The forward differentiated is FD2Dtmem::run
-(ForwardSolver2Dtmem.cpp:108-174); the reference has no adjoint.
+"""Adjoint gradients of the lossless 2-D TMz and TEz misfits
+(wave_adjoint_gradient on a TMz / TEz handle: dJ/deps_r, dJ/dsigma, dJ/dmu_r)
+against the FP64 oracle's own discrete adjoints (oracle/adjoint_impl.hpp,
+TMAdjoint2D / TEAdjoint2D, pinned to FP64 finite differences at 1e-6 in
+tests/test_oracle_adjoint.py), with CPML, ABS and no boundary, sparse and
+stencil operators; the batched entry equals the single-shot one bit for bit.
+The forwards differentiated are FD2Dtmem::run (ForwardSolver2Dtmem.cpp:
+108-174) and FD2Demem::run (ForwardSolver2Demem.cpp:112-185); the reference
+has no adjoint.
 
 Gate: relative L2 <= 1e-4 per parameter (FP32 CUDA adjoint vs FP64)."""
 import ctypes
@@ -12,7 +14,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from test_oracle_adjoint import tm_case
+from test_oracle_adjoint import te_case, tm_case
 
 pytestmark = pytest.mark.gpu
 GRAD_TOL = 1e-4
@@ -112,3 +114,76 @@ def test_tmz_adjoint_rejects_other_receiver_components(wave, refcpu):
         s.adjoint_gradient(np.zeros((2, s.nt), np.float32))
     assert e.value.code in (wave.WAVE_ERR_UNSUPPORTED, wave.WAVE_ERR_ARG)
     s.close()
+
+
+def _te_survey(wave, refcpu, boundary, stencil, reduce, order=4):
+    ocfg, model, acq = te_case(refcpu, boundary, stencil, reduce, order=order, NX=72, NY=60, nt=400)
+    cfg = _wave_cfg(wave, ocfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
+    blob = np.exp(-((xx - cfg.NX * 0.5) ** 2 + (yy - cfg.NY * 0.45) ** 2) / 60.0).reshape(-1)
+    true = dict(m32)
+    true["eps_r"] = (m32["eps_r"] * (1 + 0.1 * blob)).astype(np.float32)
+    true["sigma"] = (m32["sigma"] * (1 + 0.5 * blob)).astype(np.float32)
+    true["mu_r"] = (m32["mu_r"] * (1 + 0.05 * blob)).astype(np.float32)
+    acq32 = (acq[0], acq[1], acq[2].astype(np.float32), acq[3], acq[4])
+    s = wave.Factory.Create("2D", "emem").initForwardSolver(cfg)
+    s.prepareForModelling(true)
+    s.setSources(*acq32[:3])
+    s.setReceivers(*acq32[3:])
+    s.run(0, s.nt)
+    # scaled as in the TMz survey: the residual holds part of the direct wave
+    dobs = (0.6 * s.seismograms()).astype(np.float32)
+    s.close()
+    return ocfg, cfg, m32, acq32, dobs
+
+
+@pytest.mark.parametrize("boundary,stencil,reduce,order", [(2, 0, 0, 4), (0, 1, 0, 2), (1, 0, 0, 6), (2, 0, 1, 8)])
+def test_tez_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, stencil, reduce, order):
+    """Ey and Hz sources (the Hz source exercises the re-formed pre-taper hz),
+    Ex, Ey and Hz receivers."""
+    ocfg, cfg, m32, acq, dobs = _te_survey(wave, refcpu, boundary, stencil, reduce, order)
+    s = wave.Factory.Create("2D", "emem").initForwardSolver(cfg)
+    s.prepareForModelling(m32)
+    s.setSources(*acq[:3])
+    s.setReceivers(*acq[3:])
+    J, ge, gs, gm = s.adjoint_gradient(dobs, checkpoint_every=45)
+    s.close()
+    o = refcpu.Oracle(ocfg, {k: v.astype(np.float64) for k, v in m32.items()}, acq[0], acq[1], acq[2].astype(np.float64),
+                      acq[3], acq[4], dtype=np.float64)
+    J64, re, rs, rm = o.adjoint_gradient(dobs.astype(np.float64), checkpoint_every=45)
+    o.close()
+    errs = [_rel(a, b) for a, b in ((ge, re), (gs, rs), (gm, rm))]
+    print(f"TEz adjoint boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} vs FP64 "
+          f"{J64:.6e}; gradient rel L2 eps_r {errs[0]:.2e} sigma {errs[1]:.2e} mu_r {errs[2]:.2e}")
+    assert J > 0 and abs(J - J64) <= 1e-4 * J64
+    assert max(errs) <= GRAD_TOL
+
+
+def test_tez_batched_adjoint_equals_single_shots(wave, refcpu):
+    ocfg, cfg, m32, acq, dobs0 = _te_survey(wave, refcpu, 1, 0, 0)
+    acqs, dobs, single = [], [], []
+    for k in range(2):
+        a = (acq[0] + 7 * k, acq[1], acq[2], acq[3], acq[4])
+        acqs.append(a)
+        s = wave.Factory.Create("2D", "emem").initForwardSolver(cfg)
+        s.prepareForModelling(m32)
+        s.setSources(*a[:3])
+        s.setReceivers(*a[3:])
+        s.run(0, s.nt)
+        dobs.append(0.8 * s.seismograms())
+        single.append(s.adjoint_gradient(dobs[-1], checkpoint_every=30))
+        s.close()
+    b = wave.Batch([cfg] * 2)
+    try:
+        for shot, a in zip(b.shots, acqs):
+            shot.prepareForModelling(m32)
+            shot.setSources(*a[:3])
+            shot.setReceivers(*a[3:])
+        mis, g1, g2, g3 = b.adjoint_gradient(dobs, checkpoint_every=30, sum_shots=False)
+    finally:
+        b.close()
+    for k in range(2):
+        assert abs(mis[k] - single[k][0]) <= 1e-12 * abs(single[k][0])
+        for got, want in zip((g1[k], g2[k], g3[k]), single[k][1:]):
+            assert np.abs(want).max() > 0 and np.array_equal(got, want)

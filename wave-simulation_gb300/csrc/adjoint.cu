@@ -40,6 +40,14 @@
 // dJ/dirho to vs and rho (mu = max(rho vs^2, 1), its harmonic 2-point averages
 // along x and y, SH.cpp:424-431; irho = 1 / rho).
 //
+// The lossless 2-D TEz step (FD2Demem::run, ForwardSolver2Demem.cpp:112-185):
+//   hz' = hz - iMxy ((Dxf ey + P_eyx)' - (Dyf ex + P_exy)')
+//   ex' = CaX ex + CbX (Dyb hz' + P_hzy)',  ey' = CaY ey - CbY (Dxb hz' + P_hzx)',
+// then the ABS taper on all three, and a last kernel maps dJ/dCaX, dJ/dCbX,
+// dJ/dCaY, dJ/dCbY, dJ/diMxy to eps_r, sigma and mu_r (Ca, Cb of the 2-point
+// averages of eps and sigma along x and y, EMEM.cpp:378-392; iMxy the inverse
+// 4-point average of mu).
+//
 // Checkpointing: the forward run saves the state every K steps; the backward
 // sweep recomputes each K-step segment into a buffer of K+1 states and walks
 // it backwards. The reference has no adjoint (its inversion lives in a
@@ -78,6 +86,7 @@ struct AdjShot {
     int nrec, nt;
     int tm;                      // 1: lossless 2-D TMz (parts: hx, hy, ez; psi ezy, ezx, hyx, hxy)
     int sh;                      // 1: 2-D SH (parts: vz, sxz, syz; psi sxz_x, syz_y, vzx, vzy)
+    int te;                      // 1: lossless 2-D TEz (parts: hz, ex, ey; psi eyx, exy, hzy, hzx)
     float* vprime[2];            // vx', vy' (TMz: hx', hy') of the current step (null: the saved state's are they)
     const long long* sidx;       // sources (velocity sources are taken out of v')
     const int* stype;
@@ -404,6 +413,80 @@ __device__ __forceinline__ void adj_sh_v_body(const StepParams& P, const AdjShot
 }
 
 
+// ---- lossless 2-D TEz -------------------------------------------------------
+// parts of a TEz state in the view: AV_VX = hz, AV_SXX = ex, AV_SYY = ey,
+// AV_P1, AV_P2 = psi of eyx, exy, AV_Q1, AV_Q2 = psi of hzy, hzx; lf[0], lf[2],
+// lf[3] = adjoints of hz, ex, ey; T[0..1] = adjoints of the E-update
+// derivatives c1, c2, T[2..3] of the H-update ones a1, a2; g[0..4] = dJ/dCaX,
+// dJ/dCbX, dJ/dCaY, dJ/dCbY, dJ/diMxy
+
+// E-update transpose at step n
+template <int H>
+__device__ __forceinline__ void adj_te_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float* hz1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
+    const Slabs S = slabs_of(P, p);
+    float c1 = deriv<H, false>(hz1, i, sy, p.y, P.Dyb);
+    float c2 = deriv<H, false>(hz1, i, 1, p.x, P.Dxb);
+    if (S.sy >= 0) c1 += X1[A.off[AV_Q1] + S.py];
+    if (S.sx >= 0) c2 += X1[A.off[AV_Q2] + S.px];
+    float lex = A.lf[2][i], ley = A.lf[3][i];
+    if (pending) {
+        // the transposed H-update derivatives of ey and ex from the step after this one
+        ley += derivT<H, true>(A.T[2], i, 1, p.x, P.Dxf);
+        lex += derivT<H, true>(A.T[3], i, sy, p.y, P.Dyf);
+    }
+    if (P.abs) {
+        // the taper multiplied ey, ex and hz last: their adjoints first
+        const float d = absDamp(P, p);
+        lex *= d;
+        ley *= d;
+        A.lf[0][i] *= d;
+    }
+    const float cax = __ldg(P.m[M_CAX] + i), cbx = __ldg(P.m[M_CBX] + i);
+    const float cay = __ldg(P.m[M_CAY] + i), cby = __ldg(P.m[M_CBY] + i);
+    A.g[0][i] += lex * X0[A.off[AV_SXX] + i];
+    A.g[1][i] += lex * c1;
+    A.g[2][i] += ley * X0[A.off[AV_SYY] + i];
+    A.g[3][i] -= ley * c2;
+    float l1 = cbx * lex, l2 = -cby * ley;
+    A.lf[2][i] = cax * lex;
+    A.lf[3][i] = cay * ley;
+    if (S.sy >= 0) cpml_adj(l1, A.lpsi[4] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // hzy: y, full profile
+    if (S.sx >= 0) cpml_adj(l2, A.lpsi[5] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // hzx: x, full profile
+    A.T[0][i] = l1;
+    A.T[1][i] = l2;
+}
+
+// H-update transpose at step n (after the E transpose of every point)
+template <int H>
+__device__ __forceinline__ void adj_te_h_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    float lhz = A.lf[0][i];
+    lhz += derivT<H, false>(A.T[0], i, sy, p.y, P.Dyb);
+    lhz += derivT<H, false>(A.T[1], i, 1, p.x, P.Dxb);
+    const Slabs S = slabs_of(P, p);
+    float a1 = deriv<H, true>(X0 + A.off[AV_SYY], i, 1, p.x, P.Dxf);
+    float a2 = deriv<H, true>(X0 + A.off[AV_SXX], i, sy, p.y, P.Dyf);
+    if (S.sx >= 0) a1 += X1[A.off[AV_P1] + S.px];
+    if (S.sy >= 0) a2 += X1[A.off[AV_P2] + S.py];
+    const float im = __ldg(P.m[M_IMUXY] + i);
+    float l1 = -im * lhz, l2 = im * lhz;
+    A.g[4][i] -= lhz * (a1 - a2);
+    if (S.sx >= 0) cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // eyx: x, half profile
+    if (S.sy >= 0) cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // exy: y, half profile
+    A.T[2][i] = l1;
+    A.T[3][i] = l2;
+    A.lf[0][i] = lhz;
+}
+
+
 template <int H, int PASS>
 __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
                                                 const BatchTile* __restrict__ W, BatchSched S, int vn, int pending)
@@ -416,7 +499,9 @@ __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ P
         else if (PASS == 3) adj_tm_e_body<H>(P, A, p, vn, pending != 0);
         else if (PASS == 4) adj_tm_h_body<H>(P, A, p, vn);
         else if (PASS == 5) adj_sh_s_body<H>(P, A, p, vn, pending != 0);
-        else adj_sh_v_body<H>(P, A, p, vn);
+        else if (PASS == 6) adj_sh_v_body<H>(P, A, p, vn);
+        else if (PASS == 7) adj_te_e_body<H>(P, A, p, vn, pending != 0);
+        else adj_te_h_body<H>(P, A, p, vn);
     });
 }
 
@@ -432,7 +517,7 @@ __global__ void adj_vprime(const StepParams* __restrict__ Ps, const AdjShot* __r
         const float* X1 = A.view + (long long)(vn + 1) * A.stride;
         const float d = P.abs ? absDamp(P, p) : 1.0f;
         A.vprime[0][p.i] = X1[A.off[AV_VX] + p.i] / d;
-        if (!A.sh) A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
+        if (!A.sh && !A.te) A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
     });
 }
 
@@ -443,7 +528,7 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
     if (!A.vprime[0]) return;
     for (int k = threadIdx.x; k < A.nsrc; k += blockDim.x) {
         const int t = A.stype[k];
-        if (A.sh ? t != WAVE_TYPE_VZ : (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY)) continue;
+        if (A.te ? t != WAVE_TYPE_HZ : A.sh ? t != WAVE_TYPE_VZ : (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY)) continue;
         const long long i = A.sidx[k];
         Pt p;
         p.i = i;
@@ -451,7 +536,7 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
         p.y = static_cast<int>(i / P.NX);
         p.z = 0;
         const float d = P.abs ? absDamp(P, p) : 1.0f;
-        atomicAdd(A.vprime[(A.sh || t == WAVE_TYPE_VX) ? 0 : 1] + i, -A.signals[(long long)k * A.nt + n] / d);
+        atomicAdd(A.vprime[(A.sh || A.te || t == WAVE_TYPE_VX) ? 0 : 1] + i, -A.signals[(long long)k * A.nt + n] / d);
     }
 }
 
@@ -469,6 +554,11 @@ __global__ void adj_inject(const AdjShot* __restrict__ As, int n)
         }
         if (A.sh) {   // vz receivers
             atomicAdd(A.lf[0] + i, v);
+            continue;
+        }
+        if (A.te) {   // Ex, Ey and Hz receivers
+            const int t = A.rtype[r];
+            atomicAdd(A.lf[t == WAVE_TYPE_EX ? 2 : t == WAVE_TYPE_EY ? 3 : 0] + i, v);
             continue;
         }
         switch (A.rtype[r]) {
@@ -632,6 +722,77 @@ __global__ void adj_sh_final(PrepParams G, const StepParams P, const AdjShot A, 
     }
 }
 
+// d Ca / d eps, d Ca / d sigma, d Cb / d eps, d Cb / d sigma of
+// Ca = (1 - k) / (1 + k), Cb = (1 / eps) / (1 + k), k = sigma DT / (2 eps),
+// applied to the adjoints of Ca and Cb
+__device__ __forceinline__ void cacb_adj(float e, float sg, float DT, float gca, float gcb, float& ge, float& gs)
+{
+    const float kk = sg * DT / (2.0f * e), q = 1.0f + kk;
+    const float dca_de = 2.0f * kk / (e * q * q), dca_ds = -2.0f / (q * q) * (DT / (2.0f * e));
+    const float dcb_de = (-1.0f / (e * q) + kk / (e * q * q)) / e, dcb_ds = -(1.0f / e) / (q * q) * (DT / (2.0f * e));
+    ge = gca * dca_de + gcb * dcb_de;
+    gs = gca * dca_ds + gcb * dcb_ds;
+}
+
+// chain rule for TEz: CaX, CbX of the 2-point x averages of eps = eps_r eps0
+// and sigma (CaY, CbY along y); iMxy = 1 / (4-point average of mu = mu_r mu0)
+// (0 where invalid)
+__global__ void adj_te_final(PrepParams G, const StepParams P, const AdjShot A, float DT, float* geps, float* gsig, float* gmu,
+                             int accumulate)
+{
+    const float eps0 = 8.8541878176e-12f, mu0 = 1.2566370614e-6f;
+    const float* er = P.m[M_EPSR];
+    const float* sg = P.m[M_SIG];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
+        const int kx = static_cast<int>(k % G.NX), ky = static_cast<int>(k / G.NX);
+        float ge = 0.0f, gs = 0.0f;
+        // rows (kx, ky) and (kx-1, ky) of the x averages, (kx, ky) and (kx, ky-1) of the y averages
+        for (int d = 0; d <= 1; ++d) {
+            if (kx - d >= 0) {
+                const long long r = k - d;
+                const bool pair = kx - d + 1 < G.NX;
+                if (d == 0 || pair) {
+                    const float w = pair ? 0.5f : 1.0f;
+                    const float e = pair ? 0.5f * (er[r] * eps0) + 0.5f * (er[r + 1] * eps0) : er[r] * eps0;
+                    const float s = pair ? 0.5f * sg[r] + 0.5f * sg[r + 1] : sg[r];
+                    float a, b;
+                    cacb_adj(e, s, DT, A.g[0][r], A.g[1][r], a, b);
+                    ge += w * a;
+                    gs += w * b;
+                }
+            }
+            if (ky - d >= 0) {
+                const long long r = k - d * (long long)G.NX;
+                const bool pair = ky - d + 1 < G.NY;
+                if (d == 0 || pair) {
+                    const float w = pair ? 0.5f : 1.0f;
+                    const float e = pair ? 0.5f * (er[r] * eps0) + 0.5f * (er[r + G.NX] * eps0) : er[r] * eps0;
+                    const float s = pair ? 0.5f * sg[r] + 0.5f * sg[r + G.NX] : sg[r];
+                    float a, b;
+                    cacb_adj(e, s, DT, A.g[2][r], A.g[3][r], a, b);
+                    ge += w * a;
+                    gs += w * b;
+                }
+            }
+        }
+        float gm = 0.0f;
+        for (int dy = 0; dy <= 1; ++dy)
+            for (int dx = 0; dx <= 1; ++dx) {
+                const int x = kx - dx, y = ky - dy;
+                if (x < 0 || y < 0) continue;
+                const long long r = x + (long long)G.NX * y;
+                const float im = P.m[M_IMUXY][r];
+                if (im == 0.0f) continue;
+                const float w = w4(x, y, kx, ky, G.NX, G.NY);
+                if (w != 0.0f) gm -= A.g[4][r] * im * im * w;
+            }
+        ge *= eps0;
+        gm *= mu0;
+        if (accumulate) { geps[k] += ge; gsig[k] += gs; gmu[k] += gm; }
+        else { geps[k] = ge; gsig[k] = gs; gmu[k] = gm; }
+    }
+}
+
 template <int H>
 void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
                   int pending, cudaStream_t s)
@@ -643,7 +804,9 @@ void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const Batch
     case 3: adj_pass<H, 3><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
     case 4: adj_pass<H, 4><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
     case 5: adj_pass<H, 5><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    default: adj_pass<H, 6><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 6: adj_pass<H, 6><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 7: adj_pass<H, 7><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    default: adj_pass<H, 8><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
     }
 }
 
@@ -690,8 +853,9 @@ struct DevPool {
 std::string adjoint_supported(const wave_handle* h)
 {
     const wave_config& c = h->cfg;
-    if (c.dimension != 2 || (c.equation != WAVE_EQ_ELASTIC && c.equation != WAVE_EQ_TMEM && c.equation != WAVE_EQ_SH))
-        return "the adjoint gradient is implemented for 2-D elastic, 2-D SH and lossless 2-D TMz modelling";
+    if (c.dimension != 2 ||
+        (c.equation != WAVE_EQ_ELASTIC && c.equation != WAVE_EQ_TMEM && c.equation != WAVE_EQ_SH && c.equation != WAVE_EQ_EMEM))
+        return "the adjoint gradient is implemented for 2-D elastic, 2-D SH and lossless 2-D TMz and TEz modelling";
     if (c.equation == WAVE_EQ_TMEM) {
         for (int t : h->hRecType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez receivers only";
@@ -737,10 +901,14 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int elasticFields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
         const int tmFields[5] = {F_HX, F_HY, F_EZ, -1, -1};
         const int tmPsi[8] = {PS_EZY, PS_EZX, PS_HYX, PS_HXY, -1, -1, -1, -1};
+        // TEz: hz, -, ex, ey and the psi of eyx, exy, -, -, hzy, hzx
+        const bool te = h->cfg.equation == WAVE_EQ_EMEM;
         const int shFields[5] = {F_VZ, -1, F_SXZ, F_SYZ, -1};
         const int shPsi[8] = {PS_SXZ_X, PS_SYZ_Y, -1, -1, PS_VZX, PS_VZY, -1, -1};
-        const int* fields = tm ? tmFields : sh ? shFields : elasticFields;
-        const int* psiSlot = tm ? tmPsi : sh ? shPsi : kAdjPsiSlot;
+        const int teFields[5] = {F_HZ, -1, F_EX, F_EY, -1};
+        const int tePsi[8] = {PS_EYX, PS_EXY, -1, -1, PS_HZY, PS_HZX, -1, -1};
+        const int* fields = tm ? tmFields : sh ? shFields : te ? teFields : elasticFields;
+        const int* psiSlot = tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
         for (int k = 0; k < 5; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
         for (int k = 0; k < 8; ++k) {
             const int slot = psiSlot[k];
@@ -752,6 +920,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         AdjShot& a = A[s];
         a.tm = tm ? 1 : 0;
         a.sh = sh ? 1 : 0;
+        a.te = te ? 1 : 0;
         a.view = pool.get<float>(static_cast<size_t>(o) * (K + 1));
         a.stride = o;
         for (int k = 0; k < AV_COUNT; ++k) a.off[k] = off[k];
@@ -771,7 +940,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         float* res = pool.get<float>(static_cast<size_t>(h->nrec) * NT);
         a.res = res;
         bool velocitySources = false;
-        for (int t : h->hSrcType) velocitySources |= sh ? t == WAVE_TYPE_VZ : (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
+        for (int t : h->hSrcType)
+            velocitySources |= te ? t == WAVE_TYPE_HZ : sh ? t == WAVE_TYPE_VZ : (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
         a.vprime[0] = a.vprime[1] = nullptr;
         if (h->cfg.DampingBoundary == 1 || velocitySources) {
             a.vprime[0] = pool.get<float>(2 * N);
@@ -854,7 +1024,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             // two kernels per step: the third stage of step n (the transposed
             // derivatives of the first-pass inputs) runs inside the first kernel
             // of step n - 1; after step 0 it is not needed
-            const int first = A[0].tm ? 3 : A[0].sh ? 5 : 0;
+            const int first = A[0].tm ? 3 : A[0].sh ? 5 : A[0].te ? 7 : 0;
             const int pending = n < NT - 1 ? 1 : 0;
             launch_adj(H, first, dP, dA, dT, sched, grid, n - n0, pending, st);
             launch_adj(H, first + 1, dP, dA, dT, sched, grid, n - n0, pending, st);
@@ -871,6 +1041,9 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
                                                sum && s > 0 ? 1 : 0);
         else if (A[s].sh)
             adj_sh_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
+        else if (A[s].te)
+            adj_te_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
+                                               sum && s > 0 ? 1 : 0);
         else
             adj_grad_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
     }

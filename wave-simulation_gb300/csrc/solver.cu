@@ -919,12 +919,6 @@ int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, co
             k_inv_avg2(G, mu, 0, mat(M_IMUXZ), s);
             k_inv_avg2(G, mu, 1, mat(M_IMUYZ), s);
             coeffs(eps, dSig, dTe, dTs, M_CAZ, M_CBZ, M_CDZ0);
-            if (eq == WAVE_EQ_TMEM) {
-                // the base parameters, for the adjoint's chain rule (adjoint.cu)
-                h->check(cudaMemcpyAsync(mat(M_EPSR), dEr, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
-                h->check(cudaMemcpyAsync(mat(M_SIG), dSig, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
-                h->check(cudaMemcpyAsync(mat(M_MUR), dMr, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
-            }
         } else {
             // EMEM/ViscoEMEM::calculateAveraging (EMEM.cpp:378-392, ViscoEMEM.cpp:409-432),
             // prepareForModelling of FD2Demem/FD2Dviscoemem/FD3Demem/FD3Dviscoemem
@@ -949,6 +943,12 @@ int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, co
                 }
                 coeffs(ea, sa, ta, tsa, caS[a], cbS[a], cdS[a]);
             }
+        }
+        if ((eq == WAVE_EQ_TMEM || eq == WAVE_EQ_EMEM) && !is3d) {
+            // the base parameters, for the adjoint's chain rule (adjoint.cu)
+            h->check(cudaMemcpyAsync(mat(M_EPSR), dEr, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+            h->check(cudaMemcpyAsync(mat(M_SIG), dSig, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+            h->check(cudaMemcpyAsync(mat(M_MUR), dMr, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         }
         h->check(cudaGetLastError(), "model preparation");
         for (float* p : tmp) cudaFreeAsync(p, s);
