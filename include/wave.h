@@ -378,8 +378,9 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
 /* ---- adjoint gradient (new; the reference's inversion is a separate project) ----
  * Gradient of J = 1/2 sum over receivers and steps of (d - d_obs)^2 by the
  * discrete adjoint of the time step:
- *  - 2-D elastic (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297) with
- *    CPML, ABS or no damping boundary and with or without the free surface:
+ *  - 2-D and 3-D elastic (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297;
+ *    FD3Delastic::run, ForwardSolver3Delastic.cpp:120-414) with CPML, ABS or
+ *    no damping boundary and with or without the free surface (FreeSurface 1):
  *    grad_vp, grad_vs, grad_rho receive dJ/dvp, dJ/dvs, dJ/drho;
  *  - 2-D SH (FD2Dsh::run, ForwardSolver2Dsh.cpp:108-196) with CPML, ABS or
  *    no damping boundary and with or without the free surface: grad_vs and
@@ -396,7 +397,7 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  * receivers; seismograms are left as computed), saving the state every
  * `checkpoint_every` steps, then the backward sweep, recomputing each
  * checkpoint segment. d_obs: n_receivers x NT (dobs_mem host or device);
- * grad_*: NX*NY floats each (grad_mem). *misfit receives J. */
+ * grad_*: N floats each (grad_mem). *misfit receives J. */
 int wave_adjoint_gradient(wave_handle* h, const float* dobs, int dobs_mem, int checkpoint_every, double* misfit,
                           float* grad_vp, float* grad_vs, float* grad_rho, int grad_mem);
 

@@ -70,29 +70,32 @@ struct AverageTranspose {
     const idx_t N;
     explicit AverageTranspose(const Sim<T>& sim) : s(sim), N(sim.g.N()) {}
     // A^T y for the averaging operator `avg` (out = avg(in)), whose row r reads
-    // at most the 2 x 2 block at r (x, x+1) x (y, y+1): probed with one unit
-    // pattern per (x mod 2, y mod 2) colour, so the edge fallbacks come from
-    // the oracle's own averaging code.
+    // at most the 2 x 2 x 2 block at r (x, x+1) x (y, y+1) x (z, z+1): probed
+    // with one unit pattern per (x mod 2, y mod 2, z mod 2) colour, so the edge
+    // fallbacks come from the oracle's own averaging code.
     template <class Avg>
     void avgT(Avg avg, const std::vector<T>& y, std::vector<T>& out) const
     {
         std::vector<T> e(N), col(N);
+        const int ncz = s.g.NZ > 1 ? 2 : 1;
         for (int cx = 0; cx < 2; ++cx)
-            for (int cy = 0; cy < 2; ++cy) {
-                for (idx_t k = 0; k < N; ++k) {
-                    idx_t x, yy, z;
-                    s.g.coord(k, x, yy, z);
-                    e[k] = (x % 2 == cx && yy % 2 == cy) ? T(1) : T(0);
+            for (int cy = 0; cy < 2; ++cy)
+                for (int cz = 0; cz < ncz; ++cz) {
+                    for (idx_t k = 0; k < N; ++k) {
+                        idx_t x, yy, z;
+                        s.g.coord(k, x, yy, z);
+                        e[k] = (x % 2 == cx && yy % 2 == cy && z % 2 == cz) ? T(1) : T(0);
+                    }
+                    avg(e.data(), col.data());   // col[r] = A[r, k_c(r)]
+                    for (idx_t r = 0; r < N; ++r) {
+                        if (col[r] == T(0)) continue;
+                        idx_t x, yy, z;
+                        s.g.coord(r, x, yy, z);
+                        const idx_t kx = (x % 2 == cx) ? x : x + 1, ky = (yy % 2 == cy) ? yy : yy + 1;
+                        const idx_t kz = (z % 2 == cz) ? z : z + 1;
+                        out[s.g.index(kx, ky, kz)] += col[r] * y[r];
+                    }
                 }
-                avg(e.data(), col.data());   // col[r] = A[r, k_c(r)]
-                for (idx_t r = 0; r < N; ++r) {
-                    if (col[r] == T(0)) continue;
-                    idx_t x, yy, z;
-                    s.g.coord(r, x, yy, z);
-                    const idx_t kx = (x % 2 == cx) ? x : x + 1, ky = (yy % 2 == cy) ? yy : yy + 1;
-                    out[s.g.index(kx, ky, 0)] += col[r] * y[r];
-                }
-            }
     }
 
 };
@@ -804,9 +807,281 @@ struct TEAdjoint2D {
     }
 };
 
+// Discrete adjoint of the oracle's 3-D elastic step (Sim<T>::stepElastic,
+// restating FD3Delastic::run, ForwardSolver3Delastic.cpp:120-414, with CPML
+// CPML3D.cpp:31-371, the free surface FreeSurface3Delastic.cpp:15-47 and the
+// ABS taper ABS3D.cpp:14-60): the gradient of J = 1/2 sum (d - d_obs)^2 with
+// respect to vp, vs and rho. Per step, from X_t and X_{t+1}:
+//   a0' = Dxf sxx  a1' = DybS sxy  a2' = Dzb sxz  -> vx' = vx + irx (a0' + a1' + a2')
+//   a3' = Dxb sxy  a4' = DyfS syy  a5' = Dzb syz  -> vy' = vy + iry (a3' + a4' + a5')
+//   a6' = Dxb sxz  a7' = DybS syz  a8' = Dzf szz  -> vz' = vz + irz (a6' + a7' + a8')
+//   c0' = Dxb vx'  c1' = Dyb vy'  c2' = Dzb vz'    (normal stresses with M and 2 mu)
+//   c3' = Dyf vx'  c4' = Dxf vy' (sxy, muXY)  c5' = Dzf vx'  c6' = Dxf vz' (sxz, muXZ)
+//   c7' = Dzf vy'  c8' = Dyf vz' (syz, muYZ)
+// each with its psi of X_{t+1}; then at y = 0 with the free surface syy' = 0,
+// sxx' and szz' += sh (c0' + c2') - sv c1' (sv = M - 2 mu, sh = -sv^2 / M), then
+// the taper on all nine fields.
+template <class T>
+struct ElasticAdjoint3D {
+    Sim<T>& s;
+    const idx_t N;
+    CSR<T> DxfT, DxbT, DyfT, DybT, DzfT, DzbT, DyfST, DybST;
+    static constexpr const char* kP[9] = {"sxx_x", "sxy_y", "sxz_z", "sxy_x", "syy_y", "syz_z", "sxz_x", "syz_y", "szz_z"};
+    static constexpr const char* kQ[9] = {"vxx", "vyy", "vzz", "vxy", "vyx", "vxz", "vzx", "vyz", "vzy"};
+
+    explicit ElasticAdjoint3D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    {
+        if (!s.is3d || s.eq != WAVE_EQ_ELASTIC) throw std::invalid_argument("oracle adjoint: 3-D elastic only");
+        DxfT = transpose(s.Dxf);
+        DxbT = transpose(s.Dxb);
+        DyfT = transpose(s.Dyf);
+        DybT = transpose(s.Dyb);
+        DzfT = transpose(s.Dzf);
+        DzbT = transpose(s.Dzb);
+        DyfST = transpose(s.fs ? s.DyfFS : s.Dyf);
+        DybST = transpose(s.fs ? s.DybFS : s.Dyb);
+    }
+    struct State {
+        std::map<std::string, std::vector<T>> F, psi;
+    };
+    const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
+    {
+        auto it = x.psi.find(n);
+        return it == x.psi.end() ? zero : it->second;
+    }
+    // (a, b) profile of a psi array: forward derivatives on the half grid
+    std::pair<const std::vector<T>*, const std::vector<T>*> prof(const std::string& n) const
+    {
+        if (n == "sxx_x" || n == "vyx" || n == "vzx") return {&s.axh, &s.bxh};
+        if (n == "sxy_x" || n == "sxz_x" || n == "vxx") return {&s.ax, &s.bx};
+        if (n == "syy_y" || n == "vxy" || n == "vzy") return {&s.ayh, &s.byh};
+        if (n == "sxy_y" || n == "syz_y" || n == "vyy") return {&s.ay, &s.by};
+        if (n == "szz_z" || n == "vxz" || n == "vyz") return {&s.azh, &s.bzh};
+        return {&s.az, &s.bz};   // sxz_z, syz_z, vzz
+    }
+    void cpmlT(std::vector<T>& lc, std::vector<T>& lp, const char* n) const
+    {
+        if (!s.useCpml) return;
+        auto ab = prof(n);
+        const std::vector<T>& a = *ab.first;
+        const std::vector<T>& b = *ab.second;
+        for_n(N, [&](idx_t i) {
+            const T c = (T(1) + a[i]) * lc[i] + a[i] * lp[i];
+            lp[i] = b[i] * (lc[i] + lp[i]);
+            lc[i] = c;
+        });
+    }
+
+    double run(const std::vector<T>& vp, const std::vector<T>& vs, const std::vector<T>& rho, const T* dobs, int K,
+               T* gvp, T* gvs, T* grho)
+    {
+        const int NT = s.NT;
+        const size_t nrec = s.rec.idx.size();
+        const std::vector<T> zero(N, T(0));
+        s.reset();
+        std::vector<State> ck;
+        for (int t = 0; t < NT; ++t) {
+            if (t % K == 0) ck.push_back({s.F, s.psi});
+            s.step(t);
+        }
+        std::vector<T> res(nrec * static_cast<size_t>(NT));
+        double J = 0;
+        for (size_t k = 0; k < res.size(); ++k) {
+            res[k] = s.seis[k] - dobs[k];
+            J += 0.5 * static_cast<double>(res[k]) * static_cast<double>(res[k]);
+        }
+        std::map<std::string, std::vector<T>> lF, lpsi;
+        for (const char* n : {"vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz"}) lF[n].assign(N, 0);
+        for (int k = 0; k < 9; ++k) { lpsi[kP[k]].assign(N, 0); lpsi[kQ[k]].assign(N, 0); }
+        std::vector<T> gM(N, 0), gMu(N, 0), gMuXY(N, 0), gMuXZ(N, 0), gMuYZ(N, 0), gIrx(N, 0), gIry(N, 0), gIrz(N, 0);
+        std::vector<T> a[9], c[9], la[9], lc[9], vxp(N), vyp(N), vzp(N);
+        for (int k = 0; k < 9; ++k) { a[k].assign(N, 0); c[k].assign(N, 0); la[k].assign(N, 0); lc[k].assign(N, 0); }
+        const CSR<T>& DybS = s.fs ? s.DybFS : s.Dyb;
+        const CSR<T>& DyfS = s.fs ? s.DyfFS : s.Dyf;
+        const int nseg = static_cast<int>(ck.size());
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int t0 = seg * K, t1 = std::min(NT, t0 + K);
+            std::vector<State> X;
+            s.F = ck[seg].F;
+            s.psi = ck[seg].psi;
+            X.push_back({s.F, s.psi});
+            for (int t = t0; t < t1; ++t) {
+                s.step(t);
+                X.push_back({s.F, s.psi});
+            }
+            for (int t = t1 - 1; t >= t0; --t) {
+                const State& X0 = X[t - t0];
+                const State& X1 = X[t - t0 + 1];
+                auto f0 = [&](const char* n) { return X0.F.at(n).data(); };
+                s.Dxf.spmv(f0("sxx"), a[0].data());
+                DybS.spmv(f0("sxy"), a[1].data());
+                s.Dzb.spmv(f0("sxz"), a[2].data());
+                s.Dxb.spmv(f0("sxy"), a[3].data());
+                DyfS.spmv(f0("syy"), a[4].data());
+                s.Dzb.spmv(f0("syz"), a[5].data());
+                s.Dxb.spmv(f0("sxz"), a[6].data());
+                DybS.spmv(f0("syz"), a[7].data());
+                s.Dzf.spmv(f0("szz"), a[8].data());
+                for (int k = 0; k < 9; ++k) {
+                    const std::vector<T>& p = psiOf(X1, kP[k], zero);
+                    for_n(N, [&](idx_t i) { a[k][i] += p[i]; });
+                }
+                const auto& vx0 = X0.F.at("vx");
+                const auto& vy0 = X0.F.at("vy");
+                const auto& vz0 = X0.F.at("vz");
+                for_n(N, [&](idx_t i) {
+                    vxp[i] = vx0[i] + s.invRhoX[i] * (a[0][i] + a[1][i] + a[2][i]);
+                    vyp[i] = vy0[i] + s.invRhoY[i] * (a[3][i] + a[4][i] + a[5][i]);
+                    vzp[i] = vz0[i] + s.invRhoZ[i] * (a[6][i] + a[7][i] + a[8][i]);
+                });
+                s.Dxb.spmv(vxp.data(), c[0].data());
+                s.Dyb.spmv(vyp.data(), c[1].data());
+                s.Dzb.spmv(vzp.data(), c[2].data());
+                s.Dyf.spmv(vxp.data(), c[3].data());
+                s.Dxf.spmv(vyp.data(), c[4].data());
+                s.Dzf.spmv(vxp.data(), c[5].data());
+                s.Dxf.spmv(vzp.data(), c[6].data());
+                s.Dzf.spmv(vyp.data(), c[7].data());
+                s.Dyf.spmv(vzp.data(), c[8].data());
+                for (int k = 0; k < 9; ++k) {
+                    const std::vector<T>& q = psiOf(X1, kQ[k], zero);
+                    for_n(N, [&](idx_t i) { c[k][i] += q[i]; });
+                }
+                // receivers read X_{t+1}: a pressure trace is (sxx + syy + szz) / 3
+                for (size_t r = 0; r < nrec; ++r) {
+                    const idx_t i = s.rec.idx[r];
+                    const T v = res[r * NT + t];
+                    switch (s.rec.type[r]) {
+                    case WAVE_TYPE_P:
+                        lF["sxx"][i] += v / T(3);
+                        lF["syy"][i] += v / T(3);
+                        lF["szz"][i] += v / T(3);
+                        break;
+                    case WAVE_TYPE_VX: lF["vx"][i] += v; break;
+                    case WAVE_TYPE_VY: lF["vy"][i] += v; break;
+                    default: lF["vz"][i] += v; break;
+                    }
+                }
+                auto& lvx = lF["vx"];
+                auto& lvy = lF["vy"];
+                auto& lvz = lF["vz"];
+                auto& lxx = lF["sxx"];
+                auto& lyy = lF["syy"];
+                auto& lzz = lF["szz"];
+                auto& lxy = lF["sxy"];
+                auto& lxz = lF["sxz"];
+                auto& lyz = lF["syz"];
+                if (s.useAbs)
+                    for (auto* v : {&lxx, &lyy, &lzz, &lxy, &lxz, &lyz, &lvx, &lvy, &lvz}) {
+                        auto& w = *v;
+                        for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
+                    }
+                for (int k = 0; k < 9; ++k) std::fill(lc[k].begin(), lc[k].end(), T(0));
+                if (s.fs) {
+                    // syy *= fsZero; sxx, szz += scaleH (c0' + c2') - scaleV c1'
+                    for_n(N, [&](idx_t i) {
+                        lyy[i] *= s.fsZero[i];
+                        const T hs = lxx[i] + lzz[i];
+                        lc[0][i] += s.scaleH[i] * hs;
+                        lc[2][i] += s.scaleH[i] * hs;
+                        lc[1][i] -= s.scaleV[i] * hs;
+                        const T sel = s.fsSelect[i];
+                        if (sel != T(0)) {
+                            const T gH = hs * (c[0][i] + c[2][i]), gV = -hs * c[1][i];
+                            const T sv = s.M[i] - T(2) * s.mu[i];
+                            gM[i] += gV * sel - gH * sel * (T(2) * sv / s.M[i] - sv * sv / (s.M[i] * s.M[i]));
+                            gMu[i] += -T(2) * gV * sel + gH * sel * T(4) * sv / s.M[i];
+                        }
+                    });
+                }
+                for_n(N, [&](idx_t i) {
+                    const T ls = lxx[i] + lyy[i] + lzz[i];
+                    lc[0][i] += s.M[i] * ls - T(2) * s.mu[i] * (lyy[i] + lzz[i]);
+                    lc[1][i] += s.M[i] * ls - T(2) * s.mu[i] * (lxx[i] + lzz[i]);
+                    lc[2][i] += s.M[i] * ls - T(2) * s.mu[i] * (lxx[i] + lyy[i]);
+                    gM[i] += ls * (c[0][i] + c[1][i] + c[2][i]);
+                    gMu[i] += -T(2) * (lxx[i] * (c[1][i] + c[2][i]) + lyy[i] * (c[0][i] + c[2][i]) + lzz[i] * (c[0][i] + c[1][i]));
+                    lc[3][i] += s.muXY[i] * lxy[i];
+                    lc[4][i] += s.muXY[i] * lxy[i];
+                    gMuXY[i] += lxy[i] * (c[3][i] + c[4][i]);
+                    lc[5][i] += s.muXZ[i] * lxz[i];
+                    lc[6][i] += s.muXZ[i] * lxz[i];
+                    gMuXZ[i] += lxz[i] * (c[5][i] + c[6][i]);
+                    lc[7][i] += s.muYZ[i] * lyz[i];
+                    lc[8][i] += s.muYZ[i] * lyz[i];
+                    gMuYZ[i] += lyz[i] * (c[7][i] + c[8][i]);
+                });
+                for (int k = 0; k < 9; ++k) cpmlT(lc[k], lpsi[kQ[k]], kQ[k]);
+                spmv_add(DxbT, lc[0], lvx);
+                spmv_add(DyfT, lc[3], lvx);
+                spmv_add(DzfT, lc[5], lvx);
+                spmv_add(DybT, lc[1], lvy);
+                spmv_add(DxfT, lc[4], lvy);
+                spmv_add(DzfT, lc[7], lvy);
+                spmv_add(DzbT, lc[2], lvz);
+                spmv_add(DxfT, lc[6], lvz);
+                spmv_add(DyfT, lc[8], lvz);
+                for_n(N, [&](idx_t i) {
+                    la[0][i] = la[1][i] = la[2][i] = s.invRhoX[i] * lvx[i];
+                    la[3][i] = la[4][i] = la[5][i] = s.invRhoY[i] * lvy[i];
+                    la[6][i] = la[7][i] = la[8][i] = s.invRhoZ[i] * lvz[i];
+                    gIrx[i] += lvx[i] * (a[0][i] + a[1][i] + a[2][i]);
+                    gIry[i] += lvy[i] * (a[3][i] + a[4][i] + a[5][i]);
+                    gIrz[i] += lvz[i] * (a[6][i] + a[7][i] + a[8][i]);
+                });
+                for (int k = 0; k < 9; ++k) cpmlT(la[k], lpsi[kP[k]], kP[k]);
+                spmv_add(DxfT, la[0], lxx);
+                spmv_add(DybST, la[1], lxy);
+                spmv_add(DzbT, la[2], lxz);
+                spmv_add(DxbT, la[3], lxy);
+                spmv_add(DyfST, la[4], lyy);
+                spmv_add(DzbT, la[5], lyz);
+                spmv_add(DxbT, la[6], lxz);
+                spmv_add(DybST, la[7], lyz);
+                spmv_add(DzfT, la[8], lzz);
+            }
+        }
+        // the model preparation's transpose
+        AverageTranspose<T> probe(s);
+        std::vector<T> y(N), gmuc(gMu), t(N, 0);
+        const std::vector<T>* gPlane[3] = {&gMuXY, &gMuXZ, &gMuYZ};
+        const std::vector<T>* muPlane[3] = {&s.muXY, &s.muXZ, &s.muYZ};
+        for (int plane = 0; plane < 3; ++plane) {
+            const std::vector<T>& gp = *gPlane[plane];
+            const std::vector<T>& mp = *muPlane[plane];
+            for_n(N, [&](idx_t r) { y[r] = gp[r] * mp[r] * mp[r]; });
+            std::fill(t.begin(), t.end(), T(0));
+            probe.avgT([&](const T* in, T* out) { average4<T>(s.g, plane, in, out); }, y, t);
+            for_n(N, [&](idx_t k) { gmuc[k] += t[k] / (s.mu[k] * s.mu[k]); });
+        }
+        std::vector<T> grhoAvg(N, 0);
+        const std::vector<T>* gIr[3] = {&gIrx, &gIry, &gIrz};
+        const std::vector<T>* ir[3] = {&s.invRhoX, &s.invRhoY, &s.invRhoZ};
+        const Axis axes[3] = {Axis::X, Axis::Y, Axis::Z};
+        for (int a3 = 0; a3 < 3; ++a3) {
+            for_n(N, [&](idx_t r) { y[r] = -(*gIr[a3])[r] * (*ir[a3])[r] * (*ir[a3])[r]; });
+            probe.avgT([&](const T* in, T* out) { average2<T>(s.g, axes[a3], in, out); }, y, grhoAvg);
+        }
+        for (idx_t k = 0; k < N; ++k) {
+            T raw = rho[k];
+            raw *= vs[k];
+            raw *= vs[k];
+            const bool unclamped = raw >= T(1);
+            gvp[k] = gM[k] * T(2) * rho[k] * vp[k];
+            gvs[k] = unclamped ? gmuc[k] * T(2) * rho[k] * vs[k] : T(0);
+            grho[k] = gM[k] * vp[k] * vp[k] + (unclamped ? gmuc[k] * vs[k] * vs[k] : T(0)) + grhoAvg[k];
+        }
+        return J;
+    }
+};
+
 template <class T>
 constexpr const char* ElasticAdjoint2D<T>::kP[4];
 template <class T>
 constexpr const char* ElasticAdjoint2D<T>::kQ[4];
+template <class T>
+constexpr const char* ElasticAdjoint3D<T>::kP[9];
+template <class T>
+constexpr const char* ElasticAdjoint3D<T>::kQ[9];
 
 } // namespace refcpu

@@ -358,10 +358,10 @@ class Oracle:
 
     def adjoint_gradient(self, dobs: np.ndarray, checkpoint_every: int = 50):
         """Misfit 1/2 sum (d - dobs)^2 and its gradients with respect to vp, vs
-        and rho (2-D elastic; 2-D SH: the vp gradient is zero) or eps_r, sigma
+        and rho (2-D and 3-D elastic; 2-D SH: the vp gradient is zero) or eps_r, sigma
         and mu_r (lossless 2-D TMz and TEz), by the oracle's own discrete adjoint
         (adjoint_impl.hpp) in this oracle's value type."""
-        n = self.cfg.NX * self.cfg.NY
+        n = self.cfg.NX * self.cfg.NY * (self.cfg.NZ if self.cfg.dimension == 3 else 1)
         em = self.cfg.equation >= 5
         if self.cfg.equation == EQ["sh"]:
             m = [np.ascontiguousarray(self.model[k], dtype=np.float64) for k in ("vs", "rho")]

@@ -182,7 +182,7 @@ int refcpu_field(void* hv, const char* name, double* out)
 }
 
 // Gradient of J = 1/2 sum (d - dobs)^2 with respect to vp, vs, rho for a 2-D
-// elastic simulation (adjoint_impl.hpp), in the handle's value type; dobs is
+// or 3-D elastic simulation (adjoint_impl.hpp), in the handle's value type; dobs is
 // nrec x NT. The model arrays are the ones the handle was created with. The
 // handle's state is left at the end of the forward run. Returns the misfit
 // through *misfit; 0 on success.
@@ -194,8 +194,13 @@ int refcpu_adjoint_elastic2d(void* hv, const double* vp, const double* vs, const
         using T = typename std::decay_t<decltype(s->M)>::value_type;
         const size_t N = s->g.N(), nd = s->rec.idx.size() * static_cast<size_t>(s->NT);
         std::vector<T> P(vp, vp + N), S(vs, vs + N), R(rho, rho + N), D(dobs, dobs + nd), a(N), b(N), c(N);
-        refcpu::ElasticAdjoint2D<T> adj(*s);
-        *misfit = adj.run(P, S, R, D.data(), K, a.data(), b.data(), c.data());
+        if (s->is3d) {
+            refcpu::ElasticAdjoint3D<T> adj(*s);
+            *misfit = adj.run(P, S, R, D.data(), K, a.data(), b.data(), c.data());
+        } else {
+            refcpu::ElasticAdjoint2D<T> adj(*s);
+            *misfit = adj.run(P, S, R, D.data(), K, a.data(), b.data(), c.data());
+        }
         std::copy(a.begin(), a.end(), gvp);
         std::copy(b.begin(), b.end(), gvs);
         std::copy(c.begin(), c.end(), grho);

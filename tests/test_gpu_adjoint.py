@@ -125,14 +125,15 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("kw", [dict(dim=3)])
-def test_adjoint_rejects_unsupported_setups(wave, kw):
-    cfg = _config(wave, **kw)
+@pytest.mark.parametrize("dim,equation", [(2, "acoustic"), (3, "acoustic")])
+def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
+    """Equations without an adjoint are refused with WAVE_ERR_UNSUPPORTED."""
+    cfg = _config(wave, dim=dim)
+    cfg.equation = wave.EQUATIONS[equation]
     true, start = _models()
-    dim = kw.get("dim", 2)
     n = cfg.N
-    model = {k: np.resize(v, n).astype(np.float32) for k, v in start.items()}
-    s = wave.Factory.Create("3D" if dim == 3 else "2D", "elastic").initForwardSolver(cfg)
+    model = {k: np.resize(v, n).astype(np.float32) for k, v in start.items() if k != "vs"}
+    s = wave.Factory.Create("3D" if dim == 3 else "2D", equation).initForwardSolver(cfg)
     s.prepareForModelling(model)
     s.setSources(np.array([5], np.int64), np.array([1], np.int32), np.zeros((1, s.nt), np.float32))
     s.setReceivers(np.array([7], np.int64), np.array([2], np.int32))

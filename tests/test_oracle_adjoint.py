@@ -266,3 +266,65 @@ def test_oracle_tez_adjoint_matches_fp64_finite_differences(refcpu, boundary, st
         ad = float(np.dot(grads[name], d))
         assert abs(fd) > 0
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
+
+
+def el3_case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=24, NY=20, NZ=18, nt=110):
+    rng = np.random.default_rng(21)
+    y, z, x = np.mgrid[0:NY, 0:NZ, 0:NX]   # index x + NX (z + NZ y)
+    vp = 2000.0 + 500.0 * (y / NY) + 60.0 * np.sin(x / 4.0) + 40.0 * np.cos(z / 3.0) + 20 * rng.standard_normal((NY, NZ, NX))
+    vs = vp / 1.8
+    rho = 300.0 * vp ** 0.25
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(vp=vp, vs=vs, rho=rho).items()}
+    DH, DT = 5.0, 4e-4
+    cfg = refcpu.make_config(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=(nt - 0.4) * DT,
+                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary, BoundaryWidth=5,
+                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=25.0, VMaxCPML=2600.0,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    sidx = np.array([refcpu.grid_index(cfg, NX // 2, 2 if fs else 5, NZ // 2),
+                     refcpu.grid_index(cfg, NX // 3, 7, NZ // 3)], np.int64)
+    sig = refcpu.ricker(nt, DT, 30.0, 1.0, -0.015, np.float64)
+    rx = np.arange(3, NX - 3, 3)
+    ry = 0 if fs else 4
+    ridx = np.concatenate([rx + NX * (NZ // 2 + NZ * ry), rx + NX * (NZ // 3 + NZ * ry), rx + NX * (5 + NZ * (NY - 5)),
+                           rx + NX * (12 + NZ * (NY - 5))]).astype(np.int64)
+    rtype = np.concatenate([np.full(rx.size, 2), np.full(rx.size, 3), np.full(rx.size, 4), np.full(rx.size, 1)]).astype(np.int32)
+    return cfg, model, (sidx, np.array([1, 4], np.int32), np.stack([sig, 3e-4 * sig]), ridx, rtype)
+
+
+def smooth3(rng, cfg):
+    from scipy.ndimage import gaussian_filter
+    return gaussian_filter(rng.standard_normal((cfg.NY, cfg.NZ, cfg.NX)), 2.5, mode="nearest").reshape(-1)
+
+
+@pytest.mark.parametrize("fs,boundary,stencil,reduce", [(0, 2, 0, 1), (1, 2, 0, 1), (0, 1, 1, 0), (1, 0, 0, 0)])
+def test_oracle_elastic3d_adjoint_matches_fp64_finite_differences(refcpu, fs, boundary, stencil, reduce):
+    """The oracle's FP64 adjoint of the 3-D elastic step (gradients with
+    respect to vp, vs, rho; P and VZ sources, P / VX / VY / VZ receivers)
+    against central finite differences of its own misfit along smooth
+    directions, with CPML, ABS, no boundary and the free surface."""
+    cfg, model, acq = el3_case(refcpu, fs, boundary, stencil, reduce)
+    true = dict(model)
+    y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
+    blob = np.exp(-((x - cfg.NX * 0.5) ** 2 + (y - cfg.NY * 0.55) ** 2 + (z - cfg.NZ * 0.5) ** 2) / 18.0).reshape(-1)
+    true["vp"] = model["vp"] * (1 + 0.05 * blob)
+    true["vs"] = model["vs"] * (1 - 0.04 * blob)
+    true["rho"] = model["rho"] * (1 + 0.03 * blob)
+    o = refcpu.Oracle(cfg, true, *acq, dtype=np.float64)
+    dobs = 0.9 * o.run()
+    o.close()
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    J, gvp, gvs, grho = o.adjoint_gradient(dobs, checkpoint_every=37)
+    o.close()
+    assert J > 0 and J == pytest.approx(misfit(refcpu, cfg, model, acq, dobs), rel=1e-12)
+    rng = np.random.default_rng(23)
+    grads = dict(vp=gvp, vs=gvs, rho=grho)
+    for name in ("vp", "vs", "rho"):
+        d = smooth3(rng, cfg) * model[name]
+        h = 1e-5
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name] + h * d
+        mm[name] = model[name] - h * d
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        ad = float(np.dot(grads[name], d))
+        assert abs(fd) > 0
+        assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)

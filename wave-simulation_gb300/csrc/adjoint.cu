@@ -48,6 +48,18 @@
 // averages of eps and sigma along x and y, EMEM.cpp:378-392; iMxy the inverse
 // 4-point average of mu).
 //
+// The 3-D elastic step (FD3Delastic::run, ForwardSolver3Delastic.cpp:120-414)
+// has the same three stages over nine fields and eighteen psi arrays:
+//   vx' = vx + irx (Dxf sxx + DybS sxy + Dzb sxz)',  vy', vz' likewise,
+//   normal stresses from c0' = Dxb vx', c1' = Dyb vy', c2' = Dzb vz' with M, 2 mu;
+//   sxy, sxz, syz from the forward cross derivatives with muXY, muXZ, muYZ;
+// then at y = 0 with the free surface syy' = 0 and sxx', szz' += sh (c0' + c2')
+// - sv c1' (FreeSurface3Delastic.cpp:15-47), then the ABS taper on all nine
+// fields; the last kernel maps dJ/dM, dJ/dmu, dJ/dmuXY, dJ/dmuXZ, dJ/dmuYZ and
+// dJ/dirx, dJ/diry, dJ/dirz to vp, vs and rho through the harmonic 4-point
+// averages in the xy, xz and yz planes and the 2-point inverse density
+// averages (Modelparameter.cpp:336-639).
+//
 // Checkpointing: the forward run saves the state every K steps; the backward
 // sweep recomputes each K-step segment into a buffer of K+1 states and walks
 // it backwards. The reference has no adjoint (its inversion lives in a
@@ -61,38 +73,9 @@
 
 #include <cuda_runtime.h>
 
-#include "handle.h"
-#include "stencil.cuh"
+#include "adjoint.cuh"
 
 namespace wave {
-
-// parts of one saved state, in view order
-enum AdjPart { AV_VX, AV_VY, AV_SXX, AV_SYY, AV_SXY, AV_P1, AV_P2, AV_P3, AV_P4, AV_Q1, AV_Q2, AV_Q3, AV_Q4, AV_COUNT };
-
-// psi slot of each psi part: velocity pass P1..P4, stress pass Q1..Q4
-static const int kAdjPsiSlot[8] = {PS_SXX_X, PS_SXY_Y, PS_SXY_X, PS_SYY_Y, PS_VXX, PS_VYY, PS_VXY, PS_VYX};
-
-struct AdjShot {
-    float* view;                 // recompute buffer: K+1 states
-    long long stride;            // floats per state
-    long long off[AV_COUNT];     // part offsets within a state (0 = absent psi)
-    float* lf[5];                // adjoint fields: vx, vy, sxx, syy, sxy
-    float* lpsi[8];              // adjoint psi (slab layout of the forward psi)
-    float* T[8];                 // adjoints of the raw derivatives c1..c4, a1..a4
-    float* g[5];                 // dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry
-    const long long* ridx;
-    const int* rtype;
-    const float* res;            // residual d - d_obs, nrec x nt
-    int nrec, nt;
-    int tm;                      // 1: lossless 2-D TMz (parts: hx, hy, ez; psi ezy, ezx, hyx, hxy)
-    int sh;                      // 1: 2-D SH (parts: vz, sxz, syz; psi sxz_x, syz_y, vzx, vzy)
-    int te;                      // 1: lossless 2-D TEz (parts: hz, ex, ey; psi eyx, exy, hzy, hzx)
-    float* vprime[2];            // vx', vy' (TMz: hx', hy') of the current step (null: the saved state's are they)
-    const long long* sidx;       // sources (velocity sources are taken out of v')
-    const int* stype;
-    const float* signals;        // nsrc x nt
-    int nsrc;
-};
 
 struct CopyPart {
     const float* src;
@@ -100,410 +83,9 @@ struct CopyPart {
     long long n;
     long long srcStride, dstStride;   // per state index
 };
-
 namespace {
 
-// (D^T lam)[c] = sum_k w_{c-k}(k) lam[c-k] over the rows c-k inside the axis,
-// with the row weights of deriv(): interior weights or the edge-table row
-template <int H, bool FWD>
-__device__ __forceinline__ float derivT(const float* __restrict__ lam, long long i, long long st, int c, const Op1D& op)
-{
-    float s = 0.0f;
-    if (!op.full && c - H >= op.E && c + H < op.n - op.E) {
-        // every row c-k is an interior row: its weight at offset k is the interior weight
-#pragma unroll
-        for (int k = (FWD ? -H + 1 : -H); k <= (FWD ? H : H - 1); ++k) s += op.w[kMaxHalf + k] * __ldg(lam + i - k * st);
-        return s;
-    }
-#pragma unroll
-    for (int k = -H; k <= H; ++k) {
-        const int r = c - k;
-        if (r < 0 || r >= op.n) continue;
-        float w;
-        if (!op.full && r >= op.E && r < op.n - op.E) {
-            w = op.w[kMaxHalf + k];
-        } else {
-            const int slot = op.full ? r : (r < op.E ? r : op.E + r - (op.n - op.E));
-            w = __ldg(op.tab + slot * kTabW + kMaxHalf + k);
-        }
-        if (w != 0.0f) s += w * __ldg(lam + i - k * st);
-    }
-    return s;
-}
-
-// adjoint of (c, Q) -> (c' = (1 + a) c + b Q, Q' = a c + b Q)
-__device__ __forceinline__ void cpml_adj(float& l, float* lpsi, float a, float b)
-{
-    const float lq = *lpsi;
-    const float lc = (1.0f + a) * l + a * lq;
-    *lpsi = b * (l + lq);
-    l = lc;
-}
-
-struct Slabs {
-    int sx, sy;
-    long long px, py;
-};
-
-__device__ __forceinline__ Slabs slabs_of(const StepParams& P, const Pt& p)
-{
-    Slabs S;
-    S.sx = P.useCpml ? slab(p.x, P.cx) : -1;
-    S.sy = P.useCpml ? slab(p.y, P.cy) : -1;
-    S.px = S.sx >= 0 ? pix(P, p, S.sx) : 0;
-    S.py = S.sy >= 0 ? piy(P, p, S.sy) : 0;
-    return S;
-}
-
-// stress-pass transpose at step n (state n = view vn, state n+1 = view vn+1)
-template <int H>
-__device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
-{
-    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
-    const long long i = p.i, sy = P.NX;
-    const float* vx1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
-    const float* vy1 = A.vprime[1] ? A.vprime[1] : X1 + A.off[AV_VY];
-    const float M = __ldg(P.m[M_M] + i), mu = __ldg(P.m[M_MU] + i), mxy = __ldg(P.m[M_MUXY] + i);
-    const Slabs S = slabs_of(P, p);
-    // forward derivatives with their CPML correction, c' = c + Q_{n+1}
-    float c1 = deriv<H, false>(vx1, i, 1, p.x, P.Dxb);
-    float c2 = deriv<H, false>(vy1, i, sy, p.y, P.Dyb);
-    float c3 = deriv<H, true>(vx1, i, sy, p.y, P.Dyf);
-    float c4 = deriv<H, true>(vy1, i, 1, p.x, P.Dxf);
-    if (S.sx >= 0) { c1 += X1[A.off[AV_Q1] + S.px]; c4 += X1[A.off[AV_Q4] + S.px]; }
-    if (S.sy >= 0) { c2 += X1[A.off[AV_Q2] + S.py]; c3 += X1[A.off[AV_Q3] + S.py]; }
-    float lxx = A.lf[2][i], lyy = A.lf[3][i], lxy = A.lf[4][i];
-    if (pending) {
-        // the transposed velocity-pass derivatives of sigma from the step after
-        // this one (its third stage, folded in here to save a launch)
-        const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
-        const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
-        lxx += derivT<H, true>(A.T[4], i, 1, p.x, P.Dxf);
-        float u = derivT<H, false>(A.T[5], i, sy, p.y, DybS);
-        u += derivT<H, false>(A.T[6], i, 1, p.x, P.Dxb);
-        lxy += u;
-        lyy += derivT<H, true>(A.T[7], i, sy, p.y, DyfS);
-    }
-    if (P.abs) {
-        // the taper multiplied all five fields last: their adjoints first
-        const float d = absDamp(P, p);
-        lxx *= d; lyy *= d; lxy *= d;
-        A.lf[0][i] *= d;
-        A.lf[1][i] *= d;
-    }
-    const bool fsRow = P.fs && p.y == 0;
-    if (fsRow) lyy = 0.0f;                 // syy' = 0 on the surface
-    A.lf[2][i] = lxx;
-    A.lf[3][i] = lyy;
-    A.lf[4][i] = lxy;
-    const float lam = M - 2.0f * mu;
-    float l1 = M * lxx + lam * lyy;
-    float l2 = lam * lxx + M * lyy;
-    float l3 = mxy * lxy, l4 = l3;
-    if (fsRow) {
-        // sxx' += sh c1' - sv c2' with sv = M - 2 mu, sh = -sv^2 / M
-        const float sv = lam, sh = -(sv * sv) / M;
-        l1 += sh * lxx;
-        l2 -= sv * lxx;
-        // dJ/dsh = lxx c1', dJ/dsv = -lxx c2' (c1, c2 carry their CPML correction here);
-        // d sv / dM = 1, d sv / dmu = -2; d sh / dM = -(2 sv / M - sv^2 / M^2), d sh / dmu = 4 sv / M
-        const float gh = lxx * c1, gv = -lxx * c2;
-        A.g[0][i] += gv - gh * (2.0f * sv / M - (sv * sv) / (M * M));
-        A.g[1][i] += -2.0f * gv + gh * 4.0f * sv / M;
-    }
-    if (S.sx >= 0) {
-        cpml_adj(l1, A.lpsi[4] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // Q1 (vxx): x, full profile
-        cpml_adj(l4, A.lpsi[7] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // Q4 (vyx): x, half profile
-    }
-    if (S.sy >= 0) {
-        cpml_adj(l2, A.lpsi[5] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // Q2 (vyy): y, full profile
-        cpml_adj(l3, A.lpsi[6] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // Q3 (vxy): y, half profile
-    }
-    A.T[0][i] = l1;
-    A.T[1][i] = l2;
-    A.T[2][i] = l3;
-    A.T[3][i] = l4;
-    A.g[0][i] += (lxx + lyy) * (c1 + c2);
-    A.g[1][i] += -2.0f * (lxx * c2 + lyy * c1);
-    A.g[2][i] += lxy * (c3 + c4);
-}
-
-// velocity-pass transpose (and the transposed stress-pass derivatives of v)
-template <int H>
-__device__ __forceinline__ void adj_vel_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
-{
-    const float* X0 = A.view + (long long)vn * A.stride;
-    const float* X1 = X0 + A.stride;
-    const long long i = p.i, sy = P.NX;
-    float lvx = A.lf[0][i];
-    lvx += derivT<H, false>(A.T[0], i, 1, p.x, P.Dxb);
-    lvx += derivT<H, true>(A.T[2], i, sy, p.y, P.Dyf);
-    float lvy = A.lf[1][i];
-    lvy += derivT<H, false>(A.T[1], i, sy, p.y, P.Dyb);
-    lvy += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
-    const Slabs S = slabs_of(P, p);
-    const float *sxx = X0 + A.off[AV_SXX], *syy = X0 + A.off[AV_SYY], *sxy = X0 + A.off[AV_SXY];
-    const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
-    const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
-    float a1 = deriv<H, true>(sxx, i, 1, p.x, P.Dxf);
-    float a2 = deriv<H, false>(sxy, i, sy, p.y, DybS);
-    float a3 = deriv<H, false>(sxy, i, 1, p.x, P.Dxb);
-    float a4 = deriv<H, true>(syy, i, sy, p.y, DyfS);
-    if (S.sx >= 0) { a1 += X1[A.off[AV_P1] + S.px]; a3 += X1[A.off[AV_P3] + S.px]; }
-    if (S.sy >= 0) { a2 += X1[A.off[AV_P2] + S.py]; a4 += X1[A.off[AV_P4] + S.py]; }
-    const float irx = __ldg(P.m[M_IRX] + i), iry = __ldg(P.m[M_IRY] + i);
-    float l1 = irx * lvx, l2 = l1, l3 = iry * lvy, l4 = l3;
-    if (S.sx >= 0) {
-        cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // P1 (sxx_x): x, half profile
-        cpml_adj(l3, A.lpsi[2] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // P3 (sxy_x): x, full profile
-    }
-    if (S.sy >= 0) {
-        cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // P2 (sxy_y): y, full profile
-        cpml_adj(l4, A.lpsi[3] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // P4 (syy_y): y, half profile
-    }
-    A.T[4][i] = l1;
-    A.T[5][i] = l2;
-    A.T[6][i] = l3;
-    A.T[7][i] = l4;
-    A.lf[0][i] = lvx;
-    A.lf[1][i] = lvy;
-    A.g[3][i] += lvx * (a1 + a2);
-    A.g[4][i] += lvy * (a3 + a4);
-}
-
-
-// ---- lossless 2-D TMz --------------------------------------------------------
-// parts of a TMz state in the view: AV_VX = hx, AV_VY = hy, AV_SXX = ez,
-// AV_P1..AV_P4 = psi of ezy, ezx, hyx, hxy; lf[0..2] = adjoints of hx, hy, ez;
-// T[0..3] = adjoints of c1, c2, a1, a2; g[0..3] = dJ/dCa, dJ/dCb, dJ/diMyz, dJ/diMxz
-
-// E-update transpose at step n
-template <int H>
-__device__ __forceinline__ void adj_tm_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
-{
-    const float* X0 = A.view + (long long)vn * A.stride;
-    const float* X1 = X0 + A.stride;
-    const long long i = p.i, sy = P.NX;
-    const float* hx1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
-    const float* hy1 = A.vprime[1] ? A.vprime[1] : X1 + A.off[AV_VY];
-    const Slabs S = slabs_of(P, p);
-    float c1 = deriv<H, false>(hy1, i, 1, p.x, P.Dxb);
-    float c2 = deriv<H, false>(hx1, i, sy, p.y, P.Dyb);
-    if (S.sx >= 0) c1 += X1[A.off[AV_P3] + S.px];
-    if (S.sy >= 0) c2 += X1[A.off[AV_P4] + S.py];
-    float lez = A.lf[2][i];
-    if (pending) {
-        // the transposed H-update derivatives of ez from the step after this one
-        float u = derivT<H, true>(A.T[2], i, sy, p.y, P.Dyf);
-        u += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
-        lez += u;
-    }
-    if (P.abs) {
-        // the taper multiplied ez, hx and hy last: their adjoints first
-        const float d = absDamp(P, p);
-        lez *= d;
-        A.lf[0][i] *= d;
-        A.lf[1][i] *= d;
-    }
-    const float ca = __ldg(P.m[M_CAZ] + i), cb = __ldg(P.m[M_CBZ] + i);
-    float l1 = cb * lez, l2 = -l1;
-    A.g[0][i] += lez * X0[A.off[AV_SXX] + i];
-    A.g[1][i] += lez * (c1 - c2);
-    A.lf[2][i] = ca * lez;
-    if (S.sx >= 0) cpml_adj(l1, A.lpsi[2] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // hyx: x, full profile
-    if (S.sy >= 0) cpml_adj(l2, A.lpsi[3] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // hxy: y, full profile
-    A.T[0][i] = l1;
-    A.T[1][i] = l2;
-}
-
-// H-update transpose at step n (after the E transpose of every point)
-template <int H>
-__device__ __forceinline__ void adj_tm_h_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
-{
-    const float* X0 = A.view + (long long)vn * A.stride;
-    const float* X1 = X0 + A.stride;
-    const long long i = p.i, sy = P.NX;
-    const float lhy = A.lf[1][i] + derivT<H, false>(A.T[0], i, 1, p.x, P.Dxb);
-    const float lhx = A.lf[0][i] + derivT<H, false>(A.T[1], i, sy, p.y, P.Dyb);
-    const float* ez0 = X0 + A.off[AV_SXX];
-    const Slabs S = slabs_of(P, p);
-    float a1 = deriv<H, true>(ez0, i, sy, p.y, P.Dyf);
-    float a2 = deriv<H, true>(ez0, i, 1, p.x, P.Dxf);
-    if (S.sy >= 0) a1 += X1[A.off[AV_P1] + S.py];
-    if (S.sx >= 0) a2 += X1[A.off[AV_P2] + S.px];
-    const float imyz = __ldg(P.m[M_IMUYZ] + i), imxz = __ldg(P.m[M_IMUXZ] + i);
-    float l1 = -imyz * lhx, l2 = imxz * lhy;
-    A.g[2][i] += -lhx * a1;
-    A.g[3][i] += lhy * a2;
-    if (S.sy >= 0) cpml_adj(l1, A.lpsi[0] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // ezy: y, half profile
-    if (S.sx >= 0) cpml_adj(l2, A.lpsi[1] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // ezx: x, half profile
-    A.T[2][i] = l1;
-    A.T[3][i] = l2;
-    A.lf[0][i] = lhx;
-    A.lf[1][i] = lhy;
-}
-
-
-// ---- 2-D SH ---------------------------------------------------------------
-// parts of an SH state in the view: AV_VX = vz, AV_SXX = sxz, AV_SYY = syz,
-// AV_P1, AV_P2 = psi of sxz_x, syz_y, AV_Q1, AV_Q2 = psi of vzx, vzy;
-// lf[0], lf[2], lf[3] = adjoints of vz, sxz, syz; T[0..1] = adjoints of the
-// stress-pass derivatives c1, c2, T[2..3] of the velocity-pass ones a1, a2;
-// g[0..2] = dJ/dmuXZ, dJ/dmuYZ, dJ/dirho
-
-// stress-update transpose at step n
-template <int H>
-__device__ __forceinline__ void adj_sh_s_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
-{
-    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
-    const long long i = p.i, sy = P.NX;
-    const float* vz1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
-    const Slabs S = slabs_of(P, p);
-    float c1 = deriv<H, true>(vz1, i, 1, p.x, P.Dxf);
-    float c2 = deriv<H, true>(vz1, i, sy, p.y, P.Dyf);
-    if (S.sx >= 0) c1 += X1[A.off[AV_Q1] + S.px];
-    if (S.sy >= 0) c2 += X1[A.off[AV_Q2] + S.py];
-    float lxz = A.lf[2][i], lyz = A.lf[3][i];
-    if (pending) {
-        // the transposed velocity-update derivatives of the stresses from the step after this one
-        lxz += derivT<H, false>(A.T[2], i, 1, p.x, P.Dxb);
-        lyz += derivT<H, false>(A.T[3], i, sy, p.y, P.fs ? P.DybS : P.Dyb);
-    }
-    if (P.abs) {
-        // the taper multiplied sxz, syz and vz last: their adjoints first
-        const float d = absDamp(P, p);
-        lxz *= d;
-        lyz *= d;
-        A.lf[0][i] *= d;
-    }
-    A.lf[2][i] = lxz;
-    A.lf[3][i] = lyz;
-    float l1 = __ldg(P.m[M_MUXZ] + i) * lxz, l2 = __ldg(P.m[M_MUYZ] + i) * lyz;
-    A.g[0][i] += lxz * c1;
-    A.g[1][i] += lyz * c2;
-    if (S.sx >= 0) cpml_adj(l1, A.lpsi[4] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // vzx: x, half profile
-    if (S.sy >= 0) cpml_adj(l2, A.lpsi[5] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // vzy: y, half profile
-    A.T[0][i] = l1;
-    A.T[1][i] = l2;
-}
-
-// velocity-update transpose at step n (after the stress transpose of every point)
-template <int H>
-__device__ __forceinline__ void adj_sh_v_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
-{
-    const float* X0 = A.view + (long long)vn * A.stride;
-    const float* X1 = X0 + A.stride;
-    const long long i = p.i, sy = P.NX;
-    float lvz = A.lf[0][i];
-    lvz += derivT<H, true>(A.T[0], i, 1, p.x, P.Dxf);
-    lvz += derivT<H, true>(A.T[1], i, sy, p.y, P.Dyf);
-    const Slabs S = slabs_of(P, p);
-    float a1 = deriv<H, false>(X0 + A.off[AV_SXX], i, 1, p.x, P.Dxb);
-    float a2 = deriv<H, false>(X0 + A.off[AV_SYY], i, sy, p.y, P.fs ? P.DybS : P.Dyb);
-    if (S.sx >= 0) a1 += X1[A.off[AV_P1] + S.px];
-    if (S.sy >= 0) a2 += X1[A.off[AV_P2] + S.py];
-    const float ir = __ldg(P.m[M_IR] + i);
-    float l1 = ir * lvz, l2 = l1;
-    A.g[2][i] += lvz * (a1 + a2);
-    if (S.sx >= 0) cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // sxz_x: x, full profile
-    if (S.sy >= 0) cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // syz_y: y, full profile
-    A.T[2][i] = l1;
-    A.T[3][i] = l2;
-    A.lf[0][i] = lvz;
-}
-
-
-// ---- lossless 2-D TEz -------------------------------------------------------
-// parts of a TEz state in the view: AV_VX = hz, AV_SXX = ex, AV_SYY = ey,
-// AV_P1, AV_P2 = psi of eyx, exy, AV_Q1, AV_Q2 = psi of hzy, hzx; lf[0], lf[2],
-// lf[3] = adjoints of hz, ex, ey; T[0..1] = adjoints of the E-update
-// derivatives c1, c2, T[2..3] of the H-update ones a1, a2; g[0..4] = dJ/dCaX,
-// dJ/dCbX, dJ/dCaY, dJ/dCbY, dJ/diMxy
-
-// E-update transpose at step n
-template <int H>
-__device__ __forceinline__ void adj_te_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
-{
-    const float* X0 = A.view + (long long)vn * A.stride;
-    const float* X1 = X0 + A.stride;
-    const long long i = p.i, sy = P.NX;
-    const float* hz1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
-    const Slabs S = slabs_of(P, p);
-    float c1 = deriv<H, false>(hz1, i, sy, p.y, P.Dyb);
-    float c2 = deriv<H, false>(hz1, i, 1, p.x, P.Dxb);
-    if (S.sy >= 0) c1 += X1[A.off[AV_Q1] + S.py];
-    if (S.sx >= 0) c2 += X1[A.off[AV_Q2] + S.px];
-    float lex = A.lf[2][i], ley = A.lf[3][i];
-    if (pending) {
-        // the transposed H-update derivatives of ey and ex from the step after this one
-        ley += derivT<H, true>(A.T[2], i, 1, p.x, P.Dxf);
-        lex += derivT<H, true>(A.T[3], i, sy, p.y, P.Dyf);
-    }
-    if (P.abs) {
-        // the taper multiplied ey, ex and hz last: their adjoints first
-        const float d = absDamp(P, p);
-        lex *= d;
-        ley *= d;
-        A.lf[0][i] *= d;
-    }
-    const float cax = __ldg(P.m[M_CAX] + i), cbx = __ldg(P.m[M_CBX] + i);
-    const float cay = __ldg(P.m[M_CAY] + i), cby = __ldg(P.m[M_CBY] + i);
-    A.g[0][i] += lex * X0[A.off[AV_SXX] + i];
-    A.g[1][i] += lex * c1;
-    A.g[2][i] += ley * X0[A.off[AV_SYY] + i];
-    A.g[3][i] -= ley * c2;
-    float l1 = cbx * lex, l2 = -cby * ley;
-    A.lf[2][i] = cax * lex;
-    A.lf[3][i] = cay * ley;
-    if (S.sy >= 0) cpml_adj(l1, A.lpsi[4] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // hzy: y, full profile
-    if (S.sx >= 0) cpml_adj(l2, A.lpsi[5] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // hzx: x, full profile
-    A.T[0][i] = l1;
-    A.T[1][i] = l2;
-}
-
-// H-update transpose at step n (after the E transpose of every point)
-template <int H>
-__device__ __forceinline__ void adj_te_h_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
-{
-    const float* X0 = A.view + (long long)vn * A.stride;
-    const float* X1 = X0 + A.stride;
-    const long long i = p.i, sy = P.NX;
-    float lhz = A.lf[0][i];
-    lhz += derivT<H, false>(A.T[0], i, sy, p.y, P.Dyb);
-    lhz += derivT<H, false>(A.T[1], i, 1, p.x, P.Dxb);
-    const Slabs S = slabs_of(P, p);
-    float a1 = deriv<H, true>(X0 + A.off[AV_SYY], i, 1, p.x, P.Dxf);
-    float a2 = deriv<H, true>(X0 + A.off[AV_SXX], i, sy, p.y, P.Dyf);
-    if (S.sx >= 0) a1 += X1[A.off[AV_P1] + S.px];
-    if (S.sy >= 0) a2 += X1[A.off[AV_P2] + S.py];
-    const float im = __ldg(P.m[M_IMUXY] + i);
-    float l1 = -im * lhz, l2 = im * lhz;
-    A.g[4][i] -= lhz * (a1 - a2);
-    if (S.sx >= 0) cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // eyx: x, half profile
-    if (S.sy >= 0) cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // exy: y, half profile
-    A.T[2][i] = l1;
-    A.T[3][i] = l2;
-    A.lf[0][i] = lhz;
-}
-
-
-template <int H, int PASS>
-__global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
-                                                const BatchTile* __restrict__ W, BatchSched S, int vn, int pending)
-{
-    BATCH_SHARED_PARAMS(sP);
-    batch_loop(Ps, W, S, sP, [&](const StepParams& P, const Pt& p, int shot) {
-        const AdjShot& A = As[shot];
-        if (PASS == 0) adj_stress_body<H>(P, A, p, vn, pending != 0);
-        else if (PASS == 1) adj_vel_body<H>(P, A, p, vn);
-        else if (PASS == 3) adj_tm_e_body<H>(P, A, p, vn, pending != 0);
-        else if (PASS == 4) adj_tm_h_body<H>(P, A, p, vn);
-        else if (PASS == 5) adj_sh_s_body<H>(P, A, p, vn, pending != 0);
-        else if (PASS == 6) adj_sh_v_body<H>(P, A, p, vn);
-        else if (PASS == 7) adj_te_e_body<H>(P, A, p, vn, pending != 0);
-        else adj_te_h_body<H>(P, A, p, vn);
-    });
-}
+using namespace adj;
 
 // v' = (v_{n+1} - sources of step n) / d: the velocities the stress pass of
 // step n read (before the ABS taper and the source injection)
@@ -516,6 +98,10 @@ __global__ void adj_vprime(const StepParams* __restrict__ Ps, const AdjShot* __r
         if (!A.vprime[0]) return;
         const float* X1 = A.view + (long long)(vn + 1) * A.stride;
         const float d = P.abs ? absDamp(P, p) : 1.0f;
+        if (A.e3) {
+            for (int k = 0; k < 3; ++k) A.vprime[k][p.i] = X1[A.off[E3_VX + k] + p.i] / d;
+            return;
+        }
         A.vprime[0][p.i] = X1[A.off[AV_VX] + p.i] / d;
         if (!A.sh && !A.te) A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
     });
@@ -528,15 +114,19 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
     if (!A.vprime[0]) return;
     for (int k = threadIdx.x; k < A.nsrc; k += blockDim.x) {
         const int t = A.stype[k];
-        if (A.te ? t != WAVE_TYPE_HZ : A.sh ? t != WAVE_TYPE_VZ : (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY)) continue;
+        if (A.e3 ? (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY && t != WAVE_TYPE_VZ)
+                 : A.te ? t != WAVE_TYPE_HZ : A.sh ? t != WAVE_TYPE_VZ : (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY))
+            continue;
         const long long i = A.sidx[k];
         Pt p;
         p.i = i;
         p.x = static_cast<int>(i % P.NX);
-        p.y = static_cast<int>(i / P.NX);
-        p.z = 0;
+        const long long r = i / P.NX;   // z + NZ y
+        p.y = static_cast<int>(r / P.NZ);
+        p.z = static_cast<int>(r - (long long)p.y * P.NZ);
         const float d = P.abs ? absDamp(P, p) : 1.0f;
-        atomicAdd(A.vprime[(A.sh || A.te || t == WAVE_TYPE_VX) ? 0 : 1] + i, -A.signals[(long long)k * A.nt + n] / d);
+        const int v = A.e3 ? t - WAVE_TYPE_VX : (A.sh || A.te || t == WAVE_TYPE_VX) ? 0 : 1;
+        atomicAdd(A.vprime[v] + i, -A.signals[(long long)k * A.nt + n] / d);
     }
 }
 
@@ -554,6 +144,15 @@ __global__ void adj_inject(const AdjShot* __restrict__ As, int n)
         }
         if (A.sh) {   // vz receivers
             atomicAdd(A.lf[0] + i, v);
+            continue;
+        }
+        if (A.e3) {   // a pressure trace is (sxx + syy + szz) / 3 (FDTD3Delastic)
+            const int t = A.rtype[r];
+            if (t == WAVE_TYPE_P) {
+                for (int k = 3; k < 6; ++k) atomicAdd(A.lf[k] + i, v / 3.0f);
+            } else {
+                atomicAdd(A.lf[t - WAVE_TYPE_VX] + i, v);
+            }
             continue;
         }
         if (A.te) {   // Ex, Ey and Hz receivers
@@ -793,34 +392,80 @@ __global__ void adj_te_final(PrepParams G, const StepParams P, const AdjShot A, 
     }
 }
 
-template <int H>
-void launch_adj_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
-                  int pending, cudaStream_t s)
+// weight of point (ka, kb) in the 4-point row at (a, b) of a plane average,
+// by its two in-plane coordinates (the edge fallbacks of
+// calc4PointAverageMatrixRow, Modelparameter.cpp:448-527)
+__device__ __forceinline__ float w4p(int a, int b, int ka, int kb, int Na, int Nb) { return w4(a, b, ka, kb, Na, Nb); }
+
+// chain rule for 3-D elastic: M = rho vp^2; mu = max(rho vs^2, 1); muXY, muXZ,
+// muYZ = 1 / (4-point average of 1 / mu in the xy, xz, yz planes) (0 below 4);
+// irx, iry, irz = 1 / (2-point average of rho along x, y, z) (0 where invalid)
+__global__ void adj_e3_final(PrepParams G, const StepParams P, const AdjShot A, float* gvp, float* gvs, float* grho, int accumulate)
 {
-    const dim3 block(32, 8, 1);
-    switch (pass) {
-    case 0: adj_pass<H, 0><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    case 1: adj_pass<H, 1><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    case 3: adj_pass<H, 3><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    case 4: adj_pass<H, 4><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    case 5: adj_pass<H, 5><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    case 6: adj_pass<H, 6><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    case 7: adj_pass<H, 7><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
-    default: adj_pass<H, 8><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    const long long sy = (long long)G.NX * G.NZ, sz = G.NX;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
+        const int kx = static_cast<int>(k % G.NX);
+        const long long rest = k / G.NX;
+        const int kz = static_cast<int>(rest % G.NZ), ky = static_cast<int>(rest / G.NZ);
+        const float rho = P.m[M_RHO][k], vp = P.m[M_VP][k], vs = P.m[M_VS][k];
+        const float muk = P.m[M_MU][k];
+        float gmu = A.g[1][k];
+        // rows of the plane averages that read point k: (x, y) - {0, 1}^2 in the xy plane, etc.
+        for (int db = 0; db <= 1; ++db)
+            for (int da = 0; da <= 1; ++da) {
+                // xy plane
+                if (kx - da >= 0 && ky - db >= 0) {
+                    const long long r = k - da - db * sy;
+                    const float m = P.m[M_MUXY][r];
+                    const float w = m != 0.0f ? w4p(kx - da, ky - db, kx, ky, G.NX, G.NY) : 0.0f;
+                    if (w != 0.0f) gmu += A.g[2][r] * w * (m / muk) * (m / muk);
+                }
+                // xz plane
+                if (kx - da >= 0 && kz - db >= 0) {
+                    const long long r = k - da - db * sz;
+                    const float m = P.m[M_MUXZ][r];
+                    const float w = m != 0.0f ? w4p(kx - da, kz - db, kx, kz, G.NX, G.NZ) : 0.0f;
+                    if (w != 0.0f) gmu += A.g[3][r] * w * (m / muk) * (m / muk);
+                }
+                // yz plane
+                if (ky - da >= 0 && kz - db >= 0) {
+                    const long long r = k - da * sy - db * sz;
+                    const float m = P.m[M_MUYZ][r];
+                    const float w = m != 0.0f ? w4p(ky - da, kz - db, ky, kz, G.NY, G.NZ) : 0.0f;
+                    if (w != 0.0f) gmu += A.g[4][r] * w * (m / muk) * (m / muk);
+                }
+            }
+        float raw = rho;
+        raw *= vs;
+        raw *= vs;
+        const bool unclamped = raw >= 1.0f;
+        float gr = A.g[0][k] * vp * vp;
+        if (unclamped) gr += gmu * vs * vs;
+        // inverse density averages: rows k and k - 1 along each axis
+        const int kc[3] = {kx, ky, kz};
+        const int Nc[3] = {static_cast<int>(G.NX), static_cast<int>(G.NY), static_cast<int>(G.NZ)};
+        const long long st[3] = {1, sy, sz};
+        const int slot[3] = {M_IRX, M_IRY, M_IRZ};
+        for (int ax = 0; ax < 3; ++ax)
+            for (int d = 0; d <= 1; ++d) {
+                if (kc[ax] - d < 0) continue;
+                const long long r = k - d * st[ax];
+                const float ir = P.m[slot[ax]][r];
+                const float w = (kc[ax] - d + 1 < Nc[ax]) ? 0.5f : 1.0f;
+                if (ir != 0.0f && (d == 0 || w == 0.5f)) gr -= A.g[5 + ax][r] * ir * ir * w;
+            }
+        const float gp = A.g[0][k] * 2.0f * rho * vp;
+        const float gs = unclamped ? gmu * 2.0f * rho * vs : 0.0f;
+        if (accumulate) { gvp[k] += gp; gvs[k] += gs; grho[k] += gr; }
+        else { gvp[k] = gp; gvs[k] = gs; grho[k] = gr; }
     }
 }
 
 void launch_adj(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
                 int pending, cudaStream_t s)
 {
-    switch (H) {
-    case 1: launch_adj_h<1>(pass, Ps, As, W, S, grid, vn, pending, s); break;
-    case 2: launch_adj_h<2>(pass, Ps, As, W, S, grid, vn, pending, s); break;
-    case 3: launch_adj_h<3>(pass, Ps, As, W, S, grid, vn, pending, s); break;
-    case 4: launch_adj_h<4>(pass, Ps, As, W, S, grid, vn, pending, s); break;
-    case 5: launch_adj_h<5>(pass, Ps, As, W, S, grid, vn, pending, s); break;
-    default: launch_adj_h<6>(pass, Ps, As, W, S, grid, vn, pending, s); break;
-    }
+    if (pass >= 9) launch_adj_pass3d(H, pass, Ps, As, W, S, grid, vn, pending, s);
+    else launch_adj_pass2d(H, pass, Ps, As, W, S, grid, vn, pending, s);
 }
 
 void ck(cudaError_t e, const char* what)
@@ -853,9 +498,12 @@ struct DevPool {
 std::string adjoint_supported(const wave_handle* h)
 {
     const wave_config& c = h->cfg;
-    if (c.dimension != 2 ||
-        (c.equation != WAVE_EQ_ELASTIC && c.equation != WAVE_EQ_TMEM && c.equation != WAVE_EQ_SH && c.equation != WAVE_EQ_EMEM))
-        return "the adjoint gradient is implemented for 2-D elastic, 2-D SH and lossless 2-D TMz and TEz modelling";
+    const bool ok2 = c.dimension == 2 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_SH ||
+                                          c.equation == WAVE_EQ_EMEM);
+    const bool ok3 = c.dimension == 3 && c.equation == WAVE_EQ_ELASTIC;
+    if (!ok2 && !ok3)
+        return "the adjoint gradient is implemented for 2-D and 3-D elastic, 2-D SH and lossless 2-D TMz and TEz modelling";
+    if (ok3 && c.FreeSurface == 2) return "the 3-D adjoint takes the mirror free surface (FreeSurface = 1) or none";
     if (c.equation == WAVE_EQ_TMEM) {
         for (int t : h->hRecType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez receivers only";
@@ -895,9 +543,11 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         // state layout: 5 field parts then 8 psi parts (absent parts: length 0);
         // TMz: hx, hy, ez and the psi of ezy, ezx, hyx, hxy
         // SH: vz, -, sxz, syz and the psi of sxz_x, syz_y, -, -, vzx, vzy
+        // 3-D elastic: the Adj3Part layout
         const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
         const bool sh = h->cfg.equation == WAVE_EQ_SH;
-        long long off[AV_COUNT], len[AV_COUNT], o = 0;
+        const bool e3 = h->sp.is3d;
+        long long off[kAdjMaxParts], len[kAdjMaxParts], o = 0;
         const int elasticFields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
         const int tmFields[5] = {F_HX, F_HY, F_EZ, -1, -1};
         const int tmPsi[8] = {PS_EZY, PS_EZX, PS_HYX, PS_HXY, -1, -1, -1, -1};
@@ -907,32 +557,38 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int shPsi[8] = {PS_SXZ_X, PS_SYZ_Y, -1, -1, PS_VZX, PS_VZY, -1, -1};
         const int teFields[5] = {F_HZ, -1, F_EX, F_EY, -1};
         const int tePsi[8] = {PS_EYX, PS_EXY, -1, -1, PS_HZY, PS_HZX, -1, -1};
-        const int* fields = tm ? tmFields : sh ? shFields : te ? teFields : elasticFields;
-        const int* psiSlot = tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
-        for (int k = 0; k < 5; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
-        for (int k = 0; k < 8; ++k) {
+        const int e3Fields[9] = {F_VX, F_VY, F_VZ, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ};
+        const int e3Psi[18] = {PS_SXX_X, PS_SXY_Y, PS_SXZ_Z, PS_SXY_X, PS_SYY_Y, PS_SYZ_Z, PS_SXZ_X, PS_SYZ_Y, PS_SZZ_Z,
+                               PS_VXX,   PS_VYY,   PS_VZZ,   PS_VXY,   PS_VYX,   PS_VXZ,   PS_VZX,   PS_VYZ,   PS_VZY};
+        const int* fields = e3 ? e3Fields : tm ? tmFields : sh ? shFields : te ? teFields : elasticFields;
+        const int* psiSlot = e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
+        const int nf = e3 ? 9 : 5, np = e3 ? 18 : 8, nparts = nf + np;
+        for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
+        for (int k = 0; k < np; ++k) {
             const int slot = psiSlot[k];
-            off[5 + k] = o;
-            len[5 + k] = (slot >= 0 && h->psi[slot]) ? h->psiLen[slot] : 0;
-            o += len[5 + k];
+            off[nf + k] = o;
+            len[nf + k] = (slot >= 0 && h->psi[slot]) ? h->psiLen[slot] : 0;
+            o += len[nf + k];
         }
         stride[s] = o;
         AdjShot& a = A[s];
         a.tm = tm ? 1 : 0;
         a.sh = sh ? 1 : 0;
         a.te = te ? 1 : 0;
+        a.e3 = e3 ? 1 : 0;
         a.view = pool.get<float>(static_cast<size_t>(o) * (K + 1));
         a.stride = o;
-        for (int k = 0; k < AV_COUNT; ++k) a.off[k] = off[k];
+        for (int k = 0; k < kAdjMaxParts; ++k) a.off[k] = k < nparts ? off[k] : 0;
         float* lstate = pool.get<float>(o);
         ck(cudaMemsetAsync(lstate, 0, o * sizeof(float), st), "memset");
-        for (int k = 0; k < 5; ++k) a.lf[k] = lstate + off[k];
-        for (int k = 0; k < 8; ++k) a.lpsi[k] = lstate + off[5 + k];
-        float* temps = pool.get<float>(8 * N);
-        for (int k = 0; k < 8; ++k) a.T[k] = temps + k * N;
-        float* grads = pool.get<float>(5 * N);
-        ck(cudaMemsetAsync(grads, 0, 5 * N * sizeof(float), st), "memset");
-        for (int k = 0; k < 5; ++k) a.g[k] = grads + k * N;
+        for (int k = 0; k < nf; ++k) a.lf[k] = lstate + off[k];
+        for (int k = 0; k < np; ++k) a.lpsi[k] = lstate + off[nf + k];
+        const int ntemp = e3 ? 18 : 8, ngrad = e3 ? 8 : 5;
+        float* temps = pool.get<float>(static_cast<size_t>(ntemp) * N);
+        for (int k = 0; k < ntemp; ++k) a.T[k] = temps + k * N;
+        float* grads = pool.get<float>(static_cast<size_t>(ngrad) * N);
+        ck(cudaMemsetAsync(grads, 0, ngrad * N * sizeof(float), st), "memset");
+        for (int k = 0; k < ngrad; ++k) a.g[k] = grads + k * N;
         a.ridx = h->ridx;
         a.rtype = h->rtype;
         a.nrec = h->nrec;
@@ -941,20 +597,22 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         a.res = res;
         bool velocitySources = false;
         for (int t : h->hSrcType)
-            velocitySources |= te ? t == WAVE_TYPE_HZ : sh ? t == WAVE_TYPE_VZ : (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
-        a.vprime[0] = a.vprime[1] = nullptr;
+            velocitySources |= e3 ? (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY || t == WAVE_TYPE_VZ)
+                             : te ? t == WAVE_TYPE_HZ : sh ? t == WAVE_TYPE_VZ : (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
+        a.vprime[0] = a.vprime[1] = a.vprime[2] = nullptr;
         if (h->cfg.DampingBoundary == 1 || velocitySources) {
-            a.vprime[0] = pool.get<float>(2 * N);
-            a.vprime[1] = a.vprime[0] + N;
+            const int nv = e3 ? 3 : 2;
+            a.vprime[0] = pool.get<float>(static_cast<size_t>(nv) * N);
+            for (int k = 1; k < nv; ++k) a.vprime[k] = a.vprime[0] + k * N;
         }
         a.sidx = h->sidx;
         a.stype = h->stype;
         a.signals = h->signals;
         a.nsrc = h->nsrc;
         ckpt[s] = pool.get<float>(static_cast<size_t>(o) * nck);
-        for (int k = 0; k < AV_COUNT; ++k) {
+        for (int k = 0; k < nparts; ++k) {
             if (len[k] == 0) continue;
-            float* live = k < 5 ? h->f[fields[k]] : h->psi[psiSlot[k - 5]];
+            float* live = k < nf ? h->f[fields[k]] : h->psi[psiSlot[k - nf]];
             toView.push_back({live, a.view + off[k], len[k], 0, o});
             toCkpt.push_back({live, ckpt[s] + off[k], len[k], 0, o});
             fromCkpt.push_back({ckpt[s] + off[k], live, len[k], o, 0});
@@ -1024,7 +682,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             // two kernels per step: the third stage of step n (the transposed
             // derivatives of the first-pass inputs) runs inside the first kernel
             // of step n - 1; after step 0 it is not needed
-            const int first = A[0].tm ? 3 : A[0].sh ? 5 : A[0].te ? 7 : 0;
+            const int first = A[0].e3 ? 9 : A[0].tm ? 3 : A[0].sh ? 5 : A[0].te ? 7 : 0;
             const int pending = n < NT - 1 ? 1 : 0;
             launch_adj(H, first, dP, dA, dT, sched, grid, n - n0, pending, st);
             launch_adj(H, first + 1, dP, dA, dT, sched, grid, n - n0, pending, st);
@@ -1036,7 +694,9 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         wave_handle* h = shots[s];
         PrepParams G{h->NX, h->NY, h->NZ, h->N};
         const int o = sum ? 0 : s;
-        if (A[s].tm)
+        if (A[s].e3)
+            adj_e3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
+        else if (A[s].tm)
             adj_tm_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
                                                sum && s > 0 ? 1 : 0);
         else if (A[s].sh)

@@ -1,0 +1,635 @@
+// adjoint.cuh — the adjoint's saved-state layout, per-shot descriptor and
+// per-point transposed step bodies, shared by the host driver (adjoint.cu)
+// and the translation units that instantiate the per-pass kernels
+// (adjoint_pass2d.cu, adjoint_pass3d.cu).
+#pragma once
+
+#include "handle.h"
+#include "stencil.cuh"
+
+namespace wave {
+
+// parts of one saved state, in view order (2-D: five field parts, then eight
+// psi parts; absent parts have length 0)
+enum AdjPart { AV_VX, AV_VY, AV_SXX, AV_SYY, AV_SXY, AV_P1, AV_P2, AV_P3, AV_P4, AV_Q1, AV_Q2, AV_Q3, AV_Q4, AV_COUNT };
+// 3-D elastic: nine field parts, the nine velocity-pass psi (P0..P8) and the
+// nine stress-pass psi (Q0..Q8)
+enum Adj3Part {
+    E3_VX, E3_VY, E3_VZ, E3_SXX, E3_SYY, E3_SZZ, E3_SXY, E3_SXZ, E3_SYZ,
+    E3_P0, E3_Q0 = E3_P0 + 9, E3_COUNT = E3_Q0 + 9
+};
+constexpr int kAdjMaxParts = E3_COUNT;
+
+// psi slot of each psi part: velocity pass P1..P4, stress pass Q1..Q4
+static const int kAdjPsiSlot[8] = {PS_SXX_X, PS_SXY_Y, PS_SXY_X, PS_SYY_Y, PS_VXX, PS_VYY, PS_VXY, PS_VYX};
+
+struct AdjShot {
+    float* view;                 // recompute buffer: K+1 states
+    long long stride;            // floats per state
+    long long off[kAdjMaxParts]; // part offsets within a state (0 = absent psi)
+    float* lf[9];                // adjoint fields (2-D elastic: vx, vy, sxx, syy, sxy)
+    float* lpsi[18];             // adjoint psi (slab layout of the forward psi)
+    float* T[18];                // adjoints of the raw derivatives (2-D elastic: c1..c4, a1..a4)
+    float* g[8];                 // material adjoints (2-D elastic: dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry)
+    const long long* ridx;
+    const int* rtype;
+    const float* res;            // residual d - d_obs, nrec x nt
+    int nrec, nt;
+    int tm;                      // 1: lossless 2-D TMz (parts: hx, hy, ez; psi ezy, ezx, hyx, hxy)
+    int sh;                      // 1: 2-D SH (parts: vz, sxz, syz; psi sxz_x, syz_y, vzx, vzy)
+    int te;                      // 1: lossless 2-D TEz (parts: hz, ex, ey; psi eyx, exy, hzy, hzx)
+    int e3;                      // 1: 3-D elastic (Adj3Part layout)
+    float* vprime[3];            // vx', vy' [, vz'] (TMz: hx', hy') of the current step (null: the saved state's are they)
+    const long long* sidx;       // sources (velocity sources are taken out of v')
+    const int* stype;
+    const float* signals;        // nsrc x nt
+    int nsrc;
+};
+
+// launches one adjoint pass over the (shot, tile) work list: 2-D passes 0, 1
+// (elastic), 3, 4 (TMz), 5, 6 (SH), 7, 8 (TEz); 3-D passes 9, 10 (elastic)
+void launch_adj_pass2d(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid,
+                       int vn, int pending, cudaStream_t s);
+void launch_adj_pass3d(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid,
+                       int vn, int pending, cudaStream_t s);
+
+namespace adj {
+
+
+// (D^T lam)[c] = sum_k w_{c-k}(k) lam[c-k] over the rows c-k inside the axis,
+// with the row weights of deriv(): interior weights or the edge-table row
+template <int H, bool FWD>
+__device__ __forceinline__ float derivT(const float* __restrict__ lam, long long i, long long st, int c, const Op1D& op)
+{
+    float s = 0.0f;
+    if (!op.full && c - H >= op.E && c + H < op.n - op.E) {
+        // every row c-k is an interior row: its weight at offset k is the interior weight
+#pragma unroll
+        for (int k = (FWD ? -H + 1 : -H); k <= (FWD ? H : H - 1); ++k) s += op.w[kMaxHalf + k] * __ldg(lam + i - k * st);
+        return s;
+    }
+#pragma unroll
+    for (int k = -H; k <= H; ++k) {
+        const int r = c - k;
+        if (r < 0 || r >= op.n) continue;
+        float w;
+        if (!op.full && r >= op.E && r < op.n - op.E) {
+            w = op.w[kMaxHalf + k];
+        } else {
+            const int slot = op.full ? r : (r < op.E ? r : op.E + r - (op.n - op.E));
+            w = __ldg(op.tab + slot * kTabW + kMaxHalf + k);
+        }
+        if (w != 0.0f) s += w * __ldg(lam + i - k * st);
+    }
+    return s;
+}
+
+// adjoint of (c, Q) -> (c' = (1 + a) c + b Q, Q' = a c + b Q)
+__device__ __forceinline__ void cpml_adj(float& l, float* lpsi, float a, float b)
+{
+    const float lq = *lpsi;
+    const float lc = (1.0f + a) * l + a * lq;
+    *lpsi = b * (l + lq);
+    l = lc;
+}
+
+struct Slabs {
+    int sx, sy, sz;
+    long long px, py, pz;
+};
+
+__device__ __forceinline__ Slabs slabs_of(const StepParams& P, const Pt& p)
+{
+    Slabs S;
+    S.sx = P.useCpml ? slab(p.x, P.cx) : -1;
+    S.sy = P.useCpml ? slab(p.y, P.cy) : -1;
+    S.sz = (P.useCpml && P.is3d) ? slab(p.z, P.cz) : -1;
+    S.px = S.sx >= 0 ? pix(P, p, S.sx) : 0;
+    S.py = S.sy >= 0 ? piy(P, p, S.sy) : 0;
+    S.pz = S.sz >= 0 ? piz(P, p, S.sz) : 0;
+    return S;
+}
+
+// stress-pass transpose at step n (state n = view vn, state n+1 = view vn+1)
+template <int H>
+__device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float* vx1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
+    const float* vy1 = A.vprime[1] ? A.vprime[1] : X1 + A.off[AV_VY];
+    const float M = __ldg(P.m[M_M] + i), mu = __ldg(P.m[M_MU] + i), mxy = __ldg(P.m[M_MUXY] + i);
+    const Slabs S = slabs_of(P, p);
+    // forward derivatives with their CPML correction, c' = c + Q_{n+1}
+    float c1 = deriv<H, false>(vx1, i, 1, p.x, P.Dxb);
+    float c2 = deriv<H, false>(vy1, i, sy, p.y, P.Dyb);
+    float c3 = deriv<H, true>(vx1, i, sy, p.y, P.Dyf);
+    float c4 = deriv<H, true>(vy1, i, 1, p.x, P.Dxf);
+    if (S.sx >= 0) { c1 += X1[A.off[AV_Q1] + S.px]; c4 += X1[A.off[AV_Q4] + S.px]; }
+    if (S.sy >= 0) { c2 += X1[A.off[AV_Q2] + S.py]; c3 += X1[A.off[AV_Q3] + S.py]; }
+    float lxx = A.lf[2][i], lyy = A.lf[3][i], lxy = A.lf[4][i];
+    if (pending) {
+        // the transposed velocity-pass derivatives of sigma from the step after
+        // this one (its third stage, folded in here to save a launch)
+        const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
+        const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
+        lxx += derivT<H, true>(A.T[4], i, 1, p.x, P.Dxf);
+        float u = derivT<H, false>(A.T[5], i, sy, p.y, DybS);
+        u += derivT<H, false>(A.T[6], i, 1, p.x, P.Dxb);
+        lxy += u;
+        lyy += derivT<H, true>(A.T[7], i, sy, p.y, DyfS);
+    }
+    if (P.abs) {
+        // the taper multiplied all five fields last: their adjoints first
+        const float d = absDamp(P, p);
+        lxx *= d; lyy *= d; lxy *= d;
+        A.lf[0][i] *= d;
+        A.lf[1][i] *= d;
+    }
+    const bool fsRow = P.fs && p.y == 0;
+    if (fsRow) lyy = 0.0f;                 // syy' = 0 on the surface
+    A.lf[2][i] = lxx;
+    A.lf[3][i] = lyy;
+    A.lf[4][i] = lxy;
+    const float lam = M - 2.0f * mu;
+    float l1 = M * lxx + lam * lyy;
+    float l2 = lam * lxx + M * lyy;
+    float l3 = mxy * lxy, l4 = l3;
+    if (fsRow) {
+        // sxx' += sh c1' - sv c2' with sv = M - 2 mu, sh = -sv^2 / M
+        const float sv = lam, sh = -(sv * sv) / M;
+        l1 += sh * lxx;
+        l2 -= sv * lxx;
+        // dJ/dsh = lxx c1', dJ/dsv = -lxx c2' (c1, c2 carry their CPML correction here);
+        // d sv / dM = 1, d sv / dmu = -2; d sh / dM = -(2 sv / M - sv^2 / M^2), d sh / dmu = 4 sv / M
+        const float gh = lxx * c1, gv = -lxx * c2;
+        A.g[0][i] += gv - gh * (2.0f * sv / M - (sv * sv) / (M * M));
+        A.g[1][i] += -2.0f * gv + gh * 4.0f * sv / M;
+    }
+    if (S.sx >= 0) {
+        cpml_adj(l1, A.lpsi[4] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // Q1 (vxx): x, full profile
+        cpml_adj(l4, A.lpsi[7] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // Q4 (vyx): x, half profile
+    }
+    if (S.sy >= 0) {
+        cpml_adj(l2, A.lpsi[5] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // Q2 (vyy): y, full profile
+        cpml_adj(l3, A.lpsi[6] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // Q3 (vxy): y, half profile
+    }
+    A.T[0][i] = l1;
+    A.T[1][i] = l2;
+    A.T[2][i] = l3;
+    A.T[3][i] = l4;
+    A.g[0][i] += (lxx + lyy) * (c1 + c2);
+    A.g[1][i] += -2.0f * (lxx * c2 + lyy * c1);
+    A.g[2][i] += lxy * (c3 + c4);
+}
+
+// velocity-pass transpose (and the transposed stress-pass derivatives of v)
+template <int H>
+__device__ __forceinline__ void adj_vel_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    float lvx = A.lf[0][i];
+    lvx += derivT<H, false>(A.T[0], i, 1, p.x, P.Dxb);
+    lvx += derivT<H, true>(A.T[2], i, sy, p.y, P.Dyf);
+    float lvy = A.lf[1][i];
+    lvy += derivT<H, false>(A.T[1], i, sy, p.y, P.Dyb);
+    lvy += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
+    const Slabs S = slabs_of(P, p);
+    const float *sxx = X0 + A.off[AV_SXX], *syy = X0 + A.off[AV_SYY], *sxy = X0 + A.off[AV_SXY];
+    const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
+    const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
+    float a1 = deriv<H, true>(sxx, i, 1, p.x, P.Dxf);
+    float a2 = deriv<H, false>(sxy, i, sy, p.y, DybS);
+    float a3 = deriv<H, false>(sxy, i, 1, p.x, P.Dxb);
+    float a4 = deriv<H, true>(syy, i, sy, p.y, DyfS);
+    if (S.sx >= 0) { a1 += X1[A.off[AV_P1] + S.px]; a3 += X1[A.off[AV_P3] + S.px]; }
+    if (S.sy >= 0) { a2 += X1[A.off[AV_P2] + S.py]; a4 += X1[A.off[AV_P4] + S.py]; }
+    const float irx = __ldg(P.m[M_IRX] + i), iry = __ldg(P.m[M_IRY] + i);
+    float l1 = irx * lvx, l2 = l1, l3 = iry * lvy, l4 = l3;
+    if (S.sx >= 0) {
+        cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // P1 (sxx_x): x, half profile
+        cpml_adj(l3, A.lpsi[2] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // P3 (sxy_x): x, full profile
+    }
+    if (S.sy >= 0) {
+        cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // P2 (sxy_y): y, full profile
+        cpml_adj(l4, A.lpsi[3] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // P4 (syy_y): y, half profile
+    }
+    A.T[4][i] = l1;
+    A.T[5][i] = l2;
+    A.T[6][i] = l3;
+    A.T[7][i] = l4;
+    A.lf[0][i] = lvx;
+    A.lf[1][i] = lvy;
+    A.g[3][i] += lvx * (a1 + a2);
+    A.g[4][i] += lvy * (a3 + a4);
+}
+
+
+// ---- lossless 2-D TMz --------------------------------------------------------
+// parts of a TMz state in the view: AV_VX = hx, AV_VY = hy, AV_SXX = ez,
+// AV_P1..AV_P4 = psi of ezy, ezx, hyx, hxy; lf[0..2] = adjoints of hx, hy, ez;
+// T[0..3] = adjoints of c1, c2, a1, a2; g[0..3] = dJ/dCa, dJ/dCb, dJ/diMyz, dJ/diMxz
+
+// E-update transpose at step n
+template <int H>
+__device__ __forceinline__ void adj_tm_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float* hx1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
+    const float* hy1 = A.vprime[1] ? A.vprime[1] : X1 + A.off[AV_VY];
+    const Slabs S = slabs_of(P, p);
+    float c1 = deriv<H, false>(hy1, i, 1, p.x, P.Dxb);
+    float c2 = deriv<H, false>(hx1, i, sy, p.y, P.Dyb);
+    if (S.sx >= 0) c1 += X1[A.off[AV_P3] + S.px];
+    if (S.sy >= 0) c2 += X1[A.off[AV_P4] + S.py];
+    float lez = A.lf[2][i];
+    if (pending) {
+        // the transposed H-update derivatives of ez from the step after this one
+        float u = derivT<H, true>(A.T[2], i, sy, p.y, P.Dyf);
+        u += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
+        lez += u;
+    }
+    if (P.abs) {
+        // the taper multiplied ez, hx and hy last: their adjoints first
+        const float d = absDamp(P, p);
+        lez *= d;
+        A.lf[0][i] *= d;
+        A.lf[1][i] *= d;
+    }
+    const float ca = __ldg(P.m[M_CAZ] + i), cb = __ldg(P.m[M_CBZ] + i);
+    float l1 = cb * lez, l2 = -l1;
+    A.g[0][i] += lez * X0[A.off[AV_SXX] + i];
+    A.g[1][i] += lez * (c1 - c2);
+    A.lf[2][i] = ca * lez;
+    if (S.sx >= 0) cpml_adj(l1, A.lpsi[2] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // hyx: x, full profile
+    if (S.sy >= 0) cpml_adj(l2, A.lpsi[3] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // hxy: y, full profile
+    A.T[0][i] = l1;
+    A.T[1][i] = l2;
+}
+
+// H-update transpose at step n (after the E transpose of every point)
+template <int H>
+__device__ __forceinline__ void adj_tm_h_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float lhy = A.lf[1][i] + derivT<H, false>(A.T[0], i, 1, p.x, P.Dxb);
+    const float lhx = A.lf[0][i] + derivT<H, false>(A.T[1], i, sy, p.y, P.Dyb);
+    const float* ez0 = X0 + A.off[AV_SXX];
+    const Slabs S = slabs_of(P, p);
+    float a1 = deriv<H, true>(ez0, i, sy, p.y, P.Dyf);
+    float a2 = deriv<H, true>(ez0, i, 1, p.x, P.Dxf);
+    if (S.sy >= 0) a1 += X1[A.off[AV_P1] + S.py];
+    if (S.sx >= 0) a2 += X1[A.off[AV_P2] + S.px];
+    const float imyz = __ldg(P.m[M_IMUYZ] + i), imxz = __ldg(P.m[M_IMUXZ] + i);
+    float l1 = -imyz * lhx, l2 = imxz * lhy;
+    A.g[2][i] += -lhx * a1;
+    A.g[3][i] += lhy * a2;
+    if (S.sy >= 0) cpml_adj(l1, A.lpsi[0] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // ezy: y, half profile
+    if (S.sx >= 0) cpml_adj(l2, A.lpsi[1] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // ezx: x, half profile
+    A.T[2][i] = l1;
+    A.T[3][i] = l2;
+    A.lf[0][i] = lhx;
+    A.lf[1][i] = lhy;
+}
+
+
+// ---- 2-D SH ---------------------------------------------------------------
+// parts of an SH state in the view: AV_VX = vz, AV_SXX = sxz, AV_SYY = syz,
+// AV_P1, AV_P2 = psi of sxz_x, syz_y, AV_Q1, AV_Q2 = psi of vzx, vzy;
+// lf[0], lf[2], lf[3] = adjoints of vz, sxz, syz; T[0..1] = adjoints of the
+// stress-pass derivatives c1, c2, T[2..3] of the velocity-pass ones a1, a2;
+// g[0..2] = dJ/dmuXZ, dJ/dmuYZ, dJ/dirho
+
+// stress-update transpose at step n
+template <int H>
+__device__ __forceinline__ void adj_sh_s_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float* vz1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
+    const Slabs S = slabs_of(P, p);
+    float c1 = deriv<H, true>(vz1, i, 1, p.x, P.Dxf);
+    float c2 = deriv<H, true>(vz1, i, sy, p.y, P.Dyf);
+    if (S.sx >= 0) c1 += X1[A.off[AV_Q1] + S.px];
+    if (S.sy >= 0) c2 += X1[A.off[AV_Q2] + S.py];
+    float lxz = A.lf[2][i], lyz = A.lf[3][i];
+    if (pending) {
+        // the transposed velocity-update derivatives of the stresses from the step after this one
+        lxz += derivT<H, false>(A.T[2], i, 1, p.x, P.Dxb);
+        lyz += derivT<H, false>(A.T[3], i, sy, p.y, P.fs ? P.DybS : P.Dyb);
+    }
+    if (P.abs) {
+        // the taper multiplied sxz, syz and vz last: their adjoints first
+        const float d = absDamp(P, p);
+        lxz *= d;
+        lyz *= d;
+        A.lf[0][i] *= d;
+    }
+    A.lf[2][i] = lxz;
+    A.lf[3][i] = lyz;
+    float l1 = __ldg(P.m[M_MUXZ] + i) * lxz, l2 = __ldg(P.m[M_MUYZ] + i) * lyz;
+    A.g[0][i] += lxz * c1;
+    A.g[1][i] += lyz * c2;
+    if (S.sx >= 0) cpml_adj(l1, A.lpsi[4] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // vzx: x, half profile
+    if (S.sy >= 0) cpml_adj(l2, A.lpsi[5] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // vzy: y, half profile
+    A.T[0][i] = l1;
+    A.T[1][i] = l2;
+}
+
+// velocity-update transpose at step n (after the stress transpose of every point)
+template <int H>
+__device__ __forceinline__ void adj_sh_v_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    float lvz = A.lf[0][i];
+    lvz += derivT<H, true>(A.T[0], i, 1, p.x, P.Dxf);
+    lvz += derivT<H, true>(A.T[1], i, sy, p.y, P.Dyf);
+    const Slabs S = slabs_of(P, p);
+    float a1 = deriv<H, false>(X0 + A.off[AV_SXX], i, 1, p.x, P.Dxb);
+    float a2 = deriv<H, false>(X0 + A.off[AV_SYY], i, sy, p.y, P.fs ? P.DybS : P.Dyb);
+    if (S.sx >= 0) a1 += X1[A.off[AV_P1] + S.px];
+    if (S.sy >= 0) a2 += X1[A.off[AV_P2] + S.py];
+    const float ir = __ldg(P.m[M_IR] + i);
+    float l1 = ir * lvz, l2 = l1;
+    A.g[2][i] += lvz * (a1 + a2);
+    if (S.sx >= 0) cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // sxz_x: x, full profile
+    if (S.sy >= 0) cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // syz_y: y, full profile
+    A.T[2][i] = l1;
+    A.T[3][i] = l2;
+    A.lf[0][i] = lvz;
+}
+
+
+// ---- lossless 2-D TEz -------------------------------------------------------
+// parts of a TEz state in the view: AV_VX = hz, AV_SXX = ex, AV_SYY = ey,
+// AV_P1, AV_P2 = psi of eyx, exy, AV_Q1, AV_Q2 = psi of hzy, hzx; lf[0], lf[2],
+// lf[3] = adjoints of hz, ex, ey; T[0..1] = adjoints of the E-update
+// derivatives c1, c2, T[2..3] of the H-update ones a1, a2; g[0..4] = dJ/dCaX,
+// dJ/dCbX, dJ/dCaY, dJ/dCbY, dJ/diMxy
+
+// E-update transpose at step n
+template <int H>
+__device__ __forceinline__ void adj_te_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    const float* hz1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[AV_VX];
+    const Slabs S = slabs_of(P, p);
+    float c1 = deriv<H, false>(hz1, i, sy, p.y, P.Dyb);
+    float c2 = deriv<H, false>(hz1, i, 1, p.x, P.Dxb);
+    if (S.sy >= 0) c1 += X1[A.off[AV_Q1] + S.py];
+    if (S.sx >= 0) c2 += X1[A.off[AV_Q2] + S.px];
+    float lex = A.lf[2][i], ley = A.lf[3][i];
+    if (pending) {
+        // the transposed H-update derivatives of ey and ex from the step after this one
+        ley += derivT<H, true>(A.T[2], i, 1, p.x, P.Dxf);
+        lex += derivT<H, true>(A.T[3], i, sy, p.y, P.Dyf);
+    }
+    if (P.abs) {
+        // the taper multiplied ey, ex and hz last: their adjoints first
+        const float d = absDamp(P, p);
+        lex *= d;
+        ley *= d;
+        A.lf[0][i] *= d;
+    }
+    const float cax = __ldg(P.m[M_CAX] + i), cbx = __ldg(P.m[M_CBX] + i);
+    const float cay = __ldg(P.m[M_CAY] + i), cby = __ldg(P.m[M_CBY] + i);
+    A.g[0][i] += lex * X0[A.off[AV_SXX] + i];
+    A.g[1][i] += lex * c1;
+    A.g[2][i] += ley * X0[A.off[AV_SYY] + i];
+    A.g[3][i] -= ley * c2;
+    float l1 = cbx * lex, l2 = -cby * ley;
+    A.lf[2][i] = cax * lex;
+    A.lf[3][i] = cay * ley;
+    if (S.sy >= 0) cpml_adj(l1, A.lpsi[4] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // hzy: y, full profile
+    if (S.sx >= 0) cpml_adj(l2, A.lpsi[5] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // hzx: x, full profile
+    A.T[0][i] = l1;
+    A.T[1][i] = l2;
+}
+
+// H-update transpose at step n (after the E transpose of every point)
+template <int H>
+__device__ __forceinline__ void adj_te_h_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = P.NX;
+    float lhz = A.lf[0][i];
+    lhz += derivT<H, false>(A.T[0], i, sy, p.y, P.Dyb);
+    lhz += derivT<H, false>(A.T[1], i, 1, p.x, P.Dxb);
+    const Slabs S = slabs_of(P, p);
+    float a1 = deriv<H, true>(X0 + A.off[AV_SYY], i, 1, p.x, P.Dxf);
+    float a2 = deriv<H, true>(X0 + A.off[AV_SXX], i, sy, p.y, P.Dyf);
+    if (S.sx >= 0) a1 += X1[A.off[AV_P1] + S.px];
+    if (S.sy >= 0) a2 += X1[A.off[AV_P2] + S.py];
+    const float im = __ldg(P.m[M_IMUXY] + i);
+    float l1 = -im * lhz, l2 = im * lhz;
+    A.g[4][i] -= lhz * (a1 - a2);
+    if (S.sx >= 0) cpml_adj(l1, A.lpsi[0] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // eyx: x, half profile
+    if (S.sy >= 0) cpml_adj(l2, A.lpsi[1] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // exy: y, half profile
+    A.T[2][i] = l1;
+    A.T[3][i] = l2;
+    A.lf[0][i] = lhz;
+}
+
+
+// ---- 3-D elastic -------------------------------------------------------------
+// lf[0..8] = adjoints of vx, vy, vz, sxx, syy, szz, sxy, sxz, syz; lpsi[0..8]
+// of the velocity-pass psi P0..P8 (sxx_x, sxy_y, sxz_z, sxy_x, syy_y, syz_z,
+// sxz_x, syz_y, szz_z), lpsi[9..17] of the stress-pass psi Q0..Q8 (vxx, vyy,
+// vzz, vxy, vyx, vxz, vzx, vyz, vzy); T[0..8] = adjoints of the stress-pass
+// derivatives c0..c8, T[9..17] of the velocity-pass ones a0..a8; g[0..7] =
+// dJ/dM, dJ/dmu, dJ/dmuXY, dJ/dmuXZ, dJ/dmuYZ, dJ/dirx, dJ/diry, dJ/dirz
+
+// psi of the x, y or z slab at this point (0 outside the slabs or when absent)
+__device__ __forceinline__ float psi_at(const float* X, const AdjShot& A, int part, const Slabs& S, int axis)
+{
+    if (axis == 0) return S.sx >= 0 ? X[A.off[part] + S.px] : 0.0f;
+    if (axis == 1) return S.sy >= 0 ? X[A.off[part] + S.py] : 0.0f;
+    return S.sz >= 0 ? X[A.off[part] + S.pz] : 0.0f;
+}
+
+__device__ __forceinline__ void cpml_adj_axis(const StepParams& P, const Pt& p, const Slabs& S, float& l, float* lpsi, int axis,
+                                              bool half)
+{
+    if (axis == 0) {
+        if (S.sx >= 0) cpml_adj(l, lpsi + S.px, half ? P.cx.a_half[p.x] : P.cx.a_full[p.x], half ? P.cx.b_half[p.x] : P.cx.b_full[p.x]);
+    } else if (axis == 1) {
+        if (S.sy >= 0) cpml_adj(l, lpsi + S.py, half ? P.cy.a_half[p.y] : P.cy.a_full[p.y], half ? P.cy.b_half[p.y] : P.cy.b_full[p.y]);
+    } else {
+        if (S.sz >= 0) cpml_adj(l, lpsi + S.pz, half ? P.cz.a_half[p.z] : P.cz.a_full[p.z], half ? P.cz.b_half[p.z] : P.cz.b_full[p.z]);
+    }
+}
+
+// axis and half-grid profile of each velocity-pass derivative a0..a8 and the
+// axis of each stress-pass derivative c0..c8 (forward derivatives on the half grid)
+__host__ __device__ constexpr int e3_a_axis(int k) { return k % 3; }
+__host__ __device__ constexpr bool e3_a_half(int k) { return k == 0 || k == 4 || k == 8; }
+__host__ __device__ constexpr int e3_c_axis(int k) { return k == 0 || k == 4 || k == 6 ? 0 : k == 1 || k == 3 || k == 8 ? 1 : 2; }
+
+// stress-update transpose at step n
+template <int H>
+__device__ __forceinline__ void adj_e3_s_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
+    const long long i = p.i, sy = (long long)P.NX * P.NZ, sz = P.NX;
+    const float* vx1 = A.vprime[0] ? A.vprime[0] : X1 + A.off[E3_VX];
+    const float* vy1 = A.vprime[0] ? A.vprime[1] : X1 + A.off[E3_VY];
+    const float* vz1 = A.vprime[0] ? A.vprime[2] : X1 + A.off[E3_VZ];
+    const Slabs S = slabs_of(P, p);
+    float c[9];
+    c[0] = deriv<H, false>(vx1, i, 1, p.x, P.Dxb);
+    c[1] = deriv<H, false>(vy1, i, sy, p.y, P.Dyb);
+    c[2] = deriv<H, false>(vz1, i, sz, p.z, P.Dzb);
+    c[3] = deriv<H, true>(vx1, i, sy, p.y, P.Dyf);
+    c[4] = deriv<H, true>(vy1, i, 1, p.x, P.Dxf);
+    c[5] = deriv<H, true>(vx1, i, sz, p.z, P.Dzf);
+    c[6] = deriv<H, true>(vz1, i, 1, p.x, P.Dxf);
+    c[7] = deriv<H, true>(vy1, i, sz, p.z, P.Dzf);
+    c[8] = deriv<H, true>(vz1, i, sy, p.y, P.Dyf);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) c[k] += psi_at(X1, A, E3_Q0 + k, S, e3_c_axis(k));
+    float lxx = A.lf[3][i], lyy = A.lf[4][i], lzz = A.lf[5][i], lxy = A.lf[6][i], lxz = A.lf[7][i], lyz = A.lf[8][i];
+    if (pending) {
+        // the transposed velocity-pass derivatives of the stresses from the step after this one
+        const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
+        const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
+        lxx += derivT<H, true>(A.T[9], i, 1, p.x, P.Dxf);
+        lxy += derivT<H, false>(A.T[10], i, sy, p.y, DybS);
+        lxz += derivT<H, false>(A.T[11], i, sz, p.z, P.Dzb);
+        lxy += derivT<H, false>(A.T[12], i, 1, p.x, P.Dxb);
+        lyy += derivT<H, true>(A.T[13], i, sy, p.y, DyfS);
+        lyz += derivT<H, false>(A.T[14], i, sz, p.z, P.Dzb);
+        lxz += derivT<H, false>(A.T[15], i, 1, p.x, P.Dxb);
+        lyz += derivT<H, false>(A.T[16], i, sy, p.y, DybS);
+        lzz += derivT<H, true>(A.T[17], i, sz, p.z, P.Dzf);
+    }
+    if (P.abs) {
+        // the taper multiplied all nine fields last: their adjoints first
+        const float d = absDamp(P, p);
+        lxx *= d; lyy *= d; lzz *= d; lxy *= d; lxz *= d; lyz *= d;
+        A.lf[0][i] *= d;
+        A.lf[1][i] *= d;
+        A.lf[2][i] *= d;
+    }
+    const bool fsRow = P.fs && p.y == 0;
+    if (fsRow) lyy = 0.0f;   // syy' = 0 on the surface
+    A.lf[3][i] = lxx;
+    A.lf[4][i] = lyy;
+    A.lf[5][i] = lzz;
+    A.lf[6][i] = lxy;
+    A.lf[7][i] = lxz;
+    A.lf[8][i] = lyz;
+    const float M = __ldg(P.m[M_M] + i), mu = __ldg(P.m[M_MU] + i);
+    const float ls = lxx + lyy + lzz;
+    float l[9];
+    l[0] = M * ls - 2.0f * mu * (lyy + lzz);
+    l[1] = M * ls - 2.0f * mu * (lxx + lzz);
+    l[2] = M * ls - 2.0f * mu * (lxx + lyy);
+    l[3] = l[4] = __ldg(P.m[M_MUXY] + i) * lxy;
+    l[5] = l[6] = __ldg(P.m[M_MUXZ] + i) * lxz;
+    l[7] = l[8] = __ldg(P.m[M_MUYZ] + i) * lyz;
+    A.g[0][i] += ls * (c[0] + c[1] + c[2]);
+    A.g[1][i] += -2.0f * (lxx * (c[1] + c[2]) + lyy * (c[0] + c[2]) + lzz * (c[0] + c[1]));
+    A.g[2][i] += lxy * (c[3] + c[4]);
+    A.g[3][i] += lxz * (c[5] + c[6]);
+    A.g[4][i] += lyz * (c[7] + c[8]);
+    if (fsRow) {
+        // sxx', szz' += sh (c0' + c2') - sv c1' with sv = M - 2 mu, sh = -sv^2 / M
+        const float sv = M - 2.0f * mu, sh = -(sv * sv) / M, hs = lxx + lzz;
+        l[0] += sh * hs;
+        l[2] += sh * hs;
+        l[1] -= sv * hs;
+        const float gh = hs * (c[0] + c[2]), gv = -hs * c[1];
+        A.g[0][i] += gv - gh * (2.0f * sv / M - (sv * sv) / (M * M));
+        A.g[1][i] += -2.0f * gv + gh * 4.0f * sv / M;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        // stress-pass psi: backward derivatives (c0..c2) on the full grid, the cross ones on the half grid
+        cpml_adj_axis(P, p, S, l[k], A.lpsi[9 + k], e3_c_axis(k), k >= 3);
+        A.T[k][i] = l[k];
+    }
+}
+
+// velocity-update transpose at step n (after the stress transpose of every point)
+template <int H>
+__device__ __forceinline__ void adj_e3_v_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = (long long)P.NX * P.NZ, sz = P.NX;
+    float lvx = A.lf[0][i], lvy = A.lf[1][i], lvz = A.lf[2][i];
+    lvx += derivT<H, false>(A.T[0], i, 1, p.x, P.Dxb);
+    lvx += derivT<H, true>(A.T[3], i, sy, p.y, P.Dyf);
+    lvx += derivT<H, true>(A.T[5], i, sz, p.z, P.Dzf);
+    lvy += derivT<H, false>(A.T[1], i, sy, p.y, P.Dyb);
+    lvy += derivT<H, true>(A.T[4], i, 1, p.x, P.Dxf);
+    lvy += derivT<H, true>(A.T[7], i, sz, p.z, P.Dzf);
+    lvz += derivT<H, false>(A.T[2], i, sz, p.z, P.Dzb);
+    lvz += derivT<H, true>(A.T[6], i, 1, p.x, P.Dxf);
+    lvz += derivT<H, true>(A.T[8], i, sy, p.y, P.Dyf);
+    const Slabs S = slabs_of(P, p);
+    const Op1D& DybS = P.fs ? P.DybS : P.Dyb;
+    const Op1D& DyfS = P.fs ? P.DyfS : P.Dyf;
+    const float *sxx = X0 + A.off[E3_SXX], *syy = X0 + A.off[E3_SYY], *szz = X0 + A.off[E3_SZZ];
+    const float *sxy = X0 + A.off[E3_SXY], *sxz = X0 + A.off[E3_SXZ], *syz = X0 + A.off[E3_SYZ];
+    float a[9];
+    a[0] = deriv<H, true>(sxx, i, 1, p.x, P.Dxf);
+    a[1] = deriv<H, false>(sxy, i, sy, p.y, DybS);
+    a[2] = deriv<H, false>(sxz, i, sz, p.z, P.Dzb);
+    a[3] = deriv<H, false>(sxy, i, 1, p.x, P.Dxb);
+    a[4] = deriv<H, true>(syy, i, sy, p.y, DyfS);
+    a[5] = deriv<H, false>(syz, i, sz, p.z, P.Dzb);
+    a[6] = deriv<H, false>(sxz, i, 1, p.x, P.Dxb);
+    a[7] = deriv<H, false>(syz, i, sy, p.y, DybS);
+    a[8] = deriv<H, true>(szz, i, sz, p.z, P.Dzf);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a[k] += psi_at(X1, A, E3_P0 + k, S, e3_a_axis(k));
+    const float irx = __ldg(P.m[M_IRX] + i), iry = __ldg(P.m[M_IRY] + i), irz = __ldg(P.m[M_IRZ] + i);
+    A.g[5][i] += lvx * (a[0] + a[1] + a[2]);
+    A.g[6][i] += lvy * (a[3] + a[4] + a[5]);
+    A.g[7][i] += lvz * (a[6] + a[7] + a[8]);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        float l = (k < 3 ? irx * lvx : k < 6 ? iry * lvy : irz * lvz);
+        cpml_adj_axis(P, p, S, l, A.lpsi[k], e3_a_axis(k), e3_a_half(k));
+        A.T[9 + k][i] = l;
+    }
+    A.lf[0][i] = lvx;
+    A.lf[1][i] = lvy;
+    A.lf[2][i] = lvz;
+}
+
+
+template <int H, int PASS>
+__global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
+                                                const BatchTile* __restrict__ W, BatchSched S, int vn, int pending)
+{
+    BATCH_SHARED_PARAMS(sP);
+    batch_loop(Ps, W, S, sP, [&](const StepParams& P, const Pt& p, int shot) {
+        const AdjShot& A = As[shot];
+        if (PASS == 0) adj_stress_body<H>(P, A, p, vn, pending != 0);
+        else if (PASS == 1) adj_vel_body<H>(P, A, p, vn);
+        else if (PASS == 3) adj_tm_e_body<H>(P, A, p, vn, pending != 0);
+        else if (PASS == 4) adj_tm_h_body<H>(P, A, p, vn);
+        else if (PASS == 5) adj_sh_s_body<H>(P, A, p, vn, pending != 0);
+        else if (PASS == 6) adj_sh_v_body<H>(P, A, p, vn);
+        else if (PASS == 7) adj_te_e_body<H>(P, A, p, vn, pending != 0);
+        else if (PASS == 8) adj_te_h_body<H>(P, A, p, vn);
+        else if (PASS == 9) adj_e3_s_body<H>(P, A, p, vn, pending != 0);
+        else adj_e3_v_body<H>(P, A, p, vn);
+    });
+}
+
+} // namespace adj
+} // namespace wave

@@ -1,0 +1,41 @@
+// adjoint_pass2d.cu — the per-pass adjoint kernels of the 2-D equations (elastic, TMz, SH, TEz), instantiated for
+// every FD half-order (a translation unit of its own so that the build
+// compiles the adjoint's kernels in parallel).
+#include "adjoint.cuh"
+
+namespace wave {
+namespace {
+
+template <int H>
+void launch_h(int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
+              int pending, cudaStream_t s)
+{
+    const dim3 block(32, 8, 1);
+    switch (pass) {
+    case 0: adj::adj_pass<H, 0><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 1: adj::adj_pass<H, 1><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 3: adj::adj_pass<H, 3><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 4: adj::adj_pass<H, 4><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 5: adj::adj_pass<H, 5><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 6: adj::adj_pass<H, 6><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    case 7: adj::adj_pass<H, 7><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    default: adj::adj_pass<H, 8><<<grid, block, 0, s>>>(Ps, As, W, S, vn, pending); break;
+    }
+}
+
+} // namespace
+
+void launch_adj_pass2d(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
+                       int pending, cudaStream_t s)
+{
+    switch (H) {
+    case 1: launch_h<1>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    case 2: launch_h<2>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    case 3: launch_h<3>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    case 4: launch_h<4>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    case 5: launch_h<5>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    default: launch_h<6>(pass, Ps, As, W, S, grid, vn, pending, s); break;
+    }
+}
+
+} // namespace wave

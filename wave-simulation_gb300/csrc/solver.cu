@@ -776,7 +776,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
             }
         }
         h->check(cudaMemcpyAsync(mat(M_RHO), dRho, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
-        if (eq == WAVE_EQ_ELASTIC && !is3d) {
+        if (eq == WAVE_EQ_ELASTIC) {
             h->check(cudaMemcpyAsync(mat(M_VP), dVp, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
             h->check(cudaMemcpyAsync(mat(M_VS), dVs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         }
