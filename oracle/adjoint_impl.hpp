@@ -109,9 +109,13 @@ struct ElasticAdjoint2D {
     static constexpr const char* kP[4] = {"sxx_x", "sxy_y", "sxy_x", "syy_y"};
     static constexpr const char* kQ[4] = {"vxx", "vyy", "vxy", "vyx"};
 
-    explicit ElasticAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    const bool visco;   // 2-D visco-elastic (FD2Dviscoelastic::run, ForwardSolver2Dviscoelastic.cpp:130-321)
+
+    explicit ElasticAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N()), visco(sim.eq == WAVE_EQ_VISCOELASTIC)
     {
-        if (s.is3d || s.eq != WAVE_EQ_ELASTIC) throw std::invalid_argument("oracle adjoint: 2-D elastic only");
+        if (s.is3d || (s.eq != WAVE_EQ_ELASTIC && s.eq != WAVE_EQ_VISCOELASTIC))
+            throw std::invalid_argument("oracle adjoint: 2-D elastic or visco-elastic only");
+        if (visco && s.fs) throw std::invalid_argument("oracle adjoint: the visco-elastic free surface is not differentiated");
         DxfT = transpose(s.Dxf);
         DxbT = transpose(s.Dxb);
         DyfT = transpose(s.Dyf);
@@ -122,12 +126,14 @@ struct ElasticAdjoint2D {
 
     struct State {
         std::map<std::string, std::vector<T>> F, psi;
+        std::map<std::string, std::vector<std::vector<T>>> R;
     };
-    State save() const { return {s.F, s.psi}; }
+    State save() const { return {s.F, s.psi, s.R}; }
     void load(const State& x)
     {
         s.F = x.F;
         s.psi = x.psi;
+        s.R = x.R;
     }
     const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
     {
@@ -182,6 +188,8 @@ struct ElasticAdjoint2D {
         std::map<std::string, std::vector<T>> lF, lpsi;
         for (const char* n : {"vx", "vy", "sxx", "syy", "sxy"}) lF[n].assign(N, 0);
         for (int k = 0; k < 4; ++k) { lpsi[kP[k]].assign(N, 0); lpsi[kQ[k]].assign(N, 0); }
+        // adjoint memory variables rxx, ryy, rxy per mechanism (visco)
+        std::vector<std::vector<std::vector<T>>> lR(3, std::vector<std::vector<T>>(visco ? s.L : 0, std::vector<T>(N, 0)));
         std::vector<T> gM(N, 0), gMu(N, 0), gMuXY(N, 0), gIrx(N, 0), gIry(N, 0);
         std::vector<T> a[4], c[4], vxp(N), vyp(N), la[4], lc[4];
         for (int k = 0; k < 4; ++k) { a[k].assign(N, 0); c[k].assign(N, 0); la[k].assign(N, 0); lc[k].assign(N, 0); }
@@ -262,19 +270,64 @@ struct ElasticAdjoint2D {
                         }
                     });
                 }
-                // sxy += muXY (c3' + c4')
-                for_n(N, [&](idx_t i) {
-                    lc[2][i] += s.muXY[i] * lxy[i];
-                    lc[3][i] += s.muXY[i] * lxy[i];
-                    gMuXY[i] += lxy[i] * (c[2][i] + c[3][i]);
-                });
-                // sxx += M (c1' + c2') - 2 mu c2', syy += M (c1' + c2') - 2 mu c1'
-                for_n(N, [&](idx_t i) {
-                    lc[0][i] += s.M[i] * (lxx[i] + lyy[i]) - T(2) * s.mu[i] * lyy[i];
-                    lc[1][i] += s.M[i] * (lxx[i] + lyy[i]) - T(2) * s.mu[i] * lxx[i];
-                    gM[i] += (lxx[i] + lyy[i]) * (c[0][i] + c[1][i]);
-                    gMu[i] += -T(2) * (lxx[i] * c[1][i] + lyy[i] * c[0][i]);
-                });
+                if (visco) {
+                    // per mechanism l, with e = c1' + c2', q = c2' (sxx) or c1' (syy), m = muXY (c3' + c4'):
+                    //   Rk' = c2_l (c1_l Rk - tauP M e / tau_l + tauS 2 mu q / tau_l)
+                    //   Sk' = Sk + DT/2 sum_l (Rk + Rk') + (1 + L tauP) M e - (1 + L tauS) 2 mu q
+                    //   Rxy' = c2_l (c1_l Rxy - tauSXY m / tau_l)
+                    //   Sxy' = Sxy + DT/2 sum_l (Rxy + Rxy') + (1 + L tauS) m
+                    const T DTh = s.DThalf;
+                    for_n(N, [&](idx_t i) {
+                        const T e = c[0][i] + c[1][i], M = s.M[i], mu = s.mu[i];
+                        const T tP = s.tauP[i], tS = s.tauS[i], opP = s.onePlusLtauP[i], opS = s.onePlusLtauS[i];
+                        T le = 0, lq[2] = {0, 0};
+                        for (int k = 0; k < 2; ++k) {
+                            const T lS = k == 0 ? lxx[i] : lyy[i];
+                            const T q = k == 0 ? c[1][i] : c[0][i];
+                            le += opP * M * lS;
+                            lq[k] -= opS * T(2) * mu * lS;
+                            gM[i] += opP * e * lS;
+                            gMu[i] -= opS * T(2) * q * lS;
+                            auto& lRk = lR[k];
+                            for (int l = 0; l < s.L; ++l) {
+                                const T c1 = s.viscoC1[l], c2 = s.viscoC2[l], irt = s.invRelaxTime[l];
+                                const T LR = lRk[l][i] + DTh * lS;   // adjoint of Rk'
+                                lRk[l][i] = c2 * c1 * LR + DTh * lS;
+                                le -= c2 * irt * tP * M * LR;
+                                lq[k] += c2 * irt * tS * T(2) * mu * LR;
+                                gM[i] -= c2 * irt * tP * e * LR;
+                                gMu[i] += c2 * irt * tS * T(2) * q * LR;
+                            }
+                        }
+                        lc[0][i] += le + lq[1];
+                        lc[1][i] += le + lq[0];
+                        const T lS = lxy[i], sh = c[2][i] + c[3][i];
+                        T lm = opS * lS;
+                        for (int l = 0; l < s.L; ++l) {
+                            const T c1 = s.viscoC1[l], c2 = s.viscoC2[l], irt = s.invRelaxTime[l];
+                            const T LR = lR[2][l][i] + DTh * lS;
+                            lR[2][l][i] = c2 * c1 * LR + DTh * lS;
+                            lm -= c2 * irt * s.tauSXY[i] * LR;
+                        }
+                        gMuXY[i] += sh * lm;
+                        lc[2][i] += s.muXY[i] * lm;
+                        lc[3][i] += s.muXY[i] * lm;
+                    });
+                } else {
+                    // sxy += muXY (c3' + c4')
+                    for_n(N, [&](idx_t i) {
+                        lc[2][i] += s.muXY[i] * lxy[i];
+                        lc[3][i] += s.muXY[i] * lxy[i];
+                        gMuXY[i] += lxy[i] * (c[2][i] + c[3][i]);
+                    });
+                    // sxx += M (c1' + c2') - 2 mu c2', syy += M (c1' + c2') - 2 mu c1'
+                    for_n(N, [&](idx_t i) {
+                        lc[0][i] += s.M[i] * (lxx[i] + lyy[i]) - T(2) * s.mu[i] * lyy[i];
+                        lc[1][i] += s.M[i] * (lxx[i] + lyy[i]) - T(2) * s.mu[i] * lxx[i];
+                        gM[i] += (lxx[i] + lyy[i]) * (c[0][i] + c[1][i]);
+                        gMu[i] += -T(2) * (lxx[i] * c[1][i] + lyy[i] * c[0][i]);
+                    });
+                }
                 for (int k = 0; k < 4; ++k) cpmlT(lc[k], lpsi[kQ[k]], kQ[k]);
                 // the undamped velocities vx', vy' feed c1..c4
                 spmv_add(DxbT, lc[0], lvx);
@@ -319,15 +372,27 @@ struct ElasticAdjoint2D {
         avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::X, in, out); }, y, grhoAvg);
         for_n(N, [&](idx_t r) { y[r] = -gIry[r] * s.invRhoY[r] * s.invRhoY[r]; });
         avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::Y, in, out); }, y, grhoAvg);
+        // visco: M = rho vp^2 / (1 + sum tauP), mu = rho vs^2 / (1 + sum tauS)
+        // (Viscoelastic.cpp:650-715), the relaxation times held fixed
+        T sum = 0;
+        if (visco) {
+            const T w_ref = static_cast<T>(2.0 * M_PI * s.cfg.CenterFrequencyCPML);
+            for (int l = 0; l < s.L; ++l) {
+                const T ts = static_cast<T>(1.0 / (2.0 * M_PI * static_cast<T>(s.cfg.relaxationFrequency[l])));
+                sum += w_ref * w_ref * ts * ts / (T(1.0) + w_ref * w_ref * ts * ts);
+            }
+        }
         for (idx_t k = 0; k < N; ++k) {
-            // M = rho vp^2; mu_c = max(rho vs^2, 1) (clamped values do not move)
+            // M = rho vp^2 / fP; mu_c = max(rho vs^2 / fS, 1) (clamped values do not move)
+            const T fP = visco ? T(1) + sum * s.tauP[k] : T(1), fS = visco ? T(1) + sum * s.tauS[k] : T(1);
             T raw = rho[k];
             raw *= vs[k];
             raw *= vs[k];
+            if (visco) raw = raw / fS;
             const bool unclamped = raw >= T(1);
-            gvp[k] = gM[k] * T(2) * rho[k] * vp[k];
-            gvs[k] = unclamped ? gmuc[k] * T(2) * rho[k] * vs[k] : T(0);
-            grho[k] = gM[k] * vp[k] * vp[k] + (unclamped ? gmuc[k] * vs[k] * vs[k] : T(0)) + grhoAvg[k];
+            gvp[k] = gM[k] * T(2) * rho[k] * vp[k] / fP;
+            gvs[k] = unclamped ? gmuc[k] * T(2) * rho[k] * vs[k] / fS : T(0);
+            grho[k] = gM[k] * vp[k] * vp[k] / fP + (unclamped ? gmuc[k] * vs[k] * vs[k] / fS : T(0)) + grhoAvg[k];
         }
     }
 };

@@ -358,7 +358,8 @@ class Oracle:
 
     def adjoint_gradient(self, dobs: np.ndarray, checkpoint_every: int = 50):
         """Misfit 1/2 sum (d - dobs)^2 and its gradients with respect to vp, vs
-        and rho (2-D and 3-D elastic; 2-D SH: the vp gradient is zero) or eps_r, sigma
+        and rho (2-D and 3-D elastic, 2-D visco-elastic with the relaxation
+        times held fixed; 2-D SH: the vp gradient is zero) or eps_r, sigma
         and mu_r (lossless 2-D TMz and TEz), by the oracle's own discrete adjoint
         (adjoint_impl.hpp) in this oracle's value type."""
         n = self.cfg.NX * self.cfg.NY * (self.cfg.NZ if self.cfg.dimension == 3 else 1)

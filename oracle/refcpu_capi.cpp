@@ -182,7 +182,8 @@ int refcpu_field(void* hv, const char* name, double* out)
 }
 
 // Gradient of J = 1/2 sum (d - dobs)^2 with respect to vp, vs, rho for a 2-D
-// or 3-D elastic simulation (adjoint_impl.hpp), in the handle's value type; dobs is
+// or 3-D elastic or a 2-D visco-elastic simulation (adjoint_impl.hpp; the
+// relaxation times held fixed), in the handle's value type; dobs is
 // nrec x NT. The model arrays are the ones the handle was created with. The
 // handle's state is left at the end of the forward run. Returns the misfit
 // through *misfit; 0 on success.

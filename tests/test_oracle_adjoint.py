@@ -11,18 +11,24 @@ import numpy as np
 import pytest
 
 
-def case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, seed=3, NX=44, NY=36, nt=160):
+def case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, seed=3, NX=44, NY=36, nt=160, L=0):
+    """2-D elastic survey; L > 0: visco-elastic with L relaxation mechanisms."""
     rng = np.random.default_rng(seed)
     y, x = np.mgrid[0:NY, 0:NX]
     vp = 2000.0 + 600.0 * (y / NY) + 80.0 * np.sin(x / 5.0) + 30 * rng.standard_normal((NY, NX))
     vs = vp / 1.75
     rho = 310.0 * vp ** 0.25
-    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(vp=vp, vs=vs, rho=rho).items()}
+    fields = dict(vp=vp, vs=vs, rho=rho)
+    if L:
+        fields["taup"] = 0.04 + 0.01 * np.sin(x / 6.0) + 0.005 * (y / NY)
+        fields["taus"] = 0.05 + 0.01 * np.cos(y / 5.0)
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in fields.items()}
     DH, DT = 5.0, 4e-4
-    cfg = refcpu.make_config(dimension=2, equation="elastic", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT, T=(nt - 0.4) * DT,
-                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary, BoundaryWidth=8,
-                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=20.0, VMaxCPML=2700.0,
-                             useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    cfg = refcpu.make_config(dimension=2, equation="viscoelastic" if L else "elastic", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT,
+                             T=(nt - 0.4) * DT, spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary,
+                             BoundaryWidth=8, DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=20.0, VMaxCPML=2700.0,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce, numRelaxationMechanisms=L,
+                             relaxationFrequency=[15.0, 40.0][:L])
     sidx = np.array([refcpu.grid_index(cfg, NX // 2, 2 if fs else 6, 0)], np.int64)
     sig = refcpu.ricker(nt, DT, 25.0, 1.0, -0.02, np.float64)[None]
     rx = np.arange(4, NX - 4, 3)
@@ -320,6 +326,39 @@ def test_oracle_elastic3d_adjoint_matches_fp64_finite_differences(refcpu, fs, bo
     grads = dict(vp=gvp, vs=gvs, rho=grho)
     for name in ("vp", "vs", "rho"):
         d = smooth3(rng, cfg) * model[name]
+        h = 1e-5
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name] + h * d
+        mm[name] = model[name] - h * d
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        ad = float(np.dot(grads[name], d))
+        assert abs(fd) > 0
+        assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
+
+
+@pytest.mark.parametrize("L,boundary,stencil,reduce", [(1, 2, 0, 1), (2, 0, 1, 0), (2, 1, 0, 1)])
+def test_oracle_visco_adjoint_matches_fp64_finite_differences(refcpu, L, boundary, stencil, reduce):
+    """The oracle's FP64 adjoint of the 2-D visco-elastic step (memory
+    variables of one or two relaxation mechanisms; gradients with respect to
+    vp, vs, rho with the relaxation times held fixed) against central finite
+    differences of its own misfit, with CPML, no boundary and ABS."""
+    cfg, model, acq = case(refcpu, 0, boundary, stencil, reduce, L=L)
+    true = dict(model)
+    yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
+    blob = np.exp(-((xx - cfg.NX * 0.4) ** 2 + (yy - cfg.NY * 0.6) ** 2) / 40.0).reshape(-1)
+    true["vp"] = model["vp"] * (1 + 0.05 * blob)
+    true["vs"] = model["vs"] * (1 - 0.04 * blob)
+    o = refcpu.Oracle(cfg, true, *acq, dtype=np.float64)
+    dobs = 0.9 * o.run()
+    o.close()
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    J, gvp, gvs, grho = o.adjoint_gradient(dobs, checkpoint_every=37)
+    o.close()
+    assert J > 0 and J == pytest.approx(misfit(refcpu, cfg, model, acq, dobs), rel=1e-12)
+    rng = np.random.default_rng(29)
+    grads = dict(vp=gvp, vs=gvs, rho=grho)
+    for name in ("vp", "vs", "rho"):
+        d = smooth_direction(rng, cfg.NY, cfg.NX) * model[name]
         h = 1e-5
         mp, mm = dict(model), dict(model)
         mp[name] = model[name] + h * d

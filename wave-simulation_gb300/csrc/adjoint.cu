@@ -206,7 +206,8 @@ __device__ __forceinline__ float w4(int x, int y, int kx, int ky, int NX, int NY
 // chain rule from the prepared materials to vp, vs, rho (2-D elastic):
 // M = rho vp^2; mu = max(rho vs^2, 1); mu_xy = 1 / sum_k w_k / mu_k (0 below 4);
 // irx = 1 / (2-point average of rho along x), iry along y (0 where invalid)
-__global__ void adj_grad_final(PrepParams G, const StepParams P, const AdjShot A, float* gvp, float* gvs, float* grho, int accumulate)
+__global__ void adj_grad_final(PrepParams G, const StepParams P, const AdjShot A, float vsum, float* gvp, float* gvs, float* grho,
+                               int accumulate)
 {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
         const int kx = static_cast<int>(k % G.NX), ky = static_cast<int>(k / G.NX);
@@ -223,9 +224,15 @@ __global__ void adj_grad_final(PrepParams G, const StepParams P, const AdjShot A
                 const float w = w4(x, y, kx, ky, G.NX, G.NY);
                 if (w != 0.0f) gmu += A.g[2][r] * w * (mxy / muk) * (mxy / muk);
             }
-        const bool unclamped = rho * vs * vs >= 1.0f;
-        float gr = A.g[0][k] * vp * vp;
-        if (unclamped) gr += gmu * vs * vs;
+        // visco: M = rho vp^2 / fP, mu = max(rho vs^2 / fS, 1) with f = 1 + sum tau (the relaxation times held fixed)
+        const float fP = A.visco ? 1.0f + vsum * P.m[M_TAUP][k] : 1.0f, fS = A.visco ? 1.0f + vsum * P.m[M_TAUS][k] : 1.0f;
+        float raw = rho;
+        raw *= vs;
+        raw *= vs;
+        if (A.visco) raw = raw / fS;
+        const bool unclamped = raw >= 1.0f;
+        float gr = A.g[0][k] * vp * vp / fP;
+        if (unclamped) gr += gmu * vs * vs / fS;
         // inverse density averages: rows (kx, ky) and (kx-1, ky) along x, (kx, ky-1) along y
         for (int d = 0; d <= 1; ++d) {
             if (kx - d >= 0) {
@@ -241,8 +248,8 @@ __global__ void adj_grad_final(PrepParams G, const StepParams P, const AdjShot A
                 if (ir != 0.0f && (d == 0 || w == 0.5f)) gr -= A.g[4][r] * ir * ir * w;
             }
         }
-        const float gp = A.g[0][k] * 2.0f * rho * vp;
-        const float gs = unclamped ? gmu * 2.0f * rho * vs : 0.0f;
+        const float gp = A.g[0][k] * 2.0f * rho * vp / fP;
+        const float gs = unclamped ? gmu * 2.0f * rho * vs / fS : 0.0f;
         if (accumulate) { gvp[k] += gp; gvs[k] += gs; grho[k] += gr; }
         else { gvp[k] = gp; gvs[k] = gs; grho[k] = gr; }
     }
@@ -499,10 +506,13 @@ std::string adjoint_supported(const wave_handle* h)
 {
     const wave_config& c = h->cfg;
     const bool ok2 = c.dimension == 2 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_SH ||
-                                          c.equation == WAVE_EQ_EMEM);
+                                          c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC);
     const bool ok3 = c.dimension == 3 && c.equation == WAVE_EQ_ELASTIC;
     if (!ok2 && !ok3)
-        return "the adjoint gradient is implemented for 2-D and 3-D elastic, 2-D SH and lossless 2-D TMz and TEz modelling";
+        return "the adjoint gradient is implemented for 2-D and 3-D elastic, 2-D visco-elastic, 2-D SH and lossless 2-D TMz "
+               "and TEz modelling";
+    if (c.equation == WAVE_EQ_VISCOELASTIC && c.FreeSurface != 0)
+        return "the visco-elastic adjoint takes no free surface (its relaxation exchange is not differentiated)";
     if (ok3 && c.FreeSurface == 2) return "the 3-D adjoint takes the mirror free surface (FreeSurface = 1) or none";
     if (c.equation == WAVE_EQ_TMEM) {
         for (int t : h->hRecType)
@@ -562,7 +572,10 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
                                PS_VXX,   PS_VYY,   PS_VZZ,   PS_VXY,   PS_VYX,   PS_VXZ,   PS_VZX,   PS_VYZ,   PS_VZY};
         const int* fields = e3 ? e3Fields : tm ? tmFields : sh ? shFields : te ? teFields : elasticFields;
         const int* psiSlot = e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
-        const int nf = e3 ? 9 : 5, np = e3 ? 18 : 8, nparts = nf + np;
+        // visco-elastic: the elastic parts, then rxx, ryy, rxy of each mechanism
+        const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC;
+        const int nr = visco ? 3 * h->L : 0;
+        const int nf = e3 ? 9 : 5, np = e3 ? 18 : 8, nparts = nf + np + nr;
         for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
         for (int k = 0; k < np; ++k) {
             const int slot = psiSlot[k];
@@ -570,12 +583,16 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             len[nf + k] = (slot >= 0 && h->psi[slot]) ? h->psiLen[slot] : 0;
             o += len[nf + k];
         }
+        const int memVar[3] = {R_XX, R_YY, R_XY};
+        auto rpart = [&](int j) { return h->r[memVar[j / h->L]][j % h->L]; };
+        for (int j = 0; j < nr; ++j) { off[nf + np + j] = o; len[nf + np + j] = N; o += N; }
         stride[s] = o;
         AdjShot& a = A[s];
         a.tm = tm ? 1 : 0;
         a.sh = sh ? 1 : 0;
         a.te = te ? 1 : 0;
         a.e3 = e3 ? 1 : 0;
+        a.visco = visco ? 1 : 0;
         a.view = pool.get<float>(static_cast<size_t>(o) * (K + 1));
         a.stride = o;
         for (int k = 0; k < kAdjMaxParts; ++k) a.off[k] = k < nparts ? off[k] : 0;
@@ -583,6 +600,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         ck(cudaMemsetAsync(lstate, 0, o * sizeof(float), st), "memset");
         for (int k = 0; k < nf; ++k) a.lf[k] = lstate + off[k];
         for (int k = 0; k < np; ++k) a.lpsi[k] = lstate + off[nf + k];
+        for (int k = 0; k < 3 * kMaxL; ++k) a.lr[k] = nullptr;
+        for (int j = 0; j < nr; ++j) a.lr[(j / h->L) * kMaxL + j % h->L] = lstate + off[nf + np + j];
         const int ntemp = e3 ? 18 : 8, ngrad = e3 ? 8 : 5;
         float* temps = pool.get<float>(static_cast<size_t>(ntemp) * N);
         for (int k = 0; k < ntemp; ++k) a.T[k] = temps + k * N;
@@ -612,7 +631,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         ckpt[s] = pool.get<float>(static_cast<size_t>(o) * nck);
         for (int k = 0; k < nparts; ++k) {
             if (len[k] == 0) continue;
-            float* live = k < nf ? h->f[fields[k]] : h->psi[psiSlot[k - nf]];
+            float* live = k < nf ? h->f[fields[k]] : k < nf + np ? h->psi[psiSlot[k - nf]] : rpart(k - nf - np);
             toView.push_back({live, a.view + off[k], len[k], 0, o});
             toCkpt.push_back({live, ckpt[s] + off[k], len[k], 0, o});
             fromCkpt.push_back({ckpt[s] + off[k], live, len[k], o, 0});
@@ -651,6 +670,9 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         for (int f : h->fields) ck(cudaMemsetAsync(h->f[f], 0, h->N * sizeof(float), st), "memset");
         for (int k = 0; k < PS_COUNT; ++k)
             if (h->psi[k]) ck(cudaMemsetAsync(h->psi[k], 0, h->psiLen[k] * sizeof(float), st), "memset");
+        for (int rr = 0; rr < R_COUNT; ++rr)
+            for (int l = 0; l < kMaxL; ++l)
+                if (h->r[rr][l]) ck(cudaMemsetAsync(h->r[rr][l], 0, h->N * sizeof(float), st), "memset");
         ck(cudaMemsetAsync(h->seis, 0, static_cast<size_t>(h->nrec) * NT * sizeof(float), st), "memset");
     }
     S.set_counter(0);
@@ -705,7 +727,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             adj_te_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
                                                sum && s > 0 ? 1 : 0);
         else
-            adj_grad_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
+            adj_grad_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], A[s].visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f, gvp[o],
+                                                 gvs[o], grho[o], sum && s > 0 ? 1 : 0);
     }
     ck(cudaGetLastError(), "gradient launch");
     ck(cudaMemcpyAsync(misfit, dMisfit, ns * sizeof(double), cudaMemcpyDeviceToHost, st), "misfit copy");

@@ -39,6 +39,8 @@ struct AdjShot {
     int sh;                      // 1: 2-D SH (parts: vz, sxz, syz; psi sxz_x, syz_y, vzx, vzy)
     int te;                      // 1: lossless 2-D TEz (parts: hz, ex, ey; psi eyx, exy, hzy, hzx)
     int e3;                      // 1: 3-D elastic (Adj3Part layout)
+    int visco;                   // 1: 2-D visco-elastic (the elastic parts, then rxx, ryy, rxy per mechanism)
+    float* lr[3 * kMaxL];        // adjoint memory variables rxx, ryy, rxy of mechanism l at [k * kMaxL + l]
     float* vprime[3];            // vx', vy' [, vz'] (TMz: hx', hy') of the current step (null: the saved state's are they)
     const long long* sidx;       // sources (velocity sources are taken out of v')
     const int* stype;
@@ -155,6 +157,48 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
     float l1 = M * lxx + lam * lyy;
     float l2 = lam * lxx + M * lyy;
     float l3 = mxy * lxy, l4 = l3;
+    if (A.visco) {
+        // per mechanism l, with e = c1' + c2', q = c2' (sxx) or c1' (syy), m = mu_xy (c3' + c4'):
+        //   Rk' = c2_l (c1_l Rk - tauP M e / tau_l + tauS 2 mu q / tau_l)
+        //   Sk' = Sk + DT/2 sum_l (Rk + Rk') + (1 + L tauP) M e - (1 + L tauS) 2 mu q
+        //   Rxy' = c2_l (c1_l Rxy - tauSxy m / tau_l),  Sxy' = Sxy + DT/2 sum_l (Rxy + Rxy') + (1 + L tauS) m
+        // (ForwardSolver2Dviscoelastic.cpp:218-316); the memory variables are not tapered
+        const float e = c1 + c2, DTh = P.DThalf;
+        const float tP = __ldg(P.m[M_TAUP] + i), tS = __ldg(P.m[M_TAUS] + i);
+        const float opP = __ldg(P.m[M_OPLTP] + i), opS = __ldg(P.m[M_OPLTS] + i), tSxy = __ldg(P.m[M_TAUSXY] + i);
+        float le = 0.0f, lq[2] = {0.0f, 0.0f}, gM = 0.0f, gMu = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const float lS = k == 0 ? lxx : lyy, q = k == 0 ? c2 : c1;
+            le += opP * M * lS;
+            lq[k] -= opS * 2.0f * mu * lS;
+            gM += opP * e * lS;
+            gMu -= opS * 2.0f * q * lS;
+            for (int l = 0; l < P.L; ++l) {
+                const float cc = P.c2[l] * P.invRelax[l];
+                float* r = A.lr[k * kMaxL + l] + i;
+                const float LR = *r + DTh * lS;   // adjoint of Rk'
+                *r = P.c2[l] * P.c1[l] * LR + DTh * lS;
+                le -= cc * tP * M * LR;
+                lq[k] += cc * tS * 2.0f * mu * LR;
+                gM -= cc * tP * e * LR;
+                gMu += cc * tS * 2.0f * q * LR;
+            }
+        }
+        l1 = le + lq[1];
+        l2 = le + lq[0];
+        float lm = opS * lxy;
+        for (int l = 0; l < P.L; ++l) {
+            float* r = A.lr[2 * kMaxL + l] + i;
+            const float LR = *r + DTh * lxy;
+            *r = P.c2[l] * P.c1[l] * LR + DTh * lxy;
+            lm -= P.c2[l] * P.invRelax[l] * tSxy * LR;
+        }
+        l3 = l4 = mxy * lm;
+        A.g[0][i] += gM;
+        A.g[1][i] += gMu;
+        A.g[2][i] += lm * (c3 + c4);
+    }
     if (fsRow) {
         // sxx' += sh c1' - sv c2' with sv = M - 2 mu, sh = -sv^2 / M
         const float sv = lam, sh = -(sv * sv) / M;
@@ -178,9 +222,11 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
     A.T[1][i] = l2;
     A.T[2][i] = l3;
     A.T[3][i] = l4;
-    A.g[0][i] += (lxx + lyy) * (c1 + c2);
-    A.g[1][i] += -2.0f * (lxx * c2 + lyy * c1);
-    A.g[2][i] += lxy * (c3 + c4);
+    if (!A.visco) {
+        A.g[0][i] += (lxx + lyy) * (c1 + c2);
+        A.g[1][i] += -2.0f * (lxx * c2 + lyy * c1);
+        A.g[2][i] += lxy * (c3 + c4);
+    }
 }
 
 // velocity-pass transpose (and the transposed stress-pass derivatives of v)

@@ -136,6 +136,8 @@ struct wave_handle {
 namespace wave {
 // one forward time step of a handle on its stream (solver.cu)
 void step_once(wave_handle* h);
+// the visco modulus relaxation sum of a configuration (solver.cu)
+float visco_modulus_sum(const wave_config& c, int L);
 
 // variable grid (vargrid.cu): upload of the host-built operators, model
 // preparation, and the launches of one step (returns the kernel count;

@@ -439,6 +439,19 @@ std::vector<std::pair<void*, size_t>> state_parts(wave_handle* h)
 
 void wave::step_once(wave_handle* h) { launch_step(h); }
 
+// sum_l w^2 ts_l^2 / (1 + w^2 ts_l^2) with w = 2 pi f_CPML, ts_l = 1 / (2 pi f_l):
+// the visco modulus relaxation (Viscoelastic.cpp:650-715), M = rho vp^2 / (1 + sum tauP)
+float wave::visco_modulus_sum(const wave_config& c, int L)
+{
+    float sum = 0.0f;
+    const float w_ref = static_cast<float>(2.0 * M_PI * c.CenterFrequencyCPML);
+    for (int l = 0; l < L; ++l) {
+        const float ts = static_cast<float>(1.0 / (2.0 * M_PI * static_cast<float>(c.relaxationFrequency[l])));
+        sum += w_ref * w_ref * ts * ts / (1.0 + w_ref * w_ref * ts * ts);
+    }
+    return sum;
+}
+
 
 extern "C" {
 
@@ -767,16 +780,9 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
             h->sp.m[slot] = h->m[slot];
             return h->m[slot];
         };
-        float sum = 0.0f; // visco modulus relaxation (Viscoelastic.cpp:650-715)
-        if (visco) {
-            const float w_ref = static_cast<float>(2.0 * M_PI * h->cfg.CenterFrequencyCPML);
-            for (int l = 0; l < h->L; ++l) {
-                const float ts = static_cast<float>(1.0 / (2.0 * M_PI * static_cast<float>(h->cfg.relaxationFrequency[l])));
-                sum += w_ref * w_ref * ts * ts / (1.0 + w_ref * w_ref * ts * ts);
-            }
-        }
+        const float sum = visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f;
         h->check(cudaMemcpyAsync(mat(M_RHO), dRho, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
-        if (eq == WAVE_EQ_ELASTIC) {
+        if (eq == WAVE_EQ_ELASTIC || (eq == WAVE_EQ_VISCOELASTIC && !is3d)) {
             h->check(cudaMemcpyAsync(mat(M_VP), dVp, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
             h->check(cudaMemcpyAsync(mat(M_VS), dVs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         }
