@@ -378,6 +378,11 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
 /* ---- adjoint gradient (new; the reference's inversion is a separate project) ----
  * Gradient of J = 1/2 sum over receivers and steps of (d - d_obs)^2 by the
  * discrete adjoint of the time step:
+ *  - 2-D and 3-D acoustic (FD2Dacoustic::run, ForwardSolver2Dacoustic.cpp:
+ *    91-194; FD3Dacoustic::run, ForwardSolver3Dacoustic.cpp:91-233) with CPML,
+ *    ABS or no damping boundary and with or without the free surface
+ *    (FreeSurface 1): grad_vp and grad_rho receive dJ/dvp, dJ/drho, grad_vs
+ *    is set to zero;
  *  - 2-D and 3-D elastic (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297;
  *    FD3Delastic::run, ForwardSolver3Delastic.cpp:120-414) with CPML, ABS or
  *    no damping boundary and with or without the free surface (FreeSurface 1):

@@ -1140,6 +1140,178 @@ struct ElasticAdjoint3D {
     }
 };
 
+// Discrete adjoint of the oracle's acoustic step in 2-D and 3-D
+// (Sim<T>::stepAcoustic, restating FD2Dacoustic::run,
+// ForwardSolver2Dacoustic.cpp:91-194, and FD3Dacoustic::run,
+// ForwardSolver3Dacoustic.cpp:91-233, with CPML, the ABS taper and the free
+// surface's image operator and p = 0 on the surface row): the gradient of
+// J = 1/2 sum (d - d_obs)^2 with respect to vp and rho. Per step, from X_t and
+// X_{t+1}:
+//   a0' = Dxf p + P(p_x)  a1' = DyfS p + P(p_y)  [a2' = Dzf p + P(p_z)]
+//   vx' = vx + irx a0',  vy' = vy + iry a1'  [, vz' = vz + irz a2']
+//   c0' = Dxb vx' + P(vxx)  c1' = Dyb vy' + P(vyy)  [c2' = Dzb vz' + P(vzz)]
+//   p <- (p + M (c0' + c1' + c2')) d, v <- v' d, then p = 0 on the surface
+// with M = rho vp^2 and irx, iry, irz the inverse 2-point density averages.
+template <class T>
+struct AcousticAdjoint {
+    Sim<T>& s;
+    const idx_t N;
+    const bool d3;
+    CSR<T> DxfT, DxbT, DyfST, DybT, DzfT, DzbT;
+    explicit AcousticAdjoint(Sim<T>& sim) : s(sim), N(sim.g.N()), d3(sim.is3d)
+    {
+        if (s.eq != WAVE_EQ_ACOUSTIC) throw std::invalid_argument("oracle adjoint: acoustic only");
+        DxfT = transpose(s.Dxf);
+        DxbT = transpose(s.Dxb);
+        DyfST = transpose(s.fs ? s.DyfFS : s.Dyf);
+        DybT = transpose(s.Dyb);
+        if (d3) {
+            DzfT = transpose(s.Dzf);
+            DzbT = transpose(s.Dzb);
+        }
+    }
+    struct State {
+        std::map<std::string, std::vector<T>> F, psi;
+    };
+    const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
+    {
+        auto it = x.psi.find(n);
+        return it == x.psi.end() ? zero : it->second;
+    }
+    void cpmlT(std::vector<T>& lc, std::vector<T>& lp, const std::vector<T>& a, const std::vector<T>& b) const
+    {
+        if (!s.useCpml) return;
+        for_n(N, [&](idx_t i) {
+            const T c = (T(1) + a[i]) * lc[i] + a[i] * lp[i];
+            lp[i] = b[i] * (lc[i] + lp[i]);
+            lc[i] = c;
+        });
+    }
+
+    double run(const std::vector<T>& vp, const std::vector<T>& rho, const T* dobs, int K, T* gvp, T* grho)
+    {
+        const int NT = s.NT;
+        const size_t nrec = s.rec.idx.size();
+        const std::vector<T> zero(N, T(0));
+        const int nd = d3 ? 3 : 2;
+        s.reset();
+        std::vector<State> ck;
+        for (int t = 0; t < NT; ++t) {
+            if (t % K == 0) ck.push_back({s.F, s.psi});
+            s.step(t);
+        }
+        std::vector<T> res(nrec * static_cast<size_t>(NT));
+        double J = 0;
+        for (size_t k = 0; k < res.size(); ++k) {
+            res[k] = s.seis[k] - dobs[k];
+            J += 0.5 * static_cast<double>(res[k]) * static_cast<double>(res[k]);
+        }
+        const char* vn[3] = {"vx", "vy", "vz"};
+        const char* pP[3] = {"p_x", "p_y", "p_z"};
+        const char* pQ[3] = {"vxx", "vyy", "vzz"};
+        const std::vector<T>* aH[3] = {&s.axh, &s.ayh, &s.azh};
+        const std::vector<T>* bH[3] = {&s.bxh, &s.byh, &s.bzh};
+        const std::vector<T>* aF[3] = {&s.ax, &s.ay, &s.az};
+        const std::vector<T>* bF[3] = {&s.bx, &s.by, &s.bz};
+        const std::vector<T>* ir[3] = {&s.invRhoX, &s.invRhoY, &s.invRhoZ};
+        std::vector<T> lp(N, 0), lv[3], lP[3], lQ[3], a[3], c[3], vpr[3], la[3], lc[3], gIr[3];
+        for (int k = 0; k < 3; ++k) {
+            lv[k].assign(N, 0); lP[k].assign(N, 0); lQ[k].assign(N, 0); a[k].assign(N, 0); c[k].assign(N, 0);
+            vpr[k].assign(N, 0); la[k].assign(N, 0); lc[k].assign(N, 0); gIr[k].assign(N, 0);
+        }
+        std::vector<T> gM(N, 0);
+        const int nseg = static_cast<int>(ck.size());
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int t0 = seg * K, t1 = std::min(NT, t0 + K);
+            std::vector<State> X;
+            s.F = ck[seg].F;
+            s.psi = ck[seg].psi;
+            X.push_back({s.F, s.psi});
+            for (int t = t0; t < t1; ++t) {
+                s.step(t);
+                X.push_back({s.F, s.psi});
+            }
+            for (int t = t1 - 1; t >= t0; --t) {
+                const State& X0 = X[t - t0];
+                const State& X1 = X[t - t0 + 1];
+                const auto& p0 = X0.F.at("p");
+                s.Dxf.spmv(p0.data(), a[0].data());
+                (s.fs ? s.DyfFS : s.Dyf).spmv(p0.data(), a[1].data());
+                if (d3) s.Dzf.spmv(p0.data(), a[2].data());
+                for (int k = 0; k < nd; ++k) {
+                    const auto& ps = psiOf(X1, pP[k], zero);
+                    const auto& v0 = X0.F.at(vn[k]);
+                    const auto& irk = *ir[k];
+                    for_n(N, [&](idx_t i) {
+                        a[k][i] += ps[i];
+                        vpr[k][i] = v0[i] + irk[i] * a[k][i];
+                    });
+                }
+                s.Dxb.spmv(vpr[0].data(), c[0].data());
+                s.Dyb.spmv(vpr[1].data(), c[1].data());
+                if (d3) s.Dzb.spmv(vpr[2].data(), c[2].data());
+                for (int k = 0; k < nd; ++k) {
+                    const auto& q = psiOf(X1, pQ[k], zero);
+                    for_n(N, [&](idx_t i) { c[k][i] += q[i]; });
+                }
+                for (size_t r = 0; r < nrec; ++r) {
+                    const idx_t i = s.rec.idx[r];
+                    const T v = res[r * NT + t];
+                    switch (s.rec.type[r]) {
+                    case WAVE_TYPE_P: lp[i] += v; break;
+                    case WAVE_TYPE_VX: lv[0][i] += v; break;
+                    case WAVE_TYPE_VY: lv[1][i] += v; break;
+                    default: lv[2][i] += v; break;
+                    }
+                }
+                // p = 0 on the surface (after the taper), the taper on p and v
+                if (s.fs) for_n(N, [&](idx_t i) { lp[i] *= s.fsZero[i]; });
+                if (s.useAbs) {
+                    for_n(N, [&](idx_t i) { lp[i] *= s.damping[i]; });
+                    for (int k = 0; k < nd; ++k) for_n(N, [&](idx_t i) { lv[k][i] *= s.damping[i]; });
+                }
+                // p <- p + M (c0' + c1' + c2')
+                for_n(N, [&](idx_t i) {
+                    T cs = 0;
+                    for (int k = 0; k < nd; ++k) cs += c[k][i];
+                    gM[i] += lp[i] * cs;
+                    for (int k = 0; k < nd; ++k) lc[k][i] = s.M[i] * lp[i];
+                });
+                for (int k = 0; k < nd; ++k) cpmlT(lc[k], lQ[k], *aF[k], *bF[k]);
+                spmv_add(DxbT, lc[0], lv[0]);
+                spmv_add(DybT, lc[1], lv[1]);
+                if (d3) spmv_add(DzbT, lc[2], lv[2]);
+                // v' = v + ir a'
+                for (int k = 0; k < nd; ++k) {
+                    const auto& irk = *ir[k];
+                    for_n(N, [&](idx_t i) {
+                        la[k][i] = irk[i] * lv[k][i];
+                        gIr[k][i] += lv[k][i] * a[k][i];
+                    });
+                    cpmlT(la[k], lP[k], *aH[k], *bH[k]);
+                }
+                spmv_add(DxfT, la[0], lp);
+                spmv_add(DyfST, la[1], lp);
+                if (d3) spmv_add(DzfT, la[2], lp);
+            }
+        }
+        // M = rho vp^2; ir = 1 / A2(rho) (0 where invalid)
+        AverageTranspose<T> probe(s);
+        std::vector<T> y(N), grhoAvg(N, 0);
+        const Axis axes[3] = {Axis::X, Axis::Y, Axis::Z};
+        for (int k = 0; k < nd; ++k) {
+            const auto& irk = *ir[k];
+            for_n(N, [&](idx_t r) { y[r] = -gIr[k][r] * irk[r] * irk[r]; });
+            probe.avgT([&](const T* in, T* out) { average2<T>(s.g, axes[k], in, out); }, y, grhoAvg);
+        }
+        for (idx_t k = 0; k < N; ++k) {
+            gvp[k] = gM[k] * T(2) * rho[k] * vp[k];
+            grho[k] = gM[k] * vp[k] * vp[k] + grhoAvg[k];
+        }
+        return J;
+    }
+};
+
 template <class T>
 constexpr const char* ElasticAdjoint2D<T>::kP[4];
 template <class T>

@@ -279,6 +279,7 @@ def lib():
         L.refcpu_adjoint_elastic2d.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P, P, P]
         L.refcpu_adjoint_tmz.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P, P, P]
         L.refcpu_adjoint_sh.argtypes = [P, P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P, P]
+        L.refcpu_adjoint_acoustic.argtypes = [P, P, P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_double), P, P]
         _lib = L
     return _lib
 
@@ -359,11 +360,23 @@ class Oracle:
     def adjoint_gradient(self, dobs: np.ndarray, checkpoint_every: int = 50):
         """Misfit 1/2 sum (d - dobs)^2 and its gradients with respect to vp, vs
         and rho (2-D and 3-D elastic, 2-D visco-elastic with the relaxation
-        times held fixed; 2-D SH: the vp gradient is zero) or eps_r, sigma
+        times held fixed; 2-D SH: the vp gradient is zero; 2-D and 3-D
+        acoustic: the vs gradient is zero) or eps_r, sigma
         and mu_r (lossless 2-D TMz and TEz), by the oracle's own discrete adjoint
         (adjoint_impl.hpp) in this oracle's value type."""
         n = self.cfg.NX * self.cfg.NY * (self.cfg.NZ if self.cfg.dimension == 3 else 1)
         em = self.cfg.equation >= 5
+        if self.cfg.equation == EQ["acoustic"]:
+            m = [np.ascontiguousarray(self.model[k], dtype=np.float64) for k in ("vp", "rho")]
+            d = np.ascontiguousarray(dobs, dtype=np.float64)
+            if d.size != len(self._ridx) * self.nt:
+                raise ValueError("dobs must hold n_receivers x NT samples")
+            g = [np.zeros(n, dtype=np.float64) for _ in range(2)]
+            J = ctypes.c_double(0)
+            if lib().refcpu_adjoint_acoustic(self.h, _ptr(m[0]), _ptr(m[1]), _ptr(d), int(checkpoint_every),
+                                             ctypes.byref(J), _ptr(g[0]), _ptr(g[1])) != 0:
+                raise RuntimeError(lib().refcpu_last_error().decode())
+            return J.value, g[0], np.zeros(n, dtype=np.float64), g[1]
         if self.cfg.equation == EQ["sh"]:
             m = [np.ascontiguousarray(self.model[k], dtype=np.float64) for k in ("vs", "rho")]
             d = np.ascontiguousarray(dobs, dtype=np.float64)

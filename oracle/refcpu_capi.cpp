@@ -217,6 +217,32 @@ int refcpu_adjoint_elastic2d(void* hv, const double* vp, const double* vs, const
     }
 }
 
+// The same for an acoustic simulation (2-D or 3-D): gradients with respect to
+// vp and rho (adjoint_impl.hpp, AcousticAdjoint).
+int refcpu_adjoint_acoustic(void* hv, const double* vp, const double* rho, const double* dobs, int K, double* misfit, double* gvp,
+                            double* grho)
+{
+    auto* h = static_cast<Handle*>(hv);
+    auto run = [&](auto* s) -> int {
+        using T = typename std::decay_t<decltype(s->M)>::value_type;
+        const size_t N = s->g.N(), nd = s->rec.idx.size() * static_cast<size_t>(s->NT);
+        std::vector<T> P(vp, vp + N), R(rho, rho + N), D(dobs, dobs + nd), a(N), b(N);
+        refcpu::AcousticAdjoint<T> adj(*s);
+        *misfit = adj.run(P, R, D.data(), K, a.data(), b.data());
+        std::copy(a.begin(), a.end(), gvp);
+        std::copy(b.begin(), b.end(), grho);
+        return 0;
+    };
+    try {
+        if (K < 1) throw std::invalid_argument("checkpoint interval must be >= 1");
+        if (h->is_double) return run(static_cast<refcpu::Sim<double>*>(h->sim));
+        return run(static_cast<refcpu::Sim<float>*>(h->sim));
+    } catch (std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
+}
+
 // The same for a 2-D SH simulation (vz receivers): gradients with respect to
 // vs and rho (adjoint_impl.hpp, SHAdjoint2D).
 int refcpu_adjoint_sh(void* hv, const double* vs, const double* rho, const double* dobs, int K, double* misfit, double* gvs,

@@ -125,18 +125,23 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("dim,equation", [(2, "acoustic"), (3, "acoustic")])
+@pytest.mark.parametrize("dim,equation", [(2, "viscosh"), (3, "viscoelastic")])
 def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
     """Equations without an adjoint are refused with WAVE_ERR_UNSUPPORTED."""
     cfg = _config(wave, dim=dim)
     cfg.equation = wave.EQUATIONS[equation]
+    cfg.numRelaxationMechanisms = 1
+    cfg.relaxationFrequency[0] = 20.0
     true, start = _models()
     n = cfg.N
-    model = {k: np.resize(v, n).astype(np.float32) for k, v in start.items() if k != "vs"}
+    model = {k: np.resize(v, n).astype(np.float32) for k, v in start.items()}
+    model["taup"] = np.full(n, 0.03, np.float32)
+    model["taus"] = np.full(n, 0.03, np.float32)
     s = wave.Factory.Create("3D" if dim == 3 else "2D", equation).initForwardSolver(cfg)
     s.prepareForModelling(model)
-    s.setSources(np.array([5], np.int64), np.array([1], np.int32), np.zeros((1, s.nt), np.float32))
-    s.setReceivers(np.array([7], np.int64), np.array([2], np.int32))
+    t = 4 if equation == "viscosh" else 1
+    s.setSources(np.array([5], np.int64), np.array([t], np.int32), np.zeros((1, s.nt), np.float32))
+    s.setReceivers(np.array([7], np.int64), np.array([4 if equation == "viscosh" else 2], np.int32))
     with pytest.raises(wave.WaveError) as e:
         s.adjoint_gradient(np.zeros((1, s.nt), np.float32))
     assert e.value.code == wave.WAVE_ERR_UNSUPPORTED

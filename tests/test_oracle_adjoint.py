@@ -367,3 +367,60 @@ def test_oracle_visco_adjoint_matches_fp64_finite_differences(refcpu, L, boundar
         ad = float(np.dot(grads[name], d))
         assert abs(fd) > 0
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
+
+
+def ac_case(refcpu, dim=2, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=44, NY=36, NZ=20, nt=180):
+    rng = np.random.default_rng(31)
+    NZ = NZ if dim == 3 else 1
+    y, z, x = np.mgrid[0:NY, 0:NZ, 0:NX]
+    vp = 1800.0 + 600.0 * (y / NY) + 70.0 * np.sin(x / 5.0) + 30.0 * np.cos(z / 4.0) + 25 * rng.standard_normal((NY, NZ, NX))
+    rho = 1700.0 + 300.0 * (y > NY // 2) + 40.0 * np.cos(x / 6.0)
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(vp=vp, rho=rho).items()}
+    DH, DT = 5.0, 4e-4
+    cfg = refcpu.make_config(dimension=dim, equation="acoustic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=(nt - 0.4) * DT,
+                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary, BoundaryWidth=6,
+                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=25.0, VMaxCPML=2500.0,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    zc = NZ // 2
+    sidx = np.array([refcpu.grid_index(cfg, NX // 2, 2 if fs else 6, zc), refcpu.grid_index(cfg, NX // 3, 9, zc)], np.int64)
+    sig = refcpu.ricker(nt, DT, 25.0, 1.0, -0.02, np.float64)
+    rx = np.arange(4, NX - 4, 3)
+    ry = 1 if fs else 5
+    ridx = np.concatenate([rx + NX * (zc + NZ * ry), rx + NX * (zc + NZ * ry), rx + NX * (zc + NZ * (NY - 6))]).astype(np.int64)
+    rtype = np.concatenate([np.full(rx.size, 1), np.full(rx.size, 3), np.full(rx.size, 2)]).astype(np.int32)
+    return cfg, model, (sidx, np.array([1, 3], np.int32), np.stack([sig, 2e-3 * sig]), ridx, rtype)
+
+
+@pytest.mark.parametrize("dim,fs,boundary,stencil,reduce", [(2, 0, 2, 0, 1), (2, 1, 1, 1, 0), (2, 1, 0, 0, 1),
+                                                            (3, 0, 2, 0, 1), (3, 1, 1, 0, 0)])
+def test_oracle_acoustic_adjoint_matches_fp64_finite_differences(refcpu, dim, fs, boundary, stencil, reduce):
+    """The oracle's FP64 adjoint of the 2-D and 3-D acoustic steps (gradients
+    with respect to vp and rho; P and VY sources, P / VX / VY receivers)
+    against central finite differences of its own misfit, with CPML, ABS, no
+    boundary and the free surface."""
+    cfg, model, acq = ac_case(refcpu, dim, fs, boundary, stencil, reduce)
+    true = dict(model)
+    n = model["vp"].size
+    blob = np.exp(-np.linspace(-3, 3, n) ** 2)
+    true["vp"] = model["vp"] * (1 + 0.05 * blob)
+    true["rho"] = model["rho"] * (1 - 0.03 * blob)
+    o = refcpu.Oracle(cfg, true, *acq, dtype=np.float64)
+    dobs = 0.9 * o.run()
+    o.close()
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    J, gvp, gvs, grho = o.adjoint_gradient(dobs, checkpoint_every=37)
+    o.close()
+    assert J > 0 and J == pytest.approx(misfit(refcpu, cfg, model, acq, dobs), rel=1e-12)
+    assert not np.any(gvs)
+    rng = np.random.default_rng(37)
+    grads = dict(vp=gvp, rho=grho)
+    for name in ("vp", "rho"):
+        d = (smooth3(rng, cfg) if dim == 3 else smooth_direction(rng, cfg.NY, cfg.NX)) * model[name]
+        h = 1e-5
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name] + h * d
+        mm[name] = model[name] - h * d
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        ad = float(np.dot(grads[name], d))
+        assert abs(fd) > 0
+        assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)

@@ -102,6 +102,10 @@ __global__ void adj_vprime(const StepParams* __restrict__ Ps, const AdjShot* __r
             for (int k = 0; k < 3; ++k) A.vprime[k][p.i] = X1[A.off[E3_VX + k] + p.i] / d;
             return;
         }
+        if (A.ac) {
+            for (int k = 0; k < (P.is3d ? 3 : 2); ++k) A.vprime[k][p.i] = X1[A.off[1 + k] + p.i] / d;
+            return;
+        }
         A.vprime[0][p.i] = X1[A.off[AV_VX] + p.i] / d;
         if (!A.sh && !A.te) A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
     });
@@ -114,7 +118,7 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
     if (!A.vprime[0]) return;
     for (int k = threadIdx.x; k < A.nsrc; k += blockDim.x) {
         const int t = A.stype[k];
-        if (A.e3 ? (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY && t != WAVE_TYPE_VZ)
+        if ((A.e3 || A.ac) ? (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY && t != WAVE_TYPE_VZ)
                  : A.te ? t != WAVE_TYPE_HZ : A.sh ? t != WAVE_TYPE_VZ : (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY))
             continue;
         const long long i = A.sidx[k];
@@ -125,7 +129,7 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
         p.y = static_cast<int>(r / P.NZ);
         p.z = static_cast<int>(r - (long long)p.y * P.NZ);
         const float d = P.abs ? absDamp(P, p) : 1.0f;
-        const int v = A.e3 ? t - WAVE_TYPE_VX : (A.sh || A.te || t == WAVE_TYPE_VX) ? 0 : 1;
+        const int v = (A.e3 || A.ac) ? t - WAVE_TYPE_VX : (A.sh || A.te || t == WAVE_TYPE_VX) ? 0 : 1;
         atomicAdd(A.vprime[v] + i, -A.signals[(long long)k * A.nt + n] / d);
     }
 }
@@ -144,6 +148,11 @@ __global__ void adj_inject(const AdjShot* __restrict__ As, int n)
         }
         if (A.sh) {   // vz receivers
             atomicAdd(A.lf[0] + i, v);
+            continue;
+        }
+        if (A.ac) {   // p, vx, vy, vz receivers
+            const int t = A.rtype[r];
+            atomicAdd(A.lf[t == WAVE_TYPE_P ? 0 : 1 + t - WAVE_TYPE_VX] + i, v);
             continue;
         }
         if (A.e3) {   // a pressure trace is (sxx + syy + szz) / 3 (FDTD3Delastic)
@@ -399,6 +408,35 @@ __global__ void adj_te_final(PrepParams G, const StepParams P, const AdjShot A, 
     }
 }
 
+// chain rule for the acoustic equations: M = rho vp^2; irx, iry, irz = 1 / (2-point
+// average of rho along x, y, z) (0 where invalid); grad_vs is zero
+__global__ void adj_ac_final(PrepParams G, const StepParams P, const AdjShot A, float* gvp, float* gvs, float* grho, int accumulate)
+{
+    const long long sy = (long long)G.NX * G.NZ, sz = G.NX;
+    const int nd = G.NZ > 1 ? 3 : 2;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
+        const int kx = static_cast<int>(k % G.NX);
+        const long long rest = k / G.NX;
+        const int kz = static_cast<int>(rest % G.NZ), ky = static_cast<int>(rest / G.NZ);
+        const float rho = P.m[M_RHO][k], vp = P.m[M_VP][k];
+        float gr = A.g[0][k] * vp * vp;
+        const int kc[3] = {kx, ky, kz};
+        const int Nc[3] = {static_cast<int>(G.NX), static_cast<int>(G.NY), static_cast<int>(G.NZ)};
+        const long long st[3] = {1, sy, sz};
+        for (int ax = 0; ax < nd; ++ax)
+            for (int d = 0; d <= 1; ++d) {
+                if (kc[ax] - d < 0) continue;
+                const long long r = k - d * st[ax];
+                const float ir = P.m[M_IRX + ax][r];
+                const float w = (kc[ax] - d + 1 < Nc[ax]) ? 0.5f : 1.0f;
+                if (ir != 0.0f && (d == 0 || w == 0.5f)) gr -= A.g[1 + ax][r] * ir * ir * w;
+            }
+        const float gp = A.g[0][k] * 2.0f * rho * vp;
+        if (accumulate) { gvp[k] += gp; grho[k] += gr; }
+        else { gvp[k] = gp; gvs[k] = 0.0f; grho[k] = gr; }
+    }
+}
+
 // weight of point (ka, kb) in the 4-point row at (a, b) of a plane average,
 // by its two in-plane coordinates (the edge fallbacks of
 // calc4PointAverageMatrixRow, Modelparameter.cpp:448-527)
@@ -471,7 +509,8 @@ __global__ void adj_e3_final(PrepParams G, const StepParams P, const AdjShot A, 
 void launch_adj(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
                 int pending, cudaStream_t s)
 {
-    if (pass >= 9) launch_adj_pass3d(H, pass, Ps, As, W, S, grid, vn, pending, s);
+    if (pass >= 11) launch_adj_pass_acoustic(H, pass, Ps, As, W, S, grid, vn, pending, s);
+    else if (pass >= 9) launch_adj_pass3d(H, pass, Ps, As, W, S, grid, vn, pending, s);
     else launch_adj_pass2d(H, pass, Ps, As, W, S, grid, vn, pending, s);
 }
 
@@ -508,9 +547,11 @@ std::string adjoint_supported(const wave_handle* h)
     const bool ok2 = c.dimension == 2 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_SH ||
                                           c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC);
     const bool ok3 = c.dimension == 3 && c.equation == WAVE_EQ_ELASTIC;
-    if (!ok2 && !ok3)
-        return "the adjoint gradient is implemented for 2-D and 3-D elastic, 2-D visco-elastic, 2-D SH and lossless 2-D TMz "
-               "and TEz modelling";
+    const bool okAc = c.equation == WAVE_EQ_ACOUSTIC;
+    if (!ok2 && !ok3 && !okAc)
+        return "the adjoint gradient is implemented for 2-D and 3-D acoustic and elastic, 2-D visco-elastic, 2-D SH and lossless "
+               "2-D TMz and TEz modelling";
+    if (okAc && c.FreeSurface == 2) return "the acoustic adjoint takes the mirror free surface (FreeSurface = 1) or none";
     if (c.equation == WAVE_EQ_VISCOELASTIC && c.FreeSurface != 0)
         return "the visco-elastic adjoint takes no free surface (its relaxation exchange is not differentiated)";
     if (ok3 && c.FreeSurface == 2) return "the 3-D adjoint takes the mirror free surface (FreeSurface = 1) or none";
@@ -556,7 +597,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         // 3-D elastic: the Adj3Part layout
         const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
         const bool sh = h->cfg.equation == WAVE_EQ_SH;
-        const bool e3 = h->sp.is3d;
+        const bool ac = h->cfg.equation == WAVE_EQ_ACOUSTIC;
+        const bool e3 = h->sp.is3d && !ac;
         long long off[kAdjMaxParts], len[kAdjMaxParts], o = 0;
         const int elasticFields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
         const int tmFields[5] = {F_HX, F_HY, F_EZ, -1, -1};
@@ -570,12 +612,15 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int e3Fields[9] = {F_VX, F_VY, F_VZ, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ};
         const int e3Psi[18] = {PS_SXX_X, PS_SXY_Y, PS_SXZ_Z, PS_SXY_X, PS_SYY_Y, PS_SYZ_Z, PS_SXZ_X, PS_SYZ_Y, PS_SZZ_Z,
                                PS_VXX,   PS_VYY,   PS_VZZ,   PS_VXY,   PS_VYX,   PS_VXZ,   PS_VZX,   PS_VYZ,   PS_VZY};
-        const int* fields = e3 ? e3Fields : tm ? tmFields : sh ? shFields : te ? teFields : elasticFields;
-        const int* psiSlot = e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
+        // acoustic: p, vx, vy, vz and the psi of p_x, p_y, p_z, vxx, vyy, vzz (2-D: no vz, p_z, vzz)
+        const int acFields[4] = {F_P, F_VX, F_VY, h->sp.is3d ? F_VZ : -1};
+        const int acPsi[6] = {PS_P_X, PS_P_Y, PS_P_Z, PS_VXX, PS_VYY, PS_VZZ};
+        const int* fields = ac ? acFields : e3 ? e3Fields : tm ? tmFields : sh ? shFields : te ? teFields : elasticFields;
+        const int* psiSlot = ac ? acPsi : e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
         // visco-elastic: the elastic parts, then rxx, ryy, rxy of each mechanism
         const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC;
         const int nr = visco ? 3 * h->L : 0;
-        const int nf = e3 ? 9 : 5, np = e3 ? 18 : 8, nparts = nf + np + nr;
+        const int nf = ac ? 4 : e3 ? 9 : 5, np = ac ? 6 : e3 ? 18 : 8, nparts = nf + np + nr;
         for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
         for (int k = 0; k < np; ++k) {
             const int slot = psiSlot[k];
@@ -593,6 +638,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         a.te = te ? 1 : 0;
         a.e3 = e3 ? 1 : 0;
         a.visco = visco ? 1 : 0;
+        a.ac = ac ? 1 : 0;
         a.view = pool.get<float>(static_cast<size_t>(o) * (K + 1));
         a.stride = o;
         for (int k = 0; k < kAdjMaxParts; ++k) a.off[k] = k < nparts ? off[k] : 0;
@@ -602,7 +648,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         for (int k = 0; k < np; ++k) a.lpsi[k] = lstate + off[nf + k];
         for (int k = 0; k < 3 * kMaxL; ++k) a.lr[k] = nullptr;
         for (int j = 0; j < nr; ++j) a.lr[(j / h->L) * kMaxL + j % h->L] = lstate + off[nf + np + j];
-        const int ntemp = e3 ? 18 : 8, ngrad = e3 ? 8 : 5;
+        const int ntemp = e3 ? 18 : 8, ngrad = e3 ? 8 : 5;   // acoustic: 6 and 4 of them
         float* temps = pool.get<float>(static_cast<size_t>(ntemp) * N);
         for (int k = 0; k < ntemp; ++k) a.T[k] = temps + k * N;
         float* grads = pool.get<float>(static_cast<size_t>(ngrad) * N);
@@ -616,11 +662,11 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         a.res = res;
         bool velocitySources = false;
         for (int t : h->hSrcType)
-            velocitySources |= e3 ? (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY || t == WAVE_TYPE_VZ)
+            velocitySources |= (e3 || ac) ? (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY || t == WAVE_TYPE_VZ)
                              : te ? t == WAVE_TYPE_HZ : sh ? t == WAVE_TYPE_VZ : (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
         a.vprime[0] = a.vprime[1] = a.vprime[2] = nullptr;
         if (h->cfg.DampingBoundary == 1 || velocitySources) {
-            const int nv = e3 ? 3 : 2;
+            const int nv = (e3 || ac) ? 3 : 2;
             a.vprime[0] = pool.get<float>(static_cast<size_t>(nv) * N);
             for (int k = 1; k < nv; ++k) a.vprime[k] = a.vprime[0] + k * N;
         }
@@ -704,7 +750,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             // two kernels per step: the third stage of step n (the transposed
             // derivatives of the first-pass inputs) runs inside the first kernel
             // of step n - 1; after step 0 it is not needed
-            const int first = A[0].e3 ? 9 : A[0].tm ? 3 : A[0].sh ? 5 : A[0].te ? 7 : 0;
+            const int first = A[0].ac ? 11 : A[0].e3 ? 9 : A[0].tm ? 3 : A[0].sh ? 5 : A[0].te ? 7 : 0;
             const int pending = n < NT - 1 ? 1 : 0;
             launch_adj(H, first, dP, dA, dT, sched, grid, n - n0, pending, st);
             launch_adj(H, first + 1, dP, dA, dT, sched, grid, n - n0, pending, st);
@@ -716,7 +762,9 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         wave_handle* h = shots[s];
         PrepParams G{h->NX, h->NY, h->NZ, h->N};
         const int o = sum ? 0 : s;
-        if (A[s].e3)
+        if (A[s].ac)
+            adj_ac_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
+        else if (A[s].e3)
             adj_e3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
         else if (A[s].tm)
             adj_tm_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],

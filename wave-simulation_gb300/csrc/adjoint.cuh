@@ -40,6 +40,7 @@ struct AdjShot {
     int te;                      // 1: lossless 2-D TEz (parts: hz, ex, ey; psi eyx, exy, hzy, hzx)
     int e3;                      // 1: 3-D elastic (Adj3Part layout)
     int visco;                   // 1: 2-D visco-elastic (the elastic parts, then rxx, ryy, rxy per mechanism)
+    int ac;                      // 1: acoustic, 2-D or 3-D (parts: p, vx, vy, vz; psi p_x, p_y, p_z, vxx, vyy, vzz)
     float* lr[3 * kMaxL];        // adjoint memory variables rxx, ryy, rxy of mechanism l at [k * kMaxL + l]
     float* vprime[3];            // vx', vy' [, vz'] (TMz: hx', hy') of the current step (null: the saved state's are they)
     const long long* sidx;       // sources (velocity sources are taken out of v')
@@ -49,11 +50,15 @@ struct AdjShot {
 };
 
 // launches one adjoint pass over the (shot, tile) work list: 2-D passes 0, 1
-// (elastic), 3, 4 (TMz), 5, 6 (SH), 7, 8 (TEz); 3-D passes 9, 10 (elastic)
+// (elastic and visco-elastic), 3, 4 (TMz), 5, 6 (SH), 7, 8 (TEz); 3-D passes
+// 9, 10 (elastic); acoustic passes 11, 12
 void launch_adj_pass2d(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid,
                        int vn, int pending, cudaStream_t s);
 void launch_adj_pass3d(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid,
                        int vn, int pending, cudaStream_t s);
+// acoustic passes 11, 12 (2-D and 3-D)
+void launch_adj_pass_acoustic(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S,
+                              int grid, int vn, int pending, cudaStream_t s);
 
 namespace adj {
 
@@ -657,6 +662,88 @@ __device__ __forceinline__ void adj_e3_v_body(const StepParams& P, const AdjShot
 }
 
 
+// ---- acoustic (2-D and 3-D) ----------------------------------------------------
+// lf[0..3] = adjoints of p, vx, vy, vz; lpsi[0..2] of the velocity-pass psi
+// p_x, p_y, p_z, lpsi[3..5] of the pressure-pass psi vxx, vyy, vzz; T[0..2] =
+// adjoints of the pressure-pass derivatives c0..c2, T[3..5] of the
+// velocity-pass ones a0..a2; g[0..3] = dJ/dM, dJ/dirx, dJ/diry, dJ/dirz
+
+// pressure-update transpose at step n
+template <int H>
+__device__ __forceinline__ void adj_ac_p_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X1 = A.view + (long long)(vn + 1) * A.stride;
+    const long long i = p.i, sy = (long long)P.NX * P.NZ, sz = P.NX;
+    const float* v1[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v1[k] = A.vprime[0] ? A.vprime[k] : X1 + A.off[1 + k];
+    const Slabs S = slabs_of(P, p);
+    float c0 = deriv<H, false>(v1[0], i, 1, p.x, P.Dxb) + psi_at(X1, A, 7, S, 0);
+    float c1 = deriv<H, false>(v1[1], i, sy, p.y, P.Dyb) + psi_at(X1, A, 8, S, 1);
+    float c2 = P.is3d ? deriv<H, false>(v1[2], i, sz, p.z, P.Dzb) + psi_at(X1, A, 9, S, 2) : 0.0f;
+    float lp = A.lf[0][i];
+    if (pending) {
+        // the transposed velocity-update derivatives of p from the step after this one
+        lp += derivT<H, true>(A.T[3], i, 1, p.x, P.Dxf);
+        lp += derivT<H, true>(A.T[4], i, sy, p.y, P.fs ? P.DyfS : P.Dyf);
+        if (P.is3d) lp += derivT<H, true>(A.T[5], i, sz, p.z, P.Dzf);
+    }
+    if (P.fs && p.y == 0) lp = 0.0f;   // p = 0 on the surface, after the taper
+    if (P.abs) {
+        const float d = absDamp(P, p);
+        lp *= d;
+        A.lf[1][i] *= d;
+        A.lf[2][i] *= d;
+        if (P.is3d) A.lf[3][i] *= d;
+    }
+    A.lf[0][i] = lp;
+    A.g[0][i] += lp * (c0 + c1 + c2);
+    const float l = __ldg(P.m[M_M] + i) * lp;
+    float l0 = l, l1 = l, l2 = l;
+    cpml_adj_axis(P, p, S, l0, A.lpsi[3], 0, false);   // vxx: x, full profile
+    cpml_adj_axis(P, p, S, l1, A.lpsi[4], 1, false);   // vyy: y, full profile
+    if (P.is3d) cpml_adj_axis(P, p, S, l2, A.lpsi[5], 2, false);   // vzz: z, full profile
+    A.T[0][i] = l0;
+    A.T[1][i] = l1;
+    if (P.is3d) A.T[2][i] = l2;
+}
+
+// velocity-update transpose at step n (after the pressure transpose of every point)
+template <int H>
+__device__ __forceinline__ void adj_ac_v_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = (long long)P.NX * P.NZ, sz = P.NX;
+    const float* p0 = X0 + A.off[0];
+    const Slabs S = slabs_of(P, p);
+    const int nd = P.is3d ? 3 : 2;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (k >= nd) break;
+        float lv = A.lf[1 + k][i];
+        float a;
+        if (k == 0) {
+            lv += derivT<H, false>(A.T[0], i, 1, p.x, P.Dxb);
+            a = deriv<H, true>(p0, i, 1, p.x, P.Dxf);
+        } else if (k == 1) {
+            lv += derivT<H, false>(A.T[1], i, sy, p.y, P.Dyb);
+            a = deriv<H, true>(p0, i, sy, p.y, P.fs ? P.DyfS : P.Dyf);
+        } else {
+            lv += derivT<H, false>(A.T[2], i, sz, p.z, P.Dzb);
+            a = deriv<H, true>(p0, i, sz, p.z, P.Dzf);
+        }
+        a += psi_at(X1, A, 4 + k, S, k);
+        const float ir = __ldg(P.m[M_IRX + k] + i);
+        A.g[1 + k][i] += lv * a;
+        float l = ir * lv;
+        cpml_adj_axis(P, p, S, l, A.lpsi[k], k, true);   // p_x, p_y, p_z: half profile
+        A.T[3 + k][i] = l;
+        A.lf[1 + k][i] = lv;
+    }
+}
+
+
 template <int H, int PASS>
 __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
                                                 const BatchTile* __restrict__ W, BatchSched S, int vn, int pending)
@@ -673,7 +760,9 @@ __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ P
         else if (PASS == 7) adj_te_e_body<H>(P, A, p, vn, pending != 0);
         else if (PASS == 8) adj_te_h_body<H>(P, A, p, vn);
         else if (PASS == 9) adj_e3_s_body<H>(P, A, p, vn, pending != 0);
-        else adj_e3_v_body<H>(P, A, p, vn);
+        else if (PASS == 10) adj_e3_v_body<H>(P, A, p, vn);
+        else if (PASS == 11) adj_ac_p_body<H>(P, A, p, vn, pending != 0);
+        else adj_ac_v_body<H>(P, A, p, vn);
     });
 }
 

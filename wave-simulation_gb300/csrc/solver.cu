@@ -786,6 +786,8 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
             h->check(cudaMemcpyAsync(mat(M_VP), dVp, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
             h->check(cudaMemcpyAsync(mat(M_VS), dVs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         }
+        if (eq == WAVE_EQ_ACOUSTIC)   // the acoustic adjoint's chain rule reads vp
+            h->check(cudaMemcpyAsync(mat(M_VP), dVp, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         if (eq == WAVE_EQ_SH && !is3d)   // the SH adjoint's chain rule reads vs
             h->check(cudaMemcpyAsync(mat(M_VS), dVs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         if (needVp) k_modulus(G, dRho, dVp, dTp, sum, 0, mat(M_M), s);
