@@ -158,6 +158,10 @@ constexpr int kEm3d = 100;
 inline int kernel_eq(int eq, bool is3d) { return (is3d && eq >= WAVE_EQ_TMEM) ? eq + kEm3d : eq; }
 using StepKernel = void (*)(StepParams);
 StepKernel kernel_for(int eq, int pass, int H);
+using BatchKernel = void (*)(const StepParams*, const BatchTile*, BatchSched);
+// the EM equations' kernels (kernels_em.cu)
+StepKernel em_kernel_for(int eq, int pass, int H);
+BatchKernel em_batch_kernel_for(int eq, int pass, int H);
 // dep: programmatic dependent launch (the kernel waits for its predecessor in-kernel)
 cudaError_t launch_step_kernel(StepKernel k, dim3 grid, dim3 block, const StepParams& P, bool dep, cudaStream_t s);
 // sources and receivers of one step; returns the launches made (2 when the
