@@ -315,9 +315,27 @@ int wave_set_decomposition(wave_handle* h, int type);
  * super-shot; amp_out the (signed) amplitudes. Random numbers are the C
  * library's rand() after srand(seed) (the reference seeds with time(0)).
  * Host only. The reference's receiver-side encode/decode of per-shot
- * receiver sets (Receivers.cpp:569-573) is not part of this call. */
+ * receiver sets (Receivers.cpp:354-573) is not part of this call. */
 int wave_encode_sources(int mode, int num_domains, unsigned int seed, int n, const int* shot_no, const float* amp,
                         int* shot_no_out, float* amp_out);
+/* The frequency list of the frequency-domain encoding (gradientDomain != 0,
+ * Sources.cpp:587-611): df = 1 / (nFFT DT) with nFFT the next power of two of
+ * NT - 1 (NT = T / DT + 0.5), band indices ceil(fc / df) (fc2 = 0: twice the
+ * CPML centre frequency). encoded != 0: every second frequency from an even
+ * first index (the list the super-shots draw from); encoded = 0: every
+ * frequency of the widened band [ceil(i1 / 2), 2 i2] (the per-shot list of
+ * unencoded frequency-domain modelling). Writes min(cap, n) frequencies to
+ * freqs (may be null) and n to *nfreq. Host only. */
+int wave_encode_frequencies(int encoded, double fc1, double fc2, double T, double DT, double cpml_fc, float* freqs, int cap,
+                            int* nfreq);
+/* Frequency-domain source encoding: wave_encode_sources' super-shot
+ * assignment (the same rand() stream), then each shot of a super-shot draws a
+ * distinct random frequency of the encoded list (Sources.cpp:641-660); the
+ * reference then models each shot with wavelet shape 9 (sin) at fc_out[i].
+ * WAVE_ERR_ARG when the list holds fewer frequencies than shots per
+ * super-shot. Host only. */
+int wave_encode_sources_frequency(int mode, int num_domains, unsigned int seed, int n, const float* amp, double fc1, double fc2,
+                                  double T, double DT, double cpml_fc, int* shot_no_out, float* amp_out, float* fc_out);
 
 /* ---- seismogram output path and file formats ---- */
 /* Resampling of ntr traces (row-major ntr x nt, sample interval dt) to

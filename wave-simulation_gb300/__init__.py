@@ -45,7 +45,8 @@ ABI_SYMBOLS = (
     "wave_write_mtx", "wave_write_su", "wave_get_field", "wave_get_curl_div", "wave_envelope",
     "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
     "wave_agc_normalize_traces", "wave_grid_num_points", "wave_grid_index", "wave_grid_coordinates",
-    "wave_set_decomposition", "wave_grid_operator", "wave_encode_sources",
+    "wave_set_decomposition", "wave_grid_operator", "wave_encode_sources", "wave_encode_frequencies",
+    "wave_encode_sources_frequency",
 )
 
 
@@ -212,6 +213,9 @@ def lib():
     L.wave_grid_coordinates.argtypes = [CP(WaveConfig), P, P, P, i64, P]
     L.wave_grid_operator.argtypes = [CP(WaveConfig), I, CP(I), P, P, i64]
     L.wave_encode_sources.argtypes = [I, I, ctypes.c_uint, I, P, P, P, P]
+    D = ctypes.c_double
+    L.wave_encode_frequencies.argtypes = [I, D, D, D, D, D, P, I, CP(I)]
+    L.wave_encode_sources_frequency.argtypes = [I, I, ctypes.c_uint, I, P, D, D, D, D, D, P, P, P]
     L.wave_batch_last_error.restype = ctypes.c_char_p
     L.wave_batch_last_error.argtypes = [P]
     _lib = L
@@ -289,6 +293,31 @@ def encode_sources(mode: int, num_domains: int, seed: int, shot_no, amp):
                                            no.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p),
                                            no_out.ctypes.data_as(ctypes.c_void_p), a_out.ctypes.data_as(ctypes.c_void_p)))
     return no_out, a_out
+
+
+def encode_frequencies(encoded: bool, fc1: float, fc2: float, T: float, DT: float, cpml_fc: float) -> np.ndarray:
+    """The frequency list of frequency-domain modelling (wave_encode_frequencies)."""
+    n = ctypes.c_int(0)
+    _check(None, lib().wave_encode_frequencies(int(encoded), fc1, fc2, T, DT, cpml_fc, None, 0, ctypes.byref(n)))
+    out = np.zeros(max(n.value, 1), np.float32)
+    _check(None, lib().wave_encode_frequencies(int(encoded), fc1, fc2, T, DT, cpml_fc, out.ctypes.data_as(ctypes.c_void_p),
+                                               out.size, ctypes.byref(n)))
+    return out[:n.value]
+
+
+def encode_sources_frequency(mode: int, num_domains: int, seed: int, amp, fc1: float, fc2: float, T: float, DT: float,
+                             cpml_fc: float):
+    """Frequency-domain source encoding (wave_encode_sources_frequency):
+    (super-shot numbers, signed amplitudes, per-shot frequencies)."""
+    a = np.ascontiguousarray(amp, np.float32)
+    no = np.zeros(a.size, np.int32)
+    ao = np.zeros(a.size, np.float32)
+    fo = np.zeros(a.size, np.float32)
+    _check(None, lib().wave_encode_sources_frequency(int(mode), int(num_domains), int(seed) & 0xFFFFFFFF, a.size,
+                                                     a.ctypes.data_as(ctypes.c_void_p), fc1, fc2, T, DT, cpml_fc,
+                                                     no.ctypes.data_as(ctypes.c_void_p), ao.ctypes.data_as(ctypes.c_void_p),
+                                                     fo.ctypes.data_as(ctypes.c_void_p)))
+    return no, ao, fo
 
 
 def wavelet(shape: int, nt: int, dt: float, fc: float, amp: float, tshift: float) -> np.ndarray:

@@ -222,8 +222,19 @@ int main(int argc, char** argv)
             std::vector<int> no(srcs.size()), noOut(srcs.size());
             std::vector<float> amp(srcs.size()), ampOut(srcs.size());
             for (size_t i = 0; i < srcs.size(); ++i) { no[i] = srcs[i].no; amp[i] = static_cast<float>(srcs[i].amp); }
-            wave::gpu::check(nullptr, wave_encode_sources(encodeMode, domains, seed, static_cast<int>(srcs.size()), no.data(), amp.data(),
-                                                          noOut.data(), ampOut.data()));
+            if (key<int>(keys, "gradientDomain", 0) != 0) {
+                // frequency domain: each shot of a super-shot gets its own frequency
+                // of the band [fc1, fc2] as a synthetic sin wavelet (shape 9)
+                std::vector<float> fc(srcs.size());
+                wave::gpu::check(nullptr, wave_encode_sources_frequency(encodeMode, domains, seed, static_cast<int>(srcs.size()), amp.data(),
+                                                                        key<double>(keys, "fc1", 0.0), key<double>(keys, "fc2", 0.0), cfg.T,
+                                                                        cfg.DT, cfg.CenterFrequencyCPML, noOut.data(), ampOut.data(),
+                                                                        fc.data()));
+                for (size_t i = 0; i < srcs.size(); ++i) { srcs[i].wtype = 1; srcs[i].shape = 9; srcs[i].fc = fc[i]; }
+            } else {
+                wave::gpu::check(nullptr, wave_encode_sources(encodeMode, domains, seed, static_cast<int>(srcs.size()), no.data(), amp.data(),
+                                                              noOut.data(), ampOut.data()));
+            }
             for (size_t i = 0; i < srcs.size(); ++i) { srcs[i].no = noOut[i]; srcs[i].amp = ampOut[i]; }
         }
         std::set<int> shots;
