@@ -375,3 +375,32 @@ def test_acoustic_fused_source_receiver_step_is_bit_identical(dim, wave, refcpu)
     ref = o.run()
     o.close()
     assert rel(a, ref) < TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [2, 4, 8])
+def test_gpu_tez_equals_gpu_sh_under_the_te_sh_analogy(order, wave, refcpu):
+    """The CUDA TEz step against the CUDA SH step (which passes the reference's
+    2-D SH golden): under the TE/SH analogy of test_oracle_em.te_sh_pair the
+    Hz traces equal the mapped vz traces to FP32 rounding (the material
+    coefficients are formed differently: 1/rho from the host's rho = mu_r mu0
+    against 1/(4-point average of mu) with mu = mu_r mu0 formed on the
+    device), and both agree with the FP64 oracle."""
+    from test_oracle_em import te_sh_pair
+    (te, tm, ta), (sh, sm, sa) = te_sh_pair(refcpu, order)
+    out = []
+    for cfg, model, acq, key in ((te, tm, ta, "emem"), (sh, sm, sa, "sh")):
+        s = wave.Factory.Create("2D", key).initForwardSolver(to_wave_cfg(wave, cfg))
+        s.prepareForModelling({k: v.astype(np.float32) for k, v in model.items()})
+        s.setSources(acq[0], acq[1], acq[2].astype(np.float32))
+        s.setReceivers(acq[3], acq[4])
+        s.run(0, s.nt)
+        out.append(s.seismograms().astype(np.float64))
+        s.close()
+    o = refcpu.Oracle(sh, sm, *sa, dtype=np.float64)
+    ref = o.run()
+    o.close()
+    d_te, d_sh = out
+    print(f"TEz vs SH order {order}: rel {rel(d_te, d_sh):.2e}; TEz vs FP64 {rel(d_te, ref):.2e}; SH vs FP64 {rel(d_sh, ref):.2e}")
+    assert rel(d_te, d_sh) <= 1e-5
+    assert rel(d_te, ref) <= 1e-5 and rel(d_sh, ref) <= 1e-5

@@ -95,3 +95,58 @@ def test_lossless_tmz_oracle_equals_the_pinned_acoustic_oracle(boundary, refcpu)
     o.close()
     assert np.abs(p).max() > 0
     assert np.linalg.norm(ez - p) / np.linalg.norm(p) < 1e-8
+
+
+def te_sh_pair(refcpu, order, NX=120, NY=100, nt=150, eps_r=6.0, mu_r=1.2):
+    """A lossless TEz survey and the 2-D SH survey it maps onto: rho = mu_r mu0,
+    shear modulus 1 / (eps_r eps0) (so vs is the EM wave speed), and every SH
+    point one cell up in x and y from its TEz point:
+        vz[x, y] = hz[x-1, y-1],  sxz[x, y] = -ey[x, y-1],  syz[x, y] = ex[x-1, y].
+    Interior rows satisfy Dxb f[x] = Dxf f[x-1], so the SH update of vz from
+    Dxb sxz + Dyb syz is the TEz update of hz from -(Dxf ey - Dyf ex), and the
+    SH stress updates from Dxf vz, Dyf vz are the TEz updates of ey, ex from
+    Dxb hz, Dyb hz (Ca = 1, Cb = 1 / eps on a homogeneous lossless grid); the
+    edge rows differ, so the wavefield must not reach them (no damping
+    boundary, a short run). FD2Demem::run (ForwardSolver2Demem.cpp:112-185),
+    FD2Dsh::run (ForwardSolver2Dsh.cpp:108-196)."""
+    eps0, mu0 = 8.8541878176e-12, 1.2566370614e-6
+    DH = 0.02
+    c = 3e8 / np.sqrt(eps_r * mu_r)
+    DT = 0.3 * DH / (c * np.sqrt(2))
+    n = NX * NY
+    kw = dict(dimension=2, NX=NX, NY=NY, NZ=1, DH=DH, DT=DT, T=(nt - 0.4) * DT, spatialFDorder=order, DampingBoundary=0,
+              FreeSurface=0, edgeOrderReduction=0)
+    te = refcpu.make_config(equation="emem", **kw)
+    sh = refcpu.make_config(equation="sh", **kw)
+    x0, y0 = NX // 2, NY // 2
+    sig = refcpu.ricker(nt, DT, c / (12 * DH), 1.0, 0.0, np.float64)[None]
+    rx = np.arange(30, 90, 7)
+    ry = np.full(rx.size, 35)
+    te_model = dict(eps_r=np.full(n, eps_r), sigma=np.zeros(n), mu_r=np.full(n, mu_r))
+    sh_model = dict(rho=np.full(n, mu_r * mu0), vs=np.full(n, np.sqrt(1.0 / (eps_r * eps0) / (mu_r * mu0))))
+    te_acq = (np.array([x0 + NX * y0], np.int64), np.array([4], np.int32), sig, (rx + NX * ry).astype(np.int64),
+              np.full(rx.size, 4, np.int32))
+    sh_acq = (np.array([(x0 + 1) + NX * (y0 + 1)], np.int64), np.array([4], np.int32), sig,
+              ((rx + 1) + NX * (ry + 1)).astype(np.int64), np.full(rx.size, 4, np.int32))
+    return (te, te_model, te_acq), (sh, sh_model, sh_acq)
+
+
+@pytest.mark.parametrize("order", [2, 4, 8])
+def test_lossless_tez_oracle_equals_the_pinned_sh_oracle(order, refcpu):
+    """The TEz restatement equals the SH restatement (pinned to the reference's
+    2-D SH golden) under the TE/SH analogy: Hz traces equal the mapped vz
+    traces bit for bit and the mapped fields agree to rounding."""
+    (te, tm, ta), (sh, sm, sa) = te_sh_pair(refcpu, order)
+    o = refcpu.Oracle(te, tm, *ta, dtype=np.float64)
+    d_te = o.run()
+    hz, ex, ey = (o.field(k).reshape(te.NY, te.NX) for k in ("hz", "ex", "ey"))
+    o.close()
+    o = refcpu.Oracle(sh, sm, *sa, dtype=np.float64)
+    d_sh = o.run()
+    vz, sxz, syz = (o.field(k).reshape(sh.NY, sh.NX) for k in ("vz", "sxz", "syz"))
+    o.close()
+    assert np.abs(d_sh).max() > 0
+    assert np.array_equal(d_te, d_sh)
+    assert np.abs(vz[1:, 1:] - hz[:-1, :-1]).max() <= 1e-12 * np.abs(vz).max()
+    assert np.abs(sxz[1:, :] + ey[:-1, :]).max() <= 1e-12 * np.abs(sxz).max()
+    assert np.abs(syz[:, 1:] - ex[:, :-1]).max() <= 1e-12 * np.abs(syz).max()
