@@ -404,3 +404,27 @@ def test_gpu_tez_equals_gpu_sh_under_the_te_sh_analogy(order, wave, refcpu):
     print(f"TEz vs SH order {order}: rel {rel(d_te, d_sh):.2e}; TEz vs FP64 {rel(d_te, ref):.2e}; SH vs FP64 {rel(d_sh, ref):.2e}")
     assert rel(d_te, d_sh) <= 1e-5
     assert rel(d_te, ref) <= 1e-5 and rel(d_sh, ref) <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [2, 4, 8])
+def test_gpu_3d_em_splits_into_gpu_tmz_and_tez(order, wave, refcpu):
+    """The CUDA 3-D EM step on z-invariant line sources against the CUDA TMz
+    and TEz steps (test_oracle_em.em3_split_case): the middle slice's Ez and
+    Hz traces agree to FP32 rounding."""
+    from test_oracle_em import em3_split_case
+    out = []
+    for cfg, model, acq in em3_split_case(refcpu, order):
+        s = wave.Factory.Create("3D" if cfg.dimension == 3 else "2D", "tmem" if cfg.equation == 5 else "emem")
+        s = s.initForwardSolver(to_wave_cfg(wave, cfg))
+        s.prepareForModelling({k: v.astype(np.float32) for k, v in model.items()})
+        s.setSources(acq[0], acq[1], acq[2].astype(np.float32))
+        s.setReceivers(acq[3], acq[4])
+        s.run(0, s.nt)
+        out.append(s.seismograms().astype(np.float64))
+        s.close()
+    d3, dtm, dte = out
+    k = dtm.shape[0]
+    e1, e2 = rel(d3[:k], dtm), rel(d3[k:], dte)
+    print(f"3-D EM vs TMz / TEz order {order}: Ez {e1:.2e}, Hz {e2:.2e}")
+    assert e1 <= 1e-5 and e2 <= 1e-5

@@ -150,3 +150,59 @@ def test_lossless_tez_oracle_equals_the_pinned_sh_oracle(order, refcpu):
     assert np.abs(vz[1:, 1:] - hz[:-1, :-1]).max() <= 1e-12 * np.abs(vz).max()
     assert np.abs(sxz[1:, :] + ey[:-1, :]).max() <= 1e-12 * np.abs(sxz).max()
     assert np.abs(syz[:, 1:] - ex[:, :-1]).max() <= 1e-12 * np.abs(syz).max()
+
+
+def em3_split_case(refcpu, order, NX=64, NY=56, NZ=48, nt=90, eps_r=5.0, mu_r=1.1):
+    """A lossless 3-D EM survey with z-invariant line sources (Ez along z, and a
+    Hz line a few cells away) and receivers on the middle z slice, and the
+    lossless TMz and TEz surveys its middle slice splits into: with the
+    fields constant along z the interior z-derivatives vanish, and the 3-D
+    update (ForwardSolver3Demem.cpp:140-237) separates into the TMz step
+    (hx, hy, ez; ForwardSolver2Dtmem.cpp:108-174) and the TEz step (hz, ex,
+    ey; ForwardSolver2Demem.cpp:112-185). The z edges break the invariance;
+    the middle slice stays clear of them for the run's length (no damping
+    boundary). Returns (3-D case, TMz case, TEz case), each (cfg, model, acq)."""
+    DH = 0.02
+    c = 3e8 / np.sqrt(eps_r * mu_r)
+    DT = 0.3 * DH / (c * np.sqrt(3))
+    base = dict(DH=DH, DT=DT, T=(nt - 0.4) * DT, spatialFDorder=order, DampingBoundary=0, FreeSurface=0,
+                edgeOrderReduction=0, NX=NX, NY=NY)
+    c3 = refcpu.make_config(dimension=3, equation="emem", NZ=NZ, **base)
+    ctm = refcpu.make_config(dimension=2, equation="tmem", NZ=1, **base)
+    cte = refcpu.make_config(dimension=2, equation="emem", NZ=1, **base)
+    sig = refcpu.ricker(nt, DT, c / (12 * DH), 1.0, 0.0, np.float64)
+    x0, y0, zc = NX // 2, NY // 2, NZ // 2
+    rx = np.arange(16, 48, 5)
+    ry = np.full(rx.size, 18)
+    n3, n2 = NX * NY * NZ, NX * NY
+    m3 = dict(eps_r=np.full(n3, eps_r), sigma=np.zeros(n3), mu_r=np.full(n3, mu_r))
+    m2 = dict(eps_r=np.full(n2, eps_r), sigma=np.zeros(n2), mu_r=np.full(n2, mu_r))
+    zs = np.arange(NZ)
+    acq3 = (np.concatenate([x0 + NX * (zs + NZ * y0), (x0 - 5) + NX * (zs + NZ * (y0 + 3))]).astype(np.int64),
+            np.concatenate([np.full(NZ, 1), np.full(NZ, 4)]).astype(np.int32),
+            np.concatenate([np.tile(sig, (NZ, 1)), np.tile(300.0 * sig, (NZ, 1))]),
+            np.concatenate([rx + NX * (zc + NZ * ry), rx + NX * (zc + NZ * ry)]).astype(np.int64),
+            np.concatenate([np.full(rx.size, 1), np.full(rx.size, 4)]).astype(np.int32))
+    acqtm = (np.array([x0 + NX * y0], np.int64), np.array([1], np.int32), sig[None], (rx + NX * ry).astype(np.int64),
+             np.full(rx.size, 1, np.int32))
+    acqte = (np.array([(x0 - 5) + NX * (y0 + 3)], np.int64), np.array([4], np.int32), 300.0 * sig[None],
+             (rx + NX * ry).astype(np.int64), np.full(rx.size, 4, np.int32))
+    return (c3, m3, acq3), (ctm, m2, acqtm), (cte, m2, acqte)
+
+
+@pytest.mark.parametrize("order", [2, 4, 8])
+def test_lossless_3d_em_oracle_splits_into_the_pinned_tmz_and_tez(order, refcpu):
+    """The 3-D EM restatement on z-invariant sources equals, on its middle
+    slice, the TMz and TEz restatements (pinned to the acoustic and SH goldens
+    by the maps above): Ez and Hz traces to 1e-11 relative (the residual is
+    the z edges' reach through the stencils)."""
+    out = []
+    for cfg, model, acq in em3_split_case(refcpu, order):
+        o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+        out.append(o.run())
+        o.close()
+    d3, dtm, dte = out
+    k = dtm.shape[0]
+    assert np.abs(dtm).max() > 0 and np.abs(dte).max() > 0
+    assert np.linalg.norm(d3[:k] - dtm) <= 1e-11 * np.linalg.norm(dtm)
+    assert np.linalg.norm(d3[k:] - dte) <= 1e-11 * np.linalg.norm(dte)
