@@ -314,8 +314,7 @@ int wave_set_decomposition(wave_handle* h, int type);
  * runs of ceil(n / num_domains) shots. shot_no_out[i] = num_domains*10^4 + 1 +
  * super-shot; amp_out the (signed) amplitudes. Random numbers are the C
  * library's rand() after srand(seed) (the reference seeds with time(0)).
- * Host only. The reference's receiver-side encode/decode of per-shot
- * receiver sets (Receivers.cpp:354-573) is not part of this call. */
+ * Host only. The receiver side (Receivers.cpp:354-573) is wave_encode_traces. */
 int wave_encode_sources(int mode, int num_domains, unsigned int seed, int n, const int* shot_no, const float* amp,
                         int* shot_no_out, float* amp_out);
 /* The frequency list of the frequency-domain encoding (gradientDomain != 0,
@@ -336,6 +335,25 @@ int wave_encode_frequencies(int encoded, double fc1, double fc2, double T, doubl
  * super-shot. Host only. */
 int wave_encode_sources_frequency(int mode, int num_domains, unsigned int seed, int n, const float* amp, double fc1, double fc2,
                                   double T, double DT, double cpml_fc, int* shot_no_out, float* amp_out, float* fc_out);
+/* Receiver-side encoding of seismograms for one receiver component
+ * (Receivers::encode / Receivers::decode, Receivers.cpp:354-573): the shots of
+ * one super-shot summed into its receiver rows (decode = 0) or split back out
+ * (decode = 1). mark: nshots x nrec (receiver r recorded for shot s when
+ * nonzero), super_mark: nrec (receiver r is in the super-shot), amp: the
+ * shots' encoded amplitudes (a negative one flips the shot's traces), fc:
+ * the shots' frequencies (null: no filter; else the single-frequency ideal
+ * band-pass of frequency-domain modelling, Filter.cpp:239-342, with DT).
+ * Multi-offset data (common_offset = 0): shot_data[s] holds the rows of the
+ * shot's marked receivers among the super-shot's, in receiver order;
+ * super_data one row per super-shot receiver; the filter is the block form
+ * (2 / nFFT, then divided by the block's largest magnitude). Common-offset
+ * data (common_offset = 1, nshots == nrec): one trace per shot, super row k
+ * the k-th shot whose receiver is in the super-shot, added (or received) only
+ * where the shot's own receiver is marked for it (elsewhere the decoded trace
+ * is zero), the single-trace filter (1 / NT). Rows are nt samples; shot_data
+ * is a host array of nshots pointers, all data in `mem`. */
+int wave_encode_traces(int decode, int nshots, int nrec, int64_t nt, const int* mark, const int* super_mark, const float* amp,
+                       const float* fc, double DT, int common_offset, float* const* shot_data, float* super_data, int mem);
 
 /* ---- seismogram output path and file formats ---- */
 /* Resampling of ntr traces (row-major ntr x nt, sample interval dt) to

@@ -46,7 +46,7 @@ ABI_SYMBOLS = (
     "wave_instantaneous_phase", "wave_selftest_bounded_wait", "wave_set_dependent_launch",
     "wave_agc_normalize_traces", "wave_grid_num_points", "wave_grid_index", "wave_grid_coordinates",
     "wave_set_decomposition", "wave_grid_operator", "wave_encode_sources", "wave_encode_frequencies",
-    "wave_encode_sources_frequency",
+    "wave_encode_sources_frequency", "wave_encode_traces",
 )
 
 
@@ -216,6 +216,7 @@ def lib():
     D = ctypes.c_double
     L.wave_encode_frequencies.argtypes = [I, D, D, D, D, D, P, I, CP(I)]
     L.wave_encode_sources_frequency.argtypes = [I, I, ctypes.c_uint, I, P, D, D, D, D, D, P, P, P]
+    L.wave_encode_traces.argtypes = [I, I, I, ctypes.c_int64, P, P, P, P, D, I, P, P, I]
     L.wave_batch_last_error.restype = ctypes.c_char_p
     L.wave_batch_last_error.argtypes = [P]
     _lib = L
@@ -318,6 +319,38 @@ def encode_sources_frequency(mode: int, num_domains: int, seed: int, amp, fc1: f
                                                      no.ctypes.data_as(ctypes.c_void_p), ao.ctypes.data_as(ctypes.c_void_p),
                                                      fo.ctypes.data_as(ctypes.c_void_p)))
     return no, ao, fo
+
+
+def encode_traces(decode: bool, mark, super_mark, amp, fc=None, DT: float = 0.0, common_offset: bool = False,
+                  shot_data=None, super_data=None, nt: int = 0):
+    """Receiver-side encoding (wave_encode_traces) on host arrays: decode=False
+    returns the super-shot block from the list of per-shot blocks, decode=True
+    the list of per-shot blocks from the super-shot block."""
+    mark = np.ascontiguousarray(mark, np.int32)
+    sm = np.ascontiguousarray(super_mark, np.int32)
+    a = np.ascontiguousarray(amp, np.float32)
+    ns, nr = mark.shape
+    f = None if fc is None else np.ascontiguousarray(fc, np.float32)
+    if common_offset:
+        rows = [1] * ns
+        nsup = int(np.count_nonzero(sm))
+    else:
+        rows = [int(np.count_nonzero((mark[s] != 0) & (sm != 0))) for s in range(ns)]
+        nsup = int(np.count_nonzero(sm))
+    if decode:
+        sup = np.ascontiguousarray(super_data, np.float32)
+        nt = sup.shape[-1]
+        shots = [np.zeros((r, nt), np.float32) for r in rows]
+    else:
+        shots = [np.ascontiguousarray(d, np.float32).reshape(r, -1) for d, r in zip(shot_data, rows)]
+        nt = shots[0].shape[-1]
+        sup = np.zeros((nsup, nt), np.float32)
+    ptrs = (ctypes.c_void_p * ns)(*[d.ctypes.data_as(ctypes.c_void_p).value for d in shots])
+    _check(None, lib().wave_encode_traces(int(decode), ns, nr, nt, mark.ctypes.data_as(ctypes.c_void_p),
+                                          sm.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p),
+                                          None if f is None else f.ctypes.data_as(ctypes.c_void_p), float(DT), int(common_offset),
+                                          ptrs, sup.ctypes.data_as(ctypes.c_void_p), MEM_HOST))
+    return shots if decode else sup
 
 
 def wavelet(shape: int, nt: int, dt: float, fc: float, amp: float, tshift: float) -> np.ndarray:
