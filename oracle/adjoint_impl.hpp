@@ -894,9 +894,13 @@ struct ElasticAdjoint3D {
     static constexpr const char* kP[9] = {"sxx_x", "sxy_y", "sxz_z", "sxy_x", "syy_y", "syz_z", "sxz_x", "syz_y", "szz_z"};
     static constexpr const char* kQ[9] = {"vxx", "vyy", "vzz", "vxy", "vyx", "vxz", "vzx", "vyz", "vzy"};
 
-    explicit ElasticAdjoint3D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    const bool visco;   // 3-D visco-elastic (FD3Dviscoelastic::run, ForwardSolver3Dviscoelastic.cpp:132-457)
+
+    explicit ElasticAdjoint3D(Sim<T>& sim) : s(sim), N(sim.g.N()), visco(sim.eq == WAVE_EQ_VISCOELASTIC)
     {
-        if (!s.is3d || s.eq != WAVE_EQ_ELASTIC) throw std::invalid_argument("oracle adjoint: 3-D elastic only");
+        if (!s.is3d || (s.eq != WAVE_EQ_ELASTIC && s.eq != WAVE_EQ_VISCOELASTIC))
+            throw std::invalid_argument("oracle adjoint: 3-D elastic or visco-elastic only");
+        if (visco && s.fs) throw std::invalid_argument("oracle adjoint: the visco-elastic free surface is not differentiated");
         DxfT = transpose(s.Dxf);
         DxbT = transpose(s.Dxb);
         DyfT = transpose(s.Dyf);
@@ -908,6 +912,7 @@ struct ElasticAdjoint3D {
     }
     struct State {
         std::map<std::string, std::vector<T>> F, psi;
+        std::map<std::string, std::vector<std::vector<T>>> R;
     };
     const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
     {
@@ -946,7 +951,7 @@ struct ElasticAdjoint3D {
         s.reset();
         std::vector<State> ck;
         for (int t = 0; t < NT; ++t) {
-            if (t % K == 0) ck.push_back({s.F, s.psi});
+            if (t % K == 0) ck.push_back({s.F, s.psi, s.R});
             s.step(t);
         }
         std::vector<T> res(nrec * static_cast<size_t>(NT));
@@ -959,6 +964,8 @@ struct ElasticAdjoint3D {
         for (const char* n : {"vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz"}) lF[n].assign(N, 0);
         for (int k = 0; k < 9; ++k) { lpsi[kP[k]].assign(N, 0); lpsi[kQ[k]].assign(N, 0); }
         std::vector<T> gM(N, 0), gMu(N, 0), gMuXY(N, 0), gMuXZ(N, 0), gMuYZ(N, 0), gIrx(N, 0), gIry(N, 0), gIrz(N, 0);
+        // adjoint memory variables rxx, ryy, rzz, rxy, rxz, ryz per mechanism (visco)
+        std::vector<std::vector<std::vector<T>>> lR(6, std::vector<std::vector<T>>(visco ? s.L : 0, std::vector<T>(N, 0)));
         std::vector<T> a[9], c[9], la[9], lc[9], vxp(N), vyp(N), vzp(N);
         for (int k = 0; k < 9; ++k) { a[k].assign(N, 0); c[k].assign(N, 0); la[k].assign(N, 0); lc[k].assign(N, 0); }
         const CSR<T>& DybS = s.fs ? s.DybFS : s.Dyb;
@@ -969,10 +976,11 @@ struct ElasticAdjoint3D {
             std::vector<State> X;
             s.F = ck[seg].F;
             s.psi = ck[seg].psi;
-            X.push_back({s.F, s.psi});
+            s.R = ck[seg].R;
+            X.push_back({s.F, s.psi, s.R});
             for (int t = t0; t < t1; ++t) {
                 s.step(t);
-                X.push_back({s.F, s.psi});
+                X.push_back({s.F, s.psi, s.R});
             }
             for (int t = t1 - 1; t >= t0; --t) {
                 const State& X0 = X[t - t0];
@@ -1059,6 +1067,58 @@ struct ElasticAdjoint3D {
                         }
                     });
                 }
+                if (visco) {
+                    // per mechanism l, with e = c0' + c1' + c2' and q the normal stress's
+                    // partner sum (c1' + c2', c0' + c2', c0' + c1'), and for the shear
+                    // stresses m = mu_plane (its two cross derivatives):
+                    //   Rk' = c2_l (c1_l Rk - tauP M e / tau_l + tauS 2 mu q / tau_l)
+                    //   Sk' = Sk + DT/2 sum_l (Rk + Rk') + (1 + L tauP) M e - (1 + L tauS) 2 mu q
+                    //   Rs' = c2_l (c1_l Rs - tauS_plane m / tau_l), Ss' = Ss + DT/2 sum_l (Rs + Rs') + (1 + L tauS) m
+                    const T DTh = s.DThalf;
+                    for_n(N, [&](idx_t i) {
+                        const T e = c[0][i] + c[1][i] + c[2][i], M = s.M[i], mu = s.mu[i];
+                        const T tP = s.tauP[i], tS = s.tauS[i], opP = s.onePlusLtauP[i], opS = s.onePlusLtauS[i];
+                        const T q[3] = {c[1][i] + c[2][i], c[0][i] + c[2][i], c[0][i] + c[1][i]};
+                        const T lS3[3] = {lxx[i], lyy[i], lzz[i]};
+                        T le = 0, lq[3] = {0, 0, 0};
+                        for (int k = 0; k < 3; ++k) {
+                            const T lS = lS3[k];
+                            le += opP * M * lS;
+                            lq[k] -= opS * T(2) * mu * lS;
+                            gM[i] += opP * e * lS;
+                            gMu[i] -= opS * T(2) * q[k] * lS;
+                            for (int l = 0; l < s.L; ++l) {
+                                const T c1 = s.viscoC1[l], c2 = s.viscoC2[l], irt = s.invRelaxTime[l];
+                                const T LR = lR[k][l][i] + DTh * lS;
+                                lR[k][l][i] = c2 * c1 * LR + DTh * lS;
+                                le -= c2 * irt * tP * M * LR;
+                                lq[k] += c2 * irt * tS * T(2) * mu * LR;
+                                gM[i] -= c2 * irt * tP * e * LR;
+                                gMu[i] += c2 * irt * tS * T(2) * q[k] * LR;
+                            }
+                        }
+                        lc[0][i] += le + lq[1] + lq[2];
+                        lc[1][i] += le + lq[0] + lq[2];
+                        lc[2][i] += le + lq[0] + lq[1];
+                        const T lSh[3] = {lxy[i], lxz[i], lyz[i]};
+                        const T muP[3] = {s.muXY[i], s.muXZ[i], s.muYZ[i]};
+                        const T tauPl[3] = {s.tauSXY[i], s.tauSXZ[i], s.tauSYZ[i]};
+                        std::vector<T>* gP[3] = {&gMuXY, &gMuXZ, &gMuYZ};
+                        for (int k = 0; k < 3; ++k) {
+                            const T lS = lSh[k], sh = c[3 + 2 * k][i] + c[4 + 2 * k][i];
+                            T lm = opS * lS;
+                            for (int l = 0; l < s.L; ++l) {
+                                const T c1 = s.viscoC1[l], c2 = s.viscoC2[l], irt = s.invRelaxTime[l];
+                                const T LR = lR[3 + k][l][i] + DTh * lS;
+                                lR[3 + k][l][i] = c2 * c1 * LR + DTh * lS;
+                                lm -= c2 * irt * tauPl[k] * LR;
+                            }
+                            (*gP[k])[i] += sh * lm;
+                            lc[3 + 2 * k][i] += muP[k] * lm;
+                            lc[4 + 2 * k][i] += muP[k] * lm;
+                        }
+                    });
+                } else
                 for_n(N, [&](idx_t i) {
                     const T ls = lxx[i] + lyy[i] + lzz[i];
                     lc[0][i] += s.M[i] * ls - T(2) * s.mu[i] * (lyy[i] + lzz[i]);
@@ -1127,14 +1187,25 @@ struct ElasticAdjoint3D {
             for_n(N, [&](idx_t r) { y[r] = -(*gIr[a3])[r] * (*ir[a3])[r] * (*ir[a3])[r]; });
             probe.avgT([&](const T* in, T* out) { average2<T>(s.g, axes[a3], in, out); }, y, grhoAvg);
         }
+        // visco: M = rho vp^2 / (1 + sum tauP), mu = rho vs^2 / (1 + sum tauS), relaxation times fixed
+        T sum = 0;
+        if (visco) {
+            const T w_ref = static_cast<T>(2.0 * M_PI * s.cfg.CenterFrequencyCPML);
+            for (int l = 0; l < s.L; ++l) {
+                const T ts = static_cast<T>(1.0 / (2.0 * M_PI * static_cast<T>(s.cfg.relaxationFrequency[l])));
+                sum += w_ref * w_ref * ts * ts / (T(1.0) + w_ref * w_ref * ts * ts);
+            }
+        }
         for (idx_t k = 0; k < N; ++k) {
+            const T fP = visco ? T(1) + sum * s.tauP[k] : T(1), fS = visco ? T(1) + sum * s.tauS[k] : T(1);
             T raw = rho[k];
             raw *= vs[k];
             raw *= vs[k];
+            if (visco) raw = raw / fS;
             const bool unclamped = raw >= T(1);
-            gvp[k] = gM[k] * T(2) * rho[k] * vp[k];
-            gvs[k] = unclamped ? gmuc[k] * T(2) * rho[k] * vs[k] : T(0);
-            grho[k] = gM[k] * vp[k] * vp[k] + (unclamped ? gmuc[k] * vs[k] * vs[k] : T(0)) + grhoAvg[k];
+            gvp[k] = gM[k] * T(2) * rho[k] * vp[k] / fP;
+            gvs[k] = unclamped ? gmuc[k] * T(2) * rho[k] * vs[k] / fS : T(0);
+            grho[k] = gM[k] * vp[k] * vp[k] / fP + (unclamped ? gmuc[k] * vs[k] * vs[k] / fS : T(0)) + grhoAvg[k];
         }
         return J;
     }

@@ -115,3 +115,49 @@ def test_elastic3d_checkpoint_interval_and_batch(wave, refcpu):
         assert abs(mis[k] - single[k][0]) <= 1e-12 * abs(single[k][0])
         for got, want in zip((gvp[k], gvs[k], grho[k]), single[k][1:]):
             assert np.abs(want).max() > 0 and np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("L,boundary,stencil,reduce,order", [(1, 2, 0, 0, 4), (2, 1, 0, 1, 6), (2, 0, 1, 0, 2)])
+def test_visco3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, L, boundary, stencil, reduce, order):
+    """3-D visco-elastic (FD3Dviscoelastic::run, ForwardSolver3Dviscoelastic.cpp:132-457): six memory
+    variables per mechanism, vp / vs / rho gradients with the relaxation times fixed, against the
+    oracle's FP64 adjoint (pinned to FP64 finite differences); the free surface is refused."""
+    ocfg, model, acq = el3_case(refcpu, 0, boundary, stencil, reduce, order=order, NX=40, NY=32, NZ=36, nt=260, L=L)
+    cfg = _wave_cfg(wave, ocfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
+    blob = np.exp(-((x - cfg.NX * 0.5) ** 2 + (y - cfg.NY * 0.55) ** 2 + (z - cfg.NZ * 0.5) ** 2) / 40.0).reshape(-1)
+    true = dict(m32)
+    true["vp"] = (m32["vp"] * (1 + 0.05 * blob)).astype(np.float32)
+    true["vs"] = (m32["vs"] * (1 - 0.04 * blob)).astype(np.float32)
+    acq32 = (acq[0], acq[1], acq[2].astype(np.float32), acq[3], acq[4])
+
+    def solver(model_):
+        s = wave.Factory.Create("3D", "viscoelastic").initForwardSolver(cfg)
+        s.prepareForModelling(model_)
+        s.setSources(*acq32[:3])
+        s.setReceivers(*acq32[3:])
+        return s
+
+    s = solver(true)
+    s.run(0, s.nt)
+    dobs = (0.8 * s.seismograms()).astype(np.float32)
+    s.close()
+    s = solver(m32)
+    J, gvp, gvs, grho = s.adjoint_gradient(dobs, checkpoint_every=45)
+    s.close()
+    o = refcpu.Oracle(ocfg, {k: v.astype(np.float64) for k, v in m32.items()}, acq32[0], acq32[1],
+                      acq32[2].astype(np.float64), acq32[3], acq32[4], dtype=np.float64)
+    J64, rvp, rvs, rrho = o.adjoint_gradient(dobs.astype(np.float64), checkpoint_every=45)
+    o.close()
+    errs = [_rel(gvp, rvp), _rel(gvs, rvs), _rel(grho, rrho)]
+    print(f"3-D visco adjoint L={L} boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} "
+          f"vs FP64 {J64:.6e}; gradient rel L2 vp {errs[0]:.2e} vs {errs[1]:.2e} rho {errs[2]:.2e}")
+    assert J > 0 and abs(J - J64) <= 1e-4 * J64
+    assert max(errs) <= GRAD_TOL
+    cfg.FreeSurface = 1
+    s = solver(m32)
+    with pytest.raises(wave.WaveError) as e:
+        s.adjoint_gradient(dobs)
+    assert e.value.code == wave.WAVE_ERR_UNSUPPORTED
+    s.close()

@@ -274,18 +274,24 @@ def test_oracle_tez_adjoint_matches_fp64_finite_differences(refcpu, boundary, st
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
 
 
-def el3_case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=24, NY=20, NZ=18, nt=110):
+def el3_case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=24, NY=20, NZ=18, nt=110, L=0):
+    """3-D elastic survey; L > 0: visco-elastic with L relaxation mechanisms."""
     rng = np.random.default_rng(21)
     y, z, x = np.mgrid[0:NY, 0:NZ, 0:NX]   # index x + NX (z + NZ y)
     vp = 2000.0 + 500.0 * (y / NY) + 60.0 * np.sin(x / 4.0) + 40.0 * np.cos(z / 3.0) + 20 * rng.standard_normal((NY, NZ, NX))
     vs = vp / 1.8
     rho = 300.0 * vp ** 0.25
-    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(vp=vp, vs=vs, rho=rho).items()}
+    fields = dict(vp=vp, vs=vs, rho=rho)
+    if L:
+        fields["taup"] = 0.04 + 0.01 * np.sin(x / 5.0) + 0.005 * np.cos(z / 4.0)
+        fields["taus"] = 0.05 + 0.01 * np.cos(y / 4.0)
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in fields.items()}
     DH, DT = 5.0, 4e-4
-    cfg = refcpu.make_config(dimension=3, equation="elastic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=(nt - 0.4) * DT,
-                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary, BoundaryWidth=5,
-                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=25.0, VMaxCPML=2600.0,
-                             useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    cfg = refcpu.make_config(dimension=3, equation="viscoelastic" if L else "elastic", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT,
+                             T=(nt - 0.4) * DT, spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary,
+                             BoundaryWidth=5, DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=25.0, VMaxCPML=2600.0,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce, numRelaxationMechanisms=L,
+                             relaxationFrequency=[20.0, 50.0][:L])
     sidx = np.array([refcpu.grid_index(cfg, NX // 2, 2 if fs else 5, NZ // 2),
                      refcpu.grid_index(cfg, NX // 3, 7, NZ // 3)], np.int64)
     sig = refcpu.ricker(nt, DT, 30.0, 1.0, -0.015, np.float64)
@@ -416,6 +422,38 @@ def test_oracle_acoustic_adjoint_matches_fp64_finite_differences(refcpu, dim, fs
     grads = dict(vp=gvp, rho=grho)
     for name in ("vp", "rho"):
         d = (smooth3(rng, cfg) if dim == 3 else smooth_direction(rng, cfg.NY, cfg.NX)) * model[name]
+        h = 1e-5
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name] + h * d
+        mm[name] = model[name] - h * d
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        ad = float(np.dot(grads[name], d))
+        assert abs(fd) > 0
+        assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
+
+
+@pytest.mark.parametrize("L,boundary,stencil,reduce", [(1, 2, 0, 1), (2, 1, 1, 0), (2, 0, 0, 1)])
+def test_oracle_visco3d_adjoint_matches_fp64_finite_differences(refcpu, L, boundary, stencil, reduce):
+    """The oracle's FP64 adjoint of the 3-D visco-elastic step (six memory
+    variables per mechanism; vp, vs, rho with the relaxation times fixed)
+    against central finite differences of its own misfit."""
+    cfg, model, acq = el3_case(refcpu, 0, boundary, stencil, reduce, L=L)
+    true = dict(model)
+    y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
+    blob = np.exp(-((x - cfg.NX * 0.5) ** 2 + (y - cfg.NY * 0.55) ** 2 + (z - cfg.NZ * 0.5) ** 2) / 18.0).reshape(-1)
+    true["vp"] = model["vp"] * (1 + 0.05 * blob)
+    true["vs"] = model["vs"] * (1 - 0.04 * blob)
+    o = refcpu.Oracle(cfg, true, *acq, dtype=np.float64)
+    dobs = 0.9 * o.run()
+    o.close()
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    J, gvp, gvs, grho = o.adjoint_gradient(dobs, checkpoint_every=37)
+    o.close()
+    assert J > 0 and J == pytest.approx(misfit(refcpu, cfg, model, acq, dobs), rel=1e-12)
+    rng = np.random.default_rng(41)
+    grads = dict(vp=gvp, vs=gvs, rho=grho)
+    for name in ("vp", "vs", "rho"):
+        d = smooth3(rng, cfg) * model[name]
         h = 1e-5
         mp, mm = dict(model), dict(model)
         mp[name] = model[name] + h * d

@@ -445,7 +445,8 @@ __device__ __forceinline__ float w4p(int a, int b, int ka, int kb, int Na, int N
 // chain rule for 3-D elastic: M = rho vp^2; mu = max(rho vs^2, 1); muXY, muXZ,
 // muYZ = 1 / (4-point average of 1 / mu in the xy, xz, yz planes) (0 below 4);
 // irx, iry, irz = 1 / (2-point average of rho along x, y, z) (0 where invalid)
-__global__ void adj_e3_final(PrepParams G, const StepParams P, const AdjShot A, float* gvp, float* gvs, float* grho, int accumulate)
+__global__ void adj_e3_final(PrepParams G, const StepParams P, const AdjShot A, float vsum, float* gvp, float* gvs, float* grho,
+                             int accumulate)
 {
     const long long sy = (long long)G.NX * G.NZ, sz = G.NX;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
@@ -480,12 +481,15 @@ __global__ void adj_e3_final(PrepParams G, const StepParams P, const AdjShot A, 
                     if (w != 0.0f) gmu += A.g[4][r] * w * (m / muk) * (m / muk);
                 }
             }
+        // visco: M = rho vp^2 / fP, mu = max(rho vs^2 / fS, 1) with f = 1 + sum tau (the relaxation times held fixed)
+        const float fP = A.visco ? 1.0f + vsum * P.m[M_TAUP][k] : 1.0f, fS = A.visco ? 1.0f + vsum * P.m[M_TAUS][k] : 1.0f;
         float raw = rho;
         raw *= vs;
         raw *= vs;
+        if (A.visco) raw = raw / fS;
         const bool unclamped = raw >= 1.0f;
-        float gr = A.g[0][k] * vp * vp;
-        if (unclamped) gr += gmu * vs * vs;
+        float gr = A.g[0][k] * vp * vp / fP;
+        if (unclamped) gr += gmu * vs * vs / fS;
         // inverse density averages: rows k and k - 1 along each axis
         const int kc[3] = {kx, ky, kz};
         const int Nc[3] = {static_cast<int>(G.NX), static_cast<int>(G.NY), static_cast<int>(G.NZ)};
@@ -499,8 +503,8 @@ __global__ void adj_e3_final(PrepParams G, const StepParams P, const AdjShot A, 
                 const float w = (kc[ax] - d + 1 < Nc[ax]) ? 0.5f : 1.0f;
                 if (ir != 0.0f && (d == 0 || w == 0.5f)) gr -= A.g[5 + ax][r] * ir * ir * w;
             }
-        const float gp = A.g[0][k] * 2.0f * rho * vp;
-        const float gs = unclamped ? gmu * 2.0f * rho * vs : 0.0f;
+        const float gp = A.g[0][k] * 2.0f * rho * vp / fP;
+        const float gs = unclamped ? gmu * 2.0f * rho * vs / fS : 0.0f;
         if (accumulate) { gvp[k] += gp; gvs[k] += gs; grho[k] += gr; }
         else { gvp[k] = gp; gvs[k] = gs; grho[k] = gr; }
     }
@@ -546,10 +550,10 @@ std::string adjoint_supported(const wave_handle* h)
     const wave_config& c = h->cfg;
     const bool ok2 = c.dimension == 2 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_SH ||
                                           c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC);
-    const bool ok3 = c.dimension == 3 && c.equation == WAVE_EQ_ELASTIC;
+    const bool ok3 = c.dimension == 3 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_VISCOELASTIC);
     const bool okAc = c.equation == WAVE_EQ_ACOUSTIC;
     if (!ok2 && !ok3 && !okAc)
-        return "the adjoint gradient is implemented for 2-D and 3-D acoustic and elastic, 2-D visco-elastic, 2-D SH and lossless "
+        return "the adjoint gradient is implemented for 2-D and 3-D acoustic, elastic and visco-elastic, 2-D SH and lossless "
                "2-D TMz and TEz modelling";
     if (okAc && c.FreeSurface == 2) return "the acoustic adjoint takes the mirror free surface (FreeSurface = 1) or none";
     if (c.equation == WAVE_EQ_VISCOELASTIC && c.FreeSurface != 0)
@@ -619,7 +623,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int* psiSlot = ac ? acPsi : e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
         // visco-elastic: the elastic parts, then rxx, ryy, rxy of each mechanism
         const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC;
-        const int nr = visco ? 3 * h->L : 0;
+        const int ncomp = e3 ? 6 : 3;   // memory-variable components per mechanism
+        const int nr = visco ? ncomp * h->L : 0;
         const int nf = ac ? 4 : e3 ? 9 : 5, np = ac ? 6 : e3 ? 18 : 8, nparts = nf + np + nr;
         for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
         for (int k = 0; k < np; ++k) {
@@ -628,7 +633,9 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             len[nf + k] = (slot >= 0 && h->psi[slot]) ? h->psiLen[slot] : 0;
             o += len[nf + k];
         }
-        const int memVar[3] = {R_XX, R_YY, R_XY};
+        const int memVar2[3] = {R_XX, R_YY, R_XY};
+        const int memVar3[6] = {R_XX, R_YY, R_ZZ, R_XY, R_XZ, R_YZ};
+        const int* memVar = e3 ? memVar3 : memVar2;
         auto rpart = [&](int j) { return h->r[memVar[j / h->L]][j % h->L]; };
         for (int j = 0; j < nr; ++j) { off[nf + np + j] = o; len[nf + np + j] = N; o += N; }
         stride[s] = o;
@@ -646,7 +653,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         ck(cudaMemsetAsync(lstate, 0, o * sizeof(float), st), "memset");
         for (int k = 0; k < nf; ++k) a.lf[k] = lstate + off[k];
         for (int k = 0; k < np; ++k) a.lpsi[k] = lstate + off[nf + k];
-        for (int k = 0; k < 3 * kMaxL; ++k) a.lr[k] = nullptr;
+        for (int k = 0; k < 6 * kMaxL; ++k) a.lr[k] = nullptr;
         for (int j = 0; j < nr; ++j) a.lr[(j / h->L) * kMaxL + j % h->L] = lstate + off[nf + np + j];
         const int ntemp = e3 ? 18 : 8, ngrad = e3 ? 8 : 5;   // acoustic: 6 and 4 of them
         float* temps = pool.get<float>(static_cast<size_t>(ntemp) * N);
@@ -765,7 +772,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         if (A[s].ac)
             adj_ac_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
         else if (A[s].e3)
-            adj_e3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
+            adj_e3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], A[s].visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f, gvp[o], gvs[o],
+                                               grho[o], sum && s > 0 ? 1 : 0);
         else if (A[s].tm)
             adj_tm_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
                                                sum && s > 0 ? 1 : 0);

@@ -18,7 +18,7 @@ enum Adj3Part {
     E3_VX, E3_VY, E3_VZ, E3_SXX, E3_SYY, E3_SZZ, E3_SXY, E3_SXZ, E3_SYZ,
     E3_P0, E3_Q0 = E3_P0 + 9, E3_COUNT = E3_Q0 + 9
 };
-constexpr int kAdjMaxParts = E3_COUNT;
+constexpr int kAdjMaxParts = E3_COUNT + 6 * kMaxL;   // 3-D visco-elastic: six memory variables per mechanism
 
 // psi slot of each psi part: velocity pass P1..P4, stress pass Q1..Q4
 static const int kAdjPsiSlot[8] = {PS_SXX_X, PS_SXY_Y, PS_SXY_X, PS_SYY_Y, PS_VXX, PS_VYY, PS_VXY, PS_VYX};
@@ -39,9 +39,10 @@ struct AdjShot {
     int sh;                      // 1: 2-D SH (parts: vz, sxz, syz; psi sxz_x, syz_y, vzx, vzy)
     int te;                      // 1: lossless 2-D TEz (parts: hz, ex, ey; psi eyx, exy, hzy, hzx)
     int e3;                      // 1: 3-D elastic (Adj3Part layout)
-    int visco;                   // 1: 2-D visco-elastic (the elastic parts, then rxx, ryy, rxy per mechanism)
+    int visco;                   // 1: visco-elastic (the elastic parts, then the memory variables per mechanism)
     int ac;                      // 1: acoustic, 2-D or 3-D (parts: p, vx, vy, vz; psi p_x, p_y, p_z, vxx, vyy, vzz)
-    float* lr[3 * kMaxL];        // adjoint memory variables rxx, ryy, rxy of mechanism l at [k * kMaxL + l]
+    float* lr[6 * kMaxL];        // adjoint memory variables of mechanism l at [k * kMaxL + l]: 2-D rxx, ryy, rxy;
+                                 // 3-D rxx, ryy, rzz, rxy, rxz, ryz
     float* vprime[3];            // vx', vy' [, vz'] (TMz: hx', hy') of the current step (null: the saved state's are they)
     const long long* sidx;       // sources (velocity sources are taken out of v')
     const int* stype;
@@ -582,18 +583,71 @@ __device__ __forceinline__ void adj_e3_s_body(const StepParams& P, const AdjShot
     A.lf[8][i] = lyz;
     const float M = __ldg(P.m[M_M] + i), mu = __ldg(P.m[M_MU] + i);
     const float ls = lxx + lyy + lzz;
+    const float muP[3] = {__ldg(P.m[M_MUXY] + i), __ldg(P.m[M_MUXZ] + i), __ldg(P.m[M_MUYZ] + i)};
     float l[9];
-    l[0] = M * ls - 2.0f * mu * (lyy + lzz);
-    l[1] = M * ls - 2.0f * mu * (lxx + lzz);
-    l[2] = M * ls - 2.0f * mu * (lxx + lyy);
-    l[3] = l[4] = __ldg(P.m[M_MUXY] + i) * lxy;
-    l[5] = l[6] = __ldg(P.m[M_MUXZ] + i) * lxz;
-    l[7] = l[8] = __ldg(P.m[M_MUYZ] + i) * lyz;
-    A.g[0][i] += ls * (c[0] + c[1] + c[2]);
-    A.g[1][i] += -2.0f * (lxx * (c[1] + c[2]) + lyy * (c[0] + c[2]) + lzz * (c[0] + c[1]));
-    A.g[2][i] += lxy * (c[3] + c[4]);
-    A.g[3][i] += lxz * (c[5] + c[6]);
-    A.g[4][i] += lyz * (c[7] + c[8]);
+    if (A.visco) {
+        // per mechanism l, with e = c0' + c1' + c2', q the normal stress's partner sum and m = mu_plane (its
+        // cross derivatives): Rk' = c2_l (c1_l Rk - tauP M e / tau_l + tauS 2 mu q / tau_l),
+        // Sk' = Sk + DT/2 sum_l (Rk + Rk') + (1 + L tauP) M e - (1 + L tauS) 2 mu q;
+        // Rs' = c2_l (c1_l Rs - tauS_plane m / tau_l), Ss' = Ss + DT/2 sum_l (Rs + Rs') + (1 + L tauS) m
+        // (ForwardSolver3Dviscoelastic.cpp:283-452); the memory variables are not tapered
+        const float e = c[0] + c[1] + c[2], DTh = P.DThalf;
+        const float tP = __ldg(P.m[M_TAUP] + i), tS = __ldg(P.m[M_TAUS] + i);
+        const float opP = __ldg(P.m[M_OPLTP] + i), opS = __ldg(P.m[M_OPLTS] + i);
+        const float q[3] = {c[1] + c[2], c[0] + c[2], c[0] + c[1]};
+        const float lS3[3] = {lxx, lyy, lzz};
+        float le = 0.0f, lq[3] = {0.0f, 0.0f, 0.0f}, gM = 0.0f, gMu = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float lS = lS3[k];
+            le += opP * M * lS;
+            lq[k] -= opS * 2.0f * mu * lS;
+            gM += opP * e * lS;
+            gMu -= opS * 2.0f * q[k] * lS;
+            for (int m = 0; m < P.L; ++m) {
+                const float cc = P.c2[m] * P.invRelax[m];
+                float* r = A.lr[k * kMaxL + m] + i;
+                const float LR = *r + DTh * lS;   // adjoint of Rk'
+                *r = P.c2[m] * P.c1[m] * LR + DTh * lS;
+                le -= cc * tP * M * LR;
+                lq[k] += cc * tS * 2.0f * mu * LR;
+                gM -= cc * tP * e * LR;
+                gMu += cc * tS * 2.0f * q[k] * LR;
+            }
+        }
+        l[0] = le + lq[1] + lq[2];
+        l[1] = le + lq[0] + lq[2];
+        l[2] = le + lq[0] + lq[1];
+        const float lSh[3] = {lxy, lxz, lyz};
+        const float tPl[3] = {__ldg(P.m[M_TAUSXY] + i), __ldg(P.m[M_TAUSXZ] + i), __ldg(P.m[M_TAUSYZ] + i)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float lS = lSh[k];
+            float lm = opS * lS;
+            for (int m = 0; m < P.L; ++m) {
+                float* r = A.lr[(3 + k) * kMaxL + m] + i;
+                const float LR = *r + DTh * lS;
+                *r = P.c2[m] * P.c1[m] * LR + DTh * lS;
+                lm -= P.c2[m] * P.invRelax[m] * tPl[k] * LR;
+            }
+            A.g[2 + k][i] += lm * (c[3 + 2 * k] + c[4 + 2 * k]);
+            l[3 + 2 * k] = l[4 + 2 * k] = muP[k] * lm;
+        }
+        A.g[0][i] += gM;
+        A.g[1][i] += gMu;
+    } else {
+        l[0] = M * ls - 2.0f * mu * (lyy + lzz);
+        l[1] = M * ls - 2.0f * mu * (lxx + lzz);
+        l[2] = M * ls - 2.0f * mu * (lxx + lyy);
+        l[3] = l[4] = muP[0] * lxy;
+        l[5] = l[6] = muP[1] * lxz;
+        l[7] = l[8] = muP[2] * lyz;
+        A.g[0][i] += ls * (c[0] + c[1] + c[2]);
+        A.g[1][i] += -2.0f * (lxx * (c[1] + c[2]) + lyy * (c[0] + c[2]) + lzz * (c[0] + c[1]));
+        A.g[2][i] += lxy * (c[3] + c[4]);
+        A.g[3][i] += lxz * (c[5] + c[6]);
+        A.g[4][i] += lyz * (c[7] + c[8]);
+    }
     if (fsRow) {
         // sxx', szz' += sh (c0' + c2') - sv c1' with sv = M - 2 mu, sh = -sv^2 / M
         const float sv = M - 2.0f * mu, sh = -(sv * sv) / M, hs = lxx + lzz;

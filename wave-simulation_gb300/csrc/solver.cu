@@ -782,7 +782,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         };
         const float sum = visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f;
         h->check(cudaMemcpyAsync(mat(M_RHO), dRho, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
-        if (eq == WAVE_EQ_ELASTIC || (eq == WAVE_EQ_VISCOELASTIC && !is3d)) {
+        if (eq == WAVE_EQ_ELASTIC || eq == WAVE_EQ_VISCOELASTIC) {
             h->check(cudaMemcpyAsync(mat(M_VP), dVp, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
             h->check(cudaMemcpyAsync(mat(M_VS), dVs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         }

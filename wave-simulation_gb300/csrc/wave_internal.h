@@ -65,7 +65,7 @@ enum Mat {
     M_CAX, M_CBX, M_CAY, M_CBY, M_CAZ, M_CBZ, M_IMUXY, M_IMUXZ, M_IMUYZ,
     M_CDX0, M_CDY0 = M_CDX0 + kMaxL, M_CDZ0 = M_CDY0 + kMaxL,   // visco-EM C_d per E component and mechanism
     M_RHO = M_CDZ0 + kMaxL,       // density, kept for kernels that average it in-kernel
-    M_VP, M_VS,                   // base velocities, kept for the adjoint's chain rule (elastic, 2-D visco-elastic; vs for 2-D SH)
+    M_VP, M_VS,                   // base velocities, kept for the adjoint's chain rule (elastic, visco-elastic; vs for 2-D SH)
     M_EPSR, M_SIG, M_MUR,         // base EM parameters, kept for the adjoint's chain rule (2-D TMz, TEz)
     M_COUNT
 };
