@@ -1383,6 +1383,226 @@ struct AcousticAdjoint {
     }
 };
 
+// Discrete adjoint of the oracle's lossless 3-D EM step (Sim<T>::stepEM3D,
+// restating FD3Demem::run, ForwardSolver3Demem.cpp:119-237, with CPMLEM3D
+// and the ABS taper): the gradient of J = 1/2 sum (d - d_obs)^2 with respect
+// to eps_r, sigma and mu_r. Per step, from X_t and X_{t+1} (all E derivatives
+// forward on the half profile; H derivatives backward on the full profile
+// except hyx, which uses the half one, CPMLEM3D.cpp:67-70):
+//   hx' = hx - iMyz (a0' - a1'),  a0' = Dyf ez, a1' = Dzf ey
+//   hy' = hy - iMxz (a2' - a3'),  a2' = Dzf ex, a3' = Dxf ez
+//   hz' = hz - iMxy (a4' - a5'),  a4' = Dxf ey, a5' = Dyf ex
+//   ex' = CaX ex + CbX (c0' - c1'),  c0' = Dyb hz', c1' = Dzb hy'
+//   ey' = CaY ey + CbY (c2' - c3'),  c2' = Dzb hx', c3' = Dxb hz'
+//   ez' = CaZ ez + CbZ (c4' - c5'),  c4' = Dxb hy', c5' = Dyb hx'
+// then the taper on all six fields; Ca, Cb of the 2-point averages of
+// eps = eps_r eps0 and sigma along each E component's axis, iM the inverse
+// 4-point averages of mu = mu_r mu0 in the yz, xz and xy planes (EMEM.cpp:378-392).
+template <class T>
+struct EM3Adjoint {
+    Sim<T>& s;
+    const idx_t N;
+    CSR<T> DxfT, DyfT, DzfT, DxbT, DybT, DzbT;
+    static constexpr const char* kA[6] = {"ezy", "eyz", "exz", "ezx", "eyx", "exy"};
+    static constexpr const char* kC[6] = {"hzy", "hyz", "hxz", "hzx", "hyx", "hxy"};
+    explicit EM3Adjoint(Sim<T>& sim) : s(sim), N(sim.g.N())
+    {
+        if (!s.is3d || s.eq != WAVE_EQ_EMEM) throw std::invalid_argument("oracle adjoint: lossless 3-D EM only");
+        DxfT = transpose(s.Dxf);
+        DyfT = transpose(s.Dyf);
+        DzfT = transpose(s.Dzf);
+        DxbT = transpose(s.Dxb);
+        DybT = transpose(s.Dyb);
+        DzbT = transpose(s.Dzb);
+    }
+    struct State {
+        std::map<std::string, std::vector<T>> F, psi;
+    };
+    const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
+    {
+        auto it = x.psi.find(n);
+        return it == x.psi.end() ? zero : it->second;
+    }
+    std::pair<const std::vector<T>*, const std::vector<T>*> prof(const std::string& n) const
+    {
+        if (n == "ezx" || n == "eyx" || n == "hyx") return {&s.axh, &s.bxh};
+        if (n == "ezy" || n == "exy") return {&s.ayh, &s.byh};
+        if (n == "eyz" || n == "exz") return {&s.azh, &s.bzh};
+        if (n == "hzx") return {&s.ax, &s.bx};
+        if (n == "hzy" || n == "hxy") return {&s.ay, &s.by};
+        return {&s.az, &s.bz};   // hyz, hxz
+    }
+    void cpmlT(std::vector<T>& lc, std::vector<T>& lp, const char* n) const
+    {
+        if (!s.useCpml) return;
+        auto ab = prof(n);
+        const std::vector<T>& a = *ab.first;
+        const std::vector<T>& b = *ab.second;
+        for_n(N, [&](idx_t i) {
+            const T c = (T(1) + a[i]) * lc[i] + a[i] * lp[i];
+            lp[i] = b[i] * (lc[i] + lp[i]);
+            lc[i] = c;
+        });
+    }
+
+    double run(const std::vector<T>& epsr, const std::vector<T>& sigma, const std::vector<T>& mur, const T* dobs, int K,
+               T* geps, T* gsig, T* gmu)
+    {
+        const int NT = s.NT;
+        const size_t nrec = s.rec.idx.size();
+        const std::vector<T> zero(N, T(0));
+        s.reset();
+        std::vector<State> ck;
+        for (int t = 0; t < NT; ++t) {
+            if (t % K == 0) ck.push_back({s.F, s.psi});
+            s.step(t);
+        }
+        std::vector<T> res(nrec * static_cast<size_t>(NT));
+        double J = 0;
+        for (size_t k = 0; k < res.size(); ++k) {
+            res[k] = s.seis[k] - dobs[k];
+            J += 0.5 * static_cast<double>(res[k]) * static_cast<double>(res[k]);
+        }
+        std::map<std::string, std::vector<T>> lF, lp;
+        for (const char* n : {"hx", "hy", "hz", "ex", "ey", "ez"}) lF[n].assign(N, 0);
+        for (int k = 0; k < 6; ++k) { lp[kA[k]].assign(N, 0); lp[kC[k]].assign(N, 0); }
+        std::vector<T> gCa[3], gCb[3], gM[3], a[6], c[6], la[6], lc[6], hp[3];
+        for (int k = 0; k < 3; ++k) { gCa[k].assign(N, 0); gCb[k].assign(N, 0); gM[k].assign(N, 0); hp[k].assign(N, 0); }
+        for (int k = 0; k < 6; ++k) { a[k].assign(N, 0); c[k].assign(N, 0); la[k].assign(N, 0); lc[k].assign(N, 0); }
+        const std::vector<T>* iM[3] = {&s.invMuYZ, &s.invMuXZ, &s.invMuXY};
+        const std::vector<T>* Ca[3] = {&s.CaX, &s.CaY, &s.CaZ};
+        const std::vector<T>* Cb[3] = {&s.CbX, &s.CbY, &s.CbZ};
+        const char* hn[3] = {"hx", "hy", "hz"};
+        const char* en[3] = {"ex", "ey", "ez"};
+        const int nseg = static_cast<int>(ck.size());
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const int t0 = seg * K, t1 = std::min(NT, t0 + K);
+            std::vector<State> X;
+            s.F = ck[seg].F;
+            s.psi = ck[seg].psi;
+            X.push_back({s.F, s.psi});
+            for (int t = t0; t < t1; ++t) {
+                s.step(t);
+                X.push_back({s.F, s.psi});
+            }
+            for (int t = t1 - 1; t >= t0; --t) {
+                const State& X0 = X[t - t0];
+                const State& X1 = X[t - t0 + 1];
+                auto f0 = [&](const char* n) { return X0.F.at(n).data(); };
+                s.Dyf.spmv(f0("ez"), a[0].data());
+                s.Dzf.spmv(f0("ey"), a[1].data());
+                s.Dzf.spmv(f0("ex"), a[2].data());
+                s.Dxf.spmv(f0("ez"), a[3].data());
+                s.Dxf.spmv(f0("ey"), a[4].data());
+                s.Dyf.spmv(f0("ex"), a[5].data());
+                for (int k = 0; k < 6; ++k) {
+                    const auto& p = psiOf(X1, kA[k], zero);
+                    for_n(N, [&](idx_t i) { a[k][i] += p[i]; });
+                }
+                for (int q = 0; q < 3; ++q) {
+                    const auto& h0 = X0.F.at(hn[q]);
+                    const auto& im = *iM[q];
+                    for_n(N, [&](idx_t i) { hp[q][i] = h0[i] - im[i] * (a[2 * q][i] - a[2 * q + 1][i]); });
+                }
+                s.Dyb.spmv(hp[2].data(), c[0].data());
+                s.Dzb.spmv(hp[1].data(), c[1].data());
+                s.Dzb.spmv(hp[0].data(), c[2].data());
+                s.Dxb.spmv(hp[2].data(), c[3].data());
+                s.Dxb.spmv(hp[1].data(), c[4].data());
+                s.Dyb.spmv(hp[0].data(), c[5].data());
+                for (int k = 0; k < 6; ++k) {
+                    const auto& p = psiOf(X1, kC[k], zero);
+                    for_n(N, [&](idx_t i) { c[k][i] += p[i]; });
+                }
+                for (size_t r = 0; r < nrec; ++r) {
+                    const idx_t i = s.rec.idx[r];
+                    const T v = res[r * NT + t];
+                    const int ty = s.rec.type[r];
+                    lF[ty == WAVE_TYPE_EZ ? "ez" : ty == WAVE_TYPE_EX ? "ex" : ty == WAVE_TYPE_EY ? "ey" : "hz"][i] += v;
+                }
+                if (s.useAbs)
+                    for (const char* n : {"hx", "hy", "hz", "ex", "ey", "ez"}) {
+                        auto& w = lF[n];
+                        for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
+                    }
+                // E <- Ca E + Cb (c' - c'')
+                for (int q = 0; q < 3; ++q) {
+                    auto& le = lF[en[q]];
+                    const auto& e0 = X0.F.at(en[q]);
+                    const auto& ca = *Ca[q];
+                    const auto& cb = *Cb[q];
+                    for_n(N, [&](idx_t i) {
+                        lc[2 * q][i] = cb[i] * le[i];
+                        lc[2 * q + 1][i] = -cb[i] * le[i];
+                        gCa[q][i] += le[i] * e0[i];
+                        gCb[q][i] += le[i] * (c[2 * q][i] - c[2 * q + 1][i]);
+                        le[i] *= ca[i];
+                    });
+                }
+                for (int k = 0; k < 6; ++k) cpmlT(lc[k], lp[kC[k]], kC[k]);
+                spmv_add(DybT, lc[0], lF["hz"]);
+                spmv_add(DzbT, lc[1], lF["hy"]);
+                spmv_add(DzbT, lc[2], lF["hx"]);
+                spmv_add(DxbT, lc[3], lF["hz"]);
+                spmv_add(DxbT, lc[4], lF["hy"]);
+                spmv_add(DybT, lc[5], lF["hx"]);
+                // H' = H - iM (a' - a'')
+                for (int q = 0; q < 3; ++q) {
+                    const auto& lh = lF[hn[q]];
+                    const auto& im = *iM[q];
+                    for_n(N, [&](idx_t i) {
+                        la[2 * q][i] = -im[i] * lh[i];
+                        la[2 * q + 1][i] = im[i] * lh[i];
+                        gM[q][i] -= lh[i] * (a[2 * q][i] - a[2 * q + 1][i]);
+                    });
+                }
+                for (int k = 0; k < 6; ++k) cpmlT(la[k], lp[kA[k]], kA[k]);
+                spmv_add(DyfT, la[0], lF["ez"]);
+                spmv_add(DzfT, la[1], lF["ey"]);
+                spmv_add(DzfT, la[2], lF["ex"]);
+                spmv_add(DxfT, la[3], lF["ez"]);
+                spmv_add(DxfT, la[4], lF["ey"]);
+                spmv_add(DyfT, la[5], lF["ex"]);
+            }
+        }
+        // Ca, Cb -> the 2-point averages of eps and sigma along x, y, z; iM -> the
+        // inverse 4-point averages of mu in the yz, xz and xy planes
+        const T eps0 = static_cast<T>(8.8541878176e-12), mu0 = static_cast<T>(1.2566370614e-6);
+        const T DT = s.DT;
+        std::vector<T> eps(N), ge(N, 0), gs(N, 0), ye(N), ys(N), avE(N), avS(N), y(N), gm(N, 0);
+        for (idx_t i = 0; i < N; ++i) eps[i] = epsr[i] * eps0;
+        AverageTranspose<T> probe(s);
+        const Axis axes[3] = {Axis::X, Axis::Y, Axis::Z};
+        for (int q = 0; q < 3; ++q) {
+            average2<T>(s.g, axes[q], eps.data(), avE.data());
+            average2<T>(s.g, axes[q], sigma.data(), avS.data());
+            for (idx_t i = 0; i < N; ++i) {
+                const T e = avE[i], sg = avS[i];
+                const T k = sg * DT / (T(2) * e), qq = T(1) + k;
+                const T dCa_de = T(2) * k / (e * qq * qq), dCa_ds = -T(2) / (qq * qq) * DT / (T(2) * e);
+                const T dCb_de = -T(1) / (e * e * qq) + k / (e * e * qq * qq), dCb_ds = -(T(1) / e) / (qq * qq) * DT / (T(2) * e);
+                ye[i] = gCa[q][i] * dCa_de + gCb[q][i] * dCb_de;
+                ys[i] = gCa[q][i] * dCa_ds + gCb[q][i] * dCb_ds;
+            }
+            probe.avgT([&](const T* in, T* out) { average2<T>(s.g, axes[q], in, out); }, ye, ge);
+            probe.avgT([&](const T* in, T* out) { average2<T>(s.g, axes[q], in, out); }, ys, gs);
+        }
+        const int plane[3] = {2, 1, 0};   // iMyz, iMxz, iMxy
+        for (int q = 0; q < 3; ++q) {
+            const auto& im = *iM[q];
+            for_n(N, [&](idx_t r) { y[r] = -gM[q][r] * im[r] * im[r]; });
+            probe.avgT([&](const T* in, T* out) { average4<T>(s.g, plane[q], in, out); }, y, gm);
+        }
+        for (idx_t i = 0; i < N; ++i) {
+            geps[i] = eps0 * ge[i];
+            gsig[i] = gs[i];
+            gmu[i] = mu0 * gm[i];
+        }
+        (void)mur;
+        return J;
+    }
+};
+
 template <class T>
 constexpr const char* ElasticAdjoint2D<T>::kP[4];
 template <class T>
@@ -1391,5 +1611,9 @@ template <class T>
 constexpr const char* ElasticAdjoint3D<T>::kP[9];
 template <class T>
 constexpr const char* ElasticAdjoint3D<T>::kQ[9];
+template <class T>
+constexpr const char* EM3Adjoint<T>::kA[6];
+template <class T>
+constexpr const char* EM3Adjoint<T>::kC[6];
 
 } // namespace refcpu

@@ -1,4 +1,4 @@
-"""Adjoint gradients of the lossless 2-D TMz and TEz misfits
+"""Adjoint gradients of the lossless 2-D TMz and TEz and 3-D EM misfits
 (wave_adjoint_gradient on a TMz / TEz handle: dJ/deps_r, dJ/dsigma, dJ/dmu_r)
 against the FP64 oracle's own discrete adjoints (oracle/adjoint_impl.hpp,
 TMAdjoint2D / TEAdjoint2D, pinned to FP64 finite differences at 1e-6 in
@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from test_oracle_adjoint import te_case, tm_case
+from test_oracle_adjoint import em3_case, te_case, tm_case
 
 pytestmark = pytest.mark.gpu
 GRAD_TOL = 1e-4
@@ -187,3 +187,43 @@ def test_tez_batched_adjoint_equals_single_shots(wave, refcpu):
         assert abs(mis[k] - single[k][0]) <= 1e-12 * abs(single[k][0])
         for got, want in zip((g1[k], g2[k], g3[k]), single[k][1:]):
             assert np.abs(want).max() > 0 and np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("boundary,stencil,reduce,order", [(2, 0, 0, 4), (1, 1, 0, 2), (0, 0, 1, 6)])
+def test_em3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, stencil, reduce, order):
+    """Lossless 3-D EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237; Ez and Hz sources, Ez / Ex / Ey /
+    Hz receivers) against the oracle's FP64 3-D EM adjoint (EM3Adjoint, pinned to FP64 finite
+    differences at 1e-6)."""
+    ocfg, model, acq = em3_case(refcpu, boundary, stencil, reduce, order=order, NX=40, NY=32, NZ=36, nt=260)
+    cfg = _wave_cfg(wave, ocfg)
+    m32 = {k: v.astype(np.float32) for k, v in model.items()}
+    y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
+    blob = np.exp(-((x - cfg.NX * 0.5) ** 2 + (y - cfg.NY * 0.5) ** 2 + (z - cfg.NZ * 0.5) ** 2) / 40.0).reshape(-1)
+    true = dict(m32)
+    true["eps_r"] = (m32["eps_r"] * (1 + 0.1 * blob)).astype(np.float32)
+    true["sigma"] = (m32["sigma"] * (1 + 0.5 * blob)).astype(np.float32)
+    acq32 = (acq[0], acq[1], acq[2].astype(np.float32), acq[3], acq[4])
+
+    def solver(model_):
+        s = wave.Factory.Create("3D", "emem").initForwardSolver(cfg)
+        s.prepareForModelling(model_)
+        s.setSources(*acq32[:3])
+        s.setReceivers(*acq32[3:])
+        return s
+
+    s = solver(true)
+    s.run(0, s.nt)
+    dobs = (0.6 * s.seismograms()).astype(np.float32)
+    s.close()
+    s = solver(m32)
+    J, ge, gs, gm = s.adjoint_gradient(dobs, checkpoint_every=45)
+    s.close()
+    o = refcpu.Oracle(ocfg, {k: v.astype(np.float64) for k, v in m32.items()}, acq32[0], acq32[1],
+                      acq32[2].astype(np.float64), acq32[3], acq32[4], dtype=np.float64)
+    J64, re, rs, rm = o.adjoint_gradient(dobs.astype(np.float64), checkpoint_every=45)
+    o.close()
+    errs = [_rel(a, b) for a, b in ((ge, re), (gs, rs), (gm, rm))]
+    print(f"3-D EM adjoint boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} vs FP64 "
+          f"{J64:.6e}; gradient rel L2 eps_r {errs[0]:.2e} sigma {errs[1]:.2e} mu_r {errs[2]:.2e}")
+    assert J > 0 and abs(J - J64) <= 1e-4 * J64
+    assert max(errs) <= GRAD_TOL

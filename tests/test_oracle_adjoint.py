@@ -462,3 +462,58 @@ def test_oracle_visco3d_adjoint_matches_fp64_finite_differences(refcpu, L, bound
         ad = float(np.dot(grads[name], d))
         assert abs(fd) > 0
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
+
+
+def em3_case(refcpu, boundary=2, stencil=0, reduce=1, order=4, NX=24, NY=20, NZ=18, nt=120):
+    rng = np.random.default_rng(43)
+    y, z, x = np.mgrid[0:NY, 0:NZ, 0:NX]
+    eps = 5.0 + 6.0 * (y > NY // 2) + 0.4 * np.cos(x / 4.0) + 0.3 * np.sin(z / 3.0) + 0.1 * rng.standard_normal((NY, NZ, NX))
+    sig = 10 ** (-3.0 + 0.4 * np.sin(y / 5.0))
+    mur = 1.0 + 0.05 * (x > NX // 3)
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(eps_r=eps, sigma=sig, mu_r=mur).items()}
+    DH = 0.02
+    DT = 0.3 * DH / (3e8 * np.sqrt(3) * 1.3)
+    cfg = refcpu.make_config(dimension=3, equation="emem", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=(nt - 0.4) * DT,
+                             spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=5, DampingCoeff=8.0, NPower=4.0,
+                             CenterFrequencyCPML=5e8, VMaxCPML=1.5e8, useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    sidx = np.array([refcpu.grid_index(cfg, NX // 2, 5, NZ // 2), refcpu.grid_index(cfg, NX // 3, 8, NZ // 3)], np.int64)
+    sig_t = refcpu.ricker(nt, DT, 7e8, 1.0, 0.0, np.float64)
+    rx = np.arange(3, NX - 3, 3)
+    ridx = np.concatenate([rx + NX * (NZ // 2 + NZ * 4), rx + NX * (NZ // 2 + NZ * 4), rx + NX * (5 + NZ * (NY - 5)),
+                           rx + NX * (12 + NZ * (NY - 5))]).astype(np.int64)
+    rtype = np.concatenate([np.full(rx.size, 1), np.full(rx.size, 2), np.full(rx.size, 3), np.full(rx.size, 4)]).astype(np.int32)
+    return cfg, model, (sidx, np.array([1, 4], np.int32), np.stack([sig_t, 300.0 * sig_t]), ridx, rtype)
+
+
+@pytest.mark.parametrize("boundary,stencil,reduce", [(2, 0, 1), (1, 1, 0), (0, 0, 1)])
+def test_oracle_em3d_adjoint_matches_fp64_finite_differences(refcpu, boundary, stencil, reduce):
+    """The oracle's FP64 adjoint of the lossless 3-D EM step (gradients with
+    respect to eps_r, sigma, mu_r; Ez and Hz sources, Ez / Ex / Ey / Hz
+    receivers) against central finite differences of its own misfit, with
+    CPML, ABS and no boundary."""
+    cfg, model, acq = em3_case(refcpu, boundary, stencil, reduce)
+    true = dict(model)
+    y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
+    blob = np.exp(-((x - cfg.NX * 0.5) ** 2 + (y - cfg.NY * 0.5) ** 2 + (z - cfg.NZ * 0.5) ** 2) / 18.0).reshape(-1)
+    true["eps_r"] = model["eps_r"] * (1 + 0.1 * blob)
+    true["sigma"] = model["sigma"] * (1 + 0.5 * blob)
+    true["mu_r"] = model["mu_r"] * (1 + 0.05 * blob)
+    o = refcpu.Oracle(cfg, true, *acq, dtype=np.float64)
+    dobs = 0.9 * o.run()
+    o.close()
+    o = refcpu.Oracle(cfg, model, *acq, dtype=np.float64)
+    J, ge, gs, gm = o.adjoint_gradient(dobs, checkpoint_every=41)
+    o.close()
+    assert J > 0 and J == pytest.approx(misfit(refcpu, cfg, model, acq, dobs), rel=1e-12)
+    rng = np.random.default_rng(47)
+    grads = dict(eps_r=ge, sigma=gs, mu_r=gm)
+    for name in ("eps_r", "sigma", "mu_r"):
+        d = smooth3(rng, cfg) * model[name]
+        h = 1e-5
+        mp, mm = dict(model), dict(model)
+        mp[name] = model[name] + h * d
+        mm[name] = model[name] - h * d
+        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+        ad = float(np.dot(grads[name], d))
+        assert abs(fd) > 0
+        assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)

@@ -106,6 +106,10 @@ __global__ void adj_vprime(const StepParams* __restrict__ Ps, const AdjShot* __r
             for (int k = 0; k < (P.is3d ? 3 : 2); ++k) A.vprime[k][p.i] = X1[A.off[1 + k] + p.i] / d;
             return;
         }
+        if (A.em3) {
+            for (int k = 0; k < 3; ++k) A.vprime[k][p.i] = X1[A.off[k] + p.i] / d;
+            return;
+        }
         A.vprime[0][p.i] = X1[A.off[AV_VX] + p.i] / d;
         if (!A.sh && !A.te) A.vprime[1][p.i] = X1[A.off[AV_VY] + p.i] / d;
     });
@@ -118,7 +122,7 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
     if (!A.vprime[0]) return;
     for (int k = threadIdx.x; k < A.nsrc; k += blockDim.x) {
         const int t = A.stype[k];
-        if ((A.e3 || A.ac) ? (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY && t != WAVE_TYPE_VZ)
+        if (A.em3 ? t != WAVE_TYPE_HZ : (A.e3 || A.ac) ? (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY && t != WAVE_TYPE_VZ)
                  : A.te ? t != WAVE_TYPE_HZ : A.sh ? t != WAVE_TYPE_VZ : (t != WAVE_TYPE_VX && t != WAVE_TYPE_VY))
             continue;
         const long long i = A.sidx[k];
@@ -129,7 +133,7 @@ __global__ void adj_vprime_sources(const StepParams* __restrict__ Ps, const AdjS
         p.y = static_cast<int>(r / P.NZ);
         p.z = static_cast<int>(r - (long long)p.y * P.NZ);
         const float d = P.abs ? absDamp(P, p) : 1.0f;
-        const int v = (A.e3 || A.ac) ? t - WAVE_TYPE_VX : (A.sh || A.te || t == WAVE_TYPE_VX) ? 0 : 1;
+        const int v = A.em3 ? 2 : (A.e3 || A.ac) ? t - WAVE_TYPE_VX : (A.sh || A.te || t == WAVE_TYPE_VX) ? 0 : 1;
         atomicAdd(A.vprime[v] + i, -A.signals[(long long)k * A.nt + n] / d);
     }
 }
@@ -148,6 +152,11 @@ __global__ void adj_inject(const AdjShot* __restrict__ As, int n)
         }
         if (A.sh) {   // vz receivers
             atomicAdd(A.lf[0] + i, v);
+            continue;
+        }
+        if (A.em3) {   // Ez, Ex, Ey, Hz receivers
+            const int t = A.rtype[r];
+            atomicAdd(A.lf[t == WAVE_TYPE_EZ ? 5 : t == WAVE_TYPE_EX ? 3 : t == WAVE_TYPE_EY ? 4 : 2] + i, v);
             continue;
         }
         if (A.ac) {   // p, vx, vy, vz receivers
@@ -437,6 +446,68 @@ __global__ void adj_ac_final(PrepParams G, const StepParams P, const AdjShot A, 
     }
 }
 
+// chain rule for lossless 3-D EM: CaQ, CbQ of the 2-point averages of eps = eps_r
+// eps0 and sigma along axis Q; iMyz, iMxz, iMxy = 1 / (4-point average of mu = mu_r
+// mu0 in the yz, xz, xy plane) (0 where invalid)
+__global__ void adj_em3_final(PrepParams G, const StepParams P, const AdjShot A, float DT, float* geps, float* gsig, float* gmu,
+                              int accumulate)
+{
+    const float eps0 = 8.8541878176e-12f, mu0 = 1.2566370614e-6f;
+    const float* er = P.m[M_EPSR];
+    const float* sg = P.m[M_SIG];
+    const long long sy = (long long)G.NX * G.NZ, sz = G.NX;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
+        const int kx = static_cast<int>(k % G.NX);
+        const long long rest = k / G.NX;
+        const int kz = static_cast<int>(rest % G.NZ), ky = static_cast<int>(rest / G.NZ);
+        const int kc[3] = {kx, ky, kz};
+        const int Nc[3] = {static_cast<int>(G.NX), static_cast<int>(G.NY), static_cast<int>(G.NZ)};
+        const long long st[3] = {1, sy, sz};
+        float ge = 0.0f, gs = 0.0f;
+        for (int q = 0; q < 3; ++q)
+            for (int d = 0; d <= 1; ++d) {
+                if (kc[q] - d < 0) continue;
+                const long long r = k - d * st[q];
+                const bool pair = kc[q] - d + 1 < Nc[q];
+                if (d == 1 && !pair) continue;
+                const float w = pair ? 0.5f : 1.0f;
+                const float e = pair ? 0.5f * (er[r] * eps0) + 0.5f * (er[r + st[q]] * eps0) : er[r] * eps0;
+                const float s = pair ? 0.5f * sg[r] + 0.5f * sg[r + st[q]] : sg[r];
+                float a, b;
+                cacb_adj(e, s, DT, A.g[2 * q][r], A.g[2 * q + 1][r], a, b);
+                ge += w * a;
+                gs += w * b;
+            }
+        // plane rows that read point k: yz (iMyz, g[6]), xz (iMxz, g[7]), xy (iMxy, g[8])
+        float gm = 0.0f;
+        for (int db = 0; db <= 1; ++db)
+            for (int da = 0; da <= 1; ++da) {
+                if (ky - da >= 0 && kz - db >= 0) {
+                    const long long r = k - da * sy - db * sz;
+                    const float im = P.m[M_IMUYZ][r];
+                    const float w = im != 0.0f ? w4(ky - da, kz - db, ky, kz, G.NY, G.NZ) : 0.0f;
+                    if (w != 0.0f) gm -= A.g[6][r] * im * im * w;
+                }
+                if (kx - da >= 0 && kz - db >= 0) {
+                    const long long r = k - da - db * sz;
+                    const float im = P.m[M_IMUXZ][r];
+                    const float w = im != 0.0f ? w4(kx - da, kz - db, kx, kz, G.NX, G.NZ) : 0.0f;
+                    if (w != 0.0f) gm -= A.g[7][r] * im * im * w;
+                }
+                if (kx - da >= 0 && ky - db >= 0) {
+                    const long long r = k - da - db * sy;
+                    const float im = P.m[M_IMUXY][r];
+                    const float w = im != 0.0f ? w4(kx - da, ky - db, kx, ky, G.NX, G.NY) : 0.0f;
+                    if (w != 0.0f) gm -= A.g[8][r] * im * im * w;
+                }
+            }
+        ge *= eps0;
+        gm *= mu0;
+        if (accumulate) { geps[k] += ge; gsig[k] += gs; gmu[k] += gm; }
+        else { geps[k] = ge; gsig[k] = gs; gmu[k] = gm; }
+    }
+}
+
 // weight of point (ka, kb) in the 4-point row at (a, b) of a plane average,
 // by its two in-plane coordinates (the edge fallbacks of
 // calc4PointAverageMatrixRow, Modelparameter.cpp:448-527)
@@ -513,7 +584,8 @@ __global__ void adj_e3_final(PrepParams G, const StepParams P, const AdjShot A, 
 void launch_adj(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid, int vn,
                 int pending, cudaStream_t s)
 {
-    if (pass >= 11) launch_adj_pass_acoustic(H, pass, Ps, As, W, S, grid, vn, pending, s);
+    if (pass >= 13) launch_adj_pass_em3d(H, pass, Ps, As, W, S, grid, vn, pending, s);
+    else if (pass >= 11) launch_adj_pass_acoustic(H, pass, Ps, As, W, S, grid, vn, pending, s);
     else if (pass >= 9) launch_adj_pass3d(H, pass, Ps, As, W, S, grid, vn, pending, s);
     else launch_adj_pass2d(H, pass, Ps, As, W, S, grid, vn, pending, s);
 }
@@ -550,11 +622,11 @@ std::string adjoint_supported(const wave_handle* h)
     const wave_config& c = h->cfg;
     const bool ok2 = c.dimension == 2 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_SH ||
                                           c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC);
-    const bool ok3 = c.dimension == 3 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_VISCOELASTIC);
+    const bool ok3 = c.dimension == 3 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_VISCOELASTIC || c.equation == WAVE_EQ_EMEM);
     const bool okAc = c.equation == WAVE_EQ_ACOUSTIC;
     if (!ok2 && !ok3 && !okAc)
-        return "the adjoint gradient is implemented for 2-D and 3-D acoustic, elastic and visco-elastic, 2-D SH and lossless "
-               "2-D TMz and TEz modelling";
+        return "the adjoint gradient is implemented for 2-D and 3-D acoustic, elastic and visco-elastic, 2-D SH, lossless "
+               "2-D TMz and TEz and lossless 3-D EM modelling";
     if (okAc && c.FreeSurface == 2) return "the acoustic adjoint takes the mirror free surface (FreeSurface = 1) or none";
     if (c.equation == WAVE_EQ_VISCOELASTIC && c.FreeSurface != 0)
         return "the visco-elastic adjoint takes no free surface (its relaxation exchange is not differentiated)";
@@ -602,7 +674,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
         const bool sh = h->cfg.equation == WAVE_EQ_SH;
         const bool ac = h->cfg.equation == WAVE_EQ_ACOUSTIC;
-        const bool e3 = h->sp.is3d && !ac;
+        const bool em3 = h->sp.is3d && h->cfg.equation == WAVE_EQ_EMEM;
+        const bool e3 = h->sp.is3d && !ac && !em3;
         long long off[kAdjMaxParts], len[kAdjMaxParts], o = 0;
         const int elasticFields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
         const int tmFields[5] = {F_HX, F_HY, F_EZ, -1, -1};
@@ -619,13 +692,17 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         // acoustic: p, vx, vy, vz and the psi of p_x, p_y, p_z, vxx, vyy, vzz (2-D: no vz, p_z, vzz)
         const int acFields[4] = {F_P, F_VX, F_VY, h->sp.is3d ? F_VZ : -1};
         const int acPsi[6] = {PS_P_X, PS_P_Y, PS_P_Z, PS_VXX, PS_VYY, PS_VZZ};
-        const int* fields = ac ? acFields : e3 ? e3Fields : tm ? tmFields : sh ? shFields : te ? teFields : elasticFields;
-        const int* psiSlot = ac ? acPsi : e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
+        // lossless 3-D EM: hx, hy, hz, ex, ey, ez and the psi of the H-update then the E-update derivatives
+        const int em3Fields[6] = {F_HX, F_HY, F_HZ, F_EX, F_EY, F_EZ};
+        const int em3Psi[12] = {PS_EZY, PS_EYZ, PS_EXZ, PS_EZX, PS_EYX, PS_EXY, PS_HZY, PS_HYZ, PS_HXZ, PS_HZX, PS_HYX, PS_HXY};
+        const int* fields = em3 ? em3Fields : ac ? acFields : e3 ? e3Fields : tm ? tmFields : sh ? shFields : te ? teFields
+                                                                                                  : elasticFields;
+        const int* psiSlot = em3 ? em3Psi : ac ? acPsi : e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
         // visco-elastic: the elastic parts, then rxx, ryy, rxy of each mechanism
         const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC;
         const int ncomp = e3 ? 6 : 3;   // memory-variable components per mechanism
         const int nr = visco ? ncomp * h->L : 0;
-        const int nf = ac ? 4 : e3 ? 9 : 5, np = ac ? 6 : e3 ? 18 : 8, nparts = nf + np + nr;
+        const int nf = em3 ? 6 : ac ? 4 : e3 ? 9 : 5, np = em3 ? 12 : ac ? 6 : e3 ? 18 : 8, nparts = nf + np + nr;
         for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
         for (int k = 0; k < np; ++k) {
             const int slot = psiSlot[k];
@@ -646,6 +723,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         a.e3 = e3 ? 1 : 0;
         a.visco = visco ? 1 : 0;
         a.ac = ac ? 1 : 0;
+        a.em3 = em3 ? 1 : 0;
         a.view = pool.get<float>(static_cast<size_t>(o) * (K + 1));
         a.stride = o;
         for (int k = 0; k < kAdjMaxParts; ++k) a.off[k] = k < nparts ? off[k] : 0;
@@ -655,7 +733,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         for (int k = 0; k < np; ++k) a.lpsi[k] = lstate + off[nf + k];
         for (int k = 0; k < 6 * kMaxL; ++k) a.lr[k] = nullptr;
         for (int j = 0; j < nr; ++j) a.lr[(j / h->L) * kMaxL + j % h->L] = lstate + off[nf + np + j];
-        const int ntemp = e3 ? 18 : 8, ngrad = e3 ? 8 : 5;   // acoustic: 6 and 4 of them
+        const int ntemp = e3 ? 18 : em3 ? 12 : 8, ngrad = e3 ? 8 : em3 ? 9 : 5;   // acoustic: 6 and 4 of them
         float* temps = pool.get<float>(static_cast<size_t>(ntemp) * N);
         for (int k = 0; k < ntemp; ++k) a.T[k] = temps + k * N;
         float* grads = pool.get<float>(static_cast<size_t>(ngrad) * N);
@@ -669,11 +747,11 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         a.res = res;
         bool velocitySources = false;
         for (int t : h->hSrcType)
-            velocitySources |= (e3 || ac) ? (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY || t == WAVE_TYPE_VZ)
+            velocitySources |= em3 ? t == WAVE_TYPE_HZ : (e3 || ac) ? (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY || t == WAVE_TYPE_VZ)
                              : te ? t == WAVE_TYPE_HZ : sh ? t == WAVE_TYPE_VZ : (t == WAVE_TYPE_VX || t == WAVE_TYPE_VY);
         a.vprime[0] = a.vprime[1] = a.vprime[2] = nullptr;
         if (h->cfg.DampingBoundary == 1 || velocitySources) {
-            const int nv = (e3 || ac) ? 3 : 2;
+            const int nv = (e3 || ac || em3) ? 3 : 2;
             a.vprime[0] = pool.get<float>(static_cast<size_t>(nv) * N);
             for (int k = 1; k < nv; ++k) a.vprime[k] = a.vprime[0] + k * N;
         }
@@ -757,7 +835,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             // two kernels per step: the third stage of step n (the transposed
             // derivatives of the first-pass inputs) runs inside the first kernel
             // of step n - 1; after step 0 it is not needed
-            const int first = A[0].ac ? 11 : A[0].e3 ? 9 : A[0].tm ? 3 : A[0].sh ? 5 : A[0].te ? 7 : 0;
+            const int first = A[0].em3 ? 13 : A[0].ac ? 11 : A[0].e3 ? 9 : A[0].tm ? 3 : A[0].sh ? 5 : A[0].te ? 7 : 0;
             const int pending = n < NT - 1 ? 1 : 0;
             launch_adj(H, first, dP, dA, dT, sched, grid, n - n0, pending, st);
             launch_adj(H, first + 1, dP, dA, dT, sched, grid, n - n0, pending, st);
@@ -769,7 +847,10 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         wave_handle* h = shots[s];
         PrepParams G{h->NX, h->NY, h->NZ, h->N};
         const int o = sum ? 0 : s;
-        if (A[s].ac)
+        if (A[s].em3)
+            adj_em3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
+                                                sum && s > 0 ? 1 : 0);
+        else if (A[s].ac)
             adj_ac_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
         else if (A[s].e3)
             adj_e3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], A[s].visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f, gvp[o], gvs[o],

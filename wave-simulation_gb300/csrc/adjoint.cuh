@@ -30,7 +30,7 @@ struct AdjShot {
     float* lf[9];                // adjoint fields (2-D elastic: vx, vy, sxx, syy, sxy)
     float* lpsi[18];             // adjoint psi (slab layout of the forward psi)
     float* T[18];                // adjoints of the raw derivatives (2-D elastic: c1..c4, a1..a4)
-    float* g[8];                 // material adjoints (2-D elastic: dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry)
+    float* g[9];                 // material adjoints (2-D elastic: dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry)
     const long long* ridx;
     const int* rtype;
     const float* res;            // residual d - d_obs, nrec x nt
@@ -41,6 +41,7 @@ struct AdjShot {
     int e3;                      // 1: 3-D elastic (Adj3Part layout)
     int visco;                   // 1: visco-elastic (the elastic parts, then the memory variables per mechanism)
     int ac;                      // 1: acoustic, 2-D or 3-D (parts: p, vx, vy, vz; psi p_x, p_y, p_z, vxx, vyy, vzz)
+    int em3;                     // 1: lossless 3-D EM (parts: hx, hy, hz, ex, ey, ez; psi of the six E and six H derivatives)
     float* lr[6 * kMaxL];        // adjoint memory variables of mechanism l at [k * kMaxL + l]: 2-D rxx, ryy, rxy;
                                  // 3-D rxx, ryy, rzz, rxy, rxz, ryz
     float* vprime[3];            // vx', vy' [, vz'] (TMz: hx', hy') of the current step (null: the saved state's are they)
@@ -52,7 +53,7 @@ struct AdjShot {
 
 // launches one adjoint pass over the (shot, tile) work list: 2-D passes 0, 1
 // (elastic and visco-elastic), 3, 4 (TMz), 5, 6 (SH), 7, 8 (TEz); 3-D passes
-// 9, 10 (elastic); acoustic passes 11, 12
+// 9, 10 (elastic and visco-elastic); acoustic passes 11, 12; 3-D EM passes 13, 14
 void launch_adj_pass2d(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid,
                        int vn, int pending, cudaStream_t s);
 void launch_adj_pass3d(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid,
@@ -60,6 +61,9 @@ void launch_adj_pass3d(int H, int pass, const StepParams* Ps, const AdjShot* As,
 // acoustic passes 11, 12 (2-D and 3-D)
 void launch_adj_pass_acoustic(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S,
                               int grid, int vn, int pending, cudaStream_t s);
+// lossless 3-D EM passes 13, 14
+void launch_adj_pass_em3d(int H, int pass, const StepParams* Ps, const AdjShot* As, const BatchTile* W, const BatchSched& S, int grid,
+                          int vn, int pending, cudaStream_t s);
 
 namespace adj {
 
@@ -798,6 +802,112 @@ __device__ __forceinline__ void adj_ac_v_body(const StepParams& P, const AdjShot
 }
 
 
+// ---- lossless 3-D EM ----------------------------------------------------------
+// parts: 0..5 = hx, hy, hz, ex, ey, ez; 6..11 = psi of the H-update derivatives
+// a0..a5 (ezy, eyz, exz, ezx, eyx, exy), 12..17 = psi of the E-update ones c0..c5
+// (hzy, hyz, hxz, hzx, hyx, hxy); lf[0..5] the field adjoints, lpsi[0..11] the
+// psi adjoints in part order; T[0..5] = adjoints of c0..c5, T[6..11] of a0..a5;
+// g[0..5] = dJ/dCaX, dJ/dCbX, dJ/dCaY, dJ/dCbY, dJ/dCaZ, dJ/dCbZ, g[6..8] =
+// dJ/diMyz, dJ/diMxz, dJ/diMxy
+
+// E-update transpose at step n:  ex' = CaX ex + CbX (c0' - c1'), ey' = CaY ey + CbY (c2' - c3'),
+// ez' = CaZ ez + CbZ (c4' - c5') with c0 = Dyb hz, c1 = Dzb hy, c2 = Dzb hx, c3 = Dxb hz, c4 = Dxb hy, c5 = Dyb hx
+template <int H>
+__device__ __forceinline__ void adj_em3_e_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = (long long)P.NX * P.NZ, sz = P.NX;
+    const float* h1[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) h1[k] = A.vprime[0] ? A.vprime[k] : X1 + A.off[k];
+    const Slabs S = slabs_of(P, p);
+    float c[6];
+    c[0] = deriv<H, false>(h1[2], i, sy, p.y, P.Dyb) + psi_at(X1, A, 12, S, 1);
+    c[1] = deriv<H, false>(h1[1], i, sz, p.z, P.Dzb) + psi_at(X1, A, 13, S, 2);
+    c[2] = deriv<H, false>(h1[0], i, sz, p.z, P.Dzb) + psi_at(X1, A, 14, S, 2);
+    c[3] = deriv<H, false>(h1[2], i, 1, p.x, P.Dxb) + psi_at(X1, A, 15, S, 0);
+    c[4] = deriv<H, false>(h1[1], i, 1, p.x, P.Dxb) + psi_at(X1, A, 16, S, 0);
+    c[5] = deriv<H, false>(h1[0], i, sy, p.y, P.Dyb) + psi_at(X1, A, 17, S, 1);
+    float le[3] = {A.lf[3][i], A.lf[4][i], A.lf[5][i]};
+    if (pending) {
+        // the transposed H-update derivatives of the E fields from the step after this one
+        le[2] += derivT<H, true>(A.T[6], i, sy, p.y, P.Dyf) + derivT<H, true>(A.T[9], i, 1, p.x, P.Dxf);
+        le[1] += derivT<H, true>(A.T[7], i, sz, p.z, P.Dzf) + derivT<H, true>(A.T[10], i, 1, p.x, P.Dxf);
+        le[0] += derivT<H, true>(A.T[8], i, sz, p.z, P.Dzf) + derivT<H, true>(A.T[11], i, sy, p.y, P.Dyf);
+    }
+    if (P.abs) {
+        // the taper multiplied all six fields last: their adjoints first
+        const float d = absDamp(P, p);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            le[q] *= d;
+            A.lf[q][i] *= d;
+        }
+    }
+    float l[6];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float ca = __ldg(P.m[M_CAX + 2 * q] + i), cb = __ldg(P.m[M_CBX + 2 * q] + i);
+        A.g[2 * q][i] += le[q] * X0[A.off[3 + q] + i];
+        A.g[2 * q + 1][i] += le[q] * (c[2 * q] - c[2 * q + 1]);
+        l[2 * q] = cb * le[q];
+        l[2 * q + 1] = -cb * le[q];
+        A.lf[3 + q][i] = ca * le[q];
+    }
+    // H-derivative psi: full profiles except hyx (CPMLEM3D.cpp:67-70)
+    cpml_adj_axis(P, p, S, l[0], A.lpsi[6], 1, false);    // hzy
+    cpml_adj_axis(P, p, S, l[1], A.lpsi[7], 2, false);    // hyz
+    cpml_adj_axis(P, p, S, l[2], A.lpsi[8], 2, false);    // hxz
+    cpml_adj_axis(P, p, S, l[3], A.lpsi[9], 0, false);    // hzx
+    cpml_adj_axis(P, p, S, l[4], A.lpsi[10], 0, true);    // hyx
+    cpml_adj_axis(P, p, S, l[5], A.lpsi[11], 1, false);   // hxy
+#pragma unroll
+    for (int k = 0; k < 6; ++k) A.T[k][i] = l[k];
+}
+
+// H-update transpose at step n (after the E transpose of every point):
+// hx' = hx - iMyz (a0' - a1'), hy' = hy - iMxz (a2' - a3'), hz' = hz - iMxy (a4' - a5')
+// with a0 = Dyf ez, a1 = Dzf ey, a2 = Dzf ex, a3 = Dxf ez, a4 = Dxf ey, a5 = Dyf ex
+template <int H>
+__device__ __forceinline__ void adj_em3_h_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn)
+{
+    const float* X0 = A.view + (long long)vn * A.stride;
+    const float* X1 = X0 + A.stride;
+    const long long i = p.i, sy = (long long)P.NX * P.NZ, sz = P.NX;
+    float lh[3];
+    lh[0] = A.lf[0][i] + derivT<H, false>(A.T[2], i, sz, p.z, P.Dzb) + derivT<H, false>(A.T[5], i, sy, p.y, P.Dyb);
+    lh[1] = A.lf[1][i] + derivT<H, false>(A.T[1], i, sz, p.z, P.Dzb) + derivT<H, false>(A.T[4], i, 1, p.x, P.Dxb);
+    lh[2] = A.lf[2][i] + derivT<H, false>(A.T[0], i, sy, p.y, P.Dyb) + derivT<H, false>(A.T[3], i, 1, p.x, P.Dxb);
+    const Slabs S = slabs_of(P, p);
+    const float *ex0 = X0 + A.off[3], *ey0 = X0 + A.off[4], *ez0 = X0 + A.off[5];
+    float a[6];
+    a[0] = deriv<H, true>(ez0, i, sy, p.y, P.Dyf) + psi_at(X1, A, 6, S, 1);
+    a[1] = deriv<H, true>(ey0, i, sz, p.z, P.Dzf) + psi_at(X1, A, 7, S, 2);
+    a[2] = deriv<H, true>(ex0, i, sz, p.z, P.Dzf) + psi_at(X1, A, 8, S, 2);
+    a[3] = deriv<H, true>(ez0, i, 1, p.x, P.Dxf) + psi_at(X1, A, 9, S, 0);
+    a[4] = deriv<H, true>(ey0, i, 1, p.x, P.Dxf) + psi_at(X1, A, 10, S, 0);
+    a[5] = deriv<H, true>(ex0, i, sy, p.y, P.Dyf) + psi_at(X1, A, 11, S, 1);
+    const int slot[3] = {M_IMUYZ, M_IMUXZ, M_IMUXY};
+    const int axis[6] = {1, 2, 2, 0, 0, 1};
+    float l[6];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const float im = __ldg(P.m[slot[q]] + i);
+        A.g[6 + q][i] -= lh[q] * (a[2 * q] - a[2 * q + 1]);
+        l[2 * q] = -im * lh[q];
+        l[2 * q + 1] = im * lh[q];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        cpml_adj_axis(P, p, S, l[k], A.lpsi[k], axis[k], true);   // E-derivative psi: half profiles
+        A.T[6 + k][i] = l[k];
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) A.lf[q][i] = lh[q];
+}
+
+
 template <int H, int PASS>
 __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ Ps, const AdjShot* __restrict__ As,
                                                 const BatchTile* __restrict__ W, BatchSched S, int vn, int pending)
@@ -816,7 +926,9 @@ __global__ void __launch_bounds__(256) adj_pass(const StepParams* __restrict__ P
         else if (PASS == 9) adj_e3_s_body<H>(P, A, p, vn, pending != 0);
         else if (PASS == 10) adj_e3_v_body<H>(P, A, p, vn);
         else if (PASS == 11) adj_ac_p_body<H>(P, A, p, vn, pending != 0);
-        else adj_ac_v_body<H>(P, A, p, vn);
+        else if (PASS == 12) adj_ac_v_body<H>(P, A, p, vn);
+        else if (PASS == 13) adj_em3_e_body<H>(P, A, p, vn, pending != 0);
+        else adj_em3_h_body<H>(P, A, p, vn);
     });
 }
 

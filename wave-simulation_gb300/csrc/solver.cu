@@ -952,7 +952,7 @@ int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, co
                 coeffs(ea, sa, ta, tsa, caS[a], cbS[a], cdS[a]);
             }
         }
-        if ((eq == WAVE_EQ_TMEM || eq == WAVE_EQ_EMEM) && !is3d) {
+        if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_EMEM) {
             // the base parameters, for the adjoint's chain rule (adjoint.cu)
             h->check(cudaMemcpyAsync(mat(M_EPSR), dEr, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
             h->check(cudaMemcpyAsync(mat(M_SIG), dSig, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");

@@ -66,7 +66,7 @@ enum Mat {
     M_CDX0, M_CDY0 = M_CDX0 + kMaxL, M_CDZ0 = M_CDY0 + kMaxL,   // visco-EM C_d per E component and mechanism
     M_RHO = M_CDZ0 + kMaxL,       // density, kept for kernels that average it in-kernel
     M_VP, M_VS,                   // base velocities, kept for the adjoint's chain rule (elastic, visco-elastic; vs for 2-D SH)
-    M_EPSR, M_SIG, M_MUR,         // base EM parameters, kept for the adjoint's chain rule (2-D TMz, TEz)
+    M_EPSR, M_SIG, M_MUR,         // base EM parameters, kept for the adjoint's chain rule (TMz, TEz, 3-D EM)
     M_COUNT
 };
 
