@@ -438,6 +438,8 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *  - lossless 2-D TEz (FD2Demem::run, ForwardSolver2Demem.cpp:112-185) with
  *    Ex, Ey and Hz sources and receivers, CPML, ABS or no damping boundary:
  *    the same three outputs;
+ *  - lossless 3-D EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237) with
+ *    CPML, ABS or no damping boundary: the same three outputs;
  * other equations return WAVE_ERR_UNSUPPORTED. Runs the
  * forward over all NT steps from a zero state (the handle's sources and
  * receivers; seismograms are left as computed), saving the state every
