@@ -428,9 +428,10 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *    viscoelastic.cpp:132-457) with CPML, ABS or no damping boundary, no free
  *    surface: the same three outputs, the relaxation times (tau_p, tau_s)
  *    held fixed;
- *  - 2-D SH (FD2Dsh::run, ForwardSolver2Dsh.cpp:108-196) with CPML, ABS or
- *    no damping boundary and with or without the free surface: grad_vs and
- *    grad_rho receive dJ/dvs, dJ/drho, grad_vp is set to zero;
+ *  - 2-D SH and visco-SH (FD2Dsh::run, ForwardSolver2Dsh.cpp:108-196;
+ *    FD2Dviscosh::run, ForwardSolver2Dviscosh.cpp:126-244, tau_s fixed) with
+ *    CPML, ABS or no damping boundary and with or without the free surface:
+ *    grad_vs and grad_rho receive dJ/dvs, dJ/drho, grad_vp is set to zero;
  *  - lossless 2-D TMz (FD2Dtmem::run, ForwardSolver2Dtmem.cpp:108-174) with
  *    Ez sources and receivers, CPML, ABS or no damping boundary: the three
  *    outputs receive dJ/deps_r, dJ/dsigma, dJ/dmu_r (the model's relative

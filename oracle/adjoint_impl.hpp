@@ -569,9 +569,11 @@ struct SHAdjoint2D {
     Sim<T>& s;
     const idx_t N;
     CSR<T> DxfT, DxbT, DyfT, DybST;
-    explicit SHAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    const bool visco;   // 2-D visco-SH (FD2Dviscosh::run, ForwardSolver2Dviscosh.cpp:126-244)
+
+    explicit SHAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N()), visco(sim.eq == WAVE_EQ_VISCOSH)
     {
-        if (s.is3d || s.eq != WAVE_EQ_SH) throw std::invalid_argument("oracle adjoint: 2-D SH only");
+        if (s.is3d || (s.eq != WAVE_EQ_SH && s.eq != WAVE_EQ_VISCOSH)) throw std::invalid_argument("oracle adjoint: 2-D SH only");
         DxfT = transpose(s.Dxf);
         DxbT = transpose(s.Dxb);
         DyfT = transpose(s.Dyf);
@@ -579,6 +581,7 @@ struct SHAdjoint2D {
     }
     struct State {
         std::map<std::string, std::vector<T>> F, psi;
+        std::map<std::string, std::vector<std::vector<T>>> R;
     };
     const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
     {
@@ -605,7 +608,7 @@ struct SHAdjoint2D {
         s.reset();
         std::vector<State> ck;
         for (int t = 0; t < NT; ++t) {
-            if (t % K == 0) ck.push_back({s.F, s.psi});
+            if (t % K == 0) ck.push_back({s.F, s.psi, s.R});
             s.step(t);
         }
         std::vector<T> res(nrec * static_cast<size_t>(NT));
@@ -618,6 +621,8 @@ struct SHAdjoint2D {
         std::map<std::string, std::vector<T>> lp;
         for (const char* n : {"sxz_x", "syz_y", "vzx", "vzy"}) lp[n].assign(N, 0);
         std::vector<T> gMuXZ(N, 0), gMuYZ(N, 0), gIr(N, 0);
+        // adjoint memory variables rxz, ryz per mechanism (visco-SH)
+        std::vector<std::vector<std::vector<T>>> lR(2, std::vector<std::vector<T>>(visco ? s.L : 0, std::vector<T>(N, 0)));
         std::vector<T> a1(N), a2(N), c1(N), c2(N), vzp(N), la1(N), la2(N), lc1(N), lc2(N);
         const int nseg = static_cast<int>(ck.size());
         for (int seg = nseg - 1; seg >= 0; --seg) {
@@ -625,10 +630,11 @@ struct SHAdjoint2D {
             std::vector<State> X;
             s.F = ck[seg].F;
             s.psi = ck[seg].psi;
-            X.push_back({s.F, s.psi});
+            s.R = ck[seg].R;
+            X.push_back({s.F, s.psi, s.R});
             for (int t = t0; t < t1; ++t) {
                 s.step(t);
-                X.push_back({s.F, s.psi});
+                X.push_back({s.F, s.psi, s.R});
             }
             for (int t = t1 - 1; t >= t0; --t) {
                 const State& X0 = X[t - t0];
@@ -655,12 +661,27 @@ struct SHAdjoint2D {
                         auto& w = *v;
                         for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
                     }
-                // sxz += muXZ c1', syz += muYZ c2'
+                // sxz += muXZ c1', syz += muYZ c2'; visco-SH, per mechanism l with m = mu_k c':
+                // Rk' = c2_l (c1_l Rk - tauS_k m / tau_l), Sk' = Sk + DT/2 sum_l (Rk + Rk') + (1 + L tauS) m
                 for_n(N, [&](idx_t i) {
-                    lc1[i] = s.muXZ[i] * lxz[i];
-                    lc2[i] = s.muYZ[i] * lyz[i];
-                    gMuXZ[i] += lxz[i] * c1[i];
-                    gMuYZ[i] += lyz[i] * c2[i];
+                    T lm[2] = {lxz[i], lyz[i]};
+                    if (visco) {
+                        const T tS[2] = {s.tauSXZ[i], s.tauSYZ[i]};
+                        for (int q = 0; q < 2; ++q) {
+                            const T lS = lm[q];
+                            lm[q] = s.onePlusLtauS[i] * lS;
+                            for (int l = 0; l < s.L; ++l) {
+                                const T cc1 = s.viscoC1[l], cc2 = s.viscoC2[l], irt = s.invRelaxTime[l];
+                                const T LR = lR[q][l][i] + s.DThalf * lS;
+                                lR[q][l][i] = cc2 * cc1 * LR + s.DThalf * lS;
+                                lm[q] -= cc2 * irt * tS[q] * LR;
+                            }
+                        }
+                    }
+                    lc1[i] = s.muXZ[i] * lm[0];
+                    lc2[i] = s.muYZ[i] * lm[1];
+                    gMuXZ[i] += lm[0] * c1[i];
+                    gMuYZ[i] += lm[1] * c2[i];
                 });
                 cpmlT(lc1, lp["vzx"], s.axh, s.bxh);
                 cpmlT(lc2, lp["vzy"], s.ayh, s.byh);
@@ -684,15 +705,26 @@ struct SHAdjoint2D {
         probe.avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::X, in, out); }, y, gmu);
         for_n(N, [&](idx_t r) { y[r] = gMuYZ[r] * s.muYZ[r] * s.muYZ[r]; });
         probe.avgT([&](const T* in, T* out) { average2<T>(s.g, Axis::Y, in, out); }, y, gmu);
+        // visco-SH: mu = rho vs^2 / (1 + sum tauS) with the relaxation times fixed
+        T sum = 0;
+        if (visco) {
+            const T w_ref = static_cast<T>(2.0 * M_PI * s.cfg.CenterFrequencyCPML);
+            for (int l = 0; l < s.L; ++l) {
+                const T ts = static_cast<T>(1.0 / (2.0 * M_PI * static_cast<T>(s.cfg.relaxationFrequency[l])));
+                sum += w_ref * w_ref * ts * ts / (T(1.0) + w_ref * w_ref * ts * ts);
+            }
+        }
         for (idx_t k = 0; k < N; ++k) {
-            // mu = max(rho vs^2, 1) (clamped values do not move); irho = 1 / rho
+            // mu = max(rho vs^2 / fS, 1) (clamped values do not move); irho = 1 / rho
+            const T fS = visco ? T(1) + sum * s.tauS[k] : T(1);
             T raw = rho[k];
             raw *= vs[k];
             raw *= vs[k];
+            if (visco) raw = raw / fS;
             const bool unclamped = raw >= T(1);
             const T gm = gmu[k] / (s.mu[k] * s.mu[k]);
-            gvs[k] = unclamped ? gm * T(2) * rho[k] * vs[k] : T(0);
-            grho[k] = (unclamped ? gm * vs[k] * vs[k] : T(0)) - gIr[k] * s.invRho[k] * s.invRho[k];
+            gvs[k] = unclamped ? gm * T(2) * rho[k] * vs[k] / fS : T(0);
+            grho[k] = (unclamped ? gm * vs[k] * vs[k] / fS : T(0)) - gIr[k] * s.invRho[k] * s.invRho[k];
         }
         return J;
     }

@@ -377,7 +377,7 @@ class Oracle:
                                              ctypes.byref(J), _ptr(g[0]), _ptr(g[1])) != 0:
                 raise RuntimeError(lib().refcpu_last_error().decode())
             return J.value, g[0], np.zeros(n, dtype=np.float64), g[1]
-        if self.cfg.equation == EQ["sh"]:
+        if self.cfg.equation in (EQ["sh"], EQ["viscosh"]):
             m = [np.ascontiguousarray(self.model[k], dtype=np.float64) for k in ("vs", "rho")]
             d = np.ascontiguousarray(dobs, dtype=np.float64)
             if d.size != len(self._ridx) * self.nt:

@@ -27,15 +27,15 @@ def _wave_cfg(wave, ocfg):
 
 
 def _solver(wave, cfg, model, acq):
-    s = wave.Factory.Create("2D", "sh").initForwardSolver(cfg)
+    s = wave.Factory.Create("2D", "viscosh" if cfg.equation == wave.EQUATIONS["viscosh"] else "sh").initForwardSolver(cfg)
     s.prepareForModelling(model)
     s.setSources(*acq[:3])
     s.setReceivers(*acq[3:])
     return s
 
 
-def _survey(wave, refcpu, fs, boundary, stencil, reduce, order=4):
-    ocfg, model, acq = sh_case(refcpu, fs, boundary, stencil, reduce, order=order, NX=80, NY=64, nt=500)
+def _survey(wave, refcpu, fs, boundary, stencil, reduce, order=4, L=0):
+    ocfg, model, acq = sh_case(refcpu, fs, boundary, stencil, reduce, order=order, NX=80, NY=64, nt=500, L=L)
     cfg = _wave_cfg(wave, ocfg)
     m32 = {k: v.astype(np.float32) for k, v in model.items()}
     yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
@@ -68,16 +68,18 @@ def _oracle(refcpu, ocfg, m32, acq, dobs, K):
     return out
 
 
-@pytest.mark.parametrize("fs,boundary,stencil,reduce,order", [(0, 2, 0, 0, 4), (0, 0, 1, 0, 2), (0, 1, 0, 0, 6),
-                                                              (1, 2, 0, 0, 4), (1, 1, 1, 0, 8), (0, 2, 0, 1, 4)])
-def test_sh_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, fs, boundary, stencil, reduce, order):
-    ocfg, cfg, m32, acq, dobs = _survey(wave, refcpu, fs, boundary, stencil, reduce, order)
+@pytest.mark.parametrize("fs,boundary,stencil,reduce,order,L", [(0, 2, 0, 0, 4, 0), (0, 0, 1, 0, 2, 0), (0, 1, 0, 0, 6, 0),
+                                                                (1, 2, 0, 0, 4, 0), (1, 1, 1, 0, 8, 0), (0, 2, 0, 1, 4, 0),
+                                                                (0, 2, 0, 0, 4, 1), (1, 1, 0, 1, 6, 2)])
+def test_sh_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, fs, boundary, stencil, reduce, order, L):
+    """L > 0: visco-SH (FD2Dviscosh::run, ForwardSolver2Dviscosh.cpp:126-244), the relaxation times fixed."""
+    ocfg, cfg, m32, acq, dobs = _survey(wave, refcpu, fs, boundary, stencil, reduce, order, L)
     s = _solver(wave, cfg, m32, acq)
     J, gvp, gvs, grho = s.adjoint_gradient(dobs, checkpoint_every=45)
     s.close()
     J64, _, rs, rr = _oracle(refcpu, ocfg, m32, acq, dobs, 45)
     errs = [_rel(gvs, rs), _rel(grho, rr)]
-    print(f"SH adjoint fs={fs} boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} "
+    print(f"SH adjoint L={L} fs={fs} boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} "
           f"vs FP64 {J64:.6e}; gradient rel L2 vs {errs[0]:.2e} rho {errs[1]:.2e}")
     assert not np.any(gvp)
     assert J > 0 and abs(J - J64) <= 1e-4 * J64

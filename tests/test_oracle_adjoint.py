@@ -156,17 +156,22 @@ def test_oracle_tmz_adjoint_matches_fp64_finite_differences(refcpu, boundary, st
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
 
 
-def sh_case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=44, NY=36, nt=180):
+def sh_case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=44, NY=36, nt=180, L=0):
+    """2-D SH survey; L > 0: visco-SH with L relaxation mechanisms."""
     rng = np.random.default_rng(7)
     y, x = np.mgrid[0:NY, 0:NX]
     vs = 1200.0 + 500.0 * (y / NY) + 60.0 * np.sin(x / 5.0) + 20 * rng.standard_normal((NY, NX))
     rho = 1800.0 + 300.0 * (y > NY // 2) + 40.0 * np.cos(x / 7.0)
-    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(vs=vs, rho=rho).items()}
+    fields = dict(vs=vs, rho=rho)
+    if L:
+        fields["taus"] = 0.05 + 0.01 * np.cos(y / 5.0) + 0.005 * np.sin(x / 4.0)
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in fields.items()}
     DH, DT = 5.0, 6e-4
-    cfg = refcpu.make_config(dimension=2, equation="sh", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT, T=(nt - 0.4) * DT,
-                             spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary, BoundaryWidth=8,
-                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=20.0, VMaxCPML=1800.0,
-                             useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    cfg = refcpu.make_config(dimension=2, equation="viscosh" if L else "sh", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT,
+                             T=(nt - 0.4) * DT, spatialFDorder=order, FreeSurface=fs, DampingBoundary=boundary,
+                             BoundaryWidth=8, DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=20.0, VMaxCPML=1800.0,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce, numRelaxationMechanisms=L,
+                             relaxationFrequency=[15.0, 40.0][:L])
     sidx = np.array([refcpu.grid_index(cfg, NX // 2, 2 if fs else 6, 0)], np.int64)
     sig = refcpu.ricker(nt, DT, 20.0, 1.0, -0.02, np.float64)[None]
     rx = np.arange(4, NX - 4, 3)
@@ -174,15 +179,16 @@ def sh_case(refcpu, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=44, NY=36
     return cfg, model, (sidx, np.array([4], np.int32), sig, ridx, np.full(ridx.size, 4, np.int32))
 
 
-@pytest.mark.parametrize("fs,boundary,stencil,reduce", [(0, 2, 0, 1), (0, 0, 1, 0), (1, 2, 0, 1), (0, 1, 0, 1),
-                                                        (1, 1, 1, 0)])
-def test_oracle_sh_adjoint_matches_fp64_finite_differences(refcpu, fs, boundary, stencil, reduce):
+@pytest.mark.parametrize("fs,boundary,stencil,reduce,L", [(0, 2, 0, 1, 0), (0, 0, 1, 0, 0), (1, 2, 0, 1, 0), (0, 1, 0, 1, 0),
+                                                          (1, 1, 1, 0, 0), (0, 2, 0, 1, 1), (1, 1, 0, 0, 2)])
+def test_oracle_sh_adjoint_matches_fp64_finite_differences(refcpu, fs, boundary, stencil, reduce, L):
     """The oracle's FP64 adjoint of the 2-D SH step (gradients with respect
     to vs and rho; the vp gradient is zero) against central finite
     differences of its own misfit (relative step 1e-5) along smooth
     directions and at the point of the largest gradient, with CPML, no
-    boundary, ABS and the free surface."""
-    cfg, model, acq = sh_case(refcpu, fs, boundary, stencil, reduce)
+    boundary, ABS and the free surface, and for visco-SH with one and two
+    relaxation mechanisms (the relaxation times fixed)."""
+    cfg, model, acq = sh_case(refcpu, fs, boundary, stencil, reduce, L=L)
     true = dict(model)
     yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
     blob = np.exp(-((xx - cfg.NX * 0.45) ** 2 + (yy - cfg.NY * 0.55) ** 2) / 40.0).reshape(-1)

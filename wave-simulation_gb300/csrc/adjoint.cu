@@ -313,7 +313,8 @@ __global__ void adj_tm_final(PrepParams G, const StepParams P, const AdjShot A, 
 
 // chain rule for SH: mu = max(rho vs^2, 1); muXZ, muYZ = 1 / (2-point average
 // of 1 / mu) along x, y (0 below 4); irho = 1 / rho. grad_vp is zero.
-__global__ void adj_sh_final(PrepParams G, const StepParams P, const AdjShot A, float* gvp, float* gvs, float* grho, int accumulate)
+__global__ void adj_sh_final(PrepParams G, const StepParams P, const AdjShot A, float vsum, float* gvp, float* gvs, float* grho,
+                             int accumulate)
 {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
         const int kx = static_cast<int>(k % G.NX), ky = static_cast<int>(k / G.NX);
@@ -334,13 +335,16 @@ __global__ void adj_sh_final(PrepParams G, const StepParams P, const AdjShot A, 
                 if (m != 0.0f && (d == 0 || w == 0.5f)) gmu += A.g[1][r] * w * (m / muk) * (m / muk);
             }
         }
+        // visco-SH: mu = max(rho vs^2 / fS, 1), fS = 1 + sum tauS (the relaxation times held fixed)
+        const float fS = A.visco ? 1.0f + vsum * P.m[M_TAUS][k] : 1.0f;
         float raw = rho;
         raw *= vs;
         raw *= vs;
+        if (A.visco) raw = raw / fS;
         const bool unclamped = raw >= 1.0f;
         const float ir = P.m[M_IR][k];
-        const float gs = unclamped ? gmu * 2.0f * rho * vs : 0.0f;
-        const float gr = (unclamped ? gmu * vs * vs : 0.0f) - A.g[2][k] * ir * ir;
+        const float gs = unclamped ? gmu * 2.0f * rho * vs / fS : 0.0f;
+        const float gr = (unclamped ? gmu * vs * vs / fS : 0.0f) - A.g[2][k] * ir * ir;
         if (accumulate) { gvs[k] += gs; grho[k] += gr; }
         else { gvp[k] = 0.0f; gvs[k] = gs; grho[k] = gr; }
     }
@@ -621,12 +625,13 @@ std::string adjoint_supported(const wave_handle* h)
 {
     const wave_config& c = h->cfg;
     const bool ok2 = c.dimension == 2 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_SH ||
-                                          c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC);
+                                          c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC ||
+                                          c.equation == WAVE_EQ_VISCOSH);
     const bool ok3 = c.dimension == 3 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_VISCOELASTIC || c.equation == WAVE_EQ_EMEM);
     const bool okAc = c.equation == WAVE_EQ_ACOUSTIC;
     if (!ok2 && !ok3 && !okAc)
-        return "the adjoint gradient is implemented for 2-D and 3-D acoustic, elastic and visco-elastic, 2-D SH, lossless "
-               "2-D TMz and TEz and lossless 3-D EM modelling";
+        return "the adjoint gradient is implemented for 2-D and 3-D acoustic, elastic and visco-elastic, 2-D SH and visco-SH, "
+               "lossless 2-D TMz and TEz and lossless 3-D EM modelling";
     if (okAc && c.FreeSurface == 2) return "the acoustic adjoint takes the mirror free surface (FreeSurface = 1) or none";
     if (c.equation == WAVE_EQ_VISCOELASTIC && c.FreeSurface != 0)
         return "the visco-elastic adjoint takes no free surface (its relaxation exchange is not differentiated)";
@@ -672,7 +677,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         // SH: vz, -, sxz, syz and the psi of sxz_x, syz_y, -, -, vzx, vzy
         // 3-D elastic: the Adj3Part layout
         const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
-        const bool sh = h->cfg.equation == WAVE_EQ_SH;
+        const bool sh = h->cfg.equation == WAVE_EQ_SH || h->cfg.equation == WAVE_EQ_VISCOSH;
         const bool ac = h->cfg.equation == WAVE_EQ_ACOUSTIC;
         const bool em3 = h->sp.is3d && h->cfg.equation == WAVE_EQ_EMEM;
         const bool e3 = h->sp.is3d && !ac && !em3;
@@ -699,8 +704,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
                                                                                                   : elasticFields;
         const int* psiSlot = em3 ? em3Psi : ac ? acPsi : e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
         // visco-elastic: the elastic parts, then rxx, ryy, rxy of each mechanism
-        const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC;
-        const int ncomp = e3 ? 6 : 3;   // memory-variable components per mechanism
+        const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC || h->cfg.equation == WAVE_EQ_VISCOSH;
+        const int ncomp = e3 ? 6 : sh ? 2 : 3;   // memory-variable components per mechanism
         const int nr = visco ? ncomp * h->L : 0;
         const int nf = em3 ? 6 : ac ? 4 : e3 ? 9 : 5, np = em3 ? 12 : ac ? 6 : e3 ? 18 : 8, nparts = nf + np + nr;
         for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
@@ -712,7 +717,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         }
         const int memVar2[3] = {R_XX, R_YY, R_XY};
         const int memVar3[6] = {R_XX, R_YY, R_ZZ, R_XY, R_XZ, R_YZ};
-        const int* memVar = e3 ? memVar3 : memVar2;
+        const int memVarSH[2] = {R_XZ, R_YZ};
+        const int* memVar = e3 ? memVar3 : sh ? memVarSH : memVar2;
         auto rpart = [&](int j) { return h->r[memVar[j / h->L]][j % h->L]; };
         for (int j = 0; j < nr; ++j) { off[nf + np + j] = o; len[nf + np + j] = N; o += N; }
         stride[s] = o;
@@ -859,7 +865,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             adj_tm_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
                                                sum && s > 0 ? 1 : 0);
         else if (A[s].sh)
-            adj_sh_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);
+            adj_sh_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], A[s].visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f, gvp[o], gvs[o],
+                                               grho[o], sum && s > 0 ? 1 : 0);
         else if (A[s].te)
             adj_te_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
                                                sum && s > 0 ? 1 : 0);

@@ -389,9 +389,27 @@ __device__ __forceinline__ void adj_sh_s_body(const StepParams& P, const AdjShot
     }
     A.lf[2][i] = lxz;
     A.lf[3][i] = lyz;
-    float l1 = __ldg(P.m[M_MUXZ] + i) * lxz, l2 = __ldg(P.m[M_MUYZ] + i) * lyz;
-    A.g[0][i] += lxz * c1;
-    A.g[1][i] += lyz * c2;
+    float lm[2] = {lxz, lyz};
+    if (A.visco) {
+        // visco-SH, per mechanism l with m = mu_k c': Rk' = c2_l (c1_l Rk - tauS_k m / tau_l),
+        // Sk' = Sk + DT/2 sum_l (Rk + Rk') + (1 + L tauS) m (ForwardSolver2Dviscosh.cpp:180-240)
+        const float opS = __ldg(P.m[M_OPLTS] + i);
+        const float tS[2] = {__ldg(P.m[M_TAUSXZ] + i), __ldg(P.m[M_TAUSYZ] + i)};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const float lS = lm[q];
+            lm[q] = opS * lS;
+            for (int m = 0; m < P.L; ++m) {
+                float* r = A.lr[q * kMaxL + m] + i;
+                const float LR = *r + P.DThalf * lS;
+                *r = P.c2[m] * P.c1[m] * LR + P.DThalf * lS;
+                lm[q] -= P.c2[m] * P.invRelax[m] * tS[q] * LR;
+            }
+        }
+    }
+    float l1 = __ldg(P.m[M_MUXZ] + i) * lm[0], l2 = __ldg(P.m[M_MUYZ] + i) * lm[1];
+    A.g[0][i] += lm[0] * c1;
+    A.g[1][i] += lm[1] * c2;
     if (S.sx >= 0) cpml_adj(l1, A.lpsi[4] + S.px, P.cx.a_half[p.x], P.cx.b_half[p.x]);   // vzx: x, half profile
     if (S.sy >= 0) cpml_adj(l2, A.lpsi[5] + S.py, P.cy.a_half[p.y], P.cy.b_half[p.y]);   // vzy: y, half profile
     A.T[0][i] = l1;

@@ -788,7 +788,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         }
         if (eq == WAVE_EQ_ACOUSTIC)   // the acoustic adjoint's chain rule reads vp
             h->check(cudaMemcpyAsync(mat(M_VP), dVp, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
-        if (eq == WAVE_EQ_SH && !is3d)   // the SH adjoint's chain rule reads vs
+        if ((eq == WAVE_EQ_SH || eq == WAVE_EQ_VISCOSH) && !is3d)   // the SH adjoint's chain rule reads vs
             h->check(cudaMemcpyAsync(mat(M_VS), dVs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
         if (needVp) k_modulus(G, dRho, dVp, dTp, sum, 0, mat(M_M), s);
         if (needVs) k_modulus(G, dRho, dVs, visco ? dTs : nullptr, sum, 1, mat(M_MU), s);
@@ -804,6 +804,8 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
                 k_avg2(G, dTs, 0, mat(M_TAUSXZ), s);
                 k_avg2(G, dTs, 1, mat(M_TAUSYZ), s);
                 k_one_plus(G, dTs, static_cast<float>(h->L), mat(M_OPLTS), s);
+                // tau_s itself, for the adjoint's chain rule (adjoint.cu)
+                h->check(cudaMemcpyAsync(mat(M_TAUS), dTs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
             }
         } else {
             k_inv_avg2(G, dRho, 0, mat(M_IRX), s);
