@@ -432,7 +432,9 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *    FD2Dviscosh::run, ForwardSolver2Dviscosh.cpp:126-244, tau_s fixed) with
  *    CPML, ABS or no damping boundary and with or without the free surface:
  *    grad_vs and grad_rho receive dJ/dvs, dJ/drho, grad_vp is set to zero;
- *  - lossless 2-D TMz (FD2Dtmem::run, ForwardSolver2Dtmem.cpp:108-174) with
+ *  - 2-D TMz and visco-TMz (FD2Dtmem::run, ForwardSolver2Dtmem.cpp:108-174;
+ *    FD2Dviscotmem::run, ForwardSolver2Dviscotmem.cpp:130-205, tau_eps and
+ *    tau_sigma fixed) with
  *    Ez sources and receivers, CPML, ABS or no damping boundary: the three
  *    outputs receive dJ/deps_r, dJ/dsigma, dJ/dmu_r (the model's relative
  *    permittivity, conductivity and relative permeability);

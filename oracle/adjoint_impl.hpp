@@ -414,9 +414,11 @@ struct TMAdjoint2D {
     Sim<T>& s;
     const idx_t N;
     CSR<T> DxfT, DxbT, DyfT, DybT;
-    explicit TMAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    const bool visco;   // 2-D visco-TMz (FD2Dviscotmem::run, ForwardSolver2Dviscotmem.cpp:130-205)
+
+    explicit TMAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N()), visco(sim.eq == WAVE_EQ_VISCOTMEM)
     {
-        if (s.is3d || s.eq != WAVE_EQ_TMEM) throw std::invalid_argument("oracle adjoint: lossless 2-D TMz only");
+        if (s.is3d || (s.eq != WAVE_EQ_TMEM && s.eq != WAVE_EQ_VISCOTMEM)) throw std::invalid_argument("oracle adjoint: 2-D TMz only");
         DxfT = transpose(s.Dxf);
         DxbT = transpose(s.Dxb);
         DyfT = transpose(s.Dyf);
@@ -424,6 +426,7 @@ struct TMAdjoint2D {
     }
     struct State {
         std::map<std::string, std::vector<T>> F, psi;
+        std::map<std::string, std::vector<std::vector<T>>> R;
     };
     const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
     {
@@ -451,7 +454,7 @@ struct TMAdjoint2D {
         s.reset();
         std::vector<State> ck;
         for (int t = 0; t < NT; ++t) {
-            if (t % K == 0) ck.push_back({s.F, s.psi});
+            if (t % K == 0) ck.push_back({s.F, s.psi, s.R});
             s.step(t);
         }
         std::vector<T> res(nrec * static_cast<size_t>(NT));
@@ -464,6 +467,9 @@ struct TMAdjoint2D {
         std::map<std::string, std::vector<T>> lp;
         for (const char* n : {"ezy", "ezx", "hyx", "hxy"}) lp[n].assign(N, 0);
         std::vector<T> gCa(N, 0), gCb(N, 0), gMxz(N, 0), gMyz(N, 0);
+        // visco: adjoints of the memory variables rz_l and the material adjoints of Cd_l
+        const int L = visco ? s.L : 0;
+        std::vector<std::vector<T>> lR(L, std::vector<T>(N, 0)), gCd(L, std::vector<T>(N, 0));
         std::vector<T> a1(N), a2(N), c1(N), c2(N), hxp(N), hyp(N), la1(N), la2(N), lc1(N), lc2(N);
         const int nseg = static_cast<int>(ck.size());
         for (int seg = nseg - 1; seg >= 0; --seg) {
@@ -471,10 +477,11 @@ struct TMAdjoint2D {
             std::vector<State> X;
             s.F = ck[seg].F;
             s.psi = ck[seg].psi;
-            X.push_back({s.F, s.psi});
+            s.R = ck[seg].R;
+            X.push_back({s.F, s.psi, s.R});
             for (int t = t0; t < t1; ++t) {
                 s.step(t);
-                X.push_back({s.F, s.psi});
+                X.push_back({s.F, s.psi, s.R});
             }
             for (int t = t1 - 1; t >= t0; --t) {
                 const State& X0 = X[t - t0];
@@ -503,14 +510,23 @@ struct TMAdjoint2D {
                         auto& w = *v;
                         for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
                     }
-                // ez <- Ca ez + Cb (c1' - c2')
+                // ez <- Ca ez + Cb (c1' - c2' - DT sum_l rz_l'), rz_l' = Cc_l rz_l + Cd_l ez (visco)
                 const auto& ez0 = X0.F.at("ez");
                 for_n(N, [&](idx_t i) {
+                    T u = c1[i] - c2[i];
+                    for (int l = 0; l < L; ++l) u -= s.DT * X1.R.at("rz")[l][i];
                     lc1[i] = s.CbZ[i] * lez[i];
                     lc2[i] = -s.CbZ[i] * lez[i];
                     gCa[i] += lez[i] * ez0[i];
-                    gCb[i] += lez[i] * (c1[i] - c2[i]);
-                    lez[i] *= s.CaZ[i];
+                    gCb[i] += lez[i] * u;
+                    T ln = s.CaZ[i] * lez[i];
+                    for (int l = 0; l < L; ++l) {
+                        const T LR = lR[l][i] - s.DT * s.CbZ[i] * lez[i];   // adjoint of rz_l'
+                        ln += s.CdZ[l][i] * LR;
+                        gCd[l][i] += LR * ez0[i];
+                        lR[l][i] = s.emCc[l] * LR;
+                    }
+                    lez[i] = ln;
                 });
                 cpmlT(lc1, lp["hyx"], s.ax, s.bx);
                 cpmlT(lc2, lp["hxy"], s.ay, s.by);
@@ -532,13 +548,43 @@ struct TMAdjoint2D {
         // Ca, Cb -> eps, sigma; iMxz, iMyz -> mu
         const T eps0 = static_cast<T>(8.8541878176e-12), mu0 = static_cast<T>(1.2566370614e-6);
         const T DT = s.DT;
+        // visco: Ca, Cb of the effective optical permittivity eo = max((1 - te) e + s ts, eps0)
+        // and conductivity so = te sumInv e + s; Cd_l = -DT te cdScale_l e (ForwardSolverEM.cpp:68-152),
+        // tau_eps (te) and tau_sigma (ts, times 1 / (2 pi f_CPML)) held fixed
+        T sumInv = 0;
+        std::vector<T> cdScale(L);
+        if (visco) {
+            for (int l = 0; l < L; ++l) {
+                const double r = 1.0 / (2.0 * M_PI * static_cast<double>(static_cast<T>(s.cfg.relaxationFrequency[l])));
+                const T rt = static_cast<T>(r);
+                sumInv = static_cast<T>(static_cast<double>(sumInv) + 1.0 / static_cast<double>(rt));
+                T tv = static_cast<T>(1 / (1 + 0.5 * static_cast<double>(DT) / static_cast<double>(rt)));
+                tv /= (static_cast<T>(L) * rt * rt);
+                cdScale[l] = tv;
+            }
+            sumInv /= static_cast<T>(L);
+        }
         for (idx_t i = 0; i < N; ++i) {
-            const T e = epsr[i] * eps0, sg = sigma[i];
+            const T e0 = epsr[i] * eps0, sg0 = sigma[i];
+            T e = e0, sg = sg0, de_de = 1, de_ds = 0, ds_de = 0, ds_ds = 1;
+            if (visco) {
+                const T te = s.emTauE[i], ts = s.emTauS[i];
+                const T eo = (T(1) - te) * e0 + sg0 * ts;
+                const bool clamp = eo < eps0;
+                e = clamp ? eps0 : eo;
+                de_de = clamp ? T(0) : T(1) - te;
+                de_ds = clamp ? T(0) : ts;
+                sg = te * sumInv * e0 + sg0;
+                ds_de = te * sumInv;
+            }
             const T k = sg * DT / (T(2) * e), q = T(1) + k;
             const T dCa_de = T(2) * k / (e * q * q), dCa_ds = -T(2) / (q * q) * DT / (T(2) * e);
             const T dCb_de = -T(1) / (e * e * q) + k / (e * e * q * q), dCb_ds = -(T(1) / e) / (q * q) * DT / (T(2) * e);
-            geps[i] = eps0 * (gCa[i] * dCa_de + gCb[i] * dCb_de);
-            gsig[i] = gCa[i] * dCa_ds + gCb[i] * dCb_ds;
+            const T gE = gCa[i] * dCa_de + gCb[i] * dCb_de, gS = gCa[i] * dCa_ds + gCb[i] * dCb_ds;
+            T ge = gE * de_de + gS * ds_de, gs = gE * de_ds + gS * ds_ds;
+            for (int l = 0; l < L; ++l) ge += gCd[l][i] * (-DT) * s.emTauE[i] * cdScale[l];
+            geps[i] = eps0 * ge;
+            gsig[i] = gs;
         }
         std::vector<T> y(N), gm(N, 0);
         AverageTranspose<T> probe(s);

@@ -423,6 +423,7 @@ class Sim {
     std::vector<T> M, mu, invRhoX, invRhoY, invRhoZ, invRho, muXY, muXZ, muYZ;
     std::vector<T> tauP, tauS, tauSXY, tauSXZ, tauSYZ, onePlusLtauP, onePlusLtauS;
     std::vector<T> relaxTime, invRelaxTime, viscoC1, viscoC2;
+    std::vector<T> emTauE, emTauS;   // visco-EM tau_eps and tau_sigma (times 1 / (2 pi f_CPML)), kept for the adjoint
     T DThalf = 0;
     // EM
     std::vector<T> CaZ, CbZ, CaX, CbX, CaY, CbY, invMuXZ, invMuYZ, invMuXY;

@@ -183,6 +183,8 @@ void Sim<T>::prepareModel(const Model<T>& m)
             tauSg = m.tau_sigma;
             const T tauRef = static_cast<T>(1.0 / (2.0 * M_PI * static_cast<T>(cfg.CenterFrequencyCPML)));
             for_n(N, [&](idx_t i) { tauSg[i] *= tauRef; });
+            emTauE = tauE;
+            emTauS = tauSg;
             for (int l = 0; l < L; ++l) relax.push_back(static_cast<T>(1.0 / (2.0 * M_PI * static_cast<T>(cfg.relaxationFrequency[l]))));
         }
         auto Cinv = [&](T e, T s) { T c = T(0.5) / e; c *= s; c *= DT; c += T(1); return T(1) / c; };

@@ -125,9 +125,9 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("dim,equation", [(2, "viscotmem"), (3, "viscoelastic")])
+@pytest.mark.parametrize("dim,equation", [(2, "viscoemem"), (3, "viscoelastic")])
 def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
-    """Set-ups without an adjoint are refused with WAVE_ERR_UNSUPPORTED: visco-EM, and the visco-elastic free
+    """Set-ups without an adjoint are refused with WAVE_ERR_UNSUPPORTED: visco-TEz, and the visco-elastic free
     surface (its relaxation exchange is not differentiated)."""
     cfg = _config(wave, dim=dim, fs=1 if equation == "viscoelastic" else 0)
     cfg.equation = wave.EQUATIONS[equation]
@@ -135,7 +135,7 @@ def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
     cfg.relaxationFrequency[0] = 20.0
     true, start = _models()
     n = cfg.N
-    if equation == "viscotmem":
+    if equation == "viscoemem":
         model = dict(eps_r=np.full(n, 6.0, np.float32), sigma=np.full(n, 1e-3, np.float32), mu_r=np.ones(n, np.float32),
                      tau_eps=np.full(n, 0.1, np.float32), tau_sigma=np.full(n, 0.1, np.float32))
     else:
@@ -144,8 +144,8 @@ def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
         model["taus"] = np.full(n, 0.03, np.float32)
     s = wave.Factory.Create("3D" if dim == 3 else "2D", equation).initForwardSolver(cfg)
     s.prepareForModelling(model)
-    s.setSources(np.array([5], np.int64), np.array([1], np.int32), np.zeros((1, s.nt), np.float32))
-    s.setReceivers(np.array([7], np.int64), np.array([1 if equation == "viscotmem" else 2], np.int32))
+    s.setSources(np.array([5], np.int64), np.array([4 if equation == "viscoemem" else 1], np.int32), np.zeros((1, s.nt), np.float32))
+    s.setReceivers(np.array([7], np.int64), np.array([2], np.int32))
     with pytest.raises(wave.WaveError) as e:
         s.adjoint_gradient(np.zeros((1, s.nt), np.float32))
     assert e.value.code == wave.WAVE_ERR_UNSUPPORTED

@@ -26,8 +26,8 @@ def _wave_cfg(wave, ocfg):
     return c
 
 
-def _survey(wave, refcpu, boundary, stencil, reduce):
-    ocfg, model, acq = tm_case(refcpu, boundary, stencil, reduce, NX=72, NY=60, nt=400)
+def _survey(wave, refcpu, boundary, stencil, reduce, L=0):
+    ocfg, model, acq = tm_case(refcpu, boundary, stencil, reduce, NX=72, NY=60, nt=400, L=L)
     cfg = _wave_cfg(wave, ocfg)
     m32 = {k: v.astype(np.float32) for k, v in model.items()}
     yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
@@ -36,7 +36,7 @@ def _survey(wave, refcpu, boundary, stencil, reduce):
     true["eps_r"] = (m32["eps_r"] * (1 + 0.1 * blob)).astype(np.float32)
     true["sigma"] = (m32["sigma"] * (1 + 0.5 * blob)).astype(np.float32)
     acq32 = (acq[0], acq[1], acq[2].astype(np.float32), acq[3], acq[4])
-    s = wave.Factory.Create("2D", "tmem").initForwardSolver(cfg)
+    s = wave.Factory.Create("2D", _tm_key(cfg)).initForwardSolver(cfg)
     s.prepareForModelling(true)
     s.setSources(*acq32[:3])
     s.setReceivers(*acq32[3:])
@@ -49,14 +49,21 @@ def _survey(wave, refcpu, boundary, stencil, reduce):
     return ocfg, cfg, m32, acq32, dobs
 
 
+def _tm_key(cfg):
+    return "viscotmem" if cfg.numRelaxationMechanisms > 0 else "tmem"
+
+
 def _rel(a, b):
     return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("boundary,stencil,reduce", [(2, 0, 0), (0, 1, 0), (1, 0, 0), (2, 0, 1)])
-def test_tmz_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, stencil, reduce):
-    ocfg, cfg, m32, acq, dobs = _survey(wave, refcpu, boundary, stencil, reduce)
-    s = wave.Factory.Create("2D", "tmem").initForwardSolver(cfg)
+@pytest.mark.parametrize("boundary,stencil,reduce,L", [(2, 0, 0, 0), (0, 1, 0, 0), (1, 0, 0, 0), (2, 0, 1, 0), (2, 0, 0, 1),
+                                                      (1, 1, 0, 2)])
+def test_tmz_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, stencil, reduce, L):
+    """L > 0: visco-TMz (FD2Dviscotmem::run, ForwardSolver2Dviscotmem.cpp:130-205), tau_eps and
+    tau_sigma fixed."""
+    ocfg, cfg, m32, acq, dobs = _survey(wave, refcpu, boundary, stencil, reduce, L)
+    s = wave.Factory.Create("2D", _tm_key(cfg)).initForwardSolver(cfg)
     s.prepareForModelling(m32)
     s.setSources(*acq[:3])
     s.setReceivers(*acq[3:])
@@ -67,7 +74,7 @@ def test_tmz_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, st
     J64, re, rs, rm = o.adjoint_gradient(dobs.astype(np.float64), checkpoint_every=45)
     o.close()
     errs = [_rel(a, b) for a, b in ((ge, re), (gs, rs), (gm, rm))]
-    print(f"TMz adjoint boundary={boundary} stencil={stencil} reduce={reduce}: misfit {J:.6e} vs FP64 {J64:.6e}; "
+    print(f"TMz adjoint L={L} boundary={boundary} stencil={stencil} reduce={reduce}: misfit {J:.6e} vs FP64 {J64:.6e}; "
           f"gradient rel L2 eps_r {errs[0]:.2e} sigma {errs[1]:.2e} mu_r {errs[2]:.2e}")
     assert J > 0 and abs(J - J64) <= 1e-4 * J64
     assert max(errs) <= GRAD_TOL
@@ -80,7 +87,7 @@ def test_tmz_batched_adjoint_equals_single_shots(wave, refcpu):
         sidx = np.array([acq[0][0] + 9 * k], np.int64)
         a = (sidx, acq[1], acq[2], acq[3], acq[4])
         acqs.append(a)
-        s = wave.Factory.Create("2D", "tmem").initForwardSolver(cfg)
+        s = wave.Factory.Create("2D", _tm_key(cfg)).initForwardSolver(cfg)
         s.prepareForModelling(m32)
         s.setSources(*a[:3])
         s.setReceivers(*a[3:])
@@ -105,7 +112,7 @@ def test_tmz_batched_adjoint_equals_single_shots(wave, refcpu):
 
 def test_tmz_adjoint_rejects_other_receiver_components(wave, refcpu):
     ocfg, cfg, m32, acq, dobs = _survey(wave, refcpu, 0, 0, 0)
-    s = wave.Factory.Create("2D", "tmem").initForwardSolver(cfg)
+    s = wave.Factory.Create("2D", _tm_key(cfg)).initForwardSolver(cfg)
     s.prepareForModelling(m32)
     s.setSources(*acq[:3])
     with pytest.raises(wave.WaveError) as e:

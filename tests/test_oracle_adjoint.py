@@ -104,19 +104,25 @@ def test_oracle_adjoint_is_independent_of_the_checkpoint_interval(refcpu):
         assert np.array_equal(a, b)
 
 
-def tm_case(refcpu, boundary=2, stencil=0, reduce=1, order=4, NX=48, NY=40, nt=220):
+def tm_case(refcpu, boundary=2, stencil=0, reduce=1, order=4, NX=48, NY=40, nt=220, L=0):
+    """2-D TMz survey; L > 0: visco-TMz with L relaxation mechanisms."""
     rng = np.random.default_rng(5)
     y, x = np.mgrid[0:NY, 0:NX]
     eps = 6.0 + 8.0 * (y > NY // 2) + 0.5 * np.sin(x / 4.0) + 0.2 * rng.standard_normal((NY, NX))
     sig = 10 ** (-3.0 + 0.5 * np.cos(y / 6.0))
     mur = 1.0 + 0.05 * (x > NX // 2)
-    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(eps_r=eps, sigma=sig, mu_r=mur).items()}
+    fields = dict(eps_r=eps, sigma=sig, mu_r=mur)
+    if L:
+        fields["tau_eps"] = 0.15 + 0.05 * np.sin(x / 5.0)
+        fields["tau_sigma"] = 0.1 + 0.05 * np.cos(y / 4.0)
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in fields.items()}
     DH = 0.02
     DT = 0.3 * DH / (3e8 * np.sqrt(2) * 1.3)
-    cfg = refcpu.make_config(dimension=2, equation="tmem", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT, T=(nt - 0.4) * DT,
-                             spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=8, DampingCoeff=8.0,
-                             NPower=4.0, CenterFrequencyCPML=4e8, VMaxCPML=1.5e8, useStencilMatrix=stencil,
-                             edgeOrderReduction=reduce)
+    cfg = refcpu.make_config(dimension=2, equation="viscotmem" if L else "tmem", NX=NX, NY=NY, NZ=1, DH=DH, DT=DT,
+                             T=(nt - 0.4) * DT, spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=8,
+                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=4e8, VMaxCPML=1.5e8,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce, numRelaxationMechanisms=L,
+                             relaxationFrequency=[3e8, 9e8][:L])
     sidx = np.array([refcpu.grid_index(cfg, NX // 2, 6, 0)], np.int64)
     sig_t = refcpu.ricker(nt, DT, 6e8, 1.0, 0.0, np.float64)[None]
     rx = np.arange(4, NX - 4, 3)
@@ -124,12 +130,13 @@ def tm_case(refcpu, boundary=2, stencil=0, reduce=1, order=4, NX=48, NY=40, nt=2
     return cfg, model, (sidx, np.array([1], np.int32), sig_t, ridx, np.ones(ridx.size, np.int32))
 
 
-@pytest.mark.parametrize("boundary,stencil,reduce", [(2, 0, 1), (0, 1, 0), (1, 0, 1)])
-def test_oracle_tmz_adjoint_matches_fp64_finite_differences(refcpu, boundary, stencil, reduce):
-    """The oracle's FP64 adjoint of the lossless TMz step (gradients with
-    respect to eps_r, sigma, mu_r) against central finite differences of its
-    own misfit, with CPML, no boundary and ABS."""
-    cfg, model, acq = tm_case(refcpu, boundary, stencil, reduce)
+@pytest.mark.parametrize("boundary,stencil,reduce,L", [(2, 0, 1, 0), (0, 1, 0, 0), (1, 0, 1, 0), (2, 0, 1, 1), (1, 1, 0, 2)])
+def test_oracle_tmz_adjoint_matches_fp64_finite_differences(refcpu, boundary, stencil, reduce, L):
+    """The oracle's FP64 adjoint of the lossless TMz step and of the visco-TMz
+    step (L mechanisms, tau_eps and tau_sigma fixed; gradients with respect to
+    eps_r, sigma, mu_r) against central finite differences of its own misfit,
+    with CPML, no boundary and ABS."""
+    cfg, model, acq = tm_case(refcpu, boundary, stencil, reduce, L=L)
     true = dict(model)
     yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
     blob = np.exp(-((xx - cfg.NX * 0.5) ** 2 + (yy - cfg.NY * 0.4) ** 2) / 30.0).reshape(-1)

@@ -273,22 +273,49 @@ __global__ void adj_grad_final(PrepParams G, const StepParams P, const AdjShot A
     }
 }
 
+// d Ca / d eps, d Ca / d sigma, d Cb / d eps, d Cb / d sigma of
+// Ca = (1 - k) / (1 + k), Cb = (1 / eps) / (1 + k), k = sigma DT / (2 eps),
+// applied to the adjoints of Ca and Cb
+__device__ __forceinline__ void cacb_adj(float e, float sg, float DT, float gca, float gcb, float& ge, float& gs)
+{
+    const float kk = sg * DT / (2.0f * e), q = 1.0f + kk;
+    const float dca_de = 2.0f * kk / (e * q * q), dca_ds = -2.0f / (q * q) * (DT / (2.0f * e));
+    const float dcb_de = (-1.0f / (e * q) + kk / (e * q * q)) / e, dcb_ds = -(1.0f / e) / (q * q) * (DT / (2.0f * e));
+    ge = gca * dca_de + gcb * dcb_de;
+    gs = gca * dca_ds + gcb * dcb_ds;
+}
+
 // chain rule for TMz: Ca = (1 - k) / (1 + k), Cb = (1 / eps) / (1 + k) with
 // k = sigma DT / (2 eps), eps = eps_r eps0; iMxz, iMyz = 1 / (2-point average of
 // mu = mu_r mu0) along x, y (0 where invalid)
-__global__ void adj_tm_final(PrepParams G, const StepParams P, const AdjShot A, float DT, float* geps, float* gsig, float* gmu,
-                             int accumulate)
+__global__ void adj_tm_final(PrepParams G, const StepParams P, const AdjShot A, float DT, ViscoEmCoef vc, float* geps, float* gsig,
+                             float* gmu, int accumulate)
 {
     const float eps0 = 8.8541878176e-12f, mu0 = 1.2566370614e-6f;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < G.N; k += (long long)gridDim.x * blockDim.x) {
         const int kx = static_cast<int>(k % G.NX), ky = static_cast<int>(k / G.NX);
-        const float e = P.m[M_EPSR][k] * eps0, sg = P.m[M_SIG][k];
-        const float kk = sg * DT / (2.0f * e), q = 1.0f + kk;
-        const float gca = A.g[0][k], gcb = A.g[1][k];
-        const float dca_de = 2.0f * kk / (e * q * q), dca_ds = -2.0f / (q * q) * (DT / (2.0f * e));
-        const float dcb_de = (-1.0f / (e * q) + kk / (e * q * q)) / e, dcb_ds = -(1.0f / e) / (q * q) * (DT / (2.0f * e));
-        const float ge = eps0 * (gca * dca_de + gcb * dcb_de);
-        const float gs = gca * dca_ds + gcb * dcb_ds;
+        const float e0 = P.m[M_EPSR][k] * eps0, sg0 = P.m[M_SIG][k];
+        // visco: Ca, Cb of eo = max((1 - te) e + s ts, eps0) and so = te sumInv e + s; Cd_l = -DT te cdScale_l e
+        // (prep_visco_em, ForwardSolverEM.cpp:68-152), tau_eps (te) and tau_sigma (ts) held fixed
+        float e = e0, sg = sg0, de_de = 1.0f, de_ds = 0.0f, ds_de = 0.0f, te = 0.0f;
+        if (A.visco) {
+            te = P.m[M_TAUP][k];
+            const float ts = P.m[M_TAUS][k];
+            const float eo = (1.0f - te) * e0 + sg0 * ts;
+            const bool clamp = eo < eps0;
+            e = clamp ? eps0 : eo;
+            de_de = clamp ? 0.0f : 1.0f - te;
+            de_ds = clamp ? 0.0f : ts;
+            sg = te * vc.sumInv * e0 + sg0;
+            ds_de = te * vc.sumInv;
+        }
+        float gE, gS;
+        cacb_adj(e, sg, DT, A.g[0][k], A.g[1][k], gE, gS);
+        float ged = gE * de_de + gS * ds_de;
+        const float gs = gE * de_ds + gS;
+        if (A.visco)
+            for (int l = 0; l < vc.L; ++l) ged += A.g[4 + l][k] * (-DT) * te * vc.cdScale[l];
+        const float ge = eps0 * ged;
         // rows (kx, ky) and (kx-1, ky) of the x average, (kx, ky) and (kx, ky-1) of the y average
         float gm = 0.0f;
         for (int d = 0; d <= 1; ++d) {
@@ -350,17 +377,6 @@ __global__ void adj_sh_final(PrepParams G, const StepParams P, const AdjShot A, 
     }
 }
 
-// d Ca / d eps, d Ca / d sigma, d Cb / d eps, d Cb / d sigma of
-// Ca = (1 - k) / (1 + k), Cb = (1 / eps) / (1 + k), k = sigma DT / (2 eps),
-// applied to the adjoints of Ca and Cb
-__device__ __forceinline__ void cacb_adj(float e, float sg, float DT, float gca, float gcb, float& ge, float& gs)
-{
-    const float kk = sg * DT / (2.0f * e), q = 1.0f + kk;
-    const float dca_de = 2.0f * kk / (e * q * q), dca_ds = -2.0f / (q * q) * (DT / (2.0f * e));
-    const float dcb_de = (-1.0f / (e * q) + kk / (e * q * q)) / e, dcb_ds = -(1.0f / e) / (q * q) * (DT / (2.0f * e));
-    ge = gca * dca_de + gcb * dcb_de;
-    gs = gca * dca_ds + gcb * dcb_ds;
-}
 
 // chain rule for TEz: CaX, CbX of the 2-point x averages of eps = eps_r eps0
 // and sigma (CaY, CbY along y); iMxy = 1 / (4-point average of mu = mu_r mu0)
@@ -626,7 +642,7 @@ std::string adjoint_supported(const wave_handle* h)
     const wave_config& c = h->cfg;
     const bool ok2 = c.dimension == 2 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_SH ||
                                           c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC ||
-                                          c.equation == WAVE_EQ_VISCOSH);
+                                          c.equation == WAVE_EQ_VISCOSH || c.equation == WAVE_EQ_VISCOTMEM);
     const bool ok3 = c.dimension == 3 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_VISCOELASTIC || c.equation == WAVE_EQ_EMEM);
     const bool okAc = c.equation == WAVE_EQ_ACOUSTIC;
     if (!ok2 && !ok3 && !okAc)
@@ -636,7 +652,7 @@ std::string adjoint_supported(const wave_handle* h)
     if (c.equation == WAVE_EQ_VISCOELASTIC && c.FreeSurface != 0)
         return "the visco-elastic adjoint takes no free surface (its relaxation exchange is not differentiated)";
     if (ok3 && c.FreeSurface == 2) return "the 3-D adjoint takes the mirror free surface (FreeSurface = 1) or none";
-    if (c.equation == WAVE_EQ_TMEM) {
+    if (c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_VISCOTMEM) {
         for (int t : h->hRecType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez receivers only";
         for (int t : h->hSrcType)
@@ -676,7 +692,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         // TMz: hx, hy, ez and the psi of ezy, ezx, hyx, hxy
         // SH: vz, -, sxz, syz and the psi of sxz_x, syz_y, -, -, vzx, vzy
         // 3-D elastic: the Adj3Part layout
-        const bool tm = h->cfg.equation == WAVE_EQ_TMEM;
+        const bool tm = h->cfg.equation == WAVE_EQ_TMEM || h->cfg.equation == WAVE_EQ_VISCOTMEM;
         const bool sh = h->cfg.equation == WAVE_EQ_SH || h->cfg.equation == WAVE_EQ_VISCOSH;
         const bool ac = h->cfg.equation == WAVE_EQ_ACOUSTIC;
         const bool em3 = h->sp.is3d && h->cfg.equation == WAVE_EQ_EMEM;
@@ -704,8 +720,9 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
                                                                                                   : elasticFields;
         const int* psiSlot = em3 ? em3Psi : ac ? acPsi : e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
         // visco-elastic: the elastic parts, then rxx, ryy, rxy of each mechanism
-        const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC || h->cfg.equation == WAVE_EQ_VISCOSH;
-        const int ncomp = e3 ? 6 : sh ? 2 : 3;   // memory-variable components per mechanism
+        const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC || h->cfg.equation == WAVE_EQ_VISCOSH ||
+                           h->cfg.equation == WAVE_EQ_VISCOTMEM;
+        const int ncomp = e3 ? 6 : sh ? 2 : tm ? 1 : 3;   // memory-variable components per mechanism
         const int nr = visco ? ncomp * h->L : 0;
         const int nf = em3 ? 6 : ac ? 4 : e3 ? 9 : 5, np = em3 ? 12 : ac ? 6 : e3 ? 18 : 8, nparts = nf + np + nr;
         for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
@@ -718,7 +735,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int memVar2[3] = {R_XX, R_YY, R_XY};
         const int memVar3[6] = {R_XX, R_YY, R_ZZ, R_XY, R_XZ, R_YZ};
         const int memVarSH[2] = {R_XZ, R_YZ};
-        const int* memVar = e3 ? memVar3 : sh ? memVarSH : memVar2;
+        const int memVarTM[1] = {R_EZ};
+        const int* memVar = e3 ? memVar3 : sh ? memVarSH : tm ? memVarTM : memVar2;
         auto rpart = [&](int j) { return h->r[memVar[j / h->L]][j % h->L]; };
         for (int j = 0; j < nr; ++j) { off[nf + np + j] = o; len[nf + np + j] = N; o += N; }
         stride[s] = o;
@@ -739,7 +757,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         for (int k = 0; k < np; ++k) a.lpsi[k] = lstate + off[nf + k];
         for (int k = 0; k < 6 * kMaxL; ++k) a.lr[k] = nullptr;
         for (int j = 0; j < nr; ++j) a.lr[(j / h->L) * kMaxL + j % h->L] = lstate + off[nf + np + j];
-        const int ntemp = e3 ? 18 : em3 ? 12 : 8, ngrad = e3 ? 8 : em3 ? 9 : 5;   // acoustic: 6 and 4 of them
+        // acoustic: 6 and 4 of them; visco-TMz: dJ/dCd_l in g[4 + l]
+        const int ntemp = e3 ? 18 : em3 ? 12 : 8, ngrad = e3 ? 8 : em3 ? 9 : (tm && visco) ? 4 + h->L : 5;
         float* temps = pool.get<float>(static_cast<size_t>(ntemp) * N);
         for (int k = 0; k < ntemp; ++k) a.T[k] = temps + k * N;
         float* grads = pool.get<float>(static_cast<size_t>(ngrad) * N);
@@ -862,7 +881,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             adj_e3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], A[s].visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f, gvp[o], gvs[o],
                                                grho[o], sum && s > 0 ? 1 : 0);
         else if (A[s].tm)
-            adj_tm_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
+            adj_tm_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), h->vemc, gvp[o], gvs[o], grho[o],
                                                sum && s > 0 ? 1 : 0);
         else if (A[s].sh)
             adj_sh_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], A[s].visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f, gvp[o], gvs[o],

@@ -317,10 +317,24 @@ __device__ __forceinline__ void adj_tm_e_body(const StepParams& P, const AdjShot
         A.lf[1][i] *= d;
     }
     const float ca = __ldg(P.m[M_CAZ] + i), cb = __ldg(P.m[M_CBZ] + i);
+    const float ez0 = X0[A.off[AV_SXX] + i];
     float l1 = cb * lez, l2 = -l1;
-    A.g[0][i] += lez * X0[A.off[AV_SXX] + i];
-    A.g[1][i] += lez * (c1 - c2);
-    A.lf[2][i] = ca * lez;
+    float u = c1 - c2, ln = ca * lez;
+    if (A.visco) {
+        // visco-TMz (ForwardSolver2Dviscotmem.cpp:175-200): rz_l' = Cc_l rz_l + Cd_l ez and
+        // ez' = Ca ez + Cb (c1' - c2' - DT sum_l rz_l'); rz_l' is state part 13 + l of X_{n+1}
+        for (int l = 0; l < P.L; ++l) {
+            u -= P.DT * X1[A.off[13 + l] + i];
+            float* r = A.lr[l] + i;
+            const float LR = *r - P.DT * cb * lez;   // adjoint of rz_l'
+            ln += __ldg(P.m[M_CDZ0 + l] + i) * LR;
+            A.g[4 + l][i] += LR * ez0;
+            *r = P.Cc[l] * LR;
+        }
+    }
+    A.g[0][i] += lez * ez0;
+    A.g[1][i] += lez * u;
+    A.lf[2][i] = ln;
     if (S.sx >= 0) cpml_adj(l1, A.lpsi[2] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // hyx: x, full profile
     if (S.sy >= 0) cpml_adj(l2, A.lpsi[3] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // hxy: y, full profile
     A.T[0][i] = l1;

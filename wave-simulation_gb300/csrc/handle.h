@@ -57,6 +57,7 @@ struct wave_handle {
 
     StepParams sp{};
     SrcRecParams sq{};
+    wave::ViscoEmCoef vemc{};          // visco-EM coefficient constants of the last model (the adjoint's chain rule)
     dim3 grid, block;
     bool modelSet = false;
     std::vector<int> fields;          // allocated field slots

@@ -929,6 +929,12 @@ int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, co
             k_inv_avg2(G, mu, 0, mat(M_IMUXZ), s);
             k_inv_avg2(G, mu, 1, mat(M_IMUYZ), s);
             coeffs(eps, dSig, dTe, dTs, M_CAZ, M_CBZ, M_CDZ0);
+            if (visco) {
+                // tau_eps and the scaled tau_sigma with the coefficient constants, for the adjoint's chain rule
+                h->check(cudaMemcpyAsync(mat(M_TAUP), dTe, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+                h->check(cudaMemcpyAsync(mat(M_TAUS), dTs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+                h->vemc = vc;
+            }
         } else {
             // EMEM/ViscoEMEM::calculateAveraging (EMEM.cpp:378-392, ViscoEMEM.cpp:409-432),
             // prepareForModelling of FD2Demem/FD2Dviscoemem/FD3Demem/FD3Dviscoemem
@@ -954,7 +960,7 @@ int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, co
                 coeffs(ea, sa, ta, tsa, caS[a], cbS[a], cdS[a]);
             }
         }
-        if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_EMEM) {
+        if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_EMEM || (eq == WAVE_EQ_VISCOTMEM && !is3d)) {
             // the base parameters, for the adjoint's chain rule (adjoint.cu)
             h->check(cudaMemcpyAsync(mat(M_EPSR), dEr, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
             h->check(cudaMemcpyAsync(mat(M_SIG), dSig, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
