@@ -438,7 +438,8 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *    Ez sources and receivers, CPML, ABS or no damping boundary: the three
  *    outputs receive dJ/deps_r, dJ/dsigma, dJ/dmu_r (the model's relative
  *    permittivity, conductivity and relative permeability);
- *  - lossless 2-D TEz (FD2Demem::run, ForwardSolver2Demem.cpp:112-185) with
+ *  - 2-D TEz and visco-TEz (FD2Demem::run, ForwardSolver2Demem.cpp:112-185;
+ *    FD2Dviscoemem::run, ForwardSolver2Dviscoemem.cpp:142-228, taus fixed) with
  *    Ex, Ey and Hz sources and receivers, CPML, ABS or no damping boundary:
  *    the same three outputs;
  *  - lossless 3-D EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237) with

@@ -793,9 +793,11 @@ struct TEAdjoint2D {
     Sim<T>& s;
     const idx_t N;
     CSR<T> DxfT, DxbT, DyfT, DybT;
-    explicit TEAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N())
+    const bool visco;   // 2-D visco-TEz (FD2Dviscoemem::run, ForwardSolver2Dviscoemem.cpp:142-228)
+
+    explicit TEAdjoint2D(Sim<T>& sim) : s(sim), N(sim.g.N()), visco(sim.eq == WAVE_EQ_VISCOEMEM)
     {
-        if (s.is3d || s.eq != WAVE_EQ_EMEM) throw std::invalid_argument("oracle adjoint: lossless 2-D TEz only");
+        if (s.is3d || (s.eq != WAVE_EQ_EMEM && s.eq != WAVE_EQ_VISCOEMEM)) throw std::invalid_argument("oracle adjoint: 2-D TEz only");
         DxfT = transpose(s.Dxf);
         DxbT = transpose(s.Dxb);
         DyfT = transpose(s.Dyf);
@@ -803,6 +805,7 @@ struct TEAdjoint2D {
     }
     struct State {
         std::map<std::string, std::vector<T>> F, psi;
+        std::map<std::string, std::vector<std::vector<T>>> R;
     };
     const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
     {
@@ -828,7 +831,7 @@ struct TEAdjoint2D {
         s.reset();
         std::vector<State> ck;
         for (int t = 0; t < NT; ++t) {
-            if (t % K == 0) ck.push_back({s.F, s.psi});
+            if (t % K == 0) ck.push_back({s.F, s.psi, s.R});
             s.step(t);
         }
         std::vector<T> res(nrec * static_cast<size_t>(NT));
@@ -841,6 +844,10 @@ struct TEAdjoint2D {
         std::map<std::string, std::vector<T>> lp;
         for (const char* n : {"eyx", "exy", "hzy", "hzx"}) lp[n].assign(N, 0);
         std::vector<T> gCaX(N, 0), gCbX(N, 0), gCaY(N, 0), gCbY(N, 0), gMxy(N, 0);
+        // visco: adjoints of the memory variables rx_l, ry_l and of Cd_x,l, Cd_y,l
+        const int L = visco ? s.L : 0;
+        std::vector<std::vector<T>> lR[2], gCd[2];
+        for (int q = 0; q < 2; ++q) { lR[q].assign(L, std::vector<T>(N, 0)); gCd[q].assign(L, std::vector<T>(N, 0)); }
         std::vector<T> a1(N), a2(N), c1(N), c2(N), hzp(N), la1(N), la2(N), lc1(N), lc2(N);
         const int nseg = static_cast<int>(ck.size());
         for (int seg = nseg - 1; seg >= 0; --seg) {
@@ -848,10 +855,11 @@ struct TEAdjoint2D {
             std::vector<State> X;
             s.F = ck[seg].F;
             s.psi = ck[seg].psi;
-            X.push_back({s.F, s.psi});
+            s.R = ck[seg].R;
+            X.push_back({s.F, s.psi, s.R});
             for (int t = t0; t < t1; ++t) {
                 s.step(t);
-                X.push_back({s.F, s.psi});
+                X.push_back({s.F, s.psi, s.R});
             }
             for (int t = t1 - 1; t >= t0; --t) {
                 const State& X0 = X[t - t0];
@@ -888,16 +896,32 @@ struct TEAdjoint2D {
                         auto& w = *v;
                         for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
                     }
-                // ex <- CaX ex + CbX c1', ey <- CaY ey - CbY c2'
+                // ex <- CaX ex + CbX (c1' - DT sum_l rx_l'), ey <- CaY ey + CbY (-c2' - DT sum_l ry_l'),
+                // r_l' = Cc_l r_l + Cd_l e (visco)
                 for_n(N, [&](idx_t i) {
+                    T ux = c1[i], uy = -c2[i];
+                    for (int l = 0; l < L; ++l) {
+                        ux -= s.DT * X1.R.at("rx")[l][i];
+                        uy -= s.DT * X1.R.at("ry")[l][i];
+                    }
                     lc1[i] = s.CbX[i] * lex[i];
                     lc2[i] = -s.CbY[i] * ley[i];
                     gCaX[i] += lex[i] * ex0[i];
-                    gCbX[i] += lex[i] * c1[i];
+                    gCbX[i] += lex[i] * ux;
                     gCaY[i] += ley[i] * ey0[i];
-                    gCbY[i] -= ley[i] * c2[i];
-                    lex[i] *= s.CaX[i];
-                    ley[i] *= s.CaY[i];
+                    gCbY[i] += ley[i] * uy;
+                    T nx = s.CaX[i] * lex[i], ny = s.CaY[i] * ley[i];
+                    for (int l = 0; l < L; ++l) {
+                        const T LX = lR[0][l][i] - s.DT * s.CbX[i] * lex[i], LY = lR[1][l][i] - s.DT * s.CbY[i] * ley[i];
+                        nx += s.CdX[l][i] * LX;
+                        ny += s.CdY[l][i] * LY;
+                        gCd[0][l][i] += LX * ex0[i];
+                        gCd[1][l][i] += LY * ey0[i];
+                        lR[0][l][i] = s.emCc[l] * LX;
+                        lR[1][l][i] = s.emCc[l] * LY;
+                    }
+                    lex[i] = nx;
+                    ley[i] = ny;
                 });
                 cpmlT(lc1, lp["hzy"], s.ay, s.by);
                 cpmlT(lc2, lp["hzx"], s.ax, s.bx);
@@ -921,18 +945,48 @@ struct TEAdjoint2D {
         std::vector<T> eps(N), ge(N, 0), gs(N, 0), ye(N), ys(N), avE(N), avS(N);
         for (idx_t i = 0; i < N; ++i) eps[i] = epsr[i] * eps0;
         AverageTranspose<T> probe(s);
+        // visco: Ca, Cb of the effective optical permittivity and conductivity of the averaged
+        // eps, sigma, tau_eps, tau_sigma; Cd_l = -DT te cdScale_l e (ForwardSolverEM.cpp:68-152)
+        T sumInv = 0;
+        std::vector<T> cdScale(L), avTe(N), avTs(N);
+        for (int l = 0; l < L; ++l) {
+            const double r = 1.0 / (2.0 * M_PI * static_cast<double>(static_cast<T>(s.cfg.relaxationFrequency[l])));
+            const T rt = static_cast<T>(r);
+            sumInv = static_cast<T>(static_cast<double>(sumInv) + 1.0 / static_cast<double>(rt));
+            T tv = static_cast<T>(1 / (1 + 0.5 * static_cast<double>(DT) / static_cast<double>(rt)));
+            tv /= (static_cast<T>(L) * rt * rt);
+            cdScale[l] = tv;
+        }
+        if (L > 0) sumInv /= static_cast<T>(L);
         for (Axis a : {Axis::X, Axis::Y}) {
             average2<T>(s.g, a, eps.data(), avE.data());
             average2<T>(s.g, a, sigma.data(), avS.data());
+            if (visco) {
+                average2<T>(s.g, a, s.emTauE.data(), avTe.data());
+                average2<T>(s.g, a, s.emTauS.data(), avTs.data());
+            }
             const std::vector<T>& gCa = a == Axis::X ? gCaX : gCaY;
             const std::vector<T>& gCb = a == Axis::X ? gCbX : gCbY;
+            const auto& gCdA = gCd[a == Axis::X ? 0 : 1];
             for (idx_t i = 0; i < N; ++i) {
-                const T e = avE[i], sg = avS[i];
+                T e = avE[i], sg = avS[i], de_de = 1, de_ds = 0, ds_de = 0;
+                if (visco) {
+                    const T te = avTe[i], ts = avTs[i];
+                    const T eo = (T(1) - te) * avE[i] + avS[i] * ts;
+                    const bool clamp = eo < eps0;
+                    e = clamp ? eps0 : eo;
+                    de_de = clamp ? T(0) : T(1) - te;
+                    de_ds = clamp ? T(0) : ts;
+                    sg = te * sumInv * avE[i] + avS[i];
+                    ds_de = te * sumInv;
+                }
                 const T k = sg * DT / (T(2) * e), q = T(1) + k;
                 const T dCa_de = T(2) * k / (e * q * q), dCa_ds = -T(2) / (q * q) * DT / (T(2) * e);
                 const T dCb_de = -T(1) / (e * e * q) + k / (e * e * q * q), dCb_ds = -(T(1) / e) / (q * q) * DT / (T(2) * e);
-                ye[i] = gCa[i] * dCa_de + gCb[i] * dCb_de;
-                ys[i] = gCa[i] * dCa_ds + gCb[i] * dCb_ds;
+                const T gE = gCa[i] * dCa_de + gCb[i] * dCb_de, gS = gCa[i] * dCa_ds + gCb[i] * dCb_ds;
+                ye[i] = gE * de_de + gS * ds_de;
+                ys[i] = gE * de_ds + gS;
+                for (int l = 0; l < L; ++l) ye[i] += gCdA[l][i] * (-DT) * avTe[i] * cdScale[l];
             }
             probe.avgT([&](const T* in, T* out) { average2<T>(s.g, a, in, out); }, ye, ge);
             probe.avgT([&](const T* in, T* out) { average2<T>(s.g, a, in, out); }, ys, gs);

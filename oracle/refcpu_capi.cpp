@@ -283,7 +283,7 @@ int refcpu_adjoint_tmz(void* hv, const double* epsr, const double* sigma, const 
         if (s->eq == WAVE_EQ_EMEM && s->is3d) {
             refcpu::EM3Adjoint<T> adj(*s);
             *misfit = adj.run(E, S, U, D.data(), K, a.data(), b.data(), c.data());
-        } else if (s->eq == WAVE_EQ_EMEM) {
+        } else if (s->eq == WAVE_EQ_EMEM || s->eq == WAVE_EQ_VISCOEMEM) {
             refcpu::TEAdjoint2D<T> adj(*s);
             *misfit = adj.run(E, S, U, D.data(), K, a.data(), b.data(), c.data());
         } else {

@@ -125,10 +125,10 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("dim,equation", [(2, "viscoemem"), (3, "viscoelastic")])
+@pytest.mark.parametrize("dim,equation", [(3, "viscoemem"), (3, "viscoelastic")])
 def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
-    """Set-ups without an adjoint are refused with WAVE_ERR_UNSUPPORTED: visco-TEz, and the visco-elastic free
-    surface (its relaxation exchange is not differentiated)."""
+    """Set-ups without an adjoint are refused with WAVE_ERR_UNSUPPORTED: 3-D visco-EM, and the visco-elastic
+    free surface (its relaxation exchange is not differentiated)."""
     cfg = _config(wave, dim=dim, fs=1 if equation == "viscoelastic" else 0)
     cfg.equation = wave.EQUATIONS[equation]
     cfg.numRelaxationMechanisms = 1
@@ -144,7 +144,7 @@ def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
         model["taus"] = np.full(n, 0.03, np.float32)
     s = wave.Factory.Create("3D" if dim == 3 else "2D", equation).initForwardSolver(cfg)
     s.prepareForModelling(model)
-    s.setSources(np.array([5], np.int64), np.array([4 if equation == "viscoemem" else 1], np.int32), np.zeros((1, s.nt), np.float32))
+    s.setSources(np.array([5], np.int64), np.array([1], np.int32), np.zeros((1, s.nt), np.float32))
     s.setReceivers(np.array([7], np.int64), np.array([2], np.int32))
     with pytest.raises(wave.WaveError) as e:
         s.adjoint_gradient(np.zeros((1, s.nt), np.float32))

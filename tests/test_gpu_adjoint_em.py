@@ -49,6 +49,10 @@ def _survey(wave, refcpu, boundary, stencil, reduce, L=0):
     return ocfg, cfg, m32, acq32, dobs
 
 
+def _te_key(cfg):
+    return "viscoemem" if cfg.numRelaxationMechanisms > 0 else "emem"
+
+
 def _tm_key(cfg):
     return "viscotmem" if cfg.numRelaxationMechanisms > 0 else "tmem"
 
@@ -123,8 +127,8 @@ def test_tmz_adjoint_rejects_other_receiver_components(wave, refcpu):
     s.close()
 
 
-def _te_survey(wave, refcpu, boundary, stencil, reduce, order=4):
-    ocfg, model, acq = te_case(refcpu, boundary, stencil, reduce, order=order, NX=72, NY=60, nt=400)
+def _te_survey(wave, refcpu, boundary, stencil, reduce, order=4, L=0):
+    ocfg, model, acq = te_case(refcpu, boundary, stencil, reduce, order=order, NX=72, NY=60, nt=400, L=L)
     cfg = _wave_cfg(wave, ocfg)
     m32 = {k: v.astype(np.float32) for k, v in model.items()}
     yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
@@ -134,7 +138,7 @@ def _te_survey(wave, refcpu, boundary, stencil, reduce, order=4):
     true["sigma"] = (m32["sigma"] * (1 + 0.5 * blob)).astype(np.float32)
     true["mu_r"] = (m32["mu_r"] * (1 + 0.05 * blob)).astype(np.float32)
     acq32 = (acq[0], acq[1], acq[2].astype(np.float32), acq[3], acq[4])
-    s = wave.Factory.Create("2D", "emem").initForwardSolver(cfg)
+    s = wave.Factory.Create("2D", _te_key(cfg)).initForwardSolver(cfg)
     s.prepareForModelling(true)
     s.setSources(*acq32[:3])
     s.setReceivers(*acq32[3:])
@@ -145,12 +149,14 @@ def _te_survey(wave, refcpu, boundary, stencil, reduce, order=4):
     return ocfg, cfg, m32, acq32, dobs
 
 
-@pytest.mark.parametrize("boundary,stencil,reduce,order", [(2, 0, 0, 4), (0, 1, 0, 2), (1, 0, 0, 6), (2, 0, 1, 8)])
-def test_tez_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, stencil, reduce, order):
+@pytest.mark.parametrize("boundary,stencil,reduce,order,L", [(2, 0, 0, 4, 0), (0, 1, 0, 2, 0), (1, 0, 0, 6, 0), (2, 0, 1, 8, 0),
+                                                             (2, 0, 0, 4, 1), (1, 1, 0, 6, 2)])
+def test_tez_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, stencil, reduce, order, L):
     """Ey and Hz sources (the Hz source exercises the re-formed pre-taper hz),
-    Ex, Ey and Hz receivers."""
-    ocfg, cfg, m32, acq, dobs = _te_survey(wave, refcpu, boundary, stencil, reduce, order)
-    s = wave.Factory.Create("2D", "emem").initForwardSolver(cfg)
+    Ex, Ey and Hz receivers; L > 0: visco-TEz (FD2Dviscoemem::run,
+    ForwardSolver2Dviscoemem.cpp:142-228), tau_eps and tau_sigma fixed."""
+    ocfg, cfg, m32, acq, dobs = _te_survey(wave, refcpu, boundary, stencil, reduce, order, L)
+    s = wave.Factory.Create("2D", _te_key(cfg)).initForwardSolver(cfg)
     s.prepareForModelling(m32)
     s.setSources(*acq[:3])
     s.setReceivers(*acq[3:])
@@ -161,7 +167,7 @@ def test_tez_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, st
     J64, re, rs, rm = o.adjoint_gradient(dobs.astype(np.float64), checkpoint_every=45)
     o.close()
     errs = [_rel(a, b) for a, b in ((ge, re), (gs, rs), (gm, rm))]
-    print(f"TEz adjoint boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} vs FP64 "
+    print(f"TEz adjoint L={L} boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} vs FP64 "
           f"{J64:.6e}; gradient rel L2 eps_r {errs[0]:.2e} sigma {errs[1]:.2e} mu_r {errs[2]:.2e}")
     assert J > 0 and abs(J - J64) <= 1e-4 * J64
     assert max(errs) <= GRAD_TOL
@@ -173,7 +179,7 @@ def test_tez_batched_adjoint_equals_single_shots(wave, refcpu):
     for k in range(2):
         a = (acq[0] + 7 * k, acq[1], acq[2], acq[3], acq[4])
         acqs.append(a)
-        s = wave.Factory.Create("2D", "emem").initForwardSolver(cfg)
+        s = wave.Factory.Create("2D", _te_key(cfg)).initForwardSolver(cfg)
         s.prepareForModelling(m32)
         s.setSources(*a[:3])
         s.setReceivers(*a[3:])

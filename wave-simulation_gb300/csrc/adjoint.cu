@@ -381,8 +381,8 @@ __global__ void adj_sh_final(PrepParams G, const StepParams P, const AdjShot A, 
 // chain rule for TEz: CaX, CbX of the 2-point x averages of eps = eps_r eps0
 // and sigma (CaY, CbY along y); iMxy = 1 / (4-point average of mu = mu_r mu0)
 // (0 where invalid)
-__global__ void adj_te_final(PrepParams G, const StepParams P, const AdjShot A, float DT, float* geps, float* gsig, float* gmu,
-                             int accumulate)
+__global__ void adj_te_final(PrepParams G, const StepParams P, const AdjShot A, float DT, ViscoEmCoef vc, float* geps, float* gsig,
+                             float* gmu, int accumulate)
 {
     const float eps0 = 8.8541878176e-12f, mu0 = 1.2566370614e-6f;
     const float* er = P.m[M_EPSR];
@@ -392,31 +392,40 @@ __global__ void adj_te_final(PrepParams G, const StepParams P, const AdjShot A, 
         float ge = 0.0f, gs = 0.0f;
         // rows (kx, ky) and (kx-1, ky) of the x averages, (kx, ky) and (kx, ky-1) of the y averages
         for (int d = 0; d <= 1; ++d) {
-            if (kx - d >= 0) {
-                const long long r = k - d;
-                const bool pair = kx - d + 1 < G.NX;
-                if (d == 0 || pair) {
-                    const float w = pair ? 0.5f : 1.0f;
-                    const float e = pair ? 0.5f * (er[r] * eps0) + 0.5f * (er[r + 1] * eps0) : er[r] * eps0;
-                    const float s = pair ? 0.5f * sg[r] + 0.5f * sg[r + 1] : sg[r];
-                    float a, b;
-                    cacb_adj(e, s, DT, A.g[0][r], A.g[1][r], a, b);
-                    ge += w * a;
-                    gs += w * b;
+            for (int q = 0; q < 2; ++q) {
+                const int c = q == 0 ? kx : ky, Nc = q == 0 ? static_cast<int>(G.NX) : static_cast<int>(G.NY);
+                const long long st = q == 0 ? 1 : G.NX;
+                if (c - d < 0) continue;
+                const long long r = k - d * st;
+                const bool pair = c - d + 1 < Nc;
+                if (!(d == 0 || pair)) continue;
+                const float w = pair ? 0.5f : 1.0f;
+                const float e0 = pair ? 0.5f * (er[r] * eps0) + 0.5f * (er[r + st] * eps0) : er[r] * eps0;
+                const float s0 = pair ? 0.5f * sg[r] + 0.5f * sg[r + st] : sg[r];
+                // visco: Ca, Cb of the optical permittivity / conductivity of the averaged eps, sigma,
+                // tau_eps, tau_sigma; Cd_l = -DT te cdScale_l e (prep_visco_em), the taus held fixed
+                float e = e0, s = s0, de_de = 1.0f, de_ds = 0.0f, ds_de = 0.0f, tq = 0.0f;
+                if (A.visco) {
+                    const float* te = P.m[M_TAUP];
+                    const float* ts = P.m[M_TAUS];
+                    tq = pair ? 0.5f * te[r] + 0.5f * te[r + st] : te[r];
+                    const float sq = pair ? 0.5f * ts[r] + 0.5f * ts[r + st] : ts[r];
+                    const float eo = (1.0f - tq) * e0 + s0 * sq;
+                    const bool clamp = eo < eps0;
+                    e = clamp ? eps0 : eo;
+                    de_de = clamp ? 0.0f : 1.0f - tq;
+                    de_ds = clamp ? 0.0f : sq;
+                    s = tq * vc.sumInv * e0 + s0;
+                    ds_de = tq * vc.sumInv;
                 }
-            }
-            if (ky - d >= 0) {
-                const long long r = k - d * (long long)G.NX;
-                const bool pair = ky - d + 1 < G.NY;
-                if (d == 0 || pair) {
-                    const float w = pair ? 0.5f : 1.0f;
-                    const float e = pair ? 0.5f * (er[r] * eps0) + 0.5f * (er[r + G.NX] * eps0) : er[r] * eps0;
-                    const float s = pair ? 0.5f * sg[r] + 0.5f * sg[r + G.NX] : sg[r];
-                    float a, b;
-                    cacb_adj(e, s, DT, A.g[2][r], A.g[3][r], a, b);
-                    ge += w * a;
-                    gs += w * b;
-                }
+                float a, b;
+                cacb_adj(e, s, DT, A.g[2 * q][r], A.g[2 * q + 1][r], a, b);
+                float ga = a * de_de + b * ds_de;
+                const float gb = a * de_ds + b;
+                if (A.visco)
+                    for (int l = 0; l < vc.L; ++l) ga += A.g[5 + q * vc.L + l][r] * (-DT) * tq * vc.cdScale[l];
+                ge += w * ga;
+                gs += w * gb;
             }
         }
         float gm = 0.0f;
@@ -642,7 +651,8 @@ std::string adjoint_supported(const wave_handle* h)
     const wave_config& c = h->cfg;
     const bool ok2 = c.dimension == 2 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_SH ||
                                           c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC ||
-                                          c.equation == WAVE_EQ_VISCOSH || c.equation == WAVE_EQ_VISCOTMEM);
+                                          c.equation == WAVE_EQ_VISCOSH || c.equation == WAVE_EQ_VISCOTMEM ||
+                                          c.equation == WAVE_EQ_VISCOEMEM);
     const bool ok3 = c.dimension == 3 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_VISCOELASTIC || c.equation == WAVE_EQ_EMEM);
     const bool okAc = c.equation == WAVE_EQ_ACOUSTIC;
     if (!ok2 && !ok3 && !okAc)
@@ -702,7 +712,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int tmFields[5] = {F_HX, F_HY, F_EZ, -1, -1};
         const int tmPsi[8] = {PS_EZY, PS_EZX, PS_HYX, PS_HXY, -1, -1, -1, -1};
         // TEz: hz, -, ex, ey and the psi of eyx, exy, -, -, hzy, hzx
-        const bool te = h->cfg.equation == WAVE_EQ_EMEM;
+        const bool te = h->cfg.equation == WAVE_EQ_EMEM || h->cfg.equation == WAVE_EQ_VISCOEMEM;
         const int shFields[5] = {F_VZ, -1, F_SXZ, F_SYZ, -1};
         const int shPsi[8] = {PS_SXZ_X, PS_SYZ_Y, -1, -1, PS_VZX, PS_VZY, -1, -1};
         const int teFields[5] = {F_HZ, -1, F_EX, F_EY, -1};
@@ -721,8 +731,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int* psiSlot = em3 ? em3Psi : ac ? acPsi : e3 ? e3Psi : tm ? tmPsi : sh ? shPsi : te ? tePsi : kAdjPsiSlot;
         // visco-elastic: the elastic parts, then rxx, ryy, rxy of each mechanism
         const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC || h->cfg.equation == WAVE_EQ_VISCOSH ||
-                           h->cfg.equation == WAVE_EQ_VISCOTMEM;
-        const int ncomp = e3 ? 6 : sh ? 2 : tm ? 1 : 3;   // memory-variable components per mechanism
+                           h->cfg.equation == WAVE_EQ_VISCOTMEM || h->cfg.equation == WAVE_EQ_VISCOEMEM;
+        const int ncomp = e3 ? 6 : (sh || te) ? 2 : tm ? 1 : 3;   // memory-variable components per mechanism
         const int nr = visco ? ncomp * h->L : 0;
         const int nf = em3 ? 6 : ac ? 4 : e3 ? 9 : 5, np = em3 ? 12 : ac ? 6 : e3 ? 18 : 8, nparts = nf + np + nr;
         for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
@@ -736,7 +746,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int memVar3[6] = {R_XX, R_YY, R_ZZ, R_XY, R_XZ, R_YZ};
         const int memVarSH[2] = {R_XZ, R_YZ};
         const int memVarTM[1] = {R_EZ};
-        const int* memVar = e3 ? memVar3 : sh ? memVarSH : tm ? memVarTM : memVar2;
+        const int memVarTE[2] = {R_EX, R_EY};
+        const int* memVar = e3 ? memVar3 : sh ? memVarSH : tm ? memVarTM : te ? memVarTE : memVar2;
         auto rpart = [&](int j) { return h->r[memVar[j / h->L]][j % h->L]; };
         for (int j = 0; j < nr; ++j) { off[nf + np + j] = o; len[nf + np + j] = N; o += N; }
         stride[s] = o;
@@ -758,7 +769,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         for (int k = 0; k < 6 * kMaxL; ++k) a.lr[k] = nullptr;
         for (int j = 0; j < nr; ++j) a.lr[(j / h->L) * kMaxL + j % h->L] = lstate + off[nf + np + j];
         // acoustic: 6 and 4 of them; visco-TMz: dJ/dCd_l in g[4 + l]
-        const int ntemp = e3 ? 18 : em3 ? 12 : 8, ngrad = e3 ? 8 : em3 ? 9 : (tm && visco) ? 4 + h->L : 5;
+        const int ntemp = e3 ? 18 : em3 ? 12 : 8;
+        const int ngrad = e3 ? 8 : em3 ? 9 : (tm && visco) ? 4 + h->L : (te && visco) ? 5 + 2 * h->L : 5;
         float* temps = pool.get<float>(static_cast<size_t>(ntemp) * N);
         for (int k = 0; k < ntemp; ++k) a.T[k] = temps + k * N;
         float* grads = pool.get<float>(static_cast<size_t>(ngrad) * N);
@@ -887,7 +899,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
             adj_sh_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], A[s].visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f, gvp[o], gvs[o],
                                                grho[o], sum && s > 0 ? 1 : 0);
         else if (A[s].te)
-            adj_te_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
+            adj_te_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), h->vemc, gvp[o], gvs[o], grho[o],
                                                sum && s > 0 ? 1 : 0);
         else
             adj_grad_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], A[s].visco ? visco_modulus_sum(h->cfg, h->L) : 0.0f, gvp[o],

@@ -30,7 +30,7 @@ struct AdjShot {
     float* lf[9];                // adjoint fields (2-D elastic: vx, vy, sxx, syy, sxy)
     float* lpsi[18];             // adjoint psi (slab layout of the forward psi)
     float* T[18];                // adjoints of the raw derivatives (2-D elastic: c1..c4, a1..a4)
-    float* g[9];                 // material adjoints (2-D elastic: dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry)
+    float* g[13];                // material adjoints (2-D elastic: dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry)
     const long long* ridx;
     const int* rtype;
     const float* res;            // residual d - d_obs, nrec x nt
@@ -491,13 +491,33 @@ __device__ __forceinline__ void adj_te_e_body(const StepParams& P, const AdjShot
     }
     const float cax = __ldg(P.m[M_CAX] + i), cbx = __ldg(P.m[M_CBX] + i);
     const float cay = __ldg(P.m[M_CAY] + i), cby = __ldg(P.m[M_CBY] + i);
-    A.g[0][i] += lex * X0[A.off[AV_SXX] + i];
-    A.g[1][i] += lex * c1;
-    A.g[2][i] += ley * X0[A.off[AV_SYY] + i];
-    A.g[3][i] -= ley * c2;
+    const float ex0 = X0[A.off[AV_SXX] + i], ey0 = X0[A.off[AV_SYY] + i];
+    float ux = c1, uy = -c2, lnx = cax * lex, lny = cay * ley;
+    if (A.visco) {
+        // visco-TEz (ForwardSolver2Dviscoemem.cpp:176-220): r_l' = Cc_l r_l + Cd_l e per component, and
+        // ex' = CaX ex + CbX (c1' - DT sum_l rx_l'), ey' = CaY ey + CbY (-c2' - DT sum_l ry_l');
+        // rx_l', ry_l' are state parts 13 + l, 13 + L + l of X_{n+1}; dJ/dCd in g[5 + l], g[5 + L + l]
+        for (int l = 0; l < P.L; ++l) {
+            ux -= P.DT * X1[A.off[13 + l] + i];
+            uy -= P.DT * X1[A.off[13 + P.L + l] + i];
+            float* rx = A.lr[l] + i;
+            float* ry = A.lr[kMaxL + l] + i;
+            const float LX = *rx - P.DT * cbx * lex, LY = *ry - P.DT * cby * ley;   // adjoints of rx_l', ry_l'
+            lnx += __ldg(P.m[M_CDX0 + l] + i) * LX;
+            lny += __ldg(P.m[M_CDY0 + l] + i) * LY;
+            A.g[5 + l][i] += LX * ex0;
+            A.g[5 + P.L + l][i] += LY * ey0;
+            *rx = P.Cc[l] * LX;
+            *ry = P.Cc[l] * LY;
+        }
+    }
+    A.g[0][i] += lex * ex0;
+    A.g[1][i] += lex * ux;
+    A.g[2][i] += ley * ey0;
+    A.g[3][i] += ley * uy;
     float l1 = cbx * lex, l2 = -cby * ley;
-    A.lf[2][i] = cax * lex;
-    A.lf[3][i] = cay * ley;
+    A.lf[2][i] = lnx;
+    A.lf[3][i] = lny;
     if (S.sy >= 0) cpml_adj(l1, A.lpsi[4] + S.py, P.cy.a_full[p.y], P.cy.b_full[p.y]);   // hzy: y, full profile
     if (S.sx >= 0) cpml_adj(l2, A.lpsi[5] + S.px, P.cx.a_full[p.x], P.cx.b_full[p.x]);   // hzx: x, full profile
     A.T[0][i] = l1;
