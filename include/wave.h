@@ -442,8 +442,9 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *    FD2Dviscoemem::run, ForwardSolver2Dviscoemem.cpp:142-228, taus fixed) with
  *    Ex, Ey and Hz sources and receivers, CPML, ABS or no damping boundary:
  *    the same three outputs;
- *  - lossless 3-D EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237) with
- *    CPML, ABS or no damping boundary: the same three outputs;
+ *  - 3-D EM and visco-EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237;
+ *    FD3Dviscoemem::run, ForwardSolver3Dviscoemem.cpp:161-309, taus fixed)
+ *    with CPML, ABS or no damping boundary: the same three outputs;
  * other equations return WAVE_ERR_UNSUPPORTED. Runs the
  * forward over all NT steps from a zero state (the handle's sources and
  * receivers; seismograms are left as computed), saving the state every

@@ -1537,9 +1537,11 @@ struct EM3Adjoint {
     CSR<T> DxfT, DyfT, DzfT, DxbT, DybT, DzbT;
     static constexpr const char* kA[6] = {"ezy", "eyz", "exz", "ezx", "eyx", "exy"};
     static constexpr const char* kC[6] = {"hzy", "hyz", "hxz", "hzx", "hyx", "hxy"};
-    explicit EM3Adjoint(Sim<T>& sim) : s(sim), N(sim.g.N())
+    const bool visco;   // 3-D visco-EM (FD3Dviscoemem::run, ForwardSolver3Dviscoemem.cpp:161-309)
+
+    explicit EM3Adjoint(Sim<T>& sim) : s(sim), N(sim.g.N()), visco(sim.eq == WAVE_EQ_VISCOEMEM)
     {
-        if (!s.is3d || s.eq != WAVE_EQ_EMEM) throw std::invalid_argument("oracle adjoint: lossless 3-D EM only");
+        if (!s.is3d || (s.eq != WAVE_EQ_EMEM && s.eq != WAVE_EQ_VISCOEMEM)) throw std::invalid_argument("oracle adjoint: 3-D EM only");
         DxfT = transpose(s.Dxf);
         DyfT = transpose(s.Dyf);
         DzfT = transpose(s.Dzf);
@@ -1549,6 +1551,7 @@ struct EM3Adjoint {
     }
     struct State {
         std::map<std::string, std::vector<T>> F, psi;
+        std::map<std::string, std::vector<std::vector<T>>> R;
     };
     const std::vector<T>& psiOf(const State& x, const char* n, const std::vector<T>& zero) const
     {
@@ -1586,7 +1589,7 @@ struct EM3Adjoint {
         s.reset();
         std::vector<State> ck;
         for (int t = 0; t < NT; ++t) {
-            if (t % K == 0) ck.push_back({s.F, s.psi});
+            if (t % K == 0) ck.push_back({s.F, s.psi, s.R});
             s.step(t);
         }
         std::vector<T> res(nrec * static_cast<size_t>(NT));
@@ -1606,16 +1609,23 @@ struct EM3Adjoint {
         const std::vector<T>* Cb[3] = {&s.CbX, &s.CbY, &s.CbZ};
         const char* hn[3] = {"hx", "hy", "hz"};
         const char* en[3] = {"ex", "ey", "ez"};
+        const char* rn[3] = {"rx", "ry", "rz"};
+        // visco: adjoints of the memory variables and of Cd per component and mechanism
+        const int L = visco ? s.L : 0;
+        std::vector<std::vector<T>> lR[3], gCd[3];
+        for (int q = 0; q < 3; ++q) { lR[q].assign(L, std::vector<T>(N, 0)); gCd[q].assign(L, std::vector<T>(N, 0)); }
+        const std::vector<std::vector<T>>* Cd[3] = {&s.CdX, &s.CdY, &s.CdZ};
         const int nseg = static_cast<int>(ck.size());
         for (int seg = nseg - 1; seg >= 0; --seg) {
             const int t0 = seg * K, t1 = std::min(NT, t0 + K);
             std::vector<State> X;
             s.F = ck[seg].F;
             s.psi = ck[seg].psi;
-            X.push_back({s.F, s.psi});
+            s.R = ck[seg].R;
+            X.push_back({s.F, s.psi, s.R});
             for (int t = t0; t < t1; ++t) {
                 s.step(t);
-                X.push_back({s.F, s.psi});
+                X.push_back({s.F, s.psi, s.R});
             }
             for (int t = t1 - 1; t >= t0; --t) {
                 const State& X0 = X[t - t0];
@@ -1657,18 +1667,27 @@ struct EM3Adjoint {
                         auto& w = lF[n];
                         for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
                     }
-                // E <- Ca E + Cb (c' - c'')
+                // E <- Ca E + Cb (c' - c'' - DT sum_l r_l'), r_l' = Cc_l r_l + Cd_l E (visco)
                 for (int q = 0; q < 3; ++q) {
                     auto& le = lF[en[q]];
                     const auto& e0 = X0.F.at(en[q]);
                     const auto& ca = *Ca[q];
                     const auto& cb = *Cb[q];
                     for_n(N, [&](idx_t i) {
+                        T u = c[2 * q][i] - c[2 * q + 1][i];
+                        for (int l = 0; l < L; ++l) u -= s.DT * X1.R.at(rn[q])[l][i];
                         lc[2 * q][i] = cb[i] * le[i];
                         lc[2 * q + 1][i] = -cb[i] * le[i];
                         gCa[q][i] += le[i] * e0[i];
-                        gCb[q][i] += le[i] * (c[2 * q][i] - c[2 * q + 1][i]);
-                        le[i] *= ca[i];
+                        gCb[q][i] += le[i] * u;
+                        T ln = ca[i] * le[i];
+                        for (int l = 0; l < L; ++l) {
+                            const T LR = lR[q][l][i] - s.DT * cb[i] * le[i];
+                            ln += (*Cd[q])[l][i] * LR;
+                            gCd[q][l][i] += LR * e0[i];
+                            lR[q][l][i] = s.emCc[l] * LR;
+                        }
+                        le[i] = ln;
                     });
                 }
                 for (int k = 0; k < 6; ++k) cpmlT(lc[k], lp[kC[k]], kC[k]);
@@ -1701,20 +1720,49 @@ struct EM3Adjoint {
         // inverse 4-point averages of mu in the yz, xz and xy planes
         const T eps0 = static_cast<T>(8.8541878176e-12), mu0 = static_cast<T>(1.2566370614e-6);
         const T DT = s.DT;
-        std::vector<T> eps(N), ge(N, 0), gs(N, 0), ye(N), ys(N), avE(N), avS(N), y(N), gm(N, 0);
+        std::vector<T> eps(N), ge(N, 0), gs(N, 0), ye(N), ys(N), avE(N), avS(N), y(N), gm(N, 0), avTe(N), avTs(N);
         for (idx_t i = 0; i < N; ++i) eps[i] = epsr[i] * eps0;
+        // visco: the optical permittivity / conductivity of the averaged eps, sigma, tau_eps,
+        // tau_sigma and Cd_l = -DT te cdScale_l e (ForwardSolverEM.cpp:68-152), the taus fixed
+        T sumInv = 0;
+        std::vector<T> cdScale(L);
+        for (int l = 0; l < L; ++l) {
+            const double r = 1.0 / (2.0 * M_PI * static_cast<double>(static_cast<T>(s.cfg.relaxationFrequency[l])));
+            const T rt = static_cast<T>(r);
+            sumInv = static_cast<T>(static_cast<double>(sumInv) + 1.0 / static_cast<double>(rt));
+            T tv = static_cast<T>(1 / (1 + 0.5 * static_cast<double>(DT) / static_cast<double>(rt)));
+            tv /= (static_cast<T>(L) * rt * rt);
+            cdScale[l] = tv;
+        }
+        if (L > 0) sumInv /= static_cast<T>(L);
         AverageTranspose<T> probe(s);
         const Axis axes[3] = {Axis::X, Axis::Y, Axis::Z};
         for (int q = 0; q < 3; ++q) {
             average2<T>(s.g, axes[q], eps.data(), avE.data());
             average2<T>(s.g, axes[q], sigma.data(), avS.data());
+            if (visco) {
+                average2<T>(s.g, axes[q], s.emTauE.data(), avTe.data());
+                average2<T>(s.g, axes[q], s.emTauS.data(), avTs.data());
+            }
             for (idx_t i = 0; i < N; ++i) {
-                const T e = avE[i], sg = avS[i];
+                T e = avE[i], sg = avS[i], de_de = 1, de_ds = 0, ds_de = 0;
+                if (visco) {
+                    const T te = avTe[i], ts = avTs[i];
+                    const T eo = (T(1) - te) * avE[i] + avS[i] * ts;
+                    const bool clamp = eo < eps0;
+                    e = clamp ? eps0 : eo;
+                    de_de = clamp ? T(0) : T(1) - te;
+                    de_ds = clamp ? T(0) : ts;
+                    sg = te * sumInv * avE[i] + avS[i];
+                    ds_de = te * sumInv;
+                }
                 const T k = sg * DT / (T(2) * e), qq = T(1) + k;
                 const T dCa_de = T(2) * k / (e * qq * qq), dCa_ds = -T(2) / (qq * qq) * DT / (T(2) * e);
                 const T dCb_de = -T(1) / (e * e * qq) + k / (e * e * qq * qq), dCb_ds = -(T(1) / e) / (qq * qq) * DT / (T(2) * e);
-                ye[i] = gCa[q][i] * dCa_de + gCb[q][i] * dCb_de;
-                ys[i] = gCa[q][i] * dCa_ds + gCb[q][i] * dCb_ds;
+                const T gE = gCa[q][i] * dCa_de + gCb[q][i] * dCb_de, gS = gCa[q][i] * dCa_ds + gCb[q][i] * dCb_ds;
+                ye[i] = gE * de_de + gS * ds_de;
+                ys[i] = gE * de_ds + gS;
+                for (int l = 0; l < L; ++l) ye[i] += gCd[q][l][i] * (-DT) * avTe[i] * cdScale[l];
             }
             probe.avgT([&](const T* in, T* out) { average2<T>(s.g, axes[q], in, out); }, ye, ge);
             probe.avgT([&](const T* in, T* out) { average2<T>(s.g, axes[q], in, out); }, ys, gs);

@@ -280,7 +280,7 @@ int refcpu_adjoint_tmz(void* hv, const double* epsr, const double* sigma, const 
         using T = typename std::decay_t<decltype(s->M)>::value_type;
         const size_t N = s->g.N(), nd = s->rec.idx.size() * static_cast<size_t>(s->NT);
         std::vector<T> E(epsr, epsr + N), S(sigma, sigma + N), U(mur, mur + N), D(dobs, dobs + nd), a(N), b(N), c(N);
-        if (s->eq == WAVE_EQ_EMEM && s->is3d) {
+        if ((s->eq == WAVE_EQ_EMEM || s->eq == WAVE_EQ_VISCOEMEM) && s->is3d) {
             refcpu::EM3Adjoint<T> adj(*s);
             *misfit = adj.run(E, S, U, D.data(), K, a.data(), b.data(), c.data());
         } else if (s->eq == WAVE_EQ_EMEM || s->eq == WAVE_EQ_VISCOEMEM) {

@@ -202,12 +202,14 @@ def test_tez_batched_adjoint_equals_single_shots(wave, refcpu):
             assert np.abs(want).max() > 0 and np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("boundary,stencil,reduce,order", [(2, 0, 0, 4), (1, 1, 0, 2), (0, 0, 1, 6)])
-def test_em3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, stencil, reduce, order):
-    """Lossless 3-D EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237; Ez and Hz sources, Ez / Ex / Ey /
-    Hz receivers) against the oracle's FP64 3-D EM adjoint (EM3Adjoint, pinned to FP64 finite
+@pytest.mark.parametrize("boundary,stencil,reduce,order,L", [(2, 0, 0, 4, 0), (1, 1, 0, 2, 0), (0, 0, 1, 6, 0), (2, 0, 0, 4, 1),
+                                                             (1, 0, 1, 2, 2)])
+def test_em3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, stencil, reduce, order, L):
+    """3-D EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237; L > 0: FD3Dviscoemem::run,
+    ForwardSolver3Dviscoemem.cpp:161-309 with the taus fixed; Ez and Hz sources, Ez / Ex / Ey / Hz
+    receivers) against the oracle's FP64 3-D EM adjoint (EM3Adjoint, pinned to FP64 finite
     differences at 1e-6)."""
-    ocfg, model, acq = em3_case(refcpu, boundary, stencil, reduce, order=order, NX=40, NY=32, NZ=36, nt=260)
+    ocfg, model, acq = em3_case(refcpu, boundary, stencil, reduce, order=order, NX=40, NY=32, NZ=36, nt=260, L=L)
     cfg = _wave_cfg(wave, ocfg)
     m32 = {k: v.astype(np.float32) for k, v in model.items()}
     y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
@@ -218,7 +220,7 @@ def test_em3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, s
     acq32 = (acq[0], acq[1], acq[2].astype(np.float32), acq[3], acq[4])
 
     def solver(model_):
-        s = wave.Factory.Create("3D", "emem").initForwardSolver(cfg)
+        s = wave.Factory.Create("3D", "viscoemem" if L else "emem").initForwardSolver(cfg)
         s.prepareForModelling(model_)
         s.setSources(*acq32[:3])
         s.setReceivers(*acq32[3:])
@@ -236,7 +238,7 @@ def test_em3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, boundary, s
     J64, re, rs, rm = o.adjoint_gradient(dobs.astype(np.float64), checkpoint_every=45)
     o.close()
     errs = [_rel(a, b) for a, b in ((ge, re), (gs, rs), (gm, rm))]
-    print(f"3-D EM adjoint boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} vs FP64 "
+    print(f"3-D EM adjoint L={L} boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} vs FP64 "
           f"{J64:.6e}; gradient rel L2 eps_r {errs[0]:.2e} sigma {errs[1]:.2e} mu_r {errs[2]:.2e}")
     assert J > 0 and abs(J - J64) <= 1e-4 * J64
     assert max(errs) <= GRAD_TOL

@@ -491,18 +491,25 @@ def test_oracle_visco3d_adjoint_matches_fp64_finite_differences(refcpu, L, bound
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
 
 
-def em3_case(refcpu, boundary=2, stencil=0, reduce=1, order=4, NX=24, NY=20, NZ=18, nt=120):
+def em3_case(refcpu, boundary=2, stencil=0, reduce=1, order=4, NX=24, NY=20, NZ=18, nt=120, L=0):
+    """3-D EM survey; L > 0: 3-D visco-EM with L relaxation mechanisms."""
     rng = np.random.default_rng(43)
     y, z, x = np.mgrid[0:NY, 0:NZ, 0:NX]
     eps = 5.0 + 6.0 * (y > NY // 2) + 0.4 * np.cos(x / 4.0) + 0.3 * np.sin(z / 3.0) + 0.1 * rng.standard_normal((NY, NZ, NX))
     sig = 10 ** (-3.0 + 0.4 * np.sin(y / 5.0))
     mur = 1.0 + 0.05 * (x > NX // 3)
-    model = {k: v.reshape(-1).astype(np.float64) for k, v in dict(eps_r=eps, sigma=sig, mu_r=mur).items()}
+    fields = dict(eps_r=eps, sigma=sig, mu_r=mur)
+    if L:
+        fields["tau_eps"] = 0.15 + 0.05 * np.cos(x / 5.0) + 0.02 * np.sin(z / 4.0)
+        fields["tau_sigma"] = 0.1 + 0.05 * np.sin(y / 4.0)
+    model = {k: v.reshape(-1).astype(np.float64) for k, v in fields.items()}
     DH = 0.02
     DT = 0.3 * DH / (3e8 * np.sqrt(3) * 1.3)
-    cfg = refcpu.make_config(dimension=3, equation="emem", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT, T=(nt - 0.4) * DT,
-                             spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=5, DampingCoeff=8.0, NPower=4.0,
-                             CenterFrequencyCPML=5e8, VMaxCPML=1.5e8, useStencilMatrix=stencil, edgeOrderReduction=reduce)
+    cfg = refcpu.make_config(dimension=3, equation="viscoemem" if L else "emem", NX=NX, NY=NY, NZ=NZ, DH=DH, DT=DT,
+                             T=(nt - 0.4) * DT, spatialFDorder=order, DampingBoundary=boundary, BoundaryWidth=5,
+                             DampingCoeff=8.0, NPower=4.0, CenterFrequencyCPML=5e8, VMaxCPML=1.5e8,
+                             useStencilMatrix=stencil, edgeOrderReduction=reduce, numRelaxationMechanisms=L,
+                             relaxationFrequency=[3e8, 9e8][:L])
     sidx = np.array([refcpu.grid_index(cfg, NX // 2, 5, NZ // 2), refcpu.grid_index(cfg, NX // 3, 8, NZ // 3)], np.int64)
     sig_t = refcpu.ricker(nt, DT, 7e8, 1.0, 0.0, np.float64)
     rx = np.arange(3, NX - 3, 3)
@@ -512,13 +519,14 @@ def em3_case(refcpu, boundary=2, stencil=0, reduce=1, order=4, NX=24, NY=20, NZ=
     return cfg, model, (sidx, np.array([1, 4], np.int32), np.stack([sig_t, 300.0 * sig_t]), ridx, rtype)
 
 
-@pytest.mark.parametrize("boundary,stencil,reduce", [(2, 0, 1), (1, 1, 0), (0, 0, 1)])
-def test_oracle_em3d_adjoint_matches_fp64_finite_differences(refcpu, boundary, stencil, reduce):
+@pytest.mark.parametrize("boundary,stencil,reduce,L", [(2, 0, 1, 0), (1, 1, 0, 0), (0, 0, 1, 0), (2, 0, 1, 1), (1, 0, 0, 2)])
+def test_oracle_em3d_adjoint_matches_fp64_finite_differences(refcpu, boundary, stencil, reduce, L):
     """The oracle's FP64 adjoint of the lossless 3-D EM step (gradients with
     respect to eps_r, sigma, mu_r; Ez and Hz sources, Ez / Ex / Ey / Hz
-    receivers) against central finite differences of its own misfit, with
-    CPML, ABS and no boundary."""
-    cfg, model, acq = em3_case(refcpu, boundary, stencil, reduce)
+    receivers; L > 0: 3-D visco-EM with the taus fixed) against
+    Richardson-extrapolated central finite differences of its own misfit,
+    with CPML, ABS and no boundary."""
+    cfg, model, acq = em3_case(refcpu, boundary, stencil, reduce, L=L)
     true = dict(model)
     y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
     blob = np.exp(-((x - cfg.NX * 0.5) ** 2 + (y - cfg.NY * 0.5) ** 2 + (z - cfg.NZ * 0.5) ** 2) / 18.0).reshape(-1)
@@ -536,11 +544,15 @@ def test_oracle_em3d_adjoint_matches_fp64_finite_differences(refcpu, boundary, s
     grads = dict(eps_r=ge, sigma=gs, mu_r=gm)
     for name in ("eps_r", "sigma", "mu_r"):
         d = smooth3(rng, cfg) * model[name]
-        h = 1e-5
-        mp, mm = dict(model), dict(model)
-        mp[name] = model[name] + h * d
-        mm[name] = model[name] - h * d
-        fd = (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+
+        def central(h):
+            mp, mm = dict(model), dict(model)
+            mp[name] = model[name] + h * d
+            mm[name] = model[name] - h * d
+            return (misfit(refcpu, cfg, mp, acq, dobs) - misfit(refcpu, cfg, mm, acq, dobs)) / (2 * h)
+
+        d1 = central(2e-4)
+        fd = d1 - (central(4e-4) - d1) / 3
         ad = float(np.dot(grads[name], d))
         assert abs(fd) > 0
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)

@@ -579,8 +579,8 @@ class ForwardSolver:
         adjoint: w.r.t. (vp, vs, rho) for 2-D and 3-D elastic and visco-elastic
         (relaxation times held fixed), 2-D and 3-D acoustic (where the vs
         gradient is zero) and 2-D SH and visco-SH (where the vp
-        gradient is zero), (eps_r, sigma, mu_r) for 2-D TMz and TEz and their visco variants and
-        lossless 3-D EM. d_obs: n_receivers x NT (numpy or torch cuda).
+        gradient is zero), (eps_r, sigma, mu_r) for 2-D TMz and TEz and 3-D EM and their visco
+        variants. d_obs: n_receivers x NT (numpy or torch cuda).
         Returns (J, g1, g2, g3) as float64 / numpy arrays."""
         d = _f32(dobs)
         pd, mem = _ptr(d)

@@ -478,8 +478,8 @@ __global__ void adj_ac_final(PrepParams G, const StepParams P, const AdjShot A, 
 // chain rule for lossless 3-D EM: CaQ, CbQ of the 2-point averages of eps = eps_r
 // eps0 and sigma along axis Q; iMyz, iMxz, iMxy = 1 / (4-point average of mu = mu_r
 // mu0 in the yz, xz, xy plane) (0 where invalid)
-__global__ void adj_em3_final(PrepParams G, const StepParams P, const AdjShot A, float DT, float* geps, float* gsig, float* gmu,
-                              int accumulate)
+__global__ void adj_em3_final(PrepParams G, const StepParams P, const AdjShot A, float DT, ViscoEmCoef vc, float* geps, float* gsig,
+                              float* gmu, int accumulate)
 {
     const float eps0 = 8.8541878176e-12f, mu0 = 1.2566370614e-6f;
     const float* er = P.m[M_EPSR];
@@ -500,12 +500,32 @@ __global__ void adj_em3_final(PrepParams G, const StepParams P, const AdjShot A,
                 const bool pair = kc[q] - d + 1 < Nc[q];
                 if (d == 1 && !pair) continue;
                 const float w = pair ? 0.5f : 1.0f;
-                const float e = pair ? 0.5f * (er[r] * eps0) + 0.5f * (er[r + st[q]] * eps0) : er[r] * eps0;
-                const float s = pair ? 0.5f * sg[r] + 0.5f * sg[r + st[q]] : sg[r];
+                const float e0 = pair ? 0.5f * (er[r] * eps0) + 0.5f * (er[r + st[q]] * eps0) : er[r] * eps0;
+                const float s0 = pair ? 0.5f * sg[r] + 0.5f * sg[r + st[q]] : sg[r];
+                // visco: the optical permittivity / conductivity of the averaged eps, sigma, tau_eps,
+                // tau_sigma and Cd_l = -DT te cdScale_l e (prep_visco_em), the taus held fixed
+                float e = e0, s = s0, de_de = 1.0f, de_ds = 0.0f, ds_de = 0.0f, tq = 0.0f;
+                if (A.visco) {
+                    const float* te = P.m[M_TAUP];
+                    const float* ts = P.m[M_TAUS];
+                    tq = pair ? 0.5f * te[r] + 0.5f * te[r + st[q]] : te[r];
+                    const float sq = pair ? 0.5f * ts[r] + 0.5f * ts[r + st[q]] : ts[r];
+                    const float eo = (1.0f - tq) * e0 + s0 * sq;
+                    const bool clamp = eo < eps0;
+                    e = clamp ? eps0 : eo;
+                    de_de = clamp ? 0.0f : 1.0f - tq;
+                    de_ds = clamp ? 0.0f : sq;
+                    s = tq * vc.sumInv * e0 + s0;
+                    ds_de = tq * vc.sumInv;
+                }
                 float a, b;
                 cacb_adj(e, s, DT, A.g[2 * q][r], A.g[2 * q + 1][r], a, b);
-                ge += w * a;
-                gs += w * b;
+                float ga = a * de_de + b * ds_de;
+                const float gb = a * de_ds + b;
+                if (A.visco)
+                    for (int m = 0; m < vc.L; ++m) ga += A.g[9 + q * vc.L + m][r] * (-DT) * tq * vc.cdScale[m];
+                ge += w * ga;
+                gs += w * gb;
             }
         // plane rows that read point k: yz (iMyz, g[6]), xz (iMxz, g[7]), xy (iMxy, g[8])
         float gm = 0.0f;
@@ -653,7 +673,8 @@ std::string adjoint_supported(const wave_handle* h)
                                           c.equation == WAVE_EQ_EMEM || c.equation == WAVE_EQ_VISCOELASTIC ||
                                           c.equation == WAVE_EQ_VISCOSH || c.equation == WAVE_EQ_VISCOTMEM ||
                                           c.equation == WAVE_EQ_VISCOEMEM);
-    const bool ok3 = c.dimension == 3 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_VISCOELASTIC || c.equation == WAVE_EQ_EMEM);
+    const bool ok3 = c.dimension == 3 && (c.equation == WAVE_EQ_ELASTIC || c.equation == WAVE_EQ_VISCOELASTIC || c.equation == WAVE_EQ_EMEM ||
+                                          c.equation == WAVE_EQ_VISCOEMEM);
     const bool okAc = c.equation == WAVE_EQ_ACOUSTIC;
     if (!ok2 && !ok3 && !okAc)
         return "the adjoint gradient is implemented for 2-D and 3-D acoustic, elastic and visco-elastic, 2-D SH and visco-SH, "
@@ -705,14 +726,14 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const bool tm = h->cfg.equation == WAVE_EQ_TMEM || h->cfg.equation == WAVE_EQ_VISCOTMEM;
         const bool sh = h->cfg.equation == WAVE_EQ_SH || h->cfg.equation == WAVE_EQ_VISCOSH;
         const bool ac = h->cfg.equation == WAVE_EQ_ACOUSTIC;
-        const bool em3 = h->sp.is3d && h->cfg.equation == WAVE_EQ_EMEM;
+        const bool em3 = h->sp.is3d && (h->cfg.equation == WAVE_EQ_EMEM || h->cfg.equation == WAVE_EQ_VISCOEMEM);
         const bool e3 = h->sp.is3d && !ac && !em3;
         long long off[kAdjMaxParts], len[kAdjMaxParts], o = 0;
         const int elasticFields[5] = {F_VX, F_VY, F_SXX, F_SYY, F_SXY};
         const int tmFields[5] = {F_HX, F_HY, F_EZ, -1, -1};
         const int tmPsi[8] = {PS_EZY, PS_EZX, PS_HYX, PS_HXY, -1, -1, -1, -1};
         // TEz: hz, -, ex, ey and the psi of eyx, exy, -, -, hzy, hzx
-        const bool te = h->cfg.equation == WAVE_EQ_EMEM || h->cfg.equation == WAVE_EQ_VISCOEMEM;
+        const bool te = !h->sp.is3d && (h->cfg.equation == WAVE_EQ_EMEM || h->cfg.equation == WAVE_EQ_VISCOEMEM);
         const int shFields[5] = {F_VZ, -1, F_SXZ, F_SYZ, -1};
         const int shPsi[8] = {PS_SXZ_X, PS_SYZ_Y, -1, -1, PS_VZX, PS_VZY, -1, -1};
         const int teFields[5] = {F_HZ, -1, F_EX, F_EY, -1};
@@ -732,7 +753,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         // visco-elastic: the elastic parts, then rxx, ryy, rxy of each mechanism
         const bool visco = h->cfg.equation == WAVE_EQ_VISCOELASTIC || h->cfg.equation == WAVE_EQ_VISCOSH ||
                            h->cfg.equation == WAVE_EQ_VISCOTMEM || h->cfg.equation == WAVE_EQ_VISCOEMEM;
-        const int ncomp = e3 ? 6 : (sh || te) ? 2 : tm ? 1 : 3;   // memory-variable components per mechanism
+        const int ncomp = e3 ? 6 : (sh || te) ? 2 : tm ? 1 : 3;   // memory-variable components per mechanism (3-D EM: 3)
         const int nr = visco ? ncomp * h->L : 0;
         const int nf = em3 ? 6 : ac ? 4 : e3 ? 9 : 5, np = em3 ? 12 : ac ? 6 : e3 ? 18 : 8, nparts = nf + np + nr;
         for (int k = 0; k < nf; ++k) { off[k] = o; len[k] = fields[k] >= 0 ? N : 0; o += len[k]; }
@@ -747,7 +768,8 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         const int memVarSH[2] = {R_XZ, R_YZ};
         const int memVarTM[1] = {R_EZ};
         const int memVarTE[2] = {R_EX, R_EY};
-        const int* memVar = e3 ? memVar3 : sh ? memVarSH : tm ? memVarTM : te ? memVarTE : memVar2;
+        const int memVarEM3[3] = {R_EX, R_EY, R_EZ};
+        const int* memVar = e3 ? memVar3 : sh ? memVarSH : tm ? memVarTM : te ? memVarTE : em3 ? memVarEM3 : memVar2;
         auto rpart = [&](int j) { return h->r[memVar[j / h->L]][j % h->L]; };
         for (int j = 0; j < nr; ++j) { off[nf + np + j] = o; len[nf + np + j] = N; o += N; }
         stride[s] = o;
@@ -770,7 +792,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         for (int j = 0; j < nr; ++j) a.lr[(j / h->L) * kMaxL + j % h->L] = lstate + off[nf + np + j];
         // acoustic: 6 and 4 of them; visco-TMz: dJ/dCd_l in g[4 + l]
         const int ntemp = e3 ? 18 : em3 ? 12 : 8;
-        const int ngrad = e3 ? 8 : em3 ? 9 : (tm && visco) ? 4 + h->L : (te && visco) ? 5 + 2 * h->L : 5;
+        const int ngrad = e3 ? 8 : em3 ? 9 + (visco ? 3 * h->L : 0) : (tm && visco) ? 4 + h->L : (te && visco) ? 5 + 2 * h->L : 5;
         float* temps = pool.get<float>(static_cast<size_t>(ntemp) * N);
         for (int k = 0; k < ntemp; ++k) a.T[k] = temps + k * N;
         float* grads = pool.get<float>(static_cast<size_t>(ngrad) * N);
@@ -885,7 +907,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         PrepParams G{h->NX, h->NY, h->NZ, h->N};
         const int o = sum ? 0 : s;
         if (A[s].em3)
-            adj_em3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), gvp[o], gvs[o], grho[o],
+            adj_em3_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], static_cast<float>(h->cfg.DT), h->vemc, gvp[o], gvs[o], grho[o],
                                                 sum && s > 0 ? 1 : 0);
         else if (A[s].ac)
             adj_ac_final<<<1216, 256, 0, st>>>(G, Ps[s], A[s], gvp[o], gvs[o], grho[o], sum && s > 0 ? 1 : 0);

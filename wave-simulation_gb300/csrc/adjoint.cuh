@@ -30,7 +30,7 @@ struct AdjShot {
     float* lf[9];                // adjoint fields (2-D elastic: vx, vy, sxx, syy, sxy)
     float* lpsi[18];             // adjoint psi (slab layout of the forward psi)
     float* T[18];                // adjoints of the raw derivatives (2-D elastic: c1..c4, a1..a4)
-    float* g[13];                // material adjoints (2-D elastic: dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry)
+    float* g[9 + 3 * kMaxL];     // material adjoints (2-D elastic: dJ/dM, dJ/dmu, dJ/dmu_xy, dJ/dirx, dJ/diry)
     const long long* ridx;
     const int* rtype;
     const float* res;            // residual d - d_obs, nrec x nt
@@ -901,11 +901,26 @@ __device__ __forceinline__ void adj_em3_e_body(const StepParams& P, const AdjSho
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         const float ca = __ldg(P.m[M_CAX + 2 * q] + i), cb = __ldg(P.m[M_CBX + 2 * q] + i);
-        A.g[2 * q][i] += le[q] * X0[A.off[3 + q] + i];
-        A.g[2 * q + 1][i] += le[q] * (c[2 * q] - c[2 * q + 1]);
+        const float e0 = X0[A.off[3 + q] + i];
+        float u = c[2 * q] - c[2 * q + 1], ln = ca * le[q];
+        if (A.visco) {
+            // 3-D visco-EM (ForwardSolver3Dviscoemem.cpp:215-300): r_l' = Cc_l r_l + Cd_l e and
+            // e' = Ca e + Cb (c' - c'' - DT sum_l r_l'); r_l' of component q is state part 18 + q L + l,
+            // dJ/dCd in g[9 + q L + l]
+            for (int m = 0; m < P.L; ++m) {
+                u -= P.DT * X1[A.off[18 + q * P.L + m] + i];
+                float* r = A.lr[q * kMaxL + m] + i;
+                const float LR = *r - P.DT * cb * le[q];
+                ln += __ldg(P.m[M_CDX0 + q * kMaxL + m] + i) * LR;
+                A.g[9 + q * P.L + m][i] += LR * e0;
+                *r = P.Cc[m] * LR;
+            }
+        }
+        A.g[2 * q][i] += le[q] * e0;
+        A.g[2 * q + 1][i] += le[q] * u;
         l[2 * q] = cb * le[q];
         l[2 * q + 1] = -cb * le[q];
-        A.lf[3 + q][i] = ca * le[q];
+        A.lf[3 + q][i] = ln;
     }
     // H-derivative psi: full profiles except hyx (CPMLEM3D.cpp:67-70)
     cpml_adj_axis(P, p, S, l[0], A.lpsi[6], 1, false);    // hzy

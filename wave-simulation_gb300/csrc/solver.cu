@@ -959,14 +959,14 @@ int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, co
                 }
                 coeffs(ea, sa, ta, tsa, caS[a], cbS[a], cdS[a]);
             }
-            if (visco && !is3d) {
+            if (visco) {
                 // tau_eps and the scaled tau_sigma with the coefficient constants, for the adjoint's chain rule
                 h->check(cudaMemcpyAsync(mat(M_TAUP), dTe, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
                 h->check(cudaMemcpyAsync(mat(M_TAUS), dTs, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
                 h->vemc = vc;
             }
         }
-        if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_EMEM || ((eq == WAVE_EQ_VISCOTMEM || eq == WAVE_EQ_VISCOEMEM) && !is3d)) {
+        if (eq == WAVE_EQ_TMEM || eq == WAVE_EQ_EMEM || eq == WAVE_EQ_VISCOEMEM || (eq == WAVE_EQ_VISCOTMEM && !is3d)) {
             // the base parameters, for the adjoint's chain rule (adjoint.cu)
             h->check(cudaMemcpyAsync(mat(M_EPSR), dEr, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
             h->check(cudaMemcpyAsync(mat(M_SIG), dSig, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
