@@ -425,9 +425,9 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *    grad_vp, grad_vs, grad_rho receive dJ/dvp, dJ/dvs, dJ/drho;
  *  - 2-D and 3-D visco-elastic (FD2Dviscoelastic::run, ForwardSolver2D
  *    viscoelastic.cpp:130-321; FD3Dviscoelastic::run, ForwardSolver3D
- *    viscoelastic.cpp:132-457) with CPML, ABS or no damping boundary, no free
- *    surface: the same three outputs, the relaxation times (tau_p, tau_s)
- *    held fixed;
+ *    viscoelastic.cpp:132-457) with CPML, ABS or no damping boundary and with
+ *    or without the free surface (FreeSurface 1): the same three outputs, the
+ *    relaxation times (tau_p, tau_s) held fixed;
  *  - 2-D SH and visco-SH (FD2Dsh::run, ForwardSolver2Dsh.cpp:108-196;
  *    FD2Dviscosh::run, ForwardSolver2Dviscosh.cpp:126-244, tau_s fixed) with
  *    CPML, ABS or no damping boundary and with or without the free surface:

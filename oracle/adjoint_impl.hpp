@@ -115,7 +115,6 @@ struct ElasticAdjoint2D {
     {
         if (s.is3d || (s.eq != WAVE_EQ_ELASTIC && s.eq != WAVE_EQ_VISCOELASTIC))
             throw std::invalid_argument("oracle adjoint: 2-D elastic or visco-elastic only");
-        if (visco && s.fs) throw std::invalid_argument("oracle adjoint: the visco-elastic free surface is not differentiated");
         DxfT = transpose(s.Dxf);
         DxbT = transpose(s.Dxb);
         DyfT = transpose(s.Dyf);
@@ -162,6 +161,40 @@ struct ElasticAdjoint2D {
             lp[i] = b[i] * (lc[i] + lp[i]);
             lc[i] = c;
         });
+    }
+
+    // transpose of the visco free-surface exchange at one surface point for one
+    // horizontal normal stress S with the adjoint lS of its final value and LR[l]
+    // the adjoints of its memory variables after the regular update (lR + DT/2 lS):
+    // adds to the adjoints of the horizontal strain sum (h) and of vyy (v) and to
+    // dJ/dM, dJ/dmu
+    static void fsExchangeT(const Sim<T>& s, idx_t i, T lS, const T* LR, T h, T v, T& lh, T& lv, T& gM, T& gMu)
+    {
+        const T M = s.M[i], mu = s.mu[i], tP = s.tauP[i], tS = s.tauS[i], opP = s.onePlusLtauP[i], opS = s.onePlusLtauS[i];
+        const T mp = M * opP, sV = mp - T(2) * mu * opS, sH = -sV * sV / mp;
+        const T t3 = T(2) * mu * tS - M * tP, ratio = T(2) * mu * opS / mp - T(1);
+        T lhh = sH * lS, lvv = -sV * lS;
+        // dJ/dsH = lS h, dJ/dsV = -lS v; dJ/drh_l = LR_l h, dJ/drv_l = -LR_l v
+        const T gsH = lS * h, gsV = -lS * v;
+        T grh = 0, grv = 0;   // summed over l with the factor c2_l / tau_l
+        for (int l = 0; l < s.L; ++l) {
+            const T kk = s.viscoC2[l] / s.relaxTime[l];
+            lhh += t3 * ratio * kk * LR[l];
+            lvv -= t3 * kk * LR[l];
+            grh += LR[l] * h * kk;
+            grv += -LR[l] * v * kk;
+        }
+        lh += lhh;
+        lv += lvv;
+        // sV = M opP - 2 mu opS; sH = -sV^2 / (M opP)
+        const T dsH_dsV = -T(2) * sV / mp, dsH_dM = sV * sV / (mp * mp) * opP;
+        gM += gsV * opP + gsH * (dsH_dsV * opP + dsH_dM);
+        gMu += gsV * (-T(2) * opS) + gsH * dsH_dsV * (-T(2) * opS);
+        // rv = t3 k, rh = t3 ratio k: dt3/dM = -tauP, dt3/dmu = 2 tauS; dratio/dM = -2 mu opS / (M^2 opP),
+        // dratio/dmu = 2 opS / (M opP)
+        const T dr_dM = -T(2) * mu * opS / (M * mp), dr_dmu = T(2) * opS / mp;
+        gM += grv * (-tP) + grh * (-tP * ratio + t3 * dr_dM);
+        gMu += grv * (T(2) * tS) + grh * (T(2) * tS * ratio + t3 * dr_dmu);
     }
 
     // Returns the misfit; writes the gradients with respect to vp, vs, rho.
@@ -254,7 +287,7 @@ struct ElasticAdjoint2D {
                         for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
                     }
                 for (int k = 0; k < 4; ++k) std::fill(lc[k].begin(), lc[k].end(), T(0));
-                if (s.fs) {
+                if (s.fs && !visco) {
                     // sxx += scaleH c1' - scaleV c2'; syy *= fsZero
                     for_n(N, [&](idx_t i) {
                         lyy[i] *= s.fsZero[i];
@@ -280,6 +313,14 @@ struct ElasticAdjoint2D {
                     for_n(N, [&](idx_t i) {
                         const T e = c[0][i] + c[1][i], M = s.M[i], mu = s.mu[i];
                         const T tP = s.tauP[i], tS = s.tauS[i], opP = s.onePlusLtauP[i], opS = s.onePlusLtauS[i];
+                        // free surface (FreeSurface2Dviscoelastic.cpp): syy and ryy are zeroed on the
+                        // surface row, so their adjoints do not flow back
+                        const bool surf = s.fs && s.fsSelect[i] != T(0);
+                        if (surf) {
+                            lyy[i] = 0;
+                            for (int l = 0; l < s.L; ++l) lR[1][l][i] = 0;
+                        }
+                        T LRx[8] = {0, 0, 0, 0, 0, 0, 0, 0};
                         T le = 0, lq[2] = {0, 0};
                         for (int k = 0; k < 2; ++k) {
                             const T lS = k == 0 ? lxx[i] : lyy[i];
@@ -292,6 +333,7 @@ struct ElasticAdjoint2D {
                             for (int l = 0; l < s.L; ++l) {
                                 const T c1 = s.viscoC1[l], c2 = s.viscoC2[l], irt = s.invRelaxTime[l];
                                 const T LR = lRk[l][i] + DTh * lS;   // adjoint of Rk'
+                                if (k == 0) LRx[l] = LR;
                                 lRk[l][i] = c2 * c1 * LR + DTh * lS;
                                 le -= c2 * irt * tP * M * LR;
                                 lq[k] += c2 * irt * tS * T(2) * mu * LR;
@@ -301,6 +343,13 @@ struct ElasticAdjoint2D {
                         }
                         lc[0][i] += le + lq[1];
                         lc[1][i] += le + lq[0];
+                        if (surf) {
+                            // on the surface row: Sxx' += sH c1' - sV c2' + DT/2 sum_l dR_l,
+                            // Rxx_l' += dR_l = rh_l c1' - rv_l c2' with sV = M opP - 2 mu opS,
+                            // sH = -sV^2 / (M opP), rv_l = t3 c2_l / tau_l, rh_l = t3 ratio c2_l / tau_l,
+                            // t3 = 2 mu tauS - M tauP, ratio = 2 mu opS / (M opP) - 1
+                            fsExchangeT(s, i, lxx[i], LRx, c[0][i], c[1][i], lc[0][i], lc[1][i], gM[i], gMu[i]);
+                        }
                         const T lS = lxy[i], sh = c[2][i] + c[3][i];
                         T lm = opS * lS;
                         for (int l = 0; l < s.L; ++l) {
@@ -1032,7 +1081,6 @@ struct ElasticAdjoint3D {
     {
         if (!s.is3d || (s.eq != WAVE_EQ_ELASTIC && s.eq != WAVE_EQ_VISCOELASTIC))
             throw std::invalid_argument("oracle adjoint: 3-D elastic or visco-elastic only");
-        if (visco && s.fs) throw std::invalid_argument("oracle adjoint: the visco-elastic free surface is not differentiated");
         DxfT = transpose(s.Dxf);
         DxbT = transpose(s.Dxb);
         DyfT = transpose(s.Dyf);
@@ -1182,7 +1230,7 @@ struct ElasticAdjoint3D {
                         for_n(N, [&](idx_t i) { w[i] *= s.damping[i]; });
                     }
                 for (int k = 0; k < 9; ++k) std::fill(lc[k].begin(), lc[k].end(), T(0));
-                if (s.fs) {
+                if (s.fs && !visco) {
                     // syy *= fsZero; sxx, szz += scaleH (c0' + c2') - scaleV c1'
                     for_n(N, [&](idx_t i) {
                         lyy[i] *= s.fsZero[i];
@@ -1211,7 +1259,14 @@ struct ElasticAdjoint3D {
                         const T e = c[0][i] + c[1][i] + c[2][i], M = s.M[i], mu = s.mu[i];
                         const T tP = s.tauP[i], tS = s.tauS[i], opP = s.onePlusLtauP[i], opS = s.onePlusLtauS[i];
                         const T q[3] = {c[1][i] + c[2][i], c[0][i] + c[2][i], c[0][i] + c[1][i]};
+                        // free surface (FreeSurface3Dviscoelastic.cpp): syy and ryy zeroed on the surface row
+                        const bool surf = s.fs && s.fsSelect[i] != T(0);
+                        if (surf) {
+                            lyy[i] = 0;
+                            for (int l = 0; l < s.L; ++l) lR[1][l][i] = 0;
+                        }
                         const T lS3[3] = {lxx[i], lyy[i], lzz[i]};
+                        T LRk[3][8] = {};
                         T le = 0, lq[3] = {0, 0, 0};
                         for (int k = 0; k < 3; ++k) {
                             const T lS = lS3[k];
@@ -1222,6 +1277,7 @@ struct ElasticAdjoint3D {
                             for (int l = 0; l < s.L; ++l) {
                                 const T c1 = s.viscoC1[l], c2 = s.viscoC2[l], irt = s.invRelaxTime[l];
                                 const T LR = lR[k][l][i] + DTh * lS;
+                                LRk[k][l] = LR;
                                 lR[k][l][i] = c2 * c1 * LR + DTh * lS;
                                 le -= c2 * irt * tP * M * LR;
                                 lq[k] += c2 * irt * tS * T(2) * mu * LR;
@@ -1232,6 +1288,15 @@ struct ElasticAdjoint3D {
                         lc[0][i] += le + lq[1] + lq[2];
                         lc[1][i] += le + lq[0] + lq[2];
                         lc[2][i] += le + lq[0] + lq[1];
+                        if (surf) {
+                            // sxx and szz: the exchange with the horizontal sum c0' + c2' and vyy = c1'
+                            T lh = 0, lv = 0;
+                            for (int k = 0; k < 3; k += 2)
+                                ElasticAdjoint2D<T>::fsExchangeT(s, i, lS3[k], LRk[k], c[0][i] + c[2][i], c[1][i], lh, lv, gM[i], gMu[i]);
+                            lc[0][i] += lh;
+                            lc[2][i] += lh;
+                            lc[1][i] += lv;
+                        }
                         const T lSh[3] = {lxy[i], lxz[i], lyz[i]};
                         const T muP[3] = {s.muXY[i], s.muXZ[i], s.muYZ[i]};
                         const T tauPl[3] = {s.tauSXY[i], s.tauSXZ[i], s.tauSYZ[i]};

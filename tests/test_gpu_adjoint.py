@@ -128,8 +128,8 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
 @pytest.mark.parametrize("dim,equation", [(2, "viscoelastic"), (3, "viscoelastic")])
 def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
     """Set-ups without an adjoint are refused with WAVE_ERR_UNSUPPORTED: the visco-elastic free surface
-    (its relaxation exchange is not differentiated), in 2-D and 3-D."""
-    cfg = _config(wave, dim=dim, fs=1 if equation == "viscoelastic" else 0)
+    without the mirror (FreeSurface = 2), in 2-D and 3-D."""
+    cfg = _config(wave, dim=dim, fs=2)
     cfg.equation = wave.EQUATIONS[equation]
     cfg.numRelaxationMechanisms = 1
     cfg.relaxationFrequency[0] = 20.0

@@ -117,12 +117,15 @@ def test_elastic3d_checkpoint_interval_and_batch(wave, refcpu):
             assert np.abs(want).max() > 0 and np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("L,boundary,stencil,reduce,order", [(1, 2, 0, 0, 4), (2, 1, 0, 1, 6), (2, 0, 1, 0, 2)])
-def test_visco3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, L, boundary, stencil, reduce, order):
+@pytest.mark.parametrize("L,boundary,stencil,reduce,order,fs", [(1, 2, 0, 0, 4, 0), (2, 1, 0, 1, 6, 0), (2, 0, 1, 0, 2, 0),
+                                                                (2, 2, 0, 0, 4, 1), (1, 1, 0, 1, 8, 1)])
+def test_visco3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, L, boundary, stencil, reduce, order, fs):
     """3-D visco-elastic (FD3Dviscoelastic::run, ForwardSolver3Dviscoelastic.cpp:132-457): six memory
     variables per mechanism, vp / vs / rho gradients with the relaxation times fixed, against the
-    oracle's FP64 adjoint (pinned to FP64 finite differences); the free surface is refused."""
-    ocfg, model, acq = el3_case(refcpu, 0, boundary, stencil, reduce, order=order, NX=40, NY=32, NZ=36, nt=260, L=L)
+    oracle's FP64 adjoint (pinned to FP64 finite differences), with and without the mirror free
+    surface (FreeSurface3Dviscoelastic.cpp: sxx, szz and their memory variables exchange with the
+    horizontal strain sum and vyy)."""
+    ocfg, model, acq = el3_case(refcpu, fs, boundary, stencil, reduce, order=order, NX=40, NY=32, NZ=36, nt=260, L=L)
     cfg = _wave_cfg(wave, ocfg)
     m32 = {k: v.astype(np.float32) for k, v in model.items()}
     y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
@@ -151,13 +154,7 @@ def test_visco3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, L, bound
     J64, rvp, rvs, rrho = o.adjoint_gradient(dobs.astype(np.float64), checkpoint_every=45)
     o.close()
     errs = [_rel(gvp, rvp), _rel(gvs, rvs), _rel(grho, rrho)]
-    print(f"3-D visco adjoint L={L} boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} "
+    print(f"3-D visco adjoint L={L} fs={fs} boundary={boundary} stencil={stencil} reduce={reduce} order={order}: misfit {J:.6e} "
           f"vs FP64 {J64:.6e}; gradient rel L2 vp {errs[0]:.2e} vs {errs[1]:.2e} rho {errs[2]:.2e}")
     assert J > 0 and abs(J - J64) <= 1e-4 * J64
     assert max(errs) <= GRAD_TOL
-    cfg.FreeSurface = 1
-    s = solver(m32)
-    with pytest.raises(wave.WaveError) as e:
-        s.adjoint_gradient(dobs)
-    assert e.value.code == wave.WAVE_ERR_UNSUPPORTED
-    s.close()

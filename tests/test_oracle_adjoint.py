@@ -369,13 +369,15 @@ def test_oracle_elastic3d_adjoint_matches_fp64_finite_differences(refcpu, fs, bo
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
 
 
-@pytest.mark.parametrize("L,boundary,stencil,reduce", [(1, 2, 0, 1), (2, 0, 1, 0), (2, 1, 0, 1)])
-def test_oracle_visco_adjoint_matches_fp64_finite_differences(refcpu, L, boundary, stencil, reduce):
+@pytest.mark.parametrize("L,boundary,stencil,reduce,fs", [(1, 2, 0, 1, 0), (2, 0, 1, 0, 0), (2, 1, 0, 1, 0), (1, 2, 0, 1, 1),
+                                                           (2, 1, 1, 0, 1)])
+def test_oracle_visco_adjoint_matches_fp64_finite_differences(refcpu, L, boundary, stencil, reduce, fs):
     """The oracle's FP64 adjoint of the 2-D visco-elastic step (memory
     variables of one or two relaxation mechanisms; gradients with respect to
     vp, vs, rho with the relaxation times held fixed) against central finite
-    differences of its own misfit, with CPML, no boundary and ABS."""
-    cfg, model, acq = case(refcpu, 0, boundary, stencil, reduce, L=L)
+    differences of its own misfit, with CPML, no boundary, ABS and the free
+    surface (its visco exchange, FreeSurface2Dviscoelastic.cpp)."""
+    cfg, model, acq = case(refcpu, fs, boundary, stencil, reduce, L=L)
     true = dict(model)
     yy, xx = np.mgrid[0:cfg.NY, 0:cfg.NX]
     blob = np.exp(-((xx - cfg.NX * 0.4) ** 2 + (yy - cfg.NY * 0.6) ** 2) / 40.0).reshape(-1)
@@ -459,12 +461,14 @@ def test_oracle_acoustic_adjoint_matches_fp64_finite_differences(refcpu, dim, fs
         assert abs(ad - fd) <= 1e-6 * abs(fd), (name, ad, fd)
 
 
-@pytest.mark.parametrize("L,boundary,stencil,reduce", [(1, 2, 0, 1), (2, 1, 1, 0), (2, 0, 0, 1)])
-def test_oracle_visco3d_adjoint_matches_fp64_finite_differences(refcpu, L, boundary, stencil, reduce):
+@pytest.mark.parametrize("L,boundary,stencil,reduce,fs", [(1, 2, 0, 1, 0), (2, 1, 1, 0, 0), (2, 0, 0, 1, 0), (1, 2, 0, 1, 1),
+                                                           (2, 0, 1, 0, 1)])
+def test_oracle_visco3d_adjoint_matches_fp64_finite_differences(refcpu, L, boundary, stencil, reduce, fs):
     """The oracle's FP64 adjoint of the 3-D visco-elastic step (six memory
     variables per mechanism; vp, vs, rho with the relaxation times fixed)
-    against central finite differences of its own misfit."""
-    cfg, model, acq = el3_case(refcpu, 0, boundary, stencil, reduce, L=L)
+    against central finite differences of its own misfit, with and without
+    the free surface (its visco exchange, FreeSurface3Dviscoelastic.cpp)."""
+    cfg, model, acq = el3_case(refcpu, fs, boundary, stencil, reduce, L=L)
     true = dict(model)
     y, z, x = np.mgrid[0:cfg.NY, 0:cfg.NZ, 0:cfg.NX]
     blob = np.exp(-((x - cfg.NX * 0.5) ** 2 + (y - cfg.NY * 0.55) ** 2 + (z - cfg.NZ * 0.5) ** 2) / 18.0).reshape(-1)

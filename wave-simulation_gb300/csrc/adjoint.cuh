@@ -122,6 +122,40 @@ __device__ __forceinline__ Slabs slabs_of(const StepParams& P, const Pt& p)
     return S;
 }
 
+// transpose of the visco free-surface exchange at a surface point
+// (FreeSurface2Dviscoelastic.cpp / FreeSurface3Dviscoelastic.cpp) for one
+// horizontal normal stress: S' += sH h - sV v + DT/2 sum_l dR_l, R_l' += dR_l =
+// rh_l h - rv_l v, with h the horizontal strain sum, v = vyy, sV = M opP -
+// 2 mu opS, sH = -sV^2 / (M opP), rv_l = t3 c2_l / tau_l, rh_l = t3 ratio c2_l /
+// tau_l, t3 = 2 mu tauS - M tauP, ratio = 2 mu opS / (M opP) - 1. lS is the
+// adjoint of S's final value, LR[l] that of R_l after the regular update
+// (its final adjoint plus DT/2 lS); adds to the adjoints of h and v and to
+// dJ/dM, dJ/dmu
+__device__ __forceinline__ void visco_fs_transpose(const StepParams& P, float M, float mu, float tP, float tS, float opP, float opS,
+                                                   float lS, const float* LR, float h, float v, float& lh, float& lv, float& gM,
+                                                   float& gMu)
+{
+    const float mp = M * opP, sV = mp - 2.0f * mu * opS, sH = -sV * sV / mp;
+    const float t3 = 2.0f * mu * tS - M * tP, ratio = 2.0f * mu * opS / mp - 1.0f;
+    float lhh = sH * lS, lvv = -sV * lS, grh = 0.0f, grv = 0.0f;
+    for (int l = 0; l < P.L; ++l) {
+        const float kk = P.c2[l] / P.relaxTime[l];
+        lhh += t3 * ratio * kk * LR[l];
+        lvv -= t3 * kk * LR[l];
+        grh += LR[l] * h * kk;
+        grv -= LR[l] * v * kk;
+    }
+    lh += lhh;
+    lv += lvv;
+    const float gsH = lS * h, gsV = -lS * v;
+    const float dsH_dsV = -2.0f * sV / mp, dsH_dM = sV * sV / (mp * mp) * opP;
+    gM += gsV * opP + gsH * (dsH_dsV * opP + dsH_dM);
+    gMu += gsV * (-2.0f * opS) + gsH * dsH_dsV * (-2.0f * opS);
+    const float dr_dM = -2.0f * mu * opS / (M * mp), dr_dmu = 2.0f * opS / mp;
+    gM += grv * (-tP) + grh * (-tP * ratio + t3 * dr_dM);
+    gMu += grv * (2.0f * tS) + grh * (2.0f * tS * ratio + t3 * dr_dmu);
+}
+
 // stress-pass transpose at step n (state n = view vn, state n+1 = view vn+1)
 template <int H>
 __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjShot& A, const Pt& p, int vn, bool pending)
@@ -177,6 +211,9 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
         const float tP = __ldg(P.m[M_TAUP] + i), tS = __ldg(P.m[M_TAUS] + i);
         const float opP = __ldg(P.m[M_OPLTP] + i), opS = __ldg(P.m[M_OPLTS] + i), tSxy = __ldg(P.m[M_TAUSXY] + i);
         float le = 0.0f, lq[2] = {0.0f, 0.0f}, gM = 0.0f, gMu = 0.0f;
+        float LRx[kMaxL];
+        if (fsRow)   // syy and ryy are zeroed on the surface row: their adjoints do not flow back
+            for (int l = 0; l < P.L; ++l) A.lr[kMaxL + l][i] = 0.0f;
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const float lS = k == 0 ? lxx : lyy, q = k == 0 ? c2 : c1;
@@ -188,6 +225,7 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
                 const float cc = P.c2[l] * P.invRelax[l];
                 float* r = A.lr[k * kMaxL + l] + i;
                 const float LR = *r + DTh * lS;   // adjoint of Rk'
+                if (k == 0) LRx[l] = LR;
                 *r = P.c2[l] * P.c1[l] * LR + DTh * lS;
                 le -= cc * tP * M * LR;
                 lq[k] += cc * tS * 2.0f * mu * LR;
@@ -197,6 +235,7 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
         }
         l1 = le + lq[1];
         l2 = le + lq[0];
+        if (fsRow) visco_fs_transpose(P, M, mu, tP, tS, opP, opS, lxx, LRx, c1, c2, l1, l2, gM, gMu);
         float lm = opS * lxy;
         for (int l = 0; l < P.L; ++l) {
             float* r = A.lr[2 * kMaxL + l] + i;
@@ -209,7 +248,7 @@ __device__ __forceinline__ void adj_stress_body(const StepParams& P, const AdjSh
         A.g[1][i] += gMu;
         A.g[2][i] += lm * (c3 + c4);
     }
-    if (fsRow) {
+    if (fsRow && !A.visco) {
         // sxx' += sh c1' - sv c2' with sv = M - 2 mu, sh = -sv^2 / M
         const float sv = lam, sh = -(sv * sv) / M;
         l1 += sh * lxx;
@@ -653,6 +692,9 @@ __device__ __forceinline__ void adj_e3_s_body(const StepParams& P, const AdjShot
         const float q[3] = {c[1] + c[2], c[0] + c[2], c[0] + c[1]};
         const float lS3[3] = {lxx, lyy, lzz};
         float le = 0.0f, lq[3] = {0.0f, 0.0f, 0.0f}, gM = 0.0f, gMu = 0.0f;
+        float LRh[2][kMaxL];   // sxx's and szz's memory adjoints, for the free-surface exchange
+        if (fsRow)   // syy and ryy are zeroed on the surface row: their adjoints do not flow back
+            for (int m = 0; m < P.L; ++m) A.lr[kMaxL + m][i] = 0.0f;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const float lS = lS3[k];
@@ -664,6 +706,7 @@ __device__ __forceinline__ void adj_e3_s_body(const StepParams& P, const AdjShot
                 const float cc = P.c2[m] * P.invRelax[m];
                 float* r = A.lr[k * kMaxL + m] + i;
                 const float LR = *r + DTh * lS;   // adjoint of Rk'
+                if (k != 1) LRh[k / 2][m] = LR;
                 *r = P.c2[m] * P.c1[m] * LR + DTh * lS;
                 le -= cc * tP * M * LR;
                 lq[k] += cc * tS * 2.0f * mu * LR;
@@ -674,6 +717,15 @@ __device__ __forceinline__ void adj_e3_s_body(const StepParams& P, const AdjShot
         l[0] = le + lq[1] + lq[2];
         l[1] = le + lq[0] + lq[2];
         l[2] = le + lq[0] + lq[1];
+        if (fsRow) {
+            // sxx and szz exchange with the horizontal sum c0' + c2' and vyy = c1'
+            float lh = 0.0f, lv = 0.0f;
+            visco_fs_transpose(P, M, mu, tP, tS, opP, opS, lxx, LRh[0], c[0] + c[2], c[1], lh, lv, gM, gMu);
+            visco_fs_transpose(P, M, mu, tP, tS, opP, opS, lzz, LRh[1], c[0] + c[2], c[1], lh, lv, gM, gMu);
+            l[0] += lh;
+            l[2] += lh;
+            l[1] += lv;
+        }
         const float lSh[3] = {lxy, lxz, lyz};
         const float tPl[3] = {__ldg(P.m[M_TAUSXY] + i), __ldg(P.m[M_TAUSXZ] + i), __ldg(P.m[M_TAUSYZ] + i)};
 #pragma unroll
@@ -704,7 +756,7 @@ __device__ __forceinline__ void adj_e3_s_body(const StepParams& P, const AdjShot
         A.g[3][i] += lxz * (c[5] + c[6]);
         A.g[4][i] += lyz * (c[7] + c[8]);
     }
-    if (fsRow) {
+    if (fsRow && !A.visco) {
         // sxx', szz' += sh (c0' + c2') - sv c1' with sv = M - 2 mu, sh = -sv^2 / M
         const float sv = M - 2.0f * mu, sh = -(sv * sv) / M, hs = lxx + lzz;
         l[0] += sh * hs;
