@@ -417,16 +417,16 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *  - 2-D and 3-D acoustic (FD2Dacoustic::run, ForwardSolver2Dacoustic.cpp:
  *    91-194; FD3Dacoustic::run, ForwardSolver3Dacoustic.cpp:91-233) with CPML,
  *    ABS or no damping boundary and with or without the free surface
- *    (FreeSurface 1): grad_vp and grad_rho receive dJ/dvp, dJ/drho, grad_vs
+ *    (FreeSurface 1 or 2): grad_vp and grad_rho receive dJ/dvp, dJ/drho, grad_vs
  *    is set to zero;
  *  - 2-D and 3-D elastic (FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297;
  *    FD3Delastic::run, ForwardSolver3Delastic.cpp:120-414) with CPML, ABS or
- *    no damping boundary and with or without the free surface (FreeSurface 1):
+ *    no damping boundary and with or without the free surface (FreeSurface 1 or 2):
  *    grad_vp, grad_vs, grad_rho receive dJ/dvp, dJ/dvs, dJ/drho;
  *  - 2-D and 3-D visco-elastic (FD2Dviscoelastic::run, ForwardSolver2D
  *    viscoelastic.cpp:130-321; FD3Dviscoelastic::run, ForwardSolver3D
  *    viscoelastic.cpp:132-457) with CPML, ABS or no damping boundary and with
- *    or without the free surface (FreeSurface 1): the same three outputs, the
+ *    or without the free surface (FreeSurface 1 or 2): the same three outputs, the
  *    relaxation times (tau_p, tau_s) held fixed;
  *  - 2-D SH and visco-SH (FD2Dsh::run, ForwardSolver2Dsh.cpp:108-196;
  *    FD2Dviscosh::run, ForwardSolver2Dviscosh.cpp:126-244, tau_s fixed) with
@@ -445,7 +445,8 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *  - 3-D EM and visco-EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237;
  *    FD3Dviscoemem::run, ForwardSolver3Dviscoemem.cpp:161-309, taus fixed)
  *    with CPML, ABS or no damping boundary: the same three outputs;
- * other equations return WAVE_ERR_UNSUPPORTED. Runs the
+ * a variable grid (useVariableGrid / useVariableFDoperators) returns
+ * WAVE_ERR_UNSUPPORTED. Runs the
  * forward over all NT steps from a zero state (the handle's sources and
  * receivers; seismograms are left as computed), saving the state every
  * `checkpoint_every` steps, then the backward sweep, recomputing each

@@ -125,27 +125,27 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
             assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("dim,equation", [(2, "viscoelastic"), (3, "viscoelastic")])
-def test_adjoint_rejects_unsupported_setups(wave, dim, equation):
-    """Set-ups without an adjoint are refused with WAVE_ERR_UNSUPPORTED: the visco-elastic free surface
-    without the mirror (FreeSurface = 2), in 2-D and 3-D."""
-    cfg = _config(wave, dim=dim, fs=2)
-    cfg.equation = wave.EQUATIONS[equation]
-    cfg.numRelaxationMechanisms = 1
-    cfg.relaxationFrequency[0] = 20.0
-    true, start = _models()
-    n = cfg.N
-    if equation == "viscoemem":
-        model = dict(eps_r=np.full(n, 6.0, np.float32), sigma=np.full(n, 1e-3, np.float32), mu_r=np.ones(n, np.float32),
-                     tau_eps=np.full(n, 0.1, np.float32), tau_sigma=np.full(n, 0.1, np.float32))
-    else:
-        model = {k: np.resize(v, n).astype(np.float32) for k, v in start.items()}
-        model["taup"] = np.full(n, 0.03, np.float32)
-        model["taus"] = np.full(n, 0.03, np.float32)
-    s = wave.Factory.Create("3D" if dim == 3 else "2D", equation).initForwardSolver(cfg)
-    s.prepareForModelling(model)
-    s.setSources(np.array([5], np.int64), np.array([1], np.int32), np.zeros((1, s.nt), np.float32))
-    s.setReceivers(np.array([7], np.int64), np.array([2], np.int32))
+def test_adjoint_rejects_the_variable_grid(wave, refcpu):
+    """The adjoint is built on regular grids: a variable grid (Coordinates.cpp:35-95) is refused
+    with WAVE_ERR_UNSUPPORTED before any step runs."""
+    import ctypes
+
+    from oracle import vargrid
+    grid = [(0, 1, 4), (31, 3, 6), (70, 1, 4)]
+    nx, ny, dh, vmax = 122, 100, 5.0, 3200.0
+    dt = 0.3 * dh / (vmax * np.sqrt(2) * 1.3)
+    ocfg = refcpu.make_config(dimension=2, equation="acoustic", NX=nx, NY=ny, NZ=1, DH=dh, DT=dt, T=40 * dt,
+                              spatialFDorder=4, FreeSurface=1, DampingBoundary=2, BoundaryWidth=12, DampingCoeff=8.0,
+                              NPower=4.0, CenterFrequencyCPML=12.0, VMaxCPML=vmax, edgeOrderReduction=1,
+                              useVariableGrid=1, useVariableFDoperators=1, grid=grid)
+    cfg = wave.WaveConfig()
+    ctypes.memmove(ctypes.byref(cfg), ctypes.byref(ocfg), ctypes.sizeof(cfg))
+    g = vargrid.VarGrid(nx, ny, 1, dh, [r[0] for r in grid], [r[1] for r in grid])
+    s = wave.Factory.Create("2D", "acoustic").initForwardSolver(cfg)
+    s.prepareForModelling(dict(vp=np.full(g.N, 3000.0, np.float32), rho=np.full(g.N, 2000.0, np.float32)))
+    s.setSources(np.asarray(g.coordinate2index([nx // 2], [3], [0]), np.int64), np.array([1], np.int32),
+                 np.zeros((1, s.nt), np.float32))
+    s.setReceivers(np.asarray(g.coordinate2index([20], [5], [0]), np.int64), np.array([1], np.int32))
     with pytest.raises(wave.WaveError) as e:
         s.adjoint_gradient(np.zeros((1, s.nt), np.float32))
     assert e.value.code == wave.WAVE_ERR_UNSUPPORTED
@@ -242,7 +242,8 @@ def _survey(wave, **kw):
 @pytest.mark.parametrize("kw", [dict(order=4, boundary=2), dict(order=2, boundary=0, stencil=1),
                                 dict(order=4, boundary=2, fs=1), dict(order=4, boundary=1),
                                 dict(order=6, boundary=1, fs=1), dict(order=8, boundary=2, fs=1, stencil=1),
-                                dict(order=4, boundary=2, fs=1, reduce=0), dict(order=4, boundary=1, reduce=0)])
+                                dict(order=4, boundary=2, fs=1, reduce=0), dict(order=4, boundary=1, reduce=0),
+                                dict(order=4, boundary=2, fs=2)])
 def test_adjoint_gradient_matches_the_fp64_oracle_gradient(wave, refcpu, kw):
     """P and VY sources (the VY source exercises the re-formed pre-taper
     velocities), P / VX / VY receivers; every free-surface / ABS / CPML

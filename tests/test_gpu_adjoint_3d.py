@@ -61,7 +61,7 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("fs,boundary,stencil,reduce,order", [(0, 2, 0, 0, 4), (1, 2, 0, 0, 8), (0, 1, 1, 0, 2),
-                                                              (1, 0, 0, 1, 6), (1, 1, 0, 0, 4)])
+                                                              (1, 0, 0, 1, 6), (1, 1, 0, 0, 4), (2, 2, 0, 0, 4)])
 def test_elastic3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, fs, boundary, stencil, reduce, order):
     ocfg, cfg, m32, acq, dobs = _survey(wave, refcpu, fs, boundary, stencil, reduce, order)
     s = _solver(wave, cfg, m32, acq)
@@ -118,7 +118,7 @@ def test_elastic3d_checkpoint_interval_and_batch(wave, refcpu):
 
 
 @pytest.mark.parametrize("L,boundary,stencil,reduce,order,fs", [(1, 2, 0, 0, 4, 0), (2, 1, 0, 1, 6, 0), (2, 0, 1, 0, 2, 0),
-                                                                (2, 2, 0, 0, 4, 1), (1, 1, 0, 1, 8, 1)])
+                                                                (2, 2, 0, 0, 4, 1), (1, 1, 0, 1, 8, 1), (1, 2, 0, 0, 4, 2)])
 def test_visco3d_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, L, boundary, stencil, reduce, order, fs):
     """3-D visco-elastic (FD3Dviscoelastic::run, ForwardSolver3Dviscoelastic.cpp:132-457): six memory
     variables per mechanism, vp / vs / rho gradients with the relaxation times fixed, against the

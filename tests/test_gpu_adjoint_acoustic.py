@@ -59,7 +59,8 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("dim,fs,boundary,stencil,reduce,order", [(2, 0, 2, 0, 0, 4), (2, 1, 1, 1, 0, 8), (2, 1, 0, 0, 1, 2),
-                                                                  (3, 0, 2, 0, 0, 4), (3, 1, 1, 0, 1, 6)])
+                                                                  (3, 0, 2, 0, 0, 4), (3, 1, 1, 0, 1, 6), (2, 2, 2, 0, 0, 4),
+                                                                  (3, 2, 1, 0, 1, 4)])
 def test_acoustic_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, dim, fs, boundary, stencil, reduce, order):
     ocfg, cfg, m32, acq, dobs = _survey(wave, refcpu, dim, fs, boundary, stencil, reduce, order)
     s = _solver(wave, cfg, m32, acq)

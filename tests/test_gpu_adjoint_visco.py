@@ -58,7 +58,8 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("L,boundary,stencil,reduce,order,fs", [(1, 2, 0, 0, 4, 0), (2, 0, 1, 0, 2, 0), (2, 1, 0, 1, 6, 0),
-                                                                (1, 2, 1, 0, 8, 0), (2, 2, 0, 0, 4, 1), (1, 1, 1, 1, 6, 1)])
+                                                                (1, 2, 1, 0, 8, 0), (2, 2, 0, 0, 4, 1), (1, 1, 1, 1, 6, 1),
+                                                                (1, 2, 0, 0, 4, 2)])
 def test_visco_adjoint_matches_the_fp64_oracle_gradient(wave, refcpu, L, boundary, stencil, reduce, order, fs):
     """2-D visco-elastic, with and without the mirror free surface (FreeSurface2Dviscoelastic.cpp: the
     relaxation exchange of sxx and rxx with vxx, vyy on the surface row)."""

@@ -51,7 +51,7 @@ def smooth_direction(rng, NY, NX):
 
 
 @pytest.mark.parametrize("fs,boundary,stencil,reduce", [(0, 2, 0, 1), (0, 0, 0, 0), (1, 2, 0, 1), (0, 1, 0, 1),
-                                                        (1, 1, 1, 0)])
+                                                        (1, 1, 1, 0), (2, 2, 0, 1)])
 def test_oracle_adjoint_matches_fp64_finite_differences(refcpu, fs, boundary, stencil, reduce):
     cfg, model, acq = case(refcpu, fs, boundary, stencil, reduce)
     # observed data: the same survey on a perturbed model
@@ -335,7 +335,8 @@ def smooth3(rng, cfg):
     return gaussian_filter(rng.standard_normal((cfg.NY, cfg.NZ, cfg.NX)), 2.5, mode="nearest").reshape(-1)
 
 
-@pytest.mark.parametrize("fs,boundary,stencil,reduce", [(0, 2, 0, 1), (1, 2, 0, 1), (0, 1, 1, 0), (1, 0, 0, 0)])
+@pytest.mark.parametrize("fs,boundary,stencil,reduce", [(0, 2, 0, 1), (1, 2, 0, 1), (0, 1, 1, 0), (1, 0, 0, 0),
+                                                        (2, 2, 0, 1)])
 def test_oracle_elastic3d_adjoint_matches_fp64_finite_differences(refcpu, fs, boundary, stencil, reduce):
     """The oracle's FP64 adjoint of the 3-D elastic step (gradients with
     respect to vp, vs, rho; P and VZ sources, P / VX / VY / VZ receivers)
@@ -370,7 +371,7 @@ def test_oracle_elastic3d_adjoint_matches_fp64_finite_differences(refcpu, fs, bo
 
 
 @pytest.mark.parametrize("L,boundary,stencil,reduce,fs", [(1, 2, 0, 1, 0), (2, 0, 1, 0, 0), (2, 1, 0, 1, 0), (1, 2, 0, 1, 1),
-                                                           (2, 1, 1, 0, 1)])
+                                                           (2, 1, 1, 0, 1), (1, 2, 0, 1, 2)])
 def test_oracle_visco_adjoint_matches_fp64_finite_differences(refcpu, L, boundary, stencil, reduce, fs):
     """The oracle's FP64 adjoint of the 2-D visco-elastic step (memory
     variables of one or two relaxation mechanisms; gradients with respect to
@@ -427,7 +428,8 @@ def ac_case(refcpu, dim=2, fs=0, boundary=2, stencil=0, reduce=1, order=4, NX=44
 
 
 @pytest.mark.parametrize("dim,fs,boundary,stencil,reduce", [(2, 0, 2, 0, 1), (2, 1, 1, 1, 0), (2, 1, 0, 0, 1),
-                                                            (3, 0, 2, 0, 1), (3, 1, 1, 0, 0)])
+                                                            (3, 0, 2, 0, 1), (3, 1, 1, 0, 0), (2, 2, 2, 0, 1),
+                                                            (3, 2, 1, 0, 1)])
 def test_oracle_acoustic_adjoint_matches_fp64_finite_differences(refcpu, dim, fs, boundary, stencil, reduce):
     """The oracle's FP64 adjoint of the 2-D and 3-D acoustic steps (gradients
     with respect to vp and rho; P and VY sources, P / VX / VY receivers)
@@ -462,7 +464,7 @@ def test_oracle_acoustic_adjoint_matches_fp64_finite_differences(refcpu, dim, fs
 
 
 @pytest.mark.parametrize("L,boundary,stencil,reduce,fs", [(1, 2, 0, 1, 0), (2, 1, 1, 0, 0), (2, 0, 0, 1, 0), (1, 2, 0, 1, 1),
-                                                           (2, 0, 1, 0, 1)])
+                                                           (2, 0, 1, 0, 1), (1, 2, 0, 1, 2)])
 def test_oracle_visco3d_adjoint_matches_fp64_finite_differences(refcpu, L, boundary, stencil, reduce, fs):
     """The oracle's FP64 adjoint of the 3-D visco-elastic step (six memory
     variables per mechanism; vp, vs, rho with the relaxation times fixed)

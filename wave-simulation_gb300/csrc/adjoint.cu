@@ -679,10 +679,6 @@ std::string adjoint_supported(const wave_handle* h)
     if (!ok2 && !ok3 && !okAc)
         return "the adjoint gradient is implemented for 2-D and 3-D acoustic, elastic and visco-elastic, 2-D SH and visco-SH, "
                "lossless 2-D TMz and TEz and lossless 3-D EM modelling";
-    if (okAc && c.FreeSurface == 2) return "the acoustic adjoint takes the mirror free surface (FreeSurface = 1) or none";
-    if (c.equation == WAVE_EQ_VISCOELASTIC && c.FreeSurface == 2)
-        return "the visco-elastic adjoint takes the mirror free surface (FreeSurface = 1) or none";
-    if (ok3 && c.FreeSurface == 2) return "the 3-D adjoint takes the mirror free surface (FreeSurface = 1) or none";
     if (c.equation == WAVE_EQ_TMEM || c.equation == WAVE_EQ_VISCOTMEM) {
         for (int t : h->hRecType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez receivers only";
