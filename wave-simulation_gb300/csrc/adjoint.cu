@@ -74,6 +74,7 @@
 #include <cuda_runtime.h>
 
 #include "adjoint.cuh"
+#include "trace.h"
 
 namespace wave {
 
@@ -852,6 +853,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
     for (auto* h : shots) ck(cudaStreamSynchronize(h->stream), "shot sync");
 
     // 1. forward with checkpoints (state zeroed first)
+    TraceRange phase("adjoint.forward");
     for (auto* h : shots) {
         for (int f : h->fields) ck(cudaMemsetAsync(h->f[f], 0, h->N * sizeof(float), st), "memset");
         for (int k = 0; k < PS_COUNT; ++k)
@@ -867,11 +869,13 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         S.step();
     }
     // 2. residuals and misfits
+    phase.next("adjoint.residuals");
     for (int s = 0; s < ns; ++s) {
         const long long n = static_cast<long long>(shots[s]->nrec) * NT;
         residual_kernel<<<256, 256, 0, st>>>(shots[s]->seis, dobs[s], const_cast<float*>(A[s].res), n, dMisfit + s);
     }
     // 3. backward sweep over the checkpoint segments
+    phase.next("adjoint.backward");
     for (int seg = nck - 1; seg >= 0; --seg) {
         const int n0 = seg * K, n1 = n0 + K < NT ? n0 + K : NT;
         copy(dFromCkpt, fromCkpt.size(), seg, 0);
@@ -898,6 +902,7 @@ void adjoint_run(const std::vector<wave_handle*>& shots, const AdjStepper& S, co
         ck(cudaGetLastError(), "adjoint launch");
     }
     // 4. chain rule to vp, vs, rho
+    phase.next("adjoint.chainRule");
     for (int s = 0; s < ns; ++s) {
         wave_handle* h = shots[s];
         PrepParams G{h->NX, h->NY, h->NZ, h->N};
@@ -946,6 +951,7 @@ extern "C" int wave_adjoint_gradient(wave_handle* h, const float* dobs, int dobs
         h->err = "wave_adjoint_gradient: " + why;
         return WAVE_ERR_UNSUPPORTED;
     }
+    wave::TraceRange region("adjoint.gradient");
     try {
         const size_t nd = static_cast<size_t>(h->nrec) * h->NT;
         const size_t N = static_cast<size_t>(h->N);

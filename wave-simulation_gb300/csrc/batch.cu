@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include "handle.h"
+#include "trace.h"
 
 using namespace wave;
 
@@ -313,6 +314,8 @@ int wave_batch_step(wave_batch* b, int t_begin, int t_end)
         if (!b->shots[s]->modelSet) return bfail(b, WAVE_ERR_STATE, "wave_batch_step: shot " + std::to_string(s) + " has no model");
         if (!b->shots[s]->seis) return bfail(b, WAVE_ERR_STATE, "wave_batch_step: shot " + std::to_string(s) + " has no receivers");
     }
+    wave::TraceRange region("WAVE-Simulation.timeLoop");
+    const char* stepName = wave::trace_timestep_name(b->shots[0]->cfg.dimension, b->shots[0]->cfg.equation);
     try {
         // the shots' own streams may still run their model preparation
         for (auto* h : b->shots) ck(cudaStreamSynchronize(h->stream), "shot sync");
@@ -340,11 +343,15 @@ int wave_batch_step(wave_batch* b, int t_begin, int t_end)
                 cudaGraphDestroy(g);
             }
             for (; t + kBatchGraphSteps <= t_end; t += kBatchGraphSteps) {
+                wave::TraceRange steps(stepName);   // kBatchGraphSteps steps of every shot
                 ck(cudaGraphLaunch(b->graph, b->stream), "graph launch");
                 b->launches += (b->abs ? 4 : 3) * kBatchGraphSteps;
             }
         }
-        for (; t < t_end; ++t) launch_batch_step(b);
+        for (; t < t_end; ++t) {
+            wave::TraceRange step(stepName);
+            launch_batch_step(b);
+        }
         ck(cudaGetLastError(), "batch step");
         // the shots' seismogram reads synchronise their own streams: order them after this batch
         ck(cudaStreamSynchronize(b->stream), "batch step");
@@ -376,6 +383,7 @@ int wave_batch_adjoint_gradient(wave_batch* b, const float* const* dobs, int dob
         return static_cast<float*>(p);
     };
     int rc = WAVE_OK;
+    wave::TraceRange region("adjoint.gradient");
     try {
         for (auto* h : b->shots) ck(cudaStreamSynchronize(h->stream), "shot sync");
         if (b->dirty) {

@@ -45,6 +45,7 @@ int psi_axis(int s)
 } // namespace
 
 #include "handle.h"
+#include "trace.h"
 
 namespace {
 
@@ -598,6 +599,7 @@ int wave_solver_create(const wave_config* cfg, wave_handle** out)
     if (!cfg || !out) return fail(nullptr, WAVE_ERR_ARG, "wave_solver_create: null argument");
     *out = nullptr;
     const wave_config& c = *cfg;
+    wave::TraceRange region(wave::trace_init_name(c.dimension, c.equation));
     if (c.dimension != 2 && c.dimension != 3) return fail(nullptr, WAVE_ERR_ARG, "Unkown dimension");
     if (c.equation < WAVE_EQ_ACOUSTIC || c.equation > WAVE_EQ_VISCOEMEM) return fail(nullptr, WAVE_ERR_ARG, "Unkown type");
     const bool is3d = c.dimension == 3;
@@ -749,6 +751,7 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
                    const float* taus, size_t n, int mem)
 {
     if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_model: null handle");
+    wave::TraceRange region("WAVE-Simulation.initModel");
     const int eq = h->cfg.equation;
     if (eq_em(eq)) return fail(h, WAVE_ERR_ARG, "wave_set_model: EM equation, use wave_set_model_em");
     if (n != static_cast<size_t>(h->N)) return fail(h, WAVE_ERR_ARG, "wave_set_model: n != the number of grid points");
@@ -853,6 +856,7 @@ int wave_set_model_em(wave_handle* h, const float* eps_r, const float* sigma, co
                       const float* tau_eps, const float* tau_sigma, size_t n, int mem)
 {
     if (!h) return fail(nullptr, WAVE_ERR_ARG, "wave_set_model_em: null handle");
+    wave::TraceRange region("WAVE-Simulation.initModel");
     const int eq = h->cfg.equation;
     if (!eq_em(eq)) return fail(h, WAVE_ERR_ARG, "wave_set_model_em: seismic equation, use wave_set_model");
     if (n != static_cast<size_t>(h->N)) return fail(h, WAVE_ERR_ARG, "wave_set_model_em: n != NX*NY*NZ");
@@ -1046,13 +1050,18 @@ int wave_solver_step(wave_handle* h, int t_begin, int t_end)
     if (t_begin < 0 || t_end < t_begin || t_end > h->NT) return fail(h, WAVE_ERR_ARG, "wave_solver_step: time range outside [0, NT]");
     if (!h->modelSet) return fail(h, WAVE_ERR_STATE, "wave_solver_step: call wave_set_model first");
     if (!h->seis) return fail(h, WAVE_ERR_STATE, "wave_solver_step: call wave_set_receivers first");
+    wave::TraceRange region("WAVE-Simulation.timeLoop");
+    const char* stepName = wave::trace_timestep_name(h->cfg.dimension, h->cfg.equation);
     WAVE_TRY(h, {
         launch_set_counter(h->tcounter, t_begin, h->stream);
         h->launches += 1;
         int t = t_begin;
         if (h->timing) {
             std::vector<cudaEvent_t> ev;
-            for (; t < t_end; ++t) launch_step_timed(h, ev);
+            for (; t < t_end; ++t) {
+                wave::TraceRange step(stepName);
+                launch_step_timed(h, ev);
+            }
             h->check(cudaGetLastError(), "step launch");
             h->check(cudaStreamSynchronize(h->stream), "step");
             for (size_t k = 0; k + 2 < ev.size(); k += 3) {
@@ -1071,11 +1080,15 @@ int wave_solver_step(wave_handle* h, int t_begin, int t_end)
             if (h->graphDirty || !h->graph) build_graph(h);
             if (t_end - t >= kGraphSteps) {
                 for (; t + kGraphSteps <= t_end; t += kGraphSteps) {
+                    wave::TraceRange steps(stepName);   // kGraphSteps steps in one graph launch
                     h->check(cudaGraphLaunch(h->graph, h->stream), "graph launch");
                     h->launches += h->graphLaunchesPerStep * kGraphSteps;
                 }
             }
-            for (; t < t_end; ++t) launch_step(h);
+            for (; t < t_end; ++t) {
+                wave::TraceRange step(stepName);
+                launch_step(h);
+            }
             h->check(cudaGetLastError(), "step launch");
         }
         h->stepsSinceReset += t_end - t_begin;
