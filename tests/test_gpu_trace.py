@@ -1,7 +1,8 @@
 """The NVTX ranges around the library's phases (csrc/trace.h, the counterpart
 of the reference's SCAI_REGION markers) are host-side only: a run with the
 ranges switched off (WAVE_TRACE=0) gives bit-identical seismograms and
-gradients to a run with them on."""
+gradients to a run with them on, and the same misfit to its atomic sum's
+rounding."""
 import json
 import os
 import subprocess
@@ -51,5 +52,7 @@ def test_trace_switch_does_not_change_results():
     seis = np.frombuffer(bytes.fromhex(on["seis"]), np.float32)
     assert np.abs(seis).max() > 0
     assert on["seis"] == off["seis"]
-    assert on["J"] == off["J"] and on["J"] > 0
+    # the misfit is a double-precision atomic sum over the residual samples, its
+    # last bits follow the order the additions land in (as between any two runs)
+    assert on["J"] > 0 and abs(on["J"] - off["J"]) <= 1e-12 * on["J"]
     assert on["g"] == off["g"]
