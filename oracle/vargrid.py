@@ -517,12 +517,10 @@ class Operators:
 # --------------------------------------------------------------------------
 # model averages and CPML coefficients
 # --------------------------------------------------------------------------
-def inverse_density_averages(g: VarGrid, rho: np.ndarray, dtype=np.float32):
-    """calcAverageMatrixX/Y/Z (Modelparameter.cpp:336-446) applied to rho,
-    then 1/avg with invalid -> 0 (calcInverseAveragedParameter :633-640)."""
-    d = np.dtype(dtype).type
-    rho = rho.astype(dtype)
-    half = d(0.5)
+def density_partners(g: VarGrid):
+    """The averaging partner of every point per axis (x, y[, z]) of
+    calcAverageMatrixX/Y/Z (Modelparameter.cpp:336-446): (ok, col) with ok
+    false where the point is averaged with itself alone."""
     out = []
     axes = ["x", "y"] + (["z"] if g.NZ > 1 else [])
     f_row = np.array(g.dhf, dtype=np.int64)[g.layer]
@@ -546,6 +544,18 @@ def inverse_density_averages(g: VarGrid, rho: np.ndarray, dtype=np.float32):
             ok = Y < g.NY
             col = np.zeros(g.N, np.int64)
             col[ok] = g.coordinate2index(g.x[ok], Y[ok], g.z[ok])
+        out.append((ok, col))
+    return out
+
+
+def inverse_density_averages(g: VarGrid, rho: np.ndarray, dtype=np.float32):
+    """calcAverageMatrixX/Y/Z (Modelparameter.cpp:336-446) applied to rho,
+    then 1/avg with invalid -> 0 (calcInverseAveragedParameter :633-640)."""
+    d = np.dtype(dtype).type
+    rho = rho.astype(dtype)
+    half = d(0.5)
+    out = []
+    for ok, col in density_partners(g):
         avg = np.where(ok, (half * rho + half * rho[col]).astype(dtype), rho).astype(dtype)
         with np.errstate(divide="ignore", invalid="ignore"):
             inv = (d(1) / avg).astype(dtype)

@@ -686,7 +686,7 @@ std::string adjoint_supported(const wave_handle* h)
         for (int t : h->hSrcType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez sources only";
     }
-    if (h->vg) return "the adjoint gradient is implemented on regular grids";
+    if (h->vg && c.equation != WAVE_EQ_ACOUSTIC) return "the adjoint gradient on a variable grid is implemented for the acoustic equations";
     if (!h->modelSet) return "set the model first";
     if (!h->seis || h->nrec < 1) return "set receivers first";
     return "";
@@ -975,11 +975,16 @@ extern "C" int wave_adjoint_gradient(wave_handle* h, const float* dobs, int dobs
         float* out[3] = {grad_vp, grad_vs, grad_rho};
         float* dOut[3];
         for (int k = 0; k < 3; ++k) dOut[k] = grad_mem == WAVE_MEM_DEVICE ? out[k] : dev(N);
-        AdjStepper S;
-        S.stream = h->stream;
-        S.set_counter = [h](int n) { launch_set_counter(h->tcounter, n, h->stream); };
-        S.step = [h]() { step_once(h); };
-        adjoint_run({h}, S, &dDobs, checkpoint_every, misfit, &dOut[0], &dOut[1], &dOut[2], false);
+        if (h->vg) {
+            ck(cudaMemsetAsync(dOut[1], 0, N * sizeof(float), h->stream), "memset");
+            vargrid_adjoint(h, dDobs, checkpoint_every, misfit, dOut[0], dOut[2]);
+        } else {
+            AdjStepper S;
+            S.stream = h->stream;
+            S.set_counter = [h](int n) { launch_set_counter(h->tcounter, n, h->stream); };
+            S.step = [h]() { step_once(h); };
+            adjoint_run({h}, S, &dDobs, checkpoint_every, misfit, &dOut[0], &dOut[1], &dOut[2], false);
+        }
         if (grad_mem != WAVE_MEM_DEVICE)
             for (int k = 0; k < 3; ++k) ck(cudaMemcpy(out[k], dOut[k], N * sizeof(float), cudaMemcpyDeviceToHost), "gradient copy");
     } catch (std::exception& e) {

@@ -772,6 +772,11 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         float* dTs = visco ? stage(h, taus, n, mem, tmp) : nullptr;
         if (h->vg) {
             wave::vargrid_set_model(h, dRho, dVp, dVs);
+            if (eq == WAVE_EQ_ACOUSTIC)   // rho and vp for the adjoint's chain rule
+                for (auto [slot, src] : {std::pair<int, const float*>{M_RHO, dRho}, {M_VP, dVp}}) {
+                    if (!h->m[slot]) h->m[slot] = h->alloc<float>(h->N);
+                    h->check(cudaMemcpyAsync(h->m[slot], src, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
+                }
             for (float* p : tmp) cudaFreeAsync(p, s);
             h->check(cudaStreamSynchronize(s), "model preparation");
             h->modelSet = true;

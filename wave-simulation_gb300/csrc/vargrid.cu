@@ -32,6 +32,9 @@
 //             Dzf vy + DyfStaggeredZ vz]
 //   vg_interp sxx, syy [, szz] (Full), sxy (StaggeredX) [, sxz (StaggeredXZ),
 //             syz (StaggeredZ)]
+#include <algorithm>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "handle.h"
@@ -829,6 +832,527 @@ int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrec
                  E.v[0], E.v[1], G.is3d ? E.v[2] : nullptr});
     h->check(cudaGetLastError(), "variable grid step launch");
     return launches;
+}
+
+// ---------------------------------------------------------------- adjoint
+// Discrete adjoint of the acoustic step above (vg_vel, the velocity
+// interpolations, vg_pres with the surface zero, vg_abs, the pressure
+// interpolation, sources and receivers), for J = 1/2 sum (d - d_obs)^2 over
+// receivers and steps. Every operator of the step is an ELL block, an
+// interpolation row list or a per-point factor, so the backward step applies
+// their transposes in reverse order: the ELL blocks' transposes are built
+// once on the host, an interpolation's transpose moves each rewritten row's
+// adjoint onto its four source rows (atomics: a few rows per interface). The
+// forward intermediates a step's gradient terms need (Df p + CPML, the
+// interpolated velocities, Db v + CPML) are re-formed from the stored state.
+
+namespace {
+
+struct VgAdj {
+    long long N, nSurface;
+    int fs, cpml, naxes;
+    // forward state n and the intermediates re-formed from it
+    const float* p;
+    const float* v[3];
+    const float* psiP[3];       // p_x, p_y, p_z
+    const float* psiV[3];       // vxx, vyy, vzz
+    float* gx[3];               // Df p + CPML per axis
+    float* v2[3];               // velocities after the update (then interpolated in place)
+    float* d;                   // Dxb vx + Dyb vy [+ Dzb vz] with CPML
+    // adjoint state: of the state after step n on entry, of state n on exit
+    float* lp;
+    float* lv[3];
+    float* lpsiP[3];
+    float* lpsiV[3];
+    // adjoint temporaries and gradient sums
+    float* lp3;
+    float* lv2[3];
+    float* ldx[3];
+    float* lu[3];
+    float* gM;
+    float* gir[3];
+    const float* M;
+    const float* ir[3];
+    const float* damp;
+    const int* col[6];
+    const float* val[6];
+    int W[6];
+    const int* colT[6];
+    const float* valT[6];
+    int WT[6];
+    const unsigned short* cpc[3];
+    const float* cpt[3];
+};
+
+__device__ __forceinline__ float ell_gather(const int* __restrict__ col, const float* __restrict__ val, int W, long long N, long long i,
+                                            const float* __restrict__ u)
+{
+    float s = 0.0f;
+    for (int k = 0; k < W; ++k) s = __fmaf_rn(val[k * N + i], u[col[k * N + i]], s);
+    return s;
+}
+
+// CPML coefficients of point i on an axis (half: the velocity update's);
+// false where the point has none
+__device__ __forceinline__ bool adj_cpml(const VgAdj& A, int axis, bool half, long long i, float& a, float& b)
+{
+    if (!A.cpml) return false;
+    const unsigned code = A.cpc[axis][i];
+    if (code == 0) return false;
+    a = A.cpt[axis][4 * code + (half ? 2 : 0)];
+    b = A.cpt[axis][4 * code + (half ? 3 : 1)];
+    return a != 0.0f || b != 0.0f;
+}
+
+// the velocity update of step n again: gx = Df p + CPML, v2 = v + gx / rho
+__global__ void __launch_bounds__(256) vga_fwd_vel(VgAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    for (int ax = 0; ax < A.naxes; ++ax) {
+        float u = ell_gather(A.col[ax], A.val[ax], A.W[ax], A.N, i, A.p);
+        float a, b;
+        if (adj_cpml(A, ax, true, i, a, b)) u = __fadd_rn(u, __fadd_rn(__fmul_rn(A.psiP[ax][i], b), __fmul_rn(a, u)));
+        A.gx[ax][i] = u;
+        A.v2[ax][i] = __fadd_rn(A.v[ax][i], __fmul_rn(u, A.ir[ax][i]));
+    }
+}
+
+// the pressure update's derivative sum of step n from the interpolated velocities
+__global__ void __launch_bounds__(256) vga_fwd_div(VgAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    float d = 0.0f;
+    for (int ax = 0; ax < A.naxes; ++ax) {
+        float u = ell_gather(A.col[3 + ax], A.val[3 + ax], A.W[3 + ax], A.N, i, A.v2[ax]);
+        float a, b;
+        if (adj_cpml(A, ax, false, i, a, b)) u = __fadd_rn(u, __fadd_rn(__fmul_rn(A.psiV[ax][i], b), __fmul_rn(a, u)));
+        d = ax == 0 ? u : __fadd_rn(d, u);
+    }
+    A.d[i] = d;
+}
+
+// the residual of step n at the receivers into the adjoint of the field each reads
+__global__ void vga_inject(VgAdj A, int nrec, int nt, int n, const long long* __restrict__ ridx, const int* __restrict__ rtype,
+                           const float* __restrict__ res)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const int t = rtype[r];
+    float* f = t == 1 ? A.lp : (t >= 2 && t - 2 < A.naxes) ? A.lv[t - 2] : nullptr;
+    if (f) atomicAdd(f + ridx[r], res[static_cast<long long>(r) * nt + n]);
+}
+
+// transposed surface zero (FreeSurface.cpp:14-19): lp3 = lp outside the surface rows
+__global__ void __launch_bounds__(256) vga_surface(VgAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    A.lp3[i] = (A.fs && i < A.nSurface) ? 0.0f : A.lp[i];
+}
+
+// transposed ABS taper and pressure update, the pressure update's CPML
+__global__ void __launch_bounds__(256) vga_pres(VgAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    const float dm = A.damp ? A.damp[i] : 1.0f;
+    const float l1 = A.lp3[i] * dm;
+    for (int ax = 0; ax < A.naxes; ++ax) A.lv2[ax][i] = A.lv[ax][i] * dm;
+    A.gM[i] += l1 * A.d[i];
+    const float ld = A.M[i] * l1;
+    A.lp[i] = l1;
+    for (int ax = 0; ax < A.naxes; ++ax) {
+        float a, b;
+        if (adj_cpml(A, ax, false, i, a, b)) {
+            const float tot = A.lpsiV[ax][i] + ld;
+            A.ldx[ax][i] = ld + a * tot;
+            A.lpsiV[ax][i] = b * tot;
+        } else {
+            A.ldx[ax][i] = ld;
+        }
+    }
+}
+
+// lv = lv2 + Db^T ldx per axis
+__global__ void __launch_bounds__(256) vga_div_t(VgAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    for (int ax = 0; ax < A.naxes; ++ax)
+        A.lv[ax][i] = A.lv2[ax][i] + ell_gather(A.colT[3 + ax], A.valT[3 + ax], A.WT[3 + ax], A.N, i, A.ldx[ax]);
+}
+
+// transposed velocity update and its CPML: the density-average gradient, lu = adjoint of Df p
+__global__ void __launch_bounds__(256) vga_vel(VgAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    for (int ax = 0; ax < A.naxes; ++ax) {
+        const float l1 = A.lv[ax][i];
+        const float lg = A.ir[ax][i] * l1;
+        A.gir[ax][i] += l1 * A.gx[ax][i];
+        float a, b;
+        if (adj_cpml(A, ax, true, i, a, b)) {
+            const float tot = A.lpsiP[ax][i] + lg;
+            A.lu[ax][i] = lg + a * tot;
+            A.lpsiP[ax][i] = b * tot;
+        } else {
+            A.lu[ax][i] = lg;
+        }
+    }
+}
+
+// lp += sum over axes of Df^T lu
+__global__ void __launch_bounds__(256) vga_grad_t(VgAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    float s = A.lp[i];
+    for (int ax = 0; ax < A.naxes; ++ax) s += ell_gather(A.colT[ax], A.valT[ax], A.WT[ax], A.N, i, A.lu[ax]);
+    A.lp[i] = s;
+}
+
+// transposed interpolation rows: every list's rewritten rows hand their
+// adjoint to their four source rows. Phase 0 takes each row's adjoint into
+// the scratch and clears the row, phase 1 adds it onto the source rows.
+struct VgInterpT {
+    int n[3];
+    float* f[3];
+    float* tmp[3];
+    const int* row[3];
+    const int* col[3];
+    const float* w[3];
+};
+__global__ void __launch_bounds__(256) vga_interp_t(VgInterpT I, int phase)
+{
+    const int s = blockIdx.y;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= I.n[s]) return;
+    float* f = I.f[s];
+    if (phase == 0) {
+        const int r = I.row[s][k];
+        I.tmp[s][k] = f[r];
+        f[r] = 0.0f;
+        return;
+    }
+    const float t = I.tmp[s][k];
+    for (int q = 0; q < 4; ++q) atomicAdd(f + I.col[s][4 * k + q], I.w[s][4 * k + q] * t);
+}
+
+// dJ/dvp, dJ/drho from the sums over the steps: M = rho vp^2
+// (ModelparameterSeismic.cpp:131-136) and the inverse density averages
+// 1 / (rho_i / 2 + rho_j / 2) with the axis partner j, or 1 / rho_i alone
+// (Modelparameter.cpp:336-446, 633-640); grho starts at zero
+__global__ void __launch_bounds__(256) vga_chain(VgAdj A, const float* __restrict__ rho, const float* __restrict__ vp,
+                                                 const int* __restrict__ px, const int* __restrict__ py, const int* __restrict__ pz,
+                                                 float* gvp, float* grho)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    const float g = A.gM[i];
+    gvp[i] = g * 2.0f * rho[i] * vp[i];
+    float own = g * vp[i] * vp[i];
+    const int* part[3] = {px, py, pz};
+    for (int ax = 0; ax < A.naxes; ++ax) {
+        const float r = A.ir[ax][i];
+        const float w = -A.gir[ax][i] * r * r;
+        const int j = part[ax][i];
+        if (j >= 0) {
+            own += 0.5f * w;
+            atomicAdd(grho + j, 0.5f * w);
+        } else {
+            own += w;
+        }
+    }
+    atomicAdd(grho + i, own);
+}
+
+// residuals seis - dobs and the misfit 1/2 sum res^2 (double, one atomic per block)
+__global__ void __launch_bounds__(256) vga_residual(const float* __restrict__ seis, const float* __restrict__ dobs, float* res, long long n,
+                                                    double* misfit)
+{
+    __shared__ double part[256];
+    double acc = 0.0;
+    for (long long k = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const float r = seis[k] - dobs[k];
+        res[k] = r;
+        acc += 0.5 * static_cast<double>(r) * r;
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(misfit, part[0]);
+}
+
+// the ELL blocks' transposes (entry-major like the forward blocks; padding
+// entries point at the row itself with weight 0)
+void build_transposes(wave_handle* h)
+{
+    VarGridDev& G = *h->vg;
+    if (G.transposed) return;
+    const long long N = G.N;
+    for (int op = 0; op < 6; ++op) {
+        if (!G.col[op] || G.W[op] == 0) continue;
+        const int W = G.W[op];
+        std::vector<int> col(static_cast<size_t>(W) * N);
+        std::vector<float> val(col.size());
+        h->check(cudaMemcpy(col.data(), G.col[op], col.size() * sizeof(int), cudaMemcpyDeviceToHost), "operator download");
+        h->check(cudaMemcpy(val.data(), G.val[op], val.size() * sizeof(float), cudaMemcpyDeviceToHost), "operator download");
+        std::vector<int> count(N, 0);
+        for (long long i = 0; i < N; ++i)
+            for (int k = 0; k < W; ++k)
+                if (val[k * N + i] != 0.0f) ++count[col[k * N + i]];
+        int WT = 1;
+        for (long long c = 0; c < N; ++c) WT = count[c] > WT ? count[c] : WT;
+        std::vector<int> colT(static_cast<size_t>(WT) * N);
+        std::vector<float> valT(colT.size(), 0.0f);
+        for (long long c = 0; c < N; ++c)
+            for (int k = 0; k < WT; ++k) colT[k * N + c] = static_cast<int>(c);
+        std::fill(count.begin(), count.end(), 0);
+        for (long long i = 0; i < N; ++i)
+            for (int k = 0; k < W; ++k) {
+                const float v = val[k * N + i];
+                if (v == 0.0f) continue;
+                const int c = col[k * N + i];
+                const int slot = count[c]++;
+                colT[slot * N + c] = static_cast<int>(i);
+                valT[slot * N + c] = v;
+            }
+        G.WT[op] = WT;
+        G.colT[op] = upload(h, colT);
+        G.valT[op] = upload(h, valT);
+    }
+    G.transposed = true;
+}
+
+// the interpolation of the listed fields (kinds: 0 Full, 1 StaggeredX, 2
+// StaggeredZ), as the forward step runs it, without sources and receivers
+void interp_apply(wave_handle* h, const int* kinds, float* const* fields, int m)
+{
+    const VarGridDev& G = *h->vg;
+    VgInterp I{};
+    I.srSlot = -1;
+    int n = 0, mx = 0;
+    bool twoPhase = false;
+    long long off = 0;
+    for (int q = 0; q < m; ++q) {
+        const int kind = kinds[q];
+        if (!fields[q] || G.nInterp[kind] == 0) continue;
+        I.n[n] = G.nInterp[kind];
+        I.f[n] = fields[q];
+        I.row[n] = G.irow[kind];
+        I.col[n] = G.icol[kind];
+        I.w[n] = G.iw[kind];
+        I.tmp[n] = G.itmp + off;
+        off += G.nInterp[kind];
+        I.phase[n] = G.inplace[kind] ? 0 : 1;
+        twoPhase = twoPhase || !G.inplace[kind];
+        mx = I.n[n] > mx ? I.n[n] : mx;
+        ++n;
+    }
+    if (n == 0) return;
+    const dim3 grid(static_cast<unsigned>((mx + 255) / 256), static_cast<unsigned>(n));
+    vg_interp<<<grid, 256, 0, h->stream>>>(I);
+    if (twoPhase) {
+        for (int q = 0; q < n; ++q) I.n[q] = I.phase[q] == 1 ? I.n[q] : 0;
+        for (int q = 0; q < n; ++q) I.phase[q] = 2;
+        vg_interp<<<grid, 256, 0, h->stream>>>(I);
+    }
+}
+
+// the transpose of interp_apply on adjoint fields (tmp: scratch of the
+// summed row counts)
+void interp_transpose(wave_handle* h, const int* kinds, float* const* fields, int m, float* tmp)
+{
+    const VarGridDev& G = *h->vg;
+    VgInterpT I{};
+    int n = 0, mx = 0;
+    long long off = 0;
+    for (int q = 0; q < m; ++q) {
+        const int kind = kinds[q];
+        if (!fields[q] || G.nInterp[kind] == 0) continue;
+        I.n[n] = G.nInterp[kind];
+        I.f[n] = fields[q];
+        I.row[n] = G.irow[kind];
+        I.col[n] = G.icol[kind];
+        I.w[n] = G.iw[kind];
+        I.tmp[n] = tmp + off;
+        off += G.nInterp[kind];
+        mx = I.n[n] > mx ? I.n[n] : mx;
+        ++n;
+    }
+    if (n == 0) return;
+    const dim3 grid(static_cast<unsigned>((mx + 255) / 256), static_cast<unsigned>(n));
+    vga_interp_t<<<grid, 256, 0, h->stream>>>(I, 0);
+    vga_interp_t<<<grid, 256, 0, h->stream>>>(I, 1);
+}
+
+} // namespace
+
+void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* grho)
+{
+    build_transposes(h);
+    const VarGridDev& G = *h->vg;
+    cudaStream_t st = h->stream;
+    const long long N = G.N;
+    const int NT = h->NT;
+    const int na = G.is3d ? 3 : 2;
+    const VgParams P = params_of(h);
+    const bool cp = P.cpml != 0;
+
+    std::vector<void*> bufs;
+    struct Free {
+        std::vector<void*>& v;
+        ~Free() { for (void* p : v) cudaFree(p); }
+    } freeBufs{bufs};
+    auto dev = [&](size_t count) {
+        void* p = nullptr;
+        h->check(cudaMalloc(&p, (count > 0 ? count : 1) * sizeof(float)), "cudaMalloc");
+        bufs.push_back(p);
+        return static_cast<float*>(p);
+    };
+    auto zero = [&](float* p, size_t count) { h->check(cudaMemsetAsync(p, 0, count * sizeof(float), st), "memset"); };
+
+    // state parts: p, vx, vy [, vz] and the CPML memory variables
+    std::vector<float*> parts = {P.p, P.vx, P.vy};
+    if (G.is3d) parts.push_back(P.vz);
+    const int psiP[3] = {0, 1, 2}, psiV[3] = {3, 4, 5};
+    if (cp)
+        for (int a = 0; a < na; ++a) {
+            parts.push_back(P.psi[psiP[a]]);
+            parts.push_back(P.psi[psiV[a]]);
+        }
+    const size_t S = parts.size();
+    const int nck = (NT + K - 1) / K;
+    float* ckpt = dev(static_cast<size_t>(nck) * S * N);
+    float* view = dev(static_cast<size_t>(K) * S * N);
+    auto save = [&](float* dst) {
+        for (size_t k = 0; k < S; ++k)
+            h->check(cudaMemcpyAsync(dst + k * N, parts[k], N * sizeof(float), cudaMemcpyDeviceToDevice, st), "state copy");
+    };
+    auto restore = [&](const float* src) {
+        for (size_t k = 0; k < S; ++k)
+            h->check(cudaMemcpyAsync(parts[k], src + k * N, N * sizeof(float), cudaMemcpyDeviceToDevice, st), "state copy");
+    };
+
+    // 1. forward with checkpoints from a zero state
+    for (float* f : parts) zero(f, N);
+    launch_set_counter(h->tcounter, 0, st);
+    for (int n = 0; n < NT; ++n) {
+        if (n % K == 0) save(ckpt + static_cast<size_t>(n / K) * S * N);
+        step_once(h);
+    }
+    // 2. residuals and misfit
+    const long long nd = static_cast<long long>(h->nrec) * NT;
+    float* res = dev(nd);
+    double* dMis = nullptr;
+    h->check(cudaMalloc(&dMis, sizeof(double)), "cudaMalloc");
+    bufs.push_back(dMis);
+    h->check(cudaMemsetAsync(dMis, 0, sizeof(double), st), "memset");
+    vga_residual<<<256, 256, 0, st>>>(h->seis, dobs, res, nd, dMis);
+
+    // 3. backward sweep
+    VgAdj A{};
+    A.N = N;
+    A.nSurface = G.nSurface;
+    A.fs = G.fs;
+    A.cpml = cp ? 1 : 0;
+    A.naxes = na;
+    A.M = P.M;
+    A.damp = G.absDamp;
+    for (int k = 0; k < 6; ++k) {
+        A.col[k] = G.col[k];
+        A.val[k] = G.val[k];
+        A.W[k] = G.W[k];
+        A.colT[k] = G.colT[k];
+        A.valT[k] = G.valT[k];
+        A.WT[k] = G.WT[k];
+    }
+    for (int a = 0; a < 3; ++a) {
+        A.cpc[a] = G.cpCode[a];
+        A.cpt[a] = G.cpTab[a];
+        A.ir[a] = P.ir[a];
+    }
+    const size_t nAdj = 1 + na + (cp ? 2 * na : 0);
+    float* adj = dev(nAdj * N);
+    zero(adj, nAdj * N);
+    A.lp = adj;
+    for (int a = 0; a < na; ++a) {
+        A.lv[a] = adj + (1 + a) * N;
+        if (cp) {
+            A.lpsiP[a] = adj + (1 + na + 2 * a) * N;
+            A.lpsiV[a] = adj + (2 + na + 2 * a) * N;
+        }
+    }
+    float* tmp = dev((5 * na + 3) * static_cast<size_t>(N));
+    for (int a = 0; a < na; ++a) {
+        A.gx[a] = tmp + a * N;
+        A.v2[a] = tmp + (na + a) * N;
+        A.lv2[a] = tmp + (2 * na + a) * N;
+        A.ldx[a] = tmp + (3 * na + a) * N;
+        A.lu[a] = tmp + (4 * na + a) * N;
+    }
+    A.d = tmp + 5 * na * N;
+    A.lp3 = tmp + (5 * na + 1) * N;
+    A.gM = tmp + (5 * na + 2) * N;
+    float* gir = dev(static_cast<size_t>(na) * N);
+    zero(gir, static_cast<size_t>(na) * N);
+    zero(A.gM, N);
+    for (int a = 0; a < na; ++a) A.gir[a] = gir + a * N;
+    const long long nRows = static_cast<long long>(G.nInterp[0]) + G.nInterp[1] + G.nInterp[2];
+    float* itmp = dev(static_cast<size_t>(nRows > 0 ? nRows : 1));
+
+    const dim3 grid(static_cast<unsigned>((N + 255) / 256)), block(256);
+    const int velKinds[3] = {1, 0, 2};   // vx StaggeredX, vy Full, vz StaggeredZ
+    const int presKind[1] = {0};
+    for (int seg = nck - 1; seg >= 0; --seg) {
+        const int n0 = seg * K, n1 = n0 + K < NT ? n0 + K : NT;
+        restore(ckpt + static_cast<size_t>(seg) * S * N);
+        launch_set_counter(h->tcounter, n0, st);
+        for (int n = n0; n < n1; ++n) {
+            save(view + static_cast<size_t>(n - n0) * S * N);
+            if (n + 1 < n1) step_once(h);
+        }
+        for (int n = n1 - 1; n >= n0; --n) {
+            const float* sv = view + static_cast<size_t>(n - n0) * S * N;
+            A.p = sv;
+            for (int a = 0; a < na; ++a) A.v[a] = sv + (1 + a) * N;
+            for (int a = 0; a < na; ++a) {
+                A.psiP[a] = cp ? sv + (1 + na + 2 * a) * N : nullptr;
+                A.psiV[a] = cp ? sv + (2 + na + 2 * a) * N : nullptr;
+            }
+            vga_inject<<<(h->nrec + 127) / 128, 128, 0, st>>>(A, h->nrec, NT, n, h->ridx, h->rtype, res);
+            vga_fwd_vel<<<grid, block, 0, st>>>(A);
+            float* v2f[3] = {A.v2[0], A.v2[1], na == 3 ? A.v2[2] : nullptr};
+            interp_apply(h, velKinds, v2f, 3);
+            vga_fwd_div<<<grid, block, 0, st>>>(A);
+            vga_surface<<<grid, block, 0, st>>>(A);
+            float* lp3f[1] = {A.lp3};
+            interp_transpose(h, presKind, lp3f, 1, itmp);
+            vga_pres<<<grid, block, 0, st>>>(A);
+            vga_div_t<<<grid, block, 0, st>>>(A);
+            float* lvf[3] = {A.lv[0], A.lv[1], na == 3 ? A.lv[2] : nullptr};
+            interp_transpose(h, velKinds, lvf, 3, itmp);
+            vga_vel<<<grid, block, 0, st>>>(A);
+            vga_grad_t<<<grid, block, 0, st>>>(A);
+        }
+        h->check(cudaGetLastError(), "variable grid adjoint");
+    }
+    // 4. chain rule
+    zero(grho, N);
+    vga_chain<<<grid, block, 0, st>>>(A, h->m[M_RHO], h->m[M_VP], G.partner[0], G.partner[1], G.is3d ? G.partner[2] : nullptr,
+                                      gvp, grho);
+    h->check(cudaGetLastError(), "variable grid adjoint");
+    double J = 0.0;
+    h->check(cudaMemcpyAsync(&J, dMis, sizeof(double), cudaMemcpyDeviceToHost, st), "misfit");
+    h->check(cudaStreamSynchronize(st), "variable grid adjoint");
+    *misfit = J;
+    h->stepsSinceReset = NT;
 }
 
 } // namespace wave

@@ -124,6 +124,12 @@ struct VarGridDev {
     long long nSurface = 0;
     int fs = 0;
     const float* absDamp = nullptr;         // ABS taper per point (null: no ABS)
+    // transposes of Dxf, Dyf, Dzf, Dxb, Dyb, Dzb as ELL blocks (the adjoint;
+    // built at its first call)
+    bool transposed = false;
+    int WT[6] = {};
+    const int* colT[6] = {};
+    const float* valT[6] = {};
     // stencil classes per pass (null: not available)
     const unsigned* clsId[2] = {};
     const int* clsOff[2] = {};
