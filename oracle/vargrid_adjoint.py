@@ -1,5 +1,6 @@
-"""Discrete adjoint of the acoustic variable-grid step (oracle, test
-infrastructure only: used by tests/ as the checker, never by the library).
+"""Discrete adjoints of the acoustic and 2-D elastic variable-grid steps
+(oracle, test infrastructure only: used by tests/ as the checker, never by
+the library).
 
 The forward step is AcousticVarGrid.step (oracle/vargrid.py), the
 restatement of FD2Dacoustic / FD3Dacoustic::run on a variable grid
@@ -126,3 +127,166 @@ def adjoint_gradient(g: VarGrid, orders, DT, rho, vp, free_surface, cpml, src_id
         np.add.at(grho, col[ok], 0.5 * w[ok])
     del M
     return J, gvp, grho
+
+
+def _shear_xy_terms(g: VarGrid):
+    """The points and weights of every point's XY 4-point average
+    (shear_average_xy in oracle/vargrid_elastic.py, Modelparameter.cpp:
+    449-533): a list of (rows, partner columns, weight)."""
+    f = np.array(g.dhf, dtype=np.int64)[g.layer]
+    x2, y2 = g.x + f, g.y + f
+    okx, oky = x2 < g.NX, y2 < g.NY
+    out = []
+    i = np.nonzero(okx & oky)[0]
+    for c in (i, g.coordinate2index(x2[i], g.y[i], g.z[i]), g.coordinate2index(g.x[i], y2[i], g.z[i]),
+              g.coordinate2index(x2[i], y2[i], g.z[i])):
+        out.append((i, np.asarray(c, np.int64), 0.25))
+    b = np.nonzero(okx & ~oky)[0]
+    out += [(b, b, 0.5), (b, np.asarray(g.coordinate2index(x2[b], g.y[b], g.z[b]), np.int64), 0.5)]
+    r = np.nonzero(~okx & oky)[0]
+    out += [(r, r, 0.5), (r, np.asarray(g.coordinate2index(g.x[r], y2[r], g.z[r]), np.int64), 0.5)]
+    c = np.nonzero(~okx & ~oky)[0]
+    out.append((c, c, 1.0))
+    return out
+
+
+def elastic_adjoint_gradient_2d(g: VarGrid, orders, DT, rho, vp, vs, cpml, src_idx, src_type, signals, rec_idx, rec_type,
+                                dobs, damping=None, free_surface=False, var_order=True, edge=True, var_grid=True):
+    """(J, dJ/dvp, dJ/dvs, dJ/drho) of the 2-D elastic variable-grid run
+    (ElasticVarGrid2D, FD2Delastic::run ForwardSolver2Delastic.cpp:117-297)
+    in FP64: the transposes of its sparse step in reverse order; the chain
+    rule through M = rho vp^2, mu = rho vs^2, the inverse density averages,
+    the XY shear average of 1/max(mu, 1) and the free-surface scales
+    scaleV = M - 2 mu, scaleH = -(M - 2 mu)^2 / M (FreeSurfaceElastic.cpp:11-47)."""
+    from oracle.vargrid_elastic import ElasticVarGrid2D
+    rho = np.asarray(rho, np.float64)
+    vp = np.asarray(vp, np.float64)
+    vs = np.asarray(vs, np.float64)
+    f = ElasticVarGrid2D(g, orders, DT, rho, vp, vs, cpml, src_idx, src_type, np.asarray(signals, np.float64), rec_idx,
+                         rec_type, dtype=np.float64, var_order=var_order, edge=edge, var_grid=var_grid,
+                         free_surface=free_surface, damping=damping)
+    nt = np.asarray(signals).shape[1]
+    names = ("vx", "vy", "sxx", "syy", "sxy")
+    states, seis = [], np.zeros((len(rec_idx), nt))
+    for t in range(nt):
+        st = {k: getattr(f, k).copy() for k in names}
+        st.update({"psi_" + k: v.copy() for k, v in f.psi.items()})
+        states.append(st)
+        seis[:, t] = f.step(t)
+    res = seis - np.asarray(dobs, np.float64)
+    J = 0.5 * float(np.sum(res * res))
+
+    op, n = f.op, g.N
+    cp = cpml
+
+    def term(D, u, psi, ax, half):
+        d = D @ u
+        if cp is not None:
+            af, bf, ah, bh = cp[ax]
+            a, b = (ah, bh) if half else (af, bf)
+            d = d + (psi * b + a * d)
+        return d
+
+    def term_t(ld, lpsi, ax, half):
+        if cp is None:
+            return ld, np.zeros(n)
+        af, bf, ah, bh = cp[ax]
+        a, b = (ah, bh) if half else (af, bf)
+        tot = lpsi + ld
+        return ld + a * tot, b * tot
+
+    lam = {k: np.zeros(n) for k in names}
+    lpsi = {k: np.zeros(n) for k in f.psi}
+    gM, gmu, gmuXY, girx, giry, gsH, gsV = (np.zeros(n) for _ in range(7))
+    dmp = np.ones(n) if damping is None else np.asarray(damping, np.float64)
+    M, mu, muXY = f.M, f.mu, f.muXY
+    for t in range(nt - 1, -1, -1):
+        S = states[t]
+        for r, (i, k) in enumerate(zip(rec_idx, rec_type)):
+            if k == 1:
+                lam["sxx"][i] += 0.5 * res[r, t]
+                lam["syy"][i] += 0.5 * res[r, t]
+            else:
+                lam["vx" if k == 2 else "vy"][i] += res[r, t]
+        # forward intermediates of step t
+        gvx = term(op.Dxf, S["sxx"], S["psi_sxx_x"], "x", True) + term(f.DybSX, S["sxy"], S["psi_sxy_y"], "y", False)
+        vx2 = op.IStagX @ (S["vx"] + gvx * f.irx)
+        gvy = term(op.Dxb, S["sxy"], S["psi_sxy_x"], "x", False) + term(op.Dyf, S["syy"], S["psi_syy_y"], "y", True)
+        vy2 = op.IFull @ (S["vy"] + gvy * f.iry)
+        vxx = term(op.Dxb, vx2, S["psi_vxx"], "x", False)
+        vyy = term(op.Dyb, vy2, S["psi_vyy"], "y", False)
+        ush = term(f.DyfSX, vx2, S["psi_vxy"], "y", True) + term(op.Dxf, vy2, S["psi_vyx"], "x", True)
+        # the step's adjoint, last operation first: ABS taper, free surface
+        l = {k: dmp * lam[k] for k in names}
+        lvxx, lvyy = np.zeros(n), np.zeros(n)
+        if free_surface:
+            gsH += l["sxx"] * vxx
+            gsV -= l["sxx"] * vyy
+            lvxx += f.scaleH * l["sxx"]
+            lvyy -= f.scaleV * l["sxx"]
+            l["syy"] = l["syy"] * f.fsZero
+        new = {}
+        newpsi = {}
+        # shear stress
+        ls1 = op.IStagX.T @ l["sxy"]
+        new["sxy"] = ls1.copy()
+        gmuXY += ls1 * ush
+        lu = muXY * ls1
+        ld, newpsi["vxy"] = term_t(lu, lpsi["vxy"], "y", True)
+        lvx2 = l["vx"] + f.DyfSX.T @ ld
+        ld, newpsi["vyx"] = term_t(lu, lpsi["vyx"], "x", True)
+        lvy2 = l["vy"] + op.Dxf.T @ ld
+        # normal stresses
+        lx1 = op.IFull.T @ l["sxx"]
+        ly1 = op.IFull.T @ l["syy"]
+        new["sxx"], new["syy"] = lx1.copy(), ly1.copy()
+        lu = lx1 + ly1
+        gM += lu * (vxx + vyy)
+        gmu -= 2.0 * (vyy * lx1 + vxx * ly1)
+        lvxx += M * lu - 2.0 * mu * ly1
+        lvyy += M * lu - 2.0 * mu * lx1
+        ld, newpsi["vxx"] = term_t(lvxx, lpsi["vxx"], "x", False)
+        lvx2 = lvx2 + op.Dxb.T @ ld
+        ld, newpsi["vyy"] = term_t(lvyy, lpsi["vyy"], "y", False)
+        lvy2 = lvy2 + op.Dyb.T @ ld
+        # vy
+        lv1 = op.IFull.T @ lvy2
+        new["vy"] = lv1
+        lg = f.iry * lv1
+        giry += lv1 * gvy
+        ld, newpsi["sxy_x"] = term_t(lg, lpsi["sxy_x"], "x", False)
+        new["sxy"] += op.Dxb.T @ ld
+        ld, newpsi["syy_y"] = term_t(lg, lpsi["syy_y"], "y", True)
+        new["syy"] += op.Dyf.T @ ld
+        # vx
+        lv1 = op.IStagX.T @ lvx2
+        new["vx"] = lv1
+        lg = f.irx * lv1
+        girx += lv1 * gvx
+        ld, newpsi["sxx_x"] = term_t(lg, lpsi["sxx_x"], "x", True)
+        new["sxx"] += op.Dxf.T @ ld
+        ld, newpsi["sxy_y"] = term_t(lg, lpsi["sxy_y"], "y", False)
+        new["sxy"] += f.DybSX.T @ ld
+        lam, lpsi = new, newpsi
+
+    # chain rule: free-surface scales (surface points only), shear average
+    if free_surface:
+        sel = (g.y == 0).astype(np.float64)
+        tt = M - 2.0 * mu
+        gM += sel * (gsV + gsH * (-2.0 * tt / M + tt * tt / (M * M)))
+        gmu += sel * (-2.0 * gsV + gsH * 4.0 * tt / M)
+    ok = muXY >= 4
+    for rows, cols, w in _shear_xy_terms(g):
+        m = mu[cols]
+        dd = np.where(ok[rows] & (m > 1), gmuXY[rows] * muXY[rows] ** 2 * w / (m * m), 0.0)
+        np.add.at(gmu, cols, dd)
+    gvp = gM * 2.0 * rho * vp
+    gvs = gmu * 2.0 * rho * vs
+    grho = gM * vp * vp + gmu * vs * vs
+    for gir, (okp, col) in zip((girx, giry), density_partners(g)):
+        avg = np.where(okp, 0.5 * rho + 0.5 * rho[col], rho)
+        ir = 1.0 / avg
+        w = -gir * ir * ir
+        grho += np.where(okp, 0.5 * w, w)
+        np.add.at(grho, col[okp], 0.5 * w[okp])
+    return J, gvp, gvs, grho

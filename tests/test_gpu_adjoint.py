@@ -125,28 +125,20 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
             assert np.array_equal(a, b)
 
 
-def test_adjoint_rejects_the_elastic_variable_grid(wave, refcpu):
-    """The adjoint on a variable grid (Coordinates.cpp:35-95) is built for the acoustic equations: an
-    elastic variable grid is refused with WAVE_ERR_UNSUPPORTED before any step runs."""
+def test_adjoint_rejects_the_3d_elastic_variable_grid(wave, refcpu):
+    """The adjoint on a variable grid (Coordinates.cpp:35-95) is built for the acoustic equations and
+    2-D elastic: a 3-D elastic variable grid is refused with WAVE_ERR_UNSUPPORTED before any step
+    runs."""
     import ctypes
 
-    from oracle import vargrid
-    grid = [(0, 1, 4), (31, 3, 6), (70, 1, 4)]
-    nx, ny, dh, vmax = 122, 100, 5.0, 3200.0
-    dt = 0.3 * dh / (vmax * np.sqrt(2) * 1.3)
-    ocfg = refcpu.make_config(dimension=2, equation="elastic", NX=nx, NY=ny, NZ=1, DH=dh, DT=dt, T=40 * dt,
-                              spatialFDorder=4, FreeSurface=1, DampingBoundary=2, BoundaryWidth=12, DampingCoeff=8.0,
-                              NPower=4.0, CenterFrequencyCPML=12.0, VMaxCPML=vmax, edgeOrderReduction=1,
-                              useVariableGrid=1, useVariableFDoperators=1, grid=grid)
+    from test_oracle_vargrid_adjoint import vg_case
+    c = vg_case(refcpu, 3, 1, 2, 1, nt=40, equation="elastic")
     cfg = wave.WaveConfig()
-    ctypes.memmove(ctypes.byref(cfg), ctypes.byref(ocfg), ctypes.sizeof(cfg))
-    g = vargrid.VarGrid(nx, ny, 1, dh, [r[0] for r in grid], [r[1] for r in grid])
-    s = wave.Factory.Create("2D", "elastic").initForwardSolver(cfg)
-    s.prepareForModelling(dict(vp=np.full(g.N, 3000.0, np.float32), vs=np.full(g.N, 1700.0, np.float32),
-                               rho=np.full(g.N, 2000.0, np.float32)))
-    s.setSources(np.asarray(g.coordinate2index([g.NX // 2], [3], [0]), np.int64), np.array([1], np.int32),
-                 np.zeros((1, s.nt), np.float32))
-    s.setReceivers(np.asarray(g.coordinate2index([20], [5], [0]), np.int64), np.array([2], np.int32))
+    ctypes.memmove(ctypes.byref(cfg), ctypes.byref(c["cfg"]), ctypes.sizeof(cfg))
+    s = wave.Factory.Create("3D", "elastic").initForwardSolver(cfg)
+    s.prepareForModelling({k: c[k].astype(np.float32) for k in ("vp", "vs", "rho")})
+    s.setSources(c["src_idx"], c["src_type"], c["signals"].astype(np.float32))
+    s.setReceivers(c["rec_idx"][:1], np.array([2], np.int32))
     with pytest.raises(wave.WaveError) as e:
         s.adjoint_gradient(np.zeros((1, s.nt), np.float32))
     assert e.value.code == wave.WAVE_ERR_UNSUPPORTED

@@ -686,7 +686,8 @@ std::string adjoint_supported(const wave_handle* h)
         for (int t : h->hSrcType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez sources only";
     }
-    if (h->vg && c.equation != WAVE_EQ_ACOUSTIC) return "the adjoint gradient on a variable grid is implemented for the acoustic equations";
+    if (h->vg && c.equation != WAVE_EQ_ACOUSTIC && !(c.equation == WAVE_EQ_ELASTIC && c.dimension == 2))
+        return "the adjoint gradient on a variable grid is implemented for the acoustic equations and 2-D elastic";
     if (!h->modelSet) return "set the model first";
     if (!h->seis || h->nrec < 1) return "set receivers first";
     return "";
@@ -976,8 +977,7 @@ extern "C" int wave_adjoint_gradient(wave_handle* h, const float* dobs, int dobs
         float* dOut[3];
         for (int k = 0; k < 3; ++k) dOut[k] = grad_mem == WAVE_MEM_DEVICE ? out[k] : dev(N);
         if (h->vg) {
-            ck(cudaMemsetAsync(dOut[1], 0, N * sizeof(float), h->stream), "memset");
-            vargrid_adjoint(h, dDobs, checkpoint_every, misfit, dOut[0], dOut[2]);
+            vargrid_adjoint(h, dDobs, checkpoint_every, misfit, dOut[0], dOut[1], dOut[2]);
         } else {
             AdjStepper S;
             S.stream = h->stream;

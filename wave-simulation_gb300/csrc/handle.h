@@ -147,10 +147,11 @@ void vargrid_setup(wave_handle* h, const VarGridHost& G);
 // vs: the S-wave velocity of the 2-D elastic step (null for the acoustic step)
 void vargrid_set_model(wave_handle* h, const float* rho, const float* vp, const float* vs);
 int vargrid_launch_step(wave_handle* h, bool dep, cudaEvent_t* mid, bool* srcrecDone);
-// the adjoint gradient of an acoustic variable-grid handle: forward with a
-// checkpoint every K steps, residuals of dobs (device, nrec x NT), backward
-// sweep; gvp, grho (device, N) receive dJ/dvp, dJ/drho
-void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* grho);
+// the adjoint gradient of an acoustic or 2-D elastic variable-grid handle:
+// forward with a checkpoint every K steps, residuals of dobs (device, nrec x
+// NT), backward sweep; gvp, gvs, grho (device, N) receive dJ/dvp, dJ/dvs
+// (zero for the acoustic step), dJ/drho
+void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* gvs, float* grho);
 
 // wavefield decomposition (decompose.cu): the copy of the fields before a
 // step, and the two kernels after it (returns the kernel count)

@@ -772,8 +772,9 @@ int wave_set_model(wave_handle* h, const float* rho, const float* vp, const floa
         float* dTs = visco ? stage(h, taus, n, mem, tmp) : nullptr;
         if (h->vg) {
             wave::vargrid_set_model(h, dRho, dVp, dVs);
-            if (eq == WAVE_EQ_ACOUSTIC)   // rho and vp for the adjoint's chain rule
-                for (auto [slot, src] : {std::pair<int, const float*>{M_RHO, dRho}, {M_VP, dVp}}) {
+            // rho, vp [, vs] for the adjoint's chain rule
+            for (auto [slot, src] : {std::pair<int, const float*>{M_RHO, dRho}, {M_VP, dVp}, {M_VS, dVs}})
+                if (src) {
                     if (!h->m[slot]) h->m[slot] = h->alloc<float>(h->N);
                     h->check(cudaMemcpyAsync(h->m[slot], src, n * sizeof(float), cudaMemcpyDeviceToDevice, s), "copy");
                 }

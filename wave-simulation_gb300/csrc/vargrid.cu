@@ -33,6 +33,7 @@
 //   vg_interp sxx, syy [, szz] (Full), sxy (StaggeredX) [, sxz (StaggeredXZ),
 //             syz (StaggeredZ)]
 #include <algorithm>
+#include <functional>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -1096,7 +1097,7 @@ void build_transposes(wave_handle* h)
     VarGridDev& G = *h->vg;
     if (G.transposed) return;
     const long long N = G.N;
-    for (int op = 0; op < 6; ++op) {
+    for (int op = 0; op < 10; ++op) {
         if (!G.col[op] || G.W[op] == 0) continue;
         const int W = G.W[op];
         std::vector<int> col(static_cast<size_t>(W) * N);
@@ -1192,45 +1193,41 @@ void interp_transpose(wave_handle* h, const int* kinds, float* const* fields, in
     vga_interp_t<<<grid, 256, 0, h->stream>>>(I, 1);
 }
 
-} // namespace
-
-void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* grho)
-{
-    build_transposes(h);
-    const VarGridDev& G = *h->vg;
-    cudaStream_t st = h->stream;
-    const long long N = G.N;
-    const int NT = h->NT;
-    const int na = G.is3d ? 3 : 2;
-    const VgParams P = params_of(h);
-    const bool cp = P.cpml != 0;
-
+// device buffers of one adjoint call, freed when it returns
+struct AdjPool {
+    wave_handle* h;
     std::vector<void*> bufs;
-    struct Free {
-        std::vector<void*>& v;
-        ~Free() { for (void* p : v) cudaFree(p); }
-    } freeBufs{bufs};
-    auto dev = [&](size_t count) {
+    ~AdjPool() { for (void* p : bufs) cudaFree(p); }
+    template <class T = float>
+    T* get(size_t count)
+    {
         void* p = nullptr;
-        h->check(cudaMalloc(&p, (count > 0 ? count : 1) * sizeof(float)), "cudaMalloc");
+        h->check(cudaMalloc(&p, (count > 0 ? count : 1) * sizeof(T)), "cudaMalloc");
         bufs.push_back(p);
-        return static_cast<float*>(p);
-    };
-    auto zero = [&](float* p, size_t count) { h->check(cudaMemsetAsync(p, 0, count * sizeof(float), st), "memset"); };
+        return static_cast<T*>(p);
+    }
+    float* zeros(size_t count)
+    {
+        float* p = get(count);
+        h->check(cudaMemsetAsync(p, 0, (count > 0 ? count : 1) * sizeof(float), h->stream), "memset");
+        return p;
+    }
+};
 
-    // state parts: p, vx, vy [, vz] and the CPML memory variables
-    std::vector<float*> parts = {P.p, P.vx, P.vy};
-    if (G.is3d) parts.push_back(P.vz);
-    const int psiP[3] = {0, 1, 2}, psiV[3] = {3, 4, 5};
-    if (cp)
-        for (int a = 0; a < na; ++a) {
-            parts.push_back(P.psi[psiP[a]]);
-            parts.push_back(P.psi[psiV[a]]);
-        }
+// The sweep both variable-grid adjoints share: the forward from a zero state
+// with a copy of the state parts every K steps, the residuals and misfit,
+// then per checkpoint segment the recomputed states and back(n, state n) for
+// n from the segment's last step down to its first.
+void adjoint_sweep(wave_handle* h, AdjPool& pool, const std::vector<float*>& parts, const float* dobs, int K, double* misfit,
+                   float* res, const std::function<void(int, const float*)>& back)
+{
+    cudaStream_t st = h->stream;
+    const long long N = h->vg->N;
+    const int NT = h->NT;
     const size_t S = parts.size();
     const int nck = (NT + K - 1) / K;
-    float* ckpt = dev(static_cast<size_t>(nck) * S * N);
-    float* view = dev(static_cast<size_t>(K) * S * N);
+    float* ckpt = pool.get(static_cast<size_t>(nck) * S * N);
+    float* view = pool.get(static_cast<size_t>(K) * S * N);
     auto save = [&](float* dst) {
         for (size_t k = 0; k < S; ++k)
             h->check(cudaMemcpyAsync(dst + k * N, parts[k], N * sizeof(float), cudaMemcpyDeviceToDevice, st), "state copy");
@@ -1239,24 +1236,54 @@ void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, f
         for (size_t k = 0; k < S; ++k)
             h->check(cudaMemcpyAsync(parts[k], src + k * N, N * sizeof(float), cudaMemcpyDeviceToDevice, st), "state copy");
     };
-
-    // 1. forward with checkpoints from a zero state
-    for (float* f : parts) zero(f, N);
+    for (float* f : parts) h->check(cudaMemsetAsync(f, 0, N * sizeof(float), st), "memset");
     launch_set_counter(h->tcounter, 0, st);
     for (int n = 0; n < NT; ++n) {
         if (n % K == 0) save(ckpt + static_cast<size_t>(n / K) * S * N);
         step_once(h);
     }
-    // 2. residuals and misfit
     const long long nd = static_cast<long long>(h->nrec) * NT;
-    float* res = dev(nd);
-    double* dMis = nullptr;
-    h->check(cudaMalloc(&dMis, sizeof(double)), "cudaMalloc");
-    bufs.push_back(dMis);
+    double* dMis = pool.get<double>(1);
     h->check(cudaMemsetAsync(dMis, 0, sizeof(double), st), "memset");
     vga_residual<<<256, 256, 0, st>>>(h->seis, dobs, res, nd, dMis);
+    for (int seg = nck - 1; seg >= 0; --seg) {
+        const int n0 = seg * K, n1 = n0 + K < NT ? n0 + K : NT;
+        restore(ckpt + static_cast<size_t>(seg) * S * N);
+        launch_set_counter(h->tcounter, n0, st);
+        for (int n = n0; n < n1; ++n) {
+            save(view + static_cast<size_t>(n - n0) * S * N);
+            if (n + 1 < n1) step_once(h);
+        }
+        for (int n = n1 - 1; n >= n0; --n) back(n, view + static_cast<size_t>(n - n0) * S * N);
+        h->check(cudaGetLastError(), "variable grid adjoint");
+    }
+    double J = 0.0;
+    h->check(cudaMemcpyAsync(&J, dMis, sizeof(double), cudaMemcpyDeviceToHost, st), "misfit");
+    h->check(cudaStreamSynchronize(st), "variable grid adjoint");
+    *misfit = J;
+    h->stepsSinceReset = NT;
+}
 
-    // 3. backward sweep
+void adjoint_acoustic(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* grho)
+{
+    const VarGridDev& G = *h->vg;
+    cudaStream_t st = h->stream;
+    const long long N = G.N;
+    const int NT = h->NT;
+    const int na = G.is3d ? 3 : 2;
+    const VgParams P = params_of(h);
+    const bool cp = P.cpml != 0;
+    AdjPool pool{h};
+
+    // state parts: p, vx, vy [, vz] and the CPML memory variables
+    std::vector<float*> parts = {P.p, P.vx, P.vy};
+    if (G.is3d) parts.push_back(P.vz);
+    if (cp)
+        for (int a = 0; a < na; ++a) {
+            parts.push_back(P.psi[a]);        // p_x, p_y, p_z
+            parts.push_back(P.psi[3 + a]);    // vxx, vyy, vzz
+        }
+
     VgAdj A{};
     A.N = N;
     A.nSurface = G.nSurface;
@@ -1279,8 +1306,7 @@ void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, f
         A.ir[a] = P.ir[a];
     }
     const size_t nAdj = 1 + na + (cp ? 2 * na : 0);
-    float* adj = dev(nAdj * N);
-    zero(adj, nAdj * N);
+    float* adj = pool.zeros(nAdj * N);
     A.lp = adj;
     for (int a = 0; a < na; ++a) {
         A.lv[a] = adj + (1 + a) * N;
@@ -1289,7 +1315,7 @@ void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, f
             A.lpsiV[a] = adj + (2 + na + 2 * a) * N;
         }
     }
-    float* tmp = dev((5 * na + 3) * static_cast<size_t>(N));
+    float* tmp = pool.get((5 * na + 2) * static_cast<size_t>(N));
     for (int a = 0; a < na; ++a) {
         A.gx[a] = tmp + a * N;
         A.v2[a] = tmp + (na + a) * N;
@@ -1299,60 +1325,419 @@ void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, f
     }
     A.d = tmp + 5 * na * N;
     A.lp3 = tmp + (5 * na + 1) * N;
-    A.gM = tmp + (5 * na + 2) * N;
-    float* gir = dev(static_cast<size_t>(na) * N);
-    zero(gir, static_cast<size_t>(na) * N);
-    zero(A.gM, N);
+    A.gM = pool.zeros(N);
+    float* gir = pool.zeros(static_cast<size_t>(na) * N);
     for (int a = 0; a < na; ++a) A.gir[a] = gir + a * N;
-    const long long nRows = static_cast<long long>(G.nInterp[0]) + G.nInterp[1] + G.nInterp[2];
-    float* itmp = dev(static_cast<size_t>(nRows > 0 ? nRows : 1));
+    float* itmp = pool.get(3 * static_cast<size_t>(G.nInterp[0] + G.nInterp[1] + G.nInterp[2] + 1));
+    float* res = pool.get(static_cast<size_t>(h->nrec) * NT);
 
     const dim3 grid(static_cast<unsigned>((N + 255) / 256)), block(256);
     const int velKinds[3] = {1, 0, 2};   // vx StaggeredX, vy Full, vz StaggeredZ
     const int presKind[1] = {0};
-    for (int seg = nck - 1; seg >= 0; --seg) {
-        const int n0 = seg * K, n1 = n0 + K < NT ? n0 + K : NT;
-        restore(ckpt + static_cast<size_t>(seg) * S * N);
-        launch_set_counter(h->tcounter, n0, st);
-        for (int n = n0; n < n1; ++n) {
-            save(view + static_cast<size_t>(n - n0) * S * N);
-            if (n + 1 < n1) step_once(h);
+    adjoint_sweep(h, pool, parts, dobs, K, misfit, res, [&](int n, const float* sv) {
+        A.p = sv;
+        for (int a = 0; a < na; ++a) {
+            A.v[a] = sv + (1 + a) * N;
+            A.psiP[a] = cp ? sv + (1 + na + 2 * a) * N : nullptr;
+            A.psiV[a] = cp ? sv + (2 + na + 2 * a) * N : nullptr;
         }
-        for (int n = n1 - 1; n >= n0; --n) {
-            const float* sv = view + static_cast<size_t>(n - n0) * S * N;
-            A.p = sv;
-            for (int a = 0; a < na; ++a) A.v[a] = sv + (1 + a) * N;
-            for (int a = 0; a < na; ++a) {
-                A.psiP[a] = cp ? sv + (1 + na + 2 * a) * N : nullptr;
-                A.psiV[a] = cp ? sv + (2 + na + 2 * a) * N : nullptr;
-            }
-            vga_inject<<<(h->nrec + 127) / 128, 128, 0, st>>>(A, h->nrec, NT, n, h->ridx, h->rtype, res);
-            vga_fwd_vel<<<grid, block, 0, st>>>(A);
-            float* v2f[3] = {A.v2[0], A.v2[1], na == 3 ? A.v2[2] : nullptr};
-            interp_apply(h, velKinds, v2f, 3);
-            vga_fwd_div<<<grid, block, 0, st>>>(A);
-            vga_surface<<<grid, block, 0, st>>>(A);
-            float* lp3f[1] = {A.lp3};
-            interp_transpose(h, presKind, lp3f, 1, itmp);
-            vga_pres<<<grid, block, 0, st>>>(A);
-            vga_div_t<<<grid, block, 0, st>>>(A);
-            float* lvf[3] = {A.lv[0], A.lv[1], na == 3 ? A.lv[2] : nullptr};
-            interp_transpose(h, velKinds, lvf, 3, itmp);
-            vga_vel<<<grid, block, 0, st>>>(A);
-            vga_grad_t<<<grid, block, 0, st>>>(A);
-        }
-        h->check(cudaGetLastError(), "variable grid adjoint");
-    }
-    // 4. chain rule
-    zero(grho, N);
+        vga_inject<<<(h->nrec + 127) / 128, 128, 0, st>>>(A, h->nrec, NT, n, h->ridx, h->rtype, res);
+        vga_fwd_vel<<<grid, block, 0, st>>>(A);
+        float* v2f[3] = {A.v2[0], A.v2[1], na == 3 ? A.v2[2] : nullptr};
+        interp_apply(h, velKinds, v2f, 3);
+        vga_fwd_div<<<grid, block, 0, st>>>(A);
+        vga_surface<<<grid, block, 0, st>>>(A);
+        float* lp3f[1] = {A.lp3};
+        interp_transpose(h, presKind, lp3f, 1, itmp);
+        vga_pres<<<grid, block, 0, st>>>(A);
+        vga_div_t<<<grid, block, 0, st>>>(A);
+        float* lvf[3] = {A.lv[0], A.lv[1], na == 3 ? A.lv[2] : nullptr};
+        interp_transpose(h, velKinds, lvf, 3, itmp);
+        vga_vel<<<grid, block, 0, st>>>(A);
+        vga_grad_t<<<grid, block, 0, st>>>(A);
+    });
+    h->check(cudaMemsetAsync(grho, 0, N * sizeof(float), st), "memset");
     vga_chain<<<grid, block, 0, st>>>(A, h->m[M_RHO], h->m[M_VP], G.partner[0], G.partner[1], G.is3d ? G.partner[2] : nullptr,
                                       gvp, grho);
     h->check(cudaGetLastError(), "variable grid adjoint");
-    double J = 0.0;
-    h->check(cudaMemcpyAsync(&J, dMis, sizeof(double), cudaMemcpyDeviceToHost, st), "misfit");
     h->check(cudaStreamSynchronize(st), "variable grid adjoint");
-    *misfit = J;
-    h->stepsSinceReset = NT;
+}
+
+// ---- 2-D elastic (vge_vel, the velocity interpolations, vge_str with the
+// free-surface exchange, the stress interpolations, the ABS taper, sources
+// and receivers: FD2Delastic::run, ForwardSolver2Delastic.cpp:117-297)
+
+struct VgeAdj {
+    long long N, nSurface;
+    int fs, cpml;
+    // state n: vx, vy; sxx, syy, sxy; its CPML memory variables
+    const float* v[2];
+    const float* s[3];
+    const float* psi[Q_COUNT];
+    // forward intermediates re-formed from state n
+    float* gv[2];               // the velocity updates' derivative sums with CPML
+    float* v2[2];               // updated velocities (interpolated in place)
+    float* e[3];                // vxx, vyy with CPML; the shear sum vxy + vyx
+    // adjoint state (vx, vy; sxx, syy, sxy; memory variables) and temporaries
+    float* lv[2];
+    float* ls[3];
+    float* lpsi[Q_COUNT];
+    float* lfs[2];              // the surface exchange's adjoint onto vxx, vyy
+    float* ld[4];               // adjoints of the raw derivative terms of one pass
+    float* gM;
+    float* gmu;
+    float* gmuXY;
+    float* gir[2];
+    float* gsH;
+    float* gsV;
+    const float* M;
+    const float* mu;
+    const float* muXY;
+    const float* ir[2];
+    const float* damp;
+    const int* col[8];
+    const float* val[8];
+    int W[8];
+    const int* colT[8];
+    const float* valT[8];
+    int WT[8];
+    const unsigned short* cpc[2];
+    const float* cpt[2];
+};
+
+__device__ __forceinline__ bool vge_adj_cpml(const VgeAdj& A, int axis, bool half, long long i, float& a, float& b)
+{
+    if (!A.cpml) return false;
+    const unsigned code = A.cpc[axis][i];
+    if (code == 0) return false;
+    a = A.cpt[axis][4 * code + (half ? 2 : 0)];
+    b = A.cpt[axis][4 * code + (half ? 3 : 1)];
+    return a != 0.0f || b != 0.0f;
+}
+
+// one derivative term of the forward step from state n: operator row and CPML
+__device__ __forceinline__ float vge_fwd_term(const VgeAdj& A, int op, const float* u, int slot, int axis, bool half, long long i)
+{
+    float d = ell_gather(A.col[op], A.val[op], A.W[op], A.N, i, u);
+    float a, b;
+    if (vge_adj_cpml(A, axis, half, i, a, b)) d = __fadd_rn(d, __fadd_rn(__fmul_rn(A.psi[slot][i], b), __fmul_rn(a, d)));
+    return d;
+}
+
+// the transposed CPML of one term: the adjoint of the raw derivative, and
+// the memory variable's adjoint carried to the step before
+__device__ __forceinline__ float vge_term_t(const VgeAdj& A, float l, int slot, int axis, bool half, long long i)
+{
+    float a, b;
+    if (!vge_adj_cpml(A, axis, half, i, a, b)) return l;
+    const float tot = A.lpsi[slot][i] + l;
+    A.lpsi[slot][i] = b * tot;
+    return l + a * tot;
+}
+
+__global__ void __launch_bounds__(256) vgea_fwd_vel(VgeAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    float d = vge_fwd_term(A, O_DXF, A.s[0], Q_SXX_X, 0, true, i);
+    d = __fadd_rn(d, vge_fwd_term(A, O_DYB_SX, A.s[2], Q_SXY_Y, 1, false, i));
+    A.gv[0][i] = d;
+    A.v2[0][i] = __fadd_rn(A.v[0][i], __fmul_rn(d, A.ir[0][i]));
+    d = vge_fwd_term(A, O_DXB, A.s[2], Q_SXY_X, 0, false, i);
+    d = __fadd_rn(d, vge_fwd_term(A, O_DYF, A.s[1], Q_SYY_Y, 1, true, i));
+    A.gv[1][i] = d;
+    A.v2[1][i] = __fadd_rn(A.v[1][i], __fmul_rn(d, A.ir[1][i]));
+}
+
+__global__ void __launch_bounds__(256) vgea_fwd_str(VgeAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    A.e[0][i] = vge_fwd_term(A, O_DXB, A.v2[0], Q_VXX, 0, false, i);
+    A.e[1][i] = vge_fwd_term(A, O_DYB, A.v2[1], Q_VYY, 1, false, i);
+    A.e[2][i] = __fadd_rn(vge_fwd_term(A, O_DYF_SX, A.v2[0], Q_VXY, 1, true, i), vge_fwd_term(A, O_DXF, A.v2[1], Q_VYX, 0, true, i));
+}
+
+// receivers: pressure (type 1) reads (sxx + syy) / 2, types 2 and 3 vx, vy
+__global__ void vgea_inject(VgeAdj A, int nrec, int nt, int n, const long long* __restrict__ ridx, const int* __restrict__ rtype,
+                            const float* __restrict__ res)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const float v = res[static_cast<long long>(r) * nt + n];
+    const long long i = ridx[r];
+    const int t = rtype[r];
+    if (t == 1) {
+        atomicAdd(A.ls[0] + i, 0.5f * v);
+        atomicAdd(A.ls[1] + i, 0.5f * v);
+    } else if (t == 2 || t == 3) {
+        atomicAdd(A.lv[t - 2] + i, v);
+    }
+}
+
+// transposed ABS taper and free-surface exchange (FreeSurface2Delastic.cpp:14-40)
+__global__ void __launch_bounds__(256) vgea_abs_fs(VgeAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    if (A.damp) {
+        const float d = A.damp[i];
+        A.lv[0][i] *= d;
+        A.lv[1][i] *= d;
+        for (int k = 0; k < 3; ++k) A.ls[k][i] *= d;
+    }
+    float fx = 0.0f, fy = 0.0f;
+    if (A.fs && i < A.nSurface) {
+        const float M = A.M[i], t = M - 2.0f * A.mu[i];
+        const float sH = -(t * t) / M;
+        const float l = A.ls[0][i];
+        A.gsH[i] += l * A.e[0][i];
+        A.gsV[i] -= l * A.e[1][i];
+        fx = sH * l;
+        fy = -t * l;
+        A.ls[1][i] = 0.0f;
+    }
+    A.lfs[0][i] = fx;
+    A.lfs[1][i] = fy;
+}
+
+// transposed stress updates and their CPML (after the stress interpolations' transposes)
+__global__ void __launch_bounds__(256) vgea_str(VgeAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    const float l3 = A.ls[2][i];
+    A.gmuXY[i] += l3 * A.e[2][i];
+    const float lu = A.muXY[i] * l3;
+    A.ld[0][i] = vge_term_t(A, lu, Q_VXY, 1, true, i);
+    A.ld[1][i] = vge_term_t(A, lu, Q_VYX, 0, true, i);
+    const float lx = A.ls[0][i], ly = A.ls[1][i], vxx = A.e[0][i], vyy = A.e[1][i];
+    const float l2 = lx + ly, M = A.M[i], mu = A.mu[i];
+    A.gM[i] += l2 * (vxx + vyy);
+    A.gmu[i] -= 2.0f * (vyy * lx + vxx * ly);
+    A.ld[2][i] = vge_term_t(A, M * l2 - 2.0f * mu * ly + A.lfs[0][i], Q_VXX, 0, false, i);
+    A.ld[3][i] = vge_term_t(A, M * l2 - 2.0f * mu * lx + A.lfs[1][i], Q_VYY, 1, false, i);
+}
+
+// lvx += DyfSX^T ld0 + Dxb^T ld2, lvy += Dxf^T ld1 + Dyb^T ld3
+__global__ void __launch_bounds__(256) vgea_str_t(VgeAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    A.lv[0][i] += ell_gather(A.colT[O_DYF_SX], A.valT[O_DYF_SX], A.WT[O_DYF_SX], A.N, i, A.ld[0]) +
+                  ell_gather(A.colT[O_DXB], A.valT[O_DXB], A.WT[O_DXB], A.N, i, A.ld[2]);
+    A.lv[1][i] += ell_gather(A.colT[O_DXF], A.valT[O_DXF], A.WT[O_DXF], A.N, i, A.ld[1]) +
+                  ell_gather(A.colT[O_DYB], A.valT[O_DYB], A.WT[O_DYB], A.N, i, A.ld[3]);
+}
+
+// transposed velocity updates and their CPML (after the velocity interpolations' transposes)
+__global__ void __launch_bounds__(256) vgea_vel(VgeAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    const float ly = A.lv[1][i];
+    A.gir[1][i] += ly * A.gv[1][i];
+    const float gy = A.ir[1][i] * ly;
+    A.ld[2][i] = vge_term_t(A, gy, Q_SXY_X, 0, false, i);
+    A.ld[3][i] = vge_term_t(A, gy, Q_SYY_Y, 1, true, i);
+    const float lx = A.lv[0][i];
+    A.gir[0][i] += lx * A.gv[0][i];
+    const float gx = A.ir[0][i] * lx;
+    A.ld[0][i] = vge_term_t(A, gx, Q_SXX_X, 0, true, i);
+    A.ld[1][i] = vge_term_t(A, gx, Q_SXY_Y, 1, false, i);
+}
+
+// lsxx += Dxf^T ld0, lsyy += Dyf^T ld3, lsxy += Dxb^T ld2 + DybSX^T ld1
+__global__ void __launch_bounds__(256) vgea_vel_t(VgeAdj A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    A.ls[0][i] += ell_gather(A.colT[O_DXF], A.valT[O_DXF], A.WT[O_DXF], A.N, i, A.ld[0]);
+    A.ls[1][i] += ell_gather(A.colT[O_DYF], A.valT[O_DYF], A.WT[O_DYF], A.N, i, A.ld[3]);
+    A.ls[2][i] += ell_gather(A.colT[O_DXB], A.valT[O_DXB], A.WT[O_DXB], A.N, i, A.ld[2]) +
+                  ell_gather(A.colT[O_DYB_SX], A.valT[O_DYB_SX], A.WT[O_DYB_SX], A.N, i, A.ld[1]);
+}
+
+// chain rule, first half: the surface scales' sensitivities (scaleV = M - 2 mu,
+// scaleH = -(M - 2 mu)^2 / M), the XY shear average's (vge_shear: 1 / the
+// weighted mean of 1 / max(mu, 1), zero below 4) scattered onto its points,
+// the inverse density averages' onto rho; gMt receives the point's dJ/dM,
+// gmuT (zeroed) and grho (zeroed) the scattered sums
+__global__ void __launch_bounds__(256) vgea_chain1(VgeAdj A, const float* __restrict__ rho, const int* __restrict__ px,
+                                                   const int* __restrict__ py, const int* __restrict__ s1, const int* __restrict__ s2,
+                                                   const int* __restrict__ s3, float* gMt, float* gmuT, float* grho)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    float g = A.gM[i], gm = A.gmu[i];
+    if (A.fs && i < A.nSurface) {
+        const float M = A.M[i], t = M - 2.0f * A.mu[i];
+        const float sH = A.gsH[i], sV = A.gsV[i];
+        g += sV + sH * (-2.0f * t / M + t * t / (M * M));
+        gm += -2.0f * sV + sH * 4.0f * t / M;
+    }
+    gMt[i] = g;
+    atomicAdd(gmuT + i, gm);
+    const float mxy = A.muXY[i];
+    if (mxy >= 4.0f) {
+        const float coef = A.gmuXY[i] * mxy * mxy;
+        const int a = s1[i], b = s2[i], c = s3[i];
+        const int ii = static_cast<int>(i);
+        int pts[4];
+        float w[4];
+        int np = 0;
+        if (a >= 0 && b >= 0) {
+            pts[0] = ii; pts[1] = a; pts[2] = b; pts[3] = c >= 0 ? c : ii;
+            w[0] = w[1] = w[2] = w[3] = 0.25f;
+            np = 4;
+        } else if (a >= 0 || b >= 0) {
+            pts[0] = a >= 0 ? a : b; pts[1] = ii;
+            w[0] = w[1] = 0.5f;
+            np = 2;
+        } else {
+            pts[0] = ii;
+            w[0] = 1.0f;
+            np = 1;
+        }
+        for (int k = 0; k < np; ++k) {
+            const float m = A.mu[pts[k]];
+            if (m > 1.0f) atomicAdd(gmuT + pts[k], coef * w[k] / (m * m));
+        }
+    }
+    const int* part[2] = {px, py};
+    float own = 0.0f;
+    for (int ax = 0; ax < 2; ++ax) {
+        const float r = A.ir[ax][i];
+        const float wv = -A.gir[ax][i] * r * r;
+        const int j = part[ax][i];
+        if (j >= 0) {
+            own += 0.5f * wv;
+            atomicAdd(grho + j, 0.5f * wv);
+        } else {
+            own += wv;
+        }
+    }
+    atomicAdd(grho + i, own);
+}
+
+// chain rule, second half: M = rho vp^2, mu = rho vs^2
+__global__ void __launch_bounds__(256) vgea_chain2(long long N, const float* __restrict__ rho, const float* __restrict__ vp,
+                                                   const float* __restrict__ vs, const float* __restrict__ gMt,
+                                                   const float* __restrict__ gmuT, float* gvp, float* gvs, float* grho)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float g = gMt[i], gm = gmuT[i];
+    gvp[i] = g * 2.0f * rho[i] * vp[i];
+    gvs[i] = gm * 2.0f * rho[i] * vs[i];
+    grho[i] += g * vp[i] * vp[i] + gm * vs[i] * vs[i];
+}
+
+void adjoint_elastic2d(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* gvs, float* grho)
+{
+    const VarGridDev& G = *h->vg;
+    cudaStream_t st = h->stream;
+    const long long N = G.N;
+    const int NT = h->NT;
+    const VgeParams E = elastic_params_of(h);
+    const bool cp = G.cpCode[0] != nullptr;
+    AdjPool pool{h};
+    const int psiSlots[8] = {Q_SXX_X, Q_SXY_Y, Q_SXY_X, Q_SYY_Y, Q_VXX, Q_VYY, Q_VXY, Q_VYX};
+    std::vector<float*> parts = {E.v[0], E.v[1], E.s[0], E.s[1], E.s[3]};
+    if (cp)
+        for (int q : psiSlots) parts.push_back(E.psi[q]);
+
+    VgeAdj A{};
+    A.N = N;
+    A.nSurface = G.nSurface;
+    A.fs = G.fs;
+    A.cpml = cp ? 1 : 0;
+    A.M = E.M;
+    A.mu = E.mu;
+    A.muXY = E.muS[0];
+    A.ir[0] = E.ir[0];
+    A.ir[1] = E.ir[1];
+    A.damp = G.absDamp;
+    for (int k = 0; k < 8; ++k) {
+        A.col[k] = G.col[k];
+        A.val[k] = G.val[k];
+        A.W[k] = G.W[k];
+        A.colT[k] = G.colT[k];
+        A.valT[k] = G.valT[k];
+        A.WT[k] = G.WT[k];
+    }
+    for (int a = 0; a < 2; ++a) {
+        A.cpc[a] = G.cpCode[a];
+        A.cpt[a] = G.cpTab[a];
+    }
+    float* adj = pool.zeros((5 + (cp ? 8 : 0)) * static_cast<size_t>(N));
+    for (int k = 0; k < 2; ++k) A.lv[k] = adj + k * N;
+    for (int k = 0; k < 3; ++k) A.ls[k] = adj + (2 + k) * N;
+    if (cp)
+        for (int k = 0; k < 8; ++k) A.lpsi[psiSlots[k]] = adj + (5 + k) * N;
+    float* tmp = pool.get(13 * static_cast<size_t>(N));
+    for (int k = 0; k < 2; ++k) {
+        A.gv[k] = tmp + k * N;
+        A.v2[k] = tmp + (2 + k) * N;
+        A.lfs[k] = tmp + (4 + k) * N;
+    }
+    for (int k = 0; k < 3; ++k) A.e[k] = tmp + (6 + k) * N;
+    for (int k = 0; k < 4; ++k) A.ld[k] = tmp + (9 + k) * N;
+    float* sums = pool.zeros(7 * static_cast<size_t>(N));
+    A.gM = sums;
+    A.gmu = sums + N;
+    A.gmuXY = sums + 2 * N;
+    A.gir[0] = sums + 3 * N;
+    A.gir[1] = sums + 4 * N;
+    A.gsH = sums + 5 * N;
+    A.gsV = sums + 6 * N;
+    float* itmp = pool.get(3 * static_cast<size_t>(G.nInterp[0] + G.nInterp[1] + G.nInterp[2] + 1));
+    float* res = pool.get(static_cast<size_t>(h->nrec) * NT);
+
+    const dim3 grid(static_cast<unsigned>((N + 255) / 256)), block(256);
+    const int velKinds[2] = {1, 0};      // vx StaggeredX, vy Full
+    const int strKinds[3] = {0, 0, 1};   // sxx, syy Full, sxy StaggeredX
+    adjoint_sweep(h, pool, parts, dobs, K, misfit, res, [&](int n, const float* sv) {
+        A.v[0] = sv;
+        A.v[1] = sv + N;
+        for (int k = 0; k < 3; ++k) A.s[k] = sv + (2 + k) * N;
+        for (int k = 0; k < 8; ++k) A.psi[psiSlots[k]] = cp ? sv + (5 + k) * N : nullptr;
+        vgea_inject<<<(h->nrec + 127) / 128, 128, 0, st>>>(A, h->nrec, NT, n, h->ridx, h->rtype, res);
+        vgea_fwd_vel<<<grid, block, 0, st>>>(A);
+        float* v2f[2] = {A.v2[0], A.v2[1]};
+        interp_apply(h, velKinds, v2f, 2);
+        vgea_fwd_str<<<grid, block, 0, st>>>(A);
+        vgea_abs_fs<<<grid, block, 0, st>>>(A);
+        float* lsf[3] = {A.ls[0], A.ls[1], A.ls[2]};
+        interp_transpose(h, strKinds, lsf, 3, itmp);
+        vgea_str<<<grid, block, 0, st>>>(A);
+        vgea_str_t<<<grid, block, 0, st>>>(A);
+        float* lvf[2] = {A.lv[0], A.lv[1]};
+        interp_transpose(h, velKinds, lvf, 2, itmp);
+        vgea_vel<<<grid, block, 0, st>>>(A);
+        vgea_vel_t<<<grid, block, 0, st>>>(A);
+    });
+    float* gMt = pool.get(N);
+    float* gmuT = pool.zeros(N);
+    h->check(cudaMemsetAsync(grho, 0, N * sizeof(float), st), "memset");
+    vgea_chain1<<<grid, block, 0, st>>>(A, h->m[M_RHO], G.partner[0], G.partner[1], G.shear[0][0], G.shear[0][1], G.shear[0][2], gMt,
+                                        gmuT, grho);
+    vgea_chain2<<<grid, block, 0, st>>>(N, h->m[M_RHO], h->m[M_VP], h->m[M_VS], gMt, gmuT, gvp, gvs, grho);
+    h->check(cudaGetLastError(), "variable grid adjoint");
+    h->check(cudaStreamSynchronize(st), "variable grid adjoint");
+}
+
+} // namespace
+
+void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* gvs, float* grho)
+{
+    build_transposes(h);
+    if (h->vg->elastic) {
+        adjoint_elastic2d(h, dobs, K, misfit, gvp, gvs, grho);
+        return;
+    }
+    h->check(cudaMemsetAsync(gvs, 0, h->vg->N * sizeof(float), h->stream), "memset");
+    adjoint_acoustic(h, dobs, K, misfit, gvp, grho);
 }
 
 } // namespace wave

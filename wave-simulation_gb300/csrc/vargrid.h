@@ -124,12 +124,12 @@ struct VarGridDev {
     long long nSurface = 0;
     int fs = 0;
     const float* absDamp = nullptr;         // ABS taper per point (null: no ABS)
-    // transposes of Dxf, Dyf, Dzf, Dxb, Dyb, Dzb as ELL blocks (the adjoint;
-    // built at its first call)
+    // transposes of the operators above as ELL blocks (the adjoint; built at
+    // its first call)
     bool transposed = false;
-    int WT[6] = {};
-    const int* colT[6] = {};
-    const float* valT[6] = {};
+    int WT[10] = {};
+    const int* colT[10] = {};
+    const float* valT[10] = {};
     // stencil classes per pass (null: not available)
     const unsigned* clsId[2] = {};
     const int* clsOff[2] = {};
