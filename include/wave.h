@@ -445,9 +445,8 @@ int wave_instantaneous_phase(float* data, int64_t ntr, int64_t nt, int phase_typ
  *  - 3-D EM and visco-EM (FD3Demem::run, ForwardSolver3Demem.cpp:119-237;
  *    FD3Dviscoemem::run, ForwardSolver3Dviscoemem.cpp:161-309, taus fixed)
  *    with CPML, ABS or no damping boundary: the same three outputs;
- * the acoustic equations and 2-D elastic also on a variable grid
- * (useVariableGrid / useVariableFDoperators; vargrid.cu), where a 3-D
- * elastic variable grid returns WAVE_ERR_UNSUPPORTED. Runs the
+ * the acoustic and elastic equations also on a variable grid
+ * (useVariableGrid / useVariableFDoperators; vargrid.cu). Runs the
  * forward over all NT steps from a zero state (the handle's sources and
  * receivers; seismograms are left as computed), saving the state every
  * `checkpoint_every` steps, then the backward sweep, recomputing each

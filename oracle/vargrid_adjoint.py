@@ -1,4 +1,4 @@
-"""Discrete adjoints of the acoustic and 2-D elastic variable-grid steps
+"""Discrete adjoints of the acoustic and elastic variable-grid steps
 (oracle, test infrastructure only: used by tests/ as the checker, never by
 the library).
 
@@ -287,6 +287,178 @@ def elastic_adjoint_gradient_2d(g: VarGrid, orders, DT, rho, vp, vs, cpml, src_i
         avg = np.where(okp, 0.5 * rho + 0.5 * rho[col], rho)
         ir = 1.0 / avg
         w = -gir * ir * ir
+        grho += np.where(okp, 0.5 * w, w)
+        np.add.at(grho, col[okp], 0.5 * w[okp])
+    return J, gvp, gvs, grho
+
+
+def _shear_terms(g: VarGrid, pair: str):
+    """The points and weights of every point's 4-point average of the axis
+    pair (shear_average in oracle/vargrid_elastic.py, Modelparameter.cpp:
+    449-624): a list of (rows, partner columns, weight)."""
+    f = np.array(g.dhf, dtype=np.int64)[g.layer]
+    c = {"x": g.x, "y": g.y, "z": g.z}
+    n = {"x": g.NX, "y": g.NY, "z": g.NZ}
+    a, b = pair[0], pair[1]
+
+    def idx(sel, da, db):
+        p = {k: c[k][sel].copy() for k in "xyz"}
+        p[a] = p[a] + da * f[sel]
+        p[b] = p[b] + db * f[sel]
+        return np.asarray(g.coordinate2index(p["x"], p["y"], p["z"]), np.int64)
+
+    oka, okb = c[a] + f < n[a], c[b] + f < n[b]
+    out = []
+    i = np.nonzero(oka & okb)[0]
+    out += [(i, i, 0.25), (i, idx(i, 1, 0), 0.25), (i, idx(i, 0, 1), 0.25), (i, idx(i, 1, 1), 0.25)]
+    i = np.nonzero(oka & ~okb)[0]
+    out += [(i, i, 0.5), (i, idx(i, 1, 0), 0.5)]
+    i = np.nonzero(~oka & okb)[0]
+    out += [(i, i, 0.5), (i, idx(i, 0, 1), 0.5)]
+    i = np.nonzero(~oka & ~okb)[0]
+    out.append((i, i, 1.0))
+    return out
+
+
+def elastic_adjoint_gradient_3d(g: VarGrid, orders, DT, rho, vp, vs, cpml, src_idx, src_type, signals, rec_idx, rec_type,
+                                dobs, damping=None, free_surface=False, var_order=True, edge=True, var_grid=True):
+    """(J, dJ/dvp, dJ/dvs, dJ/drho) of the 3-D elastic variable-grid run
+    (ElasticVarGrid3D, FD3Delastic::run ForwardSolver3Delastic.cpp:120-414)
+    in FP64, as elastic_adjoint_gradient_2d with the z terms, the XZ and YZ
+    shear averages, the twice-applied StaggeredZ interpolation of syz and the
+    surface exchange of sxx and szz with vxx + vzz (FreeSurface3Delastic.cpp:
+    15-47)."""
+    from oracle.vargrid_elastic import ElasticVarGrid3D
+    rho = np.asarray(rho, np.float64)
+    vp = np.asarray(vp, np.float64)
+    vs = np.asarray(vs, np.float64)
+    f = ElasticVarGrid3D(g, orders, DT, rho, vp, vs, cpml, src_idx, src_type, np.asarray(signals, np.float64), rec_idx,
+                         rec_type, dtype=np.float64, var_order=var_order, edge=edge, var_grid=var_grid,
+                         free_surface=free_surface, damping=damping)
+    nt = np.asarray(signals).shape[1]
+    states, seis = [], np.zeros((len(rec_idx), nt))
+    for t in range(nt):
+        st = {k: v.copy() for k, v in f.f.items()}
+        st.update({"psi_" + k: v.copy() for k, v in f.psi.items()})
+        states.append(st)
+        seis[:, t] = f.step(t)
+    res = seis - np.asarray(dobs, np.float64)
+    J = 0.5 * float(np.sum(res * res))
+
+    op, n, cp = f.op, g.N, cpml
+    IStagZ2 = op.IStagZ @ op.IStagZ
+    vel = {"vx": ([(op.Dxf, "sxx", "sxx_x", "x", True), (f.DybSX, "sxy", "sxy_y", "y", False),
+                   (op.Dzb, "sxz", "sxz_z", "z", False)], f.irx, op.IStagX),
+           "vy": ([(op.Dxb, "sxy", "sxy_x", "x", False), (op.Dyf, "syy", "syy_y", "y", True),
+                   (op.Dzb, "syz", "syz_z", "z", False)], f.iry, op.IFull),
+           "vz": ([(op.Dxb, "sxz", "sxz_x", "x", False), (f.DybSZ, "syz", "syz_y", "y", False),
+                   (op.Dzf, "szz", "szz_z", "z", True)], f.irz, op.IStagZ)}
+    shear = {"sxy": ([(f.DyfSX, "vx", "vxy", "y", True), (op.Dxf, "vy", "vyx", "x", True)], f.muXY, op.IStagX),
+             "sxz": ([(op.Dzf, "vx", "vxz", "z", True), (op.Dxf, "vz", "vzx", "x", True)], f.muXZ, op.IStagXZ),
+             "syz": ([(op.Dzf, "vy", "vyz", "z", True), (f.DyfSZ, "vz", "vzy", "y", True)], f.muYZ, IStagZ2)}
+    normal = {"vx": (op.Dxb, "vxx", "x"), "vy": (op.Dyb, "vyy", "y"), "vz": (op.Dzb, "vzz", "z")}
+
+    def term(D, u, psi, ax, half):
+        d = D @ u
+        if cp is not None:
+            af, bf, ah, bh = cp[ax]
+            a, b = (ah, bh) if half else (af, bf)
+            d = d + (psi * b + a * d)
+        return d
+
+    def term_t(ld, lpsi, ax, half):
+        if cp is None:
+            return ld, np.zeros(n)
+        af, bf, ah, bh = cp[ax]
+        a, b = (ah, bh) if half else (af, bf)
+        tot = lpsi + ld
+        return ld + a * tot, b * tot
+
+    names = list(f.f)
+    lam = {k: np.zeros(n) for k in names}
+    lpsi = {k: np.zeros(n) for k in f.psi}
+    gM, gmu, girx, giry, girz, gsH, gsV = (np.zeros(n) for _ in range(7))
+    gmuS = {k: np.zeros(n) for k in shear}
+    gir = {"vx": girx, "vy": giry, "vz": girz}
+    dmp = np.ones(n) if damping is None else np.asarray(damping, np.float64)
+    M, mu = f.M, f.mu
+    for t in range(nt - 1, -1, -1):
+        S = states[t]
+        for r, (i, k) in enumerate(zip(rec_idx, rec_type)):
+            if k == 1:
+                for c in ("sxx", "syy", "szz"):
+                    lam[c][i] += res[r, t] / 3.0
+            else:
+                lam[("vx", "vy", "vz")[k - 2]][i] += res[r, t]
+        gv, v2 = {}, {}
+        for k, (terms, ir, I) in vel.items():
+            gv[k] = sum(term(D, S[fld], S["psi_" + q], ax, half) for D, fld, q, ax, half in terms)
+            v2[k] = I @ (S[k] + gv[k] * ir)
+        e = {k: term(D, v2[k], S["psi_" + q], ax, False) for k, (D, q, ax) in normal.items()}
+        ush = {k: sum(term(D, v2[fld], S["psi_" + q], ax, half) for D, fld, q, ax, half in terms)
+               for k, (terms, m, I) in shear.items()}
+        l = {k: dmp * lam[k] for k in names}
+        lnorm = {k: np.zeros(n) for k in normal}
+        if free_surface:
+            ls = l["sxx"] + l["szz"]
+            gsH += ls * (e["vx"] + e["vz"])
+            gsV -= ls * e["vy"]
+            lnorm["vx"] += f.scaleH * ls
+            lnorm["vz"] += f.scaleH * ls
+            lnorm["vy"] -= f.scaleV * ls
+            l["syy"] = l["syy"] * f.fsZero
+        new, newpsi = {}, {}
+        lv2 = {k: l[k].copy() for k in ("vx", "vy", "vz")}
+        for k, (terms, m, I) in shear.items():
+            l1 = I.T @ l[k]
+            new[k] = l1.copy()
+            gmuS[k] += l1 * ush[k]
+            lu = m * l1
+            for D, fld, q, ax, half in terms:
+                ld, newpsi[q] = term_t(lu, lpsi[q], ax, half)
+                lv2[fld] = lv2[fld] + D.T @ ld
+        l1 = {c: op.IFull.T @ l[c] for c in ("sxx", "syy", "szz")}
+        for c in l1:
+            new[c] = l1[c].copy()
+        lsum = l1["sxx"] + l1["syy"] + l1["szz"]
+        ex, ey, ez = e["vx"], e["vy"], e["vz"]
+        gM += lsum * (ex + ey + ez)
+        gmu -= 2.0 * ((ey + ez) * l1["sxx"] + (ex + ez) * l1["syy"] + (ex + ey) * l1["szz"])
+        lnorm["vx"] += M * lsum - 2.0 * mu * (l1["syy"] + l1["szz"])
+        lnorm["vy"] += M * lsum - 2.0 * mu * (l1["sxx"] + l1["szz"])
+        lnorm["vz"] += M * lsum - 2.0 * mu * (l1["sxx"] + l1["syy"])
+        for k, (D, q, ax) in normal.items():
+            ld, newpsi[q] = term_t(lnorm[k], lpsi[q], ax, False)
+            lv2[k] = lv2[k] + D.T @ ld
+        for k, (terms, ir, I) in vel.items():
+            lv1 = I.T @ lv2[k]
+            new[k] = lv1
+            lg = ir * lv1
+            gir[k] += lv1 * gv[k]
+            for D, fld, q, ax, half in terms:
+                ld, newpsi[q] = term_t(lg, lpsi[q], ax, half)
+                new[fld] = new[fld] + D.T @ ld
+        lam, lpsi = new, newpsi
+
+    if free_surface:
+        sel = (g.y == 0).astype(np.float64)
+        tt = M - 2.0 * mu
+        gM += sel * (gsV + gsH * (-2.0 * tt / M + tt * tt / (M * M)))
+        gmu += sel * (-2.0 * gsV + gsH * 4.0 * tt / M)
+    for k, pair in (("sxy", "xy"), ("sxz", "xz"), ("syz", "yz")):
+        m = shear[k][1]
+        ok = m >= 4
+        for rows, cols, w in _shear_terms(g, pair):
+            mm = mu[cols]
+            dd = np.where(ok[rows] & (mm > 1), gmuS[k][rows] * m[rows] ** 2 * w / (mm * mm), 0.0)
+            np.add.at(gmu, cols, dd)
+    gvp = gM * 2.0 * rho * vp
+    gvs = gmu * 2.0 * rho * vs
+    grho = gM * vp * vp + gmu * vs * vs
+    for gr, (okp, col) in zip((girx, giry, girz), density_partners(g)):
+        avg = np.where(okp, 0.5 * rho + 0.5 * rho[col], rho)
+        ir = 1.0 / avg
+        w = -gr * ir * ir
         grho += np.where(okp, 0.5 * w, w)
         np.add.at(grho, col[okp], 0.5 * w[okp])
     return J, gvp, gvs, grho

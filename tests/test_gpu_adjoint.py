@@ -125,26 +125,6 @@ def test_checkpoint_interval_does_not_change_the_gradient(wave):
             assert np.array_equal(a, b)
 
 
-def test_adjoint_rejects_the_3d_elastic_variable_grid(wave, refcpu):
-    """The adjoint on a variable grid (Coordinates.cpp:35-95) is built for the acoustic equations and
-    2-D elastic: a 3-D elastic variable grid is refused with WAVE_ERR_UNSUPPORTED before any step
-    runs."""
-    import ctypes
-
-    from test_oracle_vargrid_adjoint import vg_case
-    c = vg_case(refcpu, 3, 1, 2, 1, nt=40, equation="elastic")
-    cfg = wave.WaveConfig()
-    ctypes.memmove(ctypes.byref(cfg), ctypes.byref(c["cfg"]), ctypes.sizeof(cfg))
-    s = wave.Factory.Create("3D", "elastic").initForwardSolver(cfg)
-    s.prepareForModelling({k: c[k].astype(np.float32) for k in ("vp", "vs", "rho")})
-    s.setSources(c["src_idx"], c["src_type"], c["signals"].astype(np.float32))
-    s.setReceivers(c["rec_idx"][:1], np.array([2], np.int32))
-    with pytest.raises(wave.WaveError) as e:
-        s.adjoint_gradient(np.zeros((1, s.nt), np.float32))
-    assert e.value.code == wave.WAVE_ERR_UNSUPPORTED
-    s.close()
-
-
 def test_batched_adjoint_equals_single_shot_adjoints(wave):
     cfg = _config(wave)
     true, start = _models()

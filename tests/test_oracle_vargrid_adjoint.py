@@ -105,8 +105,8 @@ def test_oracle_vargrid_adjoint_matches_fp64_finite_differences(refcpu, dim, fs,
 
 
 def vge_seismograms(c, vp, vs, rho):
-    from oracle.vargrid_elastic import ElasticVarGrid2D
-    sim = ElasticVarGrid2D(c["g"], c["orders"], c["DT"], rho, vp, vs, c["cpml"], c["src_idx"], c["src_type"], c["signals"],
+    from oracle.vargrid_elastic import ElasticVarGrid2D, ElasticVarGrid3D
+    sim = (ElasticVarGrid3D if c["g"].NZ > 1 else ElasticVarGrid2D)(c["g"], c["orders"], c["DT"], rho, vp, vs, c["cpml"], c["src_idx"], c["src_type"], c["signals"],
                            c["rec_idx"], c["rec_type"], dtype=np.float64, edge=c["edge"], free_surface=c["fs"] == 1,
                            damping=c["damping"])
     return sim.run(c["nt"])
@@ -115,21 +115,22 @@ def vge_seismograms(c, vp, vs, rho):
 def vge_observed(c):
     """0.8 x the data of a model with smooth vp and vs anomalies."""
     g = c["g"]
-    blob = np.exp(-((g.x - g.NX * 0.5) ** 2 + (g.y - g.NY * 0.6) ** 2) / 40.0)
+    blob = np.exp(-((g.x - g.NX * 0.5) ** 2 + (g.y - g.NY * 0.6) ** 2 + (g.z - g.NZ * 0.5) ** 2) / 40.0)
     return 0.8 * vge_seismograms(c, c["vp"] * (1 + 0.05 * blob), c["vs"] * (1 - 0.04 * blob), c["rho"])
 
 
 def vge_gradient(c, dobs):
-    from oracle.vargrid_adjoint import elastic_adjoint_gradient_2d
-    return elastic_adjoint_gradient_2d(c["g"], c["orders"], c["DT"], c["rho"], c["vp"], c["vs"], c["cpml"], c["src_idx"],
+    from oracle.vargrid_adjoint import elastic_adjoint_gradient_2d, elastic_adjoint_gradient_3d
+    fn = elastic_adjoint_gradient_3d if c["g"].NZ > 1 else elastic_adjoint_gradient_2d
+    return fn(c["g"], c["orders"], c["DT"], c["rho"], c["vp"], c["vs"], c["cpml"], c["src_idx"],
                                        c["src_type"], c["signals"], c["rec_idx"], c["rec_type"], dobs,
                                        damping=c["damping"], free_surface=c["fs"] == 1, edge=c["edge"])
 
 
-@pytest.mark.parametrize("fs,boundary,edge", [(1, 2, 1), (0, 1, 0), (1, 0, 1), (0, 2, 1)])
-def test_oracle_elastic_vargrid_adjoint_matches_fp64_finite_differences(refcpu, fs, boundary, edge):
-    c = vg_case(refcpu, 2, fs, boundary, edge, nt=160, equation="elastic")
-    c["rec_type"] = np.where(c["rec_type"] > 3, 2, c["rec_type"]).astype(np.int32)
+@pytest.mark.parametrize("dim,fs,boundary,edge", [(2, 1, 2, 1), (2, 0, 1, 0), (2, 1, 0, 1), (2, 0, 2, 1), (3, 1, 2, 1),
+                                                 (3, 0, 1, 1)])
+def test_oracle_elastic_vargrid_adjoint_matches_fp64_finite_differences(refcpu, dim, fs, boundary, edge):
+    c = vg_case(refcpu, dim, fs, boundary, edge, nt=160 if dim == 2 else 110, equation="elastic")
     dobs = vge_observed(c)
     J, gvp, gvs, grho = vge_gradient(c, dobs)
     r = vge_seismograms(c, c["vp"], c["vs"], c["rho"]) - dobs

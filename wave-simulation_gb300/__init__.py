@@ -577,7 +577,7 @@ class ForwardSolver:
     def adjoint_gradient(self, dobs, checkpoint_every: int = 50):
         """Misfit J = 1/2 ||d - d_obs||^2 and its gradient by the discrete
         adjoint: w.r.t. (vp, vs, rho) for 2-D and 3-D elastic and visco-elastic
-        (relaxation times held fixed; 2-D elastic also on a variable grid),
+        (relaxation times held fixed; elastic also on a variable grid),
         2-D and 3-D acoustic, also on a variable grid (where the vs gradient is
         zero) and 2-D SH and visco-SH (where the vp
         gradient is zero), (eps_r, sigma, mu_r) for 2-D TMz and TEz and 3-D EM and their visco

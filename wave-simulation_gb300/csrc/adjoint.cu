@@ -686,8 +686,8 @@ std::string adjoint_supported(const wave_handle* h)
         for (int t : h->hSrcType)
             if (t != WAVE_TYPE_EZ) return "the TMz adjoint takes Ez sources only";
     }
-    if (h->vg && c.equation != WAVE_EQ_ACOUSTIC && !(c.equation == WAVE_EQ_ELASTIC && c.dimension == 2))
-        return "the adjoint gradient on a variable grid is implemented for the acoustic equations and 2-D elastic";
+    if (h->vg && c.equation != WAVE_EQ_ACOUSTIC && c.equation != WAVE_EQ_ELASTIC)
+        return "the adjoint gradient on a variable grid is implemented for the acoustic and elastic equations";
     if (!h->modelSet) return "set the model first";
     if (!h->seis || h->nrec < 1) return "set receivers first";
     return "";

@@ -34,6 +34,7 @@
 //             syz (StaggeredZ)]
 #include <algorithm>
 #include <functional>
+#include <stdexcept>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -1019,12 +1020,12 @@ __global__ void __launch_bounds__(256) vga_grad_t(VgAdj A)
 // adjoint to their four source rows. Phase 0 takes each row's adjoint into
 // the scratch and clears the row, phase 1 adds it onto the source rows.
 struct VgInterpT {
-    int n[3];
-    float* f[3];
-    float* tmp[3];
-    const int* row[3];
-    const int* col[3];
-    const float* w[3];
+    int n[kMaxInterpLists];
+    float* f[kMaxInterpLists];
+    float* tmp[kMaxInterpLists];
+    const int* row[kMaxInterpLists];
+    const int* col[kMaxInterpLists];
+    const float* w[kMaxInterpLists];
 };
 __global__ void __launch_bounds__(256) vga_interp_t(VgInterpT I, int phase)
 {
@@ -1141,6 +1142,7 @@ void interp_apply(wave_handle* h, const int* kinds, float* const* fields, int m)
     int n = 0, mx = 0;
     bool twoPhase = false;
     long long off = 0;
+    if (m > kMaxInterpLists) throw std::runtime_error("interp_apply: too many lists");
     for (int q = 0; q < m; ++q) {
         const int kind = kinds[q];
         if (!fields[q] || G.nInterp[kind] == 0) continue;
@@ -1174,6 +1176,7 @@ void interp_transpose(wave_handle* h, const int* kinds, float* const* fields, in
     VgInterpT I{};
     int n = 0, mx = 0;
     long long off = 0;
+    if (m > kMaxInterpLists) throw std::runtime_error("interp_transpose: too many lists");
     for (int q = 0; q < m; ++q) {
         const int kind = kinds[q];
         if (!fields[q] || G.nInterp[kind] == 0) continue;
@@ -1405,7 +1408,8 @@ struct VgeAdj {
     const float* cpt[2];
 };
 
-__device__ __forceinline__ bool vge_adj_cpml(const VgeAdj& A, int axis, bool half, long long i, float& a, float& b)
+template <class Adj>
+__device__ __forceinline__ bool vge_adj_cpml(const Adj& A, int axis, bool half, long long i, float& a, float& b)
 {
     if (!A.cpml) return false;
     const unsigned code = A.cpc[axis][i];
@@ -1416,7 +1420,8 @@ __device__ __forceinline__ bool vge_adj_cpml(const VgeAdj& A, int axis, bool hal
 }
 
 // one derivative term of the forward step from state n: operator row and CPML
-__device__ __forceinline__ float vge_fwd_term(const VgeAdj& A, int op, const float* u, int slot, int axis, bool half, long long i)
+template <class Adj>
+__device__ __forceinline__ float vge_fwd_term(const Adj& A, int op, const float* u, int slot, int axis, bool half, long long i)
 {
     float d = ell_gather(A.col[op], A.val[op], A.W[op], A.N, i, u);
     float a, b;
@@ -1426,7 +1431,8 @@ __device__ __forceinline__ float vge_fwd_term(const VgeAdj& A, int op, const flo
 
 // the transposed CPML of one term: the adjoint of the raw derivative, and
 // the memory variable's adjoint carried to the step before
-__device__ __forceinline__ float vge_term_t(const VgeAdj& A, float l, int slot, int axis, bool half, long long i)
+template <class Adj>
+__device__ __forceinline__ float vge_term_t(const Adj& A, float l, int slot, int axis, bool half, long long i)
 {
     float a, b;
     if (!vge_adj_cpml(A, axis, half, i, a, b)) return l;
@@ -1727,13 +1733,354 @@ void adjoint_elastic2d(wave_handle* h, const float* dobs, int K, double* misfit,
     h->check(cudaStreamSynchronize(st), "variable grid adjoint");
 }
 
+// ---- 3-D elastic (FD3Delastic::run, ForwardSolver3Delastic.cpp:120-414):
+// the same sweep with the z terms, the XZ and YZ shear averages, the
+// StaggeredXZ interpolation of sxz, the StaggeredZ one of syz (applied again
+// where it runs in two phases, as the forward step does) and the surface
+// exchange of sxx and szz with vxx + vzz (FreeSurface3Delastic.cpp:15-47)
+
+struct VgeAdj3 {
+    long long N, nSurface;
+    int fs, cpml;
+    const float* v[3];
+    const float* s[6];          // sxx syy szz sxy sxz syz
+    const float* psi[Q_COUNT];
+    float* gv[3];
+    float* v2[3];
+    float* e[6];                // vxx, vyy, vzz with CPML; the shear sums of sxy, sxz, syz
+    float* lv[3];
+    float* ls[6];
+    float* lpsi[Q_COUNT];
+    float* lfs[2];              // the surface exchange's adjoint onto vxx + vzz and onto vyy
+    float* ld[9];
+    float* gM;
+    float* gmu;
+    float* gmuS[3];
+    float* gir[3];
+    float* gsH;
+    float* gsV;
+    const float* M;
+    const float* mu;
+    const float* muS[3];
+    const float* ir[3];
+    const float* damp;
+    const int* col[10];
+    const float* val[10];
+    int W[10];
+    const int* colT[10];
+    const float* valT[10];
+    int WT[10];
+    const unsigned short* cpc[3];
+    const float* cpt[3];
+};
+
+__device__ __forceinline__ float gatherT(const VgeAdj3& A, int op, long long i, const float* u)
+{
+    return ell_gather(A.colT[op], A.valT[op], A.WT[op], A.N, i, u);
+}
+
+__global__ void __launch_bounds__(256) vgea3_fwd_vel(VgeAdj3 A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    float d = vge_fwd_term(A, O_DXF, A.s[0], Q_SXX_X, 0, true, i);
+    d = __fadd_rn(d, vge_fwd_term(A, O_DYB_SX, A.s[3], Q_SXY_Y, 1, false, i));
+    d = __fadd_rn(d, vge_fwd_term(A, O_DZB, A.s[4], Q_SXZ_Z, 2, false, i));
+    A.gv[0][i] = d;
+    A.v2[0][i] = __fadd_rn(A.v[0][i], __fmul_rn(d, A.ir[0][i]));
+    d = vge_fwd_term(A, O_DXB, A.s[3], Q_SXY_X, 0, false, i);
+    d = __fadd_rn(d, vge_fwd_term(A, O_DYF, A.s[1], Q_SYY_Y, 1, true, i));
+    d = __fadd_rn(d, vge_fwd_term(A, O_DZB, A.s[5], Q_SYZ_Z, 2, false, i));
+    A.gv[1][i] = d;
+    A.v2[1][i] = __fadd_rn(A.v[1][i], __fmul_rn(d, A.ir[1][i]));
+    d = vge_fwd_term(A, O_DXB, A.s[4], Q_SXZ_X, 0, false, i);
+    d = __fadd_rn(d, vge_fwd_term(A, O_DYB_SZ, A.s[5], Q_SYZ_Y, 1, false, i));
+    d = __fadd_rn(d, vge_fwd_term(A, O_DZF, A.s[2], Q_SZZ_Z, 2, true, i));
+    A.gv[2][i] = d;
+    A.v2[2][i] = __fadd_rn(A.v[2][i], __fmul_rn(d, A.ir[2][i]));
+}
+
+__global__ void __launch_bounds__(256) vgea3_fwd_str(VgeAdj3 A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    A.e[0][i] = vge_fwd_term(A, O_DXB, A.v2[0], Q_VXX, 0, false, i);
+    A.e[1][i] = vge_fwd_term(A, O_DYB, A.v2[1], Q_VYY, 1, false, i);
+    A.e[2][i] = vge_fwd_term(A, O_DZB, A.v2[2], Q_VZZ, 2, false, i);
+    A.e[3][i] = __fadd_rn(vge_fwd_term(A, O_DYF_SX, A.v2[0], Q_VXY, 1, true, i), vge_fwd_term(A, O_DXF, A.v2[1], Q_VYX, 0, true, i));
+    A.e[4][i] = __fadd_rn(vge_fwd_term(A, O_DZF, A.v2[0], Q_VXZ, 2, true, i), vge_fwd_term(A, O_DXF, A.v2[2], Q_VZX, 0, true, i));
+    A.e[5][i] = __fadd_rn(vge_fwd_term(A, O_DZF, A.v2[1], Q_VYZ, 2, true, i), vge_fwd_term(A, O_DYF_SZ, A.v2[2], Q_VZY, 1, true, i));
+}
+
+// receivers: pressure (type 1) reads (sxx + syy + szz) / 3, types 2-4 vx, vy, vz
+__global__ void vgea3_inject(VgeAdj3 A, int nrec, int nt, int n, const long long* __restrict__ ridx, const int* __restrict__ rtype,
+                             const float* __restrict__ res)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const float v = res[static_cast<long long>(r) * nt + n];
+    const long long i = ridx[r];
+    const int t = rtype[r];
+    if (t == 1) {
+        for (int k = 0; k < 3; ++k) atomicAdd(A.ls[k] + i, v / 3.0f);
+    } else if (t >= 2 && t <= 4) {
+        atomicAdd(A.lv[t - 2] + i, v);
+    }
+}
+
+__global__ void __launch_bounds__(256) vgea3_abs_fs(VgeAdj3 A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    if (A.damp) {
+        const float d = A.damp[i];
+        for (int k = 0; k < 3; ++k) A.lv[k][i] *= d;
+        for (int k = 0; k < 6; ++k) A.ls[k][i] *= d;
+    }
+    float fh = 0.0f, fv = 0.0f;
+    if (A.fs && i < A.nSurface) {
+        const float M = A.M[i], t = M - 2.0f * A.mu[i];
+        const float sH = -(t * t) / M;
+        const float l = A.ls[0][i] + A.ls[2][i];
+        A.gsH[i] += l * (A.e[0][i] + A.e[2][i]);
+        A.gsV[i] -= l * A.e[1][i];
+        fh = sH * l;
+        fv = -t * l;
+        A.ls[1][i] = 0.0f;
+    }
+    A.lfs[0][i] = fh;
+    A.lfs[1][i] = fv;
+}
+
+__global__ void __launch_bounds__(256) vgea3_str(VgeAdj3 A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    // shear stresses: (first term's memory slot, axis), (second term's)
+    const int slot[3][2] = {{Q_VXY, Q_VYX}, {Q_VXZ, Q_VZX}, {Q_VYZ, Q_VZY}};
+    const int axis[3][2] = {{1, 0}, {2, 0}, {2, 1}};
+    for (int c = 0; c < 3; ++c) {
+        const float l = A.ls[3 + c][i];
+        A.gmuS[c][i] += l * A.e[3 + c][i];
+        const float lu = A.muS[c][i] * l;
+        A.ld[2 * c][i] = vge_term_t(A, lu, slot[c][0], axis[c][0], true, i);
+        A.ld[2 * c + 1][i] = vge_term_t(A, lu, slot[c][1], axis[c][1], true, i);
+    }
+    const float lx = A.ls[0][i], ly = A.ls[1][i], lz = A.ls[2][i];
+    const float ex = A.e[0][i], ey = A.e[1][i], ez = A.e[2][i];
+    const float l3 = lx + ly + lz, M = A.M[i], mu = A.mu[i];
+    A.gM[i] += l3 * (ex + ey + ez);
+    A.gmu[i] -= 2.0f * ((ey + ez) * lx + (ex + ez) * ly + (ex + ey) * lz);
+    A.ld[6][i] = vge_term_t(A, M * l3 - 2.0f * mu * (ly + lz) + A.lfs[0][i], Q_VXX, 0, false, i);
+    A.ld[7][i] = vge_term_t(A, M * l3 - 2.0f * mu * (lx + lz) + A.lfs[1][i], Q_VYY, 1, false, i);
+    A.ld[8][i] = vge_term_t(A, M * l3 - 2.0f * mu * (lx + ly) + A.lfs[0][i], Q_VZZ, 2, false, i);
+}
+
+__global__ void __launch_bounds__(256) vgea3_str_t(VgeAdj3 A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    A.lv[0][i] += gatherT(A, O_DYF_SX, i, A.ld[0]) + gatherT(A, O_DZF, i, A.ld[2]) + gatherT(A, O_DXB, i, A.ld[6]);
+    A.lv[1][i] += gatherT(A, O_DXF, i, A.ld[1]) + gatherT(A, O_DZF, i, A.ld[4]) + gatherT(A, O_DYB, i, A.ld[7]);
+    A.lv[2][i] += gatherT(A, O_DXF, i, A.ld[3]) + gatherT(A, O_DYF_SZ, i, A.ld[5]) + gatherT(A, O_DZB, i, A.ld[8]);
+}
+
+__global__ void __launch_bounds__(256) vgea3_vel(VgeAdj3 A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    // per velocity: (memory slot, axis, half) of its three terms
+    const int slot[3][3] = {{Q_SXX_X, Q_SXY_Y, Q_SXZ_Z}, {Q_SXY_X, Q_SYY_Y, Q_SYZ_Z}, {Q_SXZ_X, Q_SYZ_Y, Q_SZZ_Z}};
+    for (int k = 0; k < 3; ++k) {
+        const float l = A.lv[k][i];
+        A.gir[k][i] += l * A.gv[k][i];
+        const float g = A.ir[k][i] * l;
+        for (int a = 0; a < 3; ++a) A.ld[3 * k + a][i] = vge_term_t(A, g, slot[k][a], a, a == k, i);
+    }
+}
+
+__global__ void __launch_bounds__(256) vgea3_vel_t(VgeAdj3 A)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    A.ls[0][i] += gatherT(A, O_DXF, i, A.ld[0]);
+    A.ls[1][i] += gatherT(A, O_DYF, i, A.ld[4]);
+    A.ls[2][i] += gatherT(A, O_DZF, i, A.ld[8]);
+    A.ls[3][i] += gatherT(A, O_DYB_SX, i, A.ld[1]) + gatherT(A, O_DXB, i, A.ld[3]);
+    A.ls[4][i] += gatherT(A, O_DZB, i, A.ld[2]) + gatherT(A, O_DXB, i, A.ld[6]);
+    A.ls[5][i] += gatherT(A, O_DZB, i, A.ld[5]) + gatherT(A, O_DYB_SZ, i, A.ld[7]);
+}
+
+// chain rule, first half (as vgea_chain1 with the three shear averages and axes)
+__global__ void __launch_bounds__(256) vgea3_chain1(VgeAdj3 A, const int* __restrict__ px, const int* __restrict__ py,
+                                                    const int* __restrict__ pz, const int* const* __restrict__ shear, float* gMt,
+                                                    float* gmuT, float* grho)
+{
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    float g = A.gM[i], gm = A.gmu[i];
+    if (A.fs && i < A.nSurface) {
+        const float M = A.M[i], t = M - 2.0f * A.mu[i];
+        const float sH = A.gsH[i], sV = A.gsV[i];
+        g += sV + sH * (-2.0f * t / M + t * t / (M * M));
+        gm += -2.0f * sV + sH * 4.0f * t / M;
+    }
+    gMt[i] = g;
+    atomicAdd(gmuT + i, gm);
+    const int ii = static_cast<int>(i);
+    for (int q = 0; q < 3; ++q) {
+        const float m = A.muS[q][i];
+        if (m < 4.0f) continue;
+        const float coef = A.gmuS[q][i] * m * m;
+        const int a = shear[3 * q][i], b = shear[3 * q + 1][i], c = shear[3 * q + 2][i];
+        int pts[4];
+        float w[4];
+        int np;
+        if (a >= 0 && b >= 0) {
+            pts[0] = ii; pts[1] = a; pts[2] = b; pts[3] = c >= 0 ? c : ii;
+            w[0] = w[1] = w[2] = w[3] = 0.25f;
+            np = 4;
+        } else if (a >= 0 || b >= 0) {
+            pts[0] = a >= 0 ? a : b; pts[1] = ii;
+            w[0] = w[1] = 0.5f;
+            np = 2;
+        } else {
+            pts[0] = ii;
+            w[0] = 1.0f;
+            np = 1;
+        }
+        for (int k = 0; k < np; ++k) {
+            const float mk = A.mu[pts[k]];
+            if (mk > 1.0f) atomicAdd(gmuT + pts[k], coef * w[k] / (mk * mk));
+        }
+    }
+    const int* part[3] = {px, py, pz};
+    float own = 0.0f;
+    for (int ax = 0; ax < 3; ++ax) {
+        const float r = A.ir[ax][i];
+        const float wv = -A.gir[ax][i] * r * r;
+        const int j = part[ax][i];
+        if (j >= 0) {
+            own += 0.5f * wv;
+            atomicAdd(grho + j, 0.5f * wv);
+        } else {
+            own += wv;
+        }
+    }
+    atomicAdd(grho + i, own);
+}
+
+void adjoint_elastic3d(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* gvs, float* grho)
+{
+    const VarGridDev& G = *h->vg;
+    cudaStream_t st = h->stream;
+    const long long N = G.N;
+    const int NT = h->NT;
+    const VgeParams E = elastic_params_of(h);
+    const bool cp = G.cpCode[0] != nullptr;
+    AdjPool pool{h};
+    std::vector<float*> parts = {E.v[0], E.v[1], E.v[2]};
+    for (int k = 0; k < 6; ++k) parts.push_back(E.s[k]);
+    if (cp)
+        for (int q = 0; q < Q_COUNT; ++q) parts.push_back(E.psi[q]);
+
+    VgeAdj3 A{};
+    A.N = N;
+    A.nSurface = G.nSurface;
+    A.fs = G.fs;
+    A.cpml = cp ? 1 : 0;
+    A.M = E.M;
+    A.mu = E.mu;
+    for (int k = 0; k < 3; ++k) {
+        A.muS[k] = E.muS[k];
+        A.ir[k] = E.ir[k];
+        A.cpc[k] = G.cpCode[k];
+        A.cpt[k] = G.cpTab[k];
+    }
+    A.damp = G.absDamp;
+    for (int k = 0; k < 10; ++k) {
+        A.col[k] = G.col[k];
+        A.val[k] = G.val[k];
+        A.W[k] = G.W[k];
+        A.colT[k] = G.colT[k];
+        A.valT[k] = G.valT[k];
+        A.WT[k] = G.WT[k];
+    }
+    float* adj = pool.zeros((9 + (cp ? Q_COUNT : 0)) * static_cast<size_t>(N));
+    for (int k = 0; k < 3; ++k) A.lv[k] = adj + k * N;
+    for (int k = 0; k < 6; ++k) A.ls[k] = adj + (3 + k) * N;
+    if (cp)
+        for (int q = 0; q < Q_COUNT; ++q) A.lpsi[q] = adj + (9 + q) * N;
+    float* tmp = pool.get(26 * static_cast<size_t>(N));
+    for (int k = 0; k < 3; ++k) {
+        A.gv[k] = tmp + k * N;
+        A.v2[k] = tmp + (3 + k) * N;
+    }
+    for (int k = 0; k < 6; ++k) A.e[k] = tmp + (6 + k) * N;
+    for (int k = 0; k < 2; ++k) A.lfs[k] = tmp + (12 + k) * N;
+    for (int k = 0; k < 9; ++k) A.ld[k] = tmp + (14 + k) * N;
+    float* sums = pool.zeros(10 * static_cast<size_t>(N));
+    A.gM = sums;
+    A.gmu = sums + N;
+    for (int k = 0; k < 3; ++k) {
+        A.gmuS[k] = sums + (2 + k) * N;
+        A.gir[k] = sums + (5 + k) * N;
+    }
+    A.gsH = sums + 8 * N;
+    A.gsV = sums + 9 * N;
+    float* itmp = pool.get(6 * static_cast<size_t>(G.nInterp[0] + G.nInterp[1] + G.nInterp[2] + G.nInterp[3] + 1));
+    float* res = pool.get(static_cast<size_t>(h->nrec) * NT);
+
+    const dim3 grid(static_cast<unsigned>((N + 255) / 256)), block(256);
+    const int velKinds[3] = {1, 0, 2};            // vx StaggeredX, vy Full, vz StaggeredZ
+    const int strKinds[6] = {0, 0, 0, 1, 3, 2};   // sxx syy szz Full, sxy StaggeredX, sxz StaggeredXZ, syz StaggeredZ
+    const int zKind[1] = {2};
+    const bool again = G.nInterp[2] > 0 && !G.inplace[2];
+    adjoint_sweep(h, pool, parts, dobs, K, misfit, res, [&](int n, const float* sv) {
+        for (int k = 0; k < 3; ++k) A.v[k] = sv + k * N;
+        for (int k = 0; k < 6; ++k) A.s[k] = sv + (3 + k) * N;
+        for (int q = 0; q < Q_COUNT; ++q) A.psi[q] = cp ? sv + (9 + q) * N : nullptr;
+        vgea3_inject<<<(h->nrec + 127) / 128, 128, 0, st>>>(A, h->nrec, NT, n, h->ridx, h->rtype, res);
+        vgea3_fwd_vel<<<grid, block, 0, st>>>(A);
+        float* v2f[3] = {A.v2[0], A.v2[1], A.v2[2]};
+        interp_apply(h, velKinds, v2f, 3);
+        vgea3_fwd_str<<<grid, block, 0, st>>>(A);
+        vgea3_abs_fs<<<grid, block, 0, st>>>(A);
+        if (again) {   // the second StaggeredZ pass of syz, transposed first
+            float* f5[1] = {A.ls[5]};
+            interp_transpose(h, zKind, f5, 1, itmp);
+        }
+        float* lsf[6] = {A.ls[0], A.ls[1], A.ls[2], A.ls[3], A.ls[4], A.ls[5]};
+        interp_transpose(h, strKinds, lsf, 6, itmp);
+        vgea3_str<<<grid, block, 0, st>>>(A);
+        vgea3_str_t<<<grid, block, 0, st>>>(A);
+        float* lvf[3] = {A.lv[0], A.lv[1], A.lv[2]};
+        interp_transpose(h, velKinds, lvf, 3, itmp);
+        vgea3_vel<<<grid, block, 0, st>>>(A);
+        vgea3_vel_t<<<grid, block, 0, st>>>(A);
+    });
+    float* gMt = pool.get(N);
+    float* gmuT = pool.zeros(N);
+    const int** shear = pool.get<const int*>(9);
+    const int* hs[9];
+    for (int q = 0; q < 3; ++q)
+        for (int a = 0; a < 3; ++a) hs[3 * q + a] = G.shear[q][a];
+    h->check(cudaMemcpyAsync(shear, hs, sizeof(hs), cudaMemcpyHostToDevice, st), "copy");
+    h->check(cudaMemsetAsync(grho, 0, N * sizeof(float), st), "memset");
+    vgea3_chain1<<<grid, block, 0, st>>>(A, G.partner[0], G.partner[1], G.partner[2], shear, gMt, gmuT, grho);
+    vgea_chain2<<<grid, block, 0, st>>>(N, h->m[M_RHO], h->m[M_VP], h->m[M_VS], gMt, gmuT, gvp, gvs, grho);
+    h->check(cudaGetLastError(), "variable grid adjoint");
+    h->check(cudaStreamSynchronize(st), "variable grid adjoint");
+}
+
 } // namespace
 
 void vargrid_adjoint(wave_handle* h, const float* dobs, int K, double* misfit, float* gvp, float* gvs, float* grho)
 {
     build_transposes(h);
     if (h->vg->elastic) {
-        adjoint_elastic2d(h, dobs, K, misfit, gvp, gvs, grho);
+        if (h->vg->is3d) adjoint_elastic3d(h, dobs, K, misfit, gvp, gvs, grho);
+        else adjoint_elastic2d(h, dobs, K, misfit, gvp, gvs, grho);
         return;
     }
     h->check(cudaMemsetAsync(gvs, 0, h->vg->N * sizeof(float), h->stream), "memset");
