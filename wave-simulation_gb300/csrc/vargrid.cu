@@ -32,6 +32,11 @@
 //             Dzf vy + DyfStaggeredZ vz]
 //   vg_interp sxx, syy [, szz] (Full), sxy (StaggeredX) [, sxz (StaggeredXZ),
 //             syz (StaggeredZ)]
+//
+// The end of the file holds the discrete adjoints of both steps (the
+// gradient of the seismogram misfit): the transposes of the ELL blocks,
+// interpolations and per-point factors applied in reverse order over a
+// checkpointed sweep.
 #include <algorithm>
 #include <functional>
 #include <stdexcept>
