@@ -82,7 +82,8 @@ def _gradient(c, dobs):
                             edge=c["edge"])
 
 
-@pytest.mark.parametrize("dim,fs,boundary,edge", [(2, 1, 2, 1), (2, 0, 1, 0), (2, 1, 0, 1), (3, 1, 2, 1), (3, 0, 1, 1)])
+@pytest.mark.parametrize("dim,fs,boundary,edge", [(2, 1, 2, 1), (2, 0, 1, 0), (2, 1, 0, 1), (3, 1, 2, 1), (3, 0, 1, 1),
+                                                 (2, 2, 2, 1)])
 def test_oracle_vargrid_adjoint_matches_fp64_finite_differences(refcpu, dim, fs, boundary, edge):
     c = vg_case(refcpu, dim, fs, boundary, edge, nt=120 if dim == 3 else 150)
     dobs = vg_observed(c)
